@@ -1,0 +1,778 @@
+/* TEST INFRASTRUCTURE ONLY -- the oracle restatement. See fem_oracle.h.
+ *
+ * Written in plain C99 with the reference's evaluation order kept term for
+ * term: every matrix-vector product is an accumulator started at zero and
+ * summed over the column index (src/Mal/GMatUtils.h:12-23), every matrix
+ * product likewise (src/Mal/GMat.h:133-145), division of a vector by a
+ * scalar multiplies by the reciprocal (src/Mal/GVec.h:83), and Sqrt/Sin/
+ * Cos/ATan2 go through float (src/Mal/RealUtils.h:27,45,48,63). Built with
+ * -ffp-contract=off so no multiply-add is fused.
+ */
+#include "fem_oracle.h"
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+typedef struct { double v[3]; } vec3;
+typedef struct { double m[3][3]; } mat3;
+
+/* ---- Mal scalar semantics (src/Mal/RealUtils.h) -------------------------- */
+
+/* Which scalar math the Mal functions use, per calling thread (set by every
+ * public entry point from the solid): FEM_ORC_MATH_DOUBLE evaluates Sqrt/Sin/
+ * Cos/ATan2 in double; FEM_ORC_MATH_FLOAT_LITERAL reproduces the reference
+ * FP64 build as written, T(f(float(x))) with the host's float libm
+ * (RealUtils.h:27,45,48,63). */
+static __thread int g_math = FEM_ORC_MATH_DOUBLE;
+
+static double mal_sqrt(double x)
+{
+    if (g_math == FEM_ORC_MATH_FLOAT_LITERAL) return (double)sqrtf((float)x);
+    return sqrt(x);
+}
+static double mal_atan2(double y, double x)
+{
+    if (g_math == FEM_ORC_MATH_FLOAT_LITERAL) return (double)atan2f((float)y, (float)x);
+    return atan2(y, x);
+}
+static double mal_cos(double x)
+{
+    if (g_math == FEM_ORC_MATH_FLOAT_LITERAL) return (double)cosf((float)x);
+    return cos(x);
+}
+static double mal_sin(double x)
+{
+    if (g_math == FEM_ORC_MATH_FLOAT_LITERAL) return (double)sinf((float)x);
+    return sin(x);
+}
+
+/* ---- Mal vector/matrix semantics ---------------------------------------- */
+
+static vec3 v3(double a, double b, double c) { vec3 r; r.v[0] = a; r.v[1] = b; r.v[2] = c; return r; }
+static vec3 v_add(vec3 a, vec3 b) { return v3(a.v[0] + b.v[0], a.v[1] + b.v[1], a.v[2] + b.v[2]); }
+static vec3 v_sub(vec3 a, vec3 b) { return v3(a.v[0] - b.v[0], a.v[1] - b.v[1], a.v[2] - b.v[2]); }
+static vec3 v_scale(double s, vec3 a) { return v3(s * a.v[0], s * a.v[1], s * a.v[2]); }
+static vec3 v_neg(vec3 a) { return v3(-a.v[0], -a.v[1], -a.v[2]); }
+/* GVec::operator* (dot), accumulator from zero (GVec.h:88) */
+static double v_dot(vec3 a, vec3 b)
+{
+    double acc = 0;
+    for (int i = 0; i < 3; i++) acc += a.v[i] * b.v[i];
+    return acc;
+}
+/* GVec::operator% (GVec.h:89-91) */
+static vec3 v_cross(vec3 a, vec3 b)
+{
+    return v3(a.v[1] * b.v[2] - a.v[2] * b.v[1],
+              a.v[2] * b.v[0] - a.v[0] * b.v[2],
+              a.v[0] * b.v[1] - a.v[1] * b.v[0]);
+}
+/* GVec::operator/ : multiply by the reciprocal (GVec.h:83) */
+static vec3 v_div(vec3 a, double s) { double inv = 1.0 / s; return v_scale(inv, a); }
+/* Norm = Sqrt(NormSq) (GVec.h:102-105); Normalized = v / Norm (GVec.h:97) */
+static double v_norm(vec3 a) { return mal_sqrt(v_dot(a, a)); }
+static vec3 v_normalized(vec3 a) { return v_div(a, v_norm(a)); }
+
+/* Mat-vector product (GMatUtils.h:12-23) */
+static vec3 m_mulv(const mat3* m, vec3 x)
+{
+    vec3 r;
+    for (int i = 0; i < 3; i++) {
+        double acc = 0;
+        for (int j = 0; j < 3; j++) acc += m->m[i][j] * x.v[j];
+        r.v[i] = acc;
+    }
+    return r;
+}
+/* Matrix product (GMat.h:133-145) */
+static mat3 m_mul(const mat3* a, const mat3* b)
+{
+    mat3 r;
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) {
+            double acc = 0;
+            for (int k = 0; k < 3; k++) acc += a->m[i][k] * b->m[k][j];
+            r.m[i][j] = acc;
+        }
+    return r;
+}
+static mat3 m_transposed(const mat3* a)
+{
+    mat3 r;
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) r.m[i][j] = a->m[j][i];
+    return r;
+}
+/* GMat3x3_From_Columns (GMatUtils.h:133-138) */
+static mat3 m_from_columns(vec3 c0, vec3 c1, vec3 c2)
+{
+    mat3 r;
+    for (int i = 0; i < 3; i++) { r.m[i][0] = c0.v[i]; r.m[i][1] = c1.v[i]; r.m[i][2] = c2.v[i]; }
+    return r;
+}
+/* Det 3x3 (GMat.h:236-245) */
+static double m_det(const mat3* a)
+{
+    const double (*m)[3] = a->m;
+    return m[0][0] * m[1][1] * m[2][2]
+         - m[0][0] * m[2][1] * m[1][2]
+         + m[1][0] * m[2][1] * m[0][2]
+         - m[1][0] * m[0][1] * m[2][2]
+         + m[2][0] * m[0][1] * m[1][2]
+         - m[2][0] * m[1][1] * m[0][2];
+}
+/* Inverse 3x3 (GMat.h:291-313) */
+static mat3 m_inverse(const mat3* a)
+{
+    const double (*m)[3] = a->m;
+    double inv_det = 1.0 / m_det(a);
+    mat3 r;
+    r.m[0][0] = inv_det * (m[1][1] * m[2][2] - m[1][2] * m[2][1]);
+    r.m[0][1] = inv_det * (m[0][2] * m[2][1] - m[0][1] * m[2][2]);
+    r.m[0][2] = inv_det * (m[0][1] * m[1][2] - m[0][2] * m[1][1]);
+    r.m[1][0] = inv_det * (m[1][2] * m[2][0] - m[1][0] * m[2][2]);
+    r.m[1][1] = inv_det * (m[0][0] * m[2][2] - m[0][2] * m[2][0]);
+    r.m[1][2] = inv_det * (m[0][2] * m[1][0] - m[0][0] * m[1][2]);
+    r.m[2][0] = inv_det * (m[1][0] * m[2][1] - m[1][1] * m[2][0]);
+    r.m[2][1] = inv_det * (m[0][1] * m[2][0] - m[0][0] * m[2][1]);
+    r.m[2][2] = inv_det * (m[0][0] * m[1][1] - m[0][1] * m[1][0]);
+    return r;
+}
+static vec3 m_col(const mat3* a, int j) { return v3(a->m[0][j], a->m[1][j], a->m[2][j]); }
+
+/* ---- MSVD rotation: GFastSVD3x3 (src/Mal/GMatDecomposition_SVD3x3_PhysBAM.h) */
+
+typedef struct { double x11, x21, x31, x22, x32, x33; } sym3;
+typedef struct { double x11, x21, x22; } sym2;
+
+/* Orthogonal_Vector (PhysBAM.h:35-49) */
+static vec3 orthogonal_vector(vec3 v)
+{
+    double ax = fabs(v.v[0]), ay = fabs(v.v[1]), az = fabs(v.v[2]);
+    if (ax < ay)
+        return (ax < az) ? v3(0, v.v[2], -v.v[1]) : v3(v.v[1], -v.v[0], 0);
+    return (ay < az) ? v3(-v.v[2], 0, v.v[0]) : v3(v.v[1], -v.v[0], 0);
+}
+
+/* GSymmetricMat3x3::Cofactor_Matrix (PhysBAM.h:139-147) */
+static sym3 sym3_cofactor(sym3 a)
+{
+    sym3 r;
+    r.x11 = a.x22 * a.x33 - a.x32 * a.x32;
+    r.x21 = a.x32 * a.x31 - a.x21 * a.x33;
+    r.x31 = a.x21 * a.x32 - a.x22 * a.x31;
+    r.x22 = a.x11 * a.x33 - a.x31 * a.x31;
+    r.x32 = a.x21 * a.x31 - a.x11 * a.x32;
+    r.x33 = a.x11 * a.x22 - a.x21 * a.x21;
+    return r;
+}
+
+/* GSymmetricMat3x3::Largest_Column_Normalized (PhysBAM.h:149-156) */
+static vec3 sym3_largest_column_normalized(sym3 a)
+{
+    double s11 = a.x11 * a.x11, s12 = a.x21 * a.x21, s13 = a.x31 * a.x31;
+    double s22 = a.x22 * a.x22, s23 = a.x32 * a.x32, s33 = a.x33 * a.x33;
+    double scale1 = s11 + s12 + s13, scale2 = s12 + s22 + s23, scale3 = s13 + s23 + s33;
+    if (scale1 > scale2) {
+        if (scale1 > scale3) return v_div(v3(a.x11, a.x21, a.x31), mal_sqrt(scale1));
+    } else if (scale2 > scale3)
+        return v_div(v3(a.x21, a.x22, a.x32), mal_sqrt(scale2));
+    if (scale3 > 0) return v_div(v3(a.x31, a.x32, a.x33), mal_sqrt(scale3));
+    return v3(1, 0, 0);
+}
+
+/* GSymmetricMat2x2::Largest_Column_Normalized (PhysBAM.h:75-82), on the
+ * cofactor matrix (x22, -x21, x11) of a (PhysBAM.h:70-73). */
+static void sym2_cofactor_largest_column_normalized(sym2 a, double out[2])
+{
+    double c11 = a.x22, c21 = -a.x21, c22 = a.x11;
+    double s11 = c11 * c11, s12 = c21 * c21, s22 = c22 * c22;
+    double scale1 = s11 + s12, scale2 = s12 + s22;
+    if (scale1 > scale2) {
+        double inv = 1.0 / mal_sqrt(scale1);
+        out[0] = inv * c11; out[1] = inv * c21;
+    } else if (scale2 > 0) {
+        double inv = 1.0 / mal_sqrt(scale2);
+        out[0] = inv * c21; out[1] = inv * c22;
+    } else {
+        out[0] = 1; out[1] = 0;
+    }
+}
+
+/* Fast_Eigenvalues (PhysBAM.h:161-197). Note the reference's
+ * cRootThree( Sqrt(3) ): Sqrt is a template on its argument type, the
+ * argument is the int literal 3, so it evaluates int(sqrtf(3.0f)) == 1. The
+ * restatement keeps that value. */
+static void fast_eigenvalues(sym3 a, double lambda_out[3])
+{
+    const double one_third = 1.0 / 3.0;
+    const double one_sixth = 1.0 / 6.0;
+    const double root_three = 1.0; /* reference value, see above */
+    double m = one_third * (a.x11 + a.x22 + a.x33);
+    double a11 = a.x11 - m, a22 = a.x22 - m, a33 = a.x33 - m;
+    double a12_sqr = a.x21 * a.x21, a13_sqr = a.x31 * a.x31, a23_sqr = a.x32 * a.x32;
+    double p = one_sixth * (a11 * a11 + a22 * a22 + a33 * a33 + 2 * (a12_sqr + a13_sqr + a23_sqr));
+    double q = .5 * (a11 * (a22 * a33 - a23_sqr) - a22 * a13_sqr - a33 * a12_sqr) + a.x21 * a.x31 * a.x32;
+    double sqrt_p = mal_sqrt(p), disc = p * p * p - q * q;
+    double disc_clamped = (0.0 > disc) ? 0.0 : disc; /* Max((T)0, disc), NumberUtils.h:35 */
+    double phi = one_third * mal_atan2(mal_sqrt(disc_clamped), q);
+    double c = mal_cos(phi), s = mal_sin(phi);
+    double sqrt_p_cos = sqrt_p * c, root_three_sqrt_p_sin = root_three * sqrt_p * s;
+    double l0 = m + 2 * sqrt_p_cos;
+    double l1 = m - sqrt_p_cos - root_three_sqrt_p_sin;
+    double l2 = m - sqrt_p_cos + root_three_sqrt_p_sin;
+    if (l0 < l1) {
+        if (l1 < l2) { lambda_out[0] = l2; lambda_out[1] = l1; lambda_out[2] = l0; }
+        else if (l0 < l2) { lambda_out[0] = l1; lambda_out[1] = l2; lambda_out[2] = l0; }
+        else { lambda_out[0] = l1; lambda_out[1] = l0; lambda_out[2] = l2; }
+    } else {
+        if (l1 > l2) { lambda_out[0] = l0; lambda_out[1] = l1; lambda_out[2] = l2; }
+        else if (l0 > l2) { lambda_out[0] = l0; lambda_out[1] = l2; lambda_out[2] = l1; }
+        else { lambda_out[0] = l2; lambda_out[1] = l0; lambda_out[2] = l1; }
+    }
+}
+
+/* Fast_Eigenvectors (PhysBAM.h:199-236); returns V with eigenvectors as columns */
+static mat3 fast_eigenvectors(sym3 A, const double lambda[3])
+{
+    int flipped = 0;
+    double lf[3] = {lambda[0], lambda[1], lambda[2]};
+    if (lambda[0] - lambda[1] < lambda[1] - lambda[2]) {
+        lf[0] = lambda[2];
+        lf[2] = lambda[0];
+        flipped = 1;
+    }
+    sym3 am = A;
+    am.x11 -= lf[0]; am.x22 -= lf[0]; am.x33 -= lf[0];
+    vec3 v1 = sym3_largest_column_normalized(sym3_cofactor(am));
+    vec3 v1o = v_normalized(orthogonal_vector(v1));
+    vec3 ov0 = v1o, ov1 = v_cross(v1, v1o); /* other_v columns */
+    /* Conjugate_With_Transpose(other_v, A): (A_full * other_v)^T other_v */
+    double Af[3][3] = {{A.x11, A.x21, A.x31}, {A.x21, A.x22, A.x32}, {A.x31, A.x32, A.x33}};
+    double C[3][2];
+    for (int i = 0; i < 3; i++) {
+        double acc0 = 0, acc1 = 0;
+        for (int k = 0; k < 3; k++) acc0 += Af[i][k] * ov0.v[k];
+        for (int k = 0; k < 3; k++) acc1 += Af[i][k] * ov1.v[k];
+        C[i][0] = acc0; C[i][1] = acc1;
+    }
+    sym2 ar;
+    ar.x11 = C[0][0] * ov0.v[0] + C[1][0] * ov0.v[1] + C[2][0] * ov0.v[2];
+    ar.x21 = C[0][1] * ov0.v[0] + C[1][1] * ov0.v[1] + C[2][1] * ov0.v[2];
+    ar.x22 = C[0][1] * ov1.v[0] + C[1][1] * ov1.v[1] + C[2][1] * ov1.v[2];
+    ar.x11 -= lf[2];
+    ar.x22 -= lf[2];
+    double w[2];
+    sym2_cofactor_largest_column_normalized(ar, w);
+    vec3 v3v;
+    for (int i = 0; i < 3; i++) {
+        double acc = 0;
+        acc += ov0.v[i] * w[0];
+        acc += ov1.v[i] * w[1];
+        v3v.v[i] = acc;
+    }
+    vec3 v2 = v_cross(v3v, v1);
+    return flipped ? m_from_columns(v3v, v2, v_neg(v1)) : m_from_columns(v1, v2, v3v);
+}
+
+/* GFastSVD3x3 (PhysBAM.h:247-280) reduced to the U and V it returns, then
+ * Compute_R_SVD's R = U * V^T (src/Saphyre2/ms/fem/Rotation.cpp:39-57). The
+ * singular values do not enter R and are not formed. */
+static mat3 rotation_msvd(const mat3* F)
+{
+    sym3 ne;
+    const double (*f)[3] = F->m;
+    ne.x11 = f[0][0] * f[0][0] + f[1][0] * f[1][0] + f[2][0] * f[2][0];
+    ne.x21 = f[0][1] * f[0][0] + f[1][1] * f[1][0] + f[2][1] * f[2][0];
+    ne.x31 = f[0][2] * f[0][0] + f[1][2] * f[1][0] + f[2][2] * f[2][0];
+    ne.x22 = f[0][1] * f[0][1] + f[1][1] * f[1][1] + f[2][1] * f[2][1];
+    ne.x32 = f[0][2] * f[0][1] + f[1][2] * f[1][1] + f[2][2] * f[2][1];
+    ne.x33 = f[0][2] * f[0][2] + f[1][2] * f[1][2] + f[2][2] * f[2][2];
+    double lambda[3];
+    fast_eigenvalues(ne, lambda);
+    mat3 V = fast_eigenvectors(ne, lambda);
+    vec3 u0 = v_normalized(m_mulv(F, m_col(&V, 0)));
+    vec3 o0 = v_normalized(orthogonal_vector(u0));
+    vec3 o1 = v_cross(u0, o0);
+    vec3 t = v_normalized(m_mulv(F, m_col(&V, 1)));
+    double w[2];
+    {
+        double acc0 = 0, acc1 = 0;
+        for (int k = 0; k < 3; k++) acc0 += o0.v[k] * t.v[k];
+        for (int k = 0; k < 3; k++) acc1 += o1.v[k] * t.v[k];
+        w[0] = acc0; w[1] = acc1;
+    }
+    vec3 u1;
+    for (int i = 0; i < 3; i++) {
+        double acc = 0;
+        acc += o0.v[i] * w[0];
+        acc += o1.v[i] * w[1];
+        u1.v[i] = acc;
+    }
+    vec3 u2 = v_cross(u0, u1);
+    mat3 U = m_from_columns(u0, u1, u2);
+    mat3 Vt = m_transposed(&V);
+    return m_mul(&U, &Vt);
+}
+
+void orc_rotation_svd(const double* F_in, double* R_out, int math_mode)
+{
+    g_math = math_mode;
+    mat3 F;
+    memcpy(F.m, F_in, sizeof(F.m));
+    mat3 R = rotation_msvd(&F);
+    memcpy(R_out, R.m, sizeof(R.m));
+}
+
+/* ---- Element stiffness: TetrahedronElement3 (TetrahedronElement3.h:85-173) */
+
+static mat3 compute_D(vec3 r0, vec3 r1, vec3 r2, vec3 r3)
+{
+    return m_from_columns(v_sub(r1, r0), v_sub(r2, r0), v_sub(r3, r0));
+}
+
+static double compute_volume(vec3 r0, vec3 r1, vec3 r2, vec3 r3)
+{
+    mat3 D = compute_D(r0, r1, r2, r3);
+    return m_det(&D) / 6.0;
+}
+
+/* Compute_K = V * B^T (E B) with B from AFEM-16 (TetrahedronElement3.h:106-173);
+ * K12 row-major 12x12. */
+static double compute_K(vec3 r0, vec3 r1, vec3 r2, vec3 r3, double young, double poisson, double K[12][12])
+{
+    double volume = compute_volume(r0, r1, r2, r3);
+    double x1 = r0.v[0], x2 = r1.v[0], x3 = r2.v[0], x4 = r3.v[0];
+    double y1 = r0.v[1], y2 = r1.v[1], y3 = r2.v[1], y4 = r3.v[1];
+    double z1 = r0.v[2], z2 = r1.v[2], z3 = r2.v[2], z4 = r3.v[2];
+    double J[4][4];
+    J[0][0] = x2 * (y3 * z4 - y4 * z3) + x3 * (y4 * z2 - y2 * z4) + x4 * (y2 * z3 - y3 * z2);
+    J[1][0] = x1 * (y4 * z3 - y3 * z4) + x3 * (y1 * z4 - y4 * z1) + x4 * (y3 * z1 - y1 * z3);
+    J[2][0] = x1 * (y2 * z4 - y4 * z2) + x2 * (y4 * z1 - y1 * z4) + x4 * (y1 * z2 - y2 * z1);
+    J[3][0] = x1 * (y3 * z2 - y2 * z3) + x2 * (y1 * z3 - y3 * z1) + x3 * (y2 * z1 - y1 * z2);
+    J[0][1] = (y4 - y2) * (z3 - z2) - (y3 - y2) * (z4 - z2); J[0][2] = (x3 - x2) * (z4 - z2) - (x4 - x2) * (z3 - z2); J[0][3] = (x4 - x2) * (y3 - y2) - (x3 - x2) * (y4 - y2);
+    J[1][1] = (y3 - y1) * (z4 - z3) - (y3 - y4) * (z1 - z3); J[1][2] = (x4 - x3) * (z3 - z1) - (x1 - x3) * (z3 - z4); J[1][3] = (x3 - x1) * (y4 - y3) - (x3 - x4) * (y1 - y3);
+    J[2][1] = (y2 - y4) * (z1 - z4) - (y1 - y4) * (z2 - z4); J[2][2] = (x1 - x4) * (z2 - z4) - (x2 - x4) * (z1 - z4); J[2][3] = (x2 - x4) * (y1 - y4) - (x1 - x4) * (y2 - y4);
+    J[3][1] = (y1 - y3) * (z2 - z1) - (y1 - y2) * (z3 - z1); J[3][2] = (x2 - x1) * (z1 - z3) - (x3 - x1) * (z1 - z2); J[3][3] = (x1 - x3) * (y2 - y1) - (x1 - x2) * (y3 - y1);
+    double s = 1.0 / (6.0 * volume);
+    for (int i = 0; i < 4; i++)
+        for (int j = 0; j < 4; j++) J[i][j] = s * J[i][j];
+    double a[4], b[4], c[4];
+    for (int i = 0; i < 4; i++) { a[i] = J[i][1]; b[i] = J[i][2]; c[i] = J[i][3]; }
+    double B[6][12];
+    memset(B, 0, sizeof(B));
+    for (int n = 0; n < 4; n++) {
+        B[0][3 * n] = a[n];
+        B[1][3 * n + 1] = b[n];
+        B[2][3 * n + 2] = c[n];
+        B[3][3 * n] = b[n]; B[3][3 * n + 1] = a[n];
+        B[4][3 * n + 1] = c[n]; B[4][3 * n + 2] = b[n];
+        B[5][3 * n] = c[n]; B[5][3 * n + 2] = a[n];
+    }
+    double E[6][6];
+    memset(E, 0, sizeof(E));
+    double k = young / ((1.0 + poisson) * (1.0 - 2.0 * poisson));
+    double k_nu = k * poisson, k1 = k * (1.0 - poisson), k2 = k * (0.5 - poisson);
+    E[0][0] = k1; E[0][1] = k_nu; E[0][2] = k_nu;
+    E[1][0] = k_nu; E[1][1] = k1; E[1][2] = k_nu;
+    E[2][0] = k_nu; E[2][1] = k_nu; E[2][2] = k1;
+    E[3][3] = k2; E[4][4] = k2; E[5][5] = k2;
+    double EB[6][12];
+    for (int i = 0; i < 6; i++)
+        for (int j = 0; j < 12; j++) {
+            double acc = 0;
+            for (int kk = 0; kk < 6; kk++) acc += E[i][kk] * B[kk][j];
+            EB[i][j] = acc;
+        }
+    for (int i = 0; i < 12; i++)
+        for (int j = 0; j < 12; j++) {
+            double acc = 0;
+            for (int kk = 0; kk < 6; kk++) acc += B[kk][i] * EB[kk][j];
+            K[i][j] = volume * acc;
+        }
+    return volume;
+}
+
+/* ---- Solid -------------------------------------------------------------- */
+
+struct orc_solid {
+    uint32_t N, T;
+    int math;
+    vec3* ref_pos;
+    uint32_t* tets;       /* T*4 */
+    double* volume;       /* T */
+    mat3* inv_Dm;         /* T */
+    mat3* K;              /* T*16, K[e*16 + 4*i + j] = K_ij */
+    mat3* R;              /* T */
+    double* detF;         /* T */
+    vec3 *x, *prev_x, *v, *b, *y;
+    double *r, *d, *q;    /* CG scratch, 3N */
+    double inv_mass;      /* uniform */
+    double total_volume;
+    double density, dt, rel_eps, abs_eps;
+    uint32_t max_iter;
+    vec3 gravity;
+    double rayleigh[2];
+    double factor_M, factor_K;
+    uint32_t n_knc;
+    uint32_t* knc_nid;
+    vec3 *knc_pos, *knc_vel;
+    uint32_t last_iters;
+    double last_rel, last_abs, elastic_energy, potential_energy;
+};
+
+static vec3 load3(const double* p) { return v3(p[0], p[1], p[2]); }
+
+orc_solid* orc_solid_create(uint32_t N, const double* rest, uint32_t T, const uint32_t* tets,
+                            double E, double nu, const double* E_per, const double* nu_per,
+                            double density, double damping_ratio, const double* gravity,
+                            double dt, double rel_eps, double abs_eps, uint32_t max_iter,
+                            int math_mode)
+{
+    if (N == 0 || T == 0) return NULL;
+    orc_solid* s = (orc_solid*)calloc(1, sizeof(orc_solid));
+    s->N = N; s->T = T; s->math = math_mode;
+    s->ref_pos = (vec3*)malloc(sizeof(vec3) * N);
+    s->tets = (uint32_t*)malloc(sizeof(uint32_t) * 4 * (size_t)T);
+    s->volume = (double*)malloc(sizeof(double) * T);
+    s->inv_Dm = (mat3*)malloc(sizeof(mat3) * T);
+    s->K = (mat3*)malloc(sizeof(mat3) * 16 * (size_t)T);
+    s->R = (mat3*)malloc(sizeof(mat3) * T);
+    s->detF = (double*)malloc(sizeof(double) * T);
+    s->x = (vec3*)malloc(sizeof(vec3) * N);
+    s->prev_x = (vec3*)malloc(sizeof(vec3) * N);
+    s->v = (vec3*)calloc(N, sizeof(vec3));
+    s->b = (vec3*)calloc(N, sizeof(vec3));
+    s->y = (vec3*)calloc(N, sizeof(vec3));
+    s->r = (double*)malloc(sizeof(double) * 3 * N);
+    s->d = (double*)malloc(sizeof(double) * 3 * N);
+    s->q = (double*)malloc(sizeof(double) * 3 * N);
+    for (uint32_t i = 0; i < N; i++) s->ref_pos[i] = s->x[i] = s->prev_x[i] = load3(rest + 3 * i);
+    memcpy(s->tets, tets, sizeof(uint32_t) * 4 * (size_t)T);
+    /* EditableTetrahedronElementSet3::EndEdition (TetrahedronElementSet3.cpp:2113-2166) */
+    double acc_total_volume = 0;
+    for (uint32_t e = 0; e < T; e++) {
+        const uint32_t* t = tets + 4 * (size_t)e;
+        vec3 r0 = s->ref_pos[t[0]], r1 = s->ref_pos[t[1]], r2 = s->ref_pos[t[2]], r3 = s->ref_pos[t[3]];
+        s->volume[e] = compute_volume(r0, r1, r2, r3);
+        acc_total_volume += s->volume[e];
+        double K[12][12];
+        double Ee = E_per ? E_per[e] : E, nue = nu_per ? nu_per[e] : nu;
+        compute_K(r0, r1, r2, r3, Ee, nue, K);
+        for (int bi = 0; bi < 4; bi++)
+            for (int bj = 0; bj < 4; bj++)
+                for (int i = 0; i < 3; i++)
+                    for (int j = 0; j < 3; j++) s->K[16 * (size_t)e + 4 * bi + bj].m[i][j] = K[3 * bi + i][3 * bj + j];
+        mat3 Dm = compute_D(r0, r1, r2, r3);
+        s->inv_Dm[e] = m_inverse(&Dm);
+        /* CreateCache: R = I, detF = 1 (TetrahedronElementSet3.cpp:190-209) */
+        memset(&s->R[e], 0, sizeof(mat3));
+        s->R[e].m[0][0] = s->R[e].m[1][1] = s->R[e].m[2][2] = 1;
+        s->detF[e] = 1;
+    }
+    s->total_volume = acc_total_volume;
+    s->density = density; s->dt = dt; s->rel_eps = rel_eps; s->abs_eps = abs_eps;
+    s->max_iter = max_iter;
+    s->gravity = load3(gravity);
+    /* RebuildMass: m = rho * sum(V) / N, stored as its reciprocal
+     * (LeafDSH_Solid3D_FEM.cpp:1591-1611, ParticleSystem.h:80) */
+    double total_mass = density * s->total_volume;
+    double mass_per_node = total_mass / N;
+    s->inv_mass = (double)1.0f / mass_per_node;
+    /* RebuildRayleighCoeffsFromFreqs (LeafDSH_Solid3D_FEM.h:347-354) with
+     * the default frequencies 0.1f and 10000.0f (Params.h:79) */
+    {
+        double f1 = (double)0.1f, f2 = (double)10000.0f;
+        double o00 = 1.0 / f1, o01 = f1, o10 = 1.0 / f2, o11 = f2;
+        double det = o00 * o11 - o10 * o01;
+        double inv_det = 1.0 / det;
+        double i00 = inv_det * o11, i01 = -inv_det * o01, i10 = -inv_det * o10, i11 = inv_det * o00;
+        double z0 = 2 * damping_ratio, z1 = 2 * damping_ratio;
+        double acc0 = 0, acc1 = 0;
+        acc0 += i00 * z0; acc0 += i01 * z1;
+        acc1 += i10 * z0; acc1 += i11 * z1;
+        s->rayleigh[0] = acc0;
+        s->rayleigh[1] = acc1;
+    }
+    return s;
+}
+
+void orc_solid_destroy(orc_solid* s)
+{
+    if (!s) return;
+    free(s->ref_pos); free(s->tets); free(s->volume); free(s->inv_Dm); free(s->K); free(s->R);
+    free(s->detF); free(s->x); free(s->prev_x); free(s->v); free(s->b); free(s->y);
+    free(s->r); free(s->d); free(s->q);
+    free(s->knc_nid); free(s->knc_pos); free(s->knc_vel);
+    free(s);
+}
+
+double orc_solid_total_volume(const orc_solid* s) { return s->total_volume; }
+double orc_solid_node_mass(const orc_solid* s) { return 1.0 / s->inv_mass; }
+void orc_solid_rayleigh(const orc_solid* s, double* out2) { out2[0] = s->rayleigh[0]; out2[1] = s->rayleigh[1]; }
+
+void orc_solid_element_K(const orc_solid* s, uint32_t e, double* K144)
+{
+    memcpy(K144, &s->K[16 * (size_t)e], sizeof(mat3) * 16);
+}
+
+void orc_solid_set_knc(orc_solid* s, uint32_t count, const uint32_t* nodes, const double* targets)
+{
+    free(s->knc_nid); free(s->knc_pos); free(s->knc_vel);
+    s->n_knc = count;
+    s->knc_nid = (uint32_t*)malloc(sizeof(uint32_t) * (count ? count : 1));
+    s->knc_pos = (vec3*)malloc(sizeof(vec3) * (count ? count : 1));
+    s->knc_vel = (vec3*)calloc(count ? count : 1, sizeof(vec3));
+    for (uint32_t k = 0; k < count; k++) {
+        s->knc_nid[k] = nodes[k];
+        s->knc_pos[k] = load3(targets + 3 * k);
+    }
+}
+
+void orc_solid_set_knc_targets(orc_solid* s, const double* targets)
+{
+    for (uint32_t k = 0; k < s->n_knc; k++) s->knc_pos[k] = load3(targets + 3 * k);
+}
+
+void orc_solid_set_state(orc_solid* s, const double* x, const double* v)
+{
+    for (uint32_t i = 0; i < s->N; i++) {
+        if (x) { s->x[i] = load3(x + 3 * i); s->prev_x[i] = s->x[i]; }
+        if (v) s->v[i] = load3(v + 3 * i);
+    }
+}
+
+void orc_solid_get_state(const orc_solid* s, double* x, double* v)
+{
+    for (uint32_t i = 0; i < s->N; i++)
+        for (int c = 0; c < 3; c++) {
+            if (x) x[3 * i + c] = s->x[i].v[c];
+            if (v) v[3 * i + c] = s->v[i].v[c];
+        }
+}
+
+/* BeginEvaluation for C_WRP + MSVD (TetrahedronElementSet3.cpp:219-281,777-792):
+ * Ds, F = Ds * Dm^-1, det F, R. The degeneration bookkeeping (DoC) does not
+ * feed this path and is not formed. */
+static void begin_evaluation(orc_solid* s)
+{
+    for (uint32_t e = 0; e < s->T; e++) {
+        const uint32_t* t = s->tets + 4 * (size_t)e;
+        mat3 Ds = compute_D(s->x[t[0]], s->x[t[1]], s->x[t[2]], s->x[t[3]]);
+        mat3 F = m_mul(&Ds, &s->inv_Dm[e]);
+        s->detF[e] = m_det(&F);
+        s->R[e] = rotation_msvd(&F);
+    }
+}
+
+/* C_f_e (TetrahedronElementSet3.cpp:1053-1096): f_i -= R sum_j K_ij (R^T x_j - r_j) */
+static void f_e_acc(const orc_solid* s, const vec3* x, vec3* f)
+{
+    for (uint32_t e = 0; e < s->T; e++) {
+        const uint32_t* t = s->tets + 4 * (size_t)e;
+        const mat3* K = &s->K[16 * (size_t)e];
+        mat3 Rt = m_transposed(&s->R[e]);
+        vec3 u[4];
+        for (int i = 0; i < 4; i++) u[i] = v_sub(m_mulv(&Rt, x[t[i]]), s->ref_pos[t[i]]);
+        for (int i = 0; i < 4; i++) {
+            vec3 acc = v_add(v_add(v_add(m_mulv(&K[4 * i], u[0]), m_mulv(&K[4 * i + 1], u[1])),
+                                   m_mulv(&K[4 * i + 2], u[2])), m_mulv(&K[4 * i + 3], u[3]));
+            f[t[i]] = v_sub(f[t[i]], m_mulv(&s->R[e], acc));
+        }
+    }
+}
+
+/* C_df_x with truncated differentials (TetrahedronElementSet3.cpp:1761-1836):
+ * df_i -= R sum_j K_ij R^T dx_j */
+static void df_x_acc(const orc_solid* s, const vec3* dx, vec3* df)
+{
+    for (uint32_t e = 0; e < s->T; e++) {
+        const uint32_t* t = s->tets + 4 * (size_t)e;
+        const mat3* K = &s->K[16 * (size_t)e];
+        mat3 Rt = m_transposed(&s->R[e]);
+        vec3 l[4];
+        for (int i = 0; i < 4; i++) l[i] = m_mulv(&Rt, dx[t[i]]);
+        for (int i = 0; i < 4; i++) {
+            vec3 acc = v_add(v_add(v_add(m_mulv(&K[4 * i], l[0]), m_mulv(&K[4 * i + 1], l[1])),
+                                   m_mulv(&K[4 * i + 2], l[2])), m_mulv(&K[4 * i + 3], l[3]));
+            df[t[i]] = v_sub(df[t[i]], m_mulv(&s->R[e], acc));
+        }
+    }
+}
+
+/* C_V (TetrahedronElementSet3.cpp:1456-1488) */
+static double elastic_V(const orc_solid* s)
+{
+    double acc_twice_V = 0;
+    for (uint32_t e = 0; e < s->T; e++) {
+        const uint32_t* t = s->tets + 4 * (size_t)e;
+        const mat3* K = &s->K[16 * (size_t)e];
+        mat3 Rt = m_transposed(&s->R[e]);
+        vec3 u[4];
+        for (int i = 0; i < 4; i++) u[i] = v_sub(m_mulv(&Rt, s->x[t[i]]), s->ref_pos[t[i]]);
+        for (int i = 0; i < 4; i++) {
+            vec3 acc = v_add(v_add(v_add(m_mulv(&K[4 * i], u[0]), m_mulv(&K[4 * i + 1], u[1])),
+                                   m_mulv(&K[4 * i + 2], u[2])), m_mulv(&K[4 * i + 3], u[3]));
+            acc_twice_V += v_dot(u[i], acc);
+        }
+    }
+    return 0.5 * acc_twice_V;
+}
+
+/* LS_ZeroKNC (LeafDSH_Solid3D_FEM.cpp:1045-1053) */
+static void zero_knc(const orc_solid* s, double* v)
+{
+    for (uint32_t k = 0; k < s->n_knc; k++) {
+        uint32_t n = s->knc_nid[k];
+        v[3 * n] = 0; v[3 * n + 1] = 0; v[3 * n + 2] = 0;
+    }
+}
+
+/* LS_A_times_d (LeafDSH_Solid3D_FEM.cpp:1056-1079) */
+static void a_times_d(const orc_solid* s, double factor_M, double factor_K, const double* d, double* q)
+{
+    const uint32_t n3 = 3 * s->N;
+    memset(q, 0, sizeof(double) * n3);
+    df_x_acc(s, (const vec3*)d, (vec3*)q);
+    for (uint32_t i = 0; i < n3; i++) q[i] *= -factor_K;
+    double mass = 1.0 / s->inv_mass;
+    for (uint32_t i = 0; i < s->N; i++) {
+        double factor = mass * factor_M;
+        q[3 * i] += factor * d[3 * i];
+        q[3 * i + 1] += factor * d[3 * i + 1];
+        q[3 * i + 2] += factor * d[3 * i + 2];
+    }
+}
+
+/* ILSS_CG::Solve (src/Saphyre2/ns/ILSS_CG.h:38-151) with the scalar
+ * real_array kernels (src/Saphyre2/ns/real_array.h:91-113). */
+static void cg_solve(orc_solid* s, double* x, const double* b)
+{
+    const uint32_t n = 3 * s->N;
+    double *r = s->r, *d = s->d, *q = s->q;
+    double abs_epsilon_sq = s->abs_eps * s->abs_eps;
+    a_times_d(s, s->factor_M, s->factor_K, x, r);
+    for (uint32_t i = 0; i < n; i++) r[i] = -1 * r[i] + b[i];
+    zero_knc(s, r);
+    memcpy(d, r, sizeof(double) * n);
+    double delta_0 = 0;
+    for (uint32_t i = 0; i < n; i++) delta_0 += r[i] * r[i];
+    double delta_new = delta_0, delta_old = delta_0;
+    uint32_t k = 0;
+    double delta_target = (s->rel_eps * s->rel_eps) * delta_0;
+    while (delta_new > abs_epsilon_sq && delta_new > delta_target && k < s->max_iter) {
+        a_times_d(s, s->factor_M, s->factor_K, d, q);
+        zero_knc(s, q);
+        double dot_d_q = 0;
+        for (uint32_t i = 0; i < n; i++) dot_d_q += d[i] * q[i];
+        if (fabs(dot_d_q) < abs_epsilon_sq) break;
+        double alpha = delta_new / dot_d_q;
+        for (uint32_t i = 0; i < n; i++) x[i] += alpha * d[i];
+        double neg_alpha = -alpha;
+        for (uint32_t i = 0; i < n; i++) r[i] += neg_alpha * q[i];
+        delta_old = delta_new;
+        delta_new = 0;
+        for (uint32_t i = 0; i < n; i++) delta_new += r[i] * r[i];
+        double beta = delta_new / delta_old;
+        for (uint32_t i = 0; i < n; i++) d[i] = beta * d[i] + r[i];
+        zero_knc(s, d);
+        k++;
+    }
+    s->last_iters = k;
+    s->last_rel = (delta_0 > 0) ? mal_sqrt(delta_new / delta_0) : 0;
+    s->last_abs = mal_sqrt(delta_new);
+}
+
+/* FixedStep (LeafDSH_Solid3D_FEM.cpp:898-990) with
+ * Step_QuasiImplicitEuler_v (LeafDSH_Solid3D_FEM.cpp:1205-1328). */
+void orc_solid_fixed_step(orc_solid* s)
+{
+    g_math = s->math;
+    const uint32_t N = s->N;
+    const double dt = s->dt;
+    begin_evaluation(s);
+    for (uint32_t i = 0; i < N; i++) s->prev_x[i] = s->x[i];
+    double inv_dt = 1.0 / dt;
+    double mass = 1.0 / s->inv_mass;
+    for (uint32_t i = 0; i < N; i++) s->b[i] = v3(0, 0, 0);
+    for (uint32_t i = 0; i < N; i++) s->b[i] = v_add(s->b[i], v_scale(mass, s->gravity));
+    f_e_acc(s, s->x, s->b);
+    for (uint32_t i = 0; i < N; i++) s->b[i] = v_scale(dt, s->b[i]);
+    for (uint32_t i = 0; i < N; i++) s->b[i] = v_add(s->b[i], v_scale(mass, s->v[i]));
+    for (uint32_t i = 0; i < N; i++) s->y[i] = s->v[i];
+    for (uint32_t k = 0; k < s->n_knc; k++) {
+        uint32_t nid = s->knc_nid[k];
+        vec3 vk = v_scale(inv_dt, v_sub(s->knc_pos[k], s->x[nid]));
+        double norm_vk = v_norm(vk);
+        if (norm_vk > (double)0.001f) {
+            double clamp = (norm_vk < 50.0) ? norm_vk : 50.0;
+            s->knc_vel[k] = v_scale(clamp, v_normalized(vk));
+        } else {
+            s->knc_vel[k] = v3(0, 0, 0);
+        }
+        s->b[nid] = s->knc_vel[k];
+        s->y[nid] = s->knc_vel[k];
+    }
+    s->factor_M = 1.0 + dt * s->rayleigh[0];
+    s->factor_K = dt * dt + dt * s->rayleigh[1];
+    cg_solve(s, (double*)s->y, (const double*)s->b);
+    for (uint32_t i = 0; i < N; i++) {
+        s->v[i] = s->y[i];
+        s->x[i] = v_add(s->x[i], v_scale(dt, s->y[i]));
+    }
+    s->elastic_energy = elastic_V(s);
+    /* RecomputeEnergy, potential part (LeafDSH_Solid3D_FEM.cpp:1554-1584) */
+    double pe = 0;
+    for (uint32_t e = 0; e < s->T; e++) {
+        const uint32_t* t = s->tets + 4 * (size_t)e;
+        double element_mass = s->density * s->volume[e];
+        vec3 sum = v_add(v_add(v_add(s->x[t[0]], s->x[t[1]]), s->x[t[2]]), s->x[t[3]]);
+        pe += (element_mass / 4.0) * v_dot(sum, v_neg(s->gravity));
+    }
+    s->potential_energy = pe;
+}
+
+void orc_solid_last_stats(const orc_solid* s, uint32_t* iters, double* rel_res, double* abs_res,
+                          double* elastic_energy, double* potential_energy)
+{
+    if (iters) *iters = s->last_iters;
+    if (rel_res) *rel_res = s->last_rel;
+    if (abs_res) *abs_res = s->last_abs;
+    if (elastic_energy) *elastic_energy = s->elastic_energy;
+    if (potential_energy) *potential_energy = s->potential_energy;
+}
+
+void orc_solid_begin_eval(orc_solid* s, const double* x)
+{
+    g_math = s->math;
+    for (uint32_t i = 0; i < s->N; i++) s->x[i] = load3(x + 3 * i);
+    begin_evaluation(s);
+}
+
+void orc_solid_rotations(const orc_solid* s, double* R_out)
+{
+    for (uint32_t e = 0; e < s->T; e++) memcpy(R_out + 9 * (size_t)e, s->R[e].m, sizeof(mat3));
+}
+
+void orc_solid_detF(const orc_solid* s, double* detF_out)
+{
+    memcpy(detF_out, s->detF, sizeof(double) * s->T);
+}
+
+void orc_solid_f_e(const orc_solid* s, double* f)
+{
+    f_e_acc(s, s->x, (vec3*)f);
+}
+
+void orc_solid_df_x(const orc_solid* s, const double* dx, double* df)
+{
+    df_x_acc(s, (const vec3*)dx, (vec3*)df);
+}
+
+double orc_solid_V(const orc_solid* s) { return elastic_V(s); }
+
+void orc_solid_apply_A(const orc_solid* s, double factor_M, double factor_K, const double* d, double* q)
+{
+    a_times_d(s, factor_M, factor_K, d, q);
+    zero_knc(s, q);
+}

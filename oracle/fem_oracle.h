@@ -1,0 +1,78 @@
+/* TEST INFRASTRUCTURE ONLY -- the oracle.
+ *
+ * A plain-C restatement of the reference's FP64 corotational linear-tet
+ * implicit-Euler step (Saphyre2: TetrahedronElementSet3 with C_WRP + MSVD +
+ * truncated differentials, ILSS_CG, LeafDSH_Solid3D_FEM::FixedStep with the
+ * quasi-implicit Euler "v" integrator). Each function in fem_oracle.c cites
+ * the reference file:line it follows and keeps the reference's operation
+ * order, so that it reproduces the reference bit-for-bit on the same host.
+ *
+ * Pinning: tests compare it against the reference's own translation units
+ * compiled by oracle/Makefile (oracle/_ref/libfemref*.so) on small meshes,
+ * and the committed fixtures under tests/golden/ were generated from that
+ * reference build.
+ *
+ * Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may
+ * load this library, and only as the checker. The product path never does.
+ *
+ * Differences from the reference, all deliberate:
+ *  - node and element indices are uint32 (the reference's are uint16,
+ *    TetrahedronElementSet3.h:73-74), so large meshes run;
+ *  - Mal's Sqrt/Sin/Cos/ATan2 evaluate through float in the reference even
+ *    when Real is double (RealUtils.h:27,45,48,63). As written, that makes
+ *    the FP64 rotation NaN for any F within about 1e-10 of the identity (the
+ *    squared cofactor norm underflows in float), so every scene starting at
+ *    rest freezes. FEM_ORC_MATH_DOUBLE (the default, and what the CUDA
+ *    kernels do) evaluates the four functions in double;
+ *    FEM_ORC_MATH_FLOAT_LITERAL reproduces the build as written. The
+ *    reference's Sqrt(3) with an int argument (== 1, in every build) is kept
+ *    in both modes.
+ */
+#ifndef FEM_ORACLE_H
+#define FEM_ORACLE_H
+#include <stdint.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum { FEM_ORC_MATH_DOUBLE = 0, FEM_ORC_MATH_FLOAT_LITERAL = 1 };
+
+typedef struct orc_solid orc_solid;
+
+orc_solid* orc_solid_create(uint32_t N, const double* rest, uint32_t T, const uint32_t* tets,
+                            double E, double nu, const double* E_per, const double* nu_per,
+                            double density, double damping_ratio, const double* gravity,
+                            double dt, double rel_eps, double abs_eps, uint32_t max_iter,
+                            int math_mode);
+void orc_solid_destroy(orc_solid* s);
+double orc_solid_total_volume(const orc_solid* s);
+double orc_solid_node_mass(const orc_solid* s);
+void orc_solid_rayleigh(const orc_solid* s, double* out2);
+void orc_solid_set_knc(orc_solid* s, uint32_t count, const uint32_t* nodes, const double* targets);
+void orc_solid_set_knc_targets(orc_solid* s, const double* targets);
+void orc_solid_set_state(orc_solid* s, const double* x, const double* v);
+void orc_solid_get_state(const orc_solid* s, double* x, double* v);
+void orc_solid_fixed_step(orc_solid* s);
+void orc_solid_last_stats(const orc_solid* s, uint32_t* iters, double* rel_res, double* abs_res,
+                          double* elastic_energy, double* potential_energy);
+
+/* Element-level hooks (state: the positions given to begin_eval). */
+void orc_solid_begin_eval(orc_solid* s, const double* x);
+void orc_solid_rotations(const orc_solid* s, double* R_out);   /* T*9 row-major */
+void orc_solid_detF(const orc_solid* s, double* detF_out);     /* T */
+void orc_solid_f_e(const orc_solid* s, double* f);             /* f += f_e */
+void orc_solid_df_x(const orc_solid* s, const double* dx, double* df); /* df += df_x(dx) */
+double orc_solid_V(const orc_solid* s);
+/* q = A d (LS_A_times_d) for the given factors, then the KNC projection. */
+void orc_solid_apply_A(const orc_solid* s, double factor_M, double factor_K, const double* d, double* q);
+
+/* The reference MSVD rotation of one F (row-major). */
+void orc_rotation_svd(const double* F, double* R, int math_mode);
+
+/* The per-element stiffness blocks K_ij (16 row-major 3x3, element e). */
+void orc_solid_element_K(const orc_solid* s, uint32_t e, double* K144);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
