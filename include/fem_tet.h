@@ -1,0 +1,169 @@
+/* fem_tet.h -- C ABI of the GB300-native corotational linear-tetrahedral FEM
+ * implicit-Euler step (the Saphyre2 LeafDSH_Solid3D_FEM / TetrahedronElementSet3 /
+ * ILSS_CG path), implemented by libfemtet_gb300.so with hand-written sm_103a
+ * kernels.
+ *
+ * Conventions
+ *  - Plain pointers and sizes only. Host arrays are caller-owned and copied
+ *    in or out during the call; device state is owned by the handle.
+ *  - Node vectors are AoS xyz triples (N*3 doubles), the reference's Vec3
+ *    array layout (Saphyre2 ParticleSystem m_vecPos/m_vecVel). Tets are T*4
+ *    uint32 node ids (the reference uses uint16, TetrahedronElementSet3.h:73-74).
+ *  - Every entry point returns an int status (FEM_OK on success);
+ *    fem_last_error() gives the message of the last failure on the calling
+ *    thread. The reference returns no errors (asserts only).
+ *  - One CUDA stream per handle; a handle is thread-compatible, not
+ *    thread-safe. All calls on a handle are synchronous unless named _async.
+ */
+#ifndef FEM_TET_H
+#define FEM_TET_H
+#include <stdint.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum fem_status {
+    FEM_OK = 0,
+    FEM_E_ARG = 1,       /* bad argument (null pointer, zero size, out-of-range value) */
+    FEM_E_INDEX = 2,     /* a tet or constraint names a node >= N */
+    FEM_E_NAN = 3,       /* NaN/Inf reached the solver residual */
+    FEM_E_OOM = 4,       /* device allocation failed */
+    FEM_E_CUDA = 5,      /* CUDA runtime error (message in fem_last_error) */
+    FEM_E_TIMEOUT = 6,   /* a bounded device-side wait gave up */
+    FEM_E_NODEVICE = 7,  /* no CUDA device / extension not usable */
+    FEM_E_DEGENERATE = 8 /* a tet has non-positive rest volume */
+};
+
+enum fem_precision {
+    /* Plain FP64: every product, reduction and rotation in double. The
+     * drop-in for the reference's FP64 step. */
+    FEM_PRECISION_FP64 = 0,
+    /* Mixed: FP32 element products and vector updates, FP64 dot products and
+     * norms, FP64 residual refresh r = b - A x every refresh_every
+     * iterations, FP32 rotations re-solved in FP64 where det F <=
+     * degenerate_det_F. */
+    FEM_PRECISION_MIXED = 1
+};
+
+/* Solid parameters. Mirrors bs::Solid3D::Params and Params_Extra
+ * (Saphyre2 bs/Solid3D.h:27-85) for the fields this path reads:
+ * FixedDT, Density, YoungModulus, PoissonRatio, DampingRatio, Gravity,
+ * LS_Iter, LS_RelEpsilon, and the Leaf's LS abs epsilon
+ * (LeafDSH_Solid3D_FEM.h:209-231). Methods are fixed to the reference
+ * defaults: material C_WRP, rotation MSVD, truncated differentials,
+ * QuasiImplicitEuler_v integrator, CG solver with warm start. */
+typedef struct fem_params {
+    double fixed_dt;          /* time step of one FixedStep [s] */
+    double density;           /* rho [kg/m^3]; node mass = rho * sum(V_e) / N */
+    double young_modulus;     /* E [Pa] (ignored where per-element E is given) */
+    double poisson_ratio;     /* nu (ignored where per-element nu is given) */
+    double damping_ratio;     /* zeta; Rayleigh coefficients from the reference's
+                                 default frequencies 0.1 and 1e4 Hz */
+    double gravity[3];        /* [m/s^2] */
+    double ls_rel_epsilon;    /* CG stops when |r|^2 <= rel^2 |r0|^2 */
+    double ls_abs_epsilon;    /* ... or |r|^2 <= abs^2 (and breaks if |d.q| < abs^2) */
+    uint32_t ls_max_iter;     /* CG iteration cap per step */
+    uint32_t precision;       /* enum fem_precision */
+    double degenerate_det_F;  /* mixed only: FP64 rotation re-solve threshold */
+    uint32_t refresh_every;   /* mixed only: FP64 residual refresh period (0 = never) */
+    uint32_t compute_energy;  /* 1: elastic and potential energy every step (as FixedStep) */
+} fem_params;
+
+/* Per-step statistics (the Leaf's per-step LS stats, LeafDSH_Solid3D_FEM.h:597-622). */
+typedef struct fem_step_stats {
+    uint32_t cg_iterations;   /* ILSS_CG::GetNumIterations of the last step */
+    uint32_t status;          /* enum fem_status of the last step */
+    double rel_residual;      /* sqrt(delta_new / delta_0) */
+    double abs_residual;      /* sqrt(delta_new) */
+    double elastic_energy;    /* TetrahedronElementSet3::V after the step */
+    double potential_energy;  /* LeafDSH_Solid3D_FEM::RecomputeEnergy's potential term */
+    uint32_t inverted_elements; /* elements with det F <= 0 at BeginEvaluation */
+    uint32_t fp64_resolved;   /* mixed: elements whose rotation was re-solved in FP64 */
+    uint64_t total_cg_iterations; /* sum over the steps of this call */
+} fem_step_stats;
+
+typedef struct fem_solid_s* fem_solid;
+
+/* Fills the reference defaults (fem::Params, LeafDSH_Solid3D_FEM::Params):
+ * fixed_dt 0.001, density 1000, E 1000, nu 0.25, damping 1, gravity 0,
+ * CG rel 1e-3, abs 1e-6, 20 iterations, FP64, threshold 1e-3, refresh 50,
+ * energy on. */
+int fem_params_default(fem_params* p);
+
+/* Replaces: EditableTetrahedronElementSet3::BeginEdition/AddElement/EndEdition
+ * (TetrahedronElementSet3.cpp:2084-2166), TetrahedronElementSet3::CreateCache
+ * (:190-209) and LeafDSH_Solid3D_FEM::Create (LeafDSH_Solid3D_FEM.cpp:125-223).
+ * rest_xyz: N*3; tets: T*4; young/poisson_per_elem: T each or null.
+ * Node state starts at x = rest, v = 0 (Create, :136-143). */
+int fem_solid_create(const double* rest_xyz, uint32_t N, const uint32_t* tets, uint32_t T,
+                     const fem_params* params, const double* young_per_elem,
+                     const double* poisson_per_elem, fem_solid* out);
+int fem_solid_destroy(fem_solid s);
+int fem_solid_get_sizes(fem_solid s, uint32_t* N, uint32_t* T);
+
+/* Replaces: Solid3D::FixAllNodesInBoundaryPlane / CreateKinematicPointConstraint
+ * -> KinematicNodeConstraintSet3::AddKNC (KinematicNodeConstraintSet3.h:32-40).
+ * Sets the whole constraint list: position constraints on `nodes` with the
+ * given targets (count*3). count == 0 clears it. */
+int fem_solid_set_knc(fem_solid s, const uint32_t* nodes, const double* targets, uint32_t count);
+/* Replaces: Solid3D::SetKinematicPointConstraint_Pos -> SetPosKNC
+ * (KinematicNodeConstraintSet3.h:55-60) for every constraint (count*3). */
+int fem_solid_set_knc_targets(fem_solid s, const double* targets);
+
+/* State [pos|vel] (GLeafDSH_Model::QueryState / Solid3D::Dbg_SaveState);
+ * either pointer may be null. set_state also sets the previous positions. */
+int fem_solid_set_state(fem_solid s, const double* x, const double* v);
+int fem_solid_get_state(fem_solid s, double* x, double* v);
+
+/* Replaces: LeafDSH_Solid3D_FEM::FixedStep (LeafDSH_Solid3D_FEM.cpp:898-990)
+ * with Step_QuasiImplicitEuler_v (:1205-1328), nsteps times. stats may be null. */
+int fem_solid_step(fem_solid s, uint32_t nsteps, fem_step_stats* stats);
+
+/* Host-buffer round trip in one call: upload x,v (may be null = keep),
+ * step nsteps, download x,v (may be null). */
+int fem_solid_step_host(fem_solid s, const double* x_in, const double* v_in, uint32_t nsteps,
+                        double* x_out, double* v_out, fem_step_stats* stats);
+
+/* --- Element-level hooks (the IForce3 seam, TetrahedronElementSet3.h:29-58) --- */
+
+/* Replaces TetrahedronElementSet3::BeginEvaluation (TetrahedronElementSet3.cpp:219-281):
+ * F, det F and the MSVD rotation of every element at positions x (N*3). */
+int fem_solid_begin_eval(fem_solid s, const double* x);
+/* The cached rotations (T*9, row-major) and det F (T) of the last evaluation. */
+int fem_solid_get_rotations(fem_solid s, double* R, double* detF);
+/* f += f_e at the evaluated positions (C_f_e, TetrahedronElementSet3.cpp:1053-1096). N*3. */
+int fem_solid_force_elastic(fem_solid s, double* f);
+/* df += df_x(dx) = -R K0 R^T dx (C_df_x, TetrahedronElementSet3.cpp:1761-1836). N*3. */
+int fem_solid_df_x(fem_solid s, const double* dx, double* df);
+/* q = S (factor_M M d - factor_K df_x(d)) (LS_A_times_d + LS_ZeroKNC,
+ * LeafDSH_Solid3D_FEM.cpp:1045-1079). N*3. */
+int fem_solid_apply_A(fem_solid s, double factor_M, double factor_K, const double* d, double* q);
+/* Elastic energy V at the evaluated positions (C_V, TetrahedronElementSet3.cpp:1456-1488). */
+int fem_solid_energy(fem_solid s, double* V);
+/* Uniform node mass and Rayleigh coefficients (RebuildMass, RebuildRayleighCoeffsFromFreqs). */
+int fem_solid_mass_info(fem_solid s, double* node_mass, double* rayleigh2, double* total_volume);
+
+/* --- Device-resident timing hooks (state stays in HBM) --- */
+/* Enqueue nsteps on the handle's stream without synchronising and without
+ * host copies; stats are left on the device. */
+int fem_solid_step_async(fem_solid s, uint32_t nsteps);
+int fem_solid_synchronize(fem_solid s, fem_step_stats* stats);
+/* The handle's CUDA stream (a cudaStream_t) for event timing. */
+int fem_solid_stream(fem_solid s, void** stream);
+
+/* --- Library --- */
+const char* fem_last_error(void);
+int fem_device_info(int* device, int* sm_count, int* cc_major, int* cc_minor);
+/* Number of kernels this library has launched in the calling process. */
+uint64_t fem_kernel_launches(void);
+/* Kernel timing: while enabled, launches of the named hot kernels
+ * ("elem_spmv_fp64", "node_q_fp64", ...) are bracketed by CUDA events on
+ * their launching stream. fem_profile_enable(1) clears the totals;
+ * fem_profile_read returns the summed event time and launch count. */
+int fem_profile_enable(int on);
+int fem_profile_read(const char* kernel, double* total_ms, unsigned long long* launches);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FEM_TET_H */

@@ -516,6 +516,13 @@ void orc_solid_element_K(const orc_solid* s, uint32_t e, double* K144)
     memcpy(K144, &s->K[16 * (size_t)e], sizeof(mat3) * 16);
 }
 
+void orc_solid_set_solver(orc_solid* s, double rel_eps, double abs_eps, uint32_t max_iter)
+{
+    s->rel_eps = rel_eps;
+    s->abs_eps = abs_eps;
+    s->max_iter = max_iter;
+}
+
 void orc_solid_set_knc(orc_solid* s, uint32_t count, const uint32_t* nodes, const double* targets)
 {
     free(s->knc_nid); free(s->knc_pos); free(s->knc_vel);

@@ -49,6 +49,7 @@ double orc_solid_total_volume(const orc_solid* s);
 double orc_solid_node_mass(const orc_solid* s);
 void orc_solid_rayleigh(const orc_solid* s, double* out2);
 void orc_solid_set_knc(orc_solid* s, uint32_t count, const uint32_t* nodes, const double* targets);
+void orc_solid_set_solver(orc_solid* s, double rel_eps, double abs_eps, uint32_t max_iter);
 void orc_solid_set_knc_targets(orc_solid* s, const double* targets);
 void orc_solid_set_state(orc_solid* s, const double* x, const double* v);
 void orc_solid_get_state(const orc_solid* s, double* x, double* v);

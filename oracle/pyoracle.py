@@ -90,6 +90,7 @@ def _load(path: str, prefix: str):
         lib.orc_solid_apply_A.argtypes = [C.c_void_p, C.c_double, C.c_double, _dp, _dp]
         lib.orc_rotation_svd.argtypes = [_dp, _dp, C.c_int]
         lib.orc_solid_element_K.argtypes = [C.c_void_p, C.c_uint32, _dp]
+        lib.orc_solid_set_solver.argtypes = [C.c_void_p, C.c_double, C.c_double, C.c_uint32]
         lib.orc_solid_total_volume.argtypes = [C.c_void_p]
         lib.orc_solid_total_volume.restype = C.c_double
     else:
@@ -193,6 +194,15 @@ class Solid:
         out = np.empty(2)
         getattr(self.lib, self.p + "solid_rayleigh")(self.h, _ptr(out))
         return out
+
+    def set_solver(self, rel_eps, abs_eps, max_iter):
+        self.lib.orc_solid_set_solver(self.h, rel_eps, abs_eps, max_iter)
+
+    def reset(self):
+        """Back to the scene's initial state (positions at rest, initial velocity)."""
+        v0 = np.zeros_like(self._rest) if self.scene.init_vel is None else self.scene.init_vel
+        self.set_state(self._rest, v0)
+        self.step_index = 0
 
     # ---- element-level hooks (port only) ----
     def begin_eval(self, x):

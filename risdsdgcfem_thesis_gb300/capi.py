@@ -1,0 +1,287 @@
+"""ctypes binding of include/fem_tet.h (libfemtet_gb300.so).
+
+The library is loaded from this package directory only; there is no other
+implementation behind these calls. If the shared library is missing or has
+no usable CUDA device, every entry point raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from typing import Optional
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libfemtet_gb300.so")
+
+FEM_OK = 0
+FEM_E_ARG, FEM_E_INDEX, FEM_E_NAN, FEM_E_OOM, FEM_E_CUDA, FEM_E_TIMEOUT, FEM_E_NODEVICE, FEM_E_DEGENERATE = range(1, 9)
+FEM_PRECISION_FP64 = 0
+FEM_PRECISION_MIXED = 1
+
+_dp = C.POINTER(C.c_double)
+_up = C.POINTER(C.c_uint32)
+
+
+class FemParams(C.Structure):
+    _fields_ = [
+        ("fixed_dt", C.c_double),
+        ("density", C.c_double),
+        ("young_modulus", C.c_double),
+        ("poisson_ratio", C.c_double),
+        ("damping_ratio", C.c_double),
+        ("gravity", C.c_double * 3),
+        ("ls_rel_epsilon", C.c_double),
+        ("ls_abs_epsilon", C.c_double),
+        ("ls_max_iter", C.c_uint32),
+        ("precision", C.c_uint32),
+        ("degenerate_det_F", C.c_double),
+        ("refresh_every", C.c_uint32),
+        ("compute_energy", C.c_uint32),
+    ]
+
+
+class FemStepStats(C.Structure):
+    _fields_ = [
+        ("cg_iterations", C.c_uint32),
+        ("status", C.c_uint32),
+        ("rel_residual", C.c_double),
+        ("abs_residual", C.c_double),
+        ("elastic_energy", C.c_double),
+        ("potential_energy", C.c_double),
+        ("inverted_elements", C.c_uint32),
+        ("fp64_resolved", C.c_uint32),
+        ("total_cg_iterations", C.c_uint64),
+    ]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+class FemError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"fem status {code}: {msg}")
+        self.code = code
+
+
+# Every exported symbol of include/fem_tet.h with its ctypes signature.
+SIGNATURES = {
+    "fem_params_default": (C.c_int, [C.POINTER(FemParams)]),
+    "fem_solid_create": (C.c_int, [_dp, C.c_uint32, _up, C.c_uint32, C.POINTER(FemParams), _dp, _dp,
+                                   C.POINTER(C.c_void_p)]),
+    "fem_solid_destroy": (C.c_int, [C.c_void_p]),
+    "fem_solid_get_sizes": (C.c_int, [C.c_void_p, _up, _up]),
+    "fem_solid_set_knc": (C.c_int, [C.c_void_p, _up, _dp, C.c_uint32]),
+    "fem_solid_set_knc_targets": (C.c_int, [C.c_void_p, _dp]),
+    "fem_solid_set_state": (C.c_int, [C.c_void_p, _dp, _dp]),
+    "fem_solid_get_state": (C.c_int, [C.c_void_p, _dp, _dp]),
+    "fem_solid_step": (C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(FemStepStats)]),
+    "fem_solid_step_host": (C.c_int, [C.c_void_p, _dp, _dp, C.c_uint32, _dp, _dp, C.POINTER(FemStepStats)]),
+    "fem_solid_begin_eval": (C.c_int, [C.c_void_p, _dp]),
+    "fem_solid_get_rotations": (C.c_int, [C.c_void_p, _dp, _dp]),
+    "fem_solid_force_elastic": (C.c_int, [C.c_void_p, _dp]),
+    "fem_solid_df_x": (C.c_int, [C.c_void_p, _dp, _dp]),
+    "fem_solid_apply_A": (C.c_int, [C.c_void_p, C.c_double, C.c_double, _dp, _dp]),
+    "fem_solid_energy": (C.c_int, [C.c_void_p, _dp]),
+    "fem_solid_mass_info": (C.c_int, [C.c_void_p, _dp, _dp, _dp]),
+    "fem_solid_step_async": (C.c_int, [C.c_void_p, C.c_uint32]),
+    "fem_solid_synchronize": (C.c_int, [C.c_void_p, C.POINTER(FemStepStats)]),
+    "fem_solid_stream": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
+    "fem_last_error": (C.c_char_p, []),
+    "fem_device_info": (C.c_int, [C.POINTER(C.c_int)] * 4),
+    "fem_kernel_launches": (C.c_uint64, []),
+    "fem_profile_enable": (C.c_int, [C.c_int]),
+    "fem_profile_read": (C.c_int, [C.c_char_p, _dp, C.POINTER(C.c_ulonglong)]),
+}
+
+_lib = None
+
+
+def load():
+    """Load libfemtet_gb300.so from the package directory (raises if absent)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise FemError(FEM_E_NODEVICE, f"{LIB_PATH} is missing: run __graft_entry__.build()")
+    lib = C.CDLL(LIB_PATH)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def check(code):
+    if code != FEM_OK:
+        raise FemError(code, load().fem_last_error().decode(errors="replace"))
+
+
+def _ptr(a, ctype=C.c_double):
+    return None if a is None else a.ctypes.data_as(C.POINTER(ctype))
+
+
+def _f64(a):
+    return None if a is None else np.ascontiguousarray(a, dtype=np.float64)
+
+
+def default_params() -> FemParams:
+    p = FemParams()
+    check(load().fem_params_default(C.byref(p)))
+    return p
+
+
+def params_for(scene, precision: int = FEM_PRECISION_FP64, compute_energy: bool = True) -> FemParams:
+    p = default_params()
+    p.fixed_dt = scene.dt
+    p.density = scene.density
+    p.young_modulus = scene.young
+    p.poisson_ratio = scene.poisson
+    p.damping_ratio = scene.damping_ratio
+    for i in range(3):
+        p.gravity[i] = scene.gravity[i]
+    p.ls_rel_epsilon = scene.rel_eps
+    p.ls_abs_epsilon = scene.abs_eps
+    p.ls_max_iter = scene.max_iter
+    p.precision = precision
+    p.compute_energy = 1 if compute_energy else 0
+    return p
+
+
+class Solid:
+    """One device-resident solid (the Solid3D / LeafDSH_Solid3D_FEM seam)."""
+
+    def __init__(self, scene, precision: int = FEM_PRECISION_FP64, compute_energy: bool = True,
+                 params: Optional[FemParams] = None):
+        lib = load()
+        self.lib = lib
+        self.scene = scene
+        self.N = scene.num_nodes
+        self.T = scene.num_tets
+        self.params = params if params is not None else params_for(scene, precision, compute_energy)
+        rest = _f64(scene.rest)
+        tets = np.ascontiguousarray(scene.tets, dtype=np.uint32)
+        Ep = _f64(scene.young_per_elem)
+        nup = _f64(scene.poisson_per_elem)
+        h = C.c_void_p()
+        check(lib.fem_solid_create(_ptr(rest), self.N, _ptr(tets, C.c_uint32), self.T, C.byref(self.params),
+                                   _ptr(Ep), _ptr(nup), C.byref(h)))
+        self.h = h
+        self._knc_nodes = np.ascontiguousarray(scene.knc_nodes, dtype=np.uint32)
+        if self._knc_nodes.size:
+            tg = _f64(scene.targets_at(0) if scene.knc_schedule is not None else scene.knc_targets)
+            check(lib.fem_solid_set_knc(h, _ptr(self._knc_nodes, C.c_uint32), _ptr(tg), self._knc_nodes.size))
+        if scene.init_vel is not None:
+            self.set_state(v=scene.init_vel)
+        self.step_index = 0
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.fem_solid_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_state(self, x=None, v=None):
+        x, v = _f64(x), _f64(v)
+        check(self.lib.fem_solid_set_state(self.h, _ptr(x), _ptr(v)))
+
+    def state(self):
+        x = np.empty((self.N, 3))
+        v = np.empty((self.N, 3))
+        check(self.lib.fem_solid_get_state(self.h, _ptr(x), _ptr(v)))
+        return x, v
+
+    def set_knc_targets(self, targets):
+        t = _f64(targets)
+        check(self.lib.fem_solid_set_knc_targets(self.h, _ptr(t)))
+
+    def step(self, n: int = 1):
+        st = FemStepStats()
+        sc = self.scene
+        if sc.knc_schedule is not None and self._knc_nodes.size:
+            out = []
+            for _ in range(n):
+                self.set_knc_targets(sc.targets_at(self.step_index))
+                check(self.lib.fem_solid_step(self.h, 1, C.byref(st)))
+                self.step_index += 1
+                out.append(st.as_dict())
+            return out[-1]
+        check(self.lib.fem_solid_step(self.h, n, C.byref(st)))
+        self.step_index += n
+        return st.as_dict()
+
+    def run(self, steps=None):
+        steps = self.scene.steps if steps is None else steps
+        return [self.step(1) for _ in range(steps)]
+
+    # ---- element-level hooks ----
+    def begin_eval(self, x):
+        x = _f64(x)
+        check(self.lib.fem_solid_begin_eval(self.h, _ptr(x)))
+
+    def rotations(self):
+        R = np.empty((self.T, 3, 3))
+        d = np.empty(self.T)
+        check(self.lib.fem_solid_get_rotations(self.h, _ptr(R), _ptr(d)))
+        return R, d
+
+    def f_e(self):
+        f = np.zeros((self.N, 3))
+        check(self.lib.fem_solid_force_elastic(self.h, _ptr(f)))
+        return f
+
+    def df_x(self, dx):
+        dx = _f64(dx)
+        df = np.zeros((self.N, 3))
+        check(self.lib.fem_solid_df_x(self.h, _ptr(dx), _ptr(df)))
+        return df
+
+    def apply_A(self, factor_M, factor_K, d):
+        d = _f64(d)
+        q = np.zeros((self.N, 3))
+        check(self.lib.fem_solid_apply_A(self.h, factor_M, factor_K, _ptr(d), _ptr(q)))
+        return q
+
+    def V(self):
+        v = C.c_double()
+        check(self.lib.fem_solid_energy(self.h, C.byref(v)))
+        return v.value
+
+    def mass_info(self):
+        m, tv = C.c_double(), C.c_double()
+        ray = np.empty(2)
+        check(self.lib.fem_solid_mass_info(self.h, C.byref(m), _ptr(ray), C.byref(tv)))
+        return m.value, ray, tv.value
+
+    def stream(self):
+        s = C.c_void_p()
+        check(self.lib.fem_solid_stream(self.h, C.byref(s)))
+        return s.value
+
+
+def kernel_launches() -> int:
+    return int(load().fem_kernel_launches())
+
+
+def profile_enable(on: bool = True) -> None:
+    load().fem_profile_enable(1 if on else 0)
+
+
+def profile_read(kernel: str):
+    ms = C.c_double()
+    n = C.c_ulonglong()
+    load().fem_profile_read(kernel.encode(), C.byref(ms), C.byref(n))
+    return ms.value, n.value
+
+
+def device_info():
+    vals = [C.c_int() for _ in range(4)]
+    check(load().fem_device_info(*[C.byref(v) for v in vals]))
+    return {"device": vals[0].value, "sm_count": vals[1].value, "cc": (vals[2].value, vals[3].value)}

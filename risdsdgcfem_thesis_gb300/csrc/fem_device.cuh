@@ -1,0 +1,102 @@
+// fem_device.cuh -- device-side data layout and launcher declarations shared
+// by the kernels (fem_kernels.cu, rotation.cu) and the host runtime (solid.cu).
+//
+// Layout in HBM for one solid (T tets, N nodes):
+//   tets      int4[T]          node ids of each tet
+//   Dinv      S[9][T]          Dm^-1 of each tet, row-major, component-major
+//                              arrays (coalesced per component)
+//   mat       S[3][T]          V*(lambda+2mu), V*lambda, V*mu of each tet (the
+//                              entries a_k1, a_nu, a_k2 of the reference's E
+//                              matrix, TetrahedronElement3.h:141-156, times V)
+//   R         S[9][T]          cached rotation, detF double[T]
+//   node vectors (x, v, y, b, r, d, q, rest): AoS xyz, 3N scalars, the
+//                              reference's Vec3 array layout
+//   eout      S[T][4][3]       per-element nodal products, gathered per node
+//   csr_ptr/csr_idx            node -> (4*e + slot) entries in element order,
+//                              the order the reference scatters in
+//   fixed     uint8[N]         1 where a kinematic node constraint zeroes the row
+// S is double on the FP64 path and float on the mixed path.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace femgb {
+
+// Device-resident CG and step scalars of one solid.
+struct StepScalars {
+    double delta_new, delta_old, delta_0, delta_target, abs_eps_sq;
+    double alpha, beta, dot_dq;
+    double elastic_energy, potential_energy;
+    double rel_residual, abs_residual;
+    uint32_t k, max_iter, done, status;
+    uint32_t inverted, fp64_resolved, refresh_every, pad;
+    unsigned long long total_iters;
+};
+
+template <typename S>
+struct MeshView {
+    uint32_t N, T;
+    const int4* tets;
+    const S* Dinv;     // [9][T]
+    const S* mat;      // [3][T]
+    S* R;              // [9][T]
+    double* detF;      // [T]
+    const double* vol; // [T]
+    const double* rest;          // [3N] (double)
+    const uint32_t* csr_ptr;     // [N+1]
+    const uint32_t* csr_idx;     // [4T]
+    const uint8_t* fixed;        // [N]
+    S* eout;                     // [12T]
+};
+
+struct StepConsts {
+    double dt, inv_dt, mass, factor_M, factor_K;
+    double gravity[3];
+    double density;
+    double rel_eps_sq, abs_eps_sq;
+    uint32_t max_iter;
+};
+
+constexpr int kBlock = 256;
+constexpr int kFinalizeThreads = 512;
+
+// ---- launchers (fem_kernels.cu / rotation.cu) ----
+void launch_begin_eval_fp64(const MeshView<double>& m, const double* x, double* F_out, StepScalars* st,
+                            cudaStream_t s);
+void launch_elem_spmv_fp64(const MeshView<double>& m, const double* d, const StepScalars* st, int check_done,
+                           cudaStream_t s);
+void launch_elem_force_fp64(const MeshView<double>& m, const double* x, int write_out, double* energy_partials,
+                            cudaStream_t s);
+void launch_node_b_fp64(const MeshView<double>& m, const StepConsts& c, const double* v, double* b, double* y,
+                        cudaStream_t s);
+void launch_knc_fp64(uint32_t count, const uint32_t* nodes, const double* targets, const double* x,
+                     const StepConsts& c, double* b, double* y, cudaStream_t s);
+void launch_node_residual_fp64(const MeshView<double>& m, const StepConsts& c, const double* b, const double* y,
+                               double* r, double* d, double* partials, cudaStream_t s);
+void launch_node_q_fp64(const MeshView<double>& m, const StepConsts& c, const double* d, double* q,
+                        double* partials, const StepScalars* st, cudaStream_t s);
+void launch_node_xr_fp64(uint32_t N, double* y, double* r, const double* d, const double* q, double* partials,
+                         const StepScalars* st, cudaStream_t s);
+void launch_node_d_fp64(uint32_t N, const uint8_t* fixed, double* d, const double* r, const StepScalars* st,
+                        cudaStream_t s);
+void launch_integrate_fp64(uint32_t N, double dt, double* x, double* v, const double* y, cudaStream_t s);
+void launch_potential_fp64(const MeshView<double>& m, const StepConsts& c, const double* x, double* partials,
+                           cudaStream_t s);
+void launch_apply_A_fp64(const MeshView<double>& m, double factor_M, double factor_K, double mass,
+                         const double* d, double* q, cudaStream_t s);
+void launch_gather_sum_fp64(const MeshView<double>& m, double sign, double* f, cudaStream_t s);
+
+// finalizers: one block, fixed-order sums of `count` block partials
+enum FinalizeKind { FIN_INIT = 0, FIN_ALPHA = 1, FIN_BETA = 2, FIN_ENERGY_E = 3, FIN_ENERGY_P = 4, FIN_STATS = 5 };
+void launch_finalize(int kind, const double* partials, uint32_t count, const StepConsts& c, StepScalars* st,
+                     cudaStream_t s);
+
+uint32_t grid_for(uint32_t n);    // grid size of the grid-stride kernels
+uint64_t& launch_counter();       // kernels launched by this library
+
+// Optional per-kernel timing with CUDA events recorded on the launching
+// stream around each launch of a named kernel (off unless enabled).
+void prof_begin(const char* name, cudaStream_t s);
+void prof_end(const char* name, cudaStream_t s);
+bool prof_enabled();
+}  // namespace femgb

@@ -1,0 +1,636 @@
+// fem_kernels.cu -- FP64 element products, node gathers and CG vector
+// kernels of the corotational linear-tet implicit-Euler step.
+//
+// Element products use the strain form of K0 = V B^T E B
+// (TetrahedronElement3::Compute_K, TetrahedronElement3.h:157-173): with
+// Dm^-1 rows = gradients of the shape functions of nodes 1..3 and node 0's
+// the negative sum, K0 u = V B^T sigma(eps(u)), eps = sym(H),
+// H = [u1-u0, u2-u0, u3-u0] Dm^-1. Mathematically identical to the
+// reference's 16 stored 3x3 blocks; 9+3 scalars per element instead of 144
+// and about 140 FMA per product instead of 216.
+//
+// Scatter is atomics-free: each element writes its four nodal vectors to
+// eout, and one thread per node sums its entries in element order (the order
+// the reference's serial scatter adds them). Reductions are deterministic:
+// warp shuffles, a fixed block tree, then one block summing the block
+// partials in index order.
+#include "fem_device.cuh"
+#include "msvd.cuh"
+
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+namespace femgb {
+
+// ---- kernel timing (events on the launching stream) ----
+namespace {
+struct ProfSlot {
+    std::vector<cudaEvent_t> starts, stops;
+    double done_ms = 0.0;
+    unsigned long long done_count = 0;
+};
+std::mutex g_prof_mu;
+bool g_prof_on = false;
+std::map<std::string, ProfSlot> g_prof;
+std::vector<cudaEvent_t> g_event_pool;
+
+cudaEvent_t pool_event()
+{
+    if (!g_event_pool.empty()) {
+        cudaEvent_t e = g_event_pool.back();
+        g_event_pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    return e;
+}
+}  // namespace
+
+bool prof_enabled() { return g_prof_on; }
+
+void prof_begin(const char* name, cudaStream_t s)
+{
+    if (!g_prof_on) return;
+    std::lock_guard<std::mutex> lk(g_prof_mu);
+    cudaEvent_t e = pool_event();
+    cudaEventRecord(e, s);
+    g_prof[name].starts.push_back(e);
+}
+
+void prof_end(const char* name, cudaStream_t s)
+{
+    if (!g_prof_on) return;
+    std::lock_guard<std::mutex> lk(g_prof_mu);
+    cudaEvent_t e = pool_event();
+    cudaEventRecord(e, s);
+    g_prof[name].stops.push_back(e);
+}
+
+// Folds completed event pairs into the totals (synchronises on the events).
+static void prof_collect()
+{
+    for (auto& kv : g_prof) {
+        ProfSlot& sl = kv.second;
+        const size_t n = sl.stops.size() < sl.starts.size() ? sl.stops.size() : sl.starts.size();
+        for (size_t i = 0; i < n; i++) {
+            float ms = 0.f;
+            cudaEventSynchronize(sl.stops[i]);
+            cudaEventElapsedTime(&ms, sl.starts[i], sl.stops[i]);
+            sl.done_ms += ms;
+            sl.done_count++;
+            g_event_pool.push_back(sl.starts[i]);
+            g_event_pool.push_back(sl.stops[i]);
+        }
+        sl.starts.erase(sl.starts.begin(), sl.starts.begin() + n);
+        sl.stops.erase(sl.stops.begin(), sl.stops.begin() + n);
+    }
+}
+
+}  // namespace femgb
+
+extern "C" int fem_profile_enable(int on)
+{
+    std::lock_guard<std::mutex> lk(femgb::g_prof_mu);
+    femgb::prof_collect();
+    femgb::g_prof_on = on != 0;
+    if (on) femgb::g_prof.clear();
+    return 0;
+}
+
+extern "C" int fem_profile_read(const char* kernel, double* total_ms, unsigned long long* launches)
+{
+    std::lock_guard<std::mutex> lk(femgb::g_prof_mu);
+    femgb::prof_collect();
+    auto it = femgb::g_prof.find(kernel ? kernel : "");
+    if (total_ms) *total_ms = it == femgb::g_prof.end() ? 0.0 : it->second.done_ms;
+    if (launches) *launches = it == femgb::g_prof.end() ? 0ull : it->second.done_count;
+    return 0;
+}
+
+namespace femgb {
+
+uint64_t& launch_counter()
+{
+    static uint64_t n = 0;
+    return n;
+}
+
+uint32_t grid_for(uint32_t n)
+{
+    uint32_t g = (n + kBlock - 1) / kBlock;
+    if (g < 1) g = 1;
+    if (g > 4096) g = 4096;
+    return g;
+}
+
+__device__ __forceinline__ double warp_sum(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Block sum with a fixed tree; result valid in thread 0.
+__device__ __forceinline__ double block_sum(double v)
+{
+    __shared__ double sh[32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    v = warp_sum(v);
+    __syncthreads();
+    if (lane == 0) sh[wid] = v;
+    __syncthreads();
+    const int nw = (blockDim.x + 31) >> 5;
+    v = (threadIdx.x < nw) ? sh[threadIdx.x] : 0.0;
+    if (wid == 0) v = warp_sum(v);
+    return v;
+}
+
+template <typename S>
+__device__ __forceinline__ void load_elem(const MeshView<S>& m, uint32_t e, S* R, S* Di, S& k1, S& knu, S& k2)
+{
+    const size_t T = m.T;
+#pragma unroll
+    for (int c = 0; c < 9; c++) R[c] = m.R[c * T + e];
+#pragma unroll
+    for (int c = 0; c < 9; c++) Di[c] = m.Dinv[c * T + e];
+    k1 = m.mat[e];
+    knu = m.mat[T + e];
+    k2 = m.mat[2 * T + e];
+}
+
+// Local-frame stress product: given H (displacement gradient in the element
+// frame), returns P = sigma(H) * Dinv^T (columns = forces on nodes 1..3 in
+// the element frame, V folded into the material scalars) and eps:sigma.
+template <typename S>
+__device__ __forceinline__ void stress_forces(const S* H, const S* Di, S k1, S knu, S k2, S* P, S& eps_sig)
+{
+    const S exx = H[0], eyy = H[4], ezz = H[8];
+    const S gxy = H[1] + H[3], gyz = H[5] + H[7], gzx = H[2] + H[6];
+    const S sxx = k1 * exx + knu * (eyy + ezz);
+    const S syy = k1 * eyy + knu * (exx + ezz);
+    const S szz = k1 * ezz + knu * (exx + eyy);
+    const S txy = k2 * gxy, tyz = k2 * gyz, tzx = k2 * gzx;
+    eps_sig = sxx * exx + syy * eyy + szz * ezz + txy * gxy + tyz * gyz + tzx * gzx;
+    const S Sg[9] = {sxx, txy, tzx, txy, syy, tyz, tzx, tyz, szz};
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+            P[3 * a + i] = Sg[3 * a] * Di[3 * i] + Sg[3 * a + 1] * Di[3 * i + 1] + Sg[3 * a + 2] * Di[3 * i + 2];
+}
+
+// Writes R * P (world frame) to out[4][3]: node 0 gets minus the sum.
+template <typename S>
+__device__ __forceinline__ void rotate_out(const S* R, const S* P, S* out)
+{
+    S Pw[9];
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+        for (int i = 0; i < 3; i++) Pw[3 * a + i] = R[3 * a] * P[i] + R[3 * a + 1] * P[3 + i] + R[3 * a + 2] * P[6 + i];
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        out[3 * (i + 1) + 0] = Pw[i];
+        out[3 * (i + 1) + 1] = Pw[3 + i];
+        out[3 * (i + 1) + 2] = Pw[6 + i];
+    }
+    out[0] = -(Pw[0] + Pw[1] + Pw[2]);
+    out[1] = -(Pw[3] + Pw[4] + Pw[5]);
+    out[2] = -(Pw[6] + Pw[7] + Pw[8]);
+}
+
+// Product R K0 R^T d for one element (world-frame nodal vectors d[4][3]).
+template <typename S>
+__device__ __forceinline__ void elem_RKRt(const S* R, const S* Di, S k1, S knu, S k2, const S* d, S* out)
+{
+    S D[9];  // columns d1-d0, d2-d0, d3-d0 ; D[3a+j]
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+        for (int j = 0; j < 3; j++) D[3 * a + j] = d[3 * (j + 1) + a] - d[a];
+    S Hw[9];
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+        for (int b = 0; b < 3; b++) Hw[3 * a + b] = D[3 * a] * Di[b] + D[3 * a + 1] * Di[3 + b] + D[3 * a + 2] * Di[6 + b];
+    S H[9];  // R^T Hw
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+        for (int b = 0; b < 3; b++) H[3 * a + b] = R[a] * Hw[b] + R[3 + a] * Hw[3 + b] + R[6 + a] * Hw[6 + b];
+    S P[9], es;
+    stress_forces(H, Di, k1, knu, k2, P, es);
+    rotate_out(R, P, out);
+}
+
+// ---- element kernels ----
+
+__global__ void k_elem_spmv_fp64(MeshView<double> m, const double* __restrict__ d, const StepScalars* st,
+                                 int check_done)
+{
+    if (check_done && st->done) return;
+    for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < m.T; e += gridDim.x * blockDim.x) {
+        const int4 t = m.tets[e];
+        double R[9], Di[9], k1, knu, k2;
+        load_elem(m, e, R, Di, k1, knu, k2);
+        double dl[12];
+        const int ids[4] = {t.x, t.y, t.z, t.w};
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            dl[3 * i] = d[3 * (size_t)ids[i]];
+            dl[3 * i + 1] = d[3 * (size_t)ids[i] + 1];
+            dl[3 * i + 2] = d[3 * (size_t)ids[i] + 2];
+        }
+        double out[12];
+        elem_RKRt(R, Di, k1, knu, k2, dl, out);
+        double* o = m.eout + 12 * (size_t)e;
+#pragma unroll
+        for (int c = 0; c < 12; c++) o[c] = out[c];
+    }
+}
+
+// R K0 (R^T x - r) per element (C_f_e's product); optional eout write and
+// per-block elastic-energy partial 0.5 * u^T K0 u (C_V).
+__global__ void k_elem_force_fp64(MeshView<double> m, const double* __restrict__ x, int write_out,
+                                  double* energy_partials)
+{
+    double energy = 0.0;
+    for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < m.T; e += gridDim.x * blockDim.x) {
+        const int4 t = m.tets[e];
+        double R[9], Di[9], k1, knu, k2;
+        load_elem(m, e, R, Di, k1, knu, k2);
+        const int ids[4] = {t.x, t.y, t.z, t.w};
+        double u[12];
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            const size_t n = ids[i];
+            const double xa = x[3 * n], xb = x[3 * n + 1], xc = x[3 * n + 2];
+            // u_i = R^T x_i - r_i (accumulator from zero, as the reference)
+#pragma unroll
+            for (int a = 0; a < 3; a++) {
+                double acc = 0.0;
+                acc += R[a] * xa;
+                acc += R[3 + a] * xb;
+                acc += R[6 + a] * xc;
+                u[3 * i + a] = acc - m.rest[3 * n + a];
+            }
+        }
+        double D[9];
+#pragma unroll
+        for (int a = 0; a < 3; a++)
+#pragma unroll
+            for (int j = 0; j < 3; j++) D[3 * a + j] = u[3 * (j + 1) + a] - u[a];
+        double H[9];
+#pragma unroll
+        for (int a = 0; a < 3; a++)
+#pragma unroll
+            for (int b = 0; b < 3; b++) H[3 * a + b] = D[3 * a] * Di[b] + D[3 * a + 1] * Di[3 + b] + D[3 * a + 2] * Di[6 + b];
+        double P[9], es;
+        stress_forces(H, Di, k1, knu, k2, P, es);
+        energy += 0.5 * es;
+        if (write_out) {
+            double out[12];
+            rotate_out(R, P, out);
+            double* o = m.eout + 12 * (size_t)e;
+#pragma unroll
+            for (int c = 0; c < 12; c++) o[c] = out[c];
+        }
+    }
+    if (energy_partials) {
+        double s = block_sum(energy);
+        if (threadIdx.x == 0) energy_partials[blockIdx.x] = s;
+    }
+}
+
+// Potential energy term of RecomputeEnergy (LeafDSH_Solid3D_FEM.cpp:1554-1584):
+// sum_e (rho V_e / 4) (x0+x1+x2+x3) . (-g)
+__global__ void k_potential_fp64(MeshView<double> m, StepConsts c, const double* __restrict__ x, double* partials)
+{
+    double acc = 0.0;
+    for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < m.T; e += gridDim.x * blockDim.x) {
+        const int4 t = m.tets[e];
+        const int ids[4] = {t.x, t.y, t.z, t.w};
+        double s[3] = {0, 0, 0};
+#pragma unroll
+        for (int i = 0; i < 4; i++)
+#pragma unroll
+            for (int a = 0; a < 3; a++) s[a] += x[3 * (size_t)ids[i] + a];
+        double em = c.density * m.vol[e];
+        acc += (em / 4.0) * (s[0] * -c.gravity[0] + s[1] * -c.gravity[1] + s[2] * -c.gravity[2]);
+    }
+    double v = block_sum(acc);
+    if (threadIdx.x == 0) partials[blockIdx.x] = v;
+}
+
+// ---- node kernels ----
+
+__device__ __forceinline__ void gather3(const MeshView<double>& m, uint32_t n, double& a0, double& a1, double& a2)
+{
+    const uint32_t beg = m.csr_ptr[n], end = m.csr_ptr[n + 1];
+    for (uint32_t j = beg; j < end; j++) {
+        const double* o = m.eout + 3 * (size_t)m.csr_idx[j];
+        a0 += o[0];
+        a1 += o[1];
+        a2 += o[2];
+    }
+}
+
+// b = dt (m g + f_e) + m v ; y = v   (Step_QuasiImplicitEuler_v, :1211-1231)
+__global__ void k_node_b_fp64(MeshView<double> m, StepConsts c, const double* __restrict__ v, double* b, double* y)
+{
+    for (uint32_t n = blockIdx.x * blockDim.x + threadIdx.x; n < m.N; n += gridDim.x * blockDim.x) {
+        double f0 = 0, f1 = 0, f2 = 0;
+        gather3(m, n, f0, f1, f2);
+        const size_t i = 3 * (size_t)n;
+        b[i] = (c.mass * c.gravity[0] - f0) * c.dt + c.mass * v[i];
+        b[i + 1] = (c.mass * c.gravity[1] - f1) * c.dt + c.mass * v[i + 1];
+        b[i + 2] = (c.mass * c.gravity[2] - f2) * c.dt + c.mass * v[i + 2];
+        y[i] = v[i];
+        y[i + 1] = v[i + 1];
+        y[i + 2] = v[i + 2];
+    }
+}
+
+// Position constraints -> clamped velocity, written to b and y
+// (Step_QuasiImplicitEuler_v, LeafDSH_Solid3D_FEM.cpp:1268-1295).
+__global__ void k_knc_fp64(uint32_t count, const uint32_t* __restrict__ nodes, const double* __restrict__ targets,
+                           const double* __restrict__ x, StepConsts c, double* b, double* y)
+{
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < count; k += gridDim.x * blockDim.x) {
+        const size_t n = nodes[k];
+        V3<double> vk = mk<double>(c.inv_dt * (targets[3 * k] - x[3 * n]), c.inv_dt * (targets[3 * k + 1] - x[3 * n + 1]),
+                                   c.inv_dt * (targets[3 * k + 2] - x[3 * n + 2]));
+        double norm_vk = ::sqrt(dot0(vk, vk));
+        V3<double> vel = mk<double>(0.0, 0.0, 0.0);
+        if (norm_vk > (double)0.001f) {
+            double cl = (norm_vk < 50.0) ? norm_vk : 50.0;
+            vel = scale(cl, normalized(vk));
+        }
+        b[3 * n] = vel.x; b[3 * n + 1] = vel.y; b[3 * n + 2] = vel.z;
+        y[3 * n] = vel.x; y[3 * n + 1] = vel.y; y[3 * n + 2] = vel.z;
+    }
+}
+
+// r = S (b - A y) ; d = r ; partial |r|^2   (ILSS_CG.h:53-64)
+__global__ void k_node_residual_fp64(MeshView<double> m, StepConsts c, const double* __restrict__ b,
+                                     const double* __restrict__ y, double* r, double* d, double* partials)
+{
+    double acc = 0.0;
+    const double mfm = c.mass * c.factor_M;
+    for (uint32_t n = blockIdx.x * blockDim.x + threadIdx.x; n < m.N; n += gridDim.x * blockDim.x) {
+        double s0 = 0, s1 = 0, s2 = 0;
+        gather3(m, n, s0, s1, s2);
+        const size_t i = 3 * (size_t)n;
+        double r0 = 0, r1 = 0, r2 = 0;
+        if (!m.fixed[n]) {
+            r0 = b[i] - (c.factor_K * s0 + mfm * y[i]);
+            r1 = b[i + 1] - (c.factor_K * s1 + mfm * y[i + 1]);
+            r2 = b[i + 2] - (c.factor_K * s2 + mfm * y[i + 2]);
+        }
+        r[i] = r0; r[i + 1] = r1; r[i + 2] = r2;
+        d[i] = r0; d[i + 1] = r1; d[i + 2] = r2;
+        acc += r0 * r0 + r1 * r1 + r2 * r2;
+    }
+    double s = block_sum(acc);
+    if (threadIdx.x == 0) partials[blockIdx.x] = s;
+}
+
+// q = S A d ; partial d.q   (ILSS_CG.h:90-96)
+__global__ void k_node_q_fp64(MeshView<double> m, StepConsts c, const double* __restrict__ d, double* q,
+                              double* partials, const StepScalars* st)
+{
+    if (st->done) return;
+    double acc = 0.0;
+    const double mfm = c.mass * c.factor_M;
+    for (uint32_t n = blockIdx.x * blockDim.x + threadIdx.x; n < m.N; n += gridDim.x * blockDim.x) {
+        double s0 = 0, s1 = 0, s2 = 0;
+        gather3(m, n, s0, s1, s2);
+        const size_t i = 3 * (size_t)n;
+        double q0 = 0, q1 = 0, q2 = 0;
+        if (!m.fixed[n]) {
+            q0 = c.factor_K * s0 + mfm * d[i];
+            q1 = c.factor_K * s1 + mfm * d[i + 1];
+            q2 = c.factor_K * s2 + mfm * d[i + 2];
+        }
+        q[i] = q0; q[i + 1] = q1; q[i + 2] = q2;
+        acc += d[i] * q0 + d[i + 1] * q1 + d[i + 2] * q2;
+    }
+    double s = block_sum(acc);
+    if (threadIdx.x == 0) partials[blockIdx.x] = s;
+}
+
+// y += alpha d ; r -= alpha q ; partial |r|^2   (ILSS_CG.h:100-117)
+__global__ void k_node_xr_fp64(uint32_t N, double* y, double* r, const double* __restrict__ d,
+                               const double* __restrict__ q, double* partials, const StepScalars* st)
+{
+    if (st->done) return;
+    const double alpha = st->alpha, na = -alpha;
+    double acc = 0.0;
+    const uint32_t n3 = 3 * N;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n3; i += gridDim.x * blockDim.x) {
+        y[i] += alpha * d[i];
+        double ri = r[i] + na * q[i];
+        r[i] = ri;
+        acc += ri * ri;
+    }
+    double s = block_sum(acc);
+    if (threadIdx.x == 0) partials[blockIdx.x] = s;
+}
+
+// d = S (beta d + r)   (ILSS_CG.h:133-137)
+__global__ void k_node_d_fp64(uint32_t N, const uint8_t* __restrict__ fixed, double* d, const double* __restrict__ r,
+                              const StepScalars* st)
+{
+    // Once the loop has ended (including an iteration that just ended it in
+    // FIN_BETA) d is no longer read, so the update is skipped.
+    if (st->done) return;
+    const double beta = st->beta;
+    const uint32_t n3 = 3 * N;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n3; i += gridDim.x * blockDim.x) {
+        const uint32_t n = i / 3;
+        d[i] = fixed[n] ? 0.0 : beta * d[i] + r[i];
+    }
+}
+
+// v = y ; x += dt y   (Step_QuasiImplicitEuler_v, :1322-1327)
+__global__ void k_integrate_fp64(uint32_t N, double dt, double* x, double* v, const double* __restrict__ y)
+{
+    const uint32_t n3 = 3 * N;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n3; i += gridDim.x * blockDim.x) {
+        const double yi = y[i];
+        v[i] = yi;
+        x[i] = x[i] + dt * yi;
+    }
+}
+
+// q = S (factor_M M d + factor_K sum R K R^T d) using a fresh eout
+__global__ void k_apply_A_fp64(MeshView<double> m, double factor_M, double factor_K, double mass,
+                               const double* __restrict__ d, double* q)
+{
+    const double mfm = mass * factor_M;
+    for (uint32_t n = blockIdx.x * blockDim.x + threadIdx.x; n < m.N; n += gridDim.x * blockDim.x) {
+        double s0 = 0, s1 = 0, s2 = 0;
+        gather3(m, n, s0, s1, s2);
+        const size_t i = 3 * (size_t)n;
+        if (m.fixed[n]) { q[i] = 0; q[i + 1] = 0; q[i + 2] = 0; continue; }
+        q[i] = factor_K * s0 + mfm * d[i];
+        q[i + 1] = factor_K * s1 + mfm * d[i + 1];
+        q[i + 2] = factor_K * s2 + mfm * d[i + 2];
+    }
+}
+
+// f += sign * sum(eout) per node
+__global__ void k_gather_sum_fp64(MeshView<double> m, double sign, double* f)
+{
+    for (uint32_t n = blockIdx.x * blockDim.x + threadIdx.x; n < m.N; n += gridDim.x * blockDim.x) {
+        double s0 = 0, s1 = 0, s2 = 0;
+        gather3(m, n, s0, s1, s2);
+        f[3 * (size_t)n] += sign * s0;
+        f[3 * (size_t)n + 1] += sign * s1;
+        f[3 * (size_t)n + 2] += sign * s2;
+    }
+}
+
+// ---- finalizers (one block) ----
+
+__device__ __forceinline__ bool cg_continue(const StepScalars* st)
+{
+    return st->delta_new > st->abs_eps_sq && st->delta_new > st->delta_target && st->k < st->max_iter;
+}
+
+__global__ void k_finalize(int kind, const double* __restrict__ partials, uint32_t count, StepConsts c,
+                           StepScalars* st)
+{
+    double acc = 0.0;
+    for (uint32_t i = threadIdx.x; i < count; i += blockDim.x) acc += partials[i];
+    const double total = block_sum(acc);
+    if (threadIdx.x != 0) return;
+    switch (kind) {
+    case FIN_INIT:
+        st->delta_0 = total;
+        st->delta_new = total;
+        st->delta_old = total;
+        st->delta_target = c.rel_eps_sq * total;
+        st->abs_eps_sq = c.abs_eps_sq;
+        st->max_iter = c.max_iter;
+        st->k = 0;
+        st->status = 0;
+        st->alpha = 0.0;
+        st->beta = 0.0;
+        st->done = cg_continue(st) ? 0u : 1u;
+        if (total != total) st->status = 3;  // FEM_E_NAN
+        break;
+    case FIN_ALPHA:
+        if (st->done) break;
+        st->dot_dq = total;
+        if (::fabs(total) < st->abs_eps_sq) {  // breakdown: leave before the update (ILSS_CG.h:97)
+            st->done = 1;
+            break;
+        }
+        st->alpha = st->delta_new / total;
+        break;
+    case FIN_BETA:
+        if (st->done) break;
+        st->delta_old = st->delta_new;
+        st->delta_new = total;
+        st->beta = total / st->delta_old;
+        st->k += 1;
+        st->total_iters += 1;
+        st->done = cg_continue(st) ? 0u : 1u;
+        if (total != total) st->status = 3;
+        break;
+    case FIN_ENERGY_E:
+        st->elastic_energy = total;
+        break;
+    case FIN_ENERGY_P:
+        st->potential_energy = total;
+        break;
+    case FIN_STATS:
+        st->rel_residual = (st->delta_0 > 0) ? ::sqrt(st->delta_new / st->delta_0) : 0.0;
+        st->abs_residual = ::sqrt(st->delta_new);
+        break;
+    }
+}
+
+// ---- launchers ----
+
+#define FEMGB_LAUNCH(kernel, grid, ...)                                   \
+    do {                                                                  \
+        kernel<<<(grid), kBlock, 0, s>>>(__VA_ARGS__);                    \
+        launch_counter()++;                                               \
+    } while (0)
+
+void launch_elem_spmv_fp64(const MeshView<double>& m, const double* d, const StepScalars* st, int check_done,
+                           cudaStream_t s)
+{
+    prof_begin("elem_spmv_fp64", s);
+    FEMGB_LAUNCH(k_elem_spmv_fp64, grid_for(m.T), m, d, st, check_done);
+    prof_end("elem_spmv_fp64", s);
+}
+void launch_elem_force_fp64(const MeshView<double>& m, const double* x, int write_out, double* energy_partials,
+                            cudaStream_t s)
+{
+    FEMGB_LAUNCH(k_elem_force_fp64, grid_for(m.T), m, x, write_out, energy_partials);
+}
+void launch_node_b_fp64(const MeshView<double>& m, const StepConsts& c, const double* v, double* b, double* y,
+                        cudaStream_t s)
+{
+    FEMGB_LAUNCH(k_node_b_fp64, grid_for(m.N), m, c, v, b, y);
+}
+void launch_knc_fp64(uint32_t count, const uint32_t* nodes, const double* targets, const double* x,
+                     const StepConsts& c, double* b, double* y, cudaStream_t s)
+{
+    if (count == 0) return;
+    FEMGB_LAUNCH(k_knc_fp64, grid_for(count), count, nodes, targets, x, c, b, y);
+}
+void launch_node_residual_fp64(const MeshView<double>& m, const StepConsts& c, const double* b, const double* y,
+                               double* r, double* d, double* partials, cudaStream_t s)
+{
+    FEMGB_LAUNCH(k_node_residual_fp64, grid_for(m.N), m, c, b, y, r, d, partials);
+}
+void launch_node_q_fp64(const MeshView<double>& m, const StepConsts& c, const double* d, double* q,
+                        double* partials, const StepScalars* st, cudaStream_t s)
+{
+    prof_begin("node_q_fp64", s);
+    FEMGB_LAUNCH(k_node_q_fp64, grid_for(m.N), m, c, d, q, partials, st);
+    prof_end("node_q_fp64", s);
+}
+void launch_node_xr_fp64(uint32_t N, double* y, double* r, const double* d, const double* q, double* partials,
+                         const StepScalars* st, cudaStream_t s)
+{
+    FEMGB_LAUNCH(k_node_xr_fp64, grid_for(3 * N), N, y, r, d, q, partials, st);
+}
+void launch_node_d_fp64(uint32_t N, const uint8_t* fixed, double* d, const double* r, const StepScalars* st,
+                        cudaStream_t s)
+{
+    FEMGB_LAUNCH(k_node_d_fp64, grid_for(3 * N), N, fixed, d, r, st);
+}
+void launch_integrate_fp64(uint32_t N, double dt, double* x, double* v, const double* y, cudaStream_t s)
+{
+    FEMGB_LAUNCH(k_integrate_fp64, grid_for(3 * N), N, dt, x, v, y);
+}
+void launch_potential_fp64(const MeshView<double>& m, const StepConsts& c, const double* x, double* partials,
+                           cudaStream_t s)
+{
+    FEMGB_LAUNCH(k_potential_fp64, grid_for(m.T), m, c, x, partials);
+}
+void launch_apply_A_fp64(const MeshView<double>& m, double factor_M, double factor_K, double mass,
+                         const double* d, double* q, cudaStream_t s)
+{
+    FEMGB_LAUNCH(k_apply_A_fp64, grid_for(m.N), m, factor_M, factor_K, mass, d, q);
+}
+void launch_gather_sum_fp64(const MeshView<double>& m, double sign, double* f, cudaStream_t s)
+{
+    FEMGB_LAUNCH(k_gather_sum_fp64, grid_for(m.N), m, sign, f);
+}
+void launch_finalize(int kind, const double* partials, uint32_t count, const StepConsts& c, StepScalars* st,
+                     cudaStream_t s)
+{
+    k_finalize<<<1, kFinalizeThreads, 0, s>>>(kind, partials, count, c, st);
+    launch_counter()++;
+}
+
+}  // namespace femgb

@@ -1,0 +1,620 @@
+// solid.cu -- host runtime of one device-resident solid: the C ABI in
+// include/fem_tet.h for the FP64 drop-in path.
+//
+// Set-up restates EditableTetrahedronElementSet3::EndEdition
+// (TetrahedronElementSet3.cpp:2113-2166) for the data the strain-form kernels
+// need (Dm^-1, volume, the E-matrix entries times V), and the Leaf's
+// RebuildMass / RebuildRayleighCoeffsFromFreqs (LeafDSH_Solid3D_FEM.cpp:
+// 1591-1611, LeafDSH_Solid3D_FEM.h:347-354). The step orchestrates
+// FixedStep + Step_QuasiImplicitEuler_v (LeafDSH_Solid3D_FEM.cpp:898-990,
+// 1205-1328) and ILSS_CG::Solve (ILSS_CG.h:38-151) as kernels on the
+// handle's stream; the CG loop runs in chunks of iterations whose kernels
+// turn into no-ops once the device-side loop condition fails, and the host
+// reads the condition once per chunk.
+#include "../../include/fem_tet.h"
+#include "fem_device.cuh"
+
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+using namespace femgb;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const char* fmt, ...) __attribute__((format(printf, 2, 3)));
+int fail(int code, const char* fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return code;
+}
+
+#define CK(call)                                                                              \
+    do {                                                                                      \
+        cudaError_t e_ = (call);                                                              \
+        if (e_ != cudaSuccess)                                                                \
+            return fail(e_ == cudaErrorMemoryAllocation ? FEM_E_OOM : FEM_E_CUDA, "%s: %s (%s:%d)", #call, \
+                        cudaGetErrorString(e_), __FILE__, __LINE__);                          \
+    } while (0)
+
+template <typename T>
+struct DevBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    cudaError_t alloc(size_t count)
+    {
+        n = count;
+        return cudaMalloc(&p, sizeof(T) * (count ? count : 1));
+    }
+    void release()
+    {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+};
+
+// 3x3 helpers with the reference's rounding (Mal/GMat.h:236-313), host side.
+double det3(const double* m)
+{
+    return m[0] * m[4] * m[8] - m[0] * m[7] * m[5] + m[3] * m[7] * m[2] - m[3] * m[1] * m[8] + m[6] * m[1] * m[5] -
+           m[6] * m[4] * m[2];
+}
+void inverse3(const double* m, double* r)
+{
+    double inv_det = 1.0 / det3(m);
+    r[0] = inv_det * (m[4] * m[8] - m[5] * m[7]);
+    r[1] = inv_det * (m[2] * m[7] - m[1] * m[8]);
+    r[2] = inv_det * (m[1] * m[5] - m[2] * m[4]);
+    r[3] = inv_det * (m[5] * m[6] - m[3] * m[8]);
+    r[4] = inv_det * (m[0] * m[8] - m[2] * m[6]);
+    r[5] = inv_det * (m[2] * m[3] - m[0] * m[5]);
+    r[6] = inv_det * (m[3] * m[7] - m[4] * m[6]);
+    r[7] = inv_det * (m[1] * m[6] - m[0] * m[7]);
+    r[8] = inv_det * (m[0] * m[4] - m[1] * m[3]);
+}
+
+}  // namespace
+
+struct fem_solid_s {
+    uint32_t N = 0, T = 0;
+    fem_params params{};
+    StepConsts consts{};
+    double node_mass = 0, total_volume = 0, rayleigh[2] = {0, 0};
+    cudaStream_t stream = nullptr;
+    // element data
+    DevBuf<int4> tets;
+    DevBuf<double> Dinv, mat, vol, R, detF, eout;
+    DevBuf<uint32_t> csr_ptr, csr_idx;
+    DevBuf<uint8_t> fixed;
+    // node vectors
+    DevBuf<double> rest, x, v, y, b, r, d, q, tmp;
+    // constraints
+    DevBuf<uint32_t> knc_nodes;
+    DevBuf<double> knc_targets;
+    uint32_t knc_count = 0;
+    std::vector<uint8_t> fixed_host;
+    // reductions / scalars
+    DevBuf<double> partials, partials2;
+    DevBuf<StepScalars> st;
+    StepScalars* st_host = nullptr;  // pinned
+    bool evaluated = false;
+
+    MeshView<double> view()
+    {
+        MeshView<double> m;
+        m.N = N;
+        m.T = T;
+        m.tets = tets.p;
+        m.Dinv = Dinv.p;
+        m.mat = mat.p;
+        m.R = R.p;
+        m.detF = detF.p;
+        m.vol = vol.p;
+        m.rest = rest.p;
+        m.csr_ptr = csr_ptr.p;
+        m.csr_idx = csr_idx.p;
+        m.fixed = fixed.p;
+        m.eout = eout.p;
+        return m;
+    }
+
+    void release()
+    {
+        DevBuf<double>* dbl[] = {&Dinv, &mat, &vol, &R, &detF, &eout, &rest, &x, &v, &y, &b, &r, &d, &q, &tmp,
+                                 &knc_targets, &partials, &partials2};
+        for (auto* p : dbl) p->release();
+        tets.release();
+        csr_ptr.release();
+        csr_idx.release();
+        fixed.release();
+        knc_nodes.release();
+        st.release();
+        if (st_host) cudaFreeHost(st_host);
+        st_host = nullptr;
+        if (stream) cudaStreamDestroy(stream);
+        stream = nullptr;
+    }
+};
+
+namespace {
+
+int check_handle(fem_solid s)
+{
+    if (!s) return fail(FEM_E_ARG, "null solid handle");
+    return FEM_OK;
+}
+
+// One FixedStep on the device (no host synchronisation except the per-chunk
+// read of the CG loop flag).
+int step_once(fem_solid s, int chunk)
+{
+    cudaStream_t st = s->stream;
+    MeshView<double> m = s->view();
+    const StepConsts& c = s->consts;
+    const uint32_t gE = grid_for(s->T), gN = grid_for(s->N), gV = grid_for(3 * s->N);
+    CK(cudaMemsetAsync(&s->st.p->inverted, 0, sizeof(uint32_t), st));
+    launch_begin_eval_fp64(m, s->x.p, nullptr, s->st.p, st);
+    launch_elem_force_fp64(m, s->x.p, 1, nullptr, st);
+    launch_node_b_fp64(m, c, s->v.p, s->b.p, s->y.p, st);
+    launch_knc_fp64(s->knc_count, s->knc_nodes.p, s->knc_targets.p, s->x.p, c, s->b.p, s->y.p, st);
+    launch_elem_spmv_fp64(m, s->y.p, s->st.p, 0, st);
+    launch_node_residual_fp64(m, c, s->b.p, s->y.p, s->r.p, s->d.p, s->partials.p, st);
+    launch_finalize(FIN_INIT, s->partials.p, gN, c, s->st.p, st);
+    for (;;) {
+        for (int i = 0; i < chunk; i++) {
+            launch_elem_spmv_fp64(m, s->d.p, s->st.p, 1, st);
+            launch_node_q_fp64(m, c, s->d.p, s->q.p, s->partials.p, s->st.p, st);
+            launch_finalize(FIN_ALPHA, s->partials.p, gN, c, s->st.p, st);
+            launch_node_xr_fp64(s->N, s->y.p, s->r.p, s->d.p, s->q.p, s->partials.p, s->st.p, st);
+            launch_finalize(FIN_BETA, s->partials.p, gV, c, s->st.p, st);
+            launch_node_d_fp64(s->N, s->fixed.p, s->d.p, s->r.p, s->st.p, st);
+        }
+        CK(cudaMemcpyAsync(s->st_host, s->st.p, sizeof(StepScalars), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        if (s->st_host->done) break;
+    }
+    launch_finalize(FIN_STATS, s->partials.p, 0, c, s->st.p, st);
+    launch_integrate_fp64(s->N, c.dt, s->x.p, s->v.p, s->y.p, st);
+    if (s->params.compute_energy) {
+        launch_elem_force_fp64(m, s->x.p, 0, s->partials2.p, st);
+        launch_finalize(FIN_ENERGY_E, s->partials2.p, gE, c, s->st.p, st);
+        launch_potential_fp64(m, c, s->x.p, s->partials2.p, st);
+        launch_finalize(FIN_ENERGY_P, s->partials2.p, gE, c, s->st.p, st);
+    }
+    CK(cudaGetLastError());
+    return FEM_OK;
+}
+
+void fill_stats(const StepScalars& h, fem_step_stats* out)
+{
+    out->cg_iterations = h.k;
+    out->status = h.status;
+    out->rel_residual = h.rel_residual;
+    out->abs_residual = h.abs_residual;
+    out->elastic_energy = h.elastic_energy;
+    out->potential_energy = h.potential_energy;
+    out->inverted_elements = h.inverted;
+    out->fp64_resolved = h.fp64_resolved;
+    out->total_cg_iterations = h.total_iters;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* fem_last_error(void) { return g_err.c_str(); }
+
+uint64_t fem_kernel_launches(void) { return launch_counter(); }
+
+int fem_device_info(int* device, int* sm_count, int* cc_major, int* cc_minor)
+{
+    int dev = 0, n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || n == 0) return fail(FEM_E_NODEVICE, "no CUDA device: %s", cudaGetErrorString(e));
+    CK(cudaGetDevice(&dev));
+    cudaDeviceProp p;
+    CK(cudaGetDeviceProperties(&p, dev));
+    if (device) *device = dev;
+    if (sm_count) *sm_count = p.multiProcessorCount;
+    if (cc_major) *cc_major = p.major;
+    if (cc_minor) *cc_minor = p.minor;
+    return FEM_OK;
+}
+
+int fem_params_default(fem_params* p)
+{
+    if (!p) return fail(FEM_E_ARG, "null params");
+    std::memset(p, 0, sizeof(*p));
+    p->fixed_dt = (double)0.001f;
+    p->density = 1000.0;
+    p->young_modulus = 1000.0;
+    p->poisson_ratio = (double)0.25f;
+    p->damping_ratio = 1.0;
+    p->ls_rel_epsilon = 1e-3;
+    p->ls_abs_epsilon = 1e-6;
+    p->ls_max_iter = 20;
+    p->precision = FEM_PRECISION_FP64;
+    p->degenerate_det_F = 1e-3;
+    p->refresh_every = 50;
+    p->compute_energy = 1;
+    return FEM_OK;
+}
+
+int fem_solid_create(const double* rest_xyz, uint32_t N, const uint32_t* tets, uint32_t T, const fem_params* params,
+                     const double* young_per_elem, const double* poisson_per_elem, fem_solid* out)
+{
+    if (!out) return fail(FEM_E_ARG, "null output handle");
+    *out = nullptr;
+    if (!rest_xyz || !tets || !params) return fail(FEM_E_ARG, "null rest/tets/params");
+    if (N == 0 || T == 0) return fail(FEM_E_ARG, "empty mesh (N=%u, T=%u)", N, T);
+    if (N > (1u << 30) || T > (1u << 29)) return fail(FEM_E_ARG, "mesh too large (N=%u, T=%u)", N, T);
+    if (!(params->fixed_dt > 0)) return fail(FEM_E_ARG, "fixed_dt must be > 0");
+    if (params->precision != FEM_PRECISION_FP64)
+        return fail(FEM_E_ARG, "precision %u: this entry point builds the FP64 path; use the batch API for mixed",
+                    params->precision);
+    for (size_t i = 0; i < 4 * (size_t)T; i++)
+        if (tets[i] >= N) return fail(FEM_E_INDEX, "tet %zu names node %u >= N=%u", i / 4, tets[i], N);
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(FEM_E_NODEVICE, "no CUDA device");
+
+    // ---- host set-up (EndEdition + RebuildMass + Rayleigh) ----
+    std::vector<double> Dinv(9 * (size_t)T), mat(3 * (size_t)T), vol(T);
+    double acc_total_volume = 0.0;
+    for (uint32_t e = 0; e < T; e++) {
+        const double* r0 = rest_xyz + 3 * (size_t)tets[4 * (size_t)e];
+        const double* r1 = rest_xyz + 3 * (size_t)tets[4 * (size_t)e + 1];
+        const double* r2 = rest_xyz + 3 * (size_t)tets[4 * (size_t)e + 2];
+        const double* r3 = rest_xyz + 3 * (size_t)tets[4 * (size_t)e + 3];
+        double D[9];
+        for (int i = 0; i < 3; i++) {
+            D[3 * i] = r1[i] - r0[i];
+            D[3 * i + 1] = r2[i] - r0[i];
+            D[3 * i + 2] = r3[i] - r0[i];
+        }
+        const double V = det3(D) / 6.0;
+        if (!(V > 0.0)) return fail(FEM_E_DEGENERATE, "tet %u has rest volume %g <= 0", e, V);
+        vol[e] = V;
+        acc_total_volume += V;
+        double Di[9];
+        inverse3(D, Di);
+        for (int c = 0; c < 9; c++) Dinv[(size_t)c * T + e] = Di[c];
+        const double E = young_per_elem ? young_per_elem[e] : params->young_modulus;
+        const double nu = poisson_per_elem ? poisson_per_elem[e] : params->poisson_ratio;
+        // Compute_E (TetrahedronElement3.h:141-156)
+        const double a = E / ((1.0 + nu) * (1.0 - 2.0 * nu));
+        mat[e] = V * (a * (1.0 - nu));
+        mat[(size_t)T + e] = V * (a * nu);
+        mat[2 * (size_t)T + e] = V * (a * (0.5 - nu));
+    }
+    fem_solid s = new (std::nothrow) fem_solid_s;
+    if (!s) return fail(FEM_E_OOM, "host allocation failed");
+    s->N = N;
+    s->T = T;
+    s->params = *params;
+    s->total_volume = acc_total_volume;
+    const double total_mass = params->density * acc_total_volume;
+    const double mass_per_node = total_mass / N;
+    const double inv_mass = (double)1.0f / mass_per_node;
+    s->node_mass = 1.0 / inv_mass;
+    {
+        const double f1 = (double)0.1f, f2 = (double)10000.0f;
+        const double o00 = 1.0 / f1, o01 = f1, o10 = 1.0 / f2, o11 = f2;
+        const double inv_det = 1.0 / (o00 * o11 - o10 * o01);
+        const double i00 = inv_det * o11, i01 = -inv_det * o01, i10 = -inv_det * o10, i11 = inv_det * o00;
+        const double z = 2 * params->damping_ratio;
+        double a0 = 0, a1 = 0;
+        a0 += i00 * z; a0 += i01 * z;
+        a1 += i10 * z; a1 += i11 * z;
+        s->rayleigh[0] = a0;
+        s->rayleigh[1] = a1;
+    }
+    StepConsts& c = s->consts;
+    c.dt = params->fixed_dt;
+    c.inv_dt = 1.0 / params->fixed_dt;
+    c.mass = s->node_mass;
+    c.factor_M = 1.0 + c.dt * s->rayleigh[0];
+    c.factor_K = c.dt * c.dt + c.dt * s->rayleigh[1];
+    for (int i = 0; i < 3; i++) c.gravity[i] = params->gravity[i];
+    c.density = params->density;
+    c.rel_eps_sq = params->ls_rel_epsilon * params->ls_rel_epsilon;
+    c.abs_eps_sq = params->ls_abs_epsilon * params->ls_abs_epsilon;
+    c.max_iter = params->ls_max_iter;
+
+    // node -> (4e + slot) entries, element order
+    std::vector<uint32_t> ptr(N + 1, 0), idx(4 * (size_t)T);
+    for (size_t i = 0; i < 4 * (size_t)T; i++) ptr[tets[i] + 1]++;
+    for (uint32_t n = 0; n < N; n++) ptr[n + 1] += ptr[n];
+    {
+        std::vector<uint32_t> fill(ptr.begin(), ptr.end() - 1);
+        for (size_t i = 0; i < 4 * (size_t)T; i++) idx[fill[tets[i]]++] = (uint32_t)i;
+    }
+    std::vector<int4> t4(T);
+    for (uint32_t e = 0; e < T; e++)
+        t4[e] = make_int4((int)tets[4 * (size_t)e], (int)tets[4 * (size_t)e + 1], (int)tets[4 * (size_t)e + 2],
+                          (int)tets[4 * (size_t)e + 3]);
+    s->fixed_host.assign(N, 0);
+
+    auto cleanup = [&](int code) {
+        s->release();
+        delete s;
+        return code;
+    };
+#define CKC(call)                                                                                   \
+    do {                                                                                            \
+        cudaError_t e_ = (call);                                                                    \
+        if (e_ != cudaSuccess)                                                                      \
+            return cleanup(fail(e_ == cudaErrorMemoryAllocation ? FEM_E_OOM : FEM_E_CUDA, "%s: %s", #call, \
+                                cudaGetErrorString(e_)));                                           \
+    } while (0)
+    CKC(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
+    const size_t n3 = 3 * (size_t)N;
+    CKC(s->tets.alloc(T));
+    CKC(s->Dinv.alloc(9 * (size_t)T));
+    CKC(s->mat.alloc(3 * (size_t)T));
+    CKC(s->vol.alloc(T));
+    CKC(s->R.alloc(9 * (size_t)T));
+    CKC(s->detF.alloc(T));
+    CKC(s->eout.alloc(12 * (size_t)T));
+    CKC(s->csr_ptr.alloc(N + 1));
+    CKC(s->csr_idx.alloc(4 * (size_t)T));
+    CKC(s->fixed.alloc(N));
+    DevBuf<double>* vecs[] = {&s->rest, &s->x, &s->v, &s->y, &s->b, &s->r, &s->d, &s->q, &s->tmp};
+    for (auto* vb : vecs) CKC(vb->alloc(n3));
+    CKC(s->partials.alloc(4096));
+    CKC(s->partials2.alloc(4096));
+    CKC(s->st.alloc(1));
+    CKC(cudaMallocHost(&s->st_host, sizeof(StepScalars)));
+    cudaStream_t st = s->stream;
+    CKC(cudaMemcpyAsync(s->tets.p, t4.data(), sizeof(int4) * T, cudaMemcpyHostToDevice, st));
+    CKC(cudaMemcpyAsync(s->Dinv.p, Dinv.data(), sizeof(double) * Dinv.size(), cudaMemcpyHostToDevice, st));
+    CKC(cudaMemcpyAsync(s->mat.p, mat.data(), sizeof(double) * mat.size(), cudaMemcpyHostToDevice, st));
+    CKC(cudaMemcpyAsync(s->vol.p, vol.data(), sizeof(double) * T, cudaMemcpyHostToDevice, st));
+    CKC(cudaMemcpyAsync(s->csr_ptr.p, ptr.data(), sizeof(uint32_t) * (N + 1), cudaMemcpyHostToDevice, st));
+    CKC(cudaMemcpyAsync(s->csr_idx.p, idx.data(), sizeof(uint32_t) * idx.size(), cudaMemcpyHostToDevice, st));
+    CKC(cudaMemsetAsync(s->fixed.p, 0, N, st));
+    CKC(cudaMemcpyAsync(s->rest.p, rest_xyz, sizeof(double) * n3, cudaMemcpyHostToDevice, st));
+    CKC(cudaMemcpyAsync(s->x.p, rest_xyz, sizeof(double) * n3, cudaMemcpyHostToDevice, st));
+    CKC(cudaMemsetAsync(s->v.p, 0, sizeof(double) * n3, st));
+    CKC(cudaMemsetAsync(s->y.p, 0, sizeof(double) * n3, st));
+    CKC(cudaMemsetAsync(s->st.p, 0, sizeof(StepScalars), st));
+    // R = I, det F = 1 until the first evaluation (CreateCache, TetrahedronElementSet3.cpp:190-209)
+    {
+        std::vector<double> Rh(9 * (size_t)T, 0.0), dh(T, 1.0);
+        for (uint32_t e = 0; e < T; e++) Rh[e] = Rh[4 * (size_t)T + e] = Rh[8 * (size_t)T + e] = 1.0;
+        CKC(cudaMemcpyAsync(s->R.p, Rh.data(), sizeof(double) * Rh.size(), cudaMemcpyHostToDevice, st));
+        CKC(cudaMemcpyAsync(s->detF.p, dh.data(), sizeof(double) * T, cudaMemcpyHostToDevice, st));
+        CKC(cudaStreamSynchronize(st));
+    }
+#undef CKC
+    *out = s;
+    return FEM_OK;
+}
+
+int fem_solid_destroy(fem_solid s)
+{
+    if (!s) return FEM_OK;
+    if (s->stream) cudaStreamSynchronize(s->stream);
+    s->release();
+    delete s;
+    return FEM_OK;
+}
+
+int fem_solid_get_sizes(fem_solid s, uint32_t* N, uint32_t* T)
+{
+    if (int e = check_handle(s)) return e;
+    if (N) *N = s->N;
+    if (T) *T = s->T;
+    return FEM_OK;
+}
+
+int fem_solid_set_knc(fem_solid s, const uint32_t* nodes, const double* targets, uint32_t count)
+{
+    if (int e = check_handle(s)) return e;
+    if (count && (!nodes || !targets)) return fail(FEM_E_ARG, "null constraint arrays");
+    for (uint32_t k = 0; k < count; k++)
+        if (nodes[k] >= s->N) return fail(FEM_E_INDEX, "constraint %u names node %u >= N=%u", k, nodes[k], s->N);
+    CK(cudaStreamSynchronize(s->stream));
+    s->knc_nodes.release();
+    s->knc_targets.release();
+    s->knc_count = count;
+    std::fill(s->fixed_host.begin(), s->fixed_host.end(), 0);
+    if (count) {
+        CK(s->knc_nodes.alloc(count));
+        CK(s->knc_targets.alloc(3 * (size_t)count));
+        CK(cudaMemcpyAsync(s->knc_nodes.p, nodes, sizeof(uint32_t) * count, cudaMemcpyHostToDevice, s->stream));
+        CK(cudaMemcpyAsync(s->knc_targets.p, targets, sizeof(double) * 3 * count, cudaMemcpyHostToDevice,
+                           s->stream));
+        for (uint32_t k = 0; k < count; k++) s->fixed_host[nodes[k]] = 1;
+    }
+    CK(cudaMemcpyAsync(s->fixed.p, s->fixed_host.data(), s->N, cudaMemcpyHostToDevice, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return FEM_OK;
+}
+
+int fem_solid_set_knc_targets(fem_solid s, const double* targets)
+{
+    if (int e = check_handle(s)) return e;
+    if (s->knc_count == 0) return FEM_OK;
+    if (!targets) return fail(FEM_E_ARG, "null targets");
+    CK(cudaMemcpyAsync(s->knc_targets.p, targets, sizeof(double) * 3 * s->knc_count, cudaMemcpyHostToDevice,
+                       s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return FEM_OK;
+}
+
+int fem_solid_set_state(fem_solid s, const double* x, const double* v)
+{
+    if (int e = check_handle(s)) return e;
+    const size_t bytes = sizeof(double) * 3 * (size_t)s->N;
+    if (x) CK(cudaMemcpyAsync(s->x.p, x, bytes, cudaMemcpyHostToDevice, s->stream));
+    if (v) CK(cudaMemcpyAsync(s->v.p, v, bytes, cudaMemcpyHostToDevice, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return FEM_OK;
+}
+
+int fem_solid_get_state(fem_solid s, double* x, double* v)
+{
+    if (int e = check_handle(s)) return e;
+    const size_t bytes = sizeof(double) * 3 * (size_t)s->N;
+    if (x) CK(cudaMemcpyAsync(x, s->x.p, bytes, cudaMemcpyDeviceToHost, s->stream));
+    if (v) CK(cudaMemcpyAsync(v, s->v.p, bytes, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return FEM_OK;
+}
+
+int fem_solid_step_async(fem_solid s, uint32_t nsteps)
+{
+    if (int e = check_handle(s)) return e;
+    for (uint32_t i = 0; i < nsteps; i++)
+        if (int e = step_once(s, 8)) return e;
+    return FEM_OK;
+}
+
+int fem_solid_synchronize(fem_solid s, fem_step_stats* stats)
+{
+    if (int e = check_handle(s)) return e;
+    CK(cudaMemcpyAsync(s->st_host, s->st.p, sizeof(StepScalars), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    if (stats) fill_stats(*s->st_host, stats);
+    if (s->st_host->status == FEM_E_NAN) return fail(FEM_E_NAN, "NaN in the CG residual");
+    return FEM_OK;
+}
+
+int fem_solid_step(fem_solid s, uint32_t nsteps, fem_step_stats* stats)
+{
+    if (int e = fem_solid_step_async(s, nsteps)) return e;
+    return fem_solid_synchronize(s, stats);
+}
+
+int fem_solid_step_host(fem_solid s, const double* x_in, const double* v_in, uint32_t nsteps, double* x_out,
+                        double* v_out, fem_step_stats* stats)
+{
+    if (int e = check_handle(s)) return e;
+    const size_t bytes = sizeof(double) * 3 * (size_t)s->N;
+    if (x_in) CK(cudaMemcpyAsync(s->x.p, x_in, bytes, cudaMemcpyHostToDevice, s->stream));
+    if (v_in) CK(cudaMemcpyAsync(s->v.p, v_in, bytes, cudaMemcpyHostToDevice, s->stream));
+    if (int e = fem_solid_step_async(s, nsteps)) return e;
+    if (x_out) CK(cudaMemcpyAsync(x_out, s->x.p, bytes, cudaMemcpyDeviceToHost, s->stream));
+    if (v_out) CK(cudaMemcpyAsync(v_out, s->v.p, bytes, cudaMemcpyDeviceToHost, s->stream));
+    return fem_solid_synchronize(s, stats);
+}
+
+int fem_solid_stream(fem_solid s, void** stream)
+{
+    if (int e = check_handle(s)) return e;
+    if (!stream) return fail(FEM_E_ARG, "null stream pointer");
+    *stream = (void*)s->stream;
+    return FEM_OK;
+}
+
+int fem_solid_begin_eval(fem_solid s, const double* x)
+{
+    if (int e = check_handle(s)) return e;
+    if (!x) return fail(FEM_E_ARG, "null positions");
+    CK(cudaMemcpyAsync(s->tmp.p, x, sizeof(double) * 3 * (size_t)s->N, cudaMemcpyHostToDevice, s->stream));
+    CK(cudaMemsetAsync(&s->st.p->inverted, 0, sizeof(uint32_t), s->stream));
+    launch_begin_eval_fp64(s->view(), s->tmp.p, nullptr, s->st.p, s->stream);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(s->stream));
+    s->evaluated = true;
+    return FEM_OK;
+}
+
+int fem_solid_get_rotations(fem_solid s, double* R, double* detF)
+{
+    if (int e = check_handle(s)) return e;
+    const size_t T = s->T;
+    if (R) {
+        std::vector<double> soa(9 * T);
+        CK(cudaMemcpyAsync(soa.data(), s->R.p, sizeof(double) * 9 * T, cudaMemcpyDeviceToHost, s->stream));
+        CK(cudaStreamSynchronize(s->stream));
+        for (size_t e = 0; e < T; e++)
+            for (int c = 0; c < 9; c++) R[9 * e + c] = soa[(size_t)c * T + e];
+    }
+    if (detF) {
+        CK(cudaMemcpyAsync(detF, s->detF.p, sizeof(double) * T, cudaMemcpyDeviceToHost, s->stream));
+        CK(cudaStreamSynchronize(s->stream));
+    }
+    return FEM_OK;
+}
+
+int fem_solid_force_elastic(fem_solid s, double* f)
+{
+    if (int e = check_handle(s)) return e;
+    if (!f) return fail(FEM_E_ARG, "null force array");
+    if (!s->evaluated) return fail(FEM_E_ARG, "fem_solid_begin_eval must come first");
+    const size_t bytes = sizeof(double) * 3 * (size_t)s->N;
+    // positions of the last evaluation are in tmp
+    CK(cudaMemcpyAsync(s->q.p, f, bytes, cudaMemcpyHostToDevice, s->stream));
+    launch_elem_force_fp64(s->view(), s->tmp.p, 1, nullptr, s->stream);
+    launch_gather_sum_fp64(s->view(), -1.0, s->q.p, s->stream);
+    CK(cudaMemcpyAsync(f, s->q.p, bytes, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return FEM_OK;
+}
+
+int fem_solid_df_x(fem_solid s, const double* dx, double* df)
+{
+    if (int e = check_handle(s)) return e;
+    if (!dx || !df) return fail(FEM_E_ARG, "null arrays");
+    const size_t bytes = sizeof(double) * 3 * (size_t)s->N;
+    CK(cudaMemcpyAsync(s->d.p, dx, bytes, cudaMemcpyHostToDevice, s->stream));
+    CK(cudaMemcpyAsync(s->q.p, df, bytes, cudaMemcpyHostToDevice, s->stream));
+    launch_elem_spmv_fp64(s->view(), s->d.p, s->st.p, 0, s->stream);
+    launch_gather_sum_fp64(s->view(), -1.0, s->q.p, s->stream);
+    CK(cudaMemcpyAsync(df, s->q.p, bytes, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return FEM_OK;
+}
+
+int fem_solid_apply_A(fem_solid s, double factor_M, double factor_K, const double* d, double* q)
+{
+    if (int e = check_handle(s)) return e;
+    if (!d || !q) return fail(FEM_E_ARG, "null arrays");
+    const size_t bytes = sizeof(double) * 3 * (size_t)s->N;
+    CK(cudaMemcpyAsync(s->d.p, d, bytes, cudaMemcpyHostToDevice, s->stream));
+    launch_elem_spmv_fp64(s->view(), s->d.p, s->st.p, 0, s->stream);
+    launch_apply_A_fp64(s->view(), factor_M, factor_K, s->node_mass, s->d.p, s->q.p, s->stream);
+    CK(cudaMemcpyAsync(q, s->q.p, bytes, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return FEM_OK;
+}
+
+int fem_solid_energy(fem_solid s, double* V)
+{
+    if (int e = check_handle(s)) return e;
+    if (!V) return fail(FEM_E_ARG, "null output");
+    if (!s->evaluated) return fail(FEM_E_ARG, "fem_solid_begin_eval must come first");
+    launch_elem_force_fp64(s->view(), s->tmp.p, 0, s->partials2.p, s->stream);
+    launch_finalize(FIN_ENERGY_E, s->partials2.p, grid_for(s->T), s->consts, s->st.p, s->stream);
+    CK(cudaMemcpyAsync(s->st_host, s->st.p, sizeof(StepScalars), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    *V = s->st_host->elastic_energy;
+    return FEM_OK;
+}
+
+int fem_solid_mass_info(fem_solid s, double* node_mass, double* rayleigh2, double* total_volume)
+{
+    if (int e = check_handle(s)) return e;
+    if (node_mass) *node_mass = s->node_mass;
+    if (rayleigh2) {
+        rayleigh2[0] = s->rayleigh[0];
+        rayleigh2[1] = s->rayleigh[1];
+    }
+    if (total_volume) *total_volume = s->total_volume;
+    return FEM_OK;
+}
+
+}  // extern "C"

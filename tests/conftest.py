@@ -1,0 +1,27 @@
+import os
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA device (GB300)")
+
+
+@pytest.fixture(scope="session")
+def oracle():
+    import pyoracle
+    pyoracle.build(reference=os.path.isdir(pyoracle.REFERENCE_SRC))
+    return pyoracle
+
+
+@pytest.fixture(scope="session")
+def fem_lib():
+    from risdsdgcfem_thesis_gb300 import build, capi
+    build.build()
+    capi.load()
+    return capi

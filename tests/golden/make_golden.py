@@ -1,0 +1,90 @@
+"""Generates tests/golden/*.npz from the reference's own FP64 code.
+
+Run in a container that has the reference sources (the oracle Makefile
+compiles them into oracle/_ref/): python tests/golden/make_golden.py
+
+Fixtures (all from oracle/_ref/libfemref_dbl.so, the reference translation
+units with Mal's Sqrt/Sin/Cos/ATan2 at double precision, except where noted):
+  cantilever_160.npz   x, v after each of 120 FixedSteps of the 160-tet
+                       cantilever; per-step CG iterations, residuals, energies.
+  elements_160.npz     per-element R, f_e, df_x(dx), V on a deformed state of the
+                       same mesh (bent, twisted, 3 elements inverted).
+  literal_fp64.npz     the reference FP64 build as written (float-rounded Mal
+                       math): per-step iterations and energies of the same
+                       scene (the rotations are NaN at rest, so CG stops at 0).
+"""
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.abspath(os.path.join(HERE, "..", ".."))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+sys.path.insert(0, ROOT)
+
+import pyoracle as O  # noqa: E402
+from risdsdgcfem_thesis_gb300 import scenes  # noqa: E402
+
+
+def deformed_state(sc, seed=7):
+    """A bent and twisted configuration with a few inverted elements."""
+    rng = np.random.default_rng(seed)
+    x = sc.rest.copy()
+    L = x[:, 0].max()
+    s = x[:, 0] / L
+    x[:, 2] -= 0.15 * s ** 2                       # bend
+    ang = 0.6 * s                                  # twist about the x axis
+    yc, zc = x[:, 1] - 0.1, x[:, 2] - 0.1
+    x[:, 1] = 0.1 + np.cos(ang) * yc - np.sin(ang) * zc
+    x[:, 2] = 0.1 + np.sin(ang) * yc + np.cos(ang) * zc
+    x += rng.uniform(-0.004, 0.004, size=x.shape)
+    # invert three elements by pushing one node through the opposite face
+    for e in (17, 80, 141):
+        t = sc.tets[e]
+        c = x[t[1:]].mean(axis=0)
+        x[t[0]] = c + 1.5 * (c - x[t[0]])
+    return x
+
+
+def main():
+    O.build(reference=True)
+    sc = scenes.cantilever_160()
+
+    ref = O.Solid(sc, "ref_dbl")
+    xs, vs, stats = [], [], []
+    for _ in range(sc.steps):
+        stats.append(ref.step())
+        x, v = ref.state()
+        xs.append(x)
+        vs.append(v)
+    np.savez_compressed(os.path.join(HERE, "cantilever_160.npz"), x=np.array(xs), v=np.array(vs),
+                        iters=np.array([s["iters"] for s in stats], np.int32),
+                        rel_res=np.array([s["rel_res"] for s in stats]),
+                        abs_res=np.array([s["abs_res"] for s in stats]),
+                        elastic_energy=np.array([s["elastic_energy"] for s in stats]),
+                        potential_energy=np.array([s["potential_energy"] for s in stats]))
+
+    xd = deformed_state(sc)
+    tes = O.RefElementSet(sc, dbl=True)
+    tes.begin_eval(xd)
+    R = tes.rotations()
+    fe = tes.f_e()
+    dx = np.random.default_rng(3).standard_normal(xd.shape)
+    dfx = tes.df_x(dx)
+    V = tes.V()
+    port = O.Solid(sc, "port")
+    port.begin_eval(xd)
+    np.savez_compressed(os.path.join(HERE, "elements_160.npz"), x=xd, dx=dx, R=R, f_e=fe, df_x=dfx, V=np.array(V),
+                        detF=port.detF())
+
+    lit = O.Solid(sc, "ref")
+    lst = [lit.step() for _ in range(5)]
+    xl, vl = lit.state()
+    np.savez_compressed(os.path.join(HERE, "literal_fp64.npz"), iters=np.array([s["iters"] for s in lst], np.int32),
+                        elastic_energy=np.array([s["elastic_energy"] for s in lst]), x=xl, v=vl)
+    print("wrote fixtures to", HERE)
+
+
+if __name__ == "__main__":
+    main()
