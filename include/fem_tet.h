@@ -151,6 +151,53 @@ int fem_solid_synchronize(fem_solid s, fem_step_stats* stats);
 /* The handle's CUDA stream (a cudaStream_t) for event timing. */
 int fem_solid_stream(fem_solid s, void** stream);
 
+/* --- Batches: many independent solids stepped together (tiled path) ---
+ *
+ * The reference steps several solids one after another inside its
+ * aggregate scheme (SS_AggregateDSH_Basic::MultiDSH_Solid3D_Update,
+ * SS_AggregateDSH_Basic.cpp:229-300); a batch steps them together on one GPU,
+ * each with its own parameters, constraints and CG loop, so a solid's result
+ * is the same alone and in any batch. One step of a batch is one CUDA graph
+ * launch: the CG loop of every solid runs on the device until each has met
+ * its own stopping test. */
+typedef struct fem_batch_s* fem_batch;
+
+typedef struct fem_batch_options {
+    uint32_t precision;   /* enum fem_precision for every solid of the batch */
+    uint32_t tile_elems;  /* elements per tile, 1..256 */
+    uint32_t reorder;     /* 1: Morton order of element centroids before tiling */
+    uint32_t use_graph;   /* 1: each step is one CUDA graph with a device-side CG loop */
+} fem_batch_options;
+
+int fem_batch_options_default(fem_batch_options* o);
+int fem_batch_create(const fem_batch_options* opt, fem_batch* out);
+/* Adds one solid (same inputs as fem_solid_create); returns its index. */
+int fem_batch_add_mesh(fem_batch b, const double* rest_xyz, uint32_t N, const uint32_t* tets, uint32_t T,
+                       const fem_params* params, const double* young_per_elem,
+                       const double* poisson_per_elem, uint32_t* mesh_index);
+/* Position constraints of one solid (before finalize). */
+int fem_batch_set_knc(fem_batch b, uint32_t mesh, const uint32_t* nodes, const double* targets, uint32_t count);
+/* Builds tiles and uploads everything; the batch is then device resident. */
+int fem_batch_finalize(fem_batch b);
+int fem_batch_destroy(fem_batch b);
+int fem_batch_info(fem_batch b, uint32_t* meshes, uint64_t* nodes, uint64_t* tets, uint32_t* tiles,
+                   uint64_t* device_bytes);
+int fem_batch_set_knc_targets(fem_batch b, uint32_t mesh, const double* targets);
+int fem_batch_set_state(fem_batch b, uint32_t mesh, const double* x, const double* v);
+int fem_batch_get_state(fem_batch b, uint32_t mesh, double* x, double* v);
+/* Which solids take part in the next steps (M bytes, 1 = step); null = all. */
+int fem_batch_set_active(fem_batch b, const uint8_t* mask);
+int fem_batch_step_async(fem_batch b, uint32_t nsteps);
+int fem_batch_synchronize(fem_batch b);
+int fem_batch_step(fem_batch b, uint32_t nsteps);
+/* Statistics of one solid's last step, as of the last synchronize. */
+int fem_batch_get_stats(fem_batch b, uint32_t mesh, fem_step_stats* stats);
+int fem_batch_stream(fem_batch b, void** stream);
+/* Kernels launched by `steps` steps since the last reset (the CG-loop body
+ * runs are counted on the device). */
+int fem_batch_kernel_launches(fem_batch b, uint32_t steps, uint64_t* launches);
+int fem_batch_reset_launch_count(fem_batch b);
+
 /* --- Library --- */
 const char* fem_last_error(void);
 int fem_device_info(int* device, int* sm_count, int* cc_major, int* cc_minor);

@@ -103,6 +103,7 @@ def load():
     global _lib
     if _lib is not None:
         return _lib
+    _bind_batch_signatures()
     if not os.path.exists(LIB_PATH):
         raise FemError(FEM_E_NODEVICE, f"{LIB_PATH} is missing: run __graft_entry__.build()")
     lib = C.CDLL(LIB_PATH)
@@ -285,3 +286,154 @@ def device_info():
     vals = [C.c_int() for _ in range(4)]
     check(load().fem_device_info(*[C.byref(v) for v in vals]))
     return {"device": vals[0].value, "sm_count": vals[1].value, "cc": (vals[2].value, vals[3].value)}
+
+
+# ---------------------------------------------------------------- batches
+class FemBatchOptions(C.Structure):
+    _fields_ = [("precision", C.c_uint32), ("tile_elems", C.c_uint32), ("reorder", C.c_uint32),
+                ("use_graph", C.c_uint32)]
+
+
+_u8p = C.POINTER(C.c_uint8)
+
+
+def _bind_batch_signatures():
+    SIGNATURES.update(_BATCH_SIGNATURES)
+
+
+_BATCH_SIGNATURES = {
+    "fem_batch_options_default": (C.c_int, [C.POINTER(FemBatchOptions)]),
+    "fem_batch_create": (C.c_int, [C.POINTER(FemBatchOptions), C.POINTER(C.c_void_p)]),
+    "fem_batch_add_mesh": (C.c_int, [C.c_void_p, _dp, C.c_uint32, _up, C.c_uint32, C.POINTER(FemParams), _dp, _dp,
+                                     _up]),
+    "fem_batch_set_knc": (C.c_int, [C.c_void_p, C.c_uint32, _up, _dp, C.c_uint32]),
+    "fem_batch_finalize": (C.c_int, [C.c_void_p]),
+    "fem_batch_destroy": (C.c_int, [C.c_void_p]),
+    "fem_batch_info": (C.c_int, [C.c_void_p, _up, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64), _up,
+                                 C.POINTER(C.c_uint64)]),
+    "fem_batch_set_knc_targets": (C.c_int, [C.c_void_p, C.c_uint32, _dp]),
+    "fem_batch_set_state": (C.c_int, [C.c_void_p, C.c_uint32, _dp, _dp]),
+    "fem_batch_get_state": (C.c_int, [C.c_void_p, C.c_uint32, _dp, _dp]),
+    "fem_batch_set_active": (C.c_int, [C.c_void_p, _u8p]),
+    "fem_batch_step_async": (C.c_int, [C.c_void_p, C.c_uint32]),
+    "fem_batch_synchronize": (C.c_int, [C.c_void_p]),
+    "fem_batch_step": (C.c_int, [C.c_void_p, C.c_uint32]),
+    "fem_batch_get_stats": (C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(FemStepStats)]),
+    "fem_batch_stream": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
+    "fem_batch_kernel_launches": (C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(C.c_uint64)]),
+    "fem_batch_reset_launch_count": (C.c_int, [C.c_void_p]),
+}
+
+
+def batch_options(precision=FEM_PRECISION_MIXED, tile_elems=256, reorder=True, use_graph=True):
+    o = FemBatchOptions()
+    check(load().fem_batch_options_default(C.byref(o)))
+    o.precision = precision
+    o.tile_elems = tile_elems
+    o.reorder = 1 if reorder else 0
+    o.use_graph = 1 if use_graph else 0
+    return o
+
+
+class Batch:
+    """Many independent solids stepped together on one GPU (fem_batch_*)."""
+
+    def __init__(self, scenes_list, precision=FEM_PRECISION_MIXED, tile_elems=256, reorder=True, use_graph=True,
+                 compute_energy=True, refresh_every=None, degenerate_det_F=None):
+        lib = load()
+        self.lib = lib
+        self.scenes = list(scenes_list)
+        self.precision = precision
+        h = C.c_void_p()
+        opt = batch_options(precision, tile_elems, reorder, use_graph)
+        check(lib.fem_batch_create(C.byref(opt), C.byref(h)))
+        self.h = h
+        self._knc = []
+        for sc in self.scenes:
+            p = params_for(sc, precision, compute_energy)
+            if refresh_every is not None:
+                p.refresh_every = refresh_every
+            if degenerate_det_F is not None:
+                p.degenerate_det_F = degenerate_det_F
+            rest = _f64(sc.rest)
+            tets = np.ascontiguousarray(sc.tets, dtype=np.uint32)
+            idx = C.c_uint32()
+            check(lib.fem_batch_add_mesh(h, _ptr(rest), sc.num_nodes, _ptr(tets, C.c_uint32), sc.num_tets,
+                                         C.byref(p), _ptr(_f64(sc.young_per_elem)), _ptr(_f64(sc.poisson_per_elem)),
+                                         C.byref(idx)))
+            nodes = np.ascontiguousarray(sc.knc_nodes, dtype=np.uint32)
+            self._knc.append(nodes)
+            if nodes.size:
+                tg = _f64(sc.targets_at(0) if sc.knc_schedule is not None else sc.knc_targets)
+                check(lib.fem_batch_set_knc(h, idx.value, _ptr(nodes, C.c_uint32), _ptr(tg), nodes.size))
+        check(lib.fem_batch_finalize(h))
+        for i, sc in enumerate(self.scenes):
+            if sc.init_vel is not None:
+                self.set_state(i, v=sc.init_vel)
+        self.step_index = 0
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.fem_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def info(self):
+        m, t = C.c_uint32(), C.c_uint32()
+        n, e, b = C.c_uint64(), C.c_uint64(), C.c_uint64()
+        check(self.lib.fem_batch_info(self.h, C.byref(m), C.byref(n), C.byref(e), C.byref(t), C.byref(b)))
+        return {"meshes": m.value, "nodes": n.value, "tets": e.value, "tiles": t.value, "device_bytes": b.value}
+
+    def set_state(self, i, x=None, v=None):
+        x, v = _f64(x), _f64(v)
+        check(self.lib.fem_batch_set_state(self.h, i, _ptr(x), _ptr(v)))
+
+    def state(self, i):
+        n = self.scenes[i].num_nodes
+        x = np.empty((n, 3))
+        v = np.empty((n, 3))
+        check(self.lib.fem_batch_get_state(self.h, i, _ptr(x), _ptr(v)))
+        return x, v
+
+    def set_active(self, mask=None):
+        if mask is None:
+            check(self.lib.fem_batch_set_active(self.h, None))
+        else:
+            m = np.ascontiguousarray(mask, dtype=np.uint8)
+            check(self.lib.fem_batch_set_active(self.h, m.ctypes.data_as(_u8p)))
+
+    def _drive_targets(self):
+        for i, sc in enumerate(self.scenes):
+            if sc.knc_schedule is not None and self._knc[i].size:
+                tg = _f64(sc.targets_at(self.step_index))
+                check(self.lib.fem_batch_set_knc_targets(self.h, i, _ptr(tg)))
+
+    def step(self, n=1):
+        for _ in range(n):
+            self._drive_targets()
+            check(self.lib.fem_batch_step_async(self.h, 1))
+            self.step_index += 1
+        check(self.lib.fem_batch_synchronize(self.h))
+
+    def stats(self, i):
+        st = FemStepStats()
+        check(self.lib.fem_batch_get_stats(self.h, i, C.byref(st)))
+        return st.as_dict()
+
+    def stream(self):
+        s = C.c_void_p()
+        check(self.lib.fem_batch_stream(self.h, C.byref(s)))
+        return s.value
+
+    def kernel_launches(self, steps):
+        n = C.c_uint64()
+        check(self.lib.fem_batch_kernel_launches(self.h, steps, C.byref(n)))
+        return n.value
+
+    def reset_launch_count(self):
+        check(self.lib.fem_batch_reset_launch_count(self.h))

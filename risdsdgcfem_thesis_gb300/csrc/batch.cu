@@ -1,0 +1,962 @@
+// batch.cu -- host runtime of the tiled, batched step: the fem_batch_* part
+// of include/fem_tet.h.
+//
+// A batch holds independent solids (the reference's many-solid scheme steps
+// its Solid3D leaves one after another, SS_AggregateDSH_Basic.cpp:229-300;
+// here they step together). Each solid keeps the reference's per-solid
+// semantics: its own parameters, constraints, CG loop and stopping test
+// (ILSS_CG.h:86-88), so its results do not depend on the other solids.
+//
+// Set-up (fem_batch_finalize): per mesh, elements are put in Morton order of
+// their centroids and cut into tiles of at most tile_elems tets and 256
+// local nodes; the element data (Dm^-1, E-matrix entries times V, FP64 for
+// the once-per-step kernels and in the path's type S for the CG products)
+// follow that order. Node numbering is the caller's.
+//
+// Step: one CUDA graph per batch -- the once-per-step kernels, then a
+// conditional while node whose body is one CG iteration of every mesh still
+// iterating and whose condition the per-mesh finaliser sets on the device,
+// then integration and energies. No host synchronisation inside a step.
+#include "../../include/fem_tet.h"
+#include "batch.cuh"
+#include "batch_launch.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <new>
+#include <string>
+#include <vector>
+
+using namespace femgb;
+
+namespace femgb {
+int batch_fail(int code, const char* fmt, ...);
+}
+
+namespace {
+
+#define BCK(call)                                                                                          \
+    do {                                                                                                   \
+        cudaError_t e_ = (call);                                                                           \
+        if (e_ != cudaSuccess)                                                                             \
+            return batch_fail(e_ == cudaErrorMemoryAllocation ? FEM_E_OOM : FEM_E_CUDA, "%s: %s (%s:%d)", #call, \
+                              cudaGetErrorString(e_), __FILE__, __LINE__);                                 \
+    } while (0)
+
+struct HostMesh {
+    std::vector<double> rest;
+    std::vector<uint32_t> tets;
+    fem_params p;
+    std::vector<double> E, nu;
+    std::vector<uint32_t> knc_nodes;
+    std::vector<double> knc_targets;
+};
+
+template <typename T>
+struct Dev {
+    T* p = nullptr;
+    size_t n = 0;
+    cudaError_t alloc(size_t count)
+    {
+        n = count;
+        return cudaMalloc(&p, sizeof(T) * (count ? count : 1));
+    }
+    cudaError_t upload(const std::vector<T>& h, cudaStream_t s)
+    {
+        if (h.empty()) return cudaSuccess;
+        return cudaMemcpyAsync(p, h.data(), sizeof(T) * h.size(), cudaMemcpyHostToDevice, s);
+    }
+    void release()
+    {
+        if (p) cudaFree(p);
+        p = nullptr;
+    }
+    size_t bytes() const { return sizeof(T) * n; }
+};
+
+double det3(const double* m)
+{
+    return m[0] * m[4] * m[8] - m[0] * m[7] * m[5] + m[3] * m[7] * m[2] - m[3] * m[1] * m[8] + m[6] * m[1] * m[5] -
+           m[6] * m[4] * m[2];
+}
+void inverse3(const double* m, double* r)
+{
+    double inv_det = 1.0 / det3(m);
+    r[0] = inv_det * (m[4] * m[8] - m[5] * m[7]);
+    r[1] = inv_det * (m[2] * m[7] - m[1] * m[8]);
+    r[2] = inv_det * (m[1] * m[5] - m[2] * m[4]);
+    r[3] = inv_det * (m[5] * m[6] - m[3] * m[8]);
+    r[4] = inv_det * (m[0] * m[8] - m[2] * m[6]);
+    r[5] = inv_det * (m[2] * m[3] - m[0] * m[5]);
+    r[6] = inv_det * (m[3] * m[7] - m[4] * m[6]);
+    r[7] = inv_det * (m[1] * m[6] - m[0] * m[7]);
+    r[8] = inv_det * (m[0] * m[4] - m[1] * m[3]);
+}
+
+uint32_t spread10(uint32_t v)
+{
+    v &= 0x3ff;
+    v = (v | (v << 16)) & 0x030000FF;
+    v = (v | (v << 8)) & 0x0300F00F;
+    v = (v | (v << 4)) & 0x030C30C3;
+    v = (v | (v << 2)) & 0x09249249;
+    return v;
+}
+
+}  // namespace
+
+struct fem_batch_s {
+    fem_batch_options opt{};
+    std::vector<HostMesh> meshes;
+    bool finalized = false;
+    uint32_t M = 0, ntiles = 0, nchunks = 0, K = 0;
+    uint64_t Ntot = 0, Ttot = 0, nslots = 0;
+    std::vector<MeshConsts> mc_host;
+    std::vector<uint32_t> knc_base;   // per mesh first KNC entry
+    cudaStream_t stream = nullptr;
+    // device buffers (type-erased for S)
+    Dev<TileMeta> tiles;
+    Dev<ChunkMeta> chunks;
+    Dev<MeshConsts> mc;
+    Dev<StepScalars> st;
+    Dev<uint8_t> active;
+    Dev<int4> gtets;
+    Dev<unsigned char> Dinv_s, mat_s, R_s;  // S-typed, raw bytes
+    Dev<double> Dinv64, vol, detF;
+    Dev<uint32_t> tile_nodes, lptr0, nptr, nslot, knc_node, knc_mesh;
+    Dev<uchar4> lconn;
+    Dev<uint16_t> lptr, lidx;
+    Dev<uint8_t> fixed;
+    Dev<double> rest, x, v, bvec, y, part64, cpart, tpart, knc_target;
+    Dev<unsigned char> r_s, d_s, q_s, part_s;  // S-typed
+    Dev<unsigned> counter, any_flag, refresh_flag, mcount;
+    StepScalars* st_host = nullptr;
+    // step graph
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    size_t device_bytes = 0;
+
+    size_t S_size() const { return opt.precision == FEM_PRECISION_FP64 ? 8 : 4; }
+
+    template <typename S>
+    BatchView<S> view() const
+    {
+        BatchView<S> b;
+        b.M = M;
+        b.ntiles = ntiles;
+        b.nchunks = nchunks;
+        b.Ntot = (uint32_t)Ntot;
+        b.Ttot = (uint32_t)Ttot;
+        b.tiles = tiles.p;
+        b.chunks = chunks.p;
+        b.mc = mc.p;
+        b.st = st.p;
+        b.active = active.p;
+        b.gtets = gtets.p;
+        b.Dinv = reinterpret_cast<const S*>(Dinv_s.p);
+        b.mat = reinterpret_cast<const S*>(mat_s.p);
+        b.R = reinterpret_cast<S*>(R_s.p);
+        b.Dinv64 = Dinv64.p;
+        b.vol = vol.p;
+        b.detF = detF.p;
+        b.tile_nodes = tile_nodes.p;
+        b.lconn = lconn.p;
+        b.lptr = lptr.p;
+        b.lidx = lidx.p;
+        b.lptr0 = lptr0.p;
+        b.nptr = nptr.p;
+        b.nslot = nslot.p;
+        b.fixed = fixed.p;
+        b.rest = rest.p;
+        b.knc_node = knc_node.p;
+        b.knc_mesh = knc_mesh.p;
+        b.knc_target = knc_target.p;
+        return b;
+    }
+
+    void release()
+    {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        exec = nullptr;
+        graph = nullptr;
+        tiles.release(); chunks.release(); mc.release(); st.release(); active.release(); gtets.release();
+        Dinv_s.release(); mat_s.release(); R_s.release(); Dinv64.release(); vol.release(); detF.release();
+        tile_nodes.release(); lptr0.release(); nptr.release(); nslot.release(); knc_node.release();
+        knc_mesh.release(); lconn.release(); lptr.release(); lidx.release(); fixed.release(); rest.release();
+        x.release(); v.release(); bvec.release(); y.release(); part64.release(); cpart.release(); tpart.release();
+        knc_target.release(); r_s.release(); d_s.release(); q_s.release(); part_s.release(); counter.release();
+        any_flag.release(); refresh_flag.release(); mcount.release();
+        if (st_host) cudaFreeHost(st_host);
+        st_host = nullptr;
+        if (stream) cudaStreamDestroy(stream);
+        stream = nullptr;
+    }
+};
+
+namespace femgb {
+void set_last_error(const char* msg);
+int batch_fail(int code, const char* fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    set_last_error(buf);
+    return code;
+}
+}  // namespace femgb
+
+namespace {
+
+template <typename S>
+std::vector<unsigned char> as_bytes(const std::vector<double>& src)
+{
+    std::vector<unsigned char> out(src.size() * sizeof(S));
+    S* o = reinterpret_cast<S*>(out.data());
+    for (size_t i = 0; i < src.size(); i++) o[i] = (S)src[i];
+    return out;
+}
+
+// Enqueue one step (all kernels) on `s`. In graph capture the CG loop is a
+// conditional while node; outside capture the loop runs on the host in
+// chunks, reading the device's "any mesh iterating" flag.
+template <typename S>
+int enqueue_step(fem_batch B, cudaStream_t s, bool capture)
+{
+    const BatchView<S> b = B->view<S>();
+    const bool mixed = B->opt.precision == FEM_PRECISION_MIXED;
+    S* r = reinterpret_cast<S*>(B->r_s.p);
+    S* d = reinterpret_cast<S*>(B->d_s.p);
+    S* q = reinterpret_cast<S*>(B->q_s.p);
+    S* part = reinterpret_cast<S*>(B->part_s.p);
+    using L = BatchLaunch<S>;
+    cudaGraphConditionalHandle cond = 0;
+    if (capture) {
+        cudaGraph_t g = nullptr;
+        cudaStreamCaptureStatus cs;
+        BCK(cudaStreamGetCaptureInfo(s, &cs, nullptr, &g, nullptr, nullptr, nullptr));
+        BCK(cudaGraphConditionalHandleCreate(&cond, g, 0, cudaGraphCondAssignDefault));
+    }
+    LoopSync ls;
+    ls.mcount = B->mcount.p;
+    ls.gcount = B->counter.p;
+    ls.refresh_flag = B->refresh_flag.p;
+    ls.body_runs = nullptr;
+    ls.cond = cond;
+    ls.set_cond = capture ? 1 : 0;
+    // ---- once per step ----
+    L::reset_counts(b, s);
+    L::begin_eval(b, B->x.p, s);
+    L::tile_force(b, B->x.p, B->part64.p, nullptr, s);
+    L::node_b(b, B->part64.p, B->v.p, B->bvec.p, B->y.p, s);
+    L::knc(b, B->K, B->x.p, B->bvec.p, B->y.p, s);
+    L::tile_spmv_y64(b, B->y.p, B->part64.p, 0, nullptr, s);
+    L::node_residual(b, B->part64.p, B->bvec.p, B->y.p, r, d, B->cpart.p, ls, s);
+    LoopSync lb = ls;
+    lb.body_runs = B->any_flag.p;
+    auto body_tail = [&](cudaStream_t bs) {
+        L::node_q(b, part, d, q, mixed ? B->part64.p : nullptr, B->bvec.p, B->y.p, r, B->cpart.p, lb, bs);
+        L::node_update(b, B->y.p, r, d, q, B->cpart.p, lb, bs);
+    };
+    if (capture) {
+        const cudaGraphNode_t* deps = nullptr;
+        size_t ndeps = 0;
+        cudaGraph_t g = nullptr;
+        cudaStreamCaptureStatus cs;
+        BCK(cudaStreamGetCaptureInfo(s, &cs, nullptr, &g, &deps, nullptr, &ndeps));
+        cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};
+        cp.conditional.handle = cond;
+        cp.conditional.type = cudaGraphCondTypeWhile;
+        cp.conditional.size = 1;
+        cudaGraphNode_t wnode;
+        BCK(cudaGraphAddNode(&wnode, g, deps, nullptr, ndeps, &cp));
+        cudaGraph_t bodyg = cp.conditional.phGraph_out[0];
+        cudaStream_t bs;
+        BCK(cudaStreamCreateWithFlags(&bs, cudaStreamNonBlocking));
+        cudaError_t e1 = cudaStreamBeginCaptureToGraph(bs, bodyg, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed);
+        if (e1 != cudaSuccess) {
+            cudaStreamDestroy(bs);
+            BCK(e1);
+        }
+        cudaGraphConditionalHandle ifh = 0;
+        if (mixed) {
+            e1 = cudaGraphConditionalHandleCreate(&ifh, bodyg, 0, 0);
+            if (e1 != cudaSuccess) {
+                cudaGraph_t tmp = nullptr;
+                cudaStreamEndCapture(bs, &tmp);
+                cudaStreamDestroy(bs);
+                BCK(e1);
+            }
+        }
+        L::tile_spmv(b, d, r, part, ifh, mixed ? 1 : 0, B->refresh_flag.p, bs);
+        if (mixed) {
+            // IF (some mesh refreshes this iteration) { FP64 product of y }
+            const cudaGraphNode_t* bdeps = nullptr;
+            size_t nb = 0;
+            cudaGraph_t bg = nullptr;
+            e1 = cudaStreamGetCaptureInfo(bs, &cs, nullptr, &bg, &bdeps, nullptr, &nb);
+            cudaGraphNodeParams ip = {cudaGraphNodeTypeConditional};
+            ip.conditional.handle = ifh;
+            ip.conditional.type = cudaGraphCondTypeIf;
+            ip.conditional.size = 1;
+            cudaGraphNode_t inode;
+            if (e1 == cudaSuccess) e1 = cudaGraphAddNode(&inode, bg, bdeps, nullptr, nb, &ip);
+            cudaStream_t is = nullptr;
+            if (e1 == cudaSuccess) e1 = cudaStreamCreateWithFlags(&is, cudaStreamNonBlocking);
+            if (e1 == cudaSuccess)
+                e1 = cudaStreamBeginCaptureToGraph(is, ip.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                                   cudaStreamCaptureModeRelaxed);
+            if (e1 == cudaSuccess) {
+                L::tile_spmv_y64(b, B->y.p, B->part64.p, 1, nullptr, is);
+                cudaGraph_t ig = nullptr;
+                e1 = cudaStreamEndCapture(is, &ig);
+            }
+            if (is) cudaStreamDestroy(is);
+            if (e1 == cudaSuccess)
+                e1 = cudaStreamUpdateCaptureDependencies(bs, &inode, nullptr, 1, cudaStreamSetCaptureDependencies);
+            if (e1 != cudaSuccess) {
+                cudaGraph_t tmp = nullptr;
+                cudaStreamEndCapture(bs, &tmp);
+                cudaStreamDestroy(bs);
+                BCK(e1);
+            }
+        }
+        body_tail(bs);
+        cudaGraph_t out_body = nullptr;
+        cudaError_t e2 = cudaStreamEndCapture(bs, &out_body);
+        cudaStreamDestroy(bs);
+        BCK(e2);
+        BCK(cudaStreamUpdateCaptureDependencies(s, &wnode, nullptr, 1, cudaStreamSetCaptureDependencies));
+    } else {
+        // host-driven loop: chunks of iterations, then read the per-mesh flags
+        for (;;) {
+            BCK(cudaMemcpyAsync(B->st_host, B->st.p, sizeof(StepScalars) * B->M, cudaMemcpyDeviceToHost, s));
+            BCK(cudaStreamSynchronize(s));
+            bool any = false;
+            for (uint32_t m = 0; m < B->M; m++) any |= !B->st_host[m].done;
+            if (!any) break;
+            for (int i = 0; i < 8; i++) {
+                L::tile_spmv(b, d, r, part, 0, 0, nullptr, s);
+                if (mixed) L::tile_spmv_y64(b, B->y.p, B->part64.p, 1, B->refresh_flag.p, s);
+                body_tail(s);
+            }
+        }
+    }
+    // ---- after the solve ----
+    L::integrate(b, B->x.p, B->v.p, B->y.p, s);
+    bool energy = false;
+    for (auto& m : B->meshes) energy |= m.p.compute_energy != 0;
+    if (energy) {
+        L::tile_force(b, B->x.p, nullptr, B->tpart.p, s);
+        L::fin_energy(b, FIN_ENERGY_E, B->tpart.p, s);
+        L::tile_potential(b, B->x.p, B->tpart.p, s);
+        L::fin_energy(b, FIN_ENERGY_P, B->tpart.p, s);
+    }
+    BCK(cudaGetLastError());
+    return FEM_OK;
+}
+
+int build_graph(fem_batch B)
+{
+    if (B->exec) return FEM_OK;
+    cudaStream_t s = B->stream;
+    BCK(cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed));
+    int rc = B->opt.precision == FEM_PRECISION_FP64 ? enqueue_step<double>(B, s, true) : enqueue_step<float>(B, s, true);
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(s, &g);
+    if (rc != FEM_OK) {
+        if (g) cudaGraphDestroy(g);
+        return rc;
+    }
+    BCK(e);
+    B->graph = g;
+    BCK(cudaGraphInstantiate(&B->exec, g, 0));
+    return FEM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int fem_batch_options_default(fem_batch_options* o)
+{
+    if (!o) return batch_fail(FEM_E_ARG, "null options");
+    std::memset(o, 0, sizeof(*o));
+    o->precision = FEM_PRECISION_MIXED;
+    o->tile_elems = kTileElems;
+    o->reorder = 1;
+    o->use_graph = 1;
+    return FEM_OK;
+}
+
+int fem_batch_create(const fem_batch_options* opt, fem_batch* out)
+{
+    if (!out) return batch_fail(FEM_E_ARG, "null output handle");
+    *out = nullptr;
+    fem_batch_options o;
+    fem_batch_options_default(&o);
+    if (opt) o = *opt;
+    if (o.precision != FEM_PRECISION_FP64 && o.precision != FEM_PRECISION_MIXED)
+        return batch_fail(FEM_E_ARG, "unknown precision %u", o.precision);
+    if (o.tile_elems == 0 || o.tile_elems > (uint32_t)kTileElems)
+        return batch_fail(FEM_E_ARG, "tile_elems must be in [1, %d]", kTileElems);
+    fem_batch b = new (std::nothrow) fem_batch_s;
+    if (!b) return batch_fail(FEM_E_OOM, "host allocation failed");
+    b->opt = o;
+    *out = b;
+    return FEM_OK;
+}
+
+int fem_batch_add_mesh(fem_batch b, const double* rest, uint32_t N, const uint32_t* tets, uint32_t T,
+                       const fem_params* p, const double* young_per_elem, const double* poisson_per_elem,
+                       uint32_t* mesh_index)
+{
+    if (!b) return batch_fail(FEM_E_ARG, "null batch");
+    if (b->finalized) return batch_fail(FEM_E_ARG, "batch already finalized");
+    if (!rest || !tets || !p) return batch_fail(FEM_E_ARG, "null rest/tets/params");
+    if (N == 0 || T == 0) return batch_fail(FEM_E_ARG, "empty mesh (N=%u, T=%u)", N, T);
+    if (!(p->fixed_dt > 0)) return batch_fail(FEM_E_ARG, "fixed_dt must be > 0");
+    for (size_t i = 0; i < 4 * (size_t)T; i++)
+        if (tets[i] >= N) return batch_fail(FEM_E_INDEX, "tet %zu names node %u >= N=%u", i / 4, tets[i], N);
+    HostMesh m;
+    m.rest.assign(rest, rest + 3 * (size_t)N);
+    m.tets.assign(tets, tets + 4 * (size_t)T);
+    m.p = *p;
+    if (young_per_elem) m.E.assign(young_per_elem, young_per_elem + T);
+    if (poisson_per_elem) m.nu.assign(poisson_per_elem, poisson_per_elem + T);
+    b->meshes.push_back(std::move(m));
+    if (mesh_index) *mesh_index = (uint32_t)(b->meshes.size() - 1);
+    return FEM_OK;
+}
+
+int fem_batch_set_knc(fem_batch b, uint32_t mesh, const uint32_t* nodes, const double* targets, uint32_t count)
+{
+    if (!b) return batch_fail(FEM_E_ARG, "null batch");
+    if (b->finalized) return batch_fail(FEM_E_ARG, "constraint sets are fixed at finalize; use set_knc_targets");
+    if (mesh >= b->meshes.size()) return batch_fail(FEM_E_ARG, "mesh %u out of range", mesh);
+    if (count && (!nodes || !targets)) return batch_fail(FEM_E_ARG, "null constraint arrays");
+    HostMesh& m = b->meshes[mesh];
+    const uint32_t N = (uint32_t)(m.rest.size() / 3);
+    for (uint32_t k = 0; k < count; k++)
+        if (nodes[k] >= N) return batch_fail(FEM_E_INDEX, "constraint %u names node %u >= N=%u", k, nodes[k], N);
+    m.knc_nodes.assign(nodes, nodes + count);
+    m.knc_targets.assign(targets, targets + 3 * (size_t)count);
+    return FEM_OK;
+}
+
+int fem_batch_finalize(fem_batch b)
+{
+    if (!b) return batch_fail(FEM_E_ARG, "null batch");
+    if (b->finalized) return FEM_OK;
+    if (b->meshes.empty()) return batch_fail(FEM_E_ARG, "empty batch");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return batch_fail(FEM_E_NODEVICE, "no CUDA device");
+    const bool fp64 = b->opt.precision == FEM_PRECISION_FP64;
+    const uint32_t tile_cap = b->opt.tile_elems;
+    b->M = (uint32_t)b->meshes.size();
+
+    std::vector<TileMeta> tiles;
+    std::vector<ChunkMeta> chunks;
+    std::vector<MeshConsts> mcs(b->M);
+    std::vector<int4> gtets;
+    std::vector<double> vol, rest_all;
+    std::vector<uchar4> lconn;
+    std::vector<uint32_t> tile_nodes, lptr0;
+    std::vector<uint16_t> lptr, lidx;
+    std::vector<uint8_t> fixed;
+    std::vector<uint32_t> knc_node, knc_mesh;
+    std::vector<double> knc_target;
+    // element data collected AoS then transposed
+    std::vector<double> Dinv_aos, mat_aos;
+
+    uint64_t node0 = 0, elem0 = 0;
+    for (uint32_t mi = 0; mi < b->M; mi++) {
+        HostMesh& hm = b->meshes[mi];
+        const uint32_t N = (uint32_t)(hm.rest.size() / 3), T = (uint32_t)(hm.tets.size() / 4);
+        const fem_params& p = hm.p;
+        // element order
+        std::vector<uint32_t> order(T);
+        for (uint32_t e = 0; e < T; e++) order[e] = e;
+        if (b->opt.reorder) {
+            double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+            for (uint32_t n = 0; n < N; n++)
+                for (int a = 0; a < 3; a++) {
+                    lo[a] = std::min(lo[a], hm.rest[3 * (size_t)n + a]);
+                    hi[a] = std::max(hi[a], hm.rest[3 * (size_t)n + a]);
+                }
+            double ext = std::max(hi[0] - lo[0], std::max(hi[1] - lo[1], hi[2] - lo[2]));
+            if (!(ext > 0)) ext = 1.0;
+            std::vector<uint64_t> key(T);
+            for (uint32_t e = 0; e < T; e++) {
+                double c[3] = {0, 0, 0};
+                for (int i = 0; i < 4; i++)
+                    for (int a = 0; a < 3; a++) c[a] += 0.25 * hm.rest[3 * (size_t)hm.tets[4 * (size_t)e + i] + a];
+                uint32_t qv[3];
+                for (int a = 0; a < 3; a++) {
+                    double f = (c[a] - lo[a]) / ext * 1023.0;
+                    qv[a] = (uint32_t)std::max(0.0, std::min(1023.0, f));
+                }
+                const uint32_t code = spread10(qv[0]) | (spread10(qv[1]) << 1) | (spread10(qv[2]) << 2);
+                key[e] = ((uint64_t)code << 32) | e;
+            }
+            std::sort(key.begin(), key.end());
+            for (uint32_t e = 0; e < T; e++) order[e] = (uint32_t)(key[e] & 0xffffffffu);
+        }
+        // per-element data in the new order
+        double acc_total_volume = 0.0;
+        std::vector<double> vol_orig(T);
+        for (uint32_t e = 0; e < T; e++) {
+            const uint32_t* t = &hm.tets[4 * (size_t)e];
+            double D[9];
+            for (int i = 0; i < 3; i++) {
+                D[3 * i] = hm.rest[3 * (size_t)t[1] + i] - hm.rest[3 * (size_t)t[0] + i];
+                D[3 * i + 1] = hm.rest[3 * (size_t)t[2] + i] - hm.rest[3 * (size_t)t[0] + i];
+                D[3 * i + 2] = hm.rest[3 * (size_t)t[3] + i] - hm.rest[3 * (size_t)t[0] + i];
+            }
+            const double V = det3(D) / 6.0;
+            if (!(V > 0.0)) return batch_fail(FEM_E_DEGENERATE, "mesh %u tet %u has rest volume %g <= 0", mi, e, V);
+            vol_orig[e] = V;
+            acc_total_volume += V;  // the reference's element order (EndEdition)
+        }
+        for (uint32_t k = 0; k < T; k++) {
+            const uint32_t e = order[k];
+            const uint32_t* t = &hm.tets[4 * (size_t)e];
+            double D[9];
+            for (int i = 0; i < 3; i++) {
+                D[3 * i] = hm.rest[3 * (size_t)t[1] + i] - hm.rest[3 * (size_t)t[0] + i];
+                D[3 * i + 1] = hm.rest[3 * (size_t)t[2] + i] - hm.rest[3 * (size_t)t[0] + i];
+                D[3 * i + 2] = hm.rest[3 * (size_t)t[3] + i] - hm.rest[3 * (size_t)t[0] + i];
+            }
+            double Di[9];
+            inverse3(D, Di);
+            const double V = vol_orig[e];
+            const double E = hm.E.empty() ? p.young_modulus : hm.E[e];
+            const double nu = hm.nu.empty() ? p.poisson_ratio : hm.nu[e];
+            const double a = E / ((1.0 + nu) * (1.0 - 2.0 * nu));
+            for (int c = 0; c < 9; c++) Dinv_aos.push_back(Di[c]);
+            mat_aos.push_back(V * (a * (1.0 - nu)));
+            mat_aos.push_back(V * (a * nu));
+            mat_aos.push_back(V * (a * (0.5 - nu)));
+            vol.push_back(V);
+            gtets.push_back(make_int4((int)(node0 + t[0]), (int)(node0 + t[1]), (int)(node0 + t[2]),
+                                      (int)(node0 + t[3])));
+        }
+        // tiles
+        MeshConsts& c = mcs[mi];
+        c.tile0 = (uint32_t)tiles.size();
+        std::vector<int32_t> stamp(N, -1), local(N, 0);
+        uint32_t k = 0;
+        while (k < T) {
+            TileMeta tm;
+            tm.mesh = mi;
+            tm.e0 = (uint32_t)(elem0 + k);
+            tm.n0 = (uint32_t)tile_nodes.size();
+            tm.c0 = (uint32_t)lidx.size();
+            const int32_t tid = (int32_t)tiles.size();
+            std::vector<uint32_t> lnodes;
+            uint32_t ne = 0;
+            while (k < T && ne < tile_cap) {
+                const uint32_t* t = &hm.tets[4 * (size_t)order[k]];
+                uint32_t fresh = 0;
+                for (int i = 0; i < 4; i++) {
+                    bool seen = stamp[t[i]] == tid;
+                    for (int j = 0; j < i; j++) seen |= (t[j] == t[i]);
+                    fresh += seen ? 0 : 1;
+                }
+                if (lnodes.size() + fresh > (size_t)kTileNodes) break;
+                uchar4 lc;
+                unsigned char li4[4];
+                for (int i = 0; i < 4; i++) {
+                    if (stamp[t[i]] != tid) {
+                        stamp[t[i]] = tid;
+                        local[t[i]] = (int32_t)lnodes.size();
+                        lnodes.push_back(t[i]);
+                    }
+                    li4[i] = (unsigned char)local[t[i]];
+                }
+                lc.x = li4[0]; lc.y = li4[1]; lc.z = li4[2]; lc.w = li4[3];
+                lconn.push_back(lc);
+                ne++;
+                k++;
+            }
+            tm.ne = (uint16_t)ne;
+            tm.nn = (uint16_t)lnodes.size();
+            // tile-local CSR: local node -> (element << 2 | slot), element order
+            std::vector<uint16_t> cnt(lnodes.size() + 1, 0);
+            const size_t lc0 = lconn.size() - ne;
+            for (uint32_t el = 0; el < ne; el++) {
+                const uchar4 lc = lconn[lc0 + el];
+                cnt[lc.x + 1]++; cnt[lc.y + 1]++; cnt[lc.z + 1]++; cnt[lc.w + 1]++;
+            }
+            for (size_t i = 0; i < lnodes.size(); i++) cnt[i + 1] += cnt[i];
+            lptr0.push_back((uint32_t)lptr.size());
+            for (size_t i = 0; i <= lnodes.size(); i++) lptr.push_back(cnt[i]);
+            std::vector<uint16_t> fill(cnt.begin(), cnt.end() - 1), ent(4 * ne);
+            for (uint32_t el = 0; el < ne; el++) {
+                const uchar4 lc = lconn[lc0 + el];
+                const unsigned char ids[4] = {lc.x, lc.y, lc.z, lc.w};
+                for (int sl = 0; sl < 4; sl++) ent[fill[ids[sl]]++] = (uint16_t)((el << 2) | sl);
+            }
+            lidx.insert(lidx.end(), ent.begin(), ent.end());
+            for (uint32_t n : lnodes) tile_nodes.push_back((uint32_t)(node0 + n));
+            tiles.push_back(tm);
+        }
+        c.ntiles = (uint32_t)tiles.size() - c.tile0;
+        // node chunks
+        c.chunk0 = (uint32_t)chunks.size();
+        for (uint32_t n = 0; n < N; n += kChunkNodes) {
+            ChunkMeta ch;
+            ch.mesh = mi;
+            ch.n0 = (uint32_t)(node0 + n);
+            ch.n1 = (uint32_t)(node0 + std::min<uint32_t>(N, n + kChunkNodes));
+            chunks.push_back(ch);
+        }
+        c.nchunks = (uint32_t)chunks.size() - c.chunk0;
+        // constants (RebuildMass, RebuildRayleighCoeffsFromFreqs, Step_QuasiImplicitEuler_v)
+        const double total_mass = p.density * acc_total_volume;
+        const double mass_per_node = total_mass / N;
+        const double inv_mass = (double)1.0f / mass_per_node;
+        double ray[2];
+        {
+            const double f1 = (double)0.1f, f2 = (double)10000.0f;
+            const double o00 = 1.0 / f1, o01 = f1, o10 = 1.0 / f2, o11 = f2;
+            const double inv_det = 1.0 / (o00 * o11 - o10 * o01);
+            const double i00 = inv_det * o11, i01 = -inv_det * o01, i10 = -inv_det * o10, i11 = inv_det * o00;
+            const double z = 2 * p.damping_ratio;
+            double a0 = 0, a1 = 0;
+            a0 += i00 * z; a0 += i01 * z;
+            a1 += i10 * z; a1 += i11 * z;
+            ray[0] = a0;
+            ray[1] = a1;
+        }
+        c.dt = p.fixed_dt;
+        c.inv_dt = 1.0 / p.fixed_dt;
+        c.mass = 1.0 / inv_mass;
+        c.factor_M = 1.0 + c.dt * ray[0];
+        c.factor_K = c.dt * c.dt + c.dt * ray[1];
+        for (int a = 0; a < 3; a++) c.gravity[a] = p.gravity[a];
+        c.density = p.density;
+        c.rel_eps_sq = p.ls_rel_epsilon * p.ls_rel_epsilon;
+        c.abs_eps_sq = p.ls_abs_epsilon * p.ls_abs_epsilon;
+        c.degenerate_det_F = p.degenerate_det_F;
+        c.max_iter = p.ls_max_iter;
+        c.refresh_every = fp64 ? 0u : p.refresh_every;
+        c.node0 = (uint32_t)node0;
+        c.N = N;
+        c.elem0 = (uint32_t)elem0;
+        c.T = T;
+        c.knc0 = (uint32_t)knc_node.size();
+        c.nknc = (uint32_t)hm.knc_nodes.size();
+        // nodes
+        for (size_t i = 0; i < hm.rest.size(); i++) rest_all.push_back(hm.rest[i]);
+        const size_t f0 = fixed.size();
+        fixed.resize(f0 + N, 0);
+        for (size_t kk = 0; kk < hm.knc_nodes.size(); kk++) {
+            knc_node.push_back((uint32_t)(node0 + hm.knc_nodes[kk]));
+            knc_mesh.push_back(mi);
+            for (int a = 0; a < 3; a++) knc_target.push_back(hm.knc_targets[3 * kk + a]);
+            fixed[f0 + hm.knc_nodes[kk]] = 1;
+        }
+        node0 += N;
+        elem0 += T;
+    }
+    if (node0 >= (1ull << 31) || elem0 >= (1ull << 31)) return batch_fail(FEM_E_ARG, "batch too large");
+    b->Ntot = node0;
+    b->Ttot = elem0;
+    b->ntiles = (uint32_t)tiles.size();
+    b->nchunks = (uint32_t)chunks.size();
+    b->K = (uint32_t)knc_node.size();
+    b->nslots = tile_nodes.size();
+    b->mc_host = mcs;
+    // node -> partial slots, tile order
+    std::vector<uint32_t> nptr(b->Ntot + 1, 0), nslot(b->nslots);
+    for (uint32_t g : tile_nodes) nptr[g + 1]++;
+    for (uint64_t n = 0; n < b->Ntot; n++) nptr[n + 1] += nptr[n];
+    {
+        std::vector<uint32_t> fill(nptr.begin(), nptr.end() - 1);
+        for (size_t sidx = 0; sidx < tile_nodes.size(); sidx++) nslot[fill[tile_nodes[sidx]]++] = (uint32_t)sidx;
+    }
+    // SoA transposes
+    const size_t T = b->Ttot;
+    std::vector<double> Dinv_soa(9 * T), mat_soa(3 * T);
+    for (size_t e = 0; e < T; e++) {
+        for (int c = 0; c < 9; c++) Dinv_soa[c * T + e] = Dinv_aos[9 * e + c];
+        for (int c = 0; c < 3; c++) mat_soa[c * T + e] = mat_aos[3 * e + c];
+    }
+    std::vector<double> Rinit(9 * T, 0.0);
+    for (size_t e = 0; e < T; e++) Rinit[e] = Rinit[4 * T + e] = Rinit[8 * T + e] = 1.0;
+
+    // ---- device ----
+    auto cleanup = [&](int code) {
+        b->release();
+        return code;
+    };
+#define BCKC(call)                                                                                        \
+    do {                                                                                                  \
+        cudaError_t e_ = (call);                                                                          \
+        if (e_ != cudaSuccess)                                                                            \
+            return cleanup(batch_fail(e_ == cudaErrorMemoryAllocation ? FEM_E_OOM : FEM_E_CUDA, "%s: %s", #call, \
+                                      cudaGetErrorString(e_)));                                           \
+    } while (0)
+    BCKC(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+    cudaStream_t s = b->stream;
+    const size_t SB = b->S_size();
+    const size_t N3 = 3 * b->Ntot;
+    BCKC(b->tiles.alloc(b->ntiles));
+    BCKC(b->chunks.alloc(b->nchunks));
+    BCKC(b->mc.alloc(b->M));
+    BCKC(b->st.alloc(b->M));
+    BCKC(b->active.alloc(b->M));
+    BCKC(b->gtets.alloc(T));
+    BCKC(b->Dinv_s.alloc(9 * T * SB));
+    BCKC(b->mat_s.alloc(3 * T * SB));
+    BCKC(b->R_s.alloc(9 * T * SB));
+    BCKC(b->Dinv64.alloc(9 * T));
+    BCKC(b->vol.alloc(T));
+    BCKC(b->detF.alloc(T));
+    BCKC(b->tile_nodes.alloc(b->nslots));
+    BCKC(b->lptr0.alloc(b->ntiles));
+    BCKC(b->nptr.alloc(b->Ntot + 1));
+    BCKC(b->nslot.alloc(b->nslots));
+    BCKC(b->knc_node.alloc(b->K));
+    BCKC(b->knc_mesh.alloc(b->K));
+    BCKC(b->knc_target.alloc(3 * (size_t)b->K));
+    BCKC(b->lconn.alloc(T));
+    BCKC(b->lptr.alloc(lptr.size()));
+    BCKC(b->lidx.alloc(lidx.size()));
+    BCKC(b->fixed.alloc(b->Ntot));
+    BCKC(b->rest.alloc(N3));
+    BCKC(b->x.alloc(N3));
+    BCKC(b->v.alloc(N3));
+    BCKC(b->bvec.alloc(N3));
+    BCKC(b->y.alloc(N3));
+    BCKC(b->r_s.alloc(N3 * SB));
+    BCKC(b->d_s.alloc(N3 * SB));
+    BCKC(b->q_s.alloc(N3 * SB));
+    BCKC(b->part_s.alloc(3 * b->nslots * SB));
+    BCKC(b->part64.alloc(3 * b->nslots));
+    BCKC(b->cpart.alloc(b->nchunks));
+    BCKC(b->tpart.alloc(b->ntiles));
+    BCKC(b->counter.alloc(1));
+    BCKC(b->any_flag.alloc(1));
+    BCKC(b->refresh_flag.alloc(1));
+    BCKC(b->mcount.alloc(b->M));
+    BCKC(cudaMallocHost(&b->st_host, sizeof(StepScalars) * b->M));
+    BCKC(b->tiles.upload(tiles, s));
+    BCKC(b->chunks.upload(chunks, s));
+    BCKC(b->mc.upload(mcs, s));
+    BCKC(cudaMemsetAsync(b->st.p, 0, sizeof(StepScalars) * b->M, s));
+    BCKC(cudaMemsetAsync(b->active.p, 1, b->M, s));
+    BCKC(b->gtets.upload(gtets, s));
+    {
+        std::vector<unsigned char> tmp = fp64 ? as_bytes<double>(Dinv_soa) : as_bytes<float>(Dinv_soa);
+        BCKC(b->Dinv_s.upload(tmp, s));
+        BCKC(cudaStreamSynchronize(s));
+        tmp = fp64 ? as_bytes<double>(mat_soa) : as_bytes<float>(mat_soa);
+        BCKC(b->mat_s.upload(tmp, s));
+        BCKC(cudaStreamSynchronize(s));
+        tmp = fp64 ? as_bytes<double>(Rinit) : as_bytes<float>(Rinit);
+        BCKC(b->R_s.upload(tmp, s));
+        BCKC(cudaStreamSynchronize(s));
+    }
+    BCKC(b->Dinv64.upload(Dinv_soa, s));
+    BCKC(b->vol.upload(vol, s));
+    BCKC(b->tile_nodes.upload(tile_nodes, s));
+    BCKC(b->lptr0.upload(lptr0, s));
+    BCKC(b->nptr.upload(nptr, s));
+    BCKC(b->nslot.upload(nslot, s));
+    BCKC(b->knc_node.upload(knc_node, s));
+    BCKC(b->knc_mesh.upload(knc_mesh, s));
+    BCKC(b->knc_target.upload(knc_target, s));
+    BCKC(b->lconn.upload(lconn, s));
+    BCKC(b->lptr.upload(lptr, s));
+    BCKC(b->lidx.upload(lidx, s));
+    BCKC(b->fixed.upload(fixed, s));
+    BCKC(b->rest.upload(rest_all, s));
+    BCKC(b->x.upload(rest_all, s));
+    BCKC(cudaMemsetAsync(b->v.p, 0, sizeof(double) * N3, s));
+    BCKC(cudaMemsetAsync(b->y.p, 0, sizeof(double) * N3, s));
+    BCKC(cudaMemsetAsync(b->counter.p, 0, sizeof(unsigned), s));
+    BCKC(cudaMemsetAsync(b->any_flag.p, 0, sizeof(unsigned), s));
+    BCKC(cudaMemsetAsync(b->refresh_flag.p, 0, sizeof(unsigned), s));
+    BCKC(cudaMemsetAsync(b->mcount.p, 0, sizeof(unsigned) * b->M, s));
+    BCKC(cudaStreamSynchronize(s));
+#undef BCKC
+    b->device_bytes = 0;
+    b->device_bytes += b->tiles.bytes() + b->chunks.bytes() + b->mc.bytes() + b->st.bytes() + b->gtets.bytes() +
+                       b->Dinv_s.bytes() + b->mat_s.bytes() + b->R_s.bytes() + b->Dinv64.bytes() + b->vol.bytes() +
+                       b->detF.bytes() + b->tile_nodes.bytes() + b->lptr0.bytes() + b->nptr.bytes() +
+                       b->nslot.bytes() + b->lconn.bytes() + b->lptr.bytes() + b->lidx.bytes() + b->fixed.bytes() +
+                       7 * N3 * 8 / 2 + b->r_s.bytes() * 3 + b->part_s.bytes() + b->part64.bytes();
+    b->finalized = true;
+    // host copies of the meshes are no longer needed beyond sizes
+    for (auto& m : b->meshes) {
+        std::vector<uint32_t>().swap(m.tets);
+        std::vector<double>().swap(m.E);
+        std::vector<double>().swap(m.nu);
+    }
+    if (b->opt.use_graph) {
+        int rc = build_graph(b);
+        if (rc != FEM_OK) return rc;
+    }
+    return FEM_OK;
+}
+
+int fem_batch_destroy(fem_batch b)
+{
+    if (!b) return FEM_OK;
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    b->release();
+    delete b;
+    return FEM_OK;
+}
+
+static int check_ready(fem_batch b)
+{
+    if (!b) return batch_fail(FEM_E_ARG, "null batch");
+    if (!b->finalized) return batch_fail(FEM_E_ARG, "batch not finalized");
+    return FEM_OK;
+}
+
+int fem_batch_info(fem_batch b, uint32_t* meshes, uint64_t* nodes, uint64_t* tets, uint32_t* tiles,
+                   uint64_t* device_bytes)
+{
+    if (!b) return batch_fail(FEM_E_ARG, "null batch");
+    if (meshes) *meshes = (uint32_t)b->meshes.size();
+    if (nodes) *nodes = b->Ntot;
+    if (tets) *tets = b->Ttot;
+    if (tiles) *tiles = b->ntiles;
+    if (device_bytes) *device_bytes = b->device_bytes;
+    return FEM_OK;
+}
+
+int fem_batch_set_knc_targets(fem_batch b, uint32_t mesh, const double* targets)
+{
+    if (int e = check_ready(b)) return e;
+    if (mesh >= b->M) return batch_fail(FEM_E_ARG, "mesh %u out of range", mesh);
+    const MeshConsts& c = b->mc_host[mesh];
+    if (c.nknc == 0) return FEM_OK;
+    if (!targets) return batch_fail(FEM_E_ARG, "null targets");
+    BCK(cudaMemcpyAsync(b->knc_target.p + 3 * (size_t)c.knc0, targets, sizeof(double) * 3 * c.nknc,
+                        cudaMemcpyHostToDevice, b->stream));
+    return FEM_OK;
+}
+
+int fem_batch_set_state(fem_batch b, uint32_t mesh, const double* x, const double* v)
+{
+    if (int e = check_ready(b)) return e;
+    if (mesh >= b->M) return batch_fail(FEM_E_ARG, "mesh %u out of range", mesh);
+    const MeshConsts& c = b->mc_host[mesh];
+    const size_t off = 3 * (size_t)c.node0, bytes = sizeof(double) * 3 * c.N;
+    if (x) BCK(cudaMemcpyAsync(b->x.p + off, x, bytes, cudaMemcpyHostToDevice, b->stream));
+    if (v) BCK(cudaMemcpyAsync(b->v.p + off, v, bytes, cudaMemcpyHostToDevice, b->stream));
+    return FEM_OK;
+}
+
+int fem_batch_get_state(fem_batch b, uint32_t mesh, double* x, double* v)
+{
+    if (int e = check_ready(b)) return e;
+    if (mesh >= b->M) return batch_fail(FEM_E_ARG, "mesh %u out of range", mesh);
+    const MeshConsts& c = b->mc_host[mesh];
+    const size_t off = 3 * (size_t)c.node0, bytes = sizeof(double) * 3 * c.N;
+    if (x) BCK(cudaMemcpyAsync(x, b->x.p + off, bytes, cudaMemcpyDeviceToHost, b->stream));
+    if (v) BCK(cudaMemcpyAsync(v, b->v.p + off, bytes, cudaMemcpyDeviceToHost, b->stream));
+    BCK(cudaStreamSynchronize(b->stream));
+    return FEM_OK;
+}
+
+int fem_batch_set_active(fem_batch b, const uint8_t* mask)
+{
+    if (int e = check_ready(b)) return e;
+    if (mask) BCK(cudaMemcpyAsync(b->active.p, mask, b->M, cudaMemcpyHostToDevice, b->stream));
+    else BCK(cudaMemsetAsync(b->active.p, 1, b->M, b->stream));
+    return FEM_OK;
+}
+
+int fem_batch_step_async(fem_batch b, uint32_t nsteps)
+{
+    if (int e = check_ready(b)) return e;
+    for (uint32_t i = 0; i < nsteps; i++) {
+        if (b->exec) {
+            BCK(cudaGraphLaunch(b->exec, b->stream));
+            launch_counter() += 0;  // kernels inside the graph are counted at capture
+        } else {
+            int rc = b->opt.precision == FEM_PRECISION_FP64 ? enqueue_step<double>(b, b->stream, false)
+                                                            : enqueue_step<float>(b, b->stream, false);
+            if (rc) return rc;
+        }
+    }
+    return FEM_OK;
+}
+
+int fem_batch_synchronize(fem_batch b)
+{
+    if (int e = check_ready(b)) return e;
+    BCK(cudaMemcpyAsync(b->st_host, b->st.p, sizeof(StepScalars) * b->M, cudaMemcpyDeviceToHost, b->stream));
+    BCK(cudaStreamSynchronize(b->stream));
+    for (uint32_t m = 0; m < b->M; m++)
+        if (b->st_host[m].status == FEM_E_NAN) return batch_fail(FEM_E_NAN, "NaN in the CG residual of mesh %u", m);
+    return FEM_OK;
+}
+
+int fem_batch_step(fem_batch b, uint32_t nsteps)
+{
+    if (int e = fem_batch_step_async(b, nsteps)) return e;
+    return fem_batch_synchronize(b);
+}
+
+int fem_batch_get_stats(fem_batch b, uint32_t mesh, fem_step_stats* out)
+{
+    if (int e = check_ready(b)) return e;
+    if (mesh >= b->M || !out) return batch_fail(FEM_E_ARG, "bad mesh index or null output");
+    const StepScalars& h = b->st_host[mesh];  // as of the last synchronize
+    out->cg_iterations = h.k;
+    out->status = h.status;
+    out->rel_residual = h.rel_residual;
+    out->abs_residual = h.abs_residual;
+    out->elastic_energy = h.elastic_energy;
+    out->potential_energy = h.potential_energy;
+    out->inverted_elements = h.inverted;
+    out->fp64_resolved = h.fp64_resolved;
+    out->total_cg_iterations = h.total_iters;
+    return FEM_OK;
+}
+
+int fem_batch_kernel_launches(fem_batch b, uint32_t steps, uint64_t* launches)
+{
+    if (int e = check_ready(b)) return e;
+    if (!launches) return batch_fail(FEM_E_ARG, "null output");
+    unsigned body_runs = 0;
+    BCK(cudaMemcpyAsync(&body_runs, b->any_flag.p, sizeof(unsigned), cudaMemcpyDeviceToHost, b->stream));
+    BCK(cudaStreamSynchronize(b->stream));
+    // kernels per step outside the CG loop, plus 6 per executed CG iteration
+    bool energy = false;
+    for (auto& m : b->meshes) energy |= m.p.compute_energy != 0;
+    const bool mixed = b->opt.precision == FEM_PRECISION_MIXED;
+    const uint64_t fixed = 8 + (b->K ? 1 : 0) + (energy ? 4 : 0);
+    *launches = (uint64_t)steps * fixed + (mixed ? 4ull : 3ull) * body_runs;
+    return FEM_OK;
+}
+
+int fem_batch_reset_launch_count(fem_batch b)
+{
+    if (int e = check_ready(b)) return e;
+    BCK(cudaMemsetAsync(b->any_flag.p, 0, sizeof(unsigned), b->stream));
+    return FEM_OK;
+}
+
+int fem_batch_stream(fem_batch b, void** stream)
+{
+    if (int e = check_ready(b)) return e;
+    if (!stream) return batch_fail(FEM_E_ARG, "null stream pointer");
+    *stream = (void*)b->stream;
+    return FEM_OK;
+}
+
+}  // extern "C"

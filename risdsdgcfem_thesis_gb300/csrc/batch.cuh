@@ -1,0 +1,94 @@
+// batch.cuh -- device layout of a batch of independent solids stepped in
+// lock-step (the tiled path; one solid is a batch of one).
+//
+// Meshes are concatenated: mesh m owns global nodes [node0, node0+N) in its
+// own node order and global elements [elem0, elem0+T) in a Morton order of
+// element centroids. Elements are cut into tiles of at most kTileElems tets
+// touching at most kTileNodes distinct nodes; a tile belongs to one mesh.
+//
+//   per tile     TileMeta: element range, its local node list (tile_nodes,
+//                global ids), its local connectivity (lconn, uchar4 local
+//                ids) and a tile-local CSR (lptr/lidx) giving, for each local
+//                node, the (element, slot) outputs to sum, in element order
+//   per element  Dinv/mat/R in the path's element type S (SoA), plus FP64
+//                Dinv, volume and global ids for the once-per-step kernels
+//   per node     x, v, b, y (FP64); r, d, q (S); rest (FP64); fixed flag;
+//                CSR nptr/nslot over the partial slots of the tiles that
+//                touch it, in tile order
+//   per (tile,local node)  part: the tile's summed contribution
+//
+// All sums have a fixed order, so a solid gives the same bits alone and in
+// any batch.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "fem_device.cuh"
+
+namespace femgb {
+
+constexpr int kTileElems = 256;
+constexpr int kTileNodes = 256;
+constexpr int kChunkNodes = 1024;  // node chunk = one block's share in node kernels
+constexpr int kNodeThreads = 256;  // threads per node-kernel block
+
+struct TileMeta {
+    uint32_t mesh;
+    uint32_t e0;      // first element (global)
+    uint32_t n0;      // first slot in tile_nodes / part
+    uint32_t c0;      // first entry in lidx
+    uint16_t ne, nn;  // elements, local nodes
+};
+
+struct ChunkMeta {
+    uint32_t mesh;
+    uint32_t n0, n1;  // global node range
+};
+
+// Per-mesh constants.
+struct MeshConsts {
+    double dt, inv_dt, mass, factor_M, factor_K;
+    double gravity[3];
+    double density;
+    double rel_eps_sq, abs_eps_sq;
+    double degenerate_det_F;
+    uint32_t max_iter, refresh_every;
+    uint32_t node0, N, elem0, T;
+    uint32_t tile0, ntiles, chunk0, nchunks;
+    uint32_t knc0, nknc;
+};
+
+template <typename S>
+struct BatchView {
+    uint32_t M, ntiles, nchunks, Ntot, Ttot;
+    const TileMeta* tiles;
+    const ChunkMeta* chunks;
+    const MeshConsts* mc;
+    StepScalars* st;               // [M]
+    const uint8_t* active;         // [M] meshes taking part in this step
+    // element data
+    const int4* gtets;             // [Ttot] global node ids
+    const S* Dinv;                 // [9][Ttot]
+    const S* mat;                  // [3][Ttot]
+    S* R;                          // [9][Ttot]
+    const double* Dinv64;          // [9][Ttot]
+    const double* vol;             // [Ttot]
+    double* detF;                  // [Ttot]
+    // tile structure
+    const uint32_t* tile_nodes;    // [sum nn] global node id
+    const uchar4* lconn;           // [Ttot] local ids within the tile
+    const uint16_t* lptr;          // [sum (nn+1)] per tile: offsets into lidx (tile-relative)
+    const uint16_t* lidx;          // [4 Ttot] (element-in-tile << 2 | slot), tile-relative
+    const uint32_t* lptr0;         // [ntiles] base of each tile's lptr block
+    // node data
+    const uint32_t* nptr;          // [Ntot+1]
+    const uint32_t* nslot;         // [sum nn] partial slots per node
+    const uint8_t* fixed;          // [Ntot]
+    const double* rest;            // [3 Ntot]
+    // constraints
+    const uint32_t* knc_node;      // [K] global node id
+    const uint32_t* knc_mesh;      // [K]
+    const double* knc_target;      // [3K]
+};
+
+}  // namespace femgb

@@ -1,0 +1,794 @@
+// batch_kernels.cu -- kernels of the tiled, batched step (FP64 and mixed).
+//
+// One CG iteration (Saphyre2 ns/ILSS_CG.h:90-144) over every mesh whose loop
+// is still running, in lock-step, is three kernels:
+//   k_tile_spmv   one CTA per element tile: the tile's node values of the
+//                 search direction d = S(r + beta d) are formed while staging
+//                 r and d in shared memory, each thread forms one element's
+//                 R K0 R^T d (elem_math.cuh), the 12 outputs go to shared
+//                 memory, and each local node sums its entries in element
+//                 order (tile-local CSR) into one partial per (tile, node).
+//   k_node_q      per node: the same d (written back), q = S(fK sum(partials)
+//                 + m fM d), FP64 d.q partials per node chunk; the last block
+//                 of each mesh sums its partials in a fixed order and forms
+//                 alpha (or stops the mesh on breakdown, ILSS_CG.h:97). On
+//                 refresh iterations (mixed) also the true residual b - A y
+//                 from the FP64 product of k_tile_spmv_y64.
+//   k_node_update y += alpha d (FP64), r -= alpha q, FP64 |r|^2 partials; the
+//                 last block of each mesh forms beta and the mesh's loop test,
+//                 and the last block of the grid sets the CUDA-graph while
+//                 condition (any mesh still iterating) and the refresh flag.
+// "Last block" uses per-mesh and per-grid arrival counters after a
+// __threadfence (no waiting); the sums it forms do not depend on which block
+// arrives last.
+// The once-per-step kernels (elastic force, right-hand side, constraints,
+// initial residual, integration, energies) follow
+// Step_QuasiImplicitEuler_v (LeafDSH_Solid3D_FEM.cpp:1205-1328).
+#include "batch.cuh"
+#include "batch_launch.h"
+#include "elem_math.cuh"
+#include "msvd.cuh"
+
+namespace femgb {
+
+__device__ __forceinline__ double bwarp_sum(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+__device__ __forceinline__ double bblock_sum(double v)
+{
+    __shared__ double sh[32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    v = bwarp_sum(v);
+    __syncthreads();
+    if (lane == 0) sh[wid] = v;
+    __syncthreads();
+    const int nw = (blockDim.x + 31) >> 5;
+    v = (threadIdx.x < nw) ? sh[threadIdx.x] : 0.0;
+    if (wid == 0) v = bwarp_sum(v);
+    return v;
+}
+
+template <typename S>
+__device__ __forceinline__ bool mesh_running(const BatchView<S>& b, uint32_t m)
+{
+    return !b.st[m].done;
+}
+
+// CG iteration index at which the mesh refreshes its residual in FP64.
+__device__ __forceinline__ bool refresh_now(const MeshConsts& c, const StepScalars& s)
+{
+    return c.refresh_every > 0 && ((s.k + 1) % c.refresh_every) == 0;
+}
+
+// ---------------------------------------------------------------------------
+// Element tile product of the new search direction: for each local node the
+// tile stages d = S(r + beta d) (beta of the tile's mesh; zero rows stay zero
+// because r and d are zero on constrained nodes), then part[tile node] = sum
+// over the tile's elements of R K0 R^T d at that node, in S.
+template <typename S>
+__device__ __forceinline__ S dir_update(S beta, S d, S r);
+template <>
+__device__ __forceinline__ float dir_update<float>(float beta, float d, float r) { return __fmaf_rn(beta, d, r); }
+template <>
+__device__ __forceinline__ double dir_update<double>(double beta, double d, double r) { return __fma_rn(beta, d, r); }
+
+template <typename S>
+__global__ void __launch_bounds__(256) k_tile_spmv(BatchView<S> b, const S* __restrict__ dvec,
+                                                   const S* __restrict__ rvec, S* __restrict__ part,
+                                                   cudaGraphConditionalHandle if_refresh, int set_if,
+                                                   const unsigned* __restrict__ refresh_flag)
+{
+    __shared__ S sd[3 * kTileNodes];
+    __shared__ S so[12 * kTileElems];
+    // the graph's IF node after this kernel runs the FP64 refresh product
+    // only on iterations where some mesh refreshes its residual
+    if (set_if && blockIdx.x == 0 && threadIdx.x == 0) cudaGraphSetConditional(if_refresh, *refresh_flag ? 1u : 0u);
+    const uint32_t t = blockIdx.x;
+    if (t >= b.ntiles) return;
+    const TileMeta tm = b.tiles[t];
+    if (!mesh_running(b, tm.mesh)) return;
+    const S beta = (S)b.st[tm.mesh].beta;
+    const uint16_t* lp = b.lptr + b.lptr0[t];
+    const uint16_t* li = b.lidx + tm.c0;
+    // element data first: these loads are in flight while the tile stages
+    // its node values
+    const bool has_elem = threadIdx.x < tm.ne;
+    const size_t e = tm.e0 + (has_elem ? threadIdx.x : 0);
+    const size_t T = b.Ttot;
+    S R[9], Di[9], k1 = 0, knu = 0, k2 = 0;
+    uchar4 lc = make_uchar4(0, 0, 0, 0);
+    if (has_elem) {
+#pragma unroll
+        for (int c = 0; c < 9; c++) R[c] = b.R[c * T + e];
+#pragma unroll
+        for (int c = 0; c < 9; c++) Di[c] = b.Dinv[c * T + e];
+        k1 = b.mat[e];
+        knu = b.mat[T + e];
+        k2 = b.mat[2 * T + e];
+        lc = b.lconn[e];
+    }
+    for (int i = threadIdx.x; i < tm.nn; i += blockDim.x) {
+        const size_t g = b.tile_nodes[tm.n0 + i];
+        sd[i] = dir_update<S>(beta, dvec[3 * g], rvec[3 * g]);
+        sd[kTileNodes + i] = dir_update<S>(beta, dvec[3 * g + 1], rvec[3 * g + 1]);
+        sd[2 * kTileNodes + i] = dir_update<S>(beta, dvec[3 * g + 2], rvec[3 * g + 2]);
+    }
+    __syncthreads();
+    if (has_elem) {
+        const int ids[4] = {lc.x, lc.y, lc.z, lc.w};
+        S dl[12];
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            dl[3 * i] = sd[ids[i]];
+            dl[3 * i + 1] = sd[kTileNodes + ids[i]];
+            dl[3 * i + 2] = sd[2 * kTileNodes + ids[i]];
+        }
+        S out[12];
+        elem_RKRt<S>(R, Di, k1, knu, k2, dl, out);
+#pragma unroll
+        for (int c = 0; c < 12; c++) so[c * kTileElems + threadIdx.x] = out[c];
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < tm.nn; i += blockDim.x) {
+        S a0 = 0, a1 = 0, a2 = 0;
+        for (int j = lp[i]; j < lp[i + 1]; j++) {
+            const int v = li[j], el = v >> 2, sl = v & 3;
+            a0 += so[(3 * sl) * kTileElems + el];
+            a1 += so[(3 * sl + 1) * kTileElems + el];
+            a2 += so[(3 * sl + 2) * kTileElems + el];
+        }
+        const size_t o = 3 * (size_t)(tm.n0 + i);
+        part[o] = a0;
+        part[o + 1] = a1;
+        part[o + 2] = a2;
+    }
+}
+
+// FP64 product of the iterate y (same element data, evaluated in FP64):
+// mode SPMV_Y64_ALL for every active mesh (initial residual of a step);
+// mode SPMV_Y64_REFRESH for meshes refreshing their residual this iteration,
+// and only when the finaliser raised the batch's refresh flag (otherwise the
+// launch returns at once).
+enum { SPMV_Y64_ALL = 0, SPMV_Y64_REFRESH = 1 };
+
+template <typename S>
+__global__ void __launch_bounds__(256) k_tile_spmv_y64(BatchView<S> b, const double* __restrict__ y,
+                                                       double* __restrict__ part64, int mode,
+                                                       const unsigned* __restrict__ flag)
+{
+    if (mode == SPMV_Y64_REFRESH && flag && !*flag) return;
+    __shared__ double sd[3 * kTileNodes];
+    __shared__ double so[12 * kTileElems];
+    for (uint32_t t = blockIdx.x; t < b.ntiles; t += gridDim.x) {
+        const TileMeta tm = b.tiles[t];
+        if (mode == SPMV_Y64_ALL && !b.active[tm.mesh]) continue;
+        if (mode == SPMV_Y64_REFRESH && (!mesh_running(b, tm.mesh) || !refresh_now(b.mc[tm.mesh], b.st[tm.mesh])))
+            continue;
+        const uint16_t* lp = b.lptr + b.lptr0[t];
+        const uint16_t* li = b.lidx + tm.c0;
+        for (int i = threadIdx.x; i < tm.nn; i += blockDim.x) {
+            const size_t g = b.tile_nodes[tm.n0 + i];
+            sd[i] = y[3 * g];
+            sd[kTileNodes + i] = y[3 * g + 1];
+            sd[2 * kTileNodes + i] = y[3 * g + 2];
+        }
+        __syncthreads();
+        if (threadIdx.x < tm.ne) {
+            const size_t e = tm.e0 + threadIdx.x;
+            const size_t T = b.Ttot;
+            double R[9], Di[9];
+#pragma unroll
+            for (int c = 0; c < 9; c++) R[c] = (double)b.R[c * T + e];
+#pragma unroll
+            for (int c = 0; c < 9; c++) Di[c] = (double)b.Dinv[c * T + e];
+            const double k1 = b.mat[e], knu = b.mat[T + e], k2 = b.mat[2 * T + e];
+            const uchar4 lc = b.lconn[e];
+            const int ids[4] = {lc.x, lc.y, lc.z, lc.w};
+            double dl[12];
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+                dl[3 * i] = sd[ids[i]];
+                dl[3 * i + 1] = sd[kTileNodes + ids[i]];
+                dl[3 * i + 2] = sd[2 * kTileNodes + ids[i]];
+            }
+            double out[12];
+            elem_RKRt<double>(R, Di, k1, knu, k2, dl, out);
+#pragma unroll
+            for (int c = 0; c < 12; c++) so[c * kTileElems + threadIdx.x] = out[c];
+        }
+        __syncthreads();
+        for (int i = threadIdx.x; i < tm.nn; i += blockDim.x) {
+            double a0 = 0, a1 = 0, a2 = 0;
+            for (int j = lp[i]; j < lp[i + 1]; j++) {
+                const int v = li[j], el = v >> 2, sl = v & 3;
+                a0 += so[(3 * sl) * kTileElems + el];
+                a1 += so[(3 * sl + 1) * kTileElems + el];
+                a2 += so[(3 * sl + 2) * kTileElems + el];
+            }
+            const size_t o = 3 * (size_t)(tm.n0 + i);
+            part64[o] = a0;
+            part64[o + 1] = a1;
+            part64[o + 2] = a2;
+        }
+        __syncthreads();
+    }
+}
+
+// Elastic product at positions x (FP64): part64 = R K0 (R^T x - r) per tile
+// node (C_f_e's product, TetrahedronElementSet3.cpp:1053-1096) and/or the
+// per-tile elastic energy 0.5 u^T K0 u (C_V, :1456-1488).
+template <typename S>
+__global__ void __launch_bounds__(256) k_tile_force(BatchView<S> b, const double* __restrict__ x,
+                                                    double* __restrict__ part64, double* __restrict__ tile_energy)
+{
+    __shared__ double so[12 * kTileElems];
+    for (uint32_t t = blockIdx.x; t < b.ntiles; t += gridDim.x) {
+        const TileMeta tm = b.tiles[t];
+        if (!b.active[tm.mesh]) continue;
+        double energy = 0.0;
+        if (threadIdx.x < tm.ne) {
+            const size_t e = tm.e0 + threadIdx.x;
+            const size_t T = b.Ttot;
+            double R[9], Di[9];
+#pragma unroll
+            for (int c = 0; c < 9; c++) R[c] = (double)b.R[c * T + e];
+#pragma unroll
+            for (int c = 0; c < 9; c++) Di[c] = b.Dinv64[c * T + e];
+            const double k1 = b.mat[e], knu = b.mat[T + e], k2 = b.mat[2 * T + e];
+            const int4 g = b.gtets[e];
+            const int ids[4] = {g.x, g.y, g.z, g.w};
+            double u[12];
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+                const size_t n = ids[i];
+                const double xa = x[3 * n], xb = x[3 * n + 1], xc = x[3 * n + 2];
+#pragma unroll
+                for (int a = 0; a < 3; a++) {
+                    double acc = 0.0;
+                    acc += R[a] * xa;
+                    acc += R[3 + a] * xb;
+                    acc += R[6 + a] * xc;
+                    u[3 * i + a] = acc - b.rest[3 * n + a];
+                }
+            }
+            double D[9];
+#pragma unroll
+            for (int a = 0; a < 3; a++)
+#pragma unroll
+                for (int j = 0; j < 3; j++) D[3 * a + j] = u[3 * (j + 1) + a] - u[a];
+            double H[9];
+#pragma unroll
+            for (int a = 0; a < 3; a++)
+#pragma unroll
+                for (int c = 0; c < 3; c++) H[3 * a + c] = D[3 * a] * Di[c] + D[3 * a + 1] * Di[3 + c] + D[3 * a + 2] * Di[6 + c];
+            double P[9], es;
+            stress_forces(H, Di, k1, knu, k2, P, es);
+            energy = 0.5 * es;
+            if (part64) {
+                double out[12];
+                rotate_out(R, P, out);
+#pragma unroll
+                for (int c = 0; c < 12; c++) so[c * kTileElems + threadIdx.x] = out[c];
+            }
+        }
+        if (tile_energy) {
+            const double s = bblock_sum(energy);
+            if (threadIdx.x == 0) tile_energy[t] = s;
+        }
+        if (part64) {
+            __syncthreads();
+            const uint16_t* lp = b.lptr + b.lptr0[t];
+            const uint16_t* li = b.lidx + tm.c0;
+            for (int i = threadIdx.x; i < tm.nn; i += blockDim.x) {
+                double a0 = 0, a1 = 0, a2 = 0;
+                for (int j = lp[i]; j < lp[i + 1]; j++) {
+                    const int v = li[j], el = v >> 2, sl = v & 3;
+                    a0 += so[(3 * sl) * kTileElems + el];
+                    a1 += so[(3 * sl + 1) * kTileElems + el];
+                    a2 += so[(3 * sl + 2) * kTileElems + el];
+                }
+                const size_t o = 3 * (size_t)(tm.n0 + i);
+                part64[o] = a0;
+                part64[o + 1] = a1;
+                part64[o + 2] = a2;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// Potential energy term of RecomputeEnergy per tile (LeafDSH_Solid3D_FEM.cpp:1554-1584).
+template <typename S>
+__global__ void k_tile_potential(BatchView<S> b, const double* __restrict__ x, double* __restrict__ tile_pe)
+{
+    for (uint32_t t = blockIdx.x; t < b.ntiles; t += gridDim.x) {
+        const TileMeta tm = b.tiles[t];
+        if (!b.active[tm.mesh]) continue;
+        const MeshConsts& c = b.mc[tm.mesh];
+        double acc = 0.0;
+        if (threadIdx.x < tm.ne) {
+            const size_t e = tm.e0 + threadIdx.x;
+            const int4 g = b.gtets[e];
+            const int ids[4] = {g.x, g.y, g.z, g.w};
+            double s[3] = {0, 0, 0};
+#pragma unroll
+            for (int i = 0; i < 4; i++)
+#pragma unroll
+                for (int a = 0; a < 3; a++) s[a] += x[3 * (size_t)ids[i] + a];
+            const double em = c.density * b.vol[e];
+            acc = (em / 4.0) * (s[0] * -c.gravity[0] + s[1] * -c.gravity[1] + s[2] * -c.gravity[2]);
+        }
+        const double v = bblock_sum(acc);
+        if (threadIdx.x == 0) tile_pe[t] = v;
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// node kernels: one block per node chunk (kChunkNodes nodes of one mesh,
+// kNodeThreads threads striding it)
+
+template <typename P>
+__device__ __forceinline__ void sum_parts(const uint32_t* __restrict__ nptr, const uint32_t* __restrict__ nslot,
+                                          const P* __restrict__ part, size_t n, double& a0, double& a1, double& a2)
+{
+    a0 = a1 = a2 = 0.0;
+    const uint32_t j1 = nptr[n + 1];
+    for (uint32_t j = nptr[n]; j < j1; j++) {
+        const size_t o = 3 * (size_t)nslot[j];
+        a0 += (double)part[o];
+        a1 += (double)part[o + 1];
+        a2 += (double)part[o + 2];
+    }
+}
+
+// b = dt (m g - f_e-product) + m v ; y = v
+template <typename S>
+__global__ void k_node_b(BatchView<S> b, const double* __restrict__ part64, const double* __restrict__ v,
+                         double* __restrict__ bv, double* __restrict__ y)
+{
+    for (uint32_t ci = blockIdx.x; ci < b.nchunks; ci += gridDim.x) {
+        const ChunkMeta ch = b.chunks[ci];
+        if (!b.active[ch.mesh]) continue;
+        const MeshConsts& c = b.mc[ch.mesh];
+        for (size_t n = ch.n0 + threadIdx.x; n < ch.n1; n += blockDim.x) {
+            double f0, f1, f2;
+            sum_parts(b.nptr, b.nslot, part64, n, f0, f1, f2);
+            const size_t i = 3 * n;
+            bv[i] = (c.mass * c.gravity[0] - f0) * c.dt + c.mass * v[i];
+            bv[i + 1] = (c.mass * c.gravity[1] - f1) * c.dt + c.mass * v[i + 1];
+            bv[i + 2] = (c.mass * c.gravity[2] - f2) * c.dt + c.mass * v[i + 2];
+            y[i] = v[i];
+            y[i + 1] = v[i + 1];
+            y[i + 2] = v[i + 2];
+        }
+    }
+}
+
+// position constraints -> clamped velocity in b and y (LeafDSH_Solid3D_FEM.cpp:1268-1295)
+template <typename S>
+__global__ void k_knc(BatchView<S> b, uint32_t K, const double* __restrict__ x, double* __restrict__ bv,
+                      double* __restrict__ y)
+{
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < K; k += gridDim.x * blockDim.x) {
+        const uint32_t m = b.knc_mesh[k];
+        if (!b.active[m]) continue;
+        const MeshConsts& c = b.mc[m];
+        const size_t n = b.knc_node[k];
+        const double* tg = b.knc_target + 3 * (size_t)k;
+        V3<double> vk = mk<double>(c.inv_dt * (tg[0] - x[3 * n]), c.inv_dt * (tg[1] - x[3 * n + 1]),
+                                   c.inv_dt * (tg[2] - x[3 * n + 2]));
+        const double norm_vk = ::sqrt(dot0(vk, vk));
+        V3<double> vel = mk<double>(0.0, 0.0, 0.0);
+        if (norm_vk > (double)0.001f) {
+            const double cl = (norm_vk < 50.0) ? norm_vk : 50.0;
+            vel = scale(cl, normalized(vk));
+        }
+        bv[3 * n] = vel.x; bv[3 * n + 1] = vel.y; bv[3 * n + 2] = vel.z;
+        y[3 * n] = vel.x; y[3 * n + 1] = vel.y; y[3 * n + 2] = vel.z;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Arrival counting. After a block has written its chunk partial, the block
+// that completes a mesh's set of chunks sums them (fixed order) and updates
+// the mesh's CG scalars; after a block has finished all its chunks, the block
+// that completes the grid evaluates the batch-wide loop condition. Nothing
+// waits: the last arrival does the work.
+__device__ __forceinline__ bool arrive_last(unsigned* ctr, unsigned expected)
+{
+    __shared__ unsigned s_last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const unsigned prev = atomicAdd(ctr, 1u);
+        s_last = (prev + 1u == expected) ? 1u : 0u;
+        if (s_last) *ctr = 0u;
+    }
+    __syncthreads();
+    if (s_last) __threadfence();
+    return s_last != 0;
+}
+
+// Fixed-order sum of a mesh's chunk partials by the whole block (L1 bypassed:
+// the partials were written by other blocks of this kernel).
+__device__ __forceinline__ double mesh_partial_sum(const double* cpart, uint32_t c0, uint32_t n)
+{
+    double acc = 0.0;
+    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) acc += __ldcg(cpart + c0 + i);
+    return bblock_sum(acc);
+}
+
+__device__ __forceinline__ bool cg_cont(const StepScalars& s)
+{
+    return s.delta_new > s.abs_eps_sq && s.delta_new > s.delta_target && s.k < s.max_iter;
+}
+
+__device__ __forceinline__ void finish_stats(StepScalars& s)
+{
+    s.rel_residual = (s.delta_0 > 0) ? ::sqrt(s.delta_new / s.delta_0) : 0.0;
+    s.abs_residual = ::sqrt(s.delta_new);
+}
+
+// Last block of the grid: while condition (any mesh iterating) and the
+// refresh flag for the next iteration.
+template <typename S>
+__device__ void grid_tail(const BatchView<S>& b, const LoopSync& ls)
+{
+    if (!arrive_last(ls.gcount, gridDim.x)) return;
+    int any = 0, refresh = 0;
+    for (uint32_t i = threadIdx.x; i < b.M; i += blockDim.x) {
+        volatile const StepScalars* sp = b.st + i;
+        if (!sp->done) {
+            any = 1;
+            const MeshConsts& c = b.mc[i];
+            if (c.refresh_every > 0 && ((sp->k + 1) % c.refresh_every) == 0) refresh = 1;
+        }
+    }
+    any = __syncthreads_or(any);
+    refresh = __syncthreads_or(refresh);
+    if (threadIdx.x == 0) {
+        if (ls.refresh_flag) *ls.refresh_flag = refresh ? 1u : 0u;
+        if (ls.body_runs) *ls.body_runs += 1u;
+        if (ls.set_cond) cudaGraphSetConditional(ls.cond, any ? 1u : 0u);
+    }
+}
+
+// r = S(b - A y) with A y = fK sum(part64) + m fM y ; d = 0 ; |r|^2 ; the
+// last block of a mesh starts its CG loop (ILSS_CG.h:53-73).
+template <typename S>
+__global__ void k_node_residual(BatchView<S> b, const double* __restrict__ part64, const double* __restrict__ bv,
+                                const double* __restrict__ y, S* __restrict__ r, S* __restrict__ d,
+                                double* __restrict__ cpart, LoopSync ls)
+{
+    for (uint32_t ci = blockIdx.x; ci < b.nchunks; ci += gridDim.x) {
+        const ChunkMeta ch = b.chunks[ci];
+        if (!b.active[ch.mesh]) continue;
+        const MeshConsts& c = b.mc[ch.mesh];
+        const double mfm = c.mass * c.factor_M;
+        double acc = 0.0;
+        for (size_t n = ch.n0 + threadIdx.x; n < ch.n1; n += blockDim.x) {
+            const size_t i = 3 * n;
+            S r0 = 0, r1 = 0, r2 = 0;
+            if (!b.fixed[n]) {
+                double s0, s1, s2;
+                sum_parts(b.nptr, b.nslot, part64, n, s0, s1, s2);
+                r0 = (S)(bv[i] - (c.factor_K * s0 + mfm * y[i]));
+                r1 = (S)(bv[i + 1] - (c.factor_K * s1 + mfm * y[i + 1]));
+                r2 = (S)(bv[i + 2] - (c.factor_K * s2 + mfm * y[i + 2]));
+            }
+            r[i] = r0; r[i + 1] = r1; r[i + 2] = r2;
+            d[i] = 0; d[i + 1] = 0; d[i + 2] = 0;
+            acc += (double)r0 * (double)r0 + (double)r1 * (double)r1 + (double)r2 * (double)r2;
+        }
+        const double sum = bblock_sum(acc);
+        if (threadIdx.x == 0) cpart[ci] = sum;
+        if (arrive_last(ls.mcount + ch.mesh, c.nchunks)) {
+            const double total = mesh_partial_sum(cpart, c.chunk0, c.nchunks);
+            if (threadIdx.x == 0) {
+                StepScalars& s = b.st[ch.mesh];
+                s.delta_0 = total;
+                s.delta_new = total;
+                s.delta_old = total;
+                s.delta_target = c.rel_eps_sq * total;
+                s.abs_eps_sq = c.abs_eps_sq;
+                s.max_iter = c.max_iter;
+                s.k = 0;
+                s.status = (total != total) ? 3u : 0u;
+                s.alpha = 0.0;
+                s.beta = 0.0;
+                s.done = cg_cont(s) ? 0u : 1u;
+                if (s.done) finish_stats(s);
+            }
+        }
+        __syncthreads();
+    }
+    grid_tail(b, ls);
+}
+
+// d = S(r + beta d) written back ; q = S A d ; d.q ; last block of a mesh:
+// alpha (ILSS_CG.h:90-98). On refresh iterations r becomes S(b - A y).
+template <typename S>
+__global__ void k_node_q(BatchView<S> b, const S* __restrict__ part, S* __restrict__ d, S* __restrict__ q,
+                         const double* __restrict__ part64, const double* __restrict__ bv,
+                         const double* __restrict__ y, S* __restrict__ r, double* __restrict__ cpart, LoopSync ls)
+{
+    for (uint32_t ci = blockIdx.x; ci < b.nchunks; ci += gridDim.x) {
+        const ChunkMeta ch = b.chunks[ci];
+        if (!mesh_running(b, ch.mesh)) continue;
+        const MeshConsts& c = b.mc[ch.mesh];
+        const StepScalars& sm = b.st[ch.mesh];
+        const bool refresh = part64 && refresh_now(c, sm);
+        const S beta = (S)sm.beta;
+        const double mfm = c.mass * c.factor_M;
+        double acc = 0.0;
+        for (size_t n = ch.n0 + threadIdx.x; n < ch.n1; n += blockDim.x) {
+            const size_t i = 3 * n;
+            S q0 = 0, q1 = 0, q2 = 0, dn0 = 0, dn1 = 0, dn2 = 0;
+            if (!b.fixed[n]) {
+                dn0 = dir_update<S>(beta, d[i], r[i]);
+                dn1 = dir_update<S>(beta, d[i + 1], r[i + 1]);
+                dn2 = dir_update<S>(beta, d[i + 2], r[i + 2]);
+                double s0, s1, s2;
+                sum_parts(b.nptr, b.nslot, part, n, s0, s1, s2);
+                q0 = (S)(c.factor_K * s0 + mfm * (double)dn0);
+                q1 = (S)(c.factor_K * s1 + mfm * (double)dn1);
+                q2 = (S)(c.factor_K * s2 + mfm * (double)dn2);
+                if (refresh) {
+                    sum_parts(b.nptr, b.nslot, part64, n, s0, s1, s2);
+                    r[i] = (S)(bv[i] - (c.factor_K * s0 + mfm * y[i]));
+                    r[i + 1] = (S)(bv[i + 1] - (c.factor_K * s1 + mfm * y[i + 1]));
+                    r[i + 2] = (S)(bv[i + 2] - (c.factor_K * s2 + mfm * y[i + 2]));
+                }
+            }
+            d[i] = dn0; d[i + 1] = dn1; d[i + 2] = dn2;
+            q[i] = q0; q[i + 1] = q1; q[i + 2] = q2;
+            acc += (double)dn0 * (double)q0 + (double)dn1 * (double)q1 + (double)dn2 * (double)q2;
+        }
+        const double sum = bblock_sum(acc);
+        if (threadIdx.x == 0) cpart[ci] = sum;
+        if (arrive_last(ls.mcount + ch.mesh, c.nchunks)) {
+            const double total = mesh_partial_sum(cpart, c.chunk0, c.nchunks);
+            if (threadIdx.x == 0) {
+                StepScalars& s = b.st[ch.mesh];
+                s.dot_dq = total;
+                if (::fabs(total) < s.abs_eps_sq) {  // breakdown: leave before the update
+                    s.done = 1;
+                    finish_stats(s);
+                } else {
+                    s.alpha = s.delta_new / total;
+                }
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// y += alpha d (FP64) ; r -= alpha q (in S) ; |r|^2 ; last block of a mesh:
+// beta, k += 1 and the loop test (ILSS_CG.h:100-144).
+template <typename S>
+__global__ void k_node_update(BatchView<S> b, double* __restrict__ y, S* __restrict__ r, const S* __restrict__ d,
+                              const S* __restrict__ q, double* __restrict__ cpart, LoopSync ls)
+{
+    for (uint32_t ci = blockIdx.x; ci < b.nchunks; ci += gridDim.x) {
+        const ChunkMeta ch = b.chunks[ci];
+        if (!mesh_running(b, ch.mesh)) continue;
+        const MeshConsts& c = b.mc[ch.mesh];
+        const double alpha = b.st[ch.mesh].alpha;
+        const S na = (S)(-alpha);
+        double acc = 0.0;
+        for (size_t n = ch.n0 + threadIdx.x; n < ch.n1; n += blockDim.x) {
+#pragma unroll
+            for (int a = 0; a < 3; a++) {
+                const size_t i = 3 * n + a;
+                y[i] += alpha * (double)d[i];
+                const S ri = r[i] + na * q[i];
+                r[i] = ri;
+                acc += (double)ri * (double)ri;
+            }
+        }
+        const double sum = bblock_sum(acc);
+        if (threadIdx.x == 0) cpart[ci] = sum;
+        if (arrive_last(ls.mcount + ch.mesh, c.nchunks)) {
+            const double total = mesh_partial_sum(cpart, c.chunk0, c.nchunks);
+            if (threadIdx.x == 0) {
+                StepScalars& s = b.st[ch.mesh];
+                s.delta_old = s.delta_new;
+                s.delta_new = total;
+                s.beta = total / s.delta_old;
+                s.k += 1;
+                s.total_iters += 1;
+                if (total != total) s.status = 3u;
+                s.done = cg_cont(s) ? 0u : 1u;
+                if (s.done) finish_stats(s);
+            }
+        }
+        __syncthreads();
+    }
+    grid_tail(b, ls);
+}
+
+// v = y ; x += dt y
+template <typename S>
+__global__ void k_integrate(BatchView<S> b, double* __restrict__ x, double* __restrict__ v,
+                            const double* __restrict__ y)
+{
+    for (uint32_t ci = blockIdx.x; ci < b.nchunks; ci += gridDim.x) {
+        const ChunkMeta ch = b.chunks[ci];
+        if (!b.active[ch.mesh]) continue;
+        const double dt = b.mc[ch.mesh].dt;
+        for (size_t n = ch.n0 + threadIdx.x; n < ch.n1; n += blockDim.x) {
+#pragma unroll
+            for (int a = 0; a < 3; a++) {
+                const size_t i = 3 * n + a;
+                const double yi = y[i];
+                v[i] = yi;
+                x[i] = x[i] + dt * yi;
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// once-per-step bookkeeping
+
+template <typename S>
+__global__ void k_reset_counts(BatchView<S> b)
+{
+    for (uint32_t m = blockIdx.x * blockDim.x + threadIdx.x; m < b.M; m += gridDim.x * blockDim.x) {
+        if (b.active[m]) {
+            b.st[m].inverted = 0;
+            b.st[m].fp64_resolved = 0;
+        } else {
+            b.st[m].done = 1;
+        }
+    }
+}
+
+// Per-mesh energies: one block per mesh, fixed-order sum of its tile partials.
+template <typename S>
+__global__ void k_fin_energy(BatchView<S> b, int kind, const double* __restrict__ tpart)
+{
+    for (uint32_t m = blockIdx.x; m < b.M; m += gridDim.x) {
+        if (!b.active[m]) continue;
+        const MeshConsts& c = b.mc[m];
+        double acc = 0.0;
+        for (uint32_t i = threadIdx.x; i < c.ntiles; i += blockDim.x) acc += tpart[c.tile0 + i];
+        const double total = bblock_sum(acc);
+        if (threadIdx.x == 0) {
+            if (kind == FIN_ENERGY_E) b.st[m].elastic_energy = total;
+            else b.st[m].potential_energy = total;
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// launchers
+
+template <typename S>
+void BatchLaunch<S>::tile_spmv(const BatchView<S>& b, const S* d, const S* r, S* part,
+                               cudaGraphConditionalHandle if_refresh, int set_if, const unsigned* refresh_flag,
+                               cudaStream_t s)
+{
+    prof_begin(sizeof(S) == 8 ? "tile_spmv_fp64" : "tile_spmv_mixed", s);
+    k_tile_spmv<S><<<b.ntiles ? b.ntiles : 1, kTileElems, 0, s>>>(b, d, r, part, if_refresh, set_if, refresh_flag);
+    prof_end(sizeof(S) == 8 ? "tile_spmv_fp64" : "tile_spmv_mixed", s);
+    launch_counter()++;
+}
+
+template <typename S>
+void BatchLaunch<S>::tile_spmv_y64(const BatchView<S>& b, const double* y, double* part64, int refresh,
+                                   const unsigned* flag, cudaStream_t s)
+{
+    k_tile_spmv_y64<S><<<grid_tiles(b.ntiles), kTileElems, 0, s>>>(b, y, part64,
+                                                                   refresh ? SPMV_Y64_REFRESH : SPMV_Y64_ALL, flag);
+    launch_counter()++;
+}
+
+template <typename S>
+void BatchLaunch<S>::tile_force(const BatchView<S>& b, const double* x, double* part64, double* tile_energy,
+                                cudaStream_t s)
+{
+    k_tile_force<S><<<grid_tiles(b.ntiles), kTileElems, 0, s>>>(b, x, part64, tile_energy);
+    launch_counter()++;
+}
+
+template <typename S>
+void BatchLaunch<S>::tile_potential(const BatchView<S>& b, const double* x, double* tile_pe, cudaStream_t s)
+{
+    k_tile_potential<S><<<grid_tiles(b.ntiles), kTileElems, 0, s>>>(b, x, tile_pe);
+    launch_counter()++;
+}
+
+template <typename S>
+void BatchLaunch<S>::node_b(const BatchView<S>& b, const double* part64, const double* v, double* bv, double* y,
+                            cudaStream_t s)
+{
+    k_node_b<S><<<grid_chunks(b.nchunks), kNodeThreads, 0, s>>>(b, part64, v, bv, y);
+    launch_counter()++;
+}
+
+template <typename S>
+void BatchLaunch<S>::knc(const BatchView<S>& b, uint32_t K, const double* x, double* bv, double* y, cudaStream_t s)
+{
+    if (!K) return;
+    k_knc<S><<<(K + 255) / 256 < 1024 ? (K + 255) / 256 : 1024, 256, 0, s>>>(b, K, x, bv, y);
+    launch_counter()++;
+}
+
+template <typename S>
+void BatchLaunch<S>::node_residual(const BatchView<S>& b, const double* part64, const double* bv, const double* y,
+                                   S* r, S* d, double* cpart, const LoopSync& ls, cudaStream_t s)
+{
+    k_node_residual<S><<<grid_chunks(b.nchunks), kNodeThreads, 0, s>>>(b, part64, bv, y, r, d, cpart, ls);
+    launch_counter()++;
+}
+
+template <typename S>
+void BatchLaunch<S>::node_q(const BatchView<S>& b, const S* part, S* d, S* q, const double* part64,
+                            const double* bv, const double* y, S* r, double* cpart, const LoopSync& ls,
+                            cudaStream_t s)
+{
+    prof_begin(sizeof(S) == 8 ? "node_q_fp64" : "node_q_mixed", s);
+    k_node_q<S><<<grid_chunks(b.nchunks), kNodeThreads, 0, s>>>(b, part, d, q, part64, bv, y, r, cpart, ls);
+    prof_end(sizeof(S) == 8 ? "node_q_fp64" : "node_q_mixed", s);
+    launch_counter()++;
+}
+
+template <typename S>
+void BatchLaunch<S>::node_update(const BatchView<S>& b, double* y, S* r, const S* d, const S* q, double* cpart,
+                                 const LoopSync& ls, cudaStream_t s)
+{
+    k_node_update<S><<<grid_chunks(b.nchunks), kNodeThreads, 0, s>>>(b, y, r, d, q, cpart, ls);
+    launch_counter()++;
+}
+
+template <typename S>
+void BatchLaunch<S>::integrate(const BatchView<S>& b, double* x, double* v, const double* y, cudaStream_t s)
+{
+    k_integrate<S><<<grid_chunks(b.nchunks), kNodeThreads, 0, s>>>(b, x, v, y);
+    launch_counter()++;
+}
+
+template <typename S>
+void BatchLaunch<S>::fin_energy(const BatchView<S>& b, int kind, const double* tpart, cudaStream_t s)
+{
+    k_fin_energy<S><<<b.M < 4096 ? b.M : 4096, 256, 0, s>>>(b, kind, tpart);
+    launch_counter()++;
+}
+
+template <typename S>
+void BatchLaunch<S>::reset_counts(const BatchView<S>& b, cudaStream_t s)
+{
+    k_reset_counts<S><<<(b.M + 255) / 256, 256, 0, s>>>(b);
+    launch_counter()++;
+}
+
+uint32_t grid_tiles(uint32_t ntiles)
+{
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms <= 0) sms = 152;
+    }
+    const uint32_t cap = (uint32_t)sms * 8u;
+    return ntiles < cap ? (ntiles ? ntiles : 1) : cap;
+}
+
+uint32_t grid_chunks(uint32_t nchunks)
+{
+    const uint32_t cap = 152u * 8u;
+    return nchunks < cap ? (nchunks ? nchunks : 1) : cap;
+}
+
+template struct BatchLaunch<double>;
+template struct BatchLaunch<float>;
+
+}  // namespace femgb

@@ -1,0 +1,46 @@
+// batch_launch.h -- launchers of the batched kernels (batch_kernels.cu,
+// rotation.cu), used by the batch runtime (batch.cu).
+#pragma once
+#include "batch.cuh"
+
+namespace femgb {
+
+uint32_t grid_tiles(uint32_t ntiles);
+uint32_t grid_chunks(uint32_t nchunks);
+
+// Arrival counters and graph handle of the fused CG finalisation.
+struct LoopSync {
+    unsigned* mcount;        // [M] per-mesh chunk arrivals
+    unsigned* gcount;        // grid arrivals
+    unsigned* refresh_flag;  // raised when a mesh refreshes its residual next iteration
+    unsigned* body_runs;     // CG-loop body executions (launch accounting)
+    cudaGraphConditionalHandle cond;
+    int set_cond;
+};
+
+template <typename S>
+struct BatchLaunch {
+    static void begin_eval(const BatchView<S>& b, const double* x, cudaStream_t s);  // rotation.cu
+    static void reset_counts(const BatchView<S>& b, cudaStream_t s);
+    static void tile_spmv(const BatchView<S>& b, const S* d, const S* r, S* part,
+                          cudaGraphConditionalHandle if_refresh, int set_if, const unsigned* refresh_flag,
+                          cudaStream_t s);
+    static void tile_spmv_y64(const BatchView<S>& b, const double* y, double* part64, int refresh,
+                              const unsigned* flag, cudaStream_t s);
+    static void tile_force(const BatchView<S>& b, const double* x, double* part64, double* tile_energy,
+                           cudaStream_t s);
+    static void tile_potential(const BatchView<S>& b, const double* x, double* tile_pe, cudaStream_t s);
+    static void node_b(const BatchView<S>& b, const double* part64, const double* v, double* bv, double* y,
+                       cudaStream_t s);
+    static void knc(const BatchView<S>& b, uint32_t K, const double* x, double* bv, double* y, cudaStream_t s);
+    static void node_residual(const BatchView<S>& b, const double* part64, const double* bv, const double* y, S* r,
+                              S* d, double* cpart, const LoopSync& ls, cudaStream_t s);
+    static void node_q(const BatchView<S>& b, const S* part, S* d, S* q, const double* part64,
+                       const double* bv, const double* y, S* r, double* cpart, const LoopSync& ls, cudaStream_t s);
+    static void node_update(const BatchView<S>& b, double* y, S* r, const S* d, const S* q, double* cpart,
+                            const LoopSync& ls, cudaStream_t s);
+    static void integrate(const BatchView<S>& b, double* x, double* v, const double* y, cudaStream_t s);
+    static void fin_energy(const BatchView<S>& b, int kind, const double* tpart, cudaStream_t s);
+};
+
+}  // namespace femgb

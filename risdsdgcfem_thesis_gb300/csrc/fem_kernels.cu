@@ -16,6 +16,7 @@
 // partials in index order.
 #include "fem_device.cuh"
 #include "msvd.cuh"
+#include "elem_math.cuh"
 
 #include <map>
 #include <mutex>
@@ -159,71 +160,6 @@ __device__ __forceinline__ void load_elem(const MeshView<S>& m, uint32_t e, S* R
     k1 = m.mat[e];
     knu = m.mat[T + e];
     k2 = m.mat[2 * T + e];
-}
-
-// Local-frame stress product: given H (displacement gradient in the element
-// frame), returns P = sigma(H) * Dinv^T (columns = forces on nodes 1..3 in
-// the element frame, V folded into the material scalars) and eps:sigma.
-template <typename S>
-__device__ __forceinline__ void stress_forces(const S* H, const S* Di, S k1, S knu, S k2, S* P, S& eps_sig)
-{
-    const S exx = H[0], eyy = H[4], ezz = H[8];
-    const S gxy = H[1] + H[3], gyz = H[5] + H[7], gzx = H[2] + H[6];
-    const S sxx = k1 * exx + knu * (eyy + ezz);
-    const S syy = k1 * eyy + knu * (exx + ezz);
-    const S szz = k1 * ezz + knu * (exx + eyy);
-    const S txy = k2 * gxy, tyz = k2 * gyz, tzx = k2 * gzx;
-    eps_sig = sxx * exx + syy * eyy + szz * ezz + txy * gxy + tyz * gyz + tzx * gzx;
-    const S Sg[9] = {sxx, txy, tzx, txy, syy, tyz, tzx, tyz, szz};
-#pragma unroll
-    for (int a = 0; a < 3; a++)
-#pragma unroll
-        for (int i = 0; i < 3; i++)
-            P[3 * a + i] = Sg[3 * a] * Di[3 * i] + Sg[3 * a + 1] * Di[3 * i + 1] + Sg[3 * a + 2] * Di[3 * i + 2];
-}
-
-// Writes R * P (world frame) to out[4][3]: node 0 gets minus the sum.
-template <typename S>
-__device__ __forceinline__ void rotate_out(const S* R, const S* P, S* out)
-{
-    S Pw[9];
-#pragma unroll
-    for (int a = 0; a < 3; a++)
-#pragma unroll
-        for (int i = 0; i < 3; i++) Pw[3 * a + i] = R[3 * a] * P[i] + R[3 * a + 1] * P[3 + i] + R[3 * a + 2] * P[6 + i];
-#pragma unroll
-    for (int i = 0; i < 3; i++) {
-        out[3 * (i + 1) + 0] = Pw[i];
-        out[3 * (i + 1) + 1] = Pw[3 + i];
-        out[3 * (i + 1) + 2] = Pw[6 + i];
-    }
-    out[0] = -(Pw[0] + Pw[1] + Pw[2]);
-    out[1] = -(Pw[3] + Pw[4] + Pw[5]);
-    out[2] = -(Pw[6] + Pw[7] + Pw[8]);
-}
-
-// Product R K0 R^T d for one element (world-frame nodal vectors d[4][3]).
-template <typename S>
-__device__ __forceinline__ void elem_RKRt(const S* R, const S* Di, S k1, S knu, S k2, const S* d, S* out)
-{
-    S D[9];  // columns d1-d0, d2-d0, d3-d0 ; D[3a+j]
-#pragma unroll
-    for (int a = 0; a < 3; a++)
-#pragma unroll
-        for (int j = 0; j < 3; j++) D[3 * a + j] = d[3 * (j + 1) + a] - d[a];
-    S Hw[9];
-#pragma unroll
-    for (int a = 0; a < 3; a++)
-#pragma unroll
-        for (int b = 0; b < 3; b++) Hw[3 * a + b] = D[3 * a] * Di[b] + D[3 * a + 1] * Di[3 + b] + D[3 * a + 2] * Di[6 + b];
-    S H[9];  // R^T Hw
-#pragma unroll
-    for (int a = 0; a < 3; a++)
-#pragma unroll
-        for (int b = 0; b < 3; b++) H[3 * a + b] = R[a] * Hw[b] + R[3 + a] * Hw[3 + b] + R[6 + a] * Hw[6 + b];
-    S P[9], es;
-    stress_forces(H, Di, k1, knu, k2, P, es);
-    rotate_out(R, P, out);
 }
 
 // ---- element kernels ----

@@ -6,6 +6,7 @@
 // then evaluated with the reference's rounding sequence (no fused
 // multiply-adds), which makes the GPU rotations equal to the reference's on
 // the same positions.
+#include "batch_launch.h"
 #include "fem_device.cuh"
 #include "msvd.cuh"
 
@@ -50,5 +51,79 @@ void launch_begin_eval_fp64(const MeshView<double>& m, const double* x, double* 
     k_begin_eval_fp64<<<grid_for(m.T), kBlock, 0, s>>>(m, x, F_out, st);
     launch_counter()++;
 }
+
+// ---------------------------------------------------------------------------
+// Batched BeginEvaluation: block per element tile (one mesh per tile). F and
+// det F in FP64 from FP64 positions and Dm^-1. The FP64 path takes the FP64
+// rotation; the mixed path takes the FP32 rotation unless det F <= the
+// mesh's threshold, where F is re-solved in FP64. Per-mesh counts of
+// inverted elements and FP64 re-solves are added with integer atomics (one
+// per tile), so they do not depend on scheduling.
+template <typename S>
+__global__ void k_begin_eval_batch(BatchView<S> b, const double* __restrict__ x)
+{
+    __shared__ unsigned s_inv, s_res;
+    for (uint32_t t = blockIdx.x; t < b.ntiles; t += gridDim.x) {
+        const TileMeta tm = b.tiles[t];
+        if (!b.active[tm.mesh]) continue;
+        if (threadIdx.x == 0) { s_inv = 0; s_res = 0; }
+        __syncthreads();
+        if (threadIdx.x < tm.ne) {
+            const size_t e = tm.e0 + threadIdx.x;
+            const size_t T = b.Ttot;
+            const int4 g = b.gtets[e];
+            const int ids[4] = {g.x, g.y, g.z, g.w};
+            V3<double> xs[4];
+#pragma unroll
+            for (int i = 0; i < 4; i++)
+                xs[i] = mk<double>(x[3 * (size_t)ids[i]], x[3 * (size_t)ids[i] + 1], x[3 * (size_t)ids[i] + 2]);
+            double Di[9];
+#pragma unroll
+            for (int c = 0; c < 9; c++) Di[c] = b.Dinv64[c * T + e];
+            double F[9], detF;
+            deformation_gradient(xs, Di, F, detF);
+            S Rs[9];
+            if (sizeof(S) == sizeof(double)) {
+                double R[9];
+                msvd_rotation(F, R);
+#pragma unroll
+                for (int c = 0; c < 9; c++) Rs[c] = (S)R[c];
+            } else if (detF > b.mc[tm.mesh].degenerate_det_F) {
+                float Ff[9], Rf[9];
+#pragma unroll
+                for (int c = 0; c < 9; c++) Ff[c] = (float)F[c];
+                msvd_rotation(Ff, Rf);
+#pragma unroll
+                for (int c = 0; c < 9; c++) Rs[c] = (S)Rf[c];
+            } else {
+                double R[9];
+                msvd_rotation(F, R);
+#pragma unroll
+                for (int c = 0; c < 9; c++) Rs[c] = (S)R[c];
+                atomicAdd(&s_res, 1u);
+            }
+#pragma unroll
+            for (int c = 0; c < 9; c++) b.R[c * T + e] = Rs[c];
+            b.detF[e] = detF;
+            if (detF <= 0.0) atomicAdd(&s_inv, 1u);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            if (s_inv) atomicAdd(&b.st[tm.mesh].inverted, s_inv);
+            if (s_res) atomicAdd(&b.st[tm.mesh].fp64_resolved, s_res);
+        }
+        __syncthreads();
+    }
+}
+
+template <typename S>
+void BatchLaunch<S>::begin_eval(const BatchView<S>& b, const double* x, cudaStream_t s)
+{
+    k_begin_eval_batch<S><<<grid_tiles(b.ntiles), kTileElems, 0, s>>>(b, x);
+    launch_counter()++;
+}
+
+template void BatchLaunch<double>::begin_eval(const BatchView<double>&, const double*, cudaStream_t);
+template void BatchLaunch<float>::begin_eval(const BatchView<float>&, const double*, cudaStream_t);
 
 }  // namespace femgb

@@ -24,9 +24,12 @@
 
 using namespace femgb;
 
-namespace {
-
+namespace femgb {
 thread_local std::string g_err;
+void set_last_error(const char* msg) { g_err = msg; }
+}  // namespace femgb
+
+namespace {
 
 int fail(int code, const char* fmt, ...) __attribute__((format(printf, 2, 3)));
 int fail(int code, const char* fmt, ...)

@@ -1,0 +1,140 @@
+"""Tiled, batched step on the GPU (FP64 and mixed) through the C ABI.
+
+Tolerances: FP64 as the single-solid path (rel-L2 <= max(1e-10, 10 x the
+oracle's own 1e-15-perturbation noise floor), iterations within
+max(1, 2 x spread + 1)); mixed precision rel-L2 <= 1e-5 against the FP64
+oracle; a solid alone and inside a batch: bit-identical.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from risdsdgcfem_thesis_gb300 import scenes
+from parity_util import oracle_run, rel
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def _damped_driven():
+    rng = np.random.default_rng(5)
+    sc = scenes.random_block(rng, dims=(5, 3, 4))
+    T = sc.num_tets
+    sc.young_per_elem = np.exp(rng.uniform(np.log(5e4), np.log(5e5), T))
+    sc.poisson_per_elem = rng.uniform(0.25, 0.45, T)
+    sc.damping_ratio = 1.0
+    sc.init_vel = rng.standard_normal(sc.rest.shape) * 0.1
+    base = sc.knc_targets.copy()
+    sc.knc_schedule = lambda k: base + np.array([0.0, 0.0, 0.001 * (k + 1)])
+    return sc
+
+
+def test_fp64_batch_of_one_matches_reference_cantilever(fem_lib):
+    g = np.load(os.path.join(GOLDEN, "cantilever_160.npz"))
+    sc = scenes.cantilever_160()
+    b = fem_lib.Batch([sc], precision=fem_lib.FEM_PRECISION_FP64)
+    for k in range(sc.steps):
+        b.step(1)
+        st = b.stats(0)
+        assert abs(st["cg_iterations"] - int(g["iters"][k])) <= 1, (k, st["cg_iterations"], g["iters"][k])
+    x, v = b.state(0)
+    assert rel(x, g["x"][-1]) <= 1e-10 and rel(v, g["v"][-1]) <= 1e-10, (rel(x, g["x"][-1]), rel(v, g["v"][-1]))
+    assert abs(st["elastic_energy"] - g["elastic_energy"][-1]) <= 1e-8 * abs(g["elastic_energy"][-1])
+
+
+def test_fp64_batch_matches_oracle_per_mesh(fem_lib, oracle):
+    scs = [_damped_driven(), scenes.large_block(n=8), scenes.compressed_cube(n=5, steps=20, ratio=0.3),
+           scenes.cantilever_160()]
+    steps = 12
+    b = fem_lib.Batch(scs, precision=fem_lib.FEM_PRECISION_FP64)
+    its = [[] for _ in scs]
+    for _ in range(steps):
+        b.step(1)
+        for i in range(len(scs)):
+            its[i].append(b.stats(i)["cg_iterations"])
+    for i, sc in enumerate(scs):
+        ref = oracle_run(oracle, sc, steps)
+        x, v = b.state(i)
+        ex, ev = rel(x, ref["x"]), rel(v, ref["v"])
+        assert ex <= max(1e-10, 10 * ref["noise_x"]) and ev <= max(1e-10, 10 * ref["noise_v"]), (i, ex, ev, ref)
+        worst = max(abs(a - c) for a, c in zip(its[i], ref["iters"]))
+        assert worst <= max(1, 2 * ref["spread"] + 1), (i, worst, ref["spread"])
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_alone_and_in_the_mix_are_identical(fem_lib, precision):
+    p = fem_lib.FEM_PRECISION_FP64 if precision == "fp64" else fem_lib.FEM_PRECISION_MIXED
+    rng = np.random.default_rng(21)
+    target = scenes.random_block(rng, dims=(7, 5, 6), idx=0)
+    others = [scenes.random_block(rng, idx=i) for i in range(1, 7)]
+    alone = fem_lib.Batch([target], precision=p)
+    mix = fem_lib.Batch(others[:3] + [target] + others[3:], precision=p)
+    for _ in range(6):
+        alone.step(1)
+        mix.step(1)
+        assert alone.stats(0)["cg_iterations"] == mix.stats(3)["cg_iterations"]
+    xa, va = alone.state(0)
+    xm, vm = mix.state(3)
+    assert np.array_equal(xa, xm) and np.array_equal(va, vm)
+
+
+def test_mixed_precision_error_vs_fp64_oracle(fem_lib, oracle):
+    """Mixed path (FP32 products, FP64 reductions and refresh) against the
+    FP64 oracle, tolerance 1e-5: positions by rel-L2; velocities by
+    ||v - v_oracle|| / max over the run of ||v_oracle|| (an oscillating body
+    passes through v ~ 0, where a plain relative norm divides by ~0)."""
+    for sc, steps in ((scenes.cantilever_160(), 120), (scenes.large_block(n=10), 20), (_damped_driven(), 20)):
+        b = fem_lib.Batch([sc], precision=fem_lib.FEM_PRECISION_MIXED)
+        o = oracle.Solid(sc, "port")
+        vscale = 0.0
+        for _ in range(steps):
+            b.step(1)
+            o.step()
+            vscale = max(vscale, float(np.linalg.norm(o.state()[1])))
+        x, v = b.state(0)
+        xo, vo = o.state()
+        ex = rel(x, xo)
+        ev = float(np.linalg.norm(v - vo)) / vscale
+        assert ex <= 1e-5 and ev <= 1e-5, (sc.name, ex, ev)
+
+
+def test_active_mask_leaves_inactive_meshes_untouched(fem_lib):
+    rng = np.random.default_rng(3)
+    scs = [scenes.random_block(rng, idx=i, dims=(4, 4, 4)) for i in range(4)]
+    b = fem_lib.Batch(scs, precision=fem_lib.FEM_PRECISION_MIXED)
+    b.step(1)
+    before = [b.state(i) for i in range(4)]
+    b.set_active(np.array([1, 0, 1, 0], np.uint8))
+    b.step(2)
+    after = [b.state(i) for i in range(4)]
+    for i in (1, 3):
+        assert np.array_equal(before[i][0], after[i][0]) and np.array_equal(before[i][1], after[i][1])
+    for i in (0, 2):
+        assert not np.array_equal(before[i][0], after[i][0])
+
+
+def test_graph_and_host_loop_agree(fem_lib):
+    rng = np.random.default_rng(8)
+    scs = [scenes.random_block(rng, idx=i) for i in range(3)]
+    a = fem_lib.Batch(scs, precision=fem_lib.FEM_PRECISION_MIXED, use_graph=True)
+    b = fem_lib.Batch(scs, precision=fem_lib.FEM_PRECISION_MIXED, use_graph=False)
+    a.step(3)
+    b.step(3)
+    for i in range(3):
+        xa, va = a.state(i)
+        xb, vb = b.state(i)
+        assert np.array_equal(xa, xb) and np.array_equal(va, vb)
+        assert a.stats(i)["cg_iterations"] == b.stats(i)["cg_iterations"]
+
+
+def test_compression_counts_fp64_resolves(fem_lib):
+    sc = scenes.compressed_cube(n=6, steps=20, ratio=0.2)
+    b = fem_lib.Batch([sc], precision=fem_lib.FEM_PRECISION_MIXED)
+    resolved = 0
+    for _ in range(20):
+        b.step(1)
+        st = b.stats(0)
+        resolved = max(resolved, st["fp64_resolved"])
+        assert st["status"] == 0
+    assert resolved > 0
