@@ -1,15 +1,23 @@
 #!/usr/bin/env python3
-"""Benchmark of the corotational linear-tet FEM implicit-Euler step.
+"""Benchmark of the corotational linear-tet FEM implicit-Euler step on GB300.
 
 Metric: tet.CG-iter/s -- one tet taking part in one executed CG iteration,
-summed over the timed steps, divided by the device time of those steps.
-A "step" is one FixedStep of the workload (rotation, elastic force, right-hand
-side, CG solve to tolerance, integration, energies), inputs resident in HBM.
+summed over the timed steps and divided by their time. A "step" is one
+FixedStep of every solid of the workload (rotations, elastic force,
+right-hand side, CG solve to each solid's own tolerance, integration,
+energies), with the state resident in HBM.
 
-  python bench.py [--steps K] [--warmup W] [--workload block60_fp64]
-  python bench.py --impl reference ...   # the reference's CPU path, same metric
+Default workload: 1024 independent uneven meshes (a x b x c cubes x 5 tets,
+a,b,c uniform in [4,30]) stepped together by the batched mixed-precision path
+(FP32 products, FP64 dot products and residual refresh), one CUDA graph per
+step. The plain FP64 drop-in path on the single 60^3 block (1.08M tets) is
+timed beside it as the "plain GPU" comparator.
 
-Prints one JSON line (rank 0).
+  python bench.py [--steps K] [--warmup W] [--workload batch1024|block60_mixed|block60_fp64]
+  python bench.py --impl reference ...   # the reference's CPU path on the host cores
+
+Prints one JSON line (rank 0). Under torchrun every rank steps its own batch
+(seeded by rank): replicas only, no collective on the data path.
 """
 from __future__ import annotations
 
@@ -31,21 +39,35 @@ sys.path.insert(0, ROOT)
 METRIC = "tet·CG-iter/s & p99 step latency: batched/served vs plain GPU, ≤1e-5 rel err"
 UNIT = "tet·CG-iter/s"
 L2_BYTES = 129 * 1024 * 1024
+# algorithmic bytes of one element product (16 B of node ids + 20 element
+# scalars R, Dm^-1, V lambda, V mu) and per node of the direction read once
+ALG_ELEM = {"mixed": 16 + 20 * 4, "fp64": 16 + 20 * 8}
+ALG_NODE = {"mixed": 3 * 4, "fp64": 3 * 8}
 
 
-def workload_scene(name: str):
+# ---------------------------------------------------------------- workloads
+def workload(name: str, rank: int = 0):
     from risdsdgcfem_thesis_gb300 import scenes
+    if name == "batch1024":
+        return scenes.batch_scenes(1024, seed=rank), "mixed"
+    if name == "batch128":
+        return scenes.batch_scenes(128, seed=rank), "mixed"
+    if name == "block60_mixed":
+        return [scenes.large_block(n=60, seed=rank)], "mixed"
     if name == "block60_fp64":
-        return scenes.large_block(n=60)
-    if name == "block20_fp64":
-        return scenes.large_block(n=20)
+        return [scenes.large_block(n=60, seed=rank)], "fp64"
     raise SystemExit(f"unknown workload {name}")
 
 
-def workload_desc(name, sc):
-    return (f"{sc.name}: {sc.num_tets} tets, {sc.num_nodes} nodes, h=0.01 m, jitter 0.1h, per-element E log-U"
-            f"[5e4,5e5] nu U[0.25,0.45], bottom fixed, top v0=(1,0,0), dt=1/60, CG rel 1e-6 abs 0, "
-            f"max {sc.max_iter}; plain FP64")
+def describe(name, scs, precision):
+    T = sum(s.num_tets for s in scs)
+    N = sum(s.num_nodes for s in scs)
+    if name.startswith("batch"):
+        return (f"{len(scs)} independent meshes, a x b x c cubes x 5 tets with a,b,c ~ U{{4..30}} (h=0.01 m, jitter "
+                f"0.1h), per-mesh E log-U[1e4,1e6] nu U[0.2,0.45], one random face fixed, gravity -9.81 z, dt=1/60, "
+                f"CG rel 1e-6 abs 0 max 500 per mesh; {T} tets, {N} nodes total; {precision}")
+    return (f"{scs[0].name}: {T} tets, {N} nodes, h=0.01 m, jitter 0.1h, per-element E log-U[5e4,5e5] nu "
+            f"U[0.25,0.45], bottom fixed, top v0=(1,0,0), dt=1/60, CG rel 1e-6 abs 0 max 500; {precision}")
 
 
 # ---------------------------------------------------------------- clocks
@@ -112,9 +134,9 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def profiled_traffic(kernel: str, workload: str):
+def profiled_traffic(kernel: str, workload_name: str):
     """Per-launch DRAM bytes of `kernel` from the committed ncu summary, if any."""
-    path = os.path.join(ROOT, "profiles", f"{kernel}_{workload}.md")
+    path = os.path.join(ROOT, "profiles", f"{kernel}_{workload_name}.md")
     if not os.path.exists(path):
         return None
     for line in open(path):
@@ -127,74 +149,82 @@ def profiled_traffic(kernel: str, workload: str):
 
 
 def dist_info():
-    ws = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    return ws, rank
+    return int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0"))
 
 
-def dist_init(ws):
+def aggregate(values, ws):
+    """(value, "max"|"sum") pairs reduced over ranks under torchrun (NCCL)."""
     if ws <= 1:
-        return None
+        return [v for v, _ in values]
+    import torch
     import torch.distributed as dist
-    backend = "nccl"
-    dist.init_process_group(backend=backend)
-    return dist
-
-
-def reduce_max(dist, x):
-    if dist is None:
-        return x
-    import torch
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    return float(t.item())
-
-
-def reduce_sum(dist, x):
-    if dist is None:
-        return x
-    import torch
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
-    dist.all_reduce(t, op=dist.ReduceOp.SUM)
-    return float(t.item())
+    out = []
+    for v, op in values:
+        t = torch.tensor([v], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX if op == "max" else dist.ReduceOp.SUM)
+        out.append(float(t.item()))
+    return out
 
 
 # ---------------------------------------------------------------- CPU legs
 class CpuSampler:
-    """Times the CG iterations of the first FixedStep of a workload on the
-    oracle restatement (bit-exact with the reference's FP64 translation units),
-    single-threaded like the reference path. One sample = the step with the CG
-    capped at `cap` iterations minus the same step capped at 0 iterations, so
-    the figure is the CG loop's throughput alone (the per-step fixed work --
-    rotations, elastic force, right-hand side -- is left out, which favours
-    the CPU)."""
+    """The reference's CPU path (the oracle restatement, bit-exact with the
+    reference's FP64 translation units) on the workload's meshes, one mesh per
+    thread over `threads` host threads (the reference steps solids serially,
+    one thread each). A sample times the CG iterations of each mesh's first
+    FixedStep: all meshes stepped with the CG capped at `cap` iterations,
+    minus the same with the cap at 0 (the per-step fixed work is left out,
+    which favours the CPU)."""
 
-    def __init__(self, sc):
+    def __init__(self, scs, threads):
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
         import pyoracle
         pyoracle.build(reference=False)
-        self.sc = sc
-        self.solid = pyoracle.Solid(sc, "port")
+        self.scs = scs
+        self.threads = max(1, threads)
+        self.solids = [pyoracle.Solid(sc, "port") for sc in scs]
 
-    def _timed_step(self, cap):
-        self.solid.reset()
-        self.solid.set_solver(self.sc.rel_eps, self.sc.abs_eps, cap)
+    def _region(self, cap):
+        from concurrent.futures import ThreadPoolExecutor
+        iters = [0] * len(self.solids)
+
+        def run(i):
+            s = self.solids[i]
+            s.reset()
+            s.set_solver(self.scs[i].rel_eps, self.scs[i].abs_eps, cap)
+            iters[i] = s.step()["iters"]
+
         t0 = time.perf_counter()
-        st = self.solid.step()
-        return st["iters"], time.perf_counter() - t0
+        with ThreadPoolExecutor(self.threads) as ex:
+            list(ex.map(run, range(len(self.solids))))
+        return time.perf_counter() - t0, iters
 
     def sample(self, cap):
-        _, t0 = self._timed_step(0)
-        it, tc = self._timed_step(cap)
-        return float(self.sc.num_tets) * it, max(tc - t0, 1e-9)
+        w0, _ = self._region(0)
+        wc, iters = self._region(cap)
+        units = float(sum(sc.num_tets * it for sc, it in zip(self.scs, iters)))
+        return units, max(wc - w0, 1e-9)
+
+
+def cpu_sample_set(scs, max_tets):
+    """A bounded subset of the workload's meshes for the CPU timings."""
+    out, tot = [], 0
+    for sc in scs:
+        if tot + sc.num_tets > max_tets and out:
+            break
+        out.append(sc)
+        tot += sc.num_tets
+    return out
 
 
 def run_reference(args):
     ws, rank = dist_info()
     if rank != 0:
         return 0
-    sc = workload_scene(args.workload)
-    sampler = CpuSampler(sc)
+    scs, precision = workload(args.workload)
+    sample = cpu_sample_set(scs, 1_500_000)
+    threads = (os.cpu_count() or 1) if len(sample) > 1 else 1
+    sampler = CpuSampler(sample, threads)
     cap = 8
     total_units, total_s = 0.0, 0.0
     for i in range(args.warmup + args.steps):
@@ -203,147 +233,206 @@ def run_reference(args):
             total_units += u
             total_s += s
     value = total_units / total_s
+    cores = sampler.threads
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * total_s / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": workload_desc(args.workload, sc)},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": "port",
-                         "sample": f"each step = the CG iterations of the first FixedStep of {sc.name} "
-                                   f"(step capped at {cap} iterations minus the step capped at 0), one thread "
-                                   "(the reference path is serial per mesh); oracle restatement, bit-exact with "
-                                   "the reference's FP64 translation units"},
+        "config": {"workload": describe(args.workload, scs, "reference CPU path, FP64")},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"each step = the CG iterations ({cap} per mesh) of the first FixedStep of "
+                                   f"{len(sample)} of the workload's meshes ({sum(s.num_tets for s in sample)} tets), "
+                                   f"one mesh per thread on {cores} threads; oracle restatement, bit-exact with the "
+                                   "reference's FP64 translation units"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
     return 0
 
 
-# ---------------------------------------------------------------- GPU leg
+# ---------------------------------------------------------------- GPU legs
+def time_batch(batch, steps, stream_ptr):
+    """Device time of `steps` steps, per step, plus per-mesh CG iterations."""
+    import torch
+    from risdsdgcfem_thesis_gb300 import capi
+    lib = batch.lib
+    M = len(batch.scenes)
+    before = [batch.stats(i)["total_cg_iterations"] for i in range(M)]
+    stream = torch.cuda.ExternalStream(stream_ptr)
+    evs = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
+    torch.cuda.synchronize()
+    evs[0].record(stream)
+    for k in range(steps):
+        capi.check(lib.fem_batch_step_async(batch.h, 1))
+        evs[k + 1].record(stream)
+    torch.cuda.synchronize()
+    capi.check(lib.fem_batch_synchronize(batch.h))
+    step_ms = [evs[k].elapsed_time(evs[k + 1]) for k in range(steps)]
+    iters = [batch.stats(i)["total_cg_iterations"] - before[i] for i in range(M)]
+    return step_ms, iters
+
+
+def plain_fp64_comparator(steps=3):
+    """The FP64 drop-in path (fem_solid) on the 60^3 block, device time."""
+    import torch
+    from risdsdgcfem_thesis_gb300 import capi, scenes
+    sc = scenes.large_block(n=60)
+    s = capi.Solid(sc, compute_energy=True)
+    s.step(1)
+    lib = capi.load()
+    st = capi.FemStepStats()
+    capi.check(lib.fem_solid_synchronize(s.h, C.byref(st)))
+    it0 = st.total_cg_iterations
+    stream = torch.cuda.ExternalStream(s.stream())
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    capi.check(lib.fem_solid_step_async(s.h, steps))
+    e1.record(stream)
+    torch.cuda.synchronize()
+    capi.check(lib.fem_solid_synchronize(s.h, C.byref(st)))
+    ms = e0.elapsed_time(e1)
+    units = float(sc.num_tets) * (st.total_cg_iterations - it0)
+    s.close()
+    return {"value": units / (ms * 1e-3), "unit": UNIT, "steps": steps,
+            "workload": f"{sc.name} ({sc.num_tets} tets), plain FP64 drop-in path (fem_solid_step)",
+            "ms_per_step": ms / steps}
+
+
 def run_ours(args):
     import torch
     from risdsdgcfem_thesis_gb300 import capi
     ws, rank = dist_info()
     if ws > 1:
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
-    dist = dist_init(ws)
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
     capi.load()
-    sc = workload_scene(args.workload)
-    solid = capi.Solid(sc, compute_energy=True)
-    stream = torch.cuda.ExternalStream(solid.stream())
-    for _ in range(args.warmup):
-        solid.step(1)
+    scs, precision = workload(args.workload, rank)
+    prec = capi.FEM_PRECISION_MIXED if precision == "mixed" else capi.FEM_PRECISION_FP64
+    t0 = time.perf_counter()
+    batch = capi.Batch(scs, precision=prec, compute_energy=True, use_graph=not args.no_graph)
+    setup_s = time.perf_counter() - t0
+    info = batch.info()
+    stream_ptr = batch.stream()
+    batch.step(args.warmup)
 
     # ---- device-resident timed region ----
-    lib = capi.load()
-    stats = capi.FemStepStats()
-    capi.check(lib.fem_solid_synchronize(solid.h, C.byref(stats)))
-    iters_before = stats.total_cg_iterations
-    launches_before = capi.kernel_launches()
     clocks = ClockSampler(torch.cuda.current_device())
     clocks.start()
-    capi.profile_enable(True)
-    if dist is not None:
-        dist.barrier()
-    torch.cuda.synchronize()
-    evs = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
-    evs[0].record(stream)
-    for k in range(args.steps):
-        capi.check(lib.fem_solid_step_async(solid.h, 1))
-        evs[k + 1].record(stream)
-    torch.cuda.synchronize()
-    step_ms = [evs[k].elapsed_time(evs[k + 1]) for k in range(args.steps)]
-    capi.profile_enable(False)
+    batch.reset_launch_count()
+    if ws > 1:
+        torch.distributed.barrier()
+    step_ms, iters = time_batch(batch, args.steps, stream_ptr)
     clk = clocks.stop()
-    capi.check(lib.fem_solid_synchronize(solid.h, C.byref(stats)))
-    launches = capi.kernel_launches() - launches_before
-    iters = stats.total_cg_iterations - iters_before
-    elapsed_ms = sum(step_ms)
-    elapsed_ms = reduce_max(dist, elapsed_ms)
-    units = reduce_sum(dist, float(sc.num_tets) * iters)
+    launches = batch.kernel_launches(args.steps) if not args.no_graph else None
+    units = float(sum(sc.num_tets * it for sc, it in zip(scs, iters)))
+    elapsed_ms, units = aggregate([(sum(step_ms), "max"), (units, "sum")], ws)
     value = units / (elapsed_ms * 1e-3)
 
-    # dominant kernel roofline (events around each launch on the lib stream)
-    spmv_ms, spmv_n = capi.profile_read("elem_spmv_fp64")
-    N, T = sc.num_nodes, sc.num_tets
-    alg_bytes = T * (16 + 20 * 8) + N * 3 * 8
-    avg_s = (spmv_ms / max(spmv_n, 1)) * 1e-3
-    achieved = alg_bytes / avg_s / 1e9 if avg_s > 0 else 0.0
+    # ---- dominant kernel: tile SpMV, CUDA events around each launch on its
+    # stream, over one step run launch by launch (same kernels, host loop) ----
+    kname = "tile_spmv_mixed" if precision == "mixed" else "tile_spmv_fp64"
+    capi.check(batch.lib.fem_batch_use_graph(batch.h, 0))
+    before = [batch.stats(i)["total_cg_iterations"] for i in range(len(scs))]
+    capi.profile_enable(True)
+    batch.step(1)
+    capi.profile_enable(False)
+    prof_iters = [batch.stats(i)["total_cg_iterations"] - before[i] for i in range(len(scs))]
+    capi.check(batch.lib.fem_batch_use_graph(batch.h, 0 if args.no_graph else 1))
+    k_ms, k_n = capi.profile_read(kname)
+    alg = sum(it * (ALG_ELEM[precision] * sc.num_tets + ALG_NODE[precision] * sc.num_nodes)
+              for sc, it in zip(scs, prof_iters))
+    avg_launch_s = (k_ms * 1e-3) / max(k_n, 1)
+    alg_per_launch = alg / max(k_n, 1)
+    achieved = alg_per_launch / avg_launch_s / 1e9 if avg_launch_s > 0 else 0.0
     peak, peak_kind = measured_peaks()
-    traffic = profiled_traffic("elem_spmv_fp64", args.workload)
 
-    # ---- end-to-end through the C ABI with host (pinned) buffers ----
-    n3 = 3 * N
+    # ---- end to end: host (pinned) buffers through the C ABI every step ----
+    n3 = 3 * info["nodes"]
     hx = torch.empty(n3, dtype=torch.float64, pin_memory=True)
     hv = torch.empty(n3, dtype=torch.float64, pin_memory=True)
-    capi.check(lib.fem_solid_get_state(solid.h, C.cast(hx.data_ptr(), C.POINTER(C.c_double)),
-                                       C.cast(hv.data_ptr(), C.POINTER(C.c_double))))
-    e2e_steps = max(1, min(args.steps, 10))
-    capi.check(lib.fem_solid_synchronize(solid.h, C.byref(stats)))
-    it0 = stats.total_cg_iterations
+    px = C.cast(hx.data_ptr(), C.POINTER(C.c_double))
+    pv = C.cast(hv.data_ptr(), C.POINTER(C.c_double))
+    capi.check(batch.lib.fem_batch_get_state_all(batch.h, px, pv))
+    e2e_steps = max(1, min(args.steps, 5))
+    capi.check(batch.lib.fem_batch_synchronize(batch.h))
+    before = [batch.stats(i)["total_cg_iterations"] for i in range(len(scs))]
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        px = C.cast(hx.data_ptr(), C.POINTER(C.c_double))
-        pv = C.cast(hv.data_ptr(), C.POINTER(C.c_double))
-        capi.check(lib.fem_solid_step_host(solid.h, px, pv, 1, px, pv, C.byref(stats)))
+        capi.check(batch.lib.fem_batch_step_host(batch.h, px, pv, 1, px, pv))
     e2e_s = time.perf_counter() - t0
-    e2e_iters = stats.total_cg_iterations - it0
-    e2e_s = reduce_max(dist, e2e_s)
-    e2e_value = reduce_sum(dist, float(T) * e2e_iters) / e2e_s
+    e2e_iters = [batch.stats(i)["total_cg_iterations"] - before[i] for i in range(len(scs))]
+    e2e_units = float(sum(sc.num_tets * it for sc, it in zip(scs, e2e_iters)))
+    e2e_s, e2e_units = aggregate([(e2e_s, "max"), (e2e_units, "sum")], ws)
+    batch.close()
 
-    # ---- CPU baseline (rank 0, N=1) ----
+    plain = None
     cpu = None
-    if rank == 0 and ws == 1 and not args.no_cpu:
-        cap = 30
-        sampler = CpuSampler(sc)
-        u, s = sampler.sample(cap)
-        cpu = {"value": u / s, "unit": UNIT, "cores": 1, "kind": "port",
-               "sample": f"the CG iterations of the first FixedStep of {sc.name}: step capped at {cap} "
-                         f"iterations minus the step capped at 0 ({s:.1f} s of CG), one thread, oracle "
-                         "restatement (bit-exact with the reference's FP64 translation units)"}
+    if rank == 0 and ws == 1:
+        if not args.no_plain:
+            plain = plain_fp64_comparator(3)
+        if not args.no_cpu:
+            sample = cpu_sample_set(scs, 1_500_000)
+            threads = (os.cpu_count() or 1) if len(sample) > 1 else 1
+            sampler = CpuSampler(sample, threads)
+            cap = 20
+            u, s = sampler.sample(cap)
+            cpu = {"value": u / s, "unit": UNIT, "cores": sampler.threads, "kind": "port",
+                   "sample": f"the CG iterations ({cap} per mesh) of the first FixedStep of {len(sample)} of the "
+                             f"workload's meshes ({sum(x.num_tets for x in sample)} tets), one mesh per thread on "
+                             f"{sampler.threads} threads ({s:.1f} s of CG); oracle restatement, bit-exact with the "
+                             "reference's FP64 translation units"}
 
     if rank == 0:
-        elem_bytes = T * (16 + 20 * 8 + 96)
+        elem_bytes = info["tets"] * (88 if precision == "mixed" else 176)
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": elapsed_ms / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": workload_desc(args.workload, sc), "precision": "fp64",
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32/f64" if precision == "mixed" else "f64",
+            "data": "synthetic",
+            "config": {"workload": describe(args.workload, scs, precision), "meshes": len(scs),
+                       "tets": info["tets"], "nodes": info["nodes"], "tiles": info["tiles"],
                        "parallelism": "replicas only" if ws > 1 else "1 GPU",
-                       "l2": f"inputs larger than L2: {elem_bytes / 1e6:.0f} MB of element data per CG "
+                       "l2": f"inputs larger than L2: {elem_bytes / 1e6:.0f} MB of element data streamed per CG "
                              f"iteration vs {L2_BYTES / 1e6:.0f} MB L2",
-                       "cg_iterations_timed": int(iters)},
+                       "cg_iterations_timed_max_mesh": int(max(iters)), "setup_s": round(setup_s, 2),
+                       "graph": not args.no_graph},
             "p50_step_ms": float(np.percentile(step_ms, 50)), "p99_step_ms": float(np.percentile(step_ms, 99)),
             "clocks": clk,
-            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 2 * n3 * 8,
-                    "d2h_bytes_per_step": 2 * n3 * 8 + 8 * 10, "steps": e2e_steps},
-            "gpu_launches": int(launches),
-            "roofline": {"bound": "hbm", "kernel": "elem_spmv_fp64", "achieved": achieved, "peak": peak,
-                         "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
-                         "peak_kind": peak_kind, "alg_bytes_per_launch": alg_bytes,
-                         "avg_launch_us": avg_s * 1e6, "launches": int(spmv_n),
-                         "note": "FP64 path: bound by FP64 issue on GB300, not HBM"},
+            "e2e": {"value": e2e_units / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 2 * n3 * 8,
+                    "d2h_bytes_per_step": 2 * n3 * 8, "steps": e2e_steps,
+                    "note": "fem_batch_step_host: all states up, one step, all states down, wall clock"},
+            "gpu_launches": launches,
+            "roofline": {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": profiled_traffic(kname, args.workload),
+                         "peak_kind": peak_kind, "alg_bytes_per_launch": alg_per_launch,
+                         "avg_launch_us": avg_launch_s * 1e6, "launches": int(k_n)},
+            "plain_fp64_gpu": plain,
             "cpu_baseline": cpu,
         }
+        if plain:
+            line["speedup_vs_plain_fp64_gpu"] = value / plain["value"]
         print(json.dumps(line))
-    if dist is not None:
-        dist.barrier()
-        dist.destroy_process_group()
+    if ws > 1:
+        torch.distributed.barrier()
+        torch.distributed.destroy_process_group()
     return 0
 
 
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="block60_fp64")
+    ap.add_argument("--workload", default="batch1024")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-graph", action="store_true", help="launch kernels one by one (for per-kernel profilers)")
     args = ap.parse_args()
-    if args.warmup < 3:
-        args.warmup = 3
+    args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

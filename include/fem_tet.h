@@ -185,6 +185,16 @@ int fem_batch_info(fem_batch b, uint32_t* meshes, uint64_t* nodes, uint64_t* tet
 int fem_batch_set_knc_targets(fem_batch b, uint32_t mesh, const double* targets);
 int fem_batch_set_state(fem_batch b, uint32_t mesh, const double* x, const double* v);
 int fem_batch_get_state(fem_batch b, uint32_t mesh, double* x, double* v);
+/* 1: steps run as the captured CUDA graph (device-side CG loop); 0: the same
+ * kernels launched one by one with the CG loop on the host (per-kernel
+ * profiling and timing). */
+int fem_batch_use_graph(fem_batch b, int on);
+/* All solids' states at once, concatenated in mesh order (sum N_m * 3). */
+int fem_batch_set_state_all(fem_batch b, const double* x, const double* v);
+int fem_batch_get_state_all(fem_batch b, double* x, double* v);
+/* Host-buffer round trip: upload all states (null = keep), step, download. */
+int fem_batch_step_host(fem_batch b, const double* x_in, const double* v_in, uint32_t nsteps, double* x_out,
+                        double* v_out);
 /* Which solids take part in the next steps (M bytes, 1 = step); null = all. */
 int fem_batch_set_active(fem_batch b, const uint8_t* mask);
 int fem_batch_step_async(fem_batch b, uint32_t nsteps);

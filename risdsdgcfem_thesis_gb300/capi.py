@@ -322,6 +322,10 @@ _BATCH_SIGNATURES = {
     "fem_batch_stream": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
     "fem_batch_kernel_launches": (C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(C.c_uint64)]),
     "fem_batch_reset_launch_count": (C.c_int, [C.c_void_p]),
+    "fem_batch_set_state_all": (C.c_int, [C.c_void_p, _dp, _dp]),
+    "fem_batch_use_graph": (C.c_int, [C.c_void_p, C.c_int]),
+    "fem_batch_get_state_all": (C.c_int, [C.c_void_p, _dp, _dp]),
+    "fem_batch_step_host": (C.c_int, [C.c_void_p, _dp, _dp, C.c_uint32, _dp, _dp]),
 }
 
 

@@ -132,8 +132,10 @@ struct fem_batch_s {
     Dev<uint16_t> lptr, lidx;
     Dev<uint8_t> fixed;
     Dev<double> rest, x, v, bvec, y, part64, cpart, tpart, knc_target;
-    Dev<unsigned char> r_s, d_s, q_s, part_s;  // S-typed
-    Dev<unsigned> counter, any_flag, refresh_flag, mcount;
+    Dev<unsigned char> r_s, d_s, q_s, part_s, ydelta_s;  // S-typed
+    Dev<unsigned> counter, any_flag, refresh_flag, mcount, err;
+    Dev<unsigned char> blob;
+    Dev<uint32_t> blob_off16;
     StepScalars* st_host = nullptr;
     // step graph
     cudaGraph_t graph = nullptr;
@@ -172,6 +174,9 @@ struct fem_batch_s {
         b.nslot = nslot.p;
         b.fixed = fixed.p;
         b.rest = rest.p;
+        b.ydelta = opt.precision == FEM_PRECISION_MIXED ? reinterpret_cast<S*>(ydelta_s.p) : nullptr;
+        b.blob = opt.precision == FEM_PRECISION_MIXED ? blob.p : nullptr;
+        b.blob_off16 = blob_off16.p;
         b.knc_node = knc_node.p;
         b.knc_mesh = knc_mesh.p;
         b.knc_target = knc_target.p;
@@ -189,8 +194,9 @@ struct fem_batch_s {
         tile_nodes.release(); lptr0.release(); nptr.release(); nslot.release(); knc_node.release();
         knc_mesh.release(); lconn.release(); lptr.release(); lidx.release(); fixed.release(); rest.release();
         x.release(); v.release(); bvec.release(); y.release(); part64.release(); cpart.release(); tpart.release();
-        knc_target.release(); r_s.release(); d_s.release(); q_s.release(); part_s.release(); counter.release();
-        any_flag.release(); refresh_flag.release(); mcount.release();
+        knc_target.release(); r_s.release(); d_s.release(); q_s.release(); part_s.release(); ydelta_s.release(); counter.release();
+        any_flag.release(); refresh_flag.release(); mcount.release(); err.release(); blob.release();
+        blob_off16.release();
         if (st_host) cudaFreeHost(st_host);
         st_host = nullptr;
         if (stream) cudaStreamDestroy(stream);
@@ -294,7 +300,10 @@ int enqueue_step(fem_batch B, cudaStream_t s, bool capture)
                 BCK(e1);
             }
         }
-        L::tile_spmv(b, d, r, part, ifh, mixed ? 1 : 0, B->refresh_flag.p, bs);
+        if constexpr (sizeof(S) == 4)
+            launch_tile_spmv_pipe(b, d, r, part, ifh, 1, B->refresh_flag.p, B->err.p, bs);
+        else
+            L::tile_spmv(b, d, r, part, ifh, 0, B->refresh_flag.p, bs);
         if (mixed) {
             // IF (some mesh refreshes this iteration) { FP64 product of y }
             const cudaGraphNode_t* bdeps = nullptr;
@@ -342,7 +351,10 @@ int enqueue_step(fem_batch B, cudaStream_t s, bool capture)
             for (uint32_t m = 0; m < B->M; m++) any |= !B->st_host[m].done;
             if (!any) break;
             for (int i = 0; i < 8; i++) {
-                L::tile_spmv(b, d, r, part, 0, 0, nullptr, s);
+                if constexpr (sizeof(S) == 4)
+                    launch_tile_spmv_pipe(b, d, r, part, 0, 0, nullptr, B->err.p, s);
+                else
+                    L::tile_spmv(b, d, r, part, 0, 0, nullptr, s);
                 if (mixed) L::tile_spmv_y64(b, B->y.p, B->part64.p, 1, B->refresh_flag.p, s);
                 body_tail(s);
             }
@@ -689,6 +701,44 @@ int fem_batch_finalize(fem_batch b)
         for (int c = 0; c < 9; c++) Dinv_soa[c * T + e] = Dinv_aos[9 * e + c];
         for (int c = 0; c < 3; c++) mat_soa[c * T + e] = mat_aos[3 * e + c];
     }
+    // per-tile blobs for the pipelined mixed product (element data in FP32)
+    std::vector<uint32_t> blob_off16_h;
+    std::vector<unsigned char> blob_h;
+    if (!fp64) {
+        uint64_t total = 0;
+        blob_off16_h.resize(b->ntiles);
+        for (uint32_t t = 0; t < b->ntiles; t++) {
+            blob_off16_h[t] = (uint32_t)(total / 16);
+            total += blob_bytes(tiles[t].ne, tiles[t].nn);
+        }
+        if (total / 16 >= (1ull << 32)) return batch_fail(FEM_E_ARG, "batch too large for tile blobs");
+        blob_h.assign(total, 0);
+        for (uint32_t t = 0; t < b->ntiles; t++) {
+            const TileMeta& tm = tiles[t];
+            unsigned char* base = blob_h.data() + 16ull * blob_off16_h[t];
+            float* comp = reinterpret_cast<float*>(base);
+            const uint32_t ne4 = blob_ne4(tm.ne);
+            for (uint32_t i = 0; i < tm.ne; i++) {
+                const size_t e = tm.e0 + i;
+                comp[0 * ne4 + i] = 1.f; comp[4 * ne4 + i] = 1.f; comp[8 * ne4 + i] = 1.f;  // R = I
+                for (int c = 0; c < 9; c++) comp[(9 + c) * ne4 + i] = (float)Dinv_soa[c * T + e];
+                for (int c = 0; c < 3; c++) comp[(18 + c) * ne4 + i] = (float)mat_soa[c * T + e];
+                const uchar4 lc = lconn[e];
+                const uint32_t w = (uint32_t)lc.x | ((uint32_t)lc.y << 8) | ((uint32_t)lc.z << 16) | ((uint32_t)lc.w << 24);
+                std::memcpy(&comp[21 * ne4 + i], &w, 4);
+            }
+            uint16_t* lp = reinterpret_cast<uint16_t*>(base + blob_lptr_off(tm.ne));
+            const uint16_t* src_lp = lptr.data() + lptr0[t];
+            for (uint32_t i = 0; i <= tm.nn; i++) lp[i] = src_lp[i];
+            uint16_t* li = lp + (tm.nn + 1);
+            for (uint32_t j = 0; j < 4u * tm.ne; j++) {
+                const uint16_t v = lidx[tm.c0 + j];  // (element << 2 | slot) -> (slot << 8 | element)
+                li[j] = (uint16_t)(((v & 3u) << 8) | (v >> 2));
+            }
+            uint32_t* nodes = reinterpret_cast<uint32_t*>(base + blob_nodes_off(tm.ne, tm.nn));
+            for (uint32_t i = 0; i < tm.nn; i++) nodes[i] = tile_nodes[tm.n0 + i];
+        }
+    }
     std::vector<double> Rinit(9 * T, 0.0);
     for (size_t e = 0; e < T; e++) Rinit[e] = Rinit[4 * T + e] = Rinit[8 * T + e] = 1.0;
 
@@ -740,6 +790,8 @@ int fem_batch_finalize(fem_batch b)
     BCKC(b->d_s.alloc(N3 * SB));
     BCKC(b->q_s.alloc(N3 * SB));
     BCKC(b->part_s.alloc(3 * b->nslots * SB));
+    BCKC(b->ydelta_s.alloc(N3 * SB));
+    BCKC(cudaMemsetAsync(b->ydelta_s.p, 0, N3 * SB, s));
     BCKC(b->part64.alloc(3 * b->nslots));
     BCKC(b->cpart.alloc(b->nchunks));
     BCKC(b->tpart.alloc(b->ntiles));
@@ -747,6 +799,13 @@ int fem_batch_finalize(fem_batch b)
     BCKC(b->any_flag.alloc(1));
     BCKC(b->refresh_flag.alloc(1));
     BCKC(b->mcount.alloc(b->M));
+    BCKC(b->err.alloc(1));
+    BCKC(cudaMemsetAsync(b->err.p, 0, sizeof(unsigned), s));
+    BCKC(b->blob.alloc(blob_h.size()));
+    BCKC(b->blob.upload(blob_h, s));
+    BCKC(b->blob_off16.alloc(blob_off16_h.size()));
+    BCKC(b->blob_off16.upload(blob_off16_h, s));
+    if (!fp64) prepare_tile_pipe();
     BCKC(cudaMallocHost(&b->st_host, sizeof(StepScalars) * b->M));
     BCKC(b->tiles.upload(tiles, s));
     BCKC(b->chunks.upload(chunks, s));
@@ -871,6 +930,42 @@ int fem_batch_get_state(fem_batch b, uint32_t mesh, double* x, double* v)
     return FEM_OK;
 }
 
+int fem_batch_use_graph(fem_batch b, int on)
+{
+    if (int e = check_ready(b)) return e;
+    b->opt.use_graph = on ? 1u : 0u;
+    if (on) return build_graph(b);
+    return FEM_OK;
+}
+
+int fem_batch_set_state_all(fem_batch b, const double* x, const double* v)
+{
+    if (int e = check_ready(b)) return e;
+    const size_t bytes = sizeof(double) * 3 * (size_t)b->Ntot;
+    if (x) BCK(cudaMemcpyAsync(b->x.p, x, bytes, cudaMemcpyHostToDevice, b->stream));
+    if (v) BCK(cudaMemcpyAsync(b->v.p, v, bytes, cudaMemcpyHostToDevice, b->stream));
+    return FEM_OK;
+}
+
+int fem_batch_get_state_all(fem_batch b, double* x, double* v)
+{
+    if (int e = check_ready(b)) return e;
+    const size_t bytes = sizeof(double) * 3 * (size_t)b->Ntot;
+    if (x) BCK(cudaMemcpyAsync(x, b->x.p, bytes, cudaMemcpyDeviceToHost, b->stream));
+    if (v) BCK(cudaMemcpyAsync(v, b->v.p, bytes, cudaMemcpyDeviceToHost, b->stream));
+    BCK(cudaStreamSynchronize(b->stream));
+    return FEM_OK;
+}
+
+int fem_batch_step_host(fem_batch b, const double* x_in, const double* v_in, uint32_t nsteps, double* x_out,
+                        double* v_out)
+{
+    if (int e = fem_batch_set_state_all(b, x_in, v_in)) return e;
+    if (int e = fem_batch_step_async(b, nsteps)) return e;
+    if (int e = fem_batch_get_state_all(b, x_out, v_out)) return e;
+    return fem_batch_synchronize(b);
+}
+
 int fem_batch_set_active(fem_batch b, const uint8_t* mask)
 {
     if (int e = check_ready(b)) return e;
@@ -883,7 +978,7 @@ int fem_batch_step_async(fem_batch b, uint32_t nsteps)
 {
     if (int e = check_ready(b)) return e;
     for (uint32_t i = 0; i < nsteps; i++) {
-        if (b->exec) {
+        if (b->exec && b->opt.use_graph) {
             BCK(cudaGraphLaunch(b->exec, b->stream));
             launch_counter() += 0;  // kernels inside the graph are counted at capture
         } else {
@@ -899,7 +994,10 @@ int fem_batch_synchronize(fem_batch b)
 {
     if (int e = check_ready(b)) return e;
     BCK(cudaMemcpyAsync(b->st_host, b->st.p, sizeof(StepScalars) * b->M, cudaMemcpyDeviceToHost, b->stream));
+    unsigned err = 0;
+    if (b->err.p) BCK(cudaMemcpyAsync(&err, b->err.p, sizeof(unsigned), cudaMemcpyDeviceToHost, b->stream));
     BCK(cudaStreamSynchronize(b->stream));
+    if (err) return batch_fail(FEM_E_TIMEOUT, "a bounded wait for a tile copy gave up (code %u)", err);
     for (uint32_t m = 0; m < b->M; m++)
         if (b->st_host[m].status == FEM_E_NAN) return batch_fail(FEM_E_NAN, "NaN in the CG residual of mesh %u", m);
     return FEM_OK;

@@ -29,8 +29,21 @@ namespace femgb {
 
 constexpr int kTileElems = 256;
 constexpr int kTileNodes = 256;
-constexpr int kChunkNodes = 1024;  // node chunk = one block's share in node kernels
+constexpr int kChunkNodes = 256;   // node chunk = one block's share in node kernels
 constexpr int kNodeThreads = 256;  // threads per node-kernel block
+
+// Layout of a tile's blob (mixed path, see tile_pipe.cu): element data
+// float[22][ne4], then uint16 lptr[nn+1], uint16 lidx[4 ne], uint32 nodes[nn].
+__host__ __device__ inline uint32_t blob_ne4(uint32_t ne) { return (ne + 3u) & ~3u; }
+__host__ __device__ inline uint32_t blob_lptr_off(uint32_t ne) { return 88u * blob_ne4(ne); }
+__host__ __device__ inline uint32_t blob_nodes_off(uint32_t ne, uint32_t nn)
+{
+    return (blob_lptr_off(ne) + 2u * (nn + 1u) + 8u * ne + 3u) & ~3u;
+}
+__host__ __device__ inline uint32_t blob_bytes(uint32_t ne, uint32_t nn)
+{
+    return (blob_nodes_off(ne, nn) + 4u * nn + 15u) & ~15u;
+}
 
 struct TileMeta {
     uint32_t mesh;
@@ -85,6 +98,9 @@ struct BatchView {
     const uint32_t* nslot;         // [sum nn] partial slots per node
     const uint8_t* fixed;          // [Ntot]
     const double* rest;            // [3 Ntot]
+    S* ydelta;                     // [3 Ntot] mixed: FP32 sum of this step's alpha d; null on FP64
+    unsigned char* blob;           // mixed: per-tile blobs (element data, tile CSR, node list)
+    const uint32_t* blob_off16;    // [ntiles] blob offset / 16
     // constraints
     const uint32_t* knc_node;      // [K] global node id
     const uint32_t* knc_mesh;      // [K]

@@ -52,10 +52,63 @@ __device__ __forceinline__ double bblock_sum(double v)
     return v;
 }
 
+// Block sum of one FP32 value per thread, for the FP64 reductions of the mixed
+// path: within a warp the values are added as an unevaluated sum of two
+// floats (Knuth's two-sum keeps each rounding error), which carries about
+// 48 bits, then each warp's (hi, lo) is converted to double and the warps
+// are added in FP64. The FP64 pipe of GB300 runs at a small fraction of the
+// FP32 rate, so FP64 work per node is avoided; the tree is fixed, so the
+// result does not depend on scheduling. Result valid in thread 0.
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e)
+{
+    s = a + b;
+    const float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+
+__device__ __forceinline__ double bblock_sum_f(float v)
+{
+    __shared__ double sh[32];
+    float hi = v, lo = 0.f;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const float h2 = __shfl_down_sync(0xffffffffu, hi, o);
+        const float l2 = __shfl_down_sync(0xffffffffu, lo, o);
+        float s, e;
+        two_sum(hi, h2, s, e);
+        e += lo + l2;
+        hi = s + e;
+        lo = e - (hi - s);
+    }
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) sh[wid] = (double)hi + (double)lo;
+    __syncthreads();
+    const int nw = (blockDim.x + 31) >> 5;
+    double w = (threadIdx.x < nw) ? sh[threadIdx.x] : 0.0;
+    if (wid == 0) w = bwarp_sum(w);
+    return w;
+}
+
+template <typename S>
+__device__ __forceinline__ double chunk_sum(S v);
+template <>
+__device__ __forceinline__ double chunk_sum<float>(float v) { return bblock_sum_f(v); }
+template <>
+__device__ __forceinline__ double chunk_sum<double>(double v) { return bblock_sum(v); }
+
 template <typename S>
 __device__ __forceinline__ bool mesh_running(const BatchView<S>& b, uint32_t m)
 {
     return !b.st[m].done;
+}
+
+// The CG iterate: FP64 y plus, on the mixed path, the FP32 sum of this
+// step's alpha d increments (folded in at refresh and integration).
+template <typename S>
+__device__ __forceinline__ double y_full(const BatchView<S>& b, const double* __restrict__ y, size_t i)
+{
+    return b.ydelta ? y[i] + (double)b.ydelta[i] : y[i];
 }
 
 // CG iteration index at which the mesh refreshes its residual in FP64.
@@ -172,9 +225,9 @@ __global__ void __launch_bounds__(256) k_tile_spmv_y64(BatchView<S> b, const dou
         const uint16_t* li = b.lidx + tm.c0;
         for (int i = threadIdx.x; i < tm.nn; i += blockDim.x) {
             const size_t g = b.tile_nodes[tm.n0 + i];
-            sd[i] = y[3 * g];
-            sd[kTileNodes + i] = y[3 * g + 1];
-            sd[2 * kTileNodes + i] = y[3 * g + 2];
+            sd[i] = y_full(b, y, 3 * g);
+            sd[kTileNodes + i] = y_full(b, y, 3 * g + 1);
+            sd[2 * kTileNodes + i] = y_full(b, y, 3 * g + 2);
         }
         __syncthreads();
         if (threadIdx.x < tm.ne) {
@@ -365,6 +418,11 @@ __global__ void k_node_b(BatchView<S> b, const double* __restrict__ part64, cons
             y[i] = v[i];
             y[i + 1] = v[i + 1];
             y[i + 2] = v[i + 2];
+            if (b.ydelta) {
+                b.ydelta[i] = 0;
+                b.ydelta[i + 1] = 0;
+                b.ydelta[i + 2] = 0;
+            }
         }
     }
 }
@@ -399,18 +457,22 @@ __global__ void k_knc(BatchView<S> b, uint32_t K, const double* __restrict__ x, 
 // the mesh's CG scalars; after a block has finished all its chunks, the block
 // that completes the grid evaluates the batch-wide loop condition. Nothing
 // waits: the last arrival does the work.
+// The values other blocks must see (a chunk partial, a mesh's scalars) are
+// written by thread 0, so thread 0 alone fences before arriving.
 __device__ __forceinline__ bool arrive_last(unsigned* ctr, unsigned expected)
 {
     __shared__ unsigned s_last;
-    __threadfence();
     __syncthreads();
     if (threadIdx.x == 0) {
+        __threadfence();
         const unsigned prev = atomicAdd(ctr, 1u);
         s_last = (prev + 1u == expected) ? 1u : 0u;
-        if (s_last) *ctr = 0u;
+        if (s_last) {
+            *ctr = 0u;
+            __threadfence();
+        }
     }
     __syncthreads();
-    if (s_last) __threadfence();
     return s_last != 0;
 }
 
@@ -517,15 +579,17 @@ __global__ void k_node_q(BatchView<S> b, const S* __restrict__ part, S* __restri
                          const double* __restrict__ part64, const double* __restrict__ bv,
                          const double* __restrict__ y, S* __restrict__ r, double* __restrict__ cpart, LoopSync ls)
 {
-    for (uint32_t ci = blockIdx.x; ci < b.nchunks; ci += gridDim.x) {
+    {
+        const uint32_t ci = blockIdx.x;
+        if (ci >= b.nchunks) return;
         const ChunkMeta ch = b.chunks[ci];
-        if (!mesh_running(b, ch.mesh)) continue;
+        if (!mesh_running(b, ch.mesh)) return;
         const MeshConsts& c = b.mc[ch.mesh];
         const StepScalars& sm = b.st[ch.mesh];
         const bool refresh = part64 && refresh_now(c, sm);
         const S beta = (S)sm.beta;
-        const double mfm = c.mass * c.factor_M;
-        double acc = 0.0;
+        const S fK = (S)c.factor_K, mfm = (S)(c.mass * c.factor_M);
+        S acc = 0;
         for (size_t n = ch.n0 + threadIdx.x; n < ch.n1; n += blockDim.x) {
             const size_t i = 3 * n;
             S q0 = 0, q1 = 0, q2 = 0, dn0 = 0, dn1 = 0, dn2 = 0;
@@ -533,23 +597,31 @@ __global__ void k_node_q(BatchView<S> b, const S* __restrict__ part, S* __restri
                 dn0 = dir_update<S>(beta, d[i], r[i]);
                 dn1 = dir_update<S>(beta, d[i + 1], r[i + 1]);
                 dn2 = dir_update<S>(beta, d[i + 2], r[i + 2]);
-                double s0, s1, s2;
-                sum_parts(b.nptr, b.nslot, part, n, s0, s1, s2);
-                q0 = (S)(c.factor_K * s0 + mfm * (double)dn0);
-                q1 = (S)(c.factor_K * s1 + mfm * (double)dn1);
-                q2 = (S)(c.factor_K * s2 + mfm * (double)dn2);
+                S s0 = 0, s1 = 0, s2 = 0;
+                const uint32_t j1 = b.nptr[n + 1];
+                for (uint32_t j = b.nptr[n]; j < j1; j++) {
+                    const size_t o = 3 * (size_t)b.nslot[j];
+                    s0 += part[o];
+                    s1 += part[o + 1];
+                    s2 += part[o + 2];
+                }
+                q0 = fK * s0 + mfm * dn0;
+                q1 = fK * s1 + mfm * dn1;
+                q2 = fK * s2 + mfm * dn2;
                 if (refresh) {
-                    sum_parts(b.nptr, b.nslot, part64, n, s0, s1, s2);
-                    r[i] = (S)(bv[i] - (c.factor_K * s0 + mfm * y[i]));
-                    r[i + 1] = (S)(bv[i + 1] - (c.factor_K * s1 + mfm * y[i + 1]));
-                    r[i + 2] = (S)(bv[i + 2] - (c.factor_K * s2 + mfm * y[i + 2]));
+                    double t0, t1, t2;
+                    sum_parts(b.nptr, b.nslot, part64, n, t0, t1, t2);
+                    const double mfm64 = c.mass * c.factor_M;
+                    r[i] = (S)(bv[i] - (c.factor_K * t0 + mfm64 * y_full(b, y, i)));
+                    r[i + 1] = (S)(bv[i + 1] - (c.factor_K * t1 + mfm64 * y_full(b, y, i + 1)));
+                    r[i + 2] = (S)(bv[i + 2] - (c.factor_K * t2 + mfm64 * y_full(b, y, i + 2)));
                 }
             }
             d[i] = dn0; d[i + 1] = dn1; d[i + 2] = dn2;
             q[i] = q0; q[i + 1] = q1; q[i + 2] = q2;
-            acc += (double)dn0 * (double)q0 + (double)dn1 * (double)q1 + (double)dn2 * (double)q2;
+            acc += dn0 * q0 + dn1 * q1 + dn2 * q2;
         }
-        const double sum = bblock_sum(acc);
+        const double sum = chunk_sum<S>(acc);
         if (threadIdx.x == 0) cpart[ci] = sum;
         if (arrive_last(ls.mcount + ch.mesh, c.nchunks)) {
             const double total = mesh_partial_sum(cpart, c.chunk0, c.nchunks);
@@ -564,7 +636,6 @@ __global__ void k_node_q(BatchView<S> b, const S* __restrict__ part, S* __restri
                 }
             }
         }
-        __syncthreads();
     }
 }
 
@@ -574,24 +645,27 @@ template <typename S>
 __global__ void k_node_update(BatchView<S> b, double* __restrict__ y, S* __restrict__ r, const S* __restrict__ d,
                               const S* __restrict__ q, double* __restrict__ cpart, LoopSync ls)
 {
-    for (uint32_t ci = blockIdx.x; ci < b.nchunks; ci += gridDim.x) {
-        const ChunkMeta ch = b.chunks[ci];
-        if (!mesh_running(b, ch.mesh)) continue;
+    const uint32_t ci = blockIdx.x;
+    const ChunkMeta ch = b.chunks[ci < b.nchunks ? ci : 0];
+    if (ci < b.nchunks && mesh_running(b, ch.mesh)) {
         const MeshConsts& c = b.mc[ch.mesh];
         const double alpha = b.st[ch.mesh].alpha;
-        const S na = (S)(-alpha);
-        double acc = 0.0;
+        const S alpha_s = (S)alpha, na = -alpha_s;
+        S acc = 0;
         for (size_t n = ch.n0 + threadIdx.x; n < ch.n1; n += blockDim.x) {
+            S rr = 0;
 #pragma unroll
             for (int a = 0; a < 3; a++) {
                 const size_t i = 3 * n + a;
-                y[i] += alpha * (double)d[i];
+                if (b.ydelta) b.ydelta[i] += alpha_s * d[i];
+                else y[i] += alpha * (double)d[i];
                 const S ri = r[i] + na * q[i];
                 r[i] = ri;
-                acc += (double)ri * (double)ri;
+                rr += ri * ri;
             }
+            acc += rr;
         }
-        const double sum = bblock_sum(acc);
+        const double sum = chunk_sum<S>(acc);
         if (threadIdx.x == 0) cpart[ci] = sum;
         if (arrive_last(ls.mcount + ch.mesh, c.nchunks)) {
             const double total = mesh_partial_sum(cpart, c.chunk0, c.nchunks);
@@ -607,7 +681,6 @@ __global__ void k_node_update(BatchView<S> b, double* __restrict__ y, S* __restr
                 if (s.done) finish_stats(s);
             }
         }
-        __syncthreads();
     }
     grid_tail(b, ls);
 }
@@ -625,7 +698,7 @@ __global__ void k_integrate(BatchView<S> b, double* __restrict__ x, double* __re
 #pragma unroll
             for (int a = 0; a < 3; a++) {
                 const size_t i = 3 * n + a;
-                const double yi = y[i];
+                const double yi = y_full(b, y, i);
                 v[i] = yi;
                 x[i] = x[i] + dt * yi;
             }
@@ -735,7 +808,7 @@ void BatchLaunch<S>::node_q(const BatchView<S>& b, const S* part, S* d, S* q, co
                             cudaStream_t s)
 {
     prof_begin(sizeof(S) == 8 ? "node_q_fp64" : "node_q_mixed", s);
-    k_node_q<S><<<grid_chunks(b.nchunks), kNodeThreads, 0, s>>>(b, part, d, q, part64, bv, y, r, cpart, ls);
+    k_node_q<S><<<b.nchunks ? b.nchunks : 1, kNodeThreads, 0, s>>>(b, part, d, q, part64, bv, y, r, cpart, ls);
     prof_end(sizeof(S) == 8 ? "node_q_fp64" : "node_q_mixed", s);
     launch_counter()++;
 }
@@ -744,7 +817,7 @@ template <typename S>
 void BatchLaunch<S>::node_update(const BatchView<S>& b, double* y, S* r, const S* d, const S* q, double* cpart,
                                  const LoopSync& ls, cudaStream_t s)
 {
-    k_node_update<S><<<grid_chunks(b.nchunks), kNodeThreads, 0, s>>>(b, y, r, d, q, cpart, ls);
+    k_node_update<S><<<b.nchunks ? b.nchunks : 1, kNodeThreads, 0, s>>>(b, y, r, d, q, cpart, ls);
     launch_counter()++;
 }
 

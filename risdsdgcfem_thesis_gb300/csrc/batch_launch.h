@@ -6,6 +6,8 @@
 namespace femgb {
 
 uint32_t grid_tiles(uint32_t ntiles);
+uint32_t tile_pipe_smem_bytes();
+void prepare_tile_pipe();
 uint32_t grid_chunks(uint32_t nchunks);
 
 // Arrival counters and graph handle of the fused CG finalisation.
@@ -17,6 +19,10 @@ struct LoopSync {
     cudaGraphConditionalHandle cond;
     int set_cond;
 };
+
+void launch_tile_spmv_pipe(const BatchView<float>& b, const float* d, const float* r, float* part,
+                           cudaGraphConditionalHandle if_refresh, int set_if, const unsigned* refresh_flag,
+                           unsigned* err, cudaStream_t s);
 
 template <typename S>
 struct BatchLaunch {

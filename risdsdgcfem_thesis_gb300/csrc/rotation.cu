@@ -104,6 +104,12 @@ __global__ void k_begin_eval_batch(BatchView<S> b, const double* __restrict__ x)
             }
 #pragma unroll
             for (int c = 0; c < 9; c++) b.R[c * T + e] = Rs[c];
+            if (b.blob) {
+                float* comp = reinterpret_cast<float*>(b.blob + 16ull * b.blob_off16[t]);
+                const uint32_t ne4 = blob_ne4(tm.ne);
+#pragma unroll
+                for (int c = 0; c < 9; c++) comp[c * ne4 + threadIdx.x] = (float)Rs[c];
+            }
             b.detF[e] = detF;
             if (detF <= 0.0) atomicAdd(&s_inv, 1u);
         }
