@@ -254,6 +254,7 @@ int enqueue_step(fem_batch B, cudaStream_t s, bool capture)
     ls.gcount = B->counter.p;
     ls.refresh_flag = B->refresh_flag.p;
     ls.body_runs = nullptr;
+    ls.err = B->err.p;
     ls.cond = cond;
     ls.set_cond = capture ? 1 : 0;
     // ---- once per step ----
@@ -266,9 +267,23 @@ int enqueue_step(fem_batch B, cudaStream_t s, bool capture)
     L::node_residual(b, B->part64.p, B->bvec.p, B->y.p, r, d, B->cpart.p, ls, s);
     LoopSync lb = ls;
     lb.body_runs = B->any_flag.p;
+    // mixed: the tile product also writes each tile's share of d^T A d; one
+    // fused node pass forms alpha from the shares and does the rest
+    auto body_head = [&](cudaStream_t bs, cudaGraphConditionalHandle ifh, int set_if) {
+        if constexpr (sizeof(S) == 4)
+            launch_tile_spmv_pipe(b, d, r, part, reinterpret_cast<float2*>(B->tpart.p), ifh, set_if,
+                                  set_if ? B->refresh_flag.p : nullptr, B->err.p, bs);
+        else
+            L::tile_spmv(b, d, r, part, ifh, 0, B->refresh_flag.p, bs);
+    };
     auto body_tail = [&](cudaStream_t bs) {
-        L::node_q(b, part, d, q, mixed ? B->part64.p : nullptr, B->bvec.p, B->y.p, r, B->cpart.p, lb, bs);
-        L::node_update(b, B->y.p, r, d, q, B->cpart.p, lb, bs);
+        if constexpr (sizeof(S) == 4) {
+            launch_node_update_fused(b, part, reinterpret_cast<const float2*>(B->tpart.p), B->part64.p, B->bvec.p,
+                                     B->y.p, r, d, reinterpret_cast<float2*>(B->cpart.p), lb, bs);
+        } else {
+            L::node_q(b, part, d, q, nullptr, B->bvec.p, B->y.p, r, B->cpart.p, lb, bs);
+            L::node_update(b, B->y.p, r, d, q, B->cpart.p, lb, bs);
+        }
     };
     if (capture) {
         const cudaGraphNode_t* deps = nullptr;
@@ -300,10 +315,7 @@ int enqueue_step(fem_batch B, cudaStream_t s, bool capture)
                 BCK(e1);
             }
         }
-        if constexpr (sizeof(S) == 4)
-            launch_tile_spmv_pipe(b, d, r, part, ifh, 1, B->refresh_flag.p, B->err.p, bs);
-        else
-            L::tile_spmv(b, d, r, part, ifh, 0, B->refresh_flag.p, bs);
+        body_head(bs, ifh, mixed ? 1 : 0);
         if (mixed) {
             // IF (some mesh refreshes this iteration) { FP64 product of y }
             const cudaGraphNode_t* bdeps = nullptr;
@@ -351,10 +363,7 @@ int enqueue_step(fem_batch B, cudaStream_t s, bool capture)
             for (uint32_t m = 0; m < B->M; m++) any |= !B->st_host[m].done;
             if (!any) break;
             for (int i = 0; i < 8; i++) {
-                if constexpr (sizeof(S) == 4)
-                    launch_tile_spmv_pipe(b, d, r, part, 0, 0, nullptr, B->err.p, s);
-                else
-                    L::tile_spmv(b, d, r, part, 0, 0, nullptr, s);
+                body_head(s, 0, 0);
                 if (mixed) L::tile_spmv_y64(b, B->y.p, B->part64.p, 1, B->refresh_flag.p, s);
                 body_tail(s);
             }
@@ -659,6 +668,8 @@ int fem_batch_finalize(fem_batch b)
         c.degenerate_det_F = p.degenerate_det_F;
         c.max_iter = p.ls_max_iter;
         c.refresh_every = fp64 ? 0u : p.refresh_every;
+        c.fK_f = (float)c.factor_K;
+        c.mfm_f = (float)(c.mass * c.factor_M);
         c.node0 = (uint32_t)node0;
         c.N = N;
         c.elem0 = (uint32_t)elem0;
@@ -736,7 +747,11 @@ int fem_batch_finalize(fem_batch b)
                 li[j] = (uint16_t)(((v & 3u) << 8) | (v >> 2));
             }
             uint32_t* nodes = reinterpret_cast<uint32_t*>(base + blob_nodes_off(tm.ne, tm.nn));
-            for (uint32_t i = 0; i < tm.nn; i++) nodes[i] = tile_nodes[tm.n0 + i];
+            // bit 31: this tile owns the node (the first tile, in tile order, that lists it)
+            for (uint32_t i = 0; i < tm.nn; i++) {
+                const uint32_t g = tile_nodes[tm.n0 + i];
+                nodes[i] = g | (nslot[nptr[g]] == tm.n0 + i ? 0x80000000u : 0u);
+            }
         }
     }
     std::vector<double> Rinit(9 * T, 0.0);

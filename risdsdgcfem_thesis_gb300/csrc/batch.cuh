@@ -69,6 +69,7 @@ struct MeshConsts {
     uint32_t node0, N, elem0, T;
     uint32_t tile0, ntiles, chunk0, nchunks;
     uint32_t knc0, nknc;
+    float fK_f, mfm_f;  // factor_K and mass * factor_M rounded to FP32 (mixed path)
 };
 
 template <typename S>

@@ -1,7 +1,8 @@
 // batch_kernels.cu -- kernels of the tiled, batched step (FP64 and mixed).
 //
 // One CG iteration (Saphyre2 ns/ILSS_CG.h:90-144) over every mesh whose loop
-// is still running, in lock-step, is three kernels:
+// is still running, in lock-step, is three kernels on the FP64 path (the
+// mixed path runs its iteration as two kernels, tile_pipe.cu):
 //   k_tile_spmv   one CTA per element tile: the tile's node values of the
 //                 search direction d = S(r + beta d) are formed while staging
 //                 r and d in shared memory, each thread forms one element's
@@ -516,7 +517,8 @@ __device__ void grid_tail(const BatchView<S>& b, const LoopSync& ls)
     if (threadIdx.x == 0) {
         if (ls.refresh_flag) *ls.refresh_flag = refresh ? 1u : 0u;
         if (ls.body_runs) *ls.body_runs += 1u;
-        if (ls.set_cond) cudaGraphSetConditional(ls.cond, any ? 1u : 0u);
+        const bool stop = ls.err && *(volatile const unsigned*)ls.err;
+        if (ls.set_cond) cudaGraphSetConditional(ls.cond, (any && !stop) ? 1u : 0u);
     }
 }
 
@@ -563,6 +565,7 @@ __global__ void k_node_residual(BatchView<S> b, const double* __restrict__ part6
                 s.status = (total != total) ? 3u : 0u;
                 s.alpha = 0.0;
                 s.beta = 0.0;
+                s.beta_f = 0.f;
                 s.done = cg_cont(s) ? 0u : 1u;
                 if (s.done) finish_stats(s);
             }

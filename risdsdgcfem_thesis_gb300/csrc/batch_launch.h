@@ -16,13 +16,19 @@ struct LoopSync {
     unsigned* gcount;        // grid arrivals
     unsigned* refresh_flag;  // raised when a mesh refreshes its residual next iteration
     unsigned* body_runs;     // CG-loop body executions (launch accounting)
+    const unsigned* err;     // batch error word: the loop stops once it is set
     cudaGraphConditionalHandle cond;
     int set_cond;
 };
 
-void launch_tile_spmv_pipe(const BatchView<float>& b, const float* d, const float* r, float* part,
+// Mixed path, one CG iteration (tile_pipe.cu): tile product with the
+// per-mesh alpha, then the fused node update with beta and the loop test.
+void launch_tile_spmv_pipe(const BatchView<float>& b, const float* d, const float* r, float* part, float2* tshare,
                            cudaGraphConditionalHandle if_refresh, int set_if, const unsigned* refresh_flag,
                            unsigned* err, cudaStream_t s);
+void launch_node_update_fused(const BatchView<float>& b, const float* part, const float2* tshare,
+                              const double* part64, const double* bv, const double* y, float* r, float* d,
+                              float2* cshare, const LoopSync& ls, cudaStream_t s);
 
 template <typename S>
 struct BatchLaunch {

@@ -29,7 +29,8 @@ struct StepScalars {
     double elastic_energy, potential_energy;
     double rel_residual, abs_residual;
     uint32_t k, max_iter, done, status;
-    uint32_t inverted, fp64_resolved, refresh_every, pad;
+    uint32_t inverted, fp64_resolved, refresh_every;
+    float beta_f;  // beta rounded to FP32 (mixed path)
     unsigned long long total_iters;
 };
 

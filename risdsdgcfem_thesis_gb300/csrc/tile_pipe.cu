@@ -1,21 +1,44 @@
-// tile_pipe.cu -- the mixed-precision element-tile product as a persistent,
-// double-buffered pipeline: each tile's element data, tile-local CSR and
-// node list form one contiguous 16-byte-aligned blob in HBM, copied into
-// shared memory by one bulk asynchronous copy (cp.async.bulk, completion on
-// an mbarrier) while the block computes the previous tile.
+// tile_pipe.cu -- one CG iteration of the mixed-precision path in two kernels
+// (Saphyre2 ns/ILSS_CG.h:90-144, every running mesh of the batch in
+// lock-step).
+//
+// k_tile_spmv_pipe: persistent, double-buffered element-tile product. Each
+// tile's element data, tile-local CSR and node list form one contiguous
+// 16-byte-aligned blob in HBM, copied into shared memory by one bulk
+// asynchronous copy (cp.async.bulk, completion on an mbarrier) while the
+// block computes the previous tile. The tile stages the new direction
+// d = S(r + beta d) of its nodes, forms one element's R K0 R^T d per thread
+// and sums the outputs per local node (tile-local CSR, element order) into
+// one partial per (tile, node). The gathers of d and r for the next tile
+// are issued into registers before the current tile is computed, so their
+// latency overlaps a whole tile. The tile also forms its share of d^T A d:
+//     fK * sum_e d_e . (R K0 R^T d)_e  +  m fM * sum_{nodes it owns} |d_n|^2,
+// which sums to d^T S A d (ILSS_CG.h:91-96) because d is zero on constrained
+// rows; a node is owned by the first tile (in tile order) that lists it.
+//
+// k_node_update_fused: every block first sums its mesh's tile shares (fixed
+// order, so every block of the mesh gets the same bits) and forms alpha, or
+// leaves the mesh on breakdown (ILSS_CG.h:97). Then per node: d = S(r + beta
+// d) (the values the tiles staged), q = S(fK sum(partials) + m fM d), y +=
+// alpha d (into the FP32 increment accumulator), r -= alpha q (on refresh
+// iterations r is first recomputed as S(b - A y) from the FP64 product of
+// y), |r|^2. The last block of a mesh forms beta and the loop test
+// (ILSS_CG.h:100-144), the last block of the grid sets the CUDA-graph while
+// condition and the refresh flag.
 //
 // Blob of a tile with ne elements (ne4 = ne rounded up to 4) and nn local
-// nodes, all offsets from the blob start:
-//   0                 float comp[22][ne4]: R (9), Dm^-1 (9), V(lambda+2mu),
-//                     V lambda, V mu, local ids (uchar4 as one word)
-//   88 ne4            uint16 lptr[nn+1]   tile-local CSR offsets
-//   + 2(nn+1)         uint16 lidx[4 ne]   (slot << 8 | element), element order
-//   (4-aligned)       uint32 nodes[nn]    global node id of each local node
+// nodes, offsets from the blob start:
+//   0            float comp[22][ne4]: R (9), Dm^-1 (9), V(lambda+2mu), V lambda,
+//                V mu, local ids (uchar4 as one word)
+//   88 ne4       uint16 lptr[nn+1]      tile-local CSR offsets
+//   + 2(nn+1)    uint16 lidx[4 ne]      (slot << 8 | element), element order
+//   (4-aligned)  uint32 nodes[nn]       global node id, bit 31 = owner
 //   size rounded up to 16.
 //
-// Waits on the mbarrier are bounded: a wait that gives up records an error
-// code in the batch's error word and the block stops (after waiting, again
-// bounded, for any copy it issued).
+// Every wait on an mbarrier is bounded: a wait that gives up records an error
+// code in the batch's error word; the block then issues no further copies and
+// drains, again bounded, the copies it has in flight. The CG loop stops at
+// the end of an iteration in which the error word is set.
 #include "batch.cuh"
 #include "batch_launch.h"
 #include "elem_math.cuh"
@@ -67,8 +90,8 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity)
     return ok != 0;
 }
 
-// Bounded wait: ~2^22 polls (each poll itself suspends for a hardware
-// time slice), far above any copy's latency.
+// Bounded wait: ~2^22 polls (each poll itself suspends for a hardware time
+// slice), far above any copy's latency.
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity)
 {
     for (uint32_t i = 0; i < (1u << 22); i++)
@@ -76,122 +99,247 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity
     return false;
 }
 
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e)
+{
+    s = a + b;
+    const float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+
+// Unevaluated sum hi + lo of two floats (about 48 significant bits). The
+// mixed path keeps its reductions in FP32 this way: GB300's FP64 pipe runs
+// at a small fraction of the FP32 rate, and even a block's reduction tree
+// in FP64 shows up in a kernel's time. Every tree below is fixed, so a sum
+// does not depend on scheduling.
+struct F2 {
+    float hi, lo;
+};
+
+__device__ __forceinline__ F2 f2_add(F2 a, F2 b)
+{
+    float s, e;
+    two_sum(a.hi, b.hi, s, e);
+    e += a.lo + b.lo;
+    F2 r;
+    r.hi = s + e;
+    r.lo = e - (r.hi - s);
+    return r;
+}
+
+__device__ __forceinline__ F2 warp_sum_f2(F2 v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        F2 w;
+        w.hi = __shfl_down_sync(0xffffffffu, v.hi, o);
+        w.lo = __shfl_down_sync(0xffffffffu, v.lo, o);
+        v = f2_add(v, w);
+    }
+    return v;
+}
+
+// Block sum, result valid in thread 0; every thread must call it.
+__device__ __forceinline__ F2 block_sum_f2(F2 v, float2* sh)
+{
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    __syncthreads();
+    v = warp_sum_f2(v);
+    if (lane == 0) sh[wid] = make_float2(v.hi, v.lo);
+    __syncthreads();
+    if (wid == 0) {
+        const float2 w = (lane < (int)(blockDim.x >> 5)) ? sh[lane] : make_float2(0.f, 0.f);
+        v.hi = w.x;
+        v.lo = w.y;
+        v = warp_sum_f2(v);
+    }
+    return v;
+}
+
+// Fixed-order sum of n (hi, lo) partials, result valid in thread 0.
+__device__ __forceinline__ F2 sum_partials_f2(const float2* __restrict__ p, uint32_t n, float2* sh)
+{
+    F2 a = {0.f, 0.f};
+    for (uint32_t k = threadIdx.x; k < n; k += blockDim.x) {
+        const float2 w = __ldcg(p + k);
+        a = f2_add(a, F2{w.x, w.y});
+    }
+    return block_sum_f2(a, sh);
+}
+
+// Arrival of a block on a counter: the values other blocks must see are
+// written by thread 0, which alone fences before arriving; the last arrival
+// resets the counter. Every thread must call it.
+__device__ __forceinline__ bool arrive_last_t(unsigned* ctr, unsigned expected, unsigned* s_last)
+{
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        const unsigned prev = atomicAdd(ctr, 1u);
+        *s_last = (prev + 1u == expected) ? 1u : 0u;
+        if (*s_last) {
+            *ctr = 0u;
+            __threadfence();
+        }
+    }
+    __syncthreads();
+    return *s_last != 0;
+}
+
+// CG loop test (ILSS_CG.h:76-77, 140-143)
+__device__ __forceinline__ bool cg_cont_t(const StepScalars& s)
+{
+    return s.delta_new > s.abs_eps_sq && s.delta_new > s.delta_target && s.k < s.max_iter;
+}
+
+__device__ __forceinline__ void finish_stats_t(StepScalars& s)
+{
+    s.rel_residual = (s.delta_0 > 0) ? ::sqrt(s.delta_new / s.delta_0) : 0.0;
+    s.abs_residual = ::sqrt(s.delta_new);
+}
+
 }  // namespace
 
 constexpr uint32_t kStageBytes = 26240;  // >= blob_bytes(256, 256), multiple of 128
 static_assert(kStageBytes >= 26128, "stage must hold the largest tile blob");
 
-__device__ __forceinline__ void cp_async4(void* dst, const void* src)
+// Shared memory: two blob stages, the staged direction sd4[256], the
+// element outputs so4[4][256] (slot-major), two mbarriers and the warps'
+// (hi, lo) shares.
+constexpr uint32_t kPipeSmem = 2 * kStageBytes + 16u * (kTileNodes + 4 * kTileElems) + 16u + 8u * 8u;
+
+// What a block needs to know of one tile before its blob arrives.
+struct TileLook {
+    uint32_t mesh, n0, nenn;  // nenn: ne | nn << 16
+    uint32_t boff;            // blob offset / 16
+    uint32_t g;               // global node id of this thread's local node
+    float beta;               // beta of the tile's mesh
+    bool act;                 // tile exists and its mesh is iterating
+};
+
+__device__ __forceinline__ void look_meta(const BatchView<float>& b, uint32_t t, TileLook& L)
 {
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_addr(dst)), "l"(src) : "memory");
+    L.act = t < b.ntiles;
+    if (L.act) {
+        const TileMeta tm = b.tiles[t];
+        L.mesh = tm.mesh;
+        L.n0 = tm.n0;
+        L.nenn = (uint32_t)tm.ne | ((uint32_t)tm.nn << 16);
+    }
 }
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
 
-// Shared memory: two blob stages, two gather stages (d and r of each local
-// node, [6][256] floats), the staged direction sd4 and the outputs so4.
-constexpr uint32_t kGatherBytes = 6u * kTileNodes * 4u;
+// Second half of a look-up: the loads that depend on the tile's metadata.
+__device__ __forceinline__ void look_resolve(const BatchView<float>& b, uint32_t t, TileLook& L)
+{
+    if (!L.act) return;
+    const StepScalars& st = b.st[L.mesh];
+    L.act = !st.done;
+    L.beta = st.beta_f;
+    L.boff = b.blob_off16[t];
+    L.g = threadIdx.x < (L.nenn >> 16) ? __ldg(b.tile_nodes + L.n0 + threadIdx.x) : 0u;
+}
 
-__global__ void __launch_bounds__(256) k_tile_spmv_pipe(BatchView<float> b, const float* __restrict__ dvec,
-                                                        const float* __restrict__ rvec, float* __restrict__ part,
-                                                        cudaGraphConditionalHandle if_refresh, int set_if,
-                                                        const unsigned* __restrict__ refresh_flag,
-                                                        unsigned* __restrict__ err)
+__global__ void __launch_bounds__(256, 3) k_tile_spmv_pipe(BatchView<float> b, const float* __restrict__ dvec,
+                                                           const float* __restrict__ rvec, float* __restrict__ part,
+                                                           float2* __restrict__ tshare,
+                                                           cudaGraphConditionalHandle if_refresh, int set_if,
+                                                           const unsigned* __restrict__ refresh_flag,
+                                                           unsigned* __restrict__ err)
 {
     extern __shared__ __align__(128) unsigned char smem[];
-    float* gbuf = reinterpret_cast<float*>(smem + 2 * kStageBytes);           // [2][6][256]
-    float4* sd4 = reinterpret_cast<float4*>(smem + 2 * kStageBytes + 2 * kGatherBytes);
-    float4* so4 = sd4 + kTileNodes;  // slot-major: so4[slot * 256 + element]
+    float4* sd4 = reinterpret_cast<float4*>(smem + 2 * kStageBytes);
+    float4* so4 = sd4 + kTileNodes;  // so4[slot * 256 + element]
     uint64_t* bar = reinterpret_cast<uint64_t*>(so4 + 4 * kTileElems);
+    float2* wsh = reinterpret_cast<float2*>(bar + 2);  // [8] per-warp shares
+    const uint32_t G = gridDim.x, tid = threadIdx.x;
 
-    if (set_if && blockIdx.x == 0 && threadIdx.x == 0) cudaGraphSetConditional(if_refresh, *refresh_flag ? 1u : 0u);
-    if (threadIdx.x == 0) {
+    if (set_if && blockIdx.x == 0 && tid == 0) cudaGraphSetConditional(if_refresh, *refresh_flag ? 1u : 0u);
+    if (tid == 0) {
         mbar_init(&bar[0], 1);
         mbar_init(&bar[1], 1);
         fence_mbar_init();
     }
     __syncthreads();
 
-    auto active = [&](uint32_t t) -> bool { return t < b.ntiles && !b.st[b.tiles[t].mesh].done; };
-    auto issue_blob = [&](uint32_t t, int s) {
-        const TileMeta tm = b.tiles[t];
-        const uint32_t bytes = blob_bytes(tm.ne, tm.nn);
-        mbar_expect_tx(&bar[s], bytes);
-        bulk_copy_g2s(smem + s * kStageBytes, b.blob + 16ull * b.blob_off16[t], bytes, &bar[s]);
-    };
-    // d and r of local node i of a tile into gather stage s (this thread's copies)
-    auto issue_gather = [&](uint32_t g, int s) {
-        float* gs = gbuf + s * 6 * kTileNodes + threadIdx.x;
-        const float* dp = dvec + 3 * (size_t)g;
-        const float* rp = rvec + 3 * (size_t)g;
-        cp_async4(gs, dp);
-        cp_async4(gs + kTileNodes, dp + 1);
-        cp_async4(gs + 2 * kTileNodes, dp + 2);
-        cp_async4(gs + 3 * kTileNodes, rp);
-        cp_async4(gs + 4 * kTileNodes, rp + 1);
-        cp_async4(gs + 5 * kTileNodes, rp + 2);
-    };
-
-    uint32_t phase = 0u;    // bit s: parity of stage s's next completion
-    uint32_t pending = 0u;  // bit s: a bulk copy into stage s is in flight
+    // Software pipeline over this block's tiles t, t+G, t+2G, ...: while tile
+    // t is computed, the blob of t+G is in flight (bulk copy) together with
+    // this thread's gather of d and r for its local node of t+G, and the
+    // metadata of t+2G is looked up.
     uint32_t t = blockIdx.x;
-    bool act = active(t);
-    if (act) {
-        const TileMeta tm = b.tiles[t];
-        if (threadIdx.x == 0) issue_blob(t, 0);
-        pending |= 1u;
-        if (threadIdx.x < tm.nn) issue_gather(b.tile_nodes[tm.n0 + threadIdx.x], 0);
-    }
-    cp_async_commit();
+    TileLook cur, nxt, n2;
+    look_meta(b, t, cur);
+    look_resolve(b, t, cur);
+    look_meta(b, t + G, nxt);
+    look_resolve(b, t + G, nxt);
+    uint32_t phase = 0u;    // bit s: parity of stage s's next completion
+    uint32_t pending = 0u;  // bit s: a copy into stage s is in flight
     int s = 0;
     bool failed = false;
-    for (; t < b.ntiles; t += gridDim.x) {
-        const uint32_t tn = t + gridDim.x;
-        // after a failed wait no new copies are issued
-        const bool actn = !failed && active(tn);
-        TileMeta tmn;
-        uint32_t gn = 0;
-        if (actn) {
-            tmn = b.tiles[tn];
-            if (threadIdx.x == 0) issue_blob(tn, s ^ 1);
-            pending |= 1u << (s ^ 1);
-            if (threadIdx.x < tmn.nn) gn = b.tile_nodes[tmn.n0 + threadIdx.x];  // used after this tile's compute
+    auto issue = [&](const TileLook& L, int st) {
+        const uint32_t ne = L.nenn & 0xffffu, nn = L.nenn >> 16;
+        const uint32_t bytes = blob_bytes(ne, nn);
+        mbar_expect_tx(&bar[st], bytes);
+        bulk_copy_g2s(smem + st * kStageBytes, b.blob + 16ull * L.boff, bytes, &bar[st]);
+    };
+    float cd0 = 0.f, cd1 = 0.f, cd2 = 0.f, cr0 = 0.f, cr1 = 0.f, cr2 = 0.f;
+    if (cur.act) {
+        if (tid == 0) issue(cur, 0);
+        pending |= 1u;
+        if (tid < (cur.nenn >> 16)) {
+            const size_t g = 3 * (size_t)cur.g;
+            cd0 = __ldg(dvec + g); cd1 = __ldg(dvec + g + 1); cd2 = __ldg(dvec + g + 2);
+            cr0 = __ldg(rvec + g); cr1 = __ldg(rvec + g + 1); cr2 = __ldg(rvec + g + 2);
         }
-        if (act) {
+    }
+    for (; t < b.ntiles; t += G) {
+        look_meta(b, t + 2 * G, n2);  // resolved after the element products
+        float nd0 = 0.f, nd1 = 0.f, nd2 = 0.f, nr0 = 0.f, nr1 = 0.f, nr2 = 0.f;
+        if (!failed && nxt.act) {  // after a failed wait no new copies are issued
+            if (tid == 0) issue(nxt, s ^ 1);
+            pending |= 1u << (s ^ 1);
+            if (tid < (nxt.nenn >> 16)) {
+                const size_t g = 3 * (size_t)nxt.g;
+                nd0 = __ldg(dvec + g); nd1 = __ldg(dvec + g + 1); nd2 = __ldg(dvec + g + 2);
+                nr0 = __ldg(rvec + g); nr1 = __ldg(rvec + g + 1); nr2 = __ldg(rvec + g + 2);
+            }
+        }
+        if (cur.act) {
             // every thread polls; the block agrees on the outcome so the
             // barriers below stay uniform
             const bool ok = !failed && mbar_wait_bounded(&bar[s], (phase >> s) & 1u);
             if (__syncthreads_or(!ok)) {
-                if (!failed && threadIdx.x == 0) atomicExch(err, 1u);
+                if (!failed && tid == 0) atomicExch(err, 1u);
                 failed = true;
             } else {
                 phase ^= 1u << s;
                 pending &= ~(1u << s);
             }
         }
-        const TileMeta tm = b.tiles[t < b.ntiles ? t : 0];
-        if (act && !failed) {
-            cp_async_wait_all();  // this thread's gathers of tile t
-            __syncthreads();
-            const float beta = (float)b.st[tm.mesh].beta;
-            const float* gs = gbuf + s * 6 * kTileNodes;
-            if (threadIdx.x < tm.nn) {
-                const int i = threadIdx.x;
-                sd4[i] = make_float4(__fmaf_rn(beta, gs[i], gs[3 * kTileNodes + i]),
-                                     __fmaf_rn(beta, gs[kTileNodes + i], gs[4 * kTileNodes + i]),
-                                     __fmaf_rn(beta, gs[2 * kTileNodes + i], gs[5 * kTileNodes + i]), 0.f);
+        if (cur.act && !failed) {
+            const uint32_t ne = cur.nenn & 0xffffu, nn = cur.nenn >> 16;
+            const MeshConsts& c = b.mc[cur.mesh];
+            const float fK = c.fK_f, mfm = c.mfm_f;
+            const unsigned char* stage = smem + s * kStageBytes;
+            const uint32_t ne4 = blob_ne4(ne);
+            const float* comp = reinterpret_cast<const float*>(stage);
+            const uint16_t* lp = reinterpret_cast<const uint16_t*>(stage + blob_lptr_off(ne));
+            const uint16_t* li = lp + (nn + 1);
+            const uint32_t* nodes = reinterpret_cast<const uint32_t*>(stage + blob_nodes_off(ne, nn));
+            float share = 0.f;  // this thread's part of the tile's d^T A d
+            if (tid < nn) {
+                const float dx = __fmaf_rn(cur.beta, cd0, cr0);
+                const float dy = __fmaf_rn(cur.beta, cd1, cr1);
+                const float dz = __fmaf_rn(cur.beta, cd2, cr2);
+                sd4[tid] = make_float4(dx, dy, dz, 0.f);
+                if (nodes[tid] >> 31) share = mfm * (dx * dx + dy * dy + dz * dz);
             }
             __syncthreads();
-            const unsigned char* stage = smem + s * kStageBytes;
-            const uint32_t ne4 = blob_ne4(tm.ne);
-            const float* comp = reinterpret_cast<const float*>(stage);
-            if (threadIdx.x < tm.ne) {
-                const int i = threadIdx.x;
+            if (tid < ne) {
+                const int i = tid;
                 float R[9], Di[9];
 #pragma unroll
-                for (int c = 0; c < 9; c++) R[c] = comp[c * ne4 + i];
+                for (int k = 0; k < 9; k++) R[k] = comp[k * ne4 + i];
 #pragma unroll
-                for (int c = 0; c < 9; c++) Di[c] = comp[(9 + c) * ne4 + i];
+                for (int k = 0; k < 9; k++) Di[k] = comp[(9 + k) * ne4 + i];
                 const float k1 = comp[18 * ne4 + i], knu = comp[19 * ne4 + i], k2 = comp[20 * ne4 + i];
                 const uint32_t lw = reinterpret_cast<const uint32_t*>(comp)[21 * ne4 + i];
                 const int ids[4] = {(int)(lw & 0xff), (int)((lw >> 8) & 0xff), (int)((lw >> 16) & 0xff),
@@ -206,50 +354,176 @@ __global__ void __launch_bounds__(256) k_tile_spmv_pipe(BatchView<float> b, cons
                 }
                 float out[12];
                 elem_RKRt<float>(R, Di, k1, knu, k2, dl, out);
+                float eq = 0.f;
+#pragma unroll
+                for (int k = 0; k < 12; k++) eq = __fmaf_rn(dl[k], out[k], eq);
+                share = __fmaf_rn(fK, eq, share);
 #pragma unroll
                 for (int k = 0; k < 4; k++)
                     so4[k * kTileElems + i] = make_float4(out[3 * k], out[3 * k + 1], out[3 * k + 2], 0.f);
             }
-        }
-        // the next tile's gathers go out while this tile reduces
-        if (actn && threadIdx.x < tmn.nn) issue_gather(gn, s ^ 1);
-        cp_async_commit();
-        if (act && !failed) {
+            look_resolve(b, t + 2 * G, n2);
             __syncthreads();
-            const unsigned char* stage = smem + s * kStageBytes;
-            const uint16_t* lp = reinterpret_cast<const uint16_t*>(stage + blob_lptr_off(tm.ne));
-            const uint16_t* li = lp + (tm.nn + 1);
-            if (threadIdx.x < tm.nn) {
-                const int i = threadIdx.x;
+            if (tid < nn) {
                 float a0 = 0.f, a1 = 0.f, a2 = 0.f;
-                for (int j = lp[i]; j < lp[i + 1]; j++) {
+                for (int j = lp[tid]; j < lp[tid + 1]; j++) {
                     const float4 v = so4[li[j]];
                     a0 += v.x;
                     a1 += v.y;
                     a2 += v.z;
                 }
-                const size_t o = 3 * (size_t)(tm.n0 + i);
+                const size_t o = 3 * (size_t)(cur.n0 + tid);
                 part[o] = a0;
                 part[o + 1] = a1;
                 part[o + 2] = a2;
             }
+            const F2 w = warp_sum_f2(F2{share, 0.f});
+            if ((tid & 31) == 0) wsh[tid >> 5] = make_float2(w.hi, w.lo);
+        } else {
+            look_resolve(b, t + 2 * G, n2);
         }
         __syncthreads();
-        act = actn;
+        if (cur.act && tid == 0) {
+            F2 a = {0.f, 0.f};
+            if (!failed)
+                for (int k = 0; k < (int)(blockDim.x >> 5); k++) a = f2_add(a, F2{wsh[k].x, wsh[k].y});
+            tshare[t] = make_float2(a.hi, a.lo);
+        }
+        cur = nxt;
+        nxt = n2;
+        cd0 = nd0; cd1 = nd1; cd2 = nd2;
+        cr0 = nr0; cr1 = nr1; cr2 = nr2;
         s ^= 1;
     }
-    // drain: every copy this block issued completes before it exits (bounded)
-    cp_async_wait_all();
     if (failed) {
         for (int k = 0; k < 2; k++)
             if ((pending >> k) & 1u) (void)mbar_wait_bounded(&bar[k], (phase >> k) & 1u);
     }
 }
 
-uint32_t tile_pipe_smem_bytes()
+__global__ void __launch_bounds__(256) k_node_update_fused(BatchView<float> b, const float* __restrict__ part,
+                                                           const float2* __restrict__ tshare,
+                                                           const double* __restrict__ part64,
+                                                           const double* __restrict__ bv,
+                                                           const double* __restrict__ y, float* __restrict__ r,
+                                                           float* __restrict__ d, float2* __restrict__ cshare,
+                                                           LoopSync ls)
 {
-    return 2 * kStageBytes + 2 * kGatherBytes + sizeof(float4) * (kTileNodes + 4 * kTileElems) + 2 * sizeof(uint64_t);
+    __shared__ float2 sh[32];
+    __shared__ unsigned s_last;
+    __shared__ float s_alpha;
+    __shared__ int s_brk;
+    __shared__ double s_dq;
+    const uint32_t ci = blockIdx.x;
+    const ChunkMeta ch = b.chunks[ci < b.nchunks ? ci : 0];
+    if (ci < b.nchunks && !b.st[ch.mesh].done) {
+        const MeshConsts& c = b.mc[ch.mesh];
+        const StepScalars& sm = b.st[ch.mesh];
+        // d^T A d of the mesh from its tiles' shares; every block of the mesh
+        // forms the same value (same partials, same order)
+        const F2 dq2 = sum_partials_f2(tshare + c.tile0, c.ntiles, sh);
+        if (threadIdx.x == 0) {
+            const double dq = (double)dq2.hi + (double)dq2.lo;
+            s_dq = dq;
+            s_brk = ::fabs(dq) < sm.abs_eps_sq;  // breakdown: leave before the update (ILSS_CG.h:97)
+            s_alpha = (float)(sm.delta_new / dq);
+        }
+        __syncthreads();
+        const bool brk = s_brk != 0;
+        const bool refresh = c.refresh_every > 0 && ((sm.k + 1) % c.refresh_every) == 0;
+        const float beta = sm.beta_f;
+        const float alpha_s = s_alpha, na = -alpha_s;
+        const float fK = c.fK_f, mfm = c.mfm_f;
+        float acc = 0.f;
+        for (size_t n = ch.n0 + threadIdx.x; !brk && n < ch.n1; n += blockDim.x) {
+            const size_t i = 3 * n;
+            if (b.fixed[n]) continue;  // d, r stay zero and y unchanged on constrained rows
+            const float d0 = __fmaf_rn(beta, d[i], r[i]);
+            const float d1 = __fmaf_rn(beta, d[i + 1], r[i + 1]);
+            const float d2 = __fmaf_rn(beta, d[i + 2], r[i + 2]);
+            float s0 = 0.f, s1 = 0.f, s2 = 0.f;
+            const uint32_t j1 = b.nptr[n + 1];
+            for (uint32_t j = b.nptr[n]; j < j1; j++) {
+                const size_t o = 3 * (size_t)b.nslot[j];
+                s0 += part[o];
+                s1 += part[o + 1];
+                s2 += part[o + 2];
+            }
+            const float q0 = fK * s0 + mfm * d0, q1 = fK * s1 + mfm * d1, q2 = fK * s2 + mfm * d2;
+            float r0 = r[i], r1 = r[i + 1], r2 = r[i + 2];
+            if (refresh) {
+                double t0 = 0, t1 = 0, t2 = 0;
+                for (uint32_t j = b.nptr[n]; j < j1; j++) {
+                    const size_t o = 3 * (size_t)b.nslot[j];
+                    t0 += part64[o];
+                    t1 += part64[o + 1];
+                    t2 += part64[o + 2];
+                }
+                const double mfm64 = c.mass * c.factor_M;
+                r0 = (float)(bv[i] - (c.factor_K * t0 + mfm64 * (y[i] + (double)b.ydelta[i])));
+                r1 = (float)(bv[i + 1] - (c.factor_K * t1 + mfm64 * (y[i + 1] + (double)b.ydelta[i + 1])));
+                r2 = (float)(bv[i + 2] - (c.factor_K * t2 + mfm64 * (y[i + 2] + (double)b.ydelta[i + 2])));
+            }
+            b.ydelta[i] += alpha_s * d0;
+            b.ydelta[i + 1] += alpha_s * d1;
+            b.ydelta[i + 2] += alpha_s * d2;
+            r0 += na * q0;
+            r1 += na * q1;
+            r2 += na * q2;
+            d[i] = d0; d[i + 1] = d1; d[i + 2] = d2;
+            r[i] = r0; r[i + 1] = r1; r[i + 2] = r2;
+            acc += r0 * r0 + r1 * r1 + r2 * r2;
+        }
+        const F2 rr = block_sum_f2(F2{acc, 0.f}, sh);
+        if (threadIdx.x == 0) cshare[ci] = make_float2(rr.hi, rr.lo);
+        if (arrive_last_t(ls.mcount + ch.mesh, c.nchunks, &s_last)) {
+            const F2 tot = sum_partials_f2(cshare + c.chunk0, c.nchunks, sh);
+            if (threadIdx.x == 0) {
+                StepScalars& st = b.st[ch.mesh];
+                st.dot_dq = s_dq;
+                if (brk) {
+                    st.done = 1;
+                    finish_stats_t(st);
+                } else {
+                    const double total = (double)tot.hi + (double)tot.lo;
+                    st.alpha = st.delta_new / s_dq;
+                    st.delta_old = st.delta_new;
+                    st.delta_new = total;
+                    st.beta = total / st.delta_old;
+                    st.beta_f = (float)st.beta;
+                    st.k += 1;
+                    st.total_iters += 1;
+                    if (total != total) st.status = 3u;
+                    st.done = cg_cont_t(st) ? 0u : 1u;
+                    if (st.done) finish_stats_t(st);
+                }
+            }
+        }
+    }
+    // last block of the grid: while condition and refresh flag
+    if (!arrive_last_t(ls.gcount, gridDim.x, &s_last)) return;
+    int any = 0, rf = 0;
+    for (uint32_t m = threadIdx.x; m < b.M; m += blockDim.x) {
+        volatile const StepScalars* sp = b.st + m;
+        if (!sp->done) {
+            any = 1;
+            const MeshConsts& c = b.mc[m];
+            if (c.refresh_every > 0 && ((sp->k + 1) % c.refresh_every) == 0) rf = 1;
+        }
+    }
+    any = __syncthreads_or(any);
+    rf = __syncthreads_or(rf);
+    if (threadIdx.x == 0) {
+        const bool stop = ls.err && *(volatile const unsigned*)ls.err;
+        if (ls.refresh_flag) *ls.refresh_flag = rf ? 1u : 0u;
+        if (ls.body_runs) *ls.body_runs += 1u;
+        if (ls.set_cond) cudaGraphSetConditional(ls.cond, (any && !stop) ? 1u : 0u);
+    }
 }
+
+// ---------------------------------------------------------------------------
+
+uint32_t tile_pipe_smem_bytes() { return kPipeSmem; }
 
 static int pipe_grid()
 {
@@ -258,9 +532,8 @@ static int pipe_grid()
         int dev = 0, sms = 0, per_sm = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaFuncSetAttribute(k_tile_spmv_pipe, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)tile_pipe_smem_bytes());
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tile_spmv_pipe, 256, tile_pipe_smem_bytes());
+        cudaFuncSetAttribute(k_tile_spmv_pipe, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPipeSmem);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tile_spmv_pipe, 256, kPipeSmem);
         if (sms <= 0) sms = 152;
         if (per_sm <= 0) per_sm = 1;
         grid = sms * per_sm;
@@ -268,15 +541,26 @@ static int pipe_grid()
     return grid;
 }
 
-void launch_tile_spmv_pipe(const BatchView<float>& b, const float* d, const float* r, float* part,
+void launch_tile_spmv_pipe(const BatchView<float>& b, const float* d, const float* r, float* part, float2* tshare,
                            cudaGraphConditionalHandle if_refresh, int set_if, const unsigned* refresh_flag,
                            unsigned* err, cudaStream_t s)
 {
     const int g = pipe_grid();
     const uint32_t grid = b.ntiles < (uint32_t)g ? (b.ntiles ? b.ntiles : 1) : (uint32_t)g;
     prof_begin("tile_spmv_mixed", s);
-    k_tile_spmv_pipe<<<grid, 256, tile_pipe_smem_bytes(), s>>>(b, d, r, part, if_refresh, set_if, refresh_flag, err);
+    k_tile_spmv_pipe<<<grid, 256, kPipeSmem, s>>>(b, d, r, part, tshare, if_refresh, set_if, refresh_flag, err);
     prof_end("tile_spmv_mixed", s);
+    launch_counter()++;
+}
+
+void launch_node_update_fused(const BatchView<float>& b, const float* part, const float2* tshare,
+                              const double* part64, const double* bv, const double* y, float* r, float* d,
+                              float2* cshare, const LoopSync& ls, cudaStream_t s)
+{
+    prof_begin("node_update_mixed", s);
+    k_node_update_fused<<<b.nchunks ? b.nchunks : 1, kNodeThreads, 0, s>>>(b, part, tshare, part64, bv, y, r, d,
+                                                                           cshare, ls);
+    prof_end("node_update_mixed", s);
     launch_counter()++;
 }
 
