@@ -41,8 +41,13 @@ UNIT = "tet·CG-iter/s"
 L2_BYTES = 129 * 1024 * 1024
 # algorithmic bytes of one element product (16 B of node ids + 20 element
 # scalars R, Dm^-1, V lambda, V mu) and per node of the direction read once
+# Algorithmic bytes of one element-product launch: per tet the ids (4 x
+# int32) and R (9), Dm^-1 (9), V lambda, V mu in the element type (16 + 20
+# s_e); per node d read and q written (6 s_v). One whole CG iteration touches
+# the node vectors 11 times (33 s_v per node, ITER_NODE).
 ALG_ELEM = {"mixed": 16 + 20 * 4, "fp64": 16 + 20 * 8}
-ALG_NODE = {"mixed": 3 * 4, "fp64": 3 * 8}
+ALG_NODE = {"mixed": 6 * 4, "fp64": 6 * 8}
+ITER_NODE = {"mixed": 33 * 4, "fp64": 33 * 8}
 
 
 # ---------------------------------------------------------------- workloads
@@ -134,17 +139,20 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def profiled_traffic(kernel: str, workload_name: str):
-    """Per-launch DRAM bytes of `kernel` from the committed ncu summary, if any."""
+def profiled_traffic(kernel: str, workload_name: str, tets_per_launch: float):
+    """Per-launch DRAM bytes of `kernel` from the committed ncu summary, if any:
+    either a per-launch figure or a per-tet figure (a capture on a smaller
+    batch) scaled by the tets a launch processes."""
     path = os.path.join(ROOT, "profiles", f"{kernel}_{workload_name}.md")
     if not os.path.exists(path):
         return None
     for line in open(path):
-        if line.startswith("traffic_bytes_per_launch:"):
-            try:
-                return float(line.split(":", 1)[1].split()[0])
-            except ValueError:
-                return None
+        for key, scale in (("traffic_bytes_per_launch:", 1.0), ("traffic_bytes_per_tet:", tets_per_launch)):
+            if line.startswith(key):
+                try:
+                    return float(line.split(":", 1)[1].split()[0]) * scale
+                except ValueError:
+                    return None
     return None
 
 
@@ -345,6 +353,10 @@ def run_ours(args):
               for sc, it in zip(scs, prof_iters))
     avg_launch_s = (k_ms * 1e-3) / max(k_n, 1)
     alg_per_launch = alg / max(k_n, 1)
+    tets_per_launch = sum(it * sc.num_tets for sc, it in zip(scs, prof_iters)) / max(k_n, 1)
+    # the whole CG iteration against the same peak: 11 vector touches per node
+    iter_bytes_per_tet_iter = sum(ALG_ELEM[precision] * sc.num_tets + ITER_NODE[precision] * sc.num_nodes
+                                  for sc in scs) / sum(sc.num_tets for sc in scs)
     achieved = alg_per_launch / avg_launch_s / 1e9 if avg_launch_s > 0 else 0.0
     peak, peak_kind = measured_peaks()
 
@@ -396,6 +408,7 @@ def run_ours(args):
             "data": "synthetic",
             "config": {"workload": describe(args.workload, scs, precision), "meshes": len(scs),
                        "tets": info["tets"], "nodes": info["nodes"], "tiles": info["tiles"],
+                       "device_bytes": info["device_bytes"],
                        "parallelism": "replicas only" if ws > 1 else "1 GPU",
                        "l2": f"inputs larger than L2: {elem_bytes / 1e6:.0f} MB of element data streamed per CG "
                              f"iteration vs {L2_BYTES / 1e6:.0f} MB L2",
@@ -408,9 +421,15 @@ def run_ours(args):
                     "note": "fem_batch_step_host: all states up, one step, all states down, wall clock"},
             "gpu_launches": launches,
             "roofline": {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": profiled_traffic(kname, args.workload),
+                         "frac": achieved / peak,
+                         "traffic": profiled_traffic(kname, args.workload, tets_per_launch),
                          "peak_kind": peak_kind, "alg_bytes_per_launch": alg_per_launch,
                          "avg_launch_us": avg_launch_s * 1e6, "launches": int(k_n)},
+            "roofline_iteration": {"bound": "hbm", "bytes_per_tet_iter": iter_bytes_per_tet_iter,
+                                   "achieved": value * iter_bytes_per_tet_iter / 1e9, "peak": peak,
+                                   "unit": "GB/s", "frac": value * iter_bytes_per_tet_iter / 1e9 / peak,
+                                   "note": "whole-job tet.CG-iter/s x algorithmic bytes of one CG "
+                                           "iteration (16 + 20 s_e per tet + 33 s_v per node)"},
             "plain_fp64_gpu": plain,
             "cpu_baseline": cpu,
         }
