@@ -143,6 +143,19 @@ int fem_solid_energy(fem_solid s, double* V);
 /* Uniform node mass and Rayleigh coefficients (RebuildMass, RebuildRayleighCoeffsFromFreqs). */
 int fem_solid_mass_info(fem_solid s, double* node_mass, double* rayleigh2, double* total_volume);
 
+/* No counterpart in the reference. The product of fem_solid_apply_A with its
+ * per-element scratch in a static device array (12 doubles per tet, at most
+ * FEM_NOALLOC_MAX_TETS tets: 6 MiB per device) instead of a device buffer,
+ * for callers that cannot allocate device memory when they call it (a
+ * fixed-rate control loop that cudaMalloc's implicit synchronisation would
+ * stall, a process whose device memory another allocator has reserved). It
+ * calls no allocating routine. Larger solids fail with FEM_E_ARG. All calls
+ * on a device share the array: calls that overlap on the GPU race, so
+ * serialise them. The first call on a device looks up the array's address;
+ * make it before any stream capture on that device. */
+#define FEM_NOALLOC_MAX_TETS 65536u
+int fem_solid_apply_A_noalloc(fem_solid s, double factor_M, double factor_K, const double* d, double* q);
+
 /* --- Device-resident timing hooks (state stays in HBM) --- */
 /* Enqueue nsteps on the handle's stream without synchronising and without
  * host copies; stats are left on the device. */

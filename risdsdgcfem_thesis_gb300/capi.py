@@ -85,6 +85,7 @@ SIGNATURES = {
     "fem_solid_apply_A": (C.c_int, [C.c_void_p, C.c_double, C.c_double, _dp, _dp]),
     "fem_solid_energy": (C.c_int, [C.c_void_p, _dp]),
     "fem_solid_mass_info": (C.c_int, [C.c_void_p, _dp, _dp, _dp]),
+    "fem_solid_apply_A_noalloc": (C.c_int, [C.c_void_p, C.c_double, C.c_double, _dp, _dp]),
     "fem_solid_step_async": (C.c_int, [C.c_void_p, C.c_uint32]),
     "fem_solid_synchronize": (C.c_int, [C.c_void_p, C.POINTER(FemStepStats)]),
     "fem_solid_stream": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),

@@ -18,6 +18,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <string>
 #include <vector>
@@ -621,3 +622,78 @@ int fem_solid_mass_info(fem_solid s, double* node_mass, double* rayleigh2, doubl
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// fem_solid_apply_A_noalloc: the product of fem_solid_apply_A with its
+// per-element scratch (12 doubles per tet, written by the element kernel and
+// gathered per node) in a static device array instead of the solid's own
+// buffer. It is meant for callers that cannot allocate device memory when
+// they call it: a fixed-rate control or haptics loop, where cudaMalloc's
+// implicit device synchronisation and unbounded latency would break the
+// loop's deadline, or a process whose device memory is already reserved by
+// another allocator (a framework's caching allocator, say). It calls no
+// cudaMalloc, cudaFree or other allocating CUDA, torch or library routine.
+//
+// Limits and sharing:
+//   * at most FEM_NOALLOC_MAX_TETS tets (the array is 12 * 65536 doubles,
+//     6 MiB, per device); larger solids are rejected with FEM_E_ARG;
+//   * every call on a device uses the same array, which keeps the last
+//     call's contents. Nothing in it has to start at zero: the element
+//     kernel writes all 12 T entries before the gather reads them. Calls
+//     whose work overlaps on the GPU (several host threads calling at once,
+//     on solids whose streams run concurrently) race on the array: serialise
+//     them;
+//   * the first call on a device (with that device current) looks up the
+//     array's device address once (cudaGetSymbolAddress); make that first
+//     call before any stream capture on that device.
+namespace {
+
+static __device__ __align__(256) double g_apply_scratch[12ull * FEM_NOALLOC_MAX_TETS];
+
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_apply_scratch_mu;
+double* g_apply_scratch_ptr[kNoAllocMaxDevices] = {};
+
+// Device address of the static scratch on the current device (set-up once
+// per device, under a lock).
+int apply_scratch(double** out)
+{
+    int dev = 0;
+    CK(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kNoAllocMaxDevices)
+        return fail(FEM_E_ARG, "device %d is beyond the %d devices of the static scratch table", dev,
+                    kNoAllocMaxDevices);
+    std::lock_guard<std::mutex> lock(g_apply_scratch_mu);
+    if (!g_apply_scratch_ptr[dev]) {
+        void* p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_apply_scratch);
+        if (e != cudaSuccess)
+            return fail(FEM_E_CUDA, "cudaGetSymbolAddress of the static scratch on device %d: %s", dev,
+                        cudaGetErrorString(e));
+        g_apply_scratch_ptr[dev] = static_cast<double*>(p);
+    }
+    *out = g_apply_scratch_ptr[dev];
+    return FEM_OK;
+}
+
+}  // namespace
+
+extern "C" int fem_solid_apply_A_noalloc(fem_solid s, double factor_M, double factor_K, const double* d, double* q)
+{
+    if (int e = check_handle(s)) return e;
+    if (!d || !q) return fail(FEM_E_ARG, "null arrays");
+    if (s->T > FEM_NOALLOC_MAX_TETS)
+        return fail(FEM_E_ARG, "solid has %u tets; fem_solid_apply_A_noalloc takes at most %u (static scratch)",
+                    s->T, (unsigned)FEM_NOALLOC_MAX_TETS);
+    double* scratch = nullptr;
+    if (int e = apply_scratch(&scratch)) return e;
+    MeshView<double> m = s->view();
+    m.eout = scratch;
+    const size_t bytes = sizeof(double) * 3 * (size_t)s->N;
+    CK(cudaMemcpyAsync(s->d.p, d, bytes, cudaMemcpyHostToDevice, s->stream));
+    launch_elem_spmv_fp64(m, s->d.p, s->st.p, 0, s->stream);
+    launch_apply_A_fp64(m, factor_M, factor_K, s->node_mass, s->d.p, s->q.p, s->stream);
+    CK(cudaMemcpyAsync(q, s->q.p, bytes, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return FEM_OK;
+}
