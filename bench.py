@@ -382,7 +382,10 @@ def run_ours(args):
 
     plain = None
     cpu = None
+    served = None
     if rank == 0 and ws == 1:
+        if not args.no_served:
+            served = served_leg(args.served_rate, args.served_seconds, pool_count=args.served_pool)
         if not args.no_plain:
             plain = plain_fp64_comparator(3)
         if not args.no_cpu:
@@ -432,6 +435,7 @@ def run_ours(args):
                                            "iteration (16 + 20 s_e per tet + 33 s_v per node)"},
             "plain_fp64_gpu": plain,
             "cpu_baseline": cpu,
+            "served": served,
         }
         if plain:
             line["speedup_vs_plain_fp64_gpu"] = value / plain["value"]
@@ -440,6 +444,67 @@ def run_ours(args):
         torch.distributed.barrier()
         torch.distributed.destroy_process_group()
     return 0
+
+
+# ---------------------------------------------------------------- served leg
+def served_leg(rate, seconds, pool_count=4096, seed=0, budget=120 << 30, deadline_ms=1000.0 / 60.0):
+    """Step requests over a resident pool through the server (fem_server_*):
+    `pool_count` scenes of log-uniform 200..200k tets admitted under a device
+    budget, Poisson arrivals at `rate` requests/s for `seconds` on scenes
+    drawn uniformly, continuous batching; then the same at 60 % of the
+    completion rate the first run sustained. Latency is submit -> completion
+    seen by the host loop."""
+    from risdsdgcfem_thesis_gb300 import capi, scenes
+    t0 = time.perf_counter()
+    pool = scenes.served_pool(pool_count, seed)
+    srv = capi.Server(precision=capi.FEM_PRECISION_MIXED, hbm_budget_bytes=budget)
+    for sc in pool:
+        srv.add(sc)
+    admitted = srv.admit()
+    setup_s = time.perf_counter() - t0
+    st = srv.status()
+    resident = np.array(srv.resident(), dtype=np.int64)
+    tets = np.array([sc.num_tets for sc in pool], dtype=np.float64)
+    # warm-up: every resident scene steps once
+    for i in resident:
+        srv.submit(int(i))
+    srv.drain()
+
+    def run(r, secs, rs):
+        n = int(rs.poisson(r * secs))
+        times = np.sort(rs.uniform(0.0, secs, n))
+        which = resident[rs.integers(0, len(resident), n)]
+        done, k = [], 0
+        t_start = time.perf_counter()
+        while k < n:
+            now = time.perf_counter() - t_start
+            while k < n and times[k] <= now:
+                srv.submit(int(which[k]), k)
+                k += 1
+            done += srv.pump()
+        done += srv.drain()
+        wall = time.perf_counter() - t_start
+        lat = np.array([c["latency_us"] for c in done]) / 1e3
+        units = float(sum(tets[c["scene"]] * c["cg_iterations"] for c in done))
+        return {"offered_per_s": r, "seconds": secs, "requests": n, "completed": len(done), "wall_s": wall,
+                "completed_per_s": len(done) / wall, "tet_cg_iter_per_s": units / wall,
+                "p50_ms": float(np.percentile(lat, 50)) if len(lat) else None,
+                "p99_ms": float(np.percentile(lat, 99)) if len(lat) else None,
+                "within_deadline": float(np.mean(lat <= deadline_ms)) if len(lat) else None,
+                "mean_cg_iterations": float(np.mean([c["cg_iterations"] for c in done])) if done else None,
+                "errors": int(sum(1 for c in done if c["status"] != 0))}
+
+    rs = np.random.default_rng(seed + 1)
+    offered = run(rate, seconds, rs)
+    sustain_rate = 0.6 * offered["completed_per_s"]
+    sustained = run(sustain_rate, seconds, rs)
+    st2 = srv.status()
+    srv.close()
+    return {"pool": f"{pool_count} scenes, 5*a*b*c blocks of log-uniform 200..200k tets "
+                    f"({int(tets.sum())} tets), mixed precision, CG rel 1e-6, max 500",
+            "budget_bytes": budget, "admitted": admitted, "device_bytes": st["device_bytes"],
+            "shards": st["shards"], "max_busy_shards": st2["max_busy_shards"], "setup_s": round(setup_s, 1),
+            "deadline_ms": deadline_ms, "at_offered_rate": offered, "at_60pct_of_capacity": sustained}
 
 
 def main():
@@ -452,6 +517,10 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-graph", action="store_true", help="launch kernels one by one (for per-kernel profilers)")
+    ap.add_argument("--no-served", action="store_true")
+    ap.add_argument("--served-rate", type=float, default=20000.0, help="offered step requests per second")
+    ap.add_argument("--served-seconds", type=float, default=3.0)
+    ap.add_argument("--served-pool", type=int, default=4096)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":

@@ -208,8 +208,22 @@ int fem_batch_get_state_all(fem_batch b, double* x, double* v);
 /* Host-buffer round trip: upload all states (null = keep), step, download. */
 int fem_batch_step_host(fem_batch b, const double* x_in, const double* v_in, uint32_t nsteps, double* x_out,
                         double* v_out);
-/* Which solids take part in the next steps (M bytes, 1 = step); null = all. */
+/* Which solids take part in the next launches (M bytes; null = all start):
+ * 1 = start a step, 2 = continue a step that an iteration budget
+ * (fem_batch_set_slice) interrupted, 0 = leave out (an interrupted step left
+ * out is dropped). fem_batch_get_stats' `status`/`cg_iterations` then say
+ * where each solid stands; a solid's step is complete when its CG loop has
+ * ended (fem_batch_finished). */
 int fem_batch_set_active(fem_batch b, const uint8_t* mask);
+/* Iteration budget of each following launch (0 = run every CG loop to its
+ * end, the default). With a budget, a launch stops after that many CG
+ * iterations; solids whose loop has not ended continue in a later launch
+ * (mask value 2) with bit-identical results. */
+int fem_batch_set_slice(fem_batch b, uint32_t max_iterations);
+/* Per solid (M bytes): 1 if its CG loop ended, and its step was integrated,
+ * in the last launch; 2 if its loop is still running; 0 otherwise. As of
+ * the last synchronize. */
+int fem_batch_finished(fem_batch b, uint8_t* flags);
 int fem_batch_step_async(fem_batch b, uint32_t nsteps);
 int fem_batch_synchronize(fem_batch b);
 int fem_batch_step(fem_batch b, uint32_t nsteps);
@@ -220,6 +234,84 @@ int fem_batch_stream(fem_batch b, void** stream);
  * runs are counted on the device). */
 int fem_batch_kernel_launches(fem_batch b, uint32_t steps, uint64_t* launches);
 int fem_batch_reset_launch_count(fem_batch b);
+
+/* --- Serving: step requests over device-resident scenes ---
+ *
+ * The reference steps a solid when its owner asks (bs::Solid3D::Update,
+ * bs/Solid3D.cpp:61-104) and several solids one after another
+ * (SS_AggregateDSH_Basic.cpp:229-300). A server keeps many scenes resident
+ * on the GPU and serves requests of one FixedStep each:
+ *  - scenes are registered, then admitted into device memory by
+ *    fem_server_admit while the device bytes stay within hbm_budget_bytes;
+ *    admitted scenes are grouped by size into shards (batches);
+ *  - fem_server_submit queues a request; fem_server_pump (never blocking)
+ *    harvests every shard launch that has finished, completes the requests
+ *    whose step ended, and at once relaunches every idle shard that has
+ *    steps running or requests waiting. A launch runs at most
+ *    slice_iterations CG iterations: steps in flight continue in the next
+ *    launch and requests that arrived meanwhile start there, so a request
+ *    waits at most one slice to join; shards run concurrently on their own
+ *    streams (continuous batching at CG-iteration granularity);
+ *  - a scene's result is the same alone and in the mix (bit-identical).
+ * A server is used from one host thread at a time. */
+typedef struct fem_server_s* fem_server;
+
+typedef struct fem_server_options {
+    uint32_t precision;          /* enum fem_precision of every scene */
+    uint32_t shard_max_scenes;   /* scenes per shard */
+    uint64_t shard_max_tets;     /* tets per shard */
+    uint64_t hbm_budget_bytes;   /* device bytes the resident scenes may hold */
+    uint32_t slice_iterations;   /* CG iterations per shard launch; running steps
+                                    continue in the next launch, requests that
+                                    arrived meanwhile start there (0 = whole steps) */
+    uint32_t pad;
+} fem_server_options;
+
+typedef struct fem_server_completion {
+    uint64_t tag;            /* as given to fem_server_submit */
+    uint32_t scene;
+    uint32_t status;         /* enum fem_status of the step */
+    uint32_t cg_iterations;
+    uint32_t fp64_resolved;  /* mixed: rotations re-solved in FP64 in that step */
+    double latency_us;       /* submit -> completion seen by fem_server_pump */
+    double queue_us;         /* submit -> the launch that started its step */
+    double device_us;        /* device time of the shard launches its step took part
+                                in (shared with the other scenes of those launches) */
+} fem_server_completion;
+
+typedef struct fem_server_status {
+    uint32_t resident_scenes, waiting_scenes, shards, busy_shards, max_busy_shards, pad;
+    uint64_t device_bytes;      /* bytes held by the resident shards */
+    uint64_t pending_requests;  /* submitted and not yet completed */
+} fem_server_status;
+
+/* Defaults: mixed precision, 2048 scenes and 3.2e7 tets per shard, 120 GiB,
+ * 32 CG iterations per launch. */
+int fem_server_options_default(fem_server_options* o);
+int fem_server_create(const fem_server_options* opt, fem_server* out);
+int fem_server_destroy(fem_server s);
+/* Registers a scene (same inputs as fem_solid_create plus its position
+ * constraints); it waits on the host until admitted. */
+int fem_server_add_scene(fem_server s, const double* rest_xyz, uint32_t N, const uint32_t* tets, uint32_t T,
+                         const fem_params* params, const double* young_per_elem, const double* poisson_per_elem,
+                         const uint32_t* knc_nodes, const double* knc_targets, uint32_t knc_count,
+                         uint32_t* scene);
+/* Admits waiting scenes (smallest first) while the budget allows. */
+int fem_server_admit(fem_server s, uint32_t* admitted);
+/* Frees a scene with no request pending; a shard's memory is released when
+ * its last scene goes. */
+int fem_server_remove_scene(fem_server s, uint32_t scene);
+int fem_server_submit(fem_server s, uint32_t scene, uint64_t tag);
+/* Progress without blocking; writes up to cap completions. */
+int fem_server_pump(fem_server s, fem_server_completion* out, uint32_t cap, uint32_t* n);
+/* State of a resident scene (waits for its shard's step in flight); either
+ * pointer may be null. */
+int fem_server_get_state(fem_server s, uint32_t scene, double* x, double* v);
+int fem_server_set_state(fem_server s, uint32_t scene, const double* x, const double* v);
+int fem_server_get_status(fem_server s, fem_server_status* status);
+/* One scene: state 0 waiting, 1 resident, 2 removed; its shard (~0u while
+ * waiting); requests pending (including one in flight). */
+int fem_server_scene_info(fem_server s, uint32_t scene, uint32_t* state, uint32_t* shard, uint32_t* pending);
 
 /* --- Library --- */
 const char* fem_last_error(void);

@@ -300,6 +300,41 @@ _u8p = C.POINTER(C.c_uint8)
 
 def _bind_batch_signatures():
     SIGNATURES.update(_BATCH_SIGNATURES)
+    SIGNATURES.update(_SERVER_SIGNATURES)
+
+
+class FemServerOptions(C.Structure):
+    _fields_ = [("precision", C.c_uint32), ("shard_max_scenes", C.c_uint32), ("shard_max_tets", C.c_uint64),
+                ("hbm_budget_bytes", C.c_uint64), ("slice_iterations", C.c_uint32), ("pad", C.c_uint32)]
+
+
+class FemServerCompletion(C.Structure):
+    _fields_ = [("tag", C.c_uint64), ("scene", C.c_uint32), ("status", C.c_uint32), ("cg_iterations", C.c_uint32),
+                ("fp64_resolved", C.c_uint32), ("latency_us", C.c_double), ("queue_us", C.c_double),
+                ("device_us", C.c_double)]
+
+
+class FemServerStatus(C.Structure):
+    _fields_ = [("resident_scenes", C.c_uint32), ("waiting_scenes", C.c_uint32), ("shards", C.c_uint32),
+                ("busy_shards", C.c_uint32), ("max_busy_shards", C.c_uint32), ("pad", C.c_uint32),
+                ("device_bytes", C.c_uint64), ("pending_requests", C.c_uint64)]
+
+
+_SERVER_SIGNATURES = {
+    "fem_server_options_default": (C.c_int, [C.POINTER(FemServerOptions)]),
+    "fem_server_create": (C.c_int, [C.POINTER(FemServerOptions), C.POINTER(C.c_void_p)]),
+    "fem_server_destroy": (C.c_int, [C.c_void_p]),
+    "fem_server_add_scene": (C.c_int, [C.c_void_p, _dp, C.c_uint32, _up, C.c_uint32, C.POINTER(FemParams), _dp,
+                                       _dp, _up, _dp, C.c_uint32, _up]),
+    "fem_server_admit": (C.c_int, [C.c_void_p, _up]),
+    "fem_server_remove_scene": (C.c_int, [C.c_void_p, C.c_uint32]),
+    "fem_server_submit": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint64]),
+    "fem_server_pump": (C.c_int, [C.c_void_p, C.POINTER(FemServerCompletion), C.c_uint32, _up]),
+    "fem_server_get_state": (C.c_int, [C.c_void_p, C.c_uint32, _dp, _dp]),
+    "fem_server_set_state": (C.c_int, [C.c_void_p, C.c_uint32, _dp, _dp]),
+    "fem_server_get_status": (C.c_int, [C.c_void_p, C.POINTER(FemServerStatus)]),
+    "fem_server_scene_info": (C.c_int, [C.c_void_p, C.c_uint32, _up, _up, _up]),
+}
 
 
 _BATCH_SIGNATURES = {
@@ -327,6 +362,8 @@ _BATCH_SIGNATURES = {
     "fem_batch_use_graph": (C.c_int, [C.c_void_p, C.c_int]),
     "fem_batch_get_state_all": (C.c_int, [C.c_void_p, _dp, _dp]),
     "fem_batch_step_host": (C.c_int, [C.c_void_p, _dp, _dp, C.c_uint32, _dp, _dp]),
+    "fem_batch_set_slice": (C.c_int, [C.c_void_p, C.c_uint32]),
+    "fem_batch_finished": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint8)]),
 }
 
 
@@ -388,6 +425,14 @@ class Batch:
         except Exception:
             pass
 
+    def set_slice(self, max_iterations):
+        check(self.lib.fem_batch_set_slice(self.h, int(max_iterations)))
+
+    def finished(self):
+        f = np.zeros(len(self.scenes), np.uint8)
+        check(self.lib.fem_batch_finished(self.h, f.ctypes.data_as(C.POINTER(C.c_uint8))))
+        return f
+
     def info(self):
         m, t = C.c_uint32(), C.c_uint32()
         n, e, b = C.c_uint64(), C.c_uint64(), C.c_uint64()
@@ -442,3 +487,116 @@ class Batch:
 
     def reset_launch_count(self):
         check(self.lib.fem_batch_reset_launch_count(self.h))
+
+
+class Server:
+    """Step requests over device-resident scenes (fem_server_*): admission by
+    a device-memory budget, size-sorted shards, continuous batching."""
+
+    def __init__(self, precision=FEM_PRECISION_MIXED, hbm_budget_bytes=None, shard_max_tets=None,
+                 shard_max_scenes=None, slice_iterations=None, completion_capacity=65536):
+        lib = load()
+        self.lib = lib
+        opt = FemServerOptions()
+        check(lib.fem_server_options_default(C.byref(opt)))
+        opt.precision = precision
+        if hbm_budget_bytes is not None:
+            opt.hbm_budget_bytes = int(hbm_budget_bytes)
+        if shard_max_tets is not None:
+            opt.shard_max_tets = int(shard_max_tets)
+        if shard_max_scenes is not None:
+            opt.shard_max_scenes = int(shard_max_scenes)
+        if slice_iterations is not None:
+            opt.slice_iterations = int(slice_iterations)
+        h = C.c_void_p()
+        check(lib.fem_server_create(C.byref(opt), C.byref(h)))
+        self.h = h
+        self.precision = precision
+        self.scenes = []
+        self._cap = completion_capacity
+        self._buf = (FemServerCompletion * completion_capacity)()
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.fem_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def add(self, sc, compute_energy=False):
+        p = params_for(sc, self.precision, compute_energy)
+        rest = _f64(sc.rest)
+        tets = np.ascontiguousarray(sc.tets, dtype=np.uint32)
+        nodes = np.ascontiguousarray(sc.knc_nodes, dtype=np.uint32)
+        tg = _f64(sc.knc_targets) if nodes.size else None
+        idx = C.c_uint32()
+        check(self.lib.fem_server_add_scene(self.h, _ptr(rest), sc.num_nodes, _ptr(tets, C.c_uint32), sc.num_tets,
+                                            C.byref(p), _ptr(_f64(sc.young_per_elem)),
+                                            _ptr(_f64(sc.poisson_per_elem)),
+                                            _ptr(nodes, C.c_uint32) if nodes.size else None,
+                                            _ptr(tg) if nodes.size else None, int(nodes.size), C.byref(idx)))
+        self.scenes.append(sc)
+        return idx.value
+
+    def admit(self):
+        n = C.c_uint32()
+        check(self.lib.fem_server_admit(self.h, C.byref(n)))
+        return n.value
+
+    def remove(self, scene):
+        check(self.lib.fem_server_remove_scene(self.h, scene))
+
+    def submit(self, scene, tag=0):
+        check(self.lib.fem_server_submit(self.h, scene, tag))
+
+    def pump(self):
+        """Completions of this call as a list of dicts."""
+        n = C.c_uint32()
+        check(self.lib.fem_server_pump(self.h, self._buf, self._cap, C.byref(n)))
+        out = []
+        for i in range(n.value):
+            c = self._buf[i]
+            out.append({"tag": c.tag, "scene": c.scene, "status": c.status, "cg_iterations": c.cg_iterations,
+                        "fp64_resolved": c.fp64_resolved, "latency_us": c.latency_us, "queue_us": c.queue_us,
+                        "device_us": c.device_us})
+        return out
+
+    def drain(self, timeout_s=600.0):
+        """Pump until no request is pending."""
+        import time
+        done, t0 = [], time.perf_counter()
+        while self.status()["pending_requests"]:
+            done += self.pump()
+            if time.perf_counter() - t0 > timeout_s:
+                raise FemError(FEM_E_TIMEOUT, "server drain timed out")
+        return done
+
+    def state(self, scene):
+        n = self.scenes[scene].num_nodes
+        x = np.empty((n, 3))
+        v = np.empty((n, 3))
+        check(self.lib.fem_server_get_state(self.h, scene, _ptr(x), _ptr(v)))
+        return x, v
+
+    def set_state(self, scene, x=None, v=None):
+        x, v = _f64(x), _f64(v)
+        check(self.lib.fem_server_set_state(self.h, scene, _ptr(x), _ptr(v)))
+
+    def scene_info(self, scene):
+        state, shard, pending = C.c_uint32(), C.c_uint32(), C.c_uint32()
+        check(self.lib.fem_server_scene_info(self.h, scene, C.byref(state), C.byref(shard), C.byref(pending)))
+        return {"state": ("waiting", "resident", "removed")[state.value], "shard": shard.value,
+                "pending": pending.value}
+
+    def resident(self):
+        return [i for i in range(len(self.scenes)) if self.scene_info(i)["state"] == "resident"]
+
+    def status(self):
+        st = FemServerStatus()
+        check(self.lib.fem_server_get_status(self.h, C.byref(st)))
+        return {k: getattr(st, k) for k, _ in FemServerStatus._fields_ if k != "pad"}
+

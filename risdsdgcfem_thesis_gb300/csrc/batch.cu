@@ -136,7 +136,14 @@ struct fem_batch_s {
     Dev<unsigned> counter, any_flag, refresh_flag, mcount, err;
     Dev<unsigned char> blob;
     Dev<uint32_t> blob_off16;
+    Dev<uint32_t> act_tiles, act_chunks, act_count;
+    Dev<unsigned> list_dirty;
+    Dev<unsigned> slice;                // [iteration budget of a launch (0 = none), iterations run]
+    Dev<uint32_t> start_tiles, start_chunks, launch_tiles, launch_chunks, list_count;
+    uint32_t slice_budget = 0;
+    std::vector<uint8_t> mask_host;     // last active mask (empty = all start)
     StepScalars* st_host = nullptr;
+    unsigned* err_host = nullptr;  // pinned copy of the error word (server readback)
     // step graph
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
@@ -177,6 +184,16 @@ struct fem_batch_s {
         b.ydelta = opt.precision == FEM_PRECISION_MIXED ? reinterpret_cast<S*>(ydelta_s.p) : nullptr;
         b.blob = opt.precision == FEM_PRECISION_MIXED ? blob.p : nullptr;
         b.blob_off16 = blob_off16.p;
+        const bool mixed = opt.precision == FEM_PRECISION_MIXED;
+        b.act_tiles = mixed ? act_tiles.p : nullptr;
+        b.act_chunks = mixed ? act_chunks.p : nullptr;
+        b.act_count = mixed ? act_count.p : nullptr;
+        b.list_dirty = mixed ? list_dirty.p : nullptr;
+        b.start_tiles = start_tiles.p;
+        b.start_chunks = start_chunks.p;
+        b.launch_tiles = launch_tiles.p;
+        b.launch_chunks = launch_chunks.p;
+        b.list_count = list_count.p;
         b.knc_node = knc_node.p;
         b.knc_mesh = knc_mesh.p;
         b.knc_target = knc_target.p;
@@ -197,8 +214,13 @@ struct fem_batch_s {
         knc_target.release(); r_s.release(); d_s.release(); q_s.release(); part_s.release(); ydelta_s.release(); counter.release();
         any_flag.release(); refresh_flag.release(); mcount.release(); err.release(); blob.release();
         blob_off16.release();
+        act_tiles.release(); act_chunks.release(); act_count.release(); list_dirty.release(); slice.release();
+        start_tiles.release(); start_chunks.release(); launch_tiles.release(); launch_chunks.release();
+        list_count.release();
         if (st_host) cudaFreeHost(st_host);
         st_host = nullptr;
+        if (err_host) cudaFreeHost(err_host);
+        err_host = nullptr;
         if (stream) cudaStreamDestroy(stream);
         stream = nullptr;
     }
@@ -216,6 +238,19 @@ int batch_fail(int code, const char* fmt, ...)
     set_last_error(buf);
     return code;
 }
+// Server support (server.cu): queue the per-mesh statistics and the error
+// word into pinned host memory on the batch's stream; they are valid once
+// the stream has passed this point.
+int batch_enqueue_readback(fem_batch b)
+{
+    cudaError_t e = cudaMemcpyAsync(b->st_host, b->st.p, sizeof(StepScalars) * b->M, cudaMemcpyDeviceToHost,
+                                    b->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(b->err_host, b->err.p, sizeof(unsigned), cudaMemcpyDeviceToHost, b->stream);
+    if (e != cudaSuccess) return batch_fail(FEM_E_CUDA, "stats readback: %s", cudaGetErrorString(e));
+    return FEM_OK;
+}
+unsigned batch_host_err(fem_batch b) { return b->err_host ? *b->err_host : 0u; }
 }  // namespace femgb
 
 namespace {
@@ -229,9 +264,51 @@ std::vector<unsigned char> as_bytes(const std::vector<double>& src)
     return out;
 }
 
-// Enqueue one step (all kernels) on `s`. In graph capture the CG loop is a
-// conditional while node; outside capture the loop runs on the host in
-// chunks, reading the device's "any mesh iterating" flag.
+// Adds a conditional node (IF or WHILE on `h`) after the current capture
+// point of `s`, captures `body` into its body graph on a side stream, and
+// makes the node the new capture point of `s`.
+template <typename F>
+cudaError_t capture_conditional(cudaStream_t s, cudaGraphConditionalHandle h, cudaGraphConditionalNodeType type,
+                                F&& body)
+{
+    const cudaGraphNode_t* deps = nullptr;
+    size_t ndeps = 0;
+    cudaGraph_t g = nullptr;
+    cudaStreamCaptureStatus cs;
+    cudaError_t e = cudaStreamGetCaptureInfo(s, &cs, nullptr, &g, &deps, nullptr, &ndeps);
+    if (e != cudaSuccess) return e;
+    cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};
+    cp.conditional.handle = h;
+    cp.conditional.type = type;
+    cp.conditional.size = 1;
+    cudaGraphNode_t node;
+    e = cudaGraphAddNode(&node, g, deps, nullptr, ndeps, &cp);
+    if (e != cudaSuccess) return e;
+    cudaStream_t bs = nullptr;
+    e = cudaStreamCreateWithFlags(&bs, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return e;
+    e = cudaStreamBeginCaptureToGraph(bs, cp.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                      cudaStreamCaptureModeRelaxed);
+    if (e == cudaSuccess) {
+        const cudaError_t eb = body(bs, cp.conditional.phGraph_out[0]);
+        cudaGraph_t out = nullptr;
+        e = cudaStreamEndCapture(bs, &out);
+        if (eb != cudaSuccess) e = eb;
+    }
+    cudaStreamDestroy(bs);
+    if (e != cudaSuccess) return e;
+    return cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1, cudaStreamSetCaptureDependencies);
+}
+
+// Enqueue one launch of the step on `s`:
+//   reset (one block: which meshes start, continue or are left out)
+//   IF some mesh starts: BeginEvaluation, f_e, b, constraints, A y, r0
+//   WHILE some mesh iterates (and the launch's iteration budget is not
+//         spent): one CG iteration (mixed: IF refresh { FP64 A y })
+//   integration and energies of the meshes whose loop ended in this launch.
+// In graph capture the conditions are set on the device; outside capture the
+// same kernels run with the loop on the host, in chunks, reading the meshes'
+// flags.
 template <typename S>
 int enqueue_step(fem_batch B, cudaStream_t s, bool capture)
 {
@@ -242,12 +319,13 @@ int enqueue_step(fem_batch B, cudaStream_t s, bool capture)
     S* q = reinterpret_cast<S*>(B->q_s.p);
     S* part = reinterpret_cast<S*>(B->part_s.p);
     using L = BatchLaunch<S>;
-    cudaGraphConditionalHandle cond = 0;
+    cudaGraphConditionalHandle cond = 0, if_start = 0;
     if (capture) {
         cudaGraph_t g = nullptr;
         cudaStreamCaptureStatus cs;
         BCK(cudaStreamGetCaptureInfo(s, &cs, nullptr, &g, nullptr, nullptr, nullptr));
         BCK(cudaGraphConditionalHandleCreate(&cond, g, 0, cudaGraphCondAssignDefault));
+        BCK(cudaGraphConditionalHandleCreate(&if_start, g, 0, cudaGraphCondAssignDefault));
     }
     LoopSync ls;
     ls.mcount = B->mcount.p;
@@ -255,18 +333,19 @@ int enqueue_step(fem_batch B, cudaStream_t s, bool capture)
     ls.refresh_flag = B->refresh_flag.p;
     ls.body_runs = nullptr;
     ls.err = B->err.p;
+    ls.slice = B->slice.p;
     ls.cond = cond;
     ls.set_cond = capture ? 1 : 0;
-    // ---- once per step ----
-    L::reset_counts(b, s);
-    L::begin_eval(b, B->x.p, s);
-    L::tile_force(b, B->x.p, B->part64.p, nullptr, s);
-    L::node_b(b, B->part64.p, B->v.p, B->bvec.p, B->y.p, s);
-    L::knc(b, B->K, B->x.p, B->bvec.p, B->y.p, s);
-    L::tile_spmv_y64(b, B->y.p, B->part64.p, 0, nullptr, s);
-    L::node_residual(b, B->part64.p, B->bvec.p, B->y.p, r, d, B->cpart.p, ls, s);
     LoopSync lb = ls;
     lb.body_runs = B->any_flag.p;
+    auto start_section = [&](cudaStream_t ss) {
+        L::begin_eval(b, B->x.p, ss);
+        L::tile_force(b, B->x.p, B->part64.p, nullptr, ss);
+        L::node_b(b, B->part64.p, B->v.p, B->bvec.p, B->y.p, ss);
+        L::knc(b, B->K, B->x.p, B->bvec.p, B->y.p, ss);
+        L::tile_spmv_y64(b, B->y.p, B->part64.p, 0, nullptr, ss);
+        L::node_residual(b, B->part64.p, B->bvec.p, B->y.p, r, d, B->cpart.p, ls, ss);
+    };
     // mixed: the tile product also writes each tile's share of d^T A d; one
     // fused node pass forms alpha from the shares and does the rest
     auto body_head = [&](cudaStream_t bs, cudaGraphConditionalHandle ifh, int set_if) {
@@ -285,84 +364,43 @@ int enqueue_step(fem_batch B, cudaStream_t s, bool capture)
             L::node_update(b, B->y.p, r, d, q, B->cpart.p, lb, bs);
         }
     };
+    L::reset_counts(b, ls, if_start, s);
     if (capture) {
-        const cudaGraphNode_t* deps = nullptr;
-        size_t ndeps = 0;
-        cudaGraph_t g = nullptr;
-        cudaStreamCaptureStatus cs;
-        BCK(cudaStreamGetCaptureInfo(s, &cs, nullptr, &g, &deps, nullptr, &ndeps));
-        cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};
-        cp.conditional.handle = cond;
-        cp.conditional.type = cudaGraphCondTypeWhile;
-        cp.conditional.size = 1;
-        cudaGraphNode_t wnode;
-        BCK(cudaGraphAddNode(&wnode, g, deps, nullptr, ndeps, &cp));
-        cudaGraph_t bodyg = cp.conditional.phGraph_out[0];
-        cudaStream_t bs;
-        BCK(cudaStreamCreateWithFlags(&bs, cudaStreamNonBlocking));
-        cudaError_t e1 = cudaStreamBeginCaptureToGraph(bs, bodyg, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed);
-        if (e1 != cudaSuccess) {
-            cudaStreamDestroy(bs);
-            BCK(e1);
-        }
-        cudaGraphConditionalHandle ifh = 0;
-        if (mixed) {
-            e1 = cudaGraphConditionalHandleCreate(&ifh, bodyg, 0, 0);
-            if (e1 != cudaSuccess) {
-                cudaGraph_t tmp = nullptr;
-                cudaStreamEndCapture(bs, &tmp);
-                cudaStreamDestroy(bs);
-                BCK(e1);
+        BCK(capture_conditional(s, if_start, cudaGraphCondTypeIf, [&](cudaStream_t ss, cudaGraph_t) {
+            start_section(ss);
+            return cudaGetLastError();
+        }));
+        BCK(capture_conditional(s, cond, cudaGraphCondTypeWhile, [&](cudaStream_t bs, cudaGraph_t bodyg) {
+            cudaGraphConditionalHandle ifh = 0;
+            if (mixed) {
+                const cudaError_t e = cudaGraphConditionalHandleCreate(&ifh, bodyg, 0, 0);
+                if (e != cudaSuccess) return e;
             }
-        }
-        body_head(bs, ifh, mixed ? 1 : 0);
-        if (mixed) {
-            // IF (some mesh refreshes this iteration) { FP64 product of y }
-            const cudaGraphNode_t* bdeps = nullptr;
-            size_t nb = 0;
-            cudaGraph_t bg = nullptr;
-            e1 = cudaStreamGetCaptureInfo(bs, &cs, nullptr, &bg, &bdeps, nullptr, &nb);
-            cudaGraphNodeParams ip = {cudaGraphNodeTypeConditional};
-            ip.conditional.handle = ifh;
-            ip.conditional.type = cudaGraphCondTypeIf;
-            ip.conditional.size = 1;
-            cudaGraphNode_t inode;
-            if (e1 == cudaSuccess) e1 = cudaGraphAddNode(&inode, bg, bdeps, nullptr, nb, &ip);
-            cudaStream_t is = nullptr;
-            if (e1 == cudaSuccess) e1 = cudaStreamCreateWithFlags(&is, cudaStreamNonBlocking);
-            if (e1 == cudaSuccess)
-                e1 = cudaStreamBeginCaptureToGraph(is, ip.conditional.phGraph_out[0], nullptr, nullptr, 0,
-                                                   cudaStreamCaptureModeRelaxed);
-            if (e1 == cudaSuccess) {
-                L::tile_spmv_y64(b, B->y.p, B->part64.p, 1, nullptr, is);
-                cudaGraph_t ig = nullptr;
-                e1 = cudaStreamEndCapture(is, &ig);
+            body_head(bs, ifh, mixed ? 1 : 0);
+            if (mixed) {
+                // IF (some mesh refreshes this iteration) { FP64 product of y }
+                const cudaError_t e = capture_conditional(bs, ifh, cudaGraphCondTypeIf, [&](cudaStream_t is, cudaGraph_t) {
+                    L::tile_spmv_y64(b, B->y.p, B->part64.p, 1, nullptr, is);
+                    return cudaGetLastError();
+                });
+                if (e != cudaSuccess) return e;
             }
-            if (is) cudaStreamDestroy(is);
-            if (e1 == cudaSuccess)
-                e1 = cudaStreamUpdateCaptureDependencies(bs, &inode, nullptr, 1, cudaStreamSetCaptureDependencies);
-            if (e1 != cudaSuccess) {
-                cudaGraph_t tmp = nullptr;
-                cudaStreamEndCapture(bs, &tmp);
-                cudaStreamDestroy(bs);
-                BCK(e1);
-            }
-        }
-        body_tail(bs);
-        cudaGraph_t out_body = nullptr;
-        cudaError_t e2 = cudaStreamEndCapture(bs, &out_body);
-        cudaStreamDestroy(bs);
-        BCK(e2);
-        BCK(cudaStreamUpdateCaptureDependencies(s, &wnode, nullptr, 1, cudaStreamSetCaptureDependencies));
+            body_tail(bs);
+            return cudaGetLastError();
+        }));
     } else {
+        bool any_start = B->mask_host.empty();
+        for (uint8_t a : B->mask_host) any_start |= a == 1;
+        if (any_start) start_section(s);
         // host-driven loop: chunks of iterations, then read the per-mesh flags
+        uint32_t budget = B->slice_budget, ran = 0;
         for (;;) {
             BCK(cudaMemcpyAsync(B->st_host, B->st.p, sizeof(StepScalars) * B->M, cudaMemcpyDeviceToHost, s));
             BCK(cudaStreamSynchronize(s));
             bool any = false;
             for (uint32_t m = 0; m < B->M; m++) any |= !B->st_host[m].done;
-            if (!any) break;
-            for (int i = 0; i < 8; i++) {
+            if (!any || (budget && ran >= budget)) break;
+            for (int i = 0; i < 8 && !(budget && ran >= budget); i++, ran++) {
                 body_head(s, 0, 0);
                 if (mixed) L::tile_spmv_y64(b, B->y.p, B->part64.p, 1, B->refresh_flag.p, s);
                 body_tail(s);
@@ -820,8 +858,26 @@ int fem_batch_finalize(fem_batch b)
     BCKC(b->blob.upload(blob_h, s));
     BCKC(b->blob_off16.alloc(blob_off16_h.size()));
     BCKC(b->blob_off16.upload(blob_off16_h, s));
+    BCKC(b->slice.alloc(2));
+    BCKC(cudaMemsetAsync(b->slice.p, 0, 2 * sizeof(unsigned), s));
+    BCKC(b->start_tiles.alloc(b->ntiles));
+    BCKC(b->start_chunks.alloc(b->nchunks));
+    BCKC(b->launch_tiles.alloc(b->ntiles));
+    BCKC(b->launch_chunks.alloc(b->nchunks));
+    BCKC(b->list_count.alloc(4));
+    BCKC(cudaMemsetAsync(b->list_count.p, 0, 4 * sizeof(uint32_t), s));
+    if (!fp64) {
+        BCKC(b->act_tiles.alloc(b->ntiles));
+        BCKC(b->act_chunks.alloc(b->nchunks));
+        BCKC(b->act_count.alloc(2));
+        BCKC(b->list_dirty.alloc(1));
+        BCKC(cudaMemsetAsync(b->act_count.p, 0, 2 * sizeof(uint32_t), s));
+        BCKC(cudaMemsetAsync(b->list_dirty.p, 0, sizeof(unsigned), s));
+    }
     if (!fp64) prepare_tile_pipe();
     BCKC(cudaMallocHost(&b->st_host, sizeof(StepScalars) * b->M));
+    BCKC(cudaMallocHost(&b->err_host, sizeof(unsigned)));
+    *b->err_host = 0;
     BCKC(b->tiles.upload(tiles, s));
     BCKC(b->chunks.upload(chunks, s));
     BCKC(b->mc.upload(mcs, s));
@@ -862,12 +918,19 @@ int fem_batch_finalize(fem_batch b)
     BCKC(cudaMemsetAsync(b->mcount.p, 0, sizeof(unsigned) * b->M, s));
     BCKC(cudaStreamSynchronize(s));
 #undef BCKC
-    b->device_bytes = 0;
-    b->device_bytes += b->tiles.bytes() + b->chunks.bytes() + b->mc.bytes() + b->st.bytes() + b->gtets.bytes() +
-                       b->Dinv_s.bytes() + b->mat_s.bytes() + b->R_s.bytes() + b->Dinv64.bytes() + b->vol.bytes() +
-                       b->detF.bytes() + b->tile_nodes.bytes() + b->lptr0.bytes() + b->nptr.bytes() +
-                       b->nslot.bytes() + b->lconn.bytes() + b->lptr.bytes() + b->lidx.bytes() + b->fixed.bytes() +
-                       7 * N3 * 8 / 2 + b->r_s.bytes() * 3 + b->part_s.bytes() + b->part64.bytes();
+    b->device_bytes = b->tiles.bytes() + b->chunks.bytes() + b->mc.bytes() + b->st.bytes() + b->active.bytes() +
+                      b->gtets.bytes() + b->Dinv_s.bytes() + b->mat_s.bytes() + b->R_s.bytes() +
+                      b->Dinv64.bytes() + b->vol.bytes() + b->detF.bytes() + b->tile_nodes.bytes() +
+                      b->lptr0.bytes() + b->nptr.bytes() + b->nslot.bytes() + b->knc_node.bytes() +
+                      b->knc_mesh.bytes() + b->knc_target.bytes() + b->lconn.bytes() + b->lptr.bytes() +
+                      b->lidx.bytes() + b->fixed.bytes() + b->rest.bytes() + b->x.bytes() + b->v.bytes() +
+                      b->bvec.bytes() + b->y.bytes() + b->r_s.bytes() + b->d_s.bytes() + b->q_s.bytes() +
+                      b->part_s.bytes() + b->ydelta_s.bytes() + b->part64.bytes() + b->cpart.bytes() +
+                      b->tpart.bytes() + b->counter.bytes() + b->any_flag.bytes() + b->refresh_flag.bytes() +
+                      b->mcount.bytes() + b->err.bytes() + b->blob.bytes() + b->blob_off16.bytes() +
+                      b->act_tiles.bytes() + b->act_chunks.bytes() + b->act_count.bytes() + b->list_dirty.bytes() +
+                      b->slice.bytes() + b->start_tiles.bytes() + b->start_chunks.bytes() +
+                      b->launch_tiles.bytes() + b->launch_chunks.bytes() + b->list_count.bytes();
     b->finalized = true;
     // host copies of the meshes are no longer needed beyond sizes
     for (auto& m : b->meshes) {
@@ -984,8 +1047,24 @@ int fem_batch_step_host(fem_batch b, const double* x_in, const double* v_in, uin
 int fem_batch_set_active(fem_batch b, const uint8_t* mask)
 {
     if (int e = check_ready(b)) return e;
-    if (mask) BCK(cudaMemcpyAsync(b->active.p, mask, b->M, cudaMemcpyHostToDevice, b->stream));
-    else BCK(cudaMemsetAsync(b->active.p, 1, b->M, b->stream));
+    if (mask) {
+        for (uint32_t m = 0; m < b->M; m++)
+            if (mask[m] > 2) return batch_fail(FEM_E_ARG, "mask[%u] = %u (0, 1 or 2)", m, (unsigned)mask[m]);
+        b->mask_host.assign(mask, mask + b->M);
+        BCK(cudaMemcpyAsync(b->active.p, b->mask_host.data(), b->M, cudaMemcpyHostToDevice, b->stream));
+    } else {
+        b->mask_host.clear();
+        BCK(cudaMemsetAsync(b->active.p, 1, b->M, b->stream));
+    }
+    return FEM_OK;
+}
+
+int fem_batch_set_slice(fem_batch b, uint32_t max_iterations)
+{
+    if (int e = check_ready(b)) return e;
+    b->slice_budget = max_iterations;
+    BCK(cudaMemcpyAsync(b->slice.p, &b->slice_budget, sizeof(uint32_t), cudaMemcpyHostToDevice, b->stream));
+    BCK(cudaStreamSynchronize(b->stream));
     return FEM_OK;
 }
 
@@ -1022,6 +1101,17 @@ int fem_batch_step(fem_batch b, uint32_t nsteps)
 {
     if (int e = fem_batch_step_async(b, nsteps)) return e;
     return fem_batch_synchronize(b);
+}
+
+int fem_batch_finished(fem_batch b, uint8_t* flags)
+{
+    if (int e = check_ready(b)) return e;
+    if (!flags) return batch_fail(FEM_E_ARG, "null flags");
+    for (uint32_t m = 0; m < b->M; m++) {
+        const StepScalars& h = b->st_host[m];
+        flags[m] = h.finished ? 1 : (h.done ? 0 : 2);
+    }
+    return FEM_OK;
 }
 
 int fem_batch_get_stats(fem_batch b, uint32_t mesh, fem_step_stats* out)

@@ -102,6 +102,19 @@ struct BatchView {
     S* ydelta;                     // [3 Ntot] mixed: FP32 sum of this step's alpha d; null on FP64
     unsigned char* blob;           // mixed: per-tile blobs (element data, tile CSR, node list)
     const uint32_t* blob_off16;    // [ntiles] blob offset / 16
+    // mixed: tiles and chunks of the meshes still iterating (active_list.cuh)
+    uint32_t* act_tiles;           // [ntiles]
+    uint32_t* act_chunks;          // [nchunks]
+    uint32_t* act_count;           // [2] entries in act_tiles, act_chunks
+    unsigned* list_dirty;          // set when a mesh leaves its CG loop
+    // tiles and chunks of the meshes that start a step in this launch, and
+    // of those that take part in it; list_count: start tiles, start chunks,
+    // launch tiles, launch chunks
+    uint32_t* start_tiles;         // [ntiles]
+    uint32_t* start_chunks;        // [nchunks]
+    uint32_t* launch_tiles;        // [ntiles]
+    uint32_t* launch_chunks;       // [nchunks]
+    uint32_t* list_count;          // [4]
     // constraints
     const uint32_t* knc_node;      // [K] global node id
     const uint32_t* knc_mesh;      // [K]

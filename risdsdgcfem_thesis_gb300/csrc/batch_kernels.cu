@@ -25,6 +25,7 @@
 // The once-per-step kernels (elastic force, right-hand side, constraints,
 // initial residual, integration, energies) follow
 // Step_QuasiImplicitEuler_v (LeafDSH_Solid3D_FEM.cpp:1205-1328).
+#include "active_list.cuh"
 #include "batch.cuh"
 #include "batch_launch.h"
 #include "elem_math.cuh"
@@ -217,9 +218,14 @@ __global__ void __launch_bounds__(256) k_tile_spmv_y64(BatchView<S> b, const dou
     if (mode == SPMV_Y64_REFRESH && flag && !*flag) return;
     __shared__ double sd[3 * kTileNodes];
     __shared__ double so[12 * kTileElems];
-    for (uint32_t t = blockIdx.x; t < b.ntiles; t += gridDim.x) {
+    // ALL: the meshes that start a step; REFRESH: the running meshes (their
+    // work list on the mixed path)
+    const uint32_t* list = mode == SPMV_Y64_ALL ? b.start_tiles : b.act_tiles;
+    const uint32_t n = mode == SPMV_Y64_ALL ? b.list_count[0] : (b.act_tiles ? b.act_count[0] : b.ntiles);
+    for (uint32_t i = blockIdx.x; i < n; i += gridDim.x) {
+        const uint32_t t = list_entry(list, i);
         const TileMeta tm = b.tiles[t];
-        if (mode == SPMV_Y64_ALL && !b.active[tm.mesh]) continue;
+        if (mode == SPMV_Y64_ALL && b.active[tm.mesh] != 1) continue;
         if (mode == SPMV_Y64_REFRESH && (!mesh_running(b, tm.mesh) || !refresh_now(b.mc[tm.mesh], b.st[tm.mesh])))
             continue;
         const uint16_t* lp = b.lptr + b.lptr0[t];
@@ -280,9 +286,13 @@ __global__ void __launch_bounds__(256) k_tile_force(BatchView<S> b, const double
                                                     double* __restrict__ part64, double* __restrict__ tile_energy)
 {
     __shared__ double so[12 * kTileElems];
-    for (uint32_t t = blockIdx.x; t < b.ntiles; t += gridDim.x) {
+    const uint32_t* list = part64 ? b.start_tiles : b.launch_tiles;
+    const uint32_t n = b.list_count[part64 ? 0 : 2];
+    for (uint32_t i = blockIdx.x; i < n; i += gridDim.x) {
+        const uint32_t t = list[i];
         const TileMeta tm = b.tiles[t];
-        if (!b.active[tm.mesh]) continue;
+        // the force of a starting step, or the energy of a finished one
+        if (part64 ? b.active[tm.mesh] != 1 : !b.st[tm.mesh].finished) continue;
         double energy = 0.0;
         if (threadIdx.x < tm.ne) {
             const size_t e = tm.e0 + threadIdx.x;
@@ -359,9 +369,11 @@ __global__ void __launch_bounds__(256) k_tile_force(BatchView<S> b, const double
 template <typename S>
 __global__ void k_tile_potential(BatchView<S> b, const double* __restrict__ x, double* __restrict__ tile_pe)
 {
-    for (uint32_t t = blockIdx.x; t < b.ntiles; t += gridDim.x) {
+    const uint32_t n = b.list_count[2];
+    for (uint32_t i = blockIdx.x; i < n; i += gridDim.x) {
+        const uint32_t t = b.launch_tiles[i];
         const TileMeta tm = b.tiles[t];
-        if (!b.active[tm.mesh]) continue;
+        if (!b.st[tm.mesh].finished) continue;
         const MeshConsts& c = b.mc[tm.mesh];
         double acc = 0.0;
         if (threadIdx.x < tm.ne) {
@@ -405,9 +417,11 @@ template <typename S>
 __global__ void k_node_b(BatchView<S> b, const double* __restrict__ part64, const double* __restrict__ v,
                          double* __restrict__ bv, double* __restrict__ y)
 {
-    for (uint32_t ci = blockIdx.x; ci < b.nchunks; ci += gridDim.x) {
+    const uint32_t nl = b.list_count[1];
+    for (uint32_t il = blockIdx.x; il < nl; il += gridDim.x) {
+        const uint32_t ci = b.start_chunks[il];
         const ChunkMeta ch = b.chunks[ci];
-        if (!b.active[ch.mesh]) continue;
+        if (b.active[ch.mesh] != 1) continue;
         const MeshConsts& c = b.mc[ch.mesh];
         for (size_t n = ch.n0 + threadIdx.x; n < ch.n1; n += blockDim.x) {
             double f0, f1, f2;
@@ -435,7 +449,7 @@ __global__ void k_knc(BatchView<S> b, uint32_t K, const double* __restrict__ x, 
 {
     for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < K; k += gridDim.x * blockDim.x) {
         const uint32_t m = b.knc_mesh[k];
-        if (!b.active[m]) continue;
+        if (b.active[m] != 1) continue;
         const MeshConsts& c = b.mc[m];
         const size_t n = b.knc_node[k];
         const double* tg = b.knc_target + 3 * (size_t)k;
@@ -497,12 +511,14 @@ __device__ __forceinline__ void finish_stats(StepScalars& s)
     s.abs_residual = ::sqrt(s.delta_new);
 }
 
-// Last block of the grid: while condition (any mesh iterating) and the
-// refresh flag for the next iteration.
+// Last block of the grid: while condition (any mesh iterating), the refresh
+// flag for the next iteration and, on the mixed path, the work lists of the
+// meshes that iterate.
 template <typename S>
-__device__ void grid_tail(const BatchView<S>& b, const LoopSync& ls)
+__device__ void grid_tail(const BatchView<S>& b, const LoopSync& ls, bool iteration)
 {
     if (!arrive_last(ls.gcount, gridDim.x)) return;
+    if (b.act_tiles && (!iteration || *(volatile const unsigned*)b.list_dirty)) build_active_lists(b);
     int any = 0, refresh = 0;
     for (uint32_t i = threadIdx.x; i < b.M; i += blockDim.x) {
         volatile const StepScalars* sp = b.st + i;
@@ -518,7 +534,12 @@ __device__ void grid_tail(const BatchView<S>& b, const LoopSync& ls)
         if (ls.refresh_flag) *ls.refresh_flag = refresh ? 1u : 0u;
         if (ls.body_runs) *ls.body_runs += 1u;
         const bool stop = ls.err && *(volatile const unsigned*)ls.err;
-        if (ls.set_cond) cudaGraphSetConditional(ls.cond, (any && !stop) ? 1u : 0u);
+        bool budget_left = true;
+        if (ls.slice) {
+            if (iteration) ls.slice[1] += 1u;
+            budget_left = ls.slice[0] == 0u || ls.slice[1] < ls.slice[0];
+        }
+        if (ls.set_cond) cudaGraphSetConditional(ls.cond, (any && !stop && budget_left) ? 1u : 0u);
     }
 }
 
@@ -529,9 +550,11 @@ __global__ void k_node_residual(BatchView<S> b, const double* __restrict__ part6
                                 const double* __restrict__ y, S* __restrict__ r, S* __restrict__ d,
                                 double* __restrict__ cpart, LoopSync ls)
 {
-    for (uint32_t ci = blockIdx.x; ci < b.nchunks; ci += gridDim.x) {
+    const uint32_t nl = b.list_count[1];
+    for (uint32_t il = blockIdx.x; il < nl; il += gridDim.x) {
+        const uint32_t ci = b.start_chunks[il];
         const ChunkMeta ch = b.chunks[ci];
-        if (!b.active[ch.mesh]) continue;
+        if (b.active[ch.mesh] != 1) continue;
         const MeshConsts& c = b.mc[ch.mesh];
         const double mfm = c.mass * c.factor_M;
         double acc = 0.0;
@@ -567,12 +590,15 @@ __global__ void k_node_residual(BatchView<S> b, const double* __restrict__ part6
                 s.beta = 0.0;
                 s.beta_f = 0.f;
                 s.done = cg_cont(s) ? 0u : 1u;
-                if (s.done) finish_stats(s);
+                if (s.done) {
+                    finish_stats(s);
+                    s.finished = 1;
+                }
             }
         }
         __syncthreads();
     }
-    grid_tail(b, ls);
+    grid_tail(b, ls, false);
 }
 
 // d = S(r + beta d) written back ; q = S A d ; d.q ; last block of a mesh:
@@ -633,6 +659,7 @@ __global__ void k_node_q(BatchView<S> b, const S* __restrict__ part, S* __restri
                 s.dot_dq = total;
                 if (::fabs(total) < s.abs_eps_sq) {  // breakdown: leave before the update
                     s.done = 1;
+                    s.finished = 1;
                     finish_stats(s);
                 } else {
                     s.alpha = s.delta_new / total;
@@ -681,11 +708,14 @@ __global__ void k_node_update(BatchView<S> b, double* __restrict__ y, S* __restr
                 s.total_iters += 1;
                 if (total != total) s.status = 3u;
                 s.done = cg_cont(s) ? 0u : 1u;
-                if (s.done) finish_stats(s);
+                if (s.done) {
+                    finish_stats(s);
+                    s.finished = 1;
+                }
             }
         }
     }
-    grid_tail(b, ls);
+    grid_tail(b, ls, true);
 }
 
 // v = y ; x += dt y
@@ -693,9 +723,10 @@ template <typename S>
 __global__ void k_integrate(BatchView<S> b, double* __restrict__ x, double* __restrict__ v,
                             const double* __restrict__ y)
 {
-    for (uint32_t ci = blockIdx.x; ci < b.nchunks; ci += gridDim.x) {
-        const ChunkMeta ch = b.chunks[ci];
-        if (!b.active[ch.mesh]) continue;
+    const uint32_t nl = b.list_count[3];
+    for (uint32_t il = blockIdx.x; il < nl; il += gridDim.x) {
+        const ChunkMeta ch = b.chunks[b.launch_chunks[il]];
+        if (!b.st[ch.mesh].finished) continue;
         const double dt = b.mc[ch.mesh].dt;
         for (size_t n = ch.n0 + threadIdx.x; n < ch.n1; n += blockDim.x) {
 #pragma unroll
@@ -712,15 +743,44 @@ __global__ void k_integrate(BatchView<S> b, double* __restrict__ x, double* __re
 // ---------------------------------------------------------------------------
 // once-per-step bookkeeping
 
+// One block, first kernel of a launch. active[m]: 1 starts a step, 2
+// continues a step an iteration budget interrupted, 0 leaves the mesh out
+// (a step left unfinished is dropped). Clears the finished flags and the
+// launch's iteration count; sets the IF condition of the start-of-step
+// kernels (some mesh starts) and the CG loop's while condition (some mesh
+// continues); rebuilds the work lists when a running mesh was dropped.
 template <typename S>
-__global__ void k_reset_counts(BatchView<S> b)
+__global__ void k_reset_counts(BatchView<S> b, LoopSync ls, cudaGraphConditionalHandle if_start)
 {
-    for (uint32_t m = blockIdx.x * blockDim.x + threadIdx.x; m < b.M; m += gridDim.x * blockDim.x) {
-        if (b.active[m]) {
-            b.st[m].inverted = 0;
-            b.st[m].fp64_resolved = 0;
+    int start = 0, cont = 0, dropped = 0;
+    for (uint32_t m = threadIdx.x; m < b.M; m += blockDim.x) {
+        StepScalars& s = b.st[m];
+        const uint8_t a = b.active[m];
+        s.finished = 0;
+        if (a == 1) {
+            s.inverted = 0;
+            s.fp64_resolved = 0;
+            start = 1;
+        } else if (a == 2) {
+            cont |= s.done ? 0 : 1;
         } else {
-            b.st[m].done = 1;
+            dropped |= s.done ? 0 : 1;
+            s.done = 1;
+        }
+    }
+    start = __syncthreads_or(start);
+    cont = __syncthreads_or(cont);
+    dropped = __syncthreads_or(dropped);
+    if (dropped && b.act_tiles) build_active_lists(b);
+    build_mesh_lists(
+        b, [&](uint32_t m) { return b.active[m] == 1; }, b.start_tiles, b.start_chunks, b.list_count);
+    build_mesh_lists(
+        b, [&](uint32_t m) { return b.active[m] != 0; }, b.launch_tiles, b.launch_chunks, b.list_count + 2);
+    if (threadIdx.x == 0) {
+        if (ls.slice) ls.slice[1] = 0u;
+        if (ls.set_cond) {
+            cudaGraphSetConditional(if_start, start ? 1u : 0u);
+            cudaGraphSetConditional(ls.cond, cont ? 1u : 0u);
         }
     }
 }
@@ -730,7 +790,7 @@ template <typename S>
 __global__ void k_fin_energy(BatchView<S> b, int kind, const double* __restrict__ tpart)
 {
     for (uint32_t m = blockIdx.x; m < b.M; m += gridDim.x) {
-        if (!b.active[m]) continue;
+        if (!b.st[m].finished) continue;
         const MeshConsts& c = b.mc[m];
         double acc = 0.0;
         for (uint32_t i = threadIdx.x; i < c.ntiles; i += blockDim.x) acc += tpart[c.tile0 + i];
@@ -839,9 +899,10 @@ void BatchLaunch<S>::fin_energy(const BatchView<S>& b, int kind, const double* t
 }
 
 template <typename S>
-void BatchLaunch<S>::reset_counts(const BatchView<S>& b, cudaStream_t s)
+void BatchLaunch<S>::reset_counts(const BatchView<S>& b, const LoopSync& ls, cudaGraphConditionalHandle if_start,
+                                   cudaStream_t s)
 {
-    k_reset_counts<S><<<(b.M + 255) / 256, 256, 0, s>>>(b);
+    k_reset_counts<S><<<1, 256, 0, s>>>(b, ls, if_start);
     launch_counter()++;
 }
 

@@ -17,6 +17,7 @@ struct LoopSync {
     unsigned* refresh_flag;  // raised when a mesh refreshes its residual next iteration
     unsigned* body_runs;     // CG-loop body executions (launch accounting)
     const unsigned* err;     // batch error word: the loop stops once it is set
+    unsigned* slice;         // [budget (0 = none), iterations run in this launch]
     cudaGraphConditionalHandle cond;
     int set_cond;
 };
@@ -33,7 +34,8 @@ void launch_node_update_fused(const BatchView<float>& b, const float* part, cons
 template <typename S>
 struct BatchLaunch {
     static void begin_eval(const BatchView<S>& b, const double* x, cudaStream_t s);  // rotation.cu
-    static void reset_counts(const BatchView<S>& b, cudaStream_t s);
+    static void reset_counts(const BatchView<S>& b, const LoopSync& ls, cudaGraphConditionalHandle if_start,
+                             cudaStream_t s);
     static void tile_spmv(const BatchView<S>& b, const S* d, const S* r, S* part,
                           cudaGraphConditionalHandle if_refresh, int set_if, const unsigned* refresh_flag,
                           cudaStream_t s);

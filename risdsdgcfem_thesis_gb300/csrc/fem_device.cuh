@@ -30,7 +30,9 @@ struct StepScalars {
     double rel_residual, abs_residual;
     uint32_t k, max_iter, done, status;
     uint32_t inverted, fp64_resolved, refresh_every;
-    float beta_f;  // beta rounded to FP32 (mixed path)
+    float beta_f;       // beta rounded to FP32 (mixed path)
+    uint32_t finished;  // batch: the CG loop ended during this launch (cleared at launch start)
+    uint32_t pad2;
     unsigned long long total_iters;
 };
 

@@ -63,9 +63,11 @@ template <typename S>
 __global__ void k_begin_eval_batch(BatchView<S> b, const double* __restrict__ x)
 {
     __shared__ unsigned s_inv, s_res;
-    for (uint32_t t = blockIdx.x; t < b.ntiles; t += gridDim.x) {
+    const uint32_t n = b.list_count[0];
+    for (uint32_t i = blockIdx.x; i < n; i += gridDim.x) {
+        const uint32_t t = b.start_tiles[i];
         const TileMeta tm = b.tiles[t];
-        if (!b.active[tm.mesh]) continue;
+        if (b.active[tm.mesh] != 1) continue;
         if (threadIdx.x == 0) { s_inv = 0; s_res = 0; }
         __syncthreads();
         if (threadIdx.x < tm.ne) {

@@ -39,6 +39,7 @@
 // code in the batch's error word; the block then issues no further copies and
 // drains, again bounded, the copies it has in flight. The CG loop stops at
 // the end of an iteration in which the error word is set.
+#include "active_list.cuh"
 #include "batch.cuh"
 #include "batch_launch.h"
 #include "elem_math.cuh"
@@ -209,32 +210,33 @@ constexpr uint32_t kPipeSmem = 2 * kStageBytes + 16u * (kTileNodes + 4 * kTileEl
 
 // What a block needs to know of one tile before its blob arrives.
 struct TileLook {
+    uint32_t tile;            // tile id
     uint32_t mesh, n0, nenn;  // nenn: ne | nn << 16
     uint32_t boff;            // blob offset / 16
     uint32_t g;               // global node id of this thread's local node
     float beta;               // beta of the tile's mesh
-    bool act;                 // tile exists and its mesh is iterating
+    bool act;                 // a tile to do
 };
 
-__device__ __forceinline__ void look_meta(const BatchView<float>& b, uint32_t t, TileLook& L)
+// First half of a look-up: entry i of the work list and the tile's metadata.
+__device__ __forceinline__ void look_meta(const BatchView<float>& b, uint32_t i, uint32_t n, TileLook& L)
 {
-    L.act = t < b.ntiles;
+    L.act = i < n;
     if (L.act) {
-        const TileMeta tm = b.tiles[t];
+        L.tile = b.act_tiles[i];
+        const TileMeta tm = b.tiles[L.tile];
         L.mesh = tm.mesh;
         L.n0 = tm.n0;
         L.nenn = (uint32_t)tm.ne | ((uint32_t)tm.nn << 16);
     }
 }
 
-// Second half of a look-up: the loads that depend on the tile's metadata.
-__device__ __forceinline__ void look_resolve(const BatchView<float>& b, uint32_t t, TileLook& L)
+// Second half: the loads that depend on the tile's metadata.
+__device__ __forceinline__ void look_resolve(const BatchView<float>& b, TileLook& L)
 {
     if (!L.act) return;
-    const StepScalars& st = b.st[L.mesh];
-    L.act = !st.done;
-    L.beta = st.beta_f;
-    L.boff = b.blob_off16[t];
+    L.beta = b.st[L.mesh].beta_f;
+    L.boff = b.blob_off16[L.tile];
     L.g = threadIdx.x < (L.nenn >> 16) ? __ldg(b.tile_nodes + L.n0 + threadIdx.x) : 0u;
 }
 
@@ -260,16 +262,17 @@ __global__ void __launch_bounds__(256, 3) k_tile_spmv_pipe(BatchView<float> b, c
     }
     __syncthreads();
 
-    // Software pipeline over this block's tiles t, t+G, t+2G, ...: while tile
-    // t is computed, the blob of t+G is in flight (bulk copy) together with
-    // this thread's gather of d and r for its local node of t+G, and the
-    // metadata of t+2G is looked up.
-    uint32_t t = blockIdx.x;
+    // Software pipeline over this block's entries i, i+G, i+2G, ... of the
+    // work list: while tile i is computed, the blob of i+G is in flight (bulk
+    // copy) together with this thread's gather of d and r for its local node
+    // of i+G, and the metadata of i+2G is looked up.
+    const uint32_t n_act = *(volatile const uint32_t*)b.act_count;
+    uint32_t i = blockIdx.x;
     TileLook cur, nxt, n2;
-    look_meta(b, t, cur);
-    look_resolve(b, t, cur);
-    look_meta(b, t + G, nxt);
-    look_resolve(b, t + G, nxt);
+    look_meta(b, i, n_act, cur);
+    look_resolve(b, cur);
+    look_meta(b, i + G, n_act, nxt);
+    look_resolve(b, nxt);
     uint32_t phase = 0u;    // bit s: parity of stage s's next completion
     uint32_t pending = 0u;  // bit s: a copy into stage s is in flight
     int s = 0;
@@ -290,8 +293,8 @@ __global__ void __launch_bounds__(256, 3) k_tile_spmv_pipe(BatchView<float> b, c
             cr0 = __ldg(rvec + g); cr1 = __ldg(rvec + g + 1); cr2 = __ldg(rvec + g + 2);
         }
     }
-    for (; t < b.ntiles; t += G) {
-        look_meta(b, t + 2 * G, n2);  // resolved after the element products
+    for (; i < n_act; i += G) {
+        look_meta(b, i + 2 * G, n_act, n2);  // resolved after the element products
         float nd0 = 0.f, nd1 = 0.f, nd2 = 0.f, nr0 = 0.f, nr1 = 0.f, nr2 = 0.f;
         if (!failed && nxt.act) {  // after a failed wait no new copies are issued
             if (tid == 0) issue(nxt, s ^ 1);
@@ -362,7 +365,7 @@ __global__ void __launch_bounds__(256, 3) k_tile_spmv_pipe(BatchView<float> b, c
                 for (int k = 0; k < 4; k++)
                     so4[k * kTileElems + i] = make_float4(out[3 * k], out[3 * k + 1], out[3 * k + 2], 0.f);
             }
-            look_resolve(b, t + 2 * G, n2);
+            look_resolve(b, n2);
             __syncthreads();
             if (tid < nn) {
                 float a0 = 0.f, a1 = 0.f, a2 = 0.f;
@@ -380,14 +383,14 @@ __global__ void __launch_bounds__(256, 3) k_tile_spmv_pipe(BatchView<float> b, c
             const F2 w = warp_sum_f2(F2{share, 0.f});
             if ((tid & 31) == 0) wsh[tid >> 5] = make_float2(w.hi, w.lo);
         } else {
-            look_resolve(b, t + 2 * G, n2);
+            look_resolve(b, n2);
         }
         __syncthreads();
         if (cur.act && tid == 0) {
             F2 a = {0.f, 0.f};
             if (!failed)
                 for (int k = 0; k < (int)(blockDim.x >> 5); k++) a = f2_add(a, F2{wsh[k].x, wsh[k].y});
-            tshare[t] = make_float2(a.hi, a.lo);
+            tshare[cur.tile] = make_float2(a.hi, a.lo);
         }
         cur = nxt;
         nxt = n2;
@@ -414,9 +417,10 @@ __global__ void __launch_bounds__(256) k_node_update_fused(BatchView<float> b, c
     __shared__ float s_alpha;
     __shared__ int s_brk;
     __shared__ double s_dq;
-    const uint32_t ci = blockIdx.x;
-    const ChunkMeta ch = b.chunks[ci < b.nchunks ? ci : 0];
-    if (ci < b.nchunks && !b.st[ch.mesh].done) {
+    const uint32_t n_act = *(volatile const uint32_t*)(b.act_count + 1);
+    for (uint32_t ia = blockIdx.x; ia < n_act; ia += gridDim.x) {
+        const uint32_t ci = b.act_chunks[ia];
+        const ChunkMeta ch = b.chunks[ci];
         const MeshConsts& c = b.mc[ch.mesh];
         const StepScalars& sm = b.st[ch.mesh];
         // d^T A d of the mesh from its tiles' shares; every block of the mesh
@@ -483,6 +487,8 @@ __global__ void __launch_bounds__(256) k_node_update_fused(BatchView<float> b, c
                 st.dot_dq = s_dq;
                 if (brk) {
                     st.done = 1;
+                    st.finished = 1;
+                    *b.list_dirty = 1u;
                     finish_stats_t(st);
                 } else {
                     const double total = (double)tot.hi + (double)tot.lo;
@@ -495,13 +501,19 @@ __global__ void __launch_bounds__(256) k_node_update_fused(BatchView<float> b, c
                     st.total_iters += 1;
                     if (total != total) st.status = 3u;
                     st.done = cg_cont_t(st) ? 0u : 1u;
-                    if (st.done) finish_stats_t(st);
+                    if (st.done) {
+                        finish_stats_t(st);
+                        st.finished = 1;
+                        *b.list_dirty = 1u;
+                    }
                 }
             }
         }
     }
-    // last block of the grid: while condition and refresh flag
+    // last block of the grid: work lists (when a mesh left its loop), while
+    // condition and refresh flag
     if (!arrive_last_t(ls.gcount, gridDim.x, &s_last)) return;
+    if (*(volatile const unsigned*)b.list_dirty) build_active_lists(b);
     int any = 0, rf = 0;
     for (uint32_t m = threadIdx.x; m < b.M; m += blockDim.x) {
         volatile const StepScalars* sp = b.st + m;
@@ -515,9 +527,14 @@ __global__ void __launch_bounds__(256) k_node_update_fused(BatchView<float> b, c
     rf = __syncthreads_or(rf);
     if (threadIdx.x == 0) {
         const bool stop = ls.err && *(volatile const unsigned*)ls.err;
+        bool budget_left = true;
+        if (ls.slice) {
+            ls.slice[1] += 1u;
+            budget_left = ls.slice[0] == 0u || ls.slice[1] < ls.slice[0];
+        }
         if (ls.refresh_flag) *ls.refresh_flag = rf ? 1u : 0u;
         if (ls.body_runs) *ls.body_runs += 1u;
-        if (ls.set_cond) cudaGraphSetConditional(ls.cond, (any && !stop) ? 1u : 0u);
+        if (ls.set_cond) cudaGraphSetConditional(ls.cond, (any && !stop && budget_left) ? 1u : 0u);
     }
 }
 
@@ -553,17 +570,39 @@ void launch_tile_spmv_pipe(const BatchView<float>& b, const float* d, const floa
     launch_counter()++;
 }
 
+// Grid of the node pass: the blocks that fit on the GPU at once, each
+// walking the chunk list with a stride of the grid.
+static int node_grid()
+{
+    static int grid = 0;
+    if (!grid) {
+        int dev = 0, sms = 0, per_sm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_node_update_fused, kNodeThreads, 0);
+        if (sms <= 0) sms = 152;
+        if (per_sm <= 0) per_sm = 1;
+        grid = sms * per_sm;
+    }
+    return grid;
+}
+
 void launch_node_update_fused(const BatchView<float>& b, const float* part, const float2* tshare,
                               const double* part64, const double* bv, const double* y, float* r, float* d,
                               float2* cshare, const LoopSync& ls, cudaStream_t s)
 {
+    const uint32_t g = (uint32_t)node_grid();
+    const uint32_t grid = b.nchunks < g ? (b.nchunks ? b.nchunks : 1) : g;
     prof_begin("node_update_mixed", s);
-    k_node_update_fused<<<b.nchunks ? b.nchunks : 1, kNodeThreads, 0, s>>>(b, part, tshare, part64, bv, y, r, d,
-                                                                           cshare, ls);
+    k_node_update_fused<<<grid, kNodeThreads, 0, s>>>(b, part, tshare, part64, bv, y, r, d, cshare, ls);
     prof_end("node_update_mixed", s);
     launch_counter()++;
 }
 
-void prepare_tile_pipe() { (void)pipe_grid(); }
+void prepare_tile_pipe()
+{
+    (void)pipe_grid();
+    (void)node_grid();
+}
 
 }  // namespace femgb

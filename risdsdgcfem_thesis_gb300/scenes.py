@@ -212,3 +212,13 @@ def sized_block(rng: np.random.Generator, target_tets: float, idx: int = 0) -> S
     b = max(1, int(round(math.sqrt(cubes / a))))
     c = max(1, int(round(cubes / (a * b))))
     return random_block(rng, idx=idx, dims=(a, b, c))
+
+
+def served_pool(count: int = 4096, seed: int = 0, lo: float = 200.0, hi: float = 200000.0) -> List[Scene]:
+    """The served pool: `count` scenes whose sizes are drawn log-uniform in
+    [lo, hi] tets, each realised as the nearest 5*a*b*c block (material and
+    fixed face as the batched workload)."""
+    rng = np.random.default_rng(seed)
+    targets = np.exp(rng.uniform(np.log(lo), np.log(hi), count))
+    return [sized_block(rng, float(t), idx=i) for i, t in enumerate(targets)]
+

@@ -108,3 +108,42 @@ def test_scene_generator_counts_and_orientation():
             key = tuple(sorted(t[list(f)]))
             faces[key] = faces.get(key, 0) + 1
     assert max(faces.values()) == 2
+
+
+def test_server_host_validation_without_gpu(fem_lib):
+    """Server creation, scene registration and submission checks are host-only."""
+    lib = fem_lib.load()
+    opt = fem_lib.FemServerOptions()
+    assert lib.fem_server_options_default(C.byref(opt)) == fem_lib.FEM_OK
+    assert opt.precision == fem_lib.FEM_PRECISION_MIXED and opt.hbm_budget_bytes == 120 << 30
+    assert opt.slice_iterations == 32
+    bad = fem_lib.FemServerOptions(opt.precision, opt.shard_max_scenes, opt.shard_max_tets, opt.hbm_budget_bytes)
+    bad.precision = 7
+    h = C.c_void_p()
+    assert lib.fem_server_create(C.byref(bad), C.byref(h)) == fem_lib.FEM_E_ARG
+    assert lib.fem_server_create(C.byref(opt), C.byref(h)) == fem_lib.FEM_OK
+    try:
+        rest, tets, _ = scenes.grid_mesh(2, 1, 1, 0.1, 0.0, 0)
+        p = fem_lib.params_for(scenes.cantilever_160(), fem_lib.FEM_PRECISION_MIXED)
+        rest = np.ascontiguousarray(rest, np.float64)
+        t_bad = np.ascontiguousarray(tets, np.uint32).copy()
+        t_bad[0, 0] = rest.shape[0]
+        dp = C.POINTER(C.c_double)
+        up = C.POINTER(C.c_uint32)
+        sid = C.c_uint32()
+        rc = lib.fem_server_add_scene(h, rest.ctypes.data_as(dp), rest.shape[0], t_bad.ctypes.data_as(up),
+                                      t_bad.shape[0], C.byref(p), None, None, None, None, 0, C.byref(sid))
+        assert rc == fem_lib.FEM_E_INDEX
+        t_ok = np.ascontiguousarray(tets, np.uint32)
+        rc = lib.fem_server_add_scene(h, rest.ctypes.data_as(dp), rest.shape[0], t_ok.ctypes.data_as(up),
+                                      t_ok.shape[0], C.byref(p), None, None, None, None, 0, C.byref(sid))
+        assert rc == fem_lib.FEM_OK and sid.value == 0
+        # not admitted yet: a request is refused
+        assert lib.fem_server_submit(h, 0, 1) == fem_lib.FEM_E_ARG
+        assert b"not resident" in lib.fem_last_error()
+        assert lib.fem_server_submit(h, 5, 1) == fem_lib.FEM_E_ARG
+        st = fem_lib.FemServerStatus()
+        assert lib.fem_server_get_status(h, C.byref(st)) == fem_lib.FEM_OK
+        assert st.waiting_scenes == 1 and st.resident_scenes == 0 and st.device_bytes == 0
+    finally:
+        lib.fem_server_destroy(h)

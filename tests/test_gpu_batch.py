@@ -128,6 +128,37 @@ def test_graph_and_host_loop_agree(fem_lib):
         assert a.stats(i)["cg_iterations"] == b.stats(i)["cg_iterations"]
 
 
+@pytest.mark.parametrize("precision,graph", [("fp64", True), ("mixed", True), ("mixed", False)])
+def test_sliced_launches_match_whole_steps(fem_lib, precision, graph):
+    """An iteration budget per launch (steps continued with mask value 2)
+    gives the same bits as whole steps."""
+    p = fem_lib.FEM_PRECISION_FP64 if precision == "fp64" else fem_lib.FEM_PRECISION_MIXED
+    rng = np.random.default_rng(12)
+    scs = [scenes.random_block(rng, idx=i, dims=(4 + i, 3, 5)) for i in range(4)]
+    whole = fem_lib.Batch(scs, precision=p, use_graph=graph)
+    sliced = fem_lib.Batch(scs, precision=p, use_graph=graph)
+    sliced.set_slice(7)
+    for _ in range(3):
+        whole.step(1)
+        sliced.set_active(None)
+        sliced.step(1)
+        launches = 1
+        while True:
+            f = sliced.finished()
+            if not (f == 2).any():
+                break
+            sliced.set_active(np.where(f == 2, 2, 0).astype(np.uint8))
+            sliced.step(1)
+            launches += 1
+        assert launches > 1
+        for i in range(len(scs)):
+            assert whole.stats(i)["cg_iterations"] == sliced.stats(i)["cg_iterations"]
+    for i in range(len(scs)):
+        xa, va = whole.state(i)
+        xb, vb = sliced.state(i)
+        assert np.array_equal(xa, xb) and np.array_equal(va, vb), i
+
+
 def test_compression_counts_fp64_resolves(fem_lib):
     sc = scenes.compressed_cube(n=6, steps=20, ratio=0.2)
     b = fem_lib.Batch([sc], precision=fem_lib.FEM_PRECISION_MIXED)
