@@ -161,14 +161,16 @@ def dist_info():
 
 
 def aggregate(values, ws):
-    """(value, "max"|"sum") pairs reduced over ranks under torchrun (NCCL)."""
+    """(value, "max"|"sum") pairs reduced over the ranks of the process group
+    (NCCL under torchrun on GPUs, gloo on CPU)."""
     if ws <= 1:
         return [v for v, _ in values]
     import torch
     import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
     out = []
     for v, op in values:
-        t = torch.tensor([v], dtype=torch.float64, device="cuda")
+        t = torch.tensor([v], dtype=torch.float64, device=dev)
         dist.all_reduce(t, op=dist.ReduceOp.MAX if op == "max" else dist.ReduceOp.SUM)
         out.append(float(t.item()))
     return out
@@ -318,8 +320,17 @@ def run_ours(args):
     capi.load()
     scs, precision = workload(args.workload, rank)
     prec = capi.FEM_PRECISION_MIXED if precision == "mixed" else capi.FEM_PRECISION_FP64
+    tuned = None
+    tile_elems, reorder = 256, True
+    if not args.no_tune:
+        from risdsdgcfem_thesis_gb300 import autotune
+        t0 = time.perf_counter()
+        tuned = autotune.tune(scs, prec, use_cache=False)
+        tuned["tune_s"] = round(time.perf_counter() - t0, 1)
+        tile_elems, reorder = tuned["tile_elems"], bool(tuned["reorder"])
     t0 = time.perf_counter()
-    batch = capi.Batch(scs, precision=prec, compute_energy=True, use_graph=not args.no_graph)
+    batch = capi.Batch(scs, precision=prec, tile_elems=tile_elems, reorder=reorder, compute_energy=True,
+                       use_graph=not args.no_graph)
     setup_s = time.perf_counter() - t0
     info = batch.info()
     stream_ptr = batch.stream()
@@ -383,7 +394,10 @@ def run_ours(args):
     plain = None
     cpu = None
     served = None
+    compression = None
     if rank == 0 and ws == 1:
+        if not args.no_compression:
+            compression = compression_report()
         if not args.no_served:
             served = served_leg(args.served_rate, args.served_seconds, pool_count=args.served_pool)
         if not args.no_plain:
@@ -416,6 +430,7 @@ def run_ours(args):
                        "l2": f"inputs larger than L2: {elem_bytes / 1e6:.0f} MB of element data streamed per CG "
                              f"iteration vs {L2_BYTES / 1e6:.0f} MB L2",
                        "cg_iterations_timed_max_mesh": int(max(iters)), "setup_s": round(setup_s, 2),
+                       "tile_elems": tile_elems, "reorder": reorder, "autotune": tuned,
                        "graph": not args.no_graph},
             "p50_step_ms": float(np.percentile(step_ms, 50)), "p99_step_ms": float(np.percentile(step_ms, 99)),
             "clocks": clk,
@@ -436,6 +451,7 @@ def run_ours(args):
             "plain_fp64_gpu": plain,
             "cpu_baseline": cpu,
             "served": served,
+            "compression": compression,
         }
         if plain:
             line["speedup_vs_plain_fp64_gpu"] = value / plain["value"]
@@ -444,6 +460,68 @@ def run_ours(args):
         torch.distributed.barrier()
         torch.distributed.destroy_process_group()
     return 0
+
+
+# ---------------------------------------------------------------- compression
+def compression_report(n=40, steps=120, ratio=0.4):
+    """The large-deformation case: an n^3 x 5-tet cube (E 2e5, nu 0.45)
+    compressed by its top face to `ratio` of its height over `steps` steps.
+    The mixed path (FP32 rotations; FP64 re-solve where det F <= 1e-3, and by
+    default also where the FP32 rotation is sensitive to rounding) against the
+    plain FP64 path (itself parity-tested against the FP64 oracle), step by
+    step: share of elements re-solved in FP64 and inverted, CG iterations,
+    and the final error; once with the default re-solve rule and once with
+    the det F rule alone."""
+    from risdsdgcfem_thesis_gb300 import capi, scenes
+    sc = scenes.compressed_cube(n, steps, ratio)
+    T = float(sc.num_tets)
+    f64 = capi.Batch([sc], precision=capi.FEM_PRECISION_FP64, compute_energy=False)
+    it64, xs64, vscale, t64 = [], None, 0.0, 0.0
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        f64.step(1)
+        t64 += time.perf_counter() - t0
+        it64.append(f64.stats(0)["cg_iterations"])
+        vscale = max(vscale, float(np.linalg.norm(f64.state(0)[1])))
+    x64, v64 = f64.state(0)
+    f64.close()
+    # the FP64 path's own sensitivity: the same run from an initial velocity
+    # perturbed by 1e-15 (relative to the mesh size)
+    pert = capi.Batch([sc], precision=capi.FEM_PRECISION_FP64, compute_energy=False)
+    v0 = 1e-15 * float(np.abs(sc.rest).max()) * np.random.default_rng(1).standard_normal(sc.rest.shape)
+    pert.set_state(0, v=v0)
+    pert.step(steps)
+    xp, vp = pert.state(0)
+    pert.close()
+    noise = {"x_rel": float(np.linalg.norm(xp - x64) / np.linalg.norm(x64)),
+             "v": float(np.linalg.norm(vp - v64) / vscale) if vscale > 0 else None}
+
+    def mixed(check):
+        mix = capi.Batch([sc], precision=capi.FEM_PRECISION_MIXED, compute_energy=False, rotation_check=check)
+        res, inv, itm, tm = [], [], [], 0.0
+        for _ in range(steps):
+            t0 = time.perf_counter()
+            mix.step(1)
+            tm += time.perf_counter() - t0
+            b = mix.stats(0)
+            res.append(b["fp64_resolved"] / T)
+            inv.append(b["inverted_elements"] / T)
+            itm.append(b["cg_iterations"])
+        xm, vm = mix.state(0)
+        mix.close()
+        return {"fp64_resolved_fraction_max": max(res), "fp64_resolved_fraction_mean": float(np.mean(res)),
+                "inverted_fraction_max": max(inv),
+                "x_rel_err_vs_fp64_path": float(np.linalg.norm(xm - x64) / np.linalg.norm(x64)),
+                "v_err_vs_fp64_path": float(np.linalg.norm(vm - v64) / vscale) if vscale > 0 else None,
+                "cg_iterations_mean": float(np.mean(itm)), "wall_s": tm}
+
+    return {"case": f"{n}^3 x 5 tets ({int(T)}), top face to {ratio:.0%} height over {steps} steps, "
+                    f"E 2e5, nu 0.45, dt 1/60, CG rel 1e-6",
+            "mixed_default": mixed(1e-3), "mixed_det_F_rule_only": mixed(0.0),
+            "fp64_path_noise_floor": noise,
+            "cg_iterations_fp64_mean": float(np.mean(it64)), "wall_s_fp64": t64,
+            "note": "v error normalised by the run's peak |v|; the FP64 path matches the FP64 oracle "
+                    "(tests/test_gpu_fp64.py, tests/test_gpu_batch.py)"}
 
 
 # ---------------------------------------------------------------- served leg
@@ -518,6 +596,8 @@ def main():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-graph", action="store_true", help="launch kernels one by one (for per-kernel profilers)")
     ap.add_argument("--no-served", action="store_true")
+    ap.add_argument("--no-compression", action="store_true")
+    ap.add_argument("--no-tune", action="store_true", help="default tiles (256 tets, Morton order)")
     ap.add_argument("--served-rate", type=float, default=20000.0, help="offered step requests per second")
     ap.add_argument("--served-seconds", type=float, default=3.0)
     ap.add_argument("--served-pool", type=int, default=4096)

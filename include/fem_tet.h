@@ -39,9 +39,11 @@ enum fem_precision {
      * drop-in for the reference's FP64 step. */
     FEM_PRECISION_FP64 = 0,
     /* Mixed: FP32 element products and vector updates, FP64 dot products and
-     * norms, FP64 residual refresh r = b - A x every refresh_every
-     * iterations, FP32 rotations re-solved in FP64 where det F <=
-     * degenerate_det_F. */
+     * norms, FP64 residual refresh r = b - A x when |r| has fallen by
+     * refresh_drop since the last one (or after refresh_every iterations),
+     * FP32 rotations re-solved in FP64 where det F <=
+     * degenerate_det_F or where the FP32 rotation is sensitive to rounding
+     * (rotation_check). */
     FEM_PRECISION_MIXED = 1
 };
 
@@ -65,8 +67,16 @@ typedef struct fem_params {
     uint32_t ls_max_iter;     /* CG iteration cap per step */
     uint32_t precision;       /* enum fem_precision */
     double degenerate_det_F;  /* mixed only: FP64 rotation re-solve threshold */
-    uint32_t refresh_every;   /* mixed only: FP64 residual refresh period (0 = never) */
+    uint32_t refresh_every;   /* mixed only: longest run of iterations between FP64
+                                 residuals (0 = no periodic refresh) */
     uint32_t compute_energy;  /* 1: elastic and potential energy every step (as FixedStep) */
+    double rotation_check;    /* mixed only: an FP32 rotation is also re-solved in FP64
+                                 when it moves by more than this (max entry) under a
+                                 2^-14 relative change of F; 0 = det F test only */
+    double refresh_drop;      /* mixed only: the residual is recomputed in FP64 once |r|
+                                 has fallen by this factor since the last time (reliable
+                                 updates), and at least every refresh_every iterations;
+                                 0 = by refresh_every alone */
 } fem_params;
 
 /* Per-step statistics (the Leaf's per-step LS stats, LeafDSH_Solid3D_FEM.h:597-622). */
@@ -87,7 +97,7 @@ typedef struct fem_solid_s* fem_solid;
 /* Fills the reference defaults (fem::Params, LeafDSH_Solid3D_FEM::Params):
  * fixed_dt 0.001, density 1000, E 1000, nu 0.25, damping 1, gravity 0,
  * CG rel 1e-3, abs 1e-6, 20 iterations, FP64, threshold 1e-3, refresh 50,
- * energy on. */
+ * energy on, rotation check 1e-3, refresh every 50 iterations (no drop rule). */
 int fem_params_default(fem_params* p);
 
 /* Replaces: EditableTetrahedronElementSet3::BeginEdition/AddElement/EndEdition

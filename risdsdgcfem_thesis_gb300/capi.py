@@ -39,6 +39,8 @@ class FemParams(C.Structure):
         ("degenerate_det_F", C.c_double),
         ("refresh_every", C.c_uint32),
         ("compute_energy", C.c_uint32),
+        ("rotation_check", C.c_double),
+        ("refresh_drop", C.c_double),
     ]
 
 
@@ -381,7 +383,8 @@ class Batch:
     """Many independent solids stepped together on one GPU (fem_batch_*)."""
 
     def __init__(self, scenes_list, precision=FEM_PRECISION_MIXED, tile_elems=256, reorder=True, use_graph=True,
-                 compute_energy=True, refresh_every=None, degenerate_det_F=None):
+                 compute_energy=True, refresh_every=None, degenerate_det_F=None, rotation_check=None,
+                 refresh_drop=None):
         lib = load()
         self.lib = lib
         self.scenes = list(scenes_list)
@@ -397,6 +400,10 @@ class Batch:
                 p.refresh_every = refresh_every
             if degenerate_det_F is not None:
                 p.degenerate_det_F = degenerate_det_F
+            if rotation_check is not None:
+                p.rotation_check = rotation_check
+            if refresh_drop is not None:
+                p.refresh_drop = refresh_drop
             rest = _f64(sc.rest)
             tets = np.ascontiguousarray(sc.tets, dtype=np.uint32)
             idx = C.c_uint32()

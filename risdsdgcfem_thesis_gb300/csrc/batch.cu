@@ -704,6 +704,8 @@ int fem_batch_finalize(fem_batch b)
         c.rel_eps_sq = p.ls_rel_epsilon * p.ls_rel_epsilon;
         c.abs_eps_sq = p.ls_abs_epsilon * p.ls_abs_epsilon;
         c.degenerate_det_F = p.degenerate_det_F;
+        c.rot_check = (float)p.rotation_check;
+        c.refresh_drop_sq = fp64 ? 0.0 : p.refresh_drop * p.refresh_drop;
         c.max_iter = p.ls_max_iter;
         c.refresh_every = fp64 ? 0u : p.refresh_every;
         c.fK_f = (float)c.factor_K;
@@ -781,8 +783,8 @@ int fem_batch_finalize(fem_batch b)
             for (uint32_t i = 0; i <= tm.nn; i++) lp[i] = src_lp[i];
             uint16_t* li = lp + (tm.nn + 1);
             for (uint32_t j = 0; j < 4u * tm.ne; j++) {
-                const uint16_t v = lidx[tm.c0 + j];  // (element << 2 | slot) -> (slot << 8 | element)
-                li[j] = (uint16_t)(((v & 3u) << 8) | (v >> 2));
+                const uint16_t v = lidx[tm.c0 + j];  // (element << 2 | slot) -> slot * ne4 + element
+                li[j] = (uint16_t)((v & 3u) * ne4 + (v >> 2));
             }
             uint32_t* nodes = reinterpret_cast<uint32_t*>(base + blob_nodes_off(tm.ne, tm.nn));
             // bit 31: this tile owns the node (the first tile, in tile order, that lists it)

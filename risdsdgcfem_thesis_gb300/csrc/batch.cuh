@@ -70,6 +70,9 @@ struct MeshConsts {
     uint32_t tile0, ntiles, chunk0, nchunks;
     uint32_t knc0, nknc;
     float fK_f, mfm_f;  // factor_K and mass * factor_M rounded to FP32 (mixed path)
+    float rot_check;    // mixed: FP64 re-solve when an FP32 rotation moves more than this under a small change of F
+    double refresh_drop_sq;  // mixed: FP64 residual when |r|^2 fell below this times its value at the last one
+
 };
 
 template <typename S>

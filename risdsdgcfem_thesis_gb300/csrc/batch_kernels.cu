@@ -113,11 +113,9 @@ __device__ __forceinline__ double y_full(const BatchView<S>& b, const double* __
     return b.ydelta ? y[i] + (double)b.ydelta[i] : y[i];
 }
 
-// CG iteration index at which the mesh refreshes its residual in FP64.
-__device__ __forceinline__ bool refresh_now(const MeshConsts& c, const StepScalars& s)
-{
-    return c.refresh_every > 0 && ((s.k + 1) % c.refresh_every) == 0;
-}
+// Whether the mesh's next iteration recomputes its residual in FP64 (set by
+// the last block of the mesh in the node pass, see refresh_decide).
+__device__ __forceinline__ bool refresh_now(const MeshConsts&, const StepScalars& s) { return s.refresh_next != 0; }
 
 // ---------------------------------------------------------------------------
 // Element tile product of the new search direction: for each local node the
@@ -525,7 +523,7 @@ __device__ void grid_tail(const BatchView<S>& b, const LoopSync& ls, bool iterat
         if (!sp->done) {
             any = 1;
             const MeshConsts& c = b.mc[i];
-            if (c.refresh_every > 0 && ((sp->k + 1) % c.refresh_every) == 0) refresh = 1;
+            if (sp->refresh_next) refresh = 1;
         }
     }
     any = __syncthreads_or(any);
@@ -589,6 +587,9 @@ __global__ void k_node_residual(BatchView<S> b, const double* __restrict__ part6
                 s.alpha = 0.0;
                 s.beta = 0.0;
                 s.beta_f = 0.f;
+                s.refresh_next = 0;  // r0 was formed from the FP64 product
+                s.delta_refresh = total;
+                s.k_refresh = 0;
                 s.done = cg_cont(s) ? 0u : 1u;
                 if (s.done) {
                     finish_stats(s);

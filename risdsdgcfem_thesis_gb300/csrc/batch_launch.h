@@ -28,7 +28,7 @@ void launch_tile_spmv_pipe(const BatchView<float>& b, const float* d, const floa
                            cudaGraphConditionalHandle if_refresh, int set_if, const unsigned* refresh_flag,
                            unsigned* err, cudaStream_t s);
 void launch_node_update_fused(const BatchView<float>& b, const float* part, const float2* tshare,
-                              const double* part64, const double* bv, const double* y, float* r, float* d,
+                              const double* part64, const double* bv, double* y, float* r, float* d,
                               float2* cshare, const LoopSync& ls, cudaStream_t s);
 
 template <typename S>

@@ -31,8 +31,10 @@ struct StepScalars {
     uint32_t k, max_iter, done, status;
     uint32_t inverted, fp64_resolved, refresh_every;
     float beta_f;       // beta rounded to FP32 (mixed path)
-    uint32_t finished;  // batch: the CG loop ended during this launch (cleared at launch start)
-    uint32_t pad2;
+    uint32_t finished;      // batch: the CG loop ended during this launch (cleared at launch start)
+    uint32_t refresh_next;  // mixed: the next iteration recomputes r = b - A y in FP64
+    double delta_refresh;   // mixed: |r|^2 right after the last FP64 residual
+    uint32_t k_refresh, pad3;
     unsigned long long total_iters;
 };
 

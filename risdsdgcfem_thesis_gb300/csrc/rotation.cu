@@ -59,6 +59,39 @@ void launch_begin_eval_fp64(const MeshView<double>& m, const double* x, double* 
 // mesh's threshold, where F is re-solved in FP64. Per-mesh counts of
 // inverted elements and FP64 re-solves are added with integer atomics (one
 // per tile), so they do not depend on scheduling.
+// FP32 rotation of F for the mixed path. With tol > 0 the rotation is
+// computed again for F plus a fixed 2^-14 relative change; when the two
+// differ by more than tol (max entry), the FP32 result is not trusted
+// (near-coincident singular values make the MSVD's eigenvector steps
+// sensitive to rounding) and false is returned for an FP64 re-solve.
+template <typename S>
+__device__ __forceinline__ bool rotation_fp32(const double* F, float tol, S* Rs)
+{
+    float Ff[9], Rf[9];
+    float s = 0.f;
+#pragma unroll
+    for (int c = 0; c < 9; c++) {
+        Ff[c] = (float)F[c];
+        s = fmaxf(s, fabsf(Ff[c]));
+    }
+    msvd_rotation(Ff, Rf);
+    if (tol > 0.f) {
+        const float d = s * 6.103515625e-05f;  // 2^-14 of the largest entry
+        const float P[9] = {1.f, -1.f, 0.f, 0.f, 1.f, -1.f, 1.f, 0.f, 1.f};
+        float Fp[9], Rp[9];
+#pragma unroll
+        for (int c = 0; c < 9; c++) Fp[c] = Ff[c] + d * P[c];
+        msvd_rotation(Fp, Rp);
+        float diff = 0.f;
+#pragma unroll
+        for (int c = 0; c < 9; c++) diff = fmaxf(diff, fabsf(Rf[c] - Rp[c]));
+        if (!(diff <= tol)) return false;  // also when NaN
+    }
+#pragma unroll
+    for (int c = 0; c < 9; c++) Rs[c] = (S)Rf[c];
+    return true;
+}
+
 template <typename S>
 __global__ void k_begin_eval_batch(BatchView<S> b, const double* __restrict__ x)
 {
@@ -90,13 +123,8 @@ __global__ void k_begin_eval_batch(BatchView<S> b, const double* __restrict__ x)
                 msvd_rotation(F, R);
 #pragma unroll
                 for (int c = 0; c < 9; c++) Rs[c] = (S)R[c];
-            } else if (detF > b.mc[tm.mesh].degenerate_det_F) {
-                float Ff[9], Rf[9];
-#pragma unroll
-                for (int c = 0; c < 9; c++) Ff[c] = (float)F[c];
-                msvd_rotation(Ff, Rf);
-#pragma unroll
-                for (int c = 0; c < 9; c++) Rs[c] = (S)Rf[c];
+            } else if (detF > b.mc[tm.mesh].degenerate_det_F && rotation_fp32(F, b.mc[tm.mesh].rot_check, Rs)) {
+                // FP32 rotation kept
             } else {
                 double R[9];
                 msvd_rotation(F, R);
@@ -127,7 +155,9 @@ __global__ void k_begin_eval_batch(BatchView<S> b, const double* __restrict__ x)
 template <typename S>
 void BatchLaunch<S>::begin_eval(const BatchView<S>& b, const double* x, cudaStream_t s)
 {
+    prof_begin("begin_eval_batch", s);
     k_begin_eval_batch<S><<<grid_tiles(b.ntiles), kTileElems, 0, s>>>(b, x);
+    prof_end("begin_eval_batch", s);
     launch_counter()++;
 }
 

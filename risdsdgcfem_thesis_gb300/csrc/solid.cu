@@ -251,7 +251,9 @@ int fem_params_default(fem_params* p)
     p->ls_max_iter = 20;
     p->precision = FEM_PRECISION_FP64;
     p->degenerate_det_F = 1e-3;
+    p->rotation_check = 1e-3;
     p->refresh_every = 50;
+    p->refresh_drop = 0.0;
     p->compute_energy = 1;
     return FEM_OK;
 }

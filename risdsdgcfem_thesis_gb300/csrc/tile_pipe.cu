@@ -31,7 +31,7 @@
 //   0            float comp[22][ne4]: R (9), Dm^-1 (9), V(lambda+2mu), V lambda,
 //                V mu, local ids (uchar4 as one word)
 //   88 ne4       uint16 lptr[nn+1]      tile-local CSR offsets
-//   + 2(nn+1)    uint16 lidx[4 ne]      (slot << 8 | element), element order
+//   + 2(nn+1)    uint16 lidx[4 ne]      slot * ne4 + element, element order
 //   (4-aligned)  uint32 nodes[nn]       global node id, bit 31 = owner
 //   size rounded up to 16.
 //
@@ -203,10 +203,11 @@ __device__ __forceinline__ void finish_stats_t(StepScalars& s)
 constexpr uint32_t kStageBytes = 26240;  // >= blob_bytes(256, 256), multiple of 128
 static_assert(kStageBytes >= 26128, "stage must hold the largest tile blob");
 
-// Shared memory: two blob stages, the staged direction sd4[256], the
-// element outputs so4[4][256] (slot-major), two mbarriers and the warps'
-// (hi, lo) shares.
-constexpr uint32_t kPipeSmem = 2 * kStageBytes + 16u * (kTileNodes + 4 * kTileElems) + 16u + 8u * 8u;
+// Shared memory: two blob stages (a tile's element outputs overwrite its
+// element data once every element has read it), the staged direction
+// sd4[256], two mbarriers and the warps' (hi, lo) shares: 56.7 KB, four
+// resident blocks per SM.
+constexpr uint32_t kPipeSmem = 2 * kStageBytes + 16u * kTileNodes + 16u + 8u * 8u;
 
 // What a block needs to know of one tile before its blob arrives.
 struct TileLook {
@@ -240,7 +241,7 @@ __device__ __forceinline__ void look_resolve(const BatchView<float>& b, TileLook
     L.g = threadIdx.x < (L.nenn >> 16) ? __ldg(b.tile_nodes + L.n0 + threadIdx.x) : 0u;
 }
 
-__global__ void __launch_bounds__(256, 3) k_tile_spmv_pipe(BatchView<float> b, const float* __restrict__ dvec,
+__global__ void __launch_bounds__(256, 4) k_tile_spmv_pipe(BatchView<float> b, const float* __restrict__ dvec,
                                                            const float* __restrict__ rvec, float* __restrict__ part,
                                                            float2* __restrict__ tshare,
                                                            cudaGraphConditionalHandle if_refresh, int set_if,
@@ -249,8 +250,7 @@ __global__ void __launch_bounds__(256, 3) k_tile_spmv_pipe(BatchView<float> b, c
 {
     extern __shared__ __align__(128) unsigned char smem[];
     float4* sd4 = reinterpret_cast<float4*>(smem + 2 * kStageBytes);
-    float4* so4 = sd4 + kTileNodes;  // so4[slot * 256 + element]
-    uint64_t* bar = reinterpret_cast<uint64_t*>(so4 + 4 * kTileElems);
+    uint64_t* bar = reinterpret_cast<uint64_t*>(sd4 + kTileNodes);
     float2* wsh = reinterpret_cast<float2*>(bar + 2);  // [8] per-warp shares
     const uint32_t G = gridDim.x, tid = threadIdx.x;
 
@@ -336,6 +336,7 @@ __global__ void __launch_bounds__(256, 3) k_tile_spmv_pipe(BatchView<float> b, c
                 if (nodes[tid] >> 31) share = mfm * (dx * dx + dy * dy + dz * dz);
             }
             __syncthreads();
+            float out[12];
             if (tid < ne) {
                 const int i = tid;
                 float R[9], Di[9];
@@ -355,17 +356,22 @@ __global__ void __launch_bounds__(256, 3) k_tile_spmv_pipe(BatchView<float> b, c
                     dl[3 * k + 1] = v.y;
                     dl[3 * k + 2] = v.z;
                 }
-                float out[12];
                 elem_RKRt<float>(R, Di, k1, knu, k2, dl, out);
                 float eq = 0.f;
 #pragma unroll
                 for (int k = 0; k < 12; k++) eq = __fmaf_rn(dl[k], out[k], eq);
                 share = __fmaf_rn(fK, eq, share);
-#pragma unroll
-                for (int k = 0; k < 4; k++)
-                    so4[k * kTileElems + i] = make_float4(out[3 * k], out[3 * k + 1], out[3 * k + 2], 0.f);
             }
             look_resolve(b, n2);
+            // every element's data has been read: its space takes the outputs,
+            // so4[slot * ne4 + element]
+            __syncthreads();
+            float4* so4 = reinterpret_cast<float4*>(smem + s * kStageBytes);
+            if (tid < ne) {
+#pragma unroll
+                for (int k = 0; k < 4; k++)
+                    so4[k * ne4 + tid] = make_float4(out[3 * k], out[3 * k + 1], out[3 * k + 2], 0.f);
+            }
             __syncthreads();
             if (tid < nn) {
                 float a0 = 0.f, a1 = 0.f, a2 = 0.f;
@@ -408,7 +414,7 @@ __global__ void __launch_bounds__(256) k_node_update_fused(BatchView<float> b, c
                                                            const float2* __restrict__ tshare,
                                                            const double* __restrict__ part64,
                                                            const double* __restrict__ bv,
-                                                           const double* __restrict__ y, float* __restrict__ r,
+                                                           double* __restrict__ y, float* __restrict__ r,
                                                            float* __restrict__ d, float2* __restrict__ cshare,
                                                            LoopSync ls)
 {
@@ -434,7 +440,7 @@ __global__ void __launch_bounds__(256) k_node_update_fused(BatchView<float> b, c
         }
         __syncthreads();
         const bool brk = s_brk != 0;
-        const bool refresh = c.refresh_every > 0 && ((sm.k + 1) % c.refresh_every) == 0;
+        const bool refresh = sm.refresh_next != 0;
         const float beta = sm.beta_f;
         const float alpha_s = s_alpha, na = -alpha_s;
         const float fK = c.fK_f, mfm = c.mfm_f;
@@ -455,6 +461,7 @@ __global__ void __launch_bounds__(256) k_node_update_fused(BatchView<float> b, c
             }
             const float q0 = fK * s0 + mfm * d0, q1 = fK * s1 + mfm * d1, q2 = fK * s2 + mfm * d2;
             float r0 = r[i], r1 = r[i + 1], r2 = r[i + 2];
+            float e0 = b.ydelta[i], e1 = b.ydelta[i + 1], e2 = b.ydelta[i + 2];
             if (refresh) {
                 double t0 = 0, t1 = 0, t2 = 0;
                 for (uint32_t j = b.nptr[n]; j < j1; j++) {
@@ -464,13 +471,21 @@ __global__ void __launch_bounds__(256) k_node_update_fused(BatchView<float> b, c
                     t2 += part64[o + 2];
                 }
                 const double mfm64 = c.mass * c.factor_M;
-                r0 = (float)(bv[i] - (c.factor_K * t0 + mfm64 * (y[i] + (double)b.ydelta[i])));
-                r1 = (float)(bv[i + 1] - (c.factor_K * t1 + mfm64 * (y[i + 1] + (double)b.ydelta[i + 1])));
-                r2 = (float)(bv[i + 2] - (c.factor_K * t2 + mfm64 * (y[i + 2] + (double)b.ydelta[i + 2])));
+                const double ya = y[i] + (double)e0, yb = y[i + 1] + (double)e1, yc = y[i + 2] + (double)e2;
+                r0 = (float)(bv[i] - (c.factor_K * t0 + mfm64 * ya));
+                r1 = (float)(bv[i + 1] - (c.factor_K * t1 + mfm64 * yb));
+                r2 = (float)(bv[i + 2] - (c.factor_K * t2 + mfm64 * yc));
+                // fold the FP32 increment into the FP64 iterate: later small
+                // corrections then keep their bits (an FP32 sum that has grown
+                // large would absorb them)
+                y[i] = ya;
+                y[i + 1] = yb;
+                y[i + 2] = yc;
+                e0 = e1 = e2 = 0.f;
             }
-            b.ydelta[i] += alpha_s * d0;
-            b.ydelta[i + 1] += alpha_s * d1;
-            b.ydelta[i + 2] += alpha_s * d2;
+            b.ydelta[i] = __fmaf_rn(alpha_s, d0, e0);
+            b.ydelta[i + 1] = __fmaf_rn(alpha_s, d1, e1);
+            b.ydelta[i + 2] = __fmaf_rn(alpha_s, d2, e2);
             r0 += na * q0;
             r1 += na * q1;
             r2 += na * q2;
@@ -500,6 +515,17 @@ __global__ void __launch_bounds__(256) k_node_update_fused(BatchView<float> b, c
                     st.k += 1;
                     st.total_iters += 1;
                     if (total != total) st.status = 3u;
+                    // reliable updates: recompute the residual in FP64 once |r|
+                    // has fallen by refresh_drop since the last FP64 residual,
+                    // and at least every refresh_every iterations
+                    if (st.refresh_next) {
+                        st.delta_refresh = total;
+                        st.k_refresh = st.k;
+                    }
+                    st.refresh_next = ((c.refresh_drop_sq > 0.0 && total < c.refresh_drop_sq * st.delta_refresh) ||
+                                       (c.refresh_every > 0 && st.k - st.k_refresh >= c.refresh_every))
+                                          ? 1u
+                                          : 0u;
                     st.done = cg_cont_t(st) ? 0u : 1u;
                     if (st.done) {
                         finish_stats_t(st);
@@ -520,7 +546,7 @@ __global__ void __launch_bounds__(256) k_node_update_fused(BatchView<float> b, c
         if (!sp->done) {
             any = 1;
             const MeshConsts& c = b.mc[m];
-            if (c.refresh_every > 0 && ((sp->k + 1) % c.refresh_every) == 0) rf = 1;
+            if (sp->refresh_next) rf = 1;
         }
     }
     any = __syncthreads_or(any);
@@ -588,7 +614,7 @@ static int node_grid()
 }
 
 void launch_node_update_fused(const BatchView<float>& b, const float* part, const float2* tshare,
-                              const double* part64, const double* bv, const double* y, float* r, float* d,
+                              const double* part64, const double* bv, double* y, float* r, float* d,
                               float2* cshare, const LoopSync& ls, cudaStream_t s)
 {
     const uint32_t g = (uint32_t)node_grid();

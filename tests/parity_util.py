@@ -23,8 +23,10 @@ def oracle_run(oracle, sc, steps, seeds=(1, 2, 3)):
     b = oracle.Solid(sc, "port")
     noisy = [oracle.Solid(perturbed(sc, s), "port") for s in seeds]
     it, it_noise = [], [[] for _ in noisy]
+    vmax = 0.0
     for _ in range(steps):
         it.append(b.step()["iters"])
+        vmax = max(vmax, float(np.linalg.norm(b.state()[1])))
         for c, lst in zip(noisy, it_noise):
             lst.append(c.step()["iters"])
     xb, vb = b.state()
@@ -33,4 +35,4 @@ def oracle_run(oracle, sc, steps, seeds=(1, 2, 3)):
         xc, vc = c.state()
         nx, nv = max(nx, rel(xc, xb)), max(nv, rel(vc, vb))
     spread = max(abs(i - j) for lst in it_noise for i, j in zip(it, lst))
-    return {"x": xb, "v": vb, "iters": it, "noise_x": nx, "noise_v": nv, "spread": spread}
+    return {"x": xb, "v": vb, "iters": it, "noise_x": nx, "noise_v": nv, "spread": spread, "vmax": vmax}

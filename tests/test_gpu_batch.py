@@ -159,6 +159,77 @@ def test_sliced_launches_match_whole_steps(fem_lib, precision, graph):
         assert np.array_equal(xa, xb) and np.array_equal(va, vb), i
 
 
+def test_compressed_cube_fp64_and_mixed_vs_oracle(fem_lib, oracle):
+    """Large deformation at a size the oracle runs in seconds: the 8^3 x 5
+    cube (E 2e5, nu 0.45) compressed by its top face to 40 % of its height
+    over 120 steps. The case is close to unstable: 1e-15 changes of the input
+    move the oracle's final positions by ~1e-8, and stopping its CG at rel
+    1e-7 instead of 1e-6 moves them by ~1e-7 (velocities ~1e-5).
+    FP64 path: rel-L2 <= max(1e-10, 10 x the input-noise floor).
+    Mixed path (FP32 rotations re-solved in FP64 where det F <= 1e-3 or the
+    rotation is sensitive to rounding): positions rel-L2 and velocities
+    (normalised by the run's peak |v|) <= max(1e-5, 10 x the oracle's own
+    CG-tolerance spread); some rotations take the FP64 path."""
+    sc = scenes.compressed_cube(n=8, steps=120, ratio=0.4)
+    ref = oracle_run(oracle, sc, 120)
+    tight = oracle.Solid(sc, "port")
+    tight.set_solver(sc.rel_eps / 10, sc.abs_eps, sc.max_iter)
+    for _ in range(120):
+        tight.step()
+    xt, vt = tight.state()
+    tol_x = rel(ref["x"], xt)
+    tol_v = float(np.linalg.norm(ref["v"] - vt)) / ref["vmax"]
+    f64 = fem_lib.Batch([sc], precision=fem_lib.FEM_PRECISION_FP64, compute_energy=False)
+    mix = fem_lib.Batch([sc], precision=fem_lib.FEM_PRECISION_MIXED, compute_energy=False)
+    resolved = 0
+    for _ in range(120):
+        f64.step(1)
+        mix.step(1)
+        resolved = max(resolved, mix.stats(0)["fp64_resolved"])
+        assert mix.stats(0)["status"] == 0 and f64.stats(0)["status"] == 0
+    x, v = f64.state(0)
+    assert rel(x, ref["x"]) <= max(1e-10, 10 * ref["noise_x"]), (rel(x, ref["x"]), ref["noise_x"])
+    assert rel(v, ref["v"]) <= max(1e-10, 10 * ref["noise_v"]), (rel(v, ref["v"]), ref["noise_v"])
+    xm, vm = mix.state(0)
+    ex = rel(xm, ref["x"])
+    ev = float(np.linalg.norm(vm - ref["v"])) / ref["vmax"]
+    assert ex <= max(1e-5, 10 * tol_x) and ev <= max(1e-5, 10 * tol_v), (ex, ev, tol_x, tol_v)
+    assert resolved > 0
+
+
+def test_mixed_converges_like_fp64_on_stiff_meshes(fem_lib):
+    """Stiff meshes of the batched workload (E up to 1e6 Pa): the mixed CG
+    reaches the same relative tolerance in about the iterations the FP64 CG
+    needs (per mesh within 10 % or 12 iterations, on average within 3 %: no
+    stagnation at the iteration cap), and its states stay within 1e-5 of the
+    FP64 path's."""
+    rng = np.random.default_rng(77)
+    scs = []
+    for i in range(24):
+        sc = scenes.random_block(rng, lo=6, hi=16, idx=i)
+        sc.young = float(np.exp(rng.uniform(np.log(2e5), np.log(1e6))))
+        scs.append(sc)
+    f64 = fem_lib.Batch(scs, precision=fem_lib.FEM_PRECISION_FP64, compute_energy=False)
+    mix = fem_lib.Batch(scs, precision=fem_lib.FEM_PRECISION_MIXED, compute_energy=False)
+    vmax = np.zeros(len(scs))
+    n64 = nmix = 0
+    for _ in range(4):
+        f64.step(1)
+        mix.step(1)
+        for i in range(len(scs)):
+            a, m = f64.stats(i), mix.stats(i)
+            n64 += a["cg_iterations"]
+            nmix += m["cg_iterations"]
+            assert m["cg_iterations"] <= a["cg_iterations"] + max(12, 0.1 * a["cg_iterations"]), (i, a, m)
+            assert m["rel_residual"] <= scs[i].rel_eps * 1.0001 or m["cg_iterations"] >= a["cg_iterations"], (i, m)
+            vmax[i] = max(vmax[i], float(np.linalg.norm(f64.state(i)[1])))
+    assert nmix <= 1.03 * n64, (nmix, n64)
+    for i in range(len(scs)):
+        xa, va = f64.state(i)
+        xm, vm = mix.state(i)
+        assert rel(xm, xa) <= 1e-5 and float(np.linalg.norm(vm - va)) / vmax[i] <= 1e-5, (i, rel(xm, xa))
+
+
 def test_compression_counts_fp64_resolves(fem_lib):
     sc = scenes.compressed_cube(n=6, steps=20, ratio=0.2)
     b = fem_lib.Batch([sc], precision=fem_lib.FEM_PRECISION_MIXED)
@@ -169,3 +240,30 @@ def test_compression_counts_fp64_resolves(fem_lib):
         resolved = max(resolved, st["fp64_resolved"])
         assert st["status"] == 0
     assert resolved > 0
+
+
+@pytest.mark.parametrize("tile_elems,reorder", [(64, False), (128, True), (192, True)])
+def test_tile_variants_match_reference_cantilever(fem_lib, tile_elems, reorder):
+    """Every tile size and element order the autotuner may pick gives the
+    FP64 cantilever within the FP64 bar (1e-10, +-1 iteration)."""
+    g = np.load(os.path.join(GOLDEN, "cantilever_160.npz"))
+    sc = scenes.cantilever_160()
+    b = fem_lib.Batch([sc], precision=fem_lib.FEM_PRECISION_FP64, tile_elems=tile_elems, reorder=reorder)
+    for k in range(sc.steps):
+        b.step(1)
+        assert abs(b.stats(0)["cg_iterations"] - int(g["iters"][k])) <= 1
+    x, v = b.state(0)
+    assert rel(x, g["x"][-1]) <= 1e-10 and rel(v, g["v"][-1]) <= 1e-10
+
+
+def test_autotuner_picks_a_measured_candidate(fem_lib, tmp_path, monkeypatch):
+    from risdsdgcfem_thesis_gb300 import autotune
+    monkeypatch.setenv("FEMGB_CACHE_DIR", str(tmp_path))
+    rng = np.random.default_rng(4)
+    scs = [scenes.random_block(rng, idx=i) for i in range(6)]
+    cands = ((256, 1), (128, 1))
+    out = autotune.tune(scs, fem_lib.FEM_PRECISION_MIXED, candidates=cands, iters=10, reps=2)
+    assert not out["cached"] and (out["tile_elems"], out["reorder"]) in cands
+    assert len(out["table"]) == 2 and all(r["ms_per_launch"] > 0 for r in out["table"])
+    again = autotune.tune(scs, fem_lib.FEM_PRECISION_MIXED, candidates=cands, iters=10, reps=2)
+    assert again["cached"] and again["tile_elems"] == out["tile_elems"]
