@@ -321,16 +321,16 @@ def run_ours(args):
     scs, precision = workload(args.workload, rank)
     prec = capi.FEM_PRECISION_MIXED if precision == "mixed" else capi.FEM_PRECISION_FP64
     tuned = None
-    tile_elems, reorder = 256, True
+    tile_elems, reorder, chunk_nodes = 256, True, 1024
     if not args.no_tune:
         from risdsdgcfem_thesis_gb300 import autotune
         t0 = time.perf_counter()
         tuned = autotune.tune(scs, prec, use_cache=False)
         tuned["tune_s"] = round(time.perf_counter() - t0, 1)
-        tile_elems, reorder = tuned["tile_elems"], bool(tuned["reorder"])
+        tile_elems, reorder, chunk_nodes = tuned["tile_elems"], bool(tuned["reorder"]), tuned["chunk_nodes"]
     t0 = time.perf_counter()
-    batch = capi.Batch(scs, precision=prec, tile_elems=tile_elems, reorder=reorder, compute_energy=True,
-                       use_graph=not args.no_graph)
+    batch = capi.Batch(scs, precision=prec, tile_elems=tile_elems, reorder=reorder, chunk_nodes=chunk_nodes,
+                       compute_energy=True, use_graph=not args.no_graph)
     setup_s = time.perf_counter() - t0
     info = batch.info()
     stream_ptr = batch.stream()
@@ -430,7 +430,8 @@ def run_ours(args):
                        "l2": f"inputs larger than L2: {elem_bytes / 1e6:.0f} MB of element data streamed per CG "
                              f"iteration vs {L2_BYTES / 1e6:.0f} MB L2",
                        "cg_iterations_timed_max_mesh": int(max(iters)), "setup_s": round(setup_s, 2),
-                       "tile_elems": tile_elems, "reorder": reorder, "autotune": tuned,
+                       "tile_elems": tile_elems, "reorder": reorder, "chunk_nodes": chunk_nodes,
+                       "autotune": tuned,
                        "graph": not args.no_graph},
             "p50_step_ms": float(np.percentile(step_ms, 50)), "p99_step_ms": float(np.percentile(step_ms, 99)),
             "clocks": clk,
@@ -466,12 +467,12 @@ def run_ours(args):
 def compression_report(n=40, steps=120, ratio=0.4):
     """The large-deformation case: an n^3 x 5-tet cube (E 2e5, nu 0.45)
     compressed by its top face to `ratio` of its height over `steps` steps.
-    The mixed path (FP32 rotations; FP64 re-solve where det F <= 1e-3, and by
-    default also where the FP32 rotation is sensitive to rounding) against the
-    plain FP64 path (itself parity-tested against the FP64 oracle), step by
-    step: share of elements re-solved in FP64 and inverted, CG iterations,
-    and the final error; once with the default re-solve rule and once with
-    the det F rule alone."""
+    The mixed path against the plain FP64 path (itself parity-tested against
+    the FP64 oracle), step by step: share of rotations computed in FP64 and
+    of inverted elements, CG iterations, and the final error -- with the
+    default FP64 rotations, with FP32 rotations re-solved in FP64 where
+    det F <= 1e-3 or the rotation is rounding-sensitive, and with the det F
+    rule alone."""
     from risdsdgcfem_thesis_gb300 import capi, scenes
     sc = scenes.compressed_cube(n, steps, ratio)
     T = float(sc.num_tets)
@@ -496,8 +497,9 @@ def compression_report(n=40, steps=120, ratio=0.4):
     noise = {"x_rel": float(np.linalg.norm(xp - x64) / np.linalg.norm(x64)),
              "v": float(np.linalg.norm(vp - v64) / vscale) if vscale > 0 else None}
 
-    def mixed(check):
-        mix = capi.Batch([sc], precision=capi.FEM_PRECISION_MIXED, compute_energy=False, rotation_check=check)
+    def mixed(rot32, check):
+        mix = capi.Batch([sc], precision=capi.FEM_PRECISION_MIXED, compute_energy=False, rotation_fp32=rot32,
+                         rotation_check=check)
         res, inv, itm, tm = [], [], [], 0.0
         for _ in range(steps):
             t0 = time.perf_counter()
@@ -517,7 +519,9 @@ def compression_report(n=40, steps=120, ratio=0.4):
 
     return {"case": f"{n}^3 x 5 tets ({int(T)}), top face to {ratio:.0%} height over {steps} steps, "
                     f"E 2e5, nu 0.45, dt 1/60, CG rel 1e-6",
-            "mixed_default": mixed(1e-3), "mixed_det_F_rule_only": mixed(0.0),
+            "mixed_default_fp64_rotations": mixed(0, 1e-3),
+            "mixed_fp32_rotations_checked": mixed(1, 1e-3),
+            "mixed_fp32_rotations_det_F_rule_only": mixed(1, 0.0),
             "fp64_path_noise_floor": noise,
             "cg_iterations_fp64_mean": float(np.mean(it64)), "wall_s_fp64": t64,
             "note": "v error normalised by the run's peak |v|; the FP64 path matches the FP64 oracle "

@@ -77,6 +77,10 @@ typedef struct fem_params {
                                  has fallen by this factor since the last time (reliable
                                  updates), and at least every refresh_every iterations;
                                  0 = by refresh_every alone */
+    uint32_t rotation_fp32;   /* mixed only: 1 = rotations in FP32, re-solved in FP64 where
+                                 det F <= degenerate_det_F or rotation_check flags them;
+                                 0 = every rotation in FP64 (once per step) */
+    uint32_t pad;
 } fem_params;
 
 /* Per-step statistics (the Leaf's per-step LS stats, LeafDSH_Solid3D_FEM.h:597-622). */
@@ -190,6 +194,7 @@ typedef struct fem_batch_options {
     uint32_t tile_elems;  /* elements per tile, 1..256 */
     uint32_t reorder;     /* 1: Morton order of element centroids before tiling */
     uint32_t use_graph;   /* 1: each step is one CUDA graph with a device-side CG loop */
+    uint32_t chunk_nodes; /* nodes per node-pass work item, 32..8192 (0 = 1024) */
 } fem_batch_options;
 
 int fem_batch_options_default(fem_batch_options* o);

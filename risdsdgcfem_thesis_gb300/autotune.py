@@ -3,11 +3,12 @@
 A batch cuts each mesh's elements (in Morton order of their centroids, or in
 the mesh's own order) into tiles of at most `tile_elems` tets; the tile is
 the unit of the element product's shared-memory staging and of its segmented
-sum. Which tile size and order run fastest depends on the meshes (their sizes
-and node sharing) and on the GPU, so `tune` measures: it builds the batch of a
-sample of the workload for each candidate, times launches of a fixed number
-of CG iterations (the batch's iteration budget) and returns the fastest
-options. Results are cached per device and workload signature in a JSON file
+sum. The node pass walks each mesh's nodes in chunks of `chunk_nodes`, the
+unit of its per-mesh reductions. Which sizes and order run fastest depends on
+the meshes (their sizes and node sharing) and on the GPU, so `tune`
+measures: it builds the batch of a sample of the workload for each candidate,
+times launches of a fixed number of CG iterations (the batch's iteration
+budget) and returns the fastest options. Results are cached per device and workload signature in a JSON file
 (`$FEMGB_CACHE_DIR` or `~/.cache/risdsdgcfem_thesis_gb300/autotune.json`).
 
 The choice changes speed only: every candidate computes the same step up to
@@ -21,7 +22,9 @@ from typing import Dict, Iterable, List, Optional, Sequence, Tuple
 
 from . import capi
 
-DEFAULT_CANDIDATES: Tuple[Tuple[int, int], ...] = ((256, 1), (192, 1), (128, 1), (256, 0))
+# (tile_elems, reorder, chunk_nodes)
+DEFAULT_CANDIDATES: Tuple[Tuple[int, int, int], ...] = ((256, 1, 1024), (192, 1, 1024), (128, 1, 1024),
+                                                         (256, 0, 1024), (256, 0, 512), (256, 0, 2048))
 
 
 def _cache_path() -> str:
@@ -40,9 +43,9 @@ def signature(scenes: Sequence, precision: int) -> str:
             f"T2^{int(math.log2(max(T, 1)))}/med2^{int(math.log2(max(med, 1)))}/M{len(scenes)}")
 
 
-def _time_candidate(scenes, precision, tile_elems, reorder, iters, reps) -> float:
+def _time_candidate(scenes, precision, tile_elems, reorder, chunk_nodes, iters, reps) -> float:
     b = capi.Batch(scenes, precision=precision, tile_elems=tile_elems, reorder=bool(reorder), use_graph=True,
-                   compute_energy=False)
+                   chunk_nodes=chunk_nodes, compute_energy=False)
     try:
         b.set_slice(iters)
         b.set_active(None)
@@ -59,9 +62,11 @@ def _time_candidate(scenes, precision, tile_elems, reorder, iters, reps) -> floa
 
 
 def tune(scenes: Sequence, precision: int = capi.FEM_PRECISION_MIXED,
-         candidates: Iterable[Tuple[int, int]] = DEFAULT_CANDIDATES, iters: int = 30, reps: int = 3,
+         candidates: Iterable[Tuple[int, ...]] = DEFAULT_CANDIDATES, iters: int = 30, reps: int = 3,
          sample_tets: int = 4_000_000, use_cache: bool = True) -> Dict:
-    """Returns {"tile_elems", "reorder", "table", "signature", "cached"}.
+    """Returns {"tile_elems", "reorder", "chunk_nodes", "table", "signature",
+    "cached"}. A candidate is (tile_elems, reorder) or (tile_elems, reorder,
+    chunk_nodes).
 
     The timing runs on a prefix of `scenes` holding about `sample_tets` tets
     (the whole workload's tiles behave alike; the prefix keeps tuning to
@@ -87,13 +92,15 @@ def tune(scenes: Sequence, precision: int = capi.FEM_PRECISION_MIXED,
         out["cached"] = True
         return out
     table = []
-    for tile_elems, reorder in candidates:
-        t = _time_candidate(sample, precision, tile_elems, reorder, iters, reps)
-        table.append({"tile_elems": tile_elems, "reorder": reorder, "ms_per_launch": 1e3 * t,
-                      "tet_cg_iter_per_s": tot * iters / t})
+    for cand in candidates:
+        tile_elems, reorder = cand[0], cand[1]
+        chunk_nodes = cand[2] if len(cand) > 2 else 1024
+        t = _time_candidate(sample, precision, tile_elems, reorder, chunk_nodes, iters, reps)
+        table.append({"tile_elems": tile_elems, "reorder": reorder, "chunk_nodes": chunk_nodes,
+                      "ms_per_launch": 1e3 * t, "tet_cg_iter_per_s": tot * iters / t})
     best = min(table, key=lambda r: r["ms_per_launch"])
-    out = {"tile_elems": best["tile_elems"], "reorder": best["reorder"], "table": table, "signature": sig,
-           "sample_tets": tot, "iters": iters}
+    out = {"tile_elems": best["tile_elems"], "reorder": best["reorder"], "chunk_nodes": best["chunk_nodes"],
+           "table": table, "signature": sig, "sample_tets": tot, "iters": iters}
     if use_cache:
         cache[sig] = out
         try:

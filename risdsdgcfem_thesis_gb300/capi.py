@@ -41,6 +41,8 @@ class FemParams(C.Structure):
         ("compute_energy", C.c_uint32),
         ("rotation_check", C.c_double),
         ("refresh_drop", C.c_double),
+        ("rotation_fp32", C.c_uint32),
+        ("pad", C.c_uint32),
     ]
 
 
@@ -294,7 +296,7 @@ def device_info():
 # ---------------------------------------------------------------- batches
 class FemBatchOptions(C.Structure):
     _fields_ = [("precision", C.c_uint32), ("tile_elems", C.c_uint32), ("reorder", C.c_uint32),
-                ("use_graph", C.c_uint32)]
+                ("use_graph", C.c_uint32), ("chunk_nodes", C.c_uint32)]
 
 
 _u8p = C.POINTER(C.c_uint8)
@@ -369,13 +371,15 @@ _BATCH_SIGNATURES = {
 }
 
 
-def batch_options(precision=FEM_PRECISION_MIXED, tile_elems=256, reorder=True, use_graph=True):
+def batch_options(precision=FEM_PRECISION_MIXED, tile_elems=256, reorder=True, use_graph=True, chunk_nodes=None):
     o = FemBatchOptions()
     check(load().fem_batch_options_default(C.byref(o)))
     o.precision = precision
     o.tile_elems = tile_elems
     o.reorder = 1 if reorder else 0
     o.use_graph = 1 if use_graph else 0
+    if chunk_nodes is not None:
+        o.chunk_nodes = chunk_nodes
     return o
 
 
@@ -383,14 +387,15 @@ class Batch:
     """Many independent solids stepped together on one GPU (fem_batch_*)."""
 
     def __init__(self, scenes_list, precision=FEM_PRECISION_MIXED, tile_elems=256, reorder=True, use_graph=True,
+                 chunk_nodes=None,
                  compute_energy=True, refresh_every=None, degenerate_det_F=None, rotation_check=None,
-                 refresh_drop=None):
+                 refresh_drop=None, rotation_fp32=None):
         lib = load()
         self.lib = lib
         self.scenes = list(scenes_list)
         self.precision = precision
         h = C.c_void_p()
-        opt = batch_options(precision, tile_elems, reorder, use_graph)
+        opt = batch_options(precision, tile_elems, reorder, use_graph, chunk_nodes)
         check(lib.fem_batch_create(C.byref(opt), C.byref(h)))
         self.h = h
         self._knc = []
@@ -404,6 +409,8 @@ class Batch:
                 p.rotation_check = rotation_check
             if refresh_drop is not None:
                 p.refresh_drop = refresh_drop
+            if rotation_fp32 is not None:
+                p.rotation_fp32 = rotation_fp32
             rest = _f64(sc.rest)
             tets = np.ascontiguousarray(sc.tets, dtype=np.uint32)
             idx = C.c_uint32()

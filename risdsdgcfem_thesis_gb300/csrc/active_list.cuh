@@ -91,6 +91,20 @@ __device__ void build_active_lists(const BatchView<S>& b)
     if (threadIdx.x == 0) *b.list_dirty = 0u;
 }
 
+// The tiles of the meshes whose next iteration recomputes the residual in
+// FP64 (walked by the FP64 product of y). Same calling rule as above.
+template <typename S>
+__device__ void build_refresh_lists(const BatchView<S>& b)
+{
+    build_mesh_lists(
+        b,
+        [&](uint32_t m) {
+            volatile const StepScalars* sp = b.st + m;
+            return sp->done == 0u && sp->refresh_next != 0u;
+        },
+        b.refresh_tiles, b.refresh_chunks, b.list_count + 4);
+}
+
 // Entry i of a work list, or i itself when the launch has no list.
 __device__ __forceinline__ uint32_t list_entry(const uint32_t* list, uint32_t i) { return list ? list[i] : i; }
 

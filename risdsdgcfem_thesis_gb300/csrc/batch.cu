@@ -127,7 +127,10 @@ struct fem_batch_s {
     Dev<int4> gtets;
     Dev<unsigned char> Dinv_s, mat_s, R_s;  // S-typed, raw bytes
     Dev<double> Dinv64, vol, detF;
-    Dev<uint32_t> tile_nodes, lptr0, nptr, nslot, knc_node, knc_mesh;
+    Dev<uint32_t> tile_nodes, lptr0, ov_ptr, ov_slot, knc_node, knc_mesh;
+    std::vector<uint32_t> perm_h, inv_h;  // batch node -> caller's node, and back (global ids)
+    Dev<uint32_t> perm;                   // perm_h on the device (whole-batch state transfers)
+    Dev<double> stage_x, stage_v;         // caller-order staging for whole-batch transfers
     Dev<uchar4> lconn;
     Dev<uint16_t> lptr, lidx;
     Dev<uint8_t> fixed;
@@ -139,7 +142,7 @@ struct fem_batch_s {
     Dev<uint32_t> act_tiles, act_chunks, act_count;
     Dev<unsigned> list_dirty;
     Dev<unsigned> slice;                // [iteration budget of a launch (0 = none), iterations run]
-    Dev<uint32_t> start_tiles, start_chunks, launch_tiles, launch_chunks, list_count;
+    Dev<uint32_t> start_tiles, start_chunks, launch_tiles, launch_chunks, refresh_tiles, refresh_chunks, list_count;
     uint32_t slice_budget = 0;
     std::vector<uint8_t> mask_host;     // last active mask (empty = all start)
     StepScalars* st_host = nullptr;
@@ -177,8 +180,8 @@ struct fem_batch_s {
         b.lptr = lptr.p;
         b.lidx = lidx.p;
         b.lptr0 = lptr0.p;
-        b.nptr = nptr.p;
-        b.nslot = nslot.p;
+        b.ov_ptr = ov_ptr.p;
+        b.ov_slot = ov_slot.p;
         b.fixed = fixed.p;
         b.rest = rest.p;
         b.ydelta = opt.precision == FEM_PRECISION_MIXED ? reinterpret_cast<S*>(ydelta_s.p) : nullptr;
@@ -193,6 +196,8 @@ struct fem_batch_s {
         b.start_chunks = start_chunks.p;
         b.launch_tiles = launch_tiles.p;
         b.launch_chunks = launch_chunks.p;
+        b.refresh_tiles = mixed ? refresh_tiles.p : nullptr;
+        b.refresh_chunks = mixed ? refresh_chunks.p : nullptr;
         b.list_count = list_count.p;
         b.knc_node = knc_node.p;
         b.knc_mesh = knc_mesh.p;
@@ -208,7 +213,8 @@ struct fem_batch_s {
         graph = nullptr;
         tiles.release(); chunks.release(); mc.release(); st.release(); active.release(); gtets.release();
         Dinv_s.release(); mat_s.release(); R_s.release(); Dinv64.release(); vol.release(); detF.release();
-        tile_nodes.release(); lptr0.release(); nptr.release(); nslot.release(); knc_node.release();
+        tile_nodes.release(); lptr0.release(); ov_ptr.release(); ov_slot.release(); knc_node.release();
+        perm.release(); stage_x.release(); stage_v.release();
         knc_mesh.release(); lconn.release(); lptr.release(); lidx.release(); fixed.release(); rest.release();
         x.release(); v.release(); bvec.release(); y.release(); part64.release(); cpart.release(); tpart.release();
         knc_target.release(); r_s.release(); d_s.release(); q_s.release(); part_s.release(); ydelta_s.release(); counter.release();
@@ -216,6 +222,7 @@ struct fem_batch_s {
         blob_off16.release();
         act_tiles.release(); act_chunks.release(); act_count.release(); list_dirty.release(); slice.release();
         start_tiles.release(); start_chunks.release(); launch_tiles.release(); launch_chunks.release();
+        refresh_tiles.release(); refresh_chunks.release();
         list_count.release();
         if (st_host) cudaFreeHost(st_host);
         st_host = nullptr;
@@ -451,6 +458,7 @@ int fem_batch_options_default(fem_batch_options* o)
     o->tile_elems = kTileElems;
     o->reorder = 1;
     o->use_graph = 1;
+    o->chunk_nodes = kChunkNodes;
     return FEM_OK;
 }
 
@@ -465,6 +473,9 @@ int fem_batch_create(const fem_batch_options* opt, fem_batch* out)
         return batch_fail(FEM_E_ARG, "unknown precision %u", o.precision);
     if (o.tile_elems == 0 || o.tile_elems > (uint32_t)kTileElems)
         return batch_fail(FEM_E_ARG, "tile_elems must be in [1, %d]", kTileElems);
+    if (o.chunk_nodes == 0) o.chunk_nodes = kChunkNodes;
+    if (o.chunk_nodes < 32 || o.chunk_nodes > 8192)
+        return batch_fail(FEM_E_ARG, "chunk_nodes must be in [32, 8192]");
     fem_batch b = new (std::nothrow) fem_batch_s;
     if (!b) return batch_fail(FEM_E_OOM, "host allocation failed");
     b->opt = o;
@@ -531,6 +542,8 @@ int fem_batch_finalize(fem_batch b)
     std::vector<uint8_t> fixed;
     std::vector<uint32_t> knc_node, knc_mesh;
     std::vector<double> knc_target;
+    std::vector<uint32_t> ov_node;   // node of each overflow partial slot, tile order
+    std::vector<uint32_t> perm_h;    // batch node id -> caller's node id (both global)
     // element data collected AoS then transposed
     std::vector<double> Dinv_aos, mat_aos;
 
@@ -610,6 +623,8 @@ int fem_batch_finalize(fem_batch b)
         MeshConsts& c = mcs[mi];
         c.tile0 = (uint32_t)tiles.size();
         std::vector<int32_t> stamp(N, -1), local(N, 0);
+        std::vector<int32_t> intern(N, -1);  // caller's node -> batch node (first appearance in tile order)
+        uint32_t next_id = 0;
         uint32_t k = 0;
         while (k < T) {
             TileMeta tm;
@@ -646,6 +661,37 @@ int fem_batch_finalize(fem_batch b)
             }
             tm.ne = (uint16_t)ne;
             tm.nn = (uint16_t)lnodes.size();
+            // nodes first seen in this tile get the next batch ids and lead
+            // the tile's local list; the others follow in local order
+            {
+                std::vector<uint32_t> owned, shared;
+                for (uint32_t u : lnodes) {
+                    if (intern[u] < 0) {
+                        intern[u] = (int32_t)next_id++;
+                        owned.push_back(u);
+                    } else {
+                        shared.push_back(u);
+                    }
+                }
+                std::vector<unsigned char> remap(lnodes.size());
+                for (size_t i = 0; i < owned.size(); i++) remap[local[owned[i]]] = (unsigned char)i;
+                for (size_t i = 0; i < shared.size(); i++)
+                    remap[local[shared[i]]] = (unsigned char)(owned.size() + i);
+                for (size_t el = lconn.size() - ne; el < lconn.size(); el++) {
+                    uchar4& lc = lconn[el];
+                    lc.x = remap[lc.x];
+                    lc.y = remap[lc.y];
+                    lc.z = remap[lc.z];
+                    lc.w = remap[lc.w];
+                }
+                tm.nown = (uint16_t)owned.size();
+                tm.pad = 0;
+                tm.own0 = owned.empty() ? 0u : (uint32_t)(node0 + intern[owned[0]]);
+                tm.ov0 = (uint32_t)ov_node.size();
+                for (uint32_t u : shared) ov_node.push_back((uint32_t)(node0 + intern[u]));
+                lnodes = owned;
+                lnodes.insert(lnodes.end(), shared.begin(), shared.end());
+            }
             // tile-local CSR: local node -> (element << 2 | slot), element order
             std::vector<uint16_t> cnt(lnodes.size() + 1, 0);
             const size_t lc0 = lconn.size() - ne;
@@ -663,17 +709,31 @@ int fem_batch_finalize(fem_batch b)
                 for (int sl = 0; sl < 4; sl++) ent[fill[ids[sl]]++] = (uint16_t)((el << 2) | sl);
             }
             lidx.insert(lidx.end(), ent.begin(), ent.end());
-            for (uint32_t n : lnodes) tile_nodes.push_back((uint32_t)(node0 + n));
+            for (uint32_t n : lnodes) tile_nodes.push_back((uint32_t)(node0 + intern[n]));
             tiles.push_back(tm);
         }
+        // nodes no tet names get the remaining ids (no tile writes their
+        // partial: it stays zero)
+        for (uint32_t u = 0; u < N; u++)
+            if (intern[u] < 0) intern[u] = (int32_t)next_id++;
+        for (uint32_t kk = 0; kk < T; kk++) {
+            int4& g = gtets[elem0 + kk];
+            g.x = (int)(node0 + intern[g.x - node0]);
+            g.y = (int)(node0 + intern[g.y - node0]);
+            g.z = (int)(node0 + intern[g.z - node0]);
+            g.w = (int)(node0 + intern[g.w - node0]);
+        }
+        perm_h.resize(node0 + N);
+        for (uint32_t u = 0; u < N; u++) perm_h[node0 + intern[u]] = (uint32_t)(node0 + u);
         c.ntiles = (uint32_t)tiles.size() - c.tile0;
         // node chunks
         c.chunk0 = (uint32_t)chunks.size();
-        for (uint32_t n = 0; n < N; n += kChunkNodes) {
+        const uint32_t chunk = b->opt.chunk_nodes ? b->opt.chunk_nodes : (uint32_t)kChunkNodes;
+        for (uint32_t n = 0; n < N; n += chunk) {
             ChunkMeta ch;
             ch.mesh = mi;
             ch.n0 = (uint32_t)(node0 + n);
-            ch.n1 = (uint32_t)(node0 + std::min<uint32_t>(N, n + kChunkNodes));
+            ch.n1 = (uint32_t)(node0 + std::min<uint32_t>(N, n + chunk));
             chunks.push_back(ch);
         }
         c.nchunks = (uint32_t)chunks.size() - c.chunk0;
@@ -705,6 +765,7 @@ int fem_batch_finalize(fem_batch b)
         c.abs_eps_sq = p.ls_abs_epsilon * p.ls_abs_epsilon;
         c.degenerate_det_F = p.degenerate_det_F;
         c.rot_check = (float)p.rotation_check;
+        c.rot_fp32 = p.rotation_fp32 ? 1u : 0u;
         c.refresh_drop_sq = fp64 ? 0.0 : p.refresh_drop * p.refresh_drop;
         c.max_iter = p.ls_max_iter;
         c.refresh_every = fp64 ? 0u : p.refresh_every;
@@ -716,15 +777,18 @@ int fem_batch_finalize(fem_batch b)
         c.T = T;
         c.knc0 = (uint32_t)knc_node.size();
         c.nknc = (uint32_t)hm.knc_nodes.size();
-        // nodes
-        for (size_t i = 0; i < hm.rest.size(); i++) rest_all.push_back(hm.rest[i]);
+        // nodes, in batch order
+        const size_t r0 = rest_all.size();
+        rest_all.resize(r0 + 3 * (size_t)N);
+        for (uint32_t u = 0; u < N; u++)
+            for (int a = 0; a < 3; a++) rest_all[r0 + 3 * (size_t)intern[u] + a] = hm.rest[3 * (size_t)u + a];
         const size_t f0 = fixed.size();
         fixed.resize(f0 + N, 0);
         for (size_t kk = 0; kk < hm.knc_nodes.size(); kk++) {
-            knc_node.push_back((uint32_t)(node0 + hm.knc_nodes[kk]));
+            knc_node.push_back((uint32_t)(node0 + intern[hm.knc_nodes[kk]]));
             knc_mesh.push_back(mi);
             for (int a = 0; a < 3; a++) knc_target.push_back(hm.knc_targets[3 * kk + a]);
-            fixed[f0 + hm.knc_nodes[kk]] = 1;
+            fixed[f0 + intern[hm.knc_nodes[kk]]] = 1;
         }
         node0 += N;
         elem0 += T;
@@ -735,15 +799,18 @@ int fem_batch_finalize(fem_batch b)
     b->ntiles = (uint32_t)tiles.size();
     b->nchunks = (uint32_t)chunks.size();
     b->K = (uint32_t)knc_node.size();
-    b->nslots = tile_nodes.size();
+    b->nslots = b->Ntot + ov_node.size();  // owner slots (node order) + overflow slots
     b->mc_host = mcs;
-    // node -> partial slots, tile order
-    std::vector<uint32_t> nptr(b->Ntot + 1, 0), nslot(b->nslots);
-    for (uint32_t g : tile_nodes) nptr[g + 1]++;
-    for (uint64_t n = 0; n < b->Ntot; n++) nptr[n + 1] += nptr[n];
+    b->perm_h = perm_h;
+    b->inv_h.assign(b->Ntot, 0);
+    for (uint64_t i = 0; i < b->Ntot; i++) b->inv_h[perm_h[i]] = (uint32_t)i;
+    // node -> overflow slots, tile order
+    std::vector<uint32_t> ov_ptr(b->Ntot + 1, 0), ov_slot(ov_node.size());
+    for (uint32_t g : ov_node) ov_ptr[g + 1]++;
+    for (uint64_t n = 0; n < b->Ntot; n++) ov_ptr[n + 1] += ov_ptr[n];
     {
-        std::vector<uint32_t> fill(nptr.begin(), nptr.end() - 1);
-        for (size_t sidx = 0; sidx < tile_nodes.size(); sidx++) nslot[fill[tile_nodes[sidx]]++] = (uint32_t)sidx;
+        std::vector<uint32_t> fill(ov_ptr.begin(), ov_ptr.end() - 1);
+        for (size_t kk = 0; kk < ov_node.size(); kk++) ov_slot[fill[ov_node[kk]]++] = (uint32_t)kk;
     }
     // SoA transposes
     const size_t T = b->Ttot;
@@ -787,11 +854,11 @@ int fem_batch_finalize(fem_batch b)
                 li[j] = (uint16_t)((v & 3u) * ne4 + (v >> 2));
             }
             uint32_t* nodes = reinterpret_cast<uint32_t*>(base + blob_nodes_off(tm.ne, tm.nn));
-            // bit 31: this tile owns the node (the first tile, in tile order, that lists it)
-            for (uint32_t i = 0; i < tm.nn; i++) {
-                const uint32_t g = tile_nodes[tm.n0 + i];
-                nodes[i] = g | (nslot[nptr[g]] == tm.n0 + i ? 0x80000000u : 0u);
-            }
+            for (uint32_t i = 0; i < tm.nn; i++) nodes[i] = tile_nodes[tm.n0 + i];
+            uint32_t* slots = reinterpret_cast<uint32_t*>(base + blob_slots_off(tm.ne, tm.nn));
+            slots[0] = tm.own0;
+            slots[1] = tm.ov0;
+            slots[2] = tm.nown;
         }
     }
     std::vector<double> Rinit(9 * T, 0.0);
@@ -825,10 +892,11 @@ int fem_batch_finalize(fem_batch b)
     BCKC(b->Dinv64.alloc(9 * T));
     BCKC(b->vol.alloc(T));
     BCKC(b->detF.alloc(T));
-    BCKC(b->tile_nodes.alloc(b->nslots));
+    BCKC(b->tile_nodes.alloc(tile_nodes.size()));
     BCKC(b->lptr0.alloc(b->ntiles));
-    BCKC(b->nptr.alloc(b->Ntot + 1));
-    BCKC(b->nslot.alloc(b->nslots));
+    BCKC(b->ov_ptr.alloc(b->Ntot + 1));
+    BCKC(b->ov_slot.alloc(ov_slot.size()));
+    BCKC(b->perm.alloc(b->Ntot));
     BCKC(b->knc_node.alloc(b->K));
     BCKC(b->knc_mesh.alloc(b->K));
     BCKC(b->knc_target.alloc(3 * (size_t)b->K));
@@ -845,9 +913,11 @@ int fem_batch_finalize(fem_batch b)
     BCKC(b->d_s.alloc(N3 * SB));
     BCKC(b->q_s.alloc(N3 * SB));
     BCKC(b->part_s.alloc(3 * b->nslots * SB));
+    BCKC(cudaMemsetAsync(b->part_s.p, 0, 3 * b->nslots * SB, s));  // slots of nodes no tet names stay zero
     BCKC(b->ydelta_s.alloc(N3 * SB));
     BCKC(cudaMemsetAsync(b->ydelta_s.p, 0, N3 * SB, s));
     BCKC(b->part64.alloc(3 * b->nslots));
+    BCKC(cudaMemsetAsync(b->part64.p, 0, 3 * b->nslots * sizeof(double), s));
     BCKC(b->cpart.alloc(b->nchunks));
     BCKC(b->tpart.alloc(b->ntiles));
     BCKC(b->counter.alloc(1));
@@ -866,8 +936,12 @@ int fem_batch_finalize(fem_batch b)
     BCKC(b->start_chunks.alloc(b->nchunks));
     BCKC(b->launch_tiles.alloc(b->ntiles));
     BCKC(b->launch_chunks.alloc(b->nchunks));
-    BCKC(b->list_count.alloc(4));
-    BCKC(cudaMemsetAsync(b->list_count.p, 0, 4 * sizeof(uint32_t), s));
+    if (!fp64) {
+        BCKC(b->refresh_tiles.alloc(b->ntiles));
+        BCKC(b->refresh_chunks.alloc(b->nchunks));
+    }
+    BCKC(b->list_count.alloc(6));
+    BCKC(cudaMemsetAsync(b->list_count.p, 0, 6 * sizeof(uint32_t), s));
     if (!fp64) {
         BCKC(b->act_tiles.alloc(b->ntiles));
         BCKC(b->act_chunks.alloc(b->nchunks));
@@ -901,8 +975,9 @@ int fem_batch_finalize(fem_batch b)
     BCKC(b->vol.upload(vol, s));
     BCKC(b->tile_nodes.upload(tile_nodes, s));
     BCKC(b->lptr0.upload(lptr0, s));
-    BCKC(b->nptr.upload(nptr, s));
-    BCKC(b->nslot.upload(nslot, s));
+    BCKC(b->ov_ptr.upload(ov_ptr, s));
+    BCKC(b->ov_slot.upload(ov_slot, s));
+    BCKC(b->perm.upload(perm_h, s));
     BCKC(b->knc_node.upload(knc_node, s));
     BCKC(b->knc_mesh.upload(knc_mesh, s));
     BCKC(b->knc_target.upload(knc_target, s));
@@ -923,7 +998,8 @@ int fem_batch_finalize(fem_batch b)
     b->device_bytes = b->tiles.bytes() + b->chunks.bytes() + b->mc.bytes() + b->st.bytes() + b->active.bytes() +
                       b->gtets.bytes() + b->Dinv_s.bytes() + b->mat_s.bytes() + b->R_s.bytes() +
                       b->Dinv64.bytes() + b->vol.bytes() + b->detF.bytes() + b->tile_nodes.bytes() +
-                      b->lptr0.bytes() + b->nptr.bytes() + b->nslot.bytes() + b->knc_node.bytes() +
+                      b->lptr0.bytes() + b->ov_ptr.bytes() + b->ov_slot.bytes() + b->knc_node.bytes() +
+                      b->perm.bytes() +
                       b->knc_mesh.bytes() + b->knc_target.bytes() + b->lconn.bytes() + b->lptr.bytes() +
                       b->lidx.bytes() + b->fixed.bytes() + b->rest.bytes() + b->x.bytes() + b->v.bytes() +
                       b->bvec.bytes() + b->y.bytes() + b->r_s.bytes() + b->d_s.bytes() + b->q_s.bytes() +
@@ -932,7 +1008,8 @@ int fem_batch_finalize(fem_batch b)
                       b->mcount.bytes() + b->err.bytes() + b->blob.bytes() + b->blob_off16.bytes() +
                       b->act_tiles.bytes() + b->act_chunks.bytes() + b->act_count.bytes() + b->list_dirty.bytes() +
                       b->slice.bytes() + b->start_tiles.bytes() + b->start_chunks.bytes() +
-                      b->launch_tiles.bytes() + b->launch_chunks.bytes() + b->list_count.bytes();
+                      b->launch_tiles.bytes() + b->launch_chunks.bytes() + b->refresh_tiles.bytes() +
+                      b->refresh_chunks.bytes() + b->list_count.bytes();
     b->finalized = true;
     // host copies of the meshes are no longer needed beyond sizes
     for (auto& m : b->meshes) {
@@ -987,14 +1064,26 @@ int fem_batch_set_knc_targets(fem_batch b, uint32_t mesh, const double* targets)
     return FEM_OK;
 }
 
+// Per-mesh state transfers permute on the host between the caller's node
+// order and the batch's (first appearance in tile order).
 int fem_batch_set_state(fem_batch b, uint32_t mesh, const double* x, const double* v)
 {
     if (int e = check_ready(b)) return e;
     if (mesh >= b->M) return batch_fail(FEM_E_ARG, "mesh %u out of range", mesh);
     const MeshConsts& c = b->mc_host[mesh];
     const size_t off = 3 * (size_t)c.node0, bytes = sizeof(double) * 3 * c.N;
-    if (x) BCK(cudaMemcpyAsync(b->x.p + off, x, bytes, cudaMemcpyHostToDevice, b->stream));
-    if (v) BCK(cudaMemcpyAsync(b->v.p + off, v, bytes, cudaMemcpyHostToDevice, b->stream));
+    std::vector<double> tmp(3 * (size_t)c.N);
+    const double* src[2] = {x, v};
+    double* dst[2] = {b->x.p, b->v.p};
+    for (int k = 0; k < 2; k++) {
+        if (!src[k]) continue;
+        for (uint32_t u = 0; u < c.N; u++) {
+            const size_t i = b->inv_h[c.node0 + u] - c.node0;
+            for (int a = 0; a < 3; a++) tmp[3 * i + a] = src[k][3 * (size_t)u + a];
+        }
+        BCK(cudaMemcpyAsync(dst[k] + off, tmp.data(), bytes, cudaMemcpyHostToDevice, b->stream));
+        BCK(cudaStreamSynchronize(b->stream));
+    }
     return FEM_OK;
 }
 
@@ -1004,9 +1093,18 @@ int fem_batch_get_state(fem_batch b, uint32_t mesh, double* x, double* v)
     if (mesh >= b->M) return batch_fail(FEM_E_ARG, "mesh %u out of range", mesh);
     const MeshConsts& c = b->mc_host[mesh];
     const size_t off = 3 * (size_t)c.node0, bytes = sizeof(double) * 3 * c.N;
-    if (x) BCK(cudaMemcpyAsync(x, b->x.p + off, bytes, cudaMemcpyDeviceToHost, b->stream));
-    if (v) BCK(cudaMemcpyAsync(v, b->v.p + off, bytes, cudaMemcpyDeviceToHost, b->stream));
-    BCK(cudaStreamSynchronize(b->stream));
+    std::vector<double> tmp(3 * (size_t)c.N);
+    double* dst[2] = {x, v};
+    const double* src[2] = {b->x.p, b->v.p};
+    for (int k = 0; k < 2; k++) {
+        if (!dst[k]) continue;
+        BCK(cudaMemcpyAsync(tmp.data(), src[k] + off, bytes, cudaMemcpyDeviceToHost, b->stream));
+        BCK(cudaStreamSynchronize(b->stream));
+        for (uint32_t u = 0; u < c.N; u++) {
+            const size_t i = b->inv_h[c.node0 + u] - c.node0;
+            for (int a = 0; a < 3; a++) dst[k][3 * (size_t)u + a] = tmp[3 * i + a];
+        }
+    }
     return FEM_OK;
 }
 
@@ -1018,21 +1116,54 @@ int fem_batch_use_graph(fem_batch b, int on)
     return FEM_OK;
 }
 
+// Whole-batch state transfers go through caller-order staging buffers on
+// the device (allocated at first use) and a permute kernel.
+static int ensure_staging(fem_batch b)
+{
+    if (b->stage_x.p) return FEM_OK;
+    const size_t n3 = 3 * (size_t)b->Ntot;
+    cudaError_t e = b->stage_x.alloc(n3);
+    if (e == cudaSuccess) e = b->stage_v.alloc(n3);
+    if (e != cudaSuccess) {
+        b->stage_x.release();
+        b->stage_v.release();
+        return batch_fail(e == cudaErrorMemoryAllocation ? FEM_E_OOM : FEM_E_CUDA, "staging buffers: %s",
+                          cudaGetErrorString(e));
+    }
+    b->device_bytes += 2 * n3 * sizeof(double);
+    return FEM_OK;
+}
+
 int fem_batch_set_state_all(fem_batch b, const double* x, const double* v)
 {
     if (int e = check_ready(b)) return e;
+    if (int e = ensure_staging(b)) return e;
     const size_t bytes = sizeof(double) * 3 * (size_t)b->Ntot;
-    if (x) BCK(cudaMemcpyAsync(b->x.p, x, bytes, cudaMemcpyHostToDevice, b->stream));
-    if (v) BCK(cudaMemcpyAsync(b->v.p, v, bytes, cudaMemcpyHostToDevice, b->stream));
+    if (x) {
+        BCK(cudaMemcpyAsync(b->stage_x.p, x, bytes, cudaMemcpyHostToDevice, b->stream));
+        launch_permute(b->perm.p, b->Ntot, b->stage_x.p, b->x.p, true, b->stream);
+    }
+    if (v) {
+        BCK(cudaMemcpyAsync(b->stage_v.p, v, bytes, cudaMemcpyHostToDevice, b->stream));
+        launch_permute(b->perm.p, b->Ntot, b->stage_v.p, b->v.p, true, b->stream);
+    }
+    BCK(cudaGetLastError());
     return FEM_OK;
 }
 
 int fem_batch_get_state_all(fem_batch b, double* x, double* v)
 {
     if (int e = check_ready(b)) return e;
+    if (int e = ensure_staging(b)) return e;
     const size_t bytes = sizeof(double) * 3 * (size_t)b->Ntot;
-    if (x) BCK(cudaMemcpyAsync(x, b->x.p, bytes, cudaMemcpyDeviceToHost, b->stream));
-    if (v) BCK(cudaMemcpyAsync(v, b->v.p, bytes, cudaMemcpyDeviceToHost, b->stream));
+    if (x) {
+        launch_permute(b->perm.p, b->Ntot, b->x.p, b->stage_x.p, false, b->stream);
+        BCK(cudaMemcpyAsync(x, b->stage_x.p, bytes, cudaMemcpyDeviceToHost, b->stream));
+    }
+    if (v) {
+        launch_permute(b->perm.p, b->Ntot, b->v.p, b->stage_v.p, false, b->stream);
+        BCK(cudaMemcpyAsync(v, b->stage_v.p, bytes, cudaMemcpyDeviceToHost, b->stream));
+    }
     BCK(cudaStreamSynchronize(b->stream));
     return FEM_OK;
 }

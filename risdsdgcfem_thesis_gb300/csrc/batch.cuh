@@ -1,24 +1,32 @@
 // batch.cuh -- device layout of a batch of independent solids stepped in
 // lock-step (the tiled path; one solid is a batch of one).
 //
-// Meshes are concatenated: mesh m owns global nodes [node0, node0+N) in its
-// own node order and global elements [elem0, elem0+T) in a Morton order of
-// element centroids. Elements are cut into tiles of at most kTileElems tets
-// touching at most kTileNodes distinct nodes; a tile belongs to one mesh.
+// Meshes are concatenated: mesh m owns global nodes [node0, node0+N) and
+// global elements [elem0, elem0+T). Elements are cut into tiles of at most
+// tile_elems tets touching at most kTileNodes distinct nodes; a tile belongs
+// to one mesh.
+//
+// Nodes are numbered inside the batch in the order they first appear in their
+// mesh's tile sequence (the API permutes states to and from the caller's
+// order). A tile's new nodes -- the nodes it owns -- therefore have
+// consecutive ids, and its local node list puts them first.
 //
 //   per tile     TileMeta: element range, its local node list (tile_nodes,
-//                global ids), its local connectivity (lconn, uchar4 local
-//                ids) and a tile-local CSR (lptr/lidx) giving, for each local
-//                node, the (element, slot) outputs to sum, in element order
+//                global ids, owned nodes first), its local connectivity
+//                (lconn, uchar4 local ids) and a tile-local CSR (lptr/lidx)
+//                giving, for each local node, the (element, slot) outputs to
+//                sum, in element order
 //   per element  Dinv/mat/R in the path's element type S (SoA), plus FP64
 //                Dinv, volume and global ids for the once-per-step kernels
-//   per node     x, v, b, y (FP64); r, d, q (S); rest (FP64); fixed flag;
-//                CSR nptr/nslot over the partial slots of the tiles that
-//                touch it, in tile order
-//   per (tile,local node)  part: the tile's summed contribution
+//   per node     x, v, b, y (FP64); r, d, q (S); rest (FP64); fixed flag
+//   partials     one per (tile, local node): the owner tile's at part[node]
+//                (node order, so the node pass reads it coalesced), a shared
+//                node's other tiles' in overflow slots part[Ntot + k]; per
+//                node a CSR (ov_ptr/ov_slot) over its overflow slots, in
+//                tile order
 //
-// All sums have a fixed order, so a solid gives the same bits alone and in
-// any batch.
+// All sums have a fixed order (a node's partials: owner first, then tile
+// order), so a solid gives the same bits alone and in any batch.
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -29,29 +37,40 @@ namespace femgb {
 
 constexpr int kTileElems = 256;
 constexpr int kTileNodes = 256;
-constexpr int kChunkNodes = 256;   // node chunk = one block's share in node kernels
+constexpr int kChunkNodes = 1024;  // default node chunk (one work item of a node pass)
 constexpr int kNodeThreads = 256;  // threads per node-kernel block
 
 // Layout of a tile's blob (mixed path, see tile_pipe.cu): element data
-// float[22][ne4], then uint16 lptr[nn+1], uint16 lidx[4 ne], uint32 nodes[nn].
+// float[22][ne4], then uint16 lptr[nn+1], uint16 lidx[4 ne], uint32 nodes[nn],
+// uint32 {own0, ov0, nown} (the tile's partial slots).
 __host__ __device__ inline uint32_t blob_ne4(uint32_t ne) { return (ne + 3u) & ~3u; }
 __host__ __device__ inline uint32_t blob_lptr_off(uint32_t ne) { return 88u * blob_ne4(ne); }
 __host__ __device__ inline uint32_t blob_nodes_off(uint32_t ne, uint32_t nn)
 {
     return (blob_lptr_off(ne) + 2u * (nn + 1u) + 8u * ne + 3u) & ~3u;
 }
+__host__ __device__ inline uint32_t blob_slots_off(uint32_t ne, uint32_t nn) { return blob_nodes_off(ne, nn) + 4u * nn; }
 __host__ __device__ inline uint32_t blob_bytes(uint32_t ne, uint32_t nn)
 {
-    return (blob_nodes_off(ne, nn) + 4u * nn + 15u) & ~15u;
+    return (blob_slots_off(ne, nn) + 12u + 15u) & ~15u;
 }
 
 struct TileMeta {
     uint32_t mesh;
     uint32_t e0;      // first element (global)
-    uint32_t n0;      // first slot in tile_nodes / part
+    uint32_t n0;      // first entry in tile_nodes
     uint32_t c0;      // first entry in lidx
     uint16_t ne, nn;  // elements, local nodes
+    uint32_t own0;    // global id of the first owned node (local nodes [0, nown))
+    uint32_t ov0;     // first overflow slot of the shared local nodes [nown, nn)
+    uint16_t nown, pad;
 };
+
+// Partial slot of local node i of a tile.
+__host__ __device__ inline size_t tile_slot(uint32_t Ntot, uint32_t own0, uint32_t ov0, uint32_t nown, uint32_t i)
+{
+    return i < nown ? (size_t)own0 + i : (size_t)Ntot + ov0 + (i - nown);
+}
 
 struct ChunkMeta {
     uint32_t mesh;
@@ -71,6 +90,7 @@ struct MeshConsts {
     uint32_t knc0, nknc;
     float fK_f, mfm_f;  // factor_K and mass * factor_M rounded to FP32 (mixed path)
     float rot_check;    // mixed: FP64 re-solve when an FP32 rotation moves more than this under a small change of F
+    uint32_t rot_fp32;  // mixed: 1 = FP32 rotations with FP64 re-solves, 0 = FP64 rotations
     double refresh_drop_sq;  // mixed: FP64 residual when |r|^2 fell below this times its value at the last one
 
 };
@@ -98,8 +118,8 @@ struct BatchView {
     const uint16_t* lidx;          // [4 Ttot] (element-in-tile << 2 | slot), tile-relative
     const uint32_t* lptr0;         // [ntiles] base of each tile's lptr block
     // node data
-    const uint32_t* nptr;          // [Ntot+1]
-    const uint32_t* nslot;         // [sum nn] partial slots per node
+    const uint32_t* ov_ptr;        // [Ntot+1] per node: its overflow slots
+    const uint32_t* ov_slot;       // [overflow slots] in tile order
     const uint8_t* fixed;          // [Ntot]
     const double* rest;            // [3 Ntot]
     S* ydelta;                     // [3 Ntot] mixed: FP32 sum of this step's alpha d; null on FP64
@@ -117,7 +137,9 @@ struct BatchView {
     uint32_t* start_chunks;        // [nchunks]
     uint32_t* launch_tiles;        // [ntiles]
     uint32_t* launch_chunks;       // [nchunks]
-    uint32_t* list_count;          // [4]
+    uint32_t* refresh_tiles;       // [ntiles] mixed: meshes whose next iteration recomputes r in FP64
+    uint32_t* refresh_chunks;      // [nchunks]
+    uint32_t* list_count;          // [6] (+ refresh tiles, refresh chunks)
     // constraints
     const uint32_t* knc_node;      // [K] global node id
     const uint32_t* knc_mesh;      // [K]

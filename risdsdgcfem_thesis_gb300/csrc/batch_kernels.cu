@@ -194,7 +194,7 @@ __global__ void __launch_bounds__(256) k_tile_spmv(BatchView<S> b, const S* __re
             a1 += so[(3 * sl + 1) * kTileElems + el];
             a2 += so[(3 * sl + 2) * kTileElems + el];
         }
-        const size_t o = 3 * (size_t)(tm.n0 + i);
+        const size_t o = 3 * tile_slot(b.Ntot, tm.own0, tm.ov0, tm.nown, i);
         part[o] = a0;
         part[o + 1] = a1;
         part[o + 2] = a2;
@@ -216,10 +216,10 @@ __global__ void __launch_bounds__(256) k_tile_spmv_y64(BatchView<S> b, const dou
     if (mode == SPMV_Y64_REFRESH && flag && !*flag) return;
     __shared__ double sd[3 * kTileNodes];
     __shared__ double so[12 * kTileElems];
-    // ALL: the meshes that start a step; REFRESH: the running meshes (their
-    // work list on the mixed path)
-    const uint32_t* list = mode == SPMV_Y64_ALL ? b.start_tiles : b.act_tiles;
-    const uint32_t n = mode == SPMV_Y64_ALL ? b.list_count[0] : (b.act_tiles ? b.act_count[0] : b.ntiles);
+    // ALL: the meshes that start a step; REFRESH: the meshes that refresh in
+    // this iteration (their work list on the mixed path)
+    const uint32_t* list = mode == SPMV_Y64_ALL ? b.start_tiles : b.refresh_tiles;
+    const uint32_t n = mode == SPMV_Y64_ALL ? b.list_count[0] : (b.refresh_tiles ? b.list_count[4] : b.ntiles);
     for (uint32_t i = blockIdx.x; i < n; i += gridDim.x) {
         const uint32_t t = list_entry(list, i);
         const TileMeta tm = b.tiles[t];
@@ -267,7 +267,7 @@ __global__ void __launch_bounds__(256) k_tile_spmv_y64(BatchView<S> b, const dou
                 a1 += so[(3 * sl + 1) * kTileElems + el];
                 a2 += so[(3 * sl + 2) * kTileElems + el];
             }
-            const size_t o = 3 * (size_t)(tm.n0 + i);
+            const size_t o = 3 * tile_slot(b.Ntot, tm.own0, tm.ov0, tm.nown, i);
             part64[o] = a0;
             part64[o + 1] = a1;
             part64[o + 2] = a2;
@@ -353,7 +353,7 @@ __global__ void __launch_bounds__(256) k_tile_force(BatchView<S> b, const double
                     a1 += so[(3 * sl + 1) * kTileElems + el];
                     a2 += so[(3 * sl + 2) * kTileElems + el];
                 }
-                const size_t o = 3 * (size_t)(tm.n0 + i);
+                const size_t o = 3 * tile_slot(b.Ntot, tm.own0, tm.ov0, tm.nown, i);
                 part64[o] = a0;
                 part64[o + 1] = a1;
                 part64[o + 2] = a2;
@@ -396,14 +396,18 @@ __global__ void k_tile_potential(BatchView<S> b, const double* __restrict__ x, d
 // node kernels: one block per node chunk (kChunkNodes nodes of one mesh,
 // kNodeThreads threads striding it)
 
-template <typename P>
-__device__ __forceinline__ void sum_parts(const uint32_t* __restrict__ nptr, const uint32_t* __restrict__ nslot,
-                                          const P* __restrict__ part, size_t n, double& a0, double& a1, double& a2)
+// Sum of a node's partials: its owner tile's (node order) first, then its
+// overflow slots in tile order.
+template <typename S, typename P>
+__device__ __forceinline__ void sum_parts(const BatchView<S>& b, const P* __restrict__ part, size_t n, double& a0,
+                                          double& a1, double& a2)
 {
-    a0 = a1 = a2 = 0.0;
-    const uint32_t j1 = nptr[n + 1];
-    for (uint32_t j = nptr[n]; j < j1; j++) {
-        const size_t o = 3 * (size_t)nslot[j];
+    a0 = (double)part[3 * n];
+    a1 = (double)part[3 * n + 1];
+    a2 = (double)part[3 * n + 2];
+    const uint32_t j1 = b.ov_ptr[n + 1];
+    for (uint32_t j = b.ov_ptr[n]; j < j1; j++) {
+        const size_t o = 3 * ((size_t)b.Ntot + b.ov_slot[j]);
         a0 += (double)part[o];
         a1 += (double)part[o + 1];
         a2 += (double)part[o + 2];
@@ -423,7 +427,7 @@ __global__ void k_node_b(BatchView<S> b, const double* __restrict__ part64, cons
         const MeshConsts& c = b.mc[ch.mesh];
         for (size_t n = ch.n0 + threadIdx.x; n < ch.n1; n += blockDim.x) {
             double f0, f1, f2;
-            sum_parts(b.nptr, b.nslot, part64, n, f0, f1, f2);
+            sum_parts(b, part64, n, f0, f1, f2);
             const size_t i = 3 * n;
             bv[i] = (c.mass * c.gravity[0] - f0) * c.dt + c.mass * v[i];
             bv[i + 1] = (c.mass * c.gravity[1] - f1) * c.dt + c.mass * v[i + 1];
@@ -528,6 +532,7 @@ __device__ void grid_tail(const BatchView<S>& b, const LoopSync& ls, bool iterat
     }
     any = __syncthreads_or(any);
     refresh = __syncthreads_or(refresh);
+    if (refresh && b.refresh_tiles) build_refresh_lists(b);
     if (threadIdx.x == 0) {
         if (ls.refresh_flag) *ls.refresh_flag = refresh ? 1u : 0u;
         if (ls.body_runs) *ls.body_runs += 1u;
@@ -561,7 +566,7 @@ __global__ void k_node_residual(BatchView<S> b, const double* __restrict__ part6
             S r0 = 0, r1 = 0, r2 = 0;
             if (!b.fixed[n]) {
                 double s0, s1, s2;
-                sum_parts(b.nptr, b.nslot, part64, n, s0, s1, s2);
+                sum_parts(b, part64, n, s0, s1, s2);
                 r0 = (S)(bv[i] - (c.factor_K * s0 + mfm * y[i]));
                 r1 = (S)(bv[i + 1] - (c.factor_K * s1 + mfm * y[i + 1]));
                 r2 = (S)(bv[i + 2] - (c.factor_K * s2 + mfm * y[i + 2]));
@@ -590,6 +595,7 @@ __global__ void k_node_residual(BatchView<S> b, const double* __restrict__ part6
                 s.refresh_next = 0;  // r0 was formed from the FP64 product
                 s.delta_refresh = total;
                 s.k_refresh = 0;
+                s.confirm = 0;
                 s.done = cg_cont(s) ? 0u : 1u;
                 if (s.done) {
                     finish_stats(s);
@@ -627,10 +633,10 @@ __global__ void k_node_q(BatchView<S> b, const S* __restrict__ part, S* __restri
                 dn0 = dir_update<S>(beta, d[i], r[i]);
                 dn1 = dir_update<S>(beta, d[i + 1], r[i + 1]);
                 dn2 = dir_update<S>(beta, d[i + 2], r[i + 2]);
-                S s0 = 0, s1 = 0, s2 = 0;
-                const uint32_t j1 = b.nptr[n + 1];
-                for (uint32_t j = b.nptr[n]; j < j1; j++) {
-                    const size_t o = 3 * (size_t)b.nslot[j];
+                S s0 = part[3 * n], s1 = part[3 * n + 1], s2 = part[3 * n + 2];
+                const uint32_t j1 = b.ov_ptr[n + 1];
+                for (uint32_t j = b.ov_ptr[n]; j < j1; j++) {
+                    const size_t o = 3 * ((size_t)b.Ntot + b.ov_slot[j]);
                     s0 += part[o];
                     s1 += part[o + 1];
                     s2 += part[o + 2];
@@ -640,7 +646,7 @@ __global__ void k_node_q(BatchView<S> b, const S* __restrict__ part, S* __restri
                 q2 = fK * s2 + mfm * dn2;
                 if (refresh) {
                     double t0, t1, t2;
-                    sum_parts(b.nptr, b.nslot, part64, n, t0, t1, t2);
+                    sum_parts(b, part64, n, t0, t1, t2);
                     const double mfm64 = c.mass * c.factor_M;
                     r[i] = (S)(bv[i] - (c.factor_K * t0 + mfm64 * y_full(b, y, i)));
                     r[i + 1] = (S)(bv[i + 1] - (c.factor_K * t1 + mfm64 * y_full(b, y, i + 1)));
@@ -904,6 +910,25 @@ void BatchLaunch<S>::reset_counts(const BatchView<S>& b, const LoopSync& ls, cud
                                    cudaStream_t s)
 {
     k_reset_counts<S><<<1, 256, 0, s>>>(b, ls, if_start);
+    launch_counter()++;
+}
+
+__global__ void k_permute(const uint32_t* __restrict__ perm, uint64_t n, const double* __restrict__ src,
+                          double* __restrict__ dst, int to_batch)
+{
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t p = perm[i];
+        const uint64_t di = to_batch ? i : p, si = to_batch ? p : i;
+#pragma unroll
+        for (int a = 0; a < 3; a++) dst[3 * di + a] = src[3 * si + a];
+    }
+}
+
+void launch_permute(const uint32_t* perm, uint64_t n, const double* src, double* dst, bool to_batch, cudaStream_t s)
+{
+    if (n == 0) return;
+    const uint64_t blocks = (n + 255) / 256;
+    k_permute<<<blocks < 152 * 16 ? (unsigned)blocks : 152u * 16u, 256, 0, s>>>(perm, n, src, dst, to_batch ? 1 : 0);
     launch_counter()++;
 }
 

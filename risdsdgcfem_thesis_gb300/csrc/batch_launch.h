@@ -9,6 +9,10 @@ uint32_t grid_tiles(uint32_t ntiles);
 uint32_t tile_pipe_smem_bytes();
 void prepare_tile_pipe();
 uint32_t grid_chunks(uint32_t nchunks);
+// Node-vector permutation between the caller's order and the batch's:
+// to_batch: dst[i] = src[perm[i]]; otherwise dst[perm[i]] = src[i] (xyz each).
+void launch_permute(const uint32_t* perm, uint64_t n, const double* src, double* dst, bool to_batch,
+                    cudaStream_t s);
 
 // Arrival counters and graph handle of the fused CG finalisation.
 struct LoopSync {

@@ -34,7 +34,8 @@ struct StepScalars {
     uint32_t finished;      // batch: the CG loop ended during this launch (cleared at launch start)
     uint32_t refresh_next;  // mixed: the next iteration recomputes r = b - A y in FP64
     double delta_refresh;   // mixed: |r|^2 right after the last FP64 residual
-    uint32_t k_refresh, pad3;
+    uint32_t k_refresh;
+    uint32_t confirm;       // mixed: this iteration only measures the FP64 residual (exit test)
     unsigned long long total_iters;
 };
 

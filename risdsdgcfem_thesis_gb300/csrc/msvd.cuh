@@ -39,6 +39,18 @@ template <> struct MathOf<float> {
     static __device__ __forceinline__ float abs_(float x) { return ::fabsf(x); }
 };
 
+// Branch-tie tracking for the FP32 evaluation: the MSVD below takes discrete
+// decisions (which column, which axis, which eigenvalue order, the flip)
+// and, with the reference's eigenvalue formula, its rotation jumps when a
+// decision flips. near_tie() marks a comparison whose two sides are within
+// a relative margin of each other, where FP32 rounding may decide it
+// differently from FP64; a caller re-solves such an F in FP64. FP64 calls
+// pass no tracker and are unaffected.
+template <typename T> __device__ __forceinline__ void near_tie(bool* amb, T a, T b, T scale)
+{
+    if (amb && MathOf<T>::abs_(a - b) <= T(2e-3) * scale) *amb = true;
+}
+
 template <typename T>
 struct V3 {
     T x, y, z;
@@ -65,9 +77,15 @@ template <typename T> __device__ __forceinline__ V3<T> normalized(V3<T> a)
     T inv = T(1) / n;
     return scale(inv, a);
 }
-template <typename T> __device__ __forceinline__ V3<T> orthogonal_vector(V3<T> v)
+template <typename T> __device__ __forceinline__ V3<T> orthogonal_vector(V3<T> v, bool* amb = nullptr)
 {
     T ax = MathOf<T>::abs_(v.x), ay = MathOf<T>::abs_(v.y), az = MathOf<T>::abs_(v.z);
+    if (amb) {
+        const T sum = ax + ay + az;
+        near_tie(amb, ax, ay, sum);
+        near_tie(amb, ax, az, sum);
+        near_tie(amb, ay, az, sum);
+    }
     if (ax < ay) return (ax < az) ? mk<T>(T(0), v.z, -v.y) : mk<T>(v.y, -v.x, T(0));
     return (ay < az) ? mk<T>(-v.z, T(0), v.x) : mk<T>(v.y, -v.x, T(0));
 }
@@ -96,11 +114,17 @@ template <typename T> __device__ __forceinline__ Sym3<T> cofactor(const Sym3<T>&
     return r;
 }
 
-template <typename T> __device__ __forceinline__ V3<T> largest_column_normalized(const Sym3<T>& a)
+template <typename T> __device__ __forceinline__ V3<T> largest_column_normalized(const Sym3<T>& a, bool* amb = nullptr)
 {
     T s11 = a.x11 * a.x11, s12 = a.x21 * a.x21, s13 = a.x31 * a.x31;
     T s22 = a.x22 * a.x22, s23 = a.x32 * a.x32, s33 = a.x33 * a.x33;
     T scale1 = s11 + s12 + s13, scale2 = s12 + s22 + s23, scale3 = s13 + s23 + s33;
+    if (amb) {
+        const T sum = scale1 + scale2 + scale3;
+        near_tie(amb, scale1, scale2, sum);
+        near_tie(amb, scale1, scale3, sum);
+        near_tie(amb, scale2, scale3, sum);
+    }
     if (scale1 > scale2) {
         if (scale1 > scale3) return scale(T(1) / MathOf<T>::sqrt_(scale1), mk<T>(a.x11, a.x21, a.x31));
     } else if (scale2 > scale3) {
@@ -111,8 +135,10 @@ template <typename T> __device__ __forceinline__ V3<T> largest_column_normalized
 }
 
 // Rotation of one deformation gradient F (row-major 3x3) into R (row-major).
+// With `amb`, *amb is set when a branch decision was a near tie (see
+// near_tie); the arithmetic is the same with or without it.
 template <typename T>
-__device__ __forceinline__ void msvd_rotation(const T* F, T* R)
+__device__ __forceinline__ void msvd_rotation(const T* F, T* R, bool* amb = nullptr)
 {
     // normal equations F^T F (PhysBAM.h:129-137)
     Sym3<T> ne;
@@ -140,6 +166,13 @@ __device__ __forceinline__ void msvd_rotation(const T* F, T* R)
     T l0 = m + T(2) * sqrt_p_cos;
     T l1 = m - sqrt_p_cos - root_three_sqrt_p_sin;
     T l2 = m - sqrt_p_cos + root_three_sqrt_p_sin;
+    if (amb) {
+        // eigenvalue order and the flip test, relative to the spread
+        const T spread = MathOf<T>::abs_(l0 - l1) + MathOf<T>::abs_(l1 - l2) + MathOf<T>::abs_(l0 - l2);
+        near_tie(amb, l0, l1, spread);
+        near_tie(amb, l1, l2, spread);
+        near_tie(amb, l0, l2, spread);
+    }
     T lam0, lam1, lam2;
     if (l0 < l1) {
         if (l1 < l2) { lam0 = l2; lam1 = l1; lam2 = l0; }
@@ -154,11 +187,12 @@ __device__ __forceinline__ void msvd_rotation(const T* F, T* R)
     // Fast_Eigenvectors
     bool flipped = false;
     T lf0 = lam0, lf2 = lam2;
+    near_tie(amb, lam0 - lam1, lam1 - lam2, lam0 - lam2);
     if (lam0 - lam1 < lam1 - lam2) { lf0 = lam2; lf2 = lam0; flipped = true; }
     Sym3<T> am = ne;
     am.x11 -= lf0; am.x22 -= lf0; am.x33 -= lf0;
-    V3<T> v1 = largest_column_normalized(cofactor(am));
-    V3<T> o0 = normalized(orthogonal_vector(v1));
+    V3<T> v1 = largest_column_normalized(cofactor(am), amb);
+    V3<T> o0 = normalized(orthogonal_vector(v1, amb));
     V3<T> o1 = cross(v1, o0);
     // C = A_full * other_v, then A_reduced = C^T other_v (symmetric)
     T C00, C10, C20, C01, C11, C21;
@@ -182,6 +216,7 @@ __device__ __forceinline__ void msvd_rotation(const T* F, T* R)
         T c11 = r22, c21 = -r21, c22 = r11;
         T s11 = c11 * c11, s12 = c21 * c21, s22 = c22 * c22;
         T scale1 = s11 + s12, scale2 = s12 + s22;
+        near_tie(amb, scale1, scale2, scale1 + scale2);
         if (scale1 > scale2) { T inv = T(1) / MathOf<T>::sqrt_(scale1); w0 = inv * c11; w1 = inv * c21; }
         else if (scale2 > T(0)) { T inv = T(1) / MathOf<T>::sqrt_(scale2); w0 = inv * c21; w1 = inv * c22; }
         else { w0 = T(1); w1 = T(0); }

@@ -59,11 +59,12 @@ void launch_begin_eval_fp64(const MeshView<double>& m, const double* x, double* 
 // mesh's threshold, where F is re-solved in FP64. Per-mesh counts of
 // inverted elements and FP64 re-solves are added with integer atomics (one
 // per tile), so they do not depend on scheduling.
-// FP32 rotation of F for the mixed path. With tol > 0 the rotation is
-// computed again for F plus a fixed 2^-14 relative change; when the two
-// differ by more than tol (max entry), the FP32 result is not trusted
-// (near-coincident singular values make the MSVD's eigenvector steps
-// sensitive to rounding) and false is returned for an FP64 re-solve.
+// FP32 rotation of F for the mixed path. The result is not trusted -- false
+// is returned for an FP64 re-solve -- when one of the MSVD's branch
+// decisions was a near tie (FP32 rounding may decide it differently from
+// FP64, and the rotation jumps with the decision), or, with tol > 0, when
+// the rotation computed again for F plus a fixed 2^-14 relative change
+// differs by more than tol (max entry).
 template <typename S>
 __device__ __forceinline__ bool rotation_fp32(const double* F, float tol, S* Rs)
 {
@@ -74,7 +75,9 @@ __device__ __forceinline__ bool rotation_fp32(const double* F, float tol, S* Rs)
         Ff[c] = (float)F[c];
         s = fmaxf(s, fabsf(Ff[c]));
     }
-    msvd_rotation(Ff, Rf);
+    bool tie = false;
+    msvd_rotation(Ff, Rf, &tie);
+    if (tie) return false;  // a branch decision FP32 may take differently from FP64
     if (tol > 0.f) {
         const float d = s * 6.103515625e-05f;  // 2^-14 of the largest entry
         const float P[9] = {1.f, -1.f, 0.f, 0.f, 1.f, -1.f, 1.f, 0.f, 1.f};
@@ -123,7 +126,8 @@ __global__ void k_begin_eval_batch(BatchView<S> b, const double* __restrict__ x)
                 msvd_rotation(F, R);
 #pragma unroll
                 for (int c = 0; c < 9; c++) Rs[c] = (S)R[c];
-            } else if (detF > b.mc[tm.mesh].degenerate_det_F && rotation_fp32(F, b.mc[tm.mesh].rot_check, Rs)) {
+            } else if (b.mc[tm.mesh].rot_fp32 && detF > b.mc[tm.mesh].degenerate_det_F &&
+                       rotation_fp32(F, b.mc[tm.mesh].rot_check, Rs)) {
                 // FP32 rotation kept
             } else {
                 double R[9];

@@ -14,7 +14,9 @@
 // latency overlaps a whole tile. The tile also forms its share of d^T A d:
 //     fK * sum_e d_e . (R K0 R^T d)_e  +  m fM * sum_{nodes it owns} |d_n|^2,
 // which sums to d^T S A d (ILSS_CG.h:91-96) because d is zero on constrained
-// rows; a node is owned by the first tile (in tile order) that lists it.
+// rows; a node is owned by the first tile (in tile order) that lists it, and
+// its owner writes its partial in node order (the node pass reads it
+// coalesced; shared nodes' other partials go to overflow slots).
 //
 // k_node_update_fused: every block first sums its mesh's tile shares (fixed
 // order, so every block of the mesh gets the same bits) and forms alpha, or
@@ -32,7 +34,9 @@
 //                V mu, local ids (uchar4 as one word)
 //   88 ne4       uint16 lptr[nn+1]      tile-local CSR offsets
 //   + 2(nn+1)    uint16 lidx[4 ne]      slot * ne4 + element, element order
-//   (4-aligned)  uint32 nodes[nn]       global node id, bit 31 = owner
+//   (4-aligned)  uint32 nodes[nn]       batch node id (the tile's owned nodes first)
+//   + 4 nn       uint32 own0, ov0, nown   partial slots: local node i < nown -> part[own0 + i],
+//                                         else part[Ntot + ov0 + i - nown]
 //   size rounded up to 16.
 //
 // Every wait on an mbarrier is bounded: a wait that gives up records an error
@@ -326,14 +330,15 @@ __global__ void __launch_bounds__(256, 4) k_tile_spmv_pipe(BatchView<float> b, c
             const float* comp = reinterpret_cast<const float*>(stage);
             const uint16_t* lp = reinterpret_cast<const uint16_t*>(stage + blob_lptr_off(ne));
             const uint16_t* li = lp + (nn + 1);
-            const uint32_t* nodes = reinterpret_cast<const uint32_t*>(stage + blob_nodes_off(ne, nn));
+            const uint32_t* slots = reinterpret_cast<const uint32_t*>(stage + blob_slots_off(ne, nn));
+            const uint32_t own0 = slots[0], ov0 = slots[1], nown = slots[2];
             float share = 0.f;  // this thread's part of the tile's d^T A d
             if (tid < nn) {
                 const float dx = __fmaf_rn(cur.beta, cd0, cr0);
                 const float dy = __fmaf_rn(cur.beta, cd1, cr1);
                 const float dz = __fmaf_rn(cur.beta, cd2, cr2);
                 sd4[tid] = make_float4(dx, dy, dz, 0.f);
-                if (nodes[tid] >> 31) share = mfm * (dx * dx + dy * dy + dz * dz);
+                if (tid < nown) share = mfm * (dx * dx + dy * dy + dz * dz);  // the nodes this tile owns
             }
             __syncthreads();
             float out[12];
@@ -381,7 +386,7 @@ __global__ void __launch_bounds__(256, 4) k_tile_spmv_pipe(BatchView<float> b, c
                     a1 += v.y;
                     a2 += v.z;
                 }
-                const size_t o = 3 * (size_t)(cur.n0 + tid);
+                const size_t o = 3 * tile_slot(b.Ntot, own0, ov0, nown, tid);
                 part[o] = a0;
                 part[o + 1] = a1;
                 part[o + 2] = a2;
@@ -432,11 +437,12 @@ __global__ void __launch_bounds__(256) k_node_update_fused(BatchView<float> b, c
         // d^T A d of the mesh from its tiles' shares; every block of the mesh
         // forms the same value (same partials, same order)
         const F2 dq2 = sum_partials_f2(tshare + c.tile0, c.ntiles, sh);
+        const bool confirm = sm.confirm != 0;  // measure the FP64 residual only, no CG update
         if (threadIdx.x == 0) {
             const double dq = (double)dq2.hi + (double)dq2.lo;
             s_dq = dq;
-            s_brk = ::fabs(dq) < sm.abs_eps_sq;  // breakdown: leave before the update (ILSS_CG.h:97)
-            s_alpha = (float)(sm.delta_new / dq);
+            s_brk = !confirm && ::fabs(dq) < sm.abs_eps_sq;  // breakdown: leave before the update (ILSS_CG.h:97)
+            s_alpha = confirm ? 0.f : (float)(sm.delta_new / dq);
         }
         __syncthreads();
         const bool brk = s_brk != 0;
@@ -451,10 +457,11 @@ __global__ void __launch_bounds__(256) k_node_update_fused(BatchView<float> b, c
             const float d0 = __fmaf_rn(beta, d[i], r[i]);
             const float d1 = __fmaf_rn(beta, d[i + 1], r[i + 1]);
             const float d2 = __fmaf_rn(beta, d[i + 2], r[i + 2]);
-            float s0 = 0.f, s1 = 0.f, s2 = 0.f;
-            const uint32_t j1 = b.nptr[n + 1];
-            for (uint32_t j = b.nptr[n]; j < j1; j++) {
-                const size_t o = 3 * (size_t)b.nslot[j];
+            // the owner tile's partial (node order), then the overflow slots
+            float s0 = part[i], s1 = part[i + 1], s2 = part[i + 2];
+            const uint32_t j0 = b.ov_ptr[n], j1 = b.ov_ptr[n + 1];
+            for (uint32_t j = j0; j < j1; j++) {
+                const size_t o = 3 * ((size_t)b.Ntot + b.ov_slot[j]);
                 s0 += part[o];
                 s1 += part[o + 1];
                 s2 += part[o + 2];
@@ -463,9 +470,9 @@ __global__ void __launch_bounds__(256) k_node_update_fused(BatchView<float> b, c
             float r0 = r[i], r1 = r[i + 1], r2 = r[i + 2];
             float e0 = b.ydelta[i], e1 = b.ydelta[i + 1], e2 = b.ydelta[i + 2];
             if (refresh) {
-                double t0 = 0, t1 = 0, t2 = 0;
-                for (uint32_t j = b.nptr[n]; j < j1; j++) {
-                    const size_t o = 3 * (size_t)b.nslot[j];
+                double t0 = part64[i], t1 = part64[i + 1], t2 = part64[i + 2];
+                for (uint32_t j = j0; j < j1; j++) {
+                    const size_t o = 3 * ((size_t)b.Ntot + b.ov_slot[j]);
                     t0 += part64[o];
                     t1 += part64[o + 1];
                     t2 += part64[o + 2];
@@ -483,13 +490,18 @@ __global__ void __launch_bounds__(256) k_node_update_fused(BatchView<float> b, c
                 y[i + 2] = yc;
                 e0 = e1 = e2 = 0.f;
             }
-            b.ydelta[i] = __fmaf_rn(alpha_s, d0, e0);
-            b.ydelta[i + 1] = __fmaf_rn(alpha_s, d1, e1);
-            b.ydelta[i + 2] = __fmaf_rn(alpha_s, d2, e2);
-            r0 += na * q0;
-            r1 += na * q1;
-            r2 += na * q2;
-            d[i] = d0; d[i + 1] = d1; d[i + 2] = d2;
+            if (!confirm) {
+                r0 += na * q0;
+                r1 += na * q1;
+                r2 += na * q2;
+                e0 = __fmaf_rn(alpha_s, d0, e0);
+                e1 = __fmaf_rn(alpha_s, d1, e1);
+                e2 = __fmaf_rn(alpha_s, d2, e2);
+                d[i] = d0; d[i + 1] = d1; d[i + 2] = d2;
+            }
+            b.ydelta[i] = e0;
+            b.ydelta[i + 1] = e1;
+            b.ydelta[i + 2] = e2;
             r[i] = r0; r[i + 1] = r1; r[i + 2] = r2;
             acc += r0 * r0 + r1 * r1 + r2 * r2;
         }
@@ -500,7 +512,32 @@ __global__ void __launch_bounds__(256) k_node_update_fused(BatchView<float> b, c
             if (threadIdx.x == 0) {
                 StepScalars& st = b.st[ch.mesh];
                 st.dot_dq = s_dq;
-                if (brk) {
+                if (confirm) {
+                    // the FP64 residual of the current iterate decides: leave,
+                    // or go on from it -- with the recurrence's direction
+                    // (beta from the FP64 residual, reliable-update style),
+                    // unless the recursive residual had fallen to rounding
+                    // noise, then from the residual alone (beta = 0)
+                    const double total = (double)tot.hi + (double)tot.lo;
+                    const double rec = st.delta_new;  // recursive |r|^2 at the loop test
+                    st.confirm = 0;
+                    st.delta_old = rec;
+                    st.delta_new = total;
+                    st.delta_refresh = total;
+                    st.k_refresh = st.k;
+                    st.refresh_next = 0;
+                    if (total != total) st.status = 3u;
+                    if (cg_cont_t(st)) {
+                        st.beta = (rec > 0.0 && total <= 1e3 * rec) ? total / rec : 0.0;
+                        st.beta_f = (float)st.beta;
+                        st.done = 0;
+                    } else {
+                        st.done = 1;
+                        st.finished = 1;
+                        *b.list_dirty = 1u;
+                        finish_stats_t(st);
+                    }
+                } else if (brk) {
                     st.done = 1;
                     st.finished = 1;
                     *b.list_dirty = 1u;
@@ -526,7 +563,16 @@ __global__ void __launch_bounds__(256) k_node_update_fused(BatchView<float> b, c
                                        (c.refresh_every > 0 && st.k - st.k_refresh >= c.refresh_every))
                                           ? 1u
                                           : 0u;
-                    st.done = cg_cont_t(st) ? 0u : 1u;
+                    bool cont = cg_cont_t(st);
+                    if (!cont && st.k_refresh != st.k && st.k < st.max_iter && total == total &&
+                        (c.refresh_every > 0 || c.refresh_drop_sq > 0.0)) {
+                        // converged on the FP32 recursive residual: the next
+                        // iteration measures the FP64 residual before the loop ends
+                        cont = true;
+                        st.refresh_next = 1u;
+                        st.confirm = 1u;
+                    }
+                    st.done = cont ? 0u : 1u;
                     if (st.done) {
                         finish_stats_t(st);
                         st.finished = 1;
@@ -551,6 +597,7 @@ __global__ void __launch_bounds__(256) k_node_update_fused(BatchView<float> b, c
     }
     any = __syncthreads_or(any);
     rf = __syncthreads_or(rf);
+    if (rf) build_refresh_lists(b);
     if (threadIdx.x == 0) {
         const bool stop = ls.err && *(volatile const unsigned*)ls.err;
         bool budget_left = true;

@@ -41,7 +41,7 @@ def test_params_default_matches_reference_defaults(fem_lib):
     assert p.poisson_ratio == float(np.float32(0.25)) and p.damping_ratio == 1.0
     assert p.ls_max_iter == 20 and p.precision == fem_lib.FEM_PRECISION_FP64
     # mixed-path controls of this library (no counterpart in the reference)
-    assert p.degenerate_det_F == 1e-3 and p.rotation_check == 1e-3
+    assert p.degenerate_det_F == 1e-3 and p.rotation_check == 1e-3 and p.rotation_fp32 == 0
     assert p.refresh_drop == 0.0 and p.refresh_every == 50
 
 
