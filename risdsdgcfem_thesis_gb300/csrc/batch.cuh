@@ -129,7 +129,7 @@ struct BatchView {
     uint32_t* act_tiles;           // [ntiles]
     uint32_t* act_chunks;          // [nchunks]
     uint32_t* act_count;           // [2] entries in act_tiles, act_chunks
-    unsigned* list_dirty;          // set when a mesh leaves its CG loop
+    unsigned* list_dirty;          // tiles of the CG lists whose mesh has left its loop since the last rebuild
     // tiles and chunks of the meshes that start a step in this launch, and
     // of those that take part in it; list_count: start tiles, start chunks,
     // launch tiles, launch chunks

@@ -520,7 +520,7 @@ template <typename S>
 __device__ void grid_tail(const BatchView<S>& b, const LoopSync& ls, bool iteration)
 {
     if (!arrive_last(ls.gcount, gridDim.x)) return;
-    if (b.act_tiles && (!iteration || *(volatile const unsigned*)b.list_dirty)) build_active_lists(b);
+    if (b.act_tiles && (!iteration || *(volatile const unsigned*)b.list_dirty)) build_active_lists(b);  // FP64 tail: no lists
     int any = 0, refresh = 0;
     for (uint32_t i = threadIdx.x; i < b.M; i += blockDim.x) {
         volatile const StepScalars* sp = b.st + i;

@@ -240,7 +240,10 @@ __device__ __forceinline__ void look_meta(const BatchView<float>& b, uint32_t i,
 __device__ __forceinline__ void look_resolve(const BatchView<float>& b, TileLook& L)
 {
     if (!L.act) return;
-    L.beta = b.st[L.mesh].beta_f;
+    const StepScalars& st = b.st[L.mesh];
+    L.act = st.done == 0u;  // the list may still hold meshes that have left their loop
+    if (!L.act) return;
+    L.beta = st.beta_f;
     L.boff = b.blob_off16[L.tile];
     L.g = threadIdx.x < (L.nenn >> 16) ? __ldg(b.tile_nodes + L.n0 + threadIdx.x) : 0u;
 }
@@ -432,6 +435,7 @@ __global__ void __launch_bounds__(256) k_node_update_fused(BatchView<float> b, c
     for (uint32_t ia = blockIdx.x; ia < n_act; ia += gridDim.x) {
         const uint32_t ci = b.act_chunks[ia];
         const ChunkMeta ch = b.chunks[ci];
+        if (b.st[ch.mesh].done) continue;  // left its loop; the list is rebuilt lazily
         const MeshConsts& c = b.mc[ch.mesh];
         const StepScalars& sm = b.st[ch.mesh];
         // d^T A d of the mesh from its tiles' shares; every block of the mesh
@@ -534,13 +538,13 @@ __global__ void __launch_bounds__(256) k_node_update_fused(BatchView<float> b, c
                     } else {
                         st.done = 1;
                         st.finished = 1;
-                        *b.list_dirty = 1u;
+                        atomicAdd(b.list_dirty, c.ntiles);
                         finish_stats_t(st);
                     }
                 } else if (brk) {
                     st.done = 1;
                     st.finished = 1;
-                    *b.list_dirty = 1u;
+                    atomicAdd(b.list_dirty, c.ntiles);
                     finish_stats_t(st);
                 } else {
                     const double total = (double)tot.hi + (double)tot.lo;
@@ -576,7 +580,7 @@ __global__ void __launch_bounds__(256) k_node_update_fused(BatchView<float> b, c
                     if (st.done) {
                         finish_stats_t(st);
                         st.finished = 1;
-                        *b.list_dirty = 1u;
+                        atomicAdd(b.list_dirty, c.ntiles);
                     }
                 }
             }
@@ -585,7 +589,9 @@ __global__ void __launch_bounds__(256) k_node_update_fused(BatchView<float> b, c
     // last block of the grid: work lists (when a mesh left its loop), while
     // condition and refresh flag
     if (!arrive_last_t(ls.gcount, gridDim.x, &s_last)) return;
-    if (*(volatile const unsigned*)b.list_dirty) build_active_lists(b);
+    // rebuild the CG lists once a quarter of their tiles belong to meshes that
+    // have left their loop (the kernels skip those entries until then)
+    if (4u * *(volatile const unsigned*)b.list_dirty >= *(volatile const uint32_t*)b.act_count) build_active_lists(b);
     int any = 0, rf = 0;
     for (uint32_t m = threadIdx.x; m < b.M; m += blockDim.x) {
         volatile const StepScalars* sp = b.st + m;
