@@ -14,7 +14,8 @@
 //                 of each mesh sums its partials in a fixed order and forms
 //                 alpha (or stops the mesh on breakdown, ILSS_CG.h:97). On
 //                 refresh iterations (mixed) also the true residual b - A y
-//                 from the FP64 product of k_tile_spmv_y64.
+//                 from the product of k_tile_spmv_y64 (double-float
+//                 arithmetic, FP64 partial sums).
 //   k_node_update y += alpha d (FP64), r -= alpha q, FP64 |r|^2 partials; the
 //                 last block of each mesh forms beta and the mesh's loop test,
 //                 and the last block of the grid sets the CUDA-graph while
@@ -28,6 +29,7 @@
 #include "active_list.cuh"
 #include "batch.cuh"
 #include "batch_launch.h"
+#include "df.cuh"
 #include "elem_math.cuh"
 #include "msvd.cuh"
 
@@ -201,21 +203,39 @@ __global__ void __launch_bounds__(256) k_tile_spmv(BatchView<S> b, const S* __re
     }
 }
 
-// FP64 product of the iterate y (same element data, evaluated in FP64):
+// Product of the iterate y for the residual b - A y (same element data):
 // mode SPMV_Y64_ALL for every active mesh (initial residual of a step);
 // mode SPMV_Y64_REFRESH for meshes refreshing their residual this iteration,
 // and only when the finaliser raised the batch's refresh flag (otherwise the
-// launch returns at once).
+// launch returns at once). The FP64 path evaluates it in FP64. The mixed
+// path, whose element data is FP32, evaluates it in double-float arithmetic
+// (about 48 bits; FP64 would cost about 60 times the FP32 rate on this GPU)
+// and writes FP64 partial sums, so its residual is accurate to about 1e-14
+// of the magnitudes of the terms of A y.
 enum { SPMV_Y64_ALL = 0, SPMV_Y64_REFRESH = 1 };
+
+template <typename S>
+struct Y64Value {
+    using T = double;
+};
+template <>
+struct Y64Value<float> {
+    using T = DF;
+};
+__device__ __forceinline__ void y64_set(double& a, double v) { a = v; }
+__device__ __forceinline__ void y64_set(DF& a, double v) { a = df_from_double(v); }
+__device__ __forceinline__ double y64_get(double a) { return a; }
+__device__ __forceinline__ double y64_get(DF a) { return df_to_double(a); }
 
 template <typename S>
 __global__ void __launch_bounds__(256) k_tile_spmv_y64(BatchView<S> b, const double* __restrict__ y,
                                                        double* __restrict__ part64, int mode,
                                                        const unsigned* __restrict__ flag)
 {
+    using V = typename Y64Value<S>::T;
     if (mode == SPMV_Y64_REFRESH && flag && !*flag) return;
-    __shared__ double sd[3 * kTileNodes];
-    __shared__ double so[12 * kTileElems];
+    __shared__ V sd[3 * kTileNodes];
+    __shared__ V so[12 * kTileElems];
     // ALL: the meshes that start a step; REFRESH: the meshes that refresh in
     // this iteration (their work list on the mixed path)
     const uint32_t* list = mode == SPMV_Y64_ALL ? b.start_tiles : b.refresh_tiles;
@@ -230,47 +250,47 @@ __global__ void __launch_bounds__(256) k_tile_spmv_y64(BatchView<S> b, const dou
         const uint16_t* li = b.lidx + tm.c0;
         for (int i = threadIdx.x; i < tm.nn; i += blockDim.x) {
             const size_t g = b.tile_nodes[tm.n0 + i];
-            sd[i] = y_full(b, y, 3 * g);
-            sd[kTileNodes + i] = y_full(b, y, 3 * g + 1);
-            sd[2 * kTileNodes + i] = y_full(b, y, 3 * g + 2);
+            y64_set(sd[i], y_full(b, y, 3 * g));
+            y64_set(sd[kTileNodes + i], y_full(b, y, 3 * g + 1));
+            y64_set(sd[2 * kTileNodes + i], y_full(b, y, 3 * g + 2));
         }
         __syncthreads();
         if (threadIdx.x < tm.ne) {
             const size_t e = tm.e0 + threadIdx.x;
             const size_t T = b.Ttot;
-            double R[9], Di[9];
+            S R[9], Di[9];
 #pragma unroll
-            for (int c = 0; c < 9; c++) R[c] = (double)b.R[c * T + e];
+            for (int c = 0; c < 9; c++) R[c] = b.R[c * T + e];
 #pragma unroll
-            for (int c = 0; c < 9; c++) Di[c] = (double)b.Dinv[c * T + e];
-            const double k1 = b.mat[e], knu = b.mat[T + e], k2 = b.mat[2 * T + e];
+            for (int c = 0; c < 9; c++) Di[c] = b.Dinv[c * T + e];
+            const S k1 = b.mat[e], knu = b.mat[T + e], k2 = b.mat[2 * T + e];
             const uchar4 lc = b.lconn[e];
             const int ids[4] = {lc.x, lc.y, lc.z, lc.w};
-            double dl[12];
+            V dl[12];
 #pragma unroll
             for (int i = 0; i < 4; i++) {
                 dl[3 * i] = sd[ids[i]];
                 dl[3 * i + 1] = sd[kTileNodes + ids[i]];
                 dl[3 * i + 2] = sd[2 * kTileNodes + ids[i]];
             }
-            double out[12];
-            elem_RKRt<double>(R, Di, k1, knu, k2, dl, out);
+            V out[12];
+            elem_RKRt<V, S>(R, Di, k1, knu, k2, dl, out);
 #pragma unroll
             for (int c = 0; c < 12; c++) so[c * kTileElems + threadIdx.x] = out[c];
         }
         __syncthreads();
         for (int i = threadIdx.x; i < tm.nn; i += blockDim.x) {
-            double a0 = 0, a1 = 0, a2 = 0;
+            V a0{}, a1{}, a2{};
             for (int j = lp[i]; j < lp[i + 1]; j++) {
                 const int v = li[j], el = v >> 2, sl = v & 3;
-                a0 += so[(3 * sl) * kTileElems + el];
-                a1 += so[(3 * sl + 1) * kTileElems + el];
-                a2 += so[(3 * sl + 2) * kTileElems + el];
+                a0 = a0 + so[(3 * sl) * kTileElems + el];
+                a1 = a1 + so[(3 * sl + 1) * kTileElems + el];
+                a2 = a2 + so[(3 * sl + 2) * kTileElems + el];
             }
             const size_t o = 3 * tile_slot(b.Ntot, tm.own0, tm.ov0, tm.nown, i);
-            part64[o] = a0;
-            part64[o + 1] = a1;
-            part64[o + 2] = a2;
+            part64[o] = y64_get(a0);
+            part64[o + 1] = y64_get(a1);
+            part64[o + 2] = y64_get(a2);
         }
         __syncthreads();
     }
@@ -828,8 +848,11 @@ template <typename S>
 void BatchLaunch<S>::tile_spmv_y64(const BatchView<S>& b, const double* y, double* part64, int refresh,
                                    const unsigned* flag, cudaStream_t s)
 {
+    const char* name = sizeof(S) == 8 ? "y_product_fp64" : "y_product_mixed";
+    prof_begin(name, s);
     k_tile_spmv_y64<S><<<grid_tiles(b.ntiles), kTileElems, 0, s>>>(b, y, part64,
                                                                    refresh ? SPMV_Y64_REFRESH : SPMV_Y64_ALL, flag);
+    prof_end(name, s);
     launch_counter()++;
 }
 

@@ -12,11 +12,16 @@
 
 namespace femgb {
 
+// Values (displacements, forces) are of type S; the element's coefficients
+// (R, Dm^-1, material scalars) of type C, by default the same. The mixed
+// path's recomputed residual takes S = a double-float and C = float, the
+// type its element data is stored in.
+
 // Local-frame stress product: given H (displacement gradient in the element
 // frame), returns P = sigma(H) * Dinv^T (columns = forces on nodes 1..3 in
 // the element frame, V folded into the material scalars) and eps:sigma.
-template <typename S>
-__device__ __forceinline__ void stress_forces(const S* H, const S* Di, S k1, S knu, S k2, S* P, S& eps_sig)
+template <typename S, typename C = S>
+__device__ __forceinline__ void stress_forces(const S* H, const C* Di, C k1, C knu, C k2, S* P, S& eps_sig)
 {
     const S exx = H[0], eyy = H[4], ezz = H[8];
     const S gxy = H[1] + H[3], gyz = H[5] + H[7], gzx = H[2] + H[6];
@@ -34,8 +39,8 @@ __device__ __forceinline__ void stress_forces(const S* H, const S* Di, S k1, S k
 }
 
 // Writes R * P (world frame) to out[4][3]: node 0 gets minus the sum.
-template <typename S>
-__device__ __forceinline__ void rotate_out(const S* R, const S* P, S* out)
+template <typename S, typename C = S>
+__device__ __forceinline__ void rotate_out(const C* R, const S* P, S* out)
 {
     S Pw[9];
 #pragma unroll
@@ -54,8 +59,8 @@ __device__ __forceinline__ void rotate_out(const S* R, const S* P, S* out)
 }
 
 // Product R K0 R^T d for one element (world-frame nodal vectors d[4][3]).
-template <typename S>
-__device__ __forceinline__ void elem_RKRt(const S* R, const S* Di, S k1, S knu, S k2, const S* d, S* out)
+template <typename S, typename C = S>
+__device__ __forceinline__ void elem_RKRt(const C* R, const C* Di, C k1, C knu, C k2, const S* d, S* out)
 {
     S D[9];  // columns d1-d0, d2-d0, d3-d0 ; D[3a+j]
 #pragma unroll
