@@ -623,7 +623,7 @@ int fem_batch_finalize(fem_batch b)
         MeshConsts& c = mcs[mi];
         c.tile0 = (uint32_t)tiles.size();
         std::vector<int32_t> stamp(N, -1), local(N, 0);
-        std::vector<int32_t> intern(N, -1);  // caller's node -> batch node (first appearance in tile order)
+        std::vector<int32_t> intern(N, -1);  // caller's node -> batch node (tile order; by degree within a tile)
         uint32_t next_id = 0;
         uint32_t k = 0;
         while (k < T) {
@@ -662,17 +662,22 @@ int fem_batch_finalize(fem_batch b)
             tm.ne = (uint16_t)ne;
             tm.nn = (uint16_t)lnodes.size();
             // nodes first seen in this tile get the next batch ids and lead
-            // the tile's local list; the others follow in local order
+            // the tile's local list; the others follow. Within each group
+            // the nodes are ordered by their number of entries in the tile
+            // (most first, ties in local order): one thread sums one node's
+            // entries, and a warp then runs loops of similar length.
             {
                 std::vector<uint32_t> owned, shared;
-                for (uint32_t u : lnodes) {
-                    if (intern[u] < 0) {
-                        intern[u] = (int32_t)next_id++;
-                        owned.push_back(u);
-                    } else {
-                        shared.push_back(u);
-                    }
+                std::vector<uint16_t> deg(lnodes.size(), 0);
+                for (size_t el = lconn.size() - ne; el < lconn.size(); el++) {
+                    const uchar4 lc = lconn[el];
+                    deg[lc.x]++; deg[lc.y]++; deg[lc.z]++; deg[lc.w]++;
                 }
+                for (uint32_t u : lnodes) (intern[u] < 0 ? owned : shared).push_back(u);
+                auto by_degree = [&](uint32_t a, uint32_t b2) { return deg[local[a]] > deg[local[b2]]; };
+                std::stable_sort(owned.begin(), owned.end(), by_degree);
+                std::stable_sort(shared.begin(), shared.end(), by_degree);
+                for (uint32_t u : owned) intern[u] = (int32_t)next_id++;
                 std::vector<unsigned char> remap(lnodes.size());
                 for (size_t i = 0; i < owned.size(); i++) remap[local[owned[i]]] = (unsigned char)i;
                 for (size_t i = 0; i < shared.size(); i++)
@@ -834,16 +839,16 @@ int fem_batch_finalize(fem_batch b)
         for (uint32_t t = 0; t < b->ntiles; t++) {
             const TileMeta& tm = tiles[t];
             unsigned char* base = blob_h.data() + 16ull * blob_off16_h[t];
-            float* comp = reinterpret_cast<float*>(base);
             const uint32_t ne4 = blob_ne4(tm.ne);
+            auto put = [&](uint32_t c, uint32_t i, float v) { std::memcpy(base + blob_comp_off(c, i, ne4), &v, 4); };
             for (uint32_t i = 0; i < tm.ne; i++) {
                 const size_t e = tm.e0 + i;
-                comp[0 * ne4 + i] = 1.f; comp[4 * ne4 + i] = 1.f; comp[8 * ne4 + i] = 1.f;  // R = I
-                for (int c = 0; c < 9; c++) comp[(9 + c) * ne4 + i] = (float)Dinv_soa[c * T + e];
-                for (int c = 0; c < 3; c++) comp[(18 + c) * ne4 + i] = (float)mat_soa[c * T + e];
+                put(0, i, 1.f); put(4, i, 1.f); put(8, i, 1.f);  // R = I
+                for (uint32_t c = 0; c < 9; c++) put(9 + c, i, (float)Dinv_soa[c * T + e]);
+                for (uint32_t c = 0; c < 3; c++) put(18 + c, i, (float)mat_soa[c * T + e]);
                 const uchar4 lc = lconn[e];
                 const uint32_t w = (uint32_t)lc.x | ((uint32_t)lc.y << 8) | ((uint32_t)lc.z << 16) | ((uint32_t)lc.w << 24);
-                std::memcpy(&comp[21 * ne4 + i], &w, 4);
+                std::memcpy(base + blob_comp_off(21, i, ne4), &w, 4);
             }
             uint16_t* lp = reinterpret_cast<uint16_t*>(base + blob_lptr_off(tm.ne));
             const uint16_t* src_lp = lptr.data() + lptr0[t];
@@ -853,8 +858,6 @@ int fem_batch_finalize(fem_batch b)
                 const uint16_t v = lidx[tm.c0 + j];  // (element << 2 | slot) -> slot * ne4 + element
                 li[j] = (uint16_t)((v & 3u) * ne4 + (v >> 2));
             }
-            uint32_t* nodes = reinterpret_cast<uint32_t*>(base + blob_nodes_off(tm.ne, tm.nn));
-            for (uint32_t i = 0; i < tm.nn; i++) nodes[i] = tile_nodes[tm.n0 + i];
             uint32_t* slots = reinterpret_cast<uint32_t*>(base + blob_slots_off(tm.ne, tm.nn));
             slots[0] = tm.own0;
             slots[1] = tm.ov0;

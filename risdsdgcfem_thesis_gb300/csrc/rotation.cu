@@ -139,10 +139,13 @@ __global__ void k_begin_eval_batch(BatchView<S> b, const double* __restrict__ x)
 #pragma unroll
             for (int c = 0; c < 9; c++) b.R[c * T + e] = Rs[c];
             if (b.blob) {
-                float* comp = reinterpret_cast<float*>(b.blob + 16ull * b.blob_off16[t]);
-                const uint32_t ne4 = blob_ne4(tm.ne);
-#pragma unroll
-                for (int c = 0; c < 9; c++) comp[c * ne4 + threadIdx.x] = (float)Rs[c];
+                unsigned char* base = b.blob + 16ull * b.blob_off16[t];
+                const uint32_t ne4 = blob_ne4(tm.ne), i = threadIdx.x;
+                *reinterpret_cast<float4*>(base + blob_comp_off(0, i, ne4)) =
+                    make_float4((float)Rs[0], (float)Rs[1], (float)Rs[2], (float)Rs[3]);
+                *reinterpret_cast<float4*>(base + blob_comp_off(4, i, ne4)) =
+                    make_float4((float)Rs[4], (float)Rs[5], (float)Rs[6], (float)Rs[7]);
+                *reinterpret_cast<float*>(base + blob_comp_off(8, i, ne4)) = (float)Rs[8];
             }
             b.detF[e] = detF;
             if (detF <= 0.0) atomicAdd(&s_inv, 1u);

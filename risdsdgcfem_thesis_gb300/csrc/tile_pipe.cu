@@ -30,14 +30,17 @@
 //
 // Blob of a tile with ne elements (ne4 = ne rounded up to 4) and nn local
 // nodes, offsets from the blob start:
-//   0            float comp[22][ne4]: R (9), Dm^-1 (9), V(lambda+2mu), V lambda,
-//                V mu, local ids (uchar4 as one word)
+//   0            element data, 22 FP32 components per element: R (9),
+//                Dm^-1 (9), V(lambda+2mu), V lambda, V mu, local ids (uchar4
+//                as one word), in groups of four: float4 g[5][ne4] (components
+//                0-19), float2 [ne4] (components 20, 21)
 //   88 ne4       uint16 lptr[nn+1]      tile-local CSR offsets
 //   + 2(nn+1)    uint16 lidx[4 ne]      slot * ne4 + element, element order
-//   (4-aligned)  uint32 nodes[nn]       batch node id (the tile's owned nodes first)
-//   + 4 nn       uint32 own0, ov0, nown   partial slots: local node i < nown -> part[own0 + i],
+//   (4-aligned)  uint32 own0, ov0, nown   partial slots: local node i < nown -> part[own0 + i],
 //                                         else part[Ntot + ov0 + i - nown]
-//   size rounded up to 16.
+//   size rounded up to 16. The batch node ids of the tile's local nodes
+//   (its owned nodes first) are read from the batch's tile node list, ahead
+//   of the blob.
 //
 // Every wait on an mbarrier is bounded: a wait that gives up records an error
 // code in the batch's error word; the block then issues no further copies and
@@ -204,13 +207,13 @@ __device__ __forceinline__ void finish_stats_t(StepScalars& s)
 
 }  // namespace
 
-constexpr uint32_t kStageBytes = 26240;  // >= blob_bytes(256, 256), multiple of 128
-static_assert(kStageBytes >= 26128, "stage must hold the largest tile blob");
+constexpr uint32_t kStageBytes = 25216;  // >= blob_bytes(256, 256) = 25104, multiple of 128
+static_assert(kStageBytes >= 25104, "stage must hold the largest tile blob");
 
 // Shared memory: two blob stages (a tile's element outputs overwrite its
 // element data once every element has read it), the staged direction
-// sd4[256], two mbarriers and the warps' (hi, lo) shares: 56.7 KB, four
-// resident blocks per SM.
+// sd4[256], two mbarriers and the warps' shares: 54.5 KB, four resident
+// blocks per SM.
 constexpr uint32_t kPipeSmem = 2 * kStageBytes + 16u * kTileNodes + 16u + 8u * 8u;
 
 // What a block needs to know of one tile before its blob arrives.
@@ -330,7 +333,6 @@ __global__ void __launch_bounds__(256, 4) k_tile_spmv_pipe(BatchView<float> b, c
             const float fK = c.fK_f, mfm = c.mfm_f;
             const unsigned char* stage = smem + s * kStageBytes;
             const uint32_t ne4 = blob_ne4(ne);
-            const float* comp = reinterpret_cast<const float*>(stage);
             const uint16_t* lp = reinterpret_cast<const uint16_t*>(stage + blob_lptr_off(ne));
             const uint16_t* li = lp + (nn + 1);
             const uint32_t* slots = reinterpret_cast<const uint32_t*>(stage + blob_slots_off(ne, nn));
@@ -347,13 +349,13 @@ __global__ void __launch_bounds__(256, 4) k_tile_spmv_pipe(BatchView<float> b, c
             float out[12];
             if (tid < ne) {
                 const int i = tid;
-                float R[9], Di[9];
-#pragma unroll
-                for (int k = 0; k < 9; k++) R[k] = comp[k * ne4 + i];
-#pragma unroll
-                for (int k = 0; k < 9; k++) Di[k] = comp[(9 + k) * ne4 + i];
-                const float k1 = comp[18 * ne4 + i], knu = comp[19 * ne4 + i], k2 = comp[20 * ne4 + i];
-                const uint32_t lw = reinterpret_cast<const uint32_t*>(comp)[21 * ne4 + i];
+                const float4* g4 = reinterpret_cast<const float4*>(stage) + i;
+                const float4 q0 = g4[0], q1 = g4[ne4], q2 = g4[2 * ne4], q3 = g4[3 * ne4], q4 = g4[4 * ne4];
+                const float2 q5 = reinterpret_cast<const float2*>(stage + 80u * ne4)[i];
+                const float R[9] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w, q2.x};
+                const float Di[9] = {q2.y, q2.z, q2.w, q3.x, q3.y, q3.z, q3.w, q4.x, q4.y};
+                const float k1 = q4.z, knu = q4.w, k2 = q5.x;
+                const uint32_t lw = __float_as_uint(q5.y);
                 const int ids[4] = {(int)(lw & 0xff), (int)((lw >> 8) & 0xff), (int)((lw >> 16) & 0xff),
                                     (int)(lw >> 24)};
                 float dl[12];
@@ -394,8 +396,13 @@ __global__ void __launch_bounds__(256, 4) k_tile_spmv_pipe(BatchView<float> b, c
                 part[o + 1] = a1;
                 part[o + 2] = a2;
             }
-            const F2 w = warp_sum_f2(F2{share, 0.f});
-            if ((tid & 31) == 0) wsh[tid >> 5] = make_float2(w.hi, w.lo);
+            // the terms are non-negative (d_e^T R K0 R^T d_e and m fM |d|^2),
+            // so a warp's FP32 tree sum is accurate to a few ulps; the warps'
+            // sums are added as (hi, lo) pairs
+            float w = share;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) w += __shfl_down_sync(0xffffffffu, w, o);
+            if ((tid & 31) == 0) wsh[tid >> 5] = make_float2(w, 0.f);
         } else {
             look_resolve(b, n2);
         }
