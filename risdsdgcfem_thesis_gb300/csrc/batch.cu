@@ -862,6 +862,8 @@ int fem_batch_finalize(fem_batch b)
             slots[0] = tm.own0;
             slots[1] = tm.ov0;
             slots[2] = tm.nown;
+            std::memcpy(&slots[3], &mcs[tm.mesh].fK_f, 4);
+            std::memcpy(&slots[4], &mcs[tm.mesh].mfm_f, 4);
         }
     }
     std::vector<double> Rinit(9 * T, 0.0);

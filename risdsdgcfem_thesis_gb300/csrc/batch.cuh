@@ -46,7 +46,8 @@ constexpr int kNodeThreads = 256;  // threads per node-kernel block
 // components 4g..4g+3 as float4[ne4], group 5 components 20, 21 as
 // float2[ne4] (one 16- or 8-byte load per group and element, consecutive
 // elements in consecutive words); then uint16 lptr[nn+1], uint16 lidx[4 ne],
-// uint32 {own0, ov0, nown} (the tile's partial slots).
+// uint32 {own0, ov0, nown} (the tile's partial slots) and float {fK, m fM}
+// (its mesh's FP32 factors).
 __host__ __device__ inline uint32_t blob_ne4(uint32_t ne) { return (ne + 3u) & ~3u; }
 // Byte offset of component c of element i.
 __host__ __device__ inline uint32_t blob_comp_off(uint32_t c, uint32_t i, uint32_t ne4)
@@ -60,7 +61,7 @@ __host__ __device__ inline uint32_t blob_slots_off(uint32_t ne, uint32_t nn)
 }
 __host__ __device__ inline uint32_t blob_bytes(uint32_t ne, uint32_t nn)
 {
-    return (blob_slots_off(ne, nn) + 12u + 15u) & ~15u;
+    return (blob_slots_off(ne, nn) + 20u + 15u) & ~15u;
 }
 
 struct TileMeta {

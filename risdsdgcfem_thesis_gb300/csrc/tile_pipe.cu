@@ -38,6 +38,7 @@
 //   + 2(nn+1)    uint16 lidx[4 ne]      slot * ne4 + element, element order
 //   (4-aligned)  uint32 own0, ov0, nown   partial slots: local node i < nown -> part[own0 + i],
 //                                         else part[Ntot + ov0 + i - nown]
+//   + 12         float fK, m fM         the mesh's FP32 factors
 //   size rounded up to 16. The batch node ids of the tile's local nodes
 //   (its owned nodes first) are read from the batch's tile node list, ahead
 //   of the blob.
@@ -207,8 +208,8 @@ __device__ __forceinline__ void finish_stats_t(StepScalars& s)
 
 }  // namespace
 
-constexpr uint32_t kStageBytes = 25216;  // >= blob_bytes(256, 256) = 25104, multiple of 128
-static_assert(kStageBytes >= 25104, "stage must hold the largest tile blob");
+constexpr uint32_t kStageBytes = 25216;  // >= blob_bytes(256, 256) = 25120, multiple of 128
+static_assert(kStageBytes >= 25120, "stage must hold the largest tile blob");
 
 // Shared memory: two blob stages (a tile's element outputs overwrite its
 // element data once every element has read it), the staged direction
@@ -218,37 +219,50 @@ constexpr uint32_t kPipeSmem = 2 * kStageBytes + 16u * kTileNodes + 16u + 8u * 8
 
 // What a block needs to know of one tile before its blob arrives.
 struct TileLook {
-    uint32_t tile;            // tile id
-    uint32_t mesh, n0, nenn;  // nenn: ne | nn << 16
-    uint32_t boff;            // blob offset / 16
-    uint32_t g;               // global node id of this thread's local node
-    float beta;               // beta of the tile's mesh
-    bool act;                 // a tile to do
+    uint32_t tile;      // tile id
+    uint32_t mesh, n0;  // the tile's mesh and first entry in the tile node list
+    uint32_t sizes;     // ne | nn << 10 | nown << 20; 0: not an entry of the work list
+    uint32_t boff;      // blob offset / 16
+    uint32_t g;         // batch node id of this thread's local node
+    uint32_t done;      // the mesh has left its loop (the list may still hold it)
+    float beta;         // beta of the tile's mesh
 };
+
+__device__ __forceinline__ uint32_t look_ne(const TileLook& L) { return L.sizes & 0x3ffu; }
+__device__ __forceinline__ uint32_t look_nn(const TileLook& L) { return (L.sizes >> 10) & 0x3ffu; }
+__device__ __forceinline__ uint32_t look_nown(const TileLook& L) { return L.sizes >> 20; }
+// A tile to do (valid once resolved).
+__device__ __forceinline__ bool look_live(const TileLook& L) { return L.sizes != 0u && L.done == 0u; }
 
 // First half of a look-up: entry i of the work list and the tile's metadata.
 __device__ __forceinline__ void look_meta(const BatchView<float>& b, uint32_t i, uint32_t n, TileLook& L)
 {
-    L.act = i < n;
-    if (L.act) {
+    L.sizes = 0u;
+    L.done = 0u;
+    if (i < n) {
         L.tile = b.act_tiles[i];
         const TileMeta tm = b.tiles[L.tile];
         L.mesh = tm.mesh;
         L.n0 = tm.n0;
-        L.nenn = (uint32_t)tm.ne | ((uint32_t)tm.nn << 16);
+        L.sizes = (uint32_t)tm.ne | ((uint32_t)tm.nn << 10) | ((uint32_t)tm.nown << 20);
     }
 }
 
-// Second half: the loads that depend on the tile's metadata.
+// Second half: the loads that depend on the tile's metadata, all issued
+// without waiting on one another (nothing here branches on a loaded value).
 __device__ __forceinline__ void look_resolve(const BatchView<float>& b, TileLook& L)
 {
-    if (!L.act) return;
+    if (L.sizes == 0u) return;
     const StepScalars& st = b.st[L.mesh];
-    L.act = st.done == 0u;  // the list may still hold meshes that have left their loop
-    if (!L.act) return;
+    L.done = st.done;
     L.beta = st.beta_f;
     L.boff = b.blob_off16[L.tile];
-    L.g = threadIdx.x < (L.nenn >> 16) ? __ldg(b.tile_nodes + L.n0 + threadIdx.x) : 0u;
+    L.g = threadIdx.x < look_nn(L) ? __ldg(b.tile_nodes + L.n0 + threadIdx.x) : 0u;
+}
+
+__device__ __forceinline__ void fence_proxy_async_smem()
+{
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
 
 __global__ void __launch_bounds__(256, 4) k_tile_spmv_pipe(BatchView<float> b, const float* __restrict__ dvec,
@@ -273,9 +287,15 @@ __global__ void __launch_bounds__(256, 4) k_tile_spmv_pipe(BatchView<float> b, c
     __syncthreads();
 
     // Software pipeline over this block's entries i, i+G, i+2G, ... of the
-    // work list: while tile i is computed, the blob of i+G is in flight (bulk
-    // copy) together with this thread's gather of d and r for its local node
-    // of i+G, and the metadata of i+2G is looked up.
+    // work list. Per tile (cur, in stage s):
+    //   stage the direction of its nodes in sd4 (from registers gathered one
+    //   tile earlier) | wait for its blob; barrier A, which also ends every
+    //   thread's reads of the other stage | thread 0 stores the previous
+    //   tile's d^T A d share and issues the copy of the next tile's blob into
+    //   the other stage | element products | the metadata of the tile after
+    //   next is resolved and this thread's d and r of the next tile are
+    //   gathered into registers | barrier B | outputs over the element data |
+    //   barrier C | node sums.
     const uint32_t n_act = *(volatile const uint32_t*)b.act_count;
     uint32_t i = blockIdx.x;
     TileLook cur, nxt, n2;
@@ -288,102 +308,116 @@ __global__ void __launch_bounds__(256, 4) k_tile_spmv_pipe(BatchView<float> b, c
     int s = 0;
     bool failed = false;
     auto issue = [&](const TileLook& L, int st) {
-        const uint32_t ne = L.nenn & 0xffffu, nn = L.nenn >> 16;
-        const uint32_t bytes = blob_bytes(ne, nn);
+        const uint32_t bytes = blob_bytes(look_ne(L), look_nn(L));
         mbar_expect_tx(&bar[st], bytes);
         bulk_copy_g2s(smem + st * kStageBytes, b.blob + 16ull * L.boff, bytes, &bar[st]);
     };
     float cd0 = 0.f, cd1 = 0.f, cd2 = 0.f, cr0 = 0.f, cr1 = 0.f, cr2 = 0.f;
-    if (cur.act) {
+    if (look_live(cur)) {
         if (tid == 0) issue(cur, 0);
         pending |= 1u;
-        if (tid < (cur.nenn >> 16)) {
+        if (tid < look_nn(cur)) {
             const size_t g = 3 * (size_t)cur.g;
             cd0 = __ldg(dvec + g); cd1 = __ldg(dvec + g + 1); cd2 = __ldg(dvec + g + 2);
             cr0 = __ldg(rvec + g); cr1 = __ldg(rvec + g + 1); cr2 = __ldg(rvec + g + 2);
         }
     }
+    // the previous tile whose share thread 0 stores after barrier A (kept in
+    // shared memory: only thread 0 uses it); ~0u: none
+    __shared__ uint32_t s_prev;
+    if (tid == 0) s_prev = ~0u;
     for (; i < n_act; i += G) {
-        look_meta(b, i + 2 * G, n_act, n2);  // resolved after the element products
+        const bool live = look_live(cur), nlive = look_live(nxt);
+        const uint32_t ne = look_ne(cur), nn = look_nn(cur);
+        float dd = 0.f;  // |d|^2 of this thread's node when the tile owns it
+        if (live && tid < nn) {
+            const float dx = __fmaf_rn(cur.beta, cd0, cr0);
+            const float dy = __fmaf_rn(cur.beta, cd1, cr1);
+            const float dz = __fmaf_rn(cur.beta, cd2, cr2);
+            sd4[tid] = make_float4(dx, dy, dz, 0.f);
+            if (tid < look_nown(cur)) dd = dx * dx + dy * dy + dz * dz;
+        }
+        // barrier A: every thread polls; the block agrees on the outcome so
+        // the barriers below stay uniform
+        const bool wait = live && !failed;
+        const bool ok = !wait || mbar_wait_bounded(&bar[s], (phase >> s) & 1u);
+        if (__syncthreads_or(!ok)) {
+            if (tid == 0) atomicExch(err, 1u);
+            failed = true;  // no new copies; the ones in flight are drained at the end
+        } else if (wait) {
+            phase ^= 1u << s;
+            pending &= ~(1u << s);
+        }
+        if (tid == 0) {
+            if (s_prev != ~0u) {
+                F2 a = {0.f, 0.f};
+                if (!failed)
+                    for (int k = 0; k < (int)(blockDim.x >> 5); k++) a = f2_add(a, F2{wsh[k].x, wsh[k].y});
+                tshare[s_prev] = make_float2(a.hi, a.lo);
+            }
+            s_prev = live ? cur.tile : ~0u;
+            if (!failed && nlive) issue(nxt, s ^ 1);
+        }
+        if (!failed && nlive) pending |= 1u << (s ^ 1);
+        const bool work = live && !failed;
+        const unsigned char* stage = smem + s * kStageBytes;
+        const uint32_t ne4 = blob_ne4(ne);
+        const float* fac = reinterpret_cast<const float*>(stage + blob_slots_off(ne, nn)) + 3;  // fK, m fM
+        float share = 0.f;  // this thread's part of the tile's d^T A d
+        if (work) share = fac[1] * dd;  // the nodes the tile owns
+        float out[12];
+        if (work && tid < ne) {
+            const float4* g4 = reinterpret_cast<const float4*>(stage) + tid;
+            const float4 q0 = g4[0], q1 = g4[ne4], q2 = g4[2 * ne4], q3 = g4[3 * ne4], q4 = g4[4 * ne4];
+            const float2 q5 = reinterpret_cast<const float2*>(stage + 80u * ne4)[tid];
+            const float R[9] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w, q2.x};
+            const float Di[9] = {q2.y, q2.z, q2.w, q3.x, q3.y, q3.z, q3.w, q4.x, q4.y};
+            const float k1 = q4.z, knu = q4.w, k2 = q5.x;
+            const uint32_t lw = __float_as_uint(q5.y);
+            const int ids[4] = {(int)(lw & 0xff), (int)((lw >> 8) & 0xff), (int)((lw >> 16) & 0xff),
+                                (int)(lw >> 24)};
+            float dl[12];
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                const float4 v = sd4[ids[k]];
+                dl[3 * k] = v.x;
+                dl[3 * k + 1] = v.y;
+                dl[3 * k + 2] = v.z;
+            }
+            elem_RKRt<float>(R, Di, k1, knu, k2, dl, out);
+            float eq = 0.f;
+#pragma unroll
+            for (int k = 0; k < 12; k++) eq = __fmaf_rn(dl[k], out[k], eq);
+            share = __fmaf_rn(fac[0], eq, share);
+        }
+        // the tile after next: looked up here, after the element products,
+        // so that its values do not occupy registers during them
+        look_meta(b, i + 2 * G, n_act, n2);
+        look_resolve(b, n2);
         float nd0 = 0.f, nd1 = 0.f, nd2 = 0.f, nr0 = 0.f, nr1 = 0.f, nr2 = 0.f;
-        if (!failed && nxt.act) {  // after a failed wait no new copies are issued
-            if (tid == 0) issue(nxt, s ^ 1);
-            pending |= 1u << (s ^ 1);
-            if (tid < (nxt.nenn >> 16)) {
-                const size_t g = 3 * (size_t)nxt.g;
-                nd0 = __ldg(dvec + g); nd1 = __ldg(dvec + g + 1); nd2 = __ldg(dvec + g + 2);
-                nr0 = __ldg(rvec + g); nr1 = __ldg(rvec + g + 1); nr2 = __ldg(rvec + g + 2);
-            }
+        if (nlive && tid < look_nn(nxt)) {
+            const size_t g = 3 * (size_t)nxt.g;
+            nd0 = __ldg(dvec + g); nd1 = __ldg(dvec + g + 1); nd2 = __ldg(dvec + g + 2);
+            nr0 = __ldg(rvec + g); nr1 = __ldg(rvec + g + 1); nr2 = __ldg(rvec + g + 2);
         }
-        if (cur.act) {
-            // every thread polls; the block agrees on the outcome so the
-            // barriers below stay uniform
-            const bool ok = !failed && mbar_wait_bounded(&bar[s], (phase >> s) & 1u);
-            if (__syncthreads_or(!ok)) {
-                if (!failed && tid == 0) atomicExch(err, 1u);
-                failed = true;
-            } else {
-                phase ^= 1u << s;
-                pending &= ~(1u << s);
-            }
-        }
-        if (cur.act && !failed) {
-            const uint32_t ne = cur.nenn & 0xffffu, nn = cur.nenn >> 16;
-            const MeshConsts& c = b.mc[cur.mesh];
-            const float fK = c.fK_f, mfm = c.mfm_f;
-            const unsigned char* stage = smem + s * kStageBytes;
-            const uint32_t ne4 = blob_ne4(ne);
-            const uint16_t* lp = reinterpret_cast<const uint16_t*>(stage + blob_lptr_off(ne));
-            const uint16_t* li = lp + (nn + 1);
-            const uint32_t* slots = reinterpret_cast<const uint32_t*>(stage + blob_slots_off(ne, nn));
-            const uint32_t own0 = slots[0], ov0 = slots[1], nown = slots[2];
-            float share = 0.f;  // this thread's part of the tile's d^T A d
-            if (tid < nn) {
-                const float dx = __fmaf_rn(cur.beta, cd0, cr0);
-                const float dy = __fmaf_rn(cur.beta, cd1, cr1);
-                const float dz = __fmaf_rn(cur.beta, cd2, cr2);
-                sd4[tid] = make_float4(dx, dy, dz, 0.f);
-                if (tid < nown) share = mfm * (dx * dx + dy * dy + dz * dz);  // the nodes this tile owns
-            }
-            __syncthreads();
-            float out[12];
-            if (tid < ne) {
-                const int i = tid;
-                const float4* g4 = reinterpret_cast<const float4*>(stage) + i;
-                const float4 q0 = g4[0], q1 = g4[ne4], q2 = g4[2 * ne4], q3 = g4[3 * ne4], q4 = g4[4 * ne4];
-                const float2 q5 = reinterpret_cast<const float2*>(stage + 80u * ne4)[i];
-                const float R[9] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w, q2.x};
-                const float Di[9] = {q2.y, q2.z, q2.w, q3.x, q3.y, q3.z, q3.w, q4.x, q4.y};
-                const float k1 = q4.z, knu = q4.w, k2 = q5.x;
-                const uint32_t lw = __float_as_uint(q5.y);
-                const int ids[4] = {(int)(lw & 0xff), (int)((lw >> 8) & 0xff), (int)((lw >> 16) & 0xff),
-                                    (int)(lw >> 24)};
-                float dl[12];
-#pragma unroll
-                for (int k = 0; k < 4; k++) {
-                    const float4 v = sd4[ids[k]];
-                    dl[3 * k] = v.x;
-                    dl[3 * k + 1] = v.y;
-                    dl[3 * k + 2] = v.z;
-                }
-                elem_RKRt<float>(R, Di, k1, knu, k2, dl, out);
-                float eq = 0.f;
-#pragma unroll
-                for (int k = 0; k < 12; k++) eq = __fmaf_rn(dl[k], out[k], eq);
-                share = __fmaf_rn(fK, eq, share);
-            }
-            look_resolve(b, n2);
-            // every element's data has been read: its space takes the outputs,
-            // so4[slot * ne4 + element]
+        if (work) {
+            // barrier B: every element's data has been read; its space takes
+            // the outputs, so4[slot * ne4 + element]
             __syncthreads();
             float4* so4 = reinterpret_cast<float4*>(smem + s * kStageBytes);
             if (tid < ne) {
 #pragma unroll
                 for (int k = 0; k < 4; k++)
                     so4[k * ne4 + tid] = make_float4(out[3 * k], out[3 * k + 1], out[3 * k + 2], 0.f);
+                // these generic-proxy writes precede the next bulk copy into
+                // this stage (issued after a later barrier)
+                fence_proxy_async_smem();
             }
-            __syncthreads();
+            __syncthreads();  // barrier C
             if (tid < nn) {
+                const uint16_t* lp = reinterpret_cast<const uint16_t*>(stage + blob_lptr_off(ne));
+                const uint16_t* li = lp + (nn + 1);
+                const uint32_t* slots = reinterpret_cast<const uint32_t*>(stage + blob_slots_off(ne, nn));
                 float a0 = 0.f, a1 = 0.f, a2 = 0.f;
                 for (int j = lp[tid]; j < lp[tid + 1]; j++) {
                     const float4 v = so4[li[j]];
@@ -391,7 +425,7 @@ __global__ void __launch_bounds__(256, 4) k_tile_spmv_pipe(BatchView<float> b, c
                     a1 += v.y;
                     a2 += v.z;
                 }
-                const size_t o = 3 * tile_slot(b.Ntot, own0, ov0, nown, tid);
+                const size_t o = 3 * tile_slot(b.Ntot, slots[0], slots[1], look_nown(cur), tid);
                 part[o] = a0;
                 part[o + 1] = a1;
                 part[o + 2] = a2;
@@ -403,21 +437,19 @@ __global__ void __launch_bounds__(256, 4) k_tile_spmv_pipe(BatchView<float> b, c
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) w += __shfl_down_sync(0xffffffffu, w, o);
             if ((tid & 31) == 0) wsh[tid >> 5] = make_float2(w, 0.f);
-        } else {
-            look_resolve(b, n2);
-        }
-        __syncthreads();
-        if (cur.act && tid == 0) {
-            F2 a = {0.f, 0.f};
-            if (!failed)
-                for (int k = 0; k < (int)(blockDim.x >> 5); k++) a = f2_add(a, F2{wsh[k].x, wsh[k].y});
-            tshare[cur.tile] = make_float2(a.hi, a.lo);
         }
         cur = nxt;
         nxt = n2;
         cd0 = nd0; cd1 = nd1; cd2 = nd2;
         cr0 = nr0; cr1 = nr1; cr2 = nr2;
         s ^= 1;
+    }
+    __syncthreads();
+    if (tid == 0 && s_prev != ~0u) {
+        F2 a = {0.f, 0.f};
+        if (!failed)
+            for (int k = 0; k < (int)(blockDim.x >> 5); k++) a = f2_add(a, F2{wsh[k].x, wsh[k].y});
+        tshare[s_prev] = make_float2(a.hi, a.lo);
     }
     if (failed) {
         for (int k = 0; k < 2; k++)
@@ -604,7 +636,6 @@ __global__ void __launch_bounds__(256) k_node_update_fused(BatchView<float> b, c
         volatile const StepScalars* sp = b.st + m;
         if (!sp->done) {
             any = 1;
-            const MeshConsts& c = b.mc[m];
             if (sp->refresh_next) rf = 1;
         }
     }
