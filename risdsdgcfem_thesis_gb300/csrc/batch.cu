@@ -127,7 +127,7 @@ struct fem_batch_s {
     Dev<int4> gtets;
     Dev<unsigned char> Dinv_s, mat_s, R_s;  // S-typed, raw bytes
     Dev<double> Dinv64, vol, detF;
-    Dev<uint32_t> tile_nodes, lptr0, ov_ptr, ov_slot, knc_node, knc_mesh;
+    Dev<uint32_t> tile_nodes, lptr0, ov_ptr, ov_map, knc_node, knc_mesh;
     std::vector<uint32_t> perm_h, inv_h;  // batch node -> caller's node, and back (global ids)
     Dev<uint32_t> perm;                   // perm_h on the device (whole-batch state transfers)
     Dev<double> stage_x, stage_v;         // caller-order staging for whole-batch transfers
@@ -181,7 +181,7 @@ struct fem_batch_s {
         b.lidx = lidx.p;
         b.lptr0 = lptr0.p;
         b.ov_ptr = ov_ptr.p;
-        b.ov_slot = ov_slot.p;
+        b.ov_map = ov_map.p;
         b.fixed = fixed.p;
         b.rest = rest.p;
         b.ydelta = opt.precision == FEM_PRECISION_MIXED ? reinterpret_cast<S*>(ydelta_s.p) : nullptr;
@@ -213,7 +213,7 @@ struct fem_batch_s {
         graph = nullptr;
         tiles.release(); chunks.release(); mc.release(); st.release(); active.release(); gtets.release();
         Dinv_s.release(); mat_s.release(); R_s.release(); Dinv64.release(); vol.release(); detF.release();
-        tile_nodes.release(); lptr0.release(); ov_ptr.release(); ov_slot.release(); knc_node.release();
+        tile_nodes.release(); lptr0.release(); ov_ptr.release(); ov_map.release(); knc_node.release();
         perm.release(); stage_x.release(); stage_v.release();
         knc_mesh.release(); lconn.release(); lptr.release(); lidx.release(); fixed.release(); rest.release();
         x.release(); v.release(); bvec.release(); y.release(); part64.release(); cpart.release(); tpart.release();
@@ -810,12 +810,15 @@ int fem_batch_finalize(fem_batch b)
     b->inv_h.assign(b->Ntot, 0);
     for (uint64_t i = 0; i < b->Ntot; i++) b->inv_h[perm_h[i]] = (uint32_t)i;
     // node -> overflow slots, tile order
-    std::vector<uint32_t> ov_ptr(b->Ntot + 1, 0), ov_slot(ov_node.size());
+    // a node's overflow entries get consecutive slots Ntot + [ov_ptr[n],
+    // ov_ptr[n+1]), in tile order
+    if (b->nslots >= (1ull << 32)) return batch_fail(FEM_E_ARG, "batch too large for partial slots");
+    std::vector<uint32_t> ov_ptr(b->Ntot + 1, 0), ov_map(ov_node.size());
     for (uint32_t g : ov_node) ov_ptr[g + 1]++;
     for (uint64_t n = 0; n < b->Ntot; n++) ov_ptr[n + 1] += ov_ptr[n];
     {
         std::vector<uint32_t> fill(ov_ptr.begin(), ov_ptr.end() - 1);
-        for (size_t kk = 0; kk < ov_node.size(); kk++) ov_slot[fill[ov_node[kk]]++] = (uint32_t)kk;
+        for (size_t kk = 0; kk < ov_node.size(); kk++) ov_map[kk] = (uint32_t)(b->Ntot + fill[ov_node[kk]]++);
     }
     // SoA transposes
     const size_t T = b->Ttot;
@@ -832,7 +835,7 @@ int fem_batch_finalize(fem_batch b)
         blob_off16_h.resize(b->ntiles);
         for (uint32_t t = 0; t < b->ntiles; t++) {
             blob_off16_h[t] = (uint32_t)(total / 16);
-            total += blob_bytes(tiles[t].ne, tiles[t].nn);
+            total += blob_bytes(tiles[t].ne, tiles[t].nn, tiles[t].nown);
         }
         if (total / 16 >= (1ull << 32)) return batch_fail(FEM_E_ARG, "batch too large for tile blobs");
         blob_h.assign(total, 0);
@@ -858,12 +861,11 @@ int fem_batch_finalize(fem_batch b)
                 const uint16_t v = lidx[tm.c0 + j];  // (element << 2 | slot) -> slot * ne4 + element
                 li[j] = (uint16_t)((v & 3u) * ne4 + (v >> 2));
             }
-            uint32_t* slots = reinterpret_cast<uint32_t*>(base + blob_slots_off(tm.ne, tm.nn));
-            slots[0] = tm.own0;
-            slots[1] = tm.ov0;
-            slots[2] = tm.nown;
-            std::memcpy(&slots[3], &mcs[tm.mesh].fK_f, 4);
-            std::memcpy(&slots[4], &mcs[tm.mesh].mfm_f, 4);
+            uint32_t* hdr = reinterpret_cast<uint32_t*>(base + blob_hdr_off(tm.ne, tm.nn));
+            hdr[0] = tm.own0;
+            std::memcpy(&hdr[1], &mcs[tm.mesh].fK_f, 4);
+            std::memcpy(&hdr[2], &mcs[tm.mesh].mfm_f, 4);
+            for (uint32_t i = tm.nown; i < tm.nn; i++) hdr[3 + i - tm.nown] = ov_map[tm.ov0 + i - tm.nown];
         }
     }
     std::vector<double> Rinit(9 * T, 0.0);
@@ -900,7 +902,7 @@ int fem_batch_finalize(fem_batch b)
     BCKC(b->tile_nodes.alloc(tile_nodes.size()));
     BCKC(b->lptr0.alloc(b->ntiles));
     BCKC(b->ov_ptr.alloc(b->Ntot + 1));
-    BCKC(b->ov_slot.alloc(ov_slot.size()));
+    BCKC(b->ov_map.alloc(ov_map.size()));
     BCKC(b->perm.alloc(b->Ntot));
     BCKC(b->knc_node.alloc(b->K));
     BCKC(b->knc_mesh.alloc(b->K));
@@ -981,7 +983,7 @@ int fem_batch_finalize(fem_batch b)
     BCKC(b->tile_nodes.upload(tile_nodes, s));
     BCKC(b->lptr0.upload(lptr0, s));
     BCKC(b->ov_ptr.upload(ov_ptr, s));
-    BCKC(b->ov_slot.upload(ov_slot, s));
+    BCKC(b->ov_map.upload(ov_map, s));
     BCKC(b->perm.upload(perm_h, s));
     BCKC(b->knc_node.upload(knc_node, s));
     BCKC(b->knc_mesh.upload(knc_mesh, s));
@@ -1003,7 +1005,7 @@ int fem_batch_finalize(fem_batch b)
     b->device_bytes = b->tiles.bytes() + b->chunks.bytes() + b->mc.bytes() + b->st.bytes() + b->active.bytes() +
                       b->gtets.bytes() + b->Dinv_s.bytes() + b->mat_s.bytes() + b->R_s.bytes() +
                       b->Dinv64.bytes() + b->vol.bytes() + b->detF.bytes() + b->tile_nodes.bytes() +
-                      b->lptr0.bytes() + b->ov_ptr.bytes() + b->ov_slot.bytes() + b->knc_node.bytes() +
+                      b->lptr0.bytes() + b->ov_ptr.bytes() + b->ov_map.bytes() + b->knc_node.bytes() +
                       b->perm.bytes() +
                       b->knc_mesh.bytes() + b->knc_target.bytes() + b->lconn.bytes() + b->lptr.bytes() +
                       b->lidx.bytes() + b->fixed.bytes() + b->rest.bytes() + b->x.bytes() + b->v.bytes() +

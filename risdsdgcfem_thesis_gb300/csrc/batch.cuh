@@ -7,9 +7,9 @@
 // to one mesh.
 //
 // Nodes are numbered inside the batch in the order they first appear in their
-// mesh's tile sequence (the API permutes states to and from the caller's
-// order). A tile's new nodes -- the nodes it owns -- therefore have
-// consecutive ids, and its local node list puts them first.
+// mesh's tile sequence, by degree within a tile (the API permutes states to
+// and from the caller's order). A tile's new nodes -- the nodes it owns --
+// therefore have consecutive ids, and its local node list puts them first.
 //
 //   per tile     TileMeta: element range, its local node list (tile_nodes,
 //                global ids, owned nodes first), its local connectivity
@@ -21,9 +21,9 @@
 //   per node     x, v, b, y (FP64); r, d, q (S); rest (FP64); fixed flag
 //   partials     one per (tile, local node): the owner tile's at part[node]
 //                (node order, so the node pass reads it coalesced), a shared
-//                node's other tiles' in overflow slots part[Ntot + k]; per
-//                node a CSR (ov_ptr/ov_slot) over its overflow slots, in
-//                tile order
+//                node's other tiles' in overflow slots part[Ntot + j], j in
+//                [ov_ptr[n], ov_ptr[n+1]) (contiguous per node, tile order);
+//                ov_map gives the slot of each (tile, shared local node)
 //
 // All sums have a fixed order (a node's partials: owner first, then tile
 // order), so a solid gives the same bits alone and in any batch.
@@ -46,8 +46,9 @@ constexpr int kNodeThreads = 256;  // threads per node-kernel block
 // components 4g..4g+3 as float4[ne4], group 5 components 20, 21 as
 // float2[ne4] (one 16- or 8-byte load per group and element, consecutive
 // elements in consecutive words); then uint16 lptr[nn+1], uint16 lidx[4 ne],
-// uint32 {own0, ov0, nown} (the tile's partial slots) and float {fK, m fM}
-// (its mesh's FP32 factors).
+// and, 4-aligned, the header {uint32 own0, float fK, float m fM} (the partial
+// slot of the first owned node, the mesh's FP32 factors) and uint32
+// ovslot[nn - nown] (the partial slots of the shared local nodes).
 __host__ __device__ inline uint32_t blob_ne4(uint32_t ne) { return (ne + 3u) & ~3u; }
 // Byte offset of component c of element i.
 __host__ __device__ inline uint32_t blob_comp_off(uint32_t c, uint32_t i, uint32_t ne4)
@@ -55,13 +56,13 @@ __host__ __device__ inline uint32_t blob_comp_off(uint32_t c, uint32_t i, uint32
     return c < 20u ? 16u * ((c >> 2) * ne4 + i) + 4u * (c & 3u) : 80u * ne4 + 8u * i + 4u * (c - 20u);
 }
 __host__ __device__ inline uint32_t blob_lptr_off(uint32_t ne) { return 88u * blob_ne4(ne); }
-__host__ __device__ inline uint32_t blob_slots_off(uint32_t ne, uint32_t nn)
+__host__ __device__ inline uint32_t blob_hdr_off(uint32_t ne, uint32_t nn)
 {
     return (blob_lptr_off(ne) + 2u * (nn + 1u) + 8u * ne + 3u) & ~3u;
 }
-__host__ __device__ inline uint32_t blob_bytes(uint32_t ne, uint32_t nn)
+__host__ __device__ inline uint32_t blob_bytes(uint32_t ne, uint32_t nn, uint32_t nown)
 {
-    return (blob_slots_off(ne, nn) + 20u + 15u) & ~15u;
+    return (blob_hdr_off(ne, nn) + 12u + 4u * (nn - nown) + 15u) & ~15u;
 }
 
 struct TileMeta {
@@ -71,14 +72,18 @@ struct TileMeta {
     uint32_t c0;      // first entry in lidx
     uint16_t ne, nn;  // elements, local nodes
     uint32_t own0;    // global id of the first owned node (local nodes [0, nown))
-    uint32_t ov0;     // first overflow slot of the shared local nodes [nown, nn)
+    uint32_t ov0;     // first entry in ov_map of the shared local nodes [nown, nn)
     uint16_t nown, pad;
 };
 
-// Partial slot of local node i of a tile.
-__host__ __device__ inline size_t tile_slot(uint32_t Ntot, uint32_t own0, uint32_t ov0, uint32_t nown, uint32_t i)
+// Partial slot of local node i of a tile: owned nodes write theirs in node
+// order (slot = batch node id), shared nodes the overflow slot ov_map gives
+// (Ntot + the entry's position in its node's overflow list, so each node's
+// overflow partials are contiguous).
+__host__ __device__ inline size_t tile_slot(const uint32_t* ov_map, uint32_t own0, uint32_t ov0, uint32_t nown,
+                                            uint32_t i)
 {
-    return i < nown ? (size_t)own0 + i : (size_t)Ntot + ov0 + (i - nown);
+    return i < nown ? (size_t)own0 + i : (size_t)ov_map[ov0 + (i - nown)];
 }
 
 struct ChunkMeta {
@@ -127,8 +132,8 @@ struct BatchView {
     const uint16_t* lidx;          // [4 Ttot] (element-in-tile << 2 | slot), tile-relative
     const uint32_t* lptr0;         // [ntiles] base of each tile's lptr block
     // node data
-    const uint32_t* ov_ptr;        // [Ntot+1] per node: its overflow slots
-    const uint32_t* ov_slot;       // [overflow slots] in tile order
+    const uint32_t* ov_ptr;        // [Ntot+1] per node: its overflow slots Ntot + [ov_ptr[n], ov_ptr[n+1])
+    const uint32_t* ov_map;        // [overflow entries] in tile order: the entry's partial slot
     const uint8_t* fixed;          // [Ntot]
     const double* rest;            // [3 Ntot]
     S* ydelta;                     // [3 Ntot] mixed: FP32 sum of this step's alpha d; null on FP64

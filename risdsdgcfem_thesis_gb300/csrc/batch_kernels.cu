@@ -196,7 +196,7 @@ __global__ void __launch_bounds__(256) k_tile_spmv(BatchView<S> b, const S* __re
             a1 += so[(3 * sl + 1) * kTileElems + el];
             a2 += so[(3 * sl + 2) * kTileElems + el];
         }
-        const size_t o = 3 * tile_slot(b.Ntot, tm.own0, tm.ov0, tm.nown, i);
+        const size_t o = 3 * tile_slot(b.ov_map, tm.own0, tm.ov0, tm.nown, i);
         part[o] = a0;
         part[o + 1] = a1;
         part[o + 2] = a2;
@@ -287,7 +287,7 @@ __global__ void __launch_bounds__(256) k_tile_spmv_y64(BatchView<S> b, const dou
                 a1 = a1 + so[(3 * sl + 1) * kTileElems + el];
                 a2 = a2 + so[(3 * sl + 2) * kTileElems + el];
             }
-            const size_t o = 3 * tile_slot(b.Ntot, tm.own0, tm.ov0, tm.nown, i);
+            const size_t o = 3 * tile_slot(b.ov_map, tm.own0, tm.ov0, tm.nown, i);
             part64[o] = y64_get(a0);
             part64[o + 1] = y64_get(a1);
             part64[o + 2] = y64_get(a2);
@@ -373,7 +373,7 @@ __global__ void __launch_bounds__(256) k_tile_force(BatchView<S> b, const double
                     a1 += so[(3 * sl + 1) * kTileElems + el];
                     a2 += so[(3 * sl + 2) * kTileElems + el];
                 }
-                const size_t o = 3 * tile_slot(b.Ntot, tm.own0, tm.ov0, tm.nown, i);
+                const size_t o = 3 * tile_slot(b.ov_map, tm.own0, tm.ov0, tm.nown, i);
                 part64[o] = a0;
                 part64[o + 1] = a1;
                 part64[o + 2] = a2;
@@ -417,7 +417,7 @@ __global__ void k_tile_potential(BatchView<S> b, const double* __restrict__ x, d
 // kNodeThreads threads striding it)
 
 // Sum of a node's partials: its owner tile's (node order) first, then its
-// overflow slots in tile order.
+// overflow slots (contiguous, in tile order).
 template <typename S, typename P>
 __device__ __forceinline__ void sum_parts(const BatchView<S>& b, const P* __restrict__ part, size_t n, double& a0,
                                           double& a1, double& a2)
@@ -427,7 +427,7 @@ __device__ __forceinline__ void sum_parts(const BatchView<S>& b, const P* __rest
     a2 = (double)part[3 * n + 2];
     const uint32_t j1 = b.ov_ptr[n + 1];
     for (uint32_t j = b.ov_ptr[n]; j < j1; j++) {
-        const size_t o = 3 * ((size_t)b.Ntot + b.ov_slot[j]);
+        const size_t o = 3 * ((size_t)b.Ntot + j);
         a0 += (double)part[o];
         a1 += (double)part[o + 1];
         a2 += (double)part[o + 2];
@@ -656,7 +656,7 @@ __global__ void k_node_q(BatchView<S> b, const S* __restrict__ part, S* __restri
                 S s0 = part[3 * n], s1 = part[3 * n + 1], s2 = part[3 * n + 2];
                 const uint32_t j1 = b.ov_ptr[n + 1];
                 for (uint32_t j = b.ov_ptr[n]; j < j1; j++) {
-                    const size_t o = 3 * ((size_t)b.Ntot + b.ov_slot[j]);
+                    const size_t o = 3 * ((size_t)b.Ntot + j);
                     s0 += part[o];
                     s1 += part[o + 1];
                     s2 += part[o + 2];

@@ -36,9 +36,10 @@
 //                0-19), float2 [ne4] (components 20, 21)
 //   88 ne4       uint16 lptr[nn+1]      tile-local CSR offsets
 //   + 2(nn+1)    uint16 lidx[4 ne]      slot * ne4 + element, element order
-//   (4-aligned)  uint32 own0, ov0, nown   partial slots: local node i < nown -> part[own0 + i],
-//                                         else part[Ntot + ov0 + i - nown]
-//   + 12         float fK, m fM         the mesh's FP32 factors
+//   (4-aligned)  uint32 own0; float fK, m fM   partial slot of the first owned
+//                                         node (local node i < nown -> part[own0 + i]);
+//                                         the mesh's FP32 factors
+//   + 12         uint32 ovslot[nn - nown] partial slots of the shared local nodes
 //   size rounded up to 16. The batch node ids of the tile's local nodes
 //   (its owned nodes first) are read from the batch's tile node list, ahead
 //   of the blob.
@@ -208,12 +209,12 @@ __device__ __forceinline__ void finish_stats_t(StepScalars& s)
 
 }  // namespace
 
-constexpr uint32_t kStageBytes = 25216;  // >= blob_bytes(256, 256) = 25120, multiple of 128
-static_assert(kStageBytes >= 25120, "stage must hold the largest tile blob");
+constexpr uint32_t kStageBytes = 26240;  // >= blob_bytes(256, 256, 0) = 26128, multiple of 128
+static_assert(kStageBytes >= 26128, "stage must hold the largest tile blob");
 
 // Shared memory: two blob stages (a tile's element outputs overwrite its
 // element data once every element has read it), the staged direction
-// sd4[256], two mbarriers and the warps' shares: 54.5 KB, four resident
+// sd4[256], two mbarriers and the warps' shares: 56.7 KB, four resident
 // blocks per SM.
 constexpr uint32_t kPipeSmem = 2 * kStageBytes + 16u * kTileNodes + 16u + 8u * 8u;
 
@@ -308,7 +309,7 @@ __global__ void __launch_bounds__(256, 4) k_tile_spmv_pipe(BatchView<float> b, c
     int s = 0;
     bool failed = false;
     auto issue = [&](const TileLook& L, int st) {
-        const uint32_t bytes = blob_bytes(look_ne(L), look_nn(L));
+        const uint32_t bytes = blob_bytes(look_ne(L), look_nn(L), look_nown(L));
         mbar_expect_tx(&bar[st], bytes);
         bulk_copy_g2s(smem + st * kStageBytes, b.blob + 16ull * L.boff, bytes, &bar[st]);
     };
@@ -362,7 +363,8 @@ __global__ void __launch_bounds__(256, 4) k_tile_spmv_pipe(BatchView<float> b, c
         const bool work = live && !failed;
         const unsigned char* stage = smem + s * kStageBytes;
         const uint32_t ne4 = blob_ne4(ne);
-        const float* fac = reinterpret_cast<const float*>(stage + blob_slots_off(ne, nn)) + 3;  // fK, m fM
+        const uint32_t* hdr = reinterpret_cast<const uint32_t*>(stage + blob_hdr_off(ne, nn));
+        const float* fac = reinterpret_cast<const float*>(hdr + 1);  // fK, m fM
         float share = 0.f;  // this thread's part of the tile's d^T A d
         if (work) share = fac[1] * dd;  // the nodes the tile owns
         float out[12];
@@ -417,7 +419,6 @@ __global__ void __launch_bounds__(256, 4) k_tile_spmv_pipe(BatchView<float> b, c
             if (tid < nn) {
                 const uint16_t* lp = reinterpret_cast<const uint16_t*>(stage + blob_lptr_off(ne));
                 const uint16_t* li = lp + (nn + 1);
-                const uint32_t* slots = reinterpret_cast<const uint32_t*>(stage + blob_slots_off(ne, nn));
                 float a0 = 0.f, a1 = 0.f, a2 = 0.f;
                 for (int j = lp[tid]; j < lp[tid + 1]; j++) {
                     const float4 v = so4[li[j]];
@@ -425,7 +426,8 @@ __global__ void __launch_bounds__(256, 4) k_tile_spmv_pipe(BatchView<float> b, c
                     a1 += v.y;
                     a2 += v.z;
                 }
-                const size_t o = 3 * tile_slot(b.Ntot, slots[0], slots[1], look_nown(cur), tid);
+                const uint32_t nown = look_nown(cur);
+                const size_t o = 3 * (size_t)(tid < nown ? hdr[0] + tid : hdr[3 + tid - nown]);
                 part[o] = a0;
                 part[o + 1] = a1;
                 part[o + 2] = a2;
@@ -501,10 +503,11 @@ __global__ void __launch_bounds__(256) k_node_update_fused(BatchView<float> b, c
             const float d1 = __fmaf_rn(beta, d[i + 1], r[i + 1]);
             const float d2 = __fmaf_rn(beta, d[i + 2], r[i + 2]);
             // the owner tile's partial (node order), then the overflow slots
+            // (contiguous, tile order)
             float s0 = part[i], s1 = part[i + 1], s2 = part[i + 2];
             const uint32_t j0 = b.ov_ptr[n], j1 = b.ov_ptr[n + 1];
             for (uint32_t j = j0; j < j1; j++) {
-                const size_t o = 3 * ((size_t)b.Ntot + b.ov_slot[j]);
+                const size_t o = 3 * ((size_t)b.Ntot + j);
                 s0 += part[o];
                 s1 += part[o + 1];
                 s2 += part[o + 2];
@@ -515,7 +518,7 @@ __global__ void __launch_bounds__(256) k_node_update_fused(BatchView<float> b, c
             if (refresh) {
                 double t0 = part64[i], t1 = part64[i + 1], t2 = part64[i + 2];
                 for (uint32_t j = j0; j < j1; j++) {
-                    const size_t o = 3 * ((size_t)b.Ntot + b.ov_slot[j]);
+                    const size_t o = 3 * ((size_t)b.Ntot + j);
                     t0 += part64[o];
                     t1 += part64[o + 1];
                     t2 += part64[o + 2];
