@@ -36,6 +36,8 @@ struct StepScalars {
     double delta_refresh;   // mixed: |r|^2 right after the last FP64 residual
     uint32_t k_refresh;
     uint32_t confirm;       // mixed: this iteration only measures the FP64 residual (exit test)
+    float alpha_f;          // mixed: this iteration's alpha in FP32 (0 on a confirm iteration)
+    uint32_t brk;           // mixed: this iteration breaks down (|d.q| < abs^2) and leaves the loop
     unsigned long long total_iters;
 };
 

@@ -1,4 +1,4 @@
-// tile_pipe.cu -- one CG iteration of the mixed-precision path in two kernels
+// tile_pipe.cu -- one CG iteration of the mixed-precision path in three kernels
 // (Saphyre2 ns/ILSS_CG.h:90-144, every running mesh of the batch in
 // lock-step).
 //
@@ -18,13 +18,14 @@
 // its owner writes its partial in node order (the node pass reads it
 // coalesced; shared nodes' other partials go to overflow slots).
 //
-// k_node_update_fused: every block first sums its mesh's tile shares (fixed
-// order, so every block of the mesh gets the same bits) and forms alpha, or
-// leaves the mesh on breakdown (ILSS_CG.h:97). Then per node: d = S(r + beta
-// d) (the values the tiles staged), q = S(fK sum(partials) + m fM d), y +=
-// alpha d (into the FP32 increment accumulator), r -= alpha q (on refresh
-// iterations r is first recomputed as S(b - A y) from the FP64 product of
-// y), |r|^2. The last block of a mesh forms beta and the loop test
+// k_mesh_alpha: one warp per running mesh sums its tiles' shares (fixed
+// order) and forms alpha, or the breakdown flag (ILSS_CG.h:97).
+//
+// k_node_update_fused: per node of the running meshes: d = S(r + beta d) (the
+// values the tiles staged), q = S(fK sum(partials) + m fM d), y += alpha d
+// (into the FP32 increment accumulator), r -= alpha q (on refresh iterations
+// r is first recomputed as S(b - A y) from the product of y), |r|^2; a mesh
+// that breaks down leaves its loop before the update. The last block of a mesh forms beta and the loop test
 // (ILSS_CG.h:100-144), the last block of the grid sets the CUDA-graph while
 // condition and the refresh flag.
 //
@@ -459,8 +460,34 @@ __global__ void __launch_bounds__(256, 4) k_tile_spmv_pipe(BatchView<float> b, c
     }
 }
 
+// Per running mesh: d^T A d from its tiles' shares (fixed order), alpha and
+// the breakdown test (ILSS_CG.h:91-97), once for the node pass's blocks of
+// the mesh. One warp per mesh.
+__global__ void __launch_bounds__(256) k_mesh_alpha(BatchView<float> b, const float2* __restrict__ tshare)
+{
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t m = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; m < b.M; m += nw) {
+        StepScalars& st = b.st[m];
+        if (st.done) continue;
+        const MeshConsts& c = b.mc[m];
+        F2 a = {0.f, 0.f};
+        for (uint32_t k = lane; k < c.ntiles; k += 32u) {
+            const float2 w = __ldcg(tshare + c.tile0 + k);
+            a = f2_add(a, F2{w.x, w.y});
+        }
+        a = warp_sum_f2(a);
+        if (lane == 0) {
+            const double dq = (double)a.hi + (double)a.lo;
+            const bool confirm = st.confirm != 0;  // measure the FP64 residual only, no CG update
+            st.dot_dq = dq;
+            st.brk = (!confirm && ::fabs(dq) < st.abs_eps_sq) ? 1u : 0u;  // leave before the update
+            st.alpha_f = confirm ? 0.f : (float)(st.delta_new / dq);
+        }
+    }
+}
+
 __global__ void __launch_bounds__(256) k_node_update_fused(BatchView<float> b, const float* __restrict__ part,
-                                                           const float2* __restrict__ tshare,
                                                            const double* __restrict__ part64,
                                                            const double* __restrict__ bv,
                                                            double* __restrict__ y, float* __restrict__ r,
@@ -469,36 +496,25 @@ __global__ void __launch_bounds__(256) k_node_update_fused(BatchView<float> b, c
 {
     __shared__ float2 sh[32];
     __shared__ unsigned s_last;
-    __shared__ float s_alpha;
-    __shared__ int s_brk;
-    __shared__ double s_dq;
     const uint32_t n_act = *(volatile const uint32_t*)(b.act_count + 1);
     for (uint32_t ia = blockIdx.x; ia < n_act; ia += gridDim.x) {
         const uint32_t ci = b.act_chunks[ia];
         const ChunkMeta ch = b.chunks[ci];
-        if (b.st[ch.mesh].done) continue;  // left its loop; the list is rebuilt lazily
-        const MeshConsts& c = b.mc[ch.mesh];
         const StepScalars& sm = b.st[ch.mesh];
-        // d^T A d of the mesh from its tiles' shares; every block of the mesh
-        // forms the same value (same partials, same order)
-        const F2 dq2 = sum_partials_f2(tshare + c.tile0, c.ntiles, sh);
-        const bool confirm = sm.confirm != 0;  // measure the FP64 residual only, no CG update
-        if (threadIdx.x == 0) {
-            const double dq = (double)dq2.hi + (double)dq2.lo;
-            s_dq = dq;
-            s_brk = !confirm && ::fabs(dq) < sm.abs_eps_sq;  // breakdown: leave before the update (ILSS_CG.h:97)
-            s_alpha = confirm ? 0.f : (float)(sm.delta_new / dq);
-        }
-        __syncthreads();
-        const bool brk = s_brk != 0;
+        if (sm.done) continue;  // left its loop; the list is rebuilt lazily
+        const MeshConsts& c = b.mc[ch.mesh];
+        const bool brk = sm.brk != 0;
+        const bool confirm = sm.confirm != 0;
         const bool refresh = sm.refresh_next != 0;
         const float beta = sm.beta_f;
-        const float alpha_s = s_alpha, na = -alpha_s;
+        const float alpha_s = sm.alpha_f, na = -alpha_s;
         const float fK = c.fK_f, mfm = c.mfm_f;
         float acc = 0.f;
         for (size_t n = ch.n0 + threadIdx.x; !brk && n < ch.n1; n += blockDim.x) {
             const size_t i = 3 * n;
-            if (b.fixed[n]) continue;  // d, r stay zero and y unchanged on constrained rows
+            // every load is issued before the constraint flag is known; a
+            // constrained row keeps d, r zero and y unchanged
+            const bool fixed = b.fixed[n] != 0;
             const float d0 = __fmaf_rn(beta, d[i], r[i]);
             const float d1 = __fmaf_rn(beta, d[i + 1], r[i + 1]);
             const float d2 = __fmaf_rn(beta, d[i + 2], r[i + 2]);
@@ -506,15 +522,16 @@ __global__ void __launch_bounds__(256) k_node_update_fused(BatchView<float> b, c
             // (contiguous, tile order)
             float s0 = part[i], s1 = part[i + 1], s2 = part[i + 2];
             const uint32_t j0 = b.ov_ptr[n], j1 = b.ov_ptr[n + 1];
+            float r0 = r[i], r1 = r[i + 1], r2 = r[i + 2];
+            float e0 = b.ydelta[i], e1 = b.ydelta[i + 1], e2 = b.ydelta[i + 2];
             for (uint32_t j = j0; j < j1; j++) {
                 const size_t o = 3 * ((size_t)b.Ntot + j);
                 s0 += part[o];
                 s1 += part[o + 1];
                 s2 += part[o + 2];
             }
+            if (fixed) continue;
             const float q0 = fK * s0 + mfm * d0, q1 = fK * s1 + mfm * d1, q2 = fK * s2 + mfm * d2;
-            float r0 = r[i], r1 = r[i + 1], r2 = r[i + 2];
-            float e0 = b.ydelta[i], e1 = b.ydelta[i + 1], e2 = b.ydelta[i + 2];
             if (refresh) {
                 double t0 = part64[i], t1 = part64[i + 1], t2 = part64[i + 2];
                 for (uint32_t j = j0; j < j1; j++) {
@@ -557,7 +574,6 @@ __global__ void __launch_bounds__(256) k_node_update_fused(BatchView<float> b, c
             const F2 tot = sum_partials_f2(cshare + c.chunk0, c.nchunks, sh);
             if (threadIdx.x == 0) {
                 StepScalars& st = b.st[ch.mesh];
-                st.dot_dq = s_dq;
                 if (confirm) {
                     // the FP64 residual of the current iterate decides: leave,
                     // or go on from it -- with the recurrence's direction
@@ -590,7 +606,7 @@ __global__ void __launch_bounds__(256) k_node_update_fused(BatchView<float> b, c
                     finish_stats_t(st);
                 } else {
                     const double total = (double)tot.hi + (double)tot.lo;
-                    st.alpha = st.delta_new / s_dq;
+                    st.alpha = st.delta_new / st.dot_dq;
                     st.delta_old = st.delta_new;
                     st.delta_new = total;
                     st.beta = total / st.delta_old;
@@ -713,8 +729,12 @@ void launch_node_update_fused(const BatchView<float>& b, const float* part, cons
 {
     const uint32_t g = (uint32_t)node_grid();
     const uint32_t grid = b.nchunks < g ? (b.nchunks ? b.nchunks : 1) : g;
+    prof_begin("mesh_alpha", s);
+    k_mesh_alpha<<<(b.M * 32u + kNodeThreads - 1) / kNodeThreads, kNodeThreads, 0, s>>>(b, tshare);
+    prof_end("mesh_alpha", s);
+    launch_counter()++;
     prof_begin("node_update_mixed", s);
-    k_node_update_fused<<<grid, kNodeThreads, 0, s>>>(b, part, tshare, part64, bv, y, r, d, cshare, ls);
+    k_node_update_fused<<<grid, kNodeThreads, 0, s>>>(b, part, part64, bv, y, r, d, cshare, ls);
     prof_end("node_update_mixed", s);
     launch_counter()++;
 }
