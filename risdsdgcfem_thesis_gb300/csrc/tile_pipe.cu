@@ -524,7 +524,26 @@ __global__ void __launch_bounds__(256) k_node_update_fused(BatchView<float> b, c
             const uint32_t j0 = b.ov_ptr[n], j1 = b.ov_ptr[n + 1];
             float r0 = r[i], r1 = r[i + 1], r2 = r[i + 2];
             float e0 = b.ydelta[i], e1 = b.ydelta[i + 1], e2 = b.ydelta[i + 2];
-            for (uint32_t j = j0; j < j1; j++) {
+            // the first four overflow partials are loaded together, then
+            // added in slot order (the rare rest one by one)
+            float p[4][3];
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                const bool in = j0 + k < j1;
+                const size_t o = 3 * ((size_t)b.Ntot + (in ? j0 + k : 0u));
+                p[k][0] = in ? part[o] : 0.f;
+                p[k][1] = in ? part[o + 1] : 0.f;
+                p[k][2] = in ? part[o + 2] : 0.f;
+            }
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                if (j0 + k < j1) {
+                    s0 += p[k][0];
+                    s1 += p[k][1];
+                    s2 += p[k][2];
+                }
+            }
+            for (uint32_t j = j0 + 4; j < j1; j++) {
                 const size_t o = 3 * ((size_t)b.Ntot + j);
                 s0 += part[o];
                 s1 += part[o + 1];
