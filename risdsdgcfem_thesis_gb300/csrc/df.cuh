@@ -24,6 +24,11 @@ namespace femgb {
 
 struct DF {
     float hi, lo;
+    DF() = default;
+    __host__ __device__ constexpr DF(float h, float l) : hi(h), lo(l) {}
+    // nearest double-float of an FP64 value (exact to 2^-48 relative)
+    // (conversions to float round to nearest)
+    __host__ __device__ explicit DF(double v) : hi((float)v), lo((float)(v - (double)(float)v)) {}
 };
 
 __device__ __forceinline__ DF df_two_sum(float a, float b)
@@ -47,12 +52,7 @@ __device__ __forceinline__ DF df_two_prod(float a, float b)
     return {p, __fmaf_rn(a, b, -p)};
 }
 
-// Nearest double-float of an FP64 value (exact to 2^-48 relative).
-__device__ __forceinline__ DF df_from_double(double v)
-{
-    const float hi = __double2float_rn(v);
-    return {hi, __double2float_rn(v - (double)hi)};
-}
+__device__ __forceinline__ DF df_from_double(double v) { return DF(v); }
 
 __device__ __forceinline__ double df_to_double(DF a) { return (double)a.hi + (double)a.lo; }
 
@@ -80,5 +80,36 @@ __device__ __forceinline__ DF operator*(DF x, DF y)
     const float t = __fmul_rn(x.hi, y.lo);
     return df_fast_two_sum(c.hi, __fadd_rn(c.lo, __fmaf_rn(x.lo, y.hi, t)));
 }
+
+__device__ __forceinline__ DF& operator+=(DF& x, DF y) { return x = x + y; }
+__device__ __forceinline__ DF& operator-=(DF& x, DF y) { return x = x - y; }
+
+// Quotient (DWDivDW2 of the paper above): the FP32 quotient of the leading
+// parts, corrected by the remainder x - y t_h.
+__device__ __forceinline__ DF operator/(DF x, DF y)
+{
+    const float th = __fdiv_rn(x.hi, y.hi);
+    const DF r = y * th;
+    const float d = __fadd_rn(__fsub_rn(x.hi, r.hi), __fsub_rn(x.lo, r.lo));
+    return df_fast_two_sum(th, __fdiv_rn(d, y.hi));
+}
+
+// Square root: the FP32 root s of the leading part, corrected by
+// (x - s^2) / (2 s) (one Newton step in double-float accuracy).
+__device__ __forceinline__ DF df_sqrt(DF x)
+{
+    if (!(x.hi > 0.f)) return DF(__fsqrt_rn(x.hi), 0.f);  // 0, or NaN below zero
+    const float sr = __fsqrt_rn(x.hi);
+    const DF s2 = df_two_prod(sr, sr);
+    const float rem = __fadd_rn(__fsub_rn(__fsub_rn(x.hi, s2.hi), s2.lo), x.lo);
+    return df_fast_two_sum(sr, __fdiv_rn(rem, __fmul_rn(2.f, sr)));
+}
+
+__device__ __forceinline__ DF df_abs(DF x) { return x.hi < 0.f ? -x : x; }
+
+// Order of normalised double-floats (the leading parts decide unless equal).
+__device__ __forceinline__ bool operator<(DF a, DF b) { return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo); }
+__device__ __forceinline__ bool operator>(DF a, DF b) { return b < a; }
+__device__ __forceinline__ bool operator<=(DF a, DF b) { return !(b < a) && a.hi == a.hi && b.hi == b.hi; }
 
 }  // namespace femgb

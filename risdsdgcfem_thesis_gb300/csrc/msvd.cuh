@@ -18,25 +18,92 @@
 //  * Sqrt/Sin/Cos/ATan2 are evaluated at the precision of T. (The reference's
 //    FP64 build rounds them through float, which makes R NaN near F = I;
 //    the restatement and this kernel use double there.)
+//
+// T is double (the FP64 path, bit-exact), float (the optional FP32 rotation
+// of the mixed path) or DF, a double-float (the mixed path's default: about
+// 48 bits on the FP32 pipe; GB300's FP64 rate made the FP64 rotation, with
+// its FP64 sin/cos/atan2, a tenth of the mixed step).
 #pragma once
 #include <cuda_runtime.h>
 
+#include "df.cuh"
+
 namespace femgb {
 
+// Per-type math: sqrt, abs, and eig_cos_sin(m, p, sqrt_p, q, c, s), the
+// cosine and sine of phi = atan2(sqrt(max(p^3 - q^2, 0)), q) / 3
+// (Fast_Eigenvalues, PhysBAM.h:169-173).
 template <typename T> struct MathOf;
 template <> struct MathOf<double> {
     static __device__ __forceinline__ double sqrt_(double x) { return ::sqrt(x); }
-    static __device__ __forceinline__ double sin_(double x) { return ::sin(x); }
-    static __device__ __forceinline__ double cos_(double x) { return ::cos(x); }
-    static __device__ __forceinline__ double atan2_(double y, double x) { return ::atan2(y, x); }
     static __device__ __forceinline__ double abs_(double x) { return ::fabs(x); }
+    static __device__ __forceinline__ void eig_cos_sin(double, double p, double, double q, double& c, double& s)
+    {
+        const double disc = p * p * p - q * q;
+        const double disc_c = (0.0 > disc) ? 0.0 : disc;
+        const double phi = (1.0 / 3.0) * ::atan2(::sqrt(disc_c), q);
+        c = ::cos(phi);
+        s = ::sin(phi);
+    }
 };
 template <> struct MathOf<float> {
     static __device__ __forceinline__ float sqrt_(float x) { return ::sqrtf(x); }
-    static __device__ __forceinline__ float sin_(float x) { return ::sinf(x); }
-    static __device__ __forceinline__ float cos_(float x) { return ::cosf(x); }
-    static __device__ __forceinline__ float atan2_(float y, float x) { return ::atan2f(y, x); }
     static __device__ __forceinline__ float abs_(float x) { return ::fabsf(x); }
+    static __device__ __forceinline__ void eig_cos_sin(float, float p, float, float q, float& c, float& s)
+    {
+        const float disc = p * p * p - q * q;
+        const float disc_c = (0.f > disc) ? 0.f : disc;
+        const float phi = (1.f / 3.f) * ::atan2f(::sqrtf(disc_c), q);
+        c = ::cosf(phi);
+        s = ::sinf(phi);
+    }
+};
+template <> struct MathOf<DF> {
+    static __device__ __forceinline__ DF sqrt_(DF x) { return df_sqrt(x); }
+    static __device__ __forceinline__ DF abs_(DF x) { return df_abs(x); }
+    // cos(theta) = q / p^(3/2) and sin(theta) = sqrt(1 - cos^2) (clamped):
+    // the same angle as above in a form free of p^3 and q^2, which scale
+    // with the sixth power of the deviation from isotropy and would leave
+    // FP32's exponent range. theta lies in [0, pi], phi = theta / 3 in
+    // [0, pi/3]. c = cos(phi) solves 4c^3 - 3c = cos(theta), s = sin(phi)
+    // solves 3s - 4s^3 = sin(theta) (triple-angle identities): Newton steps
+    // from the FP32 values, with the derivative's reciprocal at the FP32
+    // guess (each step gains about seven digits). Where a derivative
+    // vanishes (c = 1/2, s = 1/2) the other of the pair gives it through
+    // c^2 + s^2 = 1, away from cancellation.
+    // A nearly isotropic F^T F (sqrt(p) below 1e-7 m) returns NaN: the
+    // later cofactor products there approach FP32's underflow, and the
+    // caller re-solves such an F in FP64.
+    static __device__ __forceinline__ void eig_cos_sin(DF m, DF p, DF sqrt_p, DF q, DF& c, DF& s)
+    {
+        if (!(sqrt_p.hi >= 1e-7f * ::fabsf(m.hi))) {
+            c = s = DF(__int_as_float(0x7fffffff), 0.f);
+            return;
+        }
+        DF ct = q / (p * sqrt_p);
+        if (ct > DF(1.f, 0.f)) ct = DF(1.f, 0.f);
+        if (ct < DF(-1.f, 0.f)) ct = DF(-1.f, 0.f);
+        const DF one_m = (DF(1.f, 0.f) - ct) * (DF(1.f, 0.f) + ct);
+        const DF st = one_m.hi > 0.f ? df_sqrt(one_m) : DF(0.f, 0.f);
+        const float phf = ::atan2f(st.hi, ct.hi) * (1.f / 3.f);
+        const float cf = ::cosf(phf), sf = ::sinf(phf);
+        DF cc(cf, 0.f), ss(sf, 0.f);
+        const bool c_newton = cf >= 0.6f, s_newton = sf <= 0.35f || sf >= 0.65f;
+        if (c_newton) {
+            const float inv = 1.f / (12.f * cf * cf - 3.f);
+#pragma unroll
+            for (int k = 0; k < 3; k++) cc = cc - ((DF(4.f, 0.f) * cc * cc - DF(3.f, 0.f)) * cc - ct) * inv;
+        }
+        if (s_newton) {
+            const float inv = 1.f / (3.f - 12.f * sf * sf);
+#pragma unroll
+            for (int k = 0; k < 3; k++) ss = ss - ((DF(3.f, 0.f) - DF(4.f, 0.f) * ss * ss) * ss - st) * inv;
+        }
+        if (!c_newton) cc = df_sqrt(DF(1.f, 0.f) - ss * ss);
+        if (!s_newton) ss = df_sqrt(DF(1.f, 0.f) - cc * cc);
+        c = cc;
+        s = ss;
+    }
 };
 
 // Branch-tie tracking for the FP32 evaluation: the MSVD below takes discrete
@@ -158,10 +225,9 @@ __device__ __forceinline__ void msvd_rotation(const T* F, T* R, bool* amb = null
     T a12_sqr = ne.x21 * ne.x21, a13_sqr = ne.x31 * ne.x31, a23_sqr = ne.x32 * ne.x32;
     T p = one_sixth * (a11 * a11 + a22 * a22 + a33 * a33 + T(2) * (a12_sqr + a13_sqr + a23_sqr));
     T q = T(.5) * (a11 * (a22 * a33 - a23_sqr) - a22 * a13_sqr - a33 * a12_sqr) + ne.x21 * ne.x31 * ne.x32;
-    T sqrt_p = MathOf<T>::sqrt_(p), disc = p * p * p - q * q;
-    T disc_c = (T(0) > disc) ? T(0) : disc;
-    T phi = one_third * MathOf<T>::atan2_(MathOf<T>::sqrt_(disc_c), q);
-    T c = MathOf<T>::cos_(phi), s = MathOf<T>::sin_(phi);
+    T sqrt_p = MathOf<T>::sqrt_(p);
+    T c, s;
+    MathOf<T>::eig_cos_sin(m, p, sqrt_p, q, c, s);
     T sqrt_p_cos = sqrt_p * c, root_three_sqrt_p_sin = root_three * sqrt_p * s;
     T l0 = m + T(2) * sqrt_p_cos;
     T l1 = m - sqrt_p_cos - root_three_sqrt_p_sin;
@@ -266,6 +332,35 @@ __device__ __forceinline__ void msvd_rotation(const T* F, T* R, bool* amb = null
             acc += U[3 * i + 2] * Vt[2 * 3 + j];
             R[3 * i + j] = acc;
         }
+}
+
+// Rotation of F in double-float arithmetic, rounded to FP32 (the mixed
+// path's rotation). F is first scaled by a power of two that brings its
+// largest entry into [0.5, 1): R = U V^T does not change under a positive
+// scaling of F, and the double-float products stay inside FP32's exponent
+// range. Returns false (R not set) when the double-float evaluation cannot
+// be trusted -- a nearly isotropic F^T F (see MathOf<DF>) or a non-finite
+// F -- and the caller re-solves in FP64.
+__device__ __forceinline__ bool rotation_df(const double* F, float* Rf)
+{
+    double mx = 0.0;
+#pragma unroll
+    for (int c = 0; c < 9; c++) mx = ::fmax(mx, ::fabs(F[c]));
+    if (!(mx > 0.0 && mx <= 1.7976931348623157e308)) return false;
+    int e;
+    (void)::frexp(mx, &e);
+    const double sc = ::ldexp(1.0, -e);
+    DF Fd[9], Rd[9];
+#pragma unroll
+    for (int c = 0; c < 9; c++) Fd[c] = DF(F[c] * sc);
+    msvd_rotation(Fd, Rd);
+    bool ok = true;
+#pragma unroll
+    for (int c = 0; c < 9; c++) {
+        Rf[c] = __double2float_rn(df_to_double(Rd[c]));
+        ok = ok && Rf[c] == Rf[c];
+    }
+    return ok;
 }
 
 // F = Ds * Dm^-1 with Ds columns (x1-x0, x2-x0, x3-x0), and det F

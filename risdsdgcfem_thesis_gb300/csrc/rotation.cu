@@ -55,8 +55,9 @@ void launch_begin_eval_fp64(const MeshView<double>& m, const double* x, double* 
 // ---------------------------------------------------------------------------
 // Batched BeginEvaluation: block per element tile (one mesh per tile). F and
 // det F in FP64 from FP64 positions and Dm^-1. The FP64 path takes the FP64
-// rotation; the mixed path takes the FP32 rotation unless det F <= the
-// mesh's threshold, where F is re-solved in FP64. Per-mesh counts of
+// rotation; the mixed path the double-float rotation, or, with the FP32
+// option, the FP32 rotation unless det F <= the mesh's threshold or the
+// check below fails, where F is re-solved in double-float arithmetic. Per-mesh counts of
 // inverted elements and FP64 re-solves are added with integer atomics (one
 // per tile), so they do not depend on scheduling.
 // FP32 rotation of F for the mixed path. The result is not trusted -- false
@@ -130,10 +131,18 @@ __global__ void k_begin_eval_batch(BatchView<S> b, const double* __restrict__ x)
                        rotation_fp32(F, b.mc[tm.mesh].rot_check, Rs)) {
                 // FP32 rotation kept
             } else {
-                double R[9];
-                msvd_rotation(F, R);
+                // the double-float rotation, or the FP64 one for a degenerate
+                // element (det F <= the threshold) or a nearly isotropic F
+                // (counted as re-solves of the FP32 rotation)
+                float Rf[9];
+                if (!(detF > b.mc[tm.mesh].degenerate_det_F) || !rotation_df(F, Rf)) {
+                    double R[9];
+                    msvd_rotation(F, R);
 #pragma unroll
-                for (int c = 0; c < 9; c++) Rs[c] = (S)R[c];
+                    for (int c = 0; c < 9; c++) Rf[c] = (float)R[c];
+                }
+#pragma unroll
+                for (int c = 0; c < 9; c++) Rs[c] = (S)Rf[c];
                 atomicAdd(&s_res, 1u);
             }
 #pragma unroll
