@@ -470,9 +470,9 @@ def compression_report(n=40, steps=120, ratio=0.4):
     The mixed path against the plain FP64 path (itself parity-tested against
     the FP64 oracle), step by step: share of rotations computed in FP64 and
     of inverted elements, CG iterations, and the final error -- with the
-    default FP64 rotations, with FP32 rotations re-solved in FP64 where
-    det F <= 1e-3 or the rotation is rounding-sensitive, and with the det F
-    rule alone."""
+    default double-precision rotations (double-float, FP64 for degenerate
+    elements), with FP32 rotations re-solved so where det F <= 1e-3 or the
+    rotation is rounding-sensitive, and with the det F rule alone."""
     from risdsdgcfem_thesis_gb300 import capi, scenes
     sc = scenes.compressed_cube(n, steps, ratio)
     T = float(sc.num_tets)
@@ -519,7 +519,7 @@ def compression_report(n=40, steps=120, ratio=0.4):
 
     return {"case": f"{n}^3 x 5 tets ({int(T)}), top face to {ratio:.0%} height over {steps} steps, "
                     f"E 2e5, nu 0.45, dt 1/60, CG rel 1e-6",
-            "mixed_default_fp64_rotations": mixed(0, 1e-3),
+            "mixed_default_double_precision_rotations": mixed(0, 1e-3),
             "mixed_fp32_rotations_checked": mixed(1, 1e-3),
             "mixed_fp32_rotations_det_F_rule_only": mixed(1, 0.0),
             "fp64_path_noise_floor": noise,

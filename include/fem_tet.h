@@ -66,20 +66,24 @@ typedef struct fem_params {
     double ls_abs_epsilon;    /* ... or |r|^2 <= abs^2 (and breaks if |d.q| < abs^2) */
     uint32_t ls_max_iter;     /* CG iteration cap per step */
     uint32_t precision;       /* enum fem_precision */
-    double degenerate_det_F;  /* mixed only: FP64 rotation re-solve threshold */
+    double degenerate_det_F;  /* mixed only: elements with det F at or below this get the FP64
+                                 rotation */
     uint32_t refresh_every;   /* mixed only: longest run of iterations between FP64
                                  residuals (0 = no periodic refresh) */
     uint32_t compute_energy;  /* 1: elastic and potential energy every step (as FixedStep) */
-    double rotation_check;    /* mixed only: an FP32 rotation is also re-solved in FP64
-                                 when it moves by more than this (max entry) under a
-                                 2^-14 relative change of F; 0 = det F test only */
+    double rotation_check;    /* mixed only, with rotation_fp32: an FP32 rotation is also
+                                 re-solved when it moves by more than this (max entry)
+                                 under a 2^-14 relative change of F; 0 = det F test only */
     double refresh_drop;      /* mixed only: the residual is recomputed in FP64 once |r|
                                  has fallen by this factor since the last time (reliable
                                  updates), and at least every refresh_every iterations;
                                  0 = by refresh_every alone */
-    uint32_t rotation_fp32;   /* mixed only: 1 = rotations in FP32, re-solved in FP64 where
-                                 det F <= degenerate_det_F or rotation_check flags them;
-                                 0 = every rotation in FP64 (once per step) */
+    uint32_t rotation_fp32;   /* mixed only: 0 = every rotation re-solved at double
+                                 precision (double-float arithmetic, about 48 bits; FP64
+                                 where det F <= degenerate_det_F or F^T F is nearly
+                                 isotropic); 1 = rotations in FP32, re-solved so where
+                                 det F <= degenerate_det_F, a branch decision was a near
+                                 tie or rotation_check flags them */
     uint32_t pad;
 } fem_params;
 
@@ -92,7 +96,8 @@ typedef struct fem_step_stats {
     double elastic_energy;    /* TetrahedronElementSet3::V after the step */
     double potential_energy;  /* LeafDSH_Solid3D_FEM::RecomputeEnergy's potential term */
     uint32_t inverted_elements; /* elements with det F <= 0 at BeginEvaluation */
-    uint32_t fp64_resolved;   /* mixed: elements whose rotation was re-solved in FP64 */
+    uint32_t fp64_resolved;   /* mixed: elements whose rotation was re-solved at double
+                                 precision (every element with rotation_fp32 = 0) */
     uint64_t total_cg_iterations; /* sum over the steps of this call */
 } fem_step_stats;
 
@@ -287,7 +292,7 @@ typedef struct fem_server_completion {
     uint32_t scene;
     uint32_t status;         /* enum fem_status of the step */
     uint32_t cg_iterations;
-    uint32_t fp64_resolved;  /* mixed: rotations re-solved in FP64 in that step */
+    uint32_t fp64_resolved;  /* mixed: rotations re-solved at double precision in that step */
     double latency_us;       /* submit -> completion seen by fem_server_pump */
     double queue_us;         /* submit -> the launch that started its step */
     double device_us;        /* device time of the shard launches its step took part

@@ -170,7 +170,7 @@ def test_compressed_cube_fp64_and_mixed_vs_oracle(fem_lib, oracle):
     (initial velocities perturbed by 6e-8 of the mesh size) does to it, and
     what stopping its CG at rel 1e-7 instead of 1e-6 does to it.
     FP64 path: rel-L2 <= max(1e-10, 10 x the 1e-15 noise floor).
-    Mixed path (default FP64 rotations): positions rel-L2 and velocities
+    Mixed path (default double-precision rotations): positions rel-L2 and velocities
     (normalised by the run's peak |v|) <= max(1e-5, 2 x the larger of those
     spreads)."""
     sc = scenes.compressed_cube(n=8, steps=120, ratio=0.4)
@@ -252,8 +252,8 @@ def test_mixed_converges_like_fp64_on_stiff_meshes(fem_lib):
 
 def test_compression_counts_fp64_resolves(fem_lib):
     """FP32 rotations (rotation_fp32 = 1): under heavy compression some
-    elements are re-solved in FP64 (det F rule, branch ties, sensitivity),
-    not all; with the default FP64 rotations every rotation is."""
+    elements are re-solved at double precision (det F rule, branch ties, sensitivity),
+    not all; with the default double-precision rotations every rotation is."""
     sc = scenes.compressed_cube(n=6, steps=20, ratio=0.2)
     b = fem_lib.Batch([sc], precision=fem_lib.FEM_PRECISION_MIXED, rotation_fp32=1)
     d = fem_lib.Batch([sc], precision=fem_lib.FEM_PRECISION_MIXED)
