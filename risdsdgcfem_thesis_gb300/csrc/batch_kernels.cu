@@ -860,7 +860,9 @@ template <typename S>
 void BatchLaunch<S>::tile_force(const BatchView<S>& b, const double* x, double* part64, double* tile_energy,
                                 cudaStream_t s)
 {
+    prof_begin("tile_force", s);
     k_tile_force<S><<<grid_tiles(b.ntiles), kTileElems, 0, s>>>(b, x, part64, tile_energy);
+    prof_end("tile_force", s);
     launch_counter()++;
 }
 
