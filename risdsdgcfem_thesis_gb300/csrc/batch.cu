@@ -1279,13 +1279,14 @@ int fem_batch_kernel_launches(fem_batch b, uint32_t steps, uint64_t* launches)
     BCK(cudaMemcpyAsync(&body_runs, b->any_flag.p, sizeof(unsigned), cudaMemcpyDeviceToHost, b->stream));
     BCK(cudaStreamSynchronize(b->stream));
     // kernels per step outside the CG loop, plus per executed CG iteration 3
-    // (FP64 path) or 5 (mixed path: tile product, refresh product -- counted
-    // in every iteration, an upper bound --, mesh alpha, node pass)
+    // (FP64 path) or 6 (mixed path: tile product, refresh product -- counted
+    // in every iteration, an upper bound --, mesh alpha, node pass, mesh
+    // update)
     bool energy = false;
     for (auto& m : b->meshes) energy |= m.p.compute_energy != 0;
     const bool mixed = b->opt.precision == FEM_PRECISION_MIXED;
     const uint64_t fixed = 8 + (b->K ? 1 : 0) + (energy ? 4 : 0);
-    *launches = (uint64_t)steps * fixed + (mixed ? 5ull : 3ull) * body_runs;
+    *launches = (uint64_t)steps * fixed + (mixed ? 6ull : 3ull) * body_runs;
     return FEM_OK;
 }
 

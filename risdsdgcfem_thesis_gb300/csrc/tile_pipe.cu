@@ -24,10 +24,15 @@
 // k_node_update_fused: per node of the running meshes: d = S(r + beta d) (the
 // values the tiles staged), q = S(fK sum(partials) + m fM d), y += alpha d
 // (into the FP32 increment accumulator), r -= alpha q (on refresh iterations
-// r is first recomputed as S(b - A y) from the product of y), |r|^2; a mesh
-// that breaks down leaves its loop before the update. The last block of a mesh forms beta and the loop test
-// (ILSS_CG.h:100-144), the last block of the grid sets the CUDA-graph while
-// condition and the refresh flag.
+// r is first recomputed as S(b - A y) from the product of y), and one
+// (hi, lo) share of |r|^2 per node chunk; a mesh that breaks down leaves its
+// loop before the update.
+//
+// k_mesh_update: one warp per running mesh sums its chunk shares (fixed
+// order) and forms beta and the loop test (ILSS_CG.h:100-144); the last
+// block of the grid sets the CUDA-graph while condition and the refresh
+// flag. The per-mesh reductions thus need no arrival counters, fences or
+// atomics inside the streaming kernels.
 //
 // Blob of a tile with ne elements (ne4 = ne rounded up to 4) and nn local
 // nodes, offsets from the blob start:
@@ -164,17 +169,6 @@ __device__ __forceinline__ F2 block_sum_f2(F2 v, float2* sh)
         v = warp_sum_f2(v);
     }
     return v;
-}
-
-// Fixed-order sum of n (hi, lo) partials, result valid in thread 0.
-__device__ __forceinline__ F2 sum_partials_f2(const float2* __restrict__ p, uint32_t n, float2* sh)
-{
-    F2 a = {0.f, 0.f};
-    for (uint32_t k = threadIdx.x; k < n; k += blockDim.x) {
-        const float2 w = __ldcg(p + k);
-        a = f2_add(a, F2{w.x, w.y});
-    }
-    return block_sum_f2(a, sh);
 }
 
 // Arrival of a block on a counter: the values other blocks must see are
@@ -491,11 +485,9 @@ __global__ void __launch_bounds__(256) k_node_update_fused(BatchView<float> b, c
                                                            const double* __restrict__ part64,
                                                            const double* __restrict__ bv,
                                                            double* __restrict__ y, float* __restrict__ r,
-                                                           float* __restrict__ d, float2* __restrict__ cshare,
-                                                           LoopSync ls)
+                                                           float* __restrict__ d, float2* __restrict__ cshare)
 {
     __shared__ float2 sh[32];
-    __shared__ unsigned s_last;
     const uint32_t n_act = *(volatile const uint32_t*)(b.act_count + 1);
     for (uint32_t ia = blockIdx.x; ia < n_act; ia += gridDim.x) {
         const uint32_t ci = b.act_chunks[ia];
@@ -589,78 +581,99 @@ __global__ void __launch_bounds__(256) k_node_update_fused(BatchView<float> b, c
         }
         const F2 rr = block_sum_f2(F2{acc, 0.f}, sh);
         if (threadIdx.x == 0) cshare[ci] = make_float2(rr.hi, rr.lo);
-        if (arrive_last_t(ls.mcount + ch.mesh, c.nchunks, &s_last)) {
-            const F2 tot = sum_partials_f2(cshare + c.chunk0, c.nchunks, sh);
-            if (threadIdx.x == 0) {
-                StepScalars& st = b.st[ch.mesh];
-                if (confirm) {
-                    // the FP64 residual of the current iterate decides: leave,
-                    // or go on from it -- with the recurrence's direction
-                    // (beta from the FP64 residual, reliable-update style),
-                    // unless the recursive residual had fallen to rounding
-                    // noise, then from the residual alone (beta = 0)
-                    const double total = (double)tot.hi + (double)tot.lo;
-                    const double rec = st.delta_new;  // recursive |r|^2 at the loop test
-                    st.confirm = 0;
-                    st.delta_old = rec;
-                    st.delta_new = total;
-                    st.delta_refresh = total;
-                    st.k_refresh = st.k;
-                    st.refresh_next = 0;
-                    if (total != total) st.status = 3u;
-                    if (cg_cont_t(st)) {
-                        st.beta = (rec > 0.0 && total <= 1e3 * rec) ? total / rec : 0.0;
-                        st.beta_f = (float)st.beta;
-                        st.done = 0;
-                    } else {
-                        st.done = 1;
-                        st.finished = 1;
-                        atomicAdd(b.list_dirty, c.ntiles);
-                        finish_stats_t(st);
-                    }
-                } else if (brk) {
+    }
+}
+
+// Per running mesh, after the node pass: |r|^2 from its chunks' shares
+// (fixed order), then beta, the reliable-update and exit-confirmation rules
+// and the loop test (ILSS_CG.h:100-144). One warp per mesh; the last block
+// of the grid then rebuilds the work lists, sets the CUDA-graph while
+// condition and the refresh flag.
+__global__ void __launch_bounds__(256) k_mesh_update(BatchView<float> b, const float2* __restrict__ cshare, LoopSync ls)
+{
+    __shared__ unsigned s_last;
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t mesh = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; mesh < b.M; mesh += nw) {
+        if (b.st[mesh].done) continue;
+        const MeshConsts& c = b.mc[mesh];
+        F2 tot = {0.f, 0.f};
+        for (uint32_t k = lane; k < c.nchunks; k += 32u) {
+            const float2 w = __ldcg(cshare + c.chunk0 + k);
+            tot = f2_add(tot, F2{w.x, w.y});
+        }
+        tot = warp_sum_f2(tot);
+        if (lane == 0) {
+            const bool confirm = b.st[mesh].confirm != 0, brk = b.st[mesh].brk != 0;
+            StepScalars& st = b.st[mesh];
+            if (confirm) {
+                // the FP64 residual of the current iterate decides: leave,
+                // or go on from it -- with the recurrence's direction
+                // (beta from the FP64 residual, reliable-update style),
+                // unless the recursive residual had fallen to rounding
+                // noise, then from the residual alone (beta = 0)
+                const double total = (double)tot.hi + (double)tot.lo;
+                const double rec = st.delta_new;  // recursive |r|^2 at the loop test
+                st.confirm = 0;
+                st.delta_old = rec;
+                st.delta_new = total;
+                st.delta_refresh = total;
+                st.k_refresh = st.k;
+                st.refresh_next = 0;
+                if (total != total) st.status = 3u;
+                if (cg_cont_t(st)) {
+                    st.beta = (rec > 0.0 && total <= 1e3 * rec) ? total / rec : 0.0;
+                    st.beta_f = (float)st.beta;
+                    st.done = 0;
+                } else {
                     st.done = 1;
                     st.finished = 1;
                     atomicAdd(b.list_dirty, c.ntiles);
                     finish_stats_t(st);
-                } else {
-                    const double total = (double)tot.hi + (double)tot.lo;
-                    st.alpha = st.delta_new / st.dot_dq;
-                    st.delta_old = st.delta_new;
-                    st.delta_new = total;
-                    st.beta = total / st.delta_old;
-                    st.beta_f = (float)st.beta;
-                    st.k += 1;
-                    st.total_iters += 1;
-                    if (total != total) st.status = 3u;
-                    // reliable updates: recompute the residual in FP64 once |r|
-                    // has fallen by refresh_drop since the last FP64 residual,
-                    // and at least every refresh_every iterations
-                    if (st.refresh_next) {
-                        st.delta_refresh = total;
-                        st.k_refresh = st.k;
-                    }
-                    st.refresh_next = ((c.refresh_drop_sq > 0.0 && total < c.refresh_drop_sq * st.delta_refresh) ||
-                                       (c.refresh_every > 0 && st.k - st.k_refresh >= c.refresh_every))
-                                          ? 1u
-                                          : 0u;
-                    bool cont = cg_cont_t(st);
-                    if (!cont && st.k_refresh != st.k && st.k < st.max_iter && total == total &&
-                        (c.refresh_every > 0 || c.refresh_drop_sq > 0.0)) {
-                        // converged on the FP32 recursive residual: the next
-                        // iteration measures the FP64 residual before the loop ends
-                        cont = true;
-                        st.refresh_next = 1u;
-                        st.confirm = 1u;
-                    }
-                    st.done = cont ? 0u : 1u;
-                    if (st.done) {
-                        finish_stats_t(st);
-                        st.finished = 1;
-                        atomicAdd(b.list_dirty, c.ntiles);
-                    }
+                }
+            } else if (brk) {
+                st.done = 1;
+                st.finished = 1;
+                atomicAdd(b.list_dirty, c.ntiles);
+                finish_stats_t(st);
+            } else {
+                const double total = (double)tot.hi + (double)tot.lo;
+                st.alpha = st.delta_new / st.dot_dq;
+                st.delta_old = st.delta_new;
+                st.delta_new = total;
+                st.beta = total / st.delta_old;
+                st.beta_f = (float)st.beta;
+                st.k += 1;
+                st.total_iters += 1;
+                if (total != total) st.status = 3u;
+                // reliable updates: recompute the residual in FP64 once |r|
+                // has fallen by refresh_drop since the last FP64 residual,
+                // and at least every refresh_every iterations
+                if (st.refresh_next) {
+                    st.delta_refresh = total;
+                    st.k_refresh = st.k;
+                }
+                st.refresh_next = ((c.refresh_drop_sq > 0.0 && total < c.refresh_drop_sq * st.delta_refresh) ||
+                                   (c.refresh_every > 0 && st.k - st.k_refresh >= c.refresh_every))
+                                      ? 1u
+                                      : 0u;
+                bool cont = cg_cont_t(st);
+                if (!cont && st.k_refresh != st.k && st.k < st.max_iter && total == total &&
+                    (c.refresh_every > 0 || c.refresh_drop_sq > 0.0)) {
+                    // converged on the FP32 recursive residual: the next
+                    // iteration measures the FP64 residual before the loop ends
+                    cont = true;
+                    st.refresh_next = 1u;
+                    st.confirm = 1u;
+                }
+                st.done = cont ? 0u : 1u;
+                if (st.done) {
+                    finish_stats_t(st);
+                    st.finished = 1;
+                    atomicAdd(b.list_dirty, c.ntiles);
                 }
             }
+            __threadfence();  // the mesh's scalars before the grid arrival below
         }
     }
     // last block of the grid: work lists (when a mesh left its loop), while
@@ -753,8 +766,12 @@ void launch_node_update_fused(const BatchView<float>& b, const float* part, cons
     prof_end("mesh_alpha", s);
     launch_counter()++;
     prof_begin("node_update_mixed", s);
-    k_node_update_fused<<<grid, kNodeThreads, 0, s>>>(b, part, part64, bv, y, r, d, cshare, ls);
+    k_node_update_fused<<<grid, kNodeThreads, 0, s>>>(b, part, part64, bv, y, r, d, cshare);
     prof_end("node_update_mixed", s);
+    launch_counter()++;
+    prof_begin("mesh_update", s);
+    k_mesh_update<<<(b.M * 32u + kNodeThreads - 1) / kNodeThreads, kNodeThreads, 0, s>>>(b, cshare, ls);
+    prof_end("mesh_update", s);
     launch_counter()++;
 }
 
