@@ -9,7 +9,7 @@
 //
 // Set-up (fem_batch_finalize): per mesh, elements are put in Morton order of
 // their centroids and cut into tiles of at most tile_elems tets and 256
-// local nodes; the element data (Dm^-1, E-matrix entries times V, FP64 for
+// local nodes (120 for the mixed path's tiles of up to 128 tets); the element data (Dm^-1, E-matrix entries times V, FP64 for
 // the once-per-step kernels and in the path's type S for the CG products)
 // follow that order. Node numbering is the caller's.
 //
@@ -161,6 +161,7 @@ struct fem_batch_s {
         b.M = M;
         b.ntiles = ntiles;
         b.nchunks = nchunks;
+        b.pipe_tile = opt.tile_elems <= (uint32_t)kPipeSmallTile ? kPipeSmallTile : kTileElems;
         b.Ntot = (uint32_t)Ntot;
         b.Ttot = (uint32_t)Ttot;
         b.tiles = tiles.p;
@@ -529,6 +530,8 @@ int fem_batch_finalize(fem_batch b)
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return batch_fail(FEM_E_NODEVICE, "no CUDA device");
     const bool fp64 = b->opt.precision == FEM_PRECISION_FP64;
     const uint32_t tile_cap = b->opt.tile_elems;
+    // local nodes per tile: the mixed path's small tiles hold fewer
+    const size_t node_cap = (!fp64 && tile_cap <= (uint32_t)kPipeSmallTile) ? kPipeSmallNodes : kTileNodes;
     b->M = (uint32_t)b->meshes.size();
 
     std::vector<TileMeta> tiles;
@@ -643,7 +646,7 @@ int fem_batch_finalize(fem_batch b)
                     for (int j = 0; j < i; j++) seen |= (t[j] == t[i]);
                     fresh += seen ? 0 : 1;
                 }
-                if (lnodes.size() + fresh > (size_t)kTileNodes) break;
+                if (lnodes.size() + fresh > node_cap) break;
                 uchar4 lc;
                 unsigned char li4[4];
                 for (int i = 0; i < 4; i++) {

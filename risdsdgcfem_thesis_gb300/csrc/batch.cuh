@@ -38,6 +38,12 @@ namespace femgb {
 constexpr int kTileElems = 256;
 constexpr int kTileNodes = 256;
 constexpr int kChunkNodes = 1024;  // default node chunk (one work item of a node pass)
+// The mixed path's pipelined tile product runs one thread per element: tiles
+// of at most kPipeSmallTile tets use blocks of that many threads, with at most
+// kPipeSmallNodes local nodes (so that eight blocks fit an SM's shared
+// memory); larger tiles use kTileElems threads and up to kTileNodes nodes.
+constexpr int kPipeSmallTile = 128;
+constexpr int kPipeSmallNodes = 120;
 constexpr int kNodeThreads = 256;  // threads per node-kernel block
 
 // Layout of a tile's blob (mixed path, see tile_pipe.cu): the element data,
@@ -49,18 +55,18 @@ constexpr int kNodeThreads = 256;  // threads per node-kernel block
 // and, 4-aligned, the header {uint32 own0, float fK, float m fM} (the partial
 // slot of the first owned node, the mesh's FP32 factors) and uint32
 // ovslot[nn - nown] (the partial slots of the shared local nodes).
-__host__ __device__ inline uint32_t blob_ne4(uint32_t ne) { return (ne + 3u) & ~3u; }
+__host__ __device__ constexpr uint32_t blob_ne4(uint32_t ne) { return (ne + 3u) & ~3u; }
 // Byte offset of component c of element i.
-__host__ __device__ inline uint32_t blob_comp_off(uint32_t c, uint32_t i, uint32_t ne4)
+__host__ __device__ constexpr uint32_t blob_comp_off(uint32_t c, uint32_t i, uint32_t ne4)
 {
     return c < 20u ? 16u * ((c >> 2) * ne4 + i) + 4u * (c & 3u) : 80u * ne4 + 8u * i + 4u * (c - 20u);
 }
-__host__ __device__ inline uint32_t blob_lptr_off(uint32_t ne) { return 88u * blob_ne4(ne); }
-__host__ __device__ inline uint32_t blob_hdr_off(uint32_t ne, uint32_t nn)
+__host__ __device__ constexpr uint32_t blob_lptr_off(uint32_t ne) { return 88u * blob_ne4(ne); }
+__host__ __device__ constexpr uint32_t blob_hdr_off(uint32_t ne, uint32_t nn)
 {
     return (blob_lptr_off(ne) + 2u * (nn + 1u) + 8u * ne + 3u) & ~3u;
 }
-__host__ __device__ inline uint32_t blob_bytes(uint32_t ne, uint32_t nn, uint32_t nown)
+__host__ __device__ constexpr uint32_t blob_bytes(uint32_t ne, uint32_t nn, uint32_t nown)
 {
     return (blob_hdr_off(ne, nn) + 12u + 4u * (nn - nown) + 15u) & ~15u;
 }
@@ -112,6 +118,7 @@ struct MeshConsts {
 template <typename S>
 struct BatchView {
     uint32_t M, ntiles, nchunks, Ntot, Ttot;
+    uint32_t pipe_tile;            // mixed: threads per block of the tile product (kPipeSmallTile or kTileElems)
     const TileMeta* tiles;
     const ChunkMeta* chunks;
     const MeshConsts* mc;

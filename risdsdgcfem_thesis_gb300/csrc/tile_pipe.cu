@@ -204,14 +204,21 @@ __device__ __forceinline__ void finish_stats_t(StepScalars& s)
 
 }  // namespace
 
-constexpr uint32_t kStageBytes = 26240;  // >= blob_bytes(256, 256, 0) = 26128, multiple of 128
-static_assert(kStageBytes >= 26128, "stage must hold the largest tile blob");
-
-// Shared memory: two blob stages (a tile's element outputs overwrite its
-// element data once every element has read it), the staged direction
-// sd4[256], two mbarriers and the warps' shares: 56.7 KB, four resident
-// blocks per SM.
-constexpr uint32_t kPipeSmem = 2 * kStageBytes + 16u * kTileNodes + 16u + 8u * 8u;
+// Shared memory of a block of the TILE-thread kernel: two blob stages (a
+// tile's element outputs overwrite its element data once every element has
+// read it), the staged direction sd4[nodes], two mbarriers and the warps'
+// shares and the previous tile's id. TILE = 256: 55.1 KB, four resident
+// blocks per SM; TILE = 128 (at most 120 local nodes): 27.4 KB, eight (with
+// the 1 KB each block reserves, 227 of the SM's 228 KB).
+template <int TILE>
+struct PipeShape {
+    static constexpr uint32_t kNodes = TILE == kPipeSmallTile ? (uint32_t)kPipeSmallNodes : (uint32_t)kTileNodes;
+    static constexpr uint32_t kStage = blob_bytes(TILE, kNodes, 0);  // a multiple of 16
+    static constexpr uint32_t kSmem = 2 * kStage + 16u * kNodes + 16u + 8u * (TILE / 32) + 16u;
+    static constexpr int kMinBlocks = TILE == kPipeSmallTile ? 8 : 4;
+};
+static_assert(PipeShape<256>::kStage == 26128 && PipeShape<128>::kStage == 13024, "stage sizes");
+static_assert(8 * (((PipeShape<128>::kSmem + 127) & ~127u) + 1024) <= 233472, "eight small blocks per SM");
 
 // What a block needs to know of one tile before its blob arrives.
 struct TileLook {
@@ -261,17 +268,22 @@ __device__ __forceinline__ void fence_proxy_async_smem()
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
 
-__global__ void __launch_bounds__(256, 4) k_tile_spmv_pipe(BatchView<float> b, const float* __restrict__ dvec,
+template <int TILE>
+__global__ void __launch_bounds__(TILE, PipeShape<TILE>::kMinBlocks) k_tile_spmv_pipe(BatchView<float> b, const float* __restrict__ dvec,
                                                            const float* __restrict__ rvec, float* __restrict__ part,
                                                            float2* __restrict__ tshare,
                                                            cudaGraphConditionalHandle if_refresh, int set_if,
                                                            const unsigned* __restrict__ refresh_flag,
                                                            unsigned* __restrict__ err)
 {
+    constexpr uint32_t kStageBytes = PipeShape<TILE>::kStage;
     extern __shared__ __align__(128) unsigned char smem[];
     float4* sd4 = reinterpret_cast<float4*>(smem + 2 * kStageBytes);
-    uint64_t* bar = reinterpret_cast<uint64_t*>(sd4 + kTileNodes);
-    float2* wsh = reinterpret_cast<float2*>(bar + 2);  // [8] per-warp shares
+    uint64_t* bar = reinterpret_cast<uint64_t*>(sd4 + PipeShape<TILE>::kNodes);
+    float2* wsh = reinterpret_cast<float2*>(bar + 2);  // [TILE / 32] per-warp shares
+    // the previous tile whose share thread 0 stores after barrier A (only
+    // thread 0 uses it); ~0u: none
+    uint32_t& s_prev = *reinterpret_cast<uint32_t*>(wsh + TILE / 32);
     const uint32_t G = gridDim.x, tid = threadIdx.x;
 
     if (set_if && blockIdx.x == 0 && tid == 0) cudaGraphSetConditional(if_refresh, *refresh_flag ? 1u : 0u);
@@ -318,9 +330,6 @@ __global__ void __launch_bounds__(256, 4) k_tile_spmv_pipe(BatchView<float> b, c
             cr0 = __ldg(rvec + g); cr1 = __ldg(rvec + g + 1); cr2 = __ldg(rvec + g + 2);
         }
     }
-    // the previous tile whose share thread 0 stores after barrier A (kept in
-    // shared memory: only thread 0 uses it); ~0u: none
-    __shared__ uint32_t s_prev;
     if (tid == 0) s_prev = ~0u;
     for (; i < n_act; i += G) {
         const bool live = look_live(cur), nlive = look_live(nxt);
@@ -708,8 +717,9 @@ __global__ void __launch_bounds__(256) k_mesh_update(BatchView<float> b, const f
 
 // ---------------------------------------------------------------------------
 
-uint32_t tile_pipe_smem_bytes() { return kPipeSmem; }
+uint32_t tile_pipe_smem_bytes() { return PipeShape<256>::kSmem; }
 
+template <int TILE>
 static int pipe_grid()
 {
     static int grid = 0;
@@ -717,8 +727,9 @@ static int pipe_grid()
         int dev = 0, sms = 0, per_sm = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaFuncSetAttribute(k_tile_spmv_pipe, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPipeSmem);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tile_spmv_pipe, 256, kPipeSmem);
+        cudaFuncSetAttribute(k_tile_spmv_pipe<TILE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)PipeShape<TILE>::kSmem);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tile_spmv_pipe<TILE>, TILE, PipeShape<TILE>::kSmem);
         if (sms <= 0) sms = 152;
         if (per_sm <= 0) per_sm = 1;
         grid = sms * per_sm;
@@ -730,10 +741,16 @@ void launch_tile_spmv_pipe(const BatchView<float>& b, const float* d, const floa
                            cudaGraphConditionalHandle if_refresh, int set_if, const unsigned* refresh_flag,
                            unsigned* err, cudaStream_t s)
 {
-    const int g = pipe_grid();
+    const bool small = b.pipe_tile == (uint32_t)kPipeSmallTile;
+    const int g = small ? pipe_grid<kPipeSmallTile>() : pipe_grid<kTileElems>();
     const uint32_t grid = b.ntiles < (uint32_t)g ? (b.ntiles ? b.ntiles : 1) : (uint32_t)g;
     prof_begin("tile_spmv_mixed", s);
-    k_tile_spmv_pipe<<<grid, 256, kPipeSmem, s>>>(b, d, r, part, tshare, if_refresh, set_if, refresh_flag, err);
+    if (small)
+        k_tile_spmv_pipe<kPipeSmallTile><<<grid, kPipeSmallTile, PipeShape<kPipeSmallTile>::kSmem, s>>>(
+            b, d, r, part, tshare, if_refresh, set_if, refresh_flag, err);
+    else
+        k_tile_spmv_pipe<kTileElems><<<grid, kTileElems, PipeShape<kTileElems>::kSmem, s>>>(
+            b, d, r, part, tshare, if_refresh, set_if, refresh_flag, err);
     prof_end("tile_spmv_mixed", s);
     launch_counter()++;
 }
@@ -777,7 +794,8 @@ void launch_node_update_fused(const BatchView<float>& b, const float* part, cons
 
 void prepare_tile_pipe()
 {
-    (void)pipe_grid();
+    (void)pipe_grid<kPipeSmallTile>();
+    (void)pipe_grid<kTileElems>();
     (void)node_grid();
 }
 
