@@ -23,8 +23,8 @@ from typing import Dict, Iterable, List, Optional, Sequence, Tuple
 from . import capi
 
 # (tile_elems, reorder, chunk_nodes)
-DEFAULT_CANDIDATES: Tuple[Tuple[int, int, int], ...] = ((256, 1, 1024), (192, 1, 1024), (128, 1, 1024),
-                                                         (256, 0, 1024), (256, 0, 512), (256, 0, 2048))
+DEFAULT_CANDIDATES: Tuple[Tuple[int, int, int], ...] = ((256, 1, 1024), (256, 1, 512), (192, 1, 1024),
+                                                         (128, 1, 1024), (256, 0, 1024), (256, 0, 512))
 
 
 def _cache_path() -> str:
