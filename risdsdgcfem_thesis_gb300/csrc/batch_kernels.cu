@@ -303,7 +303,12 @@ template <typename S>
 __global__ void __launch_bounds__(256) k_tile_force(BatchView<S> b, const double* __restrict__ x,
                                                     double* __restrict__ part64, double* __restrict__ tile_energy)
 {
-    __shared__ double so[12 * kTileElems];
+    // FP64 path: FP64. Mixed path: double-float values (about 48 bits; the
+    // FP32 rotation and material scalars are exact in them, Dm^-1 comes from
+    // its FP64 copy), FP64 partial sums: the mixed operator's FP32 element
+    // data already bound its accuracy far above this evaluation's error
+    using V = typename Y64Value<S>::T;
+    __shared__ V so[12 * kTileElems];
     const uint32_t* list = part64 ? b.start_tiles : b.launch_tiles;
     const uint32_t n = b.list_count[part64 ? 0 : 2];
     for (uint32_t i = blockIdx.x; i < n; i += gridDim.x) {
@@ -315,43 +320,52 @@ __global__ void __launch_bounds__(256) k_tile_force(BatchView<S> b, const double
         if (threadIdx.x < tm.ne) {
             const size_t e = tm.e0 + threadIdx.x;
             const size_t T = b.Ttot;
-            double R[9], Di[9];
+            S R[9];
+            V Di[9];
 #pragma unroll
-            for (int c = 0; c < 9; c++) R[c] = (double)b.R[c * T + e];
+            for (int c = 0; c < 9; c++) R[c] = b.R[c * T + e];
 #pragma unroll
-            for (int c = 0; c < 9; c++) Di[c] = b.Dinv64[c * T + e];
-            const double k1 = b.mat[e], knu = b.mat[T + e], k2 = b.mat[2 * T + e];
+            for (int c = 0; c < 9; c++) y64_set(Di[c], b.Dinv64[c * T + e]);
+            V k1, knu, k2;
+            y64_set(k1, (double)b.mat[e]);
+            y64_set(knu, (double)b.mat[T + e]);
+            y64_set(k2, (double)b.mat[2 * T + e]);
             const int4 g = b.gtets[e];
             const int ids[4] = {g.x, g.y, g.z, g.w};
-            double u[12];
+            V u[12];
 #pragma unroll
             for (int i = 0; i < 4; i++) {
                 const size_t n = ids[i];
-                const double xa = x[3 * n], xb = x[3 * n + 1], xc = x[3 * n + 2];
+                V xa, xb, xc;
+                y64_set(xa, x[3 * n]);
+                y64_set(xb, x[3 * n + 1]);
+                y64_set(xc, x[3 * n + 2]);
 #pragma unroll
                 for (int a = 0; a < 3; a++) {
-                    double acc = 0.0;
+                    V acc{};
                     acc += R[a] * xa;
                     acc += R[3 + a] * xb;
                     acc += R[6 + a] * xc;
-                    u[3 * i + a] = acc - b.rest[3 * n + a];
+                    V r0;
+                    y64_set(r0, b.rest[3 * n + a]);
+                    u[3 * i + a] = acc - r0;
                 }
             }
-            double D[9];
+            V D[9];
 #pragma unroll
             for (int a = 0; a < 3; a++)
 #pragma unroll
                 for (int j = 0; j < 3; j++) D[3 * a + j] = u[3 * (j + 1) + a] - u[a];
-            double H[9];
+            V H[9];
 #pragma unroll
             for (int a = 0; a < 3; a++)
 #pragma unroll
                 for (int c = 0; c < 3; c++) H[3 * a + c] = D[3 * a] * Di[c] + D[3 * a + 1] * Di[3 + c] + D[3 * a + 2] * Di[6 + c];
-            double P[9], es;
+            V P[9], es;
             stress_forces(H, Di, k1, knu, k2, P, es);
-            energy = 0.5 * es;
+            energy = 0.5 * y64_get(es);
             if (part64) {
-                double out[12];
+                V out[12];
                 rotate_out(R, P, out);
 #pragma unroll
                 for (int c = 0; c < 12; c++) so[c * kTileElems + threadIdx.x] = out[c];
@@ -366,7 +380,7 @@ __global__ void __launch_bounds__(256) k_tile_force(BatchView<S> b, const double
             const uint16_t* lp = b.lptr + b.lptr0[t];
             const uint16_t* li = b.lidx + tm.c0;
             for (int i = threadIdx.x; i < tm.nn; i += blockDim.x) {
-                double a0 = 0, a1 = 0, a2 = 0;
+                V a0{}, a1{}, a2{};
                 for (int j = lp[i]; j < lp[i + 1]; j++) {
                     const int v = li[j], el = v >> 2, sl = v & 3;
                     a0 += so[(3 * sl) * kTileElems + el];
@@ -374,9 +388,9 @@ __global__ void __launch_bounds__(256) k_tile_force(BatchView<S> b, const double
                     a2 += so[(3 * sl + 2) * kTileElems + el];
                 }
                 const size_t o = 3 * tile_slot(b.ov_map, tm.own0, tm.ov0, tm.nown, i);
-                part64[o] = a0;
-                part64[o + 1] = a1;
-                part64[o + 2] = a2;
+                part64[o] = y64_get(a0);
+                part64[o + 1] = y64_get(a1);
+                part64[o + 2] = y64_get(a2);
             }
         }
         __syncthreads();

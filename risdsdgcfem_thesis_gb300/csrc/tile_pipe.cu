@@ -473,19 +473,21 @@ __global__ void __launch_bounds__(256) k_mesh_alpha(BatchView<float> b, const fl
     for (uint32_t m = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; m < b.M; m += nw) {
         StepScalars& st = b.st[m];
         if (st.done) continue;
-        const MeshConsts& c = b.mc[m];
+        // the scalars are loaded before the shares are summed (one round trip)
+        const uint32_t tile0 = b.mc[m].tile0, ntiles = b.mc[m].ntiles;
+        const bool confirm = st.confirm != 0;  // measure the FP64 residual only, no CG update
+        const double abs_eps_sq = st.abs_eps_sq, delta_new = st.delta_new;
         F2 a = {0.f, 0.f};
-        for (uint32_t k = lane; k < c.ntiles; k += 32u) {
-            const float2 w = __ldcg(tshare + c.tile0 + k);
+        for (uint32_t k = lane; k < ntiles; k += 32u) {
+            const float2 w = __ldcg(tshare + tile0 + k);
             a = f2_add(a, F2{w.x, w.y});
         }
         a = warp_sum_f2(a);
         if (lane == 0) {
             const double dq = (double)a.hi + (double)a.lo;
-            const bool confirm = st.confirm != 0;  // measure the FP64 residual only, no CG update
             st.dot_dq = dq;
-            st.brk = (!confirm && ::fabs(dq) < st.abs_eps_sq) ? 1u : 0u;  // leave before the update
-            st.alpha_f = confirm ? 0.f : (float)(st.delta_new / dq);
+            st.brk = (!confirm && ::fabs(dq) < abs_eps_sq) ? 1u : 0u;  // leave before the update
+            st.alpha_f = confirm ? 0.f : (float)(delta_new / dq);
         }
     }
 }
@@ -606,6 +608,10 @@ __global__ void __launch_bounds__(256) k_mesh_update(BatchView<float> b, const f
     for (uint32_t mesh = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; mesh < b.M; mesh += nw) {
         if (b.st[mesh].done) continue;
         const MeshConsts& c = b.mc[mesh];
+        // the mesh's scalars, copied before the shares are summed (one round
+        // trip for all of them), updated in registers and written back once
+        StepScalars st;
+        if (lane == 0) st = b.st[mesh];
         F2 tot = {0.f, 0.f};
         for (uint32_t k = lane; k < c.nchunks; k += 32u) {
             const float2 w = __ldcg(cshare + c.chunk0 + k);
@@ -613,8 +619,7 @@ __global__ void __launch_bounds__(256) k_mesh_update(BatchView<float> b, const f
         }
         tot = warp_sum_f2(tot);
         if (lane == 0) {
-            const bool confirm = b.st[mesh].confirm != 0, brk = b.st[mesh].brk != 0;
-            StepScalars& st = b.st[mesh];
+            const bool confirm = st.confirm != 0, brk = st.brk != 0;
             if (confirm) {
                 // the FP64 residual of the current iterate decides: leave,
                 // or go on from it -- with the recurrence's direction
@@ -682,6 +687,7 @@ __global__ void __launch_bounds__(256) k_mesh_update(BatchView<float> b, const f
                     atomicAdd(b.list_dirty, c.ntiles);
                 }
             }
+            b.st[mesh] = st;
             __threadfence();  // the mesh's scalars before the grid arrival below
         }
     }
