@@ -218,6 +218,12 @@ int fem_batch_info(fem_batch b, uint32_t* meshes, uint64_t* nodes, uint64_t* tet
 int fem_batch_set_knc_targets(fem_batch b, uint32_t mesh, const double* targets);
 int fem_batch_set_state(fem_batch b, uint32_t mesh, const double* x, const double* v);
 int fem_batch_get_state(fem_batch b, uint32_t mesh, double* x, double* v);
+/* The rotations (T*9, row-major, the caller's element order; the mixed path's
+ * FP32 rotations widened to double) and det F (T) of mesh `mesh` as of its
+ * last BeginEvaluation: the batch form of fem_solid_get_rotations (the
+ * element set's cached R and det F, TetrahedronElementSet3.cpp:219-281).
+ * Either pointer may be null. */
+int fem_batch_get_rotations(fem_batch b, uint32_t mesh, double* R, double* detF);
 /* 1: steps run as the captured CUDA graph (device-side CG loop); 0: the same
  * kernels launched one by one with the CG loop on the host (per-kernel
  * profiling and timing). */

@@ -354,6 +354,7 @@ _BATCH_SIGNATURES = {
     "fem_batch_set_knc_targets": (C.c_int, [C.c_void_p, C.c_uint32, _dp]),
     "fem_batch_set_state": (C.c_int, [C.c_void_p, C.c_uint32, _dp, _dp]),
     "fem_batch_get_state": (C.c_int, [C.c_void_p, C.c_uint32, _dp, _dp]),
+    "fem_batch_get_rotations": (C.c_int, [C.c_void_p, C.c_uint32, _dp, _dp]),
     "fem_batch_set_active": (C.c_int, [C.c_void_p, _u8p]),
     "fem_batch_step_async": (C.c_int, [C.c_void_p, C.c_uint32]),
     "fem_batch_synchronize": (C.c_int, [C.c_void_p]),
@@ -463,6 +464,15 @@ class Batch:
         v = np.empty((n, 3))
         check(self.lib.fem_batch_get_state(self.h, i, _ptr(x), _ptr(v)))
         return x, v
+
+    def rotations(self, i):
+        """Rotations (T, 3, 3) and det F (T) of mesh i as of its last
+        BeginEvaluation, in the caller's element order."""
+        t = self.scenes[i].num_tets
+        R = np.empty((t, 3, 3))
+        d = np.empty(t)
+        check(self.lib.fem_batch_get_rotations(self.h, i, _ptr(R), _ptr(d)))
+        return R, d
 
     def set_active(self, mask=None):
         if mask is None:

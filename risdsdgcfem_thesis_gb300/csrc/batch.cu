@@ -129,6 +129,7 @@ struct fem_batch_s {
     Dev<double> Dinv64, vol, detF;
     Dev<uint32_t> tile_nodes, lptr0, ov_ptr, ov_map, knc_node, knc_mesh;
     std::vector<uint32_t> perm_h, inv_h;  // batch node -> caller's node, and back (global ids)
+    std::vector<uint32_t> eperm_h;        // batch element -> the caller's element index in its mesh
     Dev<uint32_t> perm;                   // perm_h on the device (whole-batch state transfers)
     Dev<double> stage_x, stage_v;         // caller-order staging for whole-batch transfers
     Dev<uchar4> lconn;
@@ -530,6 +531,7 @@ int fem_batch_finalize(fem_batch b)
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return batch_fail(FEM_E_NODEVICE, "no CUDA device");
     const bool fp64 = b->opt.precision == FEM_PRECISION_FP64;
     const uint32_t tile_cap = b->opt.tile_elems;
+    b->eperm_h.clear();
     // local nodes per tile: the mixed path's small tiles hold fewer
     const size_t node_cap = (!fp64 && tile_cap <= (uint32_t)kPipeSmallTile) ? kPipeSmallNodes : kTileNodes;
     b->M = (uint32_t)b->meshes.size();
@@ -601,6 +603,7 @@ int fem_batch_finalize(fem_batch b)
         }
         for (uint32_t k = 0; k < T; k++) {
             const uint32_t e = order[k];
+            b->eperm_h.push_back(e);
             const uint32_t* t = &hm.tets[4 * (size_t)e];
             double D[9];
             for (int i = 0; i < 3; i++) {
@@ -1114,6 +1117,43 @@ int fem_batch_get_state(fem_batch b, uint32_t mesh, double* x, double* v)
             const size_t i = b->inv_h[c.node0 + u] - c.node0;
             for (int a = 0; a < 3; a++) dst[k][3 * (size_t)u + a] = tmp[3 * i + a];
         }
+    }
+    return FEM_OK;
+}
+
+int fem_batch_get_rotations(fem_batch b, uint32_t mesh, double* R, double* detF)
+{
+    if (int e = check_ready(b)) return e;
+    if (mesh >= b->M) return batch_fail(FEM_E_ARG, "mesh %u out of range", mesh);
+    const MeshConsts& c = b->mc_host[mesh];
+    const size_t T = b->Ttot, e0 = c.elem0, n = c.T;
+    const uint32_t* perm = b->eperm_h.data() + e0;
+    if (R) {
+        const bool fp64 = b->opt.precision == FEM_PRECISION_FP64;
+        const size_t sb = fp64 ? 8 : 4;
+        std::vector<unsigned char> tmp(9 * n * sb);
+        for (int k = 0; k < 9; k++)
+            BCK(cudaMemcpyAsync(tmp.data() + k * n * sb, b->R_s.p + (k * T + e0) * sb, n * sb, cudaMemcpyDeviceToHost,
+                                b->stream));
+        BCK(cudaStreamSynchronize(b->stream));
+        for (size_t i = 0; i < n; i++)
+            for (int k = 0; k < 9; k++) {
+                double v;
+                if (fp64) {
+                    std::memcpy(&v, tmp.data() + (k * n + i) * 8, 8);
+                } else {
+                    float f;
+                    std::memcpy(&f, tmp.data() + (k * n + i) * 4, 4);
+                    v = f;
+                }
+                R[9 * (size_t)perm[i] + k] = v;
+            }
+    }
+    if (detF) {
+        std::vector<double> tmp(n);
+        BCK(cudaMemcpyAsync(tmp.data(), b->detF.p + e0, n * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
+        BCK(cudaStreamSynchronize(b->stream));
+        for (size_t i = 0; i < n; i++) detF[perm[i]] = tmp[i];
     }
     return FEM_OK;
 }
