@@ -472,11 +472,13 @@ __global__ void __launch_bounds__(256) k_mesh_alpha(BatchView<float> b, const fl
     const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
     for (uint32_t m = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; m < b.M; m += nw) {
         StepScalars& st = b.st[m];
-        if (st.done) continue;
-        // the scalars are loaded before the shares are summed (one round trip)
+        // every load that needs only the mesh id is issued before the first
+        // branch: one round trip before the shares are read
+        const uint32_t done = st.done;
         const uint32_t tile0 = b.mc[m].tile0, ntiles = b.mc[m].ntiles;
         const bool confirm = st.confirm != 0;  // measure the FP64 residual only, no CG update
         const double abs_eps_sq = st.abs_eps_sq, delta_new = st.delta_new;
+        if (done) continue;
         F2 a = {0.f, 0.f};
         for (uint32_t k = lane; k < ntiles; k += 32u) {
             const float2 w = __ldcg(tshare + tile0 + k);
@@ -606,15 +608,18 @@ __global__ void __launch_bounds__(256) k_mesh_update(BatchView<float> b, const f
     const uint32_t lane = threadIdx.x & 31u;
     const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
     for (uint32_t mesh = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; mesh < b.M; mesh += nw) {
-        if (b.st[mesh].done) continue;
+        // the mesh's scalars, copied before the first branch and before the
+        // shares are summed (one round trip for all of them), updated in
+        // registers and written back once
+        const uint32_t done = b.st[mesh].done;
         const MeshConsts& c = b.mc[mesh];
-        // the mesh's scalars, copied before the shares are summed (one round
-        // trip for all of them), updated in registers and written back once
+        const uint32_t chunk0 = c.chunk0, nchunks = c.nchunks;
         StepScalars st;
         if (lane == 0) st = b.st[mesh];
+        if (done) continue;
         F2 tot = {0.f, 0.f};
-        for (uint32_t k = lane; k < c.nchunks; k += 32u) {
-            const float2 w = __ldcg(cshare + c.chunk0 + k);
+        for (uint32_t k = lane; k < nchunks; k += 32u) {
+            const float2 w = __ldcg(cshare + chunk0 + k);
             tot = f2_add(tot, F2{w.x, w.y});
         }
         tot = warp_sum_f2(tot);
