@@ -290,7 +290,10 @@ typedef struct fem_server_options {
     uint32_t slice_iterations;   /* CG iterations per shard launch; running steps
                                     continue in the next launch, requests that
                                     arrived meanwhile start there (0 = whole steps) */
-    uint32_t pad;
+    uint32_t chunk_nodes;        /* node chunk of the shards' node passes (as
+                                    fem_batch_options.chunk_nodes; default 256: a
+                                    lone request's iterations are shorter with more,
+                                    smaller chunks) */
 } fem_server_options;
 
 typedef struct fem_server_completion {

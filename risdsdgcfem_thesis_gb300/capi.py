@@ -309,7 +309,7 @@ def _bind_batch_signatures():
 
 class FemServerOptions(C.Structure):
     _fields_ = [("precision", C.c_uint32), ("shard_max_scenes", C.c_uint32), ("shard_max_tets", C.c_uint64),
-                ("hbm_budget_bytes", C.c_uint64), ("slice_iterations", C.c_uint32), ("pad", C.c_uint32)]
+                ("hbm_budget_bytes", C.c_uint64), ("slice_iterations", C.c_uint32), ("chunk_nodes", C.c_uint32)]
 
 
 class FemServerCompletion(C.Structure):
@@ -518,7 +518,7 @@ class Server:
     a device-memory budget, size-sorted shards, continuous batching."""
 
     def __init__(self, precision=FEM_PRECISION_MIXED, hbm_budget_bytes=None, shard_max_tets=None,
-                 shard_max_scenes=None, slice_iterations=None, completion_capacity=65536):
+                 shard_max_scenes=None, slice_iterations=None, completion_capacity=65536, chunk_nodes=None):
         lib = load()
         self.lib = lib
         opt = FemServerOptions()
@@ -532,6 +532,8 @@ class Server:
             opt.shard_max_scenes = int(shard_max_scenes)
         if slice_iterations is not None:
             opt.slice_iterations = int(slice_iterations)
+        if chunk_nodes is not None:
+            opt.chunk_nodes = int(chunk_nodes)
         h = C.c_void_p()
         check(lib.fem_server_create(C.byref(opt), C.byref(h)))
         self.h = h

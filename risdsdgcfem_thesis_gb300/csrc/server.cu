@@ -152,6 +152,7 @@ int build_shard(fem_server srv, const std::vector<uint32_t>& ids, Shard& out)
     fem_batch_options o;
     fem_batch_options_default(&o);
     o.precision = srv->opt.precision;
+    if (srv->opt.chunk_nodes) o.chunk_nodes = srv->opt.chunk_nodes;
     fem_batch b = nullptr;
     if (int e = fem_batch_create(&o, &b)) return e;
     for (uint32_t k = 0; k < ids.size(); k++) {
@@ -240,6 +241,7 @@ int fem_server_options_default(fem_server_options* o)
     o->shard_max_tets = 32000000;
     o->shard_max_scenes = 2048;
     o->slice_iterations = 32;
+    o->chunk_nodes = 256;
     return FEM_OK;
 }
 
@@ -252,6 +254,8 @@ int fem_server_create(const fem_server_options* opt, fem_server* out)
     if (opt) o = *opt;
     if (o.precision != FEM_PRECISION_FP64 && o.precision != FEM_PRECISION_MIXED)
         return batch_fail(FEM_E_ARG, "unknown precision %u", o.precision);
+    if (o.chunk_nodes && (o.chunk_nodes < 32 || o.chunk_nodes > 8192))
+        return batch_fail(FEM_E_ARG, "chunk_nodes must be 0 or in [32, 8192]");
     if (o.shard_max_tets == 0 || o.shard_max_scenes == 0)
         return batch_fail(FEM_E_ARG, "shard limits must be > 0");
     fem_server s = new (std::nothrow) fem_server_s;
