@@ -1078,7 +1078,7 @@ int fem_batch_set_knc_targets(fem_batch b, uint32_t mesh, const double* targets)
 }
 
 // Per-mesh state transfers permute on the host between the caller's node
-// order and the batch's (first appearance in tile order).
+// order and the batch's (tile order).
 int fem_batch_set_state(fem_batch b, uint32_t mesh, const double* x, const double* v)
 {
     if (int e = check_ready(b)) return e;

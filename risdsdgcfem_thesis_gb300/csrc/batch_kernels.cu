@@ -2,7 +2,7 @@
 //
 // One CG iteration (Saphyre2 ns/ILSS_CG.h:90-144) over every mesh whose loop
 // is still running, in lock-step, is three kernels on the FP64 path (the
-// mixed path runs its iteration as two kernels, tile_pipe.cu):
+// mixed path runs its iteration as four kernels, tile_pipe.cu):
 //   k_tile_spmv   one CTA per element tile: the tile's node values of the
 //                 search direction d = S(r + beta d) are formed while staging
 //                 r and d in shared memory, each thread forms one element's

@@ -16,7 +16,7 @@ void launch_permute(const uint32_t* perm, uint64_t n, const double* src, double*
 
 // Arrival counters and graph handle of the fused CG finalisation.
 struct LoopSync {
-    unsigned* mcount;        // [M] per-mesh chunk arrivals
+    unsigned* mcount;        // [M] per-mesh chunk arrivals (FP64 path)
     unsigned* gcount;        // grid arrivals
     unsigned* refresh_flag;  // raised when a mesh refreshes its residual next iteration
     unsigned* body_runs;     // CG-loop body executions (launch accounting)
@@ -26,8 +26,9 @@ struct LoopSync {
     int set_cond;
 };
 
-// Mixed path, one CG iteration (tile_pipe.cu): tile product with the
-// per-mesh alpha, then the fused node update with beta and the loop test.
+// Mixed path, one CG iteration (tile_pipe.cu): the tile product (with each
+// tile's d^T A d share), then launch_node_update_fused: the per-mesh alpha,
+// the node pass and the per-mesh update (beta, loop test, work lists).
 void launch_tile_spmv_pipe(const BatchView<float>& b, const float* d, const float* r, float* part, float2* tshare,
                            cudaGraphConditionalHandle if_refresh, int set_if, const unsigned* refresh_flag,
                            unsigned* err, cudaStream_t s);
