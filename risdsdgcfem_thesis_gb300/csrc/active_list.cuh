@@ -105,6 +105,27 @@ __device__ void build_refresh_lists(const BatchView<S>& b)
         b.refresh_tiles, b.refresh_chunks, b.list_count + 4);
 }
 
+// list_count[4] when every running mesh refreshes: the refresh product walks
+// the CG list itself (no copy; its per-tile test skips the meshes that have
+// left their loop).
+constexpr uint32_t kRefreshUsesCgList = 0xffffffffu;
+
+// The refresh work list of the next iteration; `all` = every running mesh
+// refreshes (then the CG list serves and nothing is copied: in a batch whose
+// meshes started together that is every periodic refresh, while exit
+// confirmations and staggered starts give short lists). Same calling rule
+// as above.
+template <typename S>
+__device__ void set_refresh_lists(const BatchView<S>& b, bool all)
+{
+    if (all && b.act_tiles) {
+        if (threadIdx.x == 0) b.list_count[4] = kRefreshUsesCgList;
+        __syncthreads();
+    } else {
+        build_refresh_lists(b);
+    }
+}
+
 // Entry i of a work list, or i itself when the launch has no list.
 __device__ __forceinline__ uint32_t list_entry(const uint32_t* list, uint32_t i) { return list ? list[i] : i; }
 

@@ -237,9 +237,15 @@ __global__ void __launch_bounds__(256) k_tile_spmv_y64(BatchView<S> b, const dou
     __shared__ V sd[3 * kTileNodes];
     __shared__ V so[12 * kTileElems];
     // ALL: the meshes that start a step; REFRESH: the meshes that refresh in
-    // this iteration (their work list on the mixed path)
-    const uint32_t* list = mode == SPMV_Y64_ALL ? b.start_tiles : b.refresh_tiles;
-    const uint32_t n = mode == SPMV_Y64_ALL ? b.list_count[0] : (b.refresh_tiles ? b.list_count[4] : b.ntiles);
+    // this iteration (their work list on the mixed path, or the CG list when
+    // all running meshes refresh)
+    const uint32_t rc = (mode == SPMV_Y64_REFRESH && b.refresh_tiles) ? b.list_count[4] : 0u;
+    const bool cg_list = rc == kRefreshUsesCgList;
+    const uint32_t* list = mode == SPMV_Y64_ALL ? b.start_tiles : (cg_list ? b.act_tiles : b.refresh_tiles);
+    const uint32_t n = mode == SPMV_Y64_ALL ? b.list_count[0]
+                       : !b.refresh_tiles ? b.ntiles
+                       : cg_list ? *(volatile const uint32_t*)b.act_count
+                                 : rc;
     for (uint32_t i = blockIdx.x; i < n; i += gridDim.x) {
         const uint32_t t = list_entry(list, i);
         const TileMeta tm = b.tiles[t];
@@ -555,18 +561,21 @@ __device__ void grid_tail(const BatchView<S>& b, const LoopSync& ls, bool iterat
 {
     if (!arrive_last(ls.gcount, gridDim.x)) return;
     if (b.act_tiles && (!iteration || *(volatile const unsigned*)b.list_dirty)) build_active_lists(b);  // FP64 tail: no lists
-    int any = 0, refresh = 0;
+    int any = 0, refresh = 0, norf = 0;  // norf: a running mesh that does not refresh
     for (uint32_t i = threadIdx.x; i < b.M; i += blockDim.x) {
         volatile const StepScalars* sp = b.st + i;
         if (!sp->done) {
             any = 1;
-            const MeshConsts& c = b.mc[i];
-            if (sp->refresh_next) refresh = 1;
+            if (sp->refresh_next)
+                refresh = 1;
+            else
+                norf = 1;
         }
     }
     any = __syncthreads_or(any);
     refresh = __syncthreads_or(refresh);
-    if (refresh && b.refresh_tiles) build_refresh_lists(b);
+    norf = __syncthreads_or(norf);
+    if (refresh && b.refresh_tiles) set_refresh_lists(b, !norf);
     if (threadIdx.x == 0) {
         if (ls.refresh_flag) *ls.refresh_flag = refresh ? 1u : 0u;
         if (ls.body_runs) *ls.body_runs += 1u;

@@ -702,17 +702,21 @@ __global__ void __launch_bounds__(256) k_mesh_update(BatchView<float> b, const f
     // rebuild the CG lists once a quarter of their tiles belong to meshes that
     // have left their loop (the kernels skip those entries until then)
     if (4u * *(volatile const unsigned*)b.list_dirty >= *(volatile const uint32_t*)b.act_count) build_active_lists(b);
-    int any = 0, rf = 0;
+    int any = 0, rf = 0, norf = 0;  // norf: a running mesh that does not refresh
     for (uint32_t m = threadIdx.x; m < b.M; m += blockDim.x) {
         volatile const StepScalars* sp = b.st + m;
         if (!sp->done) {
             any = 1;
-            if (sp->refresh_next) rf = 1;
+            if (sp->refresh_next)
+                rf = 1;
+            else
+                norf = 1;
         }
     }
     any = __syncthreads_or(any);
     rf = __syncthreads_or(rf);
-    if (rf) build_refresh_lists(b);
+    norf = __syncthreads_or(norf);
+    if (rf) set_refresh_lists(b, !norf);
     if (threadIdx.x == 0) {
         const bool stop = ls.err && *(volatile const unsigned*)ls.err;
         bool budget_left = true;

@@ -1,6 +1,6 @@
 """The step-request server (fem_server_*) on the GPU: a scene's result is the
 same alone and in the mix under continuous batching (bit-identical to the
-scene stepped alone in its own batch), admission respects the device-memory
+scene stepped alone in its own batch with the server's node chunk), admission respects the device-memory
 budget, and shards overlap on the device."""
 import numpy as np
 import pytest
@@ -40,8 +40,10 @@ def test_server_results_alone_and_in_the_mix_are_identical(fem_lib):
     for i in range(len(pool)):
         tags = [c["tag"] for c in done if c["scene"] == ids[i]]
         assert tags == sorted(tags)
+    # the scene alone in a batch with the server's node chunk (256): the
+    # chunk size fixes the order of the |r|^2 partial sums
     for i, sc in enumerate(pool):
-        alone = fem_lib.Batch([sc], precision=fem_lib.FEM_PRECISION_MIXED, compute_energy=False)
+        alone = fem_lib.Batch([sc], precision=fem_lib.FEM_PRECISION_MIXED, compute_energy=False, chunk_nodes=256)
         its = []
         for _ in range(steps[i]):
             alone.step(1)
@@ -66,8 +68,10 @@ def test_server_short_slices_give_the_same_results(fem_lib):
         srv.pump()
     done = srv.drain()
     assert len(done) == 2 * len(pool) and all(c["status"] == 0 for c in done)
+    # the scene alone in a batch with the server's node chunk (256): the
+    # chunk size fixes the order of the |r|^2 partial sums
     for i, sc in enumerate(pool):
-        alone = fem_lib.Batch([sc], precision=fem_lib.FEM_PRECISION_MIXED, compute_energy=False)
+        alone = fem_lib.Batch([sc], precision=fem_lib.FEM_PRECISION_MIXED, compute_energy=False, chunk_nodes=256)
         alone.step(2)
         xa, va = alone.state(0)
         xs, vs = srv.state(ids[i])
