@@ -163,6 +163,7 @@ struct fem_batch_s {
         b.ntiles = ntiles;
         b.nchunks = nchunks;
         b.pipe_tile = opt.tile_elems <= (uint32_t)kPipeSmallTile ? kPipeSmallTile : kTileElems;
+        b.fuse_alpha = opt.fuse_alpha ? 1u : 0u;
         b.Ntot = (uint32_t)Ntot;
         b.Ttot = (uint32_t)Ttot;
         b.tiles = tiles.p;
@@ -1323,13 +1324,14 @@ int fem_batch_kernel_launches(fem_batch b, uint32_t steps, uint64_t* launches)
     BCK(cudaStreamSynchronize(b->stream));
     // kernels per step outside the CG loop, plus per executed CG iteration 3
     // (FP64 path) or 6 (mixed path: tile product, refresh product -- counted
-    // in every iteration, an upper bound --, mesh alpha, node pass, mesh
-    // update)
+    // in every iteration, an upper bound --, mesh alpha unless the node pass
+    // forms it, node pass, mesh update)
     bool energy = false;
     for (auto& m : b->meshes) energy |= m.p.compute_energy != 0;
     const bool mixed = b->opt.precision == FEM_PRECISION_MIXED;
     const uint64_t fixed = 8 + (b->K ? 1 : 0) + (energy ? 4 : 0);
-    *launches = (uint64_t)steps * fixed + (mixed ? 6ull : 3ull) * body_runs;
+    const uint64_t per_iter = mixed ? (b->opt.fuse_alpha ? 5ull : 6ull) : 3ull;
+    *launches = (uint64_t)steps * fixed + per_iter * body_runs;
     return FEM_OK;
 }
 

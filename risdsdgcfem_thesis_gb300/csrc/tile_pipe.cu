@@ -466,31 +466,47 @@ __global__ void __launch_bounds__(TILE, PipeShape<TILE>::kMinBlocks) k_tile_spmv
 // Per running mesh: d^T A d from its tiles' shares (fixed order), alpha and
 // the breakdown test (ILSS_CG.h:91-97), once for the node pass's blocks of
 // the mesh. One warp per mesh.
-__global__ void __launch_bounds__(256) k_mesh_alpha(BatchView<float> b, const float2* __restrict__ tshare)
+// d^T A d of mesh m from its tile shares, alpha and the breakdown test, by
+// one warp (lane-strided sum, fixed order: the same bits wherever it runs).
+// Valid in lane 0; `publish` writes them to the mesh's scalars.
+struct MeshAlpha {
+    double dq;
+    float alpha;
+    bool brk;
+};
+__device__ __forceinline__ MeshAlpha warp_mesh_alpha(const BatchView<float>& b, const float2* __restrict__ tshare,
+                                                     uint32_t m, bool publish)
 {
     const uint32_t lane = threadIdx.x & 31u;
+    StepScalars& st = b.st[m];
+    // every load that needs only the mesh id is issued before the shares
+    const uint32_t tile0 = b.mc[m].tile0, ntiles = b.mc[m].ntiles;
+    const bool confirm = st.confirm != 0;  // measure the FP64 residual only, no CG update
+    const double abs_eps_sq = st.abs_eps_sq, delta_new = st.delta_new;
+    F2 a = {0.f, 0.f};
+    for (uint32_t k = lane; k < ntiles; k += 32u) {
+        const float2 w = __ldcg(tshare + tile0 + k);
+        a = f2_add(a, F2{w.x, w.y});
+    }
+    a = warp_sum_f2(a);
+    MeshAlpha r;
+    r.dq = (double)a.hi + (double)a.lo;
+    r.brk = !confirm && ::fabs(r.dq) < abs_eps_sq;  // leave before the update
+    r.alpha = confirm ? 0.f : (float)(delta_new / r.dq);
+    if (publish && lane == 0) {
+        st.dot_dq = r.dq;
+        st.brk = r.brk ? 1u : 0u;
+        st.alpha_f = r.alpha;
+    }
+    return r;
+}
+
+__global__ void __launch_bounds__(256) k_mesh_alpha(BatchView<float> b, const float2* __restrict__ tshare)
+{
     const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
     for (uint32_t m = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; m < b.M; m += nw) {
-        StepScalars& st = b.st[m];
-        // every load that needs only the mesh id is issued before the first
-        // branch: one round trip before the shares are read
-        const uint32_t done = st.done;
-        const uint32_t tile0 = b.mc[m].tile0, ntiles = b.mc[m].ntiles;
-        const bool confirm = st.confirm != 0;  // measure the FP64 residual only, no CG update
-        const double abs_eps_sq = st.abs_eps_sq, delta_new = st.delta_new;
-        if (done) continue;
-        F2 a = {0.f, 0.f};
-        for (uint32_t k = lane; k < ntiles; k += 32u) {
-            const float2 w = __ldcg(tshare + tile0 + k);
-            a = f2_add(a, F2{w.x, w.y});
-        }
-        a = warp_sum_f2(a);
-        if (lane == 0) {
-            const double dq = (double)a.hi + (double)a.lo;
-            st.dot_dq = dq;
-            st.brk = (!confirm && ::fabs(dq) < abs_eps_sq) ? 1u : 0u;  // leave before the update
-            st.alpha_f = confirm ? 0.f : (float)(delta_new / dq);
-        }
+        if (b.st[m].done) continue;
+        (void)warp_mesh_alpha(b, tshare, m, true);
     }
 }
 
@@ -498,9 +514,12 @@ __global__ void __launch_bounds__(256) k_node_update_fused(BatchView<float> b, c
                                                            const double* __restrict__ part64,
                                                            const double* __restrict__ bv,
                                                            double* __restrict__ y, float* __restrict__ r,
-                                                           float* __restrict__ d, float2* __restrict__ cshare)
+                                                           float* __restrict__ d, float2* __restrict__ cshare,
+                                                           const float2* __restrict__ tshare)
 {
     __shared__ float2 sh[32];
+    __shared__ float s_alpha;
+    __shared__ int s_brk;
     const uint32_t n_act = *(volatile const uint32_t*)(b.act_count + 1);
     for (uint32_t ia = blockIdx.x; ia < n_act; ia += gridDim.x) {
         const uint32_t ci = b.act_chunks[ia];
@@ -508,11 +527,29 @@ __global__ void __launch_bounds__(256) k_node_update_fused(BatchView<float> b, c
         const StepScalars& sm = b.st[ch.mesh];
         if (sm.done) continue;  // left its loop; the list is rebuilt lazily
         const MeshConsts& c = b.mc[ch.mesh];
-        const bool brk = sm.brk != 0;
+        bool brk;
+        float alpha_s;
+        if (b.fuse_alpha) {
+            // this block forms its mesh's alpha (warp 0, the same sum as
+            // k_mesh_alpha); the block of the mesh's first chunk publishes it
+            if (threadIdx.x < 32) {
+                const MeshAlpha ma = warp_mesh_alpha(b, tshare, ch.mesh, ci == c.chunk0);
+                if (threadIdx.x == 0) {
+                    s_alpha = ma.alpha;
+                    s_brk = ma.brk ? 1 : 0;
+                }
+            }
+            __syncthreads();
+            brk = s_brk != 0;
+            alpha_s = s_alpha;
+        } else {
+            brk = sm.brk != 0;
+            alpha_s = sm.alpha_f;
+        }
         const bool confirm = sm.confirm != 0;
         const bool refresh = sm.refresh_next != 0;
         const float beta = sm.beta_f;
-        const float alpha_s = sm.alpha_f, na = -alpha_s;
+        const float na = -alpha_s;
         const float fK = c.fK_f, mfm = c.mfm_f;
         float acc = 0.f;
         for (size_t n = ch.n0 + threadIdx.x; !brk && n < ch.n1; n += blockDim.x) {
@@ -793,12 +830,14 @@ void launch_node_update_fused(const BatchView<float>& b, const float* part, cons
 {
     const uint32_t g = (uint32_t)node_grid();
     const uint32_t grid = b.nchunks < g ? (b.nchunks ? b.nchunks : 1) : g;
-    prof_begin("mesh_alpha", s);
-    k_mesh_alpha<<<(b.M * 32u + kNodeThreads - 1) / kNodeThreads, kNodeThreads, 0, s>>>(b, tshare);
-    prof_end("mesh_alpha", s);
-    launch_counter()++;
+    if (!b.fuse_alpha) {
+        prof_begin("mesh_alpha", s);
+        k_mesh_alpha<<<(b.M * 32u + kNodeThreads - 1) / kNodeThreads, kNodeThreads, 0, s>>>(b, tshare);
+        prof_end("mesh_alpha", s);
+        launch_counter()++;
+    }
     prof_begin("node_update_mixed", s);
-    k_node_update_fused<<<grid, kNodeThreads, 0, s>>>(b, part, part64, bv, y, r, d, cshare);
+    k_node_update_fused<<<grid, kNodeThreads, 0, s>>>(b, part, part64, bv, y, r, d, cshare, tshare);
     prof_end("node_update_mixed", s);
     launch_counter()++;
     prof_begin("mesh_update", s);

@@ -120,7 +120,7 @@ def test_server_host_validation_without_gpu(fem_lib):
     assert lib.fem_server_options_default(C.byref(opt)) == fem_lib.FEM_OK
     assert opt.precision == fem_lib.FEM_PRECISION_MIXED and opt.hbm_budget_bytes == 120 << 30
     assert opt.slice_iterations == 32
-    assert opt.chunk_nodes == 256
+    assert opt.chunk_nodes == 256 and opt.fuse_alpha == 0
     bad = fem_lib.FemServerOptions(opt.precision, opt.shard_max_scenes, opt.shard_max_tets, opt.hbm_budget_bytes)
     bad.precision = 7
     h = C.c_void_p()

@@ -351,3 +351,26 @@ def test_edge_case_meshes_vs_oracle_alone_and_in_the_mix(fem_lib, oracle, precis
         alone.close()
     x1, v1 = mix.state(1)
     assert np.array_equal(x1, edge[1].rest) and not np.any(v1)
+
+
+def test_fused_alpha_gives_the_same_bits(fem_lib):
+    """fuse_alpha (each node-pass block forms its mesh's alpha, no separate
+    kernel) runs the same fixed-order sum as the alpha kernel: states and
+    iteration counts are bit-identical to the default."""
+    rng = np.random.default_rng(21)
+    scs = [scenes.random_block(rng, lo=3, hi=8, idx=i) for i in range(5)]
+    a = fem_lib.Batch(scs, precision=fem_lib.FEM_PRECISION_MIXED, compute_energy=False)
+    f = fem_lib.Batch(scs, precision=fem_lib.FEM_PRECISION_MIXED, compute_energy=False, fuse_alpha=True)
+    try:
+        for _ in range(3):
+            a.step(1)
+            f.step(1)
+            for i in range(len(scs)):
+                assert a.stats(i)["cg_iterations"] == f.stats(i)["cg_iterations"], i
+        for i in range(len(scs)):
+            xa, va = a.state(i)
+            xf, vf = f.state(i)
+            assert np.array_equal(xa, xf) and np.array_equal(va, vf), i
+    finally:
+        a.close()
+        f.close()
