@@ -855,10 +855,11 @@ int fem_batch_finalize(fem_batch b)
                 const size_t e = tm.e0 + i;
                 put(0, i, 1.f); put(4, i, 1.f); put(8, i, 1.f);  // R = I
                 for (uint32_t c = 0; c < 9; c++) put(9 + c, i, (float)Dinv_soa[c * T + e]);
-                for (uint32_t c = 0; c < 3; c++) put(18 + c, i, (float)mat_soa[c * T + e]);
+                put(18, i, (float)mat_soa[T + e]);      // V lambda
+                put(19, i, (float)mat_soa[2 * T + e]);  // V mu
                 const uchar4 lc = lconn[e];
                 const uint32_t w = (uint32_t)lc.x | ((uint32_t)lc.y << 8) | ((uint32_t)lc.z << 16) | ((uint32_t)lc.w << 24);
-                std::memcpy(base + blob_comp_off(21, i, ne4), &w, 4);
+                std::memcpy(base + blob_comp_off(20, i, ne4), &w, 4);
             }
             uint16_t* lp = reinterpret_cast<uint16_t*>(base + blob_lptr_off(tm.ne));
             const uint16_t* src_lp = lptr.data() + lptr0[t];

@@ -47,11 +47,12 @@ constexpr int kPipeSmallNodes = 120;
 constexpr int kNodeThreads = 256;  // threads per node-kernel block
 
 // Layout of a tile's blob (mixed path, see tile_pipe.cu): the element data,
-// 22 FP32 components per element (R 0-8, Dm^-1 9-17, V(lambda+2mu),
-// V lambda, V mu, local ids as one word) grouped by four: group g < 5 holds
-// components 4g..4g+3 as float4[ne4], group 5 components 20, 21 as
-// float2[ne4] (one 16- or 8-byte load per group and element, consecutive
-// elements in consecutive words); then uint16 lptr[nn+1], uint16 lidx[4 ne],
+// 21 FP32 components per element (R 0-8, Dm^-1 9-17, V lambda, V mu, local
+// ids as one word; V(lambda+2mu) = V lambda + 2 V mu is formed in the
+// kernel) grouped by four: group g < 5 holds components 4g..4g+3 as
+// float4[ne4], component 20 follows as a word per element (one 16- or 4-byte
+// load per group and element, consecutive elements in consecutive words);
+// then uint16 lptr[nn+1], uint16 lidx[4 ne],
 // and, 4-aligned, the header {uint32 own0, float fK, float m fM} (the partial
 // slot of the first owned node, the mesh's FP32 factors) and uint32
 // ovslot[nn - nown] (the partial slots of the shared local nodes).
@@ -59,9 +60,9 @@ __host__ __device__ constexpr uint32_t blob_ne4(uint32_t ne) { return (ne + 3u) 
 // Byte offset of component c of element i.
 __host__ __device__ constexpr uint32_t blob_comp_off(uint32_t c, uint32_t i, uint32_t ne4)
 {
-    return c < 20u ? 16u * ((c >> 2) * ne4 + i) + 4u * (c & 3u) : 80u * ne4 + 8u * i + 4u * (c - 20u);
+    return c < 20u ? 16u * ((c >> 2) * ne4 + i) + 4u * (c & 3u) : 80u * ne4 + 4u * i;
 }
-__host__ __device__ constexpr uint32_t blob_lptr_off(uint32_t ne) { return 88u * blob_ne4(ne); }
+__host__ __device__ constexpr uint32_t blob_lptr_off(uint32_t ne) { return 84u * blob_ne4(ne); }
 __host__ __device__ constexpr uint32_t blob_hdr_off(uint32_t ne, uint32_t nn)
 {
     return (blob_lptr_off(ne) + 2u * (nn + 1u) + 8u * ne + 3u) & ~3u;

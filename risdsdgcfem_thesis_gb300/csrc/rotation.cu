@@ -96,8 +96,10 @@ __device__ __forceinline__ bool rotation_fp32(const double* F, float tol, S* Rs)
     return true;
 }
 
+// Three resident blocks per SM (80 registers): the double-float MSVD's long
+// dependency chains need the extra warps more than the registers.
 template <typename S>
-__global__ void k_begin_eval_batch(BatchView<S> b, const double* __restrict__ x)
+__global__ void __launch_bounds__(256, 3) k_begin_eval_batch(BatchView<S> b, const double* __restrict__ x)
 {
     __shared__ unsigned s_inv, s_res;
     const uint32_t n = b.list_count[0];

@@ -36,11 +36,11 @@
 //
 // Blob of a tile with ne elements (ne4 = ne rounded up to 4) and nn local
 // nodes, offsets from the blob start:
-//   0            element data, 22 FP32 components per element: R (9),
-//                Dm^-1 (9), V(lambda+2mu), V lambda, V mu, local ids (uchar4
-//                as one word), in groups of four: float4 g[5][ne4] (components
-//                0-19), float2 [ne4] (components 20, 21)
-//   88 ne4       uint16 lptr[nn+1]      tile-local CSR offsets
+//   0            element data, 21 FP32 components per element: R (9),
+//                Dm^-1 (9), V lambda, V mu, local ids (uchar4 as one word), in
+//                groups of four: float4 g[5][ne4] (components 0-19), then
+//                uint32 [ne4] (component 20); V(lambda+2mu) = V lambda + 2 V mu
+//   84 ne4       uint16 lptr[nn+1]      tile-local CSR offsets
 //   + 2(nn+1)    uint16 lidx[4 ne]      slot * ne4 + element, element order
 //   (4-aligned)  uint32 own0; float fK, m fM   partial slot of the first owned
 //                                         node (local node i < nown -> part[own0 + i]);
@@ -207,9 +207,9 @@ __device__ __forceinline__ void finish_stats_t(StepScalars& s)
 // Shared memory of a block of the TILE-thread kernel: two blob stages (a
 // tile's element outputs overwrite its element data once every element has
 // read it), the staged direction sd4[nodes], two mbarriers and the warps'
-// shares and the previous tile's id. TILE = 256: 55.1 KB, four resident
-// blocks per SM; TILE = 128 (at most 120 local nodes): 27.4 KB, eight (with
-// the 1 KB each block reserves, 227 of the SM's 228 KB).
+// shares and the previous tile's id. TILE = 256: 53.1 KB, four resident
+// blocks per SM; TILE = 128 (at most 120 local nodes): 26.4 KB, eight (with
+// the 1 KB each block reserves, 219 of the SM's 228 KB).
 template <int TILE>
 struct PipeShape {
     static constexpr uint32_t kNodes = TILE == kPipeSmallTile ? (uint32_t)kPipeSmallNodes : (uint32_t)kTileNodes;
@@ -217,7 +217,7 @@ struct PipeShape {
     static constexpr uint32_t kSmem = 2 * kStage + 16u * kNodes + 16u + 8u * (TILE / 32) + 16u;
     static constexpr int kMinBlocks = TILE == kPipeSmallTile ? 8 : 4;
 };
-static_assert(PipeShape<256>::kStage == 26128 && PipeShape<128>::kStage == 13024, "stage sizes");
+static_assert(PipeShape<256>::kStage == 25104 && PipeShape<128>::kStage == 12512, "stage sizes");
 static_assert(8 * (((PipeShape<128>::kSmem + 127) & ~127u) + 1024) <= 233472, "eight small blocks per SM");
 
 // What a block needs to know of one tile before its blob arrives.
@@ -375,11 +375,10 @@ __global__ void __launch_bounds__(TILE, PipeShape<TILE>::kMinBlocks) k_tile_spmv
         if (work && tid < ne) {
             const float4* g4 = reinterpret_cast<const float4*>(stage) + tid;
             const float4 q0 = g4[0], q1 = g4[ne4], q2 = g4[2 * ne4], q3 = g4[3 * ne4], q4 = g4[4 * ne4];
-            const float2 q5 = reinterpret_cast<const float2*>(stage + 80u * ne4)[tid];
+            const uint32_t lw = reinterpret_cast<const uint32_t*>(stage + 80u * ne4)[tid];
             const float R[9] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w, q2.x};
             const float Di[9] = {q2.y, q2.z, q2.w, q3.x, q3.y, q3.z, q3.w, q4.x, q4.y};
-            const float k1 = q4.z, knu = q4.w, k2 = q5.x;
-            const uint32_t lw = __float_as_uint(q5.y);
+            const float knu = q4.z, k2 = q4.w, k1 = __fmaf_rn(2.f, k2, knu);
             const int ids[4] = {(int)(lw & 0xff), (int)((lw >> 8) & 0xff), (int)((lw >> 16) & 0xff),
                                 (int)(lw >> 24)};
             float dl[12];
