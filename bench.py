@@ -309,6 +309,45 @@ def plain_fp64_comparator(steps=3):
             "ms_per_step": ms / steps}
 
 
+def fie_leg(n=40, steps=2, cpu_n=16):
+    """The fully-implicit Euler integrator (Newton on Delta x, 3 Newton
+    iterations per step, Step_FullyImplicitEuler_dx) on the FP64 solid: the
+    n^3 block, wall clock per step (the Newton loop reads |b_k| and |y_k| on
+    the host), beside the oracle restatement's single-thread rate on the
+    cpu_n^3 block (one step)."""
+    import dataclasses
+    import torch
+    from risdsdgcfem_thesis_gb300 import capi, scenes
+    sc = dataclasses.replace(scenes.large_block(n=n), integrator=capi.FEM_INTEGRATOR_FIE_DX)
+    s = capi.Solid(sc, compute_energy=True)
+    s.step(1)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    st = [s.step(1) for _ in range(steps)]
+    wall = time.perf_counter() - t0
+    s.close()
+    cg = sum(x["cg_iterations"] for x in st)
+    out = {"value": sc.num_tets * cg / wall, "unit": UNIT, "steps": steps, "ms_per_step": 1e3 * wall / steps,
+           "workload": f"{sc.name} ({sc.num_tets} tets), FP64 solid, integrator FIE_DX, nr_max_iter 3",
+           "newton_iterations_per_step": [x["nr_iterations"] for x in st],
+           "cg_iterations_per_step": [x["cg_iterations"] for x in st]}
+    if cpu_n:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import pyoracle
+        pyoracle.build()
+        small = dataclasses.replace(scenes.large_block(n=cpu_n), integrator=1)
+        o = pyoracle.Solid(small, "port")
+        t0 = time.perf_counter()
+        so = o.step()
+        cs = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": small.num_tets * so["iters"] / cs, "unit": UNIT, "cores": 1, "kind": "port",
+                               "sample": f"one FIE step of {small.name} ({small.num_tets} tets, {so['nr_iters']} "
+                                         f"Newton iterations, {so['iters']} CG iterations, {cs:.1f} s) on one "
+                                         "thread; oracle restatement, bit-exact with the reference's "
+                                         "translation units under the restated Leaf driver"}
+    return out
+
+
 def run_ours(args):
     import torch
     from risdsdgcfem_thesis_gb300 import capi
@@ -392,6 +431,7 @@ def run_ours(args):
     batch.close()
 
     plain = None
+    fie = None
     cpu = None
     served = None
     compression = None
@@ -402,6 +442,8 @@ def run_ours(args):
             served = served_leg(args.served_rate, args.served_seconds, pool_count=args.served_pool)
         if not args.no_plain:
             plain = plain_fp64_comparator(3)
+        if not args.no_fie:
+            fie = fie_leg()
         if not args.no_cpu:
             sample = cpu_sample_set(scs, 1_500_000)
             threads = (os.cpu_count() or 1) if len(sample) > 1 else 1
@@ -450,6 +492,7 @@ def run_ours(args):
                                    "note": "whole-job tet.CG-iter/s x algorithmic bytes of one CG "
                                            "iteration (16 + 20 s_e per tet + 33 s_v per node)"},
             "plain_fp64_gpu": plain,
+            "fie_fp64_gpu": fie,
             "cpu_baseline": cpu,
             "served": served,
             "compression": compression,
@@ -602,6 +645,7 @@ def main():
     ap.add_argument("--workload", default="batch1024")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-fie", action="store_true", help="skip the fully-implicit Euler leg")
     ap.add_argument("--no-graph", action="store_true", help="launch kernels one by one (for per-kernel profilers)")
     ap.add_argument("--no-served", action="store_true")
     ap.add_argument("--no-compression", action="store_true")

@@ -47,13 +47,30 @@ enum fem_precision {
     FEM_PRECISION_MIXED = 1
 };
 
+/* Time integrators of LeafDSH_Solid3D_FEM::FixedStep
+ * (LeafDSH_Solid3D_FEM.cpp:944-963; Params::EIntegratorType,
+ * LeafDSH_Solid3D_FEM.h:110). */
+enum fem_integrator {
+    /* Step_QuasiImplicitEuler_v (LeafDSH_Solid3D_FEM.cpp:1205-1328): one
+     * linearised solve for v^{n+1} per step. The reference default. */
+    FEM_INTEGRATOR_QIE_V = 0,
+    /* Step_FullyImplicitEuler_dx(dt) (LeafDSH_Solid3D_FEM.cpp:1357-1552):
+     * Newton on Delta x = x^{n+1} - x^n, the rotations and the elastic force
+     * re-evaluated at every Newton iterate, up to nr_max_iter iterations,
+     * stopping when |b_k| < nr_abs_epsilon. FP64 solid only. */
+    FEM_INTEGRATOR_FIE_DX = 1,
+    /* Step_FullyImplicitEuler_dx(0): the same Newton loop without inertia
+     * (quasi-static equilibrium; velocities become zero). FP64 solid only. */
+    FEM_INTEGRATOR_FIE_DX_QUASISTATIC = 2
+};
+
 /* Solid parameters. Mirrors bs::Solid3D::Params and Params_Extra
  * (Saphyre2 bs/Solid3D.h:27-85) for the fields this path reads:
  * FixedDT, Density, YoungModulus, PoissonRatio, DampingRatio, Gravity,
- * LS_Iter, LS_RelEpsilon, and the Leaf's LS abs epsilon
- * (LeafDSH_Solid3D_FEM.h:209-231). Methods are fixed to the reference
- * defaults: material C_WRP, rotation MSVD, truncated differentials,
- * QuasiImplicitEuler_v integrator, CG solver with warm start. */
+ * LS_Iter, LS_RelEpsilon, and the Leaf's LS abs epsilon, integrator and NR
+ * settings (LeafDSH_Solid3D_FEM.h:209-241). Methods are fixed to the
+ * reference defaults: material C_WRP, rotation MSVD, truncated
+ * differentials, CG solver with warm start. */
 typedef struct fem_params {
     double fixed_dt;          /* time step of one FixedStep [s] */
     double density;           /* rho [kg/m^3]; node mass = rho * sum(V_e) / N */
@@ -84,14 +101,18 @@ typedef struct fem_params {
                                  isotropic); 1 = rotations in FP32, re-solved so where
                                  det F <= degenerate_det_F, a branch decision was a near
                                  tie or rotation_check flags them */
+    uint32_t integrator;      /* enum fem_integrator; the batch and server paths take QIE_V only */
+    uint32_t nr_max_iter;     /* FIE: Newton iteration cap per step (m_SolverNR_MaxIter) */
     uint32_t pad;
+    double nr_abs_epsilon;    /* FIE: Newton stops once |b_k| < this (m_SolverNR_AbsEpsilon) */
 } fem_params;
 
 /* Per-step statistics (the Leaf's per-step LS stats, LeafDSH_Solid3D_FEM.h:597-622). */
 typedef struct fem_step_stats {
-    uint32_t cg_iterations;   /* ILSS_CG::GetNumIterations of the last step */
+    uint32_t cg_iterations;   /* ILSS_CG::GetNumIterations of the last step (FIE: summed over
+                                 its Newton iterations, as m_SolverLS_NumIter) */
     uint32_t status;          /* enum fem_status of the last step */
-    double rel_residual;      /* sqrt(delta_new / delta_0) */
+    double rel_residual;      /* sqrt(delta_new / delta_0) (FIE: of the last solve; 0 if none ran) */
     double abs_residual;      /* sqrt(delta_new) */
     double elastic_energy;    /* TetrahedronElementSet3::V after the step */
     double potential_energy;  /* LeafDSH_Solid3D_FEM::RecomputeEnergy's potential term */
@@ -99,6 +120,10 @@ typedef struct fem_step_stats {
     uint32_t fp64_resolved;   /* mixed: elements whose rotation was re-solved at double
                                  precision (every element with rotation_fp32 = 0) */
     uint64_t total_cg_iterations; /* sum over the steps of this call */
+    uint32_t nr_iterations;   /* FIE: Newton iterations of the last step (m_SolverNR_NumIter); 0 for QIE */
+    uint32_t pad;
+    double nr_rel_residual;   /* FIE: last |y_k| (or |b_k| when it converged) over the first |b_0| */
+    double nr_abs_residual;   /* FIE: that last |y_k| or |b_k| (m_SolverNR_AbsPrec) */
 } fem_step_stats;
 
 typedef struct fem_solid_s* fem_solid;
@@ -106,7 +131,8 @@ typedef struct fem_solid_s* fem_solid;
 /* Fills the reference defaults (fem::Params, LeafDSH_Solid3D_FEM::Params):
  * fixed_dt 0.001, density 1000, E 1000, nu 0.25, damping 1, gravity 0,
  * CG rel 1e-3, abs 1e-6, 20 iterations, FP64, threshold 1e-3, refresh 50,
- * energy on, rotation check 1e-3, refresh every 50 iterations (no drop rule). */
+ * energy on, rotation check 1e-3, refresh every 50 iterations (no drop rule),
+ * QIE_V integrator, 3 Newton iterations with abs epsilon 1e-6. */
 int fem_params_default(fem_params* p);
 
 /* Replaces: EditableTetrahedronElementSet3::BeginEdition/AddElement/EndEdition
@@ -177,7 +203,9 @@ int fem_solid_apply_A_noalloc(fem_solid s, double factor_M, double factor_K, con
 
 /* --- Device-resident timing hooks (state stays in HBM) --- */
 /* Enqueue nsteps on the handle's stream without synchronising and without
- * host copies; stats are left on the device. */
+ * host copies; stats are left on the device. (The CG loop condition is read
+ * once per chunk of iterations; the FIE integrators also read |b_k| and
+ * |y_k| once per Newton iteration, so their steps return when done.) */
 int fem_solid_step_async(fem_solid s, uint32_t nsteps);
 int fem_solid_synchronize(fem_solid s, fem_step_stats* stats);
 /* The handle's CUDA stream (a cudaStream_t) for event timing. */

@@ -419,6 +419,12 @@ struct orc_solid {
     vec3 *knc_pos, *knc_vel;
     uint32_t last_iters;
     double last_rel, last_abs, elastic_energy, potential_energy;
+    /* fully-implicit Euler (LeafDSH_Solid3D_FEM::Params, LeafDSH_Solid3D_FEM.h:110,233-241) */
+    uint32_t integrator, nr_max_iter;
+    double nr_abs_eps;
+    vec3 *xk, *vk;        /* Newton iterates x_k, v_k (m_IE_vec_x_k, m_IE_vec_v_k) */
+    uint32_t nr_iters;
+    double nr_rel, nr_abs;
 };
 
 static vec3 load3(const double* p) { return v3(p[0], p[1], p[2]); }
@@ -447,6 +453,11 @@ orc_solid* orc_solid_create(uint32_t N, const double* rest, uint32_t T, const ui
     s->r = (double*)malloc(sizeof(double) * 3 * N);
     s->d = (double*)malloc(sizeof(double) * 3 * N);
     s->q = (double*)malloc(sizeof(double) * 3 * N);
+    s->xk = (vec3*)calloc(N, sizeof(vec3));
+    s->vk = (vec3*)calloc(N, sizeof(vec3));
+    s->integrator = FEM_ORC_QIE_V;
+    s->nr_max_iter = 3;
+    s->nr_abs_eps = 1e-6;
     for (uint32_t i = 0; i < N; i++) s->ref_pos[i] = s->x[i] = s->prev_x[i] = load3(rest + 3 * i);
     memcpy(s->tets, tets, sizeof(uint32_t) * 4 * (size_t)T);
     /* EditableTetrahedronElementSet3::EndEdition (TetrahedronElementSet3.cpp:2113-2166) */
@@ -502,7 +513,7 @@ void orc_solid_destroy(orc_solid* s)
     if (!s) return;
     free(s->ref_pos); free(s->tets); free(s->volume); free(s->inv_Dm); free(s->K); free(s->R);
     free(s->detF); free(s->x); free(s->prev_x); free(s->v); free(s->b); free(s->y);
-    free(s->r); free(s->d); free(s->q);
+    free(s->r); free(s->d); free(s->q); free(s->xk); free(s->vk);
     free(s->knc_nid); free(s->knc_pos); free(s->knc_vel);
     free(s);
 }
@@ -561,16 +572,18 @@ void orc_solid_get_state(const orc_solid* s, double* x, double* v)
 /* BeginEvaluation for C_WRP + MSVD (TetrahedronElementSet3.cpp:219-281,777-792):
  * Ds, F = Ds * Dm^-1, det F, R. The degeneration bookkeeping (DoC) does not
  * feed this path and is not formed. */
-static void begin_evaluation(orc_solid* s)
+static void begin_evaluation_at(orc_solid* s, const vec3* x)
 {
     for (uint32_t e = 0; e < s->T; e++) {
         const uint32_t* t = s->tets + 4 * (size_t)e;
-        mat3 Ds = compute_D(s->x[t[0]], s->x[t[1]], s->x[t[2]], s->x[t[3]]);
+        mat3 Ds = compute_D(x[t[0]], x[t[1]], x[t[2]], x[t[3]]);
         mat3 F = m_mul(&Ds, &s->inv_Dm[e]);
         s->detF[e] = m_det(&F);
         s->R[e] = rotation_msvd(&F);
     }
 }
+
+static void begin_evaluation(orc_solid* s) { begin_evaluation_at(s, s->x); }
 
 /* C_f_e (TetrahedronElementSet3.cpp:1053-1096): f_i -= R sum_j K_ij (R^T x_j - r_j) */
 static void f_e_acc(const orc_solid* s, const vec3* x, vec3* f)
@@ -624,6 +637,19 @@ static double elastic_V(const orc_solid* s)
         }
     }
     return 0.5 * acc_twice_V;
+}
+
+/* RecomputeEnergy, potential part (LeafDSH_Solid3D_FEM.cpp:1554-1584) */
+static double potential_energy(const orc_solid* s)
+{
+    double pe = 0;
+    for (uint32_t e = 0; e < s->T; e++) {
+        const uint32_t* t = s->tets + 4 * (size_t)e;
+        double element_mass = s->density * s->volume[e];
+        vec3 sum = v_add(v_add(v_add(s->x[t[0]], s->x[t[1]]), s->x[t[2]]), s->x[t[3]]);
+        pe += (element_mass / 4.0) * v_dot(sum, v_neg(s->gravity));
+    }
+    return pe;
 }
 
 /* LS_ZeroKNC (LeafDSH_Solid3D_FEM.cpp:1045-1053) */
@@ -690,8 +716,77 @@ static void cg_solve(orc_solid* s, double* x, const double* b)
     s->last_abs = mal_sqrt(delta_new);
 }
 
+/* real_array::norm_2 (src/Saphyre2/ns/real_array.h:97-98) */
+static double norm_2(const double* v, uint32_t n)
+{
+    double res = 0;
+    for (uint32_t i = 0; i < n; i++) res += v[i] * v[i];
+    return mal_sqrt(res);
+}
+
+/* Step_FullyImplicitEuler_dx (LeafDSH_Solid3D_FEM.cpp:1357-1552) with h = dt,
+ * or h = 0 for the quasi-static variant (FixedStep, :958-959). The Newton
+ * iterates live in xk/vk; the model's x, v stay x^n, v^n until the end. No
+ * contacts, CGS or the commented-out f_d; f_p is empty in the reference
+ * (TetrahedronElementSet3.cpp:350-353). Warm start on (the Params default). */
+static void step_fie(orc_solid* s, double h)
+{
+    const uint32_t N = s->N;
+    const double inv_dt = (h == 0) ? 0 : 1.0 / h;
+    const double mass = 1.0 / s->inv_mass;
+    for (uint32_t i = 0; i < N; i++) { s->xk[i] = s->x[i]; s->vk[i] = s->v[i]; }
+    uint32_t nr_k = 0, ls_iters = 0;
+    double nr_delta_new = 0, nr_delta_0 = -1;
+    int converged1 = 0;
+    s->last_iters = 0;
+    s->last_rel = s->last_abs = 0;
+    do {
+        for (uint32_t i = 0; i < N; i++) s->b[i] = v3(0, 0, 0);
+        for (uint32_t i = 0; i < N; i++) s->b[i] = v_add(s->b[i], v_scale(mass, s->gravity));
+        f_e_acc(s, s->xk, s->b);
+        for (uint32_t i = 0; i < N; i++)
+            s->b[i] = v_add(s->b[i], v_scale(inv_dt * mass, v_sub(s->v[i], v_scale(inv_dt, v_sub(s->xk[i], s->x[i])))));
+        if (nr_k == 0) for (uint32_t i = 0; i < N; i++) s->y[i] = v_scale(h, s->v[i]);
+        else memset(s->y, 0, sizeof(vec3) * N);
+        for (uint32_t k = 0; k < s->n_knc; k++) {
+            uint32_t nid = s->knc_nid[k];
+            /* the KNC velocity bookkeeping (:1448-1456) does not feed this integrator */
+            vec3 vk = v_scale(inv_dt, v_sub(s->knc_pos[k], s->x[nid]));
+            double norm_vk = v_norm(vk);
+            if (norm_vk > (double)0.001f) {
+                double clamp = (norm_vk < 50.0) ? norm_vk : 50.0;
+                s->knc_vel[k] = v_scale(clamp, v_normalized(vk));
+            } else {
+                s->knc_vel[k] = v3(0, 0, 0);
+            }
+            s->b[nid] = v_sub(s->knc_pos[k], s->xk[nid]);
+            s->y[nid] = v_sub(s->knc_pos[k], s->xk[nid]);
+        }
+        nr_delta_new = norm_2((const double*)s->b, 3 * N);
+        if (nr_delta_0 < 0) nr_delta_0 = nr_delta_new;
+        converged1 = nr_delta_new < s->nr_abs_eps;
+        if (!converged1) {
+            s->factor_M = inv_dt * inv_dt + inv_dt * s->rayleigh[0];
+            s->factor_K = 1.0 + inv_dt * s->rayleigh[1];
+            cg_solve(s, (double*)s->y, (const double*)s->b);
+            ls_iters += s->last_iters;
+            for (uint32_t i = 0; i < N; i++) s->xk[i] = v_add(s->xk[i], s->y[i]);
+            for (uint32_t i = 0; i < N; i++) s->vk[i] = v_scale(inv_dt, v_sub(s->xk[i], s->x[i]));
+            nr_delta_new = norm_2((const double*)s->y, 3 * N);
+            nr_k++;
+            begin_evaluation_at(s, s->xk);
+        }
+    } while (!converged1 && nr_k < s->nr_max_iter);
+    s->nr_iters = nr_k;
+    s->nr_rel = (nr_delta_0 > 0) ? nr_delta_new / nr_delta_0 : 0;
+    s->nr_abs = nr_delta_new;
+    s->last_iters = ls_iters;
+    for (uint32_t i = 0; i < N; i++) { s->x[i] = s->xk[i]; s->v[i] = s->vk[i]; }
+}
+
 /* FixedStep (LeafDSH_Solid3D_FEM.cpp:898-990) with
- * Step_QuasiImplicitEuler_v (LeafDSH_Solid3D_FEM.cpp:1205-1328). */
+ * Step_QuasiImplicitEuler_v (LeafDSH_Solid3D_FEM.cpp:1205-1328) or
+ * Step_FullyImplicitEuler_dx (:1357-1552). */
 void orc_solid_fixed_step(orc_solid* s)
 {
     g_math = s->math;
@@ -699,6 +794,12 @@ void orc_solid_fixed_step(orc_solid* s)
     const double dt = s->dt;
     begin_evaluation(s);
     for (uint32_t i = 0; i < N; i++) s->prev_x[i] = s->x[i];
+    if (s->integrator != FEM_ORC_QIE_V) {
+        step_fie(s, s->integrator == FEM_ORC_FIE_DX_QUASISTATIC ? 0.0 : dt);
+        s->elastic_energy = elastic_V(s);
+        s->potential_energy = potential_energy(s);
+        return;
+    }
     double inv_dt = 1.0 / dt;
     double mass = 1.0 / s->inv_mass;
     for (uint32_t i = 0; i < N; i++) s->b[i] = v3(0, 0, 0);
@@ -728,15 +829,21 @@ void orc_solid_fixed_step(orc_solid* s)
         s->x[i] = v_add(s->x[i], v_scale(dt, s->y[i]));
     }
     s->elastic_energy = elastic_V(s);
-    /* RecomputeEnergy, potential part (LeafDSH_Solid3D_FEM.cpp:1554-1584) */
-    double pe = 0;
-    for (uint32_t e = 0; e < s->T; e++) {
-        const uint32_t* t = s->tets + 4 * (size_t)e;
-        double element_mass = s->density * s->volume[e];
-        vec3 sum = v_add(v_add(v_add(s->x[t[0]], s->x[t[1]]), s->x[t[2]]), s->x[t[3]]);
-        pe += (element_mass / 4.0) * v_dot(sum, v_neg(s->gravity));
-    }
-    s->potential_energy = pe;
+    s->potential_energy = potential_energy(s);
+}
+
+void orc_solid_set_integrator(orc_solid* s, uint32_t integrator, uint32_t nr_max_iter, double nr_abs_eps)
+{
+    s->integrator = integrator;
+    s->nr_max_iter = nr_max_iter;
+    s->nr_abs_eps = nr_abs_eps;
+}
+
+void orc_solid_last_nr_stats(const orc_solid* s, uint32_t* nr_iters, double* nr_rel, double* nr_abs)
+{
+    if (nr_iters) *nr_iters = s->integrator == FEM_ORC_QIE_V ? 0 : s->nr_iters;
+    if (nr_rel) *nr_rel = s->integrator == FEM_ORC_QIE_V ? 0 : s->nr_rel;
+    if (nr_abs) *nr_abs = s->integrator == FEM_ORC_QIE_V ? 0 : s->nr_abs;
 }
 
 void orc_solid_last_stats(const orc_solid* s, uint32_t* iters, double* rel_res, double* abs_res,

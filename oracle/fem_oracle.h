@@ -3,7 +3,8 @@
  * A plain-C restatement of the reference's FP64 corotational linear-tet
  * implicit-Euler step (Saphyre2: TetrahedronElementSet3 with C_WRP + MSVD +
  * truncated differentials, ILSS_CG, LeafDSH_Solid3D_FEM::FixedStep with the
- * quasi-implicit Euler "v" integrator). Each function in fem_oracle.c cites
+ * quasi-implicit Euler "v" integrator or the fully-implicit Euler "dx"
+ * Newton integrator). Each function in fem_oracle.c cites
  * the reference file:line it follows and keeps the reference's operation
  * order, so that it reproduces the reference bit-for-bit on the same host.
  *
@@ -36,6 +37,8 @@ extern "C" {
 #endif
 
 enum { FEM_ORC_MATH_DOUBLE = 0, FEM_ORC_MATH_FLOAT_LITERAL = 1 };
+/* LeafDSH_Solid3D_FEM::Params::EIntegratorType values this oracle steps */
+enum { FEM_ORC_QIE_V = 0, FEM_ORC_FIE_DX = 1, FEM_ORC_FIE_DX_QUASISTATIC = 2 };
 
 typedef struct orc_solid orc_solid;
 
@@ -54,6 +57,10 @@ void orc_solid_set_knc_targets(orc_solid* s, const double* targets);
 void orc_solid_set_state(orc_solid* s, const double* x, const double* v);
 void orc_solid_get_state(const orc_solid* s, double* x, double* v);
 void orc_solid_fixed_step(orc_solid* s);
+/* Integrator (FEM_ORC_*), Newton iteration cap and |b_k| epsilon (FIE only). */
+void orc_solid_set_integrator(orc_solid* s, uint32_t integrator, uint32_t nr_max_iter, double nr_abs_eps);
+/* Newton iterations, |last| / |b_0| and |last| of the last FIE step (0 for QIE). */
+void orc_solid_last_nr_stats(const orc_solid* s, uint32_t* nr_iters, double* nr_rel, double* nr_abs);
 void orc_solid_last_stats(const orc_solid* s, uint32_t* iters, double* rel_res, double* abs_res,
                           double* elastic_energy, double* potential_energy);
 

@@ -79,6 +79,8 @@ def _load(path: str, prefix: str):
     fn("solid_rayleigh").argtypes = [C.c_void_p, _dp]
     fn("solid_node_mass").argtypes = [C.c_void_p]
     fn("solid_node_mass").restype = C.c_double
+    fn("solid_set_integrator").argtypes = [C.c_void_p, C.c_uint32, C.c_uint32, C.c_double]
+    fn("solid_last_nr_stats").argtypes = [C.c_void_p, _up, _dp, _dp]
     if P == "orc_":
         lib.orc_solid_begin_eval.argtypes = [C.c_void_p, _dp]
         lib.orc_solid_rotations.argtypes = [C.c_void_p, _dp]
@@ -146,6 +148,9 @@ class Solid:
         if scene.init_vel is not None:
             v = _f64(scene.init_vel)
             getattr(self.lib, self.p + "solid_set_state")(self.h, None, _ptr(v))
+        if getattr(scene, "integrator", 0):
+            getattr(self.lib, self.p + "solid_set_integrator")(self.h, scene.integrator, scene.nr_max_iter,
+                                                                scene.nr_abs_eps)
         self.step_index = 0
 
     def __del__(self):
@@ -179,8 +184,12 @@ class Solid:
         rel, ab, ee, pe = C.c_double(), C.c_double(), C.c_double(), C.c_double()
         getattr(self.lib, self.p + "solid_last_stats")(self.h, C.byref(it), C.byref(rel), C.byref(ab),
                                                         C.byref(ee), C.byref(pe))
+        nr_it = C.c_uint32()
+        nr_rel, nr_abs = C.c_double(), C.c_double()
+        getattr(self.lib, self.p + "solid_last_nr_stats")(self.h, C.byref(nr_it), C.byref(nr_rel), C.byref(nr_abs))
         return {"iters": it.value, "rel_res": rel.value, "abs_res": ab.value,
-                "elastic_energy": ee.value, "potential_energy": pe.value}
+                "elastic_energy": ee.value, "potential_energy": pe.value,
+                "nr_iters": nr_it.value, "nr_rel": nr_rel.value, "nr_abs": nr_abs.value}
 
     def run(self, steps=None):
         steps = self.scene.steps if steps is None else steps

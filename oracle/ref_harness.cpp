@@ -101,6 +101,12 @@ struct ref_solid {
     Real factor_M, factor_K;
     unsigned last_iters;
     Real last_rel, last_abs;
+    // fully-implicit Euler (LeafDSH_Solid3D_FEM.h:110,233-241)
+    unsigned integrator, nr_max_iter;
+    Real nr_abs_eps;
+    std::vector<Vec3> xk, vk;  // m_IE_vec_x_k, m_IE_vec_v_k
+    unsigned nr_iters;
+    Real nr_rel, nr_abs;
 };
 
 static Vec3 V3(const double* p) { return Vec3(Real(p[0]), Real(p[1]), Real(p[2])); }
@@ -219,6 +225,10 @@ ref_solid* ref_solid_create(unsigned N, const double* rest, unsigned T, const ui
     s->y.assign(N, Vec3::Zero());
     s->cg.Init(3 * N);
     s->last_iters = 0; s->last_rel = s->last_abs = 0;
+    s->integrator = 0; s->nr_max_iter = 3; s->nr_abs_eps = Real(1e-6);
+    s->xk.assign(N, Vec3::Zero());
+    s->vk.assign(N, Vec3::Zero());
+    s->nr_iters = 0; s->nr_rel = s->nr_abs = 0;
     // GParticleSystem::SetDscr(N, 666) then LeafDSH_Solid3D_FEM::RebuildMass
     // (ParticleSystem.h:46-58,80,154-159; LeafDSH_Solid3D_FEM.cpp:1591-1611)
     Real total_mass = s->density * t->tes.TotalVolume();
@@ -306,7 +316,90 @@ static void a_times_d(const ref_solid* s, Real* q, const Real* d)
     }
 }
 
-/* One FixedStep(dt) of the Leaf with the QIE-v integrator. */
+static void finish_step(ref_solid* s);
+
+/* Restated Step_FullyImplicitEuler_dx (LeafDSH_Solid3D_FEM.cpp:1357-1552)
+ * around the reference's element set and CG: contacts off, warm start on,
+ * CG solver. h = 0 is the quasi-static variant (:958-959). */
+static void step_fie(ref_solid* s, Real h)
+{
+    ref_tes* t = s->t;
+    const unsigned N = t->N;
+    const unsigned cN = 3 * N;
+    Real inv_dt(h == 0 ? 0 : mal::Rcp(h));
+    for (unsigned i = 0; i < N; i++) { s->xk[i] = t->x[i]; s->vk[i] = t->v[i]; }
+    unsigned nr_k = 0, ls_iters = 0;
+    Real nr_delta_new(0), nr_delta_0(-1);
+    bool converged1 = false;
+    s->last_iters = 0; s->last_rel = s->last_abs = 0;
+    do {
+        for (unsigned i = 0; i < N; i++) s->b[i] = Vec3::Zero();
+        for (unsigned i = 0; i < N; i++) s->b[i] += (Real(1) / t->inv_mass[i]) * s->gravity;
+        t->tes.f_e(t->cache, &s->b[0]);
+        t->tes.f_p(t->cache, &s->b[0]);
+        for (unsigned i = 0; i < N; i++)
+            s->b[i] += inv_dt * (Real(1) / t->inv_mass[i]) * (t->v[i] - inv_dt * (s->xk[i] - t->x[i]));
+        if (nr_k == 0) for (unsigned i = 0; i < N; i++) s->y[i] = h * t->v[i];
+        else for (unsigned i = 0; i < N; i++) s->y[i] = Vec3::Zero();
+        for (size_t k = 0; k < s->knc.size(); k++) {
+            RefKNC& c = s->knc[k];
+            if (c.is_position) {
+                Vec3 vk((c.pos - t->x[c.nid]) * inv_dt);
+                Real norm_vk(vk.Norm());
+                if (norm_vk > Real(0.001f))
+                    c.vel = mal::Min(norm_vk, Real(50.0f)) * vk.Normalized();
+                else
+                    c.vel = Vec3::Zero();
+            }
+            s->b[c.nid] = c.pos - s->xk[c.nid];
+            s->y[c.nid] = c.pos - s->xk[c.nid];
+        }
+        nr_delta_new = ns::real_array::norm_2(reinterpret_cast<const Real*>(&s->b[0]), cN);
+        if (nr_delta_0 < 0) nr_delta_0 = nr_delta_new;
+        converged1 = nr_delta_new < s->nr_abs_eps;
+        if (!converged1) {
+            s->factor_M = mal::Sq(inv_dt) + inv_dt * s->rayleigh[0];
+            s->factor_K = Real(1) + inv_dt * s->rayleigh[1];
+            s->cg.Solve([s](Real* Av, const Real* v) { a_times_d(s, Av, v); },
+                        [s](Real* v) { zero_knc(s, reinterpret_cast<Vec3*>(v)); },
+                        reinterpret_cast<Real*>(&s->y[0]), reinterpret_cast<const Real*>(&s->b[0]),
+                        s->rel_eps, s->abs_eps, s->max_iter);
+            ls_iters += s->cg.GetNumIterations();
+            s->last_rel = s->cg.GetRelResidual();
+            s->last_abs = s->cg.GetAbsResidual();
+            ns::real_array::addeq(reinterpret_cast<Real*>(&s->xk[0]), reinterpret_cast<const Real*>(&s->y[0]), cN);
+            for (unsigned i = 0; i < N; i++) s->vk[i] = inv_dt * (s->xk[i] - t->x[i]);
+            nr_delta_new = ns::real_array::norm_2(reinterpret_cast<const Real*>(&s->y[0]), cN);
+            if (nr_delta_0 < 0) nr_delta_0 = nr_delta_new;
+            nr_k++;
+            t->tes.EndEvaluation(t->cache);
+            t->tes.BeginEvaluation(t->cache, &t->x[0], &s->xk[0], &s->vk[0], s->total_time);
+        }
+    } while (!converged1 && nr_k < s->nr_max_iter);
+    s->nr_iters = nr_k;
+    s->nr_rel = (nr_delta_0 > 0) ? nr_delta_new / nr_delta_0 : 0;
+    s->nr_abs = nr_delta_new;
+    s->last_iters = ls_iters;
+    for (unsigned i = 0; i < N; i++) { t->x[i] = s->xk[i]; t->v[i] = s->vk[i]; }
+}
+
+void ref_solid_set_integrator(ref_solid* s, unsigned integrator, unsigned nr_max_iter, double nr_abs_eps)
+{
+    s->integrator = integrator;
+    s->nr_max_iter = nr_max_iter;
+    s->nr_abs_eps = Real(nr_abs_eps);
+}
+
+void ref_solid_last_nr_stats(ref_solid* s, unsigned* nr_iters, double* nr_rel, double* nr_abs)
+{
+    const bool fie = s->integrator != 0;
+    if (nr_iters) *nr_iters = fie ? s->nr_iters : 0;
+    if (nr_rel) *nr_rel = fie ? s->nr_rel : 0;
+    if (nr_abs) *nr_abs = fie ? s->nr_abs : 0;
+}
+
+/* One FixedStep(dt) of the Leaf with the QIE-v integrator, or with the FIE-dx
+ * integrators (1: dt, 2: quasi-static). */
 void ref_solid_fixed_step(ref_solid* s)
 {
     ref_tes* t = s->t;
@@ -314,6 +407,11 @@ void ref_solid_fixed_step(ref_solid* s)
     const Real dt = s->dt;
     t->tes.BeginEvaluation(t->cache, &t->prev_x[0], &t->x[0], &t->v[0], s->total_time);
     for (unsigned i = 0; i < N; i++) t->prev_x[i] = t->x[i];
+    if (s->integrator != 0) {
+        step_fie(s, s->integrator == 2 ? Real(0) : dt);
+        finish_step(s);
+        return;
+    }
     // Step_QuasiImplicitEuler_v
     Real inv_dt(mal::Rcp(dt));
     for (unsigned i = 0; i < N; i++) s->b[i] = Vec3::Zero();
@@ -348,6 +446,15 @@ void ref_solid_fixed_step(ref_solid* s)
         t->v[i] = s->y[i];
         t->x[i] = t->x[i] + dt * s->y[i];
     }
+    finish_step(s);
+}
+
+/* The end of FixedStep after integration (LeafDSH_Solid3D_FEM.cpp:978-989):
+ * elastic energy, EndEvaluation, RecomputeEnergy's potential term. */
+static void finish_step(ref_solid* s)
+{
+    ref_tes* t = s->t;
+    const Real dt = s->dt;
     s->elastic_energy = t->tes.V(t->cache);
     t->tes.EndEvaluation(t->cache);
     // RecomputeEnergy (LeafDSH_Solid3D_FEM.cpp:1554-1584): potential part

@@ -19,6 +19,9 @@ FEM_OK = 0
 FEM_E_ARG, FEM_E_INDEX, FEM_E_NAN, FEM_E_OOM, FEM_E_CUDA, FEM_E_TIMEOUT, FEM_E_NODEVICE, FEM_E_DEGENERATE = range(1, 9)
 FEM_PRECISION_FP64 = 0
 FEM_PRECISION_MIXED = 1
+FEM_INTEGRATOR_QIE_V = 0
+FEM_INTEGRATOR_FIE_DX = 1
+FEM_INTEGRATOR_FIE_DX_QUASISTATIC = 2
 
 _dp = C.POINTER(C.c_double)
 _up = C.POINTER(C.c_uint32)
@@ -42,7 +45,10 @@ class FemParams(C.Structure):
         ("rotation_check", C.c_double),
         ("refresh_drop", C.c_double),
         ("rotation_fp32", C.c_uint32),
+        ("integrator", C.c_uint32),
+        ("nr_max_iter", C.c_uint32),
         ("pad", C.c_uint32),
+        ("nr_abs_epsilon", C.c_double),
     ]
 
 
@@ -57,10 +63,14 @@ class FemStepStats(C.Structure):
         ("inverted_elements", C.c_uint32),
         ("fp64_resolved", C.c_uint32),
         ("total_cg_iterations", C.c_uint64),
+        ("nr_iterations", C.c_uint32),
+        ("pad", C.c_uint32),
+        ("nr_rel_residual", C.c_double),
+        ("nr_abs_residual", C.c_double),
     ]
 
     def as_dict(self):
-        return {f: getattr(self, f) for f, _ in self._fields_}
+        return {f: getattr(self, f) for f, _ in self._fields_ if f != "pad"}
 
 
 class FemError(RuntimeError):
@@ -153,6 +163,9 @@ def params_for(scene, precision: int = FEM_PRECISION_FP64, compute_energy: bool 
     p.ls_max_iter = scene.max_iter
     p.precision = precision
     p.compute_energy = 1 if compute_energy else 0
+    p.integrator = getattr(scene, "integrator", FEM_INTEGRATOR_QIE_V)
+    p.nr_max_iter = getattr(scene, "nr_max_iter", 3)
+    p.nr_abs_epsilon = getattr(scene, "nr_abs_eps", 1e-6)
     return p
 
 

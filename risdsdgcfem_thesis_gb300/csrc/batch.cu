@@ -495,6 +495,9 @@ int fem_batch_add_mesh(fem_batch b, const double* rest, uint32_t N, const uint32
     if (!rest || !tets || !p) return batch_fail(FEM_E_ARG, "null rest/tets/params");
     if (N == 0 || T == 0) return batch_fail(FEM_E_ARG, "empty mesh (N=%u, T=%u)", N, T);
     if (!(p->fixed_dt > 0)) return batch_fail(FEM_E_ARG, "fixed_dt must be > 0");
+    if (p->integrator != FEM_INTEGRATOR_QIE_V)
+        return batch_fail(FEM_E_ARG, "integrator %u: batches step with QIE_V; the FIE integrators run on fem_solid",
+                          p->integrator);
     for (size_t i = 0; i < 4 * (size_t)T; i++)
         if (tets[i] >= N) return batch_fail(FEM_E_INDEX, "tet %zu names node %u >= N=%u", i / 4, tets[i], N);
     HostMesh m;
@@ -1313,6 +1316,10 @@ int fem_batch_get_stats(fem_batch b, uint32_t mesh, fem_step_stats* out)
     out->inverted_elements = h.inverted;
     out->fp64_resolved = h.fp64_resolved;
     out->total_cg_iterations = h.total_iters;
+    out->nr_iterations = 0;
+    out->pad = 0;
+    out->nr_rel_residual = 0.0;
+    out->nr_abs_residual = 0.0;
     return FEM_OK;
 }
 

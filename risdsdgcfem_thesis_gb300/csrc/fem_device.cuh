@@ -39,6 +39,7 @@ struct StepScalars {
     float alpha_f;          // mixed: this iteration's alpha in FP32 (0 on a confirm iteration)
     uint32_t brk;           // mixed: this iteration breaks down (|d.q| < abs^2) and leaves the loop
     unsigned long long total_iters;
+    double host_sum;        // FIE: the last FIN_SUM total (|b_k|^2 or |y_k|^2), read by the host
 };
 
 template <typename S>
@@ -88,6 +89,14 @@ void launch_node_xr_fp64(uint32_t N, double* y, double* r, const double* d, cons
 void launch_node_d_fp64(uint32_t N, const uint8_t* fixed, double* d, const double* r, const StepScalars* st,
                         cudaStream_t s);
 void launch_integrate_fp64(uint32_t N, double dt, double* x, double* v, const double* y, cudaStream_t s);
+// Fully-implicit Euler (Newton on Delta x) pieces, FP64 solid path.
+void launch_node_b_fie_fp64(const MeshView<double>& m, const StepConsts& c, const double* x, const double* xn,
+                            const double* vn, int warm, double* b, double* y, cudaStream_t s);
+void launch_knc_fie_fp64(uint32_t count, const uint32_t* nodes, const double* targets, const double* x, double* b,
+                         double* y, cudaStream_t s);
+void launch_sq_norm_fp64(uint32_t n, const double* v, double* partials, cudaStream_t s);
+void launch_fie_update_fp64(uint32_t N, double inv_dt, double* x, double* v, const double* xn, const double* y,
+                            double* partials, cudaStream_t s);
 void launch_potential_fp64(const MeshView<double>& m, const StepConsts& c, const double* x, double* partials,
                            cudaStream_t s);
 void launch_apply_A_fp64(const MeshView<double>& m, double factor_M, double factor_K, double mass,
@@ -95,7 +104,10 @@ void launch_apply_A_fp64(const MeshView<double>& m, double factor_M, double fact
 void launch_gather_sum_fp64(const MeshView<double>& m, double sign, double* f, cudaStream_t s);
 
 // finalizers: one block, fixed-order sums of `count` block partials
-enum FinalizeKind { FIN_INIT = 0, FIN_ALPHA = 1, FIN_BETA = 2, FIN_ENERGY_E = 3, FIN_ENERGY_P = 4, FIN_STATS = 5 };
+enum FinalizeKind {
+    FIN_INIT = 0, FIN_ALPHA = 1, FIN_BETA = 2, FIN_ENERGY_E = 3, FIN_ENERGY_P = 4, FIN_STATS = 5,
+    FIN_SUM = 6  // host_sum = total
+};
 void launch_finalize(int kind, const double* partials, uint32_t count, const StepConsts& c, StepScalars* st,
                      cudaStream_t s);
 

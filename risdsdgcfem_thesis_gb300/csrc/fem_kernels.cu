@@ -402,6 +402,73 @@ __global__ void k_integrate_fp64(uint32_t N, double dt, double* x, double* v, co
     }
 }
 
+// ---- fully-implicit Euler, Delta x form (LeafDSH_Solid3D_FEM.cpp:1357-1552) ----
+// x holds the Newton iterate x_k, xn and vn the step's x^n and v^n; eout holds
+// the element forces at x_k (k_elem_force_fp64 with the rotations of x_k).
+
+// b = m g + f_e(x_k) + (inv_dt m) (v^n - inv_dt (x_k - x^n)) with f_p = 0 and
+// f_d left out as in the reference (:1382-1401); y = dt v^n on the first
+// Newton iteration (the warm start, :1404-1405), else 0.
+__global__ void k_node_b_fie_fp64(MeshView<double> m, StepConsts c, const double* __restrict__ x,
+                                  const double* __restrict__ xn, const double* __restrict__ vn, int warm,
+                                  double* b, double* y)
+{
+    const double im = c.inv_dt * c.mass;
+    for (uint32_t n = blockIdx.x * blockDim.x + threadIdx.x; n < m.N; n += gridDim.x * blockDim.x) {
+        double f[3] = {0, 0, 0};
+        gather3(m, n, f[0], f[1], f[2]);
+        const size_t i = 3 * (size_t)n;
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+            const double bf = c.mass * c.gravity[a] - f[a];
+            b[i + a] = bf + im * (vn[i + a] - c.inv_dt * (x[i + a] - xn[i + a]));
+            y[i + a] = warm ? c.dt * vn[i + a] : 0.0;
+        }
+    }
+}
+
+// Position constraints as Delta x rows: b = y = target - x_k (:1441-1465).
+__global__ void k_knc_fie_fp64(uint32_t count, const uint32_t* __restrict__ nodes,
+                               const double* __restrict__ targets, const double* __restrict__ x, double* b,
+                               double* y)
+{
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < count; k += gridDim.x * blockDim.x) {
+        const size_t n = nodes[k];
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+            const double dx = targets[3 * k + a] - x[3 * n + a];
+            b[3 * n + a] = dx;
+            y[3 * n + a] = dx;
+        }
+    }
+}
+
+// partial sum of v_i^2 (real_array::sq_norm_2)
+__global__ void k_sq_norm_fp64(uint32_t n, const double* __restrict__ v, double* partials)
+{
+    double acc = 0.0;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) acc += v[i] * v[i];
+    double s = block_sum(acc);
+    if (threadIdx.x == 0) partials[blockIdx.x] = s;
+}
+
+// x_k += y ; v_k = inv_dt (x_k - x^n) ; partial |y|^2   (:1500-1512)
+__global__ void k_fie_update_fp64(uint32_t N, double inv_dt, double* x, double* v, const double* __restrict__ xn,
+                                  const double* __restrict__ y, double* partials)
+{
+    double acc = 0.0;
+    const uint32_t n3 = 3 * N;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n3; i += gridDim.x * blockDim.x) {
+        const double yi = y[i];
+        const double xi = x[i] + yi;
+        x[i] = xi;
+        v[i] = inv_dt * (xi - xn[i]);
+        acc += yi * yi;
+    }
+    double s = block_sum(acc);
+    if (threadIdx.x == 0) partials[blockIdx.x] = s;
+}
+
 // q = S (factor_M M d + factor_K sum R K R^T d) using a fresh eout
 __global__ void k_apply_A_fp64(MeshView<double> m, double factor_M, double factor_K, double mass,
                                const double* __restrict__ d, double* q)
@@ -484,6 +551,9 @@ __global__ void k_finalize(int kind, const double* __restrict__ partials, uint32
     case FIN_ENERGY_P:
         st->potential_energy = total;
         break;
+    case FIN_SUM:
+        st->host_sum = total;
+        break;
     case FIN_STATS:
         st->rel_residual = (st->delta_0 > 0) ? ::sqrt(st->delta_new / st->delta_0) : 0.0;
         st->abs_residual = ::sqrt(st->delta_new);
@@ -547,6 +617,26 @@ void launch_node_d_fp64(uint32_t N, const uint8_t* fixed, double* d, const doubl
 void launch_integrate_fp64(uint32_t N, double dt, double* x, double* v, const double* y, cudaStream_t s)
 {
     FEMGB_LAUNCH(k_integrate_fp64, grid_for(3 * N), N, dt, x, v, y);
+}
+void launch_node_b_fie_fp64(const MeshView<double>& m, const StepConsts& c, const double* x, const double* xn,
+                            const double* vn, int warm, double* b, double* y, cudaStream_t s)
+{
+    FEMGB_LAUNCH(k_node_b_fie_fp64, grid_for(m.N), m, c, x, xn, vn, warm, b, y);
+}
+void launch_knc_fie_fp64(uint32_t count, const uint32_t* nodes, const double* targets, const double* x, double* b,
+                         double* y, cudaStream_t s)
+{
+    if (count == 0) return;
+    FEMGB_LAUNCH(k_knc_fie_fp64, grid_for(count), count, nodes, targets, x, b, y);
+}
+void launch_sq_norm_fp64(uint32_t n, const double* v, double* partials, cudaStream_t s)
+{
+    FEMGB_LAUNCH(k_sq_norm_fp64, grid_for(n), n, v, partials);
+}
+void launch_fie_update_fp64(uint32_t N, double inv_dt, double* x, double* v, const double* xn, const double* y,
+                            double* partials, cudaStream_t s)
+{
+    FEMGB_LAUNCH(k_fie_update_fp64, grid_for(3 * N), N, inv_dt, x, v, xn, y, partials);
 }
 void launch_potential_fp64(const MeshView<double>& m, const StepConsts& c, const double* x, double* partials,
                            cudaStream_t s)

@@ -280,6 +280,8 @@ int fem_server_add_scene(fem_server s, const double* rest, uint32_t N, const uin
     if (int e = check_server(s)) return e;
     if (!rest || !tets || !p) return batch_fail(FEM_E_ARG, "null rest/tets/params");
     if (N == 0 || T == 0) return batch_fail(FEM_E_ARG, "empty mesh (N=%u, T=%u)", N, T);
+    if (p->integrator != FEM_INTEGRATOR_QIE_V)
+        return batch_fail(FEM_E_ARG, "integrator %u: the server steps with QIE_V", p->integrator);
     if (knc_count && (!knc_nodes || !knc_targets)) return batch_fail(FEM_E_ARG, "null constraint arrays");
     for (size_t i = 0; i < 4 * (size_t)T; i++)
         if (tets[i] >= N) return batch_fail(FEM_E_INDEX, "tet %zu names node %u >= N=%u", i / 4, tets[i], N);

@@ -10,7 +10,9 @@
 // 1205-1328) and ILSS_CG::Solve (ILSS_CG.h:38-151) as kernels on the
 // handle's stream; the CG loop runs in chunks of iterations whose kernels
 // turn into no-ops once the device-side loop condition fails, and the host
-// reads the condition once per chunk.
+// reads the condition once per chunk. The fully-implicit Euler integrator
+// (Step_FullyImplicitEuler_dx, :1357-1552) runs its Newton loop on the host
+// over the same kernels, reading |b_k| and |y_k| once per Newton iteration.
 #include "../../include/fem_tet.h"
 #include "fem_device.cuh"
 
@@ -104,6 +106,11 @@ struct fem_solid_s {
     DevBuf<uint8_t> fixed;
     // node vectors
     DevBuf<double> rest, x, v, y, b, r, d, q, tmp;
+    DevBuf<double> xn, vn;  // FIE: x^n and v^n of the step (allocated for the FIE integrators only)
+    // FIE statistics of the last step (host side; the Newton loop runs on the host)
+    uint32_t nr_iters = 0, fie_cg_iters = 0;
+    double nr_rel = 0, nr_abs = 0;
+    bool fie_solved = false;
     // constraints
     DevBuf<uint32_t> knc_nodes;
     DevBuf<double> knc_targets;
@@ -137,7 +144,7 @@ struct fem_solid_s {
     void release()
     {
         DevBuf<double>* dbl[] = {&Dinv, &mat, &vol, &R, &detF, &eout, &rest, &x, &v, &y, &b, &r, &d, &q, &tmp,
-                                 &knc_targets, &partials, &partials2};
+                                 &xn, &vn, &knc_targets, &partials, &partials2};
         for (auto* p : dbl) p->release();
         tets.release();
         csr_ptr.release();
@@ -160,19 +167,15 @@ int check_handle(fem_solid s)
     return FEM_OK;
 }
 
-// One FixedStep on the device (no host synchronisation except the per-chunk
-// read of the CG loop flag).
-int step_once(fem_solid s, int chunk)
+// ILSS_CG::Solve (ILSS_CG.h:38-151) of A y = b from the warm start in y,
+// with the factors of c, on the rotations of the last evaluation. Returns
+// once the device-side loop condition has failed (the host reads it once per
+// chunk of iterations).
+int cg_solve(fem_solid s, const StepConsts& c, int chunk)
 {
     cudaStream_t st = s->stream;
     MeshView<double> m = s->view();
-    const StepConsts& c = s->consts;
-    const uint32_t gE = grid_for(s->T), gN = grid_for(s->N), gV = grid_for(3 * s->N);
-    CK(cudaMemsetAsync(&s->st.p->inverted, 0, sizeof(uint32_t), st));
-    launch_begin_eval_fp64(m, s->x.p, nullptr, s->st.p, st);
-    launch_elem_force_fp64(m, s->x.p, 1, nullptr, st);
-    launch_node_b_fp64(m, c, s->v.p, s->b.p, s->y.p, st);
-    launch_knc_fp64(s->knc_count, s->knc_nodes.p, s->knc_targets.p, s->x.p, c, s->b.p, s->y.p, st);
+    const uint32_t gN = grid_for(s->N), gV = grid_for(3 * s->N);
     launch_elem_spmv_fp64(m, s->y.p, s->st.p, 0, st);
     launch_node_residual_fp64(m, c, s->b.p, s->y.p, s->r.p, s->d.p, s->partials.p, st);
     launch_finalize(FIN_INIT, s->partials.p, gN, c, s->st.p, st);
@@ -190,18 +193,113 @@ int step_once(fem_solid s, int chunk)
         if (s->st_host->done) break;
     }
     launch_finalize(FIN_STATS, s->partials.p, 0, c, s->st.p, st);
-    launch_integrate_fp64(s->N, c.dt, s->x.p, s->v.p, s->y.p, st);
-    if (s->params.compute_energy) {
-        launch_elem_force_fp64(m, s->x.p, 0, s->partials2.p, st);
-        launch_finalize(FIN_ENERGY_E, s->partials2.p, gE, c, s->st.p, st);
-        launch_potential_fp64(m, c, s->x.p, s->partials2.p, st);
-        launch_finalize(FIN_ENERGY_P, s->partials2.p, gE, c, s->st.p, st);
-    }
     CK(cudaGetLastError());
     return FEM_OK;
 }
 
-void fill_stats(const StepScalars& h, fem_step_stats* out)
+// Sum of `count` block partials into StepScalars::host_sum, read on the host.
+int host_sum(fem_solid s, uint32_t count, double* out)
+{
+    cudaStream_t st = s->stream;
+    launch_finalize(FIN_SUM, s->partials.p, count, s->consts, s->st.p, st);
+    CK(cudaMemcpyAsync(&s->st_host->host_sum, &s->st.p->host_sum, sizeof(double), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    *out = s->st_host->host_sum;
+    return FEM_OK;
+}
+
+// Elastic and potential energy at x with the current rotations
+// (FixedStep's m_TES.V and RecomputeEnergy, LeafDSH_Solid3D_FEM.cpp:979,1554-1584).
+void energy(fem_solid s)
+{
+    cudaStream_t st = s->stream;
+    MeshView<double> m = s->view();
+    const StepConsts& c = s->consts;
+    const uint32_t gE = grid_for(s->T);
+    launch_elem_force_fp64(m, s->x.p, 0, s->partials2.p, st);
+    launch_finalize(FIN_ENERGY_E, s->partials2.p, gE, c, s->st.p, st);
+    launch_potential_fp64(m, c, s->x.p, s->partials2.p, st);
+    launch_finalize(FIN_ENERGY_P, s->partials2.p, gE, c, s->st.p, st);
+}
+
+// One FixedStep with Step_FullyImplicitEuler_dx (LeafDSH_Solid3D_FEM.cpp:
+// 1357-1552). x and v are the Newton iterates x_k and v_k in place; xn and vn
+// keep x^n and v^n. Each Newton iteration: element forces at x_k, b_k, the
+// constraint rows, |b_k| (the exit test), CG on
+//   A = (1/h^2 + a0/h) M + (1 + a1/h) K(x_k),
+// x_k += y, v_k = (x_k - x^n)/h, |y|, and BeginEvaluation at the new x_k.
+// h = 0 (quasi-static) drops every 1/h term.
+int step_fie(fem_solid s, int chunk)
+{
+    cudaStream_t st = s->stream;
+    MeshView<double> m = s->view();
+    const bool quasi = s->params.integrator == FEM_INTEGRATOR_FIE_DX_QUASISTATIC;
+    StepConsts c = s->consts;
+    c.dt = quasi ? 0.0 : s->consts.dt;
+    c.inv_dt = quasi ? 0.0 : 1.0 / s->consts.dt;
+    c.factor_M = c.inv_dt * c.inv_dt + c.inv_dt * s->rayleigh[0];
+    c.factor_K = 1.0 + c.inv_dt * s->rayleigh[1];
+    const size_t bytes = sizeof(double) * 3 * (size_t)s->N;
+    const uint32_t gV = grid_for(3 * s->N);
+    CK(cudaMemsetAsync(&s->st.p->inverted, 0, sizeof(uint32_t), st));
+    launch_begin_eval_fp64(m, s->x.p, nullptr, s->st.p, st);
+    CK(cudaMemcpyAsync(s->xn.p, s->x.p, bytes, cudaMemcpyDeviceToDevice, st));
+    CK(cudaMemcpyAsync(s->vn.p, s->v.p, bytes, cudaMemcpyDeviceToDevice, st));
+    uint32_t nr_k = 0, cg_iters = 0;
+    double delta_new = 0.0, delta_0 = -1.0, sum = 0.0;
+    bool converged = false, solved = false;
+    do {
+        launch_elem_force_fp64(m, s->x.p, 1, nullptr, st);
+        launch_node_b_fie_fp64(m, c, s->x.p, s->xn.p, s->vn.p, nr_k == 0 ? 1 : 0, s->b.p, s->y.p, st);
+        launch_knc_fie_fp64(s->knc_count, s->knc_nodes.p, s->knc_targets.p, s->x.p, s->b.p, s->y.p, st);
+        launch_sq_norm_fp64(3 * s->N, s->b.p, s->partials.p, st);
+        if (int e = host_sum(s, gV, &sum)) return e;
+        delta_new = std::sqrt(sum);
+        if (delta_0 < 0) delta_0 = delta_new;
+        if (delta_new != delta_new) return fail(FEM_E_NAN, "NaN in the Newton right-hand side");
+        converged = delta_new < s->params.nr_abs_epsilon;
+        if (!converged) {
+            if (int e = cg_solve(s, c, chunk)) return e;
+            cg_iters += s->st_host->k;
+            solved = true;
+            launch_fie_update_fp64(s->N, c.inv_dt, s->x.p, s->v.p, s->xn.p, s->y.p, s->partials.p, st);
+            if (int e = host_sum(s, gV, &sum)) return e;
+            delta_new = std::sqrt(sum);
+            nr_k++;
+            CK(cudaMemsetAsync(&s->st.p->inverted, 0, sizeof(uint32_t), st));
+            launch_begin_eval_fp64(m, s->x.p, nullptr, s->st.p, st);
+        }
+    } while (!converged && nr_k < s->params.nr_max_iter);
+    s->nr_iters = nr_k;
+    s->fie_cg_iters = cg_iters;
+    s->fie_solved = solved;
+    s->nr_abs = delta_new;
+    s->nr_rel = (delta_0 > 0) ? delta_new / delta_0 : 0.0;
+    if (s->params.compute_energy) energy(s);
+    CK(cudaGetLastError());
+    return FEM_OK;
+}
+
+// One FixedStep on the device (no host synchronisation except the per-chunk
+// read of the CG loop flag).
+int step_once(fem_solid s, int chunk)
+{
+    if (s->params.integrator != FEM_INTEGRATOR_QIE_V) return step_fie(s, chunk);
+    cudaStream_t st = s->stream;
+    MeshView<double> m = s->view();
+    const StepConsts& c = s->consts;
+    CK(cudaMemsetAsync(&s->st.p->inverted, 0, sizeof(uint32_t), st));
+    launch_begin_eval_fp64(m, s->x.p, nullptr, s->st.p, st);
+    launch_elem_force_fp64(m, s->x.p, 1, nullptr, st);
+    launch_node_b_fp64(m, c, s->v.p, s->b.p, s->y.p, st);
+    launch_knc_fp64(s->knc_count, s->knc_nodes.p, s->knc_targets.p, s->x.p, c, s->b.p, s->y.p, st);
+    if (int e = cg_solve(s, c, chunk)) return e;
+    launch_integrate_fp64(s->N, c.dt, s->x.p, s->v.p, s->y.p, st);
+    if (s->params.compute_energy) energy(s);
+    CK(cudaGetLastError());
+    return FEM_OK;
+}
+void fill_stats(fem_solid s, const StepScalars& h, fem_step_stats* out)
 {
     out->cg_iterations = h.k;
     out->status = h.status;
@@ -212,6 +310,17 @@ void fill_stats(const StepScalars& h, fem_step_stats* out)
     out->inverted_elements = h.inverted;
     out->fp64_resolved = h.fp64_resolved;
     out->total_cg_iterations = h.total_iters;
+    out->nr_iterations = 0;
+    out->pad = 0;
+    out->nr_rel_residual = 0.0;
+    out->nr_abs_residual = 0.0;
+    if (s->params.integrator != FEM_INTEGRATOR_QIE_V) {
+        out->cg_iterations = s->fie_cg_iters;
+        if (!s->fie_solved) out->rel_residual = out->abs_residual = 0.0;
+        out->nr_iterations = s->nr_iters;
+        out->nr_rel_residual = s->nr_rel;
+        out->nr_abs_residual = s->nr_abs;
+    }
 }
 
 }  // namespace
@@ -255,6 +364,10 @@ int fem_params_default(fem_params* p)
     p->refresh_every = 50;
     p->refresh_drop = 0.0;
     p->compute_energy = 1;
+    // LeafDSH_Solid3D_FEM::Params (LeafDSH_Solid3D_FEM.h:209,233-241)
+    p->integrator = FEM_INTEGRATOR_QIE_V;
+    p->nr_max_iter = 3;
+    p->nr_abs_epsilon = 1e-6;
     return FEM_OK;
 }
 
@@ -270,6 +383,10 @@ int fem_solid_create(const double* rest_xyz, uint32_t N, const uint32_t* tets, u
     if (params->precision != FEM_PRECISION_FP64)
         return fail(FEM_E_ARG, "precision %u: this entry point builds the FP64 path; use the batch API for mixed",
                     params->precision);
+    if (params->integrator > FEM_INTEGRATOR_FIE_DX_QUASISTATIC)
+        return fail(FEM_E_ARG, "integrator %u is not an enum fem_integrator value", params->integrator);
+    if (params->integrator != FEM_INTEGRATOR_QIE_V && !(params->nr_abs_epsilon >= 0))
+        return fail(FEM_E_ARG, "nr_abs_epsilon must be >= 0");
     for (size_t i = 0; i < 4 * (size_t)T; i++)
         if (tets[i] >= N) return fail(FEM_E_INDEX, "tet %zu names node %u >= N=%u", i / 4, tets[i], N);
     int ndev = 0;
@@ -378,6 +495,10 @@ int fem_solid_create(const double* rest_xyz, uint32_t N, const uint32_t* tets, u
     CKC(s->fixed.alloc(N));
     DevBuf<double>* vecs[] = {&s->rest, &s->x, &s->v, &s->y, &s->b, &s->r, &s->d, &s->q, &s->tmp};
     for (auto* vb : vecs) CKC(vb->alloc(n3));
+    if (params->integrator != FEM_INTEGRATOR_QIE_V) {
+        CKC(s->xn.alloc(n3));
+        CKC(s->vn.alloc(n3));
+    }
     CKC(s->partials.alloc(4096));
     CKC(s->partials2.alloc(4096));
     CKC(s->st.alloc(1));
@@ -493,7 +614,7 @@ int fem_solid_synchronize(fem_solid s, fem_step_stats* stats)
     if (int e = check_handle(s)) return e;
     CK(cudaMemcpyAsync(s->st_host, s->st.p, sizeof(StepScalars), cudaMemcpyDeviceToHost, s->stream));
     CK(cudaStreamSynchronize(s->stream));
-    if (stats) fill_stats(*s->st_host, stats);
+    if (stats) fill_stats(s, *s->st_host, stats);
     if (s->st_host->status == FEM_E_NAN) return fail(FEM_E_NAN, "NaN in the CG residual");
     return FEM_OK;
 }

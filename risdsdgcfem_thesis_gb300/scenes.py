@@ -69,6 +69,11 @@ class Scene:
     init_vel: Optional[np.ndarray] = None          # (N, 3)
     grid: tuple = (0, 0, 0)
     h: float = 0.0
+    # Time integrator (enum fem_integrator: 0 QIE_V, 1 FIE_DX, 2 FIE_DX
+    # quasi-static) and the Newton settings of the FIE integrators.
+    integrator: int = 0
+    nr_max_iter: int = 3
+    nr_abs_eps: float = 1e-6
 
     @property
     def num_nodes(self) -> int:

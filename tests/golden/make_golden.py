@@ -12,7 +12,17 @@ units with Mal's Sqrt/Sin/Cos/ATan2 at double precision, except where noted):
   literal_fp64.npz     the reference FP64 build as written (float-rounded Mal
                        math): per-step iterations and energies of the same
                        scene (the rotations are NaN at rest, so CG stops at 0).
+  fie_160.npz          the fully-implicit Euler (Newton, Delta x) integrator:
+                       x, v after each of 30 FixedSteps of the cantilever with
+                       3 Newton iterations per step, then 5 quasi-static steps;
+                       per-step CG and Newton statistics, energies.
+  fie_block.npz        the same integrator on a 5x3x4 block with per-element
+                       E and nu, damping, an initial velocity and a moving
+                       constraint: per-step statistics, final x and v.
+
+python tests/golden/make_golden.py fie   writes only the two FIE fixtures.
 """
+import dataclasses
 import os
 import sys
 
@@ -47,8 +57,60 @@ def deformed_state(sc, seed=7):
     return x
 
 
+def _stat_arrays(stats, prefix=""):
+    out = {}
+    for key, dt in (("iters", np.int32), ("rel_res", np.float64), ("abs_res", np.float64),
+                    ("elastic_energy", np.float64), ("potential_energy", np.float64),
+                    ("nr_iters", np.int32), ("nr_rel", np.float64), ("nr_abs", np.float64)):
+        out[prefix + key] = np.array([s[key] for s in stats], dt)
+    return out
+
+
+def fie_block_scene():
+    rng = np.random.default_rng(5)
+    sc = scenes.random_block(rng, dims=(5, 3, 4))
+    T = sc.num_tets
+    sc.young_per_elem = np.exp(rng.uniform(np.log(5e4), np.log(5e5), T))
+    sc.poisson_per_elem = rng.uniform(0.25, 0.45, T)
+    sc.damping_ratio = 1.0
+    sc.init_vel = rng.standard_normal(sc.rest.shape) * 0.1
+    base = sc.knc_targets.copy()
+    sc.knc_schedule = lambda k: base + np.array([0.0, 0.0, 0.002 * (k + 1)])
+    sc.steps = 12
+    sc.integrator = 1
+    sc.nr_max_iter = 4
+    return sc
+
+
+def fie_fixtures():
+    sc = scenes.cantilever_160()
+    sc.integrator = 1
+    ref = O.Solid(sc, "ref_dbl")
+    xs, vs, stats = [], [], []
+    for _ in range(30):
+        stats.append(ref.step())
+        x, v = ref.state()
+        xs.append(x)
+        vs.append(v)
+    qs = O.Solid(dataclasses.replace(sc, integrator=2), "ref_dbl")
+    qstats = [qs.step() for _ in range(5)]
+    xq, vq = qs.state()
+    np.savez_compressed(os.path.join(HERE, "fie_160.npz"), x=np.array(xs), v=np.array(vs), xq=xq, vq=vq,
+                        **_stat_arrays(stats), **_stat_arrays(qstats, "q_"))
+    sc = fie_block_scene()
+    ref = O.Solid(sc, "ref_dbl")
+    stats = ref.run()
+    x, v = ref.state()
+    np.savez_compressed(os.path.join(HERE, "fie_block.npz"), x=x, v=v, **_stat_arrays(stats))
+
+
 def main():
     O.build(reference=True)
+    if sys.argv[1:] == ["fie"]:
+        fie_fixtures()
+        print("wrote FIE fixtures to", HERE)
+        return
+    fie_fixtures()
     sc = scenes.cantilever_160()
 
     ref = O.Solid(sc, "ref_dbl")

@@ -43,6 +43,20 @@ def test_params_default_matches_reference_defaults(fem_lib):
     # mixed-path controls of this library (no counterpart in the reference)
     assert p.degenerate_det_F == 1e-3 and p.rotation_check == 1e-3 and p.rotation_fp32 == 0
     assert p.refresh_drop == 0.0 and p.refresh_every == 50
+    # LeafDSH_Solid3D_FEM::Params: QIE_V integrator, 3 Newton iterations, NR abs epsilon 1e-6
+    assert p.integrator == fem_lib.FEM_INTEGRATOR_QIE_V and p.nr_max_iter == 3 and p.nr_abs_epsilon == 1e-6
+
+
+def test_create_rejects_bad_integrator(fem_lib):
+    rest, tets, _ = scenes.grid_mesh(1, 1, 1, 0.1, 0.0, 0)
+    p = fem_lib.default_params()
+    p.integrator = 3
+    code, h, msg = _create(fem_lib, rest, tets, p)
+    assert code == fem_lib.FEM_E_ARG and "integrator" in msg and not h.value
+    p.integrator = fem_lib.FEM_INTEGRATOR_FIE_DX
+    p.nr_abs_epsilon = -1.0
+    code, h, msg = _create(fem_lib, rest, tets, p)
+    assert code == fem_lib.FEM_E_ARG and "nr_abs_epsilon" in msg
 
 
 def _create(fem_lib, rest, tets, params=None):
@@ -142,6 +156,11 @@ def test_server_host_validation_without_gpu(fem_lib):
                                       t_bad.shape[0], C.byref(p), None, None, None, None, 0, C.byref(sid))
         assert rc == fem_lib.FEM_E_INDEX
         t_ok = np.ascontiguousarray(tets, np.uint32)
+        p.integrator = fem_lib.FEM_INTEGRATOR_FIE_DX  # the server steps with QIE_V only
+        rc = lib.fem_server_add_scene(h, rest.ctypes.data_as(dp), rest.shape[0], t_ok.ctypes.data_as(up),
+                                      t_ok.shape[0], C.byref(p), None, None, None, None, 0, C.byref(sid))
+        assert rc == fem_lib.FEM_E_ARG and b"integrator" in lib.fem_last_error()
+        p.integrator = fem_lib.FEM_INTEGRATOR_QIE_V
         rc = lib.fem_server_add_scene(h, rest.ctypes.data_as(dp), rest.shape[0], t_ok.ctypes.data_as(up),
                                       t_ok.shape[0], C.byref(p), None, None, None, None, 0, C.byref(sid))
         assert rc == fem_lib.FEM_OK and sid.value == 0

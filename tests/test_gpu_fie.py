@@ -1,0 +1,139 @@
+"""Fully-implicit Euler (Newton on Delta x) on the FP64 solid, through the C
+ABI, against the fixtures the reference's own element set and CG wrote
+(tests/golden/fie_160.npz, fie_block.npz; the oracle restatement equals them
+bit for bit).
+
+Tolerances (FP64): positions and velocities rel-L2 <= 1e-10 after the run
+(the quasi-static case: max(1e-10, 10 x the oracle's own sensitivity));
+Newton iterations per step equal; CG iterations per step (summed over the
+step's Newton solves) within max(1 per solve, 2 %): on the damped block the
+residual plateaus near the threshold and the stopping iteration moves by a
+few between orderings of the same sums; energies rel <= 1e-8; the last
+Newton norm rel <= 1e-2 (it is |y_k| of the last correction, or |b_k| once
+that fell below nr_abs_epsilon: a residual at the CG tolerance's level, which
+moves by up to 1.5e-3 in the oracle itself under 1e-15 perturbations of the
+initial velocity).
+"""
+import dataclasses
+import os
+
+import numpy as np
+import pytest
+
+from risdsdgcfem_thesis_gb300 import scenes
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+TOL = 1e-10
+
+
+def rel(a, b):
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def _cg_slack(st):
+    """CG iterations of a step may differ by one per Newton solve, or by 2 %
+    where the residual sits on a plateau near the stopping threshold."""
+    return max(st["nr_iterations"], int(np.ceil(0.02 * st["cg_iterations"])))
+
+
+def _check_steps(stats, g, prefix=""):
+    for k, st in enumerate(stats):
+        assert st["status"] == 0
+        assert st["nr_iterations"] == int(g[prefix + "nr_iters"][k]), k
+        assert abs(st["cg_iterations"] - int(g[prefix + "iters"][k])) <= _cg_slack(st), \
+            (k, st["cg_iterations"], g[prefix + "iters"][k])
+        assert abs(st["nr_abs_residual"] - g[prefix + "nr_abs"][k]) <= 1e-2 * g[prefix + "nr_abs"][k], k
+    last = stats[-1]
+    for key, gk in (("elastic_energy", "elastic_energy"), ("potential_energy", "potential_energy")):
+        ref = float(g[prefix + gk][len(stats) - 1])
+        assert abs(last[key] - ref) <= 1e-8 * abs(ref), key
+
+
+def test_fie_cantilever_matches_reference(fem_lib):
+    g = np.load(os.path.join(GOLDEN, "fie_160.npz"))
+    sc = dataclasses.replace(scenes.cantilever_160(), integrator=fem_lib.FEM_INTEGRATOR_FIE_DX)
+    s = fem_lib.Solid(sc)
+    stats = [s.step(1) for _ in range(g["x"].shape[0])]
+    _check_steps(stats, g)
+    x, v = s.state()
+    ex, ev = rel(x, g["x"][-1]), rel(v, g["v"][-1])
+    assert ex <= TOL and ev <= TOL, (ex, ev)
+
+
+def test_fie_quasistatic_cantilever_matches_reference(fem_lib, oracle):
+    """Quasi-static steps far from equilibrium (each step stops at the Newton
+    cap with |b_k| near 5): the result is as sensitive to the last bits as
+    the CG's stopping point, so the bar is max(1e-10, 10 x the oracle's own
+    spread under 1e-15 perturbations of the initial positions), measured
+    here (about 5e-9)."""
+    g = np.load(os.path.join(GOLDEN, "fie_160.npz"))
+    sc = dataclasses.replace(scenes.cantilever_160(), integrator=fem_lib.FEM_INTEGRATOR_FIE_DX_QUASISTATIC)
+    steps = g["q_iters"].shape[0]
+    floor, spread = 0.0, 0
+    for seed in (1, 2, 3):
+        o = oracle.Solid(sc, "port")
+        x0 = sc.rest + 1e-15 * np.abs(sc.rest).max() * np.random.default_rng(seed).standard_normal(sc.rest.shape)
+        o.set_state(x0, np.zeros_like(x0))
+        its = [o.step()["iters"] for _ in range(steps)]
+        spread = max(spread, max(abs(a - int(b)) for a, b in zip(its, g["q_iters"])))
+        floor = max(floor, rel(o.state()[0], g["xq"]))
+    s = fem_lib.Solid(sc)
+    stats = [s.step(1) for _ in range(steps)]
+    for k, st in enumerate(stats):
+        assert st["status"] == 0 and st["nr_iterations"] == int(g["q_nr_iters"][k])
+        assert abs(st["cg_iterations"] - int(g["q_iters"][k])) <= max(st["nr_iterations"], 2 * spread + 1), k
+    x, v = s.state()
+    assert rel(x, g["xq"]) <= max(TOL, 10 * floor), (rel(x, g["xq"]), floor)
+    assert not np.any(v)
+
+
+def test_fie_block_moving_constraint_matches_reference(fem_lib):
+    """Per-element E and nu, damping, initial velocity and a constraint moved
+    every step; some steps leave the Newton loop on |b_k| < nr_abs_epsilon."""
+    g = np.load(os.path.join(GOLDEN, "fie_block.npz"))
+    rng = np.random.default_rng(5)
+    sc = scenes.random_block(rng, dims=(5, 3, 4))
+    T = sc.num_tets
+    sc.young_per_elem = np.exp(rng.uniform(np.log(5e4), np.log(5e5), T))
+    sc.poisson_per_elem = rng.uniform(0.25, 0.45, T)
+    sc.damping_ratio = 1.0
+    sc.init_vel = rng.standard_normal(sc.rest.shape) * 0.1
+    base = sc.knc_targets.copy()
+    sc.knc_schedule = lambda k: base + np.array([0.0, 0.0, 0.002 * (k + 1)])
+    sc.steps = 12
+    sc.integrator = fem_lib.FEM_INTEGRATOR_FIE_DX
+    sc.nr_max_iter = 4
+    s = fem_lib.Solid(sc)
+    stats = s.run()
+    _check_steps(stats, g)
+    assert min(st["nr_iterations"] for st in stats) < sc.nr_max_iter
+    x, v = s.state()
+    ex, ev = rel(x, g["x"]), rel(v, g["v"])
+    assert ex <= TOL and ev <= TOL, (ex, ev)
+
+
+def test_fie_matches_oracle_on_random_block(fem_lib, oracle):
+    """A larger block than the fixtures (2,000+ tets), FIE dynamic, against the
+    oracle restatement run here."""
+    rng = np.random.default_rng(21)
+    sc = scenes.random_block(rng, dims=(10, 6, 8))
+    sc.integrator = fem_lib.FEM_INTEGRATOR_FIE_DX
+    sc.gravity = (0.0, 0.0, -9.81)
+    sc.rel_eps, sc.max_iter = 1e-8, 400
+    a = fem_lib.Solid(sc)
+    b = oracle.Solid(sc, "port")
+    for _ in range(5):
+        sa, sb = a.step(1), b.step()
+        assert sa["nr_iterations"] == sb["nr_iters"]
+        assert abs(sa["cg_iterations"] - sb["iters"]) <= _cg_slack(sa)
+    xa, va = a.state()
+    xb, vb = b.state()
+    assert rel(xa, xb) <= TOL and rel(va, vb) <= 1e-8, (rel(xa, xb), rel(va, vb))
+
+
+def test_batch_rejects_fie(fem_lib):
+    sc = dataclasses.replace(scenes.cantilever_160(), integrator=fem_lib.FEM_INTEGRATOR_FIE_DX)
+    with pytest.raises(fem_lib.FemError) as e:
+        fem_lib.Batch([sc], precision=fem_lib.FEM_PRECISION_FP64)
+    assert e.value.code == fem_lib.FEM_E_ARG
