@@ -408,7 +408,7 @@ __global__ void k_integrate_fp64(uint32_t N, double dt, double* x, double* v, co
 
 // b = m g + f_e(x_k) + (inv_dt m) (v^n - inv_dt (x_k - x^n)) with f_p = 0 and
 // f_d left out as in the reference (:1382-1401); y = dt v^n on the first
-// Newton iteration (the warm start, :1404-1405), else 0.
+// Newton iteration (the warm start, :1406-1407), else 0.
 __global__ void k_node_b_fie_fp64(MeshView<double> m, StepConsts c, const double* __restrict__ x,
                                   const double* __restrict__ xn, const double* __restrict__ vn, int warm,
                                   double* b, double* y)
