@@ -64,6 +64,21 @@ enum fem_integrator {
     FEM_INTEGRATOR_FIE_DX_QUASISTATIC = 2
 };
 
+/* Rotation methods of the element set (ms::fem::Params::ERotationMethod,
+ * Params.h:63-67; ComputeRotations_*, TetrahedronElementSet3.cpp:267-278). */
+enum fem_rotation {
+    /* ComputeRotations_MSVD: R = U V^T of the PhysBAM-style SVD. The default. */
+    FEM_ROTATION_MSVD = 0,
+    /* ComputeRotations_DAPD (TetrahedronElementSet3.cpp:860-892): the Newton
+     * polar rotation above dapd_threshold_det_F; at or below it, the rotation
+     * of F with the collapsing vertex or edge moved along the collapse normal
+     * (Rotation.cpp:364-495), the direction of collapse found from the
+     * previous step's positions by the time-of-collapse cubic
+     * (TetrahedronElementSet3.cpp:477-743) and kept while the element stays
+     * degenerate; I where no direction is known. FP64 solid only. */
+    FEM_ROTATION_DAPD = 1
+};
+
 /* Solid parameters. Mirrors bs::Solid3D::Params and Params_Extra
  * (Saphyre2 bs/Solid3D.h:27-85) for the fields this path reads:
  * FixedDT, Density, YoungModulus, PoissonRatio, DampingRatio, Gravity,
@@ -103,8 +118,13 @@ typedef struct fem_params {
                                  tie or rotation_check flags them */
     uint32_t integrator;      /* enum fem_integrator; the batch and server paths take QIE_V only */
     uint32_t nr_max_iter;     /* FIE: Newton iteration cap per step (m_SolverNR_MaxIter) */
-    uint32_t pad;
+    uint32_t rotation;        /* enum fem_rotation; the batch and server paths take MSVD only */
     double nr_abs_epsilon;    /* FIE: Newton stops once |b_k| < this (m_SolverNR_AbsEpsilon) */
+    double dapd_threshold_det_F; /* DAPD: degenerate at or below this det F
+                                    (m_DegenerateThresholdDetF, default 0.1f) */
+    double dapd_l_factor;     /* DAPD: offset factors and exponent (m_DAPD_L_Factor 1, */
+    double dapd_nl_factor;    /*   m_DAPD_NL_Factor 0, m_DAPD_NL_Exponent 2); float32 in the */
+    double dapd_nl_exponent;  /*   reference, so they are rounded to float */
 } fem_params;
 
 /* Per-step statistics (the Leaf's per-step LS stats, LeafDSH_Solid3D_FEM.h:597-622). */
@@ -132,7 +152,8 @@ typedef struct fem_solid_s* fem_solid;
  * fixed_dt 0.001, density 1000, E 1000, nu 0.25, damping 1, gravity 0,
  * CG rel 1e-3, abs 1e-6, 20 iterations, FP64, threshold 1e-3, refresh 50,
  * energy on, rotation check 1e-3, refresh every 50 iterations (no drop rule),
- * QIE_V integrator, 3 Newton iterations with abs epsilon 1e-6. */
+ * QIE_V integrator, 3 Newton iterations with abs epsilon 1e-6, MSVD
+ * rotations (DAPD threshold 0.1f, factors 1, 0, 2). */
 int fem_params_default(fem_params* p);
 
 /* Replaces: EditableTetrahedronElementSet3::BeginEdition/AddElement/EndEdition
@@ -172,10 +193,15 @@ int fem_solid_step_host(fem_solid s, const double* x_in, const double* v_in, uin
 /* --- Element-level hooks (the IForce3 seam, TetrahedronElementSet3.h:29-58) --- */
 
 /* Replaces TetrahedronElementSet3::BeginEvaluation (TetrahedronElementSet3.cpp:219-281):
- * F, det F and the MSVD rotation of every element at positions x (N*3). */
+ * F, det F and the rotation (MSVD, or DAPD against the solid's previous-step
+ * positions) of every element at positions x (N*3). */
 int fem_solid_begin_eval(fem_solid s, const double* x);
 /* The cached rotations (T*9, row-major) and det F (T) of the last evaluation. */
 int fem_solid_get_rotations(fem_solid s, double* R, double* detF);
+/* DAPD: each element's direction of collapse (ElementCache3::m_DoC) as two
+ * bytes (vit0, vit1): V-F when equal, E-E when vit0 < vit1, none = (3, 0).
+ * T*2 bytes. FEM_E_ARG when the solid does not use DAPD. */
+int fem_solid_get_doc(fem_solid s, uint8_t* doc);
 /* f += f_e at the evaluated positions (C_f_e, TetrahedronElementSet3.cpp:1053-1096). N*3. */
 int fem_solid_force_elastic(fem_solid s, double* f);
 /* df += df_x(dx) = -R K0 R^T dx (C_df_x, TetrahedronElementSet3.cpp:1761-1836). N*3. */

@@ -315,6 +315,227 @@ static mat3 rotation_msvd(const mat3* F)
     return m_mul(&U, &Vt);
 }
 
+/* Column 2 of V of GFastSVD3x3 (PhysBAM.h:247-272): the right singular
+ * vector of the smallest singular value. */
+static vec3 svd_smallest_right_vector(const mat3* F)
+{
+    sym3 ne;
+    const double (*f)[3] = F->m;
+    ne.x11 = f[0][0] * f[0][0] + f[1][0] * f[1][0] + f[2][0] * f[2][0];
+    ne.x21 = f[0][1] * f[0][0] + f[1][1] * f[1][0] + f[2][1] * f[2][0];
+    ne.x31 = f[0][2] * f[0][0] + f[1][2] * f[1][0] + f[2][2] * f[2][0];
+    ne.x22 = f[0][1] * f[0][1] + f[1][1] * f[1][1] + f[2][1] * f[2][1];
+    ne.x32 = f[0][2] * f[0][1] + f[1][2] * f[1][1] + f[2][2] * f[2][1];
+    ne.x33 = f[0][2] * f[0][2] + f[1][2] * f[1][2] + f[2][2] * f[2][2];
+    double lambda[3];
+    fast_eigenvalues(ne, lambda);
+    mat3 V = fast_eigenvectors(ne, lambda);
+    return m_col(&V, 2);
+}
+
+static mat3 m_identity(void)
+{
+    mat3 I;
+    memset(&I, 0, sizeof(I));
+    I.m[0][0] = I.m[1][1] = I.m[2][2] = 1;
+    return I;
+}
+
+/* ---- DAPD rotations (ms::fem::Params::eRM_DAPD) -------------------------- */
+
+/* GRotation3x3_PolarDecomposition (Mal/GMatDecomposition.h:411-432): Newton
+ * iterations H <- (H + H^-T) / 2 while |H1 - H0|_F^2 > 0.01f, at most 10. */
+static mat3 polar_newton(const mat3* H)
+{
+    mat3 H0 = *H;
+    double error;
+    unsigned num_iter = 0;
+    const double prec_sq = (double)0.01f;
+    do {
+        mat3 Ht = m_transposed(&H0);
+        mat3 Hit = m_inverse(&Ht);
+        mat3 H1;
+        for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++) H1.m[i][j] = 0.5 * (H0.m[i][j] + Hit.m[i][j]);
+        error = 0;
+        for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++) {
+                double d = H1.m[i][j] - H0.m[i][j];
+                error += d * d;
+            }
+        H0 = H1;
+        num_iter++;
+    } while (num_iter < 10 && error > prec_sq);
+    return H0;
+}
+
+/* mal::IsZero with the default epsilon 0.0001f (Mal/RealUtils.h:110-114) */
+static int is_zero(double x) { return fabs(x) <= (double)0.0001f; }
+
+/* GSolvePolynomialEq1/Eq2 (Mal/GSolvePolynomialEq.h:11-40) */
+static int solve_eq1(double a, double b, double* x)
+{
+    if (is_zero(a)) return 0;
+    *x = -b / a;
+    return 1;
+}
+static int solve_eq2(double a, double b, double c, double* x1, double* x2)
+{
+    if (is_zero(a)) {
+        int n = solve_eq1(b, c, x1);
+        *x2 = *x1;
+        return n;
+    }
+    double disc = b * b - 4 * a * c;
+    if (disc < 0) return 0;
+    double root = mal_sqrt(disc);
+    double inv_divisor = 1.0 / (2.0 * a);
+    *x1 = (-b - root) * inv_divisor;
+    *x2 = (-b + root) * inv_divisor;
+    if (*x1 > *x2) { double t = *x1; *x1 = *x2; *x2 = t; }
+    return (*x1 == *x2) ? 1 : 2;
+}
+
+int gsl_poly_solve_cubic(double a, double b, double c, double* x0, double* x1, double* x2);
+
+/* mal::GSolvePolynomialEq3 as defined in TetrahedronElementSet3.cpp:49-70:
+ * GSL's monic cubic solver for a != 0, else the quadratic. */
+static int solve_eq3(double a, double b, double c, double d, double* x1, double* x2, double* x3)
+{
+    if (a != 0) return gsl_poly_solve_cubic(b / a, c / a, d / a, x1, x2, x3);
+    *x3 = 0;
+    return solve_eq2(b, c, d, x1, x2);
+}
+
+/* TetrahedronElement3::DoC (TetrahedronElement3.h:28-38): V-F when
+ * vit0 == vit1, E-E when vit0 < vit1, invalid when vit0 > vit1. */
+typedef struct { uint8_t vit0, vit1; } doc_t;
+static const doc_t kDocInvalid = {3, 0};
+static int doc_valid(doc_t d) { return d.vit0 <= d.vit1; }
+
+/* ComputeDoC (TetrahedronElementSet3.cpp:589-743): the time of collapse t in
+ * (0, 1] when det F along the straight path a -> b crosses the threshold
+ * (a cubic in t), then the kind of collapse at that time: the face whose
+ * unit-height prism volume along the collapse normal is half the total
+ * (V-F, its opposite vertex), else the crossing edge pair (E-E). */
+static doc_t compute_doc(vec3 a0, vec3 a1, vec3 a2, vec3 a3, vec3 b0, vec3 b1, vec3 b2, vec3 b3, double volume,
+                         double thr)
+{
+    doc_t doc = kDocInvalid;
+    vec3 d0 = v_sub(b0, a0), d1 = v_sub(b1, a1), d2 = v_sub(b2, a2), d3 = v_sub(b3, a3);
+    vec3 d10 = v_sub(d1, d0), d20 = v_sub(d2, d0), d30 = v_sub(d3, d0);
+    vec3 a10 = v_sub(a1, a0), a20 = v_sub(a2, a0), a30 = v_sub(a3, a0);
+#define X(a_) ((a_).v[0])
+#define Y(a_) ((a_).v[1])
+#define Z(a_) ((a_).v[2])
+    double K = thr * 6.0 * volume;
+    double A = +X(d10) * Y(d20) * Z(d30) + X(d20) * Y(d30) * Z(d10) + X(d30) * Y(d10) * Z(d20)
+               - X(d30) * Y(d20) * Z(d10) - X(d20) * Y(d10) * Z(d30) - X(d10) * Y(d30) * Z(d20);
+    double B = +(X(a10) * Y(d20) * Z(d30) + X(d10) * Y(a20) * Z(d30) + X(d10) * Y(d20) * Z(a30))
+               + (X(a20) * Y(d30) * Z(d10) + X(d20) * Y(a30) * Z(d10) + X(d20) * Y(d30) * Z(a10))
+               + (X(a30) * Y(d10) * Z(d20) + X(d30) * Y(a10) * Z(d20) + X(d30) * Y(d10) * Z(a20))
+               - (X(a30) * Y(d20) * Z(d10) + X(d30) * Y(a20) * Z(d10) + X(d30) * Y(d20) * Z(a10))
+               - (X(a20) * Y(d10) * Z(d30) + X(d20) * Y(a10) * Z(d30) + X(d20) * Y(d10) * Z(a30))
+               - (X(a10) * Y(d30) * Z(d20) + X(d10) * Y(a30) * Z(d20) + X(d10) * Y(d30) * Z(a20));
+    double C = +(X(a10) * Y(a20) * Z(d30) + X(a10) * Y(d20) * Z(a30) + X(d10) * Y(a20) * Z(a30))
+               + (X(a20) * Y(a30) * Z(d10) + X(a20) * Y(d30) * Z(a10) + X(d20) * Y(a30) * Z(a10))
+               + (X(a30) * Y(a10) * Z(d20) + X(a30) * Y(d10) * Z(a20) + X(d30) * Y(a10) * Z(a20))
+               - (X(a30) * Y(a20) * Z(d10) + X(a30) * Y(d20) * Z(a10) + X(d30) * Y(a20) * Z(a10))
+               - (X(a20) * Y(a10) * Z(d30) + X(a20) * Y(d10) * Z(a30) + X(d20) * Y(a10) * Z(a30))
+               - (X(a10) * Y(a30) * Z(d20) + X(a10) * Y(d30) * Z(a20) + X(d10) * Y(a30) * Z(a20));
+    double D = +X(a10) * Y(a20) * Z(a30) + X(a20) * Y(a30) * Z(a10) + X(a30) * Y(a10) * Z(a20)
+               - X(a30) * Y(a20) * Z(a10) - X(a20) * Y(a10) * Z(a30) - X(a10) * Y(a30) * Z(a20) - K;
+#undef X
+#undef Y
+#undef Z
+    double toc_r[3] = {0, 0, 0};
+    int num_roots = solve_eq3(A, B, C, D, &toc_r[0], &toc_r[1], &toc_r[2]);
+    if (num_roots <= 0) return doc;
+    double toc = 2;
+    int num_roots01 = 0;
+    for (int i = 0; i < num_roots; i++)
+        if (toc_r[i] > 0 && toc_r[i] <= 1 && toc_r[i] < toc) {
+            toc = toc_r[i];
+            num_roots01++;
+        }
+    if (num_roots01 != 1 && num_roots01 != 3) return doc;
+    vec3 q0 = v_add(a0, v_scale(toc, d0)), q1 = v_add(a1, v_scale(toc, d1));
+    vec3 q2 = v_add(a2, v_scale(toc, d2)), q3 = v_add(a3, v_scale(toc, d3));
+    /* collapse normal: the right singular vector of the smallest singular
+     * value (GSingularValueDecomposition_USVt = GFastSVD3x3, row 2 of V^T) */
+    mat3 Q = m_from_columns(v_sub(q1, q0), v_sub(q2, q0), v_sub(q3, q0));
+    vec3 N = svd_smallest_right_vector(&Q);
+    double area[4];
+    area[0] = fabs(v_dot(N, v_cross(v_sub(q2, q1), v_sub(q3, q1))));
+    area[1] = fabs(v_dot(N, v_cross(v_sub(q2, q0), v_sub(q3, q0))));
+    area[2] = fabs(v_dot(N, v_cross(v_sub(q1, q0), v_sub(q3, q0))));
+    area[3] = fabs(v_dot(N, v_cross(v_sub(q1, q0), v_sub(q2, q0))));
+    double sum_area = area[0] + area[1] + area[2] + area[3];
+    for (int f = 0; f < 4; f++)
+        if (fabs(area[f] - 0.5 * sum_area) <= (double)0.0001f) { doc.vit0 = (uint8_t)f; doc.vit1 = (uint8_t)f; }
+    if (!doc_valid(doc)) {
+        vec3 e1 = v_sub(q1, q0), e2 = v_sub(q2, q0), e3 = v_sub(q3, q0);
+        if (v_dot(v_cross(e1, e2), v_cross(e1, e3)) < 0) { doc.vit0 = 0; doc.vit1 = 1; }
+        else if (v_dot(v_cross(e2, e1), v_cross(e2, e3)) < 0) { doc.vit0 = 0; doc.vit1 = 2; }
+        else if (v_dot(v_cross(e3, e1), v_cross(e3, e2)) < 0) { doc.vit0 = 0; doc.vit1 = 3; }
+        else { doc.vit0 = 0; doc.vit1 = 0; }
+    }
+    return doc;
+}
+
+/* Compute_R_DAPD_Degenerate (Rotation.cpp:364-495): move the collapsing
+ * vertex (V-F) or edge (E-E) along the collapse normal past the threshold by
+ * the Hermite-spline / linear + power offset lambda_u, then the polar
+ * rotation of the projected F. */
+static mat3 dapd_degenerate(double detF, double thr, doc_t doc, vec3 p0, vec3 p1, vec3 p2, vec3 p3,
+                            double volume, const mat3* inv_Dm, double fL, double fNL, double eNL)
+{
+    vec3 X[4] = {p0, p1, p2, p3};
+    int i0, i1 = -1;
+    vec3 axis;
+    double w;
+    if (doc.vit0 == doc.vit1) {
+        int noc = doc.vit0;
+        i0 = noc;
+        vec3 x1 = X[(noc + 1) % 4], x2 = X[(noc + 2) % 4], x3 = X[(noc + 3) % 4];
+        axis = v_cross(v_sub(x2, x1), v_sub(x3, x1));
+        double len_sq = v_dot(axis, axis);
+        if (!(len_sq > (double)0.000001f)) return m_identity();
+        double len = mal_sqrt(len_sq);
+        axis = v_div(axis, len);
+        double dha = thr * 6 * volume / len;
+        w = v_dot(v_sub(X[i0], x1), axis);
+        if (w * detF < 0) { w = -w; axis = v_neg(axis); }
+        double s_ = w / dha, t = 1.0 - s_;
+        double lambda = (w > 0) ? fL * dha * ((2 - t) * t * t) : fL * dha * (t + fNL * pow(-s_, eNL));
+        X[i0] = v_add(X[i0], v_scale(lambda, axis));
+    } else {
+        int v0 = doc.vit0, v1 = doc.vit1, v2, v3;
+        switch (v1) {
+        case 1: v2 = 2; v3 = 3; break;
+        case 2: v2 = 1; v3 = 3; break;
+        default: v2 = 1; v3 = 2; break;
+        }
+        i0 = v0;
+        i1 = v1;
+        axis = v_cross(v_sub(X[v1], X[v0]), v_sub(X[v3], X[v2]));
+        double len_sq = v_dot(axis, axis);
+        if (!(len_sq > (double)0.000001f)) return m_identity();
+        double len = mal_sqrt(len_sq);
+        axis = v_div(axis, len);
+        double dha = thr * 6 * volume / len;
+        w = v_dot(v_sub(X[v0], X[v2]), axis);
+        if (w * detF < 0) { w = -w; axis = v_neg(axis); }
+        double s_ = w / dha, t = 1.0 - s_;
+        double lambda = (w > 0) ? fL * dha * ((2 - t) * t * t) : fL * dha * (t + fNL * pow(-s_, eNL));
+        X[i0] = v_add(X[i0], v_scale(lambda, axis));
+        X[i1] = v_add(X[i1], v_scale(lambda, axis));
+    }
+    mat3 projDs = m_from_columns(v_sub(X[1], X[0]), v_sub(X[2], X[0]), v_sub(X[3], X[0]));
+    mat3 projF = m_mul(&projDs, inv_Dm);
+    return polar_newton(&projF);
+}
+
 void orc_rotation_svd(const double* F_in, double* R_out, int math_mode)
 {
     g_math = math_mode;
@@ -425,6 +646,11 @@ struct orc_solid {
     vec3 *xk, *vk;        /* Newton iterates x_k, v_k (m_IE_vec_x_k, m_IE_vec_v_k) */
     uint32_t nr_iters;
     double nr_rel, nr_abs;
+    /* rotation method (ms::fem::Params::m_RM) and the DAPD parameters
+     * (m_DegenerateThresholdDetF, m_DAPD_L/NL_Factor, m_DAPD_NL_Exponent) */
+    uint32_t rotation;
+    double dapd_thr, dapd_L, dapd_NL, dapd_exp;
+    doc_t* doc;           /* per-element direction of collapse (ElementCache3::m_DoC) */
 };
 
 static vec3 load3(const double* p) { return v3(p[0], p[1], p[2]); }
@@ -455,6 +681,13 @@ orc_solid* orc_solid_create(uint32_t N, const double* rest, uint32_t T, const ui
     s->q = (double*)malloc(sizeof(double) * 3 * N);
     s->xk = (vec3*)calloc(N, sizeof(vec3));
     s->vk = (vec3*)calloc(N, sizeof(vec3));
+    s->doc = (doc_t*)malloc(sizeof(doc_t) * T);
+    for (uint32_t e = 0; e < T; e++) s->doc[e] = kDocInvalid;
+    s->rotation = FEM_ORC_ROT_MSVD;
+    s->dapd_thr = (double)0.1f;
+    s->dapd_L = 1;
+    s->dapd_NL = 0;
+    s->dapd_exp = 2;
     s->integrator = FEM_ORC_QIE_V;
     s->nr_max_iter = 3;
     s->nr_abs_eps = 1e-6;
@@ -513,7 +746,7 @@ void orc_solid_destroy(orc_solid* s)
     if (!s) return;
     free(s->ref_pos); free(s->tets); free(s->volume); free(s->inv_Dm); free(s->K); free(s->R);
     free(s->detF); free(s->x); free(s->prev_x); free(s->v); free(s->b); free(s->y);
-    free(s->r); free(s->d); free(s->q); free(s->xk); free(s->vk);
+    free(s->r); free(s->d); free(s->q); free(s->xk); free(s->vk); free(s->doc);
     free(s->knc_nid); free(s->knc_pos); free(s->knc_vel);
     free(s);
 }
@@ -572,18 +805,43 @@ void orc_solid_get_state(const orc_solid* s, double* x, double* v)
 /* BeginEvaluation for C_WRP + MSVD (TetrahedronElementSet3.cpp:219-281,777-792):
  * Ds, F = Ds * Dm^-1, det F, R. The degeneration bookkeeping (DoC) does not
  * feed this path and is not formed. */
-static void begin_evaluation_at(orc_solid* s, const vec3* x)
+static void begin_evaluation_at(orc_solid* s, const vec3* xprev, const vec3* x)
 {
     for (uint32_t e = 0; e < s->T; e++) {
         const uint32_t* t = s->tets + 4 * (size_t)e;
         mat3 Ds = compute_D(x[t[0]], x[t[1]], x[t[2]], x[t[3]]);
         mat3 F = m_mul(&Ds, &s->inv_Dm[e]);
-        s->detF[e] = m_det(&F);
-        s->R[e] = rotation_msvd(&F);
+        double detF = m_det(&F);
+        s->detF[e] = detF;
+        if (s->rotation == FEM_ORC_ROT_MSVD) {
+            s->R[e] = rotation_msvd(&F);
+            continue;
+        }
+        /* UpdateDegeneration (TetrahedronElementSet3.cpp:477-533) */
+        const double thr = s->dapd_thr;
+        if (detF > thr) {
+            s->doc[e] = kDocInvalid;
+        } else {
+            mat3 prevDs = compute_D(xprev[t[0]], xprev[t[1]], xprev[t[2]], xprev[t[3]]);
+            mat3 prevF = m_mul(&prevDs, &s->inv_Dm[e]);
+            if (m_det(&prevF) > thr)
+                s->doc[e] = compute_doc(xprev[t[0]], xprev[t[1]], xprev[t[2]], xprev[t[3]], x[t[0]], x[t[1]],
+                                        x[t[2]], x[t[3]], s->volume[e], thr);
+        }
+        /* ComputeRotations_DAPD (TetrahedronElementSet3.cpp:860-892) */
+        if (detF > thr)
+            s->R[e] = polar_newton(&F);
+        else if (doc_valid(s->doc[e]))
+            s->R[e] = dapd_degenerate(detF, thr, s->doc[e], x[t[0]], x[t[1]], x[t[2]], x[t[3]], s->volume[e],
+                                      &s->inv_Dm[e], s->dapd_L, s->dapd_NL, s->dapd_exp);
+        else
+            s->R[e] = m_identity();
     }
 }
 
-static void begin_evaluation(orc_solid* s) { begin_evaluation_at(s, s->x); }
+/* BeginEvaluation(m_vecPos0, x): the previous positions feed the DAPD
+ * collapse detection only. */
+static void begin_evaluation(orc_solid* s) { begin_evaluation_at(s, s->prev_x, s->x); }
 
 /* C_f_e (TetrahedronElementSet3.cpp:1053-1096): f_i -= R sum_j K_ij (R^T x_j - r_j) */
 static void f_e_acc(const orc_solid* s, const vec3* x, vec3* f)
@@ -774,7 +1032,7 @@ static void step_fie(orc_solid* s, double h)
             for (uint32_t i = 0; i < N; i++) s->vk[i] = v_scale(inv_dt, v_sub(s->xk[i], s->x[i]));
             nr_delta_new = norm_2((const double*)s->y, 3 * N);
             nr_k++;
-            begin_evaluation_at(s, s->xk);
+            begin_evaluation_at(s, s->x, s->xk);
         }
     } while (!converged1 && nr_k < s->nr_max_iter);
     s->nr_iters = nr_k;
@@ -830,6 +1088,26 @@ void orc_solid_fixed_step(orc_solid* s)
     }
     s->elastic_energy = elastic_V(s);
     s->potential_energy = potential_energy(s);
+}
+
+void orc_solid_set_rotation(orc_solid* s, uint32_t method, double thr, double factor_L, double factor_NL,
+                            double exponent_NL)
+{
+    s->rotation = method;
+    s->dapd_thr = thr;
+    /* float32 fields in the reference (Params.h:29) */
+    s->dapd_L = (double)(float)factor_L;
+    s->dapd_NL = (double)(float)factor_NL;
+    s->dapd_exp = (double)(float)exponent_NL;
+    for (uint32_t e = 0; e < s->T; e++) s->doc[e] = kDocInvalid;
+}
+
+void orc_solid_doc(const orc_solid* s, uint8_t* doc2)
+{
+    for (uint32_t e = 0; e < s->T; e++) {
+        doc2[2 * (size_t)e] = s->doc[e].vit0;
+        doc2[2 * (size_t)e + 1] = s->doc[e].vit1;
+    }
 }
 
 void orc_solid_set_integrator(orc_solid* s, uint32_t integrator, uint32_t nr_max_iter, double nr_abs_eps)

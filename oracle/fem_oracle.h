@@ -37,6 +37,8 @@ extern "C" {
 #endif
 
 enum { FEM_ORC_MATH_DOUBLE = 0, FEM_ORC_MATH_FLOAT_LITERAL = 1 };
+/* ms::fem::Params::ERotationMethod values this oracle evaluates */
+enum { FEM_ORC_ROT_MSVD = 0, FEM_ORC_ROT_DAPD = 1 };
 /* LeafDSH_Solid3D_FEM::Params::EIntegratorType values this oracle steps */
 enum { FEM_ORC_QIE_V = 0, FEM_ORC_FIE_DX = 1, FEM_ORC_FIE_DX_QUASISTATIC = 2 };
 
@@ -57,6 +59,12 @@ void orc_solid_set_knc_targets(orc_solid* s, const double* targets);
 void orc_solid_set_state(orc_solid* s, const double* x, const double* v);
 void orc_solid_get_state(const orc_solid* s, double* x, double* v);
 void orc_solid_fixed_step(orc_solid* s);
+/* Rotation method (FEM_ORC_ROT_*) with the DAPD degeneration threshold on
+ * det F and the offset factors; resets every element's direction of collapse. */
+void orc_solid_set_rotation(orc_solid* s, uint32_t method, double thr, double factor_L, double factor_NL,
+                            double exponent_NL);
+/* Per-element direction of collapse (vit0, vit1), T*2 bytes; (3, 0) = none. */
+void orc_solid_doc(const orc_solid* s, uint8_t* doc2);
 /* Integrator (FEM_ORC_*), Newton iteration cap and |b_k| epsilon (FIE only). */
 void orc_solid_set_integrator(orc_solid* s, uint32_t integrator, uint32_t nr_max_iter, double nr_abs_eps);
 /* Newton iterations, |last| / |b_0| and |last| of the last FIE step (0 for QIE). */

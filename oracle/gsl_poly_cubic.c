@@ -3,8 +3,9 @@
  * ascending order, count returned). Restated from the published method:
  * depress with x = t - a/3, then Viete's trigonometric form when the
  * discriminant says three real roots, Cardano's formula otherwise.
- * Only ComputeDoC (TetrahedronElementSet3.cpp:586-743) calls it, and its
- * result does not reach the MSVD rotation path. */
+ * Only ComputeDoC (TetrahedronElementSet3.cpp:586-743) calls it: the DAPD
+ * rotation's time of collapse. Its result does not reach the MSVD path. Both
+ * the reference build and the oracle restatement link this one file. */
 #include <math.h>
 #include "shims/gsl/gsl_poly.h"
 

@@ -80,6 +80,7 @@ def _load(path: str, prefix: str):
     fn("solid_node_mass").argtypes = [C.c_void_p]
     fn("solid_node_mass").restype = C.c_double
     fn("solid_set_integrator").argtypes = [C.c_void_p, C.c_uint32, C.c_uint32, C.c_double]
+    fn("solid_set_rotation").argtypes = [C.c_void_p, C.c_uint32, C.c_double, C.c_double, C.c_double, C.c_double]
     fn("solid_last_nr_stats").argtypes = [C.c_void_p, _up, _dp, _dp]
     if P == "orc_":
         lib.orc_solid_begin_eval.argtypes = [C.c_void_p, _dp]
@@ -93,6 +94,7 @@ def _load(path: str, prefix: str):
         lib.orc_rotation_svd.argtypes = [_dp, _dp, C.c_int]
         lib.orc_solid_element_K.argtypes = [C.c_void_p, C.c_uint32, _dp]
         lib.orc_solid_set_solver.argtypes = [C.c_void_p, C.c_double, C.c_double, C.c_uint32]
+        lib.orc_solid_doc.argtypes = [C.c_void_p, C.POINTER(C.c_uint8)]
         lib.orc_solid_total_volume.argtypes = [C.c_void_p]
         lib.orc_solid_total_volume.restype = C.c_double
     else:
@@ -148,6 +150,9 @@ class Solid:
         if scene.init_vel is not None:
             v = _f64(scene.init_vel)
             getattr(self.lib, self.p + "solid_set_state")(self.h, None, _ptr(v))
+        if getattr(scene, "rotation", 0):
+            getattr(self.lib, self.p + "solid_set_rotation")(self.h, scene.rotation, scene.dapd_threshold,
+                                                              scene.dapd_L, scene.dapd_NL, scene.dapd_exponent)
         if getattr(scene, "integrator", 0):
             getattr(self.lib, self.p + "solid_set_integrator")(self.h, scene.integrator, scene.nr_max_iter,
                                                                 scene.nr_abs_eps)
@@ -247,6 +252,12 @@ class Solid:
 
     def V(self):
         return self.lib.orc_solid_V(self.h)
+
+    def doc(self):
+        """Per-element direction of collapse (vit0, vit1); (3, 0) = none."""
+        d = np.empty((self.T, 2), np.uint8)
+        self.lib.orc_solid_doc(self.h, d.ctypes.data_as(C.POINTER(C.c_uint8)))
+        return d
 
     def element_K(self, e):
         K = np.empty((4, 4, 3, 3))

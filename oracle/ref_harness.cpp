@@ -48,6 +48,17 @@ typedef ms::fem::TetrahedronElementSet3 TES3;
 class PerElementTES : public ms::fem::EditableTetrahedronElementSet3
 {
 public:
+    // ms::fem::Params::m_RM and the DAPD parameters (Params.h:27-29,63-67),
+    // set in place so that per-element materials stay baked.
+    void SetRotation(unsigned method, double thr, double factor_L, double factor_NL, double exponent_NL)
+    {
+        m_Params.m_RM = method ? ms::fem::Params::eRM_DAPD : ms::fem::Params::eRM_MSVD;
+        m_Params.m_DegenerateThresholdDetF = Real(thr);
+        m_Params.m_DAPD_L_Factor = float32(factor_L);
+        m_Params.m_DAPD_NL_Factor = float32(factor_NL);
+        m_Params.m_DAPD_NL_Exponent = float32(exponent_NL);
+    }
+
     void RebakePerElement(const double* E, const double* nu)
     {
         TES3::LinearED* led = const_cast<TES3::LinearED*>(m_vecLED);
@@ -381,6 +392,20 @@ static void step_fie(ref_solid* s, Real h)
     s->nr_abs = nr_delta_new;
     s->last_iters = ls_iters;
     for (unsigned i = 0; i < N; i++) { t->x[i] = s->xk[i]; t->v[i] = s->vk[i]; }
+}
+
+/* Rotation method (0 MSVD, 1 DAPD) and DAPD parameters; call before the
+ * first step (the caches' directions of collapse start invalid). */
+void ref_tes_set_rotation(ref_tes* h, unsigned method, double thr, double factor_L, double factor_NL,
+                          double exponent_NL)
+{
+    h->tes.SetRotation(method, thr, factor_L, factor_NL, exponent_NL);
+}
+
+void ref_solid_set_rotation(ref_solid* s, unsigned method, double thr, double factor_L, double factor_NL,
+                            double exponent_NL)
+{
+    ref_tes_set_rotation(s->t, method, thr, factor_L, factor_NL, exponent_NL);
 }
 
 void ref_solid_set_integrator(ref_solid* s, unsigned integrator, unsigned nr_max_iter, double nr_abs_eps)

@@ -22,6 +22,8 @@ FEM_PRECISION_MIXED = 1
 FEM_INTEGRATOR_QIE_V = 0
 FEM_INTEGRATOR_FIE_DX = 1
 FEM_INTEGRATOR_FIE_DX_QUASISTATIC = 2
+FEM_ROTATION_MSVD = 0
+FEM_ROTATION_DAPD = 1
 
 _dp = C.POINTER(C.c_double)
 _up = C.POINTER(C.c_uint32)
@@ -47,8 +49,12 @@ class FemParams(C.Structure):
         ("rotation_fp32", C.c_uint32),
         ("integrator", C.c_uint32),
         ("nr_max_iter", C.c_uint32),
-        ("pad", C.c_uint32),
+        ("rotation", C.c_uint32),
         ("nr_abs_epsilon", C.c_double),
+        ("dapd_threshold_det_F", C.c_double),
+        ("dapd_l_factor", C.c_double),
+        ("dapd_nl_factor", C.c_double),
+        ("dapd_nl_exponent", C.c_double),
     ]
 
 
@@ -94,6 +100,7 @@ SIGNATURES = {
     "fem_solid_step_host": (C.c_int, [C.c_void_p, _dp, _dp, C.c_uint32, _dp, _dp, C.POINTER(FemStepStats)]),
     "fem_solid_begin_eval": (C.c_int, [C.c_void_p, _dp]),
     "fem_solid_get_rotations": (C.c_int, [C.c_void_p, _dp, _dp]),
+    "fem_solid_get_doc": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint8)]),
     "fem_solid_force_elastic": (C.c_int, [C.c_void_p, _dp]),
     "fem_solid_df_x": (C.c_int, [C.c_void_p, _dp, _dp]),
     "fem_solid_apply_A": (C.c_int, [C.c_void_p, C.c_double, C.c_double, _dp, _dp]),
@@ -166,6 +173,12 @@ def params_for(scene, precision: int = FEM_PRECISION_FP64, compute_energy: bool 
     p.integrator = getattr(scene, "integrator", FEM_INTEGRATOR_QIE_V)
     p.nr_max_iter = getattr(scene, "nr_max_iter", 3)
     p.nr_abs_epsilon = getattr(scene, "nr_abs_eps", 1e-6)
+    p.rotation = getattr(scene, "rotation", FEM_ROTATION_MSVD)
+    if p.rotation == FEM_ROTATION_DAPD:
+        p.dapd_threshold_det_F = scene.dapd_threshold
+        p.dapd_l_factor = scene.dapd_L
+        p.dapd_nl_factor = scene.dapd_NL
+        p.dapd_nl_exponent = scene.dapd_exponent
     return p
 
 
@@ -250,6 +263,12 @@ class Solid:
         d = np.empty(self.T)
         check(self.lib.fem_solid_get_rotations(self.h, _ptr(R), _ptr(d)))
         return R, d
+
+    def doc(self):
+        """DAPD: per-element direction of collapse (vit0, vit1); (3, 0) = none."""
+        d = np.empty((self.T, 2), np.uint8)
+        check(self.lib.fem_solid_get_doc(self.h, d.ctypes.data_as(C.POINTER(C.c_uint8))))
+        return d
 
     def f_e(self):
         f = np.zeros((self.N, 3))

@@ -498,6 +498,8 @@ int fem_batch_add_mesh(fem_batch b, const double* rest, uint32_t N, const uint32
     if (p->integrator != FEM_INTEGRATOR_QIE_V)
         return batch_fail(FEM_E_ARG, "integrator %u: batches step with QIE_V; the FIE integrators run on fem_solid",
                           p->integrator);
+    if (p->rotation != FEM_ROTATION_MSVD)
+        return batch_fail(FEM_E_ARG, "rotation %u: batches use MSVD; DAPD runs on fem_solid", p->rotation);
     for (size_t i = 0; i < 4 * (size_t)T; i++)
         if (tets[i] >= N) return batch_fail(FEM_E_INDEX, "tet %zu names node %u >= N=%u", i / 4, tets[i], N);
     HostMesh m;

@@ -72,6 +72,9 @@ constexpr int kFinalizeThreads = 512;
 // ---- launchers (fem_kernels.cu / rotation.cu) ----
 void launch_begin_eval_fp64(const MeshView<double>& m, const double* x, double* F_out, StepScalars* st,
                             cudaStream_t s);
+struct DapdParams;
+void launch_begin_eval_dapd_fp64(const MeshView<double>& m, const double* xprev, const double* x, uchar2* doc,
+                                 const DapdParams& p, StepScalars* st, cudaStream_t s);
 void launch_elem_spmv_fp64(const MeshView<double>& m, const double* d, const StepScalars* st, int check_done,
                            cudaStream_t s);
 void launch_elem_force_fp64(const MeshView<double>& m, const double* x, int write_out, double* energy_partials,

@@ -203,9 +203,11 @@ template <typename T> __device__ __forceinline__ V3<T> largest_column_normalized
 
 // Rotation of one deformation gradient F (row-major 3x3) into R (row-major).
 // With `amb`, *amb is set when a branch decision was a near tie (see
-// near_tie); the arithmetic is the same with or without it.
+// near_tie); the arithmetic is the same with or without it. With
+// `v_smallest`, only column 2 of V (the right singular vector of the
+// smallest singular value) is formed, into *v_smallest, and R is not written.
 template <typename T>
-__device__ __forceinline__ void msvd_rotation(const T* F, T* R, bool* amb = nullptr)
+__device__ __forceinline__ void msvd_rotation(const T* F, T* R, bool* amb = nullptr, V3<T>* v_smallest = nullptr)
 {
     // normal equations F^T F (PhysBAM.h:129-137)
     Sym3<T> ne;
@@ -298,6 +300,10 @@ __device__ __forceinline__ void msvd_rotation(const T* F, T* R, bool* amb = null
     V3<T> c0, c1, c2;  // columns of V
     if (flipped) { c0 = v3; c1 = v2; c2 = mk<T>(-v1.x, -v1.y, -v1.z); }
     else { c0 = v1; c1 = v2; c2 = v3; }
+    if (v_smallest) {
+        *v_smallest = c2;
+        return;
+    }
 
     // U (GFastSVD3x3, PhysBAM.h:273-279)
     V3<T> u0 = normalized(matvec0(F, c0));

@@ -7,6 +7,7 @@
 // multiply-adds), which makes the GPU rotations equal to the reference's on
 // the same positions.
 #include "batch_launch.h"
+#include "dapd.cuh"
 #include "fem_device.cuh"
 #include "msvd.cuh"
 
@@ -49,6 +50,53 @@ void launch_begin_eval_fp64(const MeshView<double>& m, const double* x, double* 
                             cudaStream_t s)
 {
     k_begin_eval_fp64<<<grid_for(m.T), kBlock, 0, s>>>(m, x, F_out, st);
+    launch_counter()++;
+}
+
+// BeginEvaluation with the DAPD rotation (ComputeRotations_DAPD,
+// TetrahedronElementSet3.cpp:860-892): xprev are the positions the previous
+// evaluation's step started from (m_vecPos0), doc the per-element direction
+// of collapse carried between evaluations. Elements above the threshold take
+// the Newton polar rotation (a few 3x3 inverses); the collapse analysis runs
+// only on elements at or below it.
+__global__ void k_begin_eval_dapd_fp64(MeshView<double> m, const double* __restrict__ xprev,
+                                       const double* __restrict__ x, uchar2* doc, DapdParams p, StepScalars* st)
+{
+    unsigned inverted = 0;
+    for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < m.T; e += gridDim.x * blockDim.x) {
+        const int4 t = m.tets[e];
+        const int ids[4] = {t.x, t.y, t.z, t.w};
+        V3<double> xs[4], xp[4];
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            const size_t n = 3 * (size_t)ids[i];
+            xs[i] = mk<double>(x[n], x[n + 1], x[n + 2]);
+            xp[i] = mk<double>(xprev[n], xprev[n + 1], xprev[n + 2]);
+        }
+        double Di[9];
+#pragma unroll
+        for (int c = 0; c < 9; c++) Di[c] = m.Dinv[c * (size_t)m.T + e];
+        double F[9], detF;
+        deformation_gradient(xs, Di, F, detF);
+        uchar2 d = doc[e];
+        double R[9];
+        dapd_rotation(xp, xs, Di, F, detF, m.vol[e], p, d, R);
+        doc[e] = d;
+#pragma unroll
+        for (int c = 0; c < 9; c++) m.R[c * (size_t)m.T + e] = R[c];
+        m.detF[e] = detF;
+        inverted += (detF <= 0.0) ? 1u : 0u;
+    }
+    unsigned w = inverted;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) w += __shfl_down_sync(0xffffffffu, w, o);
+    if ((threadIdx.x & 31) == 0 && w) atomicAdd(&st->inverted, w);
+}
+
+void launch_begin_eval_dapd_fp64(const MeshView<double>& m, const double* xprev, const double* x, uchar2* doc,
+                                 const DapdParams& p, StepScalars* st, cudaStream_t s)
+{
+    k_begin_eval_dapd_fp64<<<grid_for(m.T), kBlock, 0, s>>>(m, xprev, x, doc, p, st);
     launch_counter()++;
 }
 

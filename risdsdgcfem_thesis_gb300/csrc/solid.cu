@@ -14,6 +14,7 @@
 // (Step_FullyImplicitEuler_dx, :1357-1552) runs its Newton loop on the host
 // over the same kernels, reading |b_k| and |y_k| once per Newton iteration.
 #include "../../include/fem_tet.h"
+#include "dapd.cuh"
 #include "fem_device.cuh"
 
 #include <cmath>
@@ -107,6 +108,11 @@ struct fem_solid_s {
     // node vectors
     DevBuf<double> rest, x, v, y, b, r, d, q, tmp;
     DevBuf<double> xn, vn;  // FIE: x^n and v^n of the step (allocated for the FIE integrators only)
+    // DAPD: the positions the previous step started from (m_vecPos0) and the
+    // per-element direction of collapse (allocated for DAPD only)
+    DevBuf<double> prev_x;
+    DevBuf<uchar2> doc;
+    DapdParams dapd{};
     // FIE statistics of the last step (host side; the Newton loop runs on the host)
     uint32_t nr_iters = 0, fie_cg_iters = 0;
     double nr_rel = 0, nr_abs = 0;
@@ -144,8 +150,9 @@ struct fem_solid_s {
     void release()
     {
         DevBuf<double>* dbl[] = {&Dinv, &mat, &vol, &R, &detF, &eout, &rest, &x, &v, &y, &b, &r, &d, &q, &tmp,
-                                 &xn, &vn, &knc_targets, &partials, &partials2};
+                                 &xn, &vn, &prev_x, &knc_targets, &partials, &partials2};
         for (auto* p : dbl) p->release();
+        doc.release();
         tets.release();
         csr_ptr.release();
         csr_idx.release();
@@ -164,6 +171,31 @@ namespace {
 int check_handle(fem_solid s)
 {
     if (!s) return fail(FEM_E_ARG, "null solid handle");
+    return FEM_OK;
+}
+
+bool uses_dapd(const fem_solid s) { return s->params.rotation == FEM_ROTATION_DAPD; }
+
+// TetrahedronElementSet3::BeginEvaluation(x0 = xprev, x): F, det F and the
+// rotations at x; xprev feeds the DAPD collapse detection only.
+void begin_eval(fem_solid s, const double* xprev, const double* x)
+{
+    MeshView<double> m = s->view();
+    if (uses_dapd(s))
+        launch_begin_eval_dapd_fp64(m, xprev, x, s->doc.p, s->dapd, s->st.p, s->stream);
+    else
+        launch_begin_eval_fp64(m, x, nullptr, s->st.p, s->stream);
+}
+
+// FixedStep's opening: BeginEvaluation(m_vecPos0, x), then m_vecPos0 = x
+// (LeafDSH_Solid3D_FEM.cpp:927-935).
+int open_step(fem_solid s)
+{
+    cudaStream_t st = s->stream;
+    CK(cudaMemsetAsync(&s->st.p->inverted, 0, sizeof(uint32_t), st));
+    begin_eval(s, s->prev_x.p, s->x.p);
+    if (uses_dapd(s))
+        CK(cudaMemcpyAsync(s->prev_x.p, s->x.p, sizeof(double) * 3 * (size_t)s->N, cudaMemcpyDeviceToDevice, st));
     return FEM_OK;
 }
 
@@ -241,8 +273,7 @@ int step_fie(fem_solid s, int chunk)
     c.factor_K = 1.0 + c.inv_dt * s->rayleigh[1];
     const size_t bytes = sizeof(double) * 3 * (size_t)s->N;
     const uint32_t gV = grid_for(3 * s->N);
-    CK(cudaMemsetAsync(&s->st.p->inverted, 0, sizeof(uint32_t), st));
-    launch_begin_eval_fp64(m, s->x.p, nullptr, s->st.p, st);
+    if (int e = open_step(s)) return e;
     CK(cudaMemcpyAsync(s->xn.p, s->x.p, bytes, cudaMemcpyDeviceToDevice, st));
     CK(cudaMemcpyAsync(s->vn.p, s->v.p, bytes, cudaMemcpyDeviceToDevice, st));
     uint32_t nr_k = 0, cg_iters = 0;
@@ -266,8 +297,9 @@ int step_fie(fem_solid s, int chunk)
             if (int e = host_sum(s, gV, &sum)) return e;
             delta_new = std::sqrt(sum);
             nr_k++;
+            // BeginEvaluation(x^n, x_k) (:1529)
             CK(cudaMemsetAsync(&s->st.p->inverted, 0, sizeof(uint32_t), st));
-            launch_begin_eval_fp64(m, s->x.p, nullptr, s->st.p, st);
+            begin_eval(s, s->xn.p, s->x.p);
         }
     } while (!converged && nr_k < s->params.nr_max_iter);
     s->nr_iters = nr_k;
@@ -288,8 +320,7 @@ int step_once(fem_solid s, int chunk)
     cudaStream_t st = s->stream;
     MeshView<double> m = s->view();
     const StepConsts& c = s->consts;
-    CK(cudaMemsetAsync(&s->st.p->inverted, 0, sizeof(uint32_t), st));
-    launch_begin_eval_fp64(m, s->x.p, nullptr, s->st.p, st);
+    if (int e = open_step(s)) return e;
     launch_elem_force_fp64(m, s->x.p, 1, nullptr, st);
     launch_node_b_fp64(m, c, s->v.p, s->b.p, s->y.p, st);
     launch_knc_fp64(s->knc_count, s->knc_nodes.p, s->knc_targets.p, s->x.p, c, s->b.p, s->y.p, st);
@@ -368,6 +399,12 @@ int fem_params_default(fem_params* p)
     p->integrator = FEM_INTEGRATOR_QIE_V;
     p->nr_max_iter = 3;
     p->nr_abs_epsilon = 1e-6;
+    // ms::fem::Params (Params.h:85-95)
+    p->rotation = FEM_ROTATION_MSVD;
+    p->dapd_threshold_det_F = (double)0.1f;
+    p->dapd_l_factor = 1.0;
+    p->dapd_nl_factor = 0.0;
+    p->dapd_nl_exponent = 2.0;
     return FEM_OK;
 }
 
@@ -387,6 +424,12 @@ int fem_solid_create(const double* rest_xyz, uint32_t N, const uint32_t* tets, u
         return fail(FEM_E_ARG, "integrator %u is not an enum fem_integrator value", params->integrator);
     if (params->integrator != FEM_INTEGRATOR_QIE_V && !(params->nr_abs_epsilon >= 0))
         return fail(FEM_E_ARG, "nr_abs_epsilon must be >= 0");
+    if (params->rotation > FEM_ROTATION_DAPD)
+        return fail(FEM_E_ARG, "rotation %u is not an enum fem_rotation value", params->rotation);
+    if (params->rotation == FEM_ROTATION_DAPD &&
+        !(std::isfinite(params->dapd_threshold_det_F) && std::isfinite(params->dapd_l_factor) &&
+          std::isfinite(params->dapd_nl_factor) && std::isfinite(params->dapd_nl_exponent)))
+        return fail(FEM_E_ARG, "DAPD threshold and factors must be finite");
     for (size_t i = 0; i < 4 * (size_t)T; i++)
         if (tets[i] >= N) return fail(FEM_E_INDEX, "tet %zu names node %u >= N=%u", i / 4, tets[i], N);
     int ndev = 0;
@@ -499,6 +542,14 @@ int fem_solid_create(const double* rest_xyz, uint32_t N, const uint32_t* tets, u
         CKC(s->xn.alloc(n3));
         CKC(s->vn.alloc(n3));
     }
+    if (params->rotation == FEM_ROTATION_DAPD) {
+        CKC(s->prev_x.alloc(n3));
+        CKC(s->doc.alloc(T));
+        s->dapd.thr = params->dapd_threshold_det_F;
+        s->dapd.fL = (double)(float)params->dapd_l_factor;
+        s->dapd.fNL = (double)(float)params->dapd_nl_factor;
+        s->dapd.eNL = (double)(float)params->dapd_nl_exponent;
+    }
     CKC(s->partials.alloc(4096));
     CKC(s->partials2.alloc(4096));
     CKC(s->st.alloc(1));
@@ -513,6 +564,12 @@ int fem_solid_create(const double* rest_xyz, uint32_t N, const uint32_t* tets, u
     CKC(cudaMemsetAsync(s->fixed.p, 0, N, st));
     CKC(cudaMemcpyAsync(s->rest.p, rest_xyz, sizeof(double) * n3, cudaMemcpyHostToDevice, st));
     CKC(cudaMemcpyAsync(s->x.p, rest_xyz, sizeof(double) * n3, cudaMemcpyHostToDevice, st));
+    if (params->rotation == FEM_ROTATION_DAPD) {
+        CKC(cudaMemcpyAsync(s->prev_x.p, rest_xyz, sizeof(double) * n3, cudaMemcpyHostToDevice, st));
+        const std::vector<uchar2> none(T, make_uchar2(3, 0));  // no direction of collapse
+        CKC(cudaMemcpyAsync(s->doc.p, none.data(), sizeof(uchar2) * T, cudaMemcpyHostToDevice, st));
+        CKC(cudaStreamSynchronize(st));
+    }
     CKC(cudaMemsetAsync(s->v.p, 0, sizeof(double) * n3, st));
     CKC(cudaMemsetAsync(s->y.p, 0, sizeof(double) * n3, st));
     CKC(cudaMemsetAsync(s->st.p, 0, sizeof(StepScalars), st));
@@ -586,6 +643,9 @@ int fem_solid_set_state(fem_solid s, const double* x, const double* v)
     if (int e = check_handle(s)) return e;
     const size_t bytes = sizeof(double) * 3 * (size_t)s->N;
     if (x) CK(cudaMemcpyAsync(s->x.p, x, bytes, cudaMemcpyHostToDevice, s->stream));
+    // the previous-step positions restart at x (the Leaf's SetPos path keeps
+    // m_vecPos0 in step with the model's positions)
+    if (x && uses_dapd(s)) CK(cudaMemcpyAsync(s->prev_x.p, x, bytes, cudaMemcpyHostToDevice, s->stream));
     if (v) CK(cudaMemcpyAsync(s->v.p, v, bytes, cudaMemcpyHostToDevice, s->stream));
     CK(cudaStreamSynchronize(s->stream));
     return FEM_OK;
@@ -652,7 +712,7 @@ int fem_solid_begin_eval(fem_solid s, const double* x)
     if (!x) return fail(FEM_E_ARG, "null positions");
     CK(cudaMemcpyAsync(s->tmp.p, x, sizeof(double) * 3 * (size_t)s->N, cudaMemcpyHostToDevice, s->stream));
     CK(cudaMemsetAsync(&s->st.p->inverted, 0, sizeof(uint32_t), s->stream));
-    launch_begin_eval_fp64(s->view(), s->tmp.p, nullptr, s->st.p, s->stream);
+    begin_eval(s, s->prev_x.p, s->tmp.p);
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(s->stream));
     s->evaluated = true;
@@ -674,6 +734,16 @@ int fem_solid_get_rotations(fem_solid s, double* R, double* detF)
         CK(cudaMemcpyAsync(detF, s->detF.p, sizeof(double) * T, cudaMemcpyDeviceToHost, s->stream));
         CK(cudaStreamSynchronize(s->stream));
     }
+    return FEM_OK;
+}
+
+int fem_solid_get_doc(fem_solid s, uint8_t* doc)
+{
+    if (int e = check_handle(s)) return e;
+    if (!doc) return fail(FEM_E_ARG, "null output");
+    if (!uses_dapd(s)) return fail(FEM_E_ARG, "the solid does not use the DAPD rotation");
+    CK(cudaMemcpyAsync(doc, s->doc.p, sizeof(uchar2) * s->T, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
     return FEM_OK;
 }
 

@@ -74,6 +74,14 @@ class Scene:
     integrator: int = 0
     nr_max_iter: int = 3
     nr_abs_eps: float = 1e-6
+    # Rotation method (enum fem_rotation: 0 MSVD, 1 DAPD) and the DAPD
+    # degeneration threshold on det F and offset factors (the reference's
+    # defaults: 0.1f, 1, 0, 2).
+    rotation: int = 0
+    dapd_threshold: float = float(np.float32(0.1))
+    dapd_L: float = 1.0
+    dapd_NL: float = 0.0
+    dapd_exponent: float = 2.0
 
     @property
     def num_nodes(self) -> int:

@@ -20,7 +20,16 @@ units with Mal's Sqrt/Sin/Cos/ATan2 at double precision, except where noted):
                        E and nu, damping, an initial velocity and a moving
                        constraint: per-step statistics, final x and v.
 
-python tests/golden/make_golden.py fie   writes only the two FIE fixtures.
+  dapd_cube.npz        the DAPD rotation (ms::fem::Params::eRM_DAPD, threshold
+                       0.1f) on a 6^3-cube block crushed to 15 % of its height
+                       over 30 steps (elements invert): per-step statistics,
+                       final x, v and per-element direction of collapse, with
+                       the QIE integrator (prefix qie_) and FIE (fie_). The
+                       directions of collapse are the restatement's, whose x
+                       and v equal the reference build's bit for bit.
+
+python tests/golden/make_golden.py fie    writes only the two FIE fixtures;
+python tests/golden/make_golden.py dapd   only the DAPD fixture.
 """
 import dataclasses
 import os
@@ -104,13 +113,43 @@ def fie_fixtures():
     np.savez_compressed(os.path.join(HERE, "fie_block.npz"), x=x, v=v, **_stat_arrays(stats))
 
 
+def dapd_scene(integrator):
+    return dataclasses.replace(scenes.compressed_cube(n=6, steps=30, ratio=0.15), rotation=1,
+                               integrator=integrator)
+
+
+def dapd_fixture():
+    out = {}
+    for prefix, integ in (("qie_", 0), ("fie_", 1)):
+        sc = dapd_scene(integ)
+        ref = O.Solid(sc, "ref_dbl")
+        port = O.Solid(sc, "port")
+        stats = []
+        for _ in range(30):
+            stats.append(ref.step())
+            assert port.step() == stats[-1]
+        x, v = ref.state()
+        xp, vp = port.state()
+        assert np.array_equal(x, xp) and np.array_equal(v, vp)
+        out.update(_stat_arrays(stats, prefix))
+        out[prefix + "x"] = x
+        out[prefix + "v"] = v
+        out[prefix + "doc"] = port.doc()
+    np.savez_compressed(os.path.join(HERE, "dapd_cube.npz"), **out)
+
+
 def main():
     O.build(reference=True)
     if sys.argv[1:] == ["fie"]:
         fie_fixtures()
         print("wrote FIE fixtures to", HERE)
         return
+    if sys.argv[1:] == ["dapd"]:
+        dapd_fixture()
+        print("wrote the DAPD fixture to", HERE)
+        return
     fie_fixtures()
+    dapd_fixture()
     sc = scenes.cantilever_160()
 
     ref = O.Solid(sc, "ref_dbl")

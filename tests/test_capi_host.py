@@ -45,6 +45,9 @@ def test_params_default_matches_reference_defaults(fem_lib):
     assert p.refresh_drop == 0.0 and p.refresh_every == 50
     # LeafDSH_Solid3D_FEM::Params: QIE_V integrator, 3 Newton iterations, NR abs epsilon 1e-6
     assert p.integrator == fem_lib.FEM_INTEGRATOR_QIE_V and p.nr_max_iter == 3 and p.nr_abs_epsilon == 1e-6
+    # ms::fem::Params: MSVD rotations; DAPD threshold 0.1f, factors 1, 0, 2
+    assert p.rotation == fem_lib.FEM_ROTATION_MSVD and p.dapd_threshold_det_F == float(np.float32(0.1))
+    assert (p.dapd_l_factor, p.dapd_nl_factor, p.dapd_nl_exponent) == (1.0, 0.0, 2.0)
 
 
 def test_create_rejects_bad_integrator(fem_lib):
@@ -57,6 +60,14 @@ def test_create_rejects_bad_integrator(fem_lib):
     p.nr_abs_epsilon = -1.0
     code, h, msg = _create(fem_lib, rest, tets, p)
     assert code == fem_lib.FEM_E_ARG and "nr_abs_epsilon" in msg
+    p = fem_lib.default_params()
+    p.rotation = 2
+    code, h, msg = _create(fem_lib, rest, tets, p)
+    assert code == fem_lib.FEM_E_ARG and "rotation" in msg
+    p.rotation = fem_lib.FEM_ROTATION_DAPD
+    p.dapd_threshold_det_F = float("nan")
+    code, h, msg = _create(fem_lib, rest, tets, p)
+    assert code == fem_lib.FEM_E_ARG and "DAPD" in msg
 
 
 def _create(fem_lib, rest, tets, params=None):
