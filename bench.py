@@ -348,6 +348,38 @@ def fie_leg(n=40, steps=2, cpu_n=16):
     return out
 
 
+def rotation_leg(n=60, reps=5):
+    """BeginEvaluation (F, det F, rotation) on the FP64 solid, MSVD against
+    DAPD, on the n^3 block crushed to 15 % of its height with lateral noise:
+    DAPD takes the Newton polar rotation above det F = 0.1 and the
+    time-of-collapse analysis at or below it. Kernel time from CUDA events
+    around each launch on the solid's stream."""
+    import dataclasses
+    from risdsdgcfem_thesis_gb300 import capi, scenes
+    sc = scenes.large_block(n=n)
+    rng = np.random.default_rng(5)
+    x1 = sc.rest.copy()
+    x1[:, 2] *= 0.15
+    x1 += 0.15 * sc.h * rng.standard_normal(x1.shape)
+    out = {"workload": f"{sc.name} ({sc.num_tets} tets) crushed to 15 % of its height, lateral noise 0.15 h"}
+    for name, rot, kname in (("msvd", capi.FEM_ROTATION_MSVD, "begin_eval_msvd_fp64"),
+                             ("dapd", capi.FEM_ROTATION_DAPD, "begin_eval_dapd_fp64")):
+        s = capi.Solid(dataclasses.replace(sc, rotation=rot), compute_energy=False)
+        s.begin_eval(x1)  # warm-up (and, for DAPD, the directions of collapse from the rest state)
+        capi.profile_enable(True)
+        for _ in range(reps):
+            s.begin_eval(x1)
+        capi.profile_enable(False)
+        ms, k = capi.profile_read(kname)
+        _, detF = s.rotations()
+        s.close()
+        us = 1e3 * ms / max(k, 1)
+        out[name] = {"us_per_launch": us, "tets_per_s": sc.num_tets / (us * 1e-6), "launches": k}
+        out["degenerate_fraction"] = float(np.mean(detF <= float(np.float32(0.1))))
+    out["dapd_over_msvd_time"] = out["dapd"]["us_per_launch"] / out["msvd"]["us_per_launch"]
+    return out
+
+
 def run_ours(args):
     import torch
     from risdsdgcfem_thesis_gb300 import capi
@@ -432,6 +464,7 @@ def run_ours(args):
 
     plain = None
     fie = None
+    rotations = None
     cpu = None
     served = None
     compression = None
@@ -444,6 +477,7 @@ def run_ours(args):
             plain = plain_fp64_comparator(3)
         if not args.no_fie:
             fie = fie_leg()
+            rotations = rotation_leg()
         if not args.no_cpu:
             sample = cpu_sample_set(scs, 1_500_000)
             threads = (os.cpu_count() or 1) if len(sample) > 1 else 1
@@ -493,6 +527,7 @@ def run_ours(args):
                                            "iteration (16 + 20 s_e per tet + 33 s_v per node)"},
             "plain_fp64_gpu": plain,
             "fie_fp64_gpu": fie,
+            "rotations_fp64_gpu": rotations,
             "cpu_baseline": cpu,
             "served": served,
             "compression": compression,
@@ -645,7 +680,8 @@ def main():
     ap.add_argument("--workload", default="batch1024")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
-    ap.add_argument("--no-fie", action="store_true", help="skip the fully-implicit Euler leg")
+    ap.add_argument("--no-fie", action="store_true",
+                    help="skip the fully-implicit Euler and MSVD/DAPD rotation legs")
     ap.add_argument("--no-graph", action="store_true", help="launch kernels one by one (for per-kernel profilers)")
     ap.add_argument("--no-served", action="store_true")
     ap.add_argument("--no-compression", action="store_true")

@@ -49,7 +49,9 @@ __global__ void k_begin_eval_fp64(MeshView<double> m, const double* __restrict__
 void launch_begin_eval_fp64(const MeshView<double>& m, const double* x, double* F_out, StepScalars* st,
                             cudaStream_t s)
 {
+    prof_begin("begin_eval_msvd_fp64", s);
     k_begin_eval_fp64<<<grid_for(m.T), kBlock, 0, s>>>(m, x, F_out, st);
+    prof_end("begin_eval_msvd_fp64", s);
     launch_counter()++;
 }
 
@@ -96,7 +98,9 @@ __global__ void k_begin_eval_dapd_fp64(MeshView<double> m, const double* __restr
 void launch_begin_eval_dapd_fp64(const MeshView<double>& m, const double* xprev, const double* x, uchar2* doc,
                                  const DapdParams& p, StepScalars* st, cudaStream_t s)
 {
+    prof_begin("begin_eval_dapd_fp64", s);
     k_begin_eval_dapd_fp64<<<grid_for(m.T), kBlock, 0, s>>>(m, xprev, x, doc, p, st);
+    prof_end("begin_eval_dapd_fp64", s);
     launch_counter()++;
 }
 
