@@ -64,6 +64,19 @@ enum fem_integrator {
     FEM_INTEGRATOR_FIE_DX_QUASISTATIC = 2
 };
 
+/* Linear solvers of the step (LeafDSH_Solid3D_FEM::Params::m_SolverLS_Type,
+ * LS_Solve, LeafDSH_Solid3D_FEM.cpp:1136-1154). Both stop on |r|^2 <= abs^2,
+ * on a relative test, or at ls_max_iter. */
+enum fem_ls_solver {
+    /* ns::ILSS_CG (ILSS_CG.h:38-151): relative test |r|^2 <= rel^2 |r0|^2,
+     * breakdown when |d.q| < abs^2. The default. */
+    FEM_LS_CG = 0,
+    /* ns::ILSS_MINRES (ILSS_MINRES.h:51-168): Paige-Saunders MINRES without
+     * a preconditioner; |r| carried by the Givens sines, relative test
+     * |r|^2 <= rel^2 |b|^2. FP64 solid only. */
+    FEM_LS_MINRES = 1
+};
+
 /* Rotation methods of the element set (ms::fem::Params::ERotationMethod,
  * Params.h:63-67; ComputeRotations_*, TetrahedronElementSet3.cpp:267-278). */
 enum fem_rotation {
@@ -119,6 +132,7 @@ typedef struct fem_params {
     uint32_t integrator;      /* enum fem_integrator; the batch and server paths take QIE_V only */
     uint32_t nr_max_iter;     /* FIE: Newton iteration cap per step (m_SolverNR_MaxIter) */
     uint32_t rotation;        /* enum fem_rotation; the batch and server paths take MSVD only */
+    uint32_t ls_solver;       /* enum fem_ls_solver; the batch and server paths take CG only */
     double nr_abs_epsilon;    /* FIE: Newton stops once |b_k| < this (m_SolverNR_AbsEpsilon) */
     double dapd_threshold_det_F; /* DAPD: degenerate at or below this det F
                                     (m_DegenerateThresholdDetF, default 0.1f) */
@@ -152,7 +166,7 @@ typedef struct fem_solid_s* fem_solid;
  * fixed_dt 0.001, density 1000, E 1000, nu 0.25, damping 1, gravity 0,
  * CG rel 1e-3, abs 1e-6, 20 iterations, FP64, threshold 1e-3, refresh 50,
  * energy on, rotation check 1e-3, refresh every 50 iterations (no drop rule),
- * QIE_V integrator, 3 Newton iterations with abs epsilon 1e-6, MSVD
+ * QIE_V integrator, 3 Newton iterations with abs epsilon 1e-6, CG, MSVD
  * rotations (DAPD threshold 0.1f, factors 1, 0, 2). */
 int fem_params_default(fem_params* p);
 

@@ -651,6 +651,10 @@ struct orc_solid {
     uint32_t rotation;
     double dapd_thr, dapd_L, dapd_NL, dapd_exp;
     doc_t* doc;           /* per-element direction of collapse (ElementCache3::m_DoC) */
+    /* linear solver (LeafDSH_Solid3D_FEM::Params::m_SolverLS_Type) and the
+     * MINRES work vectors v, v0, v1, w, w1, p, p0, p0_tmp (3N each) */
+    uint32_t ls_solver;
+    double* mr;
 };
 
 static vec3 load3(const double* p) { return v3(p[0], p[1], p[2]); }
@@ -746,7 +750,7 @@ void orc_solid_destroy(orc_solid* s)
     if (!s) return;
     free(s->ref_pos); free(s->tets); free(s->volume); free(s->inv_Dm); free(s->K); free(s->R);
     free(s->detF); free(s->x); free(s->prev_x); free(s->v); free(s->b); free(s->y);
-    free(s->r); free(s->d); free(s->q); free(s->xk); free(s->vk); free(s->doc);
+    free(s->r); free(s->d); free(s->q); free(s->xk); free(s->vk); free(s->doc); free(s->mr);
     free(s->knc_nid); free(s->knc_pos); free(s->knc_vel);
     free(s);
 }
@@ -974,6 +978,8 @@ static void cg_solve(orc_solid* s, double* x, const double* b)
     s->last_abs = mal_sqrt(delta_new);
 }
 
+static void ls_solve(orc_solid* s, double* x, const double* b);
+
 /* real_array::norm_2 (src/Saphyre2/ns/real_array.h:97-98) */
 static double norm_2(const double* v, uint32_t n)
 {
@@ -1026,7 +1032,7 @@ static void step_fie(orc_solid* s, double h)
         if (!converged1) {
             s->factor_M = inv_dt * inv_dt + inv_dt * s->rayleigh[0];
             s->factor_K = 1.0 + inv_dt * s->rayleigh[1];
-            cg_solve(s, (double*)s->y, (const double*)s->b);
+            ls_solve(s, (double*)s->y, (const double*)s->b);
             ls_iters += s->last_iters;
             for (uint32_t i = 0; i < N; i++) s->xk[i] = v_add(s->xk[i], s->y[i]);
             for (uint32_t i = 0; i < N; i++) s->vk[i] = v_scale(inv_dt, v_sub(s->xk[i], s->x[i]));
@@ -1040,6 +1046,98 @@ static void step_fie(orc_solid* s, double h)
     s->nr_abs = nr_delta_new;
     s->last_iters = ls_iters;
     for (uint32_t i = 0; i < N; i++) { s->x[i] = s->xk[i]; s->v[i] = s->vk[i]; }
+}
+
+/* ILSS_MINRES::Solve (src/Saphyre2/ns/ILSS_MINRES.h:51-168): Paige-Saunders
+ * MINRES without a preconditioner, the scalar real_array kernels
+ * (src/Saphyre2/ns/real_array.h:91-113), the residual norm carried by the
+ * Givens sines, stopping on |r|^2 <= abs^2, |r|^2 <= rel^2 |b|^2 or the
+ * iteration cap. */
+static void minres_solve(orc_solid* s, double* x, const double* b)
+{
+    const uint32_t n = 3 * s->N;
+    double *v = s->mr, *v0 = v + n, *v1 = v0 + n, *w = v1 + n, *w1 = w + n, *p = w1 + n, *p0 = p + n,
+           *p0_tmp = p0 + n;
+    const double fM = s->factor_M, fK = s->factor_K;
+    double abs_epsilon_sq = s->abs_eps * s->abs_eps;
+    memset(v, 0, sizeof(double) * n);
+    a_times_d(s, fM, fK, x, v1);
+    for (uint32_t i = 0; i < n; i++) v1[i] = -1 * v1[i] + b[i];
+    zero_knc(s, v1);
+    double norm_r_sq = 0;
+    for (uint32_t i = 0; i < n; i++) norm_r_sq += v1[i] * v1[i];
+    memcpy(w1, v1, sizeof(double) * n);
+    double beta_new_sq = 0;
+    for (uint32_t i = 0; i < n; i++) beta_new_sq += v1[i] * w1[i];
+    double beta_new = mal_sqrt(beta_new_sq);
+    double beta_one = beta_new;
+    {
+        double inv = 1.0 / beta_new;
+        for (uint32_t i = 0; i < n; i++) v1[i] *= inv;
+        for (uint32_t i = 0; i < n; i++) w1[i] *= inv;
+    }
+    double c = 1.0, c_old = 1.0, sn = 0.0, sn_old = 0.0;
+    memset(p0, 0, sizeof(double) * n);
+    memset(p, 0, sizeof(double) * n);
+    double eta = 1.0;
+    uint32_t k = 0;
+    double norm_b_sq = 0;
+    for (uint32_t i = 0; i < n; i++) norm_b_sq += b[i] * b[i];
+    double delta_target = (s->rel_eps * s->rel_eps) * norm_b_sq;
+    while (norm_r_sq > abs_epsilon_sq && norm_r_sq > delta_target && k < s->max_iter) {
+        double beta = beta_new;
+        memcpy(v0, v, sizeof(double) * n);
+        memcpy(v, v1, sizeof(double) * n);
+        memcpy(w, w1, sizeof(double) * n);
+        a_times_d(s, fM, fK, w, v1);
+        zero_knc(s, v1);
+        for (uint32_t i = 0; i < n; i++) v1[i] += -beta * v0[i];
+        double alpha = 0;
+        for (uint32_t i = 0; i < n; i++) alpha += v1[i] * w[i];
+        for (uint32_t i = 0; i < n; i++) v1[i] += -alpha * v[i];
+        memcpy(w1, v1, sizeof(double) * n);
+        beta_new_sq = 0;
+        for (uint32_t i = 0; i < n; i++) beta_new_sq += v1[i] * w1[i];
+        beta_new = mal_sqrt(beta_new_sq);
+        {
+            double inv = 1.0 / beta_new;
+            for (uint32_t i = 0; i < n; i++) v1[i] *= inv;
+            for (uint32_t i = 0; i < n; i++) w1[i] *= inv;
+        }
+        const double r2 = sn * alpha + c * c_old * beta;
+        const double r3 = sn_old * beta;
+        const double r1_hat = c * alpha - c_old * sn * beta;
+        const double r1 = mal_sqrt(r1_hat * r1_hat + beta_new_sq);
+        c_old = c;
+        sn_old = sn;
+        c = r1_hat / r1;
+        sn = beta_new / r1;
+        memcpy(p0_tmp, p0, sizeof(double) * n);
+        memcpy(p0, p, sizeof(double) * n);
+        for (uint32_t i = 0; i < n; i++) p[i] = -r2 * p[i] + w[i];
+        for (uint32_t i = 0; i < n; i++) p[i] += -r3 * p0_tmp[i];
+        {
+            double inv = 1.0 / r1;
+            for (uint32_t i = 0; i < n; i++) p[i] *= inv;
+        }
+        {
+            double coef = beta_one * c * eta;
+            for (uint32_t i = 0; i < n; i++) x[i] += coef * p[i];
+        }
+        norm_r_sq *= sn * sn;
+        eta = -sn * eta;
+        k++;
+    }
+    s->last_iters = k;
+    s->last_rel = mal_sqrt(norm_r_sq / norm_b_sq);
+    s->last_abs = mal_sqrt(norm_r_sq);
+}
+
+/* LS_Solve's solver choice (LeafDSH_Solid3D_FEM.cpp:1136-1154) */
+static void ls_solve(orc_solid* s, double* x, const double* b)
+{
+    if (s->ls_solver == FEM_ORC_LS_MINRES) minres_solve(s, x, b);
+    else cg_solve(s, x, b);
 }
 
 /* FixedStep (LeafDSH_Solid3D_FEM.cpp:898-990) with
@@ -1081,7 +1179,7 @@ void orc_solid_fixed_step(orc_solid* s)
     }
     s->factor_M = 1.0 + dt * s->rayleigh[0];
     s->factor_K = dt * dt + dt * s->rayleigh[1];
-    cg_solve(s, (double*)s->y, (const double*)s->b);
+    ls_solve(s, (double*)s->y, (const double*)s->b);
     for (uint32_t i = 0; i < N; i++) {
         s->v[i] = s->y[i];
         s->x[i] = v_add(s->x[i], v_scale(dt, s->y[i]));
@@ -1108,6 +1206,12 @@ void orc_solid_doc(const orc_solid* s, uint8_t* doc2)
         doc2[2 * (size_t)e] = s->doc[e].vit0;
         doc2[2 * (size_t)e + 1] = s->doc[e].vit1;
     }
+}
+
+void orc_solid_set_ls_solver(orc_solid* s, uint32_t ls_solver)
+{
+    s->ls_solver = ls_solver;
+    if (ls_solver == FEM_ORC_LS_MINRES && !s->mr) s->mr = (double*)malloc(sizeof(double) * 8 * 3 * (size_t)s->N);
 }
 
 void orc_solid_set_integrator(orc_solid* s, uint32_t integrator, uint32_t nr_max_iter, double nr_abs_eps)

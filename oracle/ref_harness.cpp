@@ -35,6 +35,7 @@
 #include <Saphyre2/ms/fem/TetrahedronElement3.h>
 #include <Saphyre2/ms/fem/Rotation.h>
 #include <Saphyre2/ns/ILSS_CG.h>
+#include <Saphyre2/ns/ILSS_MINRES.h>
 #include <vector>
 #include <cstdint>
 #include <cstring>
@@ -109,6 +110,8 @@ struct ref_solid {
     Real elastic_energy, potential_energy;
     std::vector<Vec3> b, y;
     ns::ILSS_CG cg;
+    ns::ILSS_MINRES minres;
+    unsigned ls_solver;  // 0 CG, 1 MINRES (Params::m_SolverLS_Type)
     Real factor_M, factor_K;
     unsigned last_iters;
     Real last_rel, last_abs;
@@ -235,6 +238,8 @@ ref_solid* ref_solid_create(unsigned N, const double* rest, unsigned T, const ui
     s->b.assign(N, Vec3::Zero());
     s->y.assign(N, Vec3::Zero());
     s->cg.Init(3 * N);
+    s->minres.Init(3 * N);
+    s->ls_solver = 0;
     s->last_iters = 0; s->last_rel = s->last_abs = 0;
     s->integrator = 0; s->nr_max_iter = 3; s->nr_abs_eps = Real(1e-6);
     s->xk.assign(N, Vec3::Zero());
@@ -329,6 +334,21 @@ static void a_times_d(const ref_solid* s, Real* q, const Real* d)
 
 static void finish_step(ref_solid* s);
 
+/* LS_Solve (LeafDSH_Solid3D_FEM.cpp:1081-1154): the chosen solver's Solve
+ * with the Leaf's A*v and constraint delegates. */
+static void ls_solve(ref_solid* s)
+{
+    ns::IIterativeLinearSystemSolver* ls = s->ls_solver ? static_cast<ns::IIterativeLinearSystemSolver*>(&s->minres)
+                                                       : static_cast<ns::IIterativeLinearSystemSolver*>(&s->cg);
+    ls->Solve([s](Real* Av, const Real* v) { a_times_d(s, Av, v); },
+              [s](Real* v) { zero_knc(s, reinterpret_cast<Vec3*>(v)); },
+              reinterpret_cast<Real*>(&s->y[0]), reinterpret_cast<const Real*>(&s->b[0]),
+              s->rel_eps, s->abs_eps, s->max_iter);
+    s->last_iters = ls->GetNumIterations();
+    s->last_rel = ls->GetRelResidual();
+    s->last_abs = ls->GetAbsResidual();
+}
+
 /* Restated Step_FullyImplicitEuler_dx (LeafDSH_Solid3D_FEM.cpp:1357-1552)
  * around the reference's element set and CG: contacts off, warm start on,
  * CG solver. h = 0 is the quasi-static variant (:958-959). */
@@ -371,13 +391,8 @@ static void step_fie(ref_solid* s, Real h)
         if (!converged1) {
             s->factor_M = mal::Sq(inv_dt) + inv_dt * s->rayleigh[0];
             s->factor_K = Real(1) + inv_dt * s->rayleigh[1];
-            s->cg.Solve([s](Real* Av, const Real* v) { a_times_d(s, Av, v); },
-                        [s](Real* v) { zero_knc(s, reinterpret_cast<Vec3*>(v)); },
-                        reinterpret_cast<Real*>(&s->y[0]), reinterpret_cast<const Real*>(&s->b[0]),
-                        s->rel_eps, s->abs_eps, s->max_iter);
-            ls_iters += s->cg.GetNumIterations();
-            s->last_rel = s->cg.GetRelResidual();
-            s->last_abs = s->cg.GetAbsResidual();
+            ls_solve(s);
+            ls_iters += s->last_iters;
             ns::real_array::addeq(reinterpret_cast<Real*>(&s->xk[0]), reinterpret_cast<const Real*>(&s->y[0]), cN);
             for (unsigned i = 0; i < N; i++) s->vk[i] = inv_dt * (s->xk[i] - t->x[i]);
             nr_delta_new = ns::real_array::norm_2(reinterpret_cast<const Real*>(&s->y[0]), cN);
@@ -407,6 +422,8 @@ void ref_solid_set_rotation(ref_solid* s, unsigned method, double thr, double fa
 {
     ref_tes_set_rotation(s->t, method, thr, factor_L, factor_NL, exponent_NL);
 }
+
+void ref_solid_set_ls_solver(ref_solid* s, unsigned ls_solver) { s->ls_solver = ls_solver; }
 
 void ref_solid_set_integrator(ref_solid* s, unsigned integrator, unsigned nr_max_iter, double nr_abs_eps)
 {
@@ -460,13 +477,7 @@ void ref_solid_fixed_step(ref_solid* s)
     }
     s->factor_M = Real(1) + dt * s->rayleigh[0];
     s->factor_K = mal::Sq(dt) + dt * s->rayleigh[1];
-    s->cg.Solve([s](Real* Av, const Real* v) { a_times_d(s, Av, v); },
-                [s](Real* v) { zero_knc(s, reinterpret_cast<Vec3*>(v)); },
-                reinterpret_cast<Real*>(&s->y[0]), reinterpret_cast<const Real*>(&s->b[0]),
-                s->rel_eps, s->abs_eps, s->max_iter);
-    s->last_iters = s->cg.GetNumIterations();
-    s->last_rel = s->cg.GetRelResidual();
-    s->last_abs = s->cg.GetAbsResidual();
+    ls_solve(s);
     for (unsigned i = 0; i < N; i++) {
         t->v[i] = s->y[i];
         t->x[i] = t->x[i] + dt * s->y[i];

@@ -24,6 +24,8 @@ FEM_INTEGRATOR_FIE_DX = 1
 FEM_INTEGRATOR_FIE_DX_QUASISTATIC = 2
 FEM_ROTATION_MSVD = 0
 FEM_ROTATION_DAPD = 1
+FEM_LS_CG = 0
+FEM_LS_MINRES = 1
 
 _dp = C.POINTER(C.c_double)
 _up = C.POINTER(C.c_uint32)
@@ -50,6 +52,7 @@ class FemParams(C.Structure):
         ("integrator", C.c_uint32),
         ("nr_max_iter", C.c_uint32),
         ("rotation", C.c_uint32),
+        ("ls_solver", C.c_uint32),
         ("nr_abs_epsilon", C.c_double),
         ("dapd_threshold_det_F", C.c_double),
         ("dapd_l_factor", C.c_double),
@@ -173,6 +176,7 @@ def params_for(scene, precision: int = FEM_PRECISION_FP64, compute_energy: bool 
     p.integrator = getattr(scene, "integrator", FEM_INTEGRATOR_QIE_V)
     p.nr_max_iter = getattr(scene, "nr_max_iter", 3)
     p.nr_abs_epsilon = getattr(scene, "nr_abs_eps", 1e-6)
+    p.ls_solver = getattr(scene, "ls_solver", FEM_LS_CG)
     p.rotation = getattr(scene, "rotation", FEM_ROTATION_MSVD)
     if p.rotation == FEM_ROTATION_DAPD:
         p.dapd_threshold_det_F = scene.dapd_threshold

@@ -500,6 +500,8 @@ int fem_batch_add_mesh(fem_batch b, const double* rest, uint32_t N, const uint32
                           p->integrator);
     if (p->rotation != FEM_ROTATION_MSVD)
         return batch_fail(FEM_E_ARG, "rotation %u: batches use MSVD; DAPD runs on fem_solid", p->rotation);
+    if (p->ls_solver != FEM_LS_CG)
+        return batch_fail(FEM_E_ARG, "ls_solver %u: batches use CG; MINRES runs on fem_solid", p->ls_solver);
     for (size_t i = 0; i < 4 * (size_t)T; i++)
         if (tets[i] >= N) return batch_fail(FEM_E_INDEX, "tet %zu names node %u >= N=%u", i / 4, tets[i], N);
     HostMesh m;

@@ -22,6 +22,15 @@
 
 namespace femgb {
 
+// MINRES recurrence scalars (ILSS_MINRES::Solve, ILSS_MINRES.h:51-168).
+struct MinresScalars {
+    double norm_r_sq, norm_b_sq;     // |r|^2 carried by the Givens sines; |b|^2
+    double beta, beta_new, beta_one;  // Lanczos norms (beta_one: of the initial residual)
+    double alpha;
+    double c, c_old, s, s_old, eta;   // Givens rotation state
+    double inv_beta, neg_r2, neg_r3, inv_r1, x_coef;  // this iteration's update coefficients
+};
+
 // Device-resident CG and step scalars of one solid.
 struct StepScalars {
     double delta_new, delta_old, delta_0, delta_target, abs_eps_sq;
@@ -38,8 +47,10 @@ struct StepScalars {
     uint32_t confirm;       // mixed: this iteration only measures the FP64 residual (exit test)
     float alpha_f;          // mixed: this iteration's alpha in FP32 (0 on a confirm iteration)
     uint32_t brk;           // mixed: this iteration breaks down (|d.q| < abs^2) and leaves the loop
+    uint32_t done_prev;     // MINRES: `done` as it was at the top of the current iteration
     unsigned long long total_iters;
     double host_sum;        // FIE: the last FIN_SUM total (|b_k|^2 or |y_k|^2), read by the host
+    MinresScalars mr;       // MINRES solver state (FP64 solid)
 };
 
 template <typename S>
@@ -100,6 +111,21 @@ void launch_knc_fie_fp64(uint32_t count, const uint32_t* nodes, const double* ta
 void launch_sq_norm_fp64(uint32_t n, const double* v, double* partials, cudaStream_t s);
 void launch_fie_update_fp64(uint32_t N, double inv_dt, double* x, double* v, const double* xn, const double* y,
                             double* partials, cudaStream_t s);
+// MINRES (FP64 solid). v1 = S (b - A y) and partial |v1|^2 from a fresh eout of y.
+void launch_mr_init_fp64(const MeshView<double>& m, const StepConsts& c, const double* b, const double* y,
+                         double* v1, double* partials, cudaStream_t s);
+// v1 *= 1/beta_new ; v = p = p0 = 0
+void launch_mr_start_fp64(uint32_t N, double* v1, double* v, double* p, double* p0, const StepScalars* st,
+                          cudaStream_t s);
+// v1 = S A w - beta v0 (w = v, eout of v) ; partial v1.v
+void launch_mr_q_fp64(const MeshView<double>& m, const StepConsts& c, const double* v, const double* v0,
+                      double* v1, double* partials, const StepScalars* st, cudaStream_t s);
+// v1 -= alpha v ; partial |v1|^2
+void launch_mr_v1_fp64(uint32_t N, double* v1, const double* v, double* partials, const StepScalars* st,
+                       cudaStream_t s);
+// v1 /= beta_new ; p0 <- (w - r2 p - r3 p0) / r1 (the new p, in p0's buffer) ; y += coef p_new
+void launch_mr_update_fp64(uint32_t N, double* v1, const double* v, const double* p, double* p0, double* y,
+                           const StepScalars* st, cudaStream_t s);
 void launch_potential_fp64(const MeshView<double>& m, const StepConsts& c, const double* x, double* partials,
                            cudaStream_t s);
 void launch_apply_A_fp64(const MeshView<double>& m, double factor_M, double factor_K, double mass,
@@ -109,7 +135,9 @@ void launch_gather_sum_fp64(const MeshView<double>& m, double sign, double* f, c
 // finalizers: one block, fixed-order sums of `count` block partials
 enum FinalizeKind {
     FIN_INIT = 0, FIN_ALPHA = 1, FIN_BETA = 2, FIN_ENERGY_E = 3, FIN_ENERGY_P = 4, FIN_STATS = 5,
-    FIN_SUM = 6  // host_sum = total
+    FIN_SUM = 6,  // host_sum = total
+    // MINRES: init (|r0|^2 = total, |b|^2 from host_sum), alpha, beta + Givens, stats
+    FIN_MR_INIT = 7, FIN_MR_ALPHA = 8, FIN_MR_BETA = 9, FIN_MR_STATS = 10
 };
 void launch_finalize(int kind, const double* partials, uint32_t count, const StepConsts& c, StepScalars* st,
                      cudaStream_t s);

@@ -469,6 +469,103 @@ __global__ void k_fie_update_fp64(uint32_t N, double inv_dt, double* x, double* 
     if (threadIdx.x == 0) partials[blockIdx.x] = s;
 }
 
+// ---- MINRES (ILSS_MINRES::Solve, ILSS_MINRES.h:51-168), no preconditioner:
+// w == v, w1 == v1. The host rotates the v0/v/v1 and p0/p buffers between
+// iterations; every kernel is a no-op once the loop has ended.
+
+// v1 = S (b - A y) ; partial |v1|^2   (:66-74)
+__global__ void k_mr_init_fp64(MeshView<double> m, StepConsts c, const double* __restrict__ b,
+                               const double* __restrict__ y, double* v1, double* partials)
+{
+    double acc = 0.0;
+    const double mfm = c.mass * c.factor_M;
+    for (uint32_t n = blockIdx.x * blockDim.x + threadIdx.x; n < m.N; n += gridDim.x * blockDim.x) {
+        double f[3] = {0, 0, 0};
+        gather3(m, n, f[0], f[1], f[2]);
+        const size_t i = 3 * (size_t)n;
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+            const double r = m.fixed[n] ? 0.0 : b[i + a] - (c.factor_K * f[a] + mfm * y[i + a]);
+            v1[i + a] = r;
+            acc += r * r;
+        }
+    }
+    double s = block_sum(acc);
+    if (threadIdx.x == 0) partials[blockIdx.x] = s;
+}
+
+// v1 *= 1/beta_new ; v = p = p0 = 0   (:82-95)
+__global__ void k_mr_start_fp64(uint32_t N, double* v1, double* v, double* p, double* p0, const StepScalars* st)
+{
+    const double inv = 1.0 / st->mr.beta_new;
+    const uint32_t n3 = 3 * N;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n3; i += gridDim.x * blockDim.x) {
+        v1[i] *= inv;
+        v[i] = 0.0;
+        p[i] = 0.0;
+        p0[i] = 0.0;
+    }
+}
+
+// v1 = S A v - beta v0 ; partial v1.v   (:117-123)
+__global__ void k_mr_q_fp64(MeshView<double> m, StepConsts c, const double* __restrict__ v,
+                            const double* __restrict__ v0, double* v1, double* partials, const StepScalars* st)
+{
+    if (st->done) return;
+    const double mfm = c.mass * c.factor_M;
+    const double nb = -st->mr.beta_new;
+    double acc = 0.0;
+    for (uint32_t n = blockIdx.x * blockDim.x + threadIdx.x; n < m.N; n += gridDim.x * blockDim.x) {
+        double f[3] = {0, 0, 0};
+        gather3(m, n, f[0], f[1], f[2]);
+        const size_t i = 3 * (size_t)n;
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+            const double q = m.fixed[n] ? 0.0 : c.factor_K * f[a] + mfm * v[i + a];
+            const double w1 = q + nb * v0[i + a];
+            v1[i + a] = w1;
+            acc += w1 * v[i + a];
+        }
+    }
+    double s = block_sum(acc);
+    if (threadIdx.x == 0) partials[blockIdx.x] = s;
+}
+
+// v1 -= alpha v ; partial |v1|^2   (:125-129)
+__global__ void k_mr_v1_fp64(uint32_t N, double* v1, const double* __restrict__ v, double* partials,
+                             const StepScalars* st)
+{
+    if (st->done) return;
+    const double na = -st->mr.alpha;
+    double acc = 0.0;
+    const uint32_t n3 = 3 * N;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n3; i += gridDim.x * blockDim.x) {
+        const double r = v1[i] + na * v[i];
+        v1[i] = r;
+        acc += r * r;
+    }
+    double s = block_sum(acc);
+    if (threadIdx.x == 0) partials[blockIdx.x] = s;
+}
+
+// v1 *= 1/beta_new ; p_new = ((-r2) p + w + (-r3) p0) / r1 into p0's buffer ;
+// y += beta_one c eta p_new   (:131-156)
+__global__ void k_mr_update_fp64(uint32_t N, double* v1, const double* __restrict__ v,
+                                 const double* __restrict__ p, double* p0, double* y, const StepScalars* st)
+{
+    if (st->done_prev) return;
+    const MinresScalars mr = st->mr;
+    const uint32_t n3 = 3 * N;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n3; i += gridDim.x * blockDim.x) {
+        v1[i] *= mr.inv_beta;
+        double pn = mr.neg_r2 * p[i] + v[i];
+        pn += mr.neg_r3 * p0[i];
+        pn *= mr.inv_r1;
+        p0[i] = pn;
+        y[i] += mr.x_coef * pn;
+    }
+}
+
 // q = S (factor_M M d + factor_K sum R K R^T d) using a fresh eout
 __global__ void k_apply_A_fp64(MeshView<double> m, double factor_M, double factor_K, double mass,
                                const double* __restrict__ d, double* q)
@@ -554,6 +651,64 @@ __global__ void k_finalize(int kind, const double* __restrict__ partials, uint32
     case FIN_SUM:
         st->host_sum = total;
         break;
+    case FIN_MR_INIT: {
+        // |r0|^2 (sq_norm_2 and dot(v1, w1) are the same sum); |b|^2 from the
+        // FIN_SUM before; beta_one = |r0| (:74-107)
+        MinresScalars& mr = st->mr;
+        mr.norm_r_sq = total;
+        mr.norm_b_sq = st->host_sum;
+        mr.beta_new = ::sqrt(total);
+        mr.beta_one = mr.beta_new;
+        mr.c = 1.0; mr.c_old = 1.0; mr.s = 0.0; mr.s_old = 0.0; mr.eta = 1.0;
+        st->delta_0 = mr.norm_b_sq;
+        st->delta_target = c.rel_eps_sq * mr.norm_b_sq;
+        st->abs_eps_sq = c.abs_eps_sq;
+        st->max_iter = c.max_iter;
+        st->k = 0;
+        st->status = 0;
+        st->done = (mr.norm_r_sq > st->abs_eps_sq && mr.norm_r_sq > st->delta_target && st->k < st->max_iter) ? 0u : 1u;
+        st->done_prev = st->done;
+        if (total != total) st->status = 3;
+        break;
+    }
+    case FIN_MR_ALPHA:
+        st->done_prev = st->done;
+        if (st->done) break;
+        st->mr.beta = st->mr.beta_new;
+        st->mr.alpha = total;
+        break;
+    case FIN_MR_BETA: {
+        if (st->done) break;
+        MinresScalars& mr = st->mr;
+        const double beta_new_sq = total;
+        mr.beta_new = ::sqrt(beta_new_sq);
+        mr.inv_beta = 1.0 / mr.beta_new;
+        // Givens rotation (:135-144)
+        const double r2 = mr.s * mr.alpha + mr.c * mr.c_old * mr.beta;
+        const double r3 = mr.s_old * mr.beta;
+        const double r1_hat = mr.c * mr.alpha - mr.c_old * mr.s * mr.beta;
+        const double r1 = ::sqrt(r1_hat * r1_hat + beta_new_sq);
+        mr.c_old = mr.c;
+        mr.s_old = mr.s;
+        mr.c = r1_hat / r1;
+        mr.s = mr.beta_new / r1;
+        mr.neg_r2 = -r2;
+        mr.neg_r3 = -r3;
+        mr.inv_r1 = 1.0 / r1;
+        mr.x_coef = mr.beta_one * mr.c * mr.eta;
+        mr.norm_r_sq *= mr.s * mr.s;
+        mr.eta = -mr.s * mr.eta;
+        st->delta_new = mr.norm_r_sq;
+        st->k += 1;
+        st->total_iters += 1;
+        st->done = (mr.norm_r_sq > st->abs_eps_sq && mr.norm_r_sq > st->delta_target && st->k < st->max_iter) ? 0u : 1u;
+        if (total != total || mr.norm_r_sq != mr.norm_r_sq) st->status = 3;
+        break;
+    }
+    case FIN_MR_STATS:
+        st->rel_residual = ::sqrt(st->mr.norm_r_sq / st->mr.norm_b_sq);
+        st->abs_residual = ::sqrt(st->mr.norm_r_sq);
+        break;
     case FIN_STATS:
         st->rel_residual = (st->delta_0 > 0) ? ::sqrt(st->delta_new / st->delta_0) : 0.0;
         st->abs_residual = ::sqrt(st->delta_new);
@@ -637,6 +792,31 @@ void launch_fie_update_fp64(uint32_t N, double inv_dt, double* x, double* v, con
                             double* partials, cudaStream_t s)
 {
     FEMGB_LAUNCH(k_fie_update_fp64, grid_for(3 * N), N, inv_dt, x, v, xn, y, partials);
+}
+void launch_mr_init_fp64(const MeshView<double>& m, const StepConsts& c, const double* b, const double* y,
+                         double* v1, double* partials, cudaStream_t s)
+{
+    FEMGB_LAUNCH(k_mr_init_fp64, grid_for(m.N), m, c, b, y, v1, partials);
+}
+void launch_mr_start_fp64(uint32_t N, double* v1, double* v, double* p, double* p0, const StepScalars* st,
+                          cudaStream_t s)
+{
+    FEMGB_LAUNCH(k_mr_start_fp64, grid_for(3 * N), N, v1, v, p, p0, st);
+}
+void launch_mr_q_fp64(const MeshView<double>& m, const StepConsts& c, const double* v, const double* v0,
+                      double* v1, double* partials, const StepScalars* st, cudaStream_t s)
+{
+    FEMGB_LAUNCH(k_mr_q_fp64, grid_for(m.N), m, c, v, v0, v1, partials, st);
+}
+void launch_mr_v1_fp64(uint32_t N, double* v1, const double* v, double* partials, const StepScalars* st,
+                       cudaStream_t s)
+{
+    FEMGB_LAUNCH(k_mr_v1_fp64, grid_for(3 * N), N, v1, v, partials, st);
+}
+void launch_mr_update_fp64(uint32_t N, double* v1, const double* v, const double* p, double* p0, double* y,
+                           const StepScalars* st, cudaStream_t s)
+{
+    FEMGB_LAUNCH(k_mr_update_fp64, grid_for(3 * N), N, v1, v, p, p0, y, st);
 }
 void launch_potential_fp64(const MeshView<double>& m, const StepConsts& c, const double* x, double* partials,
                            cudaStream_t s)

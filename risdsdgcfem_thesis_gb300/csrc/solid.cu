@@ -113,6 +113,8 @@ struct fem_solid_s {
     DevBuf<double> prev_x;
     DevBuf<uchar2> doc;
     DapdParams dapd{};
+    // MINRES: the p and p0 vectors (v, v0, v1 reuse the CG's r, d, q)
+    DevBuf<double> mr_p, mr_p0;
     // FIE statistics of the last step (host side; the Newton loop runs on the host)
     uint32_t nr_iters = 0, fie_cg_iters = 0;
     double nr_rel = 0, nr_abs = 0;
@@ -150,7 +152,7 @@ struct fem_solid_s {
     void release()
     {
         DevBuf<double>* dbl[] = {&Dinv, &mat, &vol, &R, &detF, &eout, &rest, &x, &v, &y, &b, &r, &d, &q, &tmp,
-                                 &xn, &vn, &prev_x, &knc_targets, &partials, &partials2};
+                                 &xn, &vn, &prev_x, &mr_p, &mr_p0, &knc_targets, &partials, &partials2};
         for (auto* p : dbl) p->release();
         doc.release();
         tets.release();
@@ -229,6 +231,53 @@ int cg_solve(fem_solid s, const StepConsts& c, int chunk)
     return FEM_OK;
 }
 
+// ILSS_MINRES::Solve (ILSS_MINRES.h:51-168) of A y = b from the warm start in
+// y, with the factors of c: Lanczos vectors v0, v, v1 and directions p0, p
+// rotated by pointer between iterations (the kernels of an iteration after the
+// loop has ended are no-ops, so the rotation is harmless there).
+int minres_solve(fem_solid s, const StepConsts& c, int chunk)
+{
+    cudaStream_t st = s->stream;
+    MeshView<double> m = s->view();
+    const uint32_t gN = grid_for(s->N), gV = grid_for(3 * s->N);
+    double *v = s->r.p, *v0 = s->d.p, *v1 = s->q.p, *p = s->mr_p.p, *p0 = s->mr_p0.p;
+    launch_sq_norm_fp64(3 * s->N, s->b.p, s->partials.p, st);
+    launch_finalize(FIN_SUM, s->partials.p, gV, c, s->st.p, st);  // |b|^2
+    launch_elem_spmv_fp64(m, s->y.p, s->st.p, 0, st);
+    launch_mr_init_fp64(m, c, s->b.p, s->y.p, v1, s->partials.p, st);
+    launch_finalize(FIN_MR_INIT, s->partials.p, gN, c, s->st.p, st);
+    launch_mr_start_fp64(s->N, v1, v, p, p0, s->st.p, st);
+    for (;;) {
+        for (int i = 0; i < chunk; i++) {
+            double* t = v0;  // v0 <- v, v <- v1, v1 <- the old v0 buffer
+            v0 = v;
+            v = v1;
+            v1 = t;
+            launch_elem_spmv_fp64(m, v, s->st.p, 1, st);
+            launch_mr_q_fp64(m, c, v, v0, v1, s->partials.p, s->st.p, st);
+            launch_finalize(FIN_MR_ALPHA, s->partials.p, gN, c, s->st.p, st);
+            launch_mr_v1_fp64(s->N, v1, v, s->partials.p, s->st.p, st);
+            launch_finalize(FIN_MR_BETA, s->partials.p, gV, c, s->st.p, st);
+            launch_mr_update_fp64(s->N, v1, v, p, p0, s->y.p, s->st.p, st);
+            t = p;  // the new p was written into p0's buffer
+            p = p0;
+            p0 = t;
+        }
+        CK(cudaMemcpyAsync(s->st_host, s->st.p, sizeof(StepScalars), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        if (s->st_host->done) break;
+    }
+    launch_finalize(FIN_MR_STATS, s->partials.p, 0, c, s->st.p, st);
+    CK(cudaGetLastError());
+    return FEM_OK;
+}
+
+// LS_Solve's solver choice (LeafDSH_Solid3D_FEM.cpp:1136-1154)
+int ls_solve(fem_solid s, const StepConsts& c, int chunk)
+{
+    return s->params.ls_solver == FEM_LS_MINRES ? minres_solve(s, c, chunk) : cg_solve(s, c, chunk);
+}
+
 // Sum of `count` block partials into StepScalars::host_sum, read on the host.
 int host_sum(fem_solid s, uint32_t count, double* out)
 {
@@ -290,7 +339,7 @@ int step_fie(fem_solid s, int chunk)
         if (delta_new != delta_new) return fail(FEM_E_NAN, "NaN in the Newton right-hand side");
         converged = delta_new < s->params.nr_abs_epsilon;
         if (!converged) {
-            if (int e = cg_solve(s, c, chunk)) return e;
+            if (int e = ls_solve(s, c, chunk)) return e;
             cg_iters += s->st_host->k;
             solved = true;
             launch_fie_update_fp64(s->N, c.inv_dt, s->x.p, s->v.p, s->xn.p, s->y.p, s->partials.p, st);
@@ -324,7 +373,7 @@ int step_once(fem_solid s, int chunk)
     launch_elem_force_fp64(m, s->x.p, 1, nullptr, st);
     launch_node_b_fp64(m, c, s->v.p, s->b.p, s->y.p, st);
     launch_knc_fp64(s->knc_count, s->knc_nodes.p, s->knc_targets.p, s->x.p, c, s->b.p, s->y.p, st);
-    if (int e = cg_solve(s, c, chunk)) return e;
+    if (int e = ls_solve(s, c, chunk)) return e;
     launch_integrate_fp64(s->N, c.dt, s->x.p, s->v.p, s->y.p, st);
     if (s->params.compute_energy) energy(s);
     CK(cudaGetLastError());
@@ -400,6 +449,7 @@ int fem_params_default(fem_params* p)
     p->nr_max_iter = 3;
     p->nr_abs_epsilon = 1e-6;
     // ms::fem::Params (Params.h:85-95)
+    p->ls_solver = FEM_LS_CG;  // LeafDSH_Solid3D_FEM::Params m_SolverLS_Type
     p->rotation = FEM_ROTATION_MSVD;
     p->dapd_threshold_det_F = (double)0.1f;
     p->dapd_l_factor = 1.0;
@@ -424,6 +474,8 @@ int fem_solid_create(const double* rest_xyz, uint32_t N, const uint32_t* tets, u
         return fail(FEM_E_ARG, "integrator %u is not an enum fem_integrator value", params->integrator);
     if (params->integrator != FEM_INTEGRATOR_QIE_V && !(params->nr_abs_epsilon >= 0))
         return fail(FEM_E_ARG, "nr_abs_epsilon must be >= 0");
+    if (params->ls_solver > FEM_LS_MINRES)
+        return fail(FEM_E_ARG, "ls_solver %u is not an enum fem_ls_solver value", params->ls_solver);
     if (params->rotation > FEM_ROTATION_DAPD)
         return fail(FEM_E_ARG, "rotation %u is not an enum fem_rotation value", params->rotation);
     if (params->rotation == FEM_ROTATION_DAPD &&
@@ -541,6 +593,10 @@ int fem_solid_create(const double* rest_xyz, uint32_t N, const uint32_t* tets, u
     if (params->integrator != FEM_INTEGRATOR_QIE_V) {
         CKC(s->xn.alloc(n3));
         CKC(s->vn.alloc(n3));
+    }
+    if (params->ls_solver == FEM_LS_MINRES) {
+        CKC(s->mr_p.alloc(n3));
+        CKC(s->mr_p0.alloc(n3));
     }
     if (params->rotation == FEM_ROTATION_DAPD) {
         CKC(s->prev_x.alloc(n3));

@@ -77,6 +77,8 @@ class Scene:
     # Rotation method (enum fem_rotation: 0 MSVD, 1 DAPD) and the DAPD
     # degeneration threshold on det F and offset factors (the reference's
     # defaults: 0.1f, 1, 0, 2).
+    # Linear solver of the step (enum fem_ls_solver: 0 CG, 1 MINRES).
+    ls_solver: int = 0
     rotation: int = 0
     dapd_threshold: float = float(np.float32(0.1))
     dapd_L: float = 1.0

@@ -28,8 +28,15 @@ units with Mal's Sqrt/Sin/Cos/ATan2 at double precision, except where noted):
                        directions of collapse are the restatement's, whose x
                        and v equal the reference build's bit for bit.
 
-python tests/golden/make_golden.py fie    writes only the two FIE fixtures;
-python tests/golden/make_golden.py dapd   only the DAPD fixture.
+  minres.npz           the MINRES linear solver (ns::ILSS_MINRES) in place of CG:
+                       the cantilever with QIE (60 steps, prefix qie_) and FIE
+                       (20 steps, fie_), and the moving-constraint block of
+                       fie_block.npz with QIE (12 steps, block_): per-step
+                       statistics, final x and v.
+
+python tests/golden/make_golden.py fie      writes only the two FIE fixtures;
+python tests/golden/make_golden.py dapd     only the DAPD fixture;
+python tests/golden/make_golden.py minres   only the MINRES fixture.
 """
 import dataclasses
 import os
@@ -138,8 +145,31 @@ def dapd_fixture():
     np.savez_compressed(os.path.join(HERE, "dapd_cube.npz"), **out)
 
 
+def minres_cases():
+    cant = scenes.cantilever_160()
+    return (("qie_", dataclasses.replace(cant, ls_solver=1), 60),
+            ("fie_", dataclasses.replace(cant, ls_solver=1, integrator=1), 20),
+            ("block_", dataclasses.replace(fie_block_scene(), ls_solver=1, integrator=0), 12))
+
+
+def minres_fixture():
+    out = {}
+    for prefix, sc, steps in minres_cases():
+        ref = O.Solid(sc, "ref_dbl")
+        stats = [ref.step() for _ in range(steps)]
+        x, v = ref.state()
+        out.update(_stat_arrays(stats, prefix))
+        out[prefix + "x"] = x
+        out[prefix + "v"] = v
+    np.savez_compressed(os.path.join(HERE, "minres.npz"), **out)
+
+
 def main():
     O.build(reference=True)
+    if sys.argv[1:] == ["minres"]:
+        minres_fixture()
+        print("wrote the MINRES fixture to", HERE)
+        return
     if sys.argv[1:] == ["fie"]:
         fie_fixtures()
         print("wrote FIE fixtures to", HERE)
@@ -150,6 +180,7 @@ def main():
         return
     fie_fixtures()
     dapd_fixture()
+    minres_fixture()
     sc = scenes.cantilever_160()
 
     ref = O.Solid(sc, "ref_dbl")

@@ -48,6 +48,7 @@ def test_params_default_matches_reference_defaults(fem_lib):
     # ms::fem::Params: MSVD rotations; DAPD threshold 0.1f, factors 1, 0, 2
     assert p.rotation == fem_lib.FEM_ROTATION_MSVD and p.dapd_threshold_det_F == float(np.float32(0.1))
     assert (p.dapd_l_factor, p.dapd_nl_factor, p.dapd_nl_exponent) == (1.0, 0.0, 2.0)
+    assert p.ls_solver == fem_lib.FEM_LS_CG
 
 
 def test_create_rejects_bad_integrator(fem_lib):
@@ -60,6 +61,10 @@ def test_create_rejects_bad_integrator(fem_lib):
     p.nr_abs_epsilon = -1.0
     code, h, msg = _create(fem_lib, rest, tets, p)
     assert code == fem_lib.FEM_E_ARG and "nr_abs_epsilon" in msg
+    p = fem_lib.default_params()
+    p.ls_solver = 2
+    code, h, msg = _create(fem_lib, rest, tets, p)
+    assert code == fem_lib.FEM_E_ARG and "ls_solver" in msg
     p = fem_lib.default_params()
     p.rotation = 2
     code, h, msg = _create(fem_lib, rest, tets, p)
