@@ -282,11 +282,13 @@ def time_batch(batch, steps, stream_ptr):
     return step_ms, iters
 
 
-def plain_fp64_comparator(steps=3):
-    """The FP64 drop-in path (fem_solid) on the 60^3 block, device time."""
+def plain_fp64_comparator(steps=3, ls_solver=0):
+    """The FP64 drop-in path (fem_solid) on the 60^3 block, device time, with
+    CG (ls_solver 0) or MINRES (1)."""
+    import dataclasses
     import torch
     from risdsdgcfem_thesis_gb300 import capi, scenes
-    sc = scenes.large_block(n=60)
+    sc = dataclasses.replace(scenes.large_block(n=60), ls_solver=ls_solver)
     s = capi.Solid(sc, compute_energy=True)
     s.step(1)
     lib = capi.load()
@@ -305,8 +307,9 @@ def plain_fp64_comparator(steps=3):
     units = float(sc.num_tets) * (st.total_cg_iterations - it0)
     s.close()
     return {"value": units / (ms * 1e-3), "unit": UNIT, "steps": steps,
-            "workload": f"{sc.name} ({sc.num_tets} tets), plain FP64 drop-in path (fem_solid_step)",
-            "ms_per_step": ms / steps}
+            "workload": f"{sc.name} ({sc.num_tets} tets), plain FP64 drop-in path (fem_solid_step), "
+                        f"{'MINRES' if ls_solver else 'CG'}",
+            "ms_per_step": ms / steps, "iterations_per_step": (st.total_cg_iterations - it0) / steps}
 
 
 def fie_leg(n=40, steps=2, cpu_n=16):
@@ -465,6 +468,7 @@ def run_ours(args):
     plain = None
     fie = None
     rotations = None
+    minres = None
     cpu = None
     served = None
     compression = None
@@ -478,6 +482,7 @@ def run_ours(args):
         if not args.no_fie:
             fie = fie_leg()
             rotations = rotation_leg()
+            minres = plain_fp64_comparator(3, ls_solver=1)
         if not args.no_cpu:
             sample = cpu_sample_set(scs, 1_500_000)
             threads = (os.cpu_count() or 1) if len(sample) > 1 else 1
@@ -528,6 +533,7 @@ def run_ours(args):
             "plain_fp64_gpu": plain,
             "fie_fp64_gpu": fie,
             "rotations_fp64_gpu": rotations,
+            "minres_fp64_gpu": minres,
             "cpu_baseline": cpu,
             "served": served,
             "compression": compression,
@@ -681,7 +687,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-fie", action="store_true",
-                    help="skip the fully-implicit Euler and MSVD/DAPD rotation legs")
+                    help="skip the fully-implicit Euler, MSVD/DAPD rotation and MINRES legs")
     ap.add_argument("--no-graph", action="store_true", help="launch kernels one by one (for per-kernel profilers)")
     ap.add_argument("--no-served", action="store_true")
     ap.add_argument("--no-compression", action="store_true")
