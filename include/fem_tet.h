@@ -430,6 +430,25 @@ uint64_t fem_kernel_launches(void);
 int fem_profile_enable(int on);
 int fem_profile_read(const char* kernel, double* total_ms, unsigned long long* launches);
 
+/* --- Mesh ingest: TetGen .node / .ele (examples/tetgen2geo/main.cpp) --- */
+/* Reads a TetGen tetrahedral mesh as the reference's converter does: the
+ * first node id is the base of every id (0 or 1), positions are read as
+ * float, node attributes, boundary markers and tet attributes are skipped,
+ * tets with det(x1-x0, x2-x0, x3-x0) <= 0 (in float) are dropped as
+ * EditableTetSolidShape3::AddTetrahedron drops them
+ * (Geo/shape/TetSolidShape3.cpp:278-307), and natural_scale > 0 applies the
+ * converter's "-nsac" option (center the float AABB of the nodes at the
+ * origin, scale its largest extent to natural_scale). '#' comments are
+ * skipped. Outputs: N*3 positions (float values as double) and T*4 base-0
+ * ids in file order, ready for fem_solid_create. Call with rest and tets
+ * null to get num_nodes / num_tets (after dropping) first; num_dropped may
+ * be null. FEM_E_ARG for unreadable or malformed files, a dimension other
+ * than 3, other than 4 nodes per tet, or short arrays; FEM_E_INDEX for an id
+ * outside the .node file. Host only: needs no device. */
+int fem_tetgen_read(const char* node_path, const char* ele_path, double natural_scale, double* rest,
+                    uint32_t max_nodes, uint32_t* tets, uint32_t max_tets, uint32_t* num_nodes,
+                    uint32_t* num_tets, uint32_t* num_dropped);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,6 +1,7 @@
 """Build of the in-tree CUDA library libfemtet_gb300.so (sm_103a only).
 
-Compiles every translation unit under csrc/ with nvcc in parallel and links
+Compiles every translation unit under csrc/ (.cu, and the host-only .cpp)
+with nvcc in parallel and links
 one shared library next to this file. rotation.cu is compiled without fused
 multiply-adds so the FP64 rotation keeps the reference's rounding sequence.
 """
@@ -29,7 +30,7 @@ def nvcc() -> str:
 
 
 def sources():
-    return sorted(f for f in os.listdir(CSRC) if f.endswith(".cu"))
+    return sorted(f for f in os.listdir(CSRC) if f.endswith((".cu", ".cpp")))
 
 
 def build(verbose: bool = False) -> str:
@@ -42,7 +43,7 @@ def build(verbose: bool = False) -> str:
         return OUT
 
     def compile_one(src):
-        obj = os.path.join(BUILD_DIR, src.replace(".cu", ".o"))
+        obj = os.path.join(BUILD_DIR, os.path.splitext(src)[0] + ".o")
         cmd = [nv, *ARCH, *COMMON, *PER_FILE.get(src, []), "-c", os.path.join(CSRC, src), "-o", obj]
         if verbose:
             print(" ".join(cmd))

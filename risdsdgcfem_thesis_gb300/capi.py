@@ -104,6 +104,8 @@ SIGNATURES = {
     "fem_solid_begin_eval": (C.c_int, [C.c_void_p, _dp]),
     "fem_solid_get_rotations": (C.c_int, [C.c_void_p, _dp, _dp]),
     "fem_solid_get_doc": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint8)]),
+    "fem_tetgen_read": (C.c_int, [C.c_char_p, C.c_char_p, C.c_double, _dp, C.c_uint32, _up, C.c_uint32, _up, _up,
+                                  _up]),
     "fem_solid_force_elastic": (C.c_int, [C.c_void_p, _dp]),
     "fem_solid_df_x": (C.c_int, [C.c_void_p, _dp, _dp]),
     "fem_solid_apply_A": (C.c_int, [C.c_void_p, C.c_double, C.c_double, _dp, _dp]),
@@ -310,6 +312,20 @@ class Solid:
 
 def kernel_launches() -> int:
     return int(load().fem_kernel_launches())
+
+
+def read_tetgen(node_path: str, ele_path: str, natural_scale: float = 0.0):
+    """A TetGen mesh through fem_tetgen_read: (rest (N, 3) float64, tets
+    (T, 4) uint32, number of tets dropped for det <= 0)."""
+    lib = load()
+    n, t, dropped = C.c_uint32(), C.c_uint32(), C.c_uint32()
+    np_, ep = node_path.encode(), ele_path.encode()
+    check(lib.fem_tetgen_read(np_, ep, natural_scale, None, 0, None, 0, C.byref(n), C.byref(t), C.byref(dropped)))
+    rest = np.empty((n.value, 3))
+    tets = np.empty((t.value, 4), np.uint32)
+    check(lib.fem_tetgen_read(np_, ep, natural_scale, _ptr(rest), n.value, _ptr(tets, C.c_uint32), t.value,
+                              C.byref(n), C.byref(t), C.byref(dropped)))
+    return rest, tets, int(dropped.value)
 
 
 def profile_enable(on: bool = True) -> None:

@@ -237,3 +237,36 @@ def served_pool(count: int = 4096, seed: int = 0, lo: float = 200.0, hi: float =
     targets = np.exp(rng.uniform(np.log(lo), np.log(hi), count))
     return [sized_block(rng, float(t), idx=i) for i, t in enumerate(targets)]
 
+
+def write_tetgen(rest: np.ndarray, tets: np.ndarray, base_path: str, base_index: int = 1,
+                 node_attributes: int = 0, boundary_markers: bool = False) -> None:
+    """Write base_path.node / base_path.ele in TetGen's format (ids from
+    base_index; optional zero attributes and markers, which readers skip)."""
+    rest = np.asarray(rest, dtype=np.float64)
+    tets = np.asarray(tets, dtype=np.int64)
+    with open(base_path + ".node", "w") as f:
+        f.write(f"{rest.shape[0]} 3 {node_attributes} {1 if boundary_markers else 0}\n")
+        extra = " 0" * node_attributes + (" 0" if boundary_markers else "")
+        for i, p in enumerate(rest):
+            f.write(f"{i + base_index} {float(p[0])!r} {float(p[1])!r} {float(p[2])!r}{extra}\n")
+        f.write("# written by risdsdgcfem_thesis_gb300.scenes.write_tetgen\n")
+    with open(base_path + ".ele", "w") as f:
+        f.write(f"{tets.shape[0]} 4 0\n")
+        for e, t in enumerate(tets):
+            f.write(f"{e + base_index} {t[0] + base_index} {t[1] + base_index} {t[2] + base_index} "
+                    f"{t[3] + base_index}\n")
+
+
+def from_tetgen(base_path: str, natural_scale: float = 0.0, fixed_below: Optional[float] = None,
+                **scene_kwargs) -> Scene:
+    """A Scene from base_path.node / base_path.ele, read by the library's
+    fem_tetgen_read (the reference converter's semantics: float positions,
+    tets with det <= 0 dropped, optional natural scale and centering).
+    fixed_below: nodes with z <= this become fixed position constraints."""
+    from . import capi
+    rest, tets, _ = capi.read_tetgen(base_path + ".node", base_path + ".ele", natural_scale)
+    knc = np.zeros(0, np.uint32)
+    if fixed_below is not None:
+        knc = np.nonzero(rest[:, 2] <= fixed_below)[0].astype(np.uint32)
+    name = scene_kwargs.pop("name", "tetgen_" + base_path.rsplit("/", 1)[-1])
+    return Scene(name=name, rest=rest, tets=tets, knc_nodes=knc, knc_targets=rest[knc].copy(), **scene_kwargs)
