@@ -77,6 +77,23 @@ enum fem_ls_solver {
     FEM_LS_MINRES = 1
 };
 
+/* Material models of the element set (ms::fem::Params::m_MM, Params.h:48-62;
+ * f_e / df_x / V dispatch, TetrahedronElementSet3.cpp:303-400). */
+enum fem_material {
+    /* C_WRP: warped stiffness f = -R K0 (R^T x - X), df = -R K0 R^T dx. The
+     * default. */
+    FEM_MATERIAL_C_WRP = 0,
+    /* C_LCM: linear corotational in first Piola-Kirchhoff form,
+     * P = R (2 mu (S - I) + lambda tr(S - I) I) with S = R^T F, its
+     * differential without the dR term (truncated) and energy
+     * V (mu |S - I|^2 + lambda/2 tr(S - I)^2) (TetrahedronElementSet3.cpp:
+     * 1154-1178, 1838-1873, 1489-1507). mu and lambda come from the scalar
+     * young_modulus and poisson_ratio, as the reference's element set takes
+     * them from its Params even where per-element E, nu re-bake K0. FP64
+     * solid only. */
+    FEM_MATERIAL_C_LCM = 1
+};
+
 /* Rotation methods of the element set (ms::fem::Params::ERotationMethod,
  * Params.h:63-67; ComputeRotations_*, TetrahedronElementSet3.cpp:267-278). */
 enum fem_rotation {
@@ -139,6 +156,8 @@ typedef struct fem_params {
     double dapd_l_factor;     /* DAPD: offset factors and exponent (m_DAPD_L_Factor 1, */
     double dapd_nl_factor;    /*   m_DAPD_NL_Factor 0, m_DAPD_NL_Exponent 2); float32 in the */
     double dapd_nl_exponent;  /*   reference, so they are rounded to float */
+    uint32_t material;        /* enum fem_material; the batch and server paths take C_WRP only */
+    uint32_t pad;
 } fem_params;
 
 /* Per-step statistics (the Leaf's per-step LS stats, LeafDSH_Solid3D_FEM.h:597-622). */
@@ -167,7 +186,7 @@ typedef struct fem_solid_s* fem_solid;
  * CG rel 1e-3, abs 1e-6, 20 iterations, FP64, threshold 1e-3, refresh 50,
  * energy on, rotation check 1e-3, refresh every 50 iterations (no drop rule),
  * QIE_V integrator, 3 Newton iterations with abs epsilon 1e-6, CG, MSVD
- * rotations (DAPD threshold 0.1f, factors 1, 0, 2). */
+ * rotations (DAPD threshold 0.1f, factors 1, 0, 2), C_WRP material. */
 int fem_params_default(fem_params* p);
 
 /* Replaces: EditableTetrahedronElementSet3::BeginEdition/AddElement/EndEdition

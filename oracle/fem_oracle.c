@@ -655,6 +655,12 @@ struct orc_solid {
      * MINRES work vectors v, v0, v1, w, w1, p, p0, p0_tmp (3N each) */
     uint32_t ls_solver;
     double* mr;
+    /* material model (ms::fem::Params::m_MM): C_WRP or C_LCM; the set's Lame
+     * parameters from the scalar E, nu (EndEdition, TetrahedronElementSet3.cpp:
+     * 2116-2117) and each element's F of the last evaluation (ec.m_F) */
+    uint32_t material;
+    double lame_mu, lame_lambda;
+    mat3* Fm;
 };
 
 static vec3 load3(const double* p) { return v3(p[0], p[1], p[2]); }
@@ -687,6 +693,11 @@ orc_solid* orc_solid_create(uint32_t N, const double* rest, uint32_t T, const ui
     s->vk = (vec3*)calloc(N, sizeof(vec3));
     s->doc = (doc_t*)malloc(sizeof(doc_t) * T);
     for (uint32_t e = 0; e < T; e++) s->doc[e] = kDocInvalid;
+    s->Fm = (mat3*)calloc(T, sizeof(mat3));
+    s->material = FEM_ORC_MAT_C_WRP;
+    /* LameParameters_From_YoungAndPoisson (TetrahedronElementSet3.cpp:181-186) */
+    s->lame_mu = 0.5 * E / (1 + nu);
+    s->lame_lambda = E * nu / ((1.0 + nu) * (1.0 - 2.0 * nu));
     s->rotation = FEM_ORC_ROT_MSVD;
     s->dapd_thr = (double)0.1f;
     s->dapd_L = 1;
@@ -750,7 +761,7 @@ void orc_solid_destroy(orc_solid* s)
     if (!s) return;
     free(s->ref_pos); free(s->tets); free(s->volume); free(s->inv_Dm); free(s->K); free(s->R);
     free(s->detF); free(s->x); free(s->prev_x); free(s->v); free(s->b); free(s->y);
-    free(s->r); free(s->d); free(s->q); free(s->xk); free(s->vk); free(s->doc); free(s->mr);
+    free(s->r); free(s->d); free(s->q); free(s->xk); free(s->vk); free(s->doc); free(s->mr); free(s->Fm);
     free(s->knc_nid); free(s->knc_pos); free(s->knc_vel);
     free(s);
 }
@@ -817,6 +828,7 @@ static void begin_evaluation_at(orc_solid* s, const vec3* xprev, const vec3* x)
         mat3 F = m_mul(&Ds, &s->inv_Dm[e]);
         double detF = m_det(&F);
         s->detF[e] = detF;
+        s->Fm[e] = F;
         if (s->rotation == FEM_ORC_ROT_MSVD) {
             s->R[e] = rotation_msvd(&F);
             continue;
@@ -847,9 +859,109 @@ static void begin_evaluation_at(orc_solid* s, const vec3* xprev, const vec3* x)
  * collapse detection only. */
 static void begin_evaluation(orc_solid* s) { begin_evaluation_at(s, s->prev_x, s->x); }
 
+/* ---- C_LCM material (linear corotational, first Piola-Kirchhoff form) ---- */
+
+static double m_trace(const mat3* a)
+{
+    double t = 0;
+    for (int i = 0; i < 3; i++) t += a->m[i][i];
+    return t;
+}
+static mat3 m_scale(double k, const mat3* a)
+{
+    mat3 r;
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) r.m[i][j] = k * a->m[i][j];
+    return r;
+}
+static mat3 m_add(const mat3* a, const mat3* b)
+{
+    mat3 r;
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) r.m[i][j] = a->m[i][j] + b->m[i][j];
+    return r;
+}
+
+/* -V P Dm^-T scattered as h0 = -h1-h2-h3, h1..h3 = columns (the force
+ * accumulation of C_LCM_f_e / C_LCM_df_x) */
+static void pk_scatter(const orc_solid* s, uint32_t e, const mat3* P, vec3* f)
+{
+    const uint32_t* t = s->tets + 4 * (size_t)e;
+    mat3 mVP = m_scale(-s->volume[e], P);
+    mat3 DmT = m_transposed(&s->inv_Dm[e]);
+    mat3 H = m_mul(&mVP, &DmT);
+    vec3 c0 = m_col(&H, 0), c1 = m_col(&H, 1), c2 = m_col(&H, 2);
+    f[t[0]] = v_add(f[t[0]], v_sub(v_sub(v_neg(c0), c1), c2));
+    f[t[1]] = v_add(f[t[1]], c0);
+    f[t[2]] = v_add(f[t[2]], c1);
+    f[t[3]] = v_add(f[t[3]], c2);
+}
+
+/* C_LCM_f_e (TetrahedronElementSet3.cpp:1154-1178):
+ * P = R (2 mu (S - I) + lambda tr(S - I) I), S = R^T F */
+static void lcm_f_e_acc(const orc_solid* s, vec3* f)
+{
+    const mat3 I = m_identity();
+    for (uint32_t e = 0; e < s->T; e++) {
+        mat3 Rt = m_transposed(&s->R[e]);
+        mat3 S = m_mul(&Rt, &s->Fm[e]);
+        mat3 SmI;
+        for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++) SmI.m[i][j] = S.m[i][j] - I.m[i][j];
+        mat3 A = m_scale(2 * s->lame_mu, &SmI);
+        mat3 B = m_scale(s->lame_lambda * m_trace(&SmI), &I);
+        mat3 AB = m_add(&A, &B);
+        mat3 P = m_mul(&s->R[e], &AB);
+        pk_scatter(s, e, &P, f);
+    }
+}
+
+/* C_LCM_df_x with truncated differentials (TetrahedronElementSet3.cpp:
+ * 1838-1873; Compute_dR_From_RM gives no dR term under eDM_Truncated):
+ * dP = 2 mu dF + lambda tr(R^T dF) R, dF = dDs Dm^-1 */
+static void lcm_df_x_acc(const orc_solid* s, const vec3* dx, vec3* df)
+{
+    for (uint32_t e = 0; e < s->T; e++) {
+        const uint32_t* t = s->tets + 4 * (size_t)e;
+        mat3 Rt = m_transposed(&s->R[e]);
+        mat3 dDs = compute_D(dx[t[0]], dx[t[1]], dx[t[2]], dx[t[3]]);
+        mat3 dF = m_mul(&dDs, &s->inv_Dm[e]);
+        mat3 A = m_scale(2 * s->lame_mu, &dF);
+        mat3 RtdF = m_mul(&Rt, &dF);
+        mat3 B = m_scale(s->lame_lambda * m_trace(&RtdF), &s->R[e]);
+        mat3 dP = m_add(&A, &B);
+        pk_scatter(s, e, &dP, df);
+    }
+}
+
+/* C_LCM_V (TetrahedronElementSet3.cpp:1489-1507) */
+static double lcm_V(const orc_solid* s)
+{
+    const mat3 I = m_identity();
+    double acc_V = 0;
+    for (uint32_t e = 0; e < s->T; e++) {
+        mat3 Rt = m_transposed(&s->R[e]);
+        mat3 S = m_mul(&Rt, &s->Fm[e]);
+        mat3 SmI;
+        double nsq = 0;
+        for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++) {
+                SmI.m[i][j] = S.m[i][j] - I.m[i][j];
+                nsq += SmI.m[i][j] * SmI.m[i][j];
+            }
+        double tr = m_trace(&SmI);
+        acc_V += s->volume[e] * (s->lame_mu * nsq + 0.5 * s->lame_lambda * (tr * tr));
+    }
+    return acc_V;
+}
+
 /* C_f_e (TetrahedronElementSet3.cpp:1053-1096): f_i -= R sum_j K_ij (R^T x_j - r_j) */
 static void f_e_acc(const orc_solid* s, const vec3* x, vec3* f)
 {
+    if (s->material == FEM_ORC_MAT_C_LCM) {
+        lcm_f_e_acc(s, f);
+        return;
+    }
     for (uint32_t e = 0; e < s->T; e++) {
         const uint32_t* t = s->tets + 4 * (size_t)e;
         const mat3* K = &s->K[16 * (size_t)e];
@@ -868,6 +980,10 @@ static void f_e_acc(const orc_solid* s, const vec3* x, vec3* f)
  * df_i -= R sum_j K_ij R^T dx_j */
 static void df_x_acc(const orc_solid* s, const vec3* dx, vec3* df)
 {
+    if (s->material == FEM_ORC_MAT_C_LCM) {
+        lcm_df_x_acc(s, dx, df);
+        return;
+    }
     for (uint32_t e = 0; e < s->T; e++) {
         const uint32_t* t = s->tets + 4 * (size_t)e;
         const mat3* K = &s->K[16 * (size_t)e];
@@ -885,6 +1001,7 @@ static void df_x_acc(const orc_solid* s, const vec3* dx, vec3* df)
 /* C_V (TetrahedronElementSet3.cpp:1456-1488) */
 static double elastic_V(const orc_solid* s)
 {
+    if (s->material == FEM_ORC_MAT_C_LCM) return lcm_V(s);
     double acc_twice_V = 0;
     for (uint32_t e = 0; e < s->T; e++) {
         const uint32_t* t = s->tets + 4 * (size_t)e;
@@ -1207,6 +1324,8 @@ void orc_solid_doc(const orc_solid* s, uint8_t* doc2)
         doc2[2 * (size_t)e + 1] = s->doc[e].vit1;
     }
 }
+
+void orc_solid_set_material(orc_solid* s, uint32_t material) { s->material = material; }
 
 void orc_solid_set_ls_solver(orc_solid* s, uint32_t ls_solver)
 {

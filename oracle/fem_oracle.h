@@ -39,6 +39,8 @@ extern "C" {
 enum { FEM_ORC_MATH_DOUBLE = 0, FEM_ORC_MATH_FLOAT_LITERAL = 1 };
 /* ms::fem::Params::ERotationMethod values this oracle evaluates */
 enum { FEM_ORC_ROT_MSVD = 0, FEM_ORC_ROT_DAPD = 1 };
+/* ms::fem::Params::m_MM values this oracle evaluates */
+enum { FEM_ORC_MAT_C_WRP = 0, FEM_ORC_MAT_C_LCM = 1 };
 /* LeafDSH_Solid3D_FEM::Params::m_SolverLS_Type values this oracle solves with */
 enum { FEM_ORC_LS_CG = 0, FEM_ORC_LS_MINRES = 1 };
 /* LeafDSH_Solid3D_FEM::Params::EIntegratorType values this oracle steps */
@@ -67,6 +69,9 @@ void orc_solid_set_rotation(orc_solid* s, uint32_t method, double thr, double fa
                             double exponent_NL);
 /* Per-element direction of collapse (vit0, vit1), T*2 bytes; (3, 0) = none. */
 void orc_solid_doc(const orc_solid* s, uint8_t* doc2);
+/* Material model (FEM_ORC_MAT_*); C_LCM's Lame parameters come from the
+ * scalar E and nu given at creation, as the reference's element set's do. */
+void orc_solid_set_material(orc_solid* s, uint32_t material);
 /* Linear solver of the step (FEM_ORC_LS_*). */
 void orc_solid_set_ls_solver(orc_solid* s, uint32_t ls_solver);
 /* Integrator (FEM_ORC_*), Newton iteration cap and |b_k| epsilon (FIE only). */

@@ -82,6 +82,7 @@ def _load(path: str, prefix: str):
     fn("solid_set_integrator").argtypes = [C.c_void_p, C.c_uint32, C.c_uint32, C.c_double]
     fn("solid_set_rotation").argtypes = [C.c_void_p, C.c_uint32, C.c_double, C.c_double, C.c_double, C.c_double]
     fn("solid_set_ls_solver").argtypes = [C.c_void_p, C.c_uint32]
+    fn("solid_set_material").argtypes = [C.c_void_p, C.c_uint32]
     fn("solid_last_nr_stats").argtypes = [C.c_void_p, _up, _dp, _dp]
     if P == "orc_":
         lib.orc_solid_begin_eval.argtypes = [C.c_void_p, _dp]
@@ -154,6 +155,8 @@ class Solid:
         if getattr(scene, "rotation", 0):
             getattr(self.lib, self.p + "solid_set_rotation")(self.h, scene.rotation, scene.dapd_threshold,
                                                               scene.dapd_L, scene.dapd_NL, scene.dapd_exponent)
+        if getattr(scene, "material", 0):
+            getattr(self.lib, self.p + "solid_set_material")(self.h, scene.material)
         if getattr(scene, "ls_solver", 0):
             getattr(self.lib, self.p + "solid_set_ls_solver")(self.h, scene.ls_solver)
         if getattr(scene, "integrator", 0):

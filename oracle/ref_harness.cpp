@@ -51,6 +51,8 @@ class PerElementTES : public ms::fem::EditableTetrahedronElementSet3
 public:
     // ms::fem::Params::m_RM and the DAPD parameters (Params.h:27-29,63-67),
     // set in place so that per-element materials stay baked.
+    // ms::fem::Params::m_MM (Params.h:48-62): 0 C_WRP, 1 C_LCM
+    void SetMaterial(unsigned mm) { m_Params.m_MM = mm ? ms::fem::Params::eMM_C_LCM : ms::fem::Params::eMM_C_WRP; }
     void SetRotation(unsigned method, double thr, double factor_L, double factor_NL, double exponent_NL)
     {
         m_Params.m_RM = method ? ms::fem::Params::eRM_DAPD : ms::fem::Params::eRM_MSVD;
@@ -424,6 +426,8 @@ void ref_solid_set_rotation(ref_solid* s, unsigned method, double thr, double fa
 }
 
 void ref_solid_set_ls_solver(ref_solid* s, unsigned ls_solver) { s->ls_solver = ls_solver; }
+
+void ref_solid_set_material(ref_solid* s, unsigned material) { s->t->tes.SetMaterial(material); }
 
 void ref_solid_set_integrator(ref_solid* s, unsigned integrator, unsigned nr_max_iter, double nr_abs_eps)
 {

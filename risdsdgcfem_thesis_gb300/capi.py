@@ -26,6 +26,8 @@ FEM_ROTATION_MSVD = 0
 FEM_ROTATION_DAPD = 1
 FEM_LS_CG = 0
 FEM_LS_MINRES = 1
+FEM_MATERIAL_C_WRP = 0
+FEM_MATERIAL_C_LCM = 1
 
 _dp = C.POINTER(C.c_double)
 _up = C.POINTER(C.c_uint32)
@@ -58,6 +60,8 @@ class FemParams(C.Structure):
         ("dapd_l_factor", C.c_double),
         ("dapd_nl_factor", C.c_double),
         ("dapd_nl_exponent", C.c_double),
+        ("material", C.c_uint32),
+        ("pad", C.c_uint32),
     ]
 
 
@@ -179,6 +183,7 @@ def params_for(scene, precision: int = FEM_PRECISION_FP64, compute_energy: bool 
     p.nr_max_iter = getattr(scene, "nr_max_iter", 3)
     p.nr_abs_epsilon = getattr(scene, "nr_abs_eps", 1e-6)
     p.ls_solver = getattr(scene, "ls_solver", FEM_LS_CG)
+    p.material = getattr(scene, "material", FEM_MATERIAL_C_WRP)
     p.rotation = getattr(scene, "rotation", FEM_ROTATION_MSVD)
     if p.rotation == FEM_ROTATION_DAPD:
         p.dapd_threshold_det_F = scene.dapd_threshold

@@ -502,6 +502,8 @@ int fem_batch_add_mesh(fem_batch b, const double* rest, uint32_t N, const uint32
         return batch_fail(FEM_E_ARG, "rotation %u: batches use MSVD; DAPD runs on fem_solid", p->rotation);
     if (p->ls_solver != FEM_LS_CG)
         return batch_fail(FEM_E_ARG, "ls_solver %u: batches use CG; MINRES runs on fem_solid", p->ls_solver);
+    if (p->material != FEM_MATERIAL_C_WRP)
+        return batch_fail(FEM_E_ARG, "material %u: batches use C_WRP; C_LCM runs on fem_solid", p->material);
     for (size_t i = 0; i < 4 * (size_t)T; i++)
         if (tets[i] >= N) return batch_fail(FEM_E_INDEX, "tet %zu names node %u >= N=%u", i / 4, tets[i], N);
     HostMesh m;

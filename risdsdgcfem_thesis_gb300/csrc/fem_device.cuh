@@ -85,7 +85,7 @@ void launch_begin_eval_fp64(const MeshView<double>& m, const double* x, double* 
                             cudaStream_t s);
 struct DapdParams;
 void launch_begin_eval_dapd_fp64(const MeshView<double>& m, const double* xprev, const double* x, uchar2* doc,
-                                 const DapdParams& p, StepScalars* st, cudaStream_t s);
+                                 const DapdParams& p, double* F_out, StepScalars* st, cudaStream_t s);
 void launch_elem_spmv_fp64(const MeshView<double>& m, const double* d, const StepScalars* st, int check_done,
                            cudaStream_t s);
 void launch_elem_force_fp64(const MeshView<double>& m, const double* x, int write_out, double* energy_partials,
@@ -111,6 +111,12 @@ void launch_knc_fie_fp64(uint32_t count, const uint32_t* nodes, const double* ta
 void launch_sq_norm_fp64(uint32_t n, const double* v, double* partials, cudaStream_t s);
 void launch_fie_update_fp64(uint32_t N, double inv_dt, double* x, double* v, const double* xn, const double* y,
                             double* partials, cudaStream_t s);
+// C_LCM material (FP64 solid): element force and/or energy from the stored F,
+// and the truncated differential of d.
+void launch_elem_lcm_force_fp64(const MeshView<double>& m, const double* F, double mu, double lam, int write_out,
+                                double* energy_partials, cudaStream_t s);
+void launch_elem_lcm_spmv_fp64(const MeshView<double>& m, const double* d, double mu, double lam,
+                               const StepScalars* st, int check_done, cudaStream_t s);
 // MINRES (FP64 solid). v1 = S (b - A y) and partial |v1|^2 from a fresh eout of y.
 void launch_mr_init_fp64(const MeshView<double>& m, const StepConsts& c, const double* b, const double* y,
                          double* v1, double* partials, cudaStream_t s);

@@ -14,6 +14,7 @@
 // the reference's serial scatter adds them). Reductions are deterministic:
 // warp shuffles, a fixed block tree, then one block summing the block
 // partials in index order.
+#include "lcm.cuh"
 #include "fem_device.cuh"
 #include "msvd.cuh"
 #include "elem_math.cuh"
@@ -160,6 +161,68 @@ __device__ __forceinline__ void load_elem(const MeshView<S>& m, uint32_t e, S* R
     k1 = m.mat[e];
     knu = m.mat[T + e];
     k2 = m.mat[2 * T + e];
+}
+
+// ---- C_LCM element kernels (csrc/lcm.cuh): the material's force from the
+// stored F of the last evaluation (T x 9, row-major per element), its
+// truncated differential, its energy. Same eout convention as the C_WRP
+// kernels below. ----
+
+__device__ __forceinline__ void load_R_Dinv(const MeshView<double>& m, uint32_t e, double* R, double* Di)
+{
+    const size_t T = m.T;
+#pragma unroll
+    for (int c = 0; c < 9; c++) {
+        R[c] = m.R[c * T + e];
+        Di[c] = m.Dinv[c * T + e];
+    }
+}
+
+__global__ void k_elem_lcm_force_fp64(MeshView<double> m, const double* __restrict__ F, double mu, double lam,
+                                      int write_out, double* energy_partials)
+{
+    double energy = 0.0;
+    for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < m.T; e += gridDim.x * blockDim.x) {
+        double R[9], Di[9], Fl[9];
+        load_R_Dinv(m, e, R, Di);
+#pragma unroll
+        for (int c = 0; c < 9; c++) Fl[c] = F[9 * (size_t)e + c];
+        if (write_out) {
+            double out[12];
+            lcm_force(R, Fl, Di, m.vol[e], mu, lam, out);
+            double* o = m.eout + 12 * (size_t)e;
+#pragma unroll
+            for (int c = 0; c < 12; c++) o[c] = out[c];
+        }
+        if (energy_partials) energy += lcm_energy(R, Fl, m.vol[e], mu, lam);
+    }
+    if (energy_partials) {
+        double s = block_sum(energy);
+        if (threadIdx.x == 0) energy_partials[blockIdx.x] = s;
+    }
+}
+
+__global__ void k_elem_lcm_spmv_fp64(MeshView<double> m, const double* __restrict__ d, double mu, double lam,
+                                     const StepScalars* st, int check_done)
+{
+    if (check_done && st->done) return;
+    for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < m.T; e += gridDim.x * blockDim.x) {
+        const int4 t = m.tets[e];
+        const int ids[4] = {t.x, t.y, t.z, t.w};
+        double R[9], Di[9], dl[12];
+        load_R_Dinv(m, e, R, Di);
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            dl[3 * i] = d[3 * (size_t)ids[i]];
+            dl[3 * i + 1] = d[3 * (size_t)ids[i] + 1];
+            dl[3 * i + 2] = d[3 * (size_t)ids[i] + 2];
+        }
+        double out[12];
+        lcm_dforce(R, Di, m.vol[e], mu, lam, dl, out);
+        double* o = m.eout + 12 * (size_t)e;
+#pragma unroll
+        for (int c = 0; c < 12; c++) o[c] = out[c];
+    }
 }
 
 // ---- element kernels ----
@@ -817,6 +880,16 @@ void launch_mr_update_fp64(uint32_t N, double* v1, const double* v, const double
                            const StepScalars* st, cudaStream_t s)
 {
     FEMGB_LAUNCH(k_mr_update_fp64, grid_for(3 * N), N, v1, v, p, p0, y, st);
+}
+void launch_elem_lcm_force_fp64(const MeshView<double>& m, const double* F, double mu, double lam, int write_out,
+                                double* energy_partials, cudaStream_t s)
+{
+    FEMGB_LAUNCH(k_elem_lcm_force_fp64, grid_for(m.T), m, F, mu, lam, write_out, energy_partials);
+}
+void launch_elem_lcm_spmv_fp64(const MeshView<double>& m, const double* d, double mu, double lam,
+                               const StepScalars* st, int check_done, cudaStream_t s)
+{
+    FEMGB_LAUNCH(k_elem_lcm_spmv_fp64, grid_for(m.T), m, d, mu, lam, st, check_done);
 }
 void launch_potential_fp64(const MeshView<double>& m, const StepConsts& c, const double* x, double* partials,
                            cudaStream_t s)

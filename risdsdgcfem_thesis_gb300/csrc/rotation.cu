@@ -62,7 +62,8 @@ void launch_begin_eval_fp64(const MeshView<double>& m, const double* x, double* 
 // the Newton polar rotation (a few 3x3 inverses); the collapse analysis runs
 // only on elements at or below it.
 __global__ void k_begin_eval_dapd_fp64(MeshView<double> m, const double* __restrict__ xprev,
-                                       const double* __restrict__ x, uchar2* doc, DapdParams p, StepScalars* st)
+                                       const double* __restrict__ x, uchar2* doc, DapdParams p, double* F_out,
+                                       StepScalars* st)
 {
     unsigned inverted = 0;
     for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < m.T; e += gridDim.x * blockDim.x) {
@@ -87,6 +88,10 @@ __global__ void k_begin_eval_dapd_fp64(MeshView<double> m, const double* __restr
 #pragma unroll
         for (int c = 0; c < 9; c++) m.R[c * (size_t)m.T + e] = R[c];
         m.detF[e] = detF;
+        if (F_out) {
+#pragma unroll
+            for (int c = 0; c < 9; c++) F_out[9 * (size_t)e + c] = F[c];
+        }
         inverted += (detF <= 0.0) ? 1u : 0u;
     }
     unsigned w = inverted;
@@ -96,10 +101,10 @@ __global__ void k_begin_eval_dapd_fp64(MeshView<double> m, const double* __restr
 }
 
 void launch_begin_eval_dapd_fp64(const MeshView<double>& m, const double* xprev, const double* x, uchar2* doc,
-                                 const DapdParams& p, StepScalars* st, cudaStream_t s)
+                                 const DapdParams& p, double* F_out, StepScalars* st, cudaStream_t s)
 {
     prof_begin("begin_eval_dapd_fp64", s);
-    k_begin_eval_dapd_fp64<<<grid_for(m.T), kBlock, 0, s>>>(m, xprev, x, doc, p, st);
+    k_begin_eval_dapd_fp64<<<grid_for(m.T), kBlock, 0, s>>>(m, xprev, x, doc, p, F_out, st);
     prof_end("begin_eval_dapd_fp64", s);
     launch_counter()++;
 }

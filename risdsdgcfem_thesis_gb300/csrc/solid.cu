@@ -115,6 +115,10 @@ struct fem_solid_s {
     DapdParams dapd{};
     // MINRES: the p and p0 vectors (v, v0, v1 reuse the CG's r, d, q)
     DevBuf<double> mr_p, mr_p0;
+    // C_LCM: each element's F of the last evaluation (T x 9) and the set's
+    // Lame parameters (from the scalar E, nu, as the reference's element set)
+    DevBuf<double> Fe;
+    double lame_mu = 0, lame_lambda = 0;
     // FIE statistics of the last step (host side; the Newton loop runs on the host)
     uint32_t nr_iters = 0, fie_cg_iters = 0;
     double nr_rel = 0, nr_abs = 0;
@@ -152,7 +156,7 @@ struct fem_solid_s {
     void release()
     {
         DevBuf<double>* dbl[] = {&Dinv, &mat, &vol, &R, &detF, &eout, &rest, &x, &v, &y, &b, &r, &d, &q, &tmp,
-                                 &xn, &vn, &prev_x, &mr_p, &mr_p0, &knc_targets, &partials, &partials2};
+                                 &xn, &vn, &prev_x, &mr_p, &mr_p0, &Fe, &knc_targets, &partials, &partials2};
         for (auto* p : dbl) p->release();
         doc.release();
         tets.release();
@@ -177,16 +181,37 @@ int check_handle(fem_solid s)
 }
 
 bool uses_dapd(const fem_solid s) { return s->params.rotation == FEM_ROTATION_DAPD; }
+bool uses_lcm(const fem_solid s) { return s->params.material == FEM_MATERIAL_C_LCM; }
 
 // TetrahedronElementSet3::BeginEvaluation(x0 = xprev, x): F, det F and the
-// rotations at x; xprev feeds the DAPD collapse detection only.
+// rotations at x; xprev feeds the DAPD collapse detection only. C_LCM keeps F.
 void begin_eval(fem_solid s, const double* xprev, const double* x)
 {
     MeshView<double> m = s->view();
+    double* F_out = uses_lcm(s) ? s->Fe.p : nullptr;
     if (uses_dapd(s))
-        launch_begin_eval_dapd_fp64(m, xprev, x, s->doc.p, s->dapd, s->st.p, s->stream);
+        launch_begin_eval_dapd_fp64(m, xprev, x, s->doc.p, s->dapd, F_out, s->st.p, s->stream);
     else
-        launch_begin_eval_fp64(m, x, nullptr, s->st.p, s->stream);
+        launch_begin_eval_fp64(m, x, F_out, s->st.p, s->stream);
+}
+
+// The material's element force at x (C_f_e / C_LCM_f_e) into m.eout and/or
+// its energy partials (C_V / C_LCM_V); C_LCM works from the stored F.
+void elem_force(fem_solid s, const MeshView<double>& m, const double* x, int write_out, double* energy_partials)
+{
+    if (uses_lcm(s))
+        launch_elem_lcm_force_fp64(m, s->Fe.p, s->lame_mu, s->lame_lambda, write_out, energy_partials, s->stream);
+    else
+        launch_elem_force_fp64(m, x, write_out, energy_partials, s->stream);
+}
+
+// The material's element differential of d (C_df_x / C_LCM_df_x) into m.eout.
+void elem_spmv(fem_solid s, const MeshView<double>& m, const double* d, int check_done)
+{
+    if (uses_lcm(s))
+        launch_elem_lcm_spmv_fp64(m, d, s->lame_mu, s->lame_lambda, s->st.p, check_done, s->stream);
+    else
+        launch_elem_spmv_fp64(m, d, s->st.p, check_done, s->stream);
 }
 
 // FixedStep's opening: BeginEvaluation(m_vecPos0, x), then m_vecPos0 = x
@@ -210,12 +235,12 @@ int cg_solve(fem_solid s, const StepConsts& c, int chunk)
     cudaStream_t st = s->stream;
     MeshView<double> m = s->view();
     const uint32_t gN = grid_for(s->N), gV = grid_for(3 * s->N);
-    launch_elem_spmv_fp64(m, s->y.p, s->st.p, 0, st);
+    elem_spmv(s, m, s->y.p, 0);
     launch_node_residual_fp64(m, c, s->b.p, s->y.p, s->r.p, s->d.p, s->partials.p, st);
     launch_finalize(FIN_INIT, s->partials.p, gN, c, s->st.p, st);
     for (;;) {
         for (int i = 0; i < chunk; i++) {
-            launch_elem_spmv_fp64(m, s->d.p, s->st.p, 1, st);
+            elem_spmv(s, m, s->d.p, 1);
             launch_node_q_fp64(m, c, s->d.p, s->q.p, s->partials.p, s->st.p, st);
             launch_finalize(FIN_ALPHA, s->partials.p, gN, c, s->st.p, st);
             launch_node_xr_fp64(s->N, s->y.p, s->r.p, s->d.p, s->q.p, s->partials.p, s->st.p, st);
@@ -243,7 +268,7 @@ int minres_solve(fem_solid s, const StepConsts& c, int chunk)
     double *v = s->r.p, *v0 = s->d.p, *v1 = s->q.p, *p = s->mr_p.p, *p0 = s->mr_p0.p;
     launch_sq_norm_fp64(3 * s->N, s->b.p, s->partials.p, st);
     launch_finalize(FIN_SUM, s->partials.p, gV, c, s->st.p, st);  // |b|^2
-    launch_elem_spmv_fp64(m, s->y.p, s->st.p, 0, st);
+    elem_spmv(s, m, s->y.p, 0);
     launch_mr_init_fp64(m, c, s->b.p, s->y.p, v1, s->partials.p, st);
     launch_finalize(FIN_MR_INIT, s->partials.p, gN, c, s->st.p, st);
     launch_mr_start_fp64(s->N, v1, v, p, p0, s->st.p, st);
@@ -253,7 +278,7 @@ int minres_solve(fem_solid s, const StepConsts& c, int chunk)
             v0 = v;
             v = v1;
             v1 = t;
-            launch_elem_spmv_fp64(m, v, s->st.p, 1, st);
+            elem_spmv(s, m, v, 1);
             launch_mr_q_fp64(m, c, v, v0, v1, s->partials.p, s->st.p, st);
             launch_finalize(FIN_MR_ALPHA, s->partials.p, gN, c, s->st.p, st);
             launch_mr_v1_fp64(s->N, v1, v, s->partials.p, s->st.p, st);
@@ -297,7 +322,7 @@ void energy(fem_solid s)
     MeshView<double> m = s->view();
     const StepConsts& c = s->consts;
     const uint32_t gE = grid_for(s->T);
-    launch_elem_force_fp64(m, s->x.p, 0, s->partials2.p, st);
+    elem_force(s, m, s->x.p, 0, s->partials2.p);
     launch_finalize(FIN_ENERGY_E, s->partials2.p, gE, c, s->st.p, st);
     launch_potential_fp64(m, c, s->x.p, s->partials2.p, st);
     launch_finalize(FIN_ENERGY_P, s->partials2.p, gE, c, s->st.p, st);
@@ -329,7 +354,7 @@ int step_fie(fem_solid s, int chunk)
     double delta_new = 0.0, delta_0 = -1.0, sum = 0.0;
     bool converged = false, solved = false;
     do {
-        launch_elem_force_fp64(m, s->x.p, 1, nullptr, st);
+        elem_force(s, m, s->x.p, 1, nullptr);
         launch_node_b_fie_fp64(m, c, s->x.p, s->xn.p, s->vn.p, nr_k == 0 ? 1 : 0, s->b.p, s->y.p, st);
         launch_knc_fie_fp64(s->knc_count, s->knc_nodes.p, s->knc_targets.p, s->x.p, s->b.p, s->y.p, st);
         launch_sq_norm_fp64(3 * s->N, s->b.p, s->partials.p, st);
@@ -370,7 +395,7 @@ int step_once(fem_solid s, int chunk)
     MeshView<double> m = s->view();
     const StepConsts& c = s->consts;
     if (int e = open_step(s)) return e;
-    launch_elem_force_fp64(m, s->x.p, 1, nullptr, st);
+    elem_force(s, m, s->x.p, 1, nullptr);
     launch_node_b_fp64(m, c, s->v.p, s->b.p, s->y.p, st);
     launch_knc_fp64(s->knc_count, s->knc_nodes.p, s->knc_targets.p, s->x.p, c, s->b.p, s->y.p, st);
     if (int e = ls_solve(s, c, chunk)) return e;
@@ -450,6 +475,7 @@ int fem_params_default(fem_params* p)
     p->nr_abs_epsilon = 1e-6;
     // ms::fem::Params (Params.h:85-95)
     p->ls_solver = FEM_LS_CG;  // LeafDSH_Solid3D_FEM::Params m_SolverLS_Type
+    p->material = FEM_MATERIAL_C_WRP;  // ms::fem::Params m_MM
     p->rotation = FEM_ROTATION_MSVD;
     p->dapd_threshold_det_F = (double)0.1f;
     p->dapd_l_factor = 1.0;
@@ -476,6 +502,8 @@ int fem_solid_create(const double* rest_xyz, uint32_t N, const uint32_t* tets, u
         return fail(FEM_E_ARG, "nr_abs_epsilon must be >= 0");
     if (params->ls_solver > FEM_LS_MINRES)
         return fail(FEM_E_ARG, "ls_solver %u is not an enum fem_ls_solver value", params->ls_solver);
+    if (params->material > FEM_MATERIAL_C_LCM)
+        return fail(FEM_E_ARG, "material %u is not an enum fem_material value", params->material);
     if (params->rotation > FEM_ROTATION_DAPD)
         return fail(FEM_E_ARG, "rotation %u is not an enum fem_rotation value", params->rotation);
     if (params->rotation == FEM_ROTATION_DAPD &&
@@ -593,6 +621,15 @@ int fem_solid_create(const double* rest_xyz, uint32_t N, const uint32_t* tets, u
     if (params->integrator != FEM_INTEGRATOR_QIE_V) {
         CKC(s->xn.alloc(n3));
         CKC(s->vn.alloc(n3));
+    }
+    if (params->material == FEM_MATERIAL_C_LCM) {
+        CKC(s->Fe.alloc(9 * (size_t)T));
+        CKC(cudaMemsetAsync(s->Fe.p, 0, sizeof(double) * 9 * (size_t)T, s->stream));
+        // LameParameters_From_YoungAndPoisson on the set's E, nu
+        // (TetrahedronElementSet3.cpp:181-186, 2116-2117)
+        const double E = params->young_modulus, nu = params->poisson_ratio;
+        s->lame_mu = 0.5 * E / (1 + nu);
+        s->lame_lambda = E * nu / ((1.0 + nu) * (1.0 - 2.0 * nu));
     }
     if (params->ls_solver == FEM_LS_MINRES) {
         CKC(s->mr_p.alloc(n3));
@@ -811,7 +848,7 @@ int fem_solid_force_elastic(fem_solid s, double* f)
     const size_t bytes = sizeof(double) * 3 * (size_t)s->N;
     // positions of the last evaluation are in tmp
     CK(cudaMemcpyAsync(s->q.p, f, bytes, cudaMemcpyHostToDevice, s->stream));
-    launch_elem_force_fp64(s->view(), s->tmp.p, 1, nullptr, s->stream);
+    elem_force(s, s->view(), s->tmp.p, 1, nullptr);
     launch_gather_sum_fp64(s->view(), -1.0, s->q.p, s->stream);
     CK(cudaMemcpyAsync(f, s->q.p, bytes, cudaMemcpyDeviceToHost, s->stream));
     CK(cudaStreamSynchronize(s->stream));
@@ -825,7 +862,7 @@ int fem_solid_df_x(fem_solid s, const double* dx, double* df)
     const size_t bytes = sizeof(double) * 3 * (size_t)s->N;
     CK(cudaMemcpyAsync(s->d.p, dx, bytes, cudaMemcpyHostToDevice, s->stream));
     CK(cudaMemcpyAsync(s->q.p, df, bytes, cudaMemcpyHostToDevice, s->stream));
-    launch_elem_spmv_fp64(s->view(), s->d.p, s->st.p, 0, s->stream);
+    elem_spmv(s, s->view(), s->d.p, 0);
     launch_gather_sum_fp64(s->view(), -1.0, s->q.p, s->stream);
     CK(cudaMemcpyAsync(df, s->q.p, bytes, cudaMemcpyDeviceToHost, s->stream));
     CK(cudaStreamSynchronize(s->stream));
@@ -838,7 +875,7 @@ int fem_solid_apply_A(fem_solid s, double factor_M, double factor_K, const doubl
     if (!d || !q) return fail(FEM_E_ARG, "null arrays");
     const size_t bytes = sizeof(double) * 3 * (size_t)s->N;
     CK(cudaMemcpyAsync(s->d.p, d, bytes, cudaMemcpyHostToDevice, s->stream));
-    launch_elem_spmv_fp64(s->view(), s->d.p, s->st.p, 0, s->stream);
+    elem_spmv(s, s->view(), s->d.p, 0);
     launch_apply_A_fp64(s->view(), factor_M, factor_K, s->node_mass, s->d.p, s->q.p, s->stream);
     CK(cudaMemcpyAsync(q, s->q.p, bytes, cudaMemcpyDeviceToHost, s->stream));
     CK(cudaStreamSynchronize(s->stream));
@@ -850,7 +887,7 @@ int fem_solid_energy(fem_solid s, double* V)
     if (int e = check_handle(s)) return e;
     if (!V) return fail(FEM_E_ARG, "null output");
     if (!s->evaluated) return fail(FEM_E_ARG, "fem_solid_begin_eval must come first");
-    launch_elem_force_fp64(s->view(), s->tmp.p, 0, s->partials2.p, s->stream);
+    elem_force(s, s->view(), s->tmp.p, 0, s->partials2.p);
     launch_finalize(FIN_ENERGY_E, s->partials2.p, grid_for(s->T), s->consts, s->st.p, s->stream);
     CK(cudaMemcpyAsync(s->st_host, s->st.p, sizeof(StepScalars), cudaMemcpyDeviceToHost, s->stream));
     CK(cudaStreamSynchronize(s->stream));
@@ -940,7 +977,7 @@ extern "C" int fem_solid_apply_A_noalloc(fem_solid s, double factor_M, double fa
     m.eout = scratch;
     const size_t bytes = sizeof(double) * 3 * (size_t)s->N;
     CK(cudaMemcpyAsync(s->d.p, d, bytes, cudaMemcpyHostToDevice, s->stream));
-    launch_elem_spmv_fp64(m, s->d.p, s->st.p, 0, s->stream);
+    elem_spmv(s, m, s->d.p, 0);
     launch_apply_A_fp64(m, factor_M, factor_K, s->node_mass, s->d.p, s->q.p, s->stream);
     CK(cudaMemcpyAsync(q, s->q.p, bytes, cudaMemcpyDeviceToHost, s->stream));
     CK(cudaStreamSynchronize(s->stream));

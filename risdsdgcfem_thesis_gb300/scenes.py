@@ -79,6 +79,8 @@ class Scene:
     # defaults: 0.1f, 1, 0, 2).
     # Linear solver of the step (enum fem_ls_solver: 0 CG, 1 MINRES).
     ls_solver: int = 0
+    # Material model (enum fem_material: 0 C_WRP, 1 C_LCM).
+    material: int = 0
     rotation: int = 0
     dapd_threshold: float = float(np.float32(0.1))
     dapd_L: float = 1.0

@@ -34,7 +34,13 @@ units with Mal's Sqrt/Sin/Cos/ATan2 at double precision, except where noted):
                        fie_block.npz with QIE (12 steps, block_): per-step
                        statistics, final x and v.
 
+  lcm.npz              the C_LCM material (first Piola-Kirchhoff linear
+                       corotational) in place of C_WRP: the cantilever with
+                       QIE (60 steps, qie_) and FIE (20 steps, fie_), and the
+                       moving-constraint block with QIE (12 steps, block_).
+
 python tests/golden/make_golden.py fie      writes only the two FIE fixtures;
+python tests/golden/make_golden.py lcm      only the C_LCM fixture;
 python tests/golden/make_golden.py dapd     only the DAPD fixture;
 python tests/golden/make_golden.py minres   only the MINRES fixture.
 """
@@ -164,8 +170,31 @@ def minres_fixture():
     np.savez_compressed(os.path.join(HERE, "minres.npz"), **out)
 
 
+def lcm_cases():
+    cant = scenes.cantilever_160()
+    return (("qie_", dataclasses.replace(cant, material=1), 60),
+            ("fie_", dataclasses.replace(cant, material=1, integrator=1), 20),
+            ("block_", dataclasses.replace(fie_block_scene(), material=1, integrator=0), 12))
+
+
+def lcm_fixture():
+    out = {}
+    for prefix, sc, steps in lcm_cases():
+        ref = O.Solid(sc, "ref_dbl")
+        stats = [ref.step() for _ in range(steps)]
+        x, v = ref.state()
+        out.update(_stat_arrays(stats, prefix))
+        out[prefix + "x"] = x
+        out[prefix + "v"] = v
+    np.savez_compressed(os.path.join(HERE, "lcm.npz"), **out)
+
+
 def main():
     O.build(reference=True)
+    if sys.argv[1:] == ["lcm"]:
+        lcm_fixture()
+        print("wrote the C_LCM fixture to", HERE)
+        return
     if sys.argv[1:] == ["minres"]:
         minres_fixture()
         print("wrote the MINRES fixture to", HERE)
@@ -181,6 +210,7 @@ def main():
     fie_fixtures()
     dapd_fixture()
     minres_fixture()
+    lcm_fixture()
     sc = scenes.cantilever_160()
 
     ref = O.Solid(sc, "ref_dbl")
