@@ -282,13 +282,13 @@ def time_batch(batch, steps, stream_ptr):
     return step_ms, iters
 
 
-def plain_fp64_comparator(steps=3, ls_solver=0):
+def plain_fp64_comparator(steps=3, ls_solver=0, material=0):
     """The FP64 drop-in path (fem_solid) on the 60^3 block, device time, with
-    CG (ls_solver 0) or MINRES (1)."""
+    CG (ls_solver 0) or MINRES (1), material C_WRP (0) or C_LCM (1)."""
     import dataclasses
     import torch
     from risdsdgcfem_thesis_gb300 import capi, scenes
-    sc = dataclasses.replace(scenes.large_block(n=60), ls_solver=ls_solver)
+    sc = dataclasses.replace(scenes.large_block(n=60), ls_solver=ls_solver, material=material)
     s = capi.Solid(sc, compute_energy=True)
     s.step(1)
     lib = capi.load()
@@ -308,7 +308,7 @@ def plain_fp64_comparator(steps=3, ls_solver=0):
     s.close()
     return {"value": units / (ms * 1e-3), "unit": UNIT, "steps": steps,
             "workload": f"{sc.name} ({sc.num_tets} tets), plain FP64 drop-in path (fem_solid_step), "
-                        f"{'MINRES' if ls_solver else 'CG'}",
+                        f"{'MINRES' if ls_solver else 'CG'}, {'C_LCM' if material else 'C_WRP'}",
             "ms_per_step": ms / steps, "iterations_per_step": (st.total_cg_iterations - it0) / steps}
 
 
@@ -469,6 +469,7 @@ def run_ours(args):
     fie = None
     rotations = None
     minres = None
+    lcm = None
     cpu = None
     served = None
     compression = None
@@ -483,6 +484,7 @@ def run_ours(args):
             fie = fie_leg()
             rotations = rotation_leg()
             minres = plain_fp64_comparator(3, ls_solver=1)
+            lcm = plain_fp64_comparator(3, material=1)
         if not args.no_cpu:
             sample = cpu_sample_set(scs, 1_500_000)
             threads = (os.cpu_count() or 1) if len(sample) > 1 else 1
@@ -534,6 +536,7 @@ def run_ours(args):
             "fie_fp64_gpu": fie,
             "rotations_fp64_gpu": rotations,
             "minres_fp64_gpu": minres,
+            "lcm_fp64_gpu": lcm,
             "cpu_baseline": cpu,
             "served": served,
             "compression": compression,
@@ -687,7 +690,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-fie", action="store_true",
-                    help="skip the fully-implicit Euler, MSVD/DAPD rotation and MINRES legs")
+                    help="skip the fully-implicit Euler, MSVD/DAPD rotation, MINRES and C_LCM legs")
     ap.add_argument("--no-graph", action="store_true", help="launch kernels one by one (for per-kernel profilers)")
     ap.add_argument("--no-served", action="store_true")
     ap.add_argument("--no-compression", action="store_true")
