@@ -21,11 +21,13 @@
 #include "../../include/fem_tet.h"
 
 #include <cctype>
+#include <algorithm>
 #include <cerrno>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <new>
 #include <string>
 #include <vector>
 
@@ -108,9 +110,30 @@ float det_columns(const float* a, const float* b, const float* c)
 
 }  // namespace
 
+namespace {
+int tetgen_read(const char* node_path, const char* ele_path, double natural_scale, double* rest, uint32_t max_nodes,
+                uint32_t* tets, uint32_t max_tets, uint32_t* num_nodes, uint32_t* num_tets, uint32_t* num_dropped);
+}
+
+// No C++ exception leaves the C ABI: a header whose counts do not fit in host
+// memory answers FEM_E_OOM.
 extern "C" int fem_tetgen_read(const char* node_path, const char* ele_path, double natural_scale, double* rest,
                                uint32_t max_nodes, uint32_t* tets, uint32_t max_tets, uint32_t* num_nodes,
                                uint32_t* num_tets, uint32_t* num_dropped)
+{
+    try {
+        return tetgen_read(node_path, ele_path, natural_scale, rest, max_nodes, tets, max_tets, num_nodes, num_tets,
+                           num_dropped);
+    } catch (const std::bad_alloc&) {
+        return io_fail(FEM_E_OOM, "host allocation failed while reading the mesh");
+    } catch (...) {
+        return io_fail(FEM_E_ARG, "failed to read the mesh");
+    }
+}
+
+namespace {
+int tetgen_read(const char* node_path, const char* ele_path, double natural_scale, double* rest, uint32_t max_nodes,
+                uint32_t* tets, uint32_t max_tets, uint32_t* num_nodes, uint32_t* num_tets, uint32_t* num_dropped)
 {
     if (!node_path || !ele_path || !num_nodes || !num_tets)
         return io_fail(FEM_E_ARG, "null path or count output");
@@ -129,12 +152,15 @@ extern "C" int fem_tetgen_read(const char* node_path, const char* ele_path, doub
         if (dim != 3) return io_fail(FEM_E_ARG, std::string(node_path) + ": dimension is not 3");
         if (n <= 0 || n > (1L << 30) || nattr < 0 || nbnd < 0 || nbnd > 1)
             return io_fail(FEM_E_ARG, std::string(node_path) + ": bad counts in the header");
-        pos.resize(3 * (size_t)n);
+        // grown as nodes are read, so a header that promises more nodes than
+        // the file holds fails on the missing lines, not on the allocation
+        pos.reserve(3 * (size_t)std::min(n, 1L << 20));
         for (long i = 0; i < n; i++) {
             long vid = 0;
-            if (!tk.next_long(vid) || !tk.next_float(pos[3 * i]) || !tk.next_float(pos[3 * i + 1]) ||
-                !tk.next_float(pos[3 * i + 2]))
+            float p[3];
+            if (!tk.next_long(vid) || !tk.next_float(p[0]) || !tk.next_float(p[1]) || !tk.next_float(p[2]))
                 return io_fail(FEM_E_ARG, std::string(node_path) + ": malformed node " + std::to_string(i));
+            pos.insert(pos.end(), p, p + 3);
             if (i == 0) base_vid = vid;
             float dummy;
             for (long a = 0; a < nattr + nbnd; a++)
@@ -156,7 +182,7 @@ extern "C" int fem_tetgen_read(const char* node_path, const char* ele_path, doub
         if (npt != 4) return io_fail(FEM_E_ARG, std::string(ele_path) + ": not 4 nodes per tet (linear tets only)");
         if (t <= 0 || t > (1L << 29) || nattr < 0)
             return io_fail(FEM_E_ARG, std::string(ele_path) + ": bad counts in the header");
-        kept.reserve(4 * (size_t)t);
+        kept.reserve(4 * (size_t)std::min(t, 1L << 20));
         for (long e = 0; e < t; e++) {
             long tid = 0, v[4];
             if (!tk.next_long(tid) || !tk.next_long(v[0]) || !tk.next_long(v[1]) || !tk.next_long(v[2]) ||
@@ -224,3 +250,4 @@ extern "C" int fem_tetgen_read(const char* node_path, const char* ele_path, doub
     }
     return FEM_OK;
 }
+}  // namespace

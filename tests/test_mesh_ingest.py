@@ -161,3 +161,11 @@ def test_missing_file(fem_lib, tmp_path):
     with pytest.raises(fem_lib.FemError) as e:
         fem_lib.read_tetgen(str(tmp_path / "none.node"), str(tmp_path / "none.ele"))
     assert e.value.code == fem_lib.FEM_E_ARG and "cannot open" in str(e.value)
+
+
+def test_header_promising_more_than_the_file_holds(fem_lib, tmp_path):
+    """A .node header claiming a billion nodes fails on the missing lines."""
+    base = _write(tmp_path, "short", "1000000000 3 0 0\n1 0 0 0\n", CUBE_ELE)
+    with pytest.raises(fem_lib.FemError) as e:
+        fem_lib.read_tetgen(base + ".node", base + ".ele")
+    assert e.value.code == fem_lib.FEM_E_ARG and "malformed node 1" in str(e.value)
