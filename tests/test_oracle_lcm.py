@@ -61,3 +61,21 @@ def test_lcm_force_is_zero_at_rest_and_rigid(oracle):
     Q = np.array([[c, -s_, 0], [s_, c, 0], [0, 0, 1.0]])
     a.begin_eval(sc.rest @ Q.T)
     assert np.abs(a.f_e()).max() < 1e-6 * sc.young * sc.h ** 2
+
+
+def test_all_widened_options_together_bitwise(oracle):
+    """C_LCM with the DAPD rotation, the FIE integrator and MINRES on the
+    crushed cube: the restatement equals the reference build bit for bit."""
+    if not os.path.exists(oracle.REF_DBL_SO):
+        pytest.skip("reference sources not present in this container")
+    sc = dataclasses.replace(scenes.compressed_cube(n=5, steps=20, ratio=0.2), material=1, rotation=1,
+                             integrator=1, ls_solver=1)
+    a = oracle.Solid(sc, "port")
+    b = oracle.Solid(sc, "ref_dbl")
+    for k in range(20):
+        assert a.step() == b.step(), k
+    xa, va = a.state()
+    xb, vb = b.state()
+    assert np.array_equal(xa, xb) and np.array_equal(va, vb)
+    doc = a.doc()
+    assert (doc[:, 0] <= doc[:, 1]).sum() > 0  # the DAPD degenerate branch ran
