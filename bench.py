@@ -466,6 +466,7 @@ def run_ours(args):
     batch.close()
 
     plain = None
+    accuracy = None
     fie = None
     rotations = None
     minres = None
@@ -474,6 +475,13 @@ def run_ours(args):
     served = None
     compression = None
     if rank == 0 and ws == 1:
+        if not args.no_accuracy:
+            from risdsdgcfem_thesis_gb300 import scenes as _sc
+            acc_steps = args.accuracy_steps or (args.warmup + args.steps)
+            accuracy = {"C3_batched": accuracy_leg(scs, acc_steps, tile_elems, reorder, chunk_nodes),
+                        "C1_cantilever": single_mesh_error(_sc.cantilever_160(), 120),
+                        "C2_block60": single_mesh_error(_sc.large_block(n=60), 60),
+                        "C5": "see compression (the 40^3 compressed cube, 120 steps)"}
         if not args.no_compression:
             compression = compression_report()
         if not args.no_served:
@@ -532,6 +540,7 @@ def run_ours(args):
                                    "unit": "GB/s", "frac": value * iter_bytes_per_tet_iter / 1e9 / peak,
                                    "note": "whole-job tet.CG-iter/s x algorithmic bytes of one CG "
                                            "iteration (16 + 20 s_e per tet + 33 s_v per node)"},
+            "accuracy": accuracy,
             "plain_fp64_gpu": plain,
             "fie_fp64_gpu": fie,
             "rotations_fp64_gpu": rotations,
@@ -548,6 +557,103 @@ def run_ours(args):
         torch.distributed.barrier()
         torch.distributed.destroy_process_group()
     return 0
+
+
+# ---------------------------------------------------------------- accuracy
+def _vstats(a):
+    a = np.asarray(a, dtype=np.float64)
+    if a.size == 0:
+        return None
+    return {"max": float(a.max()), "p99": float(np.percentile(a, 99)), "mean": float(a.mean())}
+
+
+def accuracy_leg(scs, steps, tile_elems, reorder, chunk_nodes):
+    """Error of the timed workload: the same meshes stepped `steps` times
+    from their initial state by the mixed path (the timed configuration) and
+    by the FP64 batch path (pinned to the FP64 oracle per mesh by the GPU
+    tests). Per mesh: x rel-L2 and ||v - v64|| / max over the run of ||v64||
+    (a body that comes to rest has v ~ 0, where a plain relative norm divides
+    by ~0). Also every step that ended at the CG iteration cap, in either
+    path, with its relative residual."""
+    from risdsdgcfem_thesis_gb300 import capi
+    M = len(scs)
+    t0 = time.perf_counter()
+    mix = capi.Batch(scs, precision=capi.FEM_PRECISION_MIXED, tile_elems=tile_elems, reorder=reorder,
+                     chunk_nodes=chunk_nodes, compute_energy=False)
+    f64 = capi.Batch(scs, precision=capi.FEM_PRECISION_FP64, tile_elems=tile_elems, reorder=reorder,
+                     compute_energy=False)
+    vpeak = np.zeros(M)
+    it_m = np.zeros((steps, M), np.int64)
+    it_f = np.zeros((steps, M), np.int64)
+    res_m = np.zeros((steps, M))
+    res_f = np.zeros((steps, M))
+    for k in range(steps):
+        mix.step(1)
+        f64.step(1)
+        for i in range(M):
+            a, b = mix.stats(i), f64.stats(i)
+            it_m[k, i], res_m[k, i] = a["cg_iterations"], a["rel_residual"]
+            it_f[k, i], res_f[k, i] = b["cg_iterations"], b["rel_residual"]
+            vpeak[i] = max(vpeak[i], float(np.linalg.norm(f64.state(i)[1])))
+    ex, ev = np.zeros(M), np.zeros(M)
+    for i in range(M):
+        xm, vm = mix.state(i)
+        xf, vf = f64.state(i)
+        ex[i] = np.linalg.norm(xm - xf) / np.linalg.norm(xf)
+        ev[i] = np.linalg.norm(vm - vf) / vpeak[i] if vpeak[i] > 0 else 0.0
+    mix.close()
+    f64.close()
+    caps = np.array([sc.max_iter for sc in scs])
+    capped_m = (it_m >= caps[None, :])
+    capped_f = (it_f >= caps[None, :])
+    capped_any = capped_m.any(axis=0) | capped_f.any(axis=0)
+    conv = ~capped_any
+    worst = np.argsort(-np.maximum(ex, ev))[:5]
+    return {
+        "workload": f"the timed workload's {M} meshes, {steps} steps from their initial state, mixed path against "
+                    "the FP64 batch path",
+        "steps": steps, "tolerance": 1e-5,
+        "x_rel_err": _vstats(ex), "v_err_peak_normalised": _vstats(ev),
+        "meshes_within_1e-5": int(np.sum((ex <= 1e-5) & (ev <= 1e-5))),
+        "converged_every_step": {"meshes": int(conv.sum()), "x_rel_err": _vstats(ex[conv]),
+                                 "v_err_peak_normalised": _vstats(ev[conv])},
+        "at_cg_cap": {"meshes": int(capped_any.sum()), "x_rel_err": _vstats(ex[capped_any]),
+                      "v_err_peak_normalised": _vstats(ev[capped_any]),
+                      "steps_at_cap_mixed": int(capped_m.sum()), "steps_at_cap_fp64": int(capped_f.sum()),
+                      "rel_residual_at_cap_mixed": _vstats(res_m[capped_m]),
+                      "rel_residual_at_cap_fp64": _vstats(res_f[capped_f])},
+        "cg_iterations_mean": {"mixed": float(it_m.mean()), "fp64": float(it_f.mean())},
+        "worst_meshes": [{"mesh": int(i), "name": scs[i].name, "tets": scs[i].num_tets, "young": scs[i].young,
+                          "x_rel_err": float(ex[i]), "v_err": float(ev[i]),
+                          "steps_at_cap_mixed": int(capped_m[:, i].sum()),
+                          "steps_at_cap_fp64": int(capped_f[:, i].sum())} for i in worst],
+        "wall_s": round(time.perf_counter() - t0, 1),
+    }
+
+
+def single_mesh_error(sc, steps):
+    """One mesh stepped by the mixed batch path and by the plain FP64 drop-in
+    (fem_solid, parity-tested against the FP64 oracle): x rel-L2 and the
+    peak-normalised v error after `steps` steps, CG iterations per step."""
+    from risdsdgcfem_thesis_gb300 import capi
+    mix = capi.Batch([sc], precision=capi.FEM_PRECISION_MIXED, compute_energy=False)
+    f64 = capi.Solid(sc, compute_energy=False)
+    vpeak, it_m, it_f = 0.0, [], []
+    for _ in range(steps):
+        mix.step(1)
+        it_f.append(f64.step(1)["cg_iterations"])
+        it_m.append(mix.stats(0)["cg_iterations"])
+        vpeak = max(vpeak, float(np.linalg.norm(f64.state()[1])))
+    xm, vm = mix.state(0)
+    xf, vf = f64.state()
+    mix.close()
+    f64.close()
+    return {"mesh": f"{sc.name} ({sc.num_tets} tets)", "steps": steps,
+            "x_rel_err": float(np.linalg.norm(xm - xf) / np.linalg.norm(xf)),
+            "v_err_peak_normalised": float(np.linalg.norm(vm - vf) / vpeak) if vpeak > 0 else 0.0,
+            "cg_iterations_mean": {"mixed": float(np.mean(it_m)), "fp64": float(np.mean(it_f))},
+            "steps_at_cap": {"mixed": int(sum(i >= sc.max_iter for i in it_m)),
+                             "fp64": int(sum(i >= sc.max_iter for i in it_f))}}
 
 
 # ---------------------------------------------------------------- compression
@@ -694,6 +800,9 @@ def main():
     ap.add_argument("--no-graph", action="store_true", help="launch kernels one by one (for per-kernel profilers)")
     ap.add_argument("--no-served", action="store_true")
     ap.add_argument("--no-compression", action="store_true")
+    ap.add_argument("--no-accuracy", action="store_true",
+                    help="skip the error of the timed workload (mixed against the FP64 path) and per config")
+    ap.add_argument("--accuracy-steps", type=int, default=0, help="steps of the accuracy leg (0: warmup + steps)")
     ap.add_argument("--no-tune", action="store_true", help="default tiles (256 tets, Morton order)")
     ap.add_argument("--served-rate", type=float, default=20000.0, help="offered step requests per second")
     ap.add_argument("--served-seconds", type=float, default=3.0)

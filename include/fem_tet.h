@@ -254,9 +254,13 @@ int fem_solid_mass_info(fem_solid s, double* node_mass, double* rayleigh2, doubl
  * fixed-rate control loop that cudaMalloc's implicit synchronisation would
  * stall, a process whose device memory another allocator has reserved). It
  * calls no allocating routine. Larger solids fail with FEM_E_ARG. All calls
- * on a device share the array: calls that overlap on the GPU race, so
- * serialise them. The first call on a device looks up the array's address;
- * make it before any stream capture on that device. */
+ * on a device share the array and it keeps the last call's contents: calls
+ * that overlap on the GPU race, so serialise them. Set-up happens in
+ * fem_solid_create, which looks the array's device address up for every
+ * solid of at most FEM_NOALLOC_MAX_TETS tets (the first lookup on a device
+ * loads the array's module and reserves its 6 MiB there); only if that
+ * lookup failed does the first call on the solid retry it, and that call
+ * should then come before any stream capture. */
 #define FEM_NOALLOC_MAX_TETS 65536u
 int fem_solid_apply_A_noalloc(fem_solid s, double factor_M, double factor_K, const double* d, double* q);
 
@@ -341,6 +345,17 @@ int fem_batch_set_slice(fem_batch b, uint32_t max_iterations);
  * in the last launch; 2 if its loop is still running; 0 otherwise. As of
  * the last synchronize. */
 int fem_batch_finished(fem_batch b, uint8_t* flags);
+/* Poll limit of the device-side waits of the mixed path's tile product for
+ * each tile's copy into shared memory (every wait on the device is bounded;
+ * no counterpart in the reference, which has no device waits). A wait that
+ * gives up sets the batch's error word: the CG loops stop at the end of that
+ * iteration, the blocks drain their copies in flight, and the next
+ * fem_batch_synchronize returns FEM_E_TIMEOUT once (the word is cleared). The
+ * default (FEM_WAIT_LIMIT_DEFAULT) is 2^22 polls, far above any copy's
+ * latency; 0 makes every such wait give up at once, which exercises that
+ * error path. */
+#define FEM_WAIT_LIMIT_DEFAULT 0xffffffffu
+int fem_batch_set_wait_limit(fem_batch b, uint32_t polls);
 int fem_batch_step_async(fem_batch b, uint32_t nsteps);
 int fem_batch_synchronize(fem_batch b);
 int fem_batch_step(fem_batch b, uint32_t nsteps);

@@ -10,6 +10,7 @@
  */
 #include "fem_oracle.h"
 #include <math.h>
+#include <pthread.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -661,6 +662,12 @@ struct orc_solid {
     uint32_t material;
     double lame_mu, lame_lambda;
     mat3* Fm;
+    /* host threads of the element loops (orc_solid_set_threads); with more
+     * than one, element products go to contrib[4e + i] and are applied node
+     * by node in element order through the node -> (4e + i) list */
+    int threads;
+    uint32_t *node_ptr, *node_idx;
+    vec3* contrib;
 };
 
 static vec3 load3(const double* p) { return v3(p[0], p[1], p[2]); }
@@ -763,7 +770,26 @@ void orc_solid_destroy(orc_solid* s)
     free(s->detF); free(s->x); free(s->prev_x); free(s->v); free(s->b); free(s->y);
     free(s->r); free(s->d); free(s->q); free(s->xk); free(s->vk); free(s->doc); free(s->mr); free(s->Fm);
     free(s->knc_nid); free(s->knc_pos); free(s->knc_vel);
+    free(s->node_ptr); free(s->node_idx); free(s->contrib);
     free(s);
+}
+
+void orc_solid_set_threads(orc_solid* s, int threads)
+{
+    s->threads = threads > 1 ? threads : 1;
+    if (s->threads > 1 && !s->contrib) {
+        /* node -> (4e + i) entries in element order (the serial scatter's order) */
+        const size_t n4 = 4 * (size_t)s->T;
+        s->node_ptr = (uint32_t*)calloc((size_t)s->N + 1, sizeof(uint32_t));
+        s->node_idx = (uint32_t*)malloc(sizeof(uint32_t) * n4);
+        s->contrib = (vec3*)malloc(sizeof(vec3) * n4);
+        for (size_t j = 0; j < n4; j++) s->node_ptr[s->tets[j] + 1]++;
+        for (uint32_t n = 0; n < s->N; n++) s->node_ptr[n + 1] += s->node_ptr[n];
+        uint32_t* fill = (uint32_t*)malloc(sizeof(uint32_t) * ((size_t)s->N + 1));
+        memcpy(fill, s->node_ptr, sizeof(uint32_t) * ((size_t)s->N + 1));
+        for (size_t j = 0; j < n4; j++) s->node_idx[fill[s->tets[j]]++] = (uint32_t)j;
+        free(fill);
+    }
 }
 
 double orc_solid_total_volume(const orc_solid* s) { return s->total_volume; }
@@ -820,9 +846,21 @@ void orc_solid_get_state(const orc_solid* s, double* x, double* v)
 /* BeginEvaluation for C_WRP + MSVD (TetrahedronElementSet3.cpp:219-281,777-792):
  * Ds, F = Ds * Dm^-1, det F, R. The degeneration bookkeeping (DoC) does not
  * feed this path and is not formed. */
-static void begin_evaluation_at(orc_solid* s, const vec3* xprev, const vec3* x)
+typedef void (*orc_range_fn)(void* ctx, uint32_t lo, uint32_t hi);
+static void parallel_for(int threads, uint32_t n, orc_range_fn fn, void* ctx);
+
+typedef struct {
+    orc_solid* s;
+    const vec3 *xprev, *x;
+} eval_ctx;
+
+/* BeginEvaluation for elements [lo, hi) (each element's work is its own) */
+static void begin_eval_range(void* p, uint32_t lo, uint32_t hi)
 {
-    for (uint32_t e = 0; e < s->T; e++) {
+    const eval_ctx* c = (const eval_ctx*)p;
+    orc_solid* s = c->s;
+    const vec3 *xprev = c->xprev, *x = c->x;
+    for (uint32_t e = lo; e < hi; e++) {
         const uint32_t* t = s->tets + 4 * (size_t)e;
         mat3 Ds = compute_D(x[t[0]], x[t[1]], x[t[2]], x[t[3]]);
         mat3 F = m_mul(&Ds, &s->inv_Dm[e]);
@@ -853,6 +891,12 @@ static void begin_evaluation_at(orc_solid* s, const vec3* xprev, const vec3* x)
         else
             s->R[e] = m_identity();
     }
+}
+
+static void begin_evaluation_at(orc_solid* s, const vec3* xprev, const vec3* x)
+{
+    eval_ctx c = {s, xprev, x};
+    parallel_for(s->threads, s->T, begin_eval_range, &c);
 }
 
 /* BeginEvaluation(m_vecPos0, x): the previous positions feed the DAPD
@@ -955,11 +999,118 @@ static double lcm_V(const orc_solid* s)
     return acc_V;
 }
 
+/* ---- element loops over host threads ------------------------------------
+ * Test infrastructure speed only: the oracle's serial scatter
+ * f[t[i]] -= c_{e,i} runs element after element. With threads, each
+ * element's four terms c_{e,i} are formed in parallel (they are independent)
+ * and stored, then every node subtracts its terms in element order -- the
+ * same operations in the same order per node, so results are bit-identical
+ * to the serial loop for any thread count. */
+typedef struct {
+    orc_range_fn fn;
+    void* ctx;
+    uint32_t lo, hi;
+    int math;
+} orc_task;
+
+static void* orc_task_run(void* p)
+{
+    orc_task* t = (orc_task*)p;
+    g_math = t->math;
+    t->fn(t->ctx, t->lo, t->hi);
+    return NULL;
+}
+
+static void parallel_for(int threads, uint32_t n, orc_range_fn fn, void* ctx)
+{
+    enum { kMaxThreads = 64 };
+    if (threads > kMaxThreads) threads = kMaxThreads;
+    if (threads <= 1 || n < 1024) {
+        fn(ctx, 0, n);
+        return;
+    }
+    pthread_t th[kMaxThreads];
+    orc_task task[kMaxThreads];
+    int started[kMaxThreads];
+    const uint32_t chunk = (n + (uint32_t)threads - 1) / (uint32_t)threads;
+    for (int k = 0; k < threads; k++) {
+        const uint32_t lo = (uint32_t)k * chunk;
+        const uint32_t hi = lo + chunk < n ? lo + chunk : n;
+        task[k].fn = fn;
+        task[k].ctx = ctx;
+        task[k].lo = lo < n ? lo : n;
+        task[k].hi = hi;
+        task[k].math = g_math;
+        started[k] = 0;
+        if (k > 0 && task[k].lo < task[k].hi)
+            started[k] = pthread_create(&th[k], NULL, orc_task_run, &task[k]) == 0;
+    }
+    fn(ctx, task[0].lo, task[0].hi);
+    for (int k = 1; k < threads; k++) {
+        if (started[k])
+            pthread_join(th[k], NULL);
+        else if (task[k].lo < task[k].hi)
+            fn(ctx, task[k].lo, task[k].hi);
+    }
+}
+
+typedef struct {
+    const orc_solid* s;
+    const vec3* in;   /* x (with ref: f_e) or dx (df_x) */
+    int with_ref;     /* 1: u = R^T x - r (C_f_e); 0: l = R^T dx (C_df_x) */
+    vec3* out;
+} wrp_ctx;
+
+/* c_{e,i} = R sum_j K_ij (R^T in_j [- r_j]) for elements [lo, hi) */
+static void wrp_terms_range(void* p, uint32_t lo, uint32_t hi)
+{
+    const wrp_ctx* c = (const wrp_ctx*)p;
+    const orc_solid* s = c->s;
+    for (uint32_t e = lo; e < hi; e++) {
+        const uint32_t* t = s->tets + 4 * (size_t)e;
+        const mat3* K = &s->K[16 * (size_t)e];
+        mat3 Rt = m_transposed(&s->R[e]);
+        vec3 u[4];
+        for (int i = 0; i < 4; i++) {
+            u[i] = m_mulv(&Rt, c->in[t[i]]);
+            if (c->with_ref) u[i] = v_sub(u[i], s->ref_pos[t[i]]);
+        }
+        for (int i = 0; i < 4; i++) {
+            vec3 acc = v_add(v_add(v_add(m_mulv(&K[4 * i], u[0]), m_mulv(&K[4 * i + 1], u[1])),
+                                   m_mulv(&K[4 * i + 2], u[2])), m_mulv(&K[4 * i + 3], u[3]));
+            s->contrib[4 * (size_t)e + i] = m_mulv(&s->R[e], acc);
+        }
+    }
+}
+
+/* out[n] -= c_{e,i} over n's entries in element order, nodes [lo, hi) */
+static void node_subtract_range(void* p, uint32_t lo, uint32_t hi)
+{
+    const wrp_ctx* c = (const wrp_ctx*)p;
+    const orc_solid* s = c->s;
+    for (uint32_t n = lo; n < hi; n++) {
+        vec3 a = c->out[n];
+        for (uint32_t j = s->node_ptr[n]; j < s->node_ptr[n + 1]; j++) a = v_sub(a, s->contrib[s->node_idx[j]]);
+        c->out[n] = a;
+    }
+}
+
+static void wrp_scatter_threaded(const orc_solid* s, const vec3* in, int with_ref, vec3* out)
+{
+    wrp_ctx c = {s, in, with_ref, out};
+    parallel_for(s->threads, s->T, wrp_terms_range, &c);
+    parallel_for(s->threads, s->N, node_subtract_range, &c);
+}
+
 /* C_f_e (TetrahedronElementSet3.cpp:1053-1096): f_i -= R sum_j K_ij (R^T x_j - r_j) */
 static void f_e_acc(const orc_solid* s, const vec3* x, vec3* f)
 {
     if (s->material == FEM_ORC_MAT_C_LCM) {
         lcm_f_e_acc(s, f);
+        return;
+    }
+    if (s->threads > 1) {
+        wrp_scatter_threaded(s, x, 1, f);
         return;
     }
     for (uint32_t e = 0; e < s->T; e++) {
@@ -982,6 +1133,10 @@ static void df_x_acc(const orc_solid* s, const vec3* dx, vec3* df)
 {
     if (s->material == FEM_ORC_MAT_C_LCM) {
         lcm_df_x_acc(s, dx, df);
+        return;
+    }
+    if (s->threads > 1) {
+        wrp_scatter_threaded(s, dx, 0, df);
         return;
     }
     for (uint32_t e = 0; e < s->T; e++) {

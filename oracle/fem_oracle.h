@@ -63,6 +63,11 @@ void orc_solid_set_knc_targets(orc_solid* s, const double* targets);
 void orc_solid_set_state(orc_solid* s, const double* x, const double* v);
 void orc_solid_get_state(const orc_solid* s, double* x, double* v);
 void orc_solid_fixed_step(orc_solid* s);
+/* Host threads of the element loops (BeginEvaluation and the C_WRP f_e and
+ * df_x scatters); 1 (the default) is the serial restatement. Results are
+ * bit-identical for any count: element terms are formed in parallel and
+ * applied node by node in element order. */
+void orc_solid_set_threads(orc_solid* s, int threads);
 /* Rotation method (FEM_ORC_ROT_*) with the DAPD degeneration threshold on
  * det F and the offset factors; resets every element's direction of collapse. */
 void orc_solid_set_rotation(orc_solid* s, uint32_t method, double thr, double factor_L, double factor_NL,

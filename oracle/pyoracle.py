@@ -26,7 +26,10 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_SO = os.path.join(HERE, "_build", "libfemoracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libfemref.so")
 REF_DBL_SO = os.path.join(HERE, "_ref", "libfemref_dbl.so")
-REFERENCE_SRC = "/root/reference/src"
+# The reference tree (read only to build the checker): REFERENCE_ROOT from
+# the environment, the same variable oracle/Makefile reads.
+REFERENCE_ROOT = os.environ.get("REFERENCE_ROOT", "/root/reference")
+REFERENCE_SRC = os.path.join(REFERENCE_ROOT, "src")
 
 MATH_DOUBLE = 0
 MATH_FLOAT_LITERAL = 1
@@ -40,7 +43,7 @@ def build(reference: bool = False) -> None:
     are present and `reference` is true)."""
     subprocess.check_call(["make", "-s", "-C", HERE, "all"])
     if reference and os.path.isdir(REFERENCE_SRC):
-        subprocess.check_call(["make", "-s", "-C", HERE, "ref"])
+        subprocess.check_call(["make", "-s", "-C", HERE, "ref", f"REF={REFERENCE_ROOT}"])
 
 
 def _ptr(a, ctype=C.c_double):
@@ -97,6 +100,7 @@ def _load(path: str, prefix: str):
         lib.orc_solid_element_K.argtypes = [C.c_void_p, C.c_uint32, _dp]
         lib.orc_solid_set_solver.argtypes = [C.c_void_p, C.c_double, C.c_double, C.c_uint32]
         lib.orc_solid_doc.argtypes = [C.c_void_p, C.POINTER(C.c_uint8)]
+        lib.orc_solid_set_threads.argtypes = [C.c_void_p, C.c_int]
         lib.orc_solid_total_volume.argtypes = [C.c_void_p]
         lib.orc_solid_total_volume.restype = C.c_double
     else:
@@ -214,6 +218,12 @@ class Solid:
         out = np.empty(2)
         getattr(self.lib, self.p + "solid_rayleigh")(self.h, _ptr(out))
         return out
+
+    def set_threads(self, threads: int):
+        """Host threads of the element loops (port only); results are
+        bit-identical for any count."""
+        self.lib.orc_solid_set_threads(self.h, int(threads))
+        return self
 
     def set_solver(self, rel_eps, abs_eps, max_iter):
         self.lib.orc_solid_set_solver(self.h, rel_eps, abs_eps, max_iter)

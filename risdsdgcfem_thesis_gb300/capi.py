@@ -28,6 +28,7 @@ FEM_LS_CG = 0
 FEM_LS_MINRES = 1
 FEM_MATERIAL_C_WRP = 0
 FEM_MATERIAL_C_LCM = 1
+FEM_WAIT_LIMIT_DEFAULT = 0xFFFFFFFF
 
 _dp = C.POINTER(C.c_double)
 _up = C.POINTER(C.c_uint32)
@@ -426,6 +427,7 @@ _BATCH_SIGNATURES = {
     "fem_batch_get_state_all": (C.c_int, [C.c_void_p, _dp, _dp]),
     "fem_batch_step_host": (C.c_int, [C.c_void_p, _dp, _dp, C.c_uint32, _dp, _dp]),
     "fem_batch_set_slice": (C.c_int, [C.c_void_p, C.c_uint32]),
+    "fem_batch_set_wait_limit": (C.c_int, [C.c_void_p, C.c_uint32]),
     "fem_batch_finished": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint8)]),
 }
 
@@ -502,6 +504,11 @@ class Batch:
 
     def set_slice(self, max_iterations):
         check(self.lib.fem_batch_set_slice(self.h, int(max_iterations)))
+
+    def set_wait_limit(self, polls=None):
+        """Poll limit of the tile product's waits for a tile copy (None: the
+        default, 2^22)."""
+        check(self.lib.fem_batch_set_wait_limit(self.h, FEM_WAIT_LIMIT_DEFAULT if polls is None else int(polls)))
 
     def finished(self):
         f = np.zeros(len(self.scenes), np.uint8)

@@ -948,8 +948,12 @@ int fem_batch_finalize(fem_batch b)
     BCKC(b->any_flag.alloc(1));
     BCKC(b->refresh_flag.alloc(1));
     BCKC(b->mcount.alloc(b->M));
-    BCKC(b->err.alloc(1));
-    BCKC(cudaMemsetAsync(b->err.p, 0, sizeof(unsigned), s));
+    BCKC(b->err.alloc(2));  // [0] error word, [1] poll limit of the tile-copy waits
+    {
+        const unsigned e0[2] = {0u, kDefaultWaitPolls};
+        BCKC(cudaMemcpyAsync(b->err.p, e0, sizeof(e0), cudaMemcpyHostToDevice, s));
+        BCKC(cudaStreamSynchronize(s));
+    }
     BCKC(b->blob.alloc(blob_h.size()));
     BCKC(b->blob.upload(blob_h, s));
     BCKC(b->blob_off16.alloc(blob_off16_h.size()));
@@ -1262,6 +1266,15 @@ int fem_batch_set_slice(fem_batch b, uint32_t max_iterations)
     return FEM_OK;
 }
 
+int fem_batch_set_wait_limit(fem_batch b, uint32_t polls)
+{
+    if (int e = check_ready(b)) return e;
+    const unsigned v = polls == FEM_WAIT_LIMIT_DEFAULT ? kDefaultWaitPolls : polls;
+    BCK(cudaMemcpyAsync(b->err.p + 1, &v, sizeof(unsigned), cudaMemcpyHostToDevice, b->stream));
+    BCK(cudaStreamSynchronize(b->stream));
+    return FEM_OK;
+}
+
 int fem_batch_step_async(fem_batch b, uint32_t nsteps)
 {
     if (int e = check_ready(b)) return e;
@@ -1285,7 +1298,12 @@ int fem_batch_synchronize(fem_batch b)
     unsigned err = 0;
     if (b->err.p) BCK(cudaMemcpyAsync(&err, b->err.p, sizeof(unsigned), cudaMemcpyDeviceToHost, b->stream));
     BCK(cudaStreamSynchronize(b->stream));
-    if (err) return batch_fail(FEM_E_TIMEOUT, "a bounded wait for a tile copy gave up (code %u)", err);
+    if (err) {
+        // reported once: the next launches start with a clear word
+        BCK(cudaMemsetAsync(b->err.p, 0, sizeof(unsigned), b->stream));
+        BCK(cudaStreamSynchronize(b->stream));
+        return batch_fail(FEM_E_TIMEOUT, "a bounded wait for a tile copy gave up (code %u)", err);
+    }
     for (uint32_t m = 0; m < b->M; m++)
         if (b->st_host[m].status == FEM_E_NAN) return batch_fail(FEM_E_NAN, "NaN in the CG residual of mesh %u", m);
     return FEM_OK;

@@ -45,6 +45,9 @@ constexpr int kChunkNodes = 1024;  // default node chunk (one work item of a nod
 constexpr int kPipeSmallTile = 128;
 constexpr int kPipeSmallNodes = 120;
 constexpr int kNodeThreads = 256;  // threads per node-kernel block
+// Default poll limit of the tile product's waits for a tile copy (each poll
+// suspends for a hardware time slice: far above any copy's latency).
+constexpr unsigned kDefaultWaitPolls = 1u << 22;
 
 // Layout of a tile's blob (mixed path, see tile_pipe.cu): the element data,
 // 21 FP32 components per element (R 0-8, Dm^-1 9-17, V lambda, V mu, local

@@ -231,6 +231,10 @@ int tetgen_read(const char* node_path, const char* ele_path, double natural_scal
         float ext = 2 * h[0];
         if (2 * h[1] > ext) ext = 2 * h[1];
         if (2 * h[2] > ext) ext = 2 * h[2];
+        // one node, or every node at one point: nothing to scale to the
+        // requested size (the converter would divide by zero)
+        if (!(ext > 0.0f) || !std::isfinite(ext))
+            return io_fail(FEM_E_ARG, "natural_scale: the nodes span no extent (" + std::to_string(ext) + ")");
         const float s = (float)natural_scale / ext;
         for (long i = 0; i < N; i++)
             for (int a = 0; a < 3; a++) {

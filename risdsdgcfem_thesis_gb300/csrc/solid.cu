@@ -21,7 +21,6 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
-#include <mutex>
 #include <new>
 #include <string>
 #include <vector>
@@ -133,6 +132,9 @@ struct fem_solid_s {
     DevBuf<StepScalars> st;
     StepScalars* st_host = nullptr;  // pinned
     bool evaluated = false;
+    // fem_solid_apply_A_noalloc: device address of the static scratch array,
+    // looked up at creation (null for solids above FEM_NOALLOC_MAX_TETS)
+    double* noalloc_scratch = nullptr;
 
     MeshView<double> view()
     {
@@ -484,6 +486,10 @@ int fem_params_default(fem_params* p)
     return FEM_OK;
 }
 
+namespace {
+int apply_scratch(double** out);
+}
+
 int fem_solid_create(const double* rest_xyz, uint32_t N, const uint32_t* tets, uint32_t T, const fem_params* params,
                      const double* young_per_elem, const double* poisson_per_elem, fem_solid* out)
 {
@@ -675,6 +681,14 @@ int fem_solid_create(const double* rest_xyz, uint32_t N, const uint32_t* tets, u
         CKC(cudaStreamSynchronize(st));
     }
 #undef CKC
+    // the static scratch of fem_solid_apply_A_noalloc: its address is looked
+    // up here, where allocating is expected, so that the no-alloc call never
+    // loads its module (a failure is left for that call to report)
+    if (T <= FEM_NOALLOC_MAX_TETS) {
+        const std::string keep = g_err;
+        if (apply_scratch(&s->noalloc_scratch) != FEM_OK) s->noalloc_scratch = nullptr;
+        g_err = keep;
+    }
     *out = s;
     return FEM_OK;
 }
@@ -929,36 +943,30 @@ int fem_solid_mass_info(fem_solid s, double* node_mass, double* rayleigh2, doubl
 //     whose work overlaps on the GPU (several host threads calling at once,
 //     on solids whose streams run concurrently) race on the array: serialise
 //     them;
-//   * the first call on a device (with that device current) looks up the
-//     array's device address once (cudaGetSymbolAddress); make that first
-//     call before any stream capture on that device.
+//   * set-up: host code cannot use the array's name as a device address, so
+//     fem_solid_create looks the address up (cudaGetSymbolAddress, with the
+//     solid's device current) for every solid small enough to use it, and
+//     keeps it in the solid. The array lives in a module without kernels;
+//     under CUDA's lazy module loading that first lookup loads the module,
+//     which reserves its 6 MiB and may synchronise the device -- work done
+//     inside fem_solid_create, which allocates anyway, so that the no-alloc
+//     call itself never does it. Only if that lookup failed does the first
+//     no-alloc call on the solid retry it (and then it should come before
+//     any stream capture).
 namespace {
 
 static __device__ __align__(256) double g_apply_scratch[12ull * FEM_NOALLOC_MAX_TETS];
 
-constexpr int kNoAllocMaxDevices = 64;
-std::mutex g_apply_scratch_mu;
-double* g_apply_scratch_ptr[kNoAllocMaxDevices] = {};
-
-// Device address of the static scratch on the current device (set-up once
-// per device, under a lock).
+// Device address of the static scratch on the current device.
 int apply_scratch(double** out)
 {
-    int dev = 0;
-    CK(cudaGetDevice(&dev));
-    if (dev < 0 || dev >= kNoAllocMaxDevices)
-        return fail(FEM_E_ARG, "device %d is beyond the %d devices of the static scratch table", dev,
-                    kNoAllocMaxDevices);
-    std::lock_guard<std::mutex> lock(g_apply_scratch_mu);
-    if (!g_apply_scratch_ptr[dev]) {
-        void* p = nullptr;
-        const cudaError_t e = cudaGetSymbolAddress(&p, g_apply_scratch);
-        if (e != cudaSuccess)
-            return fail(FEM_E_CUDA, "cudaGetSymbolAddress of the static scratch on device %d: %s", dev,
-                        cudaGetErrorString(e));
-        g_apply_scratch_ptr[dev] = static_cast<double*>(p);
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_apply_scratch);
+    if (e != cudaSuccess) {
+        (void)cudaGetLastError();
+        return fail(FEM_E_CUDA, "cudaGetSymbolAddress of the static scratch: %s", cudaGetErrorString(e));
     }
-    *out = g_apply_scratch_ptr[dev];
+    *out = static_cast<double*>(p);
     return FEM_OK;
 }
 
@@ -971,10 +979,10 @@ extern "C" int fem_solid_apply_A_noalloc(fem_solid s, double factor_M, double fa
     if (s->T > FEM_NOALLOC_MAX_TETS)
         return fail(FEM_E_ARG, "solid has %u tets; fem_solid_apply_A_noalloc takes at most %u (static scratch)",
                     s->T, (unsigned)FEM_NOALLOC_MAX_TETS);
-    double* scratch = nullptr;
-    if (int e = apply_scratch(&scratch)) return e;
+    if (!s->noalloc_scratch)
+        if (int e = apply_scratch(&s->noalloc_scratch)) return e;
     MeshView<double> m = s->view();
-    m.eout = scratch;
+    m.eout = s->noalloc_scratch;
     const size_t bytes = sizeof(double) * 3 * (size_t)s->N;
     CK(cudaMemcpyAsync(s->d.p, d, bytes, cudaMemcpyHostToDevice, s->stream));
     elem_spmv(s, m, s->d.p, 0);

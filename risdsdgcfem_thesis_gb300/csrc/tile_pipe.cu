@@ -51,9 +51,11 @@
 //   of the blob.
 //
 // Every wait on an mbarrier is bounded: a wait that gives up records an error
-// code in the batch's error word; the block then issues no further copies and
-// drains, again bounded, the copies it has in flight. The CG loop stops at
-// the end of an iteration in which the error word is set.
+// code in the batch's error word (err[0] = 1; its poll limit is err[1]); the
+// block then issues no further copies and drains, again bounded (2^22 polls),
+// the copies it has in flight, recording err[0] = 2 if even that drain gives
+// up. The CG loop stops at the end of an iteration in which the error word is
+// set.
 #include "active_list.cuh"
 #include "batch.cuh"
 #include "batch_launch.h"
@@ -106,11 +108,16 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity)
     return ok != 0;
 }
 
-// Bounded wait: ~2^22 polls (each poll itself suspends for a hardware time
-// slice), far above any copy's latency.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity)
+// Bounded wait: at most `polls` polls (each poll itself suspends for a
+// hardware time slice). The drain at the end of the kernel uses the full
+// kDrainPolls; the waits for each tile's copy use the batch's limit
+// (fem_batch_set_wait_limit, default kDrainPolls, far above any copy's
+// latency; 0 makes every such wait give up at once, which exercises the
+// error path without a stuck copy).
+constexpr uint32_t kDrainPolls = 1u << 22;
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, uint32_t polls)
 {
-    for (uint32_t i = 0; i < (1u << 22); i++)
+    for (uint32_t i = 0; i < polls; i++)
         if (mbar_try_wait(bar, parity)) return true;
     return false;
 }
@@ -285,6 +292,7 @@ __global__ void __launch_bounds__(TILE, PipeShape<TILE>::kMinBlocks) k_tile_spmv
     // thread 0 uses it); ~0u: none
     uint32_t& s_prev = *reinterpret_cast<uint32_t*>(wsh + TILE / 32);
     const uint32_t G = gridDim.x, tid = threadIdx.x;
+    const uint32_t wait_polls = *(volatile const unsigned*)(err + 1);
 
     if (set_if && blockIdx.x == 0 && tid == 0) cudaGraphSetConditional(if_refresh, *refresh_flag ? 1u : 0u);
     if (tid == 0) {
@@ -345,7 +353,7 @@ __global__ void __launch_bounds__(TILE, PipeShape<TILE>::kMinBlocks) k_tile_spmv
         // barrier A: every thread polls; the block agrees on the outcome so
         // the barriers below stay uniform
         const bool wait = live && !failed;
-        const bool ok = !wait || mbar_wait_bounded(&bar[s], (phase >> s) & 1u);
+        const bool ok = !wait || mbar_wait_bounded(&bar[s], (phase >> s) & 1u, wait_polls);
         if (__syncthreads_or(!ok)) {
             if (tid == 0) atomicExch(err, 1u);
             failed = true;  // no new copies; the ones in flight are drained at the end
@@ -457,8 +465,12 @@ __global__ void __launch_bounds__(TILE, PipeShape<TILE>::kMinBlocks) k_tile_spmv
         tshare[s_prev] = make_float2(a.hi, a.lo);
     }
     if (failed) {
+        // every thread drains (the copies write this block's shared memory,
+        // so no thread may leave while one is in flight)
+        bool drained = true;
         for (int k = 0; k < 2; k++)
-            if ((pending >> k) & 1u) (void)mbar_wait_bounded(&bar[k], (phase >> k) & 1u);
+            if ((pending >> k) & 1u) drained &= mbar_wait_bounded(&bar[k], (phase >> k) & 1u, kDrainPolls);
+        if (!drained) atomicExch(err, 2u);
     }
 }
 

@@ -25,3 +25,16 @@ def fem_lib():
     build.build()
     capi.load()
     return capi
+
+
+def pytest_terminal_summary(terminalreporter):
+    """The effective bars of the calibrated parity comparisons that ran."""
+    try:
+        from parity_util import BARS
+    except ImportError:
+        return
+    if not BARS:
+        return
+    terminalreporter.write_sep("-", "calibrated parity bars (measured <= max(tol, 10 x oracle floor))")
+    for case, qty, measured, bar, floor in BARS:
+        terminalreporter.write_line(f"{case:<48} {qty:<4} measured {measured:9.3g}  bar {bar:9.3g}  floor {floor:9.3g}")

@@ -4,6 +4,34 @@ import copy
 import numpy as np
 
 
+# Every calibrated comparison of the run: (test case, quantity, measured,
+# bar used, oracle floor). conftest prints them at the end of the session so
+# the effective bars are visible in the test log.
+BARS = []
+
+
+def bar_cap(sc):
+    """Largest bar a calibrated comparison may use for scene `sc`: 100 x its
+    CG relative tolerance, at least 1e-6. CG stops on |r| <= rel |r0|, so when
+    a 1e-15 input change moves the stopping iteration by one the state moves
+    by about the tolerance times the conditioning; the oracle's own floor is
+    then of that order, and a floor far above it means something else moved."""
+    return max(1e-6, 100.0 * float(sc.rel_eps))
+
+
+def check_bar(case, quantity, measured, tol, floor, cap=1e-6, mult=10.0):
+    """Asserts measured <= max(tol, 10 x floor), the bar of the calibrated
+    comparisons, and that this bar stays within `cap` (bar_cap of the scene):
+    an oracle floor that grew (a regression that would otherwise pass inside
+    an inflated bar) fails the test instead of widening it silently. Records
+    the figures."""
+    bar = max(tol, mult * floor)
+    BARS.append((case, quantity, float(measured), float(bar), float(floor)))
+    assert bar <= cap, f"{case} {quantity}: bar {bar:.3g} from the oracle floor {floor:.3g} exceeds the cap {cap:.3g}"
+    assert measured <= bar, f"{case} {quantity}: {measured:.3g} > bar {bar:.3g} (floor {floor:.3g})"
+    return bar
+
+
 def rel(a, b):
     return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
 

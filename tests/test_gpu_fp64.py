@@ -9,6 +9,7 @@ import numpy as np
 import pytest
 
 from risdsdgcfem_thesis_gb300 import scenes
+from parity_util import bar_cap, check_bar
 
 pytestmark = pytest.mark.gpu
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
@@ -58,7 +59,7 @@ def _perturbed(sc, seed, eps=1e-15):
     return p
 
 
-def _compare_with_port(fem_lib, oracle, sc, steps, tol=TOL):
+def _compare_with_port(fem_lib, oracle, sc, steps, tol=TOL, cap=None):
     """GPU vs the oracle restatement over `steps` FixedSteps.
 
     CG stops on a residual threshold, and on stiff scenes the residual sits on
@@ -87,8 +88,9 @@ def _compare_with_port(fem_lib, oracle, sc, steps, tol=TOL):
         noise_x, noise_v = max(noise_x, rel(xc, xb)), max(noise_v, rel(vc, vb))
     spread = max(abs(i - j) for lst in it_noise for i, j in zip(it_orc, lst))
     ex, ev = rel(xa, xb), rel(va, vb)
-    tol_x, tol_v = max(tol, 10 * noise_x), max(tol, 10 * noise_v)
-    assert ex <= tol_x and ev <= tol_v, (ex, ev, noise_x, noise_v)
+    cap = bar_cap(sc) if cap is None else cap
+    check_bar(sc.name, "x", ex, tol, noise_x, cap)
+    check_bar(sc.name, "v", ev, tol, noise_v, cap)
     worst_it = max(abs(i - j) for i, j in zip(it_gpu, it_orc))
     assert worst_it <= max(1, 2 * spread + 1), (worst_it, spread, it_gpu, it_orc)
     return ex, ev
@@ -131,7 +133,12 @@ def test_single_tet(fem_lib, oracle):
     sc = scenes.Scene(name="one", rest=rest, tets=np.array([[0, 1, 2, 3]], np.uint32), gravity=(0, 0, -9.81),
                       knc_nodes=np.array([0], np.uint32), knc_targets=rest[:1].copy(), rel_eps=1e-10,
                       max_iter=100, steps=5)
-    _compare_with_port(fem_lib, oracle, sc, 5)
+    # a lone tet hanging from one node stays close to its rest shape, where
+    # F^T F is nearly isotropic and the MSVD's discrete choices (eigenvalue
+    # order, flip) turn under 1e-15 changes of the input: the oracle itself
+    # moves by ~1e-6 there, so the bar may reach 1e-4 (the GPU matches it to
+    # ~1e-16, its rotations being bit-identical)
+    _compare_with_port(fem_lib, oracle, sc, 5, cap=1e-4)
 
 
 def test_host_roundtrip_matches_device_steps(fem_lib):

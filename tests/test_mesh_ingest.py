@@ -169,3 +169,16 @@ def test_header_promising_more_than_the_file_holds(fem_lib, tmp_path):
     with pytest.raises(fem_lib.FemError) as e:
         fem_lib.read_tetgen(base + ".node", base + ".ele")
     assert e.value.code == fem_lib.FEM_E_ARG and "malformed node 1" in str(e.value)
+
+
+def test_natural_scale_of_coincident_nodes_is_rejected(fem_lib, tmp_path):
+    """-nsac on nodes that span no extent (one point) has nothing to scale
+    to: an error instead of the converter's division by zero."""
+    node = "4 3 0 0\n1 0.5 0.5 0.5\n2 0.5 0.5 0.5\n3 0.5 0.5 0.5\n4 0.5 0.5 0.5\n"
+    base = _write(tmp_path, "point", node, "1 4 0\n1 1 2 3 4\n")
+    with pytest.raises(fem_lib.FemError) as e:
+        fem_lib.read_tetgen(base + ".node", base + ".ele", natural_scale=1.0)
+    assert e.value.code == fem_lib.FEM_E_ARG and "no extent" in str(e.value)
+    # without the option the file reads (its one tet is dropped as flat)
+    rest, tets, dropped = fem_lib.read_tetgen(base + ".node", base + ".ele")
+    assert rest.shape == (4, 3) and tets.shape == (0, 4) and dropped == 1

@@ -189,3 +189,25 @@ def test_cg_solves_spd_system(oracle):
     Af = A[np.ix_(free, free)]
     np.testing.assert_allclose(Af, Af.T, rtol=0, atol=1e-9 * np.abs(Af).max())
     assert np.linalg.eigvalsh(Af).min() > 0
+
+
+@pytest.mark.parametrize("rotation", [0, 1])
+def test_threaded_oracle_is_bit_identical_to_the_serial_one(oracle, rotation):
+    """The oracle's threaded element loops (test infrastructure, for the
+    config-size parity tests) give the serial restatement's bits: x, v, CG
+    iterations and energies over a few steps of a per-element-material block,
+    under MSVD and DAPD."""
+    import dataclasses
+    from risdsdgcfem_thesis_gb300 import scenes
+    sc = dataclasses.replace(scenes.large_block(n=9), rotation=rotation)
+    serial = oracle.Solid(sc, "port")
+    threaded = oracle.Solid(sc, "port").set_threads(4)
+    for _ in range(3):
+        a, b = serial.step(), threaded.step()
+        assert a == b
+    xa, va = serial.state()
+    xb, vb = threaded.state()
+    assert np.array_equal(xa, xb) and np.array_equal(va, vb)
+    f_a = serial.f_e()
+    f_b = threaded.f_e()
+    assert np.array_equal(f_a, f_b)
