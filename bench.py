@@ -690,10 +690,33 @@ def compression_report(n=40, steps=120, ratio=0.4):
     noise = {"x_rel": float(np.linalg.norm(xp - x64) / np.linalg.norm(x64)),
              "v": float(np.linalg.norm(vp - v64) / vscale) if vscale > 0 else None}
 
+    # the FP64 path's response to FP32-sized changes of its input, the size
+    # of what the mixed path changes: initial velocities perturbed by 6e-8 of
+    # the mesh size (about one FP32 rounding of a position), and the rest
+    # positions rounded to FP32 (so Dm^-1, volumes and stiffness move by FP32
+    # roundings, as the mixed path's FP32 element data do)
+    def fp64_variant(scene, v0=None):
+        run = capi.Batch([scene], precision=capi.FEM_PRECISION_FP64, compute_energy=False)
+        if v0 is not None:
+            run.set_state(0, v=v0)
+        run.step(steps)
+        xq, vq = run.state(0)
+        run.close()
+        return {"x_rel": float(np.linalg.norm(xq - x64) / np.linalg.norm(x64)),
+                "v": float(np.linalg.norm(vq - v64) / vscale) if vscale > 0 else None}
+
+    import dataclasses
+    v32 = 6e-8 * float(np.abs(sc.rest).max()) * np.random.default_rng(2).standard_normal(sc.rest.shape)
+    rest32 = sc.rest.astype(np.float32).astype(np.float64)
+    sc32 = dataclasses.replace(sc, rest=rest32, knc_targets=sc.knc_targets.astype(np.float32).astype(np.float64))
+    fp32_sized = {"initial_velocity_6e-8": fp64_variant(sc, v32),
+                  "rest_positions_rounded_to_fp32": fp64_variant(sc32)}
+
     def mixed(rot32, check):
         mix = capi.Batch([sc], precision=capi.FEM_PRECISION_MIXED, compute_energy=False, rotation_fp32=rot32,
                          rotation_check=check)
         res, inv, itm, tm = [], [], [], 0.0
+        cause = {"det_F": [], "isotropic": [], "tie": [], "check": []}
         for _ in range(steps):
             t0 = time.perf_counter()
             mix.step(1)
@@ -702,9 +725,13 @@ def compression_report(n=40, steps=120, ratio=0.4):
             res.append(b["fp64_resolved"] / T)
             inv.append(b["inverted_elements"] / T)
             itm.append(b["cg_iterations"])
+            for k in cause:
+                cause[k].append(b["resolved_" + k] / T)
         xm, vm = mix.state(0)
         mix.close()
         return {"fp64_resolved_fraction_max": max(res), "fp64_resolved_fraction_mean": float(np.mean(res)),
+                "resolved_by_cause_mean": {k: float(np.mean(v)) for k, v in cause.items()},
+                "resolved_by_cause_max": {k: float(np.max(v)) for k, v in cause.items()},
                 "inverted_fraction_max": max(inv),
                 "x_rel_err_vs_fp64_path": float(np.linalg.norm(xm - x64) / np.linalg.norm(x64)),
                 "v_err_vs_fp64_path": float(np.linalg.norm(vm - v64) / vscale) if vscale > 0 else None,
@@ -716,9 +743,14 @@ def compression_report(n=40, steps=120, ratio=0.4):
             "mixed_fp32_rotations_checked": mixed(1, 1e-3),
             "mixed_fp32_rotations_det_F_rule_only": mixed(1, 0.0),
             "fp64_path_noise_floor": noise,
+            "fp64_path_fp32_sized_input_change": fp32_sized,
             "cg_iterations_fp64_mean": float(np.mean(it64)), "wall_s_fp64": t64,
             "note": "v error normalised by the run's peak |v|; the FP64 path matches the FP64 oracle "
-                    "(tests/test_gpu_fp64.py, tests/test_gpu_batch.py)"}
+                    "(tests/test_gpu_fp64.py, tests/test_gpu_batch.py). fp64_resolved counts rotations "
+                    "re-solved at double precision (every element under the default double-float "
+                    "rotations); resolved_by_cause splits the FP64 MSVD re-solves (det_F: det F <= 1e-3, "
+                    "isotropic: double-float unsafe) and, with FP32 rotations, why the FP32 one was "
+                    "rejected (tie, check)"}
 
 
 # ---------------------------------------------------------------- served leg

@@ -91,7 +91,20 @@ enum fem_material {
      * young_modulus and poisson_ratio, as the reference's element set takes
      * them from its Params even where per-element E, nu re-bake K0. FP64
      * solid only. */
-    FEM_MATERIAL_C_LCM = 1
+    FEM_MATERIAL_C_LCM = 1,
+    /* C_LCMH: C_LCM's force and energy, and a differential that blends LCM
+     * and warped stiffness per element by w = Clamp01(tr|S - I| / (3 k)),
+     * k = ecie_k_factor: dP = 2 mu (w dF + (1 - w) R sym(R^T dF)) +
+     * lambda tr(R^T dF) R for k > 0.1, C_LCM's dP otherwise
+     * (TetrahedronElementSet3.cpp:1875-1930). FP64 solid only. */
+    FEM_MATERIAL_C_LCMH = 2,
+    /* C_CCM: P = R (2 mu (S - I) + lambda (det S - 1) adj(S)^T) and the
+     * reference's differential, which builds dDs from nodes (0, 1, 2, 2)
+     * (TetrahedronElementSet3.cpp:1180-1206, 1932-1970; :1948): its A is not
+     * symmetric positive definite, so CG diverges and the state runs to
+     * Inf/NaN within steps, in the reference as here (FEM_E_NAN). Energy 0
+     * (its body is compiled out of the reference). FP64 solid only. */
+    FEM_MATERIAL_C_CCM = 3
 };
 
 /* Rotation methods of the element set (ms::fem::Params::ERotationMethod,
@@ -158,6 +171,8 @@ typedef struct fem_params {
     double dapd_nl_exponent;  /*   reference, so they are rounded to float */
     uint32_t material;        /* enum fem_material; the batch and server paths take C_WRP only */
     uint32_t pad;
+    double ecie_k_factor;     /* C_LCMH: blend radius k (m_ECIE_k_factor, float32 in the
+                                 reference, default 1) */
 } fem_params;
 
 /* Per-step statistics (the Leaf's per-step LS stats, LeafDSH_Solid3D_FEM.h:597-622). */
@@ -177,6 +192,13 @@ typedef struct fem_step_stats {
     uint32_t pad;
     double nr_rel_residual;   /* FIE: last |y_k| (or |b_k| when it converged) over the first |b_0| */
     double nr_abs_residual;   /* FIE: that last |y_k| or |b_k| (m_SolverNR_AbsPrec) */
+    /* mixed: the re-solved rotations of fp64_resolved by cause. FP64 MSVD:
+     * det F <= degenerate_det_F, or a nearly isotropic F^T F where the
+     * double-float MSVD would lose its precision; with rotation_fp32 = 1
+     * also why the FP32 rotation was not kept: an MSVD branch decision near
+     * a tie, or the rotation_check sensitivity test (these two are re-solved
+     * in double-float unless one of the first two applies) */
+    uint32_t resolved_det_F, resolved_isotropic, resolved_tie, resolved_check;
 } fem_step_stats;
 
 typedef struct fem_solid_s* fem_solid;
@@ -186,7 +208,8 @@ typedef struct fem_solid_s* fem_solid;
  * CG rel 1e-3, abs 1e-6, 20 iterations, FP64, threshold 1e-3, refresh 50,
  * energy on, rotation check 1e-3, refresh every 50 iterations (no drop rule),
  * QIE_V integrator, 3 Newton iterations with abs epsilon 1e-6, CG, MSVD
- * rotations (DAPD threshold 0.1f, factors 1, 0, 2), C_WRP material. */
+ * rotations (DAPD threshold 0.1f, factors 1, 0, 2), C_WRP material (C_LCMH
+ * blend radius 1). */
 int fem_params_default(fem_params* p);
 
 /* Replaces: EditableTetrahedronElementSet3::BeginEdition/AddElement/EndEdition
@@ -213,6 +236,74 @@ int fem_solid_set_knc_targets(fem_solid s, const double* targets);
  * either pointer may be null. set_state also sets the previous positions. */
 int fem_solid_set_state(fem_solid s, const double* x, const double* v);
 int fem_solid_get_state(fem_solid s, double* x, double* v);
+
+/* Replaces: Solid3D::SetParamsExtra (bs/Solid3D.h:150; applied by the Leaf's
+ * "set_params_extra", LeafDSH_Solid3D_FEM.cpp:380-492) and the Leaf's
+ * run-time parameter rebuilds (RebuildMass, RebuildRayleighCoeffsFromFreqs,
+ * RebuildFEM; LeafDSH_Solid3D_FEM.h:289-354) on a live solid, between steps.
+ * Every field may change except precision (FP64): time step, density (node
+ * mass), damping (Rayleigh coefficients), gravity, solver and tolerances,
+ * integrator and Newton settings, material, rotation method and DAPD
+ * settings, energy. Element data are kept unless young_modulus or
+ * poisson_ratio change: then every element is re-baked from those scalar
+ * values, as EditableTetrahedronElementSet3::SetParams does
+ * (TetrahedronElementSet3.cpp:2168-2200), replacing per-element values.
+ * Switching to DAPD starts it from the current positions with no direction
+ * of collapse. Unlike the reference's set_params_extra, whose ls_rel_epsilon
+ * goes through the Newton rebuild and is never applied
+ * (LeafDSH_Solid3D_FEM.cpp:461), ls_rel_epsilon takes effect. */
+int fem_solid_set_params(fem_solid s, const fem_params* params);
+int fem_solid_get_params(fem_solid s, fem_params* params);
+
+/* Replaces: the multi-solid Newton lock-step phases of the Leaf,
+ * NR_Init / NR_PreStep / NR_MidStep / NR_PostStep / NR_End
+ * (LeafDSH_Solid3D_FEM.cpp:2824-3039), which the aggregate scheme
+ * SS_AggregateDSH_Basic::MultiDSH_Solid3D_Update (SS_AggregateDSH_Basic.cpp:
+ * 229-300) calls over all its solids so that contact terms between solids
+ * can enter between them. dt is the phase's step (0: quasi-static); the
+ * solid's integrator setting is not used. The solid's x, v stay x^n, v^n
+ * until NR_End; x_k, v_k are the iterates:
+ *   nr_init      BeginEvaluation at x (DAPD: against the previous
+ *                positions), previous positions = x;
+ *   nr_prestep   x_k = x, v_k = v, the iteration count reset to 0 -- at
+ *                every NR iteration, as in the reference, so each iteration
+ *                solves from x^n with the element forces and rotations of
+ *                the previous iterate's evaluation;
+ *   nr_midstep   b = m g + f_e + (1/dt) m (v - (1/dt)(x_k - x)), warm start
+ *                y = dt v, constraint rows b = y = target - x_k, then the
+ *                solid's linear solver with factor_M = 1/dt^2 + a0/dt,
+ *                factor_K = 1 + a1/dt;
+ *   nr_poststep  x_k += y, v_k = (x_k - x)/dt, BeginEvaluation(x, x_k);
+ *   nr_end       x = x_k, v = v_k, the potential energy (the elastic energy
+ *                keeps its value: NR_End evaluates none).
+ * fem_solid_synchronize then reports the LS iterations and the iteration
+ * count since the last nr_prestep (the Leaf's m_Stats). nr_init allocates
+ * the iterates on first use. */
+int fem_solid_nr_init(fem_solid s, double dt);
+int fem_solid_nr_prestep(fem_solid s, double dt);
+int fem_solid_nr_midstep(fem_solid s, double dt);
+int fem_solid_nr_poststep(fem_solid s, double dt);
+int fem_solid_nr_end(fem_solid s, double dt);
+/* Replaces: the body of SS_AggregateDSH_Basic::MultiDSH_Solid3D_Update
+ * (SS_AggregateDSH_Basic.cpp:229-300) for nsteps fixed steps, its contact
+ * calls left out: nr_init on every solid; then, the largest nr_max_iter of
+ * the solids times, nr_prestep + nr_midstep on every solid and nr_poststep
+ * on every solid; nr_end on every solid. The aggregate's time accumulator
+ * (a step while the accumulated time exceeds the smallest fixed_dt) is the
+ * caller's, as FixedStep is for fem_solid_step. */
+int fem_multi_step(fem_solid* solids, uint32_t count, double dt, uint32_t nsteps);
+
+/* DAPD state, for checkpoint and resume: the positions the last step started
+ * from (m_vecPos0, N*3; the next BeginEvaluation's collapse test compares
+ * against them) and each element's direction of collapse (T*2 bytes, as
+ * fem_solid_get_doc). fem_solid_set_state resets the previous positions to
+ * x, so a resume calls fem_solid_set_state, then fem_solid_set_dapd_state
+ * with the saved values, and then steps as the uninterrupted run would.
+ * Either pointer may be null. FEM_E_ARG when the solid does not use DAPD or
+ * a direction is malformed. No counterpart call in the reference, which
+ * keeps this state inside the element set (TetrahedronElementSet3.cpp:477-584). */
+int fem_solid_get_dapd_state(fem_solid s, double* prev_x, uint8_t* doc);
+int fem_solid_set_dapd_state(fem_solid s, const double* prev_x, const uint8_t* doc);
 
 /* Replaces: LeafDSH_Solid3D_FEM::FixedStep (LeafDSH_Solid3D_FEM.cpp:898-990)
  * with Step_QuasiImplicitEuler_v (:1205-1328), nsteps times. stats may be null. */

@@ -662,6 +662,12 @@ struct orc_solid {
     uint32_t material;
     double lame_mu, lame_lambda;
     mat3* Fm;
+    /* multi-solid Newton lock-step (NR_* phases): iterations since the last
+     * NR_PreStep reset and LS iterations of the last NR_MidStep */
+    uint32_t lock_nr_k, lock_ls_iters;
+    /* ms::fem::Params::m_ECIE_k_factor (float32, default 1.0f): C_LCMH's
+     * radius of its LCM/WRP blend (TetrahedronElementSet3.cpp:1895-1913) */
+    double ecie_k;
     /* host threads of the element loops (orc_solid_set_threads); with more
      * than one, element products go to contrib[4e + i] and are applied node
      * by node in element order through the node -> (4e + i) list */
@@ -702,6 +708,7 @@ orc_solid* orc_solid_create(uint32_t N, const double* rest, uint32_t T, const ui
     for (uint32_t e = 0; e < T; e++) s->doc[e] = kDocInvalid;
     s->Fm = (mat3*)calloc(T, sizeof(mat3));
     s->material = FEM_ORC_MAT_C_WRP;
+    s->ecie_k = (double)1.0f;
     /* LameParameters_From_YoungAndPoisson (TetrahedronElementSet3.cpp:181-186) */
     s->lame_mu = 0.5 * E / (1 + nu);
     s->lame_lambda = E * nu / ((1.0 + nu) * (1.0 - 2.0 * nu));
@@ -999,6 +1006,146 @@ static double lcm_V(const orc_solid* s)
     return acc_V;
 }
 
+static mat3 m_sub(const mat3* a, const mat3* b)
+{
+    mat3 r;
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) r.m[i][j] = a->m[i][j] - b->m[i][j];
+    return r;
+}
+
+/* Adjugate 3x3 (GMat.h:316-329) */
+static mat3 m_adjugate(const mat3* a)
+{
+    const double (*m)[3] = a->m;
+    mat3 r;
+    r.m[0][0] = (m[1][1] * m[2][2] - m[1][2] * m[2][1]);
+    r.m[0][1] = (m[0][2] * m[2][1] - m[0][1] * m[2][2]);
+    r.m[0][2] = (m[0][1] * m[1][2] - m[0][2] * m[1][1]);
+    r.m[1][0] = (m[1][2] * m[2][0] - m[1][0] * m[2][2]);
+    r.m[1][1] = (m[0][0] * m[2][2] - m[0][2] * m[2][0]);
+    r.m[1][2] = (m[0][2] * m[1][0] - m[0][0] * m[1][2]);
+    r.m[2][0] = (m[1][0] * m[2][1] - m[1][1] * m[2][0]);
+    r.m[2][1] = (m[0][1] * m[2][0] - m[0][0] * m[2][1]);
+    r.m[2][2] = (m[0][0] * m[1][1] - m[0][1] * m[1][0]);
+    return r;
+}
+
+/* Inverse 3x3 with a given determinant (GMat.h:291-313) */
+static mat3 m_inverse_det(const mat3* a, double determinant)
+{
+    const double (*m)[3] = a->m;
+    double inv_det = 1.0 / determinant; /* mal::Rcp */
+    mat3 r;
+    r.m[0][0] = inv_det * (m[1][1] * m[2][2] - m[1][2] * m[2][1]);
+    r.m[0][1] = inv_det * (m[0][2] * m[2][1] - m[0][1] * m[2][2]);
+    r.m[0][2] = inv_det * (m[0][1] * m[1][2] - m[0][2] * m[1][1]);
+    r.m[1][0] = inv_det * (m[1][2] * m[2][0] - m[1][0] * m[2][2]);
+    r.m[1][1] = inv_det * (m[0][0] * m[2][2] - m[0][2] * m[2][0]);
+    r.m[1][2] = inv_det * (m[0][2] * m[1][0] - m[0][0] * m[1][2]);
+    r.m[2][0] = inv_det * (m[1][0] * m[2][1] - m[1][1] * m[2][0]);
+    r.m[2][1] = inv_det * (m[0][1] * m[2][0] - m[0][0] * m[2][1]);
+    r.m[2][2] = inv_det * (m[0][0] * m[1][1] - m[0][1] * m[1][0]);
+    return r;
+}
+
+/* C_LCMH_df_x with truncated differentials (TetrahedronElementSet3.cpp:
+ * 1875-1930): for m_ECIE_k_factor k > 0.1 the hybrid of LCM and WRP,
+ *   w = Clamp01(Rcp(k) tr|S - I| / 3),
+ *   dP = 2 mu (w dF + (1 - w) R sym(R^T dF)) + lambda tr(R^T dF) R;
+ * otherwise C_LCM's dP (the WRP branch for k > 10 is unreachable: k > 0.1
+ * is tested first). f_e and V are C_LCM's (:303-400). */
+static void lcmh_df_x_acc(const orc_solid* s, const vec3* dx, vec3* df)
+{
+    const mat3 I = m_identity();
+    const double k = s->ecie_k;
+    for (uint32_t e = 0; e < s->T; e++) {
+        const uint32_t* t = s->tets + 4 * (size_t)e;
+        mat3 Rt = m_transposed(&s->R[e]);
+        mat3 S = m_mul(&Rt, &s->Fm[e]);
+        mat3 dDs = compute_D(dx[t[0]], dx[t[1]], dx[t[2]], dx[t[3]]);
+        mat3 dF = m_mul(&dDs, &s->inv_Dm[e]);
+        mat3 RtdF = m_mul(&Rt, &dF);
+        mat3 dP;
+        if ((float)k > 0.1) {
+            const double cDimension = 3, cRadiusWRP = k;
+            mat3 SmI = m_sub(&S, &I);
+            mat3 A;
+            for (int i = 0; i < 3; i++)
+                for (int j = 0; j < 3; j++) A.m[i][j] = fabs(SmI.m[i][j]);
+            double w = (1.0 / cRadiusWRP) * m_trace(&A) / cDimension;
+            w = (w < 1.0) ? w : 1.0; /* mal::Clamp01 = Max(0, Min(w, 1)) */
+            w = (0.0 > w) ? 0.0 : w;
+            mat3 RtdFt = m_transposed(&RtdF);
+            mat3 sum = m_add(&RtdF, &RtdFt);
+            mat3 sym = m_scale(0.5, &sum);
+            mat3 wdF = m_scale(w, &dF);
+            mat3 oR = m_scale(1 - w, &s->R[e]);
+            mat3 oRsym = m_mul(&oR, &sym);
+            mat3 inner = m_add(&wdF, &oRsym);
+            mat3 T1 = m_scale(2 * s->lame_mu, &inner);
+            mat3 T2 = m_scale(s->lame_lambda * m_trace(&RtdF), &s->R[e]);
+            dP = m_add(&T1, &T2);
+        } else {
+            mat3 A = m_scale(2 * s->lame_mu, &dF);
+            mat3 B = m_scale(s->lame_lambda * m_trace(&RtdF), &s->R[e]);
+            dP = m_add(&A, &B);
+        }
+        pk_scatter(s, e, &dP, df);
+    }
+}
+
+/* C_CCM_f_e (TetrahedronElementSet3.cpp:1180-1206):
+ * S = R^T F, P = R (2 mu (S - I) + lambda (det S - 1) adj(S)^T) */
+static void ccm_f_e_acc(const orc_solid* s, vec3* f)
+{
+    const mat3 I = m_identity();
+    for (uint32_t e = 0; e < s->T; e++) {
+        mat3 Rt = m_transposed(&s->R[e]);
+        mat3 S = m_mul(&Rt, &s->Fm[e]);
+        double det_S = m_det(&S);
+        mat3 SmI = m_sub(&S, &I);
+        mat3 A = m_scale(2 * s->lame_mu, &SmI);
+        mat3 adj = m_adjugate(&S);
+        mat3 adjT = m_transposed(&adj);
+        mat3 B = m_scale(s->lame_lambda * (det_S - 1), &adjT);
+        mat3 AB = m_add(&A, &B);
+        mat3 P = m_mul(&s->R[e], &AB);
+        pk_scatter(s, e, &P, f);
+    }
+}
+
+/* C_CCM_df_x with truncated differentials (TetrahedronElementSet3.cpp:
+ * 1932-1970), with the reference's dDs built from nodes (0, 1, 2, 2) -- its
+ * fourth argument repeats node 2 (:1948) -- and F^-1 regularised at det F = 0
+ * by det F + Sign(det F) 1e-6f:
+ *   dP = 2 mu dF + lambda ((2 J^2 - J) tr(F^-1 dF) F^-T
+ *                          - (J^2 - J) F^-T dF^T F^-T),  J = det F */
+static void ccm_df_x_acc(const orc_solid* s, const vec3* dx, vec3* df)
+{
+    const double reg = (double)1e-6f; /* REGULARIZE_CCM_PD_U_THRESHOLD (:35) */
+    for (uint32_t e = 0; e < s->T; e++) {
+        const uint32_t* t = s->tets + 4 * (size_t)e;
+        mat3 dDs = compute_D(dx[t[0]], dx[t[1]], dx[t[2]], dx[t[2]]);
+        mat3 dF = m_mul(&dDs, &s->inv_Dm[e]);
+        mat3 dP = m_scale(2 * s->lame_mu, &dF);
+        const double J = s->detF[e];
+        const double sign = (J >= 0.0) ? 1.0 : -1.0; /* mal::Sign */
+        mat3 invF = m_inverse_det(&s->Fm[e], J + sign * reg);
+        mat3 invFt = m_transposed(&invF);
+        mat3 invFdF = m_mul(&invF, &dF);
+        mat3 X = m_scale((2 * (J * J) - J) * m_trace(&invFdF), &invFt);
+        mat3 c2invFt = m_scale((J * J) - J, &invFt);
+        mat3 dFt = m_transposed(&dF);
+        mat3 Y1 = m_mul(&c2invFt, &dFt);
+        mat3 Y = m_mul(&Y1, &invFt);
+        mat3 XY = m_sub(&X, &Y);
+        mat3 W = m_scale(s->lame_lambda, &XY);
+        dP = m_add(&dP, &W);
+        pk_scatter(s, e, &dP, df);
+    }
+}
+
 /* ---- element loops over host threads ------------------------------------
  * Test infrastructure speed only: the oracle's serial scatter
  * f[t[i]] -= c_{e,i} runs element after element. With threads, each
@@ -1105,8 +1252,13 @@ static void wrp_scatter_threaded(const orc_solid* s, const vec3* in, int with_re
 /* C_f_e (TetrahedronElementSet3.cpp:1053-1096): f_i -= R sum_j K_ij (R^T x_j - r_j) */
 static void f_e_acc(const orc_solid* s, const vec3* x, vec3* f)
 {
-    if (s->material == FEM_ORC_MAT_C_LCM) {
+    /* f_e dispatch (TetrahedronElementSet3.cpp:303-322): C_LCMH uses C_LCM's */
+    if (s->material == FEM_ORC_MAT_C_LCM || s->material == FEM_ORC_MAT_C_LCMH) {
         lcm_f_e_acc(s, f);
+        return;
+    }
+    if (s->material == FEM_ORC_MAT_C_CCM) {
+        ccm_f_e_acc(s, f);
         return;
     }
     if (s->threads > 1) {
@@ -1131,8 +1283,17 @@ static void f_e_acc(const orc_solid* s, const vec3* x, vec3* f)
  * df_i -= R sum_j K_ij R^T dx_j */
 static void df_x_acc(const orc_solid* s, const vec3* dx, vec3* df)
 {
+    /* df_x dispatch (TetrahedronElementSet3.cpp:355-377) */
     if (s->material == FEM_ORC_MAT_C_LCM) {
         lcm_df_x_acc(s, dx, df);
+        return;
+    }
+    if (s->material == FEM_ORC_MAT_C_LCMH) {
+        lcmh_df_x_acc(s, dx, df);
+        return;
+    }
+    if (s->material == FEM_ORC_MAT_C_CCM) {
+        ccm_df_x_acc(s, dx, df);
         return;
     }
     if (s->threads > 1) {
@@ -1156,7 +1317,10 @@ static void df_x_acc(const orc_solid* s, const vec3* dx, vec3* df)
 /* C_V (TetrahedronElementSet3.cpp:1456-1488) */
 static double elastic_V(const orc_solid* s)
 {
-    if (s->material == FEM_ORC_MAT_C_LCM) return lcm_V(s);
+    /* V dispatch (TetrahedronElementSet3.cpp:382-400): C_LCMH uses C_LCM_V;
+     * C_CCM_V's body is compiled out (__TO_PORT_TO_3D) and returns 0 (:1509-1545) */
+    if (s->material == FEM_ORC_MAT_C_LCM || s->material == FEM_ORC_MAT_C_LCMH) return lcm_V(s);
+    if (s->material == FEM_ORC_MAT_C_CCM) return 0.0;
     double acc_twice_V = 0;
     for (uint32_t e = 0; e < s->T; e++) {
         const uint32_t* t = s->tets + 4 * (size_t)e;
@@ -1320,6 +1484,126 @@ static void step_fie(orc_solid* s, double h)
     for (uint32_t i = 0; i < N; i++) { s->x[i] = s->xk[i]; s->v[i] = s->vk[i]; }
 }
 
+/* ---- multi-solid Newton lock-step (LeafDSH_Solid3D_FEM.cpp:2824-3039) ----
+ * The phases SS_AggregateDSH_Basic::MultiDSH_Solid3D_Update
+ * (SS_AggregateDSH_Basic.cpp:229-300) interleaves over its solids. x, v stay
+ * at x^n, v^n until NR_End; x_k, v_k are the iterates. NR_PreStep resets
+ * x_k = x^n, v_k = v^n and the iteration count at every NR iteration, so
+ * each iteration solves the first Newton system again with the element
+ * forces and rotations of the previous iterate's BeginEvaluation (the
+ * cache's positions are the x_k array, which then holds x^n again). */
+
+/* NR_Init (:2824-2845): UpdateKNC (a no-op in the default kinematic mode),
+ * BeginEvaluation(m_vecPos0, x), m_vecPos0 = x */
+void orc_solid_nr_init(orc_solid* s, double dt)
+{
+    (void)dt;
+    g_math = s->math;
+    begin_evaluation(s);
+    for (uint32_t i = 0; i < s->N; i++) s->prev_x[i] = s->x[i];
+}
+
+/* NR_PreStep (:2870-2890) */
+void orc_solid_nr_prestep(orc_solid* s, double dt)
+{
+    (void)dt;
+    for (uint32_t i = 0; i < s->N; i++) {
+        s->xk[i] = s->x[i];
+        s->vk[i] = s->v[i];
+    }
+    s->lock_nr_k = 0;
+    s->lock_ls_iters = 0;
+}
+
+/* NR_MidStep (:2892-2990): b = m g + f_e + (1/h) m (v - (1/h)(x_k - x)),
+ * warm start y = h v on the first iteration after a reset (always, since
+ * NR_PreStep resets the count), position constraints as b = y = target -
+ * x_k (the KNC velocity bookkeeping does not feed this integrator), then
+ * the linear solve with factor_M = 1/h^2 + a0/h, factor_K = 1 + a1/h. */
+void orc_solid_nr_midstep(orc_solid* s, double dt)
+{
+    g_math = s->math;
+    const uint32_t N = s->N;
+    const double inv_dt = (dt == 0) ? 0 : 1.0 / dt;
+    const double mass = 1.0 / s->inv_mass;
+    for (uint32_t i = 0; i < N; i++) s->b[i] = v3(0, 0, 0);
+    for (uint32_t i = 0; i < N; i++) s->b[i] = v_add(s->b[i], v_scale(mass, s->gravity));
+    f_e_acc(s, s->xk, s->b);
+    for (uint32_t i = 0; i < N; i++)
+        s->b[i] = v_add(s->b[i], v_scale(inv_dt * mass, v_sub(s->v[i], v_scale(inv_dt, v_sub(s->xk[i], s->x[i])))));
+    if (s->lock_nr_k == 0) for (uint32_t i = 0; i < N; i++) s->y[i] = v_scale(dt, s->v[i]);
+    else memset(s->y, 0, sizeof(vec3) * N);
+    for (uint32_t k = 0; k < s->n_knc; k++) {
+        uint32_t nid = s->knc_nid[k];
+        vec3 vk = v_scale(inv_dt, v_sub(s->knc_pos[k], s->x[nid]));
+        double norm_vk = v_norm(vk);
+        if (norm_vk > (double)0.001f) {
+            double clamp = (norm_vk < 50.0) ? norm_vk : 50.0;
+            s->knc_vel[k] = v_scale(clamp, v_normalized(vk));
+        } else {
+            s->knc_vel[k] = v3(0, 0, 0);
+        }
+        s->b[nid] = v_sub(s->knc_pos[k], s->xk[nid]);
+        s->y[nid] = v_sub(s->knc_pos[k], s->xk[nid]);
+    }
+    s->factor_M = inv_dt * inv_dt + inv_dt * s->rayleigh[0];
+    s->factor_K = 1.0 + inv_dt * s->rayleigh[1];
+    ls_solve(s, (double*)s->y, (const double*)s->b);
+    s->lock_ls_iters += s->last_iters;
+}
+
+/* NR_PostStep (:2992-3020): x_k += y, v_k = (x_k - x)/h, BeginEvaluation(x, x_k) */
+void orc_solid_nr_poststep(orc_solid* s, double dt)
+{
+    g_math = s->math;
+    const double inv_dt = (dt == 0) ? 0 : 1.0 / dt;
+    for (uint32_t i = 0; i < s->N; i++) s->xk[i] = v_add(s->xk[i], s->y[i]);
+    for (uint32_t i = 0; i < s->N; i++) s->vk[i] = v_scale(inv_dt, v_sub(s->xk[i], s->x[i]));
+    s->lock_nr_k++;
+    begin_evaluation_at(s, s->x, s->xk);
+}
+
+/* NR_End (:2847-2868): x = x_k, v = v_k, RecomputeEnergy's potential term
+ * (no air drag by default); NR_End evaluates no V, so the elastic energy
+ * keeps its value */
+void orc_solid_nr_end(orc_solid* s, double dt)
+{
+    (void)dt;
+    g_math = s->math;
+    for (uint32_t i = 0; i < s->N; i++) {
+        s->x[i] = s->xk[i];
+        s->v[i] = s->vk[i];
+    }
+    s->potential_energy = potential_energy(s);
+}
+
+/* SS_AggregateDSH_Basic::MultiDSH_Solid3D_Update's body for one fixed step
+ * (its contact calls left out): NR_Init for all; the largest nr_max_iter of
+ * the solids NR iterations of (NR_PreStep, NR_MidStep for all; NR_PostStep
+ * for all); NR_End for all -- every phase with the same dt. */
+void orc_multi_lock_step(orc_solid** solids, uint32_t count, double dt)
+{
+    uint32_t max_nr_iter = 0;
+    for (uint32_t i = 0; i < count; i++)
+        max_nr_iter = solids[i]->nr_max_iter > max_nr_iter ? solids[i]->nr_max_iter : max_nr_iter;
+    for (uint32_t i = 0; i < count; i++) orc_solid_nr_init(solids[i], dt);
+    uint32_t nr_iter = 0;
+    do {
+        for (uint32_t i = 0; i < count; i++) {
+            orc_solid_nr_prestep(solids[i], dt);
+            orc_solid_nr_midstep(solids[i], dt);
+        }
+        for (uint32_t i = 0; i < count; i++) orc_solid_nr_poststep(solids[i], dt);
+    } while (++nr_iter < max_nr_iter);
+    for (uint32_t i = 0; i < count; i++) orc_solid_nr_end(solids[i], dt);
+}
+
+void orc_solid_last_lock_stats(const orc_solid* s, uint32_t* nr_k, uint32_t* ls_iters)
+{
+    *nr_k = s->lock_nr_k;
+    *ls_iters = s->lock_ls_iters;
+}
+
 /* ILSS_MINRES::Solve (src/Saphyre2/ns/ILSS_MINRES.h:51-168): Paige-Saunders
  * MINRES without a preconditioner, the scalar real_array kernels
  * (src/Saphyre2/ns/real_array.h:91-113), the residual norm carried by the
@@ -1481,6 +1765,7 @@ void orc_solid_doc(const orc_solid* s, uint8_t* doc2)
 }
 
 void orc_solid_set_material(orc_solid* s, uint32_t material) { s->material = material; }
+void orc_solid_set_ecie_k_factor(orc_solid* s, double k) { s->ecie_k = (double)(float)k; }
 
 void orc_solid_set_ls_solver(orc_solid* s, uint32_t ls_solver)
 {

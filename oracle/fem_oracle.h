@@ -40,7 +40,7 @@ enum { FEM_ORC_MATH_DOUBLE = 0, FEM_ORC_MATH_FLOAT_LITERAL = 1 };
 /* ms::fem::Params::ERotationMethod values this oracle evaluates */
 enum { FEM_ORC_ROT_MSVD = 0, FEM_ORC_ROT_DAPD = 1 };
 /* ms::fem::Params::m_MM values this oracle evaluates */
-enum { FEM_ORC_MAT_C_WRP = 0, FEM_ORC_MAT_C_LCM = 1 };
+enum { FEM_ORC_MAT_C_WRP = 0, FEM_ORC_MAT_C_LCM = 1, FEM_ORC_MAT_C_LCMH = 2, FEM_ORC_MAT_C_CCM = 3 };
 /* LeafDSH_Solid3D_FEM::Params::m_SolverLS_Type values this oracle solves with */
 enum { FEM_ORC_LS_CG = 0, FEM_ORC_LS_MINRES = 1 };
 /* LeafDSH_Solid3D_FEM::Params::EIntegratorType values this oracle steps */
@@ -77,6 +77,8 @@ void orc_solid_doc(const orc_solid* s, uint8_t* doc2);
 /* Material model (FEM_ORC_MAT_*); C_LCM's Lame parameters come from the
  * scalar E and nu given at creation, as the reference's element set's do. */
 void orc_solid_set_material(orc_solid* s, uint32_t material);
+/* C_LCMH's blend radius m_ECIE_k_factor (float32 in the reference; default 1). */
+void orc_solid_set_ecie_k_factor(orc_solid* s, double k);
 /* Linear solver of the step (FEM_ORC_LS_*). */
 void orc_solid_set_ls_solver(orc_solid* s, uint32_t ls_solver);
 /* Integrator (FEM_ORC_*), Newton iteration cap and |b_k| epsilon (FIE only). */
@@ -85,6 +87,18 @@ void orc_solid_set_integrator(orc_solid* s, uint32_t integrator, uint32_t nr_max
 void orc_solid_last_nr_stats(const orc_solid* s, uint32_t* nr_iters, double* nr_rel, double* nr_abs);
 void orc_solid_last_stats(const orc_solid* s, uint32_t* iters, double* rel_res, double* abs_res,
                           double* elastic_energy, double* potential_energy);
+
+/* The multi-solid Newton lock-step phases (LeafDSH_Solid3D_FEM.cpp:
+ * 2824-3039) and the aggregate's loop of one fixed step over them
+ * (SS_AggregateDSH_Basic.cpp:229-300, contacts left out). */
+void orc_solid_nr_init(orc_solid* s, double dt);
+void orc_solid_nr_prestep(orc_solid* s, double dt);
+void orc_solid_nr_midstep(orc_solid* s, double dt);
+void orc_solid_nr_poststep(orc_solid* s, double dt);
+void orc_solid_nr_end(orc_solid* s, double dt);
+void orc_multi_lock_step(orc_solid** solids, uint32_t count, double dt);
+/* Iterations since the last NR_PreStep and LS iterations of its NR_MidStep. */
+void orc_solid_last_lock_stats(const orc_solid* s, uint32_t* nr_k, uint32_t* ls_iters);
 
 /* Element-level hooks (state: the positions given to begin_eval). */
 void orc_solid_begin_eval(orc_solid* s, const double* x);

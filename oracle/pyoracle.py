@@ -86,7 +86,12 @@ def _load(path: str, prefix: str):
     fn("solid_set_rotation").argtypes = [C.c_void_p, C.c_uint32, C.c_double, C.c_double, C.c_double, C.c_double]
     fn("solid_set_ls_solver").argtypes = [C.c_void_p, C.c_uint32]
     fn("solid_set_material").argtypes = [C.c_void_p, C.c_uint32]
+    fn("solid_set_ecie_k_factor").argtypes = [C.c_void_p, C.c_double]
     fn("solid_last_nr_stats").argtypes = [C.c_void_p, _up, _dp, _dp]
+    for ph in ("init", "prestep", "midstep", "poststep", "end"):
+        fn("solid_nr_" + ph).argtypes = [C.c_void_p, C.c_double]
+    fn("multi_lock_step").argtypes = [C.POINTER(C.c_void_p), C.c_uint32, C.c_double]
+    fn("solid_last_lock_stats").argtypes = [C.c_void_p, _up, _up]
     if P == "orc_":
         lib.orc_solid_begin_eval.argtypes = [C.c_void_p, _dp]
         lib.orc_solid_rotations.argtypes = [C.c_void_p, _dp]
@@ -161,6 +166,8 @@ class Solid:
                                                               scene.dapd_L, scene.dapd_NL, scene.dapd_exponent)
         if getattr(scene, "material", 0):
             getattr(self.lib, self.p + "solid_set_material")(self.h, scene.material)
+        if getattr(scene, "ecie_k_factor", 1.0) != 1.0:
+            getattr(self.lib, self.p + "solid_set_ecie_k_factor")(self.h, scene.ecie_k_factor)
         if getattr(scene, "ls_solver", 0):
             getattr(self.lib, self.p + "solid_set_ls_solver")(self.h, scene.ls_solver)
         if getattr(scene, "integrator", 0):
@@ -218,6 +225,21 @@ class Solid:
         out = np.empty(2)
         getattr(self.lib, self.p + "solid_rayleigh")(self.h, _ptr(out))
         return out
+
+    def set_knc_targets_at(self, step: int):
+        """Targets of the driven constraints at `step` of the scene's schedule."""
+        tg = _f64(self.scene.targets_at(step))
+        getattr(self.lib, self.p + "solid_set_knc_targets")(self.h, _ptr(tg))
+
+    def nr_phase(self, phase: str, dt: float):
+        """One multi-solid Newton lock-step phase: init, prestep, midstep,
+        poststep or end (the Leaf's NR_* methods)."""
+        getattr(self.lib, self.p + "solid_nr_" + phase)(self.h, dt)
+
+    def lock_stats(self):
+        k, ls = C.c_uint32(), C.c_uint32()
+        getattr(self.lib, self.p + "solid_last_lock_stats")(self.h, C.byref(k), C.byref(ls))
+        return {"nr_iters": k.value, "iters": ls.value}
 
     def set_threads(self, threads: int):
         """Host threads of the element loops (port only); results are
@@ -279,6 +301,22 @@ class Solid:
         K = np.empty((4, 4, 3, 3))
         self.lib.orc_solid_element_K(self.h, e, _ptr(K))
         return K
+
+
+def multi_lock_step(solids, dt: float):
+    """One fixed step of the multi-solid aggregate
+    (SS_AggregateDSH_Basic::MultiDSH_Solid3D_Update, contacts off) over
+    oracle solids of one kind; the schedules of driven constraints advance
+    as in Solid.step."""
+    lib, p = solids[0].lib, solids[0].p
+    for s in solids:
+        sc = s.scene
+        if sc.knc_schedule is not None and s._knc_nodes.size:
+            tg = _f64(sc.targets_at(s.step_index))
+            getattr(lib, p + "solid_set_knc_targets")(s.h, _ptr(tg))
+        s.step_index += 1
+    arr = (C.c_void_p * len(solids))(*[s.h for s in solids])
+    getattr(lib, p + "multi_lock_step")(arr, len(solids), dt)
 
 
 class RefElementSet:

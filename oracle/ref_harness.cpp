@@ -51,8 +51,15 @@ class PerElementTES : public ms::fem::EditableTetrahedronElementSet3
 public:
     // ms::fem::Params::m_RM and the DAPD parameters (Params.h:27-29,63-67),
     // set in place so that per-element materials stay baked.
-    // ms::fem::Params::m_MM (Params.h:48-62): 0 C_WRP, 1 C_LCM
-    void SetMaterial(unsigned mm) { m_Params.m_MM = mm ? ms::fem::Params::eMM_C_LCM : ms::fem::Params::eMM_C_WRP; }
+    // ms::fem::Params::m_MM (Params.h:48-62): 0 C_WRP, 1 C_LCM, 2 C_LCMH, 3 C_CCM
+    void SetMaterial(unsigned mm)
+    {
+        static const ms::fem::Params::EMaterialMethod kMM[4] = {ms::fem::Params::eMM_C_WRP, ms::fem::Params::eMM_C_LCM,
+                                                                ms::fem::Params::eMM_C_LCMH, ms::fem::Params::eMM_C_CCM};
+        m_Params.m_MM = kMM[mm < 4 ? mm : 0];
+    }
+    // ms::fem::Params::m_ECIE_k_factor (Params.h:30,89), C_LCMH's blend radius
+    void SetEcieK(double k) { m_Params.m_ECIE_k_factor = float32(k); }
     void SetRotation(unsigned method, double thr, double factor_L, double factor_NL, double exponent_NL)
     {
         m_Params.m_RM = method ? ms::fem::Params::eRM_DAPD : ms::fem::Params::eRM_MSVD;
@@ -123,6 +130,9 @@ struct ref_solid {
     std::vector<Vec3> xk, vk;  // m_IE_vec_x_k, m_IE_vec_v_k
     unsigned nr_iters;
     Real nr_rel, nr_abs;
+    // multi-solid Newton lock-step: m_NR_nr_k and the LS iterations since the
+    // last NR_PreStep (m_Stats.m_SolverLS_NumIter)
+    unsigned lock_nr_k = 0, lock_ls_iters = 0;
 };
 
 static Vec3 V3(const double* p) { return Vec3(Real(p[0]), Real(p[1]), Real(p[2])); }
@@ -428,6 +438,7 @@ void ref_solid_set_rotation(ref_solid* s, unsigned method, double thr, double fa
 void ref_solid_set_ls_solver(ref_solid* s, unsigned ls_solver) { s->ls_solver = ls_solver; }
 
 void ref_solid_set_material(ref_solid* s, unsigned material) { s->t->tes.SetMaterial(material); }
+void ref_solid_set_ecie_k_factor(ref_solid* s, double k) { s->t->tes.SetEcieK(k); }
 
 void ref_solid_set_integrator(ref_solid* s, unsigned integrator, unsigned nr_max_iter, double nr_abs_eps)
 {
@@ -491,22 +502,136 @@ void ref_solid_fixed_step(ref_solid* s)
 
 /* The end of FixedStep after integration (LeafDSH_Solid3D_FEM.cpp:978-989):
  * elastic energy, EndEvaluation, RecomputeEnergy's potential term. */
+// RecomputeEnergy (LeafDSH_Solid3D_FEM.cpp:1554-1584): potential part
+static Real potential(ref_solid* s)
+{
+    ref_tes* t = s->t;
+    Real pe(0);
+    for (unsigned e = 0; e < t->T; e++) {
+        unsigned nid[4];
+        t->tes.GetNID(e, nid[0], nid[1], nid[2], nid[3]);
+        Real element_mass(s->density * t->tes.Volume(e));
+        pe += (element_mass / Real(4)) *
+            mal::Dot(t->x[nid[0]] + t->x[nid[1]] + t->x[nid[2]] + t->x[nid[3]], -s->gravity);
+    }
+    return pe;
+}
+
 static void finish_step(ref_solid* s)
 {
     ref_tes* t = s->t;
     const Real dt = s->dt;
     s->elastic_energy = t->tes.V(t->cache);
     t->tes.EndEvaluation(t->cache);
-    // RecomputeEnergy (LeafDSH_Solid3D_FEM.cpp:1554-1584): potential part
-    s->potential_energy = Real(0);
-    for (unsigned e = 0; e < t->T; e++) {
-        unsigned nid[4];
-        t->tes.GetNID(e, nid[0], nid[1], nid[2], nid[3]);
-        Real element_mass(s->density * t->tes.Volume(e));
-        s->potential_energy += (element_mass / Real(4)) *
-            mal::Dot(t->x[nid[0]] + t->x[nid[1]] + t->x[nid[2]] + t->x[nid[3]], -s->gravity);
-    }
+    s->potential_energy = potential(s);
     s->total_time += dt;
+}
+
+/* The multi-solid Newton lock-step phases, restated from
+ * LeafDSH_Solid3D_FEM::NR_Init / NR_PreStep / NR_MidStep / NR_PostStep /
+ * NR_End (LeafDSH_Solid3D_FEM.cpp:2824-3039) around the reference's element
+ * set and solvers, contacts off, warm start on, default kinematic mode
+ * (UpdateKNC a no-op). The element set's cache keeps the position array of
+ * its last BeginEvaluation: after NR_PostStep that is xk, which the next
+ * NR_PreStep resets to x. */
+void ref_solid_nr_init(ref_solid* s, double)
+{
+    ref_tes* t = s->t;
+    t->tes.BeginEvaluation(t->cache, &t->prev_x[0], &t->x[0], &t->v[0], s->total_time);
+    for (unsigned i = 0; i < t->N; i++) t->prev_x[i] = t->x[i];
+}
+
+void ref_solid_nr_prestep(ref_solid* s, double)
+{
+    ref_tes* t = s->t;
+    for (unsigned i = 0; i < t->N; i++) {
+        s->xk[i] = t->x[i];
+        s->vk[i] = t->v[i];
+    }
+    s->lock_nr_k = 0;
+    s->lock_ls_iters = 0;
+}
+
+void ref_solid_nr_midstep(ref_solid* s, double dt_in)
+{
+    ref_tes* t = s->t;
+    const unsigned N = t->N;
+    const Real dt(dt_in);
+    const Real inv_dt(dt == 0 ? 0 : mal::Rcp(dt));
+    for (unsigned i = 0; i < N; i++) s->b[i] = Vec3::Zero();
+    for (unsigned i = 0; i < N; i++) s->b[i] += (Real(1) / t->inv_mass[i]) * s->gravity;
+    t->tes.f_e(t->cache, &s->b[0]);
+    t->tes.f_p(t->cache, &s->b[0]);
+    for (unsigned i = 0; i < N; i++)
+        s->b[i] += inv_dt * (Real(1) / t->inv_mass[i]) * (t->v[i] - inv_dt * (s->xk[i] - t->x[i]));
+    if (s->lock_nr_k == 0) for (unsigned i = 0; i < N; i++) s->y[i] = dt * t->v[i];
+    else for (unsigned i = 0; i < N; i++) s->y[i] = Vec3::Zero();
+    for (size_t k = 0; k < s->knc.size(); k++) {
+        RefKNC& c = s->knc[k];
+        if (c.is_position) {
+            Vec3 vk((c.pos - t->x[c.nid]) * inv_dt);
+            Real norm_vk(vk.Norm());
+            if (norm_vk > Real(0.001f))
+                c.vel = mal::Min(norm_vk, Real(50.0f)) * vk.Normalized();
+            else
+                c.vel = Vec3::Zero();
+        }
+        s->b[c.nid] = c.pos - s->xk[c.nid];
+        s->y[c.nid] = c.pos - s->xk[c.nid];
+    }
+    s->factor_M = mal::Sq(inv_dt) + inv_dt * s->rayleigh[0];
+    s->factor_K = Real(1) + inv_dt * s->rayleigh[1];
+    ls_solve(s);
+    s->lock_ls_iters += s->last_iters;
+}
+
+void ref_solid_nr_poststep(ref_solid* s, double dt_in)
+{
+    ref_tes* t = s->t;
+    const Real dt(dt_in);
+    const Real inv_dt(dt == 0 ? 0 : mal::Rcp(dt));
+    ns::real_array::addeq(reinterpret_cast<Real*>(&s->xk[0]), reinterpret_cast<const Real*>(&s->y[0]), 3 * t->N);
+    for (unsigned i = 0; i < t->N; i++) s->vk[i] = inv_dt * (s->xk[i] - t->x[i]);
+    s->lock_nr_k++;
+    t->tes.EndEvaluation(t->cache);
+    t->tes.BeginEvaluation(t->cache, &t->x[0], &s->xk[0], &s->vk[0], s->total_time);
+}
+
+void ref_solid_nr_end(ref_solid* s, double)
+{
+    ref_tes* t = s->t;
+    for (unsigned i = 0; i < t->N; i++) {
+        t->x[i] = s->xk[i];
+        t->v[i] = s->vk[i];
+    }
+    t->tes.EndEvaluation(t->cache);
+    // RecomputeEnergy (LeafDSH_Solid3D_FEM.cpp:1554-1584): the potential
+    // term; NR_End does not evaluate V, so the elastic energy keeps its value
+    s->potential_energy = potential(s);
+}
+
+/* SS_AggregateDSH_Basic::MultiDSH_Solid3D_Update's body for one fixed step
+ * (SS_AggregateDSH_Basic.cpp:229-300), contacts off. */
+void ref_multi_lock_step(ref_solid** solids, unsigned count, double dt)
+{
+    unsigned max_nr_iter = 0;
+    for (unsigned i = 0; i < count; i++) max_nr_iter = std::max(max_nr_iter, solids[i]->nr_max_iter);
+    for (unsigned i = 0; i < count; i++) ref_solid_nr_init(solids[i], dt);
+    unsigned nr_iter = 0;
+    do {
+        for (unsigned i = 0; i < count; i++) {
+            ref_solid_nr_prestep(solids[i], dt);
+            ref_solid_nr_midstep(solids[i], dt);
+        }
+        for (unsigned i = 0; i < count; i++) ref_solid_nr_poststep(solids[i], dt);
+    } while (++nr_iter < max_nr_iter);
+    for (unsigned i = 0; i < count; i++) ref_solid_nr_end(solids[i], dt);
+}
+
+void ref_solid_last_lock_stats(ref_solid* s, unsigned* nr_k, unsigned* ls_iters)
+{
+    *nr_k = s->lock_nr_k;
+    *ls_iters = s->lock_ls_iters;
 }
 
 void ref_solid_last_stats(ref_solid* s, unsigned* iters, double* rel_res, double* abs_res,

@@ -28,6 +28,8 @@ FEM_LS_CG = 0
 FEM_LS_MINRES = 1
 FEM_MATERIAL_C_WRP = 0
 FEM_MATERIAL_C_LCM = 1
+FEM_MATERIAL_C_LCMH = 2
+FEM_MATERIAL_C_CCM = 3
 FEM_WAIT_LIMIT_DEFAULT = 0xFFFFFFFF
 
 _dp = C.POINTER(C.c_double)
@@ -63,6 +65,7 @@ class FemParams(C.Structure):
         ("dapd_nl_exponent", C.c_double),
         ("material", C.c_uint32),
         ("pad", C.c_uint32),
+        ("ecie_k_factor", C.c_double),
     ]
 
 
@@ -81,6 +84,10 @@ class FemStepStats(C.Structure):
         ("pad", C.c_uint32),
         ("nr_rel_residual", C.c_double),
         ("nr_abs_residual", C.c_double),
+        ("resolved_det_F", C.c_uint32),
+        ("resolved_isotropic", C.c_uint32),
+        ("resolved_tie", C.c_uint32),
+        ("resolved_check", C.c_uint32),
     ]
 
     def as_dict(self):
@@ -117,6 +124,16 @@ SIGNATURES = {
     "fem_solid_energy": (C.c_int, [C.c_void_p, _dp]),
     "fem_solid_mass_info": (C.c_int, [C.c_void_p, _dp, _dp, _dp]),
     "fem_solid_apply_A_noalloc": (C.c_int, [C.c_void_p, C.c_double, C.c_double, _dp, _dp]),
+    "fem_solid_set_params": (C.c_int, [C.c_void_p, C.POINTER(FemParams)]),
+    "fem_solid_nr_init": (C.c_int, [C.c_void_p, C.c_double]),
+    "fem_solid_nr_prestep": (C.c_int, [C.c_void_p, C.c_double]),
+    "fem_solid_nr_midstep": (C.c_int, [C.c_void_p, C.c_double]),
+    "fem_solid_nr_poststep": (C.c_int, [C.c_void_p, C.c_double]),
+    "fem_solid_nr_end": (C.c_int, [C.c_void_p, C.c_double]),
+    "fem_multi_step": (C.c_int, [C.POINTER(C.c_void_p), C.c_uint32, C.c_double, C.c_uint32]),
+    "fem_solid_get_params": (C.c_int, [C.c_void_p, C.POINTER(FemParams)]),
+    "fem_solid_get_dapd_state": (C.c_int, [C.c_void_p, _dp, C.POINTER(C.c_uint8)]),
+    "fem_solid_set_dapd_state": (C.c_int, [C.c_void_p, _dp, C.POINTER(C.c_uint8)]),
     "fem_solid_step_async": (C.c_int, [C.c_void_p, C.c_uint32]),
     "fem_solid_synchronize": (C.c_int, [C.c_void_p, C.POINTER(FemStepStats)]),
     "fem_solid_stream": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
@@ -185,6 +202,7 @@ def params_for(scene, precision: int = FEM_PRECISION_FP64, compute_energy: bool 
     p.nr_abs_epsilon = getattr(scene, "nr_abs_eps", 1e-6)
     p.ls_solver = getattr(scene, "ls_solver", FEM_LS_CG)
     p.material = getattr(scene, "material", FEM_MATERIAL_C_WRP)
+    p.ecie_k_factor = getattr(scene, "ecie_k_factor", 1.0)
     p.rotation = getattr(scene, "rotation", FEM_ROTATION_MSVD)
     if p.rotation == FEM_ROTATION_DAPD:
         p.dapd_threshold_det_F = scene.dapd_threshold
@@ -245,6 +263,39 @@ class Solid:
     def set_knc_targets(self, targets):
         t = _f64(targets)
         check(self.lib.fem_solid_set_knc_targets(self.h, _ptr(t)))
+
+    def set_params(self, params):
+        """Run-time parameter change (fem_solid_set_params)."""
+        check(self.lib.fem_solid_set_params(self.h, C.byref(params)))
+        self.params = params
+
+    def get_params(self):
+        p = FemParams()
+        check(self.lib.fem_solid_get_params(self.h, C.byref(p)))
+        return p
+
+    def nr_phase(self, phase, dt):
+        """One multi-solid Newton lock-step phase (init, prestep, midstep,
+        poststep, end; fem_solid_nr_*)."""
+        check(getattr(self.lib, "fem_solid_nr_" + phase)(self.h, float(dt)))
+
+    def stats(self):
+        st = FemStepStats()
+        check(self.lib.fem_solid_synchronize(self.h, C.byref(st)))
+        return st.as_dict()
+
+    def dapd_state(self):
+        """(previous positions (N, 3), directions of collapse (T, 2))."""
+        px = np.empty((self.N, 3))
+        doc = np.empty((self.T, 2), np.uint8)
+        check(self.lib.fem_solid_get_dapd_state(self.h, _ptr(px), doc.ctypes.data_as(C.POINTER(C.c_uint8))))
+        return px, doc
+
+    def set_dapd_state(self, prev_x=None, doc=None):
+        px = _f64(prev_x)
+        d = None if doc is None else np.ascontiguousarray(doc, dtype=np.uint8)
+        check(self.lib.fem_solid_set_dapd_state(self.h, _ptr(px),
+                                                None if d is None else d.ctypes.data_as(C.POINTER(C.c_uint8))))
 
     def step(self, n: int = 1):
         st = FemStepStats()
@@ -444,6 +495,20 @@ def batch_options(precision=FEM_PRECISION_MIXED, tile_elems=256, reorder=True, u
         o.chunk_nodes = chunk_nodes
     o.fuse_alpha = 1 if fuse_alpha else 0
     return o
+
+
+def multi_step(solids, dt, nsteps=1):
+    """fem_multi_step over Solid objects (the aggregate's lock-step); the
+    schedules of driven constraints advance per step as in Solid.step."""
+    lib = load()
+    arr = (C.c_void_p * len(solids))(*[s.h.value if isinstance(s.h, C.c_void_p) else s.h for s in solids])
+    for _ in range(nsteps):
+        for s in solids:
+            sc = s.scene
+            if sc.knc_schedule is not None and s._knc_nodes.size:
+                s.set_knc_targets(sc.targets_at(s.step_index))
+            s.step_index += 1
+        check(lib.fem_multi_step(arr, len(solids), float(dt), 1))
 
 
 class Batch:

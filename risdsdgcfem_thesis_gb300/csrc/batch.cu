@@ -1305,7 +1305,7 @@ int fem_batch_synchronize(fem_batch b)
         return batch_fail(FEM_E_TIMEOUT, "a bounded wait for a tile copy gave up (code %u)", err);
     }
     for (uint32_t m = 0; m < b->M; m++)
-        if (b->st_host[m].status == FEM_E_NAN) return batch_fail(FEM_E_NAN, "NaN in the CG residual of mesh %u", m);
+        if (b->st_host[m].status == FEM_E_NAN) return batch_fail(FEM_E_NAN, "NaN or Inf in the CG residual of mesh %u", m);
     return FEM_OK;
 }
 
@@ -1344,6 +1344,10 @@ int fem_batch_get_stats(fem_batch b, uint32_t mesh, fem_step_stats* out)
     out->pad = 0;
     out->nr_rel_residual = 0.0;
     out->nr_abs_residual = 0.0;
+    out->resolved_det_F = h.res_det_F;
+    out->resolved_isotropic = h.res_isotropic;
+    out->resolved_tie = h.res_tie;
+    out->resolved_check = h.res_check;
     return FEM_OK;
 }
 

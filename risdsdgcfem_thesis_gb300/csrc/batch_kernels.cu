@@ -631,7 +631,7 @@ __global__ void k_node_residual(BatchView<S> b, const double* __restrict__ part6
                 s.abs_eps_sq = c.abs_eps_sq;
                 s.max_iter = c.max_iter;
                 s.k = 0;
-                s.status = (total != total) ? 3u : 0u;
+                s.status = (!isfinite(total)) ? 3u : 0u;
                 s.alpha = 0.0;
                 s.beta = 0.0;
                 s.beta_f = 0.f;
@@ -756,7 +756,7 @@ __global__ void k_node_update(BatchView<S> b, double* __restrict__ y, S* __restr
                 s.beta = total / s.delta_old;
                 s.k += 1;
                 s.total_iters += 1;
-                if (total != total) s.status = 3u;
+                if (!isfinite(total)) s.status = 3u;
                 s.done = cg_cont(s) ? 0u : 1u;
                 if (s.done) {
                     finish_stats(s);
@@ -810,6 +810,7 @@ __global__ void k_reset_counts(BatchView<S> b, LoopSync ls, cudaGraphConditional
         if (a == 1) {
             s.inverted = 0;
             s.fp64_resolved = 0;
+            s.res_det_F = s.res_isotropic = s.res_tie = s.res_check = 0;
             start = 1;
         } else if (a == 2) {
             cont |= s.done ? 0 : 1;

@@ -20,6 +20,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "lcm.cuh"
+
 namespace femgb {
 
 // MINRES recurrence scalars (ILSS_MINRES::Solve, ILSS_MINRES.h:51-168).
@@ -51,6 +53,11 @@ struct StepScalars {
     unsigned long long total_iters;
     double host_sum;        // FIE: the last FIN_SUM total (|b_k|^2 or |y_k|^2), read by the host
     MinresScalars mr;       // MINRES solver state (FP64 solid)
+    // mixed: rotations of this step by cause of their double-precision
+    // re-solve: det F <= degenerate_det_F (FP64 MSVD), a nearly isotropic
+    // F^T F (FP64 MSVD in place of double-float), and with FP32 rotations an
+    // MSVD branch near a tie or a failed sensitivity check
+    uint32_t res_det_F, res_isotropic, res_tie, res_check;
 };
 
 template <typename S>
@@ -113,9 +120,9 @@ void launch_fie_update_fp64(uint32_t N, double inv_dt, double* x, double* v, con
                             double* partials, cudaStream_t s);
 // C_LCM material (FP64 solid): element force and/or energy from the stored F,
 // and the truncated differential of d.
-void launch_elem_lcm_force_fp64(const MeshView<double>& m, const double* F, double mu, double lam, int write_out,
+void launch_elem_lcm_force_fp64(const MeshView<double>& m, const double* F, const PkMaterial& mat, int write_out,
                                 double* energy_partials, cudaStream_t s);
-void launch_elem_lcm_spmv_fp64(const MeshView<double>& m, const double* d, double mu, double lam,
+void launch_elem_lcm_spmv_fp64(const MeshView<double>& m, const double* d, const double* F, const PkMaterial& mat,
                                const StepScalars* st, int check_done, cudaStream_t s);
 // MINRES (FP64 solid). v1 = S (b - A y) and partial |v1|^2 from a fresh eout of y.
 void launch_mr_init_fp64(const MeshView<double>& m, const StepConsts& c, const double* b, const double* y,
@@ -137,6 +144,8 @@ void launch_potential_fp64(const MeshView<double>& m, const StepConsts& c, const
 void launch_apply_A_fp64(const MeshView<double>& m, double factor_M, double factor_K, double mass,
                          const double* d, double* q, cudaStream_t s);
 void launch_gather_sum_fp64(const MeshView<double>& m, double sign, double* f, cudaStream_t s);
+void launch_rebake_material_fp64(uint32_t T, const double* vol, double k0, double k1, double k2, double* mat,
+                                 cudaStream_t s);
 
 // finalizers: one block, fixed-order sums of `count` block partials
 enum FinalizeKind {

@@ -178,7 +178,7 @@ __device__ __forceinline__ void load_R_Dinv(const MeshView<double>& m, uint32_t 
     }
 }
 
-__global__ void k_elem_lcm_force_fp64(MeshView<double> m, const double* __restrict__ F, double mu, double lam,
+__global__ void k_elem_lcm_force_fp64(MeshView<double> m, const double* __restrict__ F, PkMaterial mat,
                                       int write_out, double* energy_partials)
 {
     double energy = 0.0;
@@ -189,12 +189,12 @@ __global__ void k_elem_lcm_force_fp64(MeshView<double> m, const double* __restri
         for (int c = 0; c < 9; c++) Fl[c] = F[9 * (size_t)e + c];
         if (write_out) {
             double out[12];
-            lcm_force(R, Fl, Di, m.vol[e], mu, lam, out);
+            pk_force(mat, R, Fl, Di, m.vol[e], out);
             double* o = m.eout + 12 * (size_t)e;
 #pragma unroll
             for (int c = 0; c < 12; c++) o[c] = out[c];
         }
-        if (energy_partials) energy += lcm_energy(R, Fl, m.vol[e], mu, lam);
+        if (energy_partials) energy += pk_energy(mat, R, Fl, m.vol[e]);
     }
     if (energy_partials) {
         double s = block_sum(energy);
@@ -202,8 +202,8 @@ __global__ void k_elem_lcm_force_fp64(MeshView<double> m, const double* __restri
     }
 }
 
-__global__ void k_elem_lcm_spmv_fp64(MeshView<double> m, const double* __restrict__ d, double mu, double lam,
-                                     const StepScalars* st, int check_done)
+__global__ void k_elem_lcm_spmv_fp64(MeshView<double> m, const double* __restrict__ d, const double* __restrict__ F,
+                                     PkMaterial mat, const StepScalars* st, int check_done)
 {
     if (check_done && st->done) return;
     for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < m.T; e += gridDim.x * blockDim.x) {
@@ -217,8 +217,13 @@ __global__ void k_elem_lcm_spmv_fp64(MeshView<double> m, const double* __restric
             dl[3 * i + 1] = d[3 * (size_t)ids[i] + 1];
             dl[3 * i + 2] = d[3 * (size_t)ids[i] + 2];
         }
+        double Fl[9];
+        if (mat.kind != 1) {  // C_LCMH and C_CCM read F (and C_CCM det F)
+#pragma unroll
+            for (int c = 0; c < 9; c++) Fl[c] = F[9 * (size_t)e + c];
+        }
         double out[12];
-        lcm_dforce(R, Di, m.vol[e], mu, lam, dl, out);
+        pk_dforce(mat, R, Fl, mat.kind == 3 ? m.detF[e] : 0.0, Di, m.vol[e], dl, out);
         double* o = m.eout + 12 * (size_t)e;
 #pragma unroll
         for (int c = 0; c < 12; c++) o[c] = out[c];
@@ -646,6 +651,28 @@ __global__ void k_apply_A_fp64(MeshView<double> m, double factor_M, double facto
 }
 
 // f += sign * sum(eout) per node
+// Material triple of every element from one E, nu (k_c = a (1 - nu), a nu,
+// a (0.5 - nu), formed on the host): mat[c][e] = V_e k_c, the product
+// EditableTetrahedronElementSet3::SetParams re-bakes for every element
+// (TetrahedronElementSet3.cpp:2168-2200).
+__global__ void k_rebake_material_fp64(uint32_t T, const double* __restrict__ vol, double k0, double k1, double k2,
+                                       double* mat)
+{
+    for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < T; e += gridDim.x * blockDim.x) {
+        const double V = vol[e];
+        mat[e] = V * k0;
+        mat[(size_t)T + e] = V * k1;
+        mat[2 * (size_t)T + e] = V * k2;
+    }
+}
+
+void launch_rebake_material_fp64(uint32_t T, const double* vol, double k0, double k1, double k2, double* mat,
+                                 cudaStream_t s)
+{
+    k_rebake_material_fp64<<<grid_for(T), kBlock, 0, s>>>(T, vol, k0, k1, k2, mat);
+    launch_counter()++;
+}
+
 __global__ void k_gather_sum_fp64(MeshView<double> m, double sign, double* f)
 {
     for (uint32_t n = blockIdx.x * blockDim.x + threadIdx.x; n < m.N; n += gridDim.x * blockDim.x) {
@@ -684,7 +711,7 @@ __global__ void k_finalize(int kind, const double* __restrict__ partials, uint32
         st->alpha = 0.0;
         st->beta = 0.0;
         st->done = cg_continue(st) ? 0u : 1u;
-        if (total != total) st->status = 3;  // FEM_E_NAN
+        if (!isfinite(total)) st->status = 3;  // FEM_E_NAN
         break;
     case FIN_ALPHA:
         if (st->done) break;
@@ -703,7 +730,7 @@ __global__ void k_finalize(int kind, const double* __restrict__ partials, uint32
         st->k += 1;
         st->total_iters += 1;
         st->done = cg_continue(st) ? 0u : 1u;
-        if (total != total) st->status = 3;
+        if (!isfinite(total)) st->status = 3;
         break;
     case FIN_ENERGY_E:
         st->elastic_energy = total;
@@ -731,7 +758,7 @@ __global__ void k_finalize(int kind, const double* __restrict__ partials, uint32
         st->status = 0;
         st->done = (mr.norm_r_sq > st->abs_eps_sq && mr.norm_r_sq > st->delta_target && st->k < st->max_iter) ? 0u : 1u;
         st->done_prev = st->done;
-        if (total != total) st->status = 3;
+        if (!isfinite(total)) st->status = 3;
         break;
     }
     case FIN_MR_ALPHA:
@@ -765,7 +792,7 @@ __global__ void k_finalize(int kind, const double* __restrict__ partials, uint32
         st->k += 1;
         st->total_iters += 1;
         st->done = (mr.norm_r_sq > st->abs_eps_sq && mr.norm_r_sq > st->delta_target && st->k < st->max_iter) ? 0u : 1u;
-        if (total != total || mr.norm_r_sq != mr.norm_r_sq) st->status = 3;
+        if (!isfinite(total) || !isfinite(mr.norm_r_sq)) st->status = 3;
         break;
     }
     case FIN_MR_STATS:
@@ -881,15 +908,15 @@ void launch_mr_update_fp64(uint32_t N, double* v1, const double* v, const double
 {
     FEMGB_LAUNCH(k_mr_update_fp64, grid_for(3 * N), N, v1, v, p, p0, y, st);
 }
-void launch_elem_lcm_force_fp64(const MeshView<double>& m, const double* F, double mu, double lam, int write_out,
+void launch_elem_lcm_force_fp64(const MeshView<double>& m, const double* F, const PkMaterial& mat, int write_out,
                                 double* energy_partials, cudaStream_t s)
 {
-    FEMGB_LAUNCH(k_elem_lcm_force_fp64, grid_for(m.T), m, F, mu, lam, write_out, energy_partials);
+    FEMGB_LAUNCH(k_elem_lcm_force_fp64, grid_for(m.T), m, F, mat, write_out, energy_partials);
 }
-void launch_elem_lcm_spmv_fp64(const MeshView<double>& m, const double* d, double mu, double lam,
+void launch_elem_lcm_spmv_fp64(const MeshView<double>& m, const double* d, const double* F, const PkMaterial& mat,
                                const StepScalars* st, int check_done, cudaStream_t s)
 {
-    FEMGB_LAUNCH(k_elem_lcm_spmv_fp64, grid_for(m.T), m, d, mu, lam, st, check_done);
+    FEMGB_LAUNCH(k_elem_lcm_spmv_fp64, grid_for(m.T), m, d, F, mat, st, check_done);
 }
 void launch_potential_fp64(const MeshView<double>& m, const StepConsts& c, const double* x, double* partials,
                            cudaStream_t s)

@@ -117,14 +117,15 @@ void launch_begin_eval_dapd_fp64(const MeshView<double>& m, const double* xprev,
 // check below fails, where F is re-solved in double-float arithmetic. Per-mesh counts of
 // inverted elements and FP64 re-solves are added with integer atomics (one
 // per tile), so they do not depend on scheduling.
-// FP32 rotation of F for the mixed path. The result is not trusted -- false
-// is returned for an FP64 re-solve -- when one of the MSVD's branch
+// FP32 rotation of F for the mixed path. The result is not trusted -- the
+// cause is returned for an FP64 re-solve -- when one of the MSVD's branch
 // decisions was a near tie (FP32 rounding may decide it differently from
 // FP64, and the rotation jumps with the decision), or, with tol > 0, when
 // the rotation computed again for F plus a fixed 2^-14 relative change
 // differs by more than tol (max entry).
+enum { kRotKept = 0, kRotTie = 1, kRotCheck = 2 };
 template <typename S>
-__device__ __forceinline__ bool rotation_fp32(const double* F, float tol, S* Rs)
+__device__ __forceinline__ int rotation_fp32(const double* F, float tol, S* Rs)
 {
     float Ff[9], Rf[9];
     float s = 0.f;
@@ -135,7 +136,7 @@ __device__ __forceinline__ bool rotation_fp32(const double* F, float tol, S* Rs)
     }
     bool tie = false;
     msvd_rotation(Ff, Rf, &tie);
-    if (tie) return false;  // a branch decision FP32 may take differently from FP64
+    if (tie) return kRotTie;  // a branch decision FP32 may take differently from FP64
     if (tol > 0.f) {
         const float d = s * 6.103515625e-05f;  // 2^-14 of the largest entry
         const float P[9] = {1.f, -1.f, 0.f, 0.f, 1.f, -1.f, 1.f, 0.f, 1.f};
@@ -146,11 +147,11 @@ __device__ __forceinline__ bool rotation_fp32(const double* F, float tol, S* Rs)
         float diff = 0.f;
 #pragma unroll
         for (int c = 0; c < 9; c++) diff = fmaxf(diff, fabsf(Rf[c] - Rp[c]));
-        if (!(diff <= tol)) return false;  // also when NaN
+        if (!(diff <= tol)) return kRotCheck;  // also when NaN
     }
 #pragma unroll
     for (int c = 0; c < 9; c++) Rs[c] = (S)Rf[c];
-    return true;
+    return kRotKept;
 }
 
 // Three resident blocks per SM (80 registers): the double-float MSVD's long
@@ -158,13 +159,13 @@ __device__ __forceinline__ bool rotation_fp32(const double* F, float tol, S* Rs)
 template <typename S>
 __global__ void __launch_bounds__(256, 3) k_begin_eval_batch(BatchView<S> b, const double* __restrict__ x)
 {
-    __shared__ unsigned s_inv, s_res;
+    __shared__ unsigned s_inv, s_res, s_cause[4];  // re-solves: det F, isotropic, tie, check
     const uint32_t n = b.list_count[0];
     for (uint32_t i = blockIdx.x; i < n; i += gridDim.x) {
         const uint32_t t = b.start_tiles[i];
         const TileMeta tm = b.tiles[t];
         if (b.active[tm.mesh] != 1) continue;
-        if (threadIdx.x == 0) { s_inv = 0; s_res = 0; }
+        if (threadIdx.x == 0) { s_inv = 0; s_res = 0; s_cause[0] = s_cause[1] = s_cause[2] = s_cause[3] = 0; }
         __syncthreads();
         if (threadIdx.x < tm.ne) {
             const size_t e = tm.e0 + threadIdx.x;
@@ -186,23 +187,31 @@ __global__ void __launch_bounds__(256, 3) k_begin_eval_batch(BatchView<S> b, con
                 msvd_rotation(F, R);
 #pragma unroll
                 for (int c = 0; c < 9; c++) Rs[c] = (S)R[c];
-            } else if (b.mc[tm.mesh].rot_fp32 && detF > b.mc[tm.mesh].degenerate_det_F &&
-                       rotation_fp32(F, b.mc[tm.mesh].rot_check, Rs)) {
-                // FP32 rotation kept
             } else {
-                // the double-float rotation, or the FP64 one for a degenerate
-                // element (det F <= the threshold) or a nearly isotropic F
-                // (counted as re-solves of the FP32 rotation)
-                float Rf[9];
-                if (!(detF > b.mc[tm.mesh].degenerate_det_F) || !rotation_df(F, Rf)) {
-                    double R[9];
-                    msvd_rotation(F, R);
+                const bool degenerate = !(detF > b.mc[tm.mesh].degenerate_det_F);
+                const int why = (b.mc[tm.mesh].rot_fp32 && !degenerate)
+                                    ? rotation_fp32(F, b.mc[tm.mesh].rot_check, Rs)
+                                    : kRotTie + kRotCheck + 1;  // no FP32 attempt
+                if (why != kRotKept) {
+                    // the double-float rotation, or the FP64 one for a
+                    // degenerate element (det F <= the threshold) or a nearly
+                    // isotropic F (counted as re-solves, by cause)
+                    float Rf[9];
+                    bool iso = false;
+                    if (degenerate || (iso = !rotation_df(F, Rf))) {
+                        double R[9];
+                        msvd_rotation(F, R);
 #pragma unroll
-                    for (int c = 0; c < 9; c++) Rf[c] = (float)R[c];
+                        for (int c = 0; c < 9; c++) Rf[c] = (float)R[c];
+                    }
+#pragma unroll
+                    for (int c = 0; c < 9; c++) Rs[c] = (S)Rf[c];
+                    atomicAdd(&s_res, 1u);
+                    if (degenerate) atomicAdd(&s_cause[0], 1u);
+                    else if (iso) atomicAdd(&s_cause[1], 1u);
+                    if (why == kRotTie) atomicAdd(&s_cause[2], 1u);
+                    if (why == kRotCheck) atomicAdd(&s_cause[3], 1u);
                 }
-#pragma unroll
-                for (int c = 0; c < 9; c++) Rs[c] = (S)Rf[c];
-                atomicAdd(&s_res, 1u);
             }
 #pragma unroll
             for (int c = 0; c < 9; c++) b.R[c * T + e] = Rs[c];
@@ -222,6 +231,10 @@ __global__ void __launch_bounds__(256, 3) k_begin_eval_batch(BatchView<S> b, con
         if (threadIdx.x == 0) {
             if (s_inv) atomicAdd(&b.st[tm.mesh].inverted, s_inv);
             if (s_res) atomicAdd(&b.st[tm.mesh].fp64_resolved, s_res);
+            if (s_cause[0]) atomicAdd(&b.st[tm.mesh].res_det_F, s_cause[0]);
+            if (s_cause[1]) atomicAdd(&b.st[tm.mesh].res_isotropic, s_cause[1]);
+            if (s_cause[2]) atomicAdd(&b.st[tm.mesh].res_tie, s_cause[2]);
+            if (s_cause[3]) atomicAdd(&b.st[tm.mesh].res_check, s_cause[3]);
         }
         __syncthreads();
     }

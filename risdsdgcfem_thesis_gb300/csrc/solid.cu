@@ -17,6 +17,7 @@
 #include "dapd.cuh"
 #include "fem_device.cuh"
 
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -132,6 +133,12 @@ struct fem_solid_s {
     DevBuf<StepScalars> st;
     StepScalars* st_host = nullptr;  // pinned
     bool evaluated = false;
+    // multi-solid Newton lock-step (fem_solid_nr_*): the iterates x_k, v_k
+    // (allocated by the first fem_solid_nr_init), the iterations since the
+    // last NR_PreStep and the LS iterations of its NR_MidStep
+    DevBuf<double> lk_x, lk_v;
+    uint32_t lock_nr_k = 0, lock_ls_iters = 0;
+    bool lock_stats = false;  // the last completed step was a lock-step (NR_End)
     // fem_solid_apply_A_noalloc: device address of the static scratch array,
     // looked up at creation (null for solids above FEM_NOALLOC_MAX_TETS)
     double* noalloc_scratch = nullptr;
@@ -158,7 +165,8 @@ struct fem_solid_s {
     void release()
     {
         DevBuf<double>* dbl[] = {&Dinv, &mat, &vol, &R, &detF, &eout, &rest, &x, &v, &y, &b, &r, &d, &q, &tmp,
-                                 &xn, &vn, &prev_x, &mr_p, &mr_p0, &Fe, &knc_targets, &partials, &partials2};
+                                 &xn, &vn, &prev_x, &mr_p, &mr_p0, &Fe, &knc_targets, &partials, &partials2,
+                                 &lk_x, &lk_v};
         for (auto* p : dbl) p->release();
         doc.release();
         tets.release();
@@ -183,7 +191,91 @@ int check_handle(fem_solid s)
 }
 
 bool uses_dapd(const fem_solid s) { return s->params.rotation == FEM_ROTATION_DAPD; }
-bool uses_lcm(const fem_solid s) { return s->params.material == FEM_MATERIAL_C_LCM; }
+// the first Piola-Kirchhoff materials (C_LCM, C_LCMH, C_CCM) keep F per element
+bool uses_lcm(const fem_solid s) { return s->params.material != FEM_MATERIAL_C_WRP; }
+
+PkMaterial pk_material(const fem_solid s)
+{
+    PkMaterial m;
+    m.kind = (int)s->params.material;
+    m.mu = s->lame_mu;
+    m.lambda = s->lame_lambda;
+    m.k = (double)(float)s->params.ecie_k_factor;  // float32 in the reference's Params
+    return m;
+}
+
+// Parameters every entry point that takes a fem_params checks (enums in
+// range, finite DAPD settings, a positive time step, the FP64 precision).
+int check_params(const fem_params* params)
+{
+    if (!(params->fixed_dt > 0)) return fail(FEM_E_ARG, "fixed_dt must be > 0");
+    if (params->precision != FEM_PRECISION_FP64)
+        return fail(FEM_E_ARG, "precision %u: this entry point builds the FP64 path; use the batch API for mixed",
+                    params->precision);
+    if (params->integrator > FEM_INTEGRATOR_FIE_DX_QUASISTATIC)
+        return fail(FEM_E_ARG, "integrator %u is not an enum fem_integrator value", params->integrator);
+    if (params->integrator != FEM_INTEGRATOR_QIE_V && !(params->nr_abs_epsilon >= 0))
+        return fail(FEM_E_ARG, "nr_abs_epsilon must be >= 0");
+    if (params->ls_solver > FEM_LS_MINRES)
+        return fail(FEM_E_ARG, "ls_solver %u is not an enum fem_ls_solver value", params->ls_solver);
+    if (params->material > FEM_MATERIAL_C_CCM)
+        return fail(FEM_E_ARG, "material %u is not an enum fem_material value", params->material);
+    if (params->material == FEM_MATERIAL_C_LCMH && !std::isfinite(params->ecie_k_factor))
+        return fail(FEM_E_ARG, "ecie_k_factor must be finite");
+    if (params->rotation > FEM_ROTATION_DAPD)
+        return fail(FEM_E_ARG, "rotation %u is not an enum fem_rotation value", params->rotation);
+    if (params->rotation == FEM_ROTATION_DAPD &&
+        !(std::isfinite(params->dapd_threshold_det_F) && std::isfinite(params->dapd_l_factor) &&
+          std::isfinite(params->dapd_nl_factor) && std::isfinite(params->dapd_nl_exponent)))
+        return fail(FEM_E_ARG, "DAPD threshold and factors must be finite");
+    return FEM_OK;
+}
+
+// The step's constants from the solid's parameters and total volume:
+// RebuildMass (m = rho sum V / N stored as its float-rounded reciprocal,
+// LeafDSH_Solid3D_FEM.cpp:1591-1611), RebuildRayleighCoeffsFromFreqs with the
+// default frequencies 0.1f and 1e4 (LeafDSH_Solid3D_FEM.h:347-354), the
+// factors of Step_QuasiImplicitEuler_v (:1300-1301) and the CG settings.
+void set_consts(fem_solid s)
+{
+    const fem_params* params = &s->params;
+    const double total_mass = params->density * s->total_volume;
+    const double mass_per_node = total_mass / s->N;
+    const double inv_mass = (double)1.0f / mass_per_node;
+    s->node_mass = 1.0 / inv_mass;
+    {
+        const double f1 = (double)0.1f, f2 = (double)10000.0f;
+        const double o00 = 1.0 / f1, o01 = f1, o10 = 1.0 / f2, o11 = f2;
+        const double inv_det = 1.0 / (o00 * o11 - o10 * o01);
+        const double i00 = inv_det * o11, i01 = -inv_det * o01, i10 = -inv_det * o10, i11 = inv_det * o00;
+        const double z = 2 * params->damping_ratio;
+        double a0 = 0, a1 = 0;
+        a0 += i00 * z; a0 += i01 * z;
+        a1 += i10 * z; a1 += i11 * z;
+        s->rayleigh[0] = a0;
+        s->rayleigh[1] = a1;
+    }
+    StepConsts& c = s->consts;
+    c.dt = params->fixed_dt;
+    c.inv_dt = 1.0 / params->fixed_dt;
+    c.mass = s->node_mass;
+    c.factor_M = 1.0 + c.dt * s->rayleigh[0];
+    c.factor_K = c.dt * c.dt + c.dt * s->rayleigh[1];
+    for (int i = 0; i < 3; i++) c.gravity[i] = params->gravity[i];
+    c.density = params->density;
+    c.rel_eps_sq = params->ls_rel_epsilon * params->ls_rel_epsilon;
+    c.abs_eps_sq = params->ls_abs_epsilon * params->ls_abs_epsilon;
+    c.max_iter = params->ls_max_iter;
+    // LameParameters_From_YoungAndPoisson on the set's E, nu
+    // (TetrahedronElementSet3.cpp:181-186, 2116-2117, 2172-2173)
+    const double E = params->young_modulus, nu = params->poisson_ratio;
+    s->lame_mu = 0.5 * E / (1 + nu);
+    s->lame_lambda = E * nu / ((1.0 + nu) * (1.0 - 2.0 * nu));
+    s->dapd.thr = params->dapd_threshold_det_F;
+    s->dapd.fL = (double)(float)params->dapd_l_factor;
+    s->dapd.fNL = (double)(float)params->dapd_nl_factor;
+    s->dapd.eNL = (double)(float)params->dapd_nl_exponent;
+}
 
 // TetrahedronElementSet3::BeginEvaluation(x0 = xprev, x): F, det F and the
 // rotations at x; xprev feeds the DAPD collapse detection only. C_LCM keeps F.
@@ -202,7 +294,7 @@ void begin_eval(fem_solid s, const double* xprev, const double* x)
 void elem_force(fem_solid s, const MeshView<double>& m, const double* x, int write_out, double* energy_partials)
 {
     if (uses_lcm(s))
-        launch_elem_lcm_force_fp64(m, s->Fe.p, s->lame_mu, s->lame_lambda, write_out, energy_partials, s->stream);
+        launch_elem_lcm_force_fp64(m, s->Fe.p, pk_material(s), write_out, energy_partials, s->stream);
     else
         launch_elem_force_fp64(m, x, write_out, energy_partials, s->stream);
 }
@@ -211,7 +303,7 @@ void elem_force(fem_solid s, const MeshView<double>& m, const double* x, int wri
 void elem_spmv(fem_solid s, const MeshView<double>& m, const double* d, int check_done)
 {
     if (uses_lcm(s))
-        launch_elem_lcm_spmv_fp64(m, d, s->lame_mu, s->lame_lambda, s->st.p, check_done, s->stream);
+        launch_elem_lcm_spmv_fp64(m, d, s->Fe.p, pk_material(s), s->st.p, check_done, s->stream);
     else
         launch_elem_spmv_fp64(m, d, s->st.p, check_done, s->stream);
 }
@@ -363,7 +455,7 @@ int step_fie(fem_solid s, int chunk)
         if (int e = host_sum(s, gV, &sum)) return e;
         delta_new = std::sqrt(sum);
         if (delta_0 < 0) delta_0 = delta_new;
-        if (delta_new != delta_new) return fail(FEM_E_NAN, "NaN in the Newton right-hand side");
+        if (!std::isfinite(delta_new)) return fail(FEM_E_NAN, "NaN or Inf in the Newton right-hand side");
         converged = delta_new < s->params.nr_abs_epsilon;
         if (!converged) {
             if (int e = ls_solve(s, c, chunk)) return e;
@@ -392,6 +484,7 @@ int step_fie(fem_solid s, int chunk)
 // read of the CG loop flag).
 int step_once(fem_solid s, int chunk)
 {
+    s->lock_stats = false;
     if (s->params.integrator != FEM_INTEGRATOR_QIE_V) return step_fie(s, chunk);
     cudaStream_t st = s->stream;
     MeshView<double> m = s->view();
@@ -421,6 +514,14 @@ void fill_stats(fem_solid s, const StepScalars& h, fem_step_stats* out)
     out->pad = 0;
     out->nr_rel_residual = 0.0;
     out->nr_abs_residual = 0.0;
+    out->resolved_det_F = out->resolved_isotropic = out->resolved_tie = out->resolved_check = 0;  // FP64: none
+    if (s->lock_stats) {
+        // the Leaf's m_Stats after NR_End: LS iterations since the last
+        // NR_PreStep, m_NR_nr_k (reset by every NR_PreStep)
+        out->cg_iterations = s->lock_ls_iters;
+        out->nr_iterations = s->lock_nr_k;
+        return;
+    }
     if (s->params.integrator != FEM_INTEGRATOR_QIE_V) {
         out->cg_iterations = s->fie_cg_iters;
         if (!s->fie_solved) out->rel_residual = out->abs_residual = 0.0;
@@ -478,6 +579,7 @@ int fem_params_default(fem_params* p)
     // ms::fem::Params (Params.h:85-95)
     p->ls_solver = FEM_LS_CG;  // LeafDSH_Solid3D_FEM::Params m_SolverLS_Type
     p->material = FEM_MATERIAL_C_WRP;  // ms::fem::Params m_MM
+    p->ecie_k_factor = 1.0;            // ms::fem::Params m_ECIE_k_factor
     p->rotation = FEM_ROTATION_MSVD;
     p->dapd_threshold_det_F = (double)0.1f;
     p->dapd_l_factor = 1.0;
@@ -498,24 +600,7 @@ int fem_solid_create(const double* rest_xyz, uint32_t N, const uint32_t* tets, u
     if (!rest_xyz || !tets || !params) return fail(FEM_E_ARG, "null rest/tets/params");
     if (N == 0 || T == 0) return fail(FEM_E_ARG, "empty mesh (N=%u, T=%u)", N, T);
     if (N > (1u << 30) || T > (1u << 29)) return fail(FEM_E_ARG, "mesh too large (N=%u, T=%u)", N, T);
-    if (!(params->fixed_dt > 0)) return fail(FEM_E_ARG, "fixed_dt must be > 0");
-    if (params->precision != FEM_PRECISION_FP64)
-        return fail(FEM_E_ARG, "precision %u: this entry point builds the FP64 path; use the batch API for mixed",
-                    params->precision);
-    if (params->integrator > FEM_INTEGRATOR_FIE_DX_QUASISTATIC)
-        return fail(FEM_E_ARG, "integrator %u is not an enum fem_integrator value", params->integrator);
-    if (params->integrator != FEM_INTEGRATOR_QIE_V && !(params->nr_abs_epsilon >= 0))
-        return fail(FEM_E_ARG, "nr_abs_epsilon must be >= 0");
-    if (params->ls_solver > FEM_LS_MINRES)
-        return fail(FEM_E_ARG, "ls_solver %u is not an enum fem_ls_solver value", params->ls_solver);
-    if (params->material > FEM_MATERIAL_C_LCM)
-        return fail(FEM_E_ARG, "material %u is not an enum fem_material value", params->material);
-    if (params->rotation > FEM_ROTATION_DAPD)
-        return fail(FEM_E_ARG, "rotation %u is not an enum fem_rotation value", params->rotation);
-    if (params->rotation == FEM_ROTATION_DAPD &&
-        !(std::isfinite(params->dapd_threshold_det_F) && std::isfinite(params->dapd_l_factor) &&
-          std::isfinite(params->dapd_nl_factor) && std::isfinite(params->dapd_nl_exponent)))
-        return fail(FEM_E_ARG, "DAPD threshold and factors must be finite");
+    if (int e = check_params(params)) return e;
     for (size_t i = 0; i < 4 * (size_t)T; i++)
         if (tets[i] >= N) return fail(FEM_E_INDEX, "tet %zu names node %u >= N=%u", i / 4, tets[i], N);
     int ndev = 0;
@@ -556,33 +641,7 @@ int fem_solid_create(const double* rest_xyz, uint32_t N, const uint32_t* tets, u
     s->T = T;
     s->params = *params;
     s->total_volume = acc_total_volume;
-    const double total_mass = params->density * acc_total_volume;
-    const double mass_per_node = total_mass / N;
-    const double inv_mass = (double)1.0f / mass_per_node;
-    s->node_mass = 1.0 / inv_mass;
-    {
-        const double f1 = (double)0.1f, f2 = (double)10000.0f;
-        const double o00 = 1.0 / f1, o01 = f1, o10 = 1.0 / f2, o11 = f2;
-        const double inv_det = 1.0 / (o00 * o11 - o10 * o01);
-        const double i00 = inv_det * o11, i01 = -inv_det * o01, i10 = -inv_det * o10, i11 = inv_det * o00;
-        const double z = 2 * params->damping_ratio;
-        double a0 = 0, a1 = 0;
-        a0 += i00 * z; a0 += i01 * z;
-        a1 += i10 * z; a1 += i11 * z;
-        s->rayleigh[0] = a0;
-        s->rayleigh[1] = a1;
-    }
-    StepConsts& c = s->consts;
-    c.dt = params->fixed_dt;
-    c.inv_dt = 1.0 / params->fixed_dt;
-    c.mass = s->node_mass;
-    c.factor_M = 1.0 + c.dt * s->rayleigh[0];
-    c.factor_K = c.dt * c.dt + c.dt * s->rayleigh[1];
-    for (int i = 0; i < 3; i++) c.gravity[i] = params->gravity[i];
-    c.density = params->density;
-    c.rel_eps_sq = params->ls_rel_epsilon * params->ls_rel_epsilon;
-    c.abs_eps_sq = params->ls_abs_epsilon * params->ls_abs_epsilon;
-    c.max_iter = params->ls_max_iter;
+    set_consts(s);
 
     // node -> (4e + slot) entries, element order
     std::vector<uint32_t> ptr(N + 1, 0), idx(4 * (size_t)T);
@@ -628,14 +687,9 @@ int fem_solid_create(const double* rest_xyz, uint32_t N, const uint32_t* tets, u
         CKC(s->xn.alloc(n3));
         CKC(s->vn.alloc(n3));
     }
-    if (params->material == FEM_MATERIAL_C_LCM) {
+    if (params->material != FEM_MATERIAL_C_WRP) {
         CKC(s->Fe.alloc(9 * (size_t)T));
         CKC(cudaMemsetAsync(s->Fe.p, 0, sizeof(double) * 9 * (size_t)T, s->stream));
-        // LameParameters_From_YoungAndPoisson on the set's E, nu
-        // (TetrahedronElementSet3.cpp:181-186, 2116-2117)
-        const double E = params->young_modulus, nu = params->poisson_ratio;
-        s->lame_mu = 0.5 * E / (1 + nu);
-        s->lame_lambda = E * nu / ((1.0 + nu) * (1.0 - 2.0 * nu));
     }
     if (params->ls_solver == FEM_LS_MINRES) {
         CKC(s->mr_p.alloc(n3));
@@ -644,10 +698,6 @@ int fem_solid_create(const double* rest_xyz, uint32_t N, const uint32_t* tets, u
     if (params->rotation == FEM_ROTATION_DAPD) {
         CKC(s->prev_x.alloc(n3));
         CKC(s->doc.alloc(T));
-        s->dapd.thr = params->dapd_threshold_det_F;
-        s->dapd.fL = (double)(float)params->dapd_l_factor;
-        s->dapd.fNL = (double)(float)params->dapd_nl_factor;
-        s->dapd.eNL = (double)(float)params->dapd_nl_exponent;
     }
     CKC(s->partials.alloc(4096));
     CKC(s->partials2.alloc(4096));
@@ -758,6 +808,230 @@ int fem_solid_set_state(fem_solid s, const double* x, const double* v)
     return FEM_OK;
 }
 
+int fem_solid_set_params(fem_solid s, const fem_params* params)
+{
+    if (int e = check_handle(s)) return e;
+    if (!params) return fail(FEM_E_ARG, "null params");
+    if (int e = check_params(params)) return e;
+    CK(cudaStreamSynchronize(s->stream));
+    const fem_params old = s->params;
+    const size_t n3 = 3 * (size_t)s->N;
+    // buffers the new methods need (kept when a method is switched off)
+    if (params->integrator != FEM_INTEGRATOR_QIE_V && !s->xn.p) {
+        CK(s->xn.alloc(n3));
+        CK(s->vn.alloc(n3));
+    }
+    if (params->ls_solver == FEM_LS_MINRES && !s->mr_p.p) {
+        CK(s->mr_p.alloc(n3));
+        CK(s->mr_p0.alloc(n3));
+    }
+    if (params->material != FEM_MATERIAL_C_WRP && !s->Fe.p) {
+        CK(s->Fe.alloc(9 * (size_t)s->T));
+        CK(cudaMemsetAsync(s->Fe.p, 0, sizeof(double) * 9 * (size_t)s->T, s->stream));
+    }
+    if (params->rotation == FEM_ROTATION_DAPD && old.rotation != FEM_ROTATION_DAPD) {
+        // DAPD from here on: the previous positions start at the current
+        // ones and no element has a direction of collapse yet (as a solid
+        // created with DAPD, TetrahedronElementSet3.cpp:190-209)
+        if (!s->prev_x.p) CK(s->prev_x.alloc(n3));
+        if (!s->doc.p) CK(s->doc.alloc(s->T));
+        CK(cudaMemcpyAsync(s->prev_x.p, s->x.p, sizeof(double) * n3, cudaMemcpyDeviceToDevice, s->stream));
+        const std::vector<uchar2> none(s->T, make_uchar2(3, 0));
+        CK(cudaMemcpyAsync(s->doc.p, none.data(), sizeof(uchar2) * s->T, cudaMemcpyHostToDevice, s->stream));
+    }
+    s->params = *params;
+    set_consts(s);
+    // a new Young's modulus or Poisson ratio re-bakes every element from the
+    // scalar values, as EditableTetrahedronElementSet3::SetParams does
+    // (TetrahedronElementSet3.cpp:2168-2200); per-element values given at
+    // creation are then replaced
+    if (params->young_modulus != old.young_modulus || params->poisson_ratio != old.poisson_ratio) {
+        const double E = params->young_modulus, nu = params->poisson_ratio;
+        const double a = E / ((1.0 + nu) * (1.0 - 2.0 * nu));  // Compute_E (TetrahedronElement3.h:141-156)
+        launch_rebake_material_fp64(s->T, s->vol.p, a * (1.0 - nu), a * nu, a * (0.5 - nu), s->mat.p, s->stream);
+        CK(cudaGetLastError());
+    }
+    CK(cudaStreamSynchronize(s->stream));
+    return FEM_OK;
+}
+
+// ---- multi-solid Newton lock-step (LeafDSH_Solid3D_FEM.cpp:2824-3039) ----
+namespace {
+
+// The factors of a lock-step phase of step dt (0: quasi-static)
+// (NR_MidStep, :2960-2962).
+StepConsts lock_consts(const fem_solid s, double dt)
+{
+    StepConsts c = s->consts;
+    c.dt = dt;
+    c.inv_dt = dt == 0 ? 0.0 : 1.0 / dt;
+    c.factor_M = c.inv_dt * c.inv_dt + c.inv_dt * s->rayleigh[0];
+    c.factor_K = 1.0 + c.inv_dt * s->rayleigh[1];
+    return c;
+}
+
+int check_lock_dt(double dt)
+{
+    if (!(dt >= 0) || !std::isfinite(dt)) return fail(FEM_E_ARG, "dt must be finite and >= 0");
+    return FEM_OK;
+}
+
+int check_lock_ready(fem_solid s)
+{
+    if (!s->lk_x.p) return fail(FEM_E_ARG, "fem_solid_nr_init must come first");
+    return FEM_OK;
+}
+
+}  // namespace
+
+int fem_solid_nr_init(fem_solid s, double dt)
+{
+    if (int e = check_handle(s)) return e;
+    if (int e = check_lock_dt(dt)) return e;
+    const size_t n3 = 3 * (size_t)s->N;
+    if (!s->lk_x.p) {
+        CK(s->lk_x.alloc(n3));
+        CK(s->lk_v.alloc(n3));
+    }
+    s->lock_stats = false;
+    // UpdateKNC (a no-op in the default kinematic mode), BeginEvaluation(
+    // m_vecPos0, x), m_vecPos0 = x
+    if (int e = open_step(s)) return e;
+    CK(cudaGetLastError());
+    return FEM_OK;
+}
+
+int fem_solid_nr_prestep(fem_solid s, double dt)
+{
+    if (int e = check_handle(s)) return e;
+    if (int e = check_lock_dt(dt)) return e;
+    if (int e = check_lock_ready(s)) return e;
+    const size_t bytes = sizeof(double) * 3 * (size_t)s->N;
+    CK(cudaMemcpyAsync(s->lk_x.p, s->x.p, bytes, cudaMemcpyDeviceToDevice, s->stream));
+    CK(cudaMemcpyAsync(s->lk_v.p, s->v.p, bytes, cudaMemcpyDeviceToDevice, s->stream));
+    s->lock_nr_k = 0;
+    s->lock_ls_iters = 0;
+    return FEM_OK;
+}
+
+int fem_solid_nr_midstep(fem_solid s, double dt)
+{
+    if (int e = check_handle(s)) return e;
+    if (int e = check_lock_dt(dt)) return e;
+    if (int e = check_lock_ready(s)) return e;
+    const StepConsts c = lock_consts(s, dt);
+    MeshView<double> m = s->view();
+    // f_e at the positions of the cache, which are x_k's array (= x^n after
+    // NR_PreStep), with the rotations of the last BeginEvaluation
+    elem_force(s, m, s->lk_x.p, 1, nullptr);
+    launch_node_b_fie_fp64(m, c, s->lk_x.p, s->x.p, s->v.p, s->lock_nr_k == 0 ? 1 : 0, s->b.p, s->y.p, s->stream);
+    launch_knc_fie_fp64(s->knc_count, s->knc_nodes.p, s->knc_targets.p, s->lk_x.p, s->b.p, s->y.p, s->stream);
+    if (int e = ls_solve(s, c, 8)) return e;
+    s->lock_ls_iters += s->st_host->k;
+    CK(cudaGetLastError());
+    if (s->st_host->status == FEM_E_NAN) return fail(FEM_E_NAN, "NaN or Inf in the CG residual");
+    return FEM_OK;
+}
+
+int fem_solid_nr_poststep(fem_solid s, double dt)
+{
+    if (int e = check_handle(s)) return e;
+    if (int e = check_lock_dt(dt)) return e;
+    if (int e = check_lock_ready(s)) return e;
+    const StepConsts c = lock_consts(s, dt);
+    launch_fie_update_fp64(s->N, c.inv_dt, s->lk_x.p, s->lk_v.p, s->x.p, s->y.p, s->partials.p, s->stream);
+    s->lock_nr_k++;
+    // EndEvaluation, BeginEvaluation(x, x_k)
+    CK(cudaMemsetAsync(&s->st.p->inverted, 0, sizeof(uint32_t), s->stream));
+    begin_eval(s, s->x.p, s->lk_x.p);
+    CK(cudaGetLastError());
+    return FEM_OK;
+}
+
+int fem_solid_nr_end(fem_solid s, double dt)
+{
+    if (int e = check_handle(s)) return e;
+    if (int e = check_lock_dt(dt)) return e;
+    if (int e = check_lock_ready(s)) return e;
+    const size_t bytes = sizeof(double) * 3 * (size_t)s->N;
+    CK(cudaMemcpyAsync(s->x.p, s->lk_x.p, bytes, cudaMemcpyDeviceToDevice, s->stream));
+    CK(cudaMemcpyAsync(s->v.p, s->lk_v.p, bytes, cudaMemcpyDeviceToDevice, s->stream));
+    // RecomputeEnergy's potential term; NR_End evaluates no V, so the elastic
+    // energy keeps its value (LeafDSH_Solid3D_FEM.cpp:2847-2868, 1554-1584)
+    if (s->params.compute_energy) {
+        MeshView<double> m = s->view();
+        launch_potential_fp64(m, s->consts, s->x.p, s->partials2.p, s->stream);
+        launch_finalize(FIN_ENERGY_P, s->partials2.p, grid_for(s->T), s->consts, s->st.p, s->stream);
+    }
+    s->lock_stats = true;
+    CK(cudaStreamSynchronize(s->stream));
+    return FEM_OK;
+}
+
+int fem_multi_step(fem_solid* solids, uint32_t count, double dt, uint32_t nsteps)
+{
+    if (!solids || count == 0) return fail(FEM_E_ARG, "no solids");
+    for (uint32_t i = 0; i < count; i++)
+        if (int e = check_handle(solids[i])) return e;
+    uint32_t max_nr_iter = 0;
+    for (uint32_t i = 0; i < count; i++) max_nr_iter = std::max(max_nr_iter, solids[i]->params.nr_max_iter);
+    for (uint32_t step = 0; step < nsteps; step++) {
+        for (uint32_t i = 0; i < count; i++)
+            if (int e = fem_solid_nr_init(solids[i], dt)) return e;
+        uint32_t nr_iter = 0;
+        do {
+            for (uint32_t i = 0; i < count; i++) {
+                if (int e = fem_solid_nr_prestep(solids[i], dt)) return e;
+                if (int e = fem_solid_nr_midstep(solids[i], dt)) return e;
+            }
+            for (uint32_t i = 0; i < count; i++)
+                if (int e = fem_solid_nr_poststep(solids[i], dt)) return e;
+        } while (++nr_iter < max_nr_iter);
+        for (uint32_t i = 0; i < count; i++)
+            if (int e = fem_solid_nr_end(solids[i], dt)) return e;
+    }
+    return FEM_OK;
+}
+
+int fem_solid_get_params(fem_solid s, fem_params* params)
+{
+    if (int e = check_handle(s)) return e;
+    if (!params) return fail(FEM_E_ARG, "null params");
+    *params = s->params;
+    return FEM_OK;
+}
+
+int fem_solid_get_dapd_state(fem_solid s, double* prev_x, uint8_t* doc)
+{
+    if (int e = check_handle(s)) return e;
+    if (!uses_dapd(s)) return fail(FEM_E_ARG, "the solid does not use the DAPD rotation");
+    if (prev_x)
+        CK(cudaMemcpyAsync(prev_x, s->prev_x.p, sizeof(double) * 3 * (size_t)s->N, cudaMemcpyDeviceToHost,
+                           s->stream));
+    if (doc) CK(cudaMemcpyAsync(doc, s->doc.p, sizeof(uchar2) * s->T, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return FEM_OK;
+}
+
+int fem_solid_set_dapd_state(fem_solid s, const double* prev_x, const uint8_t* doc)
+{
+    if (int e = check_handle(s)) return e;
+    if (!uses_dapd(s)) return fail(FEM_E_ARG, "the solid does not use the DAPD rotation");
+    if (doc)
+        for (uint32_t e = 0; e < s->T; e++) {
+            const uint8_t a = doc[2 * (size_t)e], b = doc[2 * (size_t)e + 1];
+            // none (3, 0), V-F (v, v) or E-E (a < b), vertex ids 0..3
+            if (!((a == 3 && b == 0) || (a <= 3 && b <= 3 && a <= b)))
+                return fail(FEM_E_ARG, "element %u: (%u, %u) is not a direction of collapse", e, a, b);
+        }
+    if (prev_x)
+        CK(cudaMemcpyAsync(s->prev_x.p, prev_x, sizeof(double) * 3 * (size_t)s->N, cudaMemcpyHostToDevice,
+                           s->stream));
+    if (doc) CK(cudaMemcpyAsync(s->doc.p, doc, sizeof(uchar2) * s->T, cudaMemcpyHostToDevice, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return FEM_OK;
+}
+
 int fem_solid_get_state(fem_solid s, double* x, double* v)
 {
     if (int e = check_handle(s)) return e;
@@ -782,7 +1056,7 @@ int fem_solid_synchronize(fem_solid s, fem_step_stats* stats)
     CK(cudaMemcpyAsync(s->st_host, s->st.p, sizeof(StepScalars), cudaMemcpyDeviceToHost, s->stream));
     CK(cudaStreamSynchronize(s->stream));
     if (stats) fill_stats(s, *s->st_host, stats);
-    if (s->st_host->status == FEM_E_NAN) return fail(FEM_E_NAN, "NaN in the CG residual");
+    if (s->st_host->status == FEM_E_NAN) return fail(FEM_E_NAN, "NaN or Inf in the CG residual");
     return FEM_OK;
 }
 

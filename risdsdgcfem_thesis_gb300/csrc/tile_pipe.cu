@@ -687,7 +687,7 @@ __global__ void __launch_bounds__(256) k_mesh_update(BatchView<float> b, const f
                 st.delta_refresh = total;
                 st.k_refresh = st.k;
                 st.refresh_next = 0;
-                if (total != total) st.status = 3u;
+                if (!isfinite(total)) st.status = 3u;
                 if (cg_cont_t(st)) {
                     st.beta = (rec > 0.0 && total <= 1e3 * rec) ? total / rec : 0.0;
                     st.beta_f = (float)st.beta;
@@ -712,7 +712,7 @@ __global__ void __launch_bounds__(256) k_mesh_update(BatchView<float> b, const f
                 st.beta_f = (float)st.beta;
                 st.k += 1;
                 st.total_iters += 1;
-                if (total != total) st.status = 3u;
+                if (!isfinite(total)) st.status = 3u;
                 // reliable updates: recompute the residual in FP64 once |r|
                 // has fallen by refresh_drop since the last FP64 residual,
                 // and at least every refresh_every iterations

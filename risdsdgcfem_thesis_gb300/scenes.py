@@ -79,8 +79,10 @@ class Scene:
     # defaults: 0.1f, 1, 0, 2).
     # Linear solver of the step (enum fem_ls_solver: 0 CG, 1 MINRES).
     ls_solver: int = 0
-    # Material model (enum fem_material: 0 C_WRP, 1 C_LCM).
+    # Material model (enum fem_material: 0 C_WRP, 1 C_LCM, 2 C_LCMH, 3 C_CCM)
+    # and C_LCMH's blend radius (the reference's m_ECIE_k_factor, default 1).
     material: int = 0
+    ecie_k_factor: float = 1.0
     rotation: int = 0
     dapd_threshold: float = float(np.float32(0.1))
     dapd_L: float = 1.0

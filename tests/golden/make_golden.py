@@ -39,7 +39,14 @@ units with Mal's Sqrt/Sin/Cos/ATan2 at double precision, except where noted):
                        QIE (60 steps, qie_) and FIE (20 steps, fie_), and the
                        moving-constraint block with QIE (12 steps, block_).
 
+  materials.npz        the C_LCMH (LCM/WRP hybrid, m_ECIE_k_factor 1 and 0.05)
+                       and C_CCM materials: the cantilever with QIE (30 steps;
+                       prefixes lcmh_, lcmh_k005_, ccm_) and the moving-
+                       constraint block with QIE (12 steps, lcmh_block_,
+                       ccm_block_).
+
 python tests/golden/make_golden.py fie      writes only the two FIE fixtures;
+python tests/golden/make_golden.py materials  only the C_LCMH / C_CCM fixture;
 python tests/golden/make_golden.py lcm      only the C_LCM fixture;
 python tests/golden/make_golden.py dapd     only the DAPD fixture;
 python tests/golden/make_golden.py minres   only the MINRES fixture.
@@ -189,8 +196,34 @@ def lcm_fixture():
     np.savez_compressed(os.path.join(HERE, "lcm.npz"), **out)
 
 
+def material_cases():
+    cant = scenes.cantilever_160()
+    block = dataclasses.replace(fie_block_scene(), integrator=0)
+    return (("lcmh_", dataclasses.replace(cant, material=2), 30),
+            ("lcmh_k005_", dataclasses.replace(cant, material=2, ecie_k_factor=0.05), 30),
+            ("ccm_", dataclasses.replace(cant, material=3), 30),
+            ("lcmh_block_", dataclasses.replace(block, material=2), 12),
+            ("ccm_block_", dataclasses.replace(block, material=3), 12))
+
+
+def materials_fixture():
+    out = {}
+    for prefix, sc, steps in material_cases():
+        ref = O.Solid(sc, "ref_dbl")
+        stats = [ref.step() for _ in range(steps)]
+        x, v = ref.state()
+        out.update(_stat_arrays(stats, prefix))
+        out[prefix + "x"] = x
+        out[prefix + "v"] = v
+    np.savez_compressed(os.path.join(HERE, "materials.npz"), **out)
+
+
 def main():
     O.build(reference=True)
+    if sys.argv[1:] == ["materials"]:
+        materials_fixture()
+        print("wrote the C_LCMH / C_CCM fixture to", HERE)
+        return
     if sys.argv[1:] == ["lcm"]:
         lcm_fixture()
         print("wrote the C_LCM fixture to", HERE)
@@ -211,6 +244,7 @@ def main():
     dapd_fixture()
     minres_fixture()
     lcm_fixture()
+    materials_fixture()
     sc = scenes.cantilever_160()
 
     ref = O.Solid(sc, "ref_dbl")

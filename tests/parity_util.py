@@ -27,7 +27,8 @@ def check_bar(case, quantity, measured, tol, floor, cap=1e-6, mult=10.0):
     the figures."""
     bar = max(tol, mult * floor)
     BARS.append((case, quantity, float(measured), float(bar), float(floor)))
-    assert bar <= cap, f"{case} {quantity}: bar {bar:.3g} from the oracle floor {floor:.3g} exceeds the cap {cap:.3g}"
+    assert bar <= max(cap, tol), \
+        f"{case} {quantity}: bar {bar:.3g} from the oracle floor {floor:.3g} exceeds the cap {cap:.3g}"
     assert measured <= bar, f"{case} {quantity}: {measured:.3g} > bar {bar:.3g} (floor {floor:.3g})"
     return bar
 

@@ -59,3 +59,58 @@ def test_batch_rejects_lcm(fem_lib):
     with pytest.raises(fem_lib.FemError) as e:
         fem_lib.Batch([sc], precision=fem_lib.FEM_PRECISION_FP64)
     assert e.value.code == fem_lib.FEM_E_ARG
+
+
+@pytest.mark.parametrize("case", [0, 1, 3])
+def test_lcmh_matches_reference(fem_lib, case):
+    """C_LCMH (blend radius 1, and 0.05 where it is C_LCM's differential) on
+    the cantilever and the moving-constraint block, against the fixture the
+    reference's element set built with eMM_C_LCMH wrote (materials.npz):
+    rel-L2 <= 1e-10, iterations within 1 per step, energy 1e-8."""
+    from test_oracle_materials import material_cases
+    g = np.load(os.path.join(GOLDEN, "materials.npz"))
+    prefix, sc, steps = material_cases()[case]
+    s = fem_lib.Solid(sc)
+    for k in range(steps):
+        st = s.step(1)
+        assert st["status"] == 0
+        assert abs(st["cg_iterations"] - int(g[prefix + "iters"][k])) <= 1, k
+    x, v = s.state()
+    assert rel(x, g[prefix + "x"]) <= 1e-10 and rel(v, g[prefix + "v"]) <= 1e-10, \
+        (prefix, rel(x, g[prefix + "x"]), rel(v, g[prefix + "v"]))
+    ref_e = float(g[prefix + "elastic_energy"][-1])
+    assert abs(st["elastic_energy"] - ref_e) <= 1e-8 * abs(ref_e)
+
+
+@pytest.mark.parametrize("material,k", [(2, 1.0), (3, 1.0)])
+def test_lcmh_and_ccm_element_hooks_match_oracle(fem_lib, oracle, material, k):
+    rng = np.random.default_rng(9)
+    sc = dataclasses.replace(scenes.random_block(rng, dims=(4, 3, 3)), material=material, ecie_k_factor=k)
+    x = sc.rest + 0.05 * sc.h * rng.standard_normal(sc.rest.shape)
+    dx = rng.standard_normal(sc.rest.shape)
+    g = fem_lib.Solid(sc)
+    o = oracle.Solid(sc, "port")
+    g.begin_eval(x)
+    o.begin_eval(x)
+    assert rel(g.f_e(), o.f_e()) <= 1e-12
+    assert rel(g.df_x(dx), o.df_x(dx)) <= 1e-12
+    assert abs(g.V() - o.V()) <= 1e-12 * max(abs(o.V()), 1e-300)
+
+
+def test_ccm_runs_away_as_in_the_reference(fem_lib):
+    """C_CCM's CG diverges from the first step (its A is not symmetric, see
+    the oracle tests); the reference's state then runs to Inf/NaN within 10
+    steps (materials.npz). Here the first step matches the fixture's
+    diverging CG in iteration count, and the run ends in FEM_E_NAN."""
+    from test_oracle_materials import material_cases
+    g = np.load(os.path.join(GOLDEN, "materials.npz"))
+    prefix, sc, steps = material_cases()[2]
+    assert prefix == "ccm_"
+    s = fem_lib.Solid(sc)
+    st = s.step(1)
+    assert st["cg_iterations"] == int(g["ccm_iters"][0]) == sc.max_iter
+    assert st["rel_residual"] > 1.0 and g["ccm_rel_res"][0] > 1.0
+    with pytest.raises(fem_lib.FemError) as e:
+        for _ in range(steps):
+            s.step(1)
+    assert e.value.code == fem_lib.FEM_E_NAN
