@@ -554,6 +554,18 @@ uint64_t fem_kernel_launches(void);
  * fem_profile_read returns the summed event time and launch count. */
 int fem_profile_enable(int on);
 int fem_profile_read(const char* kernel, double* total_ms, unsigned long long* launches);
+/* Index checks (a diagnostic build, no counterpart in the reference): in a
+ * library compiled with -DFEM_BOUNDS_CHECK (libfemtet_gb300_bounds.so) every
+ * data-dependent index the kernels read from a table -- node ids of
+ * elements, node CSR entries, tile node lists and tile-local ids, partial
+ * slots, constraint nodes -- is compared with its limit; a bad one is
+ * counted, the first one's site (1 element node, 2 CSR entry, 3 constraint
+ * node, 4 batch node, 5 tile-local node, 6 partial slot, 7 tile CSR entry),
+ * index and limit are kept, and the access uses index 0 instead of faulting.
+ * Reads and clears the counts of every kernel unit; *enabled is 1 in that
+ * build, 0 in the normal one (where the counts are always 0). Any pointer
+ * may be null. */
+int fem_bounds_check_status(int* enabled, uint32_t* failures, uint32_t* site, uint32_t* index, uint32_t* limit);
 
 /* --- Mesh ingest: TetGen .node / .ele (examples/tetgen2geo/main.cpp) --- */
 /* Reads a TetGen tetrahedral mesh as the reference's converter does: the

@@ -95,5 +95,14 @@ def build(verbose: bool = False, defines=(), out: str = OUT) -> str:
     return out
 
 
+BOUNDS_OUT = os.path.join(HERE, "libfemtet_gb300_bounds.so")
+
+
+def build_bounds_check(verbose: bool = False) -> str:
+    """The diagnostic variant: every table-read index in the kernels checked
+    against its limit (bounds.cuh), libfemtet_gb300_bounds.so."""
+    return build(verbose=verbose, defines=("FEM_BOUNDS_CHECK",), out=BOUNDS_OUT)
+
+
 if __name__ == "__main__":
     print(build(verbose=True))

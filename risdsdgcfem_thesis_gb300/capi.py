@@ -13,7 +13,10 @@ from typing import Optional
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "libfemtet_gb300.so")
+# FEMGB_BOUNDS_CHECK=1 selects the diagnostic build whose kernels check every
+# table-read index (build.build_bounds_check()); otherwise the normal library.
+BOUNDS_LIB_PATH = os.path.join(HERE, "libfemtet_gb300_bounds.so")
+LIB_PATH = BOUNDS_LIB_PATH if os.environ.get("FEMGB_BOUNDS_CHECK") == "1" else os.path.join(HERE, "libfemtet_gb300.so")
 
 FEM_OK = 0
 FEM_E_ARG, FEM_E_INDEX, FEM_E_NAN, FEM_E_OOM, FEM_E_CUDA, FEM_E_TIMEOUT, FEM_E_NODEVICE, FEM_E_DEGENERATE = range(1, 9)
@@ -142,6 +145,7 @@ SIGNATURES = {
     "fem_kernel_launches": (C.c_uint64, []),
     "fem_profile_enable": (C.c_int, [C.c_int]),
     "fem_profile_read": (C.c_int, [C.c_char_p, _dp, C.POINTER(C.c_ulonglong)]),
+    "fem_bounds_check_status": (C.c_int, [C.POINTER(C.c_int)] + [_up] * 4),
 }
 
 _lib = None
@@ -394,6 +398,17 @@ def profile_read(kernel: str):
     n = C.c_ulonglong()
     load().fem_profile_read(kernel.encode(), C.byref(ms), C.byref(n))
     return ms.value, n.value
+
+
+def bounds_check_status():
+    """Reads and clears the kernels' index-check counts: {"enabled",
+    "failures", "site", "index", "limit"} (enabled is False in the normal
+    library, whose counts are always 0)."""
+    en = C.c_int()
+    w = [C.c_uint32() for _ in range(4)]
+    check(load().fem_bounds_check_status(C.byref(en), *[C.byref(v) for v in w]))
+    return {"enabled": bool(en.value), "failures": w[0].value, "site": w[1].value, "index": w[2].value,
+            "limit": w[3].value}
 
 
 def device_info():

@@ -166,6 +166,7 @@ struct fem_batch_s {
         b.fuse_alpha = opt.fuse_alpha ? 1u : 0u;
         b.Ntot = (uint32_t)Ntot;
         b.Ttot = (uint32_t)Ttot;
+        b.nslots = nslots;
         b.tiles = tiles.p;
         b.chunks = chunks.p;
         b.mc = mc.p;

@@ -122,6 +122,7 @@ struct MeshConsts {
 template <typename S>
 struct BatchView {
     uint32_t M, ntiles, nchunks, Ntot, Ttot;
+    uint64_t nslots;               // partial slots: Ntot owner slots + the overflow slots
     uint32_t pipe_tile;            // mixed: threads per block of the tile product (kPipeSmallTile or kTileElems)
     uint32_t fuse_alpha;           // mixed: the node pass forms alpha (no separate alpha kernel)
     const TileMeta* tiles;

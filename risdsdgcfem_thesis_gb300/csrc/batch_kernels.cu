@@ -29,6 +29,7 @@
 #include "active_list.cuh"
 #include "batch.cuh"
 #include "batch_launch.h"
+#include "bounds.cuh"
 #include "df.cuh"
 #include "elem_math.cuh"
 #include "msvd.cuh"
@@ -167,14 +168,17 @@ __global__ void __launch_bounds__(256) k_tile_spmv(BatchView<S> b, const S* __re
         lc = b.lconn[e];
     }
     for (int i = threadIdx.x; i < tm.nn; i += blockDim.x) {
-        const size_t g = b.tile_nodes[tm.n0 + i];
+        const size_t g = bounds_idx(b.tile_nodes[tm.n0 + i], b.Ntot, kSiteBatchNode);
         sd[i] = dir_update<S>(beta, dvec[3 * g], rvec[3 * g]);
         sd[kTileNodes + i] = dir_update<S>(beta, dvec[3 * g + 1], rvec[3 * g + 1]);
         sd[2 * kTileNodes + i] = dir_update<S>(beta, dvec[3 * g + 2], rvec[3 * g + 2]);
     }
     __syncthreads();
     if (has_elem) {
-        const int ids[4] = {lc.x, lc.y, lc.z, lc.w};
+        const int ids[4] = {(int)bounds_idx((uint32_t)lc.x, tm.nn, kSiteLocalNode),
+                            (int)bounds_idx((uint32_t)lc.y, tm.nn, kSiteLocalNode),
+                            (int)bounds_idx((uint32_t)lc.z, tm.nn, kSiteLocalNode),
+                            (int)bounds_idx((uint32_t)lc.w, tm.nn, kSiteLocalNode)};
         S dl[12];
 #pragma unroll
         for (int i = 0; i < 4; i++) {
@@ -255,7 +259,7 @@ __global__ void __launch_bounds__(256) k_tile_spmv_y64(BatchView<S> b, const dou
         const uint16_t* lp = b.lptr + b.lptr0[t];
         const uint16_t* li = b.lidx + tm.c0;
         for (int i = threadIdx.x; i < tm.nn; i += blockDim.x) {
-            const size_t g = b.tile_nodes[tm.n0 + i];
+            const size_t g = bounds_idx(b.tile_nodes[tm.n0 + i], b.Ntot, kSiteBatchNode);
             y64_set(sd[i], y_full(b, y, 3 * g));
             y64_set(sd[kTileNodes + i], y_full(b, y, 3 * g + 1));
             y64_set(sd[2 * kTileNodes + i], y_full(b, y, 3 * g + 2));
@@ -271,7 +275,10 @@ __global__ void __launch_bounds__(256) k_tile_spmv_y64(BatchView<S> b, const dou
             for (int c = 0; c < 9; c++) Di[c] = b.Dinv[c * T + e];
             const S k1 = b.mat[e], knu = b.mat[T + e], k2 = b.mat[2 * T + e];
             const uchar4 lc = b.lconn[e];
-            const int ids[4] = {lc.x, lc.y, lc.z, lc.w};
+            const int ids[4] = {(int)bounds_idx((uint32_t)lc.x, tm.nn, kSiteLocalNode),
+                            (int)bounds_idx((uint32_t)lc.y, tm.nn, kSiteLocalNode),
+                            (int)bounds_idx((uint32_t)lc.z, tm.nn, kSiteLocalNode),
+                            (int)bounds_idx((uint32_t)lc.w, tm.nn, kSiteLocalNode)};
             V dl[12];
 #pragma unroll
             for (int i = 0; i < 4; i++) {
@@ -337,7 +344,10 @@ __global__ void __launch_bounds__(256) k_tile_force(BatchView<S> b, const double
             y64_set(knu, (double)b.mat[T + e]);
             y64_set(k2, (double)b.mat[2 * T + e]);
             const int4 g = b.gtets[e];
-            const int ids[4] = {g.x, g.y, g.z, g.w};
+            const int ids[4] = {(int)bounds_idx((uint32_t)g.x, b.Ntot, kSiteBatchNode),
+                            (int)bounds_idx((uint32_t)g.y, b.Ntot, kSiteBatchNode),
+                            (int)bounds_idx((uint32_t)g.z, b.Ntot, kSiteBatchNode),
+                            (int)bounds_idx((uint32_t)g.w, b.Ntot, kSiteBatchNode)};
             V u[12];
 #pragma unroll
             for (int i = 0; i < 4; i++) {
@@ -417,7 +427,10 @@ __global__ void k_tile_potential(BatchView<S> b, const double* __restrict__ x, d
         if (threadIdx.x < tm.ne) {
             const size_t e = tm.e0 + threadIdx.x;
             const int4 g = b.gtets[e];
-            const int ids[4] = {g.x, g.y, g.z, g.w};
+            const int ids[4] = {(int)bounds_idx((uint32_t)g.x, b.Ntot, kSiteBatchNode),
+                            (int)bounds_idx((uint32_t)g.y, b.Ntot, kSiteBatchNode),
+                            (int)bounds_idx((uint32_t)g.z, b.Ntot, kSiteBatchNode),
+                            (int)bounds_idx((uint32_t)g.w, b.Ntot, kSiteBatchNode)};
             double s[3] = {0, 0, 0};
 #pragma unroll
             for (int i = 0; i < 4; i++)
@@ -445,7 +458,7 @@ __device__ __forceinline__ void sum_parts(const BatchView<S>& b, const P* __rest
     a0 = (double)part[3 * n];
     a1 = (double)part[3 * n + 1];
     a2 = (double)part[3 * n + 2];
-    const uint32_t j1 = b.ov_ptr[n + 1];
+    const uint32_t j1 = bounds_idx(b.ov_ptr[n + 1], b.nslots - b.Ntot + 1, kSitePartialSlot);
     for (uint32_t j = b.ov_ptr[n]; j < j1; j++) {
         const size_t o = 3 * ((size_t)b.Ntot + j);
         a0 += (double)part[o];
@@ -493,7 +506,7 @@ __global__ void k_knc(BatchView<S> b, uint32_t K, const double* __restrict__ x, 
         const uint32_t m = b.knc_mesh[k];
         if (b.active[m] != 1) continue;
         const MeshConsts& c = b.mc[m];
-        const size_t n = b.knc_node[k];
+        const size_t n = bounds_idx(b.knc_node[k], b.Ntot, kSiteKncNode);
         const double* tg = b.knc_target + 3 * (size_t)k;
         V3<double> vk = mk<double>(c.inv_dt * (tg[0] - x[3 * n]), c.inv_dt * (tg[1] - x[3 * n + 1]),
                                    c.inv_dt * (tg[2] - x[3 * n + 2]));
@@ -677,7 +690,7 @@ __global__ void k_node_q(BatchView<S> b, const S* __restrict__ part, S* __restri
                 dn1 = dir_update<S>(beta, d[i + 1], r[i + 1]);
                 dn2 = dir_update<S>(beta, d[i + 2], r[i + 2]);
                 S s0 = part[3 * n], s1 = part[3 * n + 1], s2 = part[3 * n + 2];
-                const uint32_t j1 = b.ov_ptr[n + 1];
+                const uint32_t j1 = bounds_idx(b.ov_ptr[n + 1], b.nslots - b.Ntot + 1, kSitePartialSlot);
                 for (uint32_t j = b.ov_ptr[n]; j < j1; j++) {
                     const size_t o = 3 * ((size_t)b.Ntot + j);
                     s0 += part[o];
@@ -1002,5 +1015,7 @@ uint32_t grid_chunks(uint32_t nchunks)
 
 template struct BatchLaunch<double>;
 template struct BatchLaunch<float>;
+
+FEMGB_BOUNDS_ACCESSOR(bounds_read_batch_kernels)
 
 }  // namespace femgb

@@ -99,7 +99,7 @@ void launch_elem_force_fp64(const MeshView<double>& m, const double* x, int writ
                             cudaStream_t s);
 void launch_node_b_fp64(const MeshView<double>& m, const StepConsts& c, const double* v, double* b, double* y,
                         cudaStream_t s);
-void launch_knc_fp64(uint32_t count, const uint32_t* nodes, const double* targets, const double* x,
+void launch_knc_fp64(uint32_t N, uint32_t count, const uint32_t* nodes, const double* targets, const double* x,
                      const StepConsts& c, double* b, double* y, cudaStream_t s);
 void launch_node_residual_fp64(const MeshView<double>& m, const StepConsts& c, const double* b, const double* y,
                                double* r, double* d, double* partials, cudaStream_t s);
@@ -113,7 +113,7 @@ void launch_integrate_fp64(uint32_t N, double dt, double* x, double* v, const do
 // Fully-implicit Euler (Newton on Delta x) pieces, FP64 solid path.
 void launch_node_b_fie_fp64(const MeshView<double>& m, const StepConsts& c, const double* x, const double* xn,
                             const double* vn, int warm, double* b, double* y, cudaStream_t s);
-void launch_knc_fie_fp64(uint32_t count, const uint32_t* nodes, const double* targets, const double* x, double* b,
+void launch_knc_fie_fp64(uint32_t N, uint32_t count, const uint32_t* nodes, const double* targets, const double* x, double* b,
                          double* y, cudaStream_t s);
 void launch_sq_norm_fp64(uint32_t n, const double* v, double* partials, cudaStream_t s);
 void launch_fie_update_fp64(uint32_t N, double inv_dt, double* x, double* v, const double* xn, const double* y,

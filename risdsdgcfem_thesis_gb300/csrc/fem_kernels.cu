@@ -14,6 +14,7 @@
 // the reference's serial scatter adds them). Reductions are deterministic:
 // warp shuffles, a fixed block tree, then one block summing the block
 // partials in index order.
+#include "bounds.cuh"
 #include "lcm.cuh"
 #include "fem_device.cuh"
 #include "msvd.cuh"
@@ -208,7 +209,10 @@ __global__ void k_elem_lcm_spmv_fp64(MeshView<double> m, const double* __restric
     if (check_done && st->done) return;
     for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < m.T; e += gridDim.x * blockDim.x) {
         const int4 t = m.tets[e];
-        const int ids[4] = {t.x, t.y, t.z, t.w};
+        const int ids[4] = {(int)bounds_idx((uint32_t)t.x, m.N, kSiteElemNode),
+                            (int)bounds_idx((uint32_t)t.y, m.N, kSiteElemNode),
+                            (int)bounds_idx((uint32_t)t.z, m.N, kSiteElemNode),
+                            (int)bounds_idx((uint32_t)t.w, m.N, kSiteElemNode)};
         double R[9], Di[9], dl[12];
         load_R_Dinv(m, e, R, Di);
 #pragma unroll
@@ -241,7 +245,10 @@ __global__ void k_elem_spmv_fp64(MeshView<double> m, const double* __restrict__ 
         double R[9], Di[9], k1, knu, k2;
         load_elem(m, e, R, Di, k1, knu, k2);
         double dl[12];
-        const int ids[4] = {t.x, t.y, t.z, t.w};
+        const int ids[4] = {(int)bounds_idx((uint32_t)t.x, m.N, kSiteElemNode),
+                            (int)bounds_idx((uint32_t)t.y, m.N, kSiteElemNode),
+                            (int)bounds_idx((uint32_t)t.z, m.N, kSiteElemNode),
+                            (int)bounds_idx((uint32_t)t.w, m.N, kSiteElemNode)};
 #pragma unroll
         for (int i = 0; i < 4; i++) {
             dl[3 * i] = d[3 * (size_t)ids[i]];
@@ -266,7 +273,10 @@ __global__ void k_elem_force_fp64(MeshView<double> m, const double* __restrict__
         const int4 t = m.tets[e];
         double R[9], Di[9], k1, knu, k2;
         load_elem(m, e, R, Di, k1, knu, k2);
-        const int ids[4] = {t.x, t.y, t.z, t.w};
+        const int ids[4] = {(int)bounds_idx((uint32_t)t.x, m.N, kSiteElemNode),
+                            (int)bounds_idx((uint32_t)t.y, m.N, kSiteElemNode),
+                            (int)bounds_idx((uint32_t)t.z, m.N, kSiteElemNode),
+                            (int)bounds_idx((uint32_t)t.w, m.N, kSiteElemNode)};
         double u[12];
 #pragma unroll
         for (int i = 0; i < 4; i++) {
@@ -316,7 +326,10 @@ __global__ void k_potential_fp64(MeshView<double> m, StepConsts c, const double*
     double acc = 0.0;
     for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < m.T; e += gridDim.x * blockDim.x) {
         const int4 t = m.tets[e];
-        const int ids[4] = {t.x, t.y, t.z, t.w};
+        const int ids[4] = {(int)bounds_idx((uint32_t)t.x, m.N, kSiteElemNode),
+                            (int)bounds_idx((uint32_t)t.y, m.N, kSiteElemNode),
+                            (int)bounds_idx((uint32_t)t.z, m.N, kSiteElemNode),
+                            (int)bounds_idx((uint32_t)t.w, m.N, kSiteElemNode)};
         double s[3] = {0, 0, 0};
 #pragma unroll
         for (int i = 0; i < 4; i++)
@@ -335,7 +348,7 @@ __device__ __forceinline__ void gather3(const MeshView<double>& m, uint32_t n, d
 {
     const uint32_t beg = m.csr_ptr[n], end = m.csr_ptr[n + 1];
     for (uint32_t j = beg; j < end; j++) {
-        const double* o = m.eout + 3 * (size_t)m.csr_idx[j];
+        const double* o = m.eout + 3 * (size_t)bounds_idx(m.csr_idx[j], 4ull * m.T, kSiteCsrEntry);
         a0 += o[0];
         a1 += o[1];
         a2 += o[2];
@@ -360,11 +373,12 @@ __global__ void k_node_b_fp64(MeshView<double> m, StepConsts c, const double* __
 
 // Position constraints -> clamped velocity, written to b and y
 // (Step_QuasiImplicitEuler_v, LeafDSH_Solid3D_FEM.cpp:1268-1295).
-__global__ void k_knc_fp64(uint32_t count, const uint32_t* __restrict__ nodes, const double* __restrict__ targets,
-                           const double* __restrict__ x, StepConsts c, double* b, double* y)
+__global__ void k_knc_fp64(uint32_t N, uint32_t count, const uint32_t* __restrict__ nodes,
+                           const double* __restrict__ targets, const double* __restrict__ x, StepConsts c, double* b,
+                           double* y)
 {
     for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < count; k += gridDim.x * blockDim.x) {
-        const size_t n = nodes[k];
+        const size_t n = bounds_idx(nodes[k], N, kSiteKncNode);
         V3<double> vk = mk<double>(c.inv_dt * (targets[3 * k] - x[3 * n]), c.inv_dt * (targets[3 * k + 1] - x[3 * n + 1]),
                                    c.inv_dt * (targets[3 * k + 2] - x[3 * n + 2]));
         double norm_vk = ::sqrt(dot0(vk, vk));
@@ -496,12 +510,12 @@ __global__ void k_node_b_fie_fp64(MeshView<double> m, StepConsts c, const double
 }
 
 // Position constraints as Delta x rows: b = y = target - x_k (:1441-1465).
-__global__ void k_knc_fie_fp64(uint32_t count, const uint32_t* __restrict__ nodes,
+__global__ void k_knc_fie_fp64(uint32_t N, uint32_t count, const uint32_t* __restrict__ nodes,
                                const double* __restrict__ targets, const double* __restrict__ x, double* b,
                                double* y)
 {
     for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < count; k += gridDim.x * blockDim.x) {
-        const size_t n = nodes[k];
+        const size_t n = bounds_idx(nodes[k], N, kSiteKncNode);
 #pragma unroll
         for (int a = 0; a < 3; a++) {
             const double dx = targets[3 * k + a] - x[3 * n + a];
@@ -831,11 +845,11 @@ void launch_node_b_fp64(const MeshView<double>& m, const StepConsts& c, const do
 {
     FEMGB_LAUNCH(k_node_b_fp64, grid_for(m.N), m, c, v, b, y);
 }
-void launch_knc_fp64(uint32_t count, const uint32_t* nodes, const double* targets, const double* x,
+void launch_knc_fp64(uint32_t N, uint32_t count, const uint32_t* nodes, const double* targets, const double* x,
                      const StepConsts& c, double* b, double* y, cudaStream_t s)
 {
     if (count == 0) return;
-    FEMGB_LAUNCH(k_knc_fp64, grid_for(count), count, nodes, targets, x, c, b, y);
+    FEMGB_LAUNCH(k_knc_fp64, grid_for(count), N, count, nodes, targets, x, c, b, y);
 }
 void launch_node_residual_fp64(const MeshView<double>& m, const StepConsts& c, const double* b, const double* y,
                                double* r, double* d, double* partials, cudaStream_t s)
@@ -868,11 +882,11 @@ void launch_node_b_fie_fp64(const MeshView<double>& m, const StepConsts& c, cons
 {
     FEMGB_LAUNCH(k_node_b_fie_fp64, grid_for(m.N), m, c, x, xn, vn, warm, b, y);
 }
-void launch_knc_fie_fp64(uint32_t count, const uint32_t* nodes, const double* targets, const double* x, double* b,
-                         double* y, cudaStream_t s)
+void launch_knc_fie_fp64(uint32_t N, uint32_t count, const uint32_t* nodes, const double* targets, const double* x,
+                         double* b, double* y, cudaStream_t s)
 {
     if (count == 0) return;
-    FEMGB_LAUNCH(k_knc_fie_fp64, grid_for(count), count, nodes, targets, x, b, y);
+    FEMGB_LAUNCH(k_knc_fie_fp64, grid_for(count), N, count, nodes, targets, x, b, y);
 }
 void launch_sq_norm_fp64(uint32_t n, const double* v, double* partials, cudaStream_t s)
 {
@@ -938,5 +952,7 @@ void launch_finalize(int kind, const double* partials, uint32_t count, const Ste
     k_finalize<<<1, kFinalizeThreads, 0, s>>>(kind, partials, count, c, st);
     launch_counter()++;
 }
+
+FEMGB_BOUNDS_ACCESSOR(bounds_read_fem_kernels)
 
 }  // namespace femgb

@@ -7,6 +7,7 @@
 // multiply-adds), which makes the GPU rotations equal to the reference's on
 // the same positions.
 #include "batch_launch.h"
+#include "bounds.cuh"
 #include "dapd.cuh"
 #include "fem_device.cuh"
 #include "msvd.cuh"
@@ -19,7 +20,10 @@ __global__ void k_begin_eval_fp64(MeshView<double> m, const double* __restrict__
     unsigned inverted = 0;
     for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < m.T; e += gridDim.x * blockDim.x) {
         const int4 t = m.tets[e];
-        const int ids[4] = {t.x, t.y, t.z, t.w};
+        const int ids[4] = {(int)bounds_idx((uint32_t)t.x, m.N, kSiteElemNode),
+                            (int)bounds_idx((uint32_t)t.y, m.N, kSiteElemNode),
+                            (int)bounds_idx((uint32_t)t.z, m.N, kSiteElemNode),
+                            (int)bounds_idx((uint32_t)t.w, m.N, kSiteElemNode)};
         V3<double> xs[4];
 #pragma unroll
         for (int i = 0; i < 4; i++) xs[i] = mk<double>(x[3 * (size_t)ids[i]], x[3 * (size_t)ids[i] + 1], x[3 * (size_t)ids[i] + 2]);
@@ -68,7 +72,10 @@ __global__ void k_begin_eval_dapd_fp64(MeshView<double> m, const double* __restr
     unsigned inverted = 0;
     for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < m.T; e += gridDim.x * blockDim.x) {
         const int4 t = m.tets[e];
-        const int ids[4] = {t.x, t.y, t.z, t.w};
+        const int ids[4] = {(int)bounds_idx((uint32_t)t.x, m.N, kSiteElemNode),
+                            (int)bounds_idx((uint32_t)t.y, m.N, kSiteElemNode),
+                            (int)bounds_idx((uint32_t)t.z, m.N, kSiteElemNode),
+                            (int)bounds_idx((uint32_t)t.w, m.N, kSiteElemNode)};
         V3<double> xs[4], xp[4];
 #pragma unroll
         for (int i = 0; i < 4; i++) {
@@ -171,7 +178,10 @@ __global__ void __launch_bounds__(256, 3) k_begin_eval_batch(BatchView<S> b, con
             const size_t e = tm.e0 + threadIdx.x;
             const size_t T = b.Ttot;
             const int4 g = b.gtets[e];
-            const int ids[4] = {g.x, g.y, g.z, g.w};
+            const int ids[4] = {(int)bounds_idx((uint32_t)g.x, b.Ntot, kSiteBatchNode),
+                            (int)bounds_idx((uint32_t)g.y, b.Ntot, kSiteBatchNode),
+                            (int)bounds_idx((uint32_t)g.z, b.Ntot, kSiteBatchNode),
+                            (int)bounds_idx((uint32_t)g.w, b.Ntot, kSiteBatchNode)};
             V3<double> xs[4];
 #pragma unroll
             for (int i = 0; i < 4; i++)
@@ -251,5 +261,7 @@ void BatchLaunch<S>::begin_eval(const BatchView<S>& b, const double* x, cudaStre
 
 template void BatchLaunch<double>::begin_eval(const BatchView<double>&, const double*, cudaStream_t);
 template void BatchLaunch<float>::begin_eval(const BatchView<float>&, const double*, cudaStream_t);
+
+FEMGB_BOUNDS_ACCESSOR(bounds_read_rotation)
 
 }  // namespace femgb

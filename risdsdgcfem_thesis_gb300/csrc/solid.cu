@@ -14,6 +14,7 @@
 // (Step_FullyImplicitEuler_dx, :1357-1552) runs its Newton loop on the host
 // over the same kernels, reading |b_k| and |y_k| once per Newton iteration.
 #include "../../include/fem_tet.h"
+#include "bounds.cuh"
 #include "dapd.cuh"
 #include "fem_device.cuh"
 
@@ -450,7 +451,7 @@ int step_fie(fem_solid s, int chunk)
     do {
         elem_force(s, m, s->x.p, 1, nullptr);
         launch_node_b_fie_fp64(m, c, s->x.p, s->xn.p, s->vn.p, nr_k == 0 ? 1 : 0, s->b.p, s->y.p, st);
-        launch_knc_fie_fp64(s->knc_count, s->knc_nodes.p, s->knc_targets.p, s->x.p, s->b.p, s->y.p, st);
+        launch_knc_fie_fp64(s->N, s->knc_count, s->knc_nodes.p, s->knc_targets.p, s->x.p, s->b.p, s->y.p, st);
         launch_sq_norm_fp64(3 * s->N, s->b.p, s->partials.p, st);
         if (int e = host_sum(s, gV, &sum)) return e;
         delta_new = std::sqrt(sum);
@@ -492,7 +493,7 @@ int step_once(fem_solid s, int chunk)
     if (int e = open_step(s)) return e;
     elem_force(s, m, s->x.p, 1, nullptr);
     launch_node_b_fp64(m, c, s->v.p, s->b.p, s->y.p, st);
-    launch_knc_fp64(s->knc_count, s->knc_nodes.p, s->knc_targets.p, s->x.p, c, s->b.p, s->y.p, st);
+    launch_knc_fp64(s->N, s->knc_count, s->knc_nodes.p, s->knc_targets.p, s->x.p, c, s->b.p, s->y.p, st);
     if (int e = ls_solve(s, c, chunk)) return e;
     launch_integrate_fp64(s->N, c.dt, s->x.p, s->v.p, s->y.p, st);
     if (s->params.compute_energy) energy(s);
@@ -551,6 +552,34 @@ int fem_device_info(int* device, int* sm_count, int* cc_major, int* cc_minor)
     if (sm_count) *sm_count = p.multiProcessorCount;
     if (cc_major) *cc_major = p.major;
     if (cc_minor) *cc_minor = p.minor;
+    return FEM_OK;
+}
+
+int fem_bounds_check_status(int* enabled, uint32_t* failures, uint32_t* site, uint32_t* index, uint32_t* limit)
+{
+#ifdef FEM_BOUNDS_CHECK
+    const int on = 1;
+#else
+    const int on = 0;
+#endif
+    int (*const units[])(unsigned*) = {bounds_read_fem_kernels, bounds_read_rotation, bounds_read_batch_kernels,
+                                       bounds_read_tile_pipe};
+    unsigned total = 0, first[3] = {0u, 0u, 0u};
+    for (auto rd : units) {
+        unsigned w[4];
+        if (rd(w) != 0) return fail(FEM_E_CUDA, "reading the index-check words failed");
+        if (w[0] != 0u && total == 0u) {
+            first[0] = w[1];
+            first[1] = w[2];
+            first[2] = w[3];
+        }
+        total += w[0];
+    }
+    if (enabled) *enabled = on;
+    if (failures) *failures = total;
+    if (site) *site = first[0];
+    if (index) *index = first[1];
+    if (limit) *limit = first[2];
     return FEM_OK;
 }
 
@@ -925,7 +954,7 @@ int fem_solid_nr_midstep(fem_solid s, double dt)
     // NR_PreStep), with the rotations of the last BeginEvaluation
     elem_force(s, m, s->lk_x.p, 1, nullptr);
     launch_node_b_fie_fp64(m, c, s->lk_x.p, s->x.p, s->v.p, s->lock_nr_k == 0 ? 1 : 0, s->b.p, s->y.p, s->stream);
-    launch_knc_fie_fp64(s->knc_count, s->knc_nodes.p, s->knc_targets.p, s->lk_x.p, s->b.p, s->y.p, s->stream);
+    launch_knc_fie_fp64(s->N, s->knc_count, s->knc_nodes.p, s->knc_targets.p, s->lk_x.p, s->b.p, s->y.p, s->stream);
     if (int e = ls_solve(s, c, 8)) return e;
     s->lock_ls_iters += s->st_host->k;
     CK(cudaGetLastError());

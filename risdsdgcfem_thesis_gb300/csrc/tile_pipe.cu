@@ -59,6 +59,7 @@
 #include "active_list.cuh"
 #include "batch.cuh"
 #include "batch_launch.h"
+#include "bounds.cuh"
 #include "elem_math.cuh"
 
 namespace femgb {
@@ -267,7 +268,8 @@ __device__ __forceinline__ void look_resolve(const BatchView<float>& b, TileLook
     L.done = st.done;
     L.beta = st.beta_f;
     L.boff = b.blob_off16[L.tile];
-    L.g = threadIdx.x < look_nn(L) ? __ldg(b.tile_nodes + L.n0 + threadIdx.x) : 0u;
+    L.g = threadIdx.x < look_nn(L) ? bounds_idx(__ldg(b.tile_nodes + L.n0 + threadIdx.x), b.Ntot, kSiteBatchNode)
+                                   : 0u;
 }
 
 __device__ __forceinline__ void fence_proxy_async_smem()
@@ -387,8 +389,10 @@ __global__ void __launch_bounds__(TILE, PipeShape<TILE>::kMinBlocks) k_tile_spmv
             const float R[9] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w, q2.x};
             const float Di[9] = {q2.y, q2.z, q2.w, q3.x, q3.y, q3.z, q3.w, q4.x, q4.y};
             const float knu = q4.z, k2 = q4.w, k1 = __fmaf_rn(2.f, k2, knu);
-            const int ids[4] = {(int)(lw & 0xff), (int)((lw >> 8) & 0xff), (int)((lw >> 16) & 0xff),
-                                (int)(lw >> 24)};
+            const int ids[4] = {(int)bounds_idx(lw & 0xffu, nn, kSiteLocalNode),
+                                (int)bounds_idx((lw >> 8) & 0xffu, nn, kSiteLocalNode),
+                                (int)bounds_idx((lw >> 16) & 0xffu, nn, kSiteLocalNode),
+                                (int)bounds_idx(lw >> 24, nn, kSiteLocalNode)};
             float dl[12];
 #pragma unroll
             for (int k = 0; k < 4; k++) {
@@ -432,13 +436,14 @@ __global__ void __launch_bounds__(TILE, PipeShape<TILE>::kMinBlocks) k_tile_spmv
                 const uint16_t* li = lp + (nn + 1);
                 float a0 = 0.f, a1 = 0.f, a2 = 0.f;
                 for (int j = lp[tid]; j < lp[tid + 1]; j++) {
-                    const float4 v = so4[li[j]];
+                    const float4 v = so4[bounds_idx((uint32_t)li[j], 4u * ne4, kSiteTileEntry)];
                     a0 += v.x;
                     a1 += v.y;
                     a2 += v.z;
                 }
                 const uint32_t nown = look_nown(cur);
-                const size_t o = 3 * (size_t)(tid < nown ? hdr[0] + tid : hdr[3 + tid - nown]);
+                const size_t o =
+                    3 * (size_t)bounds_idx(tid < nown ? hdr[0] + tid : hdr[3 + tid - nown], b.nslots, kSitePartialSlot);
                 part[o] = a0;
                 part[o + 1] = a1;
                 part[o + 2] = a2;
@@ -574,7 +579,8 @@ __global__ void __launch_bounds__(256) k_node_update_fused(BatchView<float> b, c
             // the owner tile's partial (node order), then the overflow slots
             // (contiguous, tile order)
             float s0 = part[i], s1 = part[i + 1], s2 = part[i + 2];
-            const uint32_t j0 = b.ov_ptr[n], j1 = b.ov_ptr[n + 1];
+            const uint32_t j0 = b.ov_ptr[n];
+            const uint32_t j1 = bounds_idx(b.ov_ptr[n + 1], b.nslots - b.Ntot + 1, kSitePartialSlot);
             float r0 = r[i], r1 = r[i + 1], r2 = r[i + 2];
             float e0 = b.ydelta[i], e1 = b.ydelta[i + 1], e2 = b.ydelta[i + 2];
             // the first four overflow partials are loaded together, then
@@ -863,5 +869,7 @@ void prepare_tile_pipe()
     (void)pipe_grid<kTileElems>();
     (void)node_grid();
 }
+
+FEMGB_BOUNDS_ACCESSOR(bounds_read_tile_pipe)
 
 }  // namespace femgb
