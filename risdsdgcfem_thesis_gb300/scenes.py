@@ -198,6 +198,33 @@ def compressed_cube(n: int = 40, steps: int = 120, ratio: float = 0.4) -> Scene:
                  grid=(n, n, n), h=h)
 
 
+def sheared_crush(n: int = 4, steps: int = 30, ratio: float = 0.15, shear: float = 0.3, h: float = 0.1,
+                  rotation: int = 1) -> Scene:
+    """n^3 cubes of h (default 10 cm: large enough that DAPD's collapse axis
+    passes the reference's absolute area test, so its offset rotation runs),
+    E=2e5, nu=0.45; bottom face fixed, top face driven to `ratio` of the
+    height while it slides by `shear` of the height in x, linearly over
+    `steps` steps; DAPD rotations; CG rel 1e-8."""
+    rest, tets, ijk = grid_mesh(n, n, n, h, 0.1 * h, 0)
+    bottom = _face_nodes(ijk, (n, n, n), "z-")
+    top = _face_nodes(ijk, (n, n, n), "z+")
+    nodes = np.concatenate([bottom, top]).astype(np.uint32)
+    base = rest[nodes].copy()
+    nb = bottom.shape[0]
+    height = n * h
+
+    def schedule(step: int) -> np.ndarray:
+        s = min(step + 1, steps) / float(steps)
+        t = base.copy()
+        t[nb:, 2] = base[nb:, 2] - s * (1.0 - ratio) * height
+        t[nb:, 0] = base[nb:, 0] + s * shear * height
+        return t
+
+    return Scene(name=f"sheared_crush_{n}x{n}x{n}", rest=rest, tets=tets, young=2e5, poisson=0.45, density=1000.0,
+                 rel_eps=1e-8, abs_eps=0.0, max_iter=500, steps=steps, knc_nodes=nodes, knc_targets=base.copy(),
+                 knc_schedule=schedule, grid=(n, n, n), h=h, rotation=rotation)
+
+
 def random_block(rng: np.random.Generator, lo: int = 4, hi: int = 30, idx: int = 0,
                  dims=None) -> Scene:
     """One mesh of the batched workload: a x b x c cubes (uniform in [lo, hi]),

@@ -92,3 +92,39 @@ def test_batch_and_server_reject_dapd(fem_lib):
     with pytest.raises(fem_lib.FemError) as e:
         fem_lib.Batch([sc], precision=fem_lib.FEM_PRECISION_FP64)
     assert e.value.code == fem_lib.FEM_E_ARG
+
+
+def test_dapd_offset_rotations_match_oracle(fem_lib, oracle):
+    """DAPD's offset branch at the element level: the sheared crush of 10 cm
+    cubes (elements large enough for the reference's absolute area test on
+    the collapse axis), evaluated at the oracle's positions after 26 steps
+    against the previous step's positions and the directions of collapse the
+    run had reached, restored through fem_solid_set_dapd_state. Rotations
+    within 1e-12 of the oracle's, the same directions of collapse, and the
+    offset rotation (not I) on the collapsing elements. (Whole runs of this
+    scene are chaotic: the oracle itself moves by ~1e-2 under a 1e-15 input
+    change once elements collapse, so they are compared on the CPU only,
+    restatement against the reference build, bit for bit.)"""
+    sc = scenes.sheared_crush()
+    o25, o26 = oracle.Solid(sc, "port"), oracle.Solid(sc, "port")
+    for k in range(26):
+        if k < 25:
+            o25.step()
+        o26.step()
+    x25, _ = o25.state()
+    x26, v26 = o26.state()
+    doc_before = o26.doc()
+    o26.begin_eval(x26)  # BeginEvaluation(x25, x26), as the next step opens
+    g = fem_lib.Solid(sc)
+    g.set_state(x26, v26)
+    g.set_dapd_state(x25, doc_before)
+    g.begin_eval(x26)
+    Rg, dg = g.rotations()
+    Ro = o26.rotations()
+    assert np.array_equal(dg, o26.detF())
+    assert np.array_equal(g.doc(), o26.doc())
+    assert np.abs(Rg - Ro).max() < 1e-12
+    doc = o26.doc()
+    held = (doc[:, 0] <= doc[:, 1]) & (o26.detF() <= np.float32(0.1))
+    assert held.sum() > 40
+    assert (np.abs(Ro[held] - np.eye(3)).reshape(-1, 9).max(axis=1) > 1e-6).sum() > 0.9 * held.sum()

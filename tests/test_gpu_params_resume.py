@@ -92,27 +92,28 @@ def test_set_params_rejects_bad_values(fem_lib):
 
 
 def test_dapd_run_resumes_bit_for_bit_from_a_checkpoint(fem_lib):
-    # the crushed cube's elements start to collapse at step 24 (39 hold a
-    # direction of collapse then, 283 at step 30)
-    sc = dataclasses.replace(scenes.compressed_cube(n=6, steps=30, ratio=0.15), rotation=1)
+    # the sheared crush of 10 cm cubes: its elements start to collapse at
+    # step 23 and take DAPD's offset rotation, which needs each element's
+    # direction of collapse (on 1 cm cubes that rotation is I either way)
+    sc = scenes.sheared_crush()
     whole = fem_lib.Solid(sc)
-    whole.step(30)
+    whole.step(28)
     first = fem_lib.Solid(sc)
-    first.step(26)
+    first.step(24)
     x, v = first.state()
     prev_x, doc = first.dapd_state()
-    assert (doc[:, 0] <= doc[:, 1]).sum() > 20  # elements hold a direction of collapse
+    assert (doc[:, 0] <= doc[:, 1]).sum() >= 5  # elements hold a direction of collapse
     resumed = fem_lib.Solid(sc)
     resumed.set_state(x, v)
     resumed.set_dapd_state(prev_x, doc)
-    resumed.step_index = 26  # the driven face's schedule continues
+    resumed.step_index = 24  # the driven face's schedule continues
     resumed.step(4)
     assert _same(whole, resumed)
     # without the DAPD state the resumed run differs (the previous positions
     # reset to x and the directions of collapse are lost)
     naive = fem_lib.Solid(sc)
     naive.set_state(x, v)
-    naive.step_index = 26
+    naive.step_index = 24
     naive.step(4)
     assert not _same(whole, naive)
 

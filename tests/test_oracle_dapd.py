@@ -85,3 +85,29 @@ def test_dapd_rotation_of_rotated_stretch(oracle):
     m = oracle.Solid(dataclasses.replace(sc, rotation=0), "port")
     m.begin_eval(sc.rest @ (Q @ S).T)
     assert np.abs(m.rotations() - Q).max() < 1e-9
+
+
+@pytest.mark.parametrize("integrator", [0, 1])
+def test_dapd_offset_branch_port_equals_reference_bitwise(oracle, integrator):
+    """The sheared crush of 10 cm cubes: large enough elements that DAPD's
+    collapse axis passes the reference's absolute area test
+    (len^2 > 1e-6f, Rotation.cpp:364-495), so the degenerate elements take
+    the offset polar rotation (on the 1 cm cubes of the other cases that
+    test fails and R = I). The restatement equals the reference build bit
+    for bit over 30 steps, and the offset branch ran."""
+    import dataclasses
+    from risdsdgcfem_thesis_gb300 import scenes
+    if not os.path.exists(oracle.REF_DBL_SO):
+        pytest.skip("reference sources not present in this container")
+    sc = dataclasses.replace(scenes.sheared_crush(), integrator=integrator)
+    a = oracle.Solid(sc, "port")
+    b = oracle.Solid(sc, "ref_dbl")
+    for k in range(30):
+        assert a.step() == b.step(), k
+    xa, va = a.state()
+    xb, vb = b.state()
+    assert np.array_equal(xa, xb) and np.array_equal(va, vb)
+    doc, R, detF = a.doc(), a.rotations(), a.detF()
+    held = (doc[:, 0] <= doc[:, 1]) & (detF <= np.float32(0.1))
+    assert held.sum() > 40
+    assert (np.abs(R[held] - np.eye(3)).reshape(-1, 9).max(axis=1) > 1e-6).sum() > 0.9 * held.sum()
