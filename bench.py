@@ -181,10 +181,10 @@ class CpuSampler:
     """The reference's CPU path (the oracle restatement, bit-exact with the
     reference's FP64 translation units) on the workload's meshes, one mesh per
     thread over `threads` host threads (the reference steps solids serially,
-    one thread each). A sample times the CG iterations of each mesh's first
-    FixedStep: all meshes stepped with the CG capped at `cap` iterations,
-    minus the same with the cap at 0 (the per-step fixed work is left out,
-    which favours the CPU)."""
+    one thread each). A sample is one whole FixedStep of every mesh --
+    rotations, forces, right-hand side, the CG solve to each mesh's own
+    tolerance, integration and energies -- continuing from the previous
+    sample's state, as the GPU steps continue."""
 
     def __init__(self, scs, threads):
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -194,26 +194,82 @@ class CpuSampler:
         self.threads = max(1, threads)
         self.solids = [pyoracle.Solid(sc, "port") for sc in scs]
 
-    def _region(self, cap):
+    def sample(self):
         from concurrent.futures import ThreadPoolExecutor
         iters = [0] * len(self.solids)
 
         def run(i):
-            s = self.solids[i]
-            s.reset()
-            s.set_solver(self.scs[i].rel_eps, self.scs[i].abs_eps, cap)
-            iters[i] = s.step()["iters"]
+            iters[i] = self.solids[i].step()["iters"]
 
         t0 = time.perf_counter()
         with ThreadPoolExecutor(self.threads) as ex:
             list(ex.map(run, range(len(self.solids))))
-        return time.perf_counter() - t0, iters
-
-    def sample(self, cap):
-        w0, _ = self._region(0)
-        wc, iters = self._region(cap)
+        wall = time.perf_counter() - t0
         units = float(sum(sc.num_tets * it for sc, it in zip(self.scs, iters)))
-        return units, max(wc - w0, 1e-9)
+        return units, max(wall, 1e-9)
+
+
+def host_cpu():
+    """The host's CPU model and logical core count."""
+    model = None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                model = line.split(":", 1)[1].strip()
+                break
+    except (OSError, subprocess.TimeoutExpired):
+        pass
+    if not model:
+        import platform
+        model = platform.processor() or platform.machine()
+    return {"model": model, "nproc": os.cpu_count()}
+
+
+def cpu_configs_leg():
+    """The reference's CPU path on one thread (the reference steps one solid
+    on one thread), whole FixedSteps: C1 (the 160-tet cantilever, 120 steps),
+    C2 (the 60^3 block, its first step) and C5 (the 40^3 compressed cube, its
+    first step); tet.CG-iter/s and per-step latency."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+    from risdsdgcfem_thesis_gb300 import scenes
+    pyoracle.build(reference=False)
+    out = {"host": host_cpu(), "threads": 1, "kind": "port"}
+    for name, sc, steps in (("C1_cantilever", scenes.cantilever_160(), 120),
+                            ("C2_block60", scenes.large_block(n=60), 1),
+                            ("C5_compressed40", scenes.compressed_cube(40, 120, 0.4), 1)):
+        o = pyoracle.Solid(sc, "port")
+        ms, units = [], 0.0
+        for _ in range(steps):
+            t0 = time.perf_counter()
+            st = o.step()
+            ms.append(1e3 * (time.perf_counter() - t0))
+            units += sc.num_tets * st["iters"]
+        out[name] = {"tets": sc.num_tets, "steps": steps, "value": units / (1e-3 * sum(ms)), "unit": UNIT,
+                     "p50_step_ms": float(np.percentile(ms, 50)), "p99_step_ms": float(np.percentile(ms, 99)),
+                     "cg_iterations_per_step": units / sc.num_tets / steps}
+    return out
+
+
+def plain_fp64_c1_latency(steps=120):
+    """The plain FP64 drop-in (fem_solid_step, synchronous) on the C1
+    cantilever: per-step wall-clock latency. At 160 tets each CG iteration
+    is a handful of small kernels, so the step is launch-bound."""
+    from risdsdgcfem_thesis_gb300 import capi, scenes
+    sc = scenes.cantilever_160()
+    s = capi.Solid(sc, compute_energy=True)
+    s.step(3)
+    ms, units = [], 0.0
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        st = s.step(1)
+        ms.append(1e3 * (time.perf_counter() - t0))
+        units += sc.num_tets * st["cg_iterations"]
+    s.close()
+    return {"workload": f"{sc.name} ({sc.num_tets} tets), fem_solid_step, one step per call", "steps": steps,
+            "value": units / (1e-3 * sum(ms)), "unit": UNIT, "p50_step_ms": float(np.percentile(ms, 50)),
+            "p99_step_ms": float(np.percentile(ms, 99)), "cg_iterations_per_step": units / sc.num_tets / steps}
 
 
 def cpu_sample_set(scs, max_tets):
@@ -235,25 +291,27 @@ def run_reference(args):
     sample = cpu_sample_set(scs, 1_500_000)
     threads = (os.cpu_count() or 1) if len(sample) > 1 else 1
     sampler = CpuSampler(sample, threads)
-    cap = 40
-    total_units, total_s = 0.0, 0.0
+    total_units, step_s = 0.0, []
     for i in range(args.warmup + args.steps):
-        u, s = sampler.sample(cap if i >= args.warmup else 1)
+        u, t = sampler.sample()
         if i >= args.warmup:
             total_units += u
-            total_s += s
+            step_s.append(t)
+    total_s = sum(step_s)
     value = total_units / total_s
     cores = sampler.threads
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * total_s / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": describe(args.workload, scs, "reference CPU path, FP64")},
+        "p50_step_ms": float(1e3 * np.percentile(step_s, 50)), "p99_step_ms": float(1e3 * np.percentile(step_s, 99)),
+        "config": {"workload": describe(args.workload, scs, "reference CPU path, FP64"), "host": host_cpu()},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": f"each step = the CG iterations ({cap} per mesh) of the first FixedStep of "
-                                   f"{len(sample)} of the workload's meshes ({sum(s.num_tets for s in sample)} tets), "
-                                   f"one mesh per thread on {cores} threads; oracle restatement, bit-exact with the "
-                                   "reference's FP64 translation units"},
+                         "sample": f"each step = one whole FixedStep (rotations, forces, CG to each mesh's own "
+                                   f"tolerance, integration, energies) of {len(sample)} of the workload's meshes "
+                                   f"({sum(s.num_tets for s in sample)} tets), one mesh per thread on {cores} "
+                                   "threads; oracle restatement, bit-exact with the reference's FP64 translation "
+                                   "units"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -466,6 +524,8 @@ def run_ours(args):
     batch.close()
 
     plain = None
+    plain_c1 = None
+    cpu_configs = None
     accuracy = None
     fie = None
     rotations = None
@@ -488,6 +548,7 @@ def run_ours(args):
             served = served_leg(args.served_rate, args.served_seconds, pool_count=args.served_pool)
         if not args.no_plain:
             plain = plain_fp64_comparator(3)
+            plain_c1 = plain_fp64_c1_latency()
         if not args.no_fie:
             fie = fie_leg()
             rotations = rotation_leg()
@@ -497,15 +558,20 @@ def run_ours(args):
             sample = cpu_sample_set(scs, 1_500_000)
             threads = (os.cpu_count() or 1) if len(sample) > 1 else 1
             sampler = CpuSampler(sample, threads)
-            cap, u, s, reps = 40, 0.0, 0.0, 0
-            while s < 12.0 and reps < 60:  # about 12 s of CG work on the host cores
-                du, ds = sampler.sample(cap)
+            u, s, reps, step_s = 0.0, 0.0, 0, []
+            while s < 12.0 and reps < 20:  # about 12 s of whole steps on the host cores
+                du, ds = sampler.sample()
                 u, s, reps = u + du, s + ds, reps + 1
+                step_s.append(ds)
             cpu = {"value": u / s, "unit": UNIT, "cores": sampler.threads, "kind": "port",
-                   "sample": f"{reps} x the CG iterations ({cap} per mesh) of the first FixedStep of {len(sample)} "
-                             f"of the workload's meshes ({sum(x.num_tets for x in sample)} tets), one mesh per "
-                             f"thread on {sampler.threads} threads ({s:.1f} s of CG in total); oracle restatement, "
-                             "bit-exact with the reference's FP64 translation units"}
+                   "p50_step_ms": float(1e3 * np.percentile(step_s, 50)),
+                   "p99_step_ms": float(1e3 * np.percentile(step_s, 99)), "host": host_cpu(),
+                   "sample": f"{reps} whole FixedSteps (rotations, forces, CG to each mesh's own tolerance, "
+                             f"integration, energies) of {len(sample)} of the workload's meshes "
+                             f"({sum(x.num_tets for x in sample)} tets), one mesh per thread on {sampler.threads} "
+                             f"threads ({s:.1f} s in total); oracle restatement, bit-exact with the reference's "
+                             "FP64 translation units"}
+            cpu_configs = cpu_configs_leg()
 
     if rank == 0:
         elem_bytes = info["tets"] * (88 if precision == "mixed" else 176)
@@ -542,6 +608,8 @@ def run_ours(args):
                                            "iteration (16 + 20 s_e per tet + 33 s_v per node)"},
             "accuracy": accuracy,
             "plain_fp64_gpu": plain,
+            "plain_fp64_gpu_c1": plain_c1,
+            "cpu_single_thread": cpu_configs,
             "fie_fp64_gpu": fie,
             "rotations_fp64_gpu": rotations,
             "minres_fp64_gpu": minres,
