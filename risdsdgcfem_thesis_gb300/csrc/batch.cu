@@ -871,20 +871,19 @@ int fem_batch_finalize(fem_batch b)
                 const uint32_t w = (uint32_t)lc.x | ((uint32_t)lc.y << 8) | ((uint32_t)lc.z << 16) | ((uint32_t)lc.w << 24);
                 std::memcpy(base + blob_comp_off(20, i, ne4), &w, 4);
             }
-            double kb = 0.0;
-            for (uint32_t i = 0; i < tm.ne; i++) {
-                const size_t e = tm.e0 + i;
-                double Di[9];
-                for (uint32_t c = 0; c < 9; c++) Di[c] = Dinv_soa[c * T + e];
-                kb = std::max(kb, elem_out_bound(Di, mat_soa[T + e], mat_soa[2 * T + e]));
+            uint16_t* lp = reinterpret_cast<uint16_t*>(base + blob_lptr_off(tm.ne));
+            const uint16_t* src_lp = lptr.data() + lptr0[t];
+            for (uint32_t i = 0; i <= tm.nn; i++) lp[i] = src_lp[i];
+            uint16_t* li = lp + (tm.nn + 1);
+            for (uint32_t j = 0; j < 4u * tm.ne; j++) {
+                const uint16_t v = lidx[tm.c0 + j];  // (element << 2 | slot) -> slot * ne4 + element
+                li[j] = (uint16_t)((v & 3u) * ne4 + (v >> 2));
             }
-            uint32_t* hdr = reinterpret_cast<uint32_t*>(base + blob_hdr_off(tm.ne));
+            uint32_t* hdr = reinterpret_cast<uint32_t*>(base + blob_hdr_off(tm.ne, tm.nn));
             hdr[0] = tm.own0;
             std::memcpy(&hdr[1], &mcs[tm.mesh].fK_f, 4);
             std::memcpy(&hdr[2], &mcs[tm.mesh].mfm_f, 4);
-            const float kbf = (float)(kb * (1.0 + 1e-6));
-            std::memcpy(&hdr[3], &kbf, 4);
-            for (uint32_t i = tm.nown; i < tm.nn; i++) hdr[4 + i - tm.nown] = ov_map[tm.ov0 + i - tm.nown];
+            for (uint32_t i = tm.nown; i < tm.nn; i++) hdr[3 + i - tm.nown] = ov_map[tm.ov0 + i - tm.nown];
         }
     }
     std::vector<double> Rinit(9 * T, 0.0);

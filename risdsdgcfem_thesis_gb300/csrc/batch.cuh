@@ -31,8 +31,6 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
-#include <cmath>
-
 #include "fem_device.cuh"
 
 namespace femgb {
@@ -57,39 +55,24 @@ constexpr unsigned kDefaultWaitPolls = 1u << 22;
 // kernel) grouped by four: group g < 5 holds components 4g..4g+3 as
 // float4[ne4], component 20 follows as a word per element (one 16- or 4-byte
 // load per group and element, consecutive elements in consecutive words);
-// then the 16-byte header {uint32 own0, float fK, float m fM, float kb} (the
-// partial slot of the first owned node, the mesh's FP32 factors, and a bound
-// on any element output per unit of the tile's largest direction component,
-// elem_out_bound) and uint32 ovslot[nn - nown] (the partial slots of the
-// shared local nodes).
+// then uint16 lptr[nn+1], uint16 lidx[4 ne],
+// and, 4-aligned, the header {uint32 own0, float fK, float m fM} (the partial
+// slot of the first owned node, the mesh's FP32 factors) and uint32
+// ovslot[nn - nown] (the partial slots of the shared local nodes).
 __host__ __device__ constexpr uint32_t blob_ne4(uint32_t ne) { return (ne + 3u) & ~3u; }
 // Byte offset of component c of element i.
 __host__ __device__ constexpr uint32_t blob_comp_off(uint32_t c, uint32_t i, uint32_t ne4)
 {
     return c < 20u ? 16u * ((c >> 2) * ne4 + i) + 4u * (c & 3u) : 80u * ne4 + 4u * i;
 }
-__host__ __device__ constexpr uint32_t blob_hdr_off(uint32_t ne) { return 84u * blob_ne4(ne); }
+__host__ __device__ constexpr uint32_t blob_lptr_off(uint32_t ne) { return 84u * blob_ne4(ne); }
+__host__ __device__ constexpr uint32_t blob_hdr_off(uint32_t ne, uint32_t nn)
+{
+    return (blob_lptr_off(ne) + 2u * (nn + 1u) + 8u * ne + 3u) & ~3u;
+}
 __host__ __device__ constexpr uint32_t blob_bytes(uint32_t ne, uint32_t nn, uint32_t nown)
 {
-    return (blob_hdr_off(ne) + 16u + 4u * (nn - nown) + 15u) & ~15u;
-}
-
-// Bound on |(R K0 R^T d_e)_i| per unit of max |d_e| for an element with
-// Dm^-1 (row-major) and material V lambda, V mu: K0 is positive
-// semi-definite, so its largest eigenvalue is at most its trace,
-// tr K0 = V (lambda + 4 mu) sum_a |grad N_a|^2 (the rows of Dm^-1 and minus
-// their sum), and |K d_e|_inf <= tr K0 |d_e|_2 <= tr K0 sqrt(12) max|d_e|;
-// doubled to cover the FP32 rounding of the product.
-inline double elem_out_bound(const double* Dinv, double vlambda, double vmu)
-{
-    double g2 = 0.0, s[3] = {0.0, 0.0, 0.0};
-    for (int k = 0; k < 3; k++)
-        for (int j = 0; j < 3; j++) {
-            g2 += Dinv[3 * k + j] * Dinv[3 * k + j];
-            s[j] += Dinv[3 * k + j];
-        }
-    g2 += s[0] * s[0] + s[1] * s[1] + s[2] * s[2];
-    return 2.0 * 3.4641016151377544 * (std::fabs(vlambda) + 4.0 * std::fabs(vmu)) * g2;
+    return (blob_hdr_off(ne, nn) + 12u + 4u * (nn - nown) + 15u) & ~15u;
 }
 
 struct TileMeta {

@@ -212,26 +212,20 @@ __device__ __forceinline__ void finish_stats_t(StepScalars& s)
 
 }  // namespace
 
-// Shared memory of a block of the TILE-thread kernel: two blob stages, the
-// per-node fixed-point accumulators acc[3 nodes] (int64), the staged
-// direction sd4[nodes], two mbarriers, the warps' shares, the previous
-// tile's id and the largest direction component of each stage's tile.
-// TILE = 256: 54.7 KB, four resident blocks per SM; TILE = 128 (at most 120
-// local nodes): 27.4 KB, eight (with the 1 KB each block reserves, 219 of
-// the SM's 228 KB).
+// Shared memory of a block of the TILE-thread kernel: two blob stages (a
+// tile's element outputs overwrite its element data once every element has
+// read it), the staged direction sd4[nodes], two mbarriers and the warps'
+// shares and the previous tile's id. TILE = 256: 53.1 KB, four resident
+// blocks per SM; TILE = 128 (at most 120 local nodes): 26.4 KB, eight (with
+// the 1 KB each block reserves, 219 of the SM's 228 KB).
 template <int TILE>
 struct PipeShape {
     static constexpr uint32_t kNodes = TILE == kPipeSmallTile ? (uint32_t)kPipeSmallNodes : (uint32_t)kTileNodes;
     static constexpr uint32_t kStage = blob_bytes(TILE, kNodes, 0);  // a multiple of 16
-    static constexpr uint32_t kAcc = 2 * kStage;                      // int64 acc[3 kNodes]
-    static constexpr uint32_t kSd = kAcc + 24u * kNodes;              // float4 sd4[kNodes]
-    static constexpr uint32_t kBar = kSd + 16u * kNodes;
-    static constexpr uint32_t kSmem = kBar + 16u + 8u * (TILE / 32) + 16u;
+    static constexpr uint32_t kSmem = 2 * kStage + 16u * kNodes + 16u + 8u * (TILE / 32) + 16u;
     static constexpr int kMinBlocks = TILE == kPipeSmallTile ? 8 : 4;
 };
-static_assert(PipeShape<256>::kStage == 22544 && PipeShape<128>::kStage == 11248, "stage sizes");
-static_assert(PipeShape<256>::kSd % 16 == 0 && PipeShape<128>::kSd % 16 == 0, "sd4 alignment");
-static_assert(4 * (((PipeShape<256>::kSmem + 127) & ~127u) + 1024) <= 233472, "four blocks per SM");
+static_assert(PipeShape<256>::kStage == 25104 && PipeShape<128>::kStage == 12512, "stage sizes");
 static_assert(8 * (((PipeShape<128>::kSmem + 127) & ~127u) + 1024) <= 233472, "eight small blocks per SM");
 
 // What a block needs to know of one tile before its blob arrives.
@@ -278,18 +272,9 @@ __device__ __forceinline__ void look_resolve(const BatchView<float>& b, TileLook
                                    : 0u;
 }
 
-// Fixed-point scale of a tile's node sums. Every element output is at most
-// B = kb * dmax in magnitude (kb: the tile's bound per unit of direction,
-// elem_out_bound; dmax: its largest direction component) and a node has at
-// most 256 terms in a tile, so with 2^E, E = 180 - biased exponent of B
-// (clamped to the normal range), every term rounds to an integer of at most
-// 2^54 and a node's sum stays below 2^62. A term loses at most 2^-55 B to
-// the rounding; the integer sum is exact, so the order of the additions
-// does not matter, and the one rounding of the sum back to FP32 is correct.
-__device__ __forceinline__ int fixed_exponent(float kb, float dmax)
+__device__ __forceinline__ void fence_proxy_async_smem()
 {
-    const int eb = (int)((__float_as_uint(kb * dmax) >> 23) & 0xffu);
-    return min(max(180 - eb, -126), 126);
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
 
 template <int TILE>
@@ -300,18 +285,14 @@ __global__ void __launch_bounds__(TILE, PipeShape<TILE>::kMinBlocks) k_tile_spmv
                                                            const unsigned* __restrict__ refresh_flag,
                                                            unsigned* __restrict__ err)
 {
-    using Shape = PipeShape<TILE>;
-    constexpr uint32_t kStageBytes = Shape::kStage;
+    constexpr uint32_t kStageBytes = PipeShape<TILE>::kStage;
     extern __shared__ __align__(128) unsigned char smem[];
-    unsigned long long* acc = reinterpret_cast<unsigned long long*>(smem + Shape::kAcc);
-    float4* sd4 = reinterpret_cast<float4*>(smem + Shape::kSd);
-    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + Shape::kBar);
+    float4* sd4 = reinterpret_cast<float4*>(smem + 2 * kStageBytes);
+    uint64_t* bar = reinterpret_cast<uint64_t*>(sd4 + PipeShape<TILE>::kNodes);
     float2* wsh = reinterpret_cast<float2*>(bar + 2);  // [TILE / 32] per-warp shares
     // the previous tile whose share thread 0 stores after barrier A (only
     // thread 0 uses it); ~0u: none
     uint32_t& s_prev = *reinterpret_cast<uint32_t*>(wsh + TILE / 32);
-    // per stage: the largest |component| of its tile's direction (FP32 bits)
-    unsigned* s_dmax = reinterpret_cast<unsigned*>(wsh + TILE / 32) + 1;
     const uint32_t G = gridDim.x, tid = threadIdx.x;
     const uint32_t wait_polls = *(volatile const unsigned*)(err + 1);
 
@@ -320,22 +301,19 @@ __global__ void __launch_bounds__(TILE, PipeShape<TILE>::kMinBlocks) k_tile_spmv
         mbar_init(&bar[0], 1);
         mbar_init(&bar[1], 1);
         fence_mbar_init();
-        s_dmax[0] = s_dmax[1] = 0u;
     }
-    for (uint32_t k = tid; k < 3u * Shape::kNodes; k += TILE) acc[k] = 0ull;
     __syncthreads();
 
     // Software pipeline over this block's entries i, i+G, i+2G, ... of the
     // work list. Per tile (cur, in stage s):
     //   stage the direction of its nodes in sd4 (from registers gathered one
-    //   tile earlier) and their largest component | wait for its blob;
-    //   barrier A, which also ends every thread's reads of the other stage |
-    //   thread 0 stores the previous tile's d^T A d share and issues the copy
-    //   of the next tile's blob into the other stage | element products, each
-    //   output added to its node's fixed-point sum (shared-memory integer
-    //   atomics) | the metadata of the tile after next is resolved and this
-    //   thread's d and r of the next tile are gathered into registers |
-    //   barrier B | each node's sum back to FP32 into its partial slot.
+    //   tile earlier) | wait for its blob; barrier A, which also ends every
+    //   thread's reads of the other stage | thread 0 stores the previous
+    //   tile's d^T A d share and issues the copy of the next tile's blob into
+    //   the other stage | element products | the metadata of the tile after
+    //   next is resolved and this thread's d and r of the next tile are
+    //   gathered into registers | barrier B | outputs over the element data |
+    //   barrier C | node sums.
     const uint32_t n_act = *(volatile const uint32_t*)b.act_count;
     uint32_t i = blockIdx.x;
     TileLook cur, nxt, n2;
@@ -367,17 +345,13 @@ __global__ void __launch_bounds__(TILE, PipeShape<TILE>::kMinBlocks) k_tile_spmv
         const bool live = look_live(cur), nlive = look_live(nxt);
         const uint32_t ne = look_ne(cur), nn = look_nn(cur);
         float dd = 0.f;  // |d|^2 of this thread's node when the tile owns it
-        unsigned dm = 0u;  // max |component| of this thread's node (FP32 bits, ordered as unsigned)
         if (live && tid < nn) {
             const float dx = __fmaf_rn(cur.beta, cd0, cr0);
             const float dy = __fmaf_rn(cur.beta, cd1, cr1);
             const float dz = __fmaf_rn(cur.beta, cd2, cr2);
             sd4[tid] = make_float4(dx, dy, dz, 0.f);
             if (tid < look_nown(cur)) dd = dx * dx + dy * dy + dz * dz;
-            dm = __float_as_uint(fmaxf(fabsf(dx), fmaxf(fabsf(dy), fabsf(dz))));
         }
-        dm = __reduce_max_sync(0xffffffffu, dm);
-        if ((tid & 31u) == 0u && dm != 0u) atomicMax(&s_dmax[s], dm);
         // barrier A: every thread polls; the block agrees on the outcome so
         // the barriers below stay uniform
         const bool wait = live && !failed;
@@ -398,15 +372,13 @@ __global__ void __launch_bounds__(TILE, PipeShape<TILE>::kMinBlocks) k_tile_spmv
             }
             s_prev = live ? cur.tile : ~0u;
             if (!failed && nlive) issue(nxt, s ^ 1);
-            s_dmax[s ^ 1] = 0u;  // read by the previous tile before its barrier B
         }
         if (!failed && nlive) pending |= 1u << (s ^ 1);
         const bool work = live && !failed;
         const unsigned char* stage = smem + s * kStageBytes;
         const uint32_t ne4 = blob_ne4(ne);
-        const uint32_t* hdr = reinterpret_cast<const uint32_t*>(stage + blob_hdr_off(ne));
-        const float* fac = reinterpret_cast<const float*>(hdr + 1);  // fK, m fM, kb
-        const int fx = fixed_exponent(fac[2], __uint_as_float(s_dmax[s]));
+        const uint32_t* hdr = reinterpret_cast<const uint32_t*>(stage + blob_hdr_off(ne, nn));
+        const float* fac = reinterpret_cast<const float*>(hdr + 1);  // fK, m fM
         float share = 0.f;  // this thread's part of the tile's d^T A d
         if (work) share = fac[1] * dd;  // the nodes the tile owns
         float out[12];
@@ -434,13 +406,6 @@ __global__ void __launch_bounds__(TILE, PipeShape<TILE>::kMinBlocks) k_tile_spmv
 #pragma unroll
             for (int k = 0; k < 12; k++) eq = __fmaf_rn(dl[k], out[k], eq);
             share = __fmaf_rn(fac[0], eq, share);
-            // the outputs into the nodes' fixed-point sums
-            const float sc = __uint_as_float((uint32_t)(fx + 127) << 23);
-#pragma unroll
-            for (int k = 0; k < 4; k++)
-#pragma unroll
-                for (int c = 0; c < 3; c++)
-                    atomicAdd(acc + 3 * ids[k] + c, (unsigned long long)__float2ll_rn(out[3 * k + c] * sc));
         }
         // the tile after next: looked up here, after the element products,
         // so that its values do not occupy registers during them
@@ -453,19 +418,32 @@ __global__ void __launch_bounds__(TILE, PipeShape<TILE>::kMinBlocks) k_tile_spmv
             nr0 = __ldg(rvec + g); nr1 = __ldg(rvec + g + 1); nr2 = __ldg(rvec + g + 2);
         }
         if (work) {
-            __syncthreads();  // barrier B: every element output is in the sums
+            // barrier B: every element's data has been read; its space takes
+            // the outputs, so4[slot * ne4 + element]
+            __syncthreads();
+            float4* so4 = reinterpret_cast<float4*>(smem + s * kStageBytes);
+            if (tid < ne) {
+#pragma unroll
+                for (int k = 0; k < 4; k++)
+                    so4[k * ne4 + tid] = make_float4(out[3 * k], out[3 * k + 1], out[3 * k + 2], 0.f);
+                // these generic-proxy writes precede the next bulk copy into
+                // this stage (issued after a later barrier)
+                fence_proxy_async_smem();
+            }
+            __syncthreads();  // barrier C
             if (tid < nn) {
-                const float inv = __uint_as_float((uint32_t)(127 - fx) << 23);
-                unsigned long long* a = acc + 3 * tid;
-                const float a0 = (float)(long long)a[0] * inv;
-                const float a1 = (float)(long long)a[1] * inv;
-                const float a2 = (float)(long long)a[2] * inv;
-                a[0] = 0ull;
-                a[1] = 0ull;
-                a[2] = 0ull;
+                const uint16_t* lp = reinterpret_cast<const uint16_t*>(stage + blob_lptr_off(ne));
+                const uint16_t* li = lp + (nn + 1);
+                float a0 = 0.f, a1 = 0.f, a2 = 0.f;
+                for (int j = lp[tid]; j < lp[tid + 1]; j++) {
+                    const float4 v = so4[bounds_idx((uint32_t)li[j], 4u * ne4, kSiteTileEntry)];
+                    a0 += v.x;
+                    a1 += v.y;
+                    a2 += v.z;
+                }
                 const uint32_t nown = look_nown(cur);
                 const size_t o =
-                    3 * (size_t)bounds_idx(tid < nown ? hdr[0] + tid : hdr[4 + tid - nown], b.nslots, kSitePartialSlot);
+                    3 * (size_t)bounds_idx(tid < nown ? hdr[0] + tid : hdr[3 + tid - nown], b.nslots, kSitePartialSlot);
                 part[o] = a0;
                 part[o + 1] = a1;
                 part[o + 2] = a2;
