@@ -386,6 +386,13 @@ typedef struct fem_batch_options {
                              tile shares itself (one kernel fewer per CG iteration: shorter
                              iterations when few meshes run, more work when many do; the
                              same results either way) */
+    uint32_t persistent_loop; /* mixed, tile_elems > 128: 1 = the CG iterations of a launch run
+                             in one persistent cooperative kernel (the phases of an iteration
+                             separated by bounded grid barriers; the fused alpha) sized to the
+                             tiles of the meshes taking part, instead of four kernels per
+                             iteration in a CUDA graph: much shorter iterations for a few small
+                             meshes, the same results bit for bit. A grid barrier that gives up
+                             is reported as FEM_E_TIMEOUT. */
 } fem_batch_options;
 
 int fem_batch_options_default(fem_batch_options* o);
@@ -494,7 +501,7 @@ typedef struct fem_server_options {
     uint32_t fuse_alpha;         /* as fem_batch_options.fuse_alpha for the shards
                                     (default 0: measured 3 % shorter iterations for a
                                     lone request against 7 % less capacity) */
-    uint32_t pad;
+    uint32_t persistent_loop;    /* as fem_batch_options.persistent_loop for the shards */
 } fem_server_options;
 
 typedef struct fem_server_completion {

@@ -420,7 +420,8 @@ def device_info():
 # ---------------------------------------------------------------- batches
 class FemBatchOptions(C.Structure):
     _fields_ = [("precision", C.c_uint32), ("tile_elems", C.c_uint32), ("reorder", C.c_uint32),
-                ("use_graph", C.c_uint32), ("chunk_nodes", C.c_uint32), ("fuse_alpha", C.c_uint32)]
+                ("use_graph", C.c_uint32), ("chunk_nodes", C.c_uint32), ("fuse_alpha", C.c_uint32),
+                ("persistent_loop", C.c_uint32)]
 
 
 _u8p = C.POINTER(C.c_uint8)
@@ -434,7 +435,7 @@ def _bind_batch_signatures():
 class FemServerOptions(C.Structure):
     _fields_ = [("precision", C.c_uint32), ("shard_max_scenes", C.c_uint32), ("shard_max_tets", C.c_uint64),
                 ("hbm_budget_bytes", C.c_uint64), ("slice_iterations", C.c_uint32), ("chunk_nodes", C.c_uint32),
-                ("fuse_alpha", C.c_uint32), ("pad", C.c_uint32)]
+                ("fuse_alpha", C.c_uint32), ("persistent_loop", C.c_uint32)]
 
 
 class FemServerCompletion(C.Structure):
@@ -499,7 +500,7 @@ _BATCH_SIGNATURES = {
 
 
 def batch_options(precision=FEM_PRECISION_MIXED, tile_elems=256, reorder=True, use_graph=True, chunk_nodes=None,
-                  fuse_alpha=False):
+                  fuse_alpha=False, persistent_loop=False):
     o = FemBatchOptions()
     check(load().fem_batch_options_default(C.byref(o)))
     o.precision = precision
@@ -509,6 +510,7 @@ def batch_options(precision=FEM_PRECISION_MIXED, tile_elems=256, reorder=True, u
     if chunk_nodes is not None:
         o.chunk_nodes = chunk_nodes
     o.fuse_alpha = 1 if fuse_alpha else 0
+    o.persistent_loop = 1 if persistent_loop else 0
     return o
 
 
@@ -532,13 +534,13 @@ class Batch:
     def __init__(self, scenes_list, precision=FEM_PRECISION_MIXED, tile_elems=256, reorder=True, use_graph=True,
                  chunk_nodes=None,
                  compute_energy=True, refresh_every=None, degenerate_det_F=None, rotation_check=None,
-                 refresh_drop=None, rotation_fp32=None, fuse_alpha=False):
+                 refresh_drop=None, rotation_fp32=None, fuse_alpha=False, persistent_loop=False):
         lib = load()
         self.lib = lib
         self.scenes = list(scenes_list)
         self.precision = precision
         h = C.c_void_p()
-        opt = batch_options(precision, tile_elems, reorder, use_graph, chunk_nodes, fuse_alpha)
+        opt = batch_options(precision, tile_elems, reorder, use_graph, chunk_nodes, fuse_alpha, persistent_loop)
         check(lib.fem_batch_create(C.byref(opt), C.byref(h)))
         self.h = h
         self._knc = []
@@ -666,7 +668,7 @@ class Server:
 
     def __init__(self, precision=FEM_PRECISION_MIXED, hbm_budget_bytes=None, shard_max_tets=None,
                  shard_max_scenes=None, slice_iterations=None, completion_capacity=65536, chunk_nodes=None,
-                 fuse_alpha=None):
+                 fuse_alpha=None, persistent_loop=None):
         lib = load()
         self.lib = lib
         opt = FemServerOptions()
@@ -684,6 +686,8 @@ class Server:
             opt.chunk_nodes = int(chunk_nodes)
         if fuse_alpha is not None:
             opt.fuse_alpha = 1 if fuse_alpha else 0
+        if persistent_loop is not None:
+            opt.persistent_loop = 1 if persistent_loop else 0
         h = C.c_void_p()
         check(lib.fem_server_create(C.byref(opt), C.byref(h)))
         self.h = h

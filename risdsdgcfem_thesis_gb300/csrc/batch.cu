@@ -138,6 +138,7 @@ struct fem_batch_s {
     Dev<double> rest, x, v, bvec, y, part64, cpart, tpart, knc_target;
     Dev<unsigned char> r_s, d_s, q_s, part_s, ydelta_s;  // S-typed
     Dev<unsigned> counter, any_flag, refresh_flag, mcount, err;
+    Dev<unsigned> gbar;  // persistent loop: grid-barrier arrivals, generation, go flag
     Dev<unsigned char> blob;
     Dev<uint32_t> blob_off16;
     Dev<uint32_t> act_tiles, act_chunks, act_count;
@@ -222,7 +223,7 @@ struct fem_batch_s {
         knc_mesh.release(); lconn.release(); lptr.release(); lidx.release(); fixed.release(); rest.release();
         x.release(); v.release(); bvec.release(); y.release(); part64.release(); cpart.release(); tpart.release();
         knc_target.release(); r_s.release(); d_s.release(); q_s.release(); part_s.release(); ydelta_s.release(); counter.release();
-        any_flag.release(); refresh_flag.release(); mcount.release(); err.release(); blob.release();
+        any_flag.release(); refresh_flag.release(); mcount.release(); err.release(); gbar.release(); blob.release();
         blob_off16.release();
         act_tiles.release(); act_chunks.release(); act_count.release(); list_dirty.release(); slice.release();
         start_tiles.release(); start_chunks.release(); launch_tiles.release(); launch_chunks.release();
@@ -403,9 +404,28 @@ int enqueue_step(fem_batch B, cudaStream_t s, bool capture)
         bool any_start = B->mask_host.empty();
         for (uint8_t a : B->mask_host) any_start |= a == 1;
         if (any_start) start_section(s);
+        bool coop = false;
+        if constexpr (sizeof(S) == 4) {
+            if (B->opt.persistent_loop) {
+                // every iteration of this launch in one cooperative kernel,
+                // with about two tiles per block of the meshes taking part
+                uint64_t tiles = 0;
+                for (uint32_t m = 0; m < B->M; m++)
+                    if (B->mask_host.empty() || B->mask_host[m] != 0) tiles += B->mc_host[m].ntiles;
+                const uint32_t blocks = (uint32_t)std::min<uint64_t>(std::max<uint64_t>(1, (tiles + 1) / 2), 1u << 20);
+                CoopLoopArgs a;
+                a.d = d; a.r = r; a.part = part; a.tshare = reinterpret_cast<float2*>(B->tpart.p);
+                a.part64 = B->part64.p; a.bv = B->bvec.p; a.y = B->y.p;
+                a.cshare = reinterpret_cast<float2*>(B->cpart.p); a.err = B->err.p; a.gbar = B->gbar.p;
+                a.ls = lb;
+                a.ls.set_cond = 0;
+                BCK(launch_cg_coop(b, a, blocks, s));
+                coop = true;
+            }
+        }
         // host-driven loop: chunks of iterations, then read the per-mesh flags
         uint32_t budget = B->slice_budget, ran = 0;
-        for (;;) {
+        for (; !coop;) {
             BCK(cudaMemcpyAsync(B->st_host, B->st.p, sizeof(StepScalars) * B->M, cudaMemcpyDeviceToHost, s));
             BCK(cudaStreamSynchronize(s));
             bool any = false;
@@ -480,6 +500,8 @@ int fem_batch_create(const fem_batch_options* opt, fem_batch* out)
     if (o.chunk_nodes == 0) o.chunk_nodes = kChunkNodes;
     if (o.chunk_nodes < 32 || o.chunk_nodes > 8192)
         return batch_fail(FEM_E_ARG, "chunk_nodes must be in [32, 8192]");
+    if (o.persistent_loop && (o.precision != FEM_PRECISION_MIXED || o.tile_elems <= (uint32_t)kPipeSmallTile))
+        return batch_fail(FEM_E_ARG, "persistent_loop needs the mixed precision and tile_elems > %d", kPipeSmallTile);
     fem_batch b = new (std::nothrow) fem_batch_s;
     if (!b) return batch_fail(FEM_E_OOM, "host allocation failed");
     b->opt = o;
@@ -950,6 +972,7 @@ int fem_batch_finalize(fem_batch b)
     BCKC(b->refresh_flag.alloc(1));
     BCKC(b->mcount.alloc(b->M));
     BCKC(b->err.alloc(2));  // [0] error word, [1] poll limit of the tile-copy waits
+    BCKC(b->gbar.alloc(3));
     {
         const unsigned e0[2] = {0u, kDefaultWaitPolls};
         BCKC(cudaMemcpyAsync(b->err.p, e0, sizeof(e0), cudaMemcpyHostToDevice, s));
@@ -1280,7 +1303,7 @@ int fem_batch_step_async(fem_batch b, uint32_t nsteps)
 {
     if (int e = check_ready(b)) return e;
     for (uint32_t i = 0; i < nsteps; i++) {
-        if (b->exec && b->opt.use_graph) {
+        if (b->exec && b->opt.use_graph && !b->opt.persistent_loop) {
             BCK(cudaGraphLaunch(b->exec, b->stream));
             launch_counter() += 0;  // kernels inside the graph are counted at capture
         } else {
@@ -1303,7 +1326,8 @@ int fem_batch_synchronize(fem_batch b)
         // reported once: the next launches start with a clear word
         BCK(cudaMemsetAsync(b->err.p, 0, sizeof(unsigned), b->stream));
         BCK(cudaStreamSynchronize(b->stream));
-        return batch_fail(FEM_E_TIMEOUT, "a bounded wait for a tile copy gave up (code %u)", err);
+        return batch_fail(FEM_E_TIMEOUT, "a bounded device wait gave up (code %u: 1 tile copy, 2 copy drain, 3 grid "
+                                         "barrier)", err);
     }
     for (uint32_t m = 0; m < b->M; m++)
         if (b->st_host[m].status == FEM_E_NAN) return batch_fail(FEM_E_NAN, "NaN or Inf in the CG residual of mesh %u", m);

@@ -33,6 +33,7 @@
 #include "df.cuh"
 #include "elem_math.cuh"
 #include "msvd.cuh"
+#include "refresh_product.cuh"
 
 namespace femgb {
 
@@ -101,24 +102,6 @@ template <>
 __device__ __forceinline__ double chunk_sum<float>(float v) { return bblock_sum_f(v); }
 template <>
 __device__ __forceinline__ double chunk_sum<double>(double v) { return bblock_sum(v); }
-
-template <typename S>
-__device__ __forceinline__ bool mesh_running(const BatchView<S>& b, uint32_t m)
-{
-    return !b.st[m].done;
-}
-
-// The CG iterate: FP64 y plus, on the mixed path, the FP32 sum of this
-// step's alpha d increments (folded in at refresh and integration).
-template <typename S>
-__device__ __forceinline__ double y_full(const BatchView<S>& b, const double* __restrict__ y, size_t i)
-{
-    return b.ydelta ? y[i] + (double)b.ydelta[i] : y[i];
-}
-
-// Whether the mesh's next iteration recomputes its residual in FP64 (set by
-// the last block of the mesh in the node pass, see refresh_decide).
-__device__ __forceinline__ bool refresh_now(const MeshConsts&, const StepScalars& s) { return s.refresh_next != 0; }
 
 // ---------------------------------------------------------------------------
 // Element tile product of the new search direction: for each local node the
@@ -207,30 +190,6 @@ __global__ void __launch_bounds__(256) k_tile_spmv(BatchView<S> b, const S* __re
     }
 }
 
-// Product of the iterate y for the residual b - A y (same element data):
-// mode SPMV_Y64_ALL for every active mesh (initial residual of a step);
-// mode SPMV_Y64_REFRESH for meshes refreshing their residual this iteration,
-// and only when the finaliser raised the batch's refresh flag (otherwise the
-// launch returns at once). The FP64 path evaluates it in FP64. The mixed
-// path, whose element data is FP32, evaluates it in double-float arithmetic
-// (about 48 bits; FP64 would cost about 60 times the FP32 rate on this GPU)
-// and writes FP64 partial sums, so its residual is accurate to about 1e-14
-// of the magnitudes of the terms of A y.
-enum { SPMV_Y64_ALL = 0, SPMV_Y64_REFRESH = 1 };
-
-template <typename S>
-struct Y64Value {
-    using T = double;
-};
-template <>
-struct Y64Value<float> {
-    using T = DF;
-};
-__device__ __forceinline__ void y64_set(double& a, double v) { a = v; }
-__device__ __forceinline__ void y64_set(DF& a, double v) { a = df_from_double(v); }
-__device__ __forceinline__ double y64_get(double a) { return a; }
-__device__ __forceinline__ double y64_get(DF a) { return df_to_double(a); }
-
 template <typename S>
 __global__ void __launch_bounds__(256) k_tile_spmv_y64(BatchView<S> b, const double* __restrict__ y,
                                                        double* __restrict__ part64, int mode,
@@ -240,73 +199,7 @@ __global__ void __launch_bounds__(256) k_tile_spmv_y64(BatchView<S> b, const dou
     if (mode == SPMV_Y64_REFRESH && flag && !*flag) return;
     __shared__ V sd[3 * kTileNodes];
     __shared__ V so[12 * kTileElems];
-    // ALL: the meshes that start a step; REFRESH: the meshes that refresh in
-    // this iteration (their work list on the mixed path, or the CG list when
-    // all running meshes refresh)
-    const uint32_t rc = (mode == SPMV_Y64_REFRESH && b.refresh_tiles) ? b.list_count[4] : 0u;
-    const bool cg_list = rc == kRefreshUsesCgList;
-    const uint32_t* list = mode == SPMV_Y64_ALL ? b.start_tiles : (cg_list ? b.act_tiles : b.refresh_tiles);
-    const uint32_t n = mode == SPMV_Y64_ALL ? b.list_count[0]
-                       : !b.refresh_tiles ? b.ntiles
-                       : cg_list ? *(volatile const uint32_t*)b.act_count
-                                 : rc;
-    for (uint32_t i = blockIdx.x; i < n; i += gridDim.x) {
-        const uint32_t t = list_entry(list, i);
-        const TileMeta tm = b.tiles[t];
-        if (mode == SPMV_Y64_ALL && b.active[tm.mesh] != 1) continue;
-        if (mode == SPMV_Y64_REFRESH && (!mesh_running(b, tm.mesh) || !refresh_now(b.mc[tm.mesh], b.st[tm.mesh])))
-            continue;
-        const uint16_t* lp = b.lptr + b.lptr0[t];
-        const uint16_t* li = b.lidx + tm.c0;
-        for (int i = threadIdx.x; i < tm.nn; i += blockDim.x) {
-            const size_t g = bounds_idx(b.tile_nodes[tm.n0 + i], b.Ntot, kSiteBatchNode);
-            y64_set(sd[i], y_full(b, y, 3 * g));
-            y64_set(sd[kTileNodes + i], y_full(b, y, 3 * g + 1));
-            y64_set(sd[2 * kTileNodes + i], y_full(b, y, 3 * g + 2));
-        }
-        __syncthreads();
-        if (threadIdx.x < tm.ne) {
-            const size_t e = tm.e0 + threadIdx.x;
-            const size_t T = b.Ttot;
-            S R[9], Di[9];
-#pragma unroll
-            for (int c = 0; c < 9; c++) R[c] = b.R[c * T + e];
-#pragma unroll
-            for (int c = 0; c < 9; c++) Di[c] = b.Dinv[c * T + e];
-            const S k1 = b.mat[e], knu = b.mat[T + e], k2 = b.mat[2 * T + e];
-            const uchar4 lc = b.lconn[e];
-            const int ids[4] = {(int)bounds_idx((uint32_t)lc.x, tm.nn, kSiteLocalNode),
-                            (int)bounds_idx((uint32_t)lc.y, tm.nn, kSiteLocalNode),
-                            (int)bounds_idx((uint32_t)lc.z, tm.nn, kSiteLocalNode),
-                            (int)bounds_idx((uint32_t)lc.w, tm.nn, kSiteLocalNode)};
-            V dl[12];
-#pragma unroll
-            for (int i = 0; i < 4; i++) {
-                dl[3 * i] = sd[ids[i]];
-                dl[3 * i + 1] = sd[kTileNodes + ids[i]];
-                dl[3 * i + 2] = sd[2 * kTileNodes + ids[i]];
-            }
-            V out[12];
-            elem_RKRt<V, S>(R, Di, k1, knu, k2, dl, out);
-#pragma unroll
-            for (int c = 0; c < 12; c++) so[c * kTileElems + threadIdx.x] = out[c];
-        }
-        __syncthreads();
-        for (int i = threadIdx.x; i < tm.nn; i += blockDim.x) {
-            V a0{}, a1{}, a2{};
-            for (int j = lp[i]; j < lp[i + 1]; j++) {
-                const int v = li[j], el = v >> 2, sl = v & 3;
-                a0 = a0 + so[(3 * sl) * kTileElems + el];
-                a1 = a1 + so[(3 * sl + 1) * kTileElems + el];
-                a2 = a2 + so[(3 * sl + 2) * kTileElems + el];
-            }
-            const size_t o = 3 * tile_slot(b.ov_map, tm.own0, tm.ov0, tm.nown, i);
-            part64[o] = y64_get(a0);
-            part64[o + 1] = y64_get(a1);
-            part64[o + 2] = y64_get(a2);
-        }
-        __syncthreads();
-    }
+    tile_spmv_y64_pass<S>(b, y, part64, mode, sd, so, blockIdx.x, gridDim.x);
 }
 
 // Elastic product at positions x (FP64): part64 = R K0 (R^T x - r) per tile

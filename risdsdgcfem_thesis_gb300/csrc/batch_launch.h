@@ -36,6 +36,27 @@ void launch_node_update_fused(const BatchView<float>& b, const float* part, cons
                               const double* part64, const double* bv, double* y, float* r, float* d,
                               float2* cshare, const LoopSync& ls, cudaStream_t s);
 
+// Mixed path, the whole CG loop of a launch in one persistent cooperative
+// kernel (tile_pipe.cu): per iteration the tile product, the refresh product
+// when a mesh refreshes, the node pass with the fused alpha and the per-mesh
+// update, separated by grid barriers; it ends when no mesh runs, the slice
+// budget is spent or the error word is set. gbar: 3 device words.
+struct CoopLoopArgs {
+    float* d;
+    float* r;
+    float* part;
+    float2* tshare;
+    double* part64;
+    const double* bv;
+    double* y;
+    float2* cshare;
+    unsigned* err;
+    unsigned* gbar;
+    LoopSync ls;
+};
+// blocks: 0 = every block that fits the GPU; clamped to that.
+cudaError_t launch_cg_coop(const BatchView<float>& b, const CoopLoopArgs& a, uint32_t blocks, cudaStream_t s);
+
 template <typename S>
 struct BatchLaunch {
     static void begin_eval(const BatchView<S>& b, const double* x, cudaStream_t s);  // rotation.cu

@@ -154,6 +154,7 @@ int build_shard(fem_server srv, const std::vector<uint32_t>& ids, Shard& out)
     o.precision = srv->opt.precision;
     if (srv->opt.chunk_nodes) o.chunk_nodes = srv->opt.chunk_nodes;
     o.fuse_alpha = srv->opt.fuse_alpha;
+    o.persistent_loop = srv->opt.persistent_loop;
     fem_batch b = nullptr;
     if (int e = fem_batch_create(&o, &b)) return e;
     for (uint32_t k = 0; k < ids.size(); k++) {

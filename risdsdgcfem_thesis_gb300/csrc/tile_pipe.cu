@@ -61,6 +61,7 @@
 #include "batch_launch.h"
 #include "bounds.cuh"
 #include "elem_math.cuh"
+#include "refresh_product.cuh"
 
 namespace femgb {
 
@@ -272,37 +273,53 @@ __device__ __forceinline__ void look_resolve(const BatchView<float>& b, TileLook
                                    : 0u;
 }
 
+template <bool kCoherent>
+__device__ __forceinline__ float ld_dir(const float* p)
+{
+    return kCoherent ? __ldcg(p) : __ldg(p);
+}
+
 __device__ __forceinline__ void fence_proxy_async_smem()
 {
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
 
+// The block's two stage mbarriers (once per kernel; every thread calls it).
 template <int TILE>
-__global__ void __launch_bounds__(TILE, PipeShape<TILE>::kMinBlocks) k_tile_spmv_pipe(BatchView<float> b, const float* __restrict__ dvec,
-                                                           const float* __restrict__ rvec, float* __restrict__ part,
-                                                           float2* __restrict__ tshare,
-                                                           cudaGraphConditionalHandle if_refresh, int set_if,
-                                                           const unsigned* __restrict__ refresh_flag,
-                                                           unsigned* __restrict__ err)
+__device__ __forceinline__ void tile_pipe_init(unsigned char* smem)
+{
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + 2 * PipeShape<TILE>::kStage + 16u * PipeShape<TILE>::kNodes);
+    if (threadIdx.x == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+}
+
+// One pass of the tile product by this block over its entries block,
+// block + G, block + 2G, ... of the CG work list. `phase` carries the
+// parities of the block's two stage mbarriers from one pass to the next (a
+// persistent kernel runs a pass per CG iteration); every copy a pass issues
+// has completed (or, after a wait gave up, been drained) when it returns.
+// kCoherent: d and r are read through L2 (ld.global.cg) instead of the
+// read-only path, for a kernel whose other phases write them (the
+// persistent loop); the pointer parameters carry no __restrict__ for the
+// same reason (the kernels that call a pass alone have it on theirs).
+template <int TILE, bool kCoherent = false>
+__device__ __forceinline__ void tile_pipe_pass(const BatchView<float>& b, const float* dvec, const float* rvec,
+                                               float* part, float2* tshare, unsigned* err,
+                                               unsigned char* smem, uint32_t& phase, const uint32_t block,
+                                               const uint32_t G, const uint32_t wait_polls)
 {
     constexpr uint32_t kStageBytes = PipeShape<TILE>::kStage;
-    extern __shared__ __align__(128) unsigned char smem[];
     float4* sd4 = reinterpret_cast<float4*>(smem + 2 * kStageBytes);
     uint64_t* bar = reinterpret_cast<uint64_t*>(sd4 + PipeShape<TILE>::kNodes);
     float2* wsh = reinterpret_cast<float2*>(bar + 2);  // [TILE / 32] per-warp shares
     // the previous tile whose share thread 0 stores after barrier A (only
     // thread 0 uses it); ~0u: none
     uint32_t& s_prev = *reinterpret_cast<uint32_t*>(wsh + TILE / 32);
-    const uint32_t G = gridDim.x, tid = threadIdx.x;
-    const uint32_t wait_polls = *(volatile const unsigned*)(err + 1);
-
-    if (set_if && blockIdx.x == 0 && tid == 0) cudaGraphSetConditional(if_refresh, *refresh_flag ? 1u : 0u);
-    if (tid == 0) {
-        mbar_init(&bar[0], 1);
-        mbar_init(&bar[1], 1);
-        fence_mbar_init();
-    }
-    __syncthreads();
+    const uint32_t tid = threadIdx.x;
 
     // Software pipeline over this block's entries i, i+G, i+2G, ... of the
     // work list. Per tile (cur, in stage s):
@@ -315,13 +332,13 @@ __global__ void __launch_bounds__(TILE, PipeShape<TILE>::kMinBlocks) k_tile_spmv
     //   gathered into registers | barrier B | outputs over the element data |
     //   barrier C | node sums.
     const uint32_t n_act = *(volatile const uint32_t*)b.act_count;
-    uint32_t i = blockIdx.x;
+    uint32_t i = block;
     TileLook cur, nxt, n2;
     look_meta(b, i, n_act, cur);
     look_resolve(b, cur);
     look_meta(b, i + G, n_act, nxt);
     look_resolve(b, nxt);
-    uint32_t phase = 0u;    // bit s: parity of stage s's next completion
+    // phase, bit s: parity of stage s's next completion
     uint32_t pending = 0u;  // bit s: a copy into stage s is in flight
     int s = 0;
     bool failed = false;
@@ -336,8 +353,10 @@ __global__ void __launch_bounds__(TILE, PipeShape<TILE>::kMinBlocks) k_tile_spmv
         pending |= 1u;
         if (tid < look_nn(cur)) {
             const size_t g = 3 * (size_t)cur.g;
-            cd0 = __ldg(dvec + g); cd1 = __ldg(dvec + g + 1); cd2 = __ldg(dvec + g + 2);
-            cr0 = __ldg(rvec + g); cr1 = __ldg(rvec + g + 1); cr2 = __ldg(rvec + g + 2);
+            cd0 = ld_dir<kCoherent>(dvec + g); cd1 = ld_dir<kCoherent>(dvec + g + 1);
+            cd2 = ld_dir<kCoherent>(dvec + g + 2);
+            cr0 = ld_dir<kCoherent>(rvec + g); cr1 = ld_dir<kCoherent>(rvec + g + 1);
+            cr2 = ld_dir<kCoherent>(rvec + g + 2);
         }
     }
     if (tid == 0) s_prev = ~0u;
@@ -414,8 +433,10 @@ __global__ void __launch_bounds__(TILE, PipeShape<TILE>::kMinBlocks) k_tile_spmv
         float nd0 = 0.f, nd1 = 0.f, nd2 = 0.f, nr0 = 0.f, nr1 = 0.f, nr2 = 0.f;
         if (nlive && tid < look_nn(nxt)) {
             const size_t g = 3 * (size_t)nxt.g;
-            nd0 = __ldg(dvec + g); nd1 = __ldg(dvec + g + 1); nd2 = __ldg(dvec + g + 2);
-            nr0 = __ldg(rvec + g); nr1 = __ldg(rvec + g + 1); nr2 = __ldg(rvec + g + 2);
+            nd0 = ld_dir<kCoherent>(dvec + g); nd1 = ld_dir<kCoherent>(dvec + g + 1);
+            nd2 = ld_dir<kCoherent>(dvec + g + 2);
+            nr0 = ld_dir<kCoherent>(rvec + g); nr1 = ld_dir<kCoherent>(rvec + g + 1);
+            nr2 = ld_dir<kCoherent>(rvec + g + 2);
         }
         if (work) {
             // barrier B: every element's data has been read; its space takes
@@ -474,9 +495,29 @@ __global__ void __launch_bounds__(TILE, PipeShape<TILE>::kMinBlocks) k_tile_spmv
         // so no thread may leave while one is in flight)
         bool drained = true;
         for (int k = 0; k < 2; k++)
-            if ((pending >> k) & 1u) drained &= mbar_wait_bounded(&bar[k], (phase >> k) & 1u, kDrainPolls);
+            if ((pending >> k) & 1u) {
+                const bool ok = mbar_wait_bounded(&bar[k], (phase >> k) & 1u, kDrainPolls);
+                if (ok) phase ^= 1u << k;
+                drained &= ok;
+            }
         if (!drained) atomicExch(err, 2u);
     }
+}
+
+template <int TILE>
+__global__ void __launch_bounds__(TILE, PipeShape<TILE>::kMinBlocks) k_tile_spmv_pipe(BatchView<float> b, const float* __restrict__ dvec,
+                                                           const float* __restrict__ rvec, float* __restrict__ part,
+                                                           float2* __restrict__ tshare,
+                                                           cudaGraphConditionalHandle if_refresh, int set_if,
+                                                           const unsigned* __restrict__ refresh_flag,
+                                                           unsigned* __restrict__ err)
+{
+    extern __shared__ __align__(128) unsigned char smem[];
+    if (set_if && blockIdx.x == 0 && threadIdx.x == 0) cudaGraphSetConditional(if_refresh, *refresh_flag ? 1u : 0u);
+    tile_pipe_init<TILE>(smem);
+    uint32_t phase = 0u;
+    tile_pipe_pass<TILE>(b, dvec, rvec, part, tshare, err, smem, phase, blockIdx.x, gridDim.x,
+                         *(volatile const unsigned*)(err + 1));
 }
 
 // Per running mesh: d^T A d from its tiles' shares (fixed order), alpha and
@@ -526,18 +567,19 @@ __global__ void __launch_bounds__(256) k_mesh_alpha(BatchView<float> b, const fl
     }
 }
 
-__global__ void __launch_bounds__(256) k_node_update_fused(BatchView<float> b, const float* __restrict__ part,
-                                                           const double* __restrict__ part64,
-                                                           const double* __restrict__ bv,
-                                                           double* __restrict__ y, float* __restrict__ r,
-                                                           float* __restrict__ d, float2* __restrict__ cshare,
-                                                           const float2* __restrict__ tshare)
+// The node pass by this block over its entries block, block + G, ... of the
+// chunk work list (fuse: the block forms its mesh's alpha from the tile
+// shares itself).
+__device__ __forceinline__ void node_update_pass(const BatchView<float>& b, const float* part, const double* part64,
+                                                 const double* bv, double* y, float* r, float* d, float2* cshare,
+                                                 const float2* tshare,
+                                                 const uint32_t block, const uint32_t G, const bool fuse)
 {
     __shared__ float2 sh[32];
     __shared__ float s_alpha;
     __shared__ int s_brk;
     const uint32_t n_act = *(volatile const uint32_t*)(b.act_count + 1);
-    for (uint32_t ia = blockIdx.x; ia < n_act; ia += gridDim.x) {
+    for (uint32_t ia = block; ia < n_act; ia += G) {
         const uint32_t ci = b.act_chunks[ia];
         const ChunkMeta ch = b.chunks[ci];
         const StepScalars& sm = b.st[ch.mesh];
@@ -545,7 +587,7 @@ __global__ void __launch_bounds__(256) k_node_update_fused(BatchView<float> b, c
         const MeshConsts& c = b.mc[ch.mesh];
         bool brk;
         float alpha_s;
-        if (b.fuse_alpha) {
+        if (fuse) {
             // this block forms its mesh's alpha (warp 0, the same sum as
             // k_mesh_alpha); the block of the mesh's first chunk publishes it
             if (threadIdx.x < 32) {
@@ -651,17 +693,27 @@ __global__ void __launch_bounds__(256) k_node_update_fused(BatchView<float> b, c
     }
 }
 
+__global__ void __launch_bounds__(256) k_node_update_fused(BatchView<float> b, const float* __restrict__ part,
+                                                           const double* __restrict__ part64,
+                                                           const double* __restrict__ bv,
+                                                           double* __restrict__ y, float* __restrict__ r,
+                                                           float* __restrict__ d, float2* __restrict__ cshare,
+                                                           const float2* __restrict__ tshare)
+{
+    node_update_pass(b, part, part64, bv, y, r, d, cshare, tshare, blockIdx.x, gridDim.x, b.fuse_alpha != 0);
+}
+
 // Per running mesh, after the node pass: |r|^2 from its chunks' shares
 // (fixed order), then beta, the reliable-update and exit-confirmation rules
 // and the loop test (ILSS_CG.h:100-144). One warp per mesh; the last block
 // of the grid then rebuilds the work lists, sets the CUDA-graph while
 // condition and the refresh flag.
-__global__ void __launch_bounds__(256) k_mesh_update(BatchView<float> b, const float2* __restrict__ cshare, LoopSync ls)
+// Per running mesh (warp w of nw warps in all): the update above.
+__device__ __forceinline__ void mesh_update_pass(const BatchView<float>& b, const float2* cshare,
+                                                 const uint32_t w, const uint32_t nw)
 {
-    __shared__ unsigned s_last;
     const uint32_t lane = threadIdx.x & 31u;
-    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
-    for (uint32_t mesh = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; mesh < b.M; mesh += nw) {
+    for (uint32_t mesh = w; mesh < b.M; mesh += nw) {
         // the mesh's scalars, copied before the first branch and before the
         // shares are summed (one round trip for all of them), updated in
         // registers and written back once
@@ -747,12 +799,17 @@ __global__ void __launch_bounds__(256) k_mesh_update(BatchView<float> b, const f
                 }
             }
             b.st[mesh] = st;
-            __threadfence();  // the mesh's scalars before the grid arrival below
+            __threadfence();  // the mesh's scalars before the grid arrival that follows
         }
     }
-    // last block of the grid: work lists (when a mesh left its loop), while
-    // condition and refresh flag
-    if (!arrive_last_t(ls.gcount, gridDim.x, &s_last)) return;
+}
+
+// After every mesh's update, by one block (all its threads): work lists
+// (when a mesh left its loop), refresh flag, slice count, and whether the
+// loop goes on (the CUDA-graph while condition where there is one).
+__device__ __forceinline__ bool loop_control(const BatchView<float>& b, const LoopSync& ls)
+{
+    __shared__ unsigned s_go;
     // rebuild the CG lists once a quarter of their tiles belong to meshes that
     // have left their loop (the kernels skip those entries until then)
     if (4u * *(volatile const unsigned*)b.list_dirty >= *(volatile const uint32_t*)b.act_count) build_active_lists(b);
@@ -781,10 +838,181 @@ __global__ void __launch_bounds__(256) k_mesh_update(BatchView<float> b, const f
         if (ls.refresh_flag) *ls.refresh_flag = rf ? 1u : 0u;
         if (ls.body_runs) *ls.body_runs += 1u;
         if (ls.set_cond) cudaGraphSetConditional(ls.cond, (any && !stop && budget_left) ? 1u : 0u);
+        s_go = (any && !stop && budget_left) ? 1u : 0u;
     }
+    __syncthreads();
+    return s_go != 0u;
+}
+
+__global__ void __launch_bounds__(256) k_mesh_update(BatchView<float> b, const float2* __restrict__ cshare, LoopSync ls)
+{
+    __shared__ unsigned s_last;
+    mesh_update_pass(b, cshare, (blockIdx.x * blockDim.x + threadIdx.x) >> 5, (gridDim.x * blockDim.x) >> 5);
+    // last block of the grid: the loop control
+    if (!arrive_last_t(ls.gcount, gridDim.x, &s_last)) return;
+    (void)loop_control(b, ls);
 }
 
 // ---------------------------------------------------------------------------
+// The persistent form of the mixed CG loop: one cooperative launch runs the
+// iterations of a launch (up to the slice budget) with the four phases of an
+// iteration -- tile product, refresh product (when some mesh refreshes),
+// node pass with the fused alpha, per-mesh update -- separated by grid
+// barriers instead of kernel boundaries. It runs the same device code as the
+// kernels above, in the same order per value, so its results are the same
+// bits; what it saves is the launch and ramp of four kernels per iteration,
+// which dominate an iteration of a small batch (a lone scene of a served
+// shard).
+
+// Bounded polls of a grid barrier (each poll sleeps about 0.1 us): far above
+// any phase of an iteration.
+constexpr uint32_t kGridPolls = 1u << 22;
+
+// Grid barrier of a cooperative launch over G blocks: gbar[0] counts
+// arrivals (zeroed before the launch, never reset during it: generation g is
+// complete at G g arrivals) and gbar[1] holds the last completed generation.
+// The last block to arrive runs `last` (with all its threads) before it
+// releases the others. A wait that gives up sets err[0] = 3 and returns
+// false; the caller then leaves its loop.
+template <typename F>
+__device__ __forceinline__ bool grid_barrier(unsigned* gbar, uint32_t G, uint32_t& gen, unsigned* err, F&& last)
+{
+    __shared__ unsigned s_state;  // 1: this block arrived last; 2: gave up
+    __syncthreads();
+    gen++;
+    if (threadIdx.x == 0) {
+        __threadfence();
+        const unsigned prev = atomicAdd(&gbar[0], 1u);
+        s_state = (prev + 1u == G * gen) ? 1u : 0u;
+    }
+    __syncthreads();
+    const bool is_last = s_state == 1u;
+    if (is_last) {
+        last();
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            __threadfence();
+            atomicExch(&gbar[1], gen);
+        }
+    } else if (threadIdx.x == 0) {
+        uint32_t polls = 0;
+        while (*(volatile unsigned*)&gbar[1] < gen) {
+            if (++polls > kGridPolls) {
+                atomicExch(err, 3u);
+                s_state = 2u;
+                break;
+            }
+            __nanosleep(100);
+        }
+        __threadfence();
+    }
+    __syncthreads();
+    return s_state != 2u;
+}
+
+// The phases as separate functions: each gets the registers for itself
+// (inlined into one body they would share one allocation and spill).
+template <int TILE>
+__device__ __noinline__ void coop_tile_phase(const BatchView<float>& b, const CoopLoopArgs& a, unsigned char* smem,
+                                             uint32_t& phase, uint32_t blk, uint32_t G, uint32_t wait_polls)
+{
+    tile_pipe_pass<TILE, true>(b, a.d, a.r, a.part, a.tshare, a.err, smem, phase, blk, G, wait_polls);
+}
+__device__ __noinline__ void coop_refresh_phase(const BatchView<float>& b, const CoopLoopArgs& a, unsigned char* smem,
+                                                uint32_t blk, uint32_t G)
+{
+    // the product of y for the refreshing meshes, staged in the tile stages
+    // (the tile product of this iteration is done)
+    DF* sd = reinterpret_cast<DF*>(smem);
+    DF* so = sd + 3 * kTileNodes;
+    tile_spmv_y64_pass<float>(b, a.y, a.part64, SPMV_Y64_REFRESH, sd, so, blk, G);
+}
+__device__ __noinline__ void coop_node_phase(const BatchView<float>& b, const CoopLoopArgs& a, uint32_t blk,
+                                             uint32_t G)
+{
+    node_update_pass(b, a.part, a.part64, a.bv, a.y, a.r, a.d, a.cshare, a.tshare, blk, G, true);
+}
+__device__ __noinline__ void coop_mesh_phase(const BatchView<float>& b, const CoopLoopArgs& a, uint32_t warp,
+                                             uint32_t nwarps)
+{
+    mesh_update_pass(b, a.cshare, warp, nwarps);
+}
+__device__ __noinline__ void coop_loop_control(const BatchView<float>& b, const CoopLoopArgs& a)
+{
+    const bool go = loop_control(b, a.ls);
+    if (threadIdx.x == 0) a.gbar[2] = go ? 1u : 0u;
+}
+
+// Whether any mesh's CG loop runs (the start of a step may have ended them
+// all), by one block.
+__device__ __noinline__ void coop_any_running(const BatchView<float>& b, const CoopLoopArgs& a)
+{
+    int any = 0;
+    for (uint32_t m = threadIdx.x; m < b.M; m += blockDim.x) any |= (((volatile const StepScalars*)b.st) + m)->done ? 0 : 1;
+    any = __syncthreads_or(any);
+    if (threadIdx.x == 0) a.gbar[2] = any ? 1u : 0u;
+}
+
+template <int TILE>
+__global__ void __launch_bounds__(TILE, PipeShape<TILE>::kMinBlocks) k_cg_coop(BatchView<float> b, CoopLoopArgs a)
+{
+    extern __shared__ __align__(128) unsigned char smem[];
+    tile_pipe_init<TILE>(smem);
+    const uint32_t G = gridDim.x, blk = blockIdx.x;
+    const uint32_t wait_polls = *(volatile const unsigned*)(a.err + 1);
+    const uint32_t warp = (blk * blockDim.x + threadIdx.x) >> 5, nwarps = (G * blockDim.x) >> 5;
+    uint32_t phase = 0u, gen = 0u;
+    auto none = [] {};
+    if (!grid_barrier(a.gbar, G, gen, a.err, [&] { coop_any_running(b, a); })) return;
+    while (*(volatile const unsigned*)&a.gbar[2]) {
+        coop_tile_phase<TILE>(b, a, smem, phase, blk, G, wait_polls);
+        if (!grid_barrier(a.gbar, G, gen, a.err, none)) return;
+        if (*(volatile const unsigned*)a.ls.refresh_flag) {
+            coop_refresh_phase(b, a, smem, blk, G);
+            if (!grid_barrier(a.gbar, G, gen, a.err, none)) return;
+        }
+        coop_node_phase(b, a, blk, G);
+        if (!grid_barrier(a.gbar, G, gen, a.err, none)) return;
+        coop_mesh_phase(b, a, warp, nwarps);
+        if (!grid_barrier(a.gbar, G, gen, a.err, [&] { coop_loop_control(b, a); })) return;
+    }
+}
+static_assert(sizeof(DF) * (3 * kTileNodes + 12 * kTileElems) <= PipeShape<kTileElems>::kSmem,
+              "refresh staging fits the tile stages");
+
+template <int TILE>
+static int coop_max_blocks()
+{
+    static int grid = 0;
+    if (!grid) {
+        int dev = 0, sms = 0, per_sm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaFuncSetAttribute(k_cg_coop<TILE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)PipeShape<TILE>::kSmem);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cg_coop<TILE>, TILE, PipeShape<TILE>::kSmem);
+        grid = (sms > 0 ? sms : 1) * (per_sm > 0 ? per_sm : 1);
+    }
+    return grid;
+}
+
+cudaError_t launch_cg_coop(const BatchView<float>& b, const CoopLoopArgs& a, uint32_t blocks, cudaStream_t s)
+{
+    // refresh staging is sized for 256-thread blocks
+    if (b.pipe_tile == (uint32_t)kPipeSmallTile) return cudaErrorInvalidValue;
+    const uint32_t maxg = (uint32_t)coop_max_blocks<kTileElems>();
+    const uint32_t grid = blocks == 0 ? maxg : (blocks < maxg ? blocks : maxg);
+    cudaError_t e = cudaMemsetAsync(a.gbar, 0, 3 * sizeof(unsigned), s);
+    if (e != cudaSuccess) return e;
+    BatchView<float> bv = b;
+    CoopLoopArgs av = a;
+    void* args[] = {&bv, &av};
+    prof_begin("cg_coop", s);
+    e = cudaLaunchCooperativeKernel((const void*)k_cg_coop<kTileElems>, dim3(grid), dim3(kTileElems), args,
+                                    PipeShape<kTileElems>::kSmem, s);
+    prof_end("cg_coop", s);
+    launch_counter()++;
+    return e;
+}
 
 uint32_t tile_pipe_smem_bytes() { return PipeShape<256>::kSmem; }
 
