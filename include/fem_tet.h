@@ -593,6 +593,47 @@ int fem_tetgen_read(const char* node_path, const char* ele_path, double natural_
                     uint32_t max_nodes, uint32_t* tets, uint32_t max_tets, uint32_t* num_nodes,
                     uint32_t* num_tets, uint32_t* num_dropped);
 
+/* --- Tet-solid shapes (Geo/shape/TetSolidShape3.{h,cpp}) and shape files --- */
+/* EditableTetSolidShape3::EndEdition's rebuild (TetSolidShape3.cpp:558-845)
+ * of a mesh, which fixes the vertex and tet order a reference solid built
+ * from the shape uses (LeafDSH_Solid3D_FEM.cpp:158-168): vertices no tet
+ * uses are removed (the rest keep their order); each tet's neighbour across
+ * the face opposite each of its vertices (~0u on the boundary); one
+ * boundary face per unmatched face, oriented outwards (sign test in float);
+ * vertex layers by distance from the boundary, tet layer = its lowest
+ * vertex layer, tets reordered by layer (stable). Outputs (each may be
+ * null): out_rest (num_nodes*3, the kept positions), out_tets (T*4, layer
+ * order, new node ids), out_neighbors (T*4), out_tet_of (T: the input tet of
+ * each output tet), out_node_of (num_nodes: the input node of each output
+ * node), out_bfaces (num_bfaces*3, up to max_bfaces; at most 4 T),
+ * out_layers ((first, count) pairs, up to max_layers; at most T + 1).
+ * Positions are compared as float, as the reference's float shapes hold
+ * them. FEM_E_INDEX for an id >= N. Host only. */
+int fem_tetshape_rebuild(const double* rest, uint32_t N, const uint32_t* tets, uint32_t T, double* out_rest,
+                         uint32_t* out_num_nodes, uint32_t* out_tets, uint32_t* out_neighbors, uint32_t* out_tet_of,
+                         uint32_t* out_node_of, uint32_t* out_bfaces, uint32_t max_bfaces, uint32_t* out_num_bfaces,
+                         uint32_t* out_layers, uint32_t max_layers, uint32_t* out_num_layers);
+/* The shape file examples/tetgen2geo/main.cpp writes
+ * (ShapeLibrary::Register_TetSolidShape3 + Save(path, text),
+ * Geo/shape/ShapeLibrary.cpp:332-360, util/ItemStreamSerialization.cpp:14-182)
+ * for a mesh: the shape after fem_tetshape_rebuild, positions as float, one
+ * complex item "#1" with shape_type 21 (eShape_TetSolid3), version 3, the
+ * counts and the baked arrays as hex bytes. At most 65534 nodes and tets
+ * (the shape's uint16 ids): FEM_E_ARG above. Host only. */
+int fem_geo_write(const char* path, const double* rest, uint32_t N, const uint32_t* tets, uint32_t T);
+/* Reads the first tet-solid shape of a shape file (ShapeFactory's
+ * eShape_TetSolid3 case, Geo/shape/ShapeFactory.cpp:188-201): its vertices
+ * (float values as double) and tets (the shape's order, ready for
+ * fem_solid_create) and neighbours (~0u = none). Call with null arrays to
+ * get the counts. FEM_E_ARG for a missing or malformed file, a version other
+ * than 3 or arrays that do not match the counts; FEM_E_INDEX for a vertex id
+ * >= num_nodes. Host only. */
+int fem_geo_read(const char* path, double* rest, uint32_t max_nodes, uint32_t* tets, uint32_t max_tets,
+                 uint32_t* neighbors, uint32_t* num_nodes, uint32_t* num_tets);
+/* The converter as a whole (examples/tetgen2geo/main.cpp with -nsac when
+ * natural_scale > 0): fem_tetgen_read, then fem_geo_write. Host only. */
+int fem_tetgen_to_geo(const char* node_path, const char* ele_path, double natural_scale, const char* geo_path);
+
 #ifdef __cplusplus
 }
 #endif

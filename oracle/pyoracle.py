@@ -26,6 +26,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_SO = os.path.join(HERE, "_build", "libfemoracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libfemref.so")
 REF_DBL_SO = os.path.join(HERE, "_ref", "libfemref_dbl.so")
+GEO_REF_SO = os.path.join(HERE, "_ref", "libgeoref.so")
 # The reference tree (read only to build the checker): REFERENCE_ROOT from
 # the environment, the same variable oracle/Makefile reads.
 REFERENCE_ROOT = os.environ.get("REFERENCE_ROOT", "/root/reference")
@@ -44,6 +45,19 @@ def build(reference: bool = False) -> None:
     subprocess.check_call(["make", "-s", "-C", HERE, "all"])
     if reference and os.path.isdir(REFERENCE_SRC):
         subprocess.check_call(["make", "-s", "-C", HERE, "ref", f"REF={REFERENCE_ROOT}"])
+
+
+def geo_ref_convert(pos, tets, natural_scale, out_path):
+    """The reference's TetGen converter path on (float positions, tets as
+    read from the files): its EditableTetSolidShape3 and shape library
+    (oracle/geo_harness.cpp) write out_path. Returns the harness status."""
+    lib = C.CDLL(GEO_REF_SO)
+    lib.geo_ref_convert.argtypes = [C.POINTER(C.c_float), C.c_uint32, _up, C.c_uint32, C.c_float, C.c_char_p]
+    lib.geo_ref_convert.restype = C.c_int
+    pos = np.ascontiguousarray(pos, dtype=np.float32)
+    tets = np.ascontiguousarray(tets, dtype=np.uint32)
+    return lib.geo_ref_convert(pos.ctypes.data_as(C.POINTER(C.c_float)), pos.shape[0], _ptr(tets, C.c_uint32),
+                               tets.shape[0], natural_scale, out_path.encode())
 
 
 def _ptr(a, ctype=C.c_double):

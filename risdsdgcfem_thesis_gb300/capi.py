@@ -121,6 +121,11 @@ SIGNATURES = {
     "fem_solid_get_doc": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint8)]),
     "fem_tetgen_read": (C.c_int, [C.c_char_p, C.c_char_p, C.c_double, _dp, C.c_uint32, _up, C.c_uint32, _up, _up,
                                   _up]),
+    "fem_tetshape_rebuild": (C.c_int, [_dp, C.c_uint32, _up, C.c_uint32, _dp, _up, _up, _up, _up, _up, _up,
+                                       C.c_uint32, _up, _up, C.c_uint32, _up]),
+    "fem_geo_write": (C.c_int, [C.c_char_p, _dp, C.c_uint32, _up, C.c_uint32]),
+    "fem_geo_read": (C.c_int, [C.c_char_p, _dp, C.c_uint32, _up, C.c_uint32, _up, _up, _up]),
+    "fem_tetgen_to_geo": (C.c_int, [C.c_char_p, C.c_char_p, C.c_double, C.c_char_p]),
     "fem_solid_force_elastic": (C.c_int, [C.c_void_p, _dp]),
     "fem_solid_df_x": (C.c_int, [C.c_void_p, _dp, _dp]),
     "fem_solid_apply_A": (C.c_int, [C.c_void_p, C.c_double, C.c_double, _dp, _dp]),
@@ -387,6 +392,58 @@ def read_tetgen(node_path: str, ele_path: str, natural_scale: float = 0.0):
     check(lib.fem_tetgen_read(np_, ep, natural_scale, _ptr(rest), n.value, _ptr(tets, C.c_uint32), t.value,
                               C.byref(n), C.byref(t), C.byref(dropped)))
     return rest, tets, int(dropped.value)
+
+
+def tetshape_rebuild(rest, tets):
+    """fem_tetshape_rebuild: the tet-solid shape's rebuild of a mesh, as a
+    dict of rest (V, 3), tets (T, 4), neighbors (T, 4; 0xFFFFFFFF = none),
+    tet_of (T), node_of (V), bfaces (B, 3), layers (L, 2)."""
+    lib = load()
+    rest = _f64(rest)
+    tets = np.ascontiguousarray(tets, dtype=np.uint32)
+    N, T = rest.shape[0], tets.shape[0]
+    out_rest = np.empty((N, 3))
+    out_tets = np.empty((T, 4), np.uint32)
+    nb = np.empty((T, 4), np.uint32)
+    tet_of = np.empty(T, np.uint32)
+    node_of = np.empty(N, np.uint32)
+    bf = np.empty((4 * T, 3), np.uint32)
+    layers = np.empty((T + 1, 2), np.uint32)
+    V, B, L = C.c_uint32(), C.c_uint32(), C.c_uint32()
+    check(lib.fem_tetshape_rebuild(_ptr(rest), N, _ptr(tets, C.c_uint32), T, _ptr(out_rest), C.byref(V),
+                                   _ptr(out_tets, C.c_uint32), _ptr(nb, C.c_uint32), _ptr(tet_of, C.c_uint32),
+                                   _ptr(node_of, C.c_uint32), _ptr(bf, C.c_uint32), 4 * T, C.byref(B),
+                                   _ptr(layers, C.c_uint32), T + 1, C.byref(L)))
+    return {"rest": out_rest[:V.value], "tets": out_tets, "neighbors": nb, "tet_of": tet_of,
+            "node_of": node_of[:V.value], "bfaces": bf[:B.value], "layers": layers[:L.value]}
+
+
+def geo_write(path: str, rest, tets) -> None:
+    """fem_geo_write: the mesh's tet-solid shape file (.geo)."""
+    rest = _f64(rest)
+    tets = np.ascontiguousarray(tets, dtype=np.uint32)
+    check(load().fem_geo_write(path.encode(), _ptr(rest), rest.shape[0], _ptr(tets, C.c_uint32), tets.shape[0]))
+
+
+def geo_read(path: str):
+    """fem_geo_read: (rest (V, 3), tets (T, 4), neighbors (T, 4)) of the
+    file's tet-solid shape."""
+    lib = load()
+    V, T = C.c_uint32(), C.c_uint32()
+    check(lib.fem_geo_read(path.encode(), None, 0, None, 0, None, C.byref(V), C.byref(T)))
+    rest = np.empty((V.value, 3))
+    tets = np.empty((T.value, 4), np.uint32)
+    nb = np.empty((T.value, 4), np.uint32)
+    check(lib.fem_geo_read(path.encode(), _ptr(rest), V.value, _ptr(tets, C.c_uint32), T.value,
+                           _ptr(nb, C.c_uint32), C.byref(V), C.byref(T)))
+    return rest, tets, nb
+
+
+def tetgen_to_geo(base_path: str, geo_path: str, natural_scale: float = 0.0) -> None:
+    """fem_tetgen_to_geo: base_path.node / base_path.ele to a shape file, as
+    the reference's converter does."""
+    check(load().fem_tetgen_to_geo((base_path + ".node").encode(), (base_path + ".ele").encode(), natural_scale,
+                                   geo_path.encode()))
 
 
 def profile_enable(on: bool = True) -> None:

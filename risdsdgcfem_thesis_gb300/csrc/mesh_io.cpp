@@ -15,9 +15,8 @@
 //   merged node by node as GAABB::Merge does (Geo/bv/GAABB.h:27-50), then
 //   positions moved by -center and scaled by s / max(2 half_sizes).
 // The .face file is not read (the converter reads it but no longer uses it).
-// Not reproduced: EditableTetSolidShape3::EndEdition's topology rebuild
-// (boundary faces, vertex splitting at non-manifold vertices, layers) and the
-// ItemStream shape-library file the converter writes.
+// The shape the converter then builds (EndEdition's rebuild) and the
+// shape-library file it writes are in shape_io.cpp.
 #include "../../include/fem_tet.h"
 
 #include <cctype>

@@ -225,6 +225,21 @@ def sheared_crush(n: int = 4, steps: int = 30, ratio: float = 0.15, shear: float
                  knc_schedule=schedule, grid=(n, n, n), h=h, rotation=rotation)
 
 
+def from_geo(path: str, fixed_below: Optional[float] = None, **scene_kwargs) -> Scene:
+    """A Scene from the tet-solid shape of a shape file (.geo, as the
+    reference's TetGen converter writes it), read by fem_geo_read: the
+    shape's float vertices and its tets in the shape's order, the order in
+    which a reference solid adds them to its element set.
+    fixed_below: nodes with z <= this become fixed position constraints."""
+    from . import capi
+    rest, tets, _ = capi.geo_read(path)
+    knc = np.zeros(0, np.uint32)
+    if fixed_below is not None:
+        knc = np.nonzero(rest[:, 2] <= fixed_below)[0].astype(np.uint32)
+    name = scene_kwargs.pop("name", "geo_" + path.rsplit("/", 1)[-1])
+    return Scene(name=name, rest=rest, tets=tets, knc_nodes=knc, knc_targets=rest[knc].copy(), **scene_kwargs)
+
+
 def random_block(rng: np.random.Generator, lo: int = 4, hi: int = 30, idx: int = 0,
                  dims=None) -> Scene:
     """One mesh of the batched workload: a x b x c cubes (uniform in [lo, hi]),
