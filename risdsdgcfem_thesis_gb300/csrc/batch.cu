@@ -419,7 +419,10 @@ int enqueue_step(fem_batch B, cudaStream_t s, bool capture)
                 a.cshare = reinterpret_cast<float2*>(B->cpart.p); a.err = B->err.p; a.gbar = B->gbar.p;
                 a.ls = lb;
                 a.ls.set_cond = 0;
-                BCK(launch_cg_coop(b, a, blocks, s));
+                if (tiles <= cg_resident_capacity(B->M))
+                    BCK(launch_cg_resident(b, a, (uint32_t)tiles, s));
+                else
+                    BCK(launch_cg_coop(b, a, blocks, s));
                 coop = true;
             }
         }

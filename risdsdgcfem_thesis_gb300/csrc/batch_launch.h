@@ -56,6 +56,12 @@ struct CoopLoopArgs {
 };
 // blocks: 0 = every block that fits the GPU; clamped to that.
 cudaError_t launch_cg_coop(const BatchView<float>& b, const CoopLoopArgs& a, uint32_t blocks, cudaStream_t s);
+// The resident-tile form (each block keeps up to two tiles' element data in
+// shared memory for the whole launch): usable while the running tiles number
+// at most cg_resident_capacity(meshes) (0 when the batch has too many meshes
+// for its per-mesh control list); `tiles` bounds the running tiles.
+uint32_t cg_resident_capacity(uint32_t meshes);
+cudaError_t launch_cg_resident(const BatchView<float>& b, const CoopLoopArgs& a, uint32_t tiles, cudaStream_t s);
 
 template <typename S>
 struct BatchLaunch {

@@ -163,6 +163,27 @@ __device__ __forceinline__ F2 warp_sum_f2(F2 v)
     return v;
 }
 
+// This lane's part of a lane-strided sum of n (hi, lo) shares: k = lane,
+// lane + 32, ... added in that order, the loads of each round of eight
+// issued together (a mesh with hundreds of tiles would otherwise wait on a
+// chain of dependent global loads).
+__device__ __forceinline__ F2 lane_share_sum(const float2* p, uint32_t n, uint32_t lane)
+{
+    F2 a = {0.f, 0.f};
+    for (uint32_t k0 = lane; k0 < n; k0 += 256u) {
+        float2 w[8];
+#pragma unroll
+        for (int i = 0; i < 8; i++) {
+            const uint32_t k = k0 + 32u * i;
+            w[i] = k < n ? __ldcg(p + k) : make_float2(0.f, 0.f);
+        }
+#pragma unroll
+        for (int i = 0; i < 8; i++)
+            if (k0 + 32u * i < n) a = f2_add(a, F2{w[i].x, w[i].y});
+    }
+    return a;
+}
+
 // Block sum, result valid in thread 0; every thread must call it.
 __device__ __forceinline__ F2 block_sum_f2(F2 v, float2* sh)
 {
@@ -540,11 +561,7 @@ __device__ __forceinline__ MeshAlpha warp_mesh_alpha(const BatchView<float>& b, 
     const uint32_t tile0 = b.mc[m].tile0, ntiles = b.mc[m].ntiles;
     const bool confirm = st.confirm != 0;  // measure the FP64 residual only, no CG update
     const double abs_eps_sq = st.abs_eps_sq, delta_new = st.delta_new;
-    F2 a = {0.f, 0.f};
-    for (uint32_t k = lane; k < ntiles; k += 32u) {
-        const float2 w = __ldcg(tshare + tile0 + k);
-        a = f2_add(a, F2{w.x, w.y});
-    }
+    F2 a = lane_share_sum(tshare + tile0, ntiles, lane);
     a = warp_sum_f2(a);
     MeshAlpha r;
     r.dq = (double)a.hi + (double)a.lo;
@@ -567,129 +584,138 @@ __global__ void __launch_bounds__(256) k_mesh_alpha(BatchView<float> b, const fl
     }
 }
 
+// The node pass of chunk ci (every thread of the block calls it; fuse: the
+// block forms its mesh's alpha from the tile shares itself).
+__device__ __forceinline__ void node_update_chunk(const BatchView<float>& b, const float* part, const double* part64,
+                                                  const double* bv, double* y, float* r, float* d, float2* cshare,
+                                                  const float2* tshare, const uint32_t ci, const ChunkMeta& ch,
+                                                  const bool fuse)
+{
+    __shared__ float2 sh[32];
+    __shared__ float s_alpha;
+    __shared__ int s_brk;
+    const StepScalars& sm = b.st[ch.mesh];
+    if (sm.done) return;  // left its loop; the list is rebuilt lazily
+    const MeshConsts& c = b.mc[ch.mesh];
+    bool brk;
+    float alpha_s;
+    if (fuse) {
+        // this block forms its mesh's alpha (warp 0, the same sum as
+        // k_mesh_alpha); the block of the mesh's first chunk publishes it
+        if (threadIdx.x < 32) {
+            const MeshAlpha ma = warp_mesh_alpha(b, tshare, ch.mesh, ci == c.chunk0);
+            if (threadIdx.x == 0) {
+                s_alpha = ma.alpha;
+                s_brk = ma.brk ? 1 : 0;
+            }
+        }
+        __syncthreads();
+        brk = s_brk != 0;
+        alpha_s = s_alpha;
+    } else {
+        brk = sm.brk != 0;
+        alpha_s = sm.alpha_f;
+    }
+    const bool confirm = sm.confirm != 0;
+    const bool refresh = sm.refresh_next != 0;
+    const float beta = sm.beta_f;
+    const float na = -alpha_s;
+    const float fK = c.fK_f, mfm = c.mfm_f;
+    float acc = 0.f;
+    for (size_t n = ch.n0 + threadIdx.x; !brk && n < ch.n1; n += blockDim.x) {
+        const size_t i = 3 * n;
+        // every load is issued before the constraint flag is known; a
+        // constrained row keeps d, r zero and y unchanged
+        const bool fixed = b.fixed[n] != 0;
+        const float d0 = __fmaf_rn(beta, d[i], r[i]);
+        const float d1 = __fmaf_rn(beta, d[i + 1], r[i + 1]);
+        const float d2 = __fmaf_rn(beta, d[i + 2], r[i + 2]);
+        // the owner tile's partial (node order), then the overflow slots
+        // (contiguous, tile order)
+        float s0 = part[i], s1 = part[i + 1], s2 = part[i + 2];
+        const uint32_t j0 = b.ov_ptr[n];
+        const uint32_t j1 = bounds_idx(b.ov_ptr[n + 1], b.nslots - b.Ntot + 1, kSitePartialSlot);
+        float r0 = r[i], r1 = r[i + 1], r2 = r[i + 2];
+        float e0 = b.ydelta[i], e1 = b.ydelta[i + 1], e2 = b.ydelta[i + 2];
+        // the first four overflow partials are loaded together, then
+        // added in slot order (the rare rest one by one)
+        float p[4][3];
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            const bool in = j0 + k < j1;
+            const size_t o = 3 * ((size_t)b.Ntot + (in ? j0 + k : 0u));
+            p[k][0] = in ? part[o] : 0.f;
+            p[k][1] = in ? part[o + 1] : 0.f;
+            p[k][2] = in ? part[o + 2] : 0.f;
+        }
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            if (j0 + k < j1) {
+                s0 += p[k][0];
+                s1 += p[k][1];
+                s2 += p[k][2];
+            }
+        }
+        for (uint32_t j = j0 + 4; j < j1; j++) {
+            const size_t o = 3 * ((size_t)b.Ntot + j);
+            s0 += part[o];
+            s1 += part[o + 1];
+            s2 += part[o + 2];
+        }
+        if (fixed) continue;
+        const float q0 = fK * s0 + mfm * d0, q1 = fK * s1 + mfm * d1, q2 = fK * s2 + mfm * d2;
+        if (refresh) {
+            double t0 = part64[i], t1 = part64[i + 1], t2 = part64[i + 2];
+            for (uint32_t j = j0; j < j1; j++) {
+                const size_t o = 3 * ((size_t)b.Ntot + j);
+                t0 += part64[o];
+                t1 += part64[o + 1];
+                t2 += part64[o + 2];
+            }
+            const double mfm64 = c.mass * c.factor_M;
+            const double ya = y[i] + (double)e0, yb = y[i + 1] + (double)e1, yc = y[i + 2] + (double)e2;
+            r0 = (float)(bv[i] - (c.factor_K * t0 + mfm64 * ya));
+            r1 = (float)(bv[i + 1] - (c.factor_K * t1 + mfm64 * yb));
+            r2 = (float)(bv[i + 2] - (c.factor_K * t2 + mfm64 * yc));
+            // fold the FP32 increment into the FP64 iterate: later small
+            // corrections then keep their bits (an FP32 sum that has grown
+            // large would absorb them)
+            y[i] = ya;
+            y[i + 1] = yb;
+            y[i + 2] = yc;
+            e0 = e1 = e2 = 0.f;
+        }
+        if (!confirm) {
+            r0 += na * q0;
+            r1 += na * q1;
+            r2 += na * q2;
+            e0 = __fmaf_rn(alpha_s, d0, e0);
+            e1 = __fmaf_rn(alpha_s, d1, e1);
+            e2 = __fmaf_rn(alpha_s, d2, e2);
+            d[i] = d0; d[i + 1] = d1; d[i + 2] = d2;
+        }
+        b.ydelta[i] = e0;
+        b.ydelta[i + 1] = e1;
+        b.ydelta[i + 2] = e2;
+        r[i] = r0; r[i + 1] = r1; r[i + 2] = r2;
+        acc += r0 * r0 + r1 * r1 + r2 * r2;
+    }
+    const F2 rr = block_sum_f2(F2{acc, 0.f}, sh);
+    if (threadIdx.x == 0) cshare[ci] = make_float2(rr.hi, rr.lo);
+}
+
 // The node pass by this block over its entries block, block + G, ... of the
-// chunk work list (fuse: the block forms its mesh's alpha from the tile
-// shares itself).
+// chunk work list.
 __device__ __forceinline__ void node_update_pass(const BatchView<float>& b, const float* part, const double* part64,
                                                  const double* bv, double* y, float* r, float* d, float2* cshare,
                                                  const float2* tshare,
                                                  const uint32_t block, const uint32_t G, const bool fuse)
 {
-    __shared__ float2 sh[32];
-    __shared__ float s_alpha;
-    __shared__ int s_brk;
     const uint32_t n_act = *(volatile const uint32_t*)(b.act_count + 1);
     for (uint32_t ia = block; ia < n_act; ia += G) {
         const uint32_t ci = b.act_chunks[ia];
         const ChunkMeta ch = b.chunks[ci];
-        const StepScalars& sm = b.st[ch.mesh];
-        if (sm.done) continue;  // left its loop; the list is rebuilt lazily
-        const MeshConsts& c = b.mc[ch.mesh];
-        bool brk;
-        float alpha_s;
-        if (fuse) {
-            // this block forms its mesh's alpha (warp 0, the same sum as
-            // k_mesh_alpha); the block of the mesh's first chunk publishes it
-            if (threadIdx.x < 32) {
-                const MeshAlpha ma = warp_mesh_alpha(b, tshare, ch.mesh, ci == c.chunk0);
-                if (threadIdx.x == 0) {
-                    s_alpha = ma.alpha;
-                    s_brk = ma.brk ? 1 : 0;
-                }
-            }
-            __syncthreads();
-            brk = s_brk != 0;
-            alpha_s = s_alpha;
-        } else {
-            brk = sm.brk != 0;
-            alpha_s = sm.alpha_f;
-        }
-        const bool confirm = sm.confirm != 0;
-        const bool refresh = sm.refresh_next != 0;
-        const float beta = sm.beta_f;
-        const float na = -alpha_s;
-        const float fK = c.fK_f, mfm = c.mfm_f;
-        float acc = 0.f;
-        for (size_t n = ch.n0 + threadIdx.x; !brk && n < ch.n1; n += blockDim.x) {
-            const size_t i = 3 * n;
-            // every load is issued before the constraint flag is known; a
-            // constrained row keeps d, r zero and y unchanged
-            const bool fixed = b.fixed[n] != 0;
-            const float d0 = __fmaf_rn(beta, d[i], r[i]);
-            const float d1 = __fmaf_rn(beta, d[i + 1], r[i + 1]);
-            const float d2 = __fmaf_rn(beta, d[i + 2], r[i + 2]);
-            // the owner tile's partial (node order), then the overflow slots
-            // (contiguous, tile order)
-            float s0 = part[i], s1 = part[i + 1], s2 = part[i + 2];
-            const uint32_t j0 = b.ov_ptr[n];
-            const uint32_t j1 = bounds_idx(b.ov_ptr[n + 1], b.nslots - b.Ntot + 1, kSitePartialSlot);
-            float r0 = r[i], r1 = r[i + 1], r2 = r[i + 2];
-            float e0 = b.ydelta[i], e1 = b.ydelta[i + 1], e2 = b.ydelta[i + 2];
-            // the first four overflow partials are loaded together, then
-            // added in slot order (the rare rest one by one)
-            float p[4][3];
-#pragma unroll
-            for (int k = 0; k < 4; k++) {
-                const bool in = j0 + k < j1;
-                const size_t o = 3 * ((size_t)b.Ntot + (in ? j0 + k : 0u));
-                p[k][0] = in ? part[o] : 0.f;
-                p[k][1] = in ? part[o + 1] : 0.f;
-                p[k][2] = in ? part[o + 2] : 0.f;
-            }
-#pragma unroll
-            for (int k = 0; k < 4; k++) {
-                if (j0 + k < j1) {
-                    s0 += p[k][0];
-                    s1 += p[k][1];
-                    s2 += p[k][2];
-                }
-            }
-            for (uint32_t j = j0 + 4; j < j1; j++) {
-                const size_t o = 3 * ((size_t)b.Ntot + j);
-                s0 += part[o];
-                s1 += part[o + 1];
-                s2 += part[o + 2];
-            }
-            if (fixed) continue;
-            const float q0 = fK * s0 + mfm * d0, q1 = fK * s1 + mfm * d1, q2 = fK * s2 + mfm * d2;
-            if (refresh) {
-                double t0 = part64[i], t1 = part64[i + 1], t2 = part64[i + 2];
-                for (uint32_t j = j0; j < j1; j++) {
-                    const size_t o = 3 * ((size_t)b.Ntot + j);
-                    t0 += part64[o];
-                    t1 += part64[o + 1];
-                    t2 += part64[o + 2];
-                }
-                const double mfm64 = c.mass * c.factor_M;
-                const double ya = y[i] + (double)e0, yb = y[i + 1] + (double)e1, yc = y[i + 2] + (double)e2;
-                r0 = (float)(bv[i] - (c.factor_K * t0 + mfm64 * ya));
-                r1 = (float)(bv[i + 1] - (c.factor_K * t1 + mfm64 * yb));
-                r2 = (float)(bv[i + 2] - (c.factor_K * t2 + mfm64 * yc));
-                // fold the FP32 increment into the FP64 iterate: later small
-                // corrections then keep their bits (an FP32 sum that has grown
-                // large would absorb them)
-                y[i] = ya;
-                y[i + 1] = yb;
-                y[i + 2] = yc;
-                e0 = e1 = e2 = 0.f;
-            }
-            if (!confirm) {
-                r0 += na * q0;
-                r1 += na * q1;
-                r2 += na * q2;
-                e0 = __fmaf_rn(alpha_s, d0, e0);
-                e1 = __fmaf_rn(alpha_s, d1, e1);
-                e2 = __fmaf_rn(alpha_s, d2, e2);
-                d[i] = d0; d[i + 1] = d1; d[i + 2] = d2;
-            }
-            b.ydelta[i] = e0;
-            b.ydelta[i + 1] = e1;
-            b.ydelta[i + 2] = e2;
-            r[i] = r0; r[i + 1] = r1; r[i + 2] = r2;
-            acc += r0 * r0 + r1 * r1 + r2 * r2;
-        }
-        const F2 rr = block_sum_f2(F2{acc, 0.f}, sh);
-        if (threadIdx.x == 0) cshare[ci] = make_float2(rr.hi, rr.lo);
+        node_update_chunk(b, part, part64, bv, y, r, d, cshare, tshare, ci, ch, fuse);
     }
 }
 
@@ -708,111 +734,113 @@ __global__ void __launch_bounds__(256) k_node_update_fused(BatchView<float> b, c
 // and the loop test (ILSS_CG.h:100-144). One warp per mesh; the last block
 // of the grid then rebuilds the work lists, sets the CUDA-graph while
 // condition and the refresh flag.
-// Per running mesh (warp w of nw warps in all): the update above.
-__device__ __forceinline__ void mesh_update_pass(const BatchView<float>& b, const float2* cshare,
-                                                 const uint32_t w, const uint32_t nw)
+// The update of one mesh by one warp (any mesh: one that has left its loop
+// returns at once).
+__device__ __forceinline__ void mesh_update_one(const BatchView<float>& b, const float2* cshare, const uint32_t mesh)
 {
     const uint32_t lane = threadIdx.x & 31u;
-    for (uint32_t mesh = w; mesh < b.M; mesh += nw) {
-        // the mesh's scalars, copied before the first branch and before the
-        // shares are summed (one round trip for all of them), updated in
-        // registers and written back once
-        const uint32_t done = b.st[mesh].done;
-        const MeshConsts& c = b.mc[mesh];
-        const uint32_t chunk0 = c.chunk0, nchunks = c.nchunks;
-        StepScalars st;
-        if (lane == 0) st = b.st[mesh];
-        if (done) continue;
-        F2 tot = {0.f, 0.f};
-        for (uint32_t k = lane; k < nchunks; k += 32u) {
-            const float2 w = __ldcg(cshare + chunk0 + k);
-            tot = f2_add(tot, F2{w.x, w.y});
-        }
-        tot = warp_sum_f2(tot);
-        if (lane == 0) {
-            const bool confirm = st.confirm != 0, brk = st.brk != 0;
-            if (confirm) {
-                // the FP64 residual of the current iterate decides: leave,
-                // or go on from it -- with the recurrence's direction
-                // (beta from the FP64 residual, reliable-update style),
-                // unless the recursive residual had fallen to rounding
-                // noise, then from the residual alone (beta = 0)
-                const double total = (double)tot.hi + (double)tot.lo;
-                const double rec = st.delta_new;  // recursive |r|^2 at the loop test
-                st.confirm = 0;
-                st.delta_old = rec;
-                st.delta_new = total;
-                st.delta_refresh = total;
-                st.k_refresh = st.k;
-                st.refresh_next = 0;
-                if (!isfinite(total)) st.status = 3u;
-                if (cg_cont_t(st)) {
-                    st.beta = (rec > 0.0 && total <= 1e3 * rec) ? total / rec : 0.0;
-                    st.beta_f = (float)st.beta;
-                    st.done = 0;
-                } else {
-                    st.done = 1;
-                    st.finished = 1;
-                    atomicAdd(b.list_dirty, c.ntiles);
-                    finish_stats_t(st);
-                }
-            } else if (brk) {
+    // the mesh's scalars, copied before the first branch and before the
+    // shares are summed (one round trip for all of them), updated in
+    // registers and written back once
+    const uint32_t done = b.st[mesh].done;
+    const MeshConsts& c = b.mc[mesh];
+    const uint32_t chunk0 = c.chunk0, nchunks = c.nchunks;
+    StepScalars st;
+    if (lane == 0) st = b.st[mesh];
+    if (done) return;
+    F2 tot = lane_share_sum(cshare + chunk0, nchunks, lane);
+    tot = warp_sum_f2(tot);
+    if (lane == 0) {
+        const bool confirm = st.confirm != 0, brk = st.brk != 0;
+        if (confirm) {
+            // the FP64 residual of the current iterate decides: leave,
+            // or go on from it -- with the recurrence's direction
+            // (beta from the FP64 residual, reliable-update style),
+            // unless the recursive residual had fallen to rounding
+            // noise, then from the residual alone (beta = 0)
+            const double total = (double)tot.hi + (double)tot.lo;
+            const double rec = st.delta_new;  // recursive |r|^2 at the loop test
+            st.confirm = 0;
+            st.delta_old = rec;
+            st.delta_new = total;
+            st.delta_refresh = total;
+            st.k_refresh = st.k;
+            st.refresh_next = 0;
+            if (!isfinite(total)) st.status = 3u;
+            if (cg_cont_t(st)) {
+                st.beta = (rec > 0.0 && total <= 1e3 * rec) ? total / rec : 0.0;
+                st.beta_f = (float)st.beta;
+                st.done = 0;
+            } else {
                 st.done = 1;
                 st.finished = 1;
                 atomicAdd(b.list_dirty, c.ntiles);
                 finish_stats_t(st);
-            } else {
-                const double total = (double)tot.hi + (double)tot.lo;
-                st.alpha = st.delta_new / st.dot_dq;
-                st.delta_old = st.delta_new;
-                st.delta_new = total;
-                st.beta = total / st.delta_old;
-                st.beta_f = (float)st.beta;
-                st.k += 1;
-                st.total_iters += 1;
-                if (!isfinite(total)) st.status = 3u;
-                // reliable updates: recompute the residual in FP64 once |r|
-                // has fallen by refresh_drop since the last FP64 residual,
-                // and at least every refresh_every iterations
-                if (st.refresh_next) {
-                    st.delta_refresh = total;
-                    st.k_refresh = st.k;
-                }
-                st.refresh_next = ((c.refresh_drop_sq > 0.0 && total < c.refresh_drop_sq * st.delta_refresh) ||
-                                   (c.refresh_every > 0 && st.k - st.k_refresh >= c.refresh_every))
-                                      ? 1u
-                                      : 0u;
-                bool cont = cg_cont_t(st);
-                if (!cont && st.k_refresh != st.k && st.k < st.max_iter && total == total &&
-                    (c.refresh_every > 0 || c.refresh_drop_sq > 0.0)) {
-                    // converged on the FP32 recursive residual: the next
-                    // iteration measures the FP64 residual before the loop ends
-                    cont = true;
-                    st.refresh_next = 1u;
-                    st.confirm = 1u;
-                }
-                st.done = cont ? 0u : 1u;
-                if (st.done) {
-                    finish_stats_t(st);
-                    st.finished = 1;
-                    atomicAdd(b.list_dirty, c.ntiles);
-                }
             }
-            b.st[mesh] = st;
-            __threadfence();  // the mesh's scalars before the grid arrival that follows
+        } else if (brk) {
+            st.done = 1;
+            st.finished = 1;
+            atomicAdd(b.list_dirty, c.ntiles);
+            finish_stats_t(st);
+        } else {
+            const double total = (double)tot.hi + (double)tot.lo;
+            st.alpha = st.delta_new / st.dot_dq;
+            st.delta_old = st.delta_new;
+            st.delta_new = total;
+            st.beta = total / st.delta_old;
+            st.beta_f = (float)st.beta;
+            st.k += 1;
+            st.total_iters += 1;
+            if (!isfinite(total)) st.status = 3u;
+            // reliable updates: recompute the residual in FP64 once |r|
+            // has fallen by refresh_drop since the last FP64 residual,
+            // and at least every refresh_every iterations
+            if (st.refresh_next) {
+                st.delta_refresh = total;
+                st.k_refresh = st.k;
+            }
+            st.refresh_next = ((c.refresh_drop_sq > 0.0 && total < c.refresh_drop_sq * st.delta_refresh) ||
+                               (c.refresh_every > 0 && st.k - st.k_refresh >= c.refresh_every))
+                                  ? 1u
+                                  : 0u;
+            bool cont = cg_cont_t(st);
+            if (!cont && st.k_refresh != st.k && st.k < st.max_iter && total == total &&
+                (c.refresh_every > 0 || c.refresh_drop_sq > 0.0)) {
+                // converged on the FP32 recursive residual: the next
+                // iteration measures the FP64 residual before the loop ends
+                cont = true;
+                st.refresh_next = 1u;
+                st.confirm = 1u;
+            }
+            st.done = cont ? 0u : 1u;
+            if (st.done) {
+                finish_stats_t(st);
+                st.finished = 1;
+                atomicAdd(b.list_dirty, c.ntiles);
+            }
         }
+        b.st[mesh] = st;
+        __threadfence();  // the mesh's scalars before the grid arrival that follows
     }
+}
+
+// Per running mesh (warp w of nw warps in all): the update above.
+__device__ __forceinline__ void mesh_update_pass(const BatchView<float>& b, const float2* cshare,
+                                                 const uint32_t w, const uint32_t nw)
+{
+    for (uint32_t mesh = w; mesh < b.M; mesh += nw) mesh_update_one(b, cshare, mesh);
 }
 
 // After every mesh's update, by one block (all its threads): work lists
 // (when a mesh left its loop), refresh flag, slice count, and whether the
 // loop goes on (the CUDA-graph while condition where there is one).
-__device__ __forceinline__ bool loop_control(const BatchView<float>& b, const LoopSync& ls)
+__device__ __forceinline__ bool loop_control(const BatchView<float>& b, const LoopSync& ls, bool rebuild = true)
 {
     __shared__ unsigned s_go;
     // rebuild the CG lists once a quarter of their tiles belong to meshes that
     // have left their loop (the kernels skip those entries until then)
-    if (4u * *(volatile const unsigned*)b.list_dirty >= *(volatile const uint32_t*)b.act_count) build_active_lists(b);
+    if (rebuild && 4u * *(volatile const unsigned*)b.list_dirty >= *(volatile const uint32_t*)b.act_count)
+        build_active_lists(b);
     int any = 0, rf = 0, norf = 0;  // norf: a running mesh that does not refresh
     for (uint32_t m = threadIdx.x; m < b.M; m += blockDim.x) {
         volatile const StepScalars* sp = b.st + m;
@@ -864,7 +892,7 @@ __global__ void __launch_bounds__(256) k_mesh_update(BatchView<float> b, const f
 // which dominate an iteration of a small batch (a lone scene of a served
 // shard).
 
-// Bounded polls of a grid barrier (each poll sleeps about 0.1 us): far above
+// Bounded polls of a grid barrier (each poll sleeps about 20 ns after an L2 round trip): far above
 // any phase of an iteration.
 constexpr uint32_t kGridPolls = 1u << 22;
 
@@ -902,7 +930,7 @@ __device__ __forceinline__ bool grid_barrier(unsigned* gbar, uint32_t G, uint32_
                 s_state = 2u;
                 break;
             }
-            __nanosleep(100);
+            __nanosleep(20);
         }
         __threadfence();
     }
@@ -1010,6 +1038,320 @@ cudaError_t launch_cg_coop(const BatchView<float>& b, const CoopLoopArgs& a, uin
     e = cudaLaunchCooperativeKernel((const void*)k_cg_coop<kTileElems>, dim3(grid), dim3(kTileElems), args,
                                     PipeShape<kTileElems>::kSmem, s);
     prof_end("cg_coop", s);
+    launch_counter()++;
+    return e;
+}
+
+// ---------------------------------------------------------------------------
+// The resident-tile form of the persistent loop, for launches whose running
+// tiles fit the GPU at two per block: each block keeps its tiles' blobs in
+// its two stages for the whole launch (one bulk copy each, at the start) and
+// their look-ups in registers, writes the element outputs to a separate
+// area, and a CG iteration needs two grid barriers: after the tile product,
+// and after the node pass, whose last block runs the per-mesh updates and
+// the loop control. Per value it computes what the kernels above compute, in
+// the same order, so the results are the same bits. What it removes is the
+// per-iteration blob traffic and the chains of dependent global loads
+// (work lists, tile metadata) that bound a small batch's iteration.
+template <int TILE>
+struct ResShape {
+    static constexpr uint32_t kNodes = PipeShape<TILE>::kNodes;
+    static constexpr uint32_t kStage = PipeShape<TILE>::kStage;
+    static constexpr uint32_t kOut = 2 * kStage;            // float4 so4[4 TILE]; mesh list in the control
+    static constexpr uint32_t kSd = kOut + 64u * TILE;      // float4 sd4[kNodes]
+    static constexpr uint32_t kBar = kSd + 16u * kNodes;    // two mbarriers
+    static constexpr uint32_t kSmem = kBar + 16u + 8u * (TILE / 32) + 16u;
+    static constexpr int kMinBlocks = 3;
+    static constexpr uint32_t kMaxMeshes = 64u * TILE / 4u;  // the control's mesh list in the output area
+};
+static_assert(3 * (((ResShape<256>::kSmem + 127) & ~127u) + 1024) <= 233472, "three resident blocks per SM");
+static_assert(sizeof(DF) * 12 * kTileElems <= ResShape<kTileElems>::kStage &&
+                  sizeof(DF) * 3 * kTileNodes <= 64u * kTileElems,
+              "refresh staging fits stage 1 and the output area");
+
+// One resident tile's product for this iteration (every thread calls it;
+// a tile of a mesh that has left its loop is skipped as a whole).
+template <int TILE>
+__device__ __forceinline__ void resident_tile(const BatchView<float>& b, const float* dvec, const float* rvec,
+                                              float* part, float2* tshare, const TileLook& L,
+                                              const unsigned char* stage, unsigned char* smem)
+{
+    using RS = ResShape<TILE>;
+    float4* sd4 = reinterpret_cast<float4*>(smem + RS::kSd);
+    float4* so4 = reinterpret_cast<float4*>(smem + RS::kOut);
+    float2* wsh = reinterpret_cast<float2*>(smem + RS::kBar + 16u);
+    const uint32_t tid = threadIdx.x;
+    const uint32_t ne = look_ne(L), nn = look_nn(L), nown = look_nown(L);
+    // this thread's d and r and the mesh's flag and beta, loaded together
+    float cd0 = 0.f, cd1 = 0.f, cd2 = 0.f, cr0 = 0.f, cr1 = 0.f, cr2 = 0.f;
+    if (tid < nn) {
+        const size_t g = 3 * (size_t)L.g;
+        cd0 = __ldcg(dvec + g); cd1 = __ldcg(dvec + g + 1); cd2 = __ldcg(dvec + g + 2);
+        cr0 = __ldcg(rvec + g); cr1 = __ldcg(rvec + g + 1); cr2 = __ldcg(rvec + g + 2);
+    }
+    const StepScalars* sp = b.st + L.mesh;
+    const uint32_t done = *(volatile const uint32_t*)&sp->done;
+    const float beta = *(volatile const float*)&sp->beta_f;
+    if (done) return;  // uniform: every thread read the same flag after the last grid barrier
+    float dd = 0.f;
+    if (tid < nn) {
+        const float dx = __fmaf_rn(beta, cd0, cr0);
+        const float dy = __fmaf_rn(beta, cd1, cr1);
+        const float dz = __fmaf_rn(beta, cd2, cr2);
+        sd4[tid] = make_float4(dx, dy, dz, 0.f);
+        if (tid < nown) dd = dx * dx + dy * dy + dz * dz;
+    }
+    __syncthreads();
+    const uint32_t ne4 = blob_ne4(ne);
+    const uint32_t* hdr = reinterpret_cast<const uint32_t*>(stage + blob_hdr_off(ne, nn));
+    const float* fac = reinterpret_cast<const float*>(hdr + 1);  // fK, m fM
+    float share = fac[1] * dd;
+    if (tid < ne) {
+        const float4* g4 = reinterpret_cast<const float4*>(stage) + tid;
+        const float4 q0 = g4[0], q1 = g4[ne4], q2 = g4[2 * ne4], q3 = g4[3 * ne4], q4 = g4[4 * ne4];
+        const uint32_t lw = reinterpret_cast<const uint32_t*>(stage + 80u * ne4)[tid];
+        const float R[9] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w, q2.x};
+        const float Di[9] = {q2.y, q2.z, q2.w, q3.x, q3.y, q3.z, q3.w, q4.x, q4.y};
+        const float knu = q4.z, k2 = q4.w, k1 = __fmaf_rn(2.f, k2, knu);
+        const int ids[4] = {(int)bounds_idx(lw & 0xffu, nn, kSiteLocalNode),
+                            (int)bounds_idx((lw >> 8) & 0xffu, nn, kSiteLocalNode),
+                            (int)bounds_idx((lw >> 16) & 0xffu, nn, kSiteLocalNode),
+                            (int)bounds_idx(lw >> 24, nn, kSiteLocalNode)};
+        float dl[12], out[12];
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            const float4 v = sd4[ids[k]];
+            dl[3 * k] = v.x;
+            dl[3 * k + 1] = v.y;
+            dl[3 * k + 2] = v.z;
+        }
+        elem_RKRt<float>(R, Di, k1, knu, k2, dl, out);
+        float eq = 0.f;
+#pragma unroll
+        for (int k = 0; k < 12; k++) eq = __fmaf_rn(dl[k], out[k], eq);
+        share = __fmaf_rn(fac[0], eq, share);
+#pragma unroll
+        for (int k = 0; k < 4; k++) so4[k * ne4 + tid] = make_float4(out[3 * k], out[3 * k + 1], out[3 * k + 2], 0.f);
+    }
+    __syncthreads();
+    if (tid < nn) {
+        const uint16_t* lp = reinterpret_cast<const uint16_t*>(stage + blob_lptr_off(ne));
+        const uint16_t* li = lp + (nn + 1);
+        float a0 = 0.f, a1 = 0.f, a2 = 0.f;
+        for (int j = lp[tid]; j < lp[tid + 1]; j++) {
+            const float4 v = so4[bounds_idx((uint32_t)li[j], 4u * ne4, kSiteTileEntry)];
+            a0 += v.x;
+            a1 += v.y;
+            a2 += v.z;
+        }
+        const size_t o =
+            3 * (size_t)bounds_idx(tid < nown ? hdr[0] + tid : hdr[3 + tid - nown], b.nslots, kSitePartialSlot);
+        part[o] = a0;
+        part[o + 1] = a1;
+        part[o + 2] = a2;
+    }
+    float w = share;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) w += __shfl_down_sync(0xffffffffu, w, o);
+    if ((tid & 31) == 0) wsh[tid >> 5] = make_float2(w, 0.f);
+    __syncthreads();
+    if (tid == 0) {
+        F2 a = {0.f, 0.f};
+        for (int k = 0; k < (int)(blockDim.x >> 5); k++) a = f2_add(a, F2{wsh[k].x, wsh[k].y});
+        tshare[L.tile] = make_float2(a.hi, a.lo);
+    }
+    // the next tile's staging and outputs reuse sd4 and so4
+    __syncthreads();
+}
+
+// The last block after the node pass: the update of every running mesh
+// (a warp per mesh, from a list gathered in the output area), then the loop
+// control (no list rebuild: a resident tile of a mesh that has left its
+// loop is skipped where it lies).
+template <int TILE>
+__device__ __noinline__ void resident_control(const BatchView<float>& b, const CoopLoopArgs& a, unsigned char* smem)
+{
+    __shared__ unsigned s_n;
+    uint32_t* list = reinterpret_cast<uint32_t*>(smem + ResShape<TILE>::kOut);
+    if (threadIdx.x == 0) s_n = 0u;
+    __syncthreads();
+    for (uint32_t m = threadIdx.x; m < b.M; m += blockDim.x)
+        if (!*(volatile const uint32_t*)&b.st[m].done) list[atomicAdd(&s_n, 1u)] = m;
+    __syncthreads();
+    const uint32_t n = s_n, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (uint32_t i = warp; i < n; i += nw) mesh_update_one(b, a.cshare, list[i]);
+    __syncthreads();
+    const bool go = loop_control(b, a.ls, false);
+    if (threadIdx.x == 0) a.gbar[2] = go ? 1u : 0u;
+}
+
+// The node pass: the block's chunks, looked up once per launch when they
+// number at most two per block (the chunk list does not change during a
+// resident launch), else the list walk of the other kernels.
+struct ResidentChunks {
+    uint32_t n;  // 0..2 cached; ~0u: walk the list
+    uint32_t ci[2];
+    ChunkMeta ch[2];
+};
+template <int TILE>
+__device__ __noinline__ void resident_node_phase(const BatchView<float>& b, const CoopLoopArgs& a,
+                                                 const ResidentChunks& rc, uint32_t blk, uint32_t G)
+{
+    if (rc.n == ~0u) {
+        node_update_pass(b, a.part, a.part64, a.bv, a.y, a.r, a.d, a.cshare, a.tshare, blk, G, true);
+        return;
+    }
+    for (uint32_t k = 0; k < rc.n; k++)
+        node_update_chunk(b, a.part, a.part64, a.bv, a.y, a.r, a.d, a.cshare, a.tshare, rc.ci[k], rc.ch[k], true);
+}
+
+template <int TILE>
+__device__ __noinline__ void resident_refresh_phase(const BatchView<float>& b, const CoopLoopArgs& a,
+                                                    unsigned char* smem, uint32_t blk, uint32_t G)
+{
+    // staged in stage 1 and the output area (stage 1's blob is copied again after)
+    DF* so = reinterpret_cast<DF*>(smem + ResShape<TILE>::kStage);
+    DF* sd = reinterpret_cast<DF*>(smem + ResShape<TILE>::kOut);
+    tile_spmv_y64_pass<float>(b, a.y, a.part64, SPMV_Y64_REFRESH, sd, so, blk, G);
+}
+
+template <int TILE>
+__global__ void __launch_bounds__(TILE, ResShape<TILE>::kMinBlocks) k_cg_resident(BatchView<float> b, CoopLoopArgs a)
+{
+    using RS = ResShape<TILE>;
+    extern __shared__ __align__(128) unsigned char smem[];
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + RS::kBar);
+    const uint32_t G = gridDim.x, blk = blockIdx.x, tid = threadIdx.x;
+    const uint32_t wait_polls = *(volatile const unsigned*)(a.err + 1);
+    const uint32_t n_act = *(volatile const uint32_t*)b.act_count;
+    if (n_act > 2u * G) {
+        // more running tiles than the launch was sized for: nothing runs
+        if (blk == 0 && tid == 0) atomicExch(a.err, 4u);
+        return;
+    }
+    TileLook L[2];
+    look_meta(b, blk, n_act, L[0]);
+    look_resolve(b, L[0]);
+    look_meta(b, blk + G, n_act, L[1]);
+    look_resolve(b, L[1]);
+    ResidentChunks rc;
+    {
+        const uint32_t nch = *(volatile const uint32_t*)(b.act_count + 1);
+        rc.n = nch > 2u * G ? ~0u : (blk < nch) + (blk + G < nch);
+        for (uint32_t k = 0; k < 2; k++)
+            if (rc.n != ~0u && k < rc.n) {
+                rc.ci[k] = b.act_chunks[blk + k * G];
+                rc.ch[k] = b.chunks[rc.ci[k]];
+            }
+    }
+    if (tid == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    uint32_t phase = 0u, pending = 0u;
+    auto copy_blob = [&](int k) {
+        if (tid == 0) {
+            const uint32_t bytes = blob_bytes(look_ne(L[k]), look_nn(L[k]), look_nown(L[k]));
+            mbar_expect_tx(&bar[k], bytes);
+            bulk_copy_g2s(smem + k * RS::kStage, b.blob + 16ull * L[k].boff, bytes, &bar[k]);
+        }
+        pending |= 1u << k;
+    };
+    for (int k = 0; k < 2; k++)
+        if (L[k].sizes) copy_blob(k);
+    bool failed = false;
+    // waits for stage k's copy, if one is in flight (every thread polls; the
+    // block agrees on the outcome)
+    auto await = [&](int k) {
+        if (!((pending >> k) & 1u)) return;
+        const bool ok = failed || mbar_wait_bounded(&bar[k], (phase >> k) & 1u, wait_polls);
+        if (__syncthreads_or(!ok)) {
+            if (tid == 0) atomicExch(a.err, 1u);
+            failed = true;
+        } else {
+            phase ^= 1u << k;
+            pending &= ~(1u << k);
+        }
+    };
+    uint32_t gen = 0u;
+    auto none = [] {};
+    bool run = grid_barrier(a.gbar, G, gen, a.err, [&] { coop_any_running(b, a); });
+    while (run && *(volatile const unsigned*)&a.gbar[2]) {
+        for (int k = 0; k < 2; k++) {
+            if (!L[k].sizes) continue;
+            await(k);
+            if (!failed)
+                resident_tile<TILE>(b, a.d, a.r, a.part, a.tshare, L[k], smem + k * RS::kStage, smem);
+        }
+        if (!grid_barrier(a.gbar, G, gen, a.err, none)) {
+            run = false;
+            break;
+        }
+        if (*(volatile const unsigned*)a.ls.refresh_flag) {
+            await(1);  // stage 1 is about to be overwritten
+            resident_refresh_phase<TILE>(b, a, smem, blk, G);
+            // the staging writes precede the bulk copy into stage 1
+            fence_proxy_async_smem();
+            __syncthreads();
+            if (L[1].sizes && !failed) copy_blob(1);
+            if (!grid_barrier(a.gbar, G, gen, a.err, none)) {
+                run = false;
+                break;
+            }
+        }
+        resident_node_phase<TILE>(b, a, rc, blk, G);
+        if (!grid_barrier(a.gbar, G, gen, a.err, [&] { resident_control<TILE>(b, a, smem); })) {
+            run = false;
+            break;
+        }
+    }
+    // no block leaves while a copy into its shared memory is in flight
+    bool drained = true;
+    for (int k = 0; k < 2; k++)
+        if ((pending >> k) & 1u) drained &= mbar_wait_bounded(&bar[k], (phase >> k) & 1u, kDrainPolls);
+    if (!drained) atomicExch(a.err, 2u);
+}
+
+template <int TILE>
+static int resident_max_blocks()
+{
+    static int grid = 0;
+    if (!grid) {
+        int dev = 0, sms = 0, per_sm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaFuncSetAttribute(k_cg_resident<TILE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)ResShape<TILE>::kSmem);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cg_resident<TILE>, TILE, ResShape<TILE>::kSmem);
+        grid = (sms > 0 ? sms : 1) * (per_sm > 0 ? per_sm : 1);
+    }
+    return grid;
+}
+
+uint32_t cg_resident_capacity(uint32_t meshes)
+{
+    return meshes <= ResShape<kTileElems>::kMaxMeshes ? 2u * (uint32_t)resident_max_blocks<kTileElems>() : 0u;
+}
+
+cudaError_t launch_cg_resident(const BatchView<float>& b, const CoopLoopArgs& a, uint32_t tiles, cudaStream_t s)
+{
+    if (b.pipe_tile == (uint32_t)kPipeSmallTile || b.M > ResShape<kTileElems>::kMaxMeshes)
+        return cudaErrorInvalidValue;
+    const uint32_t maxg = (uint32_t)resident_max_blocks<kTileElems>();
+    if (tiles > 2u * maxg) return cudaErrorInvalidValue;
+    // one tile per block while they fit, else two
+    const uint32_t grid = tiles == 0 ? 1u : (tiles <= maxg ? tiles : (tiles + 1) / 2);
+    cudaError_t e = cudaMemsetAsync(a.gbar, 0, 3 * sizeof(unsigned), s);
+    if (e != cudaSuccess) return e;
+    BatchView<float> bv = b;
+    CoopLoopArgs av = a;
+    void* args[] = {&bv, &av};
+    prof_begin("cg_resident", s);
+    e = cudaLaunchCooperativeKernel((const void*)k_cg_resident<kTileElems>, dim3(grid), dim3(kTileElems), args,
+                                    ResShape<kTileElems>::kSmem, s);
+    prof_end("cg_resident", s);
     launch_counter()++;
     return e;
 }

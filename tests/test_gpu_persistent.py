@@ -104,3 +104,17 @@ def test_persistent_loop_options_are_checked(fem_lib):
         with pytest.raises(fem_lib.FemError) as e:
             fem_lib.Batch(sc, persistent_loop=True, **kw)
         assert e.value.code == fem_lib.FEM_E_ARG
+
+
+def test_persistent_loop_streams_tiles_beyond_the_resident_capacity(fem_lib):
+    """Running tiles beyond what the blocks can keep resident (two per block)
+    go through the streaming form of the persistent kernel (a bulk copy per
+    tile and iteration): the same bits as the graph loop."""
+    rng = np.random.default_rng(41)
+    scs = [scenes.random_block(rng, idx=i, dims=(40, 30, 30)) for i in range(2)]  # 2 x 180,000 tets
+    g = fem_lib.Batch(scs, fem_lib.FEM_PRECISION_MIXED, compute_energy=False)
+    p = fem_lib.Batch(scs, fem_lib.FEM_PRECISION_MIXED, compute_energy=False, persistent_loop=True)
+    assert g.info()["tiles"] > 1000
+    g.step(1)
+    p.step(1)
+    _same(g, p, len(scs))
