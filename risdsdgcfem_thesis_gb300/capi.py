@@ -17,6 +17,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 # table-read index (build.build_bounds_check()); otherwise the normal library.
 BOUNDS_LIB_PATH = os.path.join(HERE, "libfemtet_gb300_bounds.so")
 LIB_PATH = BOUNDS_LIB_PATH if os.environ.get("FEMGB_BOUNDS_CHECK") == "1" else os.path.join(HERE, "libfemtet_gb300.so")
+# FEMGB_LIBRARY names another build of the same library (a variant compiled
+# with other -D settings by build.build(defines=..., out=...)).
+LIB_PATH = os.environ.get("FEMGB_LIBRARY") or LIB_PATH
 
 FEM_OK = 0
 FEM_E_ARG, FEM_E_INDEX, FEM_E_NAN, FEM_E_OOM, FEM_E_CUDA, FEM_E_TIMEOUT, FEM_E_NODEVICE, FEM_E_DEGENERATE = range(1, 9)

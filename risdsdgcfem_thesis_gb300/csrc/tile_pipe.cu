@@ -294,6 +294,42 @@ __device__ __forceinline__ void look_resolve(const BatchView<float>& b, TileLook
                                    : 0u;
 }
 
+// A local node's sum of its element outputs (tile-local CSR entries
+// [j, j1), element order): the indices of kNodeSumBatch entries, then their
+// outputs, are loaded together, so a node's chain of dependent
+// shared-memory loads is that many times shorter; the additions keep the
+// entry order. (A build can set the batch with -DFEMGB_NODE_SUM_BATCH=n.)
+#ifndef FEMGB_NODE_SUM_BATCH
+#define FEMGB_NODE_SUM_BATCH 2
+#endif
+constexpr int kNodeSumBatch = FEMGB_NODE_SUM_BATCH;
+__device__ __forceinline__ void node_sum(const float4* so4, const uint16_t* li, int j, const int j1, uint32_t ne4,
+                                         float& a0, float& a1, float& a2)
+{
+    if (kNodeSumBatch > 1) {
+        for (; j + kNodeSumBatch <= j1; j += kNodeSumBatch) {
+            uint32_t i[kNodeSumBatch];
+#pragma unroll
+            for (int k = 0; k < kNodeSumBatch; k++) i[k] = bounds_idx((uint32_t)li[j + k], 4u * ne4, kSiteTileEntry);
+            float4 v[kNodeSumBatch];
+#pragma unroll
+            for (int k = 0; k < kNodeSumBatch; k++) v[k] = so4[i[k]];
+#pragma unroll
+            for (int k = 0; k < kNodeSumBatch; k++) {
+                a0 += v[k].x;
+                a1 += v[k].y;
+                a2 += v[k].z;
+            }
+        }
+    }
+    for (; j < j1; j++) {
+        const float4 v = so4[bounds_idx((uint32_t)li[j], 4u * ne4, kSiteTileEntry)];
+        a0 += v.x;
+        a1 += v.y;
+        a2 += v.z;
+    }
+}
+
 template <bool kCoherent>
 __device__ __forceinline__ float ld_dir(const float* p)
 {
@@ -477,12 +513,7 @@ __device__ __forceinline__ void tile_pipe_pass(const BatchView<float>& b, const 
                 const uint16_t* lp = reinterpret_cast<const uint16_t*>(stage + blob_lptr_off(ne));
                 const uint16_t* li = lp + (nn + 1);
                 float a0 = 0.f, a1 = 0.f, a2 = 0.f;
-                for (int j = lp[tid]; j < lp[tid + 1]; j++) {
-                    const float4 v = so4[bounds_idx((uint32_t)li[j], 4u * ne4, kSiteTileEntry)];
-                    a0 += v.x;
-                    a1 += v.y;
-                    a2 += v.z;
-                }
+                node_sum(so4, li, lp[tid], lp[tid + 1], ne4, a0, a1, a2);
                 const uint32_t nown = look_nown(cur);
                 const size_t o =
                     3 * (size_t)bounds_idx(tid < nown ? hdr[0] + tid : hdr[3 + tid - nown], b.nslots, kSitePartialSlot);
@@ -1138,12 +1169,7 @@ __device__ __forceinline__ void resident_tile(const BatchView<float>& b, const f
         const uint16_t* lp = reinterpret_cast<const uint16_t*>(stage + blob_lptr_off(ne));
         const uint16_t* li = lp + (nn + 1);
         float a0 = 0.f, a1 = 0.f, a2 = 0.f;
-        for (int j = lp[tid]; j < lp[tid + 1]; j++) {
-            const float4 v = so4[bounds_idx((uint32_t)li[j], 4u * ne4, kSiteTileEntry)];
-            a0 += v.x;
-            a1 += v.y;
-            a2 += v.z;
-        }
+        node_sum(so4, li, lp[tid], lp[tid + 1], ne4, a0, a1, a2);
         const size_t o =
             3 * (size_t)bounds_idx(tid < nown ? hdr[0] + tid : hdr[3 + tid - nown], b.nslots, kSitePartialSlot);
         part[o] = a0;
