@@ -295,33 +295,13 @@ __device__ __forceinline__ void look_resolve(const BatchView<float>& b, TileLook
 }
 
 // A local node's sum of its element outputs (tile-local CSR entries
-// [j, j1), element order): the indices of kNodeSumBatch entries, then their
-// outputs, are loaded together, so a node's chain of dependent
-// shared-memory loads is that many times shorter; the additions keep the
-// entry order. (A build can set the batch with -DFEMGB_NODE_SUM_BATCH=n.)
-#ifndef FEMGB_NODE_SUM_BATCH
-#define FEMGB_NODE_SUM_BATCH 2
-#endif
-constexpr int kNodeSumBatch = FEMGB_NODE_SUM_BATCH;
+// [j, j1), element order). (Loading the indices and outputs of two or four
+// entries together, to shorten the chain of dependent shared-memory loads,
+// measured 1.5 times slower on the 1024-mesh batch: the extra registers
+// spill.)
 __device__ __forceinline__ void node_sum(const float4* so4, const uint16_t* li, int j, const int j1, uint32_t ne4,
                                          float& a0, float& a1, float& a2)
 {
-    if (kNodeSumBatch > 1) {
-        for (; j + kNodeSumBatch <= j1; j += kNodeSumBatch) {
-            uint32_t i[kNodeSumBatch];
-#pragma unroll
-            for (int k = 0; k < kNodeSumBatch; k++) i[k] = bounds_idx((uint32_t)li[j + k], 4u * ne4, kSiteTileEntry);
-            float4 v[kNodeSumBatch];
-#pragma unroll
-            for (int k = 0; k < kNodeSumBatch; k++) v[k] = so4[i[k]];
-#pragma unroll
-            for (int k = 0; k < kNodeSumBatch; k++) {
-                a0 += v[k].x;
-                a1 += v[k].y;
-                a2 += v[k].z;
-            }
-        }
-    }
     for (; j < j1; j++) {
         const float4 v = so4[bounds_idx((uint32_t)li[j], 4u * ne4, kSiteTileEntry)];
         a0 += v.x;
