@@ -633,21 +633,49 @@ __device__ __forceinline__ void node_update_chunk(const BatchView<float>& b, con
     const float na = -alpha_s;
     const float fK = c.fK_f, mfm = c.mfm_f;
     float acc = 0.f;
-    for (size_t n = ch.n0 + threadIdx.x; !brk && n < ch.n1; n += blockDim.x) {
+    // Software pipeline over this thread's nodes n, n + blockDim.x, ...: the
+    // loads that need only the node id (constraint flag, d, r, the owner's
+    // partial, the overflow range, the increment) are issued for the next
+    // node before this node's dependent loads and its stores.
+    struct Head {
+        uint32_t fixed, j0, j1;
+        float d[3], r[3], s[3], e[3];
+    };
+    auto load_head = [&](size_t n, Head& h) {
+        const size_t i = 3 * n;
+        h.fixed = b.fixed[n];
+#pragma unroll
+        for (int c3 = 0; c3 < 3; c3++) {
+            h.d[c3] = d[i + c3];
+            h.r[c3] = r[i + c3];
+            h.s[c3] = part[i + c3];
+            h.e[c3] = b.ydelta[i + c3];
+        }
+        h.j0 = b.ov_ptr[n];
+        h.j1 = bounds_idx(b.ov_ptr[n + 1], b.nslots - b.Ntot + 1, kSitePartialSlot);
+    };
+    size_t n = ch.n0 + threadIdx.x;
+    bool have = !brk && n < ch.n1;
+    Head cur;
+    if (have) load_head(n, cur);
+    while (have) {
+        const size_t nn = n + blockDim.x;
+        const bool have_next = nn < ch.n1;
+        Head nxt;
+        if (have_next) load_head(nn, nxt);
         const size_t i = 3 * n;
         // every load is issued before the constraint flag is known; a
         // constrained row keeps d, r zero and y unchanged
-        const bool fixed = b.fixed[n] != 0;
-        const float d0 = __fmaf_rn(beta, d[i], r[i]);
-        const float d1 = __fmaf_rn(beta, d[i + 1], r[i + 1]);
-        const float d2 = __fmaf_rn(beta, d[i + 2], r[i + 2]);
+        const bool fixed = cur.fixed != 0;
+        const float d0 = __fmaf_rn(beta, cur.d[0], cur.r[0]);
+        const float d1 = __fmaf_rn(beta, cur.d[1], cur.r[1]);
+        const float d2 = __fmaf_rn(beta, cur.d[2], cur.r[2]);
         // the owner tile's partial (node order), then the overflow slots
         // (contiguous, tile order)
-        float s0 = part[i], s1 = part[i + 1], s2 = part[i + 2];
-        const uint32_t j0 = b.ov_ptr[n];
-        const uint32_t j1 = bounds_idx(b.ov_ptr[n + 1], b.nslots - b.Ntot + 1, kSitePartialSlot);
-        float r0 = r[i], r1 = r[i + 1], r2 = r[i + 2];
-        float e0 = b.ydelta[i], e1 = b.ydelta[i + 1], e2 = b.ydelta[i + 2];
+        float s0 = cur.s[0], s1 = cur.s[1], s2 = cur.s[2];
+        const uint32_t j0 = cur.j0, j1 = cur.j1;
+        float r0 = cur.r[0], r1 = cur.r[1], r2 = cur.r[2];
+        float e0 = cur.e[0], e1 = cur.e[1], e2 = cur.e[2];
         // the first four overflow partials are loaded together, then
         // added in slot order (the rare rest one by one)
         float p[4][3];
@@ -673,43 +701,47 @@ __device__ __forceinline__ void node_update_chunk(const BatchView<float>& b, con
             s1 += part[o + 1];
             s2 += part[o + 2];
         }
-        if (fixed) continue;
-        const float q0 = fK * s0 + mfm * d0, q1 = fK * s1 + mfm * d1, q2 = fK * s2 + mfm * d2;
-        if (refresh) {
-            double t0 = part64[i], t1 = part64[i + 1], t2 = part64[i + 2];
-            for (uint32_t j = j0; j < j1; j++) {
-                const size_t o = 3 * ((size_t)b.Ntot + j);
-                t0 += part64[o];
-                t1 += part64[o + 1];
-                t2 += part64[o + 2];
+        if (!fixed) {
+            const float q0 = fK * s0 + mfm * d0, q1 = fK * s1 + mfm * d1, q2 = fK * s2 + mfm * d2;
+            if (refresh) {
+                double t0 = part64[i], t1 = part64[i + 1], t2 = part64[i + 2];
+                for (uint32_t j = j0; j < j1; j++) {
+                    const size_t o = 3 * ((size_t)b.Ntot + j);
+                    t0 += part64[o];
+                    t1 += part64[o + 1];
+                    t2 += part64[o + 2];
+                }
+                const double mfm64 = c.mass * c.factor_M;
+                const double ya = y[i] + (double)e0, yb = y[i + 1] + (double)e1, yc = y[i + 2] + (double)e2;
+                r0 = (float)(bv[i] - (c.factor_K * t0 + mfm64 * ya));
+                r1 = (float)(bv[i + 1] - (c.factor_K * t1 + mfm64 * yb));
+                r2 = (float)(bv[i + 2] - (c.factor_K * t2 + mfm64 * yc));
+                // fold the FP32 increment into the FP64 iterate: later small
+                // corrections then keep their bits (an FP32 sum that has grown
+                // large would absorb them)
+                y[i] = ya;
+                y[i + 1] = yb;
+                y[i + 2] = yc;
+                e0 = e1 = e2 = 0.f;
             }
-            const double mfm64 = c.mass * c.factor_M;
-            const double ya = y[i] + (double)e0, yb = y[i + 1] + (double)e1, yc = y[i + 2] + (double)e2;
-            r0 = (float)(bv[i] - (c.factor_K * t0 + mfm64 * ya));
-            r1 = (float)(bv[i + 1] - (c.factor_K * t1 + mfm64 * yb));
-            r2 = (float)(bv[i + 2] - (c.factor_K * t2 + mfm64 * yc));
-            // fold the FP32 increment into the FP64 iterate: later small
-            // corrections then keep their bits (an FP32 sum that has grown
-            // large would absorb them)
-            y[i] = ya;
-            y[i + 1] = yb;
-            y[i + 2] = yc;
-            e0 = e1 = e2 = 0.f;
+            if (!confirm) {
+                r0 += na * q0;
+                r1 += na * q1;
+                r2 += na * q2;
+                e0 = __fmaf_rn(alpha_s, d0, e0);
+                e1 = __fmaf_rn(alpha_s, d1, e1);
+                e2 = __fmaf_rn(alpha_s, d2, e2);
+                d[i] = d0; d[i + 1] = d1; d[i + 2] = d2;
+            }
+            b.ydelta[i] = e0;
+            b.ydelta[i + 1] = e1;
+            b.ydelta[i + 2] = e2;
+            r[i] = r0; r[i + 1] = r1; r[i + 2] = r2;
+            acc += r0 * r0 + r1 * r1 + r2 * r2;
         }
-        if (!confirm) {
-            r0 += na * q0;
-            r1 += na * q1;
-            r2 += na * q2;
-            e0 = __fmaf_rn(alpha_s, d0, e0);
-            e1 = __fmaf_rn(alpha_s, d1, e1);
-            e2 = __fmaf_rn(alpha_s, d2, e2);
-            d[i] = d0; d[i + 1] = d1; d[i + 2] = d2;
-        }
-        b.ydelta[i] = e0;
-        b.ydelta[i + 1] = e1;
-        b.ydelta[i + 2] = e2;
-        r[i] = r0; r[i + 1] = r1; r[i + 2] = r2;
-        acc += r0 * r0 + r1 * r1 + r2 * r2;
+        cur = nxt;
+        n = nn;
+        have = have_next;
     }
     const F2 rr = block_sum_f2(F2{acc, 0.f}, sh);
     if (threadIdx.x == 0) cshare[ci] = make_float2(rr.hi, rr.lo);
