@@ -620,34 +620,38 @@ struct WsLook {
     uint32_t g[2];
 };
 
-// The next live tile of the work list from entry i (stride G) for node
-// thread tn: i is advanced past it; sizes = 0 when the list is exhausted.
-__device__ __forceinline__ void ws_next(const BatchView<float>& b, uint32_t& i, uint32_t G, uint32_t n_act,
-                                        uint32_t tn, WsLook& L)
+// A node thread's look-up of work-list entry e, in two halves issued one
+// pipeline step apart (no half waits on loads it issued itself): the entry's
+// tile and metadata, then what depends on them. end: past the list.
+__device__ __forceinline__ void ws_meta(const BatchView<float>& b, uint32_t e, uint32_t n_act, WsLook& L)
 {
-    for (;;) {
-        L.sizes = 0u;
-        L.done = 0u;
-        if (i >= n_act) return;
-        L.tile = b.act_tiles[i];
-        i += G;
+    L.sizes = 0u;
+    L.done = 0u;
+    L.tile = ~0u;  // ~0u: past the end of the list
+    if (e < n_act) {
+        L.tile = b.act_tiles[e];
         const TileMeta tm = b.tiles[L.tile];
         L.mesh = tm.mesh;
         L.n0 = tm.n0;
         L.sizes = (uint32_t)tm.ne | ((uint32_t)tm.nn << 10) | ((uint32_t)tm.nown << 20);
-        const StepScalars& st = b.st[L.mesh];
-        L.done = st.done;
-        L.beta = st.beta_f;
-        L.boff = b.blob_off16[L.tile];
-        const uint32_t nn = tm.nn;
-#pragma unroll
-        for (int m = 0; m < 2; m++) {
-            const uint32_t j = tn + (uint32_t)m * kWsNode;
-            L.g[m] = j < nn ? bounds_idx(__ldg(b.tile_nodes + L.n0 + j), b.Ntot, kSiteBatchNode) : 0u;
-        }
-        if (!L.done) return;
     }
 }
+__device__ __forceinline__ void ws_resolve(const BatchView<float>& b, uint32_t tn, WsLook& L)
+{
+    L.g[0] = L.g[1] = 0u;
+    if (L.sizes == 0u) return;
+    const StepScalars& st = b.st[L.mesh];
+    L.done = st.done;
+    L.beta = st.beta_f;
+    L.boff = b.blob_off16[L.tile];
+    const uint32_t nn = (L.sizes >> 10) & 0x3ffu;
+#pragma unroll
+    for (int m = 0; m < 2; m++) {
+        const uint32_t j = tn + (uint32_t)m * kWsNode;
+        L.g[m] = j < nn ? bounds_idx(__ldg(b.tile_nodes + L.n0 + j), b.Ntot, kSiteBatchNode) : 0u;
+    }
+}
+__device__ __forceinline__ bool ws_live(const WsLook& L) { return L.sizes != 0u && L.done == 0u; }
 
 __global__ void __launch_bounds__(kWsThreads, 2) k_tile_spmv_ws(BatchView<float> b, const float* __restrict__ dvec,
                                                                 const float* __restrict__ rvec, float* __restrict__ part,
@@ -675,19 +679,28 @@ __global__ void __launch_bounds__(kWsThreads, 2) k_tile_spmv_ws(BatchView<float>
 
     if (tid < (uint32_t)kWsElem) {
         // ---- element warps ----
+        uint32_t bpar = 0u;  // bit k: parity of stage k's next blob arrival (dead entries have none)
         for (uint32_t t = 0;; t++) {
             const uint32_t bf = t & 1u, par = (t >> 1) & 1u;
-            // a tile staged (or the end), its blob arrived, its output buffer free
+            // an entry staged (a tile, a skipped entry, or the end), its blob
+            // arrived, its output buffer free
             bool ok = mbar_wait_bounded(&full_sd[bf], par, wait_polls);
             const WsDesc dsc = desc[bf];
-            const bool stop = dsc.state != 1u;
-            if (ok && !stop) ok = mbar_wait_bounded(&full_blob[bf], par, wait_polls);
+            const bool stop = dsc.state == 2u, live = dsc.state == 1u;
+            if (ok && live) {
+                ok = mbar_wait_bounded(&full_blob[bf], (bpar >> bf) & 1u, wait_polls);
+                bpar ^= 1u << bf;
+            }
             if (ok && !stop && t >= 2) ok = mbar_wait_bounded(&free_out[bf], ((t - 2) >> 1) & 1u, wait_polls);
             if (named_sync_or(2, kWsElem, !ok)) {
                 if (tid == 0) atomicExch(err, 1u);
                 break;
             }
             if (stop) break;
+            if (!live) {
+                if (tid == 0) mbar_arrive(&full_out[bf]);
+                continue;
+            }
             const uint32_t ne = dsc.sizes & 0x3ffu, nn = (dsc.sizes >> 10) & 0x3ffu;
             const unsigned char* stage = smem + bf * W::kStage;
             const float4* sd4 = reinterpret_cast<const float4*>(smem + W::kSd) + bf * kTileNodes;
@@ -743,7 +756,6 @@ __global__ void __launch_bounds__(kWsThreads, 2) k_tile_spmv_ws(BatchView<float>
     // ---- node warps ----
     const uint32_t tn = tid - kWsElem;
     const uint32_t n_act = *(volatile const uint32_t*)b.act_count;
-    uint32_t i = blockIdx.x;
     // the producer (node thread 0) issues each tile's blob copy
     auto issue = [&](const WsLook& L, uint32_t bf) {
         const uint32_t bytes = blob_bytes(L.sizes & 0x3ffu, (L.sizes >> 10) & 0x3ffu, L.sizes >> 20);
@@ -758,8 +770,8 @@ __global__ void __launch_bounds__(kWsThreads, 2) k_tile_spmv_ws(BatchView<float>
             const size_t g = 3 * (size_t)L.g[m];
 #pragma unroll
             for (int c3 = 0; c3 < 3; c3++) {
-                gd[m][c3] = (L.sizes && j < nn) ? __ldg(dvec + g + c3) : 0.f;
-                gr[m][c3] = (L.sizes && j < nn) ? __ldg(rvec + g + c3) : 0.f;
+                gd[m][c3] = (ws_live(L) && j < nn) ? __ldg(dvec + g + c3) : 0.f;
+                gr[m][c3] = (ws_live(L) && j < nn) ? __ldg(rvec + g + c3) : 0.f;
             }
         }
     };
@@ -772,7 +784,7 @@ __global__ void __launch_bounds__(kWsThreads, 2) k_tile_spmv_ws(BatchView<float>
         for (int m = 0; m < 2; m++) {
             const uint32_t j = tn + (uint32_t)m * kWsNode;
             float v = 0.f;
-            if (L.sizes && j < nn) {
+            if (ws_live(L) && j < nn) {
                 const float dx = __fmaf_rn(L.beta, gd[m][0], gr[m][0]);
                 const float dy = __fmaf_rn(L.beta, gd[m][1], gr[m][1]);
                 const float dz = __fmaf_rn(L.beta, gd[m][2], gr[m][2]);
@@ -784,7 +796,7 @@ __global__ void __launch_bounds__(kWsThreads, 2) k_tile_spmv_ws(BatchView<float>
         named_sync(1, kWsNode);
         if (tn == 0) {
             WsDesc d;
-            d.state = L.sizes ? 1u : 2u;
+            d.state = L.tile == ~0u ? 2u : (ws_live(L) ? 1u : 3u);
             d.tile = L.tile;
             d.sizes = L.sizes;
             d.pad = 0u;
@@ -792,34 +804,51 @@ __global__ void __launch_bounds__(kWsThreads, 2) k_tile_spmv_ws(BatchView<float>
             mbar_arrive(&full_sd[bf]);
         }
     };
-    WsLook cur, n1, n2, n3;
-    ws_next(b, i, G, n_act, tn, cur);
-    ws_next(b, i, G, n_act, tn, n1);
-    ws_next(b, i, G, n_act, tn, n2);
-    if (tn == 0 && cur.sizes) issue(cur, 0);
-    if (tn == 0 && n1.sizes) issue(n1, 1);
+    // Entries t = 0, 1, ... are the block's work-list entries blockIdx.x +
+    // t G. Per step t: stage entry t+1 (gathered one step ago), gather entry
+    // t+2 (resolved one step ago), resolve entry t+3, look up entry t+4,
+    // then wait for entry t's element outputs, sum them per node, release
+    // the buffers and copy entry t+2's blob into the freed stage.
+    WsLook L0, L1, L2, L3, L4;
+    const uint32_t e0 = blockIdx.x;
+    ws_meta(b, e0, n_act, L0);
+    ws_resolve(b, tn, L0);
+    ws_meta(b, e0 + G, n_act, L1);
+    ws_resolve(b, tn, L1);
+    ws_meta(b, e0 + 2 * G, n_act, L2);
+    ws_resolve(b, tn, L2);
+    ws_meta(b, e0 + 3 * G, n_act, L3);
+    uint32_t copies[2] = {0u, 0u};  // issued into each stage
+    if (tn == 0 && ws_live(L0)) {
+        issue(L0, 0);
+        copies[0]++;
+    }
+    if (tn == 0 && ws_live(L1)) {
+        issue(L1, 1);
+        copies[1]++;
+    }
     float gd[2][3], gr[2][3], hd[2][3], hr[2][3];
-    gather(cur, gd, gr);
-    stage(cur, gd, gr, 0);
-    gather(n1, gd, gr);
-    uint32_t copies[2] = {cur.sizes ? 1u : 0u, n1.sizes ? 1u : 0u};  // issued into each stage
-    for (uint32_t t = 0; cur.sizes != 0u; t++) {
+    gather(L0, gd, gr);
+    stage(L0, gd, gr, 0);
+    gather(L1, gd, gr);
+    for (uint32_t t = 0; L0.tile != ~0u; t++) {
         const uint32_t bf = t & 1u;
-        // the next tile staged (or the end announced) while the element
-        // warps work on this one; its buffers were released by their output
-        // of tile t-1, which this loop waited for one iteration ago
-        stage(n1, gd, gr, bf ^ 1u);
-        ws_next(b, i, G, n_act, tn, n3);
-        gather(n2, hd, hr);
-        // this tile's element outputs
+        // entry t+1 staged while the element warps work on entry t; its
+        // buffers were released by their output of entry t-1, which this
+        // loop waited for one step ago
+        stage(L1, gd, gr, bf ^ 1u);
+        gather(L2, hd, hr);
+        ws_resolve(b, tn, L3);
+        ws_meta(b, e0 + (t + 4) * G, n_act, L4);
+        // entry t's element outputs
         const bool ok = mbar_wait_bounded(&full_out[bf], (t >> 1) & 1u, wait_polls);
         if (named_sync_or(1, kWsNode, !ok)) {
             if (tn == 0) atomicExch(err, 1u);
             break;
         }
-        {
+        if (ws_live(L0)) {
             const unsigned char* stg = smem + bf * W::kStage;
-            const uint32_t ne = cur.sizes & 0x3ffu, nn = (cur.sizes >> 10) & 0x3ffu, nown = cur.sizes >> 20;
+            const uint32_t ne = L0.sizes & 0x3ffu, nn = (L0.sizes >> 10) & 0x3ffu, nown = L0.sizes >> 20;
             const uint32_t ne4 = blob_ne4(ne);
             const uint32_t* hdr = reinterpret_cast<const uint32_t*>(stg + blob_hdr_off(ne, nn));
             const uint16_t* lp = reinterpret_cast<const uint16_t*>(stg + blob_lptr_off(ne));
@@ -839,18 +868,19 @@ __global__ void __launch_bounds__(kWsThreads, 2) k_tile_spmv_ws(BatchView<float>
                 }
             }
         }
-        // every node thread is done with this tile's outputs and element data
+        // every node thread is done with entry t's outputs and element data
         named_sync(1, kWsNode);
         if (tn == 0) {
             mbar_arrive(&free_out[bf]);
-            if (n2.sizes) {
-                issue(n2, bf);
+            if (ws_live(L2)) {
+                issue(L2, bf);
                 copies[bf]++;
             }
         }
-        cur = n1;
-        n1 = n2;
-        n2 = n3;
+        L0 = L1;
+        L1 = L2;
+        L2 = L3;
+        L3 = L4;
 #pragma unroll
         for (int m = 0; m < 2; m++)
 #pragma unroll
