@@ -462,7 +462,7 @@ def run_ours(args):
         tile_elems, reorder, chunk_nodes = tuned["tile_elems"], bool(tuned["reorder"]), tuned["chunk_nodes"]
     t0 = time.perf_counter()
     batch = capi.Batch(scs, precision=prec, tile_elems=tile_elems, reorder=reorder, chunk_nodes=chunk_nodes,
-                       compute_energy=True, use_graph=not args.no_graph, warp_specialized=args.warp_specialized)
+                       compute_energy=True, use_graph=not args.no_graph)
     setup_s = time.perf_counter() - t0
     info = batch.info()
     stream_ptr = batch.stream()
@@ -904,8 +904,6 @@ def main():
                     help="skip the error of the timed workload (mixed against the FP64 path) and per config")
     ap.add_argument("--accuracy-steps", type=int, default=0, help="steps of the accuracy leg (0: warmup + steps)")
     ap.add_argument("--no-tune", action="store_true", help="default tiles (256 tets, Morton order)")
-    ap.add_argument("--warp-specialized", type=int, default=None,
-                    help="1/0: the warp-specialised tile product on/off (default: the library's)")
     ap.add_argument("--served-rate", type=float, default=20000.0, help="offered step requests per second")
     ap.add_argument("--served-seconds", type=float, default=3.0)
     ap.add_argument("--served-pool", type=int, default=4096)

@@ -386,9 +386,6 @@ typedef struct fem_batch_options {
                              tile shares itself (one kernel fewer per CG iteration: shorter
                              iterations when few meshes run, more work when many do; the
                              same results either way) */
-    uint32_t warp_specialized; /* mixed, tile_elems > 128: 1 = the tile product's blocks split into
-                             element warps and node warps that work on consecutive tiles at once
-                             (the same results bit for bit) */
     uint32_t persistent_loop; /* mixed, tile_elems > 128: 1 = the CG iterations of a launch run
                              in one persistent cooperative kernel (the phases of an iteration
                              separated by bounded grid barriers; the fused alpha) sized to the

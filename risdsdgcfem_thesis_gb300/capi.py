@@ -481,7 +481,7 @@ def device_info():
 class FemBatchOptions(C.Structure):
     _fields_ = [("precision", C.c_uint32), ("tile_elems", C.c_uint32), ("reorder", C.c_uint32),
                 ("use_graph", C.c_uint32), ("chunk_nodes", C.c_uint32), ("fuse_alpha", C.c_uint32),
-                ("warp_specialized", C.c_uint32), ("persistent_loop", C.c_uint32)]
+                ("persistent_loop", C.c_uint32)]
 
 
 _u8p = C.POINTER(C.c_uint8)
@@ -560,7 +560,7 @@ _BATCH_SIGNATURES = {
 
 
 def batch_options(precision=FEM_PRECISION_MIXED, tile_elems=256, reorder=True, use_graph=True, chunk_nodes=None,
-                  fuse_alpha=False, persistent_loop=False, warp_specialized=None):
+                  fuse_alpha=False, persistent_loop=False):
     o = FemBatchOptions()
     check(load().fem_batch_options_default(C.byref(o)))
     o.precision = precision
@@ -571,8 +571,6 @@ def batch_options(precision=FEM_PRECISION_MIXED, tile_elems=256, reorder=True, u
         o.chunk_nodes = chunk_nodes
     o.fuse_alpha = 1 if fuse_alpha else 0
     o.persistent_loop = 1 if persistent_loop else 0
-    if warp_specialized is not None:
-        o.warp_specialized = 1 if warp_specialized else 0
     return o
 
 
@@ -596,15 +594,13 @@ class Batch:
     def __init__(self, scenes_list, precision=FEM_PRECISION_MIXED, tile_elems=256, reorder=True, use_graph=True,
                  chunk_nodes=None,
                  compute_energy=True, refresh_every=None, degenerate_det_F=None, rotation_check=None,
-                 refresh_drop=None, rotation_fp32=None, fuse_alpha=False, persistent_loop=False,
-                 warp_specialized=None):
+                 refresh_drop=None, rotation_fp32=None, fuse_alpha=False, persistent_loop=False):
         lib = load()
         self.lib = lib
         self.scenes = list(scenes_list)
         self.precision = precision
         h = C.c_void_p()
-        opt = batch_options(precision, tile_elems, reorder, use_graph, chunk_nodes, fuse_alpha, persistent_loop,
-                            warp_specialized)
+        opt = batch_options(precision, tile_elems, reorder, use_graph, chunk_nodes, fuse_alpha, persistent_loop)
         check(lib.fem_batch_create(C.byref(opt), C.byref(h)))
         self.h = h
         self._knc = []

@@ -165,7 +165,6 @@ struct fem_batch_s {
         b.nchunks = nchunks;
         b.pipe_tile = opt.tile_elems <= (uint32_t)kPipeSmallTile ? kPipeSmallTile : kTileElems;
         b.fuse_alpha = opt.fuse_alpha ? 1u : 0u;
-        b.tile_ws = opt.warp_specialized ? 1u : 0u;
         b.Ntot = (uint32_t)Ntot;
         b.Ttot = (uint32_t)Ttot;
         b.nslots = nslots;

@@ -125,7 +125,6 @@ struct BatchView {
     uint64_t nslots;               // partial slots: Ntot owner slots + the overflow slots
     uint32_t pipe_tile;            // mixed: threads per block of the tile product (kPipeSmallTile or kTileElems)
     uint32_t fuse_alpha;           // mixed: the node pass forms alpha (no separate alpha kernel)
-    uint32_t tile_ws;              // mixed, 256-tet tiles: the warp-specialised tile product
     const TileMeta* tiles;
     const ChunkMeta* chunks;
     const MeshConsts* mc;

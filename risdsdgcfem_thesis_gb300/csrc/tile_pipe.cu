@@ -552,354 +552,6 @@ __global__ void __launch_bounds__(TILE, PipeShape<TILE>::kMinBlocks) k_tile_spmv
                          *(volatile const unsigned*)(err + 1));
 }
 
-// ---------------------------------------------------------------------------
-// The warp-specialised form of the tile product (256-tet tiles). A block of
-// 384 threads: warps 0-7 compute element products (one tet per thread),
-// warps 8-11 stage directions, sum the element outputs per node and drive
-// the tile copies. The two roles work on consecutive tiles at once -- the
-// node warps sum tile t while the element warps compute tile t+1 -- and hand
-// tiles over through mbarriers instead of block-wide barriers: the element
-// outputs go to an output buffer of their own (two, alternating), so a
-// tile's element data is released as soon as both roles are done with it.
-// Per value it computes what k_tile_spmv_pipe computes, in the same order:
-// the same partials and tile shares, bit for bit.
-constexpr int kWsElem = kTileElems;  // element threads (warps 0-7)
-constexpr int kWsNode = 128;         // node threads (warps 8-11), two local nodes each
-constexpr int kWsThreads = kWsElem + kWsNode;
-
-struct WsDesc {
-    uint32_t state;  // 1: a tile to do; 2: no more tiles
-    uint32_t tile, sizes, pad;
-};
-
-struct WsShape {
-    static constexpr uint32_t kStage = PipeShape<kTileElems>::kStage;
-    static constexpr uint32_t kOut = 2 * kStage;                  // float4 out[2][4 kTileElems]
-    static constexpr uint32_t kSd = kOut + 2u * 64u * kTileElems; // float4 sd4[2][kTileNodes]
-    static constexpr uint32_t kDd = kSd + 2u * 16u * kTileNodes;  // float dd[2][kTileNodes]
-    static constexpr uint32_t kDesc = kDd + 2u * 4u * kTileNodes; // WsDesc desc[2]
-    static constexpr uint32_t kBar = kDesc + 2u * sizeof(WsDesc); // 8 mbarriers
-    static constexpr uint32_t kWsh = kBar + 64u;                  // float2 wsh[2][8]
-    static constexpr uint32_t kSmem = kWsh + 2u * 8u * 8u;
-};
-static_assert(WsShape::kOut % 16 == 0 && WsShape::kSd % 16 == 0 && WsShape::kBar % 8 == 0, "ws alignment");
-static_assert(2 * (((WsShape::kSmem + 127) & ~127u) + 1024) <= 233472, "two ws blocks per SM");
-static_assert(kTileNodes == 2 * kWsNode, "two local nodes per node thread");
-
-__device__ __forceinline__ void mbar_arrive(uint64_t* bar)
-{
-    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
-}
-
-__device__ __forceinline__ void named_sync(uint32_t id, uint32_t n)
-{
-    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory");
-}
-
-// A barrier over the n threads of barrier id that also returns whether any
-// of them passed v = true.
-__device__ __forceinline__ bool named_sync_or(uint32_t id, uint32_t n, bool v)
-{
-    uint32_t r;
-    asm volatile(
-        "{\n\t.reg .pred p, q;\n\t"
-        "setp.ne.u32 p, %1, 0;\n\t"
-        "bar.red.or.pred q, %2, %3, p;\n\t"
-        "selp.u32 %0, 1, 0, q;\n\t}"
-        : "=r"(r)
-        : "r"((uint32_t)v), "r"(id), "r"(n)
-        : "memory");
-    return r != 0;
-}
-
-// A node thread's view of a tile: as TileLook, with the batch ids of its two
-// local nodes.
-struct WsLook {
-    uint32_t tile, mesh, n0, sizes, boff, done;
-    float beta;
-    uint32_t g[2];
-};
-
-// A node thread's look-up of work-list entry e, in two halves issued one
-// pipeline step apart (no half waits on loads it issued itself): the entry's
-// tile and metadata, then what depends on them. end: past the list.
-__device__ __forceinline__ void ws_meta(const BatchView<float>& b, uint32_t e, uint32_t n_act, WsLook& L)
-{
-    L.sizes = 0u;
-    L.done = 0u;
-    L.tile = ~0u;  // ~0u: past the end of the list
-    if (e < n_act) {
-        L.tile = b.act_tiles[e];
-        const TileMeta tm = b.tiles[L.tile];
-        L.mesh = tm.mesh;
-        L.n0 = tm.n0;
-        L.sizes = (uint32_t)tm.ne | ((uint32_t)tm.nn << 10) | ((uint32_t)tm.nown << 20);
-    }
-}
-__device__ __forceinline__ void ws_resolve(const BatchView<float>& b, uint32_t tn, WsLook& L)
-{
-    L.g[0] = L.g[1] = 0u;
-    if (L.sizes == 0u) return;
-    const StepScalars& st = b.st[L.mesh];
-    L.done = st.done;
-    L.beta = st.beta_f;
-    L.boff = b.blob_off16[L.tile];
-    const uint32_t nn = (L.sizes >> 10) & 0x3ffu;
-#pragma unroll
-    for (int m = 0; m < 2; m++) {
-        const uint32_t j = tn + (uint32_t)m * kWsNode;
-        L.g[m] = j < nn ? bounds_idx(__ldg(b.tile_nodes + L.n0 + j), b.Ntot, kSiteBatchNode) : 0u;
-    }
-}
-__device__ __forceinline__ bool ws_live(const WsLook& L) { return L.sizes != 0u && L.done == 0u; }
-
-__global__ void __launch_bounds__(kWsThreads, 2) k_tile_spmv_ws(BatchView<float> b, const float* __restrict__ dvec,
-                                                                const float* __restrict__ rvec, float* __restrict__ part,
-                                                                float2* __restrict__ tshare,
-                                                                cudaGraphConditionalHandle if_refresh, int set_if,
-                                                                const unsigned* __restrict__ refresh_flag,
-                                                                unsigned* __restrict__ err)
-{
-    using W = WsShape;
-    extern __shared__ __align__(128) unsigned char smem[];
-    uint64_t* full_blob = reinterpret_cast<uint64_t*>(smem + W::kBar);
-    uint64_t* full_sd = full_blob + 2;
-    uint64_t* full_out = full_blob + 4;
-    uint64_t* free_out = full_blob + 6;
-    WsDesc* desc = reinterpret_cast<WsDesc*>(smem + W::kDesc);
-    float2* wsh = reinterpret_cast<float2*>(smem + W::kWsh);
-    const uint32_t tid = threadIdx.x, G = gridDim.x;
-    const uint32_t wait_polls = *(volatile const unsigned*)(err + 1);
-    if (set_if && blockIdx.x == 0 && tid == 0) cudaGraphSetConditional(if_refresh, *refresh_flag ? 1u : 0u);
-    if (tid == 0) {
-        for (int k = 0; k < 8; k++) mbar_init(&full_blob[k], 1);
-        fence_mbar_init();
-    }
-    __syncthreads();
-
-    if (tid < (uint32_t)kWsElem) {
-        // ---- element warps ----
-        uint32_t bpar = 0u;  // bit k: parity of stage k's next blob arrival (dead entries have none)
-        for (uint32_t t = 0;; t++) {
-            const uint32_t bf = t & 1u, par = (t >> 1) & 1u;
-            // an entry staged (a tile, a skipped entry, or the end), its blob
-            // arrived, its output buffer free
-            bool ok = mbar_wait_bounded(&full_sd[bf], par, wait_polls);
-            const WsDesc dsc = desc[bf];
-            const bool stop = dsc.state == 2u, live = dsc.state == 1u;
-            if (ok && live) {
-                ok = mbar_wait_bounded(&full_blob[bf], (bpar >> bf) & 1u, wait_polls);
-                bpar ^= 1u << bf;
-            }
-            if (ok && !stop && t >= 2) ok = mbar_wait_bounded(&free_out[bf], ((t - 2) >> 1) & 1u, wait_polls);
-            if (named_sync_or(2, kWsElem, !ok)) {
-                if (tid == 0) atomicExch(err, 1u);
-                break;
-            }
-            if (stop) break;
-            if (!live) {
-                if (tid == 0) mbar_arrive(&full_out[bf]);
-                continue;
-            }
-            const uint32_t ne = dsc.sizes & 0x3ffu, nn = (dsc.sizes >> 10) & 0x3ffu;
-            const unsigned char* stage = smem + bf * W::kStage;
-            const float4* sd4 = reinterpret_cast<const float4*>(smem + W::kSd) + bf * kTileNodes;
-            const float* dd = reinterpret_cast<const float*>(smem + W::kDd) + bf * kTileNodes;
-            float4* so4 = reinterpret_cast<float4*>(smem + W::kOut) + bf * 4u * kTileElems;
-            const uint32_t ne4 = blob_ne4(ne);
-            const uint32_t* hdr = reinterpret_cast<const uint32_t*>(stage + blob_hdr_off(ne, nn));
-            const float* fac = reinterpret_cast<const float*>(hdr + 1);  // fK, m fM
-            float share = fac[1] * dd[tid];  // the node of this index, when the tile owns it
-            if (tid < ne) {
-                const float4* g4 = reinterpret_cast<const float4*>(stage) + tid;
-                const float4 q0 = g4[0], q1 = g4[ne4], q2 = g4[2 * ne4], q3 = g4[3 * ne4], q4 = g4[4 * ne4];
-                const uint32_t lw = reinterpret_cast<const uint32_t*>(stage + 80u * ne4)[tid];
-                const float R[9] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w, q2.x};
-                const float Di[9] = {q2.y, q2.z, q2.w, q3.x, q3.y, q3.z, q3.w, q4.x, q4.y};
-                const float knu = q4.z, k2 = q4.w, k1 = __fmaf_rn(2.f, k2, knu);
-                const int ids[4] = {(int)bounds_idx(lw & 0xffu, nn, kSiteLocalNode),
-                                    (int)bounds_idx((lw >> 8) & 0xffu, nn, kSiteLocalNode),
-                                    (int)bounds_idx((lw >> 16) & 0xffu, nn, kSiteLocalNode),
-                                    (int)bounds_idx(lw >> 24, nn, kSiteLocalNode)};
-                float dl[12], out[12];
-#pragma unroll
-                for (int k = 0; k < 4; k++) {
-                    const float4 v = sd4[ids[k]];
-                    dl[3 * k] = v.x;
-                    dl[3 * k + 1] = v.y;
-                    dl[3 * k + 2] = v.z;
-                }
-                elem_RKRt<float>(R, Di, k1, knu, k2, dl, out);
-                float eq = 0.f;
-#pragma unroll
-                for (int k = 0; k < 12; k++) eq = __fmaf_rn(dl[k], out[k], eq);
-                share = __fmaf_rn(fac[0], eq, share);
-#pragma unroll
-                for (int k = 0; k < 4; k++)
-                    so4[k * ne4 + tid] = make_float4(out[3 * k], out[3 * k + 1], out[3 * k + 2], 0.f);
-            }
-            float w = share;
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) w += __shfl_down_sync(0xffffffffu, w, o);
-            if ((tid & 31) == 0) wsh[bf * 8u + (tid >> 5)] = make_float2(w, 0.f);
-            named_sync(2, kWsElem);
-            if (tid == 0) {
-                F2 a = {0.f, 0.f};
-                for (int k = 0; k < kWsElem / 32; k++) a = f2_add(a, F2{wsh[bf * 8u + k].x, wsh[bf * 8u + k].y});
-                tshare[dsc.tile] = make_float2(a.hi, a.lo);
-                mbar_arrive(&full_out[bf]);
-            }
-        }
-        return;
-    }
-
-    // ---- node warps ----
-    const uint32_t tn = tid - kWsElem;
-    const uint32_t n_act = *(volatile const uint32_t*)b.act_count;
-    // the producer (node thread 0) issues each tile's blob copy
-    auto issue = [&](const WsLook& L, uint32_t bf) {
-        const uint32_t bytes = blob_bytes(L.sizes & 0x3ffu, (L.sizes >> 10) & 0x3ffu, L.sizes >> 20);
-        mbar_expect_tx(&full_blob[bf], bytes);
-        bulk_copy_g2s(smem + bf * W::kStage, b.blob + 16ull * L.boff, bytes, &full_blob[bf]);
-    };
-    auto gather = [&](const WsLook& L, float (&gd)[2][3], float (&gr)[2][3]) {
-        const uint32_t nn = (L.sizes >> 10) & 0x3ffu;
-#pragma unroll
-        for (int m = 0; m < 2; m++) {
-            const uint32_t j = tn + (uint32_t)m * kWsNode;
-            const size_t g = 3 * (size_t)L.g[m];
-#pragma unroll
-            for (int c3 = 0; c3 < 3; c3++) {
-                gd[m][c3] = (ws_live(L) && j < nn) ? __ldg(dvec + g + c3) : 0.f;
-                gr[m][c3] = (ws_live(L) && j < nn) ? __ldg(rvec + g + c3) : 0.f;
-            }
-        }
-    };
-    // stages a tile into buffer bf from the gathered d and r (or the end)
-    auto stage = [&](const WsLook& L, const float (&gd)[2][3], const float (&gr)[2][3], uint32_t bf) {
-        float4* sd4 = reinterpret_cast<float4*>(smem + W::kSd) + bf * kTileNodes;
-        float* dd = reinterpret_cast<float*>(smem + W::kDd) + bf * kTileNodes;
-        const uint32_t nn = (L.sizes >> 10) & 0x3ffu, nown = L.sizes >> 20;
-#pragma unroll
-        for (int m = 0; m < 2; m++) {
-            const uint32_t j = tn + (uint32_t)m * kWsNode;
-            float v = 0.f;
-            if (ws_live(L) && j < nn) {
-                const float dx = __fmaf_rn(L.beta, gd[m][0], gr[m][0]);
-                const float dy = __fmaf_rn(L.beta, gd[m][1], gr[m][1]);
-                const float dz = __fmaf_rn(L.beta, gd[m][2], gr[m][2]);
-                sd4[j] = make_float4(dx, dy, dz, 0.f);
-                if (j < nown) v = dx * dx + dy * dy + dz * dz;
-            }
-            dd[j] = v;
-        }
-        named_sync(1, kWsNode);
-        if (tn == 0) {
-            WsDesc d;
-            d.state = L.tile == ~0u ? 2u : (ws_live(L) ? 1u : 3u);
-            d.tile = L.tile;
-            d.sizes = L.sizes;
-            d.pad = 0u;
-            desc[bf] = d;
-            mbar_arrive(&full_sd[bf]);
-        }
-    };
-    // Entries t = 0, 1, ... are the block's work-list entries blockIdx.x +
-    // t G. Per step t: stage entry t+1 (gathered one step ago), gather entry
-    // t+2 (resolved one step ago), resolve entry t+3, look up entry t+4,
-    // then wait for entry t's element outputs, sum them per node, release
-    // the buffers and copy entry t+2's blob into the freed stage.
-    WsLook L0, L1, L2, L3, L4;
-    const uint32_t e0 = blockIdx.x;
-    ws_meta(b, e0, n_act, L0);
-    ws_resolve(b, tn, L0);
-    ws_meta(b, e0 + G, n_act, L1);
-    ws_resolve(b, tn, L1);
-    ws_meta(b, e0 + 2 * G, n_act, L2);
-    ws_resolve(b, tn, L2);
-    ws_meta(b, e0 + 3 * G, n_act, L3);
-    uint32_t copies[2] = {0u, 0u};  // issued into each stage
-    if (tn == 0 && ws_live(L0)) {
-        issue(L0, 0);
-        copies[0]++;
-    }
-    if (tn == 0 && ws_live(L1)) {
-        issue(L1, 1);
-        copies[1]++;
-    }
-    float gd[2][3], gr[2][3], hd[2][3], hr[2][3];
-    gather(L0, gd, gr);
-    stage(L0, gd, gr, 0);
-    gather(L1, gd, gr);
-    for (uint32_t t = 0; L0.tile != ~0u; t++) {
-        const uint32_t bf = t & 1u;
-        // entry t+1 staged while the element warps work on entry t; its
-        // buffers were released by their output of entry t-1, which this
-        // loop waited for one step ago
-        stage(L1, gd, gr, bf ^ 1u);
-        gather(L2, hd, hr);
-        ws_resolve(b, tn, L3);
-        ws_meta(b, e0 + (t + 4) * G, n_act, L4);
-        // entry t's element outputs
-        const bool ok = mbar_wait_bounded(&full_out[bf], (t >> 1) & 1u, wait_polls);
-        if (named_sync_or(1, kWsNode, !ok)) {
-            if (tn == 0) atomicExch(err, 1u);
-            break;
-        }
-        if (ws_live(L0)) {
-            const unsigned char* stg = smem + bf * W::kStage;
-            const uint32_t ne = L0.sizes & 0x3ffu, nn = (L0.sizes >> 10) & 0x3ffu, nown = L0.sizes >> 20;
-            const uint32_t ne4 = blob_ne4(ne);
-            const uint32_t* hdr = reinterpret_cast<const uint32_t*>(stg + blob_hdr_off(ne, nn));
-            const uint16_t* lp = reinterpret_cast<const uint16_t*>(stg + blob_lptr_off(ne));
-            const uint16_t* li = lp + (nn + 1);
-            const float4* so4 = reinterpret_cast<const float4*>(smem + W::kOut) + bf * 4u * kTileElems;
-#pragma unroll
-            for (int m = 0; m < 2; m++) {
-                const uint32_t j = tn + (uint32_t)m * kWsNode;
-                if (j < nn) {
-                    float a0 = 0.f, a1 = 0.f, a2 = 0.f;
-                    node_sum(so4, li, lp[j], lp[j + 1], ne4, a0, a1, a2);
-                    const size_t o = 3 * (size_t)bounds_idx(j < nown ? hdr[0] + j : hdr[3 + j - nown], b.nslots,
-                                                            kSitePartialSlot);
-                    part[o] = a0;
-                    part[o + 1] = a1;
-                    part[o + 2] = a2;
-                }
-            }
-        }
-        // every node thread is done with entry t's outputs and element data
-        named_sync(1, kWsNode);
-        if (tn == 0) {
-            mbar_arrive(&free_out[bf]);
-            if (ws_live(L2)) {
-                issue(L2, bf);
-                copies[bf]++;
-            }
-        }
-        L0 = L1;
-        L1 = L2;
-        L2 = L3;
-        L3 = L4;
-#pragma unroll
-        for (int m = 0; m < 2; m++)
-#pragma unroll
-            for (int c3 = 0; c3 < 3; c3++) {
-                gd[m][c3] = hd[m][c3];
-                gr[m][c3] = hr[m][c3];
-            }
-    }
-    // no block leaves while a copy into its shared memory is in flight: the
-    // last copy into each stage has completed (the earlier ones did before
-    // their stage was reused)
-    if (tn == 0) {
-        bool drained = true;
-        for (int k = 0; k < 2; k++)
-            if (copies[k]) drained &= mbar_wait_bounded(&full_blob[k], (copies[k] - 1u) & 1u, kDrainPolls);
-        if (!drained) atomicExch(err, 2u);
-    }
-}
-
 // Per running mesh: d^T A d from its tiles' shares (fixed order), alpha and
 // the breakdown test (ILSS_CG.h:91-97), once for the node pass's blocks of
 // the mesh. One warp per mesh.
@@ -1762,35 +1414,11 @@ static int pipe_grid()
     return grid;
 }
 
-static int ws_grid()
-{
-    static int grid = 0;
-    if (!grid) {
-        int dev = 0, sms = 0, per_sm = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaFuncSetAttribute(k_tile_spmv_ws, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)WsShape::kSmem);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tile_spmv_ws, kWsThreads, WsShape::kSmem);
-        grid = (sms > 0 ? sms : 152) * (per_sm > 0 ? per_sm : 1);
-    }
-    return grid;
-}
-
 void launch_tile_spmv_pipe(const BatchView<float>& b, const float* d, const float* r, float* part, float2* tshare,
                            cudaGraphConditionalHandle if_refresh, int set_if, const unsigned* refresh_flag,
                            unsigned* err, cudaStream_t s)
 {
     const bool small = b.pipe_tile == (uint32_t)kPipeSmallTile;
-    if (b.tile_ws && !small) {
-        const int g = ws_grid();
-        const uint32_t grid = b.ntiles < (uint32_t)g ? (b.ntiles ? b.ntiles : 1) : (uint32_t)g;
-        prof_begin("tile_spmv_mixed", s);
-        k_tile_spmv_ws<<<grid, kWsThreads, WsShape::kSmem, s>>>(b, d, r, part, tshare, if_refresh, set_if,
-                                                                refresh_flag, err);
-        prof_end("tile_spmv_mixed", s);
-        launch_counter()++;
-        return;
-    }
     const int g = small ? pipe_grid<kPipeSmallTile>() : pipe_grid<kTileElems>();
     const uint32_t grid = b.ntiles < (uint32_t)g ? (b.ntiles ? b.ntiles : 1) : (uint32_t)g;
     prof_begin("tile_spmv_mixed", s);
@@ -1847,7 +1475,6 @@ void prepare_tile_pipe()
 {
     (void)pipe_grid<kPipeSmallTile>();
     (void)pipe_grid<kTileElems>();
-    (void)ws_grid();
     (void)node_grid();
 }
 

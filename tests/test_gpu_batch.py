@@ -377,25 +377,3 @@ def test_fused_alpha_gives_the_same_bits(fem_lib):
     finally:
         a.close()
         f.close()
-
-
-def test_warp_specialized_tile_product_gives_the_same_bits(fem_lib):
-    """The warp-specialised tile product (element warps and node warps on
-    consecutive tiles, mbarrier hand-offs) against the block-synchronous
-    one: the same partials and shares, so the same states and iteration
-    counts, on a batch with several tiles per block and meshes that leave
-    their loops at different iterations."""
-    rng = np.random.default_rng(61)
-    scs = [scenes.random_block(rng, idx=i, dims=d) for i, d in
-           enumerate([(30, 20, 20), (25, 25, 20), (8, 6, 5), (20, 12, 10), (4, 4, 4), (16, 16, 16)])]
-    a = fem_lib.Batch(scs, fem_lib.FEM_PRECISION_MIXED, warp_specialized=False, compute_energy=False)
-    b = fem_lib.Batch(scs, fem_lib.FEM_PRECISION_MIXED, warp_specialized=True, compute_energy=False)
-    assert a.info()["tiles"] > 600
-    for _ in range(3):
-        a.step(1)
-        b.step(1)
-        for i in range(len(scs)):
-            xa, va = a.state(i)
-            xb, vb = b.state(i)
-            assert np.array_equal(xa, xb) and np.array_equal(va, vb), i
-            assert a.stats(i)["cg_iterations"] == b.stats(i)["cg_iterations"], i
