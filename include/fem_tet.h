@@ -118,7 +118,8 @@ enum fem_rotation {
      * (Rotation.cpp:364-495), the direction of collapse found from the
      * previous step's positions by the time-of-collapse cubic
      * (TetrahedronElementSet3.cpp:477-743) and kept while the element stays
-     * degenerate; I where no direction is known. FP64 solid only. */
+     * degenerate; I where no direction is known. On the solid and in batches
+     * and servers of either precision (there in FP64, per mesh). */
     FEM_ROTATION_DAPD = 1
 };
 
@@ -417,6 +418,14 @@ int fem_batch_get_state(fem_batch b, uint32_t mesh, double* x, double* v);
  * element set's cached R and det F, TetrahedronElementSet3.cpp:219-281).
  * Either pointer may be null. */
 int fem_batch_get_rotations(fem_batch b, uint32_t mesh, double* R, double* detF);
+/* A DAPD mesh's hidden state, as fem_solid_get/set_dapd_state: the positions
+ * its last step started from (N*3) and the direction of collapse per element
+ * (T*2), in the caller's node and element order. fem_batch_set_state resets
+ * the previous positions to the new x (as on the solid), so a resume calls
+ * fem_batch_set_state, then fem_batch_set_dapd_state. FEM_E_ARG for a mesh
+ * that does not use DAPD. */
+int fem_batch_get_dapd_state(fem_batch b, uint32_t mesh, double* prev_x, uint8_t* doc);
+int fem_batch_set_dapd_state(fem_batch b, uint32_t mesh, const double* prev_x, const uint8_t* doc);
 /* 1: steps run as the captured CUDA graph (device-side CG loop); 0: the same
  * kernels launched one by one with the CG loop on the host (per-kernel
  * profiling and timing). */

@@ -541,6 +541,8 @@ _BATCH_SIGNATURES = {
     "fem_batch_set_state": (C.c_int, [C.c_void_p, C.c_uint32, _dp, _dp]),
     "fem_batch_get_state": (C.c_int, [C.c_void_p, C.c_uint32, _dp, _dp]),
     "fem_batch_get_rotations": (C.c_int, [C.c_void_p, C.c_uint32, _dp, _dp]),
+    "fem_batch_get_dapd_state": (C.c_int, [C.c_void_p, C.c_uint32, _dp, C.POINTER(C.c_uint8)]),
+    "fem_batch_set_dapd_state": (C.c_int, [C.c_void_p, C.c_uint32, _dp, C.POINTER(C.c_uint8)]),
     "fem_batch_set_active": (C.c_int, [C.c_void_p, _u8p]),
     "fem_batch_step_async": (C.c_int, [C.c_void_p, C.c_uint32]),
     "fem_batch_synchronize": (C.c_int, [C.c_void_p]),
@@ -682,6 +684,20 @@ class Batch:
         d = np.empty(t)
         check(self.lib.fem_batch_get_rotations(self.h, i, _ptr(R), _ptr(d)))
         return R, d
+
+    def dapd_state(self, i):
+        """DAPD mesh i's previous positions (N, 3) and directions of collapse (T, 2)."""
+        sc = self.scenes[i]
+        px = np.empty((sc.num_nodes, 3))
+        doc = np.empty((sc.num_tets, 2), np.uint8)
+        check(self.lib.fem_batch_get_dapd_state(self.h, i, _ptr(px), doc.ctypes.data_as(C.POINTER(C.c_uint8))))
+        return px, doc
+
+    def set_dapd_state(self, i, prev_x=None, doc=None):
+        px = _f64(prev_x)
+        d = None if doc is None else np.ascontiguousarray(doc, dtype=np.uint8)
+        check(self.lib.fem_batch_set_dapd_state(self.h, i, _ptr(px),
+                                                None if d is None else d.ctypes.data_as(C.POINTER(C.c_uint8))))
 
     def set_active(self, mask=None):
         if mask is None:

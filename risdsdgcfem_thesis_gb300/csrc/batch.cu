@@ -109,6 +109,9 @@ uint32_t spread10(uint32_t v)
 
 }  // namespace
 
+static_assert(kMeshRotationMsvd == FEM_ROTATION_MSVD && kMeshRotationDapd == FEM_ROTATION_DAPD,
+              "per-mesh rotation values are enum fem_rotation's");
+
 struct fem_batch_s {
     fem_batch_options opt{};
     std::vector<HostMesh> meshes;
@@ -139,6 +142,9 @@ struct fem_batch_s {
     Dev<unsigned char> r_s, d_s, q_s, part_s, ydelta_s;  // S-typed
     Dev<unsigned> counter, any_flag, refresh_flag, mcount, err;
     Dev<unsigned> gbar;  // persistent loop: grid-barrier arrivals, generation, go flag
+    Dev<double> prev_x;  // DAPD meshes: positions at the start of their last step (batch node order)
+    Dev<uchar2> doc;     // DAPD meshes: direction of collapse per element (batch element order)
+    bool any_dapd = false;
     Dev<unsigned char> blob;
     Dev<uint32_t> blob_off16;
     Dev<uint32_t> act_tiles, act_chunks, act_count;
@@ -192,6 +198,8 @@ struct fem_batch_s {
         b.ydelta = opt.precision == FEM_PRECISION_MIXED ? reinterpret_cast<S*>(ydelta_s.p) : nullptr;
         b.blob = opt.precision == FEM_PRECISION_MIXED ? blob.p : nullptr;
         b.blob_off16 = blob_off16.p;
+        b.prev_x = prev_x.p;
+        b.doc = doc.p;
         const bool mixed = opt.precision == FEM_PRECISION_MIXED;
         b.act_tiles = mixed ? act_tiles.p : nullptr;
         b.act_chunks = mixed ? act_chunks.p : nullptr;
@@ -224,6 +232,7 @@ struct fem_batch_s {
         x.release(); v.release(); bvec.release(); y.release(); part64.release(); cpart.release(); tpart.release();
         knc_target.release(); r_s.release(); d_s.release(); q_s.release(); part_s.release(); ydelta_s.release(); counter.release();
         any_flag.release(); refresh_flag.release(); mcount.release(); err.release(); gbar.release(); blob.release();
+        prev_x.release(); doc.release();
         blob_off16.release();
         act_tiles.release(); act_chunks.release(); act_count.release(); list_dirty.release(); slice.release();
         start_tiles.release(); start_chunks.release(); launch_tiles.release(); launch_chunks.release();
@@ -353,7 +362,7 @@ int enqueue_step(fem_batch B, cudaStream_t s, bool capture)
     auto start_section = [&](cudaStream_t ss) {
         L::begin_eval(b, B->x.p, ss);
         L::tile_force(b, B->x.p, B->part64.p, nullptr, ss);
-        L::node_b(b, B->part64.p, B->v.p, B->bvec.p, B->y.p, ss);
+        L::node_b(b, B->part64.p, B->v.p, B->x.p, B->bvec.p, B->y.p, ss);
         L::knc(b, B->K, B->x.p, B->bvec.p, B->y.p, ss);
         L::tile_spmv_y64(b, B->y.p, B->part64.p, 0, nullptr, ss);
         L::node_residual(b, B->part64.p, B->bvec.p, B->y.p, r, d, B->cpart.p, ls, ss);
@@ -524,8 +533,12 @@ int fem_batch_add_mesh(fem_batch b, const double* rest, uint32_t N, const uint32
     if (p->integrator != FEM_INTEGRATOR_QIE_V)
         return batch_fail(FEM_E_ARG, "integrator %u: batches step with QIE_V; the FIE integrators run on fem_solid",
                           p->integrator);
-    if (p->rotation != FEM_ROTATION_MSVD)
-        return batch_fail(FEM_E_ARG, "rotation %u: batches use MSVD; DAPD runs on fem_solid", p->rotation);
+    if (p->rotation != FEM_ROTATION_MSVD && p->rotation != FEM_ROTATION_DAPD)
+        return batch_fail(FEM_E_ARG, "unknown rotation %u", p->rotation);
+    if (p->rotation == FEM_ROTATION_DAPD &&
+        !(std::isfinite(p->dapd_threshold_det_F) && std::isfinite(p->dapd_l_factor) &&
+          std::isfinite(p->dapd_nl_factor) && std::isfinite(p->dapd_nl_exponent)))
+        return batch_fail(FEM_E_ARG, "non-finite DAPD parameters");
     if (p->ls_solver != FEM_LS_CG)
         return batch_fail(FEM_E_ARG, "ls_solver %u: batches use CG; MINRES runs on fem_solid", p->ls_solver);
     if (p->material != FEM_MATERIAL_C_WRP)
@@ -813,6 +826,13 @@ int fem_batch_finalize(fem_batch b)
         c.degenerate_det_F = p.degenerate_det_F;
         c.rot_check = (float)p.rotation_check;
         c.rot_fp32 = p.rotation_fp32 ? 1u : 0u;
+        c.rotation = p.rotation;
+        // the reference's DAPD factors are float (ms::fem::Params)
+        c.dapd_thr = p.dapd_threshold_det_F;
+        c.dapd_fL = (double)(float)p.dapd_l_factor;
+        c.dapd_fNL = (double)(float)p.dapd_nl_factor;
+        c.dapd_eNL = (double)(float)p.dapd_nl_exponent;
+        if (p.rotation == FEM_ROTATION_DAPD) b->any_dapd = true;
         c.refresh_drop_sq = fp64 ? 0.0 : p.refresh_drop * p.refresh_drop;
         c.max_iter = p.ls_max_iter;
         c.refresh_every = fp64 ? 0u : p.refresh_every;
@@ -1042,6 +1062,17 @@ int fem_batch_finalize(fem_batch b)
     BCKC(b->fixed.upload(fixed, s));
     BCKC(b->rest.upload(rest_all, s));
     BCKC(b->x.upload(rest_all, s));
+    std::vector<uchar2> doc_none;
+    if (b->any_dapd) {
+        // DAPD's previous positions start at the rest positions (Create,
+        // LeafDSH_Solid3D_FEM.cpp:136-147), no element has a direction of
+        // collapse
+        BCKC(b->prev_x.alloc(N3));
+        BCKC(cudaMemcpyAsync(b->prev_x.p, b->x.p, sizeof(double) * N3, cudaMemcpyDeviceToDevice, s));
+        BCKC(b->doc.alloc(b->Ttot));
+        doc_none.assign(b->Ttot, make_uchar2(3, 0));
+        BCKC(b->doc.upload(doc_none, s));
+    }
     BCKC(cudaMemsetAsync(b->v.p, 0, sizeof(double) * N3, s));
     BCKC(cudaMemsetAsync(b->y.p, 0, sizeof(double) * N3, s));
     BCKC(cudaMemsetAsync(b->counter.p, 0, sizeof(unsigned), s));
@@ -1054,7 +1085,7 @@ int fem_batch_finalize(fem_batch b)
                       b->gtets.bytes() + b->Dinv_s.bytes() + b->mat_s.bytes() + b->R_s.bytes() +
                       b->Dinv64.bytes() + b->vol.bytes() + b->detF.bytes() + b->tile_nodes.bytes() +
                       b->lptr0.bytes() + b->ov_ptr.bytes() + b->ov_map.bytes() + b->knc_node.bytes() +
-                      b->perm.bytes() +
+                      b->perm.bytes() + b->prev_x.bytes() + b->doc.bytes() +
                       b->knc_mesh.bytes() + b->knc_target.bytes() + b->lconn.bytes() + b->lptr.bytes() +
                       b->lidx.bytes() + b->fixed.bytes() + b->rest.bytes() + b->x.bytes() + b->v.bytes() +
                       b->bvec.bytes() + b->y.bytes() + b->r_s.bytes() + b->d_s.bytes() + b->q_s.bytes() +
@@ -1137,6 +1168,73 @@ int fem_batch_set_state(fem_batch b, uint32_t mesh, const double* x, const doubl
             for (int a = 0; a < 3; a++) tmp[3 * i + a] = src[k][3 * (size_t)u + a];
         }
         BCK(cudaMemcpyAsync(dst[k] + off, tmp.data(), bytes, cudaMemcpyHostToDevice, b->stream));
+        // a DAPD mesh's previous positions restart at the new x, as on the
+        // solid (fem_solid_set_state); fem_batch_set_dapd_state restores them
+        if (k == 0 && c.rotation == FEM_ROTATION_DAPD && b->prev_x.p)
+            BCK(cudaMemcpyAsync(b->prev_x.p + off, tmp.data(), bytes, cudaMemcpyHostToDevice, b->stream));
+        BCK(cudaStreamSynchronize(b->stream));
+    }
+    return FEM_OK;
+}
+
+int fem_batch_get_dapd_state(fem_batch b, uint32_t mesh, double* prev_x, uint8_t* doc)
+{
+    if (int e = check_ready(b)) return e;
+    if (mesh >= b->M) return batch_fail(FEM_E_ARG, "mesh %u out of range", mesh);
+    const MeshConsts& c = b->mc_host[mesh];
+    if (c.rotation != FEM_ROTATION_DAPD || !b->prev_x.p)
+        return batch_fail(FEM_E_ARG, "mesh %u does not use the DAPD rotation", mesh);
+    if (prev_x) {
+        std::vector<double> tmp(3 * (size_t)c.N);
+        BCK(cudaMemcpyAsync(tmp.data(), b->prev_x.p + 3 * (size_t)c.node0, sizeof(double) * tmp.size(),
+                            cudaMemcpyDeviceToHost, b->stream));
+        BCK(cudaStreamSynchronize(b->stream));
+        for (uint32_t u = 0; u < c.N; u++) {
+            const size_t i = b->inv_h[c.node0 + u] - c.node0;
+            for (int a = 0; a < 3; a++) prev_x[3 * (size_t)u + a] = tmp[3 * i + a];
+        }
+    }
+    if (doc) {
+        std::vector<uchar2> tmp(c.T);
+        BCK(cudaMemcpyAsync(tmp.data(), b->doc.p + c.elem0, sizeof(uchar2) * c.T, cudaMemcpyDeviceToHost, b->stream));
+        BCK(cudaStreamSynchronize(b->stream));
+        const uint32_t* perm = b->eperm_h.data() + c.elem0;
+        for (uint32_t i = 0; i < c.T; i++) {
+            doc[2 * (size_t)perm[i]] = tmp[i].x;
+            doc[2 * (size_t)perm[i] + 1] = tmp[i].y;
+        }
+    }
+    return FEM_OK;
+}
+
+int fem_batch_set_dapd_state(fem_batch b, uint32_t mesh, const double* prev_x, const uint8_t* doc)
+{
+    if (int e = check_ready(b)) return e;
+    if (mesh >= b->M) return batch_fail(FEM_E_ARG, "mesh %u out of range", mesh);
+    const MeshConsts& c = b->mc_host[mesh];
+    if (c.rotation != FEM_ROTATION_DAPD || !b->prev_x.p)
+        return batch_fail(FEM_E_ARG, "mesh %u does not use the DAPD rotation", mesh);
+    if (prev_x) {
+        std::vector<double> tmp(3 * (size_t)c.N);
+        for (uint32_t u = 0; u < c.N; u++) {
+            const size_t i = b->inv_h[c.node0 + u] - c.node0;
+            for (int a = 0; a < 3; a++) tmp[3 * i + a] = prev_x[3 * (size_t)u + a];
+        }
+        BCK(cudaMemcpyAsync(b->prev_x.p + 3 * (size_t)c.node0, tmp.data(), sizeof(double) * tmp.size(),
+                            cudaMemcpyHostToDevice, b->stream));
+        BCK(cudaStreamSynchronize(b->stream));
+    }
+    if (doc) {
+        std::vector<uchar2> tmp(c.T);
+        const uint32_t* perm = b->eperm_h.data() + c.elem0;
+        for (uint32_t i = 0; i < c.T; i++) {
+            const uint8_t v0 = doc[2 * (size_t)perm[i]], v1 = doc[2 * (size_t)perm[i] + 1];
+            // none (3, 0), V-F (v, v) or E-E (v0 < v1), vertex ids 0..3
+            if (!((v0 == 3 && v1 == 0) || (v0 <= 3 && v1 <= 3 && v0 <= v1)))
+                return batch_fail(FEM_E_ARG, "element %u: (%u, %u) is not a direction of collapse", perm[i], v0, v1);
+            tmp[i] = make_uchar2(v0, v1);
+        }
+        BCK(cudaMemcpyAsync(b->doc.p + c.elem0, tmp.data(), sizeof(uchar2) * c.T, cudaMemcpyHostToDevice, b->stream));
         BCK(cudaStreamSynchronize(b->stream));
     }
     return FEM_OK;
@@ -1234,6 +1332,9 @@ int fem_batch_set_state_all(fem_batch b, const double* x, const double* v)
     if (x) {
         BCK(cudaMemcpyAsync(b->stage_x.p, x, bytes, cudaMemcpyHostToDevice, b->stream));
         launch_permute(b->perm.p, b->Ntot, b->stage_x.p, b->x.p, true, b->stream);
+        // DAPD meshes' previous positions restart at the new x (the other
+        // meshes never read them)
+        if (b->prev_x.p) BCK(cudaMemcpyAsync(b->prev_x.p, b->x.p, bytes, cudaMemcpyDeviceToDevice, b->stream));
     }
     if (v) {
         BCK(cudaMemcpyAsync(b->stage_v.p, v, bytes, cudaMemcpyHostToDevice, b->stream));

@@ -75,6 +75,10 @@ __host__ __device__ constexpr uint32_t blob_bytes(uint32_t ne, uint32_t nn, uint
     return (blob_hdr_off(ne, nn) + 12u + 4u * (nn - nown) + 15u) & ~15u;
 }
 
+// Per-mesh rotation methods (the values of enum fem_rotation).
+constexpr uint32_t kMeshRotationMsvd = 0;
+constexpr uint32_t kMeshRotationDapd = 1;
+
 struct TileMeta {
     uint32_t mesh;
     uint32_t e0;      // first element (global)
@@ -116,6 +120,8 @@ struct MeshConsts {
     float rot_check;    // mixed: FP64 re-solve when an FP32 rotation moves more than this under a small change of F
     uint32_t rot_fp32;  // mixed: 1 = FP32 rotations with FP64 re-solves, 0 = FP64 rotations
     double refresh_drop_sq;  // mixed: FP64 residual when |r|^2 fell below this times its value at the last one
+    uint32_t rotation;       // kMeshRotationMsvd or kMeshRotationDapd (FP64 in either precision)
+    double dapd_thr, dapd_fL, dapd_fNL, dapd_eNL;  // DAPD: threshold on det F, offset factors, exponent
 
 };
 
@@ -123,6 +129,8 @@ template <typename S>
 struct BatchView {
     uint32_t M, ntiles, nchunks, Ntot, Ttot;
     uint64_t nslots;               // partial slots: Ntot owner slots + the overflow slots
+    double* prev_x;                // [3 Ntot] DAPD: positions at the start of each mesh's last step; null without DAPD
+    uchar2* doc;                   // [Ttot] DAPD: direction of collapse per element (batch order)
     uint32_t pipe_tile;            // mixed: threads per block of the tile product (kPipeSmallTile or kTileElems)
     uint32_t fuse_alpha;           // mixed: the node pass forms alpha (no separate alpha kernel)
     const TileMeta* tiles;

@@ -363,7 +363,7 @@ __device__ __forceinline__ void sum_parts(const BatchView<S>& b, const P* __rest
 // b = dt (m g - f_e-product) + m v ; y = v
 template <typename S>
 __global__ void k_node_b(BatchView<S> b, const double* __restrict__ part64, const double* __restrict__ v,
-                         double* __restrict__ bv, double* __restrict__ y)
+                         const double* __restrict__ x, double* __restrict__ bv, double* __restrict__ y)
 {
     const uint32_t nl = b.list_count[1];
     for (uint32_t il = blockIdx.x; il < nl; il += gridDim.x) {
@@ -371,10 +371,19 @@ __global__ void k_node_b(BatchView<S> b, const double* __restrict__ part64, cons
         const ChunkMeta ch = b.chunks[ci];
         if (b.active[ch.mesh] != 1) continue;
         const MeshConsts& c = b.mc[ch.mesh];
+        // DAPD: this step's BeginEvaluation has read the previous positions;
+        // the next one compares with this step's start (m_vecPos0 = x,
+        // LeafDSH_Solid3D_FEM.cpp:927-935)
+        const bool dapd = b.prev_x && c.rotation == kMeshRotationDapd;
         for (size_t n = ch.n0 + threadIdx.x; n < ch.n1; n += blockDim.x) {
             double f0, f1, f2;
             sum_parts(b, part64, n, f0, f1, f2);
             const size_t i = 3 * n;
+            if (dapd) {
+                b.prev_x[i] = x[i];
+                b.prev_x[i + 1] = x[i + 1];
+                b.prev_x[i + 2] = x[i + 2];
+            }
             bv[i] = (c.mass * c.gravity[0] - f0) * c.dt + c.mass * v[i];
             bv[i + 1] = (c.mass * c.gravity[1] - f1) * c.dt + c.mass * v[i + 1];
             bv[i + 2] = (c.mass * c.gravity[2] - f2) * c.dt + c.mass * v[i + 2];
@@ -804,10 +813,10 @@ void BatchLaunch<S>::tile_potential(const BatchView<S>& b, const double* x, doub
 }
 
 template <typename S>
-void BatchLaunch<S>::node_b(const BatchView<S>& b, const double* part64, const double* v, double* bv, double* y,
-                            cudaStream_t s)
+void BatchLaunch<S>::node_b(const BatchView<S>& b, const double* part64, const double* v, const double* x, double* bv,
+                            double* y, cudaStream_t s)
 {
-    k_node_b<S><<<grid_chunks(b.nchunks), kNodeThreads, 0, s>>>(b, part64, v, bv, y);
+    k_node_b<S><<<grid_chunks(b.nchunks), kNodeThreads, 0, s>>>(b, part64, v, x, bv, y);
     launch_counter()++;
 }
 

@@ -76,8 +76,8 @@ struct BatchLaunch {
     static void tile_force(const BatchView<S>& b, const double* x, double* part64, double* tile_energy,
                            cudaStream_t s);
     static void tile_potential(const BatchView<S>& b, const double* x, double* tile_pe, cudaStream_t s);
-    static void node_b(const BatchView<S>& b, const double* part64, const double* v, double* bv, double* y,
-                       cudaStream_t s);
+    static void node_b(const BatchView<S>& b, const double* part64, const double* v, const double* x, double* bv,
+                       double* y, cudaStream_t s);
     static void knc(const BatchView<S>& b, uint32_t K, const double* x, double* bv, double* y, cudaStream_t s);
     static void node_residual(const BatchView<S>& b, const double* part64, const double* bv, const double* y, S* r,
                               S* d, double* cpart, const LoopSync& ls, cudaStream_t s);

@@ -192,7 +192,30 @@ __global__ void __launch_bounds__(256, 3) k_begin_eval_batch(BatchView<S> b, con
             double F[9], detF;
             deformation_gradient(xs, Di, F, detF);
             S Rs[9];
-            if (sizeof(S) == sizeof(double)) {
+            const MeshConsts& mcm = b.mc[tm.mesh];
+            if (b.prev_x && mcm.rotation == kMeshRotationDapd) {
+                // DAPD in FP64 in either precision (ComputeRotations_DAPD,
+                // TetrahedronElementSet3.cpp:860-892), from the positions at
+                // the start of the mesh's previous step
+                V3<double> xp[4];
+#pragma unroll
+                for (int i = 0; i < 4; i++) {
+                    const size_t n3 = 3 * (size_t)ids[i];
+                    xp[i] = mk<double>(b.prev_x[n3], b.prev_x[n3 + 1], b.prev_x[n3 + 2]);
+                }
+                DapdParams dp;
+                dp.thr = mcm.dapd_thr;
+                dp.fL = mcm.dapd_fL;
+                dp.fNL = mcm.dapd_fNL;
+                dp.eNL = mcm.dapd_eNL;
+                uchar2 d = b.doc[e];
+                double R[9];
+                dapd_rotation(xp, xs, Di, F, detF, b.vol[e], dp, d, R);
+                b.doc[e] = d;
+#pragma unroll
+                for (int c = 0; c < 9; c++) Rs[c] = (S)R[c];
+                if (sizeof(S) != sizeof(double)) atomicAdd(&s_res, 1u);
+            } else if (sizeof(S) == sizeof(double)) {
                 double R[9];
                 msvd_rotation(F, R);
 #pragma unroll

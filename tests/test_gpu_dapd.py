@@ -87,10 +87,109 @@ def test_dapd_rotations_match_oracle(fem_lib, oracle):
     assert (g.doc()[:, 0] <= g.doc()[:, 1]).sum() > 10
 
 
-def test_batch_and_server_reject_dapd(fem_lib):
+def _sheared_crush_evaluation(oracle, sc):
+    """The oracle after 26 steps of sc: (x25, x26, v26, the directions of
+    collapse before the 27th BeginEvaluation, and the oracle evaluated at
+    x26 against x25)."""
+    o25, o26 = oracle.Solid(sc, "port"), oracle.Solid(sc, "port")
+    for k in range(26):
+        if k < 25:
+            o25.step()
+        o26.step()
+    x25, _ = o25.state()
+    x26, v26 = o26.state()
+    doc_before = o26.doc()
+    o26.begin_eval(x26)
+    return x25, x26, v26, doc_before, o26
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_batched_dapd_offset_rotations_match_oracle(fem_lib, oracle, precision):
+    """DAPD in a batch (FP64 rotations in either precision): the sheared
+    crush restored to the oracle's state after 26 steps (positions, the
+    previous step's positions, the directions of collapse, through
+    fem_batch_set_state / set_dapd_state), next to an MSVD mesh; the step's
+    BeginEvaluation gives the oracle's rotations (1e-12; the mixed batch
+    stores them in FP32) and directions of collapse, the offset rotation on
+    the collapsing elements."""
+    sc = scenes.sheared_crush()
+    x25, x26, v26, doc_before, o26 = _sheared_crush_evaluation(oracle, sc)
+    other = scenes.cantilever_160()
+    bt = fem_lib.Batch([other, sc], precision=precision, compute_energy=False)
+    bt.set_state(1, x26, v26)
+    bt.set_dapd_state(1, x25, doc_before)
+    bt.step_index = 26
+    bt.step(1)
+    R, detF = bt.rotations(1)
+    Ro = o26.rotations()
+    tol = 1e-12 if precision == 0 else 1e-6
+    assert np.abs(R - Ro).max() < tol
+    assert np.abs(detF - o26.detF()).max() < 1e-12
+    _, doc = bt.dapd_state(1)
+    assert np.array_equal(doc, o26.doc())
+    held = (doc[:, 0] <= doc[:, 1]) & (o26.detF() <= np.float32(0.1))
+    assert held.sum() > 40
+    assert (np.abs(Ro[held] - np.eye(3)).reshape(-1, 9).max(axis=1) > 1e-6).sum() > 0.9 * held.sum()
+
+
+def test_batched_dapd_steps_like_the_solid_and_resumes(fem_lib):
+    """A DAPD mesh in an FP64 batch steps as the FP64 solid does before its
+    elements collapse (the crushed cube's first 20 steps, 1e-10), and a
+    batch run resumed from a checkpoint of (x, v, previous positions,
+    directions of collapse) continues bit for bit, through the collapse."""
+    sc = crushed_cube(0)
+    s = fem_lib.Solid(sc)
+    bt = fem_lib.Batch([sc, scenes.cantilever_160()], precision=fem_lib.FEM_PRECISION_FP64, compute_energy=False)
+    s.step(20)
+    bt.step(20)
+    xs, vs = s.state()
+    xb, vb = bt.state(0)
+    assert rel(xb, xs) < 1e-10 and rel(vb, vs) < 1e-8
+    whole = fem_lib.Batch([sc], precision=fem_lib.FEM_PRECISION_FP64, compute_energy=False)
+    whole.step(28)
+    first = fem_lib.Batch([sc], precision=fem_lib.FEM_PRECISION_FP64, compute_energy=False)
+    first.step(24)
+    x, v = first.state(0)
+    px, doc = first.dapd_state(0)
+    resumed = fem_lib.Batch([sc], precision=fem_lib.FEM_PRECISION_FP64, compute_energy=False)
+    resumed.set_state(0, x, v)
+    resumed.set_dapd_state(0, px, doc)
+    resumed.step_index = 24
+    resumed.step(4)
+    xa, va = whole.state(0)
+    xr, vr = resumed.state(0)
+    assert np.array_equal(xa, xr) and np.array_equal(va, vr)
+    assert (whole.dapd_state(0)[1][:, 0] <= whole.dapd_state(0)[1][:, 1]).sum() > 0
+
+
+def test_mixed_batch_and_server_with_dapd_match_oracle(fem_lib, oracle):
+    """The mixed path with a DAPD mesh: within 1e-5 of the FP64 oracle after
+    10 steps of a hanging cantilever, in a batch and through the server
+    (whose result is the mixed batch's, bit for bit)."""
     sc = dataclasses.replace(scenes.cantilever_160(), rotation=1)
+    o = oracle.Solid(sc, "port")
+    for _ in range(10):
+        o.step()
+    xo, vo = o.state()
+    bt = fem_lib.Batch([sc], precision=fem_lib.FEM_PRECISION_MIXED, compute_energy=False, chunk_nodes=256)
+    bt.step(10)
+    xb, vb = bt.state(0)
+    assert rel(xb, xo) < 1e-5 and rel(vb, vo) < 1e-4
+    srv = fem_lib.Server(precision=fem_lib.FEM_PRECISION_MIXED)
+    sid = srv.add(sc)
+    srv.admit()
+    for k in range(10):
+        srv.submit(sid, k)
+    done = srv.drain()
+    assert len(done) == 10 and all(c["status"] == 0 for c in done)
+    xs, vs = srv.state(sid)
+    assert np.array_equal(xs, xb) and np.array_equal(vs, vb)
+
+
+def test_batch_dapd_state_calls_check_the_mesh(fem_lib):
+    bt = fem_lib.Batch([scenes.cantilever_160()], precision=fem_lib.FEM_PRECISION_FP64)
     with pytest.raises(fem_lib.FemError) as e:
-        fem_lib.Batch([sc], precision=fem_lib.FEM_PRECISION_FP64)
+        bt.dapd_state(0)
     assert e.value.code == fem_lib.FEM_E_ARG
 
 
