@@ -283,8 +283,8 @@ int fem_server_add_scene(fem_server s, const double* rest, uint32_t N, const uin
     if (N == 0 || T == 0) return batch_fail(FEM_E_ARG, "empty mesh (N=%u, T=%u)", N, T);
     if (p->integrator != FEM_INTEGRATOR_QIE_V)
         return batch_fail(FEM_E_ARG, "integrator %u: the server steps with QIE_V", p->integrator);
-    if (p->rotation != FEM_ROTATION_MSVD)
-        return batch_fail(FEM_E_ARG, "rotation %u: the server uses MSVD", p->rotation);
+    if (p->rotation != FEM_ROTATION_MSVD && p->rotation != FEM_ROTATION_DAPD)
+        return batch_fail(FEM_E_ARG, "unknown rotation %u", p->rotation);
     if (p->ls_solver != FEM_LS_CG)
         return batch_fail(FEM_E_ARG, "ls_solver %u: the server uses CG", p->ls_solver);
     if (p->material != FEM_MATERIAL_C_WRP)
