@@ -111,6 +111,8 @@ uint32_t spread10(uint32_t v)
 
 static_assert(kMeshRotationMsvd == FEM_ROTATION_MSVD && kMeshRotationDapd == FEM_ROTATION_DAPD,
               "per-mesh rotation values are enum fem_rotation's");
+static_assert(kTileMaterialWrp == FEM_MATERIAL_C_WRP && kTileMaterialLcm == FEM_MATERIAL_C_LCM,
+              "per-tile material values are enum fem_material's");
 
 struct fem_batch_s {
     fem_batch_options opt{};
@@ -145,6 +147,7 @@ struct fem_batch_s {
     Dev<double> prev_x;  // DAPD meshes: positions at the start of their last step (batch node order)
     Dev<uchar2> doc;     // DAPD meshes: direction of collapse per element (batch element order)
     bool any_dapd = false;
+    bool any_lcm = false;
     Dev<unsigned char> blob;
     Dev<uint32_t> blob_off16;
     Dev<uint32_t> act_tiles, act_chunks, act_count;
@@ -171,6 +174,7 @@ struct fem_batch_s {
         b.nchunks = nchunks;
         b.pipe_tile = opt.tile_elems <= (uint32_t)kPipeSmallTile ? kPipeSmallTile : kTileElems;
         b.fuse_alpha = opt.fuse_alpha ? 1u : 0u;
+        b.has_lcm = any_lcm ? 1u : 0u;
         b.Ntot = (uint32_t)Ntot;
         b.Ttot = (uint32_t)Ttot;
         b.nslots = nslots;
@@ -541,8 +545,11 @@ int fem_batch_add_mesh(fem_batch b, const double* rest, uint32_t N, const uint32
         return batch_fail(FEM_E_ARG, "non-finite DAPD parameters");
     if (p->ls_solver != FEM_LS_CG)
         return batch_fail(FEM_E_ARG, "ls_solver %u: batches use CG; MINRES runs on fem_solid", p->ls_solver);
-    if (p->material != FEM_MATERIAL_C_WRP)
-        return batch_fail(FEM_E_ARG, "material %u: batches use C_WRP; C_LCM runs on fem_solid", p->material);
+    if (p->material != FEM_MATERIAL_C_WRP && p->material != FEM_MATERIAL_C_LCM)
+        return batch_fail(FEM_E_ARG, "material %u: batches take C_WRP and C_LCM; C_LCMH and C_CCM run on fem_solid",
+                          p->material);
+    if (p->material == FEM_MATERIAL_C_LCM && b->opt.persistent_loop)
+        return batch_fail(FEM_E_ARG, "the persistent loop takes C_WRP meshes only");
     for (size_t i = 0; i < 4 * (size_t)T; i++)
         if (tets[i] >= N) return batch_fail(FEM_E_INDEX, "tet %zu names node %u >= N=%u", i / 4, tets[i], N);
     HostMesh m;
@@ -663,8 +670,11 @@ int fem_batch_finalize(fem_batch b)
             double Di[9];
             inverse3(D, Di);
             const double V = vol_orig[e];
-            const double E = hm.E.empty() ? p.young_modulus : hm.E[e];
-            const double nu = hm.nu.empty() ? p.poisson_ratio : hm.nu[e];
+            // C_LCM takes the set's scalar E and nu (per-element values would
+            // only re-bake K0, which it does not use)
+            const bool scalar_mat = p.material == FEM_MATERIAL_C_LCM;
+            const double E = (hm.E.empty() || scalar_mat) ? p.young_modulus : hm.E[e];
+            const double nu = (hm.nu.empty() || scalar_mat) ? p.poisson_ratio : hm.nu[e];
             const double a = E / ((1.0 + nu) * (1.0 - 2.0 * nu));
             for (int c = 0; c < 9; c++) Dinv_aos.push_back(Di[c]);
             mat_aos.push_back(V * (a * (1.0 - nu)));
@@ -745,7 +755,7 @@ int fem_batch_finalize(fem_batch b)
                     lc.w = remap[lc.w];
                 }
                 tm.nown = (uint16_t)owned.size();
-                tm.pad = 0;
+                tm.material = hm.p.material == FEM_MATERIAL_C_LCM ? kTileMaterialLcm : kTileMaterialWrp;
                 tm.own0 = owned.empty() ? 0u : (uint32_t)(node0 + intern[owned[0]]);
                 tm.ov0 = (uint32_t)ov_node.size();
                 for (uint32_t u : shared) ov_node.push_back((uint32_t)(node0 + intern[u]));
@@ -827,6 +837,11 @@ int fem_batch_finalize(fem_batch b)
         c.rot_check = (float)p.rotation_check;
         c.rot_fp32 = p.rotation_fp32 ? 1u : 0u;
         c.rotation = p.rotation;
+        c.material = p.material == FEM_MATERIAL_C_LCM ? kTileMaterialLcm : kTileMaterialWrp;
+        // the element set's Lame pair (from its Params, TetrahedronElementSet3.cpp:143-148)
+        c.lame_mu = 0.5 * p.young_modulus / (1 + p.poisson_ratio);
+        c.lame_lambda = p.young_modulus * p.poisson_ratio / ((1.0 + p.poisson_ratio) * (1.0 - 2.0 * p.poisson_ratio));
+        if (c.material == kTileMaterialLcm) b->any_lcm = true;
         // the reference's DAPD factors are float (ms::fem::Params)
         c.dapd_thr = p.dapd_threshold_det_F;
         c.dapd_fL = (double)(float)p.dapd_l_factor;

@@ -87,8 +87,13 @@ struct TileMeta {
     uint16_t ne, nn;  // elements, local nodes
     uint32_t own0;    // global id of the first owned node (local nodes [0, nown))
     uint32_t ov0;     // first entry in ov_map of the shared local nodes [nown, nn)
-    uint16_t nown, pad;
+    uint16_t nown;
+    uint16_t material;  // the mesh's kTileMaterial*
 };
+
+// Per-tile element products (the values of enum fem_material).
+constexpr uint16_t kTileMaterialWrp = 0;
+constexpr uint16_t kTileMaterialLcm = 1;
 
 // Partial slot of local node i of a tile: owned nodes write theirs in node
 // order (slot = batch node id), shared nodes the overflow slot ov_map gives
@@ -121,6 +126,8 @@ struct MeshConsts {
     uint32_t rot_fp32;  // mixed: 1 = FP32 rotations with FP64 re-solves, 0 = FP64 rotations
     double refresh_drop_sq;  // mixed: FP64 residual when |r|^2 fell below this times its value at the last one
     uint32_t rotation;       // kMeshRotationMsvd or kMeshRotationDapd (FP64 in either precision)
+    uint32_t material;       // kTileMaterialWrp or kTileMaterialLcm
+    double lame_mu, lame_lambda;  // C_LCM: from the mesh's scalar E and nu (per-element values re-bake only K0)
     double dapd_thr, dapd_fL, dapd_fNL, dapd_eNL;  // DAPD: threshold on det F, offset factors, exponent
 
 };
@@ -133,6 +140,7 @@ struct BatchView {
     uchar2* doc;                   // [Ttot] DAPD: direction of collapse per element (batch order)
     uint32_t pipe_tile;            // mixed: threads per block of the tile product (kPipeSmallTile or kTileElems)
     uint32_t fuse_alpha;           // mixed: the node pass forms alpha (no separate alpha kernel)
+    uint32_t has_lcm;              // some mesh takes the C_LCM product
     const TileMeta* tiles;
     const ChunkMeta* chunks;
     const MeshConsts* mc;

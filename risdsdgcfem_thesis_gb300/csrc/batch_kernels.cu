@@ -33,6 +33,7 @@
 #include "df.cuh"
 #include "elem_math.cuh"
 #include "msvd.cuh"
+#include "lcm.cuh"
 #include "refresh_product.cuh"
 
 namespace femgb {
@@ -170,7 +171,10 @@ __global__ void __launch_bounds__(256) k_tile_spmv(BatchView<S> b, const S* __re
             dl[3 * i + 2] = sd[2 * kTileNodes + ids[i]];
         }
         S out[12];
-        elem_RKRt<S>(R, Di, k1, knu, k2, dl, out);
+        if (tm.material == kTileMaterialLcm)
+            elem_lcm(b, tm.mesh, e, R, Di, knu, k2, dl, out);
+        else
+            elem_RKRt<S>(R, Di, k1, knu, k2, dl, out);
 #pragma unroll
         for (int c = 0; c < 12; c++) so[c * kTileElems + threadIdx.x] = out[c];
     }
@@ -223,7 +227,36 @@ __global__ void __launch_bounds__(256) k_tile_force(BatchView<S> b, const double
         // the force of a starting step, or the energy of a finished one
         if (part64 ? b.active[tm.mesh] != 1 : !b.st[tm.mesh].finished) continue;
         double energy = 0.0;
-        if (threadIdx.x < tm.ne) {
+        if (threadIdx.x < tm.ne && tm.material == kTileMaterialLcm) {
+            // C_LCM_f_e and C_LCM_V (TetrahedronElementSet3.cpp:1154-1178,
+            // 1489-1507) in FP64 in either precision, from F at x
+            const size_t e = tm.e0 + threadIdx.x;
+            const size_t T = b.Ttot;
+            const MeshConsts& mcm = b.mc[tm.mesh];
+            double R[9], Di[9];
+#pragma unroll
+            for (int c = 0; c < 9; c++) R[c] = (double)b.R[c * T + e];
+#pragma unroll
+            for (int c = 0; c < 9; c++) Di[c] = b.Dinv64[c * T + e];
+            const int4 g = b.gtets[e];
+            const int ids[4] = {(int)bounds_idx((uint32_t)g.x, b.Ntot, kSiteBatchNode),
+                                (int)bounds_idx((uint32_t)g.y, b.Ntot, kSiteBatchNode),
+                                (int)bounds_idx((uint32_t)g.z, b.Ntot, kSiteBatchNode),
+                                (int)bounds_idx((uint32_t)g.w, b.Ntot, kSiteBatchNode)};
+            V3<double> xs[4];
+#pragma unroll
+            for (int i = 0; i < 4; i++)
+                xs[i] = mk<double>(x[3 * (size_t)ids[i]], x[3 * (size_t)ids[i] + 1], x[3 * (size_t)ids[i] + 2]);
+            double F[9], detF;
+            deformation_gradient(xs, Di, F, detF);
+            energy = lcm_energy(R, F, b.vol[e], mcm.lame_mu, mcm.lame_lambda);
+            if (part64) {
+                double out[12];
+                lcm_force(R, F, Di, b.vol[e], mcm.lame_mu, mcm.lame_lambda, out);
+#pragma unroll
+                for (int c = 0; c < 12; c++) y64_set(so[c * kTileElems + threadIdx.x], out[c]);
+            }
+        } else if (threadIdx.x < tm.ne) {
             const size_t e = tm.e0 + threadIdx.x;
             const size_t T = b.Ttot;
             S R[9];

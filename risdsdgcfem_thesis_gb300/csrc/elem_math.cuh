@@ -82,5 +82,43 @@ __device__ __forceinline__ void elem_RKRt(const C* R, const C* Di, C k1, C knu, 
     rotate_out(R, P, out);
 }
 
+// The C_LCM differential (C_LCM_df_x, TetrahedronElementSet3.cpp:1838-1873,
+// truncated) with V folded into the Lame scalars, kl = V lambda and
+// km = V mu: dF = dDs Dm^-1, dP = 2 km dF + kl tr(R^T dF) R, and the nodal
+// products dP Dm^-T (node 0: minus their sum), the convention of
+// elem_RKRt. For the mixed path's types; the FP64 batch takes lcm_dforce,
+// the FP64 solid's own arithmetic.
+template <typename S, typename C = S>
+__device__ __forceinline__ void elem_lcm_dforce(const C* R, const C* Di, C kl, C km, const S* d, S* out)
+{
+    S dDs[9];
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+        for (int j = 0; j < 3; j++) dDs[3 * a + j] = d[3 * (j + 1) + a] - d[a];
+    S dF[9];
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+        for (int b = 0; b < 3; b++) dF[3 * a + b] = dDs[3 * a] * Di[b] + dDs[3 * a + 1] * Di[3 + b] + dDs[3 * a + 2] * Di[6 + b];
+    S tr = R[0] * dF[0];
+#pragma unroll
+    for (int c = 1; c < 9; c++) tr = tr + R[c] * dF[c];
+    const C km2 = (C)2 * km;
+    const S ktr = kl * tr;
+    S dP[9];
+#pragma unroll
+    for (int c = 0; c < 9; c++) dP[c] = km2 * dF[c] + ktr * R[c];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        S acc0 = dP[3 * a] * Di[0] + dP[3 * a + 1] * Di[1] + dP[3 * a + 2] * Di[2];
+        S acc1 = dP[3 * a] * Di[3] + dP[3 * a + 1] * Di[4] + dP[3 * a + 2] * Di[5];
+        S acc2 = dP[3 * a] * Di[6] + dP[3 * a + 1] * Di[7] + dP[3 * a + 2] * Di[8];
+        out[3 + a] = acc0;
+        out[6 + a] = acc1;
+        out[9 + a] = acc2;
+        out[a] = -(acc0 + acc1 + acc2);
+    }
+}
 
 }  // namespace femgb

@@ -7,6 +7,7 @@
 #include "bounds.cuh"
 #include "df.cuh"
 #include "elem_math.cuh"
+#include "lcm.cuh"
 
 namespace femgb {
 
@@ -27,6 +28,23 @@ __device__ __forceinline__ double y_full(const BatchView<S>& b, const double* y,
 // Whether the mesh's next iteration recomputes its residual in FP64 (set by
 // the last block of the mesh in the node pass, see refresh_decide).
 __device__ __forceinline__ bool refresh_now(const MeshConsts&, const StepScalars& s) { return s.refresh_next != 0; }
+
+// The C_LCM product of element e of `mesh` (the tile's material): in FP64
+// the FP64 solid's own arithmetic (V, mu, lambda apart), otherwise the
+// folded form of elem_math.cuh on the element's V lambda and V mu.
+template <typename S>
+__device__ __forceinline__ void elem_lcm(const BatchView<S>& b, uint32_t mesh, size_t e, const double* R,
+                                         const double* Di, double, double, const double* dl, double* out)
+{
+    const MeshConsts& c = b.mc[mesh];
+    lcm_dforce(R, Di, b.vol[e], c.lame_mu, c.lame_lambda, dl, out);
+}
+template <typename S, typename V>
+__device__ __forceinline__ void elem_lcm(const BatchView<S>&, uint32_t, size_t, const float* R, const float* Di,
+                                         float kl, float km, const V* dl, V* out)
+{
+    elem_lcm_dforce<V, float>(R, Di, kl, km, dl, out);
+}
 
 // Product of the iterate y for the residual b - A y (same element data):
 // mode SPMV_Y64_ALL for every active mesh (initial residual of a step);
@@ -108,7 +126,10 @@ __device__ __forceinline__ void tile_spmv_y64_pass(const BatchView<S>& b, const 
                 dl[3 * i + 2] = sd[2 * kTileNodes + ids[i]];
             }
             V out[12];
-            elem_RKRt<V, S>(R, Di, k1, knu, k2, dl, out);
+            if (tm.material == kTileMaterialLcm)
+                elem_lcm(b, tm.mesh, e, R, Di, knu, k2, dl, out);
+            else
+                elem_RKRt<V, S>(R, Di, k1, knu, k2, dl, out);
 #pragma unroll
             for (int c = 0; c < 12; c++) so[c * kTileElems + threadIdx.x] = out[c];
         }

@@ -254,7 +254,7 @@ static_assert(8 * (((PipeShape<128>::kSmem + 127) & ~127u) + 1024) <= 233472, "e
 struct TileLook {
     uint32_t tile;      // tile id
     uint32_t mesh, n0;  // the tile's mesh and first entry in the tile node list
-    uint32_t sizes;     // ne | nn << 10 | nown << 20; 0: not an entry of the work list
+    uint32_t sizes;     // ne | nn << 10 | nown << 20 | material << 30; 0: not an entry of the work list
     uint32_t boff;      // blob offset / 16
     uint32_t g;         // batch node id of this thread's local node
     uint32_t done;      // the mesh has left its loop (the list may still hold it)
@@ -263,7 +263,8 @@ struct TileLook {
 
 __device__ __forceinline__ uint32_t look_ne(const TileLook& L) { return L.sizes & 0x3ffu; }
 __device__ __forceinline__ uint32_t look_nn(const TileLook& L) { return (L.sizes >> 10) & 0x3ffu; }
-__device__ __forceinline__ uint32_t look_nown(const TileLook& L) { return L.sizes >> 20; }
+__device__ __forceinline__ uint32_t look_nown(const TileLook& L) { return (L.sizes >> 20) & 0x3ffu; }
+__device__ __forceinline__ bool look_lcm(const TileLook& L) { return (L.sizes >> 30) == kTileMaterialLcm; }
 // A tile to do (valid once resolved).
 __device__ __forceinline__ bool look_live(const TileLook& L) { return L.sizes != 0u && L.done == 0u; }
 
@@ -277,7 +278,7 @@ __device__ __forceinline__ void look_meta(const BatchView<float>& b, uint32_t i,
         const TileMeta tm = b.tiles[L.tile];
         L.mesh = tm.mesh;
         L.n0 = tm.n0;
-        L.sizes = (uint32_t)tm.ne | ((uint32_t)tm.nn << 10) | ((uint32_t)tm.nown << 20);
+        L.sizes = (uint32_t)tm.ne | ((uint32_t)tm.nn << 10) | ((uint32_t)tm.nown << 20) | ((uint32_t)tm.material << 30);
     }
 }
 
@@ -343,7 +344,7 @@ __device__ __forceinline__ void tile_pipe_init(unsigned char* smem)
 // read-only path, for a kernel whose other phases write them (the
 // persistent loop); the pointer parameters carry no __restrict__ for the
 // same reason (the kernels that call a pass alone have it on theirs).
-template <int TILE, bool kCoherent = false>
+template <int TILE, bool kCoherent = false, bool kLcm = false>
 __device__ __forceinline__ void tile_pipe_pass(const BatchView<float>& b, const float* dvec, const float* rvec,
                                                float* part, float2* tshare, unsigned* err,
                                                unsigned char* smem, uint32_t& phase, const uint32_t block,
@@ -457,7 +458,10 @@ __device__ __forceinline__ void tile_pipe_pass(const BatchView<float>& b, const 
                 dl[3 * k + 1] = v.y;
                 dl[3 * k + 2] = v.z;
             }
-            elem_RKRt<float>(R, Di, k1, knu, k2, dl, out);
+            if (kLcm && look_lcm(cur))
+                elem_lcm_dforce<float>(R, Di, knu, k2, dl, out);
+            else
+                elem_RKRt<float>(R, Di, k1, knu, k2, dl, out);
             float eq = 0.f;
 #pragma unroll
             for (int k = 0; k < 12; k++) eq = __fmaf_rn(dl[k], out[k], eq);
@@ -536,7 +540,7 @@ __device__ __forceinline__ void tile_pipe_pass(const BatchView<float>& b, const 
     }
 }
 
-template <int TILE>
+template <int TILE, bool kLcm>
 __global__ void __launch_bounds__(TILE, PipeShape<TILE>::kMinBlocks) k_tile_spmv_pipe(BatchView<float> b, const float* __restrict__ dvec,
                                                            const float* __restrict__ rvec, float* __restrict__ part,
                                                            float2* __restrict__ tshare,
@@ -548,8 +552,8 @@ __global__ void __launch_bounds__(TILE, PipeShape<TILE>::kMinBlocks) k_tile_spmv
     if (set_if && blockIdx.x == 0 && threadIdx.x == 0) cudaGraphSetConditional(if_refresh, *refresh_flag ? 1u : 0u);
     tile_pipe_init<TILE>(smem);
     uint32_t phase = 0u;
-    tile_pipe_pass<TILE>(b, dvec, rvec, part, tshare, err, smem, phase, blockIdx.x, gridDim.x,
-                         *(volatile const unsigned*)(err + 1));
+    tile_pipe_pass<TILE, false, kLcm>(b, dvec, rvec, part, tshare, err, smem, phase, blockIdx.x, gridDim.x,
+                                      *(volatile const unsigned*)(err + 1));
 }
 
 // Per running mesh: d^T A d from its tiles' shares (fixed order), alpha and
@@ -1396,7 +1400,7 @@ cudaError_t launch_cg_resident(const BatchView<float>& b, const CoopLoopArgs& a,
 
 uint32_t tile_pipe_smem_bytes() { return PipeShape<256>::kSmem; }
 
-template <int TILE>
+template <int TILE, bool kLcm = false>
 static int pipe_grid()
 {
     static int grid = 0;
@@ -1404,9 +1408,10 @@ static int pipe_grid()
         int dev = 0, sms = 0, per_sm = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaFuncSetAttribute(k_tile_spmv_pipe<TILE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        cudaFuncSetAttribute(k_tile_spmv_pipe<TILE, kLcm>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)PipeShape<TILE>::kSmem);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tile_spmv_pipe<TILE>, TILE, PipeShape<TILE>::kSmem);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tile_spmv_pipe<TILE, kLcm>, TILE,
+                                                      PipeShape<TILE>::kSmem);
         if (sms <= 0) sms = 152;
         if (per_sm <= 0) per_sm = 1;
         grid = sms * per_sm;
@@ -1418,15 +1423,24 @@ void launch_tile_spmv_pipe(const BatchView<float>& b, const float* d, const floa
                            cudaGraphConditionalHandle if_refresh, int set_if, const unsigned* refresh_flag,
                            unsigned* err, cudaStream_t s)
 {
-    const bool small = b.pipe_tile == (uint32_t)kPipeSmallTile;
-    const int g = small ? pipe_grid<kPipeSmallTile>() : pipe_grid<kTileElems>();
+    // the form with the C_LCM product only for batches that hold C_LCM
+    // meshes (the C_WRP form keeps its registers to itself)
+    const bool small = b.pipe_tile == (uint32_t)kPipeSmallTile, lcm = b.has_lcm != 0;
+    const int g = small ? (lcm ? pipe_grid<kPipeSmallTile, true>() : pipe_grid<kPipeSmallTile>())
+                        : (lcm ? pipe_grid<kTileElems, true>() : pipe_grid<kTileElems>());
     const uint32_t grid = b.ntiles < (uint32_t)g ? (b.ntiles ? b.ntiles : 1) : (uint32_t)g;
     prof_begin("tile_spmv_mixed", s);
-    if (small)
-        k_tile_spmv_pipe<kPipeSmallTile><<<grid, kPipeSmallTile, PipeShape<kPipeSmallTile>::kSmem, s>>>(
+    if (small && lcm)
+        k_tile_spmv_pipe<kPipeSmallTile, true><<<grid, kPipeSmallTile, PipeShape<kPipeSmallTile>::kSmem, s>>>(
+            b, d, r, part, tshare, if_refresh, set_if, refresh_flag, err);
+    else if (small)
+        k_tile_spmv_pipe<kPipeSmallTile, false><<<grid, kPipeSmallTile, PipeShape<kPipeSmallTile>::kSmem, s>>>(
+            b, d, r, part, tshare, if_refresh, set_if, refresh_flag, err);
+    else if (lcm)
+        k_tile_spmv_pipe<kTileElems, true><<<grid, kTileElems, PipeShape<kTileElems>::kSmem, s>>>(
             b, d, r, part, tshare, if_refresh, set_if, refresh_flag, err);
     else
-        k_tile_spmv_pipe<kTileElems><<<grid, kTileElems, PipeShape<kTileElems>::kSmem, s>>>(
+        k_tile_spmv_pipe<kTileElems, false><<<grid, kTileElems, PipeShape<kTileElems>::kSmem, s>>>(
             b, d, r, part, tshare, if_refresh, set_if, refresh_flag, err);
     prof_end("tile_spmv_mixed", s);
     launch_counter()++;

@@ -54,11 +54,57 @@ def test_lcm_element_hooks_match_oracle(fem_lib, oracle):
     assert abs(g.V() - o.V()) <= 1e-12 * abs(o.V())
 
 
-def test_batch_rejects_lcm(fem_lib):
-    sc = dataclasses.replace(scenes.cantilever_160(), material=1)
-    with pytest.raises(fem_lib.FemError) as e:
-        fem_lib.Batch([sc], precision=fem_lib.FEM_PRECISION_FP64)
-    assert e.value.code == fem_lib.FEM_E_ARG
+@pytest.mark.parametrize("case", [0, 2])
+def test_fp64_batch_lcm_matches_reference(fem_lib, case):
+    """C_LCM meshes in an FP64 batch (the FP64 solid's element arithmetic,
+    V, mu and lambda apart), next to a C_WRP mesh: the QIE cases of the
+    fixture the reference's element set wrote, rel-L2 <= 1e-10, iterations
+    within 1 per step, elastic energy 1e-8."""
+    from test_oracle_lcm import lcm_cases
+    g = np.load(os.path.join(GOLDEN, "lcm.npz"))
+    prefix, sc, steps = lcm_cases()[case]
+    bt = fem_lib.Batch([scenes.cantilever_160(), sc], precision=fem_lib.FEM_PRECISION_FP64)
+    for k in range(steps):
+        bt.step(1)
+        st = bt.stats(1)
+        assert abs(st["cg_iterations"] - int(g[prefix + "iters"][k])) <= 1, k
+    x, v = bt.state(1)
+    assert rel(x, g[prefix + "x"]) <= 1e-10 and rel(v, g[prefix + "v"]) <= 1e-10, \
+        (rel(x, g[prefix + "x"]), rel(v, g[prefix + "v"]))
+    ref_e = float(g[prefix + "elastic_energy"][-1])
+    assert abs(st["elastic_energy"] - ref_e) <= 1e-8 * abs(ref_e)
+
+
+def test_mixed_batch_and_server_lcm_match_reference(fem_lib):
+    """C_LCM on the mixed path (FP32 products on the element's V lambda and V
+    mu, FP64 force and refresh): within 1e-5 of the reference's fixture after
+    the 60 cantilever steps, in a batch and through the server (the mixed
+    batch's bits)."""
+    from test_oracle_lcm import lcm_cases
+    g = np.load(os.path.join(GOLDEN, "lcm.npz"))
+    prefix, sc, steps = lcm_cases()[0]
+    bt = fem_lib.Batch([sc], precision=fem_lib.FEM_PRECISION_MIXED, compute_energy=False, chunk_nodes=256)
+    bt.step(steps)
+    x, v = bt.state(0)
+    assert rel(x, g[prefix + "x"]) <= 1e-5 and rel(v, g[prefix + "v"]) <= 1e-4, \
+        (rel(x, g[prefix + "x"]), rel(v, g[prefix + "v"]))
+    srv = fem_lib.Server(precision=fem_lib.FEM_PRECISION_MIXED)
+    sid = srv.add(sc)
+    srv.admit()
+    for k in range(steps):
+        srv.submit(sid, k)
+    done = srv.drain()
+    assert len(done) == steps and all(c["status"] == 0 for c in done)
+    xs, vs = srv.state(sid)
+    assert np.array_equal(xs, x) and np.array_equal(vs, v)
+
+
+def test_batch_rejects_lcmh_and_ccm(fem_lib):
+    for mat in (2, 3):
+        sc = dataclasses.replace(scenes.cantilever_160(), material=mat)
+        with pytest.raises(fem_lib.FemError) as e:
+            fem_lib.Batch([sc], precision=fem_lib.FEM_PRECISION_FP64)
+        assert e.value.code == fem_lib.FEM_E_ARG
 
 
 @pytest.mark.parametrize("case", [0, 1, 3])
