@@ -146,6 +146,7 @@ struct fem_batch_s {
     Dev<unsigned> gbar;  // persistent loop: grid-barrier arrivals, generation, go flag
     Dev<double> prev_x;  // DAPD meshes: positions at the start of their last step (batch node order)
     Dev<uchar2> doc;     // DAPD meshes: direction of collapse per element (batch element order)
+    Dev<double> Fe;      // C_LCM meshes: F of the last BeginEvaluation (SoA, batch element order)
     bool any_dapd = false;
     bool any_lcm = false;
     Dev<unsigned char> blob;
@@ -204,6 +205,7 @@ struct fem_batch_s {
         b.blob_off16 = blob_off16.p;
         b.prev_x = prev_x.p;
         b.doc = doc.p;
+        b.Fe = Fe.p;
         const bool mixed = opt.precision == FEM_PRECISION_MIXED;
         b.act_tiles = mixed ? act_tiles.p : nullptr;
         b.act_chunks = mixed ? act_chunks.p : nullptr;
@@ -236,7 +238,7 @@ struct fem_batch_s {
         x.release(); v.release(); bvec.release(); y.release(); part64.release(); cpart.release(); tpart.release();
         knc_target.release(); r_s.release(); d_s.release(); q_s.release(); part_s.release(); ydelta_s.release(); counter.release();
         any_flag.release(); refresh_flag.release(); mcount.release(); err.release(); gbar.release(); blob.release();
-        prev_x.release(); doc.release();
+        prev_x.release(); doc.release(); Fe.release();
         blob_off16.release();
         act_tiles.release(); act_chunks.release(); act_count.release(); list_dirty.release(); slice.release();
         start_tiles.release(); start_chunks.release(); launch_tiles.release(); launch_chunks.release();
@@ -1077,6 +1079,10 @@ int fem_batch_finalize(fem_batch b)
     BCKC(b->fixed.upload(fixed, s));
     BCKC(b->rest.upload(rest_all, s));
     BCKC(b->x.upload(rest_all, s));
+    if (b->any_lcm) {
+        BCKC(b->Fe.alloc(9 * (size_t)b->Ttot));
+        BCKC(cudaMemsetAsync(b->Fe.p, 0, sizeof(double) * 9 * (size_t)b->Ttot, s));
+    }
     std::vector<uchar2> doc_none;
     if (b->any_dapd) {
         // DAPD's previous positions start at the rest positions (Create,
@@ -1100,7 +1106,7 @@ int fem_batch_finalize(fem_batch b)
                       b->gtets.bytes() + b->Dinv_s.bytes() + b->mat_s.bytes() + b->R_s.bytes() +
                       b->Dinv64.bytes() + b->vol.bytes() + b->detF.bytes() + b->tile_nodes.bytes() +
                       b->lptr0.bytes() + b->ov_ptr.bytes() + b->ov_map.bytes() + b->knc_node.bytes() +
-                      b->perm.bytes() + b->prev_x.bytes() + b->doc.bytes() +
+                      b->perm.bytes() + b->prev_x.bytes() + b->doc.bytes() + b->Fe.bytes() +
                       b->knc_mesh.bytes() + b->knc_target.bytes() + b->lconn.bytes() + b->lptr.bytes() +
                       b->lidx.bytes() + b->fixed.bytes() + b->rest.bytes() + b->x.bytes() + b->v.bytes() +
                       b->bvec.bytes() + b->y.bytes() + b->r_s.bytes() + b->d_s.bytes() + b->q_s.bytes() +

@@ -138,6 +138,7 @@ struct BatchView {
     uint64_t nslots;               // partial slots: Ntot owner slots + the overflow slots
     double* prev_x;                // [3 Ntot] DAPD: positions at the start of each mesh's last step; null without DAPD
     uchar2* doc;                   // [Ttot] DAPD: direction of collapse per element (batch order)
+    double* Fe;                    // [9 Ttot] C_LCM: F of the last BeginEvaluation (the element cache's), SoA; null without C_LCM
     uint32_t pipe_tile;            // mixed: threads per block of the tile product (kPipeSmallTile or kTileElems)
     uint32_t fuse_alpha;           // mixed: the node pass forms alpha (no separate alpha kernel)
     uint32_t has_lcm;              // some mesh takes the C_LCM product

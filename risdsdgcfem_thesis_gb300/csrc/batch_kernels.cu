@@ -229,26 +229,19 @@ __global__ void __launch_bounds__(256) k_tile_force(BatchView<S> b, const double
         double energy = 0.0;
         if (threadIdx.x < tm.ne && tm.material == kTileMaterialLcm) {
             // C_LCM_f_e and C_LCM_V (TetrahedronElementSet3.cpp:1154-1178,
-            // 1489-1507) in FP64 in either precision, from F at x
+            // 1489-1507) in FP64 in either precision, on the F of the last
+            // BeginEvaluation (the element cache's, as the reference's V()
+            // after a step also reads it)
             const size_t e = tm.e0 + threadIdx.x;
             const size_t T = b.Ttot;
             const MeshConsts& mcm = b.mc[tm.mesh];
-            double R[9], Di[9];
+            double R[9], Di[9], F[9];
 #pragma unroll
             for (int c = 0; c < 9; c++) R[c] = (double)b.R[c * T + e];
 #pragma unroll
             for (int c = 0; c < 9; c++) Di[c] = b.Dinv64[c * T + e];
-            const int4 g = b.gtets[e];
-            const int ids[4] = {(int)bounds_idx((uint32_t)g.x, b.Ntot, kSiteBatchNode),
-                                (int)bounds_idx((uint32_t)g.y, b.Ntot, kSiteBatchNode),
-                                (int)bounds_idx((uint32_t)g.z, b.Ntot, kSiteBatchNode),
-                                (int)bounds_idx((uint32_t)g.w, b.Ntot, kSiteBatchNode)};
-            V3<double> xs[4];
 #pragma unroll
-            for (int i = 0; i < 4; i++)
-                xs[i] = mk<double>(x[3 * (size_t)ids[i]], x[3 * (size_t)ids[i] + 1], x[3 * (size_t)ids[i] + 2]);
-            double F[9], detF;
-            deformation_gradient(xs, Di, F, detF);
+            for (int c = 0; c < 9; c++) F[c] = b.Fe[c * T + e];
             energy = lcm_energy(R, F, b.vol[e], mcm.lame_mu, mcm.lame_lambda);
             if (part64) {
                 double out[12];

@@ -258,6 +258,11 @@ __global__ void __launch_bounds__(256, 3) k_begin_eval_batch(BatchView<S> b, con
                 *reinterpret_cast<float*>(base + blob_comp_off(8, i, ne4)) = (float)Rs[8];
             }
             b.detF[e] = detF;
+            if (b.Fe && mcm.material == kTileMaterialLcm) {
+                // the element cache's F, which C_LCM_f_e and C_LCM_V read
+#pragma unroll
+                for (int c = 0; c < 9; c++) b.Fe[c * T + e] = F[c];
+            }
             if (detF <= 0.0) atomicAdd(&s_inv, 1u);
         }
         __syncthreads();
