@@ -111,6 +111,7 @@ uint32_t spread10(uint32_t v)
 
 static_assert(kMeshRotationMsvd == FEM_ROTATION_MSVD && kMeshRotationDapd == FEM_ROTATION_DAPD,
               "per-mesh rotation values are enum fem_rotation's");
+static_assert(kMeshSolverCg == FEM_LS_CG && kMeshSolverMinres == FEM_LS_MINRES, "solver ids follow fem_tet.h");
 static_assert(kTileMaterialWrp == FEM_MATERIAL_C_WRP && kTileMaterialLcm == FEM_MATERIAL_C_LCM,
               "per-tile material values are enum fem_material's");
 
@@ -149,6 +150,9 @@ struct fem_batch_s {
     Dev<double> Fe;      // C_LCM meshes: F of the last BeginEvaluation (SoA, batch element order)
     bool any_dapd = false;
     bool any_lcm = false;
+    bool any_minres = false;
+    Dev<unsigned char> mr_p_s, mr_p0_s;  // MINRES meshes: directions p, p0 (S-typed)
+    Dev<double> cpart_b;                 // MINRES meshes: per-chunk |b|^2 partials
     Dev<unsigned char> blob;
     Dev<uint32_t> blob_off16;
     Dev<uint32_t> act_tiles, act_chunks, act_count;
@@ -206,6 +210,10 @@ struct fem_batch_s {
         b.prev_x = prev_x.p;
         b.doc = doc.p;
         b.Fe = Fe.p;
+        b.mr_p = reinterpret_cast<S*>(mr_p_s.p);
+        b.mr_p0 = reinterpret_cast<S*>(mr_p0_s.p);
+        b.mr_v1 = reinterpret_cast<S*>(q_s.p);
+        b.cpart_b = cpart_b.p;
         const bool mixed = opt.precision == FEM_PRECISION_MIXED;
         b.act_tiles = mixed ? act_tiles.p : nullptr;
         b.act_chunks = mixed ? act_chunks.p : nullptr;
@@ -239,6 +247,7 @@ struct fem_batch_s {
         knc_target.release(); r_s.release(); d_s.release(); q_s.release(); part_s.release(); ydelta_s.release(); counter.release();
         any_flag.release(); refresh_flag.release(); mcount.release(); err.release(); gbar.release(); blob.release();
         prev_x.release(); doc.release(); Fe.release();
+        mr_p_s.release(); mr_p0_s.release(); cpart_b.release();
         blob_off16.release();
         act_tiles.release(); act_chunks.release(); act_count.release(); list_dirty.release(); slice.release();
         start_tiles.release(); start_chunks.release(); launch_tiles.release(); launch_chunks.release();
@@ -372,6 +381,7 @@ int enqueue_step(fem_batch B, cudaStream_t s, bool capture)
         L::knc(b, B->K, B->x.p, B->bvec.p, B->y.p, ss);
         L::tile_spmv_y64(b, B->y.p, B->part64.p, 0, nullptr, ss);
         L::node_residual(b, B->part64.p, B->bvec.p, B->y.p, r, d, B->cpart.p, ls, ss);
+        if (B->any_minres) L::node_mr_finish(b, B->y.p, r, d, q, ls, ss);
     };
     // mixed: the tile product also writes each tile's share of d^T A d; one
     // fused node pass forms alpha from the shares and does the rest
@@ -390,6 +400,9 @@ int enqueue_step(fem_batch B, cudaStream_t s, bool capture)
             L::node_q(b, part, d, q, nullptr, B->bvec.p, B->y.p, r, B->cpart.p, lb, bs);
             L::node_update(b, B->y.p, r, d, q, B->cpart.p, lb, bs);
         }
+        // MINRES meshes: the iteration's vector and iterate updates, after
+        // their loop test
+        if (B->any_minres) L::node_mr_finish(b, B->y.p, r, d, q, ls, bs);
     };
     L::reset_counts(b, ls, if_start, s);
     if (capture) {
@@ -545,8 +558,10 @@ int fem_batch_add_mesh(fem_batch b, const double* rest, uint32_t N, const uint32
         !(std::isfinite(p->dapd_threshold_det_F) && std::isfinite(p->dapd_l_factor) &&
           std::isfinite(p->dapd_nl_factor) && std::isfinite(p->dapd_nl_exponent)))
         return batch_fail(FEM_E_ARG, "non-finite DAPD parameters");
-    if (p->ls_solver != FEM_LS_CG)
-        return batch_fail(FEM_E_ARG, "ls_solver %u: batches use CG; MINRES runs on fem_solid", p->ls_solver);
+    if (p->ls_solver != FEM_LS_CG && p->ls_solver != FEM_LS_MINRES)
+        return batch_fail(FEM_E_ARG, "unknown ls_solver %u", p->ls_solver);
+    if (p->ls_solver == FEM_LS_MINRES && b->opt.persistent_loop)
+        return batch_fail(FEM_E_ARG, "the persistent loop takes CG meshes only");
     if (p->material != FEM_MATERIAL_C_WRP && p->material != FEM_MATERIAL_C_LCM)
         return batch_fail(FEM_E_ARG, "material %u: batches take C_WRP and C_LCM; C_LCMH and C_CCM run on fem_solid",
                           p->material);
@@ -850,6 +865,8 @@ int fem_batch_finalize(fem_batch b)
         c.dapd_fNL = (double)(float)p.dapd_nl_factor;
         c.dapd_eNL = (double)(float)p.dapd_nl_exponent;
         if (p.rotation == FEM_ROTATION_DAPD) b->any_dapd = true;
+        c.solver = p.ls_solver;
+        if (p.ls_solver == FEM_LS_MINRES) b->any_minres = true;
         c.refresh_drop_sq = fp64 ? 0.0 : p.refresh_drop * p.refresh_drop;
         c.max_iter = p.ls_max_iter;
         c.refresh_every = fp64 ? 0u : p.refresh_every;
@@ -1083,6 +1100,13 @@ int fem_batch_finalize(fem_batch b)
         BCKC(b->Fe.alloc(9 * (size_t)b->Ttot));
         BCKC(cudaMemsetAsync(b->Fe.p, 0, sizeof(double) * 9 * (size_t)b->Ttot, s));
     }
+    if (b->any_minres) {
+        BCKC(b->mr_p_s.alloc(N3 * SB));
+        BCKC(b->mr_p0_s.alloc(N3 * SB));
+        BCKC(cudaMemsetAsync(b->mr_p_s.p, 0, N3 * SB, s));
+        BCKC(cudaMemsetAsync(b->mr_p0_s.p, 0, N3 * SB, s));
+        BCKC(b->cpart_b.alloc(b->nchunks));
+    }
     std::vector<uchar2> doc_none;
     if (b->any_dapd) {
         // DAPD's previous positions start at the rest positions (Create,
@@ -1106,7 +1130,8 @@ int fem_batch_finalize(fem_batch b)
                       b->gtets.bytes() + b->Dinv_s.bytes() + b->mat_s.bytes() + b->R_s.bytes() +
                       b->Dinv64.bytes() + b->vol.bytes() + b->detF.bytes() + b->tile_nodes.bytes() +
                       b->lptr0.bytes() + b->ov_ptr.bytes() + b->ov_map.bytes() + b->knc_node.bytes() +
-                      b->perm.bytes() + b->prev_x.bytes() + b->doc.bytes() + b->Fe.bytes() +
+                      b->perm.bytes() + b->prev_x.bytes() + b->doc.bytes() + b->Fe.bytes() + b->mr_p_s.bytes() +
+                      b->mr_p0_s.bytes() + b->cpart_b.bytes() +
                       b->knc_mesh.bytes() + b->knc_target.bytes() + b->lconn.bytes() + b->lptr.bytes() +
                       b->lidx.bytes() + b->fixed.bytes() + b->rest.bytes() + b->x.bytes() + b->v.bytes() +
                       b->bvec.bytes() + b->y.bytes() + b->r_s.bytes() + b->d_s.bytes() + b->q_s.bytes() +

@@ -79,6 +79,14 @@ __host__ __device__ constexpr uint32_t blob_bytes(uint32_t ne, uint32_t nn, uint
 constexpr uint32_t kMeshRotationMsvd = 0;
 constexpr uint32_t kMeshRotationDapd = 1;
 
+// The mesh's linear solver (LS_Solve's choice, LeafDSH_Solid3D_FEM.cpp:
+// 1136-1154). A MINRES mesh keeps its Lanczos vectors in the CG buffers:
+// v (the vector the tile product multiplies) in r, with beta = 0 so that the
+// product's direction update r + beta d leaves it exact; v0 in d; v1 in q;
+// and the directions p, p0 in their own buffers.
+constexpr uint32_t kMeshSolverCg = 0;
+constexpr uint32_t kMeshSolverMinres = 1;
+
 struct TileMeta {
     uint32_t mesh;
     uint32_t e0;      // first element (global)
@@ -127,6 +135,7 @@ struct MeshConsts {
     double refresh_drop_sq;  // mixed: FP64 residual when |r|^2 fell below this times its value at the last one
     uint32_t rotation;       // kMeshRotationMsvd or kMeshRotationDapd (FP64 in either precision)
     uint32_t material;       // kTileMaterialWrp or kTileMaterialLcm
+    uint32_t solver;         // kMeshSolverCg or kMeshSolverMinres
     double lame_mu, lame_lambda;  // C_LCM: from the mesh's scalar E and nu (per-element values re-bake only K0)
     double dapd_thr, dapd_fL, dapd_fNL, dapd_eNL;  // DAPD: threshold on det F, offset factors, exponent
 
@@ -139,6 +148,10 @@ struct BatchView {
     double* prev_x;                // [3 Ntot] DAPD: positions at the start of each mesh's last step; null without DAPD
     uchar2* doc;                   // [Ttot] DAPD: direction of collapse per element (batch order)
     double* Fe;                    // [9 Ttot] C_LCM: F of the last BeginEvaluation (the element cache's), SoA; null without C_LCM
+    S* mr_p;                       // [3 Ntot] MINRES: direction p; null without a MINRES mesh
+    S* mr_p0;                      // [3 Ntot] MINRES: the previous direction p0
+    S* mr_v1;                      // [3 Ntot] MINRES: the Lanczos vector v1 (the q buffer)
+    double* cpart_b;               // [nchunks] MINRES: per-chunk partials of |b|^2 at the start of a step
     uint32_t pipe_tile;            // mixed: threads per block of the tile product (kPipeSmallTile or kTileElems)
     uint32_t fuse_alpha;           // mixed: the node pass forms alpha (no separate alpha kernel)
     uint32_t has_lcm;              // some mesh takes the C_LCM product

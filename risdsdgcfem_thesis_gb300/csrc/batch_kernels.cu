@@ -544,7 +544,8 @@ __global__ void k_node_residual(BatchView<S> b, const double* __restrict__ part6
         if (b.active[ch.mesh] != 1) continue;
         const MeshConsts& c = b.mc[ch.mesh];
         const double mfm = c.mass * c.factor_M;
-        double acc = 0.0;
+        const bool minres = c.solver == kMeshSolverMinres;
+        double acc = 0.0, acc_b = 0.0;
         for (size_t n = ch.n0 + threadIdx.x; n < ch.n1; n += blockDim.x) {
             const size_t i = 3 * n;
             S r0 = 0, r1 = 0, r2 = 0;
@@ -558,12 +559,46 @@ __global__ void k_node_residual(BatchView<S> b, const double* __restrict__ part6
             r[i] = r0; r[i + 1] = r1; r[i + 2] = r2;
             d[i] = 0; d[i + 1] = 0; d[i + 2] = 0;
             acc += (double)r0 * (double)r0 + (double)r1 * (double)r1 + (double)r2 * (double)r2;
+            // MINRES's relative test is on |b| (every row, constrained ones too)
+            if (minres) acc_b += bv[i] * bv[i] + bv[i + 1] * bv[i + 1] + bv[i + 2] * bv[i + 2];
         }
         const double sum = bblock_sum(acc);
-        if (threadIdx.x == 0) cpart[ci] = sum;
+        const double sum_b = minres ? bblock_sum(acc_b) : 0.0;
+        if (threadIdx.x == 0) {
+            cpart[ci] = sum;
+            if (minres) b.cpart_b[ci] = sum_b;
+        }
         if (arrive_last(ls.mcount + ch.mesh, c.nchunks)) {
             const double total = mesh_partial_sum(cpart, c.chunk0, c.nchunks);
-            if (threadIdx.x == 0) {
+            const double total_b = minres ? mesh_partial_sum(b.cpart_b, c.chunk0, c.nchunks) : 0.0;
+            if (threadIdx.x == 0 && minres) {
+                // ILSS_MINRES::Solve's start (ILSS_MINRES.h:66-107); the
+                // next finishing pass normalises v = r0 / |r0|
+                StepScalars& s = b.st[ch.mesh];
+                minres_start(s.mr, total);
+                s.mr.norm_b_sq = total_b;
+                s.delta_0 = total_b;
+                s.delta_new = total;
+                s.delta_old = total;
+                s.delta_target = c.rel_eps_sq * total_b;
+                s.abs_eps_sq = c.abs_eps_sq;
+                s.max_iter = c.max_iter;
+                s.k = 0;
+                s.status = (!isfinite(total)) ? 3u : 0u;
+                s.alpha = 0.0;
+                s.beta = 0.0;
+                s.beta_f = 0.f;
+                s.refresh_next = 0;
+                s.delta_refresh = total;
+                s.k_refresh = 0;
+                s.confirm = 0;
+                s.done = cg_cont(s) ? 0u : 1u;
+                s.mr_pending = s.done ? 0u : 2u;
+                if (s.done) {
+                    finish_stats(s);
+                    s.finished = 1;
+                }
+            } else if (threadIdx.x == 0) {
                 StepScalars& s = b.st[ch.mesh];
                 s.delta_0 = total;
                 s.delta_new = total;
@@ -592,6 +627,98 @@ __global__ void k_node_residual(BatchView<S> b, const double* __restrict__ part6
     grid_tail(b, ls, false);
 }
 
+// Sum of node n's tile partials: its owner slot, then its overflow slots.
+template <typename S>
+__device__ __forceinline__ void node_part_sum(const BatchView<S>& b, const S* part, size_t n, S& s0, S& s1, S& s2)
+{
+    s0 = part[3 * n];
+    s1 = part[3 * n + 1];
+    s2 = part[3 * n + 2];
+    const uint32_t j1 = bounds_idx(b.ov_ptr[n + 1], b.nslots - b.Ntot + 1, kSitePartialSlot);
+    for (uint32_t j = b.ov_ptr[n]; j < j1; j++) {
+        const size_t o = 3 * ((size_t)b.Ntot + j);
+        s0 += part[o];
+        s1 += part[o + 1];
+        s2 += part[o + 2];
+    }
+}
+
+// MINRES, after the product of v (in r): v1 = S A v - beta v0 into q and
+// v1.v; the last block of the mesh takes alpha = v1.v (ILSS_MINRES.h:
+// 117-124).
+template <typename S>
+__device__ void node_q_minres(const BatchView<S>& b, const MeshConsts& c, const StepScalars& sm, uint32_t ci,
+                              const ChunkMeta& ch, const S* part, const S* v, const S* v0, S* v1, double* cpart,
+                              const LoopSync& ls)
+{
+    const S fK = (S)c.factor_K, mfm = (S)(c.mass * c.factor_M);
+    const S nb = (S)(-sm.mr.beta_new);
+    S acc = 0;
+    for (size_t n = ch.n0 + threadIdx.x; n < ch.n1; n += blockDim.x) {
+        const size_t i = 3 * n;
+        S s[3] = {0, 0, 0};
+        const bool fixed = b.fixed[n] != 0;
+        if (!fixed) node_part_sum(b, part, n, s[0], s[1], s[2]);
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+            const S qa = fixed ? (S)0 : fK * s[a] + mfm * v[i + a];
+            const S w = qa + nb * v0[i + a];
+            v1[i + a] = w;
+            acc += w * v[i + a];
+        }
+    }
+    const double sum = chunk_sum<S>(acc);
+    if (threadIdx.x == 0) cpart[ci] = sum;
+    if (arrive_last(ls.mcount + ch.mesh, c.nchunks)) {
+        const double total = mesh_partial_sum(cpart, c.chunk0, c.nchunks);
+        if (threadIdx.x == 0) {
+            StepScalars& s = b.st[ch.mesh];
+            s.mr.beta = s.mr.beta_new;
+            s.mr.alpha = total;
+        }
+    }
+}
+
+// MINRES: v1 -= alpha v and |v1|^2; the last block of the mesh forms the
+// Givens rotation, the residual estimate and the loop test (ILSS_MINRES.h:
+// 125-160); the finishing pass then applies the iteration's updates.
+template <typename S>
+__device__ void node_update_minres(const BatchView<S>& b, const MeshConsts& c, const StepScalars& sm, uint32_t ci,
+                                   const ChunkMeta& ch, const S* v, S* v1, double* cpart, const LoopSync& ls)
+{
+    const S na = (S)(-sm.mr.alpha);
+    S acc = 0;
+    for (size_t n = ch.n0 + threadIdx.x; n < ch.n1; n += blockDim.x) {
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+            const size_t i = 3 * n + a;
+            const S w = v1[i] + na * v[i];
+            v1[i] = w;
+            acc += w * w;
+        }
+    }
+    const double sum = chunk_sum<S>(acc);
+    if (threadIdx.x == 0) cpart[ci] = sum;
+    if (arrive_last(ls.mcount + ch.mesh, c.nchunks)) {
+        const double total = mesh_partial_sum(cpart, c.chunk0, c.nchunks);
+        if (threadIdx.x == 0) {
+            StepScalars& s = b.st[ch.mesh];
+            minres_givens(s.mr, total);
+            s.delta_old = s.delta_new;
+            s.delta_new = s.mr.norm_r_sq;
+            s.k += 1;
+            s.total_iters += 1;
+            if (!isfinite(total) || !isfinite(s.mr.norm_r_sq)) s.status = 3u;
+            s.mr_pending = 1u;
+            s.done = cg_cont(s) ? 0u : 1u;
+            if (s.done) {
+                finish_stats(s);
+                s.finished = 1;
+            }
+        }
+    }
+}
+
 // d = S(r + beta d) written back ; q = S A d ; d.q ; last block of a mesh:
 // alpha (ILSS_CG.h:90-98). On refresh iterations r becomes S(b - A y).
 template <typename S>
@@ -606,6 +733,10 @@ __global__ void k_node_q(BatchView<S> b, const S* __restrict__ part, S* __restri
         if (!mesh_running(b, ch.mesh)) return;
         const MeshConsts& c = b.mc[ch.mesh];
         const StepScalars& sm = b.st[ch.mesh];
+        if (c.solver == kMeshSolverMinres) {
+            node_q_minres(b, c, sm, ci, ch, part, r, d, q, cpart, ls);
+            return;
+        }
         const bool refresh = part64 && refresh_now(c, sm);
         const S beta = (S)sm.beta;
         const S fK = (S)c.factor_K, mfm = (S)(c.mass * c.factor_M);
@@ -664,11 +795,13 @@ __global__ void k_node_q(BatchView<S> b, const S* __restrict__ part, S* __restri
 // beta, k += 1 and the loop test (ILSS_CG.h:100-144).
 template <typename S>
 __global__ void k_node_update(BatchView<S> b, double* __restrict__ y, S* __restrict__ r, const S* __restrict__ d,
-                              const S* __restrict__ q, double* __restrict__ cpart, LoopSync ls)
+                              S* __restrict__ q, double* __restrict__ cpart, LoopSync ls)
 {
     const uint32_t ci = blockIdx.x;
     const ChunkMeta ch = b.chunks[ci < b.nchunks ? ci : 0];
-    if (ci < b.nchunks && mesh_running(b, ch.mesh)) {
+    if (ci < b.nchunks && mesh_running(b, ch.mesh) && b.mc[ch.mesh].solver == kMeshSolverMinres) {
+        node_update_minres(b, b.mc[ch.mesh], b.st[ch.mesh], ci, ch, r, q, cpart, ls);
+    } else if (ci < b.nchunks && mesh_running(b, ch.mesh)) {
         const MeshConsts& c = b.mc[ch.mesh];
         const double alpha = b.st[ch.mesh].alpha;
         const S alpha_s = (S)alpha, na = -alpha_s;
@@ -707,6 +840,57 @@ __global__ void k_node_update(BatchView<S> b, double* __restrict__ y, S* __restr
         }
     }
     grid_tail(b, ls, true);
+}
+
+// MINRES's finishing pass per chunk of a mesh with an update due, after the
+// mesh's loop test (either precision):
+//   mr_pending 2 (start or restart): v = r0 / |r0| (ILSS_MINRES.h:82-95),
+//     v0 = p = p0 = 0;
+//   mr_pending 1 (an iteration): p_new = (v - r2 p - r3 p0) / r1,
+//     y += beta_one c eta p_new, p0 = p, p = p_new, v0 = v,
+//     v = v1 / beta_new (ILSS_MINRES.h:131-156).
+// The last block of the mesh clears the flag.
+template <typename S>
+__global__ void k_node_mr_finish(BatchView<S> b, double* __restrict__ y, S* __restrict__ r, S* __restrict__ d,
+                                 const S* __restrict__ q, LoopSync ls)
+{
+    const uint32_t nl = b.list_count[3];
+    for (uint32_t il = blockIdx.x; il < nl; il += gridDim.x) {
+        const uint32_t ci = b.launch_chunks[il];
+        const ChunkMeta ch = b.chunks[ci];
+        const MeshConsts& c = b.mc[ch.mesh];
+        if (c.solver != kMeshSolverMinres) continue;
+        const StepScalars& sm = b.st[ch.mesh];
+        const uint32_t pending = sm.mr_pending;
+        if (!pending) continue;
+        const MinresScalars mr = sm.mr;
+        S* p = b.mr_p;
+        S* p0 = b.mr_p0;
+        if (pending == 2u) {
+            const S inv = (S)mr.inv_beta;
+            for (size_t i = 3 * (size_t)ch.n0 + threadIdx.x; i < 3 * (size_t)ch.n1; i += blockDim.x) {
+                r[i] *= inv;
+                d[i] = 0;
+                p[i] = 0;
+                p0[i] = 0;
+            }
+        } else {
+            const S inv = (S)mr.inv_beta, nr2 = (S)mr.neg_r2, nr3 = (S)mr.neg_r3, ir1 = (S)mr.inv_r1;
+            for (size_t i = 3 * (size_t)ch.n0 + threadIdx.x; i < 3 * (size_t)ch.n1; i += blockDim.x) {
+                const S v = r[i];
+                const S pi = p[i];
+                S pn = nr2 * pi + v;
+                pn += nr3 * p0[i];
+                pn *= ir1;
+                p0[i] = pi;
+                p[i] = pn;
+                y[i] += mr.x_coef * (double)pn;
+                d[i] = v;
+                r[i] = q[i] * inv;
+            }
+        }
+        if (arrive_last(ls.mcount + ch.mesh, c.nchunks) && threadIdx.x == 0) b.st[ch.mesh].mr_pending = 0u;
+    }
 }
 
 // v = y ; x += dt y
@@ -874,10 +1058,18 @@ void BatchLaunch<S>::node_q(const BatchView<S>& b, const S* part, S* d, S* q, co
 }
 
 template <typename S>
-void BatchLaunch<S>::node_update(const BatchView<S>& b, double* y, S* r, const S* d, const S* q, double* cpart,
+void BatchLaunch<S>::node_update(const BatchView<S>& b, double* y, S* r, const S* d, S* q, double* cpart,
                                  const LoopSync& ls, cudaStream_t s)
 {
     k_node_update<S><<<b.nchunks ? b.nchunks : 1, kNodeThreads, 0, s>>>(b, y, r, d, q, cpart, ls);
+    launch_counter()++;
+}
+
+template <typename S>
+void BatchLaunch<S>::node_mr_finish(const BatchView<S>& b, double* y, S* r, S* d, const S* q, const LoopSync& ls,
+                                    cudaStream_t s)
+{
+    k_node_mr_finish<S><<<grid_chunks(b.nchunks), kNodeThreads, 0, s>>>(b, y, r, d, q, ls);
     launch_counter()++;
 }
 

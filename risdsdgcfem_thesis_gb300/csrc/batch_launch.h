@@ -83,8 +83,11 @@ struct BatchLaunch {
                               S* d, double* cpart, const LoopSync& ls, cudaStream_t s);
     static void node_q(const BatchView<S>& b, const S* part, S* d, S* q, const double* part64,
                        const double* bv, const double* y, S* r, double* cpart, const LoopSync& ls, cudaStream_t s);
-    static void node_update(const BatchView<S>& b, double* y, S* r, const S* d, const S* q, double* cpart,
+    static void node_update(const BatchView<S>& b, double* y, S* r, const S* d, S* q, double* cpart,
                             const LoopSync& ls, cudaStream_t s);
+    // MINRES meshes: the finishing pass of the start or of an iteration
+    static void node_mr_finish(const BatchView<S>& b, double* y, S* r, S* d, const S* q, const LoopSync& ls,
+                               cudaStream_t s);
     static void integrate(const BatchView<S>& b, double* x, double* v, const double* y, cudaStream_t s);
     static void fin_energy(const BatchView<S>& b, int kind, const double* tpart, cudaStream_t s);
 };

@@ -50,6 +50,8 @@ struct StepScalars {
     float alpha_f;          // mixed: this iteration's alpha in FP32 (0 on a confirm iteration)
     uint32_t brk;           // mixed: this iteration breaks down (|d.q| < abs^2) and leaves the loop
     uint32_t done_prev;     // MINRES: `done` as it was at the top of the current iteration
+    uint32_t mr_pending;    // batch MINRES: 1 = this iteration's vector and iterate update is due,
+                            // 2 = the start (or restart) residual is to be normalised
     unsigned long long total_iters;
     double host_sum;        // FIE: the last FIN_SUM total (|b_k|^2 or |y_k|^2), read by the host
     MinresScalars mr;       // MINRES solver state (FP64 solid)
@@ -59,6 +61,41 @@ struct StepScalars {
     // MSVD branch near a tie or a failed sensitivity check
     uint32_t res_det_F, res_isotropic, res_tie, res_check;
 };
+
+// One MINRES iteration's Givens rotation and update coefficients from
+// |v1|^2 after the Lanczos step (ILSS_MINRES.h:131-156): beta_new, the
+// rotation (c, s), the coefficients of the direction and iterate updates,
+// and the residual norm carried by the sines.
+__device__ __forceinline__ void minres_givens(MinresScalars& mr, double beta_new_sq)
+{
+    mr.beta_new = ::sqrt(beta_new_sq);
+    mr.inv_beta = 1.0 / mr.beta_new;
+    const double r2 = mr.s * mr.alpha + mr.c * mr.c_old * mr.beta;
+    const double r3 = mr.s_old * mr.beta;
+    const double r1_hat = mr.c * mr.alpha - mr.c_old * mr.s * mr.beta;
+    const double r1 = ::sqrt(r1_hat * r1_hat + beta_new_sq);
+    mr.c_old = mr.c;
+    mr.s_old = mr.s;
+    mr.c = r1_hat / r1;
+    mr.s = mr.beta_new / r1;
+    mr.neg_r2 = -r2;
+    mr.neg_r3 = -r3;
+    mr.inv_r1 = 1.0 / r1;
+    mr.x_coef = mr.beta_one * mr.c * mr.eta;
+    mr.norm_r_sq *= mr.s * mr.s;
+    mr.eta = -mr.s * mr.eta;
+}
+
+// MINRES start from the residual r0 (ILSS_MINRES.h:74-107): |r0|^2 and the
+// Givens state of an empty Lanczos basis.
+__device__ __forceinline__ void minres_start(MinresScalars& mr, double r0_sq)
+{
+    mr.norm_r_sq = r0_sq;
+    mr.beta_new = ::sqrt(r0_sq);
+    mr.beta_one = mr.beta_new;
+    mr.inv_beta = 1.0 / mr.beta_new;
+    mr.c = 1.0; mr.c_old = 1.0; mr.s = 0.0; mr.s_old = 0.0; mr.eta = 1.0;
+}
 
 template <typename S>
 struct MeshView {

@@ -759,11 +759,8 @@ __global__ void k_finalize(int kind, const double* __restrict__ partials, uint32
         // |r0|^2 (sq_norm_2 and dot(v1, w1) are the same sum); |b|^2 from the
         // FIN_SUM before; beta_one = |r0| (:74-107)
         MinresScalars& mr = st->mr;
-        mr.norm_r_sq = total;
+        minres_start(mr, total);
         mr.norm_b_sq = st->host_sum;
-        mr.beta_new = ::sqrt(total);
-        mr.beta_one = mr.beta_new;
-        mr.c = 1.0; mr.c_old = 1.0; mr.s = 0.0; mr.s_old = 0.0; mr.eta = 1.0;
         st->delta_0 = mr.norm_b_sq;
         st->delta_target = c.rel_eps_sq * mr.norm_b_sq;
         st->abs_eps_sq = c.abs_eps_sq;
@@ -784,24 +781,7 @@ __global__ void k_finalize(int kind, const double* __restrict__ partials, uint32
     case FIN_MR_BETA: {
         if (st->done) break;
         MinresScalars& mr = st->mr;
-        const double beta_new_sq = total;
-        mr.beta_new = ::sqrt(beta_new_sq);
-        mr.inv_beta = 1.0 / mr.beta_new;
-        // Givens rotation (:135-144)
-        const double r2 = mr.s * mr.alpha + mr.c * mr.c_old * mr.beta;
-        const double r3 = mr.s_old * mr.beta;
-        const double r1_hat = mr.c * mr.alpha - mr.c_old * mr.s * mr.beta;
-        const double r1 = ::sqrt(r1_hat * r1_hat + beta_new_sq);
-        mr.c_old = mr.c;
-        mr.s_old = mr.s;
-        mr.c = r1_hat / r1;
-        mr.s = mr.beta_new / r1;
-        mr.neg_r2 = -r2;
-        mr.neg_r3 = -r3;
-        mr.inv_r1 = 1.0 / r1;
-        mr.x_coef = mr.beta_one * mr.c * mr.eta;
-        mr.norm_r_sq *= mr.s * mr.s;
-        mr.eta = -mr.s * mr.eta;
+        minres_givens(mr, total);  // Givens rotation (:135-144)
         st->delta_new = mr.norm_r_sq;
         st->k += 1;
         st->total_iters += 1;

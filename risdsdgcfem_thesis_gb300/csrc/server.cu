@@ -285,10 +285,12 @@ int fem_server_add_scene(fem_server s, const double* rest, uint32_t N, const uin
         return batch_fail(FEM_E_ARG, "integrator %u: the server steps with QIE_V", p->integrator);
     if (p->rotation != FEM_ROTATION_MSVD && p->rotation != FEM_ROTATION_DAPD)
         return batch_fail(FEM_E_ARG, "unknown rotation %u", p->rotation);
-    if (p->ls_solver != FEM_LS_CG)
-        return batch_fail(FEM_E_ARG, "ls_solver %u: the server uses CG", p->ls_solver);
+    if (p->ls_solver != FEM_LS_CG && p->ls_solver != FEM_LS_MINRES)
+        return batch_fail(FEM_E_ARG, "unknown ls_solver %u", p->ls_solver);
     if (p->material != FEM_MATERIAL_C_WRP && p->material != FEM_MATERIAL_C_LCM)
         return batch_fail(FEM_E_ARG, "material %u: the server takes C_WRP and C_LCM", p->material);
+    if (s->opt.persistent_loop && (p->ls_solver != FEM_LS_CG || p->material != FEM_MATERIAL_C_WRP))
+        return batch_fail(FEM_E_ARG, "the persistent loop takes CG meshes of C_WRP only");
     if (knc_count && (!knc_nodes || !knc_targets)) return batch_fail(FEM_E_ARG, "null constraint arrays");
     for (size_t i = 0; i < 4 * (size_t)T; i++)
         if (tets[i] >= N) return batch_fail(FEM_E_INDEX, "tet %zu names node %u >= N=%u", i / 4, tets[i], N);

@@ -576,12 +576,16 @@ __device__ __forceinline__ MeshAlpha warp_mesh_alpha(const BatchView<float>& b, 
     const uint32_t tile0 = b.mc[m].tile0, ntiles = b.mc[m].ntiles;
     const bool confirm = st.confirm != 0;  // measure the FP64 residual only, no CG update
     const double abs_eps_sq = st.abs_eps_sq, delta_new = st.delta_new;
+    const bool minres = b.mc[m].solver == kMeshSolverMinres;
     F2 a = lane_share_sum(tshare + tile0, ntiles, lane);
     a = warp_sum_f2(a);
     MeshAlpha r;
     r.dq = (double)a.hi + (double)a.lo;
-    r.brk = !confirm && ::fabs(r.dq) < abs_eps_sq;  // leave before the update
-    r.alpha = confirm ? 0.f : (float)(delta_new / r.dq);
+    r.brk = !minres && !confirm && ::fabs(r.dq) < abs_eps_sq;  // leave before the update
+    // MINRES: alpha = v^T A v (v is the product's operand; v1.v of the
+    // reference's order is the same in exact arithmetic, since v0 is
+    // orthogonal to v)
+    r.alpha = confirm ? 0.f : minres ? (float)r.dq : (float)(delta_new / r.dq);
     if (publish && lane == 0) {
         st.dot_dq = r.dq;
         st.brk = r.brk ? 1u : 0u;
@@ -597,6 +601,70 @@ __global__ void __launch_bounds__(256) k_mesh_alpha(BatchView<float> b, const fl
         if (b.st[m].done) continue;
         (void)warp_mesh_alpha(b, tshare, m, true);
     }
+}
+
+// The node pass of chunk ci of a MINRES mesh (v in r, v0 in d, v1 into
+// b.mr_v1): v1 = S A v - beta v0 - alpha v and its |v1|^2 share
+// (ILSS_MINRES.h:117-130, alpha from the tile shares). On a confirming
+// iteration (the residual estimate carried by the Givens sines has passed
+// the test) the FP64 residual of the iterate goes into r instead, and its
+// |r|^2 decides in the per-mesh update whether the mesh leaves or restarts.
+__device__ __noinline__ void node_mr_chunk(const BatchView<float>& b, const float* part, const double* part64,
+                                           const double* bv, const double* y, float* r, const float* d,
+                                           float2* cshare, const uint32_t ci, const ChunkMeta ch,
+                                           const float alpha_s)
+{
+    __shared__ float2 sh[32];
+    const StepScalars& sm = b.st[ch.mesh];
+    const MeshConsts& c = b.mc[ch.mesh];
+    const bool confirm = sm.confirm != 0;
+    const float nb = -(float)sm.mr.beta_new, na = -alpha_s;
+    const float fK = c.fK_f, mfm = c.mfm_f;
+    float* v1 = b.mr_v1;
+    float acc = 0.f;
+    for (size_t n = ch.n0 + threadIdx.x; n < ch.n1; n += blockDim.x) {
+        const size_t i = 3 * n;
+        if (b.fixed[n]) {
+            if (!confirm) v1[i] = v1[i + 1] = v1[i + 2] = 0.f;
+            continue;
+        }
+        float s0 = part[i], s1 = part[i + 1], s2 = part[i + 2];
+        const uint32_t j0 = b.ov_ptr[n];
+        const uint32_t j1 = bounds_idx(b.ov_ptr[n + 1], b.nslots - b.Ntot + 1, kSitePartialSlot);
+        for (uint32_t j = j0; j < j1; j++) {
+            const size_t o = 3 * ((size_t)b.Ntot + j);
+            s0 += part[o];
+            s1 += part[o + 1];
+            s2 += part[o + 2];
+        }
+        if (confirm) {
+            double t0 = part64[i], t1 = part64[i + 1], t2 = part64[i + 2];
+            for (uint32_t j = j0; j < j1; j++) {
+                const size_t o = 3 * ((size_t)b.Ntot + j);
+                t0 += part64[o];
+                t1 += part64[o + 1];
+                t2 += part64[o + 2];
+            }
+            const double mfm64 = c.mass * c.factor_M;
+            const float r0 = (float)(bv[i] - (c.factor_K * t0 + mfm64 * y_full(b, y, i)));
+            const float r1 = (float)(bv[i + 1] - (c.factor_K * t1 + mfm64 * y_full(b, y, i + 1)));
+            const float r2 = (float)(bv[i + 2] - (c.factor_K * t2 + mfm64 * y_full(b, y, i + 2)));
+            r[i] = r0; r[i + 1] = r1; r[i + 2] = r2;
+            acc += r0 * r0 + r1 * r1 + r2 * r2;
+        } else {
+            const float v0 = r[i], va = r[i + 1], vb = r[i + 2];
+            float w0 = __fmaf_rn(nb, d[i], fK * s0 + mfm * v0);
+            float w1 = __fmaf_rn(nb, d[i + 1], fK * s1 + mfm * va);
+            float w2 = __fmaf_rn(nb, d[i + 2], fK * s2 + mfm * vb);
+            w0 = __fmaf_rn(na, v0, w0);
+            w1 = __fmaf_rn(na, va, w1);
+            w2 = __fmaf_rn(na, vb, w2);
+            v1[i] = w0; v1[i + 1] = w1; v1[i + 2] = w2;
+            acc += w0 * w0 + w1 * w1 + w2 * w2;
+        }
+    }
+    const F2 rr = block_sum_f2(F2{acc, 0.f}, sh);
+    if (threadIdx.x == 0) cshare[ci] = make_float2(rr.hi, rr.lo);
 }
 
 // The node pass of chunk ci (every thread of the block calls it; fuse: the
@@ -630,6 +698,10 @@ __device__ __forceinline__ void node_update_chunk(const BatchView<float>& b, con
     } else {
         brk = sm.brk != 0;
         alpha_s = sm.alpha_f;
+    }
+    if (c.solver == kMeshSolverMinres) {
+        node_mr_chunk(b, part, part64, bv, y, r, d, cshare, ci, ch, alpha_s);
+        return;
     }
     const bool confirm = sm.confirm != 0;
     const bool refresh = sm.refresh_next != 0;
@@ -776,6 +848,58 @@ __global__ void __launch_bounds__(256) k_node_update_fused(BatchView<float> b, c
     node_update_pass(b, part, part64, bv, y, r, d, cshare, tshare, blockIdx.x, gridDim.x, b.fuse_alpha != 0);
 }
 
+// A MINRES mesh's update from |v1|^2 (or, on a confirming iteration, the
+// FP64 |r|^2): the Givens rotation, the residual estimate and the loop test
+// (ILSS_MINRES.h:131-160). When the estimate passes, the next iteration
+// measures the FP64 residual of the iterate (the FP32 Lanczos vectors carry
+// the estimate only to FP32 accuracy); if that fails the test, MINRES
+// restarts from it.
+__device__ __forceinline__ void mesh_update_minres(const BatchView<float>& b, const MeshConsts& c, StepScalars& st,
+                                                   const double total)
+{
+    if (st.confirm) {
+        st.confirm = 0;
+        st.refresh_next = 0;
+        st.delta_old = st.delta_new;
+        st.delta_new = total;
+        if (!isfinite(total)) st.status = 3u;
+        if (cg_cont_t(st)) {
+            minres_start(st.mr, total);
+            st.mr_pending = 2u;
+            st.done = 0;
+        } else {
+            st.mr_pending = 0u;
+            st.done = 1;
+            st.finished = 1;
+            atomicAdd(b.list_dirty, c.ntiles);
+            finish_stats_t(st);
+        }
+        return;
+    }
+    st.mr.beta = st.mr.beta_new;
+    st.mr.alpha = (double)st.alpha_f;
+    minres_givens(st.mr, total);
+    st.delta_old = st.delta_new;
+    st.delta_new = st.mr.norm_r_sq;
+    st.k += 1;
+    st.total_iters += 1;
+    const bool finite = isfinite(total) && isfinite(st.mr.norm_r_sq);
+    if (!finite) st.status = 3u;
+    st.mr_pending = 1u;
+    bool cont = cg_cont_t(st);
+    if (!cont && finite && st.k < st.max_iter) {
+        cont = true;
+        st.confirm = 1u;
+        st.refresh_next = 1u;
+    }
+    st.done = cont ? 0u : 1u;
+    if (st.done) {
+        finish_stats_t(st);
+        st.finished = 1;
+        atomicAdd(b.list_dirty, c.ntiles);
+    }
+}
+
 // Per running mesh, after the node pass: |r|^2 from its chunks' shares
 // (fixed order), then beta, the reliable-update and exit-confirmation rules
 // and the loop test (ILSS_CG.h:100-144). One warp per mesh; the last block
@@ -797,7 +921,11 @@ __device__ __forceinline__ void mesh_update_one(const BatchView<float>& b, const
     if (done) return;
     F2 tot = lane_share_sum(cshare + chunk0, nchunks, lane);
     tot = warp_sum_f2(tot);
-    if (lane == 0) {
+    if (lane == 0 && c.solver == kMeshSolverMinres) {
+        mesh_update_minres(b, c, st, (double)tot.hi + (double)tot.lo);
+        b.st[mesh] = st;
+        __threadfence();  // the mesh's scalars before the grid arrival that follows
+    } else if (lane == 0) {
         const bool confirm = st.confirm != 0, brk = st.brk != 0;
         if (confirm) {
             // the FP64 residual of the current iterate decides: leave,
