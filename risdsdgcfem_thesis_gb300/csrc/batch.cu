@@ -112,6 +112,9 @@ uint32_t spread10(uint32_t v)
 static_assert(kMeshRotationMsvd == FEM_ROTATION_MSVD && kMeshRotationDapd == FEM_ROTATION_DAPD,
               "per-mesh rotation values are enum fem_rotation's");
 static_assert(kMeshSolverCg == FEM_LS_CG && kMeshSolverMinres == FEM_LS_MINRES, "solver ids follow fem_tet.h");
+static_assert(kMeshQie == FEM_INTEGRATOR_QIE_V && kMeshFie == FEM_INTEGRATOR_FIE_DX &&
+                  kMeshFieQuasi == FEM_INTEGRATOR_FIE_DX_QUASISTATIC,
+              "integrator ids follow fem_tet.h");
 static_assert(kTileMaterialWrp == FEM_MATERIAL_C_WRP && kTileMaterialLcm == FEM_MATERIAL_C_LCM,
               "per-tile material values are enum fem_material's");
 
@@ -151,6 +154,8 @@ struct fem_batch_s {
     bool any_dapd = false;
     bool any_lcm = false;
     bool any_minres = false;
+    bool any_fie = false;
+    Dev<double> xn, vn;                  // FIE meshes: x^n, v^n of the step
     Dev<unsigned char> mr_p_s, mr_p0_s;  // MINRES meshes: directions p, p0 (S-typed)
     Dev<double> cpart_b;                 // MINRES meshes: per-chunk |b|^2 partials
     Dev<unsigned char> blob;
@@ -214,6 +219,8 @@ struct fem_batch_s {
         b.mr_p0 = reinterpret_cast<S*>(mr_p0_s.p);
         b.mr_v1 = reinterpret_cast<S*>(q_s.p);
         b.cpart_b = cpart_b.p;
+        b.xn = xn.p;
+        b.vn = vn.p;
         const bool mixed = opt.precision == FEM_PRECISION_MIXED;
         b.act_tiles = mixed ? act_tiles.p : nullptr;
         b.act_chunks = mixed ? act_chunks.p : nullptr;
@@ -247,7 +254,7 @@ struct fem_batch_s {
         knc_target.release(); r_s.release(); d_s.release(); q_s.release(); part_s.release(); ydelta_s.release(); counter.release();
         any_flag.release(); refresh_flag.release(); mcount.release(); err.release(); gbar.release(); blob.release();
         prev_x.release(); doc.release(); Fe.release();
-        mr_p_s.release(); mr_p0_s.release(); cpart_b.release();
+        mr_p_s.release(); mr_p0_s.release(); cpart_b.release(); xn.release(); vn.release();
         blob_off16.release();
         act_tiles.release(); act_chunks.release(); act_count.release(); list_dirty.release(); slice.release();
         start_tiles.release(); start_chunks.release(); launch_tiles.release(); launch_chunks.release();
@@ -342,26 +349,37 @@ cudaError_t capture_conditional(cudaStream_t s, cudaGraphConditionalHandle h, cu
 //   WHILE some mesh iterates (and the launch's iteration budget is not
 //         spent): one CG iteration (mixed: IF refresh { FP64 A y })
 //   integration and energies of the meshes whose loop ended in this launch.
+// With an FIE mesh in the batch the step has a Newton level:
+//   reset
+//   IF some mesh starts: BeginEvaluation
+//   WHILE some mesh takes a Newton iteration (QIE meshes take one):
+//     f_e, b_k, constraints, A y, r0 and the per-mesh |b_k| test
+//     WHILE some mesh iterates: one CG (or MINRES) iteration
+//     QIE: integration; FIE: x_k += y, v_k, |y|, the Newton count and
+//     limit, BeginEvaluation(x^n, x_k); the next iteration's lists
+//   energies.
 // In graph capture the conditions are set on the device; outside capture the
-// same kernels run with the loop on the host, in chunks, reading the meshes'
-// flags.
+// same kernels run with the loops on the host, in chunks, reading the
+// meshes' flags.
 template <typename S>
 int enqueue_step(fem_batch B, cudaStream_t s, bool capture)
 {
     const BatchView<S> b = B->view<S>();
     const bool mixed = B->opt.precision == FEM_PRECISION_MIXED;
+    const bool newton = B->any_fie;
     S* r = reinterpret_cast<S*>(B->r_s.p);
     S* d = reinterpret_cast<S*>(B->d_s.p);
     S* q = reinterpret_cast<S*>(B->q_s.p);
     S* part = reinterpret_cast<S*>(B->part_s.p);
     using L = BatchLaunch<S>;
-    cudaGraphConditionalHandle cond = 0, if_start = 0;
+    cudaGraphConditionalHandle cond = 0, if_start = 0, nw = 0;
+    cudaGraph_t top = nullptr;
     if (capture) {
-        cudaGraph_t g = nullptr;
         cudaStreamCaptureStatus cs;
-        BCK(cudaStreamGetCaptureInfo(s, &cs, nullptr, &g, nullptr, nullptr, nullptr));
-        BCK(cudaGraphConditionalHandleCreate(&cond, g, 0, cudaGraphCondAssignDefault));
-        BCK(cudaGraphConditionalHandleCreate(&if_start, g, 0, cudaGraphCondAssignDefault));
+        BCK(cudaStreamGetCaptureInfo(s, &cs, nullptr, &top, nullptr, nullptr, nullptr));
+        if (!newton) BCK(cudaGraphConditionalHandleCreate(&cond, top, 0, cudaGraphCondAssignDefault));
+        BCK(cudaGraphConditionalHandleCreate(&if_start, top, 0, cudaGraphCondAssignDefault));
+        if (newton) BCK(cudaGraphConditionalHandleCreate(&nw, top, 0, cudaGraphCondAssignDefault));
     }
     LoopSync ls;
     ls.mcount = B->mcount.p;
@@ -374,8 +392,8 @@ int enqueue_step(fem_batch B, cudaStream_t s, bool capture)
     ls.set_cond = capture ? 1 : 0;
     LoopSync lb = ls;
     lb.body_runs = B->any_flag.p;
-    auto start_section = [&](cudaStream_t ss) {
-        L::begin_eval(b, B->x.p, ss);
+    // f_e, b, constraints, A y, r0 of the meshes in the start lists
+    auto solve_start = [&](cudaStream_t ss) {
         L::tile_force(b, B->x.p, B->part64.p, nullptr, ss);
         L::node_b(b, B->part64.p, B->v.p, B->x.p, B->bvec.p, B->y.p, ss);
         L::knc(b, B->K, B->x.p, B->bvec.p, B->y.p, ss);
@@ -404,13 +422,9 @@ int enqueue_step(fem_batch B, cudaStream_t s, bool capture)
         // their loop test
         if (B->any_minres) L::node_mr_finish(b, B->y.p, r, d, q, ls, bs);
     };
-    L::reset_counts(b, ls, if_start, s);
-    if (capture) {
-        BCK(capture_conditional(s, if_start, cudaGraphCondTypeIf, [&](cudaStream_t ss, cudaGraph_t) {
-            start_section(ss);
-            return cudaGetLastError();
-        }));
-        BCK(capture_conditional(s, cond, cudaGraphCondTypeWhile, [&](cudaStream_t bs, cudaGraph_t bodyg) {
+    // the CG loop as a WHILE node after the capture point of `cs`
+    auto capture_cg = [&](cudaStream_t cs) {
+        return capture_conditional(cs, ls.cond, cudaGraphCondTypeWhile, [&](cudaStream_t bs, cudaGraph_t bodyg) {
             cudaGraphConditionalHandle ifh = 0;
             if (mixed) {
                 const cudaError_t e = cudaGraphConditionalHandleCreate(&ifh, bodyg, 0, 0);
@@ -427,11 +441,11 @@ int enqueue_step(fem_batch B, cudaStream_t s, bool capture)
             }
             body_tail(bs);
             return cudaGetLastError();
-        }));
-    } else {
-        bool any_start = B->mask_host.empty();
-        for (uint8_t a : B->mask_host) any_start |= a == 1;
-        if (any_start) start_section(s);
+        });
+    };
+    // the CG loop driven from the host: chunks of iterations, then read the
+    // per-mesh flags
+    auto host_cg = [&]() -> int {
         bool coop = false;
         if constexpr (sizeof(S) == 4) {
             if (B->opt.persistent_loop) {
@@ -454,7 +468,6 @@ int enqueue_step(fem_batch B, cudaStream_t s, bool capture)
                 coop = true;
             }
         }
-        // host-driven loop: chunks of iterations, then read the per-mesh flags
         uint32_t budget = B->slice_budget, ran = 0;
         for (; !coop;) {
             BCK(cudaMemcpyAsync(B->st_host, B->st.p, sizeof(StepScalars) * B->M, cudaMemcpyDeviceToHost, s));
@@ -468,9 +481,64 @@ int enqueue_step(fem_batch B, cudaStream_t s, bool capture)
                 body_tail(s);
             }
         }
+        return FEM_OK;
+    };
+    // after a solve: QIE integration or the FIE update, re-evaluation and
+    // the next Newton iteration's lists
+    auto after_solve = [&](cudaStream_t as) {
+        L::integrate(b, B->x.p, B->v.p, B->y.p, B->cpart.p, ls, as);
+        if (newton) {
+            L::begin_eval(b, B->x.p, 1, as);
+            L::newton_tail(b, ls, nw, as);
+        }
+    };
+    L::reset_counts(b, ls, if_start, nw, newton ? 1 : 0, s);
+    bool any_start = B->mask_host.empty();
+    for (uint8_t a : B->mask_host) any_start |= a == 1;
+    if (capture && !newton) {
+        BCK(capture_conditional(s, if_start, cudaGraphCondTypeIf, [&](cudaStream_t ss, cudaGraph_t) {
+            L::begin_eval(b, B->x.p, 0, ss);
+            solve_start(ss);
+            return cudaGetLastError();
+        }));
+        BCK(capture_cg(s));
+        after_solve(s);
+    } else if (capture) {
+        BCK(capture_conditional(s, if_start, cudaGraphCondTypeIf, [&](cudaStream_t ss, cudaGraph_t) {
+            L::begin_eval(b, B->x.p, 0, ss);
+            return cudaGetLastError();
+        }));
+        BCK(capture_conditional(s, nw, cudaGraphCondTypeWhile, [&](cudaStream_t ns, cudaGraph_t nbody) {
+            // the CG loop's condition belongs to the Newton body; the start
+            // section's last kernel sets it
+            cudaError_t e = cudaGraphConditionalHandleCreate(&ls.cond, nbody, 0, cudaGraphCondAssignDefault);
+            if (e != cudaSuccess) return e;
+            lb.cond = ls.cond;
+            solve_start(ns);
+            e = capture_cg(ns);
+            if (e != cudaSuccess) return e;
+            after_solve(ns);
+            return cudaGetLastError();
+        }));
+    } else {
+        if (any_start) {
+            L::begin_eval(b, B->x.p, 0, s);
+            solve_start(s);
+        }
+        if (int e = host_cg()) return e;
+        after_solve(s);
+        // further Newton iterations while some FIE mesh goes on
+        while (newton) {
+            BCK(cudaMemcpyAsync(B->st_host, B->st.p, sizeof(StepScalars) * B->M, cudaMemcpyDeviceToHost, s));
+            BCK(cudaStreamSynchronize(s));
+            bool go = false;
+            for (uint32_t m = 0; m < B->M; m++) go |= B->st_host[m].nr_go != 0;
+            if (!go) break;
+            solve_start(s);
+            if (int e = host_cg()) return e;
+            after_solve(s);
+        }
     }
-    // ---- after the solve ----
-    L::integrate(b, B->x.p, B->v.p, B->y.p, s);
     bool energy = false;
     for (auto& m : B->meshes) energy |= m.p.compute_energy != 0;
     if (energy) {
@@ -549,9 +617,13 @@ int fem_batch_add_mesh(fem_batch b, const double* rest, uint32_t N, const uint32
     if (!rest || !tets || !p) return batch_fail(FEM_E_ARG, "null rest/tets/params");
     if (N == 0 || T == 0) return batch_fail(FEM_E_ARG, "empty mesh (N=%u, T=%u)", N, T);
     if (!(p->fixed_dt > 0)) return batch_fail(FEM_E_ARG, "fixed_dt must be > 0");
-    if (p->integrator != FEM_INTEGRATOR_QIE_V)
-        return batch_fail(FEM_E_ARG, "integrator %u: batches step with QIE_V; the FIE integrators run on fem_solid",
-                          p->integrator);
+    if (p->integrator != FEM_INTEGRATOR_QIE_V && p->integrator != FEM_INTEGRATOR_FIE_DX &&
+        p->integrator != FEM_INTEGRATOR_FIE_DX_QUASISTATIC)
+        return batch_fail(FEM_E_ARG, "unknown integrator %u", p->integrator);
+    if (p->integrator != FEM_INTEGRATOR_QIE_V && b->opt.persistent_loop)
+        return batch_fail(FEM_E_ARG, "the persistent loop takes QIE_V meshes only");
+    if (p->integrator != FEM_INTEGRATOR_QIE_V && !(p->nr_abs_epsilon >= 0))
+        return batch_fail(FEM_E_ARG, "nr_abs_epsilon must be >= 0");
     if (p->rotation != FEM_ROTATION_MSVD && p->rotation != FEM_ROTATION_DAPD)
         return batch_fail(FEM_E_ARG, "unknown rotation %u", p->rotation);
     if (p->rotation == FEM_ROTATION_DAPD &&
@@ -846,6 +918,20 @@ int fem_batch_finalize(fem_batch b)
         c.mass = 1.0 / inv_mass;
         c.factor_M = 1.0 + c.dt * ray[0];
         c.factor_K = c.dt * c.dt + c.dt * ray[1];
+        c.integrator = p.integrator;
+        c.nr_max_iter = p.nr_max_iter;
+        c.nr_abs_eps = p.nr_abs_epsilon;
+        if (p.integrator != FEM_INTEGRATOR_QIE_V) {
+            // Step_FullyImplicitEuler_dx's system (LeafDSH_Solid3D_FEM.cpp:
+            // 1357-1411): A = (1/h^2 + a0/h) M + (1 + a1/h) K; the
+            // quasi-static variant drops every 1/h term
+            b->any_fie = true;
+            const bool quasi = p.integrator == FEM_INTEGRATOR_FIE_DX_QUASISTATIC;
+            c.dt = quasi ? 0.0 : p.fixed_dt;
+            c.inv_dt = quasi ? 0.0 : 1.0 / p.fixed_dt;
+            c.factor_M = c.inv_dt * c.inv_dt + c.inv_dt * ray[0];
+            c.factor_K = 1.0 + c.inv_dt * ray[1];
+        }
         for (int a = 0; a < 3; a++) c.gravity[a] = p.gravity[a];
         c.density = p.density;
         c.rel_eps_sq = p.ls_rel_epsilon * p.ls_rel_epsilon;
@@ -1105,7 +1191,11 @@ int fem_batch_finalize(fem_batch b)
         BCKC(b->mr_p0_s.alloc(N3 * SB));
         BCKC(cudaMemsetAsync(b->mr_p_s.p, 0, N3 * SB, s));
         BCKC(cudaMemsetAsync(b->mr_p0_s.p, 0, N3 * SB, s));
-        BCKC(b->cpart_b.alloc(b->nchunks));
+    }
+    if (b->any_minres || b->any_fie) BCKC(b->cpart_b.alloc(b->nchunks));
+    if (b->any_fie) {
+        BCKC(b->xn.alloc(N3));
+        BCKC(b->vn.alloc(N3));
     }
     std::vector<uchar2> doc_none;
     if (b->any_dapd) {
@@ -1131,7 +1221,7 @@ int fem_batch_finalize(fem_batch b)
                       b->Dinv64.bytes() + b->vol.bytes() + b->detF.bytes() + b->tile_nodes.bytes() +
                       b->lptr0.bytes() + b->ov_ptr.bytes() + b->ov_map.bytes() + b->knc_node.bytes() +
                       b->perm.bytes() + b->prev_x.bytes() + b->doc.bytes() + b->Fe.bytes() + b->mr_p_s.bytes() +
-                      b->mr_p0_s.bytes() + b->cpart_b.bytes() +
+                      b->mr_p0_s.bytes() + b->cpart_b.bytes() + b->xn.bytes() + b->vn.bytes() +
                       b->knc_mesh.bytes() + b->knc_target.bytes() + b->lconn.bytes() + b->lptr.bytes() +
                       b->lidx.bytes() + b->fixed.bytes() + b->rest.bytes() + b->x.bytes() + b->v.bytes() +
                       b->bvec.bytes() + b->y.bytes() + b->r_s.bytes() + b->d_s.bytes() + b->q_s.bytes() +
@@ -1434,6 +1524,8 @@ int fem_batch_set_active(fem_batch b, const uint8_t* mask)
 int fem_batch_set_slice(fem_batch b, uint32_t max_iterations)
 {
     if (int e = check_ready(b)) return e;
+    if (max_iterations && b->any_fie)
+        return batch_fail(FEM_E_ARG, "iteration budgets are for QIE_V batches (a Newton step runs whole)");
     b->slice_budget = max_iterations;
     BCK(cudaMemcpyAsync(b->slice.p, &b->slice_budget, sizeof(uint32_t), cudaMemcpyHostToDevice, b->stream));
     BCK(cudaStreamSynchronize(b->stream));
@@ -1496,7 +1588,7 @@ int fem_batch_finished(fem_batch b, uint8_t* flags)
     if (!flags) return batch_fail(FEM_E_ARG, "null flags");
     for (uint32_t m = 0; m < b->M; m++) {
         const StepScalars& h = b->st_host[m];
-        flags[m] = h.finished ? 1 : (h.done ? 0 : 2);
+        flags[m] = h.step_done ? 1 : (h.done ? 0 : 2);
     }
     return FEM_OK;
 }
@@ -1523,6 +1615,15 @@ int fem_batch_get_stats(fem_batch b, uint32_t mesh, fem_step_stats* out)
     out->resolved_isotropic = h.res_isotropic;
     out->resolved_tie = h.res_tie;
     out->resolved_check = h.res_check;
+    if (b->mc_host[mesh].integrator != kMeshQie) {
+        // the Leaf's FIE stats (m_SolverLS_NumIter summed over the Newton
+        // iterations, m_SolverNR_NumIter, m_SolverNR_AbsPrec)
+        out->cg_iterations = h.fie_cg;
+        if (!h.nr_solved) out->rel_residual = out->abs_residual = 0.0;
+        out->nr_iterations = h.nr_k;
+        out->nr_abs_residual = h.nr_abs;
+        out->nr_rel_residual = h.nr_delta0 > 0 ? h.nr_abs / h.nr_delta0 : 0.0;
+    }
     return FEM_OK;
 }
 

@@ -87,6 +87,14 @@ constexpr uint32_t kMeshRotationDapd = 1;
 constexpr uint32_t kMeshSolverCg = 0;
 constexpr uint32_t kMeshSolverMinres = 1;
 
+// The mesh's integrator: QIE_V (one linear solve per step), or the
+// fully-implicit Newton on Delta x (dynamic or quasi-static), whose steps
+// loop over Newton iterations on the device, each mesh leaving the loop on
+// its own |b_k| test or iteration limit.
+constexpr uint32_t kMeshQie = 0;
+constexpr uint32_t kMeshFie = 1;
+constexpr uint32_t kMeshFieQuasi = 2;
+
 struct TileMeta {
     uint32_t mesh;
     uint32_t e0;      // first element (global)
@@ -136,6 +144,9 @@ struct MeshConsts {
     uint32_t rotation;       // kMeshRotationMsvd or kMeshRotationDapd (FP64 in either precision)
     uint32_t material;       // kTileMaterialWrp or kTileMaterialLcm
     uint32_t solver;         // kMeshSolverCg or kMeshSolverMinres
+    uint32_t integrator;     // kMeshQie, kMeshFie or kMeshFieQuasi
+    uint32_t nr_max_iter;    // FIE: Newton iteration limit
+    double nr_abs_eps;       // FIE: the Newton loop ends once |b_k| is below this
     double lame_mu, lame_lambda;  // C_LCM: from the mesh's scalar E and nu (per-element values re-bake only K0)
     double dapd_thr, dapd_fL, dapd_fNL, dapd_eNL;  // DAPD: threshold on det F, offset factors, exponent
 
@@ -151,7 +162,9 @@ struct BatchView {
     S* mr_p;                       // [3 Ntot] MINRES: direction p; null without a MINRES mesh
     S* mr_p0;                      // [3 Ntot] MINRES: the previous direction p0
     S* mr_v1;                      // [3 Ntot] MINRES: the Lanczos vector v1 (the q buffer)
-    double* cpart_b;               // [nchunks] MINRES: per-chunk partials of |b|^2 at the start of a step
+    double* cpart_b;               // [nchunks] MINRES, FIE: per-chunk partials of |b|^2 at the start of a solve
+    double* xn;                    // [3 Ntot] FIE: x^n, the positions at the start of the step; null without FIE
+    double* vn;                    // [3 Ntot] FIE: v^n
     uint32_t pipe_tile;            // mixed: threads per block of the tile product (kPipeSmallTile or kTileElems)
     uint32_t fuse_alpha;           // mixed: the node pass forms alpha (no separate alpha kernel)
     uint32_t has_lcm;              // some mesh takes the C_LCM product
@@ -202,5 +215,13 @@ struct BatchView {
     const uint32_t* knc_mesh;      // [K]
     const double* knc_target;      // [3K]
 };
+
+// Whether mesh m takes part in the current start section (the opening of a
+// step, or of a further Newton iteration of an FIE mesh).
+template <typename S>
+__device__ __forceinline__ bool mesh_starts(const BatchView<S>& b, uint32_t m)
+{
+    return b.st[m].nr_go != 0;
+}
 
 }  // namespace femgb

@@ -225,7 +225,7 @@ __global__ void __launch_bounds__(256) k_tile_force(BatchView<S> b, const double
         const uint32_t t = list[i];
         const TileMeta tm = b.tiles[t];
         // the force of a starting step, or the energy of a finished one
-        if (part64 ? b.active[tm.mesh] != 1 : !b.st[tm.mesh].finished) continue;
+        if (part64 ? !mesh_starts(b, tm.mesh) : !b.st[tm.mesh].step_done) continue;
         double energy = 0.0;
         if (threadIdx.x < tm.ne && tm.material == kTileMaterialLcm) {
             // C_LCM_f_e and C_LCM_V (TetrahedronElementSet3.cpp:1154-1178,
@@ -340,7 +340,7 @@ __global__ void k_tile_potential(BatchView<S> b, const double* __restrict__ x, d
     for (uint32_t i = blockIdx.x; i < n; i += gridDim.x) {
         const uint32_t t = b.launch_tiles[i];
         const TileMeta tm = b.tiles[t];
-        if (!b.st[tm.mesh].finished) continue;
+        if (!b.st[tm.mesh].step_done) continue;
         const MeshConsts& c = b.mc[tm.mesh];
         double acc = 0.0;
         if (threadIdx.x < tm.ne) {
@@ -386,7 +386,11 @@ __device__ __forceinline__ void sum_parts(const BatchView<S>& b, const P* __rest
     }
 }
 
-// b = dt (m g - f_e-product) + m v ; y = v
+// QIE: b = dt (m g - f_e-product) + m v ; y = v.
+// FIE (Step_FullyImplicitEuler_dx, LeafDSH_Solid3D_FEM.cpp:1412-1440): on
+// the first Newton iteration x^n = x, v^n = v and the warm start
+// y = h v^n (else 0); b_k = m g - f(x_k) + (m/h)(v^n - (x_k - x^n)/h)
+// (quasi-static: 1/h = 0).
 template <typename S>
 __global__ void k_node_b(BatchView<S> b, const double* __restrict__ part64, const double* __restrict__ v,
                          const double* __restrict__ x, double* __restrict__ bv, double* __restrict__ y)
@@ -395,8 +399,30 @@ __global__ void k_node_b(BatchView<S> b, const double* __restrict__ part64, cons
     for (uint32_t il = blockIdx.x; il < nl; il += gridDim.x) {
         const uint32_t ci = b.start_chunks[il];
         const ChunkMeta ch = b.chunks[ci];
-        if (b.active[ch.mesh] != 1) continue;
+        if (!mesh_starts(b, ch.mesh)) continue;
         const MeshConsts& c = b.mc[ch.mesh];
+        const bool opening = c.integrator == kMeshQie || b.st[ch.mesh].nr_k == 0;
+        if (c.integrator != kMeshQie) {
+            const double im = c.inv_dt * c.mass;
+            for (size_t n = ch.n0 + threadIdx.x; n < ch.n1; n += blockDim.x) {
+                double f[3];
+                sum_parts(b, part64, n, f[0], f[1], f[2]);
+                const size_t i = 3 * n;
+#pragma unroll
+                for (int a = 0; a < 3; a++) {
+                    if (opening) {
+                        b.xn[i + a] = x[i + a];
+                        b.vn[i + a] = v[i + a];
+                        if (b.prev_x && c.rotation == kMeshRotationDapd) b.prev_x[i + a] = x[i + a];
+                    }
+                    const double bf = c.mass * c.gravity[a] - f[a];
+                    bv[i + a] = bf + im * (b.vn[i + a] - c.inv_dt * (x[i + a] - b.xn[i + a]));
+                    y[i + a] = opening ? c.dt * b.vn[i + a] : 0.0;
+                    if (b.ydelta) b.ydelta[i + a] = 0;
+                }
+            }
+            continue;
+        }
         // DAPD: this step's BeginEvaluation has read the previous positions;
         // the next one compares with this step's start (m_vecPos0 = x,
         // LeafDSH_Solid3D_FEM.cpp:927-935)
@@ -432,10 +458,21 @@ __global__ void k_knc(BatchView<S> b, uint32_t K, const double* __restrict__ x, 
 {
     for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < K; k += gridDim.x * blockDim.x) {
         const uint32_t m = b.knc_mesh[k];
-        if (b.active[m] != 1) continue;
+        if (!mesh_starts(b, m)) continue;
         const MeshConsts& c = b.mc[m];
         const size_t n = bounds_idx(b.knc_node[k], b.Ntot, kSiteKncNode);
         const double* tg = b.knc_target + 3 * (size_t)k;
+        if (c.integrator != kMeshQie) {
+            // FIE: the constraint rows as Delta x, b = y = target - x_k
+            // (LeafDSH_Solid3D_FEM.cpp:1441-1465)
+#pragma unroll
+            for (int a = 0; a < 3; a++) {
+                const double dx = tg[a] - x[3 * n + a];
+                bv[3 * n + a] = dx;
+                y[3 * n + a] = dx;
+            }
+            continue;
+        }
         V3<double> vk = mk<double>(c.inv_dt * (tg[0] - x[3 * n]), c.inv_dt * (tg[1] - x[3 * n + 1]),
                                    c.inv_dt * (tg[2] - x[3 * n + 2]));
         const double norm_vk = ::sqrt(dot0(vk, vk));
@@ -541,10 +578,12 @@ __global__ void k_node_residual(BatchView<S> b, const double* __restrict__ part6
     for (uint32_t il = blockIdx.x; il < nl; il += gridDim.x) {
         const uint32_t ci = b.start_chunks[il];
         const ChunkMeta ch = b.chunks[ci];
-        if (b.active[ch.mesh] != 1) continue;
+        if (!mesh_starts(b, ch.mesh)) continue;
         const MeshConsts& c = b.mc[ch.mesh];
         const double mfm = c.mass * c.factor_M;
         const bool minres = c.solver == kMeshSolverMinres;
+        const bool fie = c.integrator != kMeshQie;
+        const bool need_b = minres || fie;
         double acc = 0.0, acc_b = 0.0;
         for (size_t n = ch.n0 + threadIdx.x; n < ch.n1; n += blockDim.x) {
             const size_t i = 3 * n;
@@ -559,19 +598,42 @@ __global__ void k_node_residual(BatchView<S> b, const double* __restrict__ part6
             r[i] = r0; r[i + 1] = r1; r[i + 2] = r2;
             d[i] = 0; d[i + 1] = 0; d[i + 2] = 0;
             acc += (double)r0 * (double)r0 + (double)r1 * (double)r1 + (double)r2 * (double)r2;
-            // MINRES's relative test is on |b| (every row, constrained ones too)
-            if (minres) acc_b += bv[i] * bv[i] + bv[i + 1] * bv[i + 1] + bv[i + 2] * bv[i + 2];
+            // |b| over every row, constrained ones too: MINRES's relative
+            // test and FIE's Newton test
+            if (need_b) acc_b += bv[i] * bv[i] + bv[i + 1] * bv[i + 1] + bv[i + 2] * bv[i + 2];
         }
         const double sum = bblock_sum(acc);
-        const double sum_b = minres ? bblock_sum(acc_b) : 0.0;
+        const double sum_b = need_b ? bblock_sum(acc_b) : 0.0;
         if (threadIdx.x == 0) {
             cpart[ci] = sum;
-            if (minres) b.cpart_b[ci] = sum_b;
+            if (need_b) b.cpart_b[ci] = sum_b;
         }
         if (arrive_last(ls.mcount + ch.mesh, c.nchunks)) {
             const double total = mesh_partial_sum(cpart, c.chunk0, c.nchunks);
-            const double total_b = minres ? mesh_partial_sum(b.cpart_b, c.chunk0, c.nchunks) : 0.0;
-            if (threadIdx.x == 0 && minres) {
+            const double total_b = need_b ? mesh_partial_sum(b.cpart_b, c.chunk0, c.nchunks) : 0.0;
+            bool newton_ends = false;
+            if (threadIdx.x == 0) {
+                StepScalars& s = b.st[ch.mesh];
+                if (c.integrator == kMeshQie) {
+                    s.nr_go = 0;
+                } else {
+                    // the Newton test on |b_k| (LeafDSH_Solid3D_FEM.cpp:1466-1480):
+                    // below the tolerance (or not finite) the loop ends
+                    // without a solve
+                    const double nb = ::sqrt(total_b);
+                    if (s.nr_k == 0) s.nr_delta0 = nb;
+                    s.nr_abs = nb;
+                    if (!isfinite(nb) || nb < c.nr_abs_eps) {
+                        newton_ends = true;
+                        if (!isfinite(nb)) s.status = 3u;
+                        s.done = 1;
+                        s.nr_go = 0;
+                        s.mr_pending = 0;
+                        s.step_done = 1;
+                    }
+                }
+            }
+            if (threadIdx.x == 0 && !newton_ends && minres) {
                 // ILSS_MINRES::Solve's start (ILSS_MINRES.h:66-107); the
                 // next finishing pass normalises v = r0 / |r0|
                 StepScalars& s = b.st[ch.mesh];
@@ -598,7 +660,7 @@ __global__ void k_node_residual(BatchView<S> b, const double* __restrict__ part6
                     finish_stats(s);
                     s.finished = 1;
                 }
-            } else if (threadIdx.x == 0) {
+            } else if (threadIdx.x == 0 && !newton_ends) {
                 StepScalars& s = b.st[ch.mesh];
                 s.delta_0 = total;
                 s.delta_new = total;
@@ -893,25 +955,84 @@ __global__ void k_node_mr_finish(BatchView<S> b, double* __restrict__ y, S* __re
     }
 }
 
-// v = y ; x += dt y
+// After a linear solve, per chunk of a mesh whose loop ended in it:
+// QIE: v = y ; x += dt y, and the step is done.
+// FIE (LeafDSH_Solid3D_FEM.cpp:1500-1529): x_k += y ; v_k = (x_k - x^n)/h ;
+// |y|; the last block of the mesh counts the Newton iteration and decides
+// whether the loop goes on (below the iteration limit); the step's
+// BeginEvaluation at x_k follows in any case.
 template <typename S>
 __global__ void k_integrate(BatchView<S> b, double* __restrict__ x, double* __restrict__ v,
-                            const double* __restrict__ y)
+                            const double* __restrict__ y, double* __restrict__ cpart, LoopSync ls)
 {
     const uint32_t nl = b.list_count[3];
     for (uint32_t il = blockIdx.x; il < nl; il += gridDim.x) {
-        const ChunkMeta ch = b.chunks[b.launch_chunks[il]];
+        const uint32_t ci = b.launch_chunks[il];
+        const ChunkMeta ch = b.chunks[ci];
         if (!b.st[ch.mesh].finished) continue;
-        const double dt = b.mc[ch.mesh].dt;
+        const MeshConsts& c = b.mc[ch.mesh];
+        if (c.integrator == kMeshQie) {
+            const double dt = c.dt;
+            for (size_t n = ch.n0 + threadIdx.x; n < ch.n1; n += blockDim.x) {
+#pragma unroll
+                for (int a = 0; a < 3; a++) {
+                    const size_t i = 3 * n + a;
+                    const double yi = y_full(b, y, i);
+                    v[i] = yi;
+                    x[i] = x[i] + dt * yi;
+                }
+            }
+            if (threadIdx.x == 0) b.st[ch.mesh].step_done = 1;
+            continue;
+        }
+        double acc = 0.0;
         for (size_t n = ch.n0 + threadIdx.x; n < ch.n1; n += blockDim.x) {
 #pragma unroll
             for (int a = 0; a < 3; a++) {
                 const size_t i = 3 * n + a;
                 const double yi = y_full(b, y, i);
-                v[i] = yi;
-                x[i] = x[i] + dt * yi;
+                const double xi = x[i] + yi;
+                x[i] = xi;
+                v[i] = c.inv_dt * (xi - b.xn[i]);
+                acc += yi * yi;
             }
         }
+        const double sum = bblock_sum(acc);
+        if (threadIdx.x == 0) cpart[ci] = sum;
+        if (arrive_last(ls.mcount + ch.mesh, c.nchunks)) {
+            const double total = mesh_partial_sum(cpart, c.chunk0, c.nchunks);
+            if (threadIdx.x == 0) {
+                StepScalars& s = b.st[ch.mesh];
+                s.nr_abs = ::sqrt(total);
+                s.nr_k += 1;
+                s.fie_cg += s.k;
+                s.nr_solved = 1;
+                s.nr_go = s.nr_k < c.nr_max_iter ? 1u : 0u;
+                if (!s.nr_go) s.step_done = 1;
+                s.inverted = 0;  // counted again by the re-evaluation at x_k
+            }
+        }
+    }
+}
+
+// One block, last kernel of a Newton iteration: the start lists of the next
+// iteration (the FIE meshes going on), the finished flags cleared, and the
+// Newton loop's condition.
+template <typename S>
+__global__ void k_newton_tail(BatchView<S> b, LoopSync ls, cudaGraphConditionalHandle newton)
+{
+    int go = 0;
+    for (uint32_t m = threadIdx.x; m < b.M; m += blockDim.x) {
+        StepScalars& s = b.st[m];
+        s.finished = 0;
+        go |= s.nr_go ? 1 : 0;
+    }
+    go = __syncthreads_or(go);
+    build_mesh_lists(
+        b, [&](uint32_t m) { return b.st[m].nr_go != 0u; }, b.start_tiles, b.start_chunks, b.list_count);
+    if (threadIdx.x == 0) {
+        const bool stop = ls.err && *(volatile const unsigned*)ls.err;
+        if (ls.set_cond) cudaGraphSetConditional(newton, (go && !stop) ? 1u : 0u);
     }
 }
 
@@ -925,17 +1046,25 @@ __global__ void k_integrate(BatchView<S> b, double* __restrict__ x, double* __re
 // kernels (some mesh starts) and the CG loop's while condition (some mesh
 // continues); rebuilds the work lists when a running mesh was dropped.
 template <typename S>
-__global__ void k_reset_counts(BatchView<S> b, LoopSync ls, cudaGraphConditionalHandle if_start)
+__global__ void k_reset_counts(BatchView<S> b, LoopSync ls, cudaGraphConditionalHandle if_start,
+                               cudaGraphConditionalHandle newton, int newton_form)
 {
     int start = 0, cont = 0, dropped = 0;
     for (uint32_t m = threadIdx.x; m < b.M; m += blockDim.x) {
         StepScalars& s = b.st[m];
         const uint8_t a = b.active[m];
         s.finished = 0;
+        s.step_done = 0;
+        s.nr_go = a == 1 ? 1u : 0u;
         if (a == 1) {
             s.inverted = 0;
             s.fp64_resolved = 0;
             s.res_det_F = s.res_isotropic = s.res_tie = s.res_check = 0;
+            s.nr_k = 0;
+            s.nr_solved = 0;
+            s.fie_cg = 0;
+            s.nr_delta0 = 0.0;
+            s.nr_abs = 0.0;
             start = 1;
         } else if (a == 2) {
             cont |= s.done ? 0 : 1;
@@ -956,7 +1085,12 @@ __global__ void k_reset_counts(BatchView<S> b, LoopSync ls, cudaGraphConditional
         if (ls.slice) ls.slice[1] = 0u;
         if (ls.set_cond) {
             cudaGraphSetConditional(if_start, start ? 1u : 0u);
-            cudaGraphSetConditional(ls.cond, cont ? 1u : 0u);
+            // with a Newton level, the CG loop's condition belongs to the
+            // Newton body and is set there, by the start section
+            if (newton_form)
+                cudaGraphSetConditional(newton, (start || cont) ? 1u : 0u);
+            else
+                cudaGraphSetConditional(ls.cond, cont ? 1u : 0u);
         }
     }
 }
@@ -966,7 +1100,7 @@ template <typename S>
 __global__ void k_fin_energy(BatchView<S> b, int kind, const double* __restrict__ tpart)
 {
     for (uint32_t m = blockIdx.x; m < b.M; m += gridDim.x) {
-        if (!b.st[m].finished) continue;
+        if (!b.st[m].step_done) continue;
         const MeshConsts& c = b.mc[m];
         double acc = 0.0;
         for (uint32_t i = threadIdx.x; i < c.ntiles; i += blockDim.x) acc += tpart[c.tile0 + i];
@@ -1074,9 +1208,18 @@ void BatchLaunch<S>::node_mr_finish(const BatchView<S>& b, double* y, S* r, S* d
 }
 
 template <typename S>
-void BatchLaunch<S>::integrate(const BatchView<S>& b, double* x, double* v, const double* y, cudaStream_t s)
+void BatchLaunch<S>::integrate(const BatchView<S>& b, double* x, double* v, const double* y, double* cpart,
+                               const LoopSync& ls, cudaStream_t s)
 {
-    k_integrate<S><<<grid_chunks(b.nchunks), kNodeThreads, 0, s>>>(b, x, v, y);
+    k_integrate<S><<<grid_chunks(b.nchunks), kNodeThreads, 0, s>>>(b, x, v, y, cpart, ls);
+    launch_counter()++;
+}
+
+template <typename S>
+void BatchLaunch<S>::newton_tail(const BatchView<S>& b, const LoopSync& ls, cudaGraphConditionalHandle newton,
+                                 cudaStream_t s)
+{
+    k_newton_tail<S><<<1, 256, 0, s>>>(b, ls, newton);
     launch_counter()++;
 }
 
@@ -1089,9 +1232,9 @@ void BatchLaunch<S>::fin_energy(const BatchView<S>& b, int kind, const double* t
 
 template <typename S>
 void BatchLaunch<S>::reset_counts(const BatchView<S>& b, const LoopSync& ls, cudaGraphConditionalHandle if_start,
-                                   cudaStream_t s)
+                                   cudaGraphConditionalHandle newton, int newton_form, cudaStream_t s)
 {
-    k_reset_counts<S><<<1, 256, 0, s>>>(b, ls, if_start);
+    k_reset_counts<S><<<1, 256, 0, s>>>(b, ls, if_start, newton, newton_form);
     launch_counter()++;
 }
 

@@ -65,9 +65,13 @@ cudaError_t launch_cg_resident(const BatchView<float>& b, const CoopLoopArgs& a,
 
 template <typename S>
 struct BatchLaunch {
-    static void begin_eval(const BatchView<S>& b, const double* x, cudaStream_t s);  // rotation.cu
+    // rotation.cu; newton: the re-evaluation at x_k of the FIE meshes that
+    // have just updated (otherwise the meshes of the start section)
+    static void begin_eval(const BatchView<S>& b, const double* x, int newton, cudaStream_t s);
+    // newton: the Newton loop's while condition, set when newton_form (the
+    // step has a Newton level: some mesh integrates with FIE)
     static void reset_counts(const BatchView<S>& b, const LoopSync& ls, cudaGraphConditionalHandle if_start,
-                             cudaStream_t s);
+                             cudaGraphConditionalHandle newton, int newton_form, cudaStream_t s);
     static void tile_spmv(const BatchView<S>& b, const S* d, const S* r, S* part,
                           cudaGraphConditionalHandle if_refresh, int set_if, const unsigned* refresh_flag,
                           cudaStream_t s);
@@ -88,7 +92,10 @@ struct BatchLaunch {
     // MINRES meshes: the finishing pass of the start or of an iteration
     static void node_mr_finish(const BatchView<S>& b, double* y, S* r, S* d, const S* q, const LoopSync& ls,
                                cudaStream_t s);
-    static void integrate(const BatchView<S>& b, double* x, double* v, const double* y, cudaStream_t s);
+    static void integrate(const BatchView<S>& b, double* x, double* v, const double* y, double* cpart,
+                          const LoopSync& ls, cudaStream_t s);
+    static void newton_tail(const BatchView<S>& b, const LoopSync& ls, cudaGraphConditionalHandle newton,
+                            cudaStream_t s);
     static void fin_energy(const BatchView<S>& b, int kind, const double* tpart, cudaStream_t s);
 };
 

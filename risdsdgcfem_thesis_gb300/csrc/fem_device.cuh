@@ -52,6 +52,14 @@ struct StepScalars {
     uint32_t done_prev;     // MINRES: `done` as it was at the top of the current iteration
     uint32_t mr_pending;    // batch MINRES: 1 = this iteration's vector and iterate update is due,
                             // 2 = the start (or restart) residual is to be normalised
+    // batch: the step's Newton level (QIE meshes make one pass of it)
+    uint32_t nr_go;         // takes part in the next start section (b, constraints, r0)
+    uint32_t nr_k;          // FIE: Newton iterations of this step so far
+    uint32_t nr_solved;     // FIE: some linear solve ran in this step
+    uint32_t step_done;     // the step ended during this launch (energy, completion flag)
+    uint32_t fie_cg;        // FIE: linear-solver iterations summed over this step's Newton iterations
+    double nr_delta0;       // FIE: |b_0| of this step
+    double nr_abs;          // FIE: the last |b_k| or |y_k|
     unsigned long long total_iters;
     double host_sum;        // FIE: the last FIN_SUM total (|b_k|^2 or |y_k|^2), read by the host
     MinresScalars mr;       // MINRES solver state (FP64 solid)

@@ -92,7 +92,7 @@ __device__ __forceinline__ void tile_spmv_y64_pass(const BatchView<S>& b, const 
     for (uint32_t i = block; i < n; i += G) {
         const uint32_t t = list_entry(list, i);
         const TileMeta tm = b.tiles[t];
-        if (mode == SPMV_Y64_ALL && b.active[tm.mesh] != 1) continue;
+        if (mode == SPMV_Y64_ALL && !mesh_starts(b, tm.mesh)) continue;
         if (mode == SPMV_Y64_REFRESH && (!mesh_running(b, tm.mesh) || !refresh_now(b.mc[tm.mesh], b.st[tm.mesh])))
             continue;
         const uint16_t* lp = b.lptr + b.lptr0[t];

@@ -164,14 +164,19 @@ __device__ __forceinline__ int rotation_fp32(const double* F, float tol, S* Rs)
 // Three resident blocks per SM (80 registers): the double-float MSVD's long
 // dependency chains need the extra warps more than the registers.
 template <typename S>
-__global__ void __launch_bounds__(256, 3) k_begin_eval_batch(BatchView<S> b, const double* __restrict__ x)
+__global__ void __launch_bounds__(256, 3) k_begin_eval_batch(BatchView<S> b, const double* __restrict__ x,
+                                                              int newton)
 {
     __shared__ unsigned s_inv, s_res, s_cause[4];  // re-solves: det F, isotropic, tie, check
     const uint32_t n = b.list_count[0];
     for (uint32_t i = blockIdx.x; i < n; i += gridDim.x) {
         const uint32_t t = b.start_tiles[i];
         const TileMeta tm = b.tiles[t];
-        if (b.active[tm.mesh] != 1) continue;
+        // newton: the FIE meshes whose solve has just updated x_k
+        // (BeginEvaluation(x^n, x_k), LeafDSH_Solid3D_FEM.cpp:1529; their
+        // DAPD previous positions are x^n); otherwise the start section's
+        if (newton ? (b.mc[tm.mesh].integrator == kMeshQie || !b.st[tm.mesh].finished) : !mesh_starts(b, tm.mesh))
+            continue;
         if (threadIdx.x == 0) { s_inv = 0; s_res = 0; s_cause[0] = s_cause[1] = s_cause[2] = s_cause[3] = 0; }
         __syncthreads();
         if (threadIdx.x < tm.ne) {
@@ -279,16 +284,16 @@ __global__ void __launch_bounds__(256, 3) k_begin_eval_batch(BatchView<S> b, con
 }
 
 template <typename S>
-void BatchLaunch<S>::begin_eval(const BatchView<S>& b, const double* x, cudaStream_t s)
+void BatchLaunch<S>::begin_eval(const BatchView<S>& b, const double* x, int newton, cudaStream_t s)
 {
     prof_begin("begin_eval_batch", s);
-    k_begin_eval_batch<S><<<grid_tiles(b.ntiles), kTileElems, 0, s>>>(b, x);
+    k_begin_eval_batch<S><<<grid_tiles(b.ntiles), kTileElems, 0, s>>>(b, x, newton);
     prof_end("begin_eval_batch", s);
     launch_counter()++;
 }
 
-template void BatchLaunch<double>::begin_eval(const BatchView<double>&, const double*, cudaStream_t);
-template void BatchLaunch<float>::begin_eval(const BatchView<float>&, const double*, cudaStream_t);
+template void BatchLaunch<double>::begin_eval(const BatchView<double>&, const double*, int, cudaStream_t);
+template void BatchLaunch<float>::begin_eval(const BatchView<float>&, const double*, int, cudaStream_t);
 
 FEMGB_BOUNDS_ACCESSOR(bounds_read_rotation)
 

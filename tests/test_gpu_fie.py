@@ -132,8 +132,116 @@ def test_fie_matches_oracle_on_random_block(fem_lib, oracle):
     assert rel(xa, xb) <= TOL and rel(va, vb) <= 1e-8, (rel(xa, xb), rel(va, vb))
 
 
-def test_batch_rejects_fie(fem_lib):
+def _block_scene():
+    from test_oracle_fie import _fie_block_scene
+    return _fie_block_scene()
+
+
+def test_fp64_batch_fie_matches_reference(fem_lib):
+    """FIE meshes in an FP64 batch, each leaving the device-side Newton loop
+    on its own test (the cantilever stops at the Newton cap, the block with
+    a moving constraint partly on |b_k|), next to a QIE mesh: each against
+    the fixture the reference's element set wrote, with the solid's bars
+    (x, v 1e-10; Newton iterations equal; CG iterations within one per
+    solve or 2 %; energies 1e-8). The QIE mesh's result is the same bits as
+    in a batch of its own, and the host-driven loops give the graph's bits."""
+    g = np.load(os.path.join(GOLDEN, "fie_160.npz"))
+    gb = np.load(os.path.join(GOLDEN, "fie_block.npz"))
+    cant = dataclasses.replace(scenes.cantilever_160(), integrator=fem_lib.FEM_INTEGRATOR_FIE_DX)
+    block = _block_scene()
+    qie = scenes.cantilever_160()
+    bt = fem_lib.Batch([cant, block, qie], precision=fem_lib.FEM_PRECISION_FP64)
+    host = fem_lib.Batch([cant, block, qie], precision=fem_lib.FEM_PRECISION_FP64, use_graph=False)
+    alone = fem_lib.Batch([qie], precision=fem_lib.FEM_PRECISION_FP64)
+    stats0, stats1 = [], []
+    for k in range(g["x"].shape[0]):
+        bt.step(1)
+        host.step(1)
+        alone.step(1)
+        stats0.append(bt.stats(0))
+        if k < len(gb["iters"]):
+            stats1.append(bt.stats(1))
+        if k + 1 == len(gb["iters"]):
+            xb, vb = bt.state(1)
+            assert rel(xb, gb["x"]) <= TOL and rel(vb, gb["v"]) <= TOL, (rel(xb, gb["x"]), rel(vb, gb["v"]))
+    _check_steps(stats0, g)
+    _check_steps(stats1, gb)
+    assert min(st["nr_iterations"] for st in stats1) < block.nr_max_iter
+    x, v = bt.state(0)
+    assert rel(x, g["x"][-1]) <= TOL and rel(v, g["v"][-1]) <= TOL, (rel(x, g["x"][-1]), rel(v, g["v"][-1]))
+    xa, va = alone.state(0)
+    xq, vq = bt.state(2)
+    assert np.array_equal(xa, xq) and np.array_equal(va, vq)
+    for i in range(3):
+        xh, vh = host.state(i)
+        xg, vg = bt.state(i)
+        assert np.array_equal(xh, xg) and np.array_equal(vh, vg), i
+
+
+def test_fp64_batch_fie_quasistatic_matches_reference(fem_lib, oracle):
+    """The quasi-static cantilever (every step at the Newton cap) in a batch
+    next to a dynamic FIE mesh, with the solid's bar: max(1e-10, 10 x the
+    oracle's own spread under 1e-15 perturbations of the initial
+    positions)."""
+    g = np.load(os.path.join(GOLDEN, "fie_160.npz"))
+    sc = dataclasses.replace(scenes.cantilever_160(), integrator=fem_lib.FEM_INTEGRATOR_FIE_DX_QUASISTATIC)
+    steps = g["q_iters"].shape[0]
+    floor, spread = 0.0, 0
+    for seed in (1, 2, 3):
+        o = oracle.Solid(sc, "port")
+        x0 = sc.rest + 1e-15 * np.abs(sc.rest).max() * np.random.default_rng(seed).standard_normal(sc.rest.shape)
+        o.set_state(x0, np.zeros_like(x0))
+        its = [o.step()["iters"] for _ in range(steps)]
+        spread = max(spread, max(abs(a - int(b)) for a, b in zip(its, g["q_iters"])))
+        floor = max(floor, rel(o.state()[0], g["xq"]))
+    other = dataclasses.replace(scenes.cantilever_160(), integrator=fem_lib.FEM_INTEGRATOR_FIE_DX)
+    bt = fem_lib.Batch([other, sc], precision=fem_lib.FEM_PRECISION_FP64)
+    for k in range(steps):
+        bt.step(1)
+        st = bt.stats(1)
+        assert st["status"] == 0 and st["nr_iterations"] == int(g["q_nr_iters"][k])
+        assert abs(st["cg_iterations"] - int(g["q_iters"][k])) <= max(st["nr_iterations"], 2 * spread + 1), k
+    x, v = bt.state(1)
+    assert rel(x, g["xq"]) <= max(TOL, 10 * floor), (rel(x, g["xq"]), floor)
+    assert not np.any(v)
+
+
+def test_mixed_batch_fie_matches_reference(fem_lib):
+    """FIE on the mixed path (FP32 products in the CG loops, FP64 Newton
+    level: b_k, the update, the tests): the cantilever and the block with
+    a moving constraint within 1e-5 (x) and 1e-4 (v) of the fixtures, every
+    step's status 0; graph and host-driven loops give the same bits."""
+    g = np.load(os.path.join(GOLDEN, "fie_160.npz"))
+    gb = np.load(os.path.join(GOLDEN, "fie_block.npz"))
+    cant = dataclasses.replace(scenes.cantilever_160(), integrator=fem_lib.FEM_INTEGRATOR_FIE_DX)
+    block = _block_scene()
+    bt = fem_lib.Batch([cant, block], precision=fem_lib.FEM_PRECISION_MIXED, chunk_nodes=256)
+    host = fem_lib.Batch([cant, block], precision=fem_lib.FEM_PRECISION_MIXED, chunk_nodes=256, use_graph=False)
+    nb = len(gb["iters"])
+    for k in range(g["x"].shape[0]):
+        bt.step(1)
+        host.step(1)
+        assert bt.stats(0)["status"] == 0 and bt.stats(1)["status"] == 0, k
+        assert bt.stats(0)["nr_iterations"] == int(g["nr_iters"][k]), k
+        if k + 1 == nb:
+            xb, vb = bt.state(1)
+            assert rel(xb, gb["x"]) <= 1e-5 and rel(vb, gb["v"]) <= 1e-4, (rel(xb, gb["x"]), rel(vb, gb["v"]))
+    x, v = bt.state(0)
+    assert rel(x, g["x"][-1]) <= 1e-5 and rel(v, g["v"][-1]) <= 1e-4, (rel(x, g["x"][-1]), rel(v, g["v"][-1]))
+    for i in range(2):
+        xh, vh = host.state(i)
+        xg, vg = bt.state(i)
+        assert np.array_equal(xh, xg) and np.array_equal(vh, vg), i
+
+
+def test_fie_batch_runs_newton_steps_whole(fem_lib):
+    """A batch with an FIE mesh takes no iteration budget (a Newton step runs
+    whole); the persistent loop takes QIE meshes only."""
     sc = dataclasses.replace(scenes.cantilever_160(), integrator=fem_lib.FEM_INTEGRATOR_FIE_DX)
+    bt = fem_lib.Batch([sc], precision=fem_lib.FEM_PRECISION_FP64)
     with pytest.raises(fem_lib.FemError) as e:
-        fem_lib.Batch([sc], precision=fem_lib.FEM_PRECISION_FP64)
+        bt.set_slice(10)
+    assert e.value.code == fem_lib.FEM_E_ARG
+    with pytest.raises(fem_lib.FemError) as e:
+        fem_lib.Batch([sc], precision=fem_lib.FEM_PRECISION_MIXED, persistent_loop=1)
     assert e.value.code == fem_lib.FEM_E_ARG
