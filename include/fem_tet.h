@@ -57,10 +57,12 @@ enum fem_integrator {
     /* Step_FullyImplicitEuler_dx(dt) (LeafDSH_Solid3D_FEM.cpp:1357-1552):
      * Newton on Delta x = x^{n+1} - x^n, the rotations and the elastic force
      * re-evaluated at every Newton iterate, up to nr_max_iter iterations,
-     * stopping when |b_k| < nr_abs_epsilon. FP64 solid only. */
+     * stopping when |b_k| < nr_abs_epsilon. On the solid and in batches of
+     * either precision (a device-side Newton loop, each solid leaving on its
+     * own test); not in servers. */
     FEM_INTEGRATOR_FIE_DX = 1,
     /* Step_FullyImplicitEuler_dx(0): the same Newton loop without inertia
-     * (quasi-static equilibrium; velocities become zero). FP64 solid only. */
+     * (quasi-static equilibrium; velocities become zero). As FIE_DX. */
     FEM_INTEGRATOR_FIE_DX_QUASISTATIC = 2
 };
 
@@ -73,7 +75,9 @@ enum fem_ls_solver {
     FEM_LS_CG = 0,
     /* ns::ILSS_MINRES (ILSS_MINRES.h:51-168): Paige-Saunders MINRES without
      * a preconditioner; |r| carried by the Givens sines, relative test
-     * |r|^2 <= rel^2 |b|^2. FP64 solid only. */
+     * |r|^2 <= rel^2 |b|^2. On the solid, in batches and servers (mixed
+     * precision: FP32 Lanczos vectors; when the estimate passes, the FP64
+     * residual of the iterate decides, restarting MINRES from it if needed). */
     FEM_LS_MINRES = 1
 };
 
@@ -446,11 +450,35 @@ int fem_batch_set_active(fem_batch b, const uint8_t* mask);
 /* Iteration budget of each following launch (0 = run every CG loop to its
  * end, the default). With a budget, a launch stops after that many CG
  * iterations; solids whose loop has not ended continue in a later launch
- * (mask value 2) with bit-identical results. */
+ * (mask value 2) with bit-identical results. FEM_E_ARG in a batch with an
+ * FIE solid (its Newton steps run whole). */
 int fem_batch_set_slice(fem_batch b, uint32_t max_iterations);
-/* Per solid (M bytes): 1 if its CG loop ended, and its step was integrated,
- * in the last launch; 2 if its loop is still running; 0 otherwise. As of
- * the last synchronize. */
+/* Replaces: the Leaf's NR_Init / NR_PreStep / NR_MidStep / NR_PostStep /
+ * NR_End (LeafDSH_Solid3D_FEM.cpp:2824-3039) on every solid of the batch
+ * that takes part (fem_batch_set_active value 1; all by default) at once,
+ * with the semantics of fem_solid_nr_* (the FIE system of step dt, 0 =
+ * quasi-static; x, v stay x^n, v^n until nr_end; each nr_prestep restarts
+ * the iterate at x^n), so a caller can add terms between the phases. Any
+ * integrator, solver, rotation and material the batch takes; either
+ * precision. nr_midstep returns once the solves have ended; nr_end
+ * recomputes the potential energy only, and fem_batch_get_stats then reports
+ * the solver iterations and iterate count since the last nr_prestep. Steps
+ * (fem_batch_step*) are refused between nr_init and nr_end, and the phases
+ * under an iteration budget. */
+int fem_batch_nr_init(fem_batch b, double dt);
+int fem_batch_nr_prestep(fem_batch b, double dt);
+int fem_batch_nr_midstep(fem_batch b, double dt);
+int fem_batch_nr_poststep(fem_batch b, double dt);
+int fem_batch_nr_end(fem_batch b, double dt);
+/* Replaces: SS_AggregateDSH_Basic::MultiDSH_Solid3D_Update
+ * (SS_AggregateDSH_Basic.cpp:229-300), its contact calls left out, over the
+ * solids of the batch, nsteps times: nr_init; the largest nr_max_iter of
+ * the solids times nr_prestep, nr_midstep, nr_poststep; nr_end (as
+ * fem_multi_step over fem_solid handles). */
+int fem_batch_multi_step(fem_batch b, double dt, uint32_t nsteps);
+/* Per solid (M bytes): 1 if its step ended (its CG loop, or FIE Newton
+ * loop, ended and the step was integrated) in the last launch; 2 if its loop
+ * is still running; 0 otherwise. As of the last synchronize. */
 int fem_batch_finished(fem_batch b, uint8_t* flags);
 /* Poll limit of the device-side waits of the mixed path's tile product for
  * each tile's copy into shared memory (every wait on the device is bounded;

@@ -556,6 +556,12 @@ _BATCH_SIGNATURES = {
     "fem_batch_get_state_all": (C.c_int, [C.c_void_p, _dp, _dp]),
     "fem_batch_step_host": (C.c_int, [C.c_void_p, _dp, _dp, C.c_uint32, _dp, _dp]),
     "fem_batch_set_slice": (C.c_int, [C.c_void_p, C.c_uint32]),
+    "fem_batch_nr_init": (C.c_int, [C.c_void_p, C.c_double]),
+    "fem_batch_nr_prestep": (C.c_int, [C.c_void_p, C.c_double]),
+    "fem_batch_nr_midstep": (C.c_int, [C.c_void_p, C.c_double]),
+    "fem_batch_nr_poststep": (C.c_int, [C.c_void_p, C.c_double]),
+    "fem_batch_nr_end": (C.c_int, [C.c_void_p, C.c_double]),
+    "fem_batch_multi_step": (C.c_int, [C.c_void_p, C.c_double, C.c_uint32]),
     "fem_batch_set_wait_limit": (C.c_int, [C.c_void_p, C.c_uint32]),
     "fem_batch_finished": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint8)]),
 }
@@ -723,6 +729,23 @@ class Batch:
         st = FemStepStats()
         check(self.lib.fem_batch_get_stats(self.h, i, C.byref(st)))
         return st.as_dict()
+
+    def nr_phase(self, phase, dt):
+        """One lock-step phase (init, prestep, midstep, poststep, end;
+        fem_batch_nr_*) on every solid taking part; init advances the
+        schedules of driven constraints as a step does."""
+        if phase == "init":
+            self._drive_targets()
+            self.step_index += 1
+        check(getattr(self.lib, "fem_batch_nr_" + phase)(self.h, float(dt)))
+
+    def multi_step(self, dt, nsteps=1):
+        """fem_batch_multi_step: the aggregate's lock-step over the batch's
+        solids, one step per call so that driven constraints advance."""
+        for _ in range(nsteps):
+            self._drive_targets()
+            check(self.lib.fem_batch_multi_step(self.h, float(dt), 1))
+            self.step_index += 1
 
     def stream(self):
         s = C.c_void_p()

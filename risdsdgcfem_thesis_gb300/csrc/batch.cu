@@ -155,7 +155,14 @@ struct fem_batch_s {
     bool any_lcm = false;
     bool any_minres = false;
     bool any_fie = false;
-    Dev<double> xn, vn;                  // FIE meshes: x^n, v^n of the step
+    Dev<double> xn, vn;                  // FIE meshes: x^n, v^n of the step (lock-step: x_k, v_k)
+    // the multi-solid Newton lock-step (fem_batch_nr_*)
+    std::vector<double> ray0, ray1;      // per mesh: the Rayleigh coefficients a0, a1
+    Dev<MeshConsts> mc_lock;             // the meshes' constants with the lock-step's factors
+    double lock_dt = -1.0;               // dt of mc_lock (-1: none yet)
+    bool lock = false;                   // views use mc_lock and the lock-step's branches
+    bool lock_open = false;              // between fem_batch_nr_init and fem_batch_nr_end
+    bool lock_stats = false;             // the last call was fem_batch_nr_end (its statistics)
     Dev<unsigned char> mr_p_s, mr_p0_s;  // MINRES meshes: directions p, p0 (S-typed)
     Dev<double> cpart_b;                 // MINRES meshes: per-chunk |b|^2 partials
     Dev<unsigned char> blob;
@@ -185,12 +192,13 @@ struct fem_batch_s {
         b.pipe_tile = opt.tile_elems <= (uint32_t)kPipeSmallTile ? kPipeSmallTile : kTileElems;
         b.fuse_alpha = opt.fuse_alpha ? 1u : 0u;
         b.has_lcm = any_lcm ? 1u : 0u;
+        b.lock = lock ? 1u : 0u;
         b.Ntot = (uint32_t)Ntot;
         b.Ttot = (uint32_t)Ttot;
         b.nslots = nslots;
         b.tiles = tiles.p;
         b.chunks = chunks.p;
-        b.mc = mc.p;
+        b.mc = lock ? mc_lock.p : mc.p;
         b.st = st.p;
         b.active = active.p;
         b.gtets = gtets.p;
@@ -254,7 +262,7 @@ struct fem_batch_s {
         knc_target.release(); r_s.release(); d_s.release(); q_s.release(); part_s.release(); ydelta_s.release(); counter.release();
         any_flag.release(); refresh_flag.release(); mcount.release(); err.release(); gbar.release(); blob.release();
         prev_x.release(); doc.release(); Fe.release();
-        mr_p_s.release(); mr_p0_s.release(); cpart_b.release(); xn.release(); vn.release();
+        mr_p_s.release(); mr_p0_s.release(); cpart_b.release(); xn.release(); vn.release(); mc_lock.release();
         blob_off16.release();
         act_tiles.release(); act_chunks.release(); act_count.release(); list_dirty.release(); slice.release();
         start_tiles.release(); start_chunks.release(); launch_tiles.release(); launch_chunks.release();
@@ -362,7 +370,7 @@ cudaError_t capture_conditional(cudaStream_t s, cudaGraphConditionalHandle h, cu
 // same kernels run with the loops on the host, in chunks, reading the
 // meshes' flags.
 template <typename S>
-int enqueue_step(fem_batch B, cudaStream_t s, bool capture)
+int enqueue_step(fem_batch B, cudaStream_t s, bool capture, int lock_phase = 0)
 {
     const BatchView<S> b = B->view<S>();
     const bool mixed = B->opt.precision == FEM_PRECISION_MIXED;
@@ -392,11 +400,13 @@ int enqueue_step(fem_batch B, cudaStream_t s, bool capture)
     ls.set_cond = capture ? 1 : 0;
     LoopSync lb = ls;
     lb.body_runs = B->any_flag.p;
-    // f_e, b, constraints, A y, r0 of the meshes in the start lists
+    // f_e, b, constraints, A y, r0 of the meshes in the start lists (the
+    // lock-step's at its iterate x_k)
+    const double* xk = B->lock ? B->xn.p : B->x.p;
     auto solve_start = [&](cudaStream_t ss) {
-        L::tile_force(b, B->x.p, B->part64.p, nullptr, ss);
+        L::tile_force(b, xk, B->part64.p, nullptr, ss);
         L::node_b(b, B->part64.p, B->v.p, B->x.p, B->bvec.p, B->y.p, ss);
-        L::knc(b, B->K, B->x.p, B->bvec.p, B->y.p, ss);
+        L::knc(b, B->K, xk, B->bvec.p, B->y.p, ss);
         L::tile_spmv_y64(b, B->y.p, B->part64.p, 0, nullptr, ss);
         L::node_residual(b, B->part64.p, B->bvec.p, B->y.p, r, d, B->cpart.p, ls, ss);
         if (B->any_minres) L::node_mr_finish(b, B->y.p, r, d, q, ls, ss);
@@ -487,11 +497,20 @@ int enqueue_step(fem_batch B, cudaStream_t s, bool capture)
     // the next Newton iteration's lists
     auto after_solve = [&](cudaStream_t as) {
         L::integrate(b, B->x.p, B->v.p, B->y.p, B->cpart.p, ls, as);
-        if (newton) {
-            L::begin_eval(b, B->x.p, 1, as);
+        if (newton || B->lock) {
+            L::begin_eval(b, xk, 1, as);
             L::newton_tail(b, ls, nw, as);
         }
     };
+    if (lock_phase == 1) {  // NR_MidStep: the solve at x_k
+        solve_start(s);
+        return host_cg();
+    }
+    if (lock_phase == 2) {  // NR_PostStep: the update and the re-evaluation at x_k
+        after_solve(s);
+        BCK(cudaGetLastError());
+        return FEM_OK;
+    }
     L::reset_counts(b, ls, if_start, nw, newton ? 1 : 0, s);
     bool any_start = B->mask_host.empty();
     for (uint8_t a : B->mask_host) any_start |= a == 1;
@@ -684,6 +703,8 @@ int fem_batch_finalize(fem_batch b)
     std::vector<TileMeta> tiles;
     std::vector<ChunkMeta> chunks;
     std::vector<MeshConsts> mcs(b->M);
+    b->ray0.clear();
+    b->ray1.clear();
     std::vector<int4> gtets;
     std::vector<double> vol, rest_all;
     std::vector<uchar4> lconn;
@@ -913,6 +934,8 @@ int fem_batch_finalize(fem_batch b)
             ray[0] = a0;
             ray[1] = a1;
         }
+        b->ray0.push_back(ray[0]);
+        b->ray1.push_back(ray[1]);
         c.dt = p.fixed_dt;
         c.inv_dt = 1.0 / p.fixed_dt;
         c.mass = 1.0 / inv_mass;
@@ -1544,6 +1567,8 @@ int fem_batch_set_wait_limit(fem_batch b, uint32_t polls)
 int fem_batch_step_async(fem_batch b, uint32_t nsteps)
 {
     if (int e = check_ready(b)) return e;
+    if (b->lock_open) return batch_fail(FEM_E_ARG, "a lock-step is open: fem_batch_nr_end first");
+    b->lock_stats = false;
     for (uint32_t i = 0; i < nsteps; i++) {
         if (b->exec && b->opt.use_graph && !b->opt.persistent_loop) {
             BCK(cudaGraphLaunch(b->exec, b->stream));
@@ -1553,6 +1578,205 @@ int fem_batch_step_async(fem_batch b, uint32_t nsteps)
                                                             : enqueue_step<float>(b, b->stream, false);
             if (rc) return rc;
         }
+    }
+    return FEM_OK;
+}
+
+}  // extern "C"
+
+// ---- the multi-solid Newton lock-step over the meshes of a batch ----
+
+namespace {
+
+int lock_check(fem_batch b, double dt, bool opened)
+{
+    if (int e = check_ready(b)) return e;
+    if (!(dt >= 0) || !std::isfinite(dt)) return batch_fail(FEM_E_ARG, "dt must be finite and >= 0");
+    if (b->slice_budget) return batch_fail(FEM_E_ARG, "the lock-step's solves run whole: no iteration budget");
+    if (opened && !b->lock_open) return batch_fail(FEM_E_ARG, "fem_batch_nr_init must come first");
+    return FEM_OK;
+}
+
+// The meshes' constants with the lock-step's factors for step dt (NR_MidStep,
+// LeafDSH_Solid3D_FEM.cpp:2960-2962: the FIE system, 1/h = 0 when dt = 0).
+int lock_consts(fem_batch b, double dt)
+{
+    if (b->lock_dt == dt && b->mc_lock.p) return FEM_OK;
+    std::vector<MeshConsts> mcs = b->mc_host;
+    for (uint32_t m = 0; m < b->M; m++) {
+        MeshConsts& c = mcs[m];
+        c.dt = dt;
+        c.inv_dt = dt == 0 ? 0.0 : 1.0 / dt;
+        c.factor_M = c.inv_dt * c.inv_dt + c.inv_dt * b->ray0[m];
+        c.factor_K = 1.0 + c.inv_dt * b->ray1[m];
+        c.fK_f = (float)c.factor_K;
+        c.mfm_f = (float)(c.mass * c.factor_M);
+    }
+    if (!b->mc_lock.p) BCK(b->mc_lock.alloc(b->M));
+    BCK(b->mc_lock.upload(mcs, b->stream));
+    BCK(cudaStreamSynchronize(b->stream));
+    b->lock_dt = dt;
+    return FEM_OK;
+}
+
+// The mixed path's tile blobs carry FP32 copies of the factors: the
+// lock-step's while it is open, the step's otherwise.
+void blob_factors(fem_batch b, bool lock)
+{
+    if (b->opt.precision != FEM_PRECISION_MIXED) return;
+    b->lock = lock;
+    launch_blob_factors(b->view<float>(), b->stream);
+    b->lock = false;
+}
+
+template <typename S>
+int lock_run(fem_batch b, int phase)
+{
+    b->lock = true;
+    const int rc = enqueue_step<S>(b, b->stream, false, phase);
+    b->lock = false;
+    return rc;
+}
+
+int lock_solve_phase(fem_batch b, int phase)
+{
+    return b->opt.precision == FEM_PRECISION_FP64 ? lock_run<double>(b, phase) : lock_run<float>(b, phase);
+}
+
+}  // namespace
+
+extern "C" {
+
+int fem_batch_nr_init(fem_batch b, double dt)
+{
+    if (int e = lock_check(b, dt, false)) return e;
+    if (int e = lock_consts(b, dt)) return e;
+    const size_t n3 = 3 * (size_t)b->Ntot;
+    if (!b->xn.p) {
+        BCK(b->xn.alloc(n3));
+        BCK(b->vn.alloc(n3));
+    }
+    cudaStream_t s = b->stream;
+    blob_factors(b, true);
+    b->lock_open = true;
+    b->lock_stats = false;
+    b->lock = true;
+    // the per-mesh counts and start lists of the meshes taking part; then
+    // UpdateKNC (a no-op in the default kinematic mode), BeginEvaluation(
+    // m_vecPos0, x), m_vecPos0 = x (LeafDSH_Solid3D_FEM.cpp:2824-2846)
+    LoopSync ls{};
+    ls.mcount = b->mcount.p;
+    ls.gcount = b->counter.p;
+    ls.err = b->err.p;
+    if (b->opt.precision == FEM_PRECISION_FP64) {
+        BatchLaunch<double>::reset_counts(b->view<double>(), ls, 0, 0, 0, s);
+        BatchLaunch<double>::begin_eval(b->view<double>(), b->x.p, 0, s);
+    } else {
+        BatchLaunch<float>::reset_counts(b->view<float>(), ls, 0, 0, 0, s);
+        BatchLaunch<float>::begin_eval(b->view<float>(), b->x.p, 0, s);
+    }
+    b->lock = false;
+    if (b->any_dapd) BCK(cudaMemcpyAsync(b->prev_x.p, b->x.p, sizeof(double) * n3, cudaMemcpyDeviceToDevice, s));
+    // the iterate starts at x^n (nr_end right after nr_init leaves x, v as they are)
+    BCK(cudaMemcpyAsync(b->xn.p, b->x.p, sizeof(double) * n3, cudaMemcpyDeviceToDevice, s));
+    BCK(cudaMemcpyAsync(b->vn.p, b->v.p, sizeof(double) * n3, cudaMemcpyDeviceToDevice, s));
+    BCK(cudaGetLastError());
+    return FEM_OK;
+}
+
+int fem_batch_nr_prestep(fem_batch b, double dt)
+{
+    if (int e = lock_check(b, dt, true)) return e;
+    if (int e = lock_consts(b, dt)) return e;
+    blob_factors(b, true);
+    const size_t bytes = sizeof(double) * 3 * (size_t)b->Ntot;
+    cudaStream_t s = b->stream;
+    // x_k = x^n, v_k = v^n; the iterate and solver counts restart
+    // (LeafDSH_Solid3D_FEM.cpp:2869-2929)
+    BCK(cudaMemcpyAsync(b->xn.p, b->x.p, bytes, cudaMemcpyDeviceToDevice, s));
+    BCK(cudaMemcpyAsync(b->vn.p, b->v.p, bytes, cudaMemcpyDeviceToDevice, s));
+    b->lock = true;
+    if (b->opt.precision == FEM_PRECISION_FP64)
+        BatchLaunch<double>::lock_phase(b->view<double>(), 0, s);
+    else
+        BatchLaunch<float>::lock_phase(b->view<float>(), 0, s);
+    b->lock = false;
+    BCK(cudaGetLastError());
+    return FEM_OK;
+}
+
+int fem_batch_nr_midstep(fem_batch b, double dt)
+{
+    if (int e = lock_check(b, dt, true)) return e;
+    if (int e = lock_consts(b, dt)) return e;
+    blob_factors(b, true);
+    if (int e = lock_solve_phase(b, 1)) return e;
+    BCK(cudaMemcpyAsync(b->st_host, b->st.p, sizeof(StepScalars) * b->M, cudaMemcpyDeviceToHost, b->stream));
+    BCK(cudaStreamSynchronize(b->stream));
+    for (uint32_t m = 0; m < b->M; m++)
+        if (b->st_host[m].status == FEM_E_NAN) return batch_fail(FEM_E_NAN, "NaN or Inf in the residual of mesh %u", m);
+    return FEM_OK;
+}
+
+int fem_batch_nr_poststep(fem_batch b, double dt)
+{
+    if (int e = lock_check(b, dt, true)) return e;
+    if (int e = lock_consts(b, dt)) return e;
+    return lock_solve_phase(b, 2);
+}
+
+int fem_batch_nr_end(fem_batch b, double dt)
+{
+    if (int e = lock_check(b, dt, true)) return e;
+    if (int e = lock_consts(b, dt)) return e;
+    const size_t bytes = sizeof(double) * 3 * (size_t)b->Ntot;
+    cudaStream_t s = b->stream;
+    // x = x_k, v = v_k; RecomputeEnergy's potential term (NR_End evaluates
+    // no V: the elastic energy keeps its value; LeafDSH_Solid3D_FEM.cpp:
+    // 2847-2868, 1554-1584)
+    BCK(cudaMemcpyAsync(b->x.p, b->xn.p, bytes, cudaMemcpyDeviceToDevice, s));
+    BCK(cudaMemcpyAsync(b->v.p, b->vn.p, bytes, cudaMemcpyDeviceToDevice, s));
+    bool energy = false;
+    for (auto& m : b->meshes) energy |= m.p.compute_energy != 0;
+    b->lock = true;
+    if (b->opt.precision == FEM_PRECISION_FP64) {
+        BatchLaunch<double>::lock_phase(b->view<double>(), 1, s);
+        if (energy) {
+            BatchLaunch<double>::tile_potential(b->view<double>(), b->x.p, b->tpart.p, s);
+            BatchLaunch<double>::fin_energy(b->view<double>(), FIN_ENERGY_P, b->tpart.p, s);
+        }
+    } else {
+        BatchLaunch<float>::lock_phase(b->view<float>(), 1, s);
+        if (energy) {
+            BatchLaunch<float>::tile_potential(b->view<float>(), b->x.p, b->tpart.p, s);
+            BatchLaunch<float>::fin_energy(b->view<float>(), FIN_ENERGY_P, b->tpart.p, s);
+        }
+    }
+    b->lock = false;
+    blob_factors(b, false);
+    b->lock_open = false;
+    b->lock_stats = true;
+    BCK(cudaMemcpyAsync(b->st_host, b->st.p, sizeof(StepScalars) * b->M, cudaMemcpyDeviceToHost, s));
+    BCK(cudaStreamSynchronize(s));
+    return FEM_OK;
+}
+
+int fem_batch_multi_step(fem_batch b, double dt, uint32_t nsteps)
+{
+    if (int e = lock_check(b, dt, false)) return e;
+    uint32_t max_nr_iter = 0;
+    for (uint32_t m = 0; m < b->M; m++)
+        if (b->mask_host.empty() || b->mask_host[m] == 1)
+            max_nr_iter = std::max(max_nr_iter, b->meshes[m].p.nr_max_iter);
+    for (uint32_t step = 0; step < nsteps; step++) {
+        if (int e = fem_batch_nr_init(b, dt)) return e;
+        uint32_t nr_iter = 0;
+        do {
+            if (int e = fem_batch_nr_prestep(b, dt)) return e;
+            if (int e = fem_batch_nr_midstep(b, dt)) return e;
+            if (int e = fem_batch_nr_poststep(b, dt)) return e;
+        } while (++nr_iter < max_nr_iter);
+        if (int e = fem_batch_nr_end(b, dt)) return e;
     }
     return FEM_OK;
 }
@@ -1615,7 +1839,12 @@ int fem_batch_get_stats(fem_batch b, uint32_t mesh, fem_step_stats* out)
     out->resolved_isotropic = h.res_isotropic;
     out->resolved_tie = h.res_tie;
     out->resolved_check = h.res_check;
-    if (b->mc_host[mesh].integrator != kMeshQie) {
+    if (b->lock_stats) {
+        // the Leaf's m_Stats after NR_End: solver iterations since the last
+        // NR_PreStep, m_NR_nr_k (reset by every NR_PreStep)
+        out->cg_iterations = h.fie_cg;
+        out->nr_iterations = h.nr_k;
+    } else if (b->mc_host[mesh].integrator != kMeshQie) {
         // the Leaf's FIE stats (m_SolverLS_NumIter summed over the Newton
         // iterations, m_SolverNR_NumIter, m_SolverNR_AbsPrec)
         out->cg_iterations = h.fie_cg;

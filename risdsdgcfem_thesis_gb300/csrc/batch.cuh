@@ -163,11 +163,13 @@ struct BatchView {
     S* mr_p0;                      // [3 Ntot] MINRES: the previous direction p0
     S* mr_v1;                      // [3 Ntot] MINRES: the Lanczos vector v1 (the q buffer)
     double* cpart_b;               // [nchunks] MINRES, FIE: per-chunk partials of |b|^2 at the start of a solve
-    double* xn;                    // [3 Ntot] FIE: x^n, the positions at the start of the step; null without FIE
-    double* vn;                    // [3 Ntot] FIE: v^n
+    double* xn;                    // [3 Ntot] FIE: x^n, the positions at the start of the step (lock-step:
+                                   // the iterate x_k); null without FIE or a lock-step
+    double* vn;                    // [3 Ntot] FIE: v^n (lock-step: v_k)
     uint32_t pipe_tile;            // mixed: threads per block of the tile product (kPipeSmallTile or kTileElems)
     uint32_t fuse_alpha;           // mixed: the node pass forms alpha (no separate alpha kernel)
     uint32_t has_lcm;              // some mesh takes the C_LCM product
+    uint32_t lock;                 // the multi-solid Newton lock-step's phases (x_k, v_k in xn, vn; x, v hold x^n, v^n)
     const TileMeta* tiles;
     const ChunkMeta* chunks;
     const MeshConsts* mc;

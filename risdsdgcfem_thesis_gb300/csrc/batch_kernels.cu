@@ -402,6 +402,26 @@ __global__ void k_node_b(BatchView<S> b, const double* __restrict__ part64, cons
         if (!mesh_starts(b, ch.mesh)) continue;
         const MeshConsts& c = b.mc[ch.mesh];
         const bool opening = c.integrator == kMeshQie || b.st[ch.mesh].nr_k == 0;
+        if (b.lock) {
+            // NR_MidStep (LeafDSH_Solid3D_FEM.cpp:2930-2990): the FIE
+            // right-hand side at the iterate x_k with x^n = x, v^n = v, warm
+            // start h v^n on the phase's first solve since NR_PreStep
+            const double im = c.inv_dt * c.mass;
+            const bool warm = b.st[ch.mesh].nr_k == 0;
+            for (size_t n = ch.n0 + threadIdx.x; n < ch.n1; n += blockDim.x) {
+                double f[3];
+                sum_parts(b, part64, n, f[0], f[1], f[2]);
+                const size_t i = 3 * n;
+#pragma unroll
+                for (int a = 0; a < 3; a++) {
+                    const double bf = c.mass * c.gravity[a] - f[a];
+                    bv[i + a] = bf + im * (v[i + a] - c.inv_dt * (b.xn[i + a] - x[i + a]));
+                    y[i + a] = warm ? c.dt * v[i + a] : 0.0;
+                    if (b.ydelta) b.ydelta[i + a] = 0;
+                }
+            }
+            continue;
+        }
         if (c.integrator != kMeshQie) {
             const double im = c.inv_dt * c.mass;
             for (size_t n = ch.n0 + threadIdx.x; n < ch.n1; n += blockDim.x) {
@@ -462,7 +482,7 @@ __global__ void k_knc(BatchView<S> b, uint32_t K, const double* __restrict__ x, 
         const MeshConsts& c = b.mc[m];
         const size_t n = bounds_idx(b.knc_node[k], b.Ntot, kSiteKncNode);
         const double* tg = b.knc_target + 3 * (size_t)k;
-        if (c.integrator != kMeshQie) {
+        if (c.integrator != kMeshQie || b.lock) {
             // FIE: the constraint rows as Delta x, b = y = target - x_k
             // (LeafDSH_Solid3D_FEM.cpp:1441-1465)
 #pragma unroll
@@ -582,7 +602,7 @@ __global__ void k_node_residual(BatchView<S> b, const double* __restrict__ part6
         const MeshConsts& c = b.mc[ch.mesh];
         const double mfm = c.mass * c.factor_M;
         const bool minres = c.solver == kMeshSolverMinres;
-        const bool fie = c.integrator != kMeshQie;
+        const bool fie = c.integrator != kMeshQie && !b.lock;  // the lock-step's solves have no |b_k| test
         const bool need_b = minres || fie;
         double acc = 0.0, acc_b = 0.0;
         for (size_t n = ch.n0 + threadIdx.x; n < ch.n1; n += blockDim.x) {
@@ -614,7 +634,8 @@ __global__ void k_node_residual(BatchView<S> b, const double* __restrict__ part6
             bool newton_ends = false;
             if (threadIdx.x == 0) {
                 StepScalars& s = b.st[ch.mesh];
-                if (c.integrator == kMeshQie) {
+                if (b.lock) {
+                } else if (c.integrator == kMeshQie) {
                     s.nr_go = 0;
                 } else {
                     // the Newton test on |b_k| (LeafDSH_Solid3D_FEM.cpp:1466-1480):
@@ -971,6 +992,26 @@ __global__ void k_integrate(BatchView<S> b, double* __restrict__ x, double* __re
         const ChunkMeta ch = b.chunks[ci];
         if (!b.st[ch.mesh].finished) continue;
         const MeshConsts& c = b.mc[ch.mesh];
+        if (b.lock) {
+            // NR_PostStep (LeafDSH_Solid3D_FEM.cpp:2991-3010): x_k += y,
+            // v_k = (x_k - x^n)/h with x^n = x; the phase's counts
+            for (size_t n = ch.n0 + threadIdx.x; n < ch.n1; n += blockDim.x) {
+#pragma unroll
+                for (int a = 0; a < 3; a++) {
+                    const size_t i = 3 * n + a;
+                    const double xi = b.xn[i] + y_full(b, y, i);
+                    b.xn[i] = xi;
+                    b.vn[i] = c.inv_dt * (xi - x[i]);
+                }
+            }
+            if (arrive_last(ls.mcount + ch.mesh, c.nchunks) && threadIdx.x == 0) {
+                StepScalars& s = b.st[ch.mesh];
+                s.nr_k += 1;
+                s.fie_cg += s.k;
+                s.inverted = 0;  // counted again by the re-evaluation at x_k
+            }
+            continue;
+        }
         if (c.integrator == kMeshQie) {
             const double dt = c.dt;
             for (size_t n = ch.n0 + threadIdx.x; n < ch.n1; n += blockDim.x) {
@@ -1013,6 +1054,45 @@ __global__ void k_integrate(BatchView<S> b, double* __restrict__ x, double* __re
             }
         }
     }
+}
+
+// The lock-step's per-mesh bookkeeping, one block: phase 0 (NR_PreStep)
+// restarts the iterate count and the solver-iteration count of every mesh
+// taking part; phase 1 (NR_End) marks their steps done.
+template <typename S>
+__global__ void k_lock_phase(BatchView<S> b, int phase)
+{
+    for (uint32_t m = threadIdx.x; m < b.M; m += blockDim.x) {
+        StepScalars& s = b.st[m];
+        if (b.active[m] != 1) continue;
+        if (phase == 0) {
+            s.nr_k = 0;
+            s.fie_cg = 0;
+            s.nr_go = 1;
+            s.finished = 0;
+        } else {
+            s.step_done = 1;
+        }
+    }
+}
+
+// The mixed path's per-tile copies of the system factors (factor_K and
+// m factor_M in FP32, in each tile blob's header) from the meshes' constants
+// in the view: the lock-step's own, then the step's again.
+__global__ void k_blob_factors(BatchView<float> b)
+{
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < b.ntiles; t += gridDim.x * blockDim.x) {
+        const TileMeta tm = b.tiles[t];
+        float* fac = reinterpret_cast<float*>(b.blob + 16ull * b.blob_off16[t] + blob_hdr_off(tm.ne, tm.nn) + 4u);
+        fac[0] = b.mc[tm.mesh].fK_f;
+        fac[1] = b.mc[tm.mesh].mfm_f;
+    }
+}
+
+void launch_blob_factors(const BatchView<float>& b, cudaStream_t s)
+{
+    k_blob_factors<<<(b.ntiles + 255) / 256 < 1024 ? (b.ntiles + 255) / 256 : 1024, 256, 0, s>>>(b);
+    launch_counter()++;
 }
 
 // One block, last kernel of a Newton iteration: the start lists of the next
@@ -1212,6 +1292,13 @@ void BatchLaunch<S>::integrate(const BatchView<S>& b, double* x, double* v, cons
                                const LoopSync& ls, cudaStream_t s)
 {
     k_integrate<S><<<grid_chunks(b.nchunks), kNodeThreads, 0, s>>>(b, x, v, y, cpart, ls);
+    launch_counter()++;
+}
+
+template <typename S>
+void BatchLaunch<S>::lock_phase(const BatchView<S>& b, int phase, cudaStream_t s)
+{
+    k_lock_phase<S><<<1, 256, 0, s>>>(b, phase);
     launch_counter()++;
 }
 

@@ -36,6 +36,9 @@ void launch_node_update_fused(const BatchView<float>& b, const float* part, cons
                               const double* part64, const double* bv, double* y, float* r, float* d,
                               float2* cshare, const LoopSync& ls, cudaStream_t s);
 
+// Mixed path: rewrite each tile blob's FP32 system factors from b.mc.
+void launch_blob_factors(const BatchView<float>& b, cudaStream_t s);
+
 // Mixed path, the whole CG loop of a launch in one persistent cooperative
 // kernel (tile_pipe.cu): per iteration the tile product, the refresh product
 // when a mesh refreshes, the node pass with the fused alpha and the per-mesh
@@ -96,6 +99,8 @@ struct BatchLaunch {
                           const LoopSync& ls, cudaStream_t s);
     static void newton_tail(const BatchView<S>& b, const LoopSync& ls, cudaGraphConditionalHandle newton,
                             cudaStream_t s);
+    // the lock-step's bookkeeping: 0 = NR_PreStep's counts, 1 = NR_End's
+    static void lock_phase(const BatchView<S>& b, int phase, cudaStream_t s);
     static void fin_energy(const BatchView<S>& b, int kind, const double* tpart, cudaStream_t s);
 };
 

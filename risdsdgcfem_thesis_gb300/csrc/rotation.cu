@@ -175,7 +175,8 @@ __global__ void __launch_bounds__(256, 3) k_begin_eval_batch(BatchView<S> b, con
         // newton: the FIE meshes whose solve has just updated x_k
         // (BeginEvaluation(x^n, x_k), LeafDSH_Solid3D_FEM.cpp:1529; their
         // DAPD previous positions are x^n); otherwise the start section's
-        if (newton ? (b.mc[tm.mesh].integrator == kMeshQie || !b.st[tm.mesh].finished) : !mesh_starts(b, tm.mesh))
+        if (newton ? ((!b.lock && b.mc[tm.mesh].integrator == kMeshQie) || !b.st[tm.mesh].finished)
+                   : !mesh_starts(b, tm.mesh))
             continue;
         if (threadIdx.x == 0) { s_inv = 0; s_res = 0; s_cause[0] = s_cause[1] = s_cause[2] = s_cause[3] = 0; }
         __syncthreads();
