@@ -441,6 +441,53 @@ def rotation_leg(n=60, reps=5):
     return out
 
 
+def batch_variants_leg(meshes=128, steps=3, seed=7):
+    """The reference's alternatives on the batched mixed path, one batch of
+    `meshes` meshes of the batched workload's generator per variant (every
+    mesh with the variant): the step (QIE, CG, C_WRP, MSVD), MINRES, C_LCM,
+    DAPD, FIE (Newton on Delta x, nr_max_iter 3) and the multi-solid Newton
+    lock-step (fem_batch_multi_step, 3 NR iterations). Device time per step
+    (CUDA events; the lock-step's phases read the loop flags on the host, so
+    it is timed by the wall clock), after one warm-up step."""
+    import dataclasses
+    import torch
+    from risdsdgcfem_thesis_gb300 import capi, scenes
+    base = scenes.batch_scenes(meshes, seed=seed)
+    variants = (("step", {}), ("minres", {"ls_solver": capi.FEM_LS_MINRES}),
+                ("c_lcm", {"material": capi.FEM_MATERIAL_C_LCM}), ("dapd", {"rotation": capi.FEM_ROTATION_DAPD}),
+                ("fie", {"integrator": capi.FEM_INTEGRATOR_FIE_DX, "nr_max_iter": 3}),
+                ("lock_step", {"nr_max_iter": 3}))
+    T = sum(sc.num_tets for sc in base)
+    out = {"workload": f"{meshes} meshes of the batched workload's generator (seed {seed}), {T} tets, mixed",
+           "steps": steps}
+    for name, kw in variants:
+        scs = [dataclasses.replace(sc, **kw) for sc in base]
+        bt = capi.Batch(scs, precision=capi.FEM_PRECISION_MIXED, compute_energy=False)
+        if name == "lock_step":
+            dt = scs[0].dt
+            bt.multi_step(dt, 1)
+            torch.cuda.synchronize()
+            it0 = [bt.stats(i)["total_cg_iterations"] for i in range(len(scs))]
+            t0 = time.perf_counter()
+            bt.multi_step(dt, steps)
+            ms = [1e3 * (time.perf_counter() - t0) / steps] * steps
+            tet_iters = float(sum(sc.num_tets * (bt.stats(i)["total_cg_iterations"] - it0[i])
+                                  for i, sc in enumerate(scs)))
+        else:
+            bt.step(1)
+            step_ms, iters = time_batch(bt, steps, bt.stream())
+            ms = step_ms
+            tet_iters = float(sum(sc.num_tets * it for sc, it in zip(scs, iters)))
+        tot = sum(ms)
+        out[name] = {"ms_per_step": tot / steps, "tet_cg_iter_per_s": tet_iters / (tot * 1e-3),
+                     "status": max(bt.stats(i)["status"] for i in range(len(scs)))}
+        if name in ("fie", "lock_step"):
+            out[name]["nr_iterations_mean"] = float(np.mean([bt.stats(i)["nr_iterations"] for i in range(len(scs))]))
+        bt.close()
+        torch.cuda.synchronize()
+    return out
+
+
 def run_ours(args):
     import torch
     from risdsdgcfem_thesis_gb300 import capi
@@ -531,6 +578,7 @@ def run_ours(args):
     rotations = None
     minres = None
     lcm = None
+    variants = None
     cpu = None
     served = None
     compression = None
@@ -554,6 +602,7 @@ def run_ours(args):
             rotations = rotation_leg()
             minres = plain_fp64_comparator(3, ls_solver=1)
             lcm = plain_fp64_comparator(3, material=1)
+            variants = batch_variants_leg()
         if not args.no_cpu:
             sample = cpu_sample_set(scs, 1_500_000)
             threads = (os.cpu_count() or 1) if len(sample) > 1 else 1
@@ -614,6 +663,7 @@ def run_ours(args):
             "rotations_fp64_gpu": rotations,
             "minres_fp64_gpu": minres,
             "lcm_fp64_gpu": lcm,
+            "batch_variants_mixed": variants,
             "cpu_baseline": cpu,
             "served": served,
             "compression": compression,
