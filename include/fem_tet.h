@@ -93,21 +93,24 @@ enum fem_material {
      * V (mu |S - I|^2 + lambda/2 tr(S - I)^2) (TetrahedronElementSet3.cpp:
      * 1154-1178, 1838-1873, 1489-1507). mu and lambda come from the scalar
      * young_modulus and poisson_ratio, as the reference's element set takes
-     * them from its Params even where per-element E, nu re-bake K0. FP64
-     * solid only. */
+     * them from its Params even where per-element E, nu re-bake K0. On the
+     * solid, in batches and servers of either precision. */
     FEM_MATERIAL_C_LCM = 1,
     /* C_LCMH: C_LCM's force and energy, and a differential that blends LCM
      * and warped stiffness per element by w = Clamp01(tr|S - I| / (3 k)),
      * k = ecie_k_factor: dP = 2 mu (w dF + (1 - w) R sym(R^T dF)) +
      * lambda tr(R^T dF) R for k > 0.1, C_LCM's dP otherwise
-     * (TetrahedronElementSet3.cpp:1875-1930). FP64 solid only. */
+     * (TetrahedronElementSet3.cpp:1875-1930). On the solid, in batches and
+     * servers of either precision (mixed: w of each element's last
+     * evaluation, FP32 products). */
     FEM_MATERIAL_C_LCMH = 2,
     /* C_CCM: P = R (2 mu (S - I) + lambda (det S - 1) adj(S)^T) and the
      * reference's differential, which builds dDs from nodes (0, 1, 2, 2)
      * (TetrahedronElementSet3.cpp:1180-1206, 1932-1970; :1948): its A is not
      * symmetric positive definite, so CG diverges and the state runs to
      * Inf/NaN within steps, in the reference as here (FEM_E_NAN). Energy 0
-     * (its body is compiled out of the reference). FP64 solid only. */
+     * (its body is compiled out of the reference). On the solid and in FP64
+     * batches and servers. */
     FEM_MATERIAL_C_CCM = 3
 };
 

@@ -115,7 +115,8 @@ static_assert(kMeshSolverCg == FEM_LS_CG && kMeshSolverMinres == FEM_LS_MINRES, 
 static_assert(kMeshQie == FEM_INTEGRATOR_QIE_V && kMeshFie == FEM_INTEGRATOR_FIE_DX &&
                   kMeshFieQuasi == FEM_INTEGRATOR_FIE_DX_QUASISTATIC,
               "integrator ids follow fem_tet.h");
-static_assert(kTileMaterialWrp == FEM_MATERIAL_C_WRP && kTileMaterialLcm == FEM_MATERIAL_C_LCM,
+static_assert(kTileMaterialWrp == FEM_MATERIAL_C_WRP && kTileMaterialLcm == FEM_MATERIAL_C_LCM &&
+                  kTileMaterialLcmh == FEM_MATERIAL_C_LCMH && kTileMaterialCcm == FEM_MATERIAL_C_CCM,
               "per-tile material values are enum fem_material's");
 
 struct fem_batch_s {
@@ -152,7 +153,9 @@ struct fem_batch_s {
     Dev<uchar2> doc;     // DAPD meshes: direction of collapse per element (batch element order)
     Dev<double> Fe;      // C_LCM meshes: F of the last BeginEvaluation (SoA, batch element order)
     bool any_dapd = false;
-    bool any_lcm = false;
+    bool any_lcm = false;   // some mesh has a P-K material (C_LCM, C_LCMH, C_CCM)
+    bool any_lcmh = false;
+    Dev<float> lcmh_w;      // mixed C_LCMH meshes: the blend weight per element
     bool any_minres = false;
     bool any_fie = false;
     Dev<double> xn, vn;                  // FIE meshes: x^n, v^n of the step (lock-step: x_k, v_k)
@@ -223,6 +226,7 @@ struct fem_batch_s {
         b.prev_x = prev_x.p;
         b.doc = doc.p;
         b.Fe = Fe.p;
+        b.lcmh_w = lcmh_w.p;
         b.mr_p = reinterpret_cast<S*>(mr_p_s.p);
         b.mr_p0 = reinterpret_cast<S*>(mr_p0_s.p);
         b.mr_v1 = reinterpret_cast<S*>(q_s.p);
@@ -261,7 +265,7 @@ struct fem_batch_s {
         x.release(); v.release(); bvec.release(); y.release(); part64.release(); cpart.release(); tpart.release();
         knc_target.release(); r_s.release(); d_s.release(); q_s.release(); part_s.release(); ydelta_s.release(); counter.release();
         any_flag.release(); refresh_flag.release(); mcount.release(); err.release(); gbar.release(); blob.release();
-        prev_x.release(); doc.release(); Fe.release();
+        prev_x.release(); doc.release(); Fe.release(); lcmh_w.release();
         mr_p_s.release(); mr_p0_s.release(); cpart_b.release(); xn.release(); vn.release(); mc_lock.release();
         blob_off16.release();
         act_tiles.release(); act_chunks.release(); act_count.release(); list_dirty.release(); slice.release();
@@ -653,10 +657,13 @@ int fem_batch_add_mesh(fem_batch b, const double* rest, uint32_t N, const uint32
         return batch_fail(FEM_E_ARG, "unknown ls_solver %u", p->ls_solver);
     if (p->ls_solver == FEM_LS_MINRES && b->opt.persistent_loop)
         return batch_fail(FEM_E_ARG, "the persistent loop takes CG meshes only");
-    if (p->material != FEM_MATERIAL_C_WRP && p->material != FEM_MATERIAL_C_LCM)
-        return batch_fail(FEM_E_ARG, "material %u: batches take C_WRP and C_LCM; C_LCMH and C_CCM run on fem_solid",
-                          p->material);
-    if (p->material == FEM_MATERIAL_C_LCM && b->opt.persistent_loop)
+    if (p->material > FEM_MATERIAL_C_CCM) return batch_fail(FEM_E_ARG, "unknown material %u", p->material);
+    if (p->material == FEM_MATERIAL_C_CCM && b->opt.precision == FEM_PRECISION_MIXED)
+        return batch_fail(FEM_E_ARG, "C_CCM runs in FP64 batches (its differential is not symmetric: CG diverges "
+                                     "on it, in the reference too)");
+    if (p->material == FEM_MATERIAL_C_LCMH && !std::isfinite(p->ecie_k_factor))
+        return batch_fail(FEM_E_ARG, "ecie_k_factor must be finite");
+    if (p->material != FEM_MATERIAL_C_WRP && b->opt.persistent_loop)
         return batch_fail(FEM_E_ARG, "the persistent loop takes C_WRP meshes only");
     for (size_t i = 0; i < 4 * (size_t)T; i++)
         if (tets[i] >= N) return batch_fail(FEM_E_INDEX, "tet %zu names node %u >= N=%u", i / 4, tets[i], N);
@@ -782,7 +789,7 @@ int fem_batch_finalize(fem_batch b)
             const double V = vol_orig[e];
             // C_LCM takes the set's scalar E and nu (per-element values would
             // only re-bake K0, which it does not use)
-            const bool scalar_mat = p.material == FEM_MATERIAL_C_LCM;
+            const bool scalar_mat = p.material != FEM_MATERIAL_C_WRP;
             const double E = (hm.E.empty() || scalar_mat) ? p.young_modulus : hm.E[e];
             const double nu = (hm.nu.empty() || scalar_mat) ? p.poisson_ratio : hm.nu[e];
             const double a = E / ((1.0 + nu) * (1.0 - 2.0 * nu));
@@ -865,7 +872,7 @@ int fem_batch_finalize(fem_batch b)
                     lc.w = remap[lc.w];
                 }
                 tm.nown = (uint16_t)owned.size();
-                tm.material = hm.p.material == FEM_MATERIAL_C_LCM ? kTileMaterialLcm : kTileMaterialWrp;
+                tm.material = (uint16_t)hm.p.material;
                 tm.own0 = owned.empty() ? 0u : (uint32_t)(node0 + intern[owned[0]]);
                 tm.ov0 = (uint32_t)ov_node.size();
                 for (uint32_t u : shared) ov_node.push_back((uint32_t)(node0 + intern[u]));
@@ -963,11 +970,13 @@ int fem_batch_finalize(fem_batch b)
         c.rot_check = (float)p.rotation_check;
         c.rot_fp32 = p.rotation_fp32 ? 1u : 0u;
         c.rotation = p.rotation;
-        c.material = p.material == FEM_MATERIAL_C_LCM ? kTileMaterialLcm : kTileMaterialWrp;
+        c.material = p.material;
+        c.ecie_k = (double)(float)p.ecie_k_factor;  // float32 in the reference's Params
         // the element set's Lame pair (from its Params, TetrahedronElementSet3.cpp:143-148)
         c.lame_mu = 0.5 * p.young_modulus / (1 + p.poisson_ratio);
         c.lame_lambda = p.young_modulus * p.poisson_ratio / ((1.0 + p.poisson_ratio) * (1.0 - 2.0 * p.poisson_ratio));
-        if (c.material == kTileMaterialLcm) b->any_lcm = true;
+        if (c.material != kTileMaterialWrp) b->any_lcm = true;
+        if (c.material == kTileMaterialLcmh) b->any_lcmh = true;
         // the reference's DAPD factors are float (ms::fem::Params)
         c.dapd_thr = p.dapd_threshold_det_F;
         c.dapd_fL = (double)(float)p.dapd_l_factor;
@@ -1209,6 +1218,10 @@ int fem_batch_finalize(fem_batch b)
         BCKC(b->Fe.alloc(9 * (size_t)b->Ttot));
         BCKC(cudaMemsetAsync(b->Fe.p, 0, sizeof(double) * 9 * (size_t)b->Ttot, s));
     }
+    if (b->any_lcmh && !fp64) {
+        BCKC(b->lcmh_w.alloc(b->Ttot));
+        BCKC(cudaMemsetAsync(b->lcmh_w.p, 0, sizeof(float) * (size_t)b->Ttot, s));
+    }
     if (b->any_minres) {
         BCKC(b->mr_p_s.alloc(N3 * SB));
         BCKC(b->mr_p0_s.alloc(N3 * SB));
@@ -1243,7 +1256,7 @@ int fem_batch_finalize(fem_batch b)
                       b->gtets.bytes() + b->Dinv_s.bytes() + b->mat_s.bytes() + b->R_s.bytes() +
                       b->Dinv64.bytes() + b->vol.bytes() + b->detF.bytes() + b->tile_nodes.bytes() +
                       b->lptr0.bytes() + b->ov_ptr.bytes() + b->ov_map.bytes() + b->knc_node.bytes() +
-                      b->perm.bytes() + b->prev_x.bytes() + b->doc.bytes() + b->Fe.bytes() + b->mr_p_s.bytes() +
+                      b->perm.bytes() + b->prev_x.bytes() + b->doc.bytes() + b->Fe.bytes() + b->lcmh_w.bytes() + b->mr_p_s.bytes() +
                       b->mr_p0_s.bytes() + b->cpart_b.bytes() + b->xn.bytes() + b->vn.bytes() +
                       b->knc_mesh.bytes() + b->knc_target.bytes() + b->lconn.bytes() + b->lptr.bytes() +
                       b->lidx.bytes() + b->fixed.bytes() + b->rest.bytes() + b->x.bytes() + b->v.bytes() +

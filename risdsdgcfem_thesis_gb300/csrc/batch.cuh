@@ -107,9 +107,13 @@ struct TileMeta {
     uint16_t material;  // the mesh's kTileMaterial*
 };
 
-// Per-tile element products (the values of enum fem_material).
+// Per-tile element products (the values of enum fem_material): C_WRP's
+// stiffness product, or a first Piola-Kirchhoff material's differential
+// (C_LCM, C_LCMH, C_CCM; csrc/lcm.cuh).
 constexpr uint16_t kTileMaterialWrp = 0;
 constexpr uint16_t kTileMaterialLcm = 1;
+constexpr uint16_t kTileMaterialLcmh = 2;
+constexpr uint16_t kTileMaterialCcm = 3;
 
 // Partial slot of local node i of a tile: owned nodes write theirs in node
 // order (slot = batch node id), shared nodes the overflow slot ov_map gives
@@ -142,7 +146,8 @@ struct MeshConsts {
     uint32_t rot_fp32;  // mixed: 1 = FP32 rotations with FP64 re-solves, 0 = FP64 rotations
     double refresh_drop_sq;  // mixed: FP64 residual when |r|^2 fell below this times its value at the last one
     uint32_t rotation;       // kMeshRotationMsvd or kMeshRotationDapd (FP64 in either precision)
-    uint32_t material;       // kTileMaterialWrp or kTileMaterialLcm
+    uint32_t material;       // kTileMaterial* (the mesh's fem_material)
+    double ecie_k;           // C_LCMH: the blend radius k (float32 in the reference)
     uint32_t solver;         // kMeshSolverCg or kMeshSolverMinres
     uint32_t integrator;     // kMeshQie, kMeshFie or kMeshFieQuasi
     uint32_t nr_max_iter;    // FIE: Newton iteration limit
@@ -158,7 +163,8 @@ struct BatchView {
     uint64_t nslots;               // partial slots: Ntot owner slots + the overflow slots
     double* prev_x;                // [3 Ntot] DAPD: positions at the start of each mesh's last step; null without DAPD
     uchar2* doc;                   // [Ttot] DAPD: direction of collapse per element (batch order)
-    double* Fe;                    // [9 Ttot] C_LCM: F of the last BeginEvaluation (the element cache's), SoA; null without C_LCM
+    double* Fe;                    // [9 Ttot] P-K materials: F of the last BeginEvaluation (the element cache's), SoA; null without them
+    float* lcmh_w;                 // [Ttot] mixed C_LCMH: the blend weight w of the last BeginEvaluation; null without it
     S* mr_p;                       // [3 Ntot] MINRES: direction p; null without a MINRES mesh
     S* mr_p0;                      // [3 Ntot] MINRES: the previous direction p0
     S* mr_v1;                      // [3 Ntot] MINRES: the Lanczos vector v1 (the q buffer)

@@ -171,8 +171,8 @@ __global__ void __launch_bounds__(256) k_tile_spmv(BatchView<S> b, const S* __re
             dl[3 * i + 2] = sd[2 * kTileNodes + ids[i]];
         }
         S out[12];
-        if (tm.material == kTileMaterialLcm)
-            elem_lcm(b, tm.mesh, e, R, Di, knu, k2, dl, out);
+        if (tm.material != kTileMaterialWrp)
+            elem_pk(b, tm.material, tm.mesh, e, R, Di, knu, k2, dl, out);
         else
             elem_RKRt<S>(R, Di, k1, knu, k2, dl, out);
 #pragma unroll
@@ -227,11 +227,12 @@ __global__ void __launch_bounds__(256) k_tile_force(BatchView<S> b, const double
         // the force of a starting step, or the energy of a finished one
         if (part64 ? !mesh_starts(b, tm.mesh) : !b.st[tm.mesh].step_done) continue;
         double energy = 0.0;
-        if (threadIdx.x < tm.ne && tm.material == kTileMaterialLcm) {
-            // C_LCM_f_e and C_LCM_V (TetrahedronElementSet3.cpp:1154-1178,
-            // 1489-1507) in FP64 in either precision, on the F of the last
-            // BeginEvaluation (the element cache's, as the reference's V()
-            // after a step also reads it)
+        if (threadIdx.x < tm.ne && tm.material != kTileMaterialWrp) {
+            // the P-K material's f_e and V (C_LCM_f_e / C_CCM_f_e, C_LCM_V,
+            // TetrahedronElementSet3.cpp:1154-1206, 1489-1545) in FP64 in
+            // either precision, on the F of the last BeginEvaluation (the
+            // element cache's, as the reference's V() after a step also
+            // reads it)
             const size_t e = tm.e0 + threadIdx.x;
             const size_t T = b.Ttot;
             const MeshConsts& mcm = b.mc[tm.mesh];
@@ -242,10 +243,11 @@ __global__ void __launch_bounds__(256) k_tile_force(BatchView<S> b, const double
             for (int c = 0; c < 9; c++) Di[c] = b.Dinv64[c * T + e];
 #pragma unroll
             for (int c = 0; c < 9; c++) F[c] = b.Fe[c * T + e];
-            energy = lcm_energy(R, F, b.vol[e], mcm.lame_mu, mcm.lame_lambda);
+            const PkMaterial pm{(int)tm.material, mcm.lame_mu, mcm.lame_lambda, mcm.ecie_k};
+            energy = pk_energy(pm, R, F, b.vol[e]);
             if (part64) {
                 double out[12];
-                lcm_force(R, F, Di, b.vol[e], mcm.lame_mu, mcm.lame_lambda, out);
+                pk_force(pm, R, F, Di, b.vol[e], out);
 #pragma unroll
                 for (int c = 0; c < 12; c++) y64_set(so[c * kTileElems + threadIdx.x], out[c]);
             }

@@ -121,4 +121,54 @@ __device__ __forceinline__ void elem_lcm_dforce(const C* R, const C* Di, C kl, C
     }
 }
 
+// The C_LCMH differential (C_LCMH_df_x, TetrahedronElementSet3.cpp:
+// 1875-1930) in the same folded form, with the element's blend weight w
+// (Clamp01(tr|S - I| / (3 k)) at the last evaluation; 1 when k <= 0.1,
+// where the reference takes C_LCM's): dP = 2 km (w dF + (1 - w) R
+// sym(R^T dF)) + kl tr(R^T dF) R.
+template <typename S, typename C = S>
+__device__ __forceinline__ void elem_lcmh_dforce(const C* R, const C* Di, C kl, C km, C w, const S* d, S* out)
+{
+    S dDs[9];
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+        for (int j = 0; j < 3; j++) dDs[3 * a + j] = d[3 * (j + 1) + a] - d[a];
+    S dF[9];
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+        for (int b = 0; b < 3; b++) dF[3 * a + b] = dDs[3 * a] * Di[b] + dDs[3 * a + 1] * Di[3 + b] + dDs[3 * a + 2] * Di[6 + b];
+    S RtdF[9];  // R^T dF
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+        for (int b = 0; b < 3; b++) RtdF[3 * a + b] = R[a] * dF[b] + R[3 + a] * dF[3 + b] + R[6 + a] * dF[6 + b];
+    const S ktr = kl * (RtdF[0] + RtdF[4] + RtdF[8]);
+    const C km2 = (C)2 * km, ow = (C)1 - w;
+    S sym[9];
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+        for (int b = 0; b < 3; b++) sym[3 * a + b] = (RtdF[3 * a + b] + RtdF[3 * b + a]) * (C)0.5;
+    S dP[9];
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+        for (int b = 0; b < 3; b++) {
+            const S Rs = R[3 * a] * sym[b] + R[3 * a + 1] * sym[3 + b] + R[3 * a + 2] * sym[6 + b];
+            dP[3 * a + b] = km2 * (w * dF[3 * a + b] + ow * Rs) + ktr * R[3 * a + b];
+        }
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        S acc0 = dP[3 * a] * Di[0] + dP[3 * a + 1] * Di[1] + dP[3 * a + 2] * Di[2];
+        S acc1 = dP[3 * a] * Di[3] + dP[3 * a + 1] * Di[4] + dP[3 * a + 2] * Di[5];
+        S acc2 = dP[3 * a] * Di[6] + dP[3 * a + 1] * Di[7] + dP[3 * a + 2] * Di[8];
+        out[3 + a] = acc0;
+        out[6 + a] = acc1;
+        out[9 + a] = acc2;
+        out[a] = -(acc0 + acc1 + acc2);
+    }
+}
+
 }  // namespace femgb

@@ -29,21 +29,36 @@ __device__ __forceinline__ double y_full(const BatchView<S>& b, const double* y,
 // the last block of the mesh in the node pass, see refresh_decide).
 __device__ __forceinline__ bool refresh_now(const MeshConsts&, const StepScalars& s) { return s.refresh_next != 0; }
 
-// The C_LCM product of element e of `mesh` (the tile's material): in FP64
-// the FP64 solid's own arithmetic (V, mu, lambda apart), otherwise the
-// folded form of elem_math.cuh on the element's V lambda and V mu.
+// The P-K product of element e of `mesh` (the tile's material: C_LCM,
+// C_LCMH or C_CCM): in FP64 the FP64 solid's own arithmetic (pk_dforce, on
+// the F and det F of the last evaluation), otherwise the folded forms of
+// elem_math.cuh on the element's V lambda and V mu (C_LCMH with its blend
+// weight of the last evaluation; the mixed path takes no C_CCM).
 template <typename S>
-__device__ __forceinline__ void elem_lcm(const BatchView<S>& b, uint32_t mesh, size_t e, const double* R,
-                                         const double* Di, double, double, const double* dl, double* out)
+__device__ __forceinline__ void elem_pk(const BatchView<S>& b, uint32_t material, uint32_t mesh, size_t e,
+                                        const double* R, const double* Di, double, double, const double* dl,
+                                        double* out)
 {
     const MeshConsts& c = b.mc[mesh];
-    lcm_dforce(R, Di, b.vol[e], c.lame_mu, c.lame_lambda, dl, out);
+    if (material == kTileMaterialLcm) {
+        lcm_dforce(R, Di, b.vol[e], c.lame_mu, c.lame_lambda, dl, out);
+        return;
+    }
+    double F[9];
+    const size_t T = b.Ttot;
+#pragma unroll
+    for (int k = 0; k < 9; k++) F[k] = b.Fe[k * T + e];
+    const PkMaterial m{(int)material, c.lame_mu, c.lame_lambda, c.ecie_k};
+    pk_dforce(m, R, F, b.detF[e], Di, b.vol[e], dl, out);
 }
 template <typename S, typename V>
-__device__ __forceinline__ void elem_lcm(const BatchView<S>&, uint32_t, size_t, const float* R, const float* Di,
-                                         float kl, float km, const V* dl, V* out)
+__device__ __forceinline__ void elem_pk(const BatchView<S>& b, uint32_t material, uint32_t, size_t e,
+                                        const float* R, const float* Di, float kl, float km, const V* dl, V* out)
 {
-    elem_lcm_dforce<V, float>(R, Di, kl, km, dl, out);
+    if (material == kTileMaterialLcmh)
+        elem_lcmh_dforce<V, float>(R, Di, kl, km, b.lcmh_w[e], dl, out);
+    else
+        elem_lcm_dforce<V, float>(R, Di, kl, km, dl, out);
 }
 
 // Product of the iterate y for the residual b - A y (same element data):
@@ -126,8 +141,8 @@ __device__ __forceinline__ void tile_spmv_y64_pass(const BatchView<S>& b, const 
                 dl[3 * i + 2] = sd[2 * kTileNodes + ids[i]];
             }
             V out[12];
-            if (tm.material == kTileMaterialLcm)
-                elem_lcm(b, tm.mesh, e, R, Di, knu, k2, dl, out);
+            if (tm.material != kTileMaterialWrp)
+                elem_pk(b, tm.material, tm.mesh, e, R, Di, knu, k2, dl, out);
             else
                 elem_RKRt<V, S>(R, Di, k1, knu, k2, dl, out);
 #pragma unroll

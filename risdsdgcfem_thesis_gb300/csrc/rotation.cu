@@ -264,10 +264,32 @@ __global__ void __launch_bounds__(256, 3) k_begin_eval_batch(BatchView<S> b, con
                 *reinterpret_cast<float*>(base + blob_comp_off(8, i, ne4)) = (float)Rs[8];
             }
             b.detF[e] = detF;
-            if (b.Fe && mcm.material == kTileMaterialLcm) {
-                // the element cache's F, which C_LCM_f_e and C_LCM_V read
+            if (b.Fe && mcm.material != kTileMaterialWrp) {
+                // the element cache's F, which the P-K materials' f_e, V
+                // and differentials read
 #pragma unroll
                 for (int c = 0; c < 9; c++) b.Fe[c * T + e] = F[c];
+                if (b.lcmh_w && mcm.material == kTileMaterialLcmh) {
+                    // the mixed path's C_LCMH blend weight
+                    // (TetrahedronElementSet3.cpp:1886-1897) on the stored
+                    // rotation: w = Clamp01(tr|R^T F - I| / (3 k)); 1 when
+                    // (float)k <= 0.1, where the differential is C_LCM's
+                    double w = 1.0;
+                    if ((float)mcm.ecie_k > 0.1f) {
+                        double tr = 0.0;
+#pragma unroll
+                        for (int a = 0; a < 3; a++) {
+                            double sa = 0.0;
+#pragma unroll
+                            for (int k = 0; k < 3; k++) sa += (double)Rs[3 * k + a] * F[3 * k + a];
+                            tr += fabs(sa - 1.0);
+                        }
+                        w = (1.0 / mcm.ecie_k) * tr / 3.0;
+                        w = (w < 1.0) ? w : 1.0;
+                        w = (0.0 > w) ? 0.0 : w;
+                    }
+                    b.lcmh_w[e] = (float)w;
+                }
             }
             if (detF <= 0.0) atomicAdd(&s_inv, 1u);
         }

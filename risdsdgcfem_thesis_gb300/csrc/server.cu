@@ -287,8 +287,9 @@ int fem_server_add_scene(fem_server s, const double* rest, uint32_t N, const uin
         return batch_fail(FEM_E_ARG, "unknown rotation %u", p->rotation);
     if (p->ls_solver != FEM_LS_CG && p->ls_solver != FEM_LS_MINRES)
         return batch_fail(FEM_E_ARG, "unknown ls_solver %u", p->ls_solver);
-    if (p->material != FEM_MATERIAL_C_WRP && p->material != FEM_MATERIAL_C_LCM)
-        return batch_fail(FEM_E_ARG, "material %u: the server takes C_WRP and C_LCM", p->material);
+    if (p->material > FEM_MATERIAL_C_CCM) return batch_fail(FEM_E_ARG, "unknown material %u", p->material);
+    if (p->material == FEM_MATERIAL_C_CCM && s->opt.precision != FEM_PRECISION_FP64)
+        return batch_fail(FEM_E_ARG, "C_CCM runs in FP64 (its differential is not symmetric)");
     if (s->opt.persistent_loop && (p->ls_solver != FEM_LS_CG || p->material != FEM_MATERIAL_C_WRP))
         return batch_fail(FEM_E_ARG, "the persistent loop takes CG meshes of C_WRP only");
     if (knc_count && (!knc_nodes || !knc_targets)) return batch_fail(FEM_E_ARG, "null constraint arrays");

@@ -264,7 +264,7 @@ struct TileLook {
 __device__ __forceinline__ uint32_t look_ne(const TileLook& L) { return L.sizes & 0x3ffu; }
 __device__ __forceinline__ uint32_t look_nn(const TileLook& L) { return (L.sizes >> 10) & 0x3ffu; }
 __device__ __forceinline__ uint32_t look_nown(const TileLook& L) { return (L.sizes >> 20) & 0x3ffu; }
-__device__ __forceinline__ bool look_lcm(const TileLook& L) { return (L.sizes >> 30) == kTileMaterialLcm; }
+__device__ __forceinline__ bool look_lcm(const TileLook& L) { return (L.sizes >> 30) != kTileMaterialWrp; }
 // A tile to do (valid once resolved).
 __device__ __forceinline__ bool look_live(const TileLook& L) { return L.sizes != 0u && L.done == 0u; }
 
@@ -458,8 +458,12 @@ __device__ __forceinline__ void tile_pipe_pass(const BatchView<float>& b, const 
                 dl[3 * k + 1] = v.y;
                 dl[3 * k + 2] = v.z;
             }
-            if (kLcm && look_lcm(cur))
-                elem_lcm_dforce<float>(R, Di, knu, k2, dl, out);
+            if (kLcm && look_lcm(cur)) {
+                if ((cur.sizes >> 30) == kTileMaterialLcmh)
+                    elem_lcmh_dforce<float>(R, Di, knu, k2, b.lcmh_w[b.tiles[cur.tile].e0 + tid], dl, out);
+                else
+                    elem_lcm_dforce<float>(R, Di, knu, k2, dl, out);
+            }
             else
                 elem_RKRt<float>(R, Di, k1, knu, k2, dl, out);
             float eq = 0.f;

@@ -99,12 +99,70 @@ def test_mixed_batch_and_server_lcm_match_reference(fem_lib):
     assert np.array_equal(xs, x) and np.array_equal(vs, v)
 
 
-def test_batch_rejects_lcmh_and_ccm(fem_lib):
-    for mat in (2, 3):
-        sc = dataclasses.replace(scenes.cantilever_160(), material=mat)
-        with pytest.raises(fem_lib.FemError) as e:
-            fem_lib.Batch([sc], precision=fem_lib.FEM_PRECISION_FP64)
-        assert e.value.code == fem_lib.FEM_E_ARG
+@pytest.mark.parametrize("case", [0, 1, 3])
+def test_fp64_batch_lcmh_matches_reference(fem_lib, case):
+    """C_LCMH meshes in an FP64 batch (the solid's pk_dforce on the F and
+    det F of the last evaluation), next to a C_WRP mesh: the fixture's cases
+    (blend radius 1 and 0.05) with the solid's bars."""
+    from test_oracle_materials import material_cases
+    g = np.load(os.path.join(GOLDEN, "materials.npz"))
+    prefix, sc, steps = material_cases()[case]
+    bt = fem_lib.Batch([scenes.cantilever_160(), sc], precision=fem_lib.FEM_PRECISION_FP64)
+    for k in range(steps):
+        bt.step(1)
+        st = bt.stats(1)
+        assert st["status"] == 0
+        assert abs(st["cg_iterations"] - int(g[prefix + "iters"][k])) <= 1, k
+    x, v = bt.state(1)
+    assert rel(x, g[prefix + "x"]) <= 1e-10 and rel(v, g[prefix + "v"]) <= 1e-10, \
+        (prefix, rel(x, g[prefix + "x"]), rel(v, g[prefix + "v"]))
+    ref_e = float(g[prefix + "elastic_energy"][-1])
+    assert abs(st["elastic_energy"] - ref_e) <= 1e-8 * abs(ref_e)
+
+
+def test_mixed_batch_and_server_lcmh_match_reference(fem_lib):
+    """C_LCMH on the mixed path (the blend weight of each element from the
+    last evaluation, FP32 products): the cantilever within 1e-5 (x) and 1e-4
+    (v) of the fixture, in a batch and, the same bits, through the server."""
+    from test_oracle_materials import material_cases
+    g = np.load(os.path.join(GOLDEN, "materials.npz"))
+    prefix, sc, steps = material_cases()[0]
+    bt = fem_lib.Batch([sc], precision=fem_lib.FEM_PRECISION_MIXED, compute_energy=False, chunk_nodes=256)
+    bt.step(steps)
+    x, v = bt.state(0)
+    assert rel(x, g[prefix + "x"]) <= 1e-5 and rel(v, g[prefix + "v"]) <= 1e-4, \
+        (rel(x, g[prefix + "x"]), rel(v, g[prefix + "v"]))
+    srv = fem_lib.Server(precision=fem_lib.FEM_PRECISION_MIXED)
+    sid = srv.add(sc)
+    srv.admit()
+    for k in range(steps):
+        srv.submit(sid, k)
+    done = srv.drain()
+    assert len(done) == steps and all(c["status"] == 0 for c in done)
+    xs, vs = srv.state(sid)
+    assert np.array_equal(xs, x) and np.array_equal(vs, v)
+
+
+def test_fp64_batch_ccm_runs_away_as_in_the_reference(fem_lib):
+    """C_CCM in an FP64 batch: the first step's CG diverges as the fixture's
+    (iteration cap, relative residual > 1), the run ends in FEM_E_NAN; the
+    mixed path refuses C_CCM."""
+    from test_oracle_materials import material_cases
+    g = np.load(os.path.join(GOLDEN, "materials.npz"))
+    prefix, sc, steps = material_cases()[2]
+    assert prefix == "ccm_"
+    bt = fem_lib.Batch([sc], precision=fem_lib.FEM_PRECISION_FP64)
+    bt.step(1)
+    st = bt.stats(0)
+    assert st["cg_iterations"] == int(g["ccm_iters"][0]) == sc.max_iter
+    assert st["rel_residual"] > 1.0
+    with pytest.raises(fem_lib.FemError) as e:
+        for _ in range(steps):
+            bt.step(1)
+    assert e.value.code == fem_lib.FEM_E_NAN
+    with pytest.raises(fem_lib.FemError) as e:
+        fem_lib.Batch([sc], precision=fem_lib.FEM_PRECISION_MIXED)
+    assert e.value.code == fem_lib.FEM_E_ARG
 
 
 @pytest.mark.parametrize("case", [0, 1, 3])
