@@ -59,7 +59,8 @@ enum fem_integrator {
      * re-evaluated at every Newton iterate, up to nr_max_iter iterations,
      * stopping when |b_k| < nr_abs_epsilon. On the solid and in batches of
      * either precision (a device-side Newton loop, each solid leaving on its
-     * own test); not in servers. */
+     * own test), and in servers (shards of their own that run whole
+     * steps). */
     FEM_INTEGRATOR_FIE_DX = 1,
     /* Step_FullyImplicitEuler_dx(0): the same Newton loop without inertia
      * (quasi-static equilibrium; velocities become zero). As FIE_DX. */

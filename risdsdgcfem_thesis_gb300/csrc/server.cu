@@ -19,7 +19,8 @@
 //  * Shards. A shard is one batch (batch.cu): its scenes stay resident; a
 //    launch of the shard is one CUDA-graph launch on the shard's own stream
 //    that runs at most slice_iterations CG iterations (the batch's
-//    iteration budget). Scenes whose step is running continue (mask 2),
+//    iteration budget; shards of FIE scenes, whose Newton steps take no
+//    budget, run whole steps). Scenes whose step is running continue (mask 2),
 //    scenes with a request waiting start a step (mask 1), the others sit
 //    out (mask 0).
 //  * Continuous batching. fem_server_pump never blocks: it harvests every
@@ -172,7 +173,9 @@ int build_shard(fem_server srv, const std::vector<uint32_t>& ids, Shard& out)
         }
     }
     int e = fem_batch_finalize(b);
-    if (!e) e = fem_batch_set_slice(b, srv->opt.slice_iterations);
+    // FIE shards step whole (a Newton step takes no iteration budget)
+    const bool newton = srv->scenes[ids[0]].params.integrator != FEM_INTEGRATOR_QIE_V;
+    if (!e) e = fem_batch_set_slice(b, newton ? 0u : srv->opt.slice_iterations);
     if (e) {
         fem_batch_destroy(b);
         return e;
@@ -281,8 +284,10 @@ int fem_server_add_scene(fem_server s, const double* rest, uint32_t N, const uin
     if (int e = check_server(s)) return e;
     if (!rest || !tets || !p) return batch_fail(FEM_E_ARG, "null rest/tets/params");
     if (N == 0 || T == 0) return batch_fail(FEM_E_ARG, "empty mesh (N=%u, T=%u)", N, T);
-    if (p->integrator != FEM_INTEGRATOR_QIE_V)
-        return batch_fail(FEM_E_ARG, "integrator %u: the server steps with QIE_V", p->integrator);
+    if (p->integrator > FEM_INTEGRATOR_FIE_DX_QUASISTATIC)
+        return batch_fail(FEM_E_ARG, "unknown integrator %u", p->integrator);
+    if (p->integrator != FEM_INTEGRATOR_QIE_V && s->opt.persistent_loop)
+        return batch_fail(FEM_E_ARG, "the persistent loop takes QIE_V scenes only");
     if (p->rotation != FEM_ROTATION_MSVD && p->rotation != FEM_ROTATION_DAPD)
         return batch_fail(FEM_E_ARG, "unknown rotation %u", p->rotation);
     if (p->ls_solver != FEM_LS_CG && p->ls_solver != FEM_LS_MINRES)
@@ -322,16 +327,21 @@ int fem_server_admit(fem_server s, uint32_t* admitted)
     for (uint32_t i = 0; i < s->scenes.size(); i++)
         if (s->scenes[i].state == SCENE_WAITING) wait.push_back(i);
     // similar sizes share a shard (a shard's step lasts as long as its
-    // slowest scene's CG loop)
-    std::stable_sort(wait.begin(), wait.end(),
-                     [&](uint32_t a, uint32_t b) { return s->scenes[a].T < s->scenes[b].T; });
+    // slowest scene's CG loop); FIE scenes, whose Newton steps run whole,
+    // get shards of their own, so QIE shards keep their slices
+    auto newton = [&](uint32_t i) { return s->scenes[i].params.integrator != FEM_INTEGRATOR_QIE_V; };
+    std::stable_sort(wait.begin(), wait.end(), [&](uint32_t a, uint32_t b) {
+        if (newton(a) != newton(b)) return !newton(a);
+        return s->scenes[a].T < s->scenes[b].T;
+    });
     size_t k = 0;
     uint32_t count = 0;
     while (k < wait.size()) {
         std::vector<uint32_t> ids;
         uint64_t T = 0, N = 0;
         while (k < wait.size() && ids.size() < s->opt.shard_max_scenes &&
-               (ids.empty() || T + s->scenes[wait[k]].T <= s->opt.shard_max_tets)) {
+               (ids.empty() || (T + s->scenes[wait[k]].T <= s->opt.shard_max_tets &&
+                                newton(wait[k]) == newton(ids[0])))) {
             T += s->scenes[wait[k]].T;
             N += s->scenes[wait[k]].N;
             ids.push_back(wait[k++]);

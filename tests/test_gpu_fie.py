@@ -245,3 +245,31 @@ def test_fie_batch_runs_newton_steps_whole(fem_lib):
     with pytest.raises(fem_lib.FemError) as e:
         fem_lib.Batch([sc], precision=fem_lib.FEM_PRECISION_MIXED, persistent_loop=1)
     assert e.value.code == fem_lib.FEM_E_ARG
+
+
+def test_server_steps_fie_scenes_in_whole_step_shards(fem_lib):
+    """The server takes FIE scenes into shards of their own (whole Newton
+    steps, no iteration budget) beside sliced QIE shards: each scene's
+    result is the bits of a mixed batch of its own, the FIE cantilever
+    within 1e-5 of the fixture."""
+    g = np.load(os.path.join(GOLDEN, "fie_160.npz"))
+    cant = dataclasses.replace(scenes.cantilever_160(), integrator=fem_lib.FEM_INTEGRATOR_FIE_DX)
+    quasi = dataclasses.replace(scenes.cantilever_160(), integrator=fem_lib.FEM_INTEGRATOR_FIE_DX_QUASISTATIC)
+    qie = scenes.cantilever_160()
+    steps = 10
+    srv = fem_lib.Server(precision=fem_lib.FEM_PRECISION_MIXED)
+    ids = [srv.add(sc) for sc in (cant, qie, quasi)]
+    srv.admit()
+    for k in range(steps):
+        for i in ids:
+            srv.submit(i, k)
+    done = srv.drain()
+    assert len(done) == 3 * steps and all(c["status"] == 0 for c in done)
+    for i, sc in zip(ids, (cant, qie, quasi)):
+        one = fem_lib.Batch([sc], precision=fem_lib.FEM_PRECISION_MIXED, compute_energy=False, chunk_nodes=256)
+        one.step(steps)
+        xs, vs = srv.state(i)
+        xo, vo = one.state(0)
+        assert np.array_equal(xs, xo) and np.array_equal(vs, vo), sc.integrator
+    x, v = srv.state(ids[0])
+    assert rel(x, g["x"][steps - 1]) <= 1e-5 and rel(v, g["v"][steps - 1]) <= 1e-4
