@@ -441,7 +441,7 @@ def rotation_leg(n=60, reps=5):
     return out
 
 
-def batch_variants_leg(meshes=128, steps=3, seed=7):
+def batch_variants_leg(meshes=128, steps=3, seed=7, names=None, use_graph=True):
     """The reference's alternatives on the batched mixed path, one batch of
     `meshes` meshes of the batched workload's generator per variant (every
     mesh with the variant): the step (QIE, CG, C_WRP, MSVD), MINRES, C_LCM,
@@ -457,12 +457,14 @@ def batch_variants_leg(meshes=128, steps=3, seed=7):
                 ("c_lcm", {"material": capi.FEM_MATERIAL_C_LCM}), ("dapd", {"rotation": capi.FEM_ROTATION_DAPD}),
                 ("fie", {"integrator": capi.FEM_INTEGRATOR_FIE_DX, "nr_max_iter": 3}),
                 ("lock_step", {"nr_max_iter": 3}))
+    if names:
+        variants = tuple(v for v in variants if v[0] in names)
     T = sum(sc.num_tets for sc in base)
     out = {"workload": f"{meshes} meshes of the batched workload's generator (seed {seed}), {T} tets, mixed",
            "steps": steps}
     for name, kw in variants:
         scs = [dataclasses.replace(sc, **kw) for sc in base]
-        bt = capi.Batch(scs, precision=capi.FEM_PRECISION_MIXED, compute_energy=False)
+        bt = capi.Batch(scs, precision=capi.FEM_PRECISION_MIXED, compute_energy=False, use_graph=use_graph)
         if name == "lock_step":
             dt = scs[0].dt
             bt.multi_step(dt, 1)
@@ -957,10 +959,19 @@ def main():
     ap.add_argument("--served-rate", type=float, default=20000.0, help="offered step requests per second")
     ap.add_argument("--served-seconds", type=float, default=3.0)
     ap.add_argument("--served-pool", type=int, default=4096)
+    ap.add_argument("--only-variants", action="store_true",
+                    help="run only the batched variants leg and print its JSON (for per-kernel profiles)")
+    ap.add_argument("--variants", default="step,minres,c_lcm,dapd,fie,lock_step",
+                    help="comma-separated variants of the batched variants leg")
+    ap.add_argument("--variants-meshes", type=int, default=128)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
         return run_reference(args)
+    if args.only_variants:
+        print(json.dumps(batch_variants_leg(meshes=args.variants_meshes, steps=args.steps,
+                                            names=args.variants.split(","), use_graph=not args.no_graph)))
+        return 0
     return run_ours(args)
 
 
