@@ -949,8 +949,10 @@ __global__ void k_node_mr_finish(BatchView<S> b, double* __restrict__ y, S* __re
         const uint32_t pending = sm.mr_pending;
         if (!pending) continue;
         const MinresScalars mr = sm.mr;
-        S* p = b.mr_p;
-        S* p0 = b.mr_p0;
+        // the six vectors are distinct buffers: restrict lets the loads of
+        // the next entries go ahead of this entry's stores
+        S* __restrict__ p = b.mr_p;
+        S* __restrict__ p0 = b.mr_p0;
         if (pending == 2u) {
             const S inv = (S)mr.inv_beta;
             for (size_t i = 3 * (size_t)ch.n0 + threadIdx.x; i < 3 * (size_t)ch.n1; i += blockDim.x) {
@@ -961,6 +963,7 @@ __global__ void k_node_mr_finish(BatchView<S> b, double* __restrict__ y, S* __re
             }
         } else {
             const S inv = (S)mr.inv_beta, nr2 = (S)mr.neg_r2, nr3 = (S)mr.neg_r3, ir1 = (S)mr.inv_r1;
+#pragma unroll 4
             for (size_t i = 3 * (size_t)ch.n0 + threadIdx.x; i < 3 * (size_t)ch.n1; i += blockDim.x) {
                 const S v = r[i];
                 const S pi = p[i];
