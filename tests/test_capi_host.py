@@ -172,7 +172,7 @@ def test_server_host_validation_without_gpu(fem_lib):
                                       t_bad.shape[0], C.byref(p), None, None, None, None, 0, C.byref(sid))
         assert rc == fem_lib.FEM_E_INDEX
         t_ok = np.ascontiguousarray(tets, np.uint32)
-        p.integrator = fem_lib.FEM_INTEGRATOR_FIE_DX  # the server steps with QIE_V only
+        p.integrator = 7  # no such integrator
         rc = lib.fem_server_add_scene(h, rest.ctypes.data_as(dp), rest.shape[0], t_ok.ctypes.data_as(up),
                                       t_ok.shape[0], C.byref(p), None, None, None, None, 0, C.byref(sid))
         assert rc == fem_lib.FEM_E_ARG and b"integrator" in lib.fem_last_error()
