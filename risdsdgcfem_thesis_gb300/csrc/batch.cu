@@ -194,7 +194,7 @@ struct fem_batch_s {
         b.nchunks = nchunks;
         b.pipe_tile = opt.tile_elems <= (uint32_t)kPipeSmallTile ? kPipeSmallTile : kTileElems;
         b.fuse_alpha = opt.fuse_alpha ? 1u : 0u;
-        b.has_lcm = any_lcm ? 1u : 0u;
+        b.has_lcm = any_lcmh ? 2u : any_lcm ? 1u : 0u;
         b.lock = lock ? 1u : 0u;
         b.Ntot = (uint32_t)Ntot;
         b.Ttot = (uint32_t)Ttot;

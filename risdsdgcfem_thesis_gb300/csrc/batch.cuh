@@ -174,7 +174,7 @@ struct BatchView {
     double* vn;                    // [3 Ntot] FIE: v^n (lock-step: v_k)
     uint32_t pipe_tile;            // mixed: threads per block of the tile product (kPipeSmallTile or kTileElems)
     uint32_t fuse_alpha;           // mixed: the node pass forms alpha (no separate alpha kernel)
-    uint32_t has_lcm;              // some mesh takes the C_LCM product
+    uint32_t has_lcm;              // the P-K products some mesh takes: 0 none, 1 C_LCM (or C_CCM), 2 also C_LCMH
     uint32_t lock;                 // the multi-solid Newton lock-step's phases (x_k, v_k in xn, vn; x, v hold x^n, v^n)
     const TileMeta* tiles;
     const ChunkMeta* chunks;

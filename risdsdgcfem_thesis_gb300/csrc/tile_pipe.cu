@@ -344,7 +344,10 @@ __device__ __forceinline__ void tile_pipe_init(unsigned char* smem)
 // read-only path, for a kernel whose other phases write them (the
 // persistent loop); the pointer parameters carry no __restrict__ for the
 // same reason (the kernels that call a pass alone have it on theirs).
-template <int TILE, bool kCoherent = false, bool kLcm = false>
+// kPk: the P-K products compiled in -- 0 none (C_WRP only), 1 C_LCM, 2 C_LCM
+// and C_LCMH (each form only for batches that need it: the products' extra
+// registers would otherwise cost the simpler forms).
+template <int TILE, bool kCoherent = false, int kPk = 0>
 __device__ __forceinline__ void tile_pipe_pass(const BatchView<float>& b, const float* dvec, const float* rvec,
                                                float* part, float2* tshare, unsigned* err,
                                                unsigned char* smem, uint32_t& phase, const uint32_t block,
@@ -458,8 +461,8 @@ __device__ __forceinline__ void tile_pipe_pass(const BatchView<float>& b, const 
                 dl[3 * k + 1] = v.y;
                 dl[3 * k + 2] = v.z;
             }
-            if (kLcm && look_lcm(cur)) {
-                if ((cur.sizes >> 30) == kTileMaterialLcmh)
+            if (kPk != 0 && look_lcm(cur)) {
+                if (kPk == 2 && (cur.sizes >> 30) == kTileMaterialLcmh)
                     elem_lcmh_dforce<float>(R, Di, knu, k2, b.lcmh_w[b.tiles[cur.tile].e0 + tid], dl, out);
                 else
                     elem_lcm_dforce<float>(R, Di, knu, k2, dl, out);
@@ -544,7 +547,7 @@ __device__ __forceinline__ void tile_pipe_pass(const BatchView<float>& b, const 
     }
 }
 
-template <int TILE, bool kLcm>
+template <int TILE, int kPk>
 __global__ void __launch_bounds__(TILE, PipeShape<TILE>::kMinBlocks) k_tile_spmv_pipe(BatchView<float> b, const float* __restrict__ dvec,
                                                            const float* __restrict__ rvec, float* __restrict__ part,
                                                            float2* __restrict__ tshare,
@@ -556,7 +559,7 @@ __global__ void __launch_bounds__(TILE, PipeShape<TILE>::kMinBlocks) k_tile_spmv
     if (set_if && blockIdx.x == 0 && threadIdx.x == 0) cudaGraphSetConditional(if_refresh, *refresh_flag ? 1u : 0u);
     tile_pipe_init<TILE>(smem);
     uint32_t phase = 0u;
-    tile_pipe_pass<TILE, false, kLcm>(b, dvec, rvec, part, tshare, err, smem, phase, blockIdx.x, gridDim.x,
+    tile_pipe_pass<TILE, false, kPk>(b, dvec, rvec, part, tshare, err, smem, phase, blockIdx.x, gridDim.x,
                                       *(volatile const unsigned*)(err + 1));
 }
 
@@ -1532,7 +1535,7 @@ cudaError_t launch_cg_resident(const BatchView<float>& b, const CoopLoopArgs& a,
 
 uint32_t tile_pipe_smem_bytes() { return PipeShape<256>::kSmem; }
 
-template <int TILE, bool kLcm = false>
+template <int TILE, int kPk = 0>
 static int pipe_grid()
 {
     static int grid = 0;
@@ -1540,9 +1543,9 @@ static int pipe_grid()
         int dev = 0, sms = 0, per_sm = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaFuncSetAttribute(k_tile_spmv_pipe<TILE, kLcm>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        cudaFuncSetAttribute(k_tile_spmv_pipe<TILE, kPk>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)PipeShape<TILE>::kSmem);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tile_spmv_pipe<TILE, kLcm>, TILE,
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tile_spmv_pipe<TILE, kPk>, TILE,
                                                       PipeShape<TILE>::kSmem);
         if (sms <= 0) sms = 152;
         if (per_sm <= 0) per_sm = 1;
@@ -1551,29 +1554,40 @@ static int pipe_grid()
     return grid;
 }
 
+template <int TILE, int kPk>
+static void launch_pipe_form(const BatchView<float>& b, const float* d, const float* r, float* part, float2* tshare,
+                             cudaGraphConditionalHandle if_refresh, int set_if, const unsigned* refresh_flag,
+                             unsigned* err, cudaStream_t s)
+{
+    const int g = pipe_grid<TILE, kPk>();
+    const uint32_t grid = b.ntiles < (uint32_t)g ? (b.ntiles ? b.ntiles : 1) : (uint32_t)g;
+    k_tile_spmv_pipe<TILE, kPk><<<grid, TILE, PipeShape<TILE>::kSmem, s>>>(b, d, r, part, tshare, if_refresh, set_if,
+                                                                         refresh_flag, err);
+}
+
 void launch_tile_spmv_pipe(const BatchView<float>& b, const float* d, const float* r, float* part, float2* tshare,
                            cudaGraphConditionalHandle if_refresh, int set_if, const unsigned* refresh_flag,
                            unsigned* err, cudaStream_t s)
 {
-    // the form with the C_LCM product only for batches that hold C_LCM
-    // meshes (the C_WRP form keeps its registers to itself)
-    const bool small = b.pipe_tile == (uint32_t)kPipeSmallTile, lcm = b.has_lcm != 0;
-    const int g = small ? (lcm ? pipe_grid<kPipeSmallTile, true>() : pipe_grid<kPipeSmallTile>())
-                        : (lcm ? pipe_grid<kTileElems, true>() : pipe_grid<kTileElems>());
-    const uint32_t grid = b.ntiles < (uint32_t)g ? (b.ntiles ? b.ntiles : 1) : (uint32_t)g;
+    // the form with the P-K products only for batches that hold such meshes
+    // (b.has_lcm: 1 C_LCM, 2 also C_LCMH)
+    const bool small = b.pipe_tile == (uint32_t)kPipeSmallTile;
     prof_begin("tile_spmv_mixed", s);
-    if (small && lcm)
-        k_tile_spmv_pipe<kPipeSmallTile, true><<<grid, kPipeSmallTile, PipeShape<kPipeSmallTile>::kSmem, s>>>(
-            b, d, r, part, tshare, if_refresh, set_if, refresh_flag, err);
-    else if (small)
-        k_tile_spmv_pipe<kPipeSmallTile, false><<<grid, kPipeSmallTile, PipeShape<kPipeSmallTile>::kSmem, s>>>(
-            b, d, r, part, tshare, if_refresh, set_if, refresh_flag, err);
-    else if (lcm)
-        k_tile_spmv_pipe<kTileElems, true><<<grid, kTileElems, PipeShape<kTileElems>::kSmem, s>>>(
-            b, d, r, part, tshare, if_refresh, set_if, refresh_flag, err);
-    else
-        k_tile_spmv_pipe<kTileElems, false><<<grid, kTileElems, PipeShape<kTileElems>::kSmem, s>>>(
-            b, d, r, part, tshare, if_refresh, set_if, refresh_flag, err);
+    if (small) {
+        if (b.has_lcm == 2u)
+            launch_pipe_form<kPipeSmallTile, 2>(b, d, r, part, tshare, if_refresh, set_if, refresh_flag, err, s);
+        else if (b.has_lcm)
+            launch_pipe_form<kPipeSmallTile, 1>(b, d, r, part, tshare, if_refresh, set_if, refresh_flag, err, s);
+        else
+            launch_pipe_form<kPipeSmallTile, 0>(b, d, r, part, tshare, if_refresh, set_if, refresh_flag, err, s);
+    } else {
+        if (b.has_lcm == 2u)
+            launch_pipe_form<kTileElems, 2>(b, d, r, part, tshare, if_refresh, set_if, refresh_flag, err, s);
+        else if (b.has_lcm)
+            launch_pipe_form<kTileElems, 1>(b, d, r, part, tshare, if_refresh, set_if, refresh_flag, err, s);
+        else
+            launch_pipe_form<kTileElems, 0>(b, d, r, part, tshare, if_refresh, set_if, refresh_flag, err, s);
+    }
     prof_end("tile_spmv_mixed", s);
     launch_counter()++;
 }
