@@ -273,3 +273,31 @@ def test_server_steps_fie_scenes_in_whole_step_shards(fem_lib):
         assert np.array_equal(xs, xo) and np.array_equal(vs, vo), sc.integrator
     x, v = srv.state(ids[0])
     assert rel(x, g["x"][steps - 1]) <= 1e-5 and rel(v, g["v"][steps - 1]) <= 1e-4
+
+
+def test_fp64_batch_fie_with_every_alternative_matches_oracle(fem_lib, oracle):
+    """One FP64 batch holding the crushed cube with FIE, DAPD, C_LCM and
+    MINRES together, next to a QIE cantilever: the cube against the oracle
+    restatement over 8 steps within max(1e-10, 10 x the oracle's movement
+    under a 1e-13 change of the initial velocities), capped per scene; the
+    Newton iteration counts equal the oracle's."""
+    from parity_util import bar_cap, check_bar, perturbed
+    sc = dataclasses.replace(scenes.compressed_cube(n=4, steps=10, ratio=0.4), rotation=1, material=1,
+                             ls_solver=1, integrator=fem_lib.FEM_INTEGRATOR_FIE_DX)
+    steps = 8
+    o = oracle.Solid(sc, "port")
+    noisy = [oracle.Solid(perturbed(sc, s, eps=1e-13), "port") for s in (1, 2, 3)]
+    bt = fem_lib.Batch([scenes.cantilever_160(), sc], precision=fem_lib.FEM_PRECISION_FP64)
+    for k in range(steps):
+        so = o.step()
+        for n in noisy:
+            n.step()
+        bt.step(1)
+        st = bt.stats(1)
+        assert st["status"] == 0 and st["nr_iterations"] == so["nr_iters"], (k, st, so)
+    xo, vo = o.state()
+    xg, vg = bt.state(1)
+    fx = max(rel(n.state()[0], xo) for n in noisy)
+    fv = max(rel(n.state()[1], vo) for n in noisy)
+    check_bar("fp64 batch FIE+DAPD+C_LCM+MINRES", "x", rel(xg, xo), TOL, fx, bar_cap(sc))
+    check_bar("fp64 batch FIE+DAPD+C_LCM+MINRES", "v", rel(vg, vo), TOL, fv, bar_cap(sc))
