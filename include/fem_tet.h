@@ -468,7 +468,7 @@ int fem_batch_set_slice(fem_batch b, uint32_t max_iterations);
  * recomputes the potential energy only, and fem_batch_get_stats then reports
  * the solver iterations and iterate count since the last nr_prestep. Steps
  * (fem_batch_step*) are refused between nr_init and nr_end, and the phases
- * under an iteration budget. */
+ * under an iteration budget or with fem_batch_options.persistent_loop. */
 int fem_batch_nr_init(fem_batch b, double dt);
 int fem_batch_nr_prestep(fem_batch b, double dt);
 int fem_batch_nr_midstep(fem_batch b, double dt);

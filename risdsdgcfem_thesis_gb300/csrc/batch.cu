@@ -1606,6 +1606,7 @@ int lock_check(fem_batch b, double dt, bool opened)
     if (int e = check_ready(b)) return e;
     if (!(dt >= 0) || !std::isfinite(dt)) return batch_fail(FEM_E_ARG, "dt must be finite and >= 0");
     if (b->slice_budget) return batch_fail(FEM_E_ARG, "the lock-step's solves run whole: no iteration budget");
+    if (b->opt.persistent_loop) return batch_fail(FEM_E_ARG, "the lock-step runs with the kernel-per-phase CG loop");
     if (opened && !b->lock_open) return batch_fail(FEM_E_ARG, "fem_batch_nr_init must come first");
     return FEM_OK;
 }
