@@ -301,3 +301,22 @@ def test_fp64_batch_fie_with_every_alternative_matches_oracle(fem_lib, oracle):
     fv = max(rel(n.state()[1], vo) for n in noisy)
     check_bar("fp64 batch FIE+DAPD+C_LCM+MINRES", "x", rel(xg, xo), TOL, fx, bar_cap(sc))
     check_bar("fp64 batch FIE+DAPD+C_LCM+MINRES", "v", rel(vg, vo), TOL, fv, bar_cap(sc))
+
+
+def test_fie_batch_with_a_mesh_left_out(fem_lib):
+    """fem_batch_set_active over an FIE batch: the mesh left out keeps its
+    state, the other steps as in a batch of its own (same bits)."""
+    cant = dataclasses.replace(scenes.cantilever_160(), integrator=fem_lib.FEM_INTEGRATOR_FIE_DX)
+    block = _block_scene()
+    bt = fem_lib.Batch([cant, block], precision=fem_lib.FEM_PRECISION_FP64)
+    x1, v1 = bt.state(1)
+    bt.set_active(np.array([1, 0], np.uint8))
+    bt.step(3)
+    xb, vb = bt.state(1)
+    assert np.array_equal(xb, x1) and np.array_equal(vb, v1)
+    alone = fem_lib.Batch([cant], precision=fem_lib.FEM_PRECISION_FP64)
+    alone.step(3)
+    xa, va = alone.state(0)
+    x0, v0 = bt.state(0)
+    assert np.array_equal(xa, x0) and np.array_equal(va, v0)
+    assert bt.stats(0)["nr_iterations"] == alone.stats(0)["nr_iterations"]

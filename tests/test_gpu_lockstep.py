@@ -164,3 +164,24 @@ def test_batch_phases_keep_their_order(fem_lib):
     assert e.value.code == fem_lib.FEM_E_ARG
     bt.nr_phase("end", 1.0 / 60.0)
     bt.step(1)
+
+
+def test_batch_lock_step_leaves_out_inactive_solids(fem_lib):
+    """The lock-step's phases act on the solids taking part
+    (fem_batch_set_active value 1): a solid left out keeps its state, the
+    others step as in a batch of their own."""
+    from test_oracle_lockstep import lock_scenes
+    scs = lock_scenes()
+    dt = scs[0].dt
+    bt = fem_lib.Batch(scs, precision=fem_lib.FEM_PRECISION_FP64)
+    x1, v1 = bt.state(1)
+    bt.set_active(np.array([1, 0, 1], np.uint8))
+    bt.multi_step(dt, 2)
+    xb, vb = bt.state(1)
+    assert np.array_equal(xb, x1) and np.array_equal(vb, v1)
+    pair = fem_lib.Batch([scs[0], scs[2]], precision=fem_lib.FEM_PRECISION_FP64)
+    pair.multi_step(dt, 2)
+    for i, j in ((0, 0), (2, 1)):
+        xa, va = pair.state(j)
+        xg, vg = bt.state(i)
+        assert np.array_equal(xa, xg) and np.array_equal(va, vg), i
