@@ -419,6 +419,22 @@ int fem_batch_info(fem_batch b, uint32_t* meshes, uint64_t* nodes, uint64_t* tet
                    uint64_t* device_bytes);
 int fem_batch_set_knc_targets(fem_batch b, uint32_t mesh, const double* targets);
 int fem_batch_set_state(fem_batch b, uint32_t mesh, const double* x, const double* v);
+/* Replaces: Solid3D::SetParams / SetParamsExtra on one solid of an aggregate
+ * (bs/Solid3D.h:96,150; LeafDSH_Solid3D_FEM.cpp:380-492) -- as
+ * fem_solid_set_params, between steps, for mesh `mesh` of the batch: every
+ * field may change except precision (the batch's). The mesh's constants
+ * become those of a batch built with these parameters; a new
+ * young_modulus or poisson_ratio re-bakes its elements from those scalar
+ * values, replacing per-element ones; switching to DAPD starts it from the
+ * mesh's current positions with no direction of collapse; buffers a new
+ * method needs are allocated and the step graph is captured anew. On the
+ * mixed path a P-K material takes its Lame pair from the element data, so
+ * a mesh built with per-element E or nu whose data were re-baked for a P-K
+ * material cannot return to C_WRP without new scalar values (FEM_E_ARG). The
+ * batch's restrictions hold (C_CCM only in FP64 batches, the persistent
+ * loop's, no FIE under an iteration budget); FEM_E_ARG while a lock-step is
+ * open. */
+int fem_batch_set_params(fem_batch b, uint32_t mesh, const fem_params* params);
 int fem_batch_get_state(fem_batch b, uint32_t mesh, double* x, double* v);
 /* The rotations (T*9, row-major, the caller's element order; the mixed path's
  * FP32 rotations widened to double) and det F (T) of mesh `mesh` as of its

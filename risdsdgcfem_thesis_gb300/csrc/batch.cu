@@ -161,6 +161,9 @@ struct fem_batch_s {
     Dev<double> xn, vn;                  // FIE meshes: x^n, v^n of the step (lock-step: x_k, v_k)
     // the multi-solid Newton lock-step (fem_batch_nr_*)
     std::vector<double> ray0, ray1;      // per mesh: the Rayleigh coefficients a0, a1
+    std::vector<double> vol_total;       // per mesh: rest volume summed in the reference's element order
+    std::vector<uint8_t> elem_mat;       // per mesh: per-element E or nu were given (and not replaced since)
+    std::vector<uint8_t> mat_scalar;     // per mesh: its element data hold values baked from the scalar E, nu
     Dev<MeshConsts> mc_lock;             // the meshes' constants with the lock-step's factors
     double lock_dt = -1.0;               // dt of mc_lock (-1: none yet)
     bool lock = false;                   // views use mc_lock and the lock-step's branches
@@ -317,6 +320,74 @@ std::vector<unsigned char> as_bytes(const std::vector<double>& src)
     S* o = reinterpret_cast<S*>(out.data());
     for (size_t i = 0; i < src.size(); i++) o[i] = (S)src[i];
     return out;
+}
+
+// The parameter-dependent constants of a mesh from its params, its total
+// rest volume (summed in the reference's element order) and node count:
+// node mass (RebuildMass), Rayleigh coefficients (RebuildRayleighCoeffsFrom
+// Freqs), the system factors of the integrator (Step_QuasiImplicitEuler_v,
+// Step_FullyImplicitEuler_dx), tolerances and the method settings. The
+// structural fields of c (ranges of nodes, elements, tiles, chunks,
+// constraints) are left as they are; ray receives a0, a1.
+void param_consts(MeshConsts& c, const fem_params& p, double acc_total_volume, uint32_t N, bool fp64, double* ray)
+{
+    const double total_mass = p.density * acc_total_volume;
+    const double mass_per_node = total_mass / N;
+    const double inv_mass = (double)1.0f / mass_per_node;
+    {
+        const double f1 = (double)0.1f, f2 = (double)10000.0f;
+        const double o00 = 1.0 / f1, o01 = f1, o10 = 1.0 / f2, o11 = f2;
+        const double inv_det = 1.0 / (o00 * o11 - o10 * o01);
+        const double i00 = inv_det * o11, i01 = -inv_det * o01, i10 = -inv_det * o10, i11 = inv_det * o00;
+        const double z = 2 * p.damping_ratio;
+        double a0 = 0, a1 = 0;
+        a0 += i00 * z; a0 += i01 * z;
+        a1 += i10 * z; a1 += i11 * z;
+        ray[0] = a0;
+        ray[1] = a1;
+    }
+    c.dt = p.fixed_dt;
+    c.inv_dt = 1.0 / p.fixed_dt;
+    c.mass = 1.0 / inv_mass;
+    c.factor_M = 1.0 + c.dt * ray[0];
+    c.factor_K = c.dt * c.dt + c.dt * ray[1];
+    c.integrator = p.integrator;
+    c.nr_max_iter = p.nr_max_iter;
+    c.nr_abs_eps = p.nr_abs_epsilon;
+    if (p.integrator != FEM_INTEGRATOR_QIE_V) {
+        // Step_FullyImplicitEuler_dx's system (LeafDSH_Solid3D_FEM.cpp:
+        // 1357-1411): A = (1/h^2 + a0/h) M + (1 + a1/h) K; the
+        // quasi-static variant drops every 1/h term
+        const bool quasi = p.integrator == FEM_INTEGRATOR_FIE_DX_QUASISTATIC;
+        c.dt = quasi ? 0.0 : p.fixed_dt;
+        c.inv_dt = quasi ? 0.0 : 1.0 / p.fixed_dt;
+        c.factor_M = c.inv_dt * c.inv_dt + c.inv_dt * ray[0];
+        c.factor_K = 1.0 + c.inv_dt * ray[1];
+    }
+    for (int a = 0; a < 3; a++) c.gravity[a] = p.gravity[a];
+    c.density = p.density;
+    c.rel_eps_sq = p.ls_rel_epsilon * p.ls_rel_epsilon;
+    c.abs_eps_sq = p.ls_abs_epsilon * p.ls_abs_epsilon;
+    c.degenerate_det_F = p.degenerate_det_F;
+    c.rot_check = (float)p.rotation_check;
+    c.rot_fp32 = p.rotation_fp32 ? 1u : 0u;
+    c.rotation = p.rotation;
+    c.material = p.material;
+    c.ecie_k = (double)(float)p.ecie_k_factor;  // float32 in the reference's Params
+    // the element set's Lame pair (from its Params, TetrahedronElementSet3.cpp:143-148)
+    c.lame_mu = 0.5 * p.young_modulus / (1 + p.poisson_ratio);
+    c.lame_lambda = p.young_modulus * p.poisson_ratio / ((1.0 + p.poisson_ratio) * (1.0 - 2.0 * p.poisson_ratio));
+    // the reference's DAPD factors are float (ms::fem::Params)
+    c.dapd_thr = p.dapd_threshold_det_F;
+    c.dapd_fL = (double)(float)p.dapd_l_factor;
+    c.dapd_fNL = (double)(float)p.dapd_nl_factor;
+    c.dapd_eNL = (double)(float)p.dapd_nl_exponent;
+    c.solver = p.ls_solver;
+    c.refresh_drop_sq = fp64 ? 0.0 : p.refresh_drop * p.refresh_drop;
+    c.max_iter = p.ls_max_iter;
+    c.refresh_every = fp64 ? 0u : p.refresh_every;
+    c.fK_f = (float)c.factor_K;
+    c.mfm_f = (float)(c.mass * c.factor_M);
 }
 
 // Adds a conditional node (IF or WHILE on `h`) after the current capture
@@ -631,14 +702,9 @@ int fem_batch_create(const fem_batch_options* opt, fem_batch* out)
     return FEM_OK;
 }
 
-int fem_batch_add_mesh(fem_batch b, const double* rest, uint32_t N, const uint32_t* tets, uint32_t T,
-                       const fem_params* p, const double* young_per_elem, const double* poisson_per_elem,
-                       uint32_t* mesh_index)
+// The parameters a batch takes for a mesh (either precision unless said).
+static int check_mesh_params(fem_batch b, const fem_params* p)
 {
-    if (!b) return batch_fail(FEM_E_ARG, "null batch");
-    if (b->finalized) return batch_fail(FEM_E_ARG, "batch already finalized");
-    if (!rest || !tets || !p) return batch_fail(FEM_E_ARG, "null rest/tets/params");
-    if (N == 0 || T == 0) return batch_fail(FEM_E_ARG, "empty mesh (N=%u, T=%u)", N, T);
     if (!(p->fixed_dt > 0)) return batch_fail(FEM_E_ARG, "fixed_dt must be > 0");
     if (p->integrator != FEM_INTEGRATOR_QIE_V && p->integrator != FEM_INTEGRATOR_FIE_DX &&
         p->integrator != FEM_INTEGRATOR_FIE_DX_QUASISTATIC)
@@ -665,6 +731,18 @@ int fem_batch_add_mesh(fem_batch b, const double* rest, uint32_t N, const uint32
         return batch_fail(FEM_E_ARG, "ecie_k_factor must be finite");
     if (p->material != FEM_MATERIAL_C_WRP && b->opt.persistent_loop)
         return batch_fail(FEM_E_ARG, "the persistent loop takes C_WRP meshes only");
+    return FEM_OK;
+}
+
+int fem_batch_add_mesh(fem_batch b, const double* rest, uint32_t N, const uint32_t* tets, uint32_t T,
+                       const fem_params* p, const double* young_per_elem, const double* poisson_per_elem,
+                       uint32_t* mesh_index)
+{
+    if (!b) return batch_fail(FEM_E_ARG, "null batch");
+    if (b->finalized) return batch_fail(FEM_E_ARG, "batch already finalized");
+    if (!rest || !tets || !p) return batch_fail(FEM_E_ARG, "null rest/tets/params");
+    if (N == 0 || T == 0) return batch_fail(FEM_E_ARG, "empty mesh (N=%u, T=%u)", N, T);
+    if (int e = check_mesh_params(b, p)) return e;
     for (size_t i = 0; i < 4 * (size_t)T; i++)
         if (tets[i] >= N) return batch_fail(FEM_E_INDEX, "tet %zu names node %u >= N=%u", i / 4, tets[i], N);
     HostMesh m;
@@ -712,6 +790,9 @@ int fem_batch_finalize(fem_batch b)
     std::vector<MeshConsts> mcs(b->M);
     b->ray0.clear();
     b->ray1.clear();
+    b->vol_total.clear();
+    b->elem_mat.clear();
+    b->mat_scalar.clear();
     std::vector<int4> gtets;
     std::vector<double> vol, rest_all;
     std::vector<uchar4> lconn;
@@ -787,9 +868,11 @@ int fem_batch_finalize(fem_batch b)
             double Di[9];
             inverse3(D, Di);
             const double V = vol_orig[e];
-            // C_LCM takes the set's scalar E and nu (per-element values would
-            // only re-bake K0, which it does not use)
-            const bool scalar_mat = p.material != FEM_MATERIAL_C_WRP;
+            // the mixed path's P-K products take V lambda and V mu from the
+            // element data: from the set's scalar E and nu (per-element
+            // values would only re-bake K0, which they do not use; the FP64
+            // products take V, mu and lambda directly)
+            const bool scalar_mat = !fp64 && p.material != FEM_MATERIAL_C_WRP;
             const double E = (hm.E.empty() || scalar_mat) ? p.young_modulus : hm.E[e];
             const double nu = (hm.nu.empty() || scalar_mat) ? p.poisson_ratio : hm.nu[e];
             const double a = E / ((1.0 + nu) * (1.0 - 2.0 * nu));
@@ -924,72 +1007,19 @@ int fem_batch_finalize(fem_batch b)
             chunks.push_back(ch);
         }
         c.nchunks = (uint32_t)chunks.size() - c.chunk0;
-        // constants (RebuildMass, RebuildRayleighCoeffsFromFreqs, Step_QuasiImplicitEuler_v)
-        const double total_mass = p.density * acc_total_volume;
-        const double mass_per_node = total_mass / N;
-        const double inv_mass = (double)1.0f / mass_per_node;
         double ray[2];
-        {
-            const double f1 = (double)0.1f, f2 = (double)10000.0f;
-            const double o00 = 1.0 / f1, o01 = f1, o10 = 1.0 / f2, o11 = f2;
-            const double inv_det = 1.0 / (o00 * o11 - o10 * o01);
-            const double i00 = inv_det * o11, i01 = -inv_det * o01, i10 = -inv_det * o10, i11 = inv_det * o00;
-            const double z = 2 * p.damping_ratio;
-            double a0 = 0, a1 = 0;
-            a0 += i00 * z; a0 += i01 * z;
-            a1 += i10 * z; a1 += i11 * z;
-            ray[0] = a0;
-            ray[1] = a1;
-        }
+        param_consts(c, p, acc_total_volume, N, fp64, ray);
         b->ray0.push_back(ray[0]);
         b->ray1.push_back(ray[1]);
-        c.dt = p.fixed_dt;
-        c.inv_dt = 1.0 / p.fixed_dt;
-        c.mass = 1.0 / inv_mass;
-        c.factor_M = 1.0 + c.dt * ray[0];
-        c.factor_K = c.dt * c.dt + c.dt * ray[1];
-        c.integrator = p.integrator;
-        c.nr_max_iter = p.nr_max_iter;
-        c.nr_abs_eps = p.nr_abs_epsilon;
-        if (p.integrator != FEM_INTEGRATOR_QIE_V) {
-            // Step_FullyImplicitEuler_dx's system (LeafDSH_Solid3D_FEM.cpp:
-            // 1357-1411): A = (1/h^2 + a0/h) M + (1 + a1/h) K; the
-            // quasi-static variant drops every 1/h term
-            b->any_fie = true;
-            const bool quasi = p.integrator == FEM_INTEGRATOR_FIE_DX_QUASISTATIC;
-            c.dt = quasi ? 0.0 : p.fixed_dt;
-            c.inv_dt = quasi ? 0.0 : 1.0 / p.fixed_dt;
-            c.factor_M = c.inv_dt * c.inv_dt + c.inv_dt * ray[0];
-            c.factor_K = 1.0 + c.inv_dt * ray[1];
-        }
-        for (int a = 0; a < 3; a++) c.gravity[a] = p.gravity[a];
-        c.density = p.density;
-        c.rel_eps_sq = p.ls_rel_epsilon * p.ls_rel_epsilon;
-        c.abs_eps_sq = p.ls_abs_epsilon * p.ls_abs_epsilon;
-        c.degenerate_det_F = p.degenerate_det_F;
-        c.rot_check = (float)p.rotation_check;
-        c.rot_fp32 = p.rotation_fp32 ? 1u : 0u;
-        c.rotation = p.rotation;
-        c.material = p.material;
-        c.ecie_k = (double)(float)p.ecie_k_factor;  // float32 in the reference's Params
-        // the element set's Lame pair (from its Params, TetrahedronElementSet3.cpp:143-148)
-        c.lame_mu = 0.5 * p.young_modulus / (1 + p.poisson_ratio);
-        c.lame_lambda = p.young_modulus * p.poisson_ratio / ((1.0 + p.poisson_ratio) * (1.0 - 2.0 * p.poisson_ratio));
+        b->vol_total.push_back(acc_total_volume);
+        const bool given = !hm.E.empty() || !hm.nu.empty();
+        b->elem_mat.push_back(given ? 1u : 0u);
+        b->mat_scalar.push_back(!given || (!fp64 && p.material != FEM_MATERIAL_C_WRP) ? 1u : 0u);
+        if (p.integrator != FEM_INTEGRATOR_QIE_V) b->any_fie = true;
         if (c.material != kTileMaterialWrp) b->any_lcm = true;
         if (c.material == kTileMaterialLcmh) b->any_lcmh = true;
-        // the reference's DAPD factors are float (ms::fem::Params)
-        c.dapd_thr = p.dapd_threshold_det_F;
-        c.dapd_fL = (double)(float)p.dapd_l_factor;
-        c.dapd_fNL = (double)(float)p.dapd_nl_factor;
-        c.dapd_eNL = (double)(float)p.dapd_nl_exponent;
         if (p.rotation == FEM_ROTATION_DAPD) b->any_dapd = true;
-        c.solver = p.ls_solver;
         if (p.ls_solver == FEM_LS_MINRES) b->any_minres = true;
-        c.refresh_drop_sq = fp64 ? 0.0 : p.refresh_drop * p.refresh_drop;
-        c.max_iter = p.ls_max_iter;
-        c.refresh_every = fp64 ? 0u : p.refresh_every;
-        c.fK_f = (float)c.factor_K;
-        c.mfm_f = (float)(c.mass * c.factor_M);
         c.node0 = (uint32_t)node0;
         c.N = N;
         c.elem0 = (uint32_t)elem0;
@@ -1409,6 +1439,112 @@ int fem_batch_set_dapd_state(fem_batch b, uint32_t mesh, const double* prev_x, c
         BCK(cudaMemcpyAsync(b->doc.p + c.elem0, tmp.data(), sizeof(uchar2) * c.T, cudaMemcpyHostToDevice, b->stream));
         BCK(cudaStreamSynchronize(b->stream));
     }
+    return FEM_OK;
+}
+
+int fem_batch_set_params(fem_batch b, uint32_t mesh, const fem_params* params)
+{
+    if (int e = check_ready(b)) return e;
+    if (mesh >= b->M || !params) return batch_fail(FEM_E_ARG, "bad mesh index or null params");
+    if (int e = check_mesh_params(b, params)) return e;
+    if (b->lock_open) return batch_fail(FEM_E_ARG, "a lock-step is open: fem_batch_nr_end first");
+    if (params->integrator != FEM_INTEGRATOR_QIE_V && b->slice_budget)
+        return batch_fail(FEM_E_ARG, "an FIE mesh in a batch with an iteration budget");
+    const bool fp64 = b->opt.precision == FEM_PRECISION_FP64;
+    const fem_params old = b->meshes[mesh].p;
+    const bool pk_new = params->material != FEM_MATERIAL_C_WRP;
+    const bool en_changed = params->young_modulus != old.young_modulus || params->poisson_ratio != old.poisson_ratio;
+    // the mixed path's P-K products take the element data's V lambda and V
+    // mu from the scalar E and nu: a mesh built with per-element values
+    // cannot go back to them from a P-K material
+    if (!fp64 && !pk_new && !en_changed && b->elem_mat[mesh] && b->mat_scalar[mesh])
+        return batch_fail(FEM_E_ARG, "mesh %u: its per-element E, nu were replaced by the scalar ones for a P-K "
+                                     "material", mesh);
+    cudaStream_t s = b->stream;
+    BCK(cudaStreamSynchronize(s));
+    const size_t n3 = 3 * (size_t)b->Ntot;
+    const size_t SB = b->S_size();
+    MeshConsts c = b->mc_host[mesh];
+    // buffers the new methods need (kept when a method is switched off)
+    if (params->integrator != FEM_INTEGRATOR_QIE_V && !b->xn.p) {
+        BCK(b->xn.alloc(n3));
+        BCK(b->vn.alloc(n3));
+    }
+    if ((params->integrator != FEM_INTEGRATOR_QIE_V || params->ls_solver == FEM_LS_MINRES) && !b->cpart_b.p)
+        BCK(b->cpart_b.alloc(b->nchunks));
+    if (params->ls_solver == FEM_LS_MINRES && !b->mr_p_s.p) {
+        BCK(b->mr_p_s.alloc(n3 * SB));
+        BCK(b->mr_p0_s.alloc(n3 * SB));
+        BCK(cudaMemsetAsync(b->mr_p_s.p, 0, n3 * SB, s));
+        BCK(cudaMemsetAsync(b->mr_p0_s.p, 0, n3 * SB, s));
+    }
+    if (pk_new && !b->Fe.p) {
+        BCK(b->Fe.alloc(9 * (size_t)b->Ttot));
+        BCK(cudaMemsetAsync(b->Fe.p, 0, sizeof(double) * 9 * (size_t)b->Ttot, s));
+    }
+    if (params->material == FEM_MATERIAL_C_LCMH && !fp64 && !b->lcmh_w.p) {
+        BCK(b->lcmh_w.alloc(b->Ttot));
+        BCK(cudaMemsetAsync(b->lcmh_w.p, 0, sizeof(float) * (size_t)b->Ttot, s));
+    }
+    if (params->rotation == FEM_ROTATION_DAPD && old.rotation != FEM_ROTATION_DAPD) {
+        // DAPD from here on: the mesh's previous positions start at its
+        // current ones and none of its elements has a direction of collapse
+        // (as a solid created with DAPD, TetrahedronElementSet3.cpp:190-209)
+        if (!b->prev_x.p) {
+            BCK(b->prev_x.alloc(n3));
+            BCK(cudaMemcpyAsync(b->prev_x.p, b->x.p, sizeof(double) * n3, cudaMemcpyDeviceToDevice, s));
+        } else {
+            BCK(cudaMemcpyAsync(b->prev_x.p + 3 * (size_t)c.node0, b->x.p + 3 * (size_t)c.node0,
+                                sizeof(double) * 3 * (size_t)c.N, cudaMemcpyDeviceToDevice, s));
+        }
+        const std::vector<uchar2> none(b->doc.p ? c.T : b->Ttot, make_uchar2(3, 0));
+        if (!b->doc.p) {
+            BCK(b->doc.alloc(b->Ttot));
+            BCK(cudaMemcpyAsync(b->doc.p, none.data(), sizeof(uchar2) * b->Ttot, cudaMemcpyHostToDevice, s));
+        } else {
+            BCK(cudaMemcpyAsync(b->doc.p + c.elem0, none.data(), sizeof(uchar2) * c.T, cudaMemcpyHostToDevice, s));
+        }
+        BCK(cudaStreamSynchronize(s));
+    }
+    if (params->integrator != FEM_INTEGRATOR_QIE_V) b->any_fie = true;
+    if (params->ls_solver == FEM_LS_MINRES) b->any_minres = true;
+    if (pk_new) b->any_lcm = true;
+    if (params->material == FEM_MATERIAL_C_LCMH) b->any_lcmh = true;
+    if (params->rotation == FEM_ROTATION_DAPD) b->any_dapd = true;
+    // the constants (node mass, Rayleigh coefficients, system factors,
+    // tolerances, methods), as a batch built with these parameters has them
+    double ray[2];
+    param_consts(c, *params, b->vol_total[mesh], c.N, fp64, ray);
+    b->ray0[mesh] = ray[0];
+    b->ray1[mesh] = ray[1];
+    b->mc_host[mesh] = c;
+    BCK(b->mc.upload(b->mc_host, s));
+    // element data: re-baked from the scalar E and nu when they change (as
+    // EditableTetrahedronElementSet3::SetParams does, replacing per-element
+    // values), or when the mixed path's P-K products need them; the tiles
+    // take the mesh's material
+    const bool rebake = en_changed || (!fp64 && pk_new && !b->mat_scalar[mesh]);
+    const double E = params->young_modulus, nu = params->poisson_ratio;
+    const double a = E / ((1.0 + nu) * (1.0 - 2.0 * nu));  // Compute_E (TetrahedronElement3.h:141-156)
+    if (fp64)
+        launch_rebake_mesh(b->view<double>(), c.tile0, c.ntiles, a * (1.0 - nu), a * nu, a * (0.5 - nu),
+                           rebake ? 1 : 0, (uint16_t)params->material, s);
+    else
+        launch_rebake_mesh(b->view<float>(), c.tile0, c.ntiles, a * (1.0 - nu), a * nu, a * (0.5 - nu),
+                           rebake ? 1 : 0, (uint16_t)params->material, s);
+    if (rebake) b->mat_scalar[mesh] = 1;
+    if (en_changed) b->elem_mat[mesh] = 0;  // replaced by the scalar values
+    if (!fp64) launch_blob_factors(b->view<float>(), s);
+    b->meshes[mesh].p = *params;
+    b->lock_dt = -1.0;  // the lock-step's constants are rebuilt at its next phase
+    BCK(cudaGetLastError());
+    BCK(cudaStreamSynchronize(s));
+    // the step graph holds the forms the batch's methods need: capture anew
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    b->exec = nullptr;
+    b->graph = nullptr;
+    if (b->opt.use_graph) return build_graph(b);
     return FEM_OK;
 }
 

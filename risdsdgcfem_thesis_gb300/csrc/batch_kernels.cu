@@ -1330,6 +1330,53 @@ void BatchLaunch<S>::reset_counts(const BatchView<S>& b, const LoopSync& ls, cud
     launch_counter()++;
 }
 
+// One mesh's element material triple re-baked from scalar values (k0, k1,
+// k2 = a (1 - nu), a nu, a (0.5 - nu), formed on the host):
+// mat[c][e] = V_e k_c, rounded to the path's type, and on the mixed path the
+// tile blobs' V lambda and V mu -- the values a batch built with those
+// scalars holds (EditableTetrahedronElementSet3::SetParams,
+// TetrahedronElementSet3.cpp:2168-2200). The mesh's tiles and element
+// range; the material of its tiles set to `material`.
+template <typename S>
+__global__ void k_rebake_mesh(BatchView<S> b, uint32_t tile0, uint32_t ntiles, double k0, double k1, double k2,
+                              int rebake, uint16_t material)
+{
+    S* mat = const_cast<S*>(b.mat);
+    const size_t T = b.Ttot;
+    for (uint32_t i = blockIdx.x; i < ntiles; i += gridDim.x) {
+        const uint32_t t = tile0 + i;
+        const TileMeta tm = b.tiles[t];
+        if (threadIdx.x == 0) const_cast<TileMeta*>(b.tiles)[t].material = material;
+        if (!rebake || threadIdx.x >= tm.ne) continue;
+        const size_t e = tm.e0 + threadIdx.x;
+        const double V = b.vol[e];
+        const double m0 = V * k0, m1 = V * k1, m2 = V * k2;
+        mat[e] = (S)m0;
+        mat[T + e] = (S)m1;
+        mat[2 * T + e] = (S)m2;
+        if (b.blob) {
+            unsigned char* base = b.blob + 16ull * b.blob_off16[t];
+            const uint32_t ne4 = blob_ne4(tm.ne);
+            *reinterpret_cast<float*>(base + blob_comp_off(18, threadIdx.x, ne4)) = (float)m1;
+            *reinterpret_cast<float*>(base + blob_comp_off(19, threadIdx.x, ne4)) = (float)m2;
+        }
+    }
+}
+
+template <typename S>
+void launch_rebake_mesh(const BatchView<S>& b, uint32_t tile0, uint32_t ntiles, double k0, double k1, double k2,
+                        int rebake, uint16_t material, cudaStream_t s)
+{
+    if (!ntiles) return;
+    k_rebake_mesh<S><<<ntiles < 1216u ? ntiles : 1216u, kTileElems, 0, s>>>(b, tile0, ntiles, k0, k1, k2, rebake,
+                                                                          material);
+    launch_counter()++;
+}
+template void launch_rebake_mesh<double>(const BatchView<double>&, uint32_t, uint32_t, double, double, double, int,
+                                         uint16_t, cudaStream_t);
+template void launch_rebake_mesh<float>(const BatchView<float>&, uint32_t, uint32_t, double, double, double, int,
+                                        uint16_t, cudaStream_t);
+
 __global__ void k_permute(const uint32_t* __restrict__ perm, uint64_t n, const double* __restrict__ src,
                           double* __restrict__ dst, int to_batch)
 {

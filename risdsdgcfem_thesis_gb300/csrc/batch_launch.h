@@ -36,6 +36,12 @@ void launch_node_update_fused(const BatchView<float>& b, const float* part, cons
                               const double* part64, const double* bv, double* y, float* r, float* d,
                               float2* cshare, const LoopSync& ls, cudaStream_t s);
 
+// One mesh's element material triple re-baked from scalar values (rebake;
+// on the mixed path also its tile blobs' copies) and its tiles' material.
+template <typename S>
+void launch_rebake_mesh(const BatchView<S>& b, uint32_t tile0, uint32_t ntiles, double k0, double k1, double k2,
+                        int rebake, uint16_t material, cudaStream_t s);
+
 // Mixed path: rewrite each tile blob's FP32 system factors from b.mc.
 void launch_blob_factors(const BatchView<float>& b, cudaStream_t s);
 

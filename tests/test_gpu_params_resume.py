@@ -129,3 +129,63 @@ def test_dapd_state_rejects_malformed_directions(fem_lib):
     plain = fem_lib.Solid(scenes.compressed_cube(n=3, steps=5, ratio=0.5))
     with pytest.raises(fem_lib.FemError):
         plain.dapd_state()
+
+
+# ---- fem_batch_set_params: one solid of an aggregate changes its parameters
+
+def _batch_fresh_like(fem_lib, scs, src, precision):
+    """A fresh batch of scenes `scs` given the states of batch `src`."""
+    fresh = fem_lib.Batch(scs, precision=precision, chunk_nodes=256)
+    for i in range(len(scs)):
+        x, v = src.state(i)
+        fresh.set_state(i, x, v)
+    fresh.step_index = src.step_index
+    return fresh
+
+
+def _batch_same(a, b, i):
+    xa, va = a.state(i)
+    xb, vb = b.state(i)
+    return np.array_equal(xa, xb) and np.array_equal(va, vb)
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("change", ["scalars", "young", "material", "rotation", "solver", "integrator"])
+def test_batch_set_params_equals_a_batch_built_with_them(fem_lib, precision, change):
+    """A mesh of a batch whose parameters change between steps steps as in a
+    batch built with the new parameters and given the same states (the same
+    bits), in either precision; the other mesh is untouched by the change."""
+    other = scenes.cantilever_160()
+    sc = scenes.large_block(n=5)  # per-element E and nu at creation
+    kw = {"scalars": dict(rel_eps=1e-8, max_iter=300, gravity=(0.5, 0.0, -9.81), damping_ratio=0.3, dt=1.0 / 120.0,
+                          density=1500.0),
+          "young": dict(young=3e5, poisson=0.33, young_per_elem=None, poisson_per_elem=None),
+          "material": dict(material=1),
+          "rotation": dict(rotation=1),
+          "solver": dict(ls_solver=1),
+          "integrator": dict(integrator=1)}[change]
+    sc2 = dataclasses.replace(sc, **kw)
+    bt = fem_lib.Batch([other, sc], precision=precision, chunk_nodes=256)
+    bt.step(3)
+    bt.set_params(1, fem_lib.params_for(sc2, precision))
+    ref = _batch_fresh_like(fem_lib, [other, sc2], bt, precision)
+    bt.step(3)
+    ref.step(3)
+    assert _batch_same(bt, ref, 1) and _batch_same(bt, ref, 0)
+    assert bt.stats(1)["status"] == 0
+
+
+def test_mixed_batch_refuses_a_return_to_per_element_data(fem_lib):
+    """On the mixed path a mesh built with per-element E, nu whose data were
+    re-baked for a P-K material cannot go back to C_WRP without new scalar
+    values; with them it can."""
+    sc = scenes.large_block(n=4)
+    bt = fem_lib.Batch([sc], precision=fem_lib.FEM_PRECISION_MIXED, chunk_nodes=256)
+    bt.set_params(0, fem_lib.params_for(dataclasses.replace(sc, material=1), fem_lib.FEM_PRECISION_MIXED))
+    bt.step(1)
+    with pytest.raises(fem_lib.FemError) as e:
+        bt.set_params(0, fem_lib.params_for(sc, fem_lib.FEM_PRECISION_MIXED))
+    assert e.value.code == fem_lib.FEM_E_ARG
+    bt.set_params(0, fem_lib.params_for(dataclasses.replace(sc, young=2e5), fem_lib.FEM_PRECISION_MIXED))
+    bt.step(1)
+    assert bt.stats(0)["status"] == 0
