@@ -595,6 +595,11 @@ int fem_server_admit(fem_server s, uint32_t* admitted);
 /* Frees a scene with no request pending; a shard's memory is released when
  * its last scene goes. */
 int fem_server_remove_scene(fem_server s, uint32_t scene);
+/* Run-time parameter change of a scene with no request pending or in
+ * flight (fem_batch_set_params on its shard when it is resident); a change
+ * between QIE_V and the FIE integrators, which live in shards of different
+ * kinds, needs the scene removed and added again (FEM_E_ARG). */
+int fem_server_set_params(fem_server s, uint32_t scene, const fem_params* params);
 int fem_server_submit(fem_server s, uint32_t scene, uint64_t tag);
 /* Progress without blocking; writes up to cap completions. */
 int fem_server_pump(fem_server s, fem_server_completion* out, uint32_t cap, uint32_t* n);

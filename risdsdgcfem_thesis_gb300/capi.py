@@ -557,6 +557,7 @@ _BATCH_SIGNATURES = {
     "fem_batch_step_host": (C.c_int, [C.c_void_p, _dp, _dp, C.c_uint32, _dp, _dp]),
     "fem_batch_set_slice": (C.c_int, [C.c_void_p, C.c_uint32]),
     "fem_batch_set_params": (C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p]),
+    "fem_server_set_params": (C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p]),
     "fem_batch_nr_init": (C.c_int, [C.c_void_p, C.c_double]),
     "fem_batch_nr_prestep": (C.c_int, [C.c_void_p, C.c_double]),
     "fem_batch_nr_midstep": (C.c_int, [C.c_void_p, C.c_double]),
@@ -831,6 +832,11 @@ class Server:
         n = C.c_uint32()
         check(self.lib.fem_server_admit(self.h, C.byref(n)))
         return n.value
+
+    def set_params(self, scene, params):
+        """fem_server_set_params: run-time parameter change of a scene with
+        no request pending."""
+        check(self.lib.fem_server_set_params(self.h, scene, C.byref(params)))
 
     def remove(self, scene):
         check(self.lib.fem_server_remove_scene(self.h, scene))

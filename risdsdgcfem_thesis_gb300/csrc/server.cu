@@ -373,6 +373,30 @@ int fem_server_admit(fem_server s, uint32_t* admitted)
     return FEM_OK;
 }
 
+int fem_server_set_params(fem_server s, uint32_t scene, const fem_params* params)
+{
+    if (int e = check_server(s)) return e;
+    if (scene >= s->scenes.size() || !params) return batch_fail(FEM_E_ARG, "bad scene index or null params");
+    Scene& sc = s->scenes[scene];
+    if (sc.state == SCENE_REMOVED) return batch_fail(FEM_E_ARG, "scene %u was removed", scene);
+    if (!sc.queue.empty() || sc.inflight)
+        return batch_fail(FEM_E_ARG, "scene %u has requests pending or in flight", scene);
+    fem_params p = *params;
+    p.precision = s->opt.precision;
+    if (sc.state == SCENE_RESIDENT) {
+        // the shard's batch takes it (its restrictions hold: an FIE scene
+        // in a sliced shard is refused; remove and add it again)
+        const bool newton_old = sc.params.integrator != FEM_INTEGRATOR_QIE_V;
+        const bool newton_new = p.integrator != FEM_INTEGRATOR_QIE_V;
+        if (newton_old != newton_new)
+            return batch_fail(FEM_E_ARG, "scene %u: an integrator change moves it between shard kinds; remove and "
+                                         "add it again", scene);
+        if (int e = fem_batch_set_params(s->shards[sc.shard].b, sc.mesh, &p)) return e;
+    }
+    sc.params = p;
+    return FEM_OK;
+}
+
 int fem_server_remove_scene(fem_server s, uint32_t scene)
 {
     if (int e = check_server(s)) return e;

@@ -123,3 +123,33 @@ def test_server_shards_overlap_on_the_device(fem_lib):
     done = srv.drain()
     assert len(done) == len(pool) and srv.status()["max_busy_shards"] == 4
     srv.close()
+
+
+def test_server_scene_parameter_change_equals_the_batch(fem_lib):
+    """fem_server_set_params on a resident scene between requests: the
+    scene's results are those of a batch whose mesh takes the same change at
+    the same point (the same bits); a change of integrator kind is refused."""
+    import dataclasses
+    sc = scenes.cantilever_160()
+    sc2 = dataclasses.replace(sc, gravity=(0.3, 0.0, -9.81), rel_eps=1e-8, damping_ratio=0.2)
+    srv = fem_lib.Server(precision=fem_lib.FEM_PRECISION_MIXED)
+    sid = srv.add(sc)
+    srv.admit()
+    for k in range(3):
+        srv.submit(sid, k)
+    assert len(srv.drain()) == 3
+    srv.set_params(sid, fem_lib.params_for(sc2, fem_lib.FEM_PRECISION_MIXED))
+    for k in range(3, 6):
+        srv.submit(sid, k)
+    done = srv.drain()
+    assert len(done) == 3 and all(c["status"] == 0 for c in done)
+    bt = fem_lib.Batch([sc], precision=fem_lib.FEM_PRECISION_MIXED, compute_energy=False, chunk_nodes=256)
+    bt.step(3)
+    bt.set_params(0, fem_lib.params_for(sc2, fem_lib.FEM_PRECISION_MIXED))
+    bt.step(3)
+    xs, vs = srv.state(sid)
+    xb, vb = bt.state(0)
+    assert np.array_equal(xs, xb) and np.array_equal(vs, vb)
+    with pytest.raises(fem_lib.FemError) as e:
+        srv.set_params(sid, fem_lib.params_for(dataclasses.replace(sc, integrator=1), fem_lib.FEM_PRECISION_MIXED))
+    assert e.value.code == fem_lib.FEM_E_ARG
