@@ -435,6 +435,8 @@ int fem_batch_set_state(fem_batch b, uint32_t mesh, const double* x, const doubl
  * loop's, no FIE under an iteration budget); FEM_E_ARG while a lock-step is
  * open. */
 int fem_batch_set_params(fem_batch b, uint32_t mesh, const fem_params* params);
+/* The parameters mesh `mesh` steps with (its precision: the batch's). */
+int fem_batch_get_params(fem_batch b, uint32_t mesh, fem_params* params);
 int fem_batch_get_state(fem_batch b, uint32_t mesh, double* x, double* v);
 /* The rotations (T*9, row-major, the caller's element order; the mixed path's
  * FP32 rotations widened to double) and det F (T) of mesh `mesh` as of its

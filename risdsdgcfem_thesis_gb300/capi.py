@@ -557,6 +557,7 @@ _BATCH_SIGNATURES = {
     "fem_batch_step_host": (C.c_int, [C.c_void_p, _dp, _dp, C.c_uint32, _dp, _dp]),
     "fem_batch_set_slice": (C.c_int, [C.c_void_p, C.c_uint32]),
     "fem_batch_set_params": (C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p]),
+    "fem_batch_get_params": (C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p]),
     "fem_server_set_params": (C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p]),
     "fem_batch_nr_init": (C.c_int, [C.c_void_p, C.c_double]),
     "fem_batch_nr_prestep": (C.c_int, [C.c_void_p, C.c_double]),
@@ -736,6 +737,11 @@ class Batch:
         """fem_batch_set_params: mesh i takes new parameters (a FemParams,
         e.g. params_for(scene)) between steps."""
         check(self.lib.fem_batch_set_params(self.h, i, C.byref(params)))
+
+    def get_params(self, i):
+        p = FemParams()
+        check(self.lib.fem_batch_get_params(self.h, i, C.byref(p)))
+        return p
 
     def nr_phase(self, phase, dt):
         """One lock-step phase (init, prestep, midstep, poststep, end;

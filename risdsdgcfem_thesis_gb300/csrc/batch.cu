@@ -1548,6 +1548,15 @@ int fem_batch_set_params(fem_batch b, uint32_t mesh, const fem_params* params)
     return FEM_OK;
 }
 
+int fem_batch_get_params(fem_batch b, uint32_t mesh, fem_params* params)
+{
+    if (!b) return batch_fail(FEM_E_ARG, "null batch");
+    if (mesh >= b->meshes.size() || !params) return batch_fail(FEM_E_ARG, "bad mesh index or null params");
+    *params = b->meshes[mesh].p;
+    params->precision = b->opt.precision;
+    return FEM_OK;
+}
+
 int fem_batch_get_state(fem_batch b, uint32_t mesh, double* x, double* v)
 {
     if (int e = check_ready(b)) return e;

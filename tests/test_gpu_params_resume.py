@@ -173,6 +173,11 @@ def test_batch_set_params_equals_a_batch_built_with_them(fem_lib, precision, cha
     ref.step(3)
     assert _batch_same(bt, ref, 1) and _batch_same(bt, ref, 0)
     assert bt.stats(1)["status"] == 0
+    got = bt.get_params(1)
+    want = fem_lib.params_for(sc2, precision)
+    assert (got.material, got.rotation, got.ls_solver, got.integrator) == \
+        (want.material, want.rotation, want.ls_solver, want.integrator)
+    assert got.fixed_dt == want.fixed_dt and got.young_modulus == want.young_modulus
 
 
 def test_mixed_batch_refuses_a_return_to_per_element_data(fem_lib):
