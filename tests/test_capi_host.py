@@ -104,6 +104,14 @@ def test_create_rejects_empty_and_null(fem_lib):
     lib = fem_lib.load()
     assert lib.fem_solid_step(None, 1, None) == fem_lib.FEM_E_ARG
     assert lib.fem_solid_create(None, 0, None, 0, None, None, None, None) == fem_lib.FEM_E_ARG
+    # batch calls on a null handle answer on the host
+    p = fem_lib.default_params()
+    for fn, args in (("fem_batch_nr_init", (0.01,)), ("fem_batch_nr_prestep", (0.01,)),
+                     ("fem_batch_nr_midstep", (0.01,)), ("fem_batch_nr_poststep", (0.01,)),
+                     ("fem_batch_nr_end", (0.01,)), ("fem_batch_multi_step", (0.01, 1)),
+                     ("fem_batch_set_params", (0, C.byref(p))), ("fem_batch_get_params", (0, C.byref(p))),
+                     ("fem_server_set_params", (0, C.byref(p)))):
+        assert getattr(lib, fn)(None, *args) == fem_lib.FEM_E_ARG, fn
 
 
 def test_create_rejects_bad_dt(fem_lib):
