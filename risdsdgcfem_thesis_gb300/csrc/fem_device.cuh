@@ -199,8 +199,11 @@ enum FinalizeKind {
     // MINRES: init (|r0|^2 = total, |b|^2 from host_sum), alpha, beta + Givens, stats
     FIN_MR_INIT = 7, FIN_MR_ALPHA = 8, FIN_MR_BETA = 9, FIN_MR_STATS = 10
 };
+// set_cond: the kinds that end a solver's loop test (init, alpha, beta and
+// their MINRES forms) also set the step graph's WHILE condition `cond` to
+// "the loop goes on"
 void launch_finalize(int kind, const double* partials, uint32_t count, const StepConsts& c, StepScalars* st,
-                     cudaStream_t s);
+                     cudaStream_t s, cudaGraphConditionalHandle cond = 0, int set_cond = 0);
 
 uint32_t grid_for(uint32_t n);    // grid size of the grid-stride kernels
 uint64_t& launch_counter();       // kernels launched by this library

@@ -706,7 +706,7 @@ __device__ __forceinline__ bool cg_continue(const StepScalars* st)
 }
 
 __global__ void k_finalize(int kind, const double* __restrict__ partials, uint32_t count, StepConsts c,
-                           StepScalars* st)
+                           StepScalars* st, cudaGraphConditionalHandle cond, int set_cond)
 {
     double acc = 0.0;
     for (uint32_t i = threadIdx.x; i < count; i += blockDim.x) acc += partials[i];
@@ -798,6 +798,9 @@ __global__ void k_finalize(int kind, const double* __restrict__ partials, uint32
         st->abs_residual = ::sqrt(st->delta_new);
         break;
     }
+    if (set_cond && (kind == FIN_INIT || kind == FIN_ALPHA || kind == FIN_BETA || kind == FIN_MR_INIT ||
+                     kind == FIN_MR_ALPHA || kind == FIN_MR_BETA))
+        cudaGraphSetConditional(cond, st->done ? 0u : 1u);
 }
 
 // ---- launchers ----
@@ -927,9 +930,9 @@ void launch_gather_sum_fp64(const MeshView<double>& m, double sign, double* f, c
     FEMGB_LAUNCH(k_gather_sum_fp64, grid_for(m.N), m, sign, f);
 }
 void launch_finalize(int kind, const double* partials, uint32_t count, const StepConsts& c, StepScalars* st,
-                     cudaStream_t s)
+                     cudaStream_t s, cudaGraphConditionalHandle cond, int set_cond)
 {
-    k_finalize<<<1, kFinalizeThreads, 0, s>>>(kind, partials, count, c, st);
+    k_finalize<<<1, kFinalizeThreads, 0, s>>>(kind, partials, count, c, st, cond, set_cond);
     launch_counter()++;
 }
 

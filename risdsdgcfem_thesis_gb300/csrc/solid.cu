@@ -17,6 +17,7 @@
 #include "bounds.cuh"
 #include "dapd.cuh"
 #include "fem_device.cuh"
+#include "graph_capture.h"
 
 #include <algorithm>
 #include <cmath>
@@ -143,6 +144,19 @@ struct fem_solid_s {
     // fem_solid_apply_A_noalloc: device address of the static scratch array,
     // looked up at creation (null for solids above FEM_NOALLOC_MAX_TETS)
     double* noalloc_scratch = nullptr;
+    // the QIE_V step as one CUDA graph (its solver loop a WHILE node),
+    // captured at the first step and again after a change of parameters or
+    // constraints; FIE steps stay host-driven (their Newton tests)
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+
+    void drop_graph()
+    {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        exec = nullptr;
+        graph = nullptr;
+    }
 
     MeshView<double> view()
     {
@@ -178,6 +192,7 @@ struct fem_solid_s {
         st.release();
         if (st_host) cudaFreeHost(st_host);
         st_host = nullptr;
+        drop_graph();
         if (stream) cudaStreamDestroy(stream);
         stream = nullptr;
     }
@@ -398,6 +413,73 @@ int ls_solve(fem_solid s, const StepConsts& c, int chunk)
     return s->params.ls_solver == FEM_LS_MINRES ? minres_solve(s, c, chunk) : cg_solve(s, c, chunk);
 }
 
+// The solver of ls_solve enqueued for capture into the step graph: the same
+// kernels in the same order, the loop a WHILE node whose condition the
+// finalisers set (the kernels of an iteration after the loop test failed
+// are no-ops, as in the host-driven loop). The body is captured with
+// s->stream pointing at the body's capture stream.
+cudaError_t ls_solve_capture(fem_solid s, const StepConsts& c, cudaGraph_t top)
+{
+    cudaStream_t st = s->stream;
+    MeshView<double> m = s->view();
+    const uint32_t gN = grid_for(s->N), gV = grid_for(3 * s->N);
+    cudaGraphConditionalHandle cond = 0;
+    cudaError_t e = cudaGraphConditionalHandleCreate(&cond, top, 0, cudaGraphCondAssignDefault);
+    if (e != cudaSuccess) return e;
+    if (s->params.ls_solver != FEM_LS_MINRES) {
+        elem_spmv(s, m, s->y.p, 0);
+        launch_node_residual_fp64(m, c, s->b.p, s->y.p, s->r.p, s->d.p, s->partials.p, st);
+        launch_finalize(FIN_INIT, s->partials.p, gN, c, s->st.p, st, cond, 1);
+        e = capture_conditional(st, cond, cudaGraphCondTypeWhile, [&](cudaStream_t bs, cudaGraph_t) {
+            s->stream = bs;
+            elem_spmv(s, m, s->d.p, 1);
+            launch_node_q_fp64(m, c, s->d.p, s->q.p, s->partials.p, s->st.p, bs);
+            launch_finalize(FIN_ALPHA, s->partials.p, gN, c, s->st.p, bs, cond, 1);
+            launch_node_xr_fp64(s->N, s->y.p, s->r.p, s->d.p, s->q.p, s->partials.p, s->st.p, bs);
+            launch_finalize(FIN_BETA, s->partials.p, gV, c, s->st.p, bs, cond, 1);
+            launch_node_d_fp64(s->N, s->fixed.p, s->d.p, s->r.p, s->st.p, bs);
+            s->stream = st;
+            return cudaGetLastError();
+        });
+        if (e != cudaSuccess) return e;
+        launch_finalize(FIN_STATS, s->partials.p, 0, c, s->st.p, st);
+        return cudaGetLastError();
+    }
+    // MINRES: the host loop rotates v0, v, v1 (period 3) and p, p0
+    // (period 2) between iterations; the body holds six iterations, after
+    // which every buffer is back in its place
+    double *v = s->r.p, *v0 = s->d.p, *v1 = s->q.p, *p = s->mr_p.p, *p0 = s->mr_p0.p;
+    launch_sq_norm_fp64(3 * s->N, s->b.p, s->partials.p, st);
+    launch_finalize(FIN_SUM, s->partials.p, gV, c, s->st.p, st);  // |b|^2
+    elem_spmv(s, m, s->y.p, 0);
+    launch_mr_init_fp64(m, c, s->b.p, s->y.p, v1, s->partials.p, st);
+    launch_finalize(FIN_MR_INIT, s->partials.p, gN, c, s->st.p, st, cond, 1);
+    launch_mr_start_fp64(s->N, v1, v, p, p0, s->st.p, st);
+    e = capture_conditional(st, cond, cudaGraphCondTypeWhile, [&](cudaStream_t bs, cudaGraph_t) {
+        s->stream = bs;
+        for (int i = 0; i < 6; i++) {
+            double* t = v0;  // v0 <- v, v <- v1, v1 <- the old v0 buffer
+            v0 = v;
+            v = v1;
+            v1 = t;
+            elem_spmv(s, m, v, 1);
+            launch_mr_q_fp64(m, c, v, v0, v1, s->partials.p, s->st.p, bs);
+            launch_finalize(FIN_MR_ALPHA, s->partials.p, gN, c, s->st.p, bs, cond, 1);
+            launch_mr_v1_fp64(s->N, v1, v, s->partials.p, s->st.p, bs);
+            launch_finalize(FIN_MR_BETA, s->partials.p, gV, c, s->st.p, bs, cond, 1);
+            launch_mr_update_fp64(s->N, v1, v, p, p0, s->y.p, s->st.p, bs);
+            t = p;  // the new p was written into p0's buffer
+            p = p0;
+            p0 = t;
+        }
+        s->stream = st;
+        return cudaGetLastError();
+    });
+    if (e != cudaSuccess) return e;
+    launch_finalize(FIN_MR_STATS, s->partials.p, 0, c, s->st.p, st);
+    return cudaGetLastError();
+}
+
 // Sum of `count` block partials into StepScalars::host_sum, read on the host.
 int host_sum(fem_solid s, uint32_t count, double* out)
 {
@@ -481,23 +563,62 @@ int step_fie(fem_solid s, int chunk)
     return FEM_OK;
 }
 
-// One FixedStep on the device (no host synchronisation except the per-chunk
-// read of the CG loop flag).
+// One FixedStep's QIE_V pipeline after the opening: f_e, b, constraints,
+// the solve, integration and energies.
+void qie_head(fem_solid s)
+{
+    cudaStream_t st = s->stream;
+    MeshView<double> m = s->view();
+    const StepConsts& c = s->consts;
+    elem_force(s, m, s->x.p, 1, nullptr);
+    launch_node_b_fp64(m, c, s->v.p, s->b.p, s->y.p, st);
+    launch_knc_fp64(s->N, s->knc_count, s->knc_nodes.p, s->knc_targets.p, s->x.p, c, s->b.p, s->y.p, st);
+}
+void qie_tail(fem_solid s)
+{
+    const StepConsts& c = s->consts;
+    launch_integrate_fp64(s->N, c.dt, s->x.p, s->v.p, s->y.p, s->stream);
+    if (s->params.compute_energy) energy(s);
+}
+
+// The QIE_V step as one graph: the opening, the pipeline and the solver's
+// loop on the device.
+int capture_step(fem_solid s)
+{
+    s->drop_graph();
+    cudaStream_t st = s->stream;
+    CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed));
+    cudaGraph_t top = nullptr;
+    cudaStreamCaptureStatus cs;
+    cudaError_t e = cudaStreamGetCaptureInfo(st, &cs, nullptr, &top, nullptr, nullptr, nullptr);
+    int rc = e == cudaSuccess ? open_step(s) : FEM_E_CUDA;
+    if (rc == FEM_OK) {
+        qie_head(s);
+        e = ls_solve_capture(s, s->consts, top);
+        if (e == cudaSuccess) qie_tail(s);
+    }
+    cudaGraph_t g = nullptr;
+    const cudaError_t e2 = cudaStreamEndCapture(st, &g);
+    if (e == cudaSuccess) e = e2;
+    if (rc != FEM_OK || e != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        if (rc != FEM_OK) return rc;
+        return fail(FEM_E_CUDA, "step graph capture: %s", cudaGetErrorString(e));
+    }
+    s->graph = g;
+    CK(cudaGraphInstantiate(&s->exec, g, 0));
+    return FEM_OK;
+}
+
+// One FixedStep on the device: QIE_V as the step graph (no host
+// synchronisation); FIE with its Newton loop on the host.
 int step_once(fem_solid s, int chunk)
 {
     s->lock_stats = false;
     if (s->params.integrator != FEM_INTEGRATOR_QIE_V) return step_fie(s, chunk);
-    cudaStream_t st = s->stream;
-    MeshView<double> m = s->view();
-    const StepConsts& c = s->consts;
-    if (int e = open_step(s)) return e;
-    elem_force(s, m, s->x.p, 1, nullptr);
-    launch_node_b_fp64(m, c, s->v.p, s->b.p, s->y.p, st);
-    launch_knc_fp64(s->N, s->knc_count, s->knc_nodes.p, s->knc_targets.p, s->x.p, c, s->b.p, s->y.p, st);
-    if (int e = ls_solve(s, c, chunk)) return e;
-    launch_integrate_fp64(s->N, c.dt, s->x.p, s->v.p, s->y.p, st);
-    if (s->params.compute_energy) energy(s);
-    CK(cudaGetLastError());
+    if (!s->exec)
+        if (int e = capture_step(s)) return e;
+    CK(cudaGraphLaunch(s->exec, s->stream));
     return FEM_OK;
 }
 void fill_stats(fem_solid s, const StepScalars& h, fem_step_stats* out)
@@ -791,6 +912,7 @@ int fem_solid_get_sizes(fem_solid s, uint32_t* N, uint32_t* T)
 
 int fem_solid_set_knc(fem_solid s, const uint32_t* nodes, const double* targets, uint32_t count)
 {
+    if (s) s->drop_graph();  // the step graph's constraint launch follows the count
     if (int e = check_handle(s)) return e;
     if (count && (!nodes || !targets)) return fail(FEM_E_ARG, "null constraint arrays");
     for (uint32_t k = 0; k < count; k++)
@@ -843,6 +965,7 @@ int fem_solid_set_params(fem_solid s, const fem_params* params)
     if (!params) return fail(FEM_E_ARG, "null params");
     if (int e = check_params(params)) return e;
     CK(cudaStreamSynchronize(s->stream));
+    s->drop_graph();  // the step graph holds the constants and methods by value
     const fem_params old = s->params;
     const size_t n3 = 3 * (size_t)s->N;
     // buffers the new methods need (kept when a method is switched off)
