@@ -705,6 +705,52 @@ __device__ __forceinline__ bool cg_continue(const StepScalars* st)
     return st->delta_new > st->abs_eps_sq && st->delta_new > st->delta_target && st->k < st->max_iter;
 }
 
+// ILSS_CG::Solve's scalar steps (ILSS_CG.h:53-151) on a reduced total: the
+// start, alpha with the breakdown test, beta with the loop test, and the
+// statistics at the end. Shared by the finaliser kernel and the one-block
+// solver below.
+__device__ __forceinline__ void fin_init(StepScalars* st, const StepConsts& c, double total)
+{
+    st->delta_0 = total;
+    st->delta_new = total;
+    st->delta_old = total;
+    st->delta_target = c.rel_eps_sq * total;
+    st->abs_eps_sq = c.abs_eps_sq;
+    st->max_iter = c.max_iter;
+    st->k = 0;
+    st->status = 0;
+    st->alpha = 0.0;
+    st->beta = 0.0;
+    st->done = cg_continue(st) ? 0u : 1u;
+    if (!isfinite(total)) st->status = 3;  // FEM_E_NAN
+}
+__device__ __forceinline__ void fin_alpha(StepScalars* st, double total)
+{
+    if (st->done) return;
+    st->dot_dq = total;
+    if (::fabs(total) < st->abs_eps_sq) {  // breakdown: leave before the update (ILSS_CG.h:97)
+        st->done = 1;
+        return;
+    }
+    st->alpha = st->delta_new / total;
+}
+__device__ __forceinline__ void fin_beta(StepScalars* st, double total)
+{
+    if (st->done) return;
+    st->delta_old = st->delta_new;
+    st->delta_new = total;
+    st->beta = total / st->delta_old;
+    st->k += 1;
+    st->total_iters += 1;
+    st->done = cg_continue(st) ? 0u : 1u;
+    if (!isfinite(total)) st->status = 3;
+}
+__device__ __forceinline__ void fin_stats(StepScalars* st)
+{
+    st->rel_residual = (st->delta_0 > 0) ? ::sqrt(st->delta_new / st->delta_0) : 0.0;
+    st->abs_residual = ::sqrt(st->delta_new);
+}
+
 __global__ void k_finalize(int kind, const double* __restrict__ partials, uint32_t count, StepConsts c,
                            StepScalars* st, cudaGraphConditionalHandle cond, int set_cond)
 {
@@ -714,37 +760,13 @@ __global__ void k_finalize(int kind, const double* __restrict__ partials, uint32
     if (threadIdx.x != 0) return;
     switch (kind) {
     case FIN_INIT:
-        st->delta_0 = total;
-        st->delta_new = total;
-        st->delta_old = total;
-        st->delta_target = c.rel_eps_sq * total;
-        st->abs_eps_sq = c.abs_eps_sq;
-        st->max_iter = c.max_iter;
-        st->k = 0;
-        st->status = 0;
-        st->alpha = 0.0;
-        st->beta = 0.0;
-        st->done = cg_continue(st) ? 0u : 1u;
-        if (!isfinite(total)) st->status = 3;  // FEM_E_NAN
+        fin_init(st, c, total);
         break;
     case FIN_ALPHA:
-        if (st->done) break;
-        st->dot_dq = total;
-        if (::fabs(total) < st->abs_eps_sq) {  // breakdown: leave before the update (ILSS_CG.h:97)
-            st->done = 1;
-            break;
-        }
-        st->alpha = st->delta_new / total;
+        fin_alpha(st, total);
         break;
     case FIN_BETA:
-        if (st->done) break;
-        st->delta_old = st->delta_new;
-        st->delta_new = total;
-        st->beta = total / st->delta_old;
-        st->k += 1;
-        st->total_iters += 1;
-        st->done = cg_continue(st) ? 0u : 1u;
-        if (!isfinite(total)) st->status = 3;
+        fin_beta(st, total);
         break;
     case FIN_ENERGY_E:
         st->elastic_energy = total;
@@ -794,13 +816,120 @@ __global__ void k_finalize(int kind, const double* __restrict__ partials, uint32
         st->abs_residual = ::sqrt(st->mr.norm_r_sq);
         break;
     case FIN_STATS:
-        st->rel_residual = (st->delta_0 > 0) ? ::sqrt(st->delta_new / st->delta_0) : 0.0;
-        st->abs_residual = ::sqrt(st->delta_new);
+        fin_stats(st);
         break;
     }
     if (set_cond && (kind == FIN_INIT || kind == FIN_ALPHA || kind == FIN_BETA || kind == FIN_MR_INIT ||
                      kind == FIN_MR_ALPHA || kind == FIN_MR_BETA))
         cudaGraphSetConditional(cond, st->done ? 0u : 1u);
+}
+
+// The whole of ILSS_CG::Solve (ILSS_CG.h:38-151) for a small C_WRP solid in
+// one block of kBlock threads: the same per-element products, per-node
+// gathers and scalar steps as the kernel-per-phase loop, the phases
+// separated by block barriers instead of launches (the reductions of a
+// solid whose node and vector loops fit one block of the grid kernels are
+// the same sums, so the same bits). The loop ends on the solver's own tests
+// (at most max_iter iterations).
+__global__ void __launch_bounds__(kBlock) k_cg_block_fp64(MeshView<double> m, StepConsts c,
+                                                          const double* __restrict__ b, double* y, double* r,
+                                                          double* d, double* q, StepScalars* st)
+{
+    const uint32_t tid = threadIdx.x, nt = blockDim.x;
+    const double mfm = c.mass * c.factor_M;
+    volatile const StepScalars* vst = st;
+    auto elem_products = [&](const double* u) {
+        for (uint32_t e = tid; e < m.T; e += nt) {
+            const int4 t = m.tets[e];
+            double R[9], Di[9], k1, knu, k2;
+            load_elem(m, e, R, Di, k1, knu, k2);
+            const int ids[4] = {(int)bounds_idx((uint32_t)t.x, m.N, kSiteElemNode),
+                                (int)bounds_idx((uint32_t)t.y, m.N, kSiteElemNode),
+                                (int)bounds_idx((uint32_t)t.z, m.N, kSiteElemNode),
+                                (int)bounds_idx((uint32_t)t.w, m.N, kSiteElemNode)};
+            double dl[12];
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+                dl[3 * i] = u[3 * (size_t)ids[i]];
+                dl[3 * i + 1] = u[3 * (size_t)ids[i] + 1];
+                dl[3 * i + 2] = u[3 * (size_t)ids[i] + 2];
+            }
+            double out[12];
+            elem_RKRt(R, Di, k1, knu, k2, dl, out);
+            double* o = m.eout + 12 * (size_t)e;
+#pragma unroll
+            for (int k = 0; k < 12; k++) o[k] = out[k];
+        }
+        __syncthreads();
+    };
+    // r = S(b - A y), d = r, |r|^2
+    elem_products(y);
+    double acc = 0.0;
+    for (uint32_t n = tid; n < m.N; n += nt) {
+        double s0 = 0, s1 = 0, s2 = 0;
+        gather3(m, n, s0, s1, s2);
+        const size_t i = 3 * (size_t)n;
+        double r0 = 0, r1 = 0, r2 = 0;
+        if (!m.fixed[n]) {
+            r0 = b[i] - (c.factor_K * s0 + mfm * y[i]);
+            r1 = b[i + 1] - (c.factor_K * s1 + mfm * y[i + 1]);
+            r2 = b[i + 2] - (c.factor_K * s2 + mfm * y[i + 2]);
+        }
+        r[i] = r0; r[i + 1] = r1; r[i + 2] = r2;
+        d[i] = r0; d[i + 1] = r1; d[i + 2] = r2;
+        acc += r0 * r0 + r1 * r1 + r2 * r2;
+    }
+    double total = block_sum(acc);
+    if (tid == 0) fin_init(st, c, total);
+    __syncthreads();
+    const uint32_t n3 = 3 * m.N;
+    while (!vst->done) {
+        // q = S A d, d.q, alpha
+        elem_products(d);
+        acc = 0.0;
+        for (uint32_t n = tid; n < m.N; n += nt) {
+            double s0 = 0, s1 = 0, s2 = 0;
+            gather3(m, n, s0, s1, s2);
+            const size_t i = 3 * (size_t)n;
+            double q0 = 0, q1 = 0, q2 = 0;
+            if (!m.fixed[n]) {
+                q0 = c.factor_K * s0 + mfm * d[i];
+                q1 = c.factor_K * s1 + mfm * d[i + 1];
+                q2 = c.factor_K * s2 + mfm * d[i + 2];
+            }
+            q[i] = q0; q[i + 1] = q1; q[i + 2] = q2;
+            acc += d[i] * q0 + d[i + 1] * q1 + d[i + 2] * q2;
+        }
+        total = block_sum(acc);
+        if (tid == 0) fin_alpha(st, total);
+        __syncthreads();
+        if (vst->done) break;
+        // y += alpha d, r -= alpha q, |r|^2, beta and the loop test
+        const double alpha = vst->alpha, na = -alpha;
+        acc = 0.0;
+        for (uint32_t i = tid; i < n3; i += nt) {
+            y[i] += alpha * d[i];
+            const double ri = r[i] + na * q[i];
+            r[i] = ri;
+            acc += ri * ri;
+        }
+        total = block_sum(acc);
+        if (tid == 0) fin_beta(st, total);
+        __syncthreads();
+        if (vst->done) break;
+        // d = S (beta d + r)
+        const double beta = vst->beta;
+        for (uint32_t i = tid; i < n3; i += nt) d[i] = m.fixed[i / 3] ? 0.0 : beta * d[i] + r[i];
+        __syncthreads();
+    }
+    if (tid == 0) fin_stats(st);
+}
+
+void launch_cg_block_fp64(const MeshView<double>& m, const StepConsts& c, const double* b, double* y, double* r,
+                          double* d, double* q, StepScalars* st, cudaStream_t s)
+{
+    k_cg_block_fp64<<<1, kBlock, 0, s>>>(m, c, b, y, r, d, q, st);
+    launch_counter()++;
 }
 
 // ---- launchers ----
