@@ -205,9 +205,10 @@ enum FinalizeKind {
 void launch_finalize(int kind, const double* partials, uint32_t count, const StepConsts& c, StepScalars* st,
                      cudaStream_t s, cudaGraphConditionalHandle cond = 0, int set_cond = 0);
 
-// The whole CG solve of a small C_WRP solid in one block (fem_kernels.cu).
-void launch_cg_block_fp64(const MeshView<double>& m, const StepConsts& c, const double* b, double* y, double* r,
-                          double* d, double* q, StepScalars* st, cudaStream_t s);
+// The whole CG solve of a small C_WRP solid (at most kBlock tets and nodes)
+// in one block, on chip (fem_kernels.cu).
+void launch_cg_block_fp64(const MeshView<double>& m, const StepConsts& c, const double* b, double* y, StepScalars* st,
+                          cudaStream_t s);
 
 uint32_t grid_for(uint32_t n);    // grid size of the grid-stride kernels
 uint64_t& launch_counter();       // kernels launched by this library

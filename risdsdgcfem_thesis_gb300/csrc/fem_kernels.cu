@@ -824,111 +824,156 @@ __global__ void k_finalize(int kind, const double* __restrict__ partials, uint32
         cudaGraphSetConditional(cond, st->done ? 0u : 1u);
 }
 
-// The whole of ILSS_CG::Solve (ILSS_CG.h:38-151) for a small C_WRP solid in
-// one block of kBlock threads: the same per-element products, per-node
-// gathers and scalar steps as the kernel-per-phase loop, the phases
-// separated by block barriers instead of launches (the reductions of a
-// solid whose node and vector loops fit one block of the grid kernels are
-// the same sums, so the same bits). The loop ends on the solver's own tests
-// (at most max_iter iterations).
+// The whole of ILSS_CG::Solve (ILSS_CG.h:38-151) for a small C_WRP solid (at
+// most kBlock tets and nodes) in one block, on chip: each thread keeps its
+// element's R, Dm^-1 and material scalars in registers; the element
+// outputs, the node vectors, the node CSR and the solver's scalars live in
+// shared memory; the phases are separated by block barriers. The element
+// products, the per-node gathers (same order) and the scalar steps are
+// those of the kernel-per-phase loop, and its node loop and (for up to 85
+// nodes) vector loop are the grid kernels' single block, so the same sums.
+// y and the statistics are written back at the end; the loop ends on the
+// solver's own tests (at most max_iter iterations).
 __global__ void __launch_bounds__(kBlock) k_cg_block_fp64(MeshView<double> m, StepConsts c,
-                                                          const double* __restrict__ b, double* y, double* r,
-                                                          double* d, double* q, StepScalars* st)
+                                                          const double* __restrict__ b, double* y, StepScalars* st)
 {
-    const uint32_t tid = threadIdx.x, nt = blockDim.x;
+    extern __shared__ __align__(16) unsigned char cg_smem[];
+    const uint32_t tid = threadIdx.x, nt = blockDim.x, N = m.N, T = m.T, n3 = 3 * N;
+    double* eo = reinterpret_cast<double*>(cg_smem);  // [12 T]
+    double* vy = eo + 12 * (size_t)T;                   // [3 N] each
+    double* vr = vy + n3;
+    double* vd = vr + n3;
+    double* vq = vd + n3;
+    double* vb = vq + n3;
+    uint32_t* cptr = reinterpret_cast<uint32_t*>(vb + n3);  // [N + 1]
+    uint32_t* cidx = cptr + N + 1;                          // [4 T]
+    uint8_t* fx = reinterpret_cast<uint8_t*>(cidx + 4 * (size_t)T);
+    __shared__ StepScalars sst;
     const double mfm = c.mass * c.factor_M;
-    volatile const StepScalars* vst = st;
+    for (uint32_t i = tid; i < n3; i += nt) {
+        vy[i] = y[i];
+        vb[i] = b[i];
+    }
+    for (uint32_t i = tid; i <= N; i += nt) cptr[i] = m.csr_ptr[i];
+    for (uint32_t i = tid; i < 4 * T; i += nt) cidx[i] = bounds_idx(m.csr_idx[i], 4u * T, kSiteCsrEntry);
+    for (uint32_t i = tid; i < N; i += nt) fx[i] = m.fixed[i];
+    if (tid == 0) sst = *st;
+    // this thread's element (tid < T)
+    double R[9], Di[9], k1 = 0, knu = 0, k2 = 0;
+    int ids[4] = {0, 0, 0, 0};
+    if (tid < T) {
+        load_elem(m, tid, R, Di, k1, knu, k2);
+        const int4 t = m.tets[tid];
+        ids[0] = (int)bounds_idx((uint32_t)t.x, N, kSiteElemNode);
+        ids[1] = (int)bounds_idx((uint32_t)t.y, N, kSiteElemNode);
+        ids[2] = (int)bounds_idx((uint32_t)t.z, N, kSiteElemNode);
+        ids[3] = (int)bounds_idx((uint32_t)t.w, N, kSiteElemNode);
+    }
+    __syncthreads();
     auto elem_products = [&](const double* u) {
-        for (uint32_t e = tid; e < m.T; e += nt) {
-            const int4 t = m.tets[e];
-            double R[9], Di[9], k1, knu, k2;
-            load_elem(m, e, R, Di, k1, knu, k2);
-            const int ids[4] = {(int)bounds_idx((uint32_t)t.x, m.N, kSiteElemNode),
-                                (int)bounds_idx((uint32_t)t.y, m.N, kSiteElemNode),
-                                (int)bounds_idx((uint32_t)t.z, m.N, kSiteElemNode),
-                                (int)bounds_idx((uint32_t)t.w, m.N, kSiteElemNode)};
+        if (tid < T) {
             double dl[12];
 #pragma unroll
             for (int i = 0; i < 4; i++) {
-                dl[3 * i] = u[3 * (size_t)ids[i]];
-                dl[3 * i + 1] = u[3 * (size_t)ids[i] + 1];
-                dl[3 * i + 2] = u[3 * (size_t)ids[i] + 2];
+                dl[3 * i] = u[3 * ids[i]];
+                dl[3 * i + 1] = u[3 * ids[i] + 1];
+                dl[3 * i + 2] = u[3 * ids[i] + 2];
             }
             double out[12];
             elem_RKRt(R, Di, k1, knu, k2, dl, out);
-            double* o = m.eout + 12 * (size_t)e;
 #pragma unroll
-            for (int k = 0; k < 12; k++) o[k] = out[k];
+            for (int k = 0; k < 12; k++) eo[12 * tid + k] = out[k];
         }
         __syncthreads();
     };
-    // r = S(b - A y), d = r, |r|^2
-    elem_products(y);
-    double acc = 0.0;
-    for (uint32_t n = tid; n < m.N; n += nt) {
-        double s0 = 0, s1 = 0, s2 = 0;
-        gather3(m, n, s0, s1, s2);
-        const size_t i = 3 * (size_t)n;
-        double r0 = 0, r1 = 0, r2 = 0;
-        if (!m.fixed[n]) {
-            r0 = b[i] - (c.factor_K * s0 + mfm * y[i]);
-            r1 = b[i + 1] - (c.factor_K * s1 + mfm * y[i + 1]);
-            r2 = b[i + 2] - (c.factor_K * s2 + mfm * y[i + 2]);
+    auto gather = [&](uint32_t n, double& a0, double& a1, double& a2) {
+        for (uint32_t j = cptr[n]; j < cptr[n + 1]; j++) {
+            const double* o = eo + 3 * (size_t)cidx[j];
+            a0 += o[0];
+            a1 += o[1];
+            a2 += o[2];
         }
-        r[i] = r0; r[i + 1] = r1; r[i + 2] = r2;
-        d[i] = r0; d[i + 1] = r1; d[i + 2] = r2;
+    };
+    // r = S(b - A y), d = r, |r|^2
+    elem_products(vy);
+    double acc = 0.0;
+    for (uint32_t n = tid; n < N; n += nt) {
+        double s0 = 0, s1 = 0, s2 = 0;
+        gather(n, s0, s1, s2);
+        const uint32_t i = 3 * n;
+        double r0 = 0, r1 = 0, r2 = 0;
+        if (!fx[n]) {
+            r0 = vb[i] - (c.factor_K * s0 + mfm * vy[i]);
+            r1 = vb[i + 1] - (c.factor_K * s1 + mfm * vy[i + 1]);
+            r2 = vb[i + 2] - (c.factor_K * s2 + mfm * vy[i + 2]);
+        }
+        vr[i] = r0; vr[i + 1] = r1; vr[i + 2] = r2;
+        vd[i] = r0; vd[i + 1] = r1; vd[i + 2] = r2;
         acc += r0 * r0 + r1 * r1 + r2 * r2;
     }
     double total = block_sum(acc);
-    if (tid == 0) fin_init(st, c, total);
+    if (tid == 0) fin_init(&sst, c, total);
     __syncthreads();
-    const uint32_t n3 = 3 * m.N;
-    while (!vst->done) {
+    while (!sst.done) {
         // q = S A d, d.q, alpha
-        elem_products(d);
+        elem_products(vd);
         acc = 0.0;
-        for (uint32_t n = tid; n < m.N; n += nt) {
+        for (uint32_t n = tid; n < N; n += nt) {
             double s0 = 0, s1 = 0, s2 = 0;
-            gather3(m, n, s0, s1, s2);
-            const size_t i = 3 * (size_t)n;
+            gather(n, s0, s1, s2);
+            const uint32_t i = 3 * n;
             double q0 = 0, q1 = 0, q2 = 0;
-            if (!m.fixed[n]) {
-                q0 = c.factor_K * s0 + mfm * d[i];
-                q1 = c.factor_K * s1 + mfm * d[i + 1];
-                q2 = c.factor_K * s2 + mfm * d[i + 2];
+            if (!fx[n]) {
+                q0 = c.factor_K * s0 + mfm * vd[i];
+                q1 = c.factor_K * s1 + mfm * vd[i + 1];
+                q2 = c.factor_K * s2 + mfm * vd[i + 2];
             }
-            q[i] = q0; q[i + 1] = q1; q[i + 2] = q2;
-            acc += d[i] * q0 + d[i + 1] * q1 + d[i + 2] * q2;
+            vq[i] = q0; vq[i + 1] = q1; vq[i + 2] = q2;
+            acc += vd[i] * q0 + vd[i + 1] * q1 + vd[i + 2] * q2;
         }
         total = block_sum(acc);
-        if (tid == 0) fin_alpha(st, total);
+        if (tid == 0) fin_alpha(&sst, total);
         __syncthreads();
-        if (vst->done) break;
+        if (sst.done) break;
         // y += alpha d, r -= alpha q, |r|^2, beta and the loop test
-        const double alpha = vst->alpha, na = -alpha;
+        const double alpha = sst.alpha, na = -alpha;
         acc = 0.0;
         for (uint32_t i = tid; i < n3; i += nt) {
-            y[i] += alpha * d[i];
-            const double ri = r[i] + na * q[i];
-            r[i] = ri;
+            vy[i] += alpha * vd[i];
+            const double ri = vr[i] + na * vq[i];
+            vr[i] = ri;
             acc += ri * ri;
         }
         total = block_sum(acc);
-        if (tid == 0) fin_beta(st, total);
+        if (tid == 0) fin_beta(&sst, total);
         __syncthreads();
-        if (vst->done) break;
+        if (sst.done) break;
         // d = S (beta d + r)
-        const double beta = vst->beta;
-        for (uint32_t i = tid; i < n3; i += nt) d[i] = m.fixed[i / 3] ? 0.0 : beta * d[i] + r[i];
+        const double beta = sst.beta;
+        for (uint32_t i = tid; i < n3; i += nt) vd[i] = fx[i / 3] ? 0.0 : beta * vd[i] + vr[i];
         __syncthreads();
     }
-    if (tid == 0) fin_stats(st);
+    for (uint32_t i = tid; i < n3; i += nt) y[i] = vy[i];
+    if (tid == 0) {
+        fin_stats(&sst);
+        *st = sst;
+    }
 }
 
-void launch_cg_block_fp64(const MeshView<double>& m, const StepConsts& c, const double* b, double* y, double* r,
-                          double* d, double* q, StepScalars* st, cudaStream_t s)
+size_t cg_block_smem_bytes(uint32_t N, uint32_t T)
 {
-    k_cg_block_fp64<<<1, kBlock, 0, s>>>(m, c, b, y, r, d, q, st);
+    return sizeof(double) * (12 * (size_t)T + 5 * 3 * (size_t)N) + sizeof(uint32_t) * ((size_t)N + 1 + 4 * (size_t)T) +
+           N;
+}
+
+void launch_cg_block_fp64(const MeshView<double>& m, const StepConsts& c, const double* b, double* y, StepScalars* st,
+                          cudaStream_t s)
+{
+    static const cudaError_t attr = cudaFuncSetAttribute(
+        k_cg_block_fp64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cg_block_smem_bytes(kBlock, kBlock));
+    (void)attr;
+    const size_t smem = cg_block_smem_bytes(m.N, m.T);
+    k_cg_block_fp64<<<1, kBlock, smem, s>>>(m, c, b, y, st);
     launch_counter()++;
 }
 

@@ -337,9 +337,9 @@ int open_step(fem_solid s)
 }
 
 // A C_WRP solid small enough for the one-block CG kernel (its iteration a
-// few block barriers instead of six launches; each of them waits on a few
-// dependent global accesses, so one block only wins while its loops take
-// one round: 17.7 us per iteration at 160 tets against 33.8 for the graph
+// few block barriers on shared memory instead of six launches; the FP64
+// element products of one SM bound it, so one block only wins while there
+// are few: 16.9 us per iteration at 160 tets against 33.8 for the graph
 // loop, 65 against 37 at 1,080 tets).
 constexpr uint32_t kCgBlockMaxTets = 256, kCgBlockMaxNodes = 256;
 bool cg_in_one_block(const fem_solid s)
@@ -356,7 +356,7 @@ int cg_solve(fem_solid s, const StepConsts& c, int chunk)
     cudaStream_t st = s->stream;
     MeshView<double> m = s->view();
     if (cg_in_one_block(s)) {
-        launch_cg_block_fp64(m, c, s->b.p, s->y.p, s->r.p, s->d.p, s->q.p, s->st.p, st);
+        launch_cg_block_fp64(m, c, s->b.p, s->y.p, s->st.p, st);
         CK(cudaMemcpyAsync(s->st_host, s->st.p, sizeof(StepScalars), cudaMemcpyDeviceToHost, st));
         CK(cudaStreamSynchronize(st));
         CK(cudaGetLastError());
@@ -442,7 +442,7 @@ cudaError_t ls_solve_capture(fem_solid s, const StepConsts& c, cudaGraph_t top)
     MeshView<double> m = s->view();
     const uint32_t gN = grid_for(s->N), gV = grid_for(3 * s->N);
     if (s->params.ls_solver != FEM_LS_MINRES && cg_in_one_block(s)) {
-        launch_cg_block_fp64(m, c, s->b.p, s->y.p, s->r.p, s->d.p, s->q.p, s->st.p, st);
+        launch_cg_block_fp64(m, c, s->b.p, s->y.p, s->st.p, st);
         return cudaGetLastError();
     }
     cudaGraphConditionalHandle cond = 0;
