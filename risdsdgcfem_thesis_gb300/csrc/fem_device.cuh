@@ -205,10 +205,24 @@ enum FinalizeKind {
 void launch_finalize(int kind, const double* partials, uint32_t count, const StepConsts& c, StepScalars* st,
                      cudaStream_t s, cudaGraphConditionalHandle cond = 0, int set_cond = 0);
 
-// The whole CG solve of a small C_WRP solid (at most kBlock tets and nodes)
-// in one block, on chip (fem_kernels.cu).
-void launch_cg_block_fp64(const MeshView<double>& m, const StepConsts& c, const double* b, double* y, StepScalars* st,
-                          cudaStream_t s);
+// The whole CG solve of a small C_WRP solid on one thread-block cluster
+// (fem_kernels.cu): CTA r of `ctas` owns the elements [r ept, (r+1) ept) and
+// the nodes [r npt, (r+1) npt); ent_max bounds a CTA's CSR entries; smem is
+// its dynamic shared memory (cg_cluster_smem_bytes).
+constexpr uint32_t kCgClusterMaxCtas = 16, kCgClusterMaxThreads = 512;
+constexpr size_t kCgClusterMaxSmem = 200 * 1024;
+struct CgClusterPlan {
+    uint32_t ctas, threads, ept, npt, ent_max;
+    size_t smem;
+};
+size_t cg_cluster_smem_bytes(uint32_t ept, uint32_t npt, uint32_t ent_max);
+// The plan launches on this device (its cluster size, threads and shared
+// memory give at least one resident cluster).
+bool cg_cluster_fits(const CgClusterPlan& p);
+// ent: per CSR entry, (CTA owning the corner's element) << 24 | (local
+// element index * 4 + corner).
+cudaError_t launch_cg_cluster_fp64(const MeshView<double>& m, const StepConsts& c, const CgClusterPlan& p,
+                                   const uint32_t* ent, const double* b, double* y, StepScalars* st, cudaStream_t s);
 
 uint32_t grid_for(uint32_t n);    // grid size of the grid-stride kernels
 uint64_t& launch_counter();       // kernels launched by this library

@@ -20,6 +20,8 @@
 #include "msvd.cuh"
 #include "elem_math.cuh"
 
+#include <cooperative_groups.h>
+
 #include <map>
 #include <mutex>
 #include <string>
@@ -824,85 +826,124 @@ __global__ void k_finalize(int kind, const double* __restrict__ partials, uint32
         cudaGraphSetConditional(cond, st->done ? 0u : 1u);
 }
 
-// The whole of ILSS_CG::Solve (ILSS_CG.h:38-151) for a small C_WRP solid (at
-// most kBlock tets and nodes) in one block, on chip: each thread keeps its
-// element's R, Dm^-1 and material scalars in registers; the element
-// outputs, the node vectors, the node CSR and the solver's scalars live in
-// shared memory; the phases are separated by block barriers. The element
-// products, the per-node gathers (same order) and the scalar steps are
-// those of the kernel-per-phase loop, and its node loop and (for up to 85
-// nodes) vector loop are the grid kernels' single block, so the same sums.
-// y and the statistics are written back at the end; the loop ends on the
-// solver's own tests (at most max_iter iterations).
-__global__ void __launch_bounds__(kBlock) k_cg_block_fp64(MeshView<double> m, StepConsts c,
-                                                          const double* __restrict__ b, double* y, StepScalars* st)
+// The whole of ILSS_CG::Solve (ILSS_CG.h:38-151) for a C_WRP solid of up to
+// kCgClusterMaxCtas x kCgClusterMaxThreads tets on one thread-block cluster,
+// on chip. CTA r owns the elements [r ept, (r+1) ept) and the nodes
+// [r npt, (r+1) npt): each thread keeps one element's R, Dm^-1 and material
+// scalars in registers and its element output in its CTA's shared memory;
+// the CTA keeps its nodes' y, r, d, q, b, CSR rows and fixed flags. An
+// element product reads its four nodes' d from the owning CTAs' shared
+// memory (distributed shared memory); a node's gather reads its element
+// corners' outputs the same way (ent: per CSR entry, the owning CTA << 24 |
+// its local corner). A reduction sums each CTA's block total into a slot of
+// every CTA, then every CTA adds the slots in rank order, so all CTAs take
+// the same scalar steps and leave the loop together. Four cluster barriers
+// per iteration: element outputs complete, d.q, |r|^2, the new d. y and the
+// statistics are written back at the end; the loop ends on the solver's own
+// tests (at most max_iter iterations).
+__global__ void __launch_bounds__(kCgClusterMaxThreads, 1)
+    k_cg_cluster_fp64(MeshView<double> m, StepConsts c, CgClusterPlan p, const uint32_t* __restrict__ ent,
+                      const double* __restrict__ b, double* y, StepScalars* st)
 {
-    extern __shared__ __align__(16) unsigned char cg_smem[];
-    const uint32_t tid = threadIdx.x, nt = blockDim.x, N = m.N, T = m.T, n3 = 3 * N;
-    double* eo = reinterpret_cast<double*>(cg_smem);  // [12 T]
-    double* vy = eo + 12 * (size_t)T;                   // [3 N] each
-    double* vr = vy + n3;
-    double* vd = vr + n3;
-    double* vq = vd + n3;
-    double* vb = vq + n3;
-    uint32_t* cptr = reinterpret_cast<uint32_t*>(vb + n3);  // [N + 1]
-    uint32_t* cidx = cptr + N + 1;                          // [4 T]
-    uint8_t* fx = reinterpret_cast<uint8_t*>(cidx + 4 * (size_t)T);
+    namespace cgr = cooperative_groups;
+    cgr::cluster_group cl = cgr::this_cluster();
+    extern __shared__ __align__(16) unsigned char cl_smem[];
+    const uint32_t tid = threadIdx.x, nt = blockDim.x, rank = cl.block_rank(), C = p.ctas;
+    const uint32_t N = m.N, T = m.T;
+    const uint32_t e0 = rank * p.ept, n0 = rank * p.npt;
+    const uint32_t ne = e0 < T ? min(p.ept, T - e0) : 0u, nn = n0 < N ? min(p.npt, N - n0) : 0u, n3 = 3 * nn;
+    const size_t v3 = 3 * (size_t)p.npt;
+    double* eo = reinterpret_cast<double*>(cl_smem);  // [12 ept]
+    double* vy = eo + 12 * (size_t)p.ept;               // [3 npt] each
+    double* vr = vy + v3;
+    double* vd = vr + v3;
+    double* vq = vd + v3;
+    double* vb = vq + v3;
+    double* part = vb + v3;                                   // [3][kCgClusterMaxCtas]
+    uint32_t* cptr = reinterpret_cast<uint32_t*>(part + 3 * kCgClusterMaxCtas);  // [npt + 1]
+    uint32_t* cent = cptr + p.npt + 1;                                          // [ent_max]
+    uint8_t* fx = reinterpret_cast<uint8_t*>(cent + p.ent_max);                 // [npt]
     __shared__ StepScalars sst;
     const double mfm = c.mass * c.factor_M;
+    const uint32_t base = nn ? m.csr_ptr[n0] : 0u;
     for (uint32_t i = tid; i < n3; i += nt) {
-        vy[i] = y[i];
-        vb[i] = b[i];
+        vy[i] = y[3 * (size_t)n0 + i];
+        vb[i] = b[3 * (size_t)n0 + i];
     }
-    for (uint32_t i = tid; i <= N; i += nt) cptr[i] = m.csr_ptr[i];
-    for (uint32_t i = tid; i < 4 * T; i += nt) cidx[i] = bounds_idx(m.csr_idx[i], 4u * T, kSiteCsrEntry);
-    for (uint32_t i = tid; i < N; i += nt) fx[i] = m.fixed[i];
+    for (uint32_t i = tid; i <= nn; i += nt) cptr[i] = nn ? m.csr_ptr[n0 + i] - base : 0u;
+    const uint32_t ne_ent = nn ? min(m.csr_ptr[n0 + nn] - base, p.ent_max) : 0u;
+    for (uint32_t i = tid; i < ne_ent; i += nt) cent[i] = ent[base + i];
+    for (uint32_t i = tid; i < nn; i += nt) fx[i] = m.fixed[n0 + i];
     if (tid == 0) sst = *st;
-    // this thread's element (tid < T)
+    // this thread's element (tid < ne) and where its nodes live
     double R[9], Di[9], k1 = 0, knu = 0, k2 = 0;
-    int ids[4] = {0, 0, 0, 0};
-    if (tid < T) {
-        load_elem(m, tid, R, Di, k1, knu, k2);
-        const int4 t = m.tets[tid];
-        ids[0] = (int)bounds_idx((uint32_t)t.x, N, kSiteElemNode);
-        ids[1] = (int)bounds_idx((uint32_t)t.y, N, kSiteElemNode);
-        ids[2] = (int)bounds_idx((uint32_t)t.z, N, kSiteElemNode);
-        ids[3] = (int)bounds_idx((uint32_t)t.w, N, kSiteElemNode);
+    uint32_t nr[4] = {0, 0, 0, 0}, nl[4] = {0, 0, 0, 0};
+    if (tid < ne) {
+        load_elem(m, e0 + tid, R, Di, k1, knu, k2);
+        const int4 t = m.tets[e0 + tid];
+        const uint32_t ids[4] = {bounds_idx((uint32_t)t.x, N, kSiteElemNode), bounds_idx((uint32_t)t.y, N, kSiteElemNode),
+                                 bounds_idx((uint32_t)t.z, N, kSiteElemNode), bounds_idx((uint32_t)t.w, N, kSiteElemNode)};
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            nr[k] = ids[k] / p.npt;
+            nl[k] = 3 * (ids[k] - nr[k] * p.npt);
+        }
     }
-    __syncthreads();
-    auto elem_products = [&](const double* u) {
-        if (tid < T) {
+    const double* pd[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) pd[k] = cl.map_shared_rank(vd, nr[k]) + nl[k];
+    cl.sync();  // every CTA's y, d and CSR rows are in place
+    auto elem_products = [&](const double* const* u) {
+        if (tid < ne) {
             double dl[12];
 #pragma unroll
-            for (int i = 0; i < 4; i++) {
-                dl[3 * i] = u[3 * ids[i]];
-                dl[3 * i + 1] = u[3 * ids[i] + 1];
-                dl[3 * i + 2] = u[3 * ids[i] + 2];
+            for (int k = 0; k < 4; k++) {
+                dl[3 * k] = u[k][0];
+                dl[3 * k + 1] = u[k][1];
+                dl[3 * k + 2] = u[k][2];
             }
             double out[12];
             elem_RKRt(R, Di, k1, knu, k2, dl, out);
 #pragma unroll
             for (int k = 0; k < 12; k++) eo[12 * tid + k] = out[k];
         }
-        __syncthreads();
+        cl.sync();  // all element outputs complete
     };
-    auto gather = [&](uint32_t n, double& a0, double& a1, double& a2) {
-        for (uint32_t j = cptr[n]; j < cptr[n + 1]; j++) {
-            const double* o = eo + 3 * (size_t)cidx[j];
+    auto gather = [&](uint32_t ln, double& a0, double& a1, double& a2) {
+        const uint32_t jend = min(cptr[ln + 1], ne_ent);
+        for (uint32_t j = cptr[ln]; j < jend; j++) {
+            const uint32_t e = cent[j];
+            const double* o = cl.map_shared_rank(eo, e >> 24) + 3 * (e & 0xffffffu);
             a0 += o[0];
             a1 += o[1];
             a2 += o[2];
         }
     };
+    // the cluster's total of every thread's acc (valid in thread 0)
+    auto cluster_total = [&](double acc, int slot) -> double {
+        const double v = block_sum(acc);
+        if (tid == 0)
+            for (uint32_t r = 0; r < C; r++) cl.map_shared_rank(part, r)[slot * kCgClusterMaxCtas + rank] = v;
+        cl.sync();
+        double total = 0.0;
+        if (tid == 0)
+            for (uint32_t r = 0; r < C; r++) total += part[slot * kCgClusterMaxCtas + r];
+        return total;
+    };
     // r = S(b - A y), d = r, |r|^2
-    elem_products(vy);
+    {
+        const double* py[4];
+#pragma unroll
+        for (int k = 0; k < 4; k++) py[k] = cl.map_shared_rank(vy, nr[k]) + nl[k];
+        elem_products(py);
+    }
     double acc = 0.0;
-    for (uint32_t n = tid; n < N; n += nt) {
+    for (uint32_t ln = tid; ln < nn; ln += nt) {
         double s0 = 0, s1 = 0, s2 = 0;
-        gather(n, s0, s1, s2);
-        const uint32_t i = 3 * n;
+        gather(ln, s0, s1, s2);
+        const uint32_t i = 3 * ln;
         double r0 = 0, r1 = 0, r2 = 0;
-        if (!fx[n]) {
+        if (!fx[ln]) {
             r0 = vb[i] - (c.factor_K * s0 + mfm * vy[i]);
             r1 = vb[i + 1] - (c.factor_K * s1 + mfm * vy[i + 1]);
             r2 = vb[i + 2] - (c.factor_K * s2 + mfm * vy[i + 2]);
@@ -911,19 +952,19 @@ __global__ void __launch_bounds__(kBlock) k_cg_block_fp64(MeshView<double> m, St
         vd[i] = r0; vd[i + 1] = r1; vd[i + 2] = r2;
         acc += r0 * r0 + r1 * r1 + r2 * r2;
     }
-    double total = block_sum(acc);
+    double total = cluster_total(acc, 0);
     if (tid == 0) fin_init(&sst, c, total);
     __syncthreads();
     while (!sst.done) {
         // q = S A d, d.q, alpha
-        elem_products(vd);
+        elem_products(pd);
         acc = 0.0;
-        for (uint32_t n = tid; n < N; n += nt) {
+        for (uint32_t ln = tid; ln < nn; ln += nt) {
             double s0 = 0, s1 = 0, s2 = 0;
-            gather(n, s0, s1, s2);
-            const uint32_t i = 3 * n;
+            gather(ln, s0, s1, s2);
+            const uint32_t i = 3 * ln;
             double q0 = 0, q1 = 0, q2 = 0;
-            if (!fx[n]) {
+            if (!fx[ln]) {
                 q0 = c.factor_K * s0 + mfm * vd[i];
                 q1 = c.factor_K * s1 + mfm * vd[i + 1];
                 q2 = c.factor_K * s2 + mfm * vd[i + 2];
@@ -931,7 +972,7 @@ __global__ void __launch_bounds__(kBlock) k_cg_block_fp64(MeshView<double> m, St
             vq[i] = q0; vq[i + 1] = q1; vq[i + 2] = q2;
             acc += vd[i] * q0 + vd[i + 1] * q1 + vd[i + 2] * q2;
         }
-        total = block_sum(acc);
+        total = cluster_total(acc, 1);
         if (tid == 0) fin_alpha(&sst, total);
         __syncthreads();
         if (sst.done) break;
@@ -944,37 +985,83 @@ __global__ void __launch_bounds__(kBlock) k_cg_block_fp64(MeshView<double> m, St
             vr[i] = ri;
             acc += ri * ri;
         }
-        total = block_sum(acc);
+        total = cluster_total(acc, 2);
         if (tid == 0) fin_beta(&sst, total);
         __syncthreads();
         if (sst.done) break;
         // d = S (beta d + r)
         const double beta = sst.beta;
         for (uint32_t i = tid; i < n3; i += nt) vd[i] = fx[i / 3] ? 0.0 : beta * vd[i] + vr[i];
-        __syncthreads();
+        cl.sync();  // the new d is complete
     }
-    for (uint32_t i = tid; i < n3; i += nt) y[i] = vy[i];
-    if (tid == 0) {
+    for (uint32_t i = tid; i < n3; i += nt) y[3 * (size_t)n0 + i] = vy[i];
+    if (rank == 0 && tid == 0) {
         fin_stats(&sst);
         *st = sst;
     }
+    cl.sync();  // no CTA leaves while another may still read its shared memory
 }
 
-size_t cg_block_smem_bytes(uint32_t N, uint32_t T)
+size_t cg_cluster_smem_bytes(uint32_t ept, uint32_t npt, uint32_t ent_max)
 {
-    return sizeof(double) * (12 * (size_t)T + 5 * 3 * (size_t)N) + sizeof(uint32_t) * ((size_t)N + 1 + 4 * (size_t)T) +
-           N;
+    return sizeof(double) * (12 * (size_t)ept + 15 * (size_t)npt + 3 * kCgClusterMaxCtas) +
+           sizeof(uint32_t) * ((size_t)npt + 1 + ent_max) + npt;
 }
 
-void launch_cg_block_fp64(const MeshView<double>& m, const StepConsts& c, const double* b, double* y, StepScalars* st,
-                          cudaStream_t s)
+namespace {
+cudaError_t cg_cluster_attrs()
 {
-    static const cudaError_t attr = cudaFuncSetAttribute(
-        k_cg_block_fp64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cg_block_smem_bytes(kBlock, kBlock));
-    (void)attr;
-    const size_t smem = cg_block_smem_bytes(m.N, m.T);
-    k_cg_block_fp64<<<1, kBlock, smem, s>>>(m, c, b, y, st);
+    static const cudaError_t e = [] {
+        cudaError_t r = cudaFuncSetAttribute(k_cg_cluster_fp64, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)kCgClusterMaxSmem);
+        if (r == cudaSuccess) r = cudaFuncSetAttribute(k_cg_cluster_fp64, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+        return r;
+    }();
+    return e;
+}
+void cluster_config(cudaLaunchConfig_t& cfg, cudaLaunchAttribute& at, const CgClusterPlan& p, cudaStream_t s)
+{
+    cfg = cudaLaunchConfig_t{};
+    cfg.gridDim = dim3(p.ctas);
+    cfg.blockDim = dim3(p.threads);
+    cfg.dynamicSmemBytes = p.smem;
+    cfg.stream = s;
+    at.id = cudaLaunchAttributeClusterDimension;
+    at.val.clusterDim.x = p.ctas;
+    at.val.clusterDim.y = 1;
+    at.val.clusterDim.z = 1;
+    cfg.attrs = &at;
+    cfg.numAttrs = 1;
+}
+}  // namespace
+
+bool cg_cluster_fits(const CgClusterPlan& p)
+{
+    if (p.ctas < 1 || p.ctas > kCgClusterMaxCtas || p.threads < 32 || p.threads > kCgClusterMaxThreads ||
+        p.smem > kCgClusterMaxSmem || cg_cluster_attrs() != cudaSuccess)
+        return false;
+    cudaLaunchConfig_t cfg;
+    cudaLaunchAttribute at;
+    cluster_config(cfg, at, p, nullptr);
+    int n = 0;
+    if (cudaOccupancyMaxActiveClusters(&n, k_cg_cluster_fp64, &cfg) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return n >= 1;
+}
+
+cudaError_t launch_cg_cluster_fp64(const MeshView<double>& m, const StepConsts& c, const CgClusterPlan& p,
+                                   const uint32_t* ent, const double* b, double* y, StepScalars* st, cudaStream_t s)
+{
+    cudaError_t e = cg_cluster_attrs();
+    if (e != cudaSuccess) return e;
+    cudaLaunchConfig_t cfg;
+    cudaLaunchAttribute at;
+    cluster_config(cfg, at, p, s);
+    e = cudaLaunchKernelEx(&cfg, k_cg_cluster_fp64, m, c, p, ent, b, y, st);
     launch_counter()++;
+    return e;
 }
 
 // ---- launchers ----

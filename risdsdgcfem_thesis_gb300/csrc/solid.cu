@@ -107,6 +107,10 @@ struct fem_solid_s {
     DevBuf<double> Dinv, mat, vol, R, detF, eout;
     DevBuf<uint32_t> csr_ptr, csr_idx;
     DevBuf<uint8_t> fixed;
+    // the one-cluster CG of a small solid (ctas 0: none); cl_ent as csr_idx,
+    // each entry as the owning CTA and its local corner
+    CgClusterPlan cl_plan{};
+    DevBuf<uint32_t> cl_ent;
     // node vectors
     DevBuf<double> rest, x, v, y, b, r, d, q, tmp;
     DevBuf<double> xn, vn;  // FIE: x^n and v^n of the step (allocated for the FIE integrators only)
@@ -187,6 +191,7 @@ struct fem_solid_s {
         tets.release();
         csr_ptr.release();
         csr_idx.release();
+        cl_ent.release();
         fixed.release();
         knc_nodes.release();
         st.release();
@@ -336,15 +341,42 @@ int open_step(fem_solid s)
     return FEM_OK;
 }
 
-// A C_WRP solid small enough for the one-block CG kernel (its iteration a
-// few block barriers on shared memory instead of six launches; the FP64
-// element products of one SM bound it, so one block only wins while there
-// are few: 16.9 us per iteration at 160 tets against 33.8 for the graph
-// loop, 65 against 37 at 1,080 tets).
-constexpr uint32_t kCgBlockMaxTets = 256, kCgBlockMaxNodes = 256;
-bool cg_in_one_block(const fem_solid s)
+// A C_WRP solid with a one-cluster CG plan. GB300's FP64 rate is about two
+// FMAs per clock per SM (one warp instruction per 16 clocks per sub-
+// partition), so a warp's 140-FMA element product takes about 9k clocks:
+// the plan puts at most one warp of elements on each sub-partition (128 per
+// CTA) over up to 16 CTAs, and its iteration is four cluster barriers
+// instead of six launches.
+bool cg_on_cluster(const fem_solid s)
 {
-    return s->params.material == FEM_MATERIAL_C_WRP && s->T <= kCgBlockMaxTets && s->N <= kCgBlockMaxNodes;
+    return s->params.material == FEM_MATERIAL_C_WRP && s->cl_plan.ctas > 0;
+}
+
+// The one-cluster CG plan of a solid (see cg_on_cluster): 128 elements per
+// CTA on ceil(T / 128) CTAs, or the fewest CTAs below that a resident
+// cluster fits (at most kCgClusterMaxThreads elements per CTA); none when
+// the solid is too large. ptr: the node CSR's row starts.
+CgClusterPlan plan_cg_cluster(uint32_t N, uint32_t T, const std::vector<uint32_t>& ptr)
+{
+    if (T == 0 || N == 0) return CgClusterPlan{};
+    const uint32_t want = std::min<uint32_t>(kCgClusterMaxCtas, std::max<uint32_t>(1u, (T + 127) / 128));
+    for (uint32_t C = want; C >= 1; C--) {
+        CgClusterPlan p{};
+        p.ctas = C;
+        p.ept = (T + C - 1) / C;
+        if (p.ept > kCgClusterMaxThreads) break;  // fewer CTAs only take more
+        p.npt = (N + C - 1) / C;
+        uint32_t emax = 0;
+        for (uint32_t r = 0; r < C; r++) {
+            const uint32_t a = std::min(N, r * p.npt), b = std::min(N, (r + 1) * p.npt);
+            emax = std::max(emax, ptr[b] - ptr[a]);
+        }
+        p.ent_max = emax;
+        p.threads = std::min<uint32_t>(kCgClusterMaxThreads, std::max<uint32_t>(128u, (p.ept + 31) / 32 * 32));
+        p.smem = cg_cluster_smem_bytes(p.ept, p.npt, p.ent_max);
+        if (cg_cluster_fits(p)) return p;
+    }
+    return CgClusterPlan{};
 }
 
 // ILSS_CG::Solve (ILSS_CG.h:38-151) of A y = b from the warm start in y,
@@ -355,8 +387,8 @@ int cg_solve(fem_solid s, const StepConsts& c, int chunk)
 {
     cudaStream_t st = s->stream;
     MeshView<double> m = s->view();
-    if (cg_in_one_block(s)) {
-        launch_cg_block_fp64(m, c, s->b.p, s->y.p, s->st.p, st);
+    if (cg_on_cluster(s)) {
+        CK(launch_cg_cluster_fp64(m, c, s->cl_plan, s->cl_ent.p, s->b.p, s->y.p, s->st.p, st));
         CK(cudaMemcpyAsync(s->st_host, s->st.p, sizeof(StepScalars), cudaMemcpyDeviceToHost, st));
         CK(cudaStreamSynchronize(st));
         CK(cudaGetLastError());
@@ -441,10 +473,8 @@ cudaError_t ls_solve_capture(fem_solid s, const StepConsts& c, cudaGraph_t top)
     cudaStream_t st = s->stream;
     MeshView<double> m = s->view();
     const uint32_t gN = grid_for(s->N), gV = grid_for(3 * s->N);
-    if (s->params.ls_solver != FEM_LS_MINRES && cg_in_one_block(s)) {
-        launch_cg_block_fp64(m, c, s->b.p, s->y.p, s->st.p, st);
-        return cudaGetLastError();
-    }
+    if (s->params.ls_solver != FEM_LS_MINRES && cg_on_cluster(s))
+        return launch_cg_cluster_fp64(m, c, s->cl_plan, s->cl_ent.p, s->b.p, s->y.p, s->st.p, st);
     cudaGraphConditionalHandle cond = 0;
     cudaError_t e = cudaGraphConditionalHandleCreate(&cond, top, 0, cudaGraphCondAssignDefault);
     if (e != cudaSuccess) return e;
@@ -882,6 +912,17 @@ int fem_solid_create(const double* rest_xyz, uint32_t N, const uint32_t* tets, u
     CKC(cudaMemcpyAsync(s->vol.p, vol.data(), sizeof(double) * T, cudaMemcpyHostToDevice, st));
     CKC(cudaMemcpyAsync(s->csr_ptr.p, ptr.data(), sizeof(uint32_t) * (N + 1), cudaMemcpyHostToDevice, st));
     CKC(cudaMemcpyAsync(s->csr_idx.p, idx.data(), sizeof(uint32_t) * idx.size(), cudaMemcpyHostToDevice, st));
+    s->cl_plan = plan_cg_cluster(N, T, ptr);
+    if (s->cl_plan.ctas) {
+        std::vector<uint32_t> ent(idx.size());
+        for (size_t j = 0; j < idx.size(); j++) {
+            const uint32_t e = idx[j] >> 2, r = e / s->cl_plan.ept;
+            ent[j] = (r << 24) | (4 * (e - r * s->cl_plan.ept) + (idx[j] & 3));
+        }
+        CKC(s->cl_ent.alloc(ent.size()));
+        CKC(cudaMemcpyAsync(s->cl_ent.p, ent.data(), sizeof(uint32_t) * ent.size(), cudaMemcpyHostToDevice, st));
+        CKC(cudaStreamSynchronize(st));
+    }
     CKC(cudaMemsetAsync(s->fixed.p, 0, N, st));
     CKC(cudaMemcpyAsync(s->rest.p, rest_xyz, sizeof(double) * n3, cudaMemcpyHostToDevice, st));
     CKC(cudaMemcpyAsync(s->x.p, rest_xyz, sizeof(double) * n3, cudaMemcpyHostToDevice, st));
