@@ -211,8 +211,9 @@ void launch_finalize(int kind, const double* partials, uint32_t count, const Ste
 // its dynamic shared memory (cg_cluster_smem_bytes).
 constexpr uint32_t kCgClusterMaxCtas = 16, kCgClusterMaxThreads = 512;
 constexpr size_t kCgClusterMaxSmem = 200 * 1024;
+// split: three lanes per element (ten elements per warp), else one.
 struct CgClusterPlan {
-    uint32_t ctas, threads, ept, npt, ent_max;
+    uint32_t ctas, threads, ept, npt, ent_max, split;
     size_t smem;
 };
 size_t cg_cluster_smem_bytes(uint32_t ept, uint32_t npt, uint32_t ent_max);

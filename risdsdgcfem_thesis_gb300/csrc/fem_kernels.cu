@@ -826,14 +826,69 @@ __global__ void k_finalize(int kind, const double* __restrict__ partials, uint32
         cudaGraphSetConditional(cond, st->done ? 0u : 1u);
 }
 
+// elem_RKRt over three lanes of a warp (lane a of lanes 3g..3g+2 computes
+// component a): u_i = R^T d_i, the element-frame gradient row a, the stress
+// row a after exchanging the gradient's diagonal and column a, the force
+// row a, and after exchanging the force rows component a of R P (node 0:
+// minus the sum). About 50 FP64 instructions per lane against 140 for one
+// lane; GB300 gives a warp's FP64 instruction about 64 clocks whatever the
+// lanes, so a few warps of elements take a third of the time. Every lane of
+// the warp must call it (invalid lanes with zeros); out4 = component a of
+// nodes 0..3.
+// Rc: column a of R; Rr: row a of R as (R[a][a], R[a][a+1], R[a][a+2])
+// (indexes mod 3).
+__device__ __forceinline__ void elem_RKRt_lanes(const double* Rc, const double* Rr, const double* Di, double k1,
+                                                double knu, double k2, const double* d, uint32_t a, uint32_t base,
+                                                double* out4)
+{
+    const uint32_t l1 = base + (a == 2 ? 0u : a + 1), l2 = base + (a == 0 ? 2u : a - 1);  // lanes of a+1, a+2 (mod 3)
+    double u[4];
+#pragma unroll
+    for (int i = 0; i < 4; i++) u[i] = Rc[0] * d[3 * i] + Rc[1] * d[3 * i + 1] + Rc[2] * d[3 * i + 2];
+    const double D0 = u[1] - u[0], D1 = u[2] - u[0], D2 = u[3] - u[0];
+    double H[3];  // row a of the element-frame gradient
+#pragma unroll
+    for (int b = 0; b < 3; b++) H[b] = D0 * Di[b] + D1 * Di[3 + b] + D2 * Di[6 + b];
+    // the lane of component b sends H[b][a'] for the receiver a' = b - 1 or b - 2
+    const double Ha = a == 0 ? H[0] : (a == 1 ? H[1] : H[2]);
+    const double send1 = a == 0 ? H[2] : (a == 1 ? H[0] : H[1]);  // to a - 1
+    const double send2 = a == 0 ? H[1] : (a == 1 ? H[2] : H[0]);  // to a - 2
+    const double e1 = __shfl_sync(0xffffffffu, Ha, l1), e2 = __shfl_sync(0xffffffffu, Ha, l2);
+    const double c1 = __shfl_sync(0xffffffffu, send1, l1), c2 = __shfl_sync(0xffffffffu, send2, l2);
+    const double h1 = a == 0 ? H[1] : (a == 1 ? H[2] : H[0]), h2 = a == 0 ? H[2] : (a == 1 ? H[0] : H[1]);
+    const double saa = k1 * Ha + knu * (e1 + e2);
+    const double s1 = k2 * (h1 + c1), s2 = k2 * (h2 + c2);
+    double Sg[3];  // row a of the stress
+    Sg[0] = a == 0 ? saa : (a == 1 ? s2 : s1);
+    Sg[1] = a == 1 ? saa : (a == 2 ? s2 : s1);
+    Sg[2] = a == 2 ? saa : (a == 0 ? s2 : s1);
+    double P[3];
+#pragma unroll
+    for (int i = 0; i < 3; i++) P[i] = Sg[0] * Di[3 * i] + Sg[1] * Di[3 * i + 1] + Sg[2] * Di[3 * i + 2];
+    double Q1[3], Q2[3];
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        Q1[i] = __shfl_sync(0xffffffffu, P[i], l1);
+        Q2[i] = __shfl_sync(0xffffffffu, P[i], l2);
+    }
+    double w[3];
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        w[i] = Rr[0] * P[i] + Rr[1] * Q1[i] + Rr[2] * Q2[i];
+        out4[i + 1] = w[i];
+    }
+    out4[0] = -(w[0] + w[1] + w[2]);
+}
+
 // The whole of ILSS_CG::Solve (ILSS_CG.h:38-151) for a C_WRP solid of up to
 // kCgClusterMaxCtas x kCgClusterMaxThreads tets on one thread-block cluster,
 // on chip. CTA r owns the elements [r ept, (r+1) ept) and the nodes
-// [r npt, (r+1) npt): each thread keeps one element's R, Dm^-1 and material
-// scalars in registers and its element output in its CTA's shared memory;
-// the CTA keeps its nodes' y, r, d, q, b, CSR rows and fixed flags. An
-// element product reads its four nodes' d from the owning CTAs' shared
-// memory (distributed shared memory); a node's gather reads its element
+// [r npt, (r+1) npt): a thread (kSplit: three lanes, elem_RKRt_lanes)
+// keeps one element's R, Dm^-1 and material scalars in registers and its
+// element output in its CTA's shared memory; the CTA keeps its nodes' y,
+// r, d, q, b, CSR rows and fixed flags. An element product reads its four
+// nodes' d from the owning CTAs' shared memory (distributed shared memory);
+// a node component's gather (one thread per component) reads its element
 // corners' outputs the same way (ent: per CSR entry, the owning CTA << 24 |
 // its local corner). A reduction sums each CTA's block total into a slot of
 // every CTA, then every CTA adds the slots in rank order, so all CTAs take
@@ -841,6 +896,7 @@ __global__ void k_finalize(int kind, const double* __restrict__ partials, uint32
 // per iteration: element outputs complete, d.q, |r|^2, the new d. y and the
 // statistics are written back at the end; the loop ends on the solver's own
 // tests (at most max_iter iterations).
+template <int kSplit>
 __global__ void __launch_bounds__(kCgClusterMaxThreads, 1)
     k_cg_cluster_fp64(MeshView<double> m, StepConsts c, CgClusterPlan p, const uint32_t* __restrict__ ent,
                       const double* __restrict__ b, double* y, StepScalars* st)
@@ -875,12 +931,31 @@ __global__ void __launch_bounds__(kCgClusterMaxThreads, 1)
     for (uint32_t i = tid; i < ne_ent; i += nt) cent[i] = ent[base + i];
     for (uint32_t i = tid; i < nn; i += nt) fx[i] = m.fixed[n0 + i];
     if (tid == 0) sst = *st;
-    // this thread's element (tid < ne) and where its nodes live
+    // this thread's element and where its nodes live: element tid, or with
+    // kSplit lane 3g + a (a < 3, g < 10) of warp w takes component a of
+    // element 10 w + g
+    const uint32_t lane = tid & 31, ca = kSplit ? lane % 3 : 0u, cbase = lane - ca;
+    const uint32_t le = kSplit ? (lane < 30 ? 10 * (tid >> 5) + lane / 3 : 0xffffffffu) : tid;
+    const bool has_elem = le < ne;
     double R[9], Di[9], k1 = 0, knu = 0, k2 = 0;
+#pragma unroll
+    for (int k = 0; k < 9; k++) R[k] = Di[k] = 0.0;
+    double Rc[3] = {0, 0, 0}, Rr[3] = {0, 0, 0};  // kSplit: column a of R, row a from (a, a)
     uint32_t nr[4] = {0, 0, 0, 0}, nl[4] = {0, 0, 0, 0};
-    if (tid < ne) {
-        load_elem(m, e0 + tid, R, Di, k1, knu, k2);
-        const int4 t = m.tets[e0 + tid];
+    if (has_elem) {
+        load_elem(m, e0 + le, R, Di, k1, knu, k2);
+        if constexpr (kSplit != 0) {
+            double row[3];
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                Rc[k] = ca == 0 ? R[3 * k] : (ca == 1 ? R[3 * k + 1] : R[3 * k + 2]);
+                row[k] = ca == 0 ? R[k] : (ca == 1 ? R[3 + k] : R[6 + k]);
+            }
+            Rr[0] = ca == 0 ? row[0] : (ca == 1 ? row[1] : row[2]);
+            Rr[1] = ca == 0 ? row[1] : (ca == 1 ? row[2] : row[0]);
+            Rr[2] = ca == 0 ? row[2] : (ca == 1 ? row[0] : row[1]);
+        }
+        const int4 t = m.tets[e0 + le];
         const uint32_t ids[4] = {bounds_idx((uint32_t)t.x, N, kSiteElemNode), bounds_idx((uint32_t)t.y, N, kSiteElemNode),
                                  bounds_idx((uint32_t)t.z, N, kSiteElemNode), bounds_idx((uint32_t)t.w, N, kSiteElemNode)};
 #pragma unroll
@@ -894,30 +969,37 @@ __global__ void __launch_bounds__(kCgClusterMaxThreads, 1)
     for (int k = 0; k < 4; k++) pd[k] = cl.map_shared_rank(vd, nr[k]) + nl[k];
     cl.sync();  // every CTA's y, d and CSR rows are in place
     auto elem_products = [&](const double* const* u) {
-        if (tid < ne) {
-            double dl[12];
+        double dl[12];
 #pragma unroll
-            for (int k = 0; k < 4; k++) {
-                dl[3 * k] = u[k][0];
-                dl[3 * k + 1] = u[k][1];
-                dl[3 * k + 2] = u[k][2];
-            }
+        for (int k = 0; k < 4; k++) {
+            dl[3 * k] = has_elem ? u[k][0] : 0.0;
+            dl[3 * k + 1] = has_elem ? u[k][1] : 0.0;
+            dl[3 * k + 2] = has_elem ? u[k][2] : 0.0;
+        }
+        if constexpr (kSplit != 0) {
+            double o4[4];
+            elem_RKRt_lanes(Rc, Rr, Di, k1, knu, k2, dl, ca, cbase, o4);
+            if (has_elem)
+#pragma unroll
+                for (int k = 0; k < 4; k++) eo[12 * le + 3 * k + ca] = o4[k];
+        } else if (has_elem) {
             double out[12];
             elem_RKRt(R, Di, k1, knu, k2, dl, out);
 #pragma unroll
-            for (int k = 0; k < 12; k++) eo[12 * tid + k] = out[k];
+            for (int k = 0; k < 12; k++) eo[12 * le + k] = out[k];
         }
         cl.sync();  // all element outputs complete
     };
-    auto gather = [&](uint32_t ln, double& a0, double& a1, double& a2) {
+    // component a of node ln's element sum
+    auto gather = [&](uint32_t ln, uint32_t a) {
         const uint32_t jend = min(cptr[ln + 1], ne_ent);
+        double acc = 0.0;
+#pragma unroll 4
         for (uint32_t j = cptr[ln]; j < jend; j++) {
             const uint32_t e = cent[j];
-            const double* o = cl.map_shared_rank(eo, e >> 24) + 3 * (e & 0xffffffu);
-            a0 += o[0];
-            a1 += o[1];
-            a2 += o[2];
+            acc += cl.map_shared_rank(eo, e >> 24)[3 * (e & 0xffffffu) + a];
         }
+        return acc;
     };
     // the cluster's total of every thread's acc (valid in thread 0)
     auto cluster_total = [&](double acc, int slot) -> double {
@@ -938,19 +1020,13 @@ __global__ void __launch_bounds__(kCgClusterMaxThreads, 1)
         elem_products(py);
     }
     double acc = 0.0;
-    for (uint32_t ln = tid; ln < nn; ln += nt) {
-        double s0 = 0, s1 = 0, s2 = 0;
-        gather(ln, s0, s1, s2);
-        const uint32_t i = 3 * ln;
-        double r0 = 0, r1 = 0, r2 = 0;
-        if (!fx[ln]) {
-            r0 = vb[i] - (c.factor_K * s0 + mfm * vy[i]);
-            r1 = vb[i + 1] - (c.factor_K * s1 + mfm * vy[i + 1]);
-            r2 = vb[i + 2] - (c.factor_K * s2 + mfm * vy[i + 2]);
-        }
-        vr[i] = r0; vr[i + 1] = r1; vr[i + 2] = r2;
-        vd[i] = r0; vd[i + 1] = r1; vd[i + 2] = r2;
-        acc += r0 * r0 + r1 * r1 + r2 * r2;
+    for (uint32_t i = tid; i < n3; i += nt) {
+        const uint32_t ln = i / 3;
+        const double s = gather(ln, i - 3 * ln);
+        const double ri = fx[ln] ? 0.0 : vb[i] - (c.factor_K * s + mfm * vy[i]);
+        vr[i] = ri;
+        vd[i] = ri;
+        acc += ri * ri;
     }
     double total = cluster_total(acc, 0);
     if (tid == 0) fin_init(&sst, c, total);
@@ -959,18 +1035,12 @@ __global__ void __launch_bounds__(kCgClusterMaxThreads, 1)
         // q = S A d, d.q, alpha
         elem_products(pd);
         acc = 0.0;
-        for (uint32_t ln = tid; ln < nn; ln += nt) {
-            double s0 = 0, s1 = 0, s2 = 0;
-            gather(ln, s0, s1, s2);
-            const uint32_t i = 3 * ln;
-            double q0 = 0, q1 = 0, q2 = 0;
-            if (!fx[ln]) {
-                q0 = c.factor_K * s0 + mfm * vd[i];
-                q1 = c.factor_K * s1 + mfm * vd[i + 1];
-                q2 = c.factor_K * s2 + mfm * vd[i + 2];
-            }
-            vq[i] = q0; vq[i + 1] = q1; vq[i + 2] = q2;
-            acc += vd[i] * q0 + vd[i + 1] * q1 + vd[i + 2] * q2;
+        for (uint32_t i = tid; i < n3; i += nt) {
+            const uint32_t ln = i / 3;
+            const double s = gather(ln, i - 3 * ln);
+            const double qi = fx[ln] ? 0.0 : c.factor_K * s + mfm * vd[i];
+            vq[i] = qi;
+            acc += vd[i] * qi;
         }
         total = cluster_total(acc, 1);
         if (tid == 0) fin_alpha(&sst, total);
@@ -1009,12 +1079,14 @@ size_t cg_cluster_smem_bytes(uint32_t ept, uint32_t npt, uint32_t ent_max)
 }
 
 namespace {
+template <int kSplit>
 cudaError_t cg_cluster_attrs()
 {
     static const cudaError_t e = [] {
-        cudaError_t r = cudaFuncSetAttribute(k_cg_cluster_fp64, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        cudaError_t r = cudaFuncSetAttribute(k_cg_cluster_fp64<kSplit>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)kCgClusterMaxSmem);
-        if (r == cudaSuccess) r = cudaFuncSetAttribute(k_cg_cluster_fp64, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+        if (r == cudaSuccess)
+            r = cudaFuncSetAttribute(k_cg_cluster_fp64<kSplit>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
         return r;
     }();
     return e;
@@ -1038,13 +1110,17 @@ void cluster_config(cudaLaunchConfig_t& cfg, cudaLaunchAttribute& at, const CgCl
 bool cg_cluster_fits(const CgClusterPlan& p)
 {
     if (p.ctas < 1 || p.ctas > kCgClusterMaxCtas || p.threads < 32 || p.threads > kCgClusterMaxThreads ||
-        p.smem > kCgClusterMaxSmem || cg_cluster_attrs() != cudaSuccess)
+        p.threads % 32 || p.smem > kCgClusterMaxSmem ||
+        p.ept > (p.split ? 10 * (p.threads / 32) : p.threads) ||
+        (p.split ? cg_cluster_attrs<1>() : cg_cluster_attrs<0>()) != cudaSuccess)
         return false;
     cudaLaunchConfig_t cfg;
     cudaLaunchAttribute at;
     cluster_config(cfg, at, p, nullptr);
     int n = 0;
-    if (cudaOccupancyMaxActiveClusters(&n, k_cg_cluster_fp64, &cfg) != cudaSuccess) {
+    const cudaError_t e = p.split ? cudaOccupancyMaxActiveClusters(&n, k_cg_cluster_fp64<1>, &cfg)
+                                  : cudaOccupancyMaxActiveClusters(&n, k_cg_cluster_fp64<0>, &cfg);
+    if (e != cudaSuccess) {
         cudaGetLastError();
         return false;
     }
@@ -1054,12 +1130,13 @@ bool cg_cluster_fits(const CgClusterPlan& p)
 cudaError_t launch_cg_cluster_fp64(const MeshView<double>& m, const StepConsts& c, const CgClusterPlan& p,
                                    const uint32_t* ent, const double* b, double* y, StepScalars* st, cudaStream_t s)
 {
-    cudaError_t e = cg_cluster_attrs();
+    cudaError_t e = p.split ? cg_cluster_attrs<1>() : cg_cluster_attrs<0>();
     if (e != cudaSuccess) return e;
     cudaLaunchConfig_t cfg;
     cudaLaunchAttribute at;
     cluster_config(cfg, at, p, s);
-    e = cudaLaunchKernelEx(&cfg, k_cg_cluster_fp64, m, c, p, ent, b, y, st);
+    e = p.split ? cudaLaunchKernelEx(&cfg, k_cg_cluster_fp64<1>, m, c, p, ent, b, y, st)
+                : cudaLaunchKernelEx(&cfg, k_cg_cluster_fp64<0>, m, c, p, ent, b, y, st);
     launch_counter()++;
     return e;
 }

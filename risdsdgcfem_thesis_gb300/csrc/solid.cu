@@ -341,30 +341,31 @@ int open_step(fem_solid s)
     return FEM_OK;
 }
 
-// A C_WRP solid with a one-cluster CG plan. GB300's FP64 rate is about two
-// FMAs per clock per SM (one warp instruction per 16 clocks per sub-
-// partition), so a warp's 140-FMA element product takes about 9k clocks:
-// the plan puts at most one warp of elements on each sub-partition (128 per
-// CTA) over up to 16 CTAs, and its iteration is four cluster barriers
-// instead of six launches.
+// A C_WRP solid with a one-cluster CG plan. GB300 gives a warp's FP64
+// instruction about 64 clocks whatever its active lanes, and an SM about
+// one every 19 clocks over all its warps: a 140-instruction element product
+// takes about 9k clocks, so the plan spreads the elements thin (at most a
+// few warps of them per SM) over up to 16 CTAs, and its iteration is four
+// cluster barriers instead of six launches.
 bool cg_on_cluster(const fem_solid s)
 {
     return s->params.material == FEM_MATERIAL_C_WRP && s->cl_plan.ctas > 0;
 }
 
-// The one-cluster CG plan of a solid (see cg_on_cluster): 128 elements per
-// CTA on ceil(T / 128) CTAs, or the fewest CTAs below that a resident
-// cluster fits (at most kCgClusterMaxThreads elements per CTA); none when
-// the solid is too large. ptr: the node CSR's row starts.
+// The one-cluster CG plan of a solid (see cg_on_cluster). Up to 1,440 tets,
+// three lanes per element (about 50 FP64 instructions each) and 30
+// elements per CTA on ceil(T / 30) CTAs; beyond, one lane per element and
+// 128 per CTA on ceil(T / 128). When a cluster of that size does not fit,
+// the fewest CTAs below it that do, with at most kCgClusterMaxThreads
+// threads; none when the solid is too large. ptr: the node CSR's row starts.
 CgClusterPlan plan_cg_cluster(uint32_t N, uint32_t T, const std::vector<uint32_t>& ptr)
 {
     if (T == 0 || N == 0) return CgClusterPlan{};
-    const uint32_t want = std::min<uint32_t>(kCgClusterMaxCtas, std::max<uint32_t>(1u, (T + 127) / 128));
-    for (uint32_t C = want; C >= 1; C--) {
-        CgClusterPlan p{};
+    auto try_plan = [&](uint32_t C, uint32_t split, CgClusterPlan& p) {
+        p = CgClusterPlan{};
         p.ctas = C;
+        p.split = split;
         p.ept = (T + C - 1) / C;
-        if (p.ept > kCgClusterMaxThreads) break;  // fewer CTAs only take more
         p.npt = (N + C - 1) / C;
         uint32_t emax = 0;
         for (uint32_t r = 0; r < C; r++) {
@@ -372,9 +373,21 @@ CgClusterPlan plan_cg_cluster(uint32_t N, uint32_t T, const std::vector<uint32_t
             emax = std::max(emax, ptr[b] - ptr[a]);
         }
         p.ent_max = emax;
-        p.threads = std::min<uint32_t>(kCgClusterMaxThreads, std::max<uint32_t>(128u, (p.ept + 31) / 32 * 32));
+        const uint32_t need = split ? 32 * ((p.ept + 9) / 10) : (p.ept + 31) / 32 * 32;
+        p.threads = std::max<uint32_t>(128u, need);
         p.smem = cg_cluster_smem_bytes(p.ept, p.npt, p.ent_max);
-        if (cg_cluster_fits(p)) return p;
+        return p.threads <= kCgClusterMaxThreads && cg_cluster_fits(p);
+    };
+    CgClusterPlan p{};
+    if (T <= 1440) {
+        const uint32_t want = std::min<uint32_t>(kCgClusterMaxCtas, std::max<uint32_t>(1u, (T + 29) / 30));
+        for (uint32_t C = want; C >= 1; C--)
+            if (try_plan(C, 1, p)) return p;
+    }
+    const uint32_t want = std::min<uint32_t>(kCgClusterMaxCtas, std::max<uint32_t>(1u, (T + 127) / 128));
+    for (uint32_t C = want; C >= 1; C--) {
+        if ((T + C - 1) / C > kCgClusterMaxThreads) break;  // fewer CTAs only take more
+        if (try_plan(C, 0, p)) return p;
     }
     return CgClusterPlan{};
 }
