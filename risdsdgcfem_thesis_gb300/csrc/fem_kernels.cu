@@ -1002,14 +1002,28 @@ __global__ void __launch_bounds__(kCgClusterMaxThreads, 1)
         return acc;
     };
     // the cluster's total of every thread's acc (valid in thread 0)
+    // (each FP64 add costs a warp about 64 clocks: the CTA's warp totals and
+    // the CTAs' totals are added in shuffle trees of log2 depth, the same
+    // fixed trees in every CTA)
+    __shared__ double wsum[kCgClusterMaxThreads / 32];
+    const uint32_t nw = nt >> 5;
+    const uint32_t wtop = nw > 1 ? 1u << (31 - __clz(nw - 1)) : 0u, ctop = C > 1 ? 1u << (31 - __clz(C - 1)) : 0u;
     auto cluster_total = [&](double acc, int slot) -> double {
-        const double v = block_sum(acc);
-        if (tid == 0)
-            for (uint32_t r = 0; r < C; r++) cl.map_shared_rank(part, r)[slot * kCgClusterMaxCtas + rank] = v;
+        double v = warp_sum(acc);
+        if (lane == 0) wsum[tid >> 5] = v;
+        __syncthreads();
+        if (tid < 32) {
+            v = lane < nw ? wsum[lane] : 0.0;
+            for (uint32_t o = wtop; o >= 1; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            v = __shfl_sync(0xffffffffu, v, 0);
+            if (lane < C) cl.map_shared_rank(part, lane)[slot * kCgClusterMaxCtas + rank] = v;
+        }
         cl.sync();
         double total = 0.0;
-        if (tid == 0)
-            for (uint32_t r = 0; r < C; r++) total += part[slot * kCgClusterMaxCtas + r];
+        if (tid < 32) {
+            total = lane < C ? part[slot * kCgClusterMaxCtas + lane] : 0.0;
+            for (uint32_t o = ctop; o >= 1; o >>= 1) total += __shfl_xor_sync(0xffffffffu, total, o);
+        }
         return total;
     };
     // r = S(b - A y), d = r, |r|^2
