@@ -26,6 +26,7 @@ enum BoundsSite : uint32_t {
     kSiteLocalNode = 5,    // batch: tile-local node id >= the tile's node count
     kSitePartialSlot = 6,  // batch: partial slot >= the batch's slot count
     kSiteTileEntry = 7,    // batch: tile-local CSR entry >= 4 ne4
+    kSiteBsrEntry = 8,     // FP64 solid: assembled block's column >= N, or its element >= T
 };
 
 #ifdef FEM_BOUNDS_CHECK

@@ -119,6 +119,13 @@ struct MeshView {
     const uint32_t* csr_idx;     // [4T]
     const uint8_t* fixed;        // [N]
     S* eout;                     // [12T]
+    // FP64 solid: the assembled stiffness K = sum_e R K0 R^T as 3x3 blocks
+    // (row starts [N+1], columns [nnzb], blocks [nnzb][9] row-major); when
+    // set, the solvers' node kernels take K u from it instead of gathering
+    // the element outputs
+    const uint32_t* bsr_row = nullptr;
+    const uint32_t* bsr_col = nullptr;
+    const double* bsr_val = nullptr;
 };
 
 struct StepConsts {
@@ -204,6 +211,12 @@ enum FinalizeKind {
 // "the loop goes on"
 void launch_finalize(int kind, const double* partials, uint32_t count, const StepConsts& c, StepScalars* st,
                      cudaStream_t s, cudaGraphConditionalHandle cond = 0, int set_cond = 0);
+
+// The assembled stiffness's blocks (MeshView::bsr_*): block slot s sums, in
+// element order, R K0[li][lj] R^T over its contributions contrib[cptr[s]..
+// cptr[s+1]) = element << 4 | li << 2 | lj.
+void launch_bsr_assemble_fp64(const MeshView<double>& m, uint32_t nnzb, const uint32_t* cptr,
+                              const uint32_t* contrib, double* val, cudaStream_t s);
 
 // The whole CG solve of a small C_WRP solid on one thread-block cluster
 // (fem_kernels.cu): CTA r of `ctas` owns the elements [r ept, (r+1) ept) and

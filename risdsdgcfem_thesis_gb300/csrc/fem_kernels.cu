@@ -357,6 +357,85 @@ __device__ __forceinline__ void gather3(const MeshView<double>& m, uint32_t n, d
     }
 }
 
+// K u at node n for the solvers' node kernels: the assembled row when the
+// solid has one (9 FMAs per block), else the gather of the element outputs
+// of the product the solver launched before.
+__device__ __forceinline__ void node_Ku(const MeshView<double>& m, const double* __restrict__ u, uint32_t n,
+                                        double& a0, double& a1, double& a2)
+{
+    if (m.bsr_val) {
+        const uint32_t beg = m.bsr_row[n], end = m.bsr_row[n + 1];
+        for (uint32_t k = beg; k < end; k++) {
+            const size_t j = 3 * (size_t)bounds_idx(m.bsr_col[k], m.N, kSiteBsrEntry);
+            const double* A = m.bsr_val + 9 * (size_t)k;
+            const double u0 = u[j], u1 = u[j + 1], u2 = u[j + 2];
+            a0 = fma(A[0], u0, a0);
+            a0 = fma(A[1], u1, a0);
+            a0 = fma(A[2], u2, a0);
+            a1 = fma(A[3], u0, a1);
+            a1 = fma(A[4], u1, a1);
+            a1 = fma(A[5], u2, a1);
+            a2 = fma(A[6], u0, a2);
+            a2 = fma(A[7], u1, a2);
+            a2 = fma(A[8], u2, a2);
+        }
+    } else {
+        gather3(m, n, a0, a1, a2);
+    }
+}
+
+// One block of the assembled stiffness per thread (see
+// launch_bsr_assemble_fp64). The element block in the element frame, from
+// the strain form of elem_RKRt (g_i the shape gradients: rows of Dm^-1,
+// node 0 minus their sum; k1 = V(lambda + 2 mu), knu = V lambda, k2 = V mu):
+// K0[a][a] = k1 gi_a gj_a + k2 (gi.gj - gi_a gj_a),
+// K0[a][b] = knu gi_a gj_b + k2 gj_a gi_b (a != b); the world block R K0 R^T.
+__global__ void k_bsr_assemble_fp64(MeshView<double> m, uint32_t nnzb, const uint32_t* __restrict__ cptr,
+                                    const uint32_t* __restrict__ contrib, double* __restrict__ val)
+{
+    for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < nnzb; s += gridDim.x * blockDim.x) {
+        double acc[9];
+#pragma unroll
+        for (int k = 0; k < 9; k++) acc[k] = 0.0;
+        for (uint32_t k = cptr[s]; k < cptr[s + 1]; k++) {
+            const uint32_t cb = contrib[k], e = bounds_idx(cb >> 4, m.T, kSiteBsrEntry);
+            const uint32_t li = (cb >> 2) & 3u, lj = cb & 3u;
+            double R[9], Di[9], k1, knu, k2;
+            load_elem(m, e, R, Di, k1, knu, k2);
+            double gi[3], gj[3];
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                const double g0 = -(Di[c] + Di[3 + c] + Di[6 + c]);
+                gi[c] = li == 0 ? g0 : (li == 1 ? Di[c] : (li == 2 ? Di[3 + c] : Di[6 + c]));
+                gj[c] = lj == 0 ? g0 : (lj == 1 ? Di[c] : (lj == 2 ? Di[3 + c] : Di[6 + c]));
+            }
+            const double dot = gi[0] * gj[0] + gi[1] * gj[1] + gi[2] * gj[2];
+            double K0[9];
+#pragma unroll
+            for (int a = 0; a < 3; a++)
+#pragma unroll
+                for (int b = 0; b < 3; b++) {
+                    const double p = gi[a] * gj[b];
+                    K0[3 * a + b] = a == b ? k1 * p + k2 * (dot - p) : knu * p + k2 * gj[a] * gi[b];
+                }
+            double T1[9];  // R K0
+#pragma unroll
+            for (int a = 0; a < 3; a++)
+#pragma unroll
+                for (int b = 0; b < 3; b++)
+                    T1[3 * a + b] = R[3 * a] * K0[b] + R[3 * a + 1] * K0[3 + b] + R[3 * a + 2] * K0[6 + b];
+#pragma unroll
+            for (int a = 0; a < 3; a++)
+#pragma unroll
+                for (int b = 0; b < 3; b++)
+                    acc[3 * a + b] += T1[3 * a] * R[3 * b] + T1[3 * a + 1] * R[3 * b + 1] + T1[3 * a + 2] * R[3 * b + 2];
+        }
+        double* o = val + 9 * (size_t)s;
+#pragma unroll
+        for (int k = 0; k < 9; k++) o[k] = acc[k];
+    }
+}
+
 // b = dt (m g + f_e) + m v ; y = v   (Step_QuasiImplicitEuler_v, :1211-1231)
 __global__ void k_node_b_fp64(MeshView<double> m, StepConsts c, const double* __restrict__ v, double* b, double* y)
 {
@@ -402,7 +481,7 @@ __global__ void k_node_residual_fp64(MeshView<double> m, StepConsts c, const dou
     const double mfm = c.mass * c.factor_M;
     for (uint32_t n = blockIdx.x * blockDim.x + threadIdx.x; n < m.N; n += gridDim.x * blockDim.x) {
         double s0 = 0, s1 = 0, s2 = 0;
-        gather3(m, n, s0, s1, s2);
+        node_Ku(m, y, n, s0, s1, s2);
         const size_t i = 3 * (size_t)n;
         double r0 = 0, r1 = 0, r2 = 0;
         if (!m.fixed[n]) {
@@ -427,7 +506,7 @@ __global__ void k_node_q_fp64(MeshView<double> m, StepConsts c, const double* __
     const double mfm = c.mass * c.factor_M;
     for (uint32_t n = blockIdx.x * blockDim.x + threadIdx.x; n < m.N; n += gridDim.x * blockDim.x) {
         double s0 = 0, s1 = 0, s2 = 0;
-        gather3(m, n, s0, s1, s2);
+        node_Ku(m, d, n, s0, s1, s2);
         const size_t i = 3 * (size_t)n;
         double q0 = 0, q1 = 0, q2 = 0;
         if (!m.fixed[n]) {
@@ -565,7 +644,7 @@ __global__ void k_mr_init_fp64(MeshView<double> m, StepConsts c, const double* _
     const double mfm = c.mass * c.factor_M;
     for (uint32_t n = blockIdx.x * blockDim.x + threadIdx.x; n < m.N; n += gridDim.x * blockDim.x) {
         double f[3] = {0, 0, 0};
-        gather3(m, n, f[0], f[1], f[2]);
+        node_Ku(m, y, n, f[0], f[1], f[2]);
         const size_t i = 3 * (size_t)n;
 #pragma unroll
         for (int a = 0; a < 3; a++) {
@@ -601,7 +680,7 @@ __global__ void k_mr_q_fp64(MeshView<double> m, StepConsts c, const double* __re
     double acc = 0.0;
     for (uint32_t n = blockIdx.x * blockDim.x + threadIdx.x; n < m.N; n += gridDim.x * blockDim.x) {
         double f[3] = {0, 0, 0};
-        gather3(m, n, f[0], f[1], f[2]);
+        node_Ku(m, v, n, f[0], f[1], f[2]);
         const size_t i = 3 * (size_t)n;
 #pragma unroll
         for (int a = 0; a < 3; a++) {
@@ -1231,6 +1310,13 @@ void launch_fie_update_fp64(uint32_t N, double inv_dt, double* x, double* v, con
                             double* partials, cudaStream_t s)
 {
     FEMGB_LAUNCH(k_fie_update_fp64, grid_for(3 * N), N, inv_dt, x, v, xn, y, partials);
+}
+void launch_bsr_assemble_fp64(const MeshView<double>& m, uint32_t nnzb, const uint32_t* cptr,
+                              const uint32_t* contrib, double* val, cudaStream_t s)
+{
+    prof_begin("bsr_assemble_fp64", s);
+    FEMGB_LAUNCH(k_bsr_assemble_fp64, grid_for(nnzb), m, nnzb, cptr, contrib, val);
+    prof_end("bsr_assemble_fp64", s);
 }
 void launch_mr_init_fp64(const MeshView<double>& m, const StepConsts& c, const double* b, const double* y,
                          double* v1, double* partials, cudaStream_t s)

@@ -111,6 +111,12 @@ struct fem_solid_s {
     // each entry as the owning CTA and its local corner
     CgClusterPlan cl_plan{};
     DevBuf<uint32_t> cl_ent;
+    // the assembled stiffness (MeshView::bsr_*): pattern, per-slot
+    // contributions and blocks; bsr_use: the solvers take it (set_bsr_use)
+    DevBuf<uint32_t> bsr_row, bsr_col, bsr_cptr, bsr_contrib;
+    DevBuf<double> bsr_val;
+    uint32_t bsr_nnzb = 0;
+    bool bsr_use = false;
     // node vectors
     DevBuf<double> rest, x, v, y, b, r, d, q, tmp;
     DevBuf<double> xn, vn;  // FIE: x^n and v^n of the step (allocated for the FIE integrators only)
@@ -178,12 +184,17 @@ struct fem_solid_s {
         m.csr_idx = csr_idx.p;
         m.fixed = fixed.p;
         m.eout = eout.p;
+        if (bsr_use) {
+            m.bsr_row = bsr_row.p;
+            m.bsr_col = bsr_col.p;
+            m.bsr_val = bsr_val.p;
+        }
         return m;
     }
 
     void release()
     {
-        DevBuf<double>* dbl[] = {&Dinv, &mat, &vol, &R, &detF, &eout, &rest, &x, &v, &y, &b, &r, &d, &q, &tmp,
+        DevBuf<double>* dbl[] = {&Dinv, &mat, &vol, &R, &detF, &eout, &bsr_val, &rest, &x, &v, &y, &b, &r, &d, &q, &tmp,
                                  &xn, &vn, &prev_x, &mr_p, &mr_p0, &Fe, &knc_targets, &partials, &partials2,
                                  &lk_x, &lk_v};
         for (auto* p : dbl) p->release();
@@ -192,6 +203,10 @@ struct fem_solid_s {
         csr_ptr.release();
         csr_idx.release();
         cl_ent.release();
+        bsr_row.release();
+        bsr_col.release();
+        bsr_cptr.release();
+        bsr_contrib.release();
         fixed.release();
         knc_nodes.release();
         st.release();
@@ -308,6 +323,8 @@ void begin_eval(fem_solid s, const double* xprev, const double* x)
         launch_begin_eval_dapd_fp64(m, xprev, x, s->doc.p, s->dapd, F_out, s->st.p, s->stream);
     else
         launch_begin_eval_fp64(m, x, F_out, s->st.p, s->stream);
+    if (s->bsr_use)  // the solvers' operator on the new rotations
+        launch_bsr_assemble_fp64(m, s->bsr_nnzb, s->bsr_cptr.p, s->bsr_contrib.p, s->bsr_val.p, s->stream);
 }
 
 // The material's element force at x (C_f_e / C_LCM_f_e) into m.eout and/or
@@ -327,6 +344,13 @@ void elem_spmv(fem_solid s, const MeshView<double>& m, const double* d, int chec
         launch_elem_lcm_spmv_fp64(m, d, s->Fe.p, pk_material(s), s->st.p, check_done, s->stream);
     else
         launch_elem_spmv_fp64(m, d, s->st.p, check_done, s->stream);
+}
+
+// The solvers' product ahead of their node kernels: nothing when those take
+// K u from the assembled stiffness (m.bsr_val), else the element outputs.
+void solve_product(fem_solid s, const MeshView<double>& m, const double* d, int check_done)
+{
+    if (!m.bsr_val) elem_spmv(s, m, d, check_done);
 }
 
 // FixedStep's opening: BeginEvaluation(m_vecPos0, x), then m_vecPos0 = x
@@ -350,6 +374,75 @@ int open_step(fem_solid s)
 bool cg_on_cluster(const fem_solid s)
 {
     return s->params.material == FEM_MATERIAL_C_WRP && s->cl_plan.ctas > 0;
+}
+
+// Whether the solvers take K u from the assembled stiffness (its pattern
+// built): every C_WRP solid whose solve is not the one-cluster CG. GB300's
+// FP64 element product is bound by the FP64 pipe at about 140 instructions
+// per tet per iteration; the assembled rows take 9 FMAs per block, about
+// 27 per tet, at the price of one assembly per evaluation (about 90 per
+// element corner pair, 16 pairs per tet).
+void set_bsr_use(fem_solid s)
+{
+    s->bsr_use = s->bsr_nnzb > 0 && s->params.material == FEM_MATERIAL_C_WRP &&
+                 !(s->params.ls_solver != FEM_LS_MINRES && cg_on_cluster(s));
+}
+
+// The assembled stiffness's pattern and contributions (MeshView::bsr_*):
+// row n holds n's neighbours through its elements and n itself, ascending;
+// slot (n, j) sums the corner pairs (li of n, lj of j) of the elements
+// holding both, in element order. ptr/idx: the node CSR of element corners.
+int build_bsr(fem_solid s, const uint32_t* tets, const std::vector<uint32_t>& ptr, const std::vector<uint32_t>& idx)
+{
+    const uint32_t N = s->N, T = s->T;
+    if ((uint64_t)T >= (1ull << 28)) return FEM_OK;  // contributions pack the element in 28 bits
+    std::vector<uint32_t> brow(N + 1, 0), bcol, nb;
+    bcol.reserve(16 * (size_t)N);
+    for (uint32_t n = 0; n < N; n++) {
+        nb.clear();
+        nb.push_back(n);
+        for (uint32_t j = ptr[n]; j < ptr[n + 1]; j++) {
+            const size_t e = idx[j] >> 2;
+            for (int k = 0; k < 4; k++) nb.push_back(tets[4 * e + k]);
+        }
+        std::sort(nb.begin(), nb.end());
+        nb.erase(std::unique(nb.begin(), nb.end()), nb.end());
+        bcol.insert(bcol.end(), nb.begin(), nb.end());
+        if (bcol.size() >= (1ull << 32)) return FEM_OK;
+        brow[n + 1] = (uint32_t)bcol.size();
+    }
+    const size_t nnzb = bcol.size();
+    auto slot_of = [&](uint32_t n, uint32_t col) {
+        return (size_t)(std::lower_bound(bcol.begin() + brow[n], bcol.begin() + brow[n + 1], col) - bcol.begin());
+    };
+    std::vector<uint32_t> bcptr(nnzb + 1, 0), bcon(16 * (size_t)T);
+    for (uint32_t n = 0; n < N; n++)
+        for (uint32_t j = ptr[n]; j < ptr[n + 1]; j++)
+            for (int lj = 0; lj < 4; lj++) bcptr[slot_of(n, tets[4 * (size_t)(idx[j] >> 2) + lj]) + 1]++;
+    for (size_t k = 0; k < nnzb; k++) bcptr[k + 1] += bcptr[k];
+    {
+        std::vector<uint32_t> fill(bcptr.begin(), bcptr.end() - 1);
+        for (uint32_t n = 0; n < N; n++)
+            for (uint32_t j = ptr[n]; j < ptr[n + 1]; j++) {
+                const uint32_t e = idx[j] >> 2, li = idx[j] & 3u;
+                for (uint32_t lj = 0; lj < 4; lj++)
+                    bcon[fill[slot_of(n, tets[4 * (size_t)e + lj])]++] = (e << 4) | (li << 2) | lj;
+            }
+    }
+    cudaStream_t st = s->stream;
+    CK(s->bsr_row.alloc(N + 1));
+    CK(s->bsr_col.alloc(nnzb));
+    CK(s->bsr_cptr.alloc(nnzb + 1));
+    CK(s->bsr_contrib.alloc(bcon.size()));
+    CK(s->bsr_val.alloc(9 * nnzb));
+    CK(cudaMemcpyAsync(s->bsr_row.p, brow.data(), sizeof(uint32_t) * brow.size(), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(s->bsr_col.p, bcol.data(), sizeof(uint32_t) * nnzb, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(s->bsr_cptr.p, bcptr.data(), sizeof(uint32_t) * bcptr.size(), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(s->bsr_contrib.p, bcon.data(), sizeof(uint32_t) * bcon.size(), cudaMemcpyHostToDevice, st));
+    CK(cudaMemsetAsync(s->bsr_val.p, 0, sizeof(double) * 9 * nnzb, st));
+    CK(cudaStreamSynchronize(st));
+    s->bsr_nnzb = (uint32_t)nnzb;
+    return FEM_OK;
 }
 
 // The one-cluster CG plan of a solid (see cg_on_cluster). Up to 1,440 tets,
@@ -408,12 +501,12 @@ int cg_solve(fem_solid s, const StepConsts& c, int chunk)
         return FEM_OK;
     }
     const uint32_t gN = grid_for(s->N), gV = grid_for(3 * s->N);
-    elem_spmv(s, m, s->y.p, 0);
+    solve_product(s, m, s->y.p, 0);
     launch_node_residual_fp64(m, c, s->b.p, s->y.p, s->r.p, s->d.p, s->partials.p, st);
     launch_finalize(FIN_INIT, s->partials.p, gN, c, s->st.p, st);
     for (;;) {
         for (int i = 0; i < chunk; i++) {
-            elem_spmv(s, m, s->d.p, 1);
+            solve_product(s, m, s->d.p, 1);
             launch_node_q_fp64(m, c, s->d.p, s->q.p, s->partials.p, s->st.p, st);
             launch_finalize(FIN_ALPHA, s->partials.p, gN, c, s->st.p, st);
             launch_node_xr_fp64(s->N, s->y.p, s->r.p, s->d.p, s->q.p, s->partials.p, s->st.p, st);
@@ -441,7 +534,7 @@ int minres_solve(fem_solid s, const StepConsts& c, int chunk)
     double *v = s->r.p, *v0 = s->d.p, *v1 = s->q.p, *p = s->mr_p.p, *p0 = s->mr_p0.p;
     launch_sq_norm_fp64(3 * s->N, s->b.p, s->partials.p, st);
     launch_finalize(FIN_SUM, s->partials.p, gV, c, s->st.p, st);  // |b|^2
-    elem_spmv(s, m, s->y.p, 0);
+    solve_product(s, m, s->y.p, 0);
     launch_mr_init_fp64(m, c, s->b.p, s->y.p, v1, s->partials.p, st);
     launch_finalize(FIN_MR_INIT, s->partials.p, gN, c, s->st.p, st);
     launch_mr_start_fp64(s->N, v1, v, p, p0, s->st.p, st);
@@ -451,7 +544,7 @@ int minres_solve(fem_solid s, const StepConsts& c, int chunk)
             v0 = v;
             v = v1;
             v1 = t;
-            elem_spmv(s, m, v, 1);
+            solve_product(s, m, v, 1);
             launch_mr_q_fp64(m, c, v, v0, v1, s->partials.p, s->st.p, st);
             launch_finalize(FIN_MR_ALPHA, s->partials.p, gN, c, s->st.p, st);
             launch_mr_v1_fp64(s->N, v1, v, s->partials.p, s->st.p, st);
@@ -492,12 +585,12 @@ cudaError_t ls_solve_capture(fem_solid s, const StepConsts& c, cudaGraph_t top)
     cudaError_t e = cudaGraphConditionalHandleCreate(&cond, top, 0, cudaGraphCondAssignDefault);
     if (e != cudaSuccess) return e;
     if (s->params.ls_solver != FEM_LS_MINRES) {
-        elem_spmv(s, m, s->y.p, 0);
+        solve_product(s, m, s->y.p, 0);
         launch_node_residual_fp64(m, c, s->b.p, s->y.p, s->r.p, s->d.p, s->partials.p, st);
         launch_finalize(FIN_INIT, s->partials.p, gN, c, s->st.p, st, cond, 1);
         e = capture_conditional(st, cond, cudaGraphCondTypeWhile, [&](cudaStream_t bs, cudaGraph_t) {
             s->stream = bs;
-            elem_spmv(s, m, s->d.p, 1);
+            solve_product(s, m, s->d.p, 1);
             launch_node_q_fp64(m, c, s->d.p, s->q.p, s->partials.p, s->st.p, bs);
             launch_finalize(FIN_ALPHA, s->partials.p, gN, c, s->st.p, bs, cond, 1);
             launch_node_xr_fp64(s->N, s->y.p, s->r.p, s->d.p, s->q.p, s->partials.p, s->st.p, bs);
@@ -516,7 +609,7 @@ cudaError_t ls_solve_capture(fem_solid s, const StepConsts& c, cudaGraph_t top)
     double *v = s->r.p, *v0 = s->d.p, *v1 = s->q.p, *p = s->mr_p.p, *p0 = s->mr_p0.p;
     launch_sq_norm_fp64(3 * s->N, s->b.p, s->partials.p, st);
     launch_finalize(FIN_SUM, s->partials.p, gV, c, s->st.p, st);  // |b|^2
-    elem_spmv(s, m, s->y.p, 0);
+    solve_product(s, m, s->y.p, 0);
     launch_mr_init_fp64(m, c, s->b.p, s->y.p, v1, s->partials.p, st);
     launch_finalize(FIN_MR_INIT, s->partials.p, gN, c, s->st.p, st, cond, 1);
     launch_mr_start_fp64(s->N, v1, v, p, p0, s->st.p, st);
@@ -527,7 +620,7 @@ cudaError_t ls_solve_capture(fem_solid s, const StepConsts& c, cudaGraph_t top)
             v0 = v;
             v = v1;
             v1 = t;
-            elem_spmv(s, m, v, 1);
+            solve_product(s, m, v, 1);
             launch_mr_q_fp64(m, c, v, v0, v1, s->partials.p, s->st.p, bs);
             launch_finalize(FIN_MR_ALPHA, s->partials.p, gN, c, s->st.p, bs, cond, 1);
             launch_mr_v1_fp64(s->N, v1, v, s->partials.p, s->st.p, bs);
@@ -936,6 +1029,8 @@ int fem_solid_create(const double* rest_xyz, uint32_t N, const uint32_t* tets, u
         CKC(cudaMemcpyAsync(s->cl_ent.p, ent.data(), sizeof(uint32_t) * ent.size(), cudaMemcpyHostToDevice, st));
         CKC(cudaStreamSynchronize(st));
     }
+    if (int e = build_bsr(s, tets, ptr, idx)) return cleanup(e);
+    set_bsr_use(s);
     CKC(cudaMemsetAsync(s->fixed.p, 0, N, st));
     CKC(cudaMemcpyAsync(s->rest.p, rest_xyz, sizeof(double) * n3, cudaMemcpyHostToDevice, st));
     CKC(cudaMemcpyAsync(s->x.p, rest_xyz, sizeof(double) * n3, cudaMemcpyHostToDevice, st));
@@ -1068,6 +1163,7 @@ int fem_solid_set_params(fem_solid s, const fem_params* params)
         CK(cudaMemcpyAsync(s->doc.p, none.data(), sizeof(uchar2) * s->T, cudaMemcpyHostToDevice, s->stream));
     }
     s->params = *params;
+    set_bsr_use(s);
     set_consts(s);
     // a new Young's modulus or Poisson ratio re-bakes every element from the
     // scalar values, as EditableTetrahedronElementSet3::SetParams does
