@@ -254,8 +254,9 @@ def cpu_configs_leg():
 
 def plain_fp64_c1_latency(steps=120):
     """The plain FP64 drop-in (fem_solid_step, synchronous) on the C1
-    cantilever: per-step wall-clock latency. At 160 tets each CG iteration
-    is a handful of small kernels, so the step is launch-bound."""
+    cantilever: per-step wall-clock latency. At 160 tets the CG solve is
+    one thread-block-cluster kernel; the step's other kernels and the host
+    round trip make up the rest."""
     from risdsdgcfem_thesis_gb300 import capi, scenes
     sc = scenes.cantilever_160()
     s = capi.Solid(sc, compute_energy=True)
@@ -964,10 +965,20 @@ def main():
     ap.add_argument("--variants", default="step,minres,c_lcm,dapd,fie,lock_step",
                     help="comma-separated variants of the batched variants leg")
     ap.add_argument("--variants-meshes", type=int, default=128)
+    ap.add_argument("--only-plain", action="store_true",
+                    help="run only the plain FP64 solid legs: the FIE step of the 40^3 block (host-driven "
+                         "solver loop, so per-kernel profilers see its kernels), the 60^3 block (CG and MINRES, "
+                         "C_WRP) and the cantilever's latency, and print their JSON")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
         return run_reference(args)
+    if args.only_plain:
+        print(json.dumps({"fie_fp64_gpu": fie_leg(cpu_n=0),
+                          "plain_fp64_gpu": plain_fp64_comparator(args.steps),
+                          "minres_fp64_gpu": plain_fp64_comparator(args.steps, ls_solver=1),
+                          "plain_fp64_gpu_c1": plain_fp64_c1_latency()}))
+        return 0
     if args.only_variants:
         print(json.dumps(batch_variants_leg(meshes=args.variants_meshes, steps=args.steps,
                                             names=args.variants.split(","), use_graph=not args.no_graph)))
