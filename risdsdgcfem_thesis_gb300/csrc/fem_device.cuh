@@ -68,6 +68,7 @@ struct StepScalars {
     // F^T F (FP64 MSVD in place of double-float), and with FP32 rotations an
     // MSVD branch near a tie or a failed sensitivity check
     uint32_t res_det_F, res_isotropic, res_tie, res_check;
+    uint32_t fin_ticket;    // FP64 solid: blocks of the running kernel done with their partial (0 between kernels)
 };
 
 // One MINRES iteration's Givens rotation and update coefficients from
@@ -155,10 +156,15 @@ void launch_knc_fp64(uint32_t N, uint32_t count, const uint32_t* nodes, const do
                      const StepConsts& c, double* b, double* y, cudaStream_t s);
 void launch_node_residual_fp64(const MeshView<double>& m, const StepConsts& c, const double* b, const double* y,
                                double* r, double* d, double* partials, cudaStream_t s);
+// The CG iteration's two reductions end in the kernel that makes their
+// partials: the block that finishes last adds them (slot order) and takes
+// the scalar step (alpha; beta and the loop test), and with set_cond sets
+// the step graph's WHILE condition.
 void launch_node_q_fp64(const MeshView<double>& m, const StepConsts& c, const double* d, double* q,
-                        double* partials, const StepScalars* st, cudaStream_t s);
+                        double* partials, StepScalars* st, cudaStream_t s, cudaGraphConditionalHandle cond = 0,
+                        int set_cond = 0);
 void launch_node_xr_fp64(uint32_t N, double* y, double* r, const double* d, const double* q, double* partials,
-                         const StepScalars* st, cudaStream_t s);
+                         StepScalars* st, cudaStream_t s, cudaGraphConditionalHandle cond = 0, int set_cond = 0);
 void launch_node_d_fp64(uint32_t N, const uint8_t* fixed, double* d, const double* r, const StepScalars* st,
                         cudaStream_t s);
 void launch_integrate_fp64(uint32_t N, double dt, double* x, double* v, const double* y, cudaStream_t s);

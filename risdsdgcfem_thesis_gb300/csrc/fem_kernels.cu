@@ -474,6 +474,32 @@ __global__ void k_knc_fp64(uint32_t N, uint32_t count, const uint32_t* __restric
 }
 
 // r = S (b - A y) ; d = r ; partial |r|^2   (ILSS_CG.h:53-64)
+__device__ __forceinline__ void fin_alpha(StepScalars* st, double total);
+__device__ __forceinline__ void fin_beta(StepScalars* st, double total);
+
+// The grid's total of the blocks' values (v in thread 0 of each), added in
+// the block that finishes last: each block leaves its value in its slot and
+// takes a ticket; the last one (true) adds the slots in order (a strided
+// sum per thread, then the block tree) into thread 0's total and resets
+// the ticket for the next kernel.
+__device__ __forceinline__ bool grid_total_last(double v, double* partials, uint32_t* ticket, double& total)
+{
+    __shared__ bool last;
+    if (threadIdx.x == 0) {
+        partials[blockIdx.x] = v;
+        __threadfence();
+        last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!last) return false;
+    __threadfence();
+    double acc = 0.0;
+    for (uint32_t i = threadIdx.x; i < gridDim.x; i += blockDim.x) acc += __ldcg(partials + i);
+    total = block_sum(acc);
+    if (threadIdx.x == 0) *ticket = 0;
+    return true;
+}
+
 __global__ void k_node_residual_fp64(MeshView<double> m, StepConsts c, const double* __restrict__ b,
                                      const double* __restrict__ y, double* r, double* d, double* partials)
 {
@@ -499,7 +525,7 @@ __global__ void k_node_residual_fp64(MeshView<double> m, StepConsts c, const dou
 
 // q = S A d ; partial d.q   (ILSS_CG.h:90-96)
 __global__ void k_node_q_fp64(MeshView<double> m, StepConsts c, const double* __restrict__ d, double* q,
-                              double* partials, const StepScalars* st)
+                              double* partials, StepScalars* st, cudaGraphConditionalHandle cond, int set_cond)
 {
     if (st->done) return;
     double acc = 0.0;
@@ -517,13 +543,17 @@ __global__ void k_node_q_fp64(MeshView<double> m, StepConsts c, const double* __
         q[i] = q0; q[i + 1] = q1; q[i + 2] = q2;
         acc += d[i] * q0 + d[i + 1] * q1 + d[i + 2] * q2;
     }
-    double s = block_sum(acc);
-    if (threadIdx.x == 0) partials[blockIdx.x] = s;
+    double total = 0.0;
+    if (grid_total_last(block_sum(acc), partials, &st->fin_ticket, total) && threadIdx.x == 0) {
+        fin_alpha(st, total);
+        if (set_cond) cudaGraphSetConditional(cond, st->done ? 0u : 1u);
+    }
 }
 
 // y += alpha d ; r -= alpha q ; partial |r|^2   (ILSS_CG.h:100-117)
 __global__ void k_node_xr_fp64(uint32_t N, double* y, double* r, const double* __restrict__ d,
-                               const double* __restrict__ q, double* partials, const StepScalars* st)
+                               const double* __restrict__ q, double* partials, StepScalars* st,
+                               cudaGraphConditionalHandle cond, int set_cond)
 {
     if (st->done) return;
     const double alpha = st->alpha, na = -alpha;
@@ -535,8 +565,11 @@ __global__ void k_node_xr_fp64(uint32_t N, double* y, double* r, const double* _
         r[i] = ri;
         acc += ri * ri;
     }
-    double s = block_sum(acc);
-    if (threadIdx.x == 0) partials[blockIdx.x] = s;
+    double total = 0.0;
+    if (grid_total_last(block_sum(acc), partials, &st->fin_ticket, total) && threadIdx.x == 0) {
+        fin_beta(st, total);
+        if (set_cond) cudaGraphSetConditional(cond, st->done ? 0u : 1u);
+    }
 }
 
 // d = S (beta d + r)   (ILSS_CG.h:133-137)
@@ -1271,16 +1304,17 @@ void launch_node_residual_fp64(const MeshView<double>& m, const StepConsts& c, c
     FEMGB_LAUNCH(k_node_residual_fp64, grid_for(m.N), m, c, b, y, r, d, partials);
 }
 void launch_node_q_fp64(const MeshView<double>& m, const StepConsts& c, const double* d, double* q,
-                        double* partials, const StepScalars* st, cudaStream_t s)
+                        double* partials, StepScalars* st, cudaStream_t s, cudaGraphConditionalHandle cond,
+                        int set_cond)
 {
     prof_begin("node_q_fp64", s);
-    FEMGB_LAUNCH(k_node_q_fp64, grid_for(m.N), m, c, d, q, partials, st);
+    FEMGB_LAUNCH(k_node_q_fp64, grid_for(m.N), m, c, d, q, partials, st, cond, set_cond);
     prof_end("node_q_fp64", s);
 }
 void launch_node_xr_fp64(uint32_t N, double* y, double* r, const double* d, const double* q, double* partials,
-                         const StepScalars* st, cudaStream_t s)
+                         StepScalars* st, cudaStream_t s, cudaGraphConditionalHandle cond, int set_cond)
 {
-    FEMGB_LAUNCH(k_node_xr_fp64, grid_for(3 * N), N, y, r, d, q, partials, st);
+    FEMGB_LAUNCH(k_node_xr_fp64, grid_for(3 * N), N, y, r, d, q, partials, st, cond, set_cond);
 }
 void launch_node_d_fp64(uint32_t N, const uint8_t* fixed, double* d, const double* r, const StepScalars* st,
                         cudaStream_t s)

@@ -508,9 +508,7 @@ int cg_solve(fem_solid s, const StepConsts& c, int chunk)
         for (int i = 0; i < chunk; i++) {
             solve_product(s, m, s->d.p, 1);
             launch_node_q_fp64(m, c, s->d.p, s->q.p, s->partials.p, s->st.p, st);
-            launch_finalize(FIN_ALPHA, s->partials.p, gN, c, s->st.p, st);
             launch_node_xr_fp64(s->N, s->y.p, s->r.p, s->d.p, s->q.p, s->partials.p, s->st.p, st);
-            launch_finalize(FIN_BETA, s->partials.p, gV, c, s->st.p, st);
             launch_node_d_fp64(s->N, s->fixed.p, s->d.p, s->r.p, s->st.p, st);
         }
         CK(cudaMemcpyAsync(s->st_host, s->st.p, sizeof(StepScalars), cudaMemcpyDeviceToHost, st));
@@ -591,10 +589,8 @@ cudaError_t ls_solve_capture(fem_solid s, const StepConsts& c, cudaGraph_t top)
         e = capture_conditional(st, cond, cudaGraphCondTypeWhile, [&](cudaStream_t bs, cudaGraph_t) {
             s->stream = bs;
             solve_product(s, m, s->d.p, 1);
-            launch_node_q_fp64(m, c, s->d.p, s->q.p, s->partials.p, s->st.p, bs);
-            launch_finalize(FIN_ALPHA, s->partials.p, gN, c, s->st.p, bs, cond, 1);
-            launch_node_xr_fp64(s->N, s->y.p, s->r.p, s->d.p, s->q.p, s->partials.p, s->st.p, bs);
-            launch_finalize(FIN_BETA, s->partials.p, gV, c, s->st.p, bs, cond, 1);
+            launch_node_q_fp64(m, c, s->d.p, s->q.p, s->partials.p, s->st.p, bs, cond, 1);
+            launch_node_xr_fp64(s->N, s->y.p, s->r.p, s->d.p, s->q.p, s->partials.p, s->st.p, bs, cond, 1);
             launch_node_d_fp64(s->N, s->fixed.p, s->d.p, s->r.p, s->st.p, bs);
             s->stream = st;
             return cudaGetLastError();
