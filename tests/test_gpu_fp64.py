@@ -114,6 +114,15 @@ def test_block_with_initial_velocity(fem_lib, oracle):
     _compare_with_port(fem_lib, oracle, sc, 10)
 
 
+def test_block_on_the_assembled_stiffness(fem_lib, oracle):
+    """A block above the one-cluster CG's 8,192 tets (13,720): its CG takes
+    K u from the assembled 3x3-block stiffness, rebuilt at every evaluation;
+    within the oracle's bar after 4 steps."""
+    sc = scenes.large_block(n=14)
+    assert sc.num_tets > 8192
+    _compare_with_port(fem_lib, oracle, sc, 4)
+
+
 def test_compression_with_inversions(fem_lib, oracle):
     sc = scenes.compressed_cube(n=6, steps=30, ratio=0.2)
     _compare_with_port(fem_lib, oracle, sc, 30, tol=1e-9)
