@@ -341,14 +341,17 @@ def time_batch(batch, steps, stream_ptr):
     return step_ms, iters
 
 
-def plain_fp64_comparator(steps=3, ls_solver=0, material=0):
+def plain_fp64_comparator(steps=3, ls_solver=0, material=0, assembled=False):
     """The FP64 drop-in path (fem_solid) on the 60^3 block, device time, with
-    CG (ls_solver 0) or MINRES (1), material C_WRP (0) or C_LCM (1)."""
+    CG (ls_solver 0) or MINRES (1), material C_WRP (0) or C_LCM (1), with the
+    matrix-free element product (the drop-in's default) or the assembled
+    stiffness (fem_solid_set_assembled)."""
     import dataclasses
     import torch
     from risdsdgcfem_thesis_gb300 import capi, scenes
     sc = dataclasses.replace(scenes.large_block(n=60), ls_solver=ls_solver, material=material)
     s = capi.Solid(sc, compute_energy=True)
+    s.set_assembled(assembled)
     s.step(1)
     lib = capi.load()
     st = capi.FemStepStats()
@@ -367,7 +370,8 @@ def plain_fp64_comparator(steps=3, ls_solver=0, material=0):
     s.close()
     return {"value": units / (ms * 1e-3), "unit": UNIT, "steps": steps,
             "workload": f"{sc.name} ({sc.num_tets} tets), plain FP64 drop-in path (fem_solid_step), "
-                        f"{'MINRES' if ls_solver else 'CG'}, {'C_LCM' if material else 'C_WRP'}",
+                        f"{'MINRES' if ls_solver else 'CG'}, {'C_LCM' if material else 'C_WRP'}, "
+                        f"{'assembled stiffness' if assembled else 'matrix-free element product'}",
             "ms_per_step": ms / steps, "iterations_per_step": (st.total_cg_iterations - it0) / steps}
 
 
@@ -573,7 +577,7 @@ def run_ours(args):
     e2e_s, e2e_units = aggregate([(e2e_s, "max"), (e2e_units, "sum")], ws)
     batch.close()
 
-    plain = None
+    plain = plain_asm = None
     plain_c1 = None
     cpu_configs = None
     accuracy = None
@@ -599,6 +603,7 @@ def run_ours(args):
             served = served_leg(args.served_rate, args.served_seconds, pool_count=args.served_pool)
         if not args.no_plain:
             plain = plain_fp64_comparator(3)
+            plain_asm = plain_fp64_comparator(3, assembled=True)
             plain_c1 = plain_fp64_c1_latency()
         if not args.no_fie:
             fie = fie_leg()
@@ -660,6 +665,7 @@ def run_ours(args):
                                            "iteration (16 + 20 s_e per tet + 33 s_v per node)"},
             "accuracy": accuracy,
             "plain_fp64_gpu": plain,
+            "plain_fp64_gpu_assembled": plain_asm,
             "plain_fp64_gpu_c1": plain_c1,
             "cpu_single_thread": cpu_configs,
             "fie_fp64_gpu": fie,
@@ -673,6 +679,8 @@ def run_ours(args):
         }
         if plain:
             line["speedup_vs_plain_fp64_gpu"] = value / plain["value"]
+        if plain_asm:
+            line["speedup_vs_plain_fp64_gpu_assembled"] = value / plain_asm["value"]
         print(json.dumps(line))
     if ws > 1:
         torch.distributed.barrier()
@@ -976,6 +984,7 @@ def main():
     if args.only_plain:
         print(json.dumps({"fie_fp64_gpu": fie_leg(cpu_n=0),
                           "plain_fp64_gpu": plain_fp64_comparator(args.steps),
+                          "plain_fp64_gpu_assembled": plain_fp64_comparator(args.steps, assembled=True),
                           "minres_fp64_gpu": plain_fp64_comparator(args.steps, ls_solver=1),
                           "plain_fp64_gpu_c1": plain_fp64_c1_latency()}))
         return 0

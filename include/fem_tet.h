@@ -263,6 +263,19 @@ int fem_solid_get_state(fem_solid s, double* x, double* v);
  * (LeafDSH_Solid3D_FEM.cpp:461), ls_rel_epsilon takes effect. */
 int fem_solid_set_params(fem_solid s, const fem_params* params);
 int fem_solid_get_params(fem_solid s, fem_params* params);
+/* The FP64 solid's solver operator, an option of this library. The
+ * reference's solvers apply the element set's product matrix-free
+ * (ILSS_CG.h:38-151 over TetrahedronElementSet3's R K0 R^T products), and
+ * so does this solid by default (on = 0). With on = 1 a C_WRP solid keeps
+ * K = sum_e R K0 R^T as 3x3 blocks over the node graph, rebuilt at every
+ * evaluation, and CG and MINRES take K u from its rows: about 24 FP64 FMAs
+ * per tet and iteration against about 140, at the price of 76 B per block
+ * (12.6 blocks per node on grid meshes) and one assembly per evaluation;
+ * the sums run in another order, so other bits, within the same parity
+ * tolerances. Other materials keep the element product, and so does the
+ * one-cluster CG of solids of at most 8,192 tets. FEM_E_OOM when the blocks
+ * do not fit. */
+int fem_solid_set_assembled(fem_solid s, int on);
 
 /* Replaces: the multi-solid Newton lock-step phases of the Leaf,
  * NR_Init / NR_PreStep / NR_MidStep / NR_PostStep / NR_End

@@ -136,6 +136,7 @@ SIGNATURES = {
     "fem_solid_mass_info": (C.c_int, [C.c_void_p, _dp, _dp, _dp]),
     "fem_solid_apply_A_noalloc": (C.c_int, [C.c_void_p, C.c_double, C.c_double, _dp, _dp]),
     "fem_solid_set_params": (C.c_int, [C.c_void_p, C.POINTER(FemParams)]),
+    "fem_solid_set_assembled": (C.c_int, [C.c_void_p, C.c_int]),
     "fem_solid_nr_init": (C.c_int, [C.c_void_p, C.c_double]),
     "fem_solid_nr_prestep": (C.c_int, [C.c_void_p, C.c_double]),
     "fem_solid_nr_midstep": (C.c_int, [C.c_void_p, C.c_double]),
@@ -285,6 +286,12 @@ class Solid:
         p = FemParams()
         check(self.lib.fem_solid_get_params(self.h, C.byref(p)))
         return p
+
+    def set_assembled(self, on: bool = True):
+        """fem_solid_set_assembled: the solvers take K u from an assembled
+        3x3-block stiffness (on) or from the element products (off, the
+        default)."""
+        check(self.lib.fem_solid_set_assembled(self.h, 1 if on else 0))
 
     def nr_phase(self, phase, dt):
         """One multi-solid Newton lock-step phase (init, prestep, midstep,

@@ -116,7 +116,7 @@ struct fem_solid_s {
     DevBuf<uint32_t> bsr_row, bsr_col, bsr_cptr, bsr_contrib;
     DevBuf<double> bsr_val;
     uint32_t bsr_nnzb = 0;
-    bool bsr_use = false;
+    bool bsr_want = false, bsr_use = false;  // fem_solid_set_assembled; the solvers take it now
     // node vectors
     DevBuf<double> rest, x, v, y, b, r, d, q, tmp;
     DevBuf<double> xn, vn;  // FIE: x^n and v^n of the step (allocated for the FIE integrators only)
@@ -376,15 +376,16 @@ bool cg_on_cluster(const fem_solid s)
     return s->params.material == FEM_MATERIAL_C_WRP && s->cl_plan.ctas > 0;
 }
 
-// Whether the solvers take K u from the assembled stiffness (its pattern
-// built): every C_WRP solid whose solve is not the one-cluster CG. GB300's
+// Whether the solvers take K u from the assembled stiffness (asked for by
+// fem_solid_set_assembled and built): a C_WRP solid whose solve is not the
+// one-cluster CG. GB300's
 // FP64 element product is bound by the FP64 pipe at about 140 instructions
 // per tet per iteration; the assembled rows take 9 FMAs per block, about
 // 27 per tet, at the price of one assembly per evaluation (about 90 per
 // element corner pair, 16 pairs per tet).
 void set_bsr_use(fem_solid s)
 {
-    s->bsr_use = s->bsr_nnzb > 0 && s->params.material == FEM_MATERIAL_C_WRP &&
+    s->bsr_use = s->bsr_want && s->bsr_nnzb > 0 && s->params.material == FEM_MATERIAL_C_WRP &&
                  !(s->params.ls_solver != FEM_LS_MINRES && cg_on_cluster(s));
 }
 
@@ -1025,7 +1026,6 @@ int fem_solid_create(const double* rest_xyz, uint32_t N, const uint32_t* tets, u
         CKC(cudaMemcpyAsync(s->cl_ent.p, ent.data(), sizeof(uint32_t) * ent.size(), cudaMemcpyHostToDevice, st));
         CKC(cudaStreamSynchronize(st));
     }
-    if (int e = build_bsr(s, tets, ptr, idx)) return cleanup(e);
     set_bsr_use(s);
     CKC(cudaMemsetAsync(s->fixed.p, 0, N, st));
     CKC(cudaMemcpyAsync(s->rest.p, rest_xyz, sizeof(double) * n3, cudaMemcpyHostToDevice, st));
@@ -1066,6 +1066,44 @@ int fem_solid_destroy(fem_solid s)
     if (s->stream) cudaStreamSynchronize(s->stream);
     s->release();
     delete s;
+    return FEM_OK;
+}
+
+int fem_solid_set_assembled(fem_solid s, int on)
+{
+    if (int e = check_handle(s)) return e;
+    s->drop_graph();  // the step graph holds the operator's launches
+    if (on && !s->bsr_nnzb) {
+        const uint32_t N = s->N, T = s->T;
+        std::vector<int4> t4(T);
+        std::vector<uint32_t> tets(4 * (size_t)T), ptr(N + 1), idx(4 * (size_t)T);
+        CK(cudaMemcpyAsync(t4.data(), s->tets.p, sizeof(int4) * T, cudaMemcpyDeviceToHost, s->stream));
+        CK(cudaMemcpyAsync(ptr.data(), s->csr_ptr.p, sizeof(uint32_t) * (N + 1), cudaMemcpyDeviceToHost, s->stream));
+        CK(cudaMemcpyAsync(idx.data(), s->csr_idx.p, sizeof(uint32_t) * idx.size(), cudaMemcpyDeviceToHost,
+                           s->stream));
+        CK(cudaStreamSynchronize(s->stream));
+        for (uint32_t e = 0; e < T; e++) {
+            tets[4 * (size_t)e] = (uint32_t)t4[e].x;
+            tets[4 * (size_t)e + 1] = (uint32_t)t4[e].y;
+            tets[4 * (size_t)e + 2] = (uint32_t)t4[e].z;
+            tets[4 * (size_t)e + 3] = (uint32_t)t4[e].w;
+        }
+        if (int e = build_bsr(s, tets.data(), ptr, idx)) {
+            s->bsr_row.release();
+            s->bsr_col.release();
+            s->bsr_cptr.release();
+            s->bsr_contrib.release();
+            s->bsr_val.release();
+            s->bsr_nnzb = 0;
+            return e;
+        }
+        // the current rotations' blocks, for a solve before the next evaluation
+        MeshView<double> m = s->view();
+        launch_bsr_assemble_fp64(m, s->bsr_nnzb, s->bsr_cptr.p, s->bsr_contrib.p, s->bsr_val.p, s->stream);
+        CK(cudaStreamSynchronize(s->stream));
+    }
+    s->bsr_want = on != 0;
+    set_bsr_use(s);
     return FEM_OK;
 }
 

@@ -59,7 +59,7 @@ def _perturbed(sc, seed, eps=1e-15):
     return p
 
 
-def _compare_with_port(fem_lib, oracle, sc, steps, tol=TOL, cap=None):
+def _compare_with_port(fem_lib, oracle, sc, steps, tol=TOL, cap=None, assembled=False):
     """GPU vs the oracle restatement over `steps` FixedSteps.
 
     CG stops on a residual threshold, and on stiff scenes the residual sits on
@@ -71,6 +71,7 @@ def _compare_with_port(fem_lib, oracle, sc, steps, tol=TOL, cap=None):
     max(tol, 10 x that floor) in state and within max(1, 2 x spread + 1) in
     iterations per step."""
     a = fem_lib.Solid(sc)
+    a.set_assembled(assembled)
     b = oracle.Solid(sc, "port")
     noisy = [oracle.Solid(_perturbed(sc, seed), "port") for seed in (1, 2, 3)]
     it_gpu, it_orc = [], []
@@ -115,12 +116,12 @@ def test_block_with_initial_velocity(fem_lib, oracle):
 
 
 def test_block_on_the_assembled_stiffness(fem_lib, oracle):
-    """A block above the one-cluster CG's 8,192 tets (13,720): its CG takes
-    K u from the assembled 3x3-block stiffness, rebuilt at every evaluation;
-    within the oracle's bar after 4 steps."""
+    """A block above the one-cluster CG's 8,192 tets (13,720) whose CG takes
+    K u from the assembled 3x3-block stiffness (fem_solid_set_assembled),
+    rebuilt at every evaluation; within the oracle's bar after 4 steps."""
     sc = scenes.large_block(n=14)
     assert sc.num_tets > 8192
-    _compare_with_port(fem_lib, oracle, sc, 4)
+    _compare_with_port(fem_lib, oracle, sc, 4, assembled=True)
 
 
 def test_compression_with_inversions(fem_lib, oracle):

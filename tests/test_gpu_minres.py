@@ -70,8 +70,10 @@ def test_minres_driven_block_matches_reference(fem_lib, oracle):
     assert rel(v, g[prefix + "v"]) <= max(1e-10, 10 * fv), (rel(v, g[prefix + "v"]), fv)
 
 
-def test_minres_matches_oracle_on_random_block(fem_lib, oracle):
-    """2,400 tets under gravity, MINRES with FIE, against the oracle run here."""
+@pytest.mark.parametrize("assembled", [False, True])
+def test_minres_matches_oracle_on_random_block(fem_lib, oracle, assembled):
+    """2,400 tets under gravity, MINRES with FIE, against the oracle run here;
+    with the element products and with the assembled stiffness."""
     rng = np.random.default_rng(21)
     sc = scenes.random_block(rng, dims=(10, 6, 8))
     sc.integrator = fem_lib.FEM_INTEGRATOR_FIE_DX
@@ -79,6 +81,7 @@ def test_minres_matches_oracle_on_random_block(fem_lib, oracle):
     sc.gravity = (0.0, 0.0, -9.81)
     sc.rel_eps, sc.max_iter = 1e-8, 400
     a = fem_lib.Solid(sc)
+    a.set_assembled(assembled)
     b = oracle.Solid(sc, "port")
     for _ in range(4):
         sa, sb = a.step(1), b.step()
