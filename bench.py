@@ -375,7 +375,7 @@ def plain_fp64_comparator(steps=3, ls_solver=0, material=0, assembled=False):
             "ms_per_step": ms / steps, "iterations_per_step": (st.total_cg_iterations - it0) / steps}
 
 
-def fie_leg(n=40, steps=2, cpu_n=16):
+def fie_leg(n=40, steps=2, cpu_n=16, assembled=False):
     """The fully-implicit Euler integrator (Newton on Delta x, 3 Newton
     iterations per step, Step_FullyImplicitEuler_dx) on the FP64 solid: the
     n^3 block, wall clock per step (the Newton loop reads |b_k| and |y_k| on
@@ -386,6 +386,7 @@ def fie_leg(n=40, steps=2, cpu_n=16):
     from risdsdgcfem_thesis_gb300 import capi, scenes
     sc = dataclasses.replace(scenes.large_block(n=n), integrator=capi.FEM_INTEGRATOR_FIE_DX)
     s = capi.Solid(sc, compute_energy=True)
+    s.set_assembled(assembled)
     s.step(1)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -394,7 +395,8 @@ def fie_leg(n=40, steps=2, cpu_n=16):
     s.close()
     cg = sum(x["cg_iterations"] for x in st)
     out = {"value": sc.num_tets * cg / wall, "unit": UNIT, "steps": steps, "ms_per_step": 1e3 * wall / steps,
-           "workload": f"{sc.name} ({sc.num_tets} tets), FP64 solid, integrator FIE_DX, nr_max_iter 3",
+           "workload": f"{sc.name} ({sc.num_tets} tets), FP64 solid, integrator FIE_DX, nr_max_iter 3"
+                       + (", assembled stiffness" if assembled else ""),
            "newton_iterations_per_step": [x["nr_iterations"] for x in st],
            "cg_iterations_per_step": [x["cg_iterations"] for x in st]}
     if cpu_n:
@@ -974,15 +976,17 @@ def main():
                     help="comma-separated variants of the batched variants leg")
     ap.add_argument("--variants-meshes", type=int, default=128)
     ap.add_argument("--only-plain", action="store_true",
-                    help="run only the plain FP64 solid legs: the FIE step of the 40^3 block (host-driven "
-                         "solver loop, so per-kernel profilers see its kernels), the 60^3 block (CG and MINRES, "
-                         "C_WRP) and the cantilever's latency, and print their JSON")
+                    help="run only the plain FP64 solid legs: the FIE step of the 40^3 block with the assembled "
+                         "stiffness, then matrix-free (host-driven solver loop, so per-kernel profilers see its "
+                         "kernels), the 60^3 block (CG matrix-free and assembled, MINRES; C_WRP) and the "
+                         "cantilever's latency, and print their JSON")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
         return run_reference(args)
     if args.only_plain:
-        print(json.dumps({"fie_fp64_gpu": fie_leg(cpu_n=0),
+        print(json.dumps({"fie_fp64_gpu_assembled": fie_leg(cpu_n=0, assembled=True),
+                          "fie_fp64_gpu": fie_leg(cpu_n=0),
                           "plain_fp64_gpu": plain_fp64_comparator(args.steps),
                           "plain_fp64_gpu_assembled": plain_fp64_comparator(args.steps, assembled=True),
                           "minres_fp64_gpu": plain_fp64_comparator(args.steps, ls_solver=1),
