@@ -110,7 +110,7 @@ def test_create_rejects_empty_and_null(fem_lib):
                      ("fem_batch_nr_midstep", (0.01,)), ("fem_batch_nr_poststep", (0.01,)),
                      ("fem_batch_nr_end", (0.01,)), ("fem_batch_multi_step", (0.01, 1)),
                      ("fem_batch_set_params", (0, C.byref(p))), ("fem_batch_get_params", (0, C.byref(p))),
-                     ("fem_server_set_params", (0, C.byref(p)))):
+                     ("fem_server_set_params", (0, C.byref(p))), ("fem_solid_set_assembled", (1,))):
         assert getattr(lib, fn)(None, *args) == fem_lib.FEM_E_ARG, fn
 
 

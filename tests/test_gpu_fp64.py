@@ -124,6 +124,26 @@ def test_block_on_the_assembled_stiffness(fem_lib, oracle):
     _compare_with_port(fem_lib, oracle, sc, 4, assembled=True)
 
 
+def test_assembled_toggle_between_steps(fem_lib):
+    """fem_solid_set_assembled switched on and off between steps (its first
+    switch-on assembles on the current rotations): a 13,720-tet block stepped
+    matrix-free, assembled, then matrix-free again stays as close to the
+    same block stepped matrix-free throughout as the oracle stays to itself
+    under 1e-15 perturbations on this block (x about 1e-9, v about 2e-6,
+    the CG's residual plateau); MINRES the same."""
+    for solver in (fem_lib.FEM_LS_CG, fem_lib.FEM_LS_MINRES):
+        sc = scenes.large_block(n=14)
+        sc.ls_solver = solver
+        ref, sw = fem_lib.Solid(sc), fem_lib.Solid(sc)
+        for on in (False, True, False, True):
+            sw.set_assembled(on)
+            ref.step(2)
+            sw.step(2)
+        xr, vr = ref.state()
+        xs, vs = sw.state()
+        assert rel(xs, xr) < 1e-8 and rel(vs, vr) < 5e-6, (solver, rel(xs, xr), rel(vs, vr))
+
+
 def test_compression_with_inversions(fem_lib, oracle):
     sc = scenes.compressed_cube(n=6, steps=30, ratio=0.2)
     _compare_with_port(fem_lib, oracle, sc, 30, tol=1e-9)
