@@ -27,9 +27,10 @@ def _blocks():
 def workloads():
     """(name, callable returning {array name: array})."""
 
-    def solid(sc, steps):
+    def solid(sc, steps, assembled=False):
         def run():
             s = capi.Solid(sc)
+            s.set_assembled(assembled)
             s.step(steps)
             x, v = s.state()
             s.close()
@@ -71,6 +72,7 @@ def workloads():
         ("solid_dapd", solid(crush, 28)),
         ("solid_lcm", solid(dataclasses.replace(blk, material=capi.FEM_MATERIAL_C_LCM), 4)),
         ("solid_minres", solid(dataclasses.replace(cant, ls_solver=capi.FEM_LS_MINRES), 4)),
+        ("solid_minres_assembled", solid(dataclasses.replace(blk, ls_solver=capi.FEM_LS_MINRES), 4, True)),
         ("solid_fie", solid(dataclasses.replace(cant, integrator=capi.FEM_INTEGRATOR_FIE_DX), 3)),
         ("batch_fp64", batch(capi.FEM_PRECISION_FP64)),
         ("batch_mixed", batch(capi.FEM_PRECISION_MIXED)),

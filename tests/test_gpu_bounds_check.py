@@ -1,9 +1,11 @@
 """The index-checking build (-DFEM_BOUNDS_CHECK, bounds.cuh) on small
-workloads of every kernel family: the FP64 solid (MSVD, DAPD through its
-collapse branch, C_LCM, MINRES, FIE), the FP64 and mixed batches and the
-served path. Every data-dependent index the kernels read from a table
-(element node ids, node CSR entries, tile node lists, tile-local ids and CSR
-entries, partial slots, constraint nodes) is checked against its limit; no
+workloads of every kernel family: the FP64 solid (MSVD with the one-cluster
+CG, DAPD through its collapse branch, C_LCM, MINRES matrix-free and on the
+assembled stiffness, FIE), the FP64 and mixed batches and the served path.
+Every data-dependent index the kernels read from a table (element node ids,
+node CSR entries, assembled blocks' columns and contributions, tile node
+lists, tile-local ids and CSR entries, partial slots, constraint nodes) is
+checked against its limit; no
 check may fire, and the results agree with the normal library's to 1e-5 of
 each array's largest entry (the checks change which index an out-of-range
 access would use, not the formulas; the compiler may still contract a
